@@ -1,0 +1,292 @@
+/*
+ * nanofiller_gb300.h -- C ABI of the GB300-native NanoFiller hot path.
+ *
+ * The path: Monte Carlo rod candidates drawn from a density and an orientation
+ * profile -> cell-list hard-core rejection with sequential-insertion semantics
+ * -> tunnelling-contact extraction (count/record, screening, electrode roles)
+ * -> conductance-network solve -> adjoint of the effective conductance.
+ *
+ * Conventions (all entry points):
+ *   - every call returns nf_status; nothing prints, nothing exits;
+ *   - lengths are in micrometres and angles in radians, like the reference's
+ *     simPrms (src/simPrms.cpp:22-117);
+ *   - host arrays are caller-owned; sizes are in elements;
+ *   - one handle per host thread; a handle owns its device memory and runs on
+ *     the stream given to nf_set_stream (default: the legacy stream);
+ *   - no global device state: parameters travel in kernel arguments.
+ *
+ * Each declaration names the reference interface it replaces (file:line in
+ * pyrlinum/NanoFiller).
+ */
+#ifndef NANOFILLER_GB300_H
+#define NANOFILLER_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define NF_ABI_VERSION 1
+
+/* Electrode pseudo-rod ids in contact lists (inc/definitions.h:18-20). */
+#define NF_SRC_ELEC 0xFFFFFFFFu
+#define NF_SNK_ELEC 0xFFFFFFFEu
+
+typedef enum nf_status {
+    NF_OK = 0,
+    NF_ERR_PARAM = 1,         /* invalid parameter, size or pointer */
+    NF_ERR_CUDA = 2,          /* CUDA runtime error (text in nf_last_error) */
+    NF_ERR_NO_DEVICE = 3,     /* no CUDA device visible */
+    NF_ERR_ALLOC = 4,         /* device or host allocation failed */
+    NF_ERR_CAPACITY = 5,      /* caller buffer too small; ->count holds the need */
+    NF_ERR_OVERFLOW = 6,      /* a fixed-capacity internal list overflowed */
+    NF_ERR_NOT_CONVERGED = 7, /* the network solve missed its tolerance */
+    NF_ERR_IO = 8,            /* file could not be opened or written */
+    NF_ERR_FORMAT = 9,        /* malformed or truncated input file */
+    NF_ERR_STATE = 10,        /* call out of order (e.g. contacts before rods) */
+    NF_ERR_UNSUPPORTED = 11,  /* parsed reference option this path does not run */
+    NF_ERR_TIMEOUT = 12       /* a bounded device-side wait gave up */
+} nf_status;
+
+enum { NF_ORIENT_ISOTROPIC = 0, NF_ORIENT_VMF = 1 };
+enum { NF_SIZE_CONST = 0, NF_SIZE_LOGNORMAL = 1, NF_SIZE_UNIFORM = 2 };
+
+/*
+ * Parameters. The first block mirrors the reference keyword surface
+ * (inc/parameter_input.h:8-68, parsed in src/simPrms.cpp:212-327; defaults
+ * src/simPrms.cpp:22-117). The second block holds the project keys that the
+ * reference has no keyword for (seeded stream, size and orientation laws,
+ * tunnelling law, solver).
+ */
+typedef struct nf_params {
+    /* --- reference keywords --- */
+    float vf;               /* VOLUME_PERCENT / 100                          */
+    float vf_precision;     /* VOL_FRAC_PRECISION (parsed; stop is exact)    */
+    float box[3];           /* physDim: SPAT_DISTR_FILE NONE Lx Ly Lz        */
+    int32_t mesh_ext[3];    /* SPAT_DISTR_FILE NONE ... nx ny nz             */
+    char density_file[256]; /* SPAT_DISTR_FILE <file> (read_density format)  */
+    float pref_ort[2];      /* PREF_ORT_PHI, PREF_ORT_THETA (rad)            */
+    float theta_med;        /* DEF_THETA_MED (rad)                           */
+    float theta_dev;        /* DEF_THETA_DEV (rad, <=0: isotropic)           */
+    float phi_med;          /* DEF_PHI_MED (rad)                             */
+    float phi_dev;          /* DEF_PHI_DEV (rad, <=0: uniform)               */
+    float l;                /* INC_LEN_MED: rod length (median if lognormal) */
+    float a;                /* INC_RAD_MED: rod radius                       */
+    float l_dev;            /* INC_LEN_DEV (parsed)                          */
+    float a_dev;            /* INC_RAD_DEV (parsed)                          */
+    float sep;              /* INC_SEPARATION: hard-core gap                 */
+    float sc_frac;          /* INC_SOFTCORE: hard-core radius fraction       */
+    float tol;              /* TOL: geometric epsilon (1e-6)                 */
+    float stat_dist_lim;    /* STAT_DIST_LIM: tunnelling cutoff              */
+    int32_t wrt_bin;        /* WRT_BIN                                       */
+    int32_t self_align_step;/* SELF_ALLIGN_STEP (only 0 is run)              */
+    int32_t clust_flag;     /* CLUST_FLAG (only 0 is run)                    */
+    int32_t reduce_flag;    /* REDUCE_FLAG (only 0 is run)                   */
+    /* --- project keys --- */
+    uint64_t seed;          /* SEED: Philox4x32-10 key                       */
+    uint64_t n_candidates;  /* CANDIDATES: stream budget                     */
+    int64_t n_target;       /* TARGET_COUNT: 0 -> ceil(vf V / (pi a^2 l))    */
+    int32_t gen_periodic;   /* PERIODIC: bitmask x=1 y=2 z=4                 */
+    int32_t field_dir;      /* FIELD_DIR: electrode axis 1,2,4 (0: none)     */
+    int32_t orient_mode;    /* ORIENT: NF_ORIENT_*                           */
+    float vmf_kappa;        /* VMF_KAPPA                                     */
+    int32_t len_mode;       /* LEN_LAW: NF_SIZE_CONST / NF_SIZE_LOGNORMAL    */
+    float len_sigma_ln;     /* LEN_SIGMA_LN                                  */
+    float len_min, len_max; /* LEN_CLIP lo hi                                */
+    int32_t rad_mode;       /* RAD_LAW: NF_SIZE_CONST / NF_SIZE_UNIFORM      */
+    float rad_min, rad_max; /* RAD_RANGE lo hi                               */
+    float density_default;  /* DENSITY_DEFAULT: rho when no mesh (1.0)       */
+    float cell_edge;        /* CELL_EDGE: 0 -> smallest legal edge           */
+    double G0;              /* TUNNEL_G0 (S)                                 */
+    double lambda;          /* TUNNEL_LAMBDA (um)                            */
+    double d_c;             /* TUNNEL_DC (um): gap floor and law offset      */
+    int32_t ref_parallel_typo; /* REF_PARALLEL_TYPO: hard-core parallel branch as in
+                                  inc/intersection_dev.h:51                 */
+    int32_t screening;      /* SCREENING: drop contacts crossed by a rod     */
+    int32_t round_candidates; /* ROUND_CANDIDATES: 0 -> adaptive             */
+    int32_t solve_max_iter; /* SOLVE_MAX_ITER (inner FP32 CG iterations)     */
+    double solve_tol;       /* SOLVE_TOL: FP64 relative residual             */
+} nf_params;
+
+/* Rods, structure of arrays, caller-owned host buffers. Any array may be NULL. */
+typedef struct nf_rods {
+    size_t capacity;        /* in: rods the arrays hold                    */
+    size_t count;           /* out: rods written (or needed on CAPACITY)   */
+    float *x, *y, *z;       /* centre                                      */
+    float *cx, *cy, *cz;    /* unit axis                                   */
+    float *l, *a;           /* length, radius                              */
+    uint64_t *stream_index; /* candidate index k that produced the rod     */
+    uint32_t *cell;         /* global cell id (the reference's field k)    */
+} nf_rods;
+
+/* Contacts, sorted by (I, J). Electrode contacts carry J = NF_SRC_ELEC/NF_SNK_ELEC. */
+typedef struct nf_contact_list {
+    size_t capacity;
+    size_t count;
+    uint32_t *I, *J;        /* rod ids (acceptance order), I < J           */
+    float *tI, *tJ;         /* clamped axis parameters of the contact pts  */
+    double *D;              /* axis distance at (tI,tJ); gap = D - aI - aJ */
+    double *G;              /* edge conductance (S)                        */
+    double *S;              /* contact area estimate (um^2)                */
+    int8_t *image;          /* 3 per contact: periodic image of J          */
+} nf_contact_list;
+
+typedef struct nf_gen_stats {
+    uint64_t candidates_drawn;  /* stream indices consumed                 */
+    uint64_t density_accepted;  /* candidates passing u < rho(x)           */
+    uint64_t accepted;          /* rods                                    */
+    uint64_t target;            /* rods asked for                          */
+    uint64_t pair_tests;        /* FP32 filter evaluations                 */
+    uint64_t exact_evals;       /* FP64 evaluations of the reference test  */
+    uint64_t fp32_would_flip;   /* of those, decisions pure FP32 gets wrong*/
+    int32_t rounds;
+    int32_t target_reached;
+    double ms;
+} nf_gen_stats;
+
+typedef struct nf_contact_stats {
+    uint64_t contacts;          /* rod-rod contacts after screening        */
+    uint64_t screened;          /* contacts dropped by screening           */
+    uint64_t n_source, n_sink;  /* electrode contacts                      */
+    uint64_t pair_tests, exact_evals, fp32_would_flip;
+    double ms;
+} nf_contact_stats;
+
+typedef struct nf_solve_stats {
+    double G_eff;               /* effective conductance (S)               */
+    double residual;            /* final ||b - K v|| / ||b|| in FP64       */
+    int32_t outer_iters;        /* FP64 refinement steps                   */
+    int32_t inner_iters;        /* FP32 CG iterations, all steps           */
+    int64_t n_nodes;            /* rods in the network                     */
+    int64_t n_active;           /* unknowns: rods linked to both electrodes*/
+    int32_t percolating;        /* a path joins source and sink            */
+    double ms;
+} nf_solve_stats;
+
+typedef struct nf_batch_result {
+    uint64_t accepted;
+    uint64_t contacts;
+    double G_eff;
+    double residual;
+    int32_t percolating;
+    int32_t status;             /* nf_status of this realisation           */
+} nf_batch_result;
+
+typedef struct nf_batch_stats {
+    int32_t n;
+    int32_t rounds;
+    uint64_t rods, contacts;
+    double ms;
+} nf_batch_stats;
+
+typedef struct nf_handle nf_handle;
+
+/* ---- library ---------------------------------------------------------- */
+int nf_abi_version(void);
+/* Human-readable name of a status code (static string). */
+const char *nf_status_string(nf_status s);
+
+/* ---- parameters (src/simPrms.cpp:22-117, :212-327) ---------------------- */
+/* Fill with the reference defaults plus project defaults. */
+nf_status nf_params_default(nf_params *p);
+/* Parse a reference keyword file (inc/parameter_input.h:8-68) plus project
+ * keys; unknown keys are counted in *n_unknown (may be NULL), as the
+ * reference warns and continues (src/simPrms.cpp:317-319). */
+nf_status nf_params_from_file(const char *path, nf_params *p, int *n_unknown);
+/* Target count N = ceil(vf V / (pi a^2 l)) (src/simPrms.cpp:987-1002). */
+nf_status nf_target_count(const nf_params *p, int64_t *n);
+
+/* ---- handle ------------------------------------------------------------ */
+/* Replaces the simPrms object + device set-up (src/simPrms.cpp:393-502,
+ * src/cudaMain.cu:61-90). */
+nf_status nf_create(const nf_params *p, nf_handle **out);
+nf_status nf_destroy(nf_handle *h);
+/* cudaStream_t passed as void*; NULL is the legacy stream. */
+nf_status nf_set_stream(nf_handle *h, void *stream);
+/* Last error text of this handle. */
+nf_status nf_last_error(const nf_handle *h, char *buf, size_t n);
+
+/* ---- inputs ------------------------------------------------------------ */
+/* Density mesh, read_density order values[i*ny*nz + j*nz + k]
+ * (src/IO.cpp:11-36; uploaded like density2Tex, inc/den2tex.h:5-53). */
+nf_status nf_load_density(nf_handle *h, int nx, int ny, int nz,
+                          const float *values);
+/* Read a read_density file into host memory (header then values). */
+nf_status nf_read_density_file(const char *path, int ext[3], float dim[3],
+                               float *values, size_t capacity);
+
+/* ---- generation (src/cudaMain.cu:61-161, :219-351) ---------------------- */
+/* Draws the seeded stream until the target count or the budget is reached.
+ * Accepted set == sequential insertion in stream order. */
+nf_status nf_generate(nf_handle *h, nf_gen_stats *stats);
+/* Candidate stream itself (for checking): candidates [k0, k0+n), all fields,
+ * with the von Neumann variate in u and rho(x) in rho. */
+nf_status nf_stream_candidates(nf_handle *h, uint64_t k0, uint64_t n,
+                               float *x, float *y, float *z, float *cx,
+                               float *cy, float *cz, float *l, float *a,
+                               float *u, float *rho);
+/* Copy the accepted rods out (simPrms::asmbl_cnt_data, src/simPrms.cpp:329-391). */
+nf_status nf_get_rods(nf_handle *h, nf_rods *out);
+/* Replace the rod set (inject, e.g. from output.bin; stream_index may be NULL). */
+nf_status nf_set_rods(nf_handle *h, const nf_rods *in);
+
+/* ---- contacts (src/conductivity.cu:140-226, src/get_contact_arrays.cu:12-140,
+ *      src/check_screened_Interactions.cu:12-70, src/get_contact_data.cu:28-230) */
+nf_status nf_contacts(nf_handle *h, nf_contact_stats *stats);
+/* Rod-rod contacts first, then sink, then source (save_coo order). */
+nf_status nf_get_contacts(nf_handle *h, nf_contact_list *out);
+
+/* ---- network solve (tools/kirchhoff/kirchhoff.py:211-269,
+ *      tools/kirchhoff/lib/solver.cpp:185-269) --------------------------- */
+nf_status nf_solve(nf_handle *h, nf_solve_stats *stats);
+/* Node voltages (rods; 0 for rods outside the source-sink network). */
+nf_status nf_get_voltages(nf_handle *h, double *v, size_t capacity);
+
+/* ---- adjoint (no reference counterpart) ------------------------------- */
+/* dG_eff/d(endpoints) as N x 6 (e0.xyz, e1.xyz with e0/1 = r -/+ l/2 c),
+ * dG_eff/dlambda and dG_eff/dG0, contact topology held fixed. */
+nf_status nf_adjoint(nf_handle *h, float *dG_dend, size_t capacity,
+                     double *dG_dlambda, double *dG_dG0);
+
+/* ---- batched realisations (no reference counterpart; the reference runs
+ *      one realisation per process, src/NanoFiller.cpp:37-162) ------------ */
+nf_status nf_batch_run(const nf_params *params, int n, nf_batch_result *out,
+                       nf_batch_stats *stats);
+
+/* ---- files ------------------------------------------------------------- */
+/* VTK rods (src/IO.cpp:38-76). */
+nf_status nf_write_vtk(nf_handle *h, const char *path);
+/* output.bin state (src/stateSR.cpp:54-89 / :90-134). */
+nf_status nf_write_state_bin(nf_handle *h, const char *path);
+nf_status nf_read_state_bin(nf_handle *h, const char *path);
+/* internal.srt.coo, sink.elec.coo, source.elec.coo in dir (src/conductivity.cu:838-879). */
+nf_status nf_write_coo(nf_handle *h, const char *dir);
+
+/* Host-only format writers/readers on caller arrays (no device needed). */
+nf_status nf_format_write_vtk(const char *path, size_t n, const float *x,
+                              const float *y, const float *z, const float *cx,
+                              const float *cy, const float *cz, const float *l,
+                              const float *a, const float *k);
+typedef struct nf_state_header {
+    float phys_dim[3];
+    float edge[3];
+    int32_t ext[3];
+    float l, a;
+    int32_t ttl;            /* slots (== rods after repack)                */
+    int32_t num;            /* rods                                        */
+    float tol;
+} nf_state_header;
+nf_status nf_format_write_state_bin(const char *path, const nf_state_header *hd,
+                                    const int16_t *occ, const int32_t *addr,
+                                    const float *planes /* 9 x ttl */);
+/* Reads the header; occ/addr/planes may be NULL to query sizes first. */
+nf_status nf_format_read_state_bin(const char *path, nf_state_header *hd,
+                                   int16_t *occ, int32_t *addr, float *planes,
+                                   size_t cells_cap, size_t planes_cap);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* NANOFILLER_GB300_H */

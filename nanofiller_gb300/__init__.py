@@ -1,0 +1,245 @@
+"""GB300-native NanoFiller hot path: Python front end of the C ABI.
+
+    import nanofiller_gb300 as nf
+    sim = nf.Simulation(nf.configs.SMALL)
+    sim.generate(); sim.contacts(); sim.solve()
+
+Parameters are dicts of nf_params field names (lengths in micrometres); any
+field not given keeps the library default (nf_params_default). The library is
+the CUDA build in nanofiller_gb300/_build/; there is no CPU path.
+"""
+import ctypes as C
+
+import numpy as np
+
+from . import configs  # noqa: F401
+from ._abi import (LIB_PATH, SNK_ELEC, SRC_ELEC, STATUS, NfBatchResult, NfBatchStats,  # noqa: F401
+                   NfContactList, NfContactStats, NfGenStats, NfParams, NfRods, NfSolveStats,
+                   NfStateHeader, load)
+
+__all__ = ["Simulation", "NanoFillerError", "make_params", "params_from_file", "batch_run",
+           "target_count", "configs", "SRC_ELEC", "SNK_ELEC"]
+
+
+class NanoFillerError(RuntimeError):
+    def __init__(self, status, msg=""):
+        self.status = status
+        super().__init__(f"{STATUS.get(status, status)}: {msg}")
+
+
+def _check(st, h=None, what=""):
+    if st != 0:
+        msg = what
+        if h:
+            buf = C.create_string_buffer(512)
+            load().nf_last_error(h, buf, 512)
+            if buf.value:
+                msg = f"{what}: {buf.value.decode()}"
+        raise NanoFillerError(st, msg)
+
+
+def make_params(d=None, **kw):
+    p = NfParams()
+    _check(load().nf_params_default(C.byref(p)))
+    full = dict(d or {})
+    full.update(kw)
+    for k, v in full.items():
+        if k == "lambda":
+            k = "lambda_"
+        if isinstance(v, (tuple, list)):
+            arr = getattr(p, k)
+            for i, x in enumerate(v):
+                arr[i] = x
+        elif k == "density_file":
+            p.density_file = v if isinstance(v, bytes) else str(v).encode()
+        else:
+            setattr(p, k, v)
+    return p
+
+
+def params_to_dict(p):
+    out = {}
+    for name, _ in NfParams._fields_:
+        v = getattr(p, name)
+        if hasattr(v, "__len__") and not isinstance(v, (bytes, str)):
+            v = tuple(v)
+        out[name] = v
+    return out
+
+
+def params_from_file(path, base=None):
+    p = make_params(base)
+    unk = C.c_int(0)
+    _check(load().nf_params_from_file(str(path).encode(), C.byref(p), C.byref(unk)), what=str(path))
+    return params_to_dict(p), unk.value
+
+
+def target_count(params):
+    n = C.c_int64()
+    _check(load().nf_target_count(C.byref(make_params(params)), C.byref(n)))
+    return n.value
+
+
+def _f32p(a):
+    return a.ctypes.data_as(C.POINTER(C.c_float))
+
+
+class Simulation:
+    """One realisation on the current CUDA device (a C-ABI handle)."""
+
+    def __init__(self, params, mesh=None, stream=None):
+        self._L = load()
+        self.params = make_params(params)
+        h = C.c_void_p()
+        _check(self._L.nf_create(C.byref(self.params), C.byref(h)), what="nf_create")
+        self._h = h
+        if stream is not None:
+            _check(self._L.nf_set_stream(h, C.c_void_p(stream)), h)
+        if mesh is not None:
+            self.load_density(mesh)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._L.nf_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # inputs
+    def load_density(self, mesh):
+        m = np.ascontiguousarray(mesh, np.float32)
+        nx, ny, nz = m.shape
+        _check(self._L.nf_load_density(self._h, nx, ny, nz, m.ctypes.data_as(C.c_void_p)), self._h)
+
+    # stages
+    def generate(self):
+        s = NfGenStats()
+        _check(self._L.nf_generate(self._h, C.byref(s)), self._h, "nf_generate")
+        return {k: getattr(s, k) for k, _ in s._fields_}
+
+    def contacts(self):
+        s = NfContactStats()
+        _check(self._L.nf_contacts(self._h, C.byref(s)), self._h, "nf_contacts")
+        return {k: getattr(s, k) for k, _ in s._fields_}
+
+    def solve(self, check=True):
+        s = NfSolveStats()
+        st = self._L.nf_solve(self._h, C.byref(s))
+        if check:
+            _check(st, self._h, "nf_solve")
+        out = {k: getattr(s, k) for k, _ in s._fields_}
+        out["status"] = st
+        return out
+
+    def adjoint(self):
+        n = self.n_rods()
+        g = np.zeros((n, 6), np.float32)
+        dl, dg0 = C.c_double(), C.c_double()
+        _check(self._L.nf_adjoint(self._h, g.ctypes.data_as(C.c_void_p), n, C.byref(dl), C.byref(dg0)),
+               self._h, "nf_adjoint")
+        return g, dl.value, dg0.value
+
+    # outputs
+    def n_rods(self):
+        r = NfRods()
+        r.capacity = 0
+        st = self._L.nf_get_rods(self._h, C.byref(r))
+        if st not in (0, 5):
+            _check(st, self._h, "nf_get_rods")
+        return int(r.count)
+
+    def rods(self):
+        n = self.n_rods()
+        out = {f: np.zeros(n, np.float32) for f in ("x", "y", "z", "cx", "cy", "cz", "l", "a")}
+        out["stream_index"] = np.zeros(n, np.uint64)
+        out["cell"] = np.zeros(n, np.uint32)
+        r = NfRods()
+        r.capacity = n
+        for f in ("x", "y", "z", "cx", "cy", "cz", "l", "a"):
+            setattr(r, f, _f32p(out[f]))
+        r.stream_index = out["stream_index"].ctypes.data_as(C.POINTER(C.c_uint64))
+        r.cell = out["cell"].ctypes.data_as(C.POINTER(C.c_uint32))
+        _check(self._L.nf_get_rods(self._h, C.byref(r)), self._h, "nf_get_rods")
+        return out
+
+    def set_rods(self, rods):
+        n = len(rods["x"])
+        arrs = {f: np.ascontiguousarray(rods[f], np.float32) for f in ("x", "y", "z", "cx", "cy", "cz", "l", "a")}
+        r = NfRods()
+        r.capacity = n
+        r.count = n
+        for f, a in arrs.items():
+            setattr(r, f, _f32p(a))
+        si = None
+        if rods.get("stream_index") is not None:
+            si = np.ascontiguousarray(rods["stream_index"], np.uint64)
+            r.stream_index = si.ctypes.data_as(C.POINTER(C.c_uint64))
+        _check(self._L.nf_set_rods(self._h, C.byref(r)), self._h, "nf_set_rods")
+
+    def contact_list(self):
+        c = NfContactList()
+        c.capacity = 0
+        st = self._L.nf_get_contacts(self._h, C.byref(c))
+        if st not in (0, 5):
+            _check(st, self._h, "nf_get_contacts")
+        n = int(c.count)
+        out = dict(I=np.zeros(n, np.uint32), J=np.zeros(n, np.uint32), tI=np.zeros(n, np.float32),
+                   tJ=np.zeros(n, np.float32), D=np.zeros(n), G=np.zeros(n), S=np.zeros(n),
+                   image=np.zeros((n, 3), np.int8))
+        c.capacity = n
+        c.I = out["I"].ctypes.data_as(C.POINTER(C.c_uint32))
+        c.J = out["J"].ctypes.data_as(C.POINTER(C.c_uint32))
+        c.tI = _f32p(out["tI"])
+        c.tJ = _f32p(out["tJ"])
+        for f in ("D", "G", "S"):
+            setattr(c, f, out[f].ctypes.data_as(C.POINTER(C.c_double)))
+        c.image = out["image"].ctypes.data_as(C.POINTER(C.c_int8))
+        _check(self._L.nf_get_contacts(self._h, C.byref(c)), self._h, "nf_get_contacts")
+        return out
+
+    def voltages(self):
+        n = self.n_rods()
+        v = np.zeros(n)
+        _check(self._L.nf_get_voltages(self._h, v.ctypes.data_as(C.c_void_p), n), self._h, "nf_get_voltages")
+        return v
+
+    def stream(self, k0, n):
+        out = np.zeros((10, n), np.float32)
+        ptrs = [out[i].ctypes.data_as(C.c_void_p) for i in range(10)]
+        _check(self._L.nf_stream_candidates(self._h, k0, n, *ptrs), self._h, "nf_stream_candidates")
+        return out.T.copy()
+
+    # files
+    def write_vtk(self, path):
+        _check(self._L.nf_write_vtk(self._h, str(path).encode()), self._h, "nf_write_vtk")
+
+    def write_state(self, path):
+        _check(self._L.nf_write_state_bin(self._h, str(path).encode()), self._h, "nf_write_state_bin")
+
+    def read_state(self, path):
+        _check(self._L.nf_read_state_bin(self._h, str(path).encode()), self._h, "nf_read_state_bin")
+
+    def write_coo(self, directory):
+        _check(self._L.nf_write_coo(self._h, str(directory).encode()), self._h, "nf_write_coo")
+
+
+def batch_run(param_list):
+    """All realisations in one engine (shared launches); returns (results, stats)."""
+    L = load()
+    n = len(param_list)
+    arr = (NfParams * n)(*[make_params(p) for p in param_list])
+    res = (NfBatchResult * n)()
+    st = NfBatchStats()
+    _check(L.nf_batch_run(arr, n, res, C.byref(st)), what="nf_batch_run")
+    out = [{k: getattr(r, k) for k, _ in r._fields_} for r in res]
+    return out, {k: getattr(st, k) for k, _ in st._fields_}

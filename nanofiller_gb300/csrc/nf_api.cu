@@ -1,0 +1,695 @@
+// nf_api.cu -- the C ABI (include/nanofiller_gb300.h) over the GB300 engine,
+// the reference keyword parser and the reference file formats.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <iomanip>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "nf_engine.cuh"
+
+struct nf_handle {
+    nf::Engine E;
+    nf_params p;
+};
+
+namespace {
+
+nf_status fail(nf_handle* h, nf_status s, const std::string& msg) {
+    if (h) h->E.err = msg;
+    return s;
+}
+
+bool read_density(const char* path, int ext[3], float dim[3], std::vector<float>* vals) {
+    // read_density (src/IO.cpp:11-36): "Lx Ly Lz" "nx ny nz" then nx*ny*nz values.
+    std::ifstream f(path);
+    if (!f.is_open()) return false;
+    if (!(f >> dim[0] >> dim[1] >> dim[2] >> ext[0] >> ext[1] >> ext[2])) return false;
+    if (ext[0] <= 0 || ext[1] <= 0 || ext[2] <= 0) return false;
+    size_t n = (size_t)ext[0] * ext[1] * ext[2];
+    if (vals) {
+        vals->resize(n);
+        for (size_t i = 0; i < n; ++i)
+            if (!(f >> (*vals)[i])) return false;
+    }
+    return true;
+}
+
+nf_status validate(const nf_params& p, std::string* why) {
+    for (int d = 0; d < 3; ++d)
+        if (!(p.box[d] > 0)) { *why = "box edges must be positive"; return NF_ERR_PARAM; }
+    if (!(p.l > 0) || !(p.a > 0)) { *why = "rod length and radius must be positive"; return NF_ERR_PARAM; }
+    if (!(p.vf > 0) && p.n_target <= 0) { *why = "volume fraction or target count required"; return NF_ERR_PARAM; }
+    if (p.field_dir != 0 && p.field_dir != 1 && p.field_dir != 2 && p.field_dir != 4) {
+        *why = "FIELD_DIR must be 0, 1, 2 or 4"; return NF_ERR_PARAM;
+    }
+    if (p.self_align_step > 0 || p.clust_flag || p.reduce_flag) {
+        *why = "self-alignment, clusterisation and thin-out are not run by this path"; return NF_ERR_UNSUPPORTED;
+    }
+    if (p.theta_dev > 0 || p.phi_dev > 0) {
+        *why = "truncated-normal orientation is not run by this path (use ORIENT VMF)"; return NF_ERR_UNSUPPORTED;
+    }
+    if (p.orient_mode == NF_ORIENT_VMF && !(p.vmf_kappa > 0)) { *why = "VMF_KAPPA must be positive"; return NF_ERR_PARAM; }
+    if (p.len_mode == NF_SIZE_LOGNORMAL && !(p.len_min > 0 && p.len_max >= p.len_min)) {
+        *why = "LEN_CLIP lo hi required for lognormal lengths"; return NF_ERR_PARAM;
+    }
+    if (p.rad_mode == NF_SIZE_UNIFORM && !(p.rad_min > 0 && p.rad_max >= p.rad_min)) {
+        *why = "RAD_RANGE lo hi required for uniform radii"; return NF_ERR_PARAM;
+    }
+    if (!(p.lambda > 0) || !(p.G0 > 0)) { *why = "tunnelling law needs G0 > 0 and lambda > 0"; return NF_ERR_PARAM; }
+    double reach = nf::stage_reach(p);
+    for (int d = 0; d < 3; ++d)
+        if ((p.gen_periodic >> d & 1) && p.box[d] < reach) {
+            *why = "a periodic box edge is shorter than the pair reach (rod would meet its own image)";
+            return NF_ERR_PARAM;
+        }
+    return NF_OK;
+}
+
+float rad(float deg, float pi) { return deg / 180 * pi; }
+
+}  // namespace
+
+extern "C" {
+
+int nf_abi_version(void) { return NF_ABI_VERSION; }
+
+const char* nf_status_string(nf_status s) {
+    switch (s) {
+        case NF_OK: return "ok";
+        case NF_ERR_PARAM: return "invalid parameter";
+        case NF_ERR_CUDA: return "CUDA error";
+        case NF_ERR_NO_DEVICE: return "no CUDA device";
+        case NF_ERR_ALLOC: return "allocation failed";
+        case NF_ERR_CAPACITY: return "buffer too small";
+        case NF_ERR_OVERFLOW: return "internal list overflow";
+        case NF_ERR_NOT_CONVERGED: return "solve not converged";
+        case NF_ERR_IO: return "I/O error";
+        case NF_ERR_FORMAT: return "malformed file";
+        case NF_ERR_STATE: return "call out of order";
+        case NF_ERR_UNSUPPORTED: return "unsupported option";
+        case NF_ERR_TIMEOUT: return "bounded wait expired";
+    }
+    return "unknown status";
+}
+
+nf_status nf_params_default(nf_params* p) {
+    if (!p) return NF_ERR_PARAM;
+    std::memset(p, 0, sizeof(*p));
+    // simPrms::simPrms (src/simPrms.cpp:22-117)
+    p->vf = 0.05f / 100.0f;
+    p->vf_precision = 0.05f;
+    p->theta_med = 0; p->theta_dev = -1; p->phi_med = 0; p->phi_dev = -1;
+    p->l = 4; p->a = 0.010f; p->l_dev = -1; p->a_dev = -1;
+    p->tol = 1.e-6f;
+    p->sep = 0; p->sc_frac = 1.0f;
+    p->stat_dist_lim = 0.015f;
+    p->wrt_bin = 0;
+    p->self_align_step = 0;  // the reference defaults to 50; this path runs without self-alignment
+    p->clust_flag = 0; p->reduce_flag = 0;
+    // project keys
+    p->seed = 0;
+    p->n_candidates = 1ull << 20;
+    p->n_target = 0;
+    p->gen_periodic = 7;
+    p->field_dir = 4;
+    p->orient_mode = NF_ORIENT_ISOTROPIC;
+    p->density_default = 1.0f;
+    p->G0 = 1e-5;
+    p->lambda = 0.18e-3;
+    p->d_c = 0.34e-3;
+    p->screening = 1;
+    p->solve_max_iter = 20000;
+    p->solve_tol = 1e-10;
+    return NF_OK;
+}
+
+nf_status nf_params_from_file(const char* path, nf_params* p, int* n_unknown) {
+    if (!path || !p) return NF_ERR_PARAM;
+    std::ifstream f(path);
+    if (!f.is_open()) return NF_ERR_IO;
+    const float PI_ = 3.141593f, Pi = 3.14159265359f;  // inc/vectorMath.h:7, inc/simPrms.h:82
+    int unknown = 0;
+    std::string line;
+    while (std::getline(f, line)) {
+        if (line.empty()) continue;
+        size_t k = line.find_first_of(" \t");
+        std::string key = line.substr(0, k);
+        std::string rest = k == std::string::npos ? "" : line.substr(k + 1);
+        std::istringstream in(rest);
+        if (key.empty() || key[0] == '#') continue;
+        float v;
+        if (key == "WRT_BIN") in >> p->wrt_bin;
+        else if (key == "VOLUME_PERCENT") { in >> v; p->vf = v / 100; }
+        else if (key == "VOLUME_PERCENT_LIST") { int n; in >> n; for (int i = 0; i < n; ++i) in >> v; }
+        else if (key == "VOL_FRAC_PRECISION") in >> p->vf_precision;
+        else if (key == "SPAT_DISTR_FILE") {
+            std::string name;
+            in >> name;
+            if (name == "NONE") {
+                in >> p->box[0] >> p->box[1] >> p->box[2] >> p->mesh_ext[0] >> p->mesh_ext[1] >> p->mesh_ext[2];
+                p->density_file[0] = 0;
+            } else {
+                std::snprintf(p->density_file, sizeof(p->density_file), "%s", name.c_str());
+            }
+        }
+        else if (key == "PREF_ORT_PHI") { in >> v; p->pref_ort[0] = rad(v, PI_); }
+        else if (key == "PREF_ORT_THETA") { in >> v; p->pref_ort[1] = rad(v, Pi); }
+        else if (key == "DEF_THETA_MED") { in >> v; p->theta_med = rad(v, Pi); }
+        else if (key == "DEF_PHI_MED") { in >> v; p->phi_med = rad(v, Pi); }
+        else if (key == "DEF_THETA_DEV") { in >> v; p->theta_dev = v > 0 ? rad(v, Pi) : -1; }
+        else if (key == "DEF_PHI_DEV") { in >> v; p->phi_dev = v > 0 ? rad(v, Pi) : -1; }
+        else if (key == "INC_LEN_MED") in >> p->l;
+        else if (key == "INC_LEN_DEV") in >> p->l_dev;
+        else if (key == "INC_RAD_MED") in >> p->a;
+        else if (key == "INC_RAD_DEV") in >> p->a_dev;
+        else if (key == "INC_SEPARATION") in >> p->sep;
+        else if (key == "INC_SOFTCORE") in >> p->sc_frac;
+        else if (key == "STAT_DIST_LIM") in >> p->stat_dist_lim;
+        else if (key == "SELF_ALLIGN_STEP") in >> p->self_align_step;
+        else if (key == "REDUCE_FLAG") in >> p->reduce_flag;
+        else if (key == "CLUST_FLAG") in >> p->clust_flag;
+        else if (key == "CLUST_DIST_LIM" || key == "CLUST_ANGL_LIM" || key == "SPAT_DIMENSIONS" ||
+                 key == "ORNT_DISTR_FILE" || key == "IDIM_DISTR_FILE" || key == "MATH_TOLERANCE" ||
+                 key == "DMN_CELL_MARGE") { /* parsed and ignored, as the reference does */ }
+        // project keys
+        else if (key == "SEED") { unsigned long long s; in >> s; p->seed = s; }
+        else if (key == "CANDIDATES") { unsigned long long s; in >> s; p->n_candidates = s; }
+        else if (key == "TARGET_COUNT") { long long s; in >> s; p->n_target = s; }
+        else if (key == "PERIODIC") in >> p->gen_periodic;
+        else if (key == "FIELD_DIR") in >> p->field_dir;
+        else if (key == "ORIENT") {
+            std::string m; in >> m;
+            p->orient_mode = (m == "VMF" || m == "1") ? NF_ORIENT_VMF : NF_ORIENT_ISOTROPIC;
+        }
+        else if (key == "VMF_KAPPA") in >> p->vmf_kappa;
+        else if (key == "LEN_LAW") { std::string m; in >> m; p->len_mode = (m == "LOGNORMAL" || m == "1") ? NF_SIZE_LOGNORMAL : NF_SIZE_CONST; }
+        else if (key == "LEN_SIGMA_LN") in >> p->len_sigma_ln;
+        else if (key == "LEN_CLIP") in >> p->len_min >> p->len_max;
+        else if (key == "RAD_LAW") { std::string m; in >> m; p->rad_mode = (m == "UNIFORM" || m == "2") ? NF_SIZE_UNIFORM : NF_SIZE_CONST; }
+        else if (key == "RAD_RANGE") in >> p->rad_min >> p->rad_max;
+        else if (key == "DENSITY_DEFAULT") in >> p->density_default;
+        else if (key == "CELL_EDGE") in >> p->cell_edge;
+        else if (key == "TUNNEL_G0") in >> p->G0;
+        else if (key == "TUNNEL_LAMBDA") in >> p->lambda;
+        else if (key == "TUNNEL_DC") in >> p->d_c;
+        else if (key == "REF_PARALLEL_TYPO") in >> p->ref_parallel_typo;
+        else if (key == "SCREENING") in >> p->screening;
+        else if (key == "ROUND_CANDIDATES") in >> p->round_candidates;
+        else if (key == "SOLVE_MAX_ITER") in >> p->solve_max_iter;
+        else if (key == "SOLVE_TOL") in >> p->solve_tol;
+        else ++unknown;  // the reference prints "UNRECOGNISED STRING FOUND" and continues
+    }
+    if (n_unknown) *n_unknown = unknown;
+    return NF_OK;
+}
+
+nf_status nf_target_count(const nf_params* p, int64_t* n) {
+    if (!p || !n) return NF_ERR_PARAM;
+    *n = nf::target_count(*p);
+    return NF_OK;
+}
+
+nf_status nf_read_density_file(const char* path, int ext[3], float dim[3], float* values, size_t capacity) {
+    if (!path || !ext || !dim) return NF_ERR_PARAM;
+    std::vector<float> v;
+    std::ifstream f(path);
+    if (!f.is_open()) return NF_ERR_IO;
+    f.close();
+    if (!read_density(path, ext, dim, values ? &v : nullptr)) return NF_ERR_FORMAT;
+    if (values) {
+        if (capacity < v.size()) return NF_ERR_CAPACITY;
+        std::copy(v.begin(), v.end(), values);
+    }
+    return NF_OK;
+}
+
+nf_status nf_create(const nf_params* p, nf_handle** out) {
+    if (!p || !out) return NF_ERR_PARAM;
+    *out = nullptr;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return NF_ERR_NO_DEVICE;
+    nf_handle* h = new (std::nothrow) nf_handle();
+    if (!h) return NF_ERR_ALLOC;
+    h->p = *p;
+    std::vector<float> mesh;
+    if (h->p.density_file[0]) {
+        int ext[3];
+        float dim[3];
+        std::ifstream f(h->p.density_file);
+        if (!f.is_open()) { delete h; return NF_ERR_IO; }
+        f.close();
+        if (!read_density(h->p.density_file, ext, dim, &mesh)) { delete h; return NF_ERR_FORMAT; }
+        for (int d = 0; d < 3; ++d) { h->p.box[d] = dim[d]; h->p.mesh_ext[d] = ext[d]; }
+    }
+    std::string why;
+    nf_status s = validate(h->p, &why);
+    if (s != NF_OK) { delete h; return s; }
+    std::vector<const float*> meshes(1, mesh.empty() ? nullptr : mesh.data());
+    if (mesh.empty()) h->p.mesh_ext[0] = h->p.mesh_ext[1] = h->p.mesh_ext[2] = 0;
+    s = h->E.init(&h->p, 1, meshes);
+    if (s != NF_OK) { delete h; return s; }
+    *out = h;
+    return NF_OK;
+}
+
+nf_status nf_destroy(nf_handle* h) {
+    if (!h) return NF_ERR_PARAM;
+    h->E.release();
+    delete h;
+    return NF_OK;
+}
+
+nf_status nf_set_stream(nf_handle* h, void* stream) {
+    if (!h) return NF_ERR_PARAM;
+    h->E.st = (cudaStream_t)stream;
+    return NF_OK;
+}
+
+nf_status nf_last_error(const nf_handle* h, char* buf, size_t n) {
+    if (!h || !buf || n == 0) return NF_ERR_PARAM;
+    std::snprintf(buf, n, "%s", h->E.err.c_str());
+    return NF_OK;
+}
+
+nf_status nf_load_density(nf_handle* h, int nx, int ny, int nz, const float* values) {
+    if (!h || !values || nx <= 0 || ny <= 0 || nz <= 0) return NF_ERR_PARAM;
+    h->p.mesh_ext[0] = nx; h->p.mesh_ext[1] = ny; h->p.mesh_ext[2] = nz;
+    return h->E.set_density(0, nx, ny, nz, values);
+}
+
+nf_status nf_generate(nf_handle* h, nf_gen_stats* stats) {
+    if (!h) return NF_ERR_PARAM;
+    nf_status s = h->E.generate();
+    if (stats) *stats = h->E.gst;
+    return s;
+}
+
+nf_status nf_stream_candidates(nf_handle* h, uint64_t k0, uint64_t n, float* x, float* y, float* z, float* cx,
+                               float* cy, float* cz, float* l, float* a, float* u, float* rho) {
+    if (!h) return NF_ERR_PARAM;
+    std::vector<float> o(10 * n);
+    nf_status s = h->E.stream_dump(k0, n, o.data());
+    if (s != NF_OK) return s;
+    float* dst[10] = {x, y, z, cx, cy, cz, l, a, u, rho};
+    for (int f = 0; f < 10; ++f)
+        if (dst[f])
+            for (uint64_t i = 0; i < n; ++i) dst[f][i] = o[10 * i + f];
+    return NF_OK;
+}
+
+nf_status nf_get_rods(nf_handle* h, nf_rods* out) {
+    if (!h || !out) return NF_ERR_PARAM;
+    nf::Engine& E = h->E;
+    if (E.count.empty() || !E.cells_valid) return fail(h, NF_ERR_STATE, "no rods");
+    size_t n = E.count[0];
+    out->count = n;
+    if (out->capacity < n) return NF_ERR_CAPACITY;
+    std::vector<float4> p(n), d(n);
+    std::vector<uint64_t> k(n);
+    cudaError_t e = cudaMemcpyAsync(p.data(), E.pos.p, sizeof(float4) * n, cudaMemcpyDeviceToHost, E.st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d.data(), E.dir.p, sizeof(float4) * n, cudaMemcpyDeviceToHost, E.st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(k.data(), E.sidx.p, sizeof(uint64_t) * n, cudaMemcpyDeviceToHost, E.st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(E.st);
+    if (e != cudaSuccess) return E.cuda_fail(e, "nf_get_rods");
+    const nf::Real& Re = E.hreal[0];
+    for (size_t i = 0; i < n; ++i) {
+        if (out->x) out->x[i] = p[i].x;
+        if (out->y) out->y[i] = p[i].y;
+        if (out->z) out->z[i] = p[i].z;
+        if (out->l) out->l[i] = p[i].w;
+        if (out->cx) out->cx[i] = d[i].x;
+        if (out->cy) out->cy[i] = d[i].y;
+        if (out->cz) out->cz[i] = d[i].z;
+        if (out->a) out->a[i] = d[i].w;
+        if (out->stream_index) out->stream_index[i] = k[i];
+        if (out->cell) out->cell[i] = nf::cell_of(Re, p[i].x, p[i].y, p[i].z);
+    }
+    return NF_OK;
+}
+
+nf_status nf_set_rods(nf_handle* h, const nf_rods* in) {
+    if (!h || !in || !in->x || !in->y || !in->z || !in->cx || !in->cy || !in->cz || !in->l || !in->a)
+        return NF_ERR_PARAM;
+    size_t n = in->count;
+    std::vector<float4> p(n), d(n);
+    for (size_t i = 0; i < n; ++i) {
+        p[i] = make_float4(in->x[i], in->y[i], in->z[i], in->l[i]);
+        d[i] = make_float4(in->cx[i], in->cy[i], in->cz[i], in->a[i]);
+    }
+    return h->E.inject(n, p.data(), d.data(), in->stream_index);
+}
+
+nf_status nf_contacts(nf_handle* h, nf_contact_stats* stats) {
+    if (!h) return NF_ERR_PARAM;
+    nf_status s = h->E.contacts();
+    if (stats) *stats = h->E.cst;
+    return s;
+}
+
+nf_status nf_get_contacts(nf_handle* h, nf_contact_list* out) {
+    if (!h || !out) return NF_ERR_PARAM;
+    nf::Engine& E = h->E;
+    if (!E.contacts_valid) return fail(h, NF_ERR_STATE, "no contacts");
+    size_t lo = E.ct_off[0], n = E.ct_off[1] - lo;
+    out->count = n;
+    if (out->capacity < n) return NF_ERR_CAPACITY;
+    std::vector<uint32_t> I(n), J(n);
+    std::vector<double> t0(n), t1(n), D(n), G(n), S(n);
+    std::vector<int8_t> img(3 * n);
+    cudaError_t e = cudaSuccess;
+    auto cp = [&](void* dst, const void* src, size_t bytes) {
+        if (e == cudaSuccess && bytes) e = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, E.st);
+    };
+    cp(I.data(), E.cI.p + lo, 4 * n); cp(J.data(), E.cJ.p + lo, 4 * n);
+    cp(t0.data(), E.ct0.p + lo, 8 * n); cp(t1.data(), E.ct1.p + lo, 8 * n);
+    cp(D.data(), E.cD.p + lo, 8 * n); cp(G.data(), E.cG.p + lo, 8 * n); cp(S.data(), E.cS.p + lo, 8 * n);
+    cp(img.data(), E.cimg.p + 3 * lo, 3 * n);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(E.st);
+    if (e != cudaSuccess) return E.cuda_fail(e, "nf_get_contacts");
+    const uint32_t off = E.hreal[0].rod_off;
+    for (size_t q = 0; q < n; ++q) {
+        if (out->I) out->I[q] = I[q] - off;
+        if (out->J) out->J[q] = J[q] >= NF_SNK_ELEC ? J[q] : J[q] - off;
+        if (out->tI) out->tI[q] = (float)t0[q];
+        if (out->tJ) out->tJ[q] = (float)t1[q];
+        if (out->D) out->D[q] = D[q];
+        if (out->G) out->G[q] = G[q];
+        if (out->S) out->S[q] = S[q];
+        if (out->image) for (int d = 0; d < 3; ++d) out->image[3 * q + d] = img[3 * q + d];
+    }
+    return NF_OK;
+}
+
+nf_status nf_solve(nf_handle* h, nf_solve_stats* stats) {
+    if (!h) return NF_ERR_PARAM;
+    nf_status s = h->E.solve();
+    if (stats && !h->E.solve_st.empty()) *stats = h->E.solve_st[0];
+    return s;
+}
+
+nf_status nf_get_voltages(nf_handle* h, double* v, size_t capacity) {
+    if (!h || !v) return NF_ERR_PARAM;
+    nf::Engine& E = h->E;
+    if (!E.solve_valid) return fail(h, NF_ERR_STATE, "no solution");
+    size_t n = E.count[0];
+    if (capacity < n) return NF_ERR_CAPACITY;
+    cudaError_t e = cudaMemcpyAsync(v, E.volt.p, sizeof(double) * n, cudaMemcpyDeviceToHost, E.st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(E.st);
+    if (e != cudaSuccess) return E.cuda_fail(e, "nf_get_voltages");
+    return NF_OK;
+}
+
+nf_status nf_adjoint(nf_handle* h, float* dG_dend, size_t capacity, double* dG_dlambda, double* dG_dG0) {
+    if (!h) return NF_ERR_PARAM;
+    return h->E.adjoint(0, dG_dend, capacity, dG_dlambda, dG_dG0);
+}
+
+nf_status nf_batch_run(const nf_params* params, int n, nf_batch_result* out, nf_batch_stats* stats) {
+    if (!params || n <= 0 || !out) return NF_ERR_PARAM;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return NF_ERR_NO_DEVICE;
+    std::vector<nf_params> ps(params, params + n);
+    std::vector<std::vector<float>> meshes(n);
+    std::vector<const float*> mp(n, nullptr);
+    for (int r = 0; r < n; ++r) {
+        std::string why;
+        if (ps[r].density_file[0]) {
+            int ext[3];
+            float dim[3];
+            if (!read_density(ps[r].density_file, ext, dim, &meshes[r])) return NF_ERR_FORMAT;
+            for (int d = 0; d < 3; ++d) { ps[r].box[d] = dim[d]; ps[r].mesh_ext[d] = ext[d]; }
+            mp[r] = meshes[r].data();
+        } else {
+            ps[r].mesh_ext[0] = ps[r].mesh_ext[1] = ps[r].mesh_ext[2] = 0;
+        }
+        nf_status s = validate(ps[r], &why);
+        if (s != NF_OK) return s;
+    }
+    nf::Engine E;
+    nf_status s = E.init(ps.data(), n, mp);
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (s == NF_OK) {
+        cudaEventCreate(&e0);
+        cudaEventCreate(&e1);
+        cudaEventRecord(e0, E.st);
+        s = E.generate();
+    }
+    if (s == NF_OK) s = E.contacts();
+    nf_status ss = NF_OK;
+    if (s == NF_OK) ss = E.solve();
+    if (s == NF_OK && (ss == NF_OK || ss == NF_ERR_NOT_CONVERGED)) {
+        for (int r = 0; r < n; ++r) {
+            const nf_solve_stats& S = E.solve_st[r];
+            out[r].accepted = E.count[r];
+            out[r].contacts = E.ct_int[r];
+            out[r].G_eff = S.G_eff;
+            out[r].residual = S.residual;
+            out[r].percolating = S.percolating;
+            out[r].status = (S.n_active > 0 && !(S.residual <= ps[r].solve_tol)) ? NF_ERR_NOT_CONVERGED : NF_OK;
+        }
+        if (stats) {
+            float ms = 0;
+            cudaEventRecord(e1, E.st);
+            cudaEventSynchronize(e1);
+            cudaEventElapsedTime(&ms, e0, e1);
+            stats->n = n;
+            stats->rounds = E.gst.rounds;
+            stats->rods = E.gst.accepted;
+            stats->contacts = E.cst.contacts;
+            stats->ms = ms;
+        }
+    } else if (s == NF_OK) {
+        s = ss;
+    }
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    E.release();
+    return s;
+}
+
+// ---------------------------------------------------------------------------
+// Files.
+// ---------------------------------------------------------------------------
+nf_status nf_format_write_vtk(const char* path, size_t n, const float* x, const float* y, const float* z,
+                              const float* cx, const float* cy, const float* cz, const float* l, const float* a,
+                              const float* k) {
+    if (!path || (n && (!x || !y || !z || !cx || !cy || !cz || !l || !a || !k))) return NF_ERR_PARAM;
+    // write_CNTvtk (src/IO.cpp:38-76)
+    std::ofstream v(path, std::ios::out | std::ios::trunc);
+    if (!v.is_open()) return NF_ERR_IO;
+    v << "# vtk DataFile Version 2.0" << std::endl;
+    v << "CUDA generated CNTs" << std::endl;
+    v << "ASCII" << std::endl;
+    v << "DATASET UNSTRUCTURED_GRID" << std::endl;
+    v << "POINTS " << n << " float" << std::endl;
+    for (size_t i = 0; i < n; ++i)
+        v << std::setw(12) << std::setprecision(6) << x[i] << std::setw(12) << std::setprecision(6) << y[i]
+          << std::setw(12) << std::setprecision(6) << z[i] << std::endl;
+    v << "POINT_DATA " << n << std::endl;
+    v << "VECTORS CNT float" << std::endl;
+    for (size_t i = 0; i < n; ++i)
+        v << std::setw(15) << std::setprecision(6) << cx[i] << std::setw(15) << std::setprecision(6) << cy[i]
+          << std::setw(15) << std::setprecision(6) << cz[i] << std::endl;
+    v << "SCALARS LAK float 3" << std::endl;
+    v << "LOOKUP_TABLE default" << std::endl;
+    for (size_t i = 0; i < n; ++i)
+        v << std::setw(12) << std::setprecision(6) << l[i] << std::setw(12) << std::setprecision(6) << a[i]
+          << std::setw(12) << std::setprecision(6) << k[i] << std::endl;
+    return v.good() ? NF_OK : NF_ERR_IO;
+}
+
+nf_status nf_format_write_state_bin(const char* path, const nf_state_header* hd, const int16_t* occ,
+                                    const int32_t* addr, const float* planes) {
+    if (!path || !hd) return NF_ERR_PARAM;
+    size_t cells = (size_t)hd->ext[0] * hd->ext[1] * hd->ext[2];
+    if ((cells && (!occ || !addr)) || (hd->ttl > 0 && !planes)) return NF_ERR_PARAM;
+    // save_state_BIN (src/stateSR.cpp:54-89)
+    std::ofstream o(path, std::ios::out | std::ios::binary);
+    if (!o.is_open()) return NF_ERR_IO;
+    o.write((const char*)hd->phys_dim, 3 * sizeof(float));
+    o.write((const char*)hd->edge, 3 * sizeof(float));
+    o.write((const char*)hd->ext, 3 * sizeof(int32_t));
+    o.write((const char*)&hd->l, sizeof(float));
+    o.write((const char*)&hd->a, sizeof(float));
+    o.write((const char*)&hd->ttl, sizeof(int32_t));
+    o.write((const char*)&hd->num, sizeof(int32_t));
+    o.write((const char*)&hd->tol, sizeof(float));
+    o.write((const char*)occ, cells * sizeof(int16_t));
+    o.write((const char*)addr, cells * sizeof(int32_t));
+    o.write((const char*)planes, 9ull * hd->ttl * sizeof(float));
+    return o.good() ? NF_OK : NF_ERR_IO;
+}
+
+nf_status nf_format_read_state_bin(const char* path, nf_state_header* hd, int16_t* occ, int32_t* addr,
+                                   float* planes, size_t cells_cap, size_t planes_cap) {
+    if (!path || !hd) return NF_ERR_PARAM;
+    // read_state_BIN (src/stateSR.cpp:90-134)
+    std::ifstream f(path, std::ios::in | std::ios::binary);
+    if (!f.is_open()) return NF_ERR_IO;
+    f.read((char*)hd->phys_dim, 3 * sizeof(float));
+    f.read((char*)hd->edge, 3 * sizeof(float));
+    f.read((char*)hd->ext, 3 * sizeof(int32_t));
+    f.read((char*)&hd->l, sizeof(float));
+    f.read((char*)&hd->a, sizeof(float));
+    f.read((char*)&hd->ttl, sizeof(int32_t));
+    f.read((char*)&hd->num, sizeof(int32_t));
+    f.read((char*)&hd->tol, sizeof(float));
+    if (!f.good()) return NF_ERR_FORMAT;
+    if (hd->ext[0] <= 0 || hd->ext[1] <= 0 || hd->ext[2] <= 0 || hd->ttl < 0 || hd->num < 0) return NF_ERR_FORMAT;
+    size_t cells = (size_t)hd->ext[0] * hd->ext[1] * hd->ext[2];
+    if (!occ && !addr && !planes) return NF_OK;
+    if (cells_cap < cells || planes_cap < 9ull * hd->ttl) return NF_ERR_CAPACITY;
+    std::vector<int16_t> o(cells);
+    std::vector<int32_t> a(cells);
+    f.read((char*)o.data(), cells * sizeof(int16_t));
+    f.read((char*)a.data(), cells * sizeof(int32_t));
+    std::vector<float> pl(9ull * hd->ttl);
+    f.read((char*)pl.data(), pl.size() * sizeof(float));
+    if (!f.good()) return NF_ERR_FORMAT;
+    if (occ) std::copy(o.begin(), o.end(), occ);
+    if (addr) std::copy(a.begin(), a.end(), addr);
+    if (planes) std::copy(pl.begin(), pl.end(), planes);
+    return NF_OK;
+}
+
+// Rods of the handle grouped by cell (the repacked layout of simPrms::repack,
+// src/simPrms.cpp:691-743), k = global cell id (set_k2dmnIdx, src/simPrms_device.cu:7-39).
+static nf_status cell_layout(nf_handle* h, nf_state_header* hd, std::vector<int16_t>* occ, std::vector<int32_t>* addr,
+                             std::vector<float>* planes, std::vector<uint32_t>* order) {
+    nf::Engine& E = h->E;
+    size_t n = E.count.empty() ? 0 : E.count[0];
+    std::vector<float> x(n), y(n), z(n), cx(n), cy(n), cz(n), l(n), a(n);
+    std::vector<uint32_t> cell(n);
+    nf_rods r{};
+    r.capacity = n;
+    r.x = x.data(); r.y = y.data(); r.z = z.data(); r.cx = cx.data(); r.cy = cy.data(); r.cz = cz.data();
+    r.l = l.data(); r.a = a.data(); r.cell = cell.data();
+    nf_status s = nf_get_rods(h, &r);
+    if (s != NF_OK) return s;
+    const nf::Real& Re = E.hreal[0];
+    size_t ncell = (size_t)Re.n[0] * Re.n[1] * Re.n[2];
+    occ->assign(ncell, 0);
+    addr->assign(ncell, 0);
+    std::vector<uint32_t> cnt(ncell, 0);
+    for (size_t i = 0; i < n; ++i) ++cnt[cell[i]];
+    for (size_t c = 0; c < ncell; ++c) {
+        if (cnt[c] > 32767) return fail(h, NF_ERR_OVERFLOW, "cell occupancy exceeds the short range of output.bin");
+        (*occ)[c] = (int16_t)cnt[c];
+        (*addr)[c] = (int32_t)(cnt[c] + (c ? (*addr)[c - 1] : 0));
+    }
+    order->resize(n);
+    std::vector<uint32_t> cur(ncell, 0);
+    for (size_t i = 0; i < n; ++i) {
+        uint32_t c = cell[i];
+        uint32_t q = (c ? (*addr)[c - 1] : 0) + cur[c]++;
+        (*order)[q] = (uint32_t)i;
+    }
+    planes->assign(9 * n, 0.0f);
+    for (size_t q = 0; q < n; ++q) {
+        uint32_t i = (*order)[q];
+        float v[9] = {x[i], y[i], z[i], cx[i], cy[i], cz[i], l[i], a[i], (float)cell[i]};
+        for (int f = 0; f < 9; ++f) (*planes)[f * n + q] = v[f];
+    }
+    for (int d = 0; d < 3; ++d) {
+        hd->phys_dim[d] = Re.L[d];
+        hd->ext[d] = Re.n[d];
+        hd->edge[d] = Re.L[d] / Re.n[d];
+    }
+    hd->l = h->p.l;
+    hd->a = h->p.a;
+    hd->ttl = (int32_t)n;
+    hd->num = (int32_t)n;
+    hd->tol = h->p.tol;
+    return NF_OK;
+}
+
+nf_status nf_write_vtk(nf_handle* h, const char* path) {
+    if (!h || !path) return NF_ERR_PARAM;
+    nf_state_header hd;
+    std::vector<int16_t> occ;
+    std::vector<int32_t> addr;
+    std::vector<float> pl;
+    std::vector<uint32_t> order;
+    nf_status s = cell_layout(h, &hd, &occ, &addr, &pl, &order);
+    if (s != NF_OK) return s;
+    size_t n = hd.num;
+    const float* P = pl.data();
+    return nf_format_write_vtk(path, n, P, P + n, P + 2 * n, P + 3 * n, P + 4 * n, P + 5 * n, P + 6 * n, P + 7 * n,
+                               P + 8 * n);
+}
+
+nf_status nf_write_state_bin(nf_handle* h, const char* path) {
+    if (!h || !path) return NF_ERR_PARAM;
+    nf_state_header hd;
+    std::vector<int16_t> occ;
+    std::vector<int32_t> addr;
+    std::vector<float> pl;
+    std::vector<uint32_t> order;
+    nf_status s = cell_layout(h, &hd, &occ, &addr, &pl, &order);
+    if (s != NF_OK) return s;
+    return nf_format_write_state_bin(path, &hd, occ.data(), addr.data(), pl.data());
+}
+
+nf_status nf_read_state_bin(nf_handle* h, const char* path) {
+    if (!h || !path) return NF_ERR_PARAM;
+    nf_state_header hd;
+    nf_status s = nf_format_read_state_bin(path, &hd, nullptr, nullptr, nullptr, 0, 0);
+    if (s != NF_OK) return s;
+    size_t cells = (size_t)hd.ext[0] * hd.ext[1] * hd.ext[2];
+    std::vector<int16_t> occ(cells);
+    std::vector<int32_t> addr(cells);
+    std::vector<float> pl(9ull * hd.ttl);
+    s = nf_format_read_state_bin(path, &hd, occ.data(), addr.data(), pl.data(), cells, pl.size());
+    if (s != NF_OK) return s;
+    // Valid slots of cell c: [Addr[c-1], Addr[c-1] + Occ[c]).
+    std::vector<float4> p, d;
+    size_t ttl = hd.ttl;
+    for (size_t c = 0; c < cells; ++c) {
+        size_t b = c ? (size_t)addr[c - 1] : 0;
+        for (int k = 0; k < occ[c]; ++k) {
+            size_t q = b + k;
+            if (q >= ttl) return NF_ERR_FORMAT;
+            p.push_back(make_float4(pl[q], pl[ttl + q], pl[2 * ttl + q], pl[6 * ttl + q]));
+            d.push_back(make_float4(pl[3 * ttl + q], pl[4 * ttl + q], pl[5 * ttl + q], pl[7 * ttl + q]));
+        }
+    }
+    for (int k = 0; k < 3; ++k) h->p.box[k] = hd.phys_dim[k];
+    h->E.prm[0].box[0] = hd.phys_dim[0];
+    h->E.prm[0].box[1] = hd.phys_dim[1];
+    h->E.prm[0].box[2] = hd.phys_dim[2];
+    return h->E.inject(p.size(), p.data(), d.data(), nullptr);
+}
+
+nf_status nf_write_coo(nf_handle* h, const char* dir) {
+    if (!h || !dir) return NF_ERR_PARAM;
+    nf::Engine& E = h->E;
+    if (!E.contacts_valid) return fail(h, NF_ERR_STATE, "no contacts");
+    size_t n = E.ct_off[1] - E.ct_off[0];
+    std::vector<uint32_t> I(n), J(n);
+    std::vector<double> D(n), S(n);
+    nf_contact_list c{};
+    c.capacity = n;
+    c.I = I.data(); c.J = J.data(); c.D = D.data(); c.S = S.data();
+    nf_status s = nf_get_contacts(h, &c);
+    if (s != NF_OK) return s;
+    // save_coo (src/conductivity.cu:838-879): internal, sink, source.
+    const char* names[3] = {"internal.srt.coo", "sink.elec.coo", "source.elec.coo"};
+    size_t b[4] = {0, E.ct_int[0], E.ct_int[0] + E.ct_snk[0], n};
+    for (int f = 0; f < 3; ++f) {
+        std::string p = std::string(dir) + "/" + names[f];
+        std::ofstream o(p);
+        if (!o.is_open()) return NF_ERR_IO;
+        o << "#\tI\tJ\tD\tS\n";
+        for (size_t q = b[f]; q < b[f + 1]; ++q)
+            o << "\t" << I[q] << "\t" << J[q] << "\t" << (float)D[q] << "\t" << (float)S[q] << "\n";
+        if (!o.good()) return NF_ERR_IO;
+    }
+    return NF_OK;
+}
+
+}  // extern "C"

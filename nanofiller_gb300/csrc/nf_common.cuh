@@ -1,0 +1,445 @@
+// nf_common.cuh -- device-side building blocks shared by the GB300 kernels.
+//
+//  * no-contraction arithmetic: the seeded stream and the FP64 decision path
+//    must give the same bits on the host (gcc, -ffp-contract=off) and on sm_103a,
+//    so every multiply/add there goes through the _rn intrinsics;
+//  * the project candidate stream (Philox4x32-10 + float transforms);
+//  * the reference's pair routine in FP64 (cnt_intersec_shr,
+//    inc/intersection_dev.h:10-80, and distance_cylinder_capped,
+//    inc/intersect/intersect_cylinder_capped.h:69-147), one template body for
+//    the hard-core and the contact test;
+//  * the FP32 conservative filter that decides every far pair without FP64.
+#pragma once
+#include <cstdint>
+#include <cstring>
+#include <cmath>
+#include <cuda_runtime.h>
+
+#define NF_HD __host__ __device__ __forceinline__
+
+namespace nf {
+
+// ---------------------------------------------------------------------------
+// Arithmetic without fused multiply-add.
+// ---------------------------------------------------------------------------
+#ifdef __CUDA_ARCH__
+NF_HD float fmul(float a, float b) { return __fmul_rn(a, b); }
+NF_HD float fadd(float a, float b) { return __fadd_rn(a, b); }
+NF_HD float fsub(float a, float b) { return __fsub_rn(a, b); }
+NF_HD float fdiv(float a, float b) { return __fdiv_rn(a, b); }
+NF_HD float fsqrt(float a) { return __fsqrt_rn(a); }
+NF_HD double dmul(double a, double b) { return __dmul_rn(a, b); }
+NF_HD double dadd(double a, double b) { return __dadd_rn(a, b); }
+NF_HD double dsub(double a, double b) { return __dsub_rn(a, b); }
+NF_HD double ddiv(double a, double b) { return __ddiv_rn(a, b); }
+NF_HD double dsqrt(double a) { return __dsqrt_rn(a); }
+NF_HD uint32_t f2u(float f) { return __float_as_uint(f); }
+NF_HD float u2f(uint32_t u) { return __uint_as_float(u); }
+NF_HD uint32_t mulhi32(uint32_t a, uint32_t b) { return __umulhi(a, b); }
+#else
+NF_HD float fmul(float a, float b) { return a * b; }
+NF_HD float fadd(float a, float b) { return a + b; }
+NF_HD float fsub(float a, float b) { return a - b; }
+NF_HD float fdiv(float a, float b) { return a / b; }
+NF_HD float fsqrt(float a) { return sqrtf(a); }
+NF_HD double dmul(double a, double b) { return a * b; }
+NF_HD double dadd(double a, double b) { return a + b; }
+NF_HD double dsub(double a, double b) { return a - b; }
+NF_HD double ddiv(double a, double b) { return a / b; }
+NF_HD double dsqrt(double a) { return sqrt(a); }
+NF_HD uint32_t f2u(float f) { uint32_t u; memcpy(&u, &f, 4); return u; }
+NF_HD float u2f(uint32_t u) { float f; memcpy(&f, &u, 4); return f; }
+NF_HD uint32_t mulhi32(uint32_t a, uint32_t b) { return (uint32_t)(((uint64_t)a * b) >> 32); }
+#endif
+NF_HD double dabs(double v) { return v < 0.0 ? -v : v; }
+
+// ---------------------------------------------------------------------------
+// Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11).
+// ---------------------------------------------------------------------------
+struct U4 { uint32_t x, y, z, w; };
+
+NF_HD U4 philox(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3, uint32_t k0, uint32_t k1) {
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+        uint32_t lo0 = 0xD2511F53u * c0, hi0 = mulhi32(0xD2511F53u, c0);
+        uint32_t lo1 = 0xCD9E8D57u * c2, hi1 = mulhi32(0xCD9E8D57u, c2);
+        uint32_t n0 = hi1 ^ c1 ^ k0, n2 = hi0 ^ c3 ^ k1;
+        c0 = n0; c1 = lo1; c2 = n2; c3 = lo0;
+        k0 += 0x9E3779B9u; k1 += 0xBB67AE85u;
+    }
+    return U4{c0, c1, c2, c3};
+}
+
+NF_HD float uni(uint32_t u) { return fmul((float)(u >> 8), 5.9604644775390625e-08f); }
+
+// sin/cos(2 pi t): exact quadrant reduction in turns, Taylor polynomials on
+// [-pi/4, pi/4] (degree 9 / 10), Horner without fused multiply-add.
+NF_HD void sincos_turns(float t, float* c, float* s) {
+    float t4 = fmul(t, 4.0f);
+    float q = floorf(fadd(t4, 0.5f));
+    float r = fsub(t4, q);
+    float x = fmul(r, (float)(3.14159265358979323846 / 2.0));
+    float x2 = fmul(x, x);
+    float ps = (float)(1.0 / 362880.0);
+    ps = fadd(fmul(ps, x2), (float)(-1.0 / 5040.0));
+    ps = fadd(fmul(ps, x2), (float)(1.0 / 120.0));
+    ps = fadd(fmul(ps, x2), (float)(-1.0 / 6.0));
+    float sn = fadd(x, fmul(fmul(x, x2), ps));
+    float pc = (float)(-1.0 / 3628800.0);
+    pc = fadd(fmul(pc, x2), (float)(1.0 / 40320.0));
+    pc = fadd(fmul(pc, x2), (float)(-1.0 / 720.0));
+    pc = fadd(fmul(pc, x2), (float)(1.0 / 24.0));
+    pc = fadd(fmul(pc, x2), -0.5f);
+    float cs = fadd(1.0f, fmul(x2, pc));
+    int qi = ((int)q) & 3;
+    if (qi == 0) { *c = cs; *s = sn; }
+    else if (qi == 1) { *c = -sn; *s = cs; }
+    else if (qi == 2) { *c = -cs; *s = -sn; }
+    else { *c = sn; *s = -cs; }
+}
+
+// ln v (v > 0, normal): exponent split, mantissa in [sqrt(1/2), sqrt(2)),
+// ln m = 2 atanh((m-1)/(m+1)) by its odd series to s^11.
+NF_HD float log_nf(float v) {
+    uint32_t b = f2u(v);
+    int e = (int)((b >> 23) & 0xffu) - 127;
+    float m = u2f((b & 0x007fffffu) | 0x3f800000u);
+    if (m > 1.41421354f) { m = fmul(m, 0.5f); e += 1; }
+    float s = fdiv(fsub(m, 1.0f), fadd(m, 1.0f));
+    float s2 = fmul(s, s);
+    float p = (float)(1.0 / 11.0);
+    p = fadd(fmul(p, s2), (float)(1.0 / 9.0));
+    p = fadd(fmul(p, s2), (float)(1.0 / 7.0));
+    p = fadd(fmul(p, s2), (float)(1.0 / 5.0));
+    p = fadd(fmul(p, s2), (float)(1.0 / 3.0));
+    float two_s = fadd(s, s);
+    float lm = fadd(two_s, fmul(two_s, fmul(s2, p)));
+    return fadd(fmul((float)e, (float)0.69314718055994530942), lm);
+}
+
+// e^x: Cody-Waite reduction by ln 2, degree-8 Taylor polynomial, 2^k scaling.
+NF_HD float exp_nf(float x) {
+    float kf = floorf(fadd(fmul(x, (float)(1.0 / 0.69314718055994530942)), 0.5f));
+    float r = fsub(fsub(x, fmul(kf, 0.693145751953125f)), fmul(kf, 1.428606765330187e-06f));
+    float p = (float)(1.0 / 40320.0);
+    p = fadd(fmul(p, r), (float)(1.0 / 5040.0));
+    p = fadd(fmul(p, r), (float)(1.0 / 720.0));
+    p = fadd(fmul(p, r), (float)(1.0 / 120.0));
+    p = fadd(fmul(p, r), (float)(1.0 / 24.0));
+    p = fadd(fmul(p, r), (float)(1.0 / 6.0));
+    p = fadd(fmul(p, r), 0.5f);
+    p = fadd(fmul(p, r), 1.0f);
+    p = fadd(fmul(p, r), 1.0f);
+    int k = (int)kf;
+    k = k < -126 ? -126 : (k > 127 ? 127 : k);
+    return fmul(p, u2f((uint32_t)(k + 127) << 23));
+}
+
+// ---------------------------------------------------------------------------
+// Realisation descriptor: stream, density, grid, thresholds.
+// ---------------------------------------------------------------------------
+struct Real {
+    // stream
+    float L[3];
+    uint32_t key[2];
+    int32_t orient, len_mode, rad_mode, rot;
+    float kappa, E2;
+    float m[9];
+    float l, a, sigma, lmin, lmax, rmin, rmax;
+    // density
+    const float* mesh;
+    int32_t mn[3];
+    float dflt;
+    // cell grid (shared by generation, contacts and screening)
+    int32_t n[3];
+    float invE[3];
+    int32_t per_gen, per_con;
+    uint32_t cell_off, ncell;
+    // rods
+    uint32_t rod_off, target;
+    // hard core (cnt_intersec_shr) and contacts (distance_cylinder_capped)
+    float eps, scf, sep, cut;
+    int32_t typo;
+    float slack;            // FP32 filter: absolute slack for coordinate rounding
+    int32_t field_axis;     // 0,1,2 or -1
+    double G0, lambda, dc;
+};
+
+NF_HD float lerp_nf(float a, float b, float f) { return fadd(a, fmul(fsub(b, a), f)); }
+
+// Trilinear density with wrap addressing, texel centres at (i+0.5)/n
+// (the texture set-up of inc/den2tex.h:36-40, evaluated in full FP32).
+NF_HD float density(const Real& R, float x, float y, float z) {
+    if (!R.mesh) return R.dflt;
+    float pos[3] = {x, y, z};
+    int i0[3], i1[3];
+    float f[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        float g = fsub(fmul(fdiv(pos[d], R.L[d]), (float)R.mn[d]), 0.5f);
+        float fl = floorf(g);
+        f[d] = fsub(g, fl);
+        int i = (int)fl;
+        i %= R.mn[d];
+        if (i < 0) i += R.mn[d];
+        i0[d] = i;
+        i1[d] = (i + 1 == R.mn[d]) ? 0 : i + 1;
+    }
+    const int ny = R.mn[1], nz = R.mn[2];
+#define NF_V(i, j, k) R.mesh[((size_t)(i) * ny + (j)) * nz + (k)]
+    float c00 = lerp_nf(NF_V(i0[0], i0[1], i0[2]), NF_V(i1[0], i0[1], i0[2]), f[0]);
+    float c10 = lerp_nf(NF_V(i0[0], i1[1], i0[2]), NF_V(i1[0], i1[1], i0[2]), f[0]);
+    float c01 = lerp_nf(NF_V(i0[0], i0[1], i1[2]), NF_V(i1[0], i0[1], i1[2]), f[0]);
+    float c11 = lerp_nf(NF_V(i0[0], i1[1], i1[2]), NF_V(i1[0], i1[1], i1[2]), f[0]);
+#undef NF_V
+    float c0 = lerp_nf(c00, c10, f[1]);
+    float c1 = lerp_nf(c01, c11, f[1]);
+    return lerp_nf(c0, c1, f[2]);
+}
+
+// Candidate k of the stream: pos = (x,y,z,l), dir = (cx,cy,cz,a), u, rho.
+NF_HD void candidate(const Real& R, uint64_t k, float4* pos, float4* dir, float* u, float* rho) {
+    const uint32_t klo = (uint32_t)k, khi = (uint32_t)(k >> 32);
+    U4 A = philox(klo, khi, 0u, 0u, R.key[0], R.key[1]);
+    U4 B = philox(klo, khi, 1u, 0u, R.key[0], R.key[1]);
+    float x = fmul(uni(A.x), R.L[0]);
+    float y = fmul(uni(A.y), R.L[1]);
+    float z = fmul(uni(A.z), R.L[2]);
+    float uu = uni(A.w);
+    float cz;
+    if (R.orient == 1) {
+        float w = fsub(1.0f, uni(B.x));
+        float v = fadd(w, fmul(fsub(1.0f, w), R.E2));
+        cz = fadd(1.0f, fdiv(log_nf(v), R.kappa));
+        cz = cz < -1.0f ? -1.0f : (cz > 1.0f ? 1.0f : cz);
+    } else {
+        cz = fsub(fmul(uni(B.x), 2.0f), 1.0f);
+    }
+    float cp, sp;
+    sincos_turns(uni(B.y), &cp, &sp);
+    float sr = fsub(1.0f, fmul(cz, cz));
+    float s = fsqrt(sr > 0.0f ? sr : 0.0f);
+    float cx = fmul(s, cp), cy = fmul(s, sp);
+    if (R.rot) {
+        float rx = fadd(fadd(fmul(R.m[0], cx), fmul(R.m[1], cy)), fmul(R.m[2], cz));
+        float ry = fadd(fadd(fmul(R.m[3], cx), fmul(R.m[4], cy)), fmul(R.m[5], cz));
+        float rz = fadd(fadd(fmul(R.m[6], cx), fmul(R.m[7], cy)), fmul(R.m[8], cz));
+        cx = rx; cy = ry; cz = rz;
+    }
+    float len = R.l;
+    if (R.len_mode == 1) {
+        float cb, sb;
+        sincos_turns(uni(B.w), &cb, &sb);
+        float g = fmul(fsqrt(fmul(-2.0f, log_nf(fsub(1.0f, uni(B.z))))), cb);
+        len = fmul(R.l, exp_nf(fmul(R.sigma, g)));
+        len = len < R.lmin ? R.lmin : (len > R.lmax ? R.lmax : len);
+    }
+    float rad = R.a;
+    if (R.rad_mode == 2) {
+        U4 Cc = philox(klo, khi, 2u, 0u, R.key[0], R.key[1]);
+        rad = fadd(R.rmin, fmul(fsub(R.rmax, R.rmin), uni(Cc.x)));
+    }
+    *pos = make_float4(x, y, z, len);
+    *dir = make_float4(cx, cy, cz, rad);
+    *u = uu;
+    *rho = density(R, x, y, z);
+}
+
+// ---------------------------------------------------------------------------
+// Cells.
+// ---------------------------------------------------------------------------
+NF_HD int cell_coord(const Real& R, int d, float x) {
+    int c = (int)(x * R.invE[d]);
+    if (x < 0.0f) c = -1;
+    c = c < 0 ? 0 : (c >= R.n[d] ? R.n[d] - 1 : c);
+    return c;
+}
+
+NF_HD uint32_t cell_of(const Real& R, float x, float y, float z) {
+    int cx = cell_coord(R, 0, x), cy = cell_coord(R, 1, y), cz = cell_coord(R, 2, z);
+    return R.cell_off + (uint32_t)(cx + R.n[0] * (cy + R.n[1] * cz));
+}
+
+// Neighbour of cell (c) by offset o in {-1,0,1}^3 under periodic mask `per`.
+// Returns false when the offset leaves an open axis; img = periodic image of
+// the neighbour cell relative to the box (the stride2dspl shift).
+NF_HD bool stencil(const Real& R, const int c[3], int o, int per, uint32_t* cell, int img[3]) {
+    int off[3] = {o % 3 - 1, (o / 3) % 3 - 1, o / 9 - 1};
+    int q[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        int v = c[d] + off[d];
+        img[d] = 0;
+        if (v < 0) {
+            if (!(per & (1 << d))) return false;
+            v += R.n[d]; img[d] = -1;
+        } else if (v >= R.n[d]) {
+            if (!(per & (1 << d))) return false;
+            v -= R.n[d]; img[d] = 1;
+        }
+        q[d] = v;
+    }
+    *cell = R.cell_off + (uint32_t)(q[0] + R.n[0] * (q[1] + R.n[1] * q[2]));
+    return true;
+}
+
+// ---------------------------------------------------------------------------
+// FP32 conservative filter. The reference's points lie within (l/2+a+eps)|c|
+// of each centre and on the axis lines, so
+//   d >= |b| - hA - hB   and   d >= |(cA x cB) . b| / |cA x cB|.
+// A pair is "far" when either bound, evaluated in FP32 with error margins
+// (relative 2e-6 / 2e-4, absolute `slack` for coordinate rounding), clears
+// the threshold. Far pairs cannot satisfy d < thr in any precision; the rest
+// go to the FP64 routine.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ bool maybe_near(const float4& pA, const float4& cA, const float4& pB,
+                                           const float4& cB, float sx, float sy, float sz,
+                                           float thr, float eps, float slack) {
+    float bx = (pB.x + sx) - pA.x, by = (pB.y + sy) - pA.y, bz = (pB.z + sz) - pA.z;
+    float hA = pA.w * 0.5f + cA.w + eps, hB = pB.w * 0.5f + cB.w + eps;
+    float Rr = (hA + hB + thr) * 1.000002f + slack;
+    float bb = bx * bx + by * by + bz * bz;
+    if (bb > Rr * Rr) return false;
+    float nx = cA.y * cB.z - cA.z * cB.y;
+    float ny = cA.z * cB.x - cA.x * cB.z;
+    float nz = cA.x * cB.y - cA.y * cB.x;
+    float nn = nx * nx + ny * ny + nz * nz;
+    if (nn > 1e-4f) {
+        float nb = fabsf(nx * bx + ny * by + nz * bz);
+        float s = sqrtf(nn);
+        if (nb - 4e-6f * (1.0f + sqrtf(bb)) - slack > thr * s * 1.0002f) return false;
+    }
+    return true;
+}
+
+// ---------------------------------------------------------------------------
+// The reference routine in FP64, without contraction (matches the oracle).
+// A in "registers", B shifted by (sx,sy,sz). Returns d; t0,t1 clamped;
+// u0,u1 unclamped; Dx the perpendicular distance at (u0,u1).
+// ---------------------------------------------------------------------------
+struct RodD { double x, y, z, cx, cy, cz, l, a; };
+
+NF_HD RodD rodd(const float4& p, const float4& c) {
+    return RodD{(double)p.x, (double)p.y, (double)p.z, (double)c.x, (double)c.y, (double)c.z,
+                (double)p.w, (double)c.w};
+}
+
+NF_HD double ref_distance_d(const RodD& A, const RodD& B, double sx, double sy, double sz,
+                            double eps, bool typo, double* t0o, double* t1o, double* u0o,
+                            double* u1o, double* Dxo) {
+    const double Bx = dadd(B.x, sx), By = dadd(B.y, sy), Bz = dadd(B.z, sz);
+    const double bx = dsub(Bx, A.x), by = dsub(By, A.y), bz = dsub(Bz, A.z);
+    double d = dadd(dadd(dmul(A.cx, B.cx), dmul(A.cy, B.cy)), dmul(A.cz, B.cz));
+    double t0, t1;
+    if (dsub(1.0, dabs(d)) > eps) {
+        double ax = dsub(dmul(d, B.cx), A.cx), ay = dsub(dmul(d, B.cy), A.cy), az = dsub(dmul(d, B.cz), A.cz);
+        t0 = dadd(dadd(dmul(ax, bx), dmul(ay, by)), dmul(az, bz));
+        ax = dsub(B.cx, dmul(d, A.cx)); ay = dsub(B.cy, dmul(d, A.cy)); az = dsub(B.cz, dmul(d, A.cz));
+        t1 = dadd(dadd(dmul(ax, bx), dmul(ay, by)), dmul(az, bz));
+        double den = dsub(dmul(d, d), 1.0);
+        t0 = ddiv(t0, den);
+        t1 = ddiv(t1, den);
+    } else {
+        t0 = copysign(ddiv(A.l, 2.0), dadd(dadd(dmul(bx, A.cx), dmul(by, A.cy)), dmul(bz, A.cz)));
+        double dot = typo ? dadd(dadd(dmul(bx, B.cx), dmul(bx, B.cy)), dmul(bx, B.cz))
+                          : dadd(dadd(dmul(bx, B.cx), dmul(by, B.cy)), dmul(bz, B.cz));
+        t1 = dadd(dmul(-1.0, dot), dmul(d, t0));
+    }
+    const double u0 = t0, u1 = t1;
+    const double hA = ddiv(A.l, 2.0), hB = ddiv(B.l, 2.0);
+    bool f1 = dabs(t0) <= dadd(dadd(hA, A.a), eps);
+    bool f2 = dabs(t1) <= dadd(dadd(hB, B.a), eps);
+    if (!(f1 && f2)) {
+        bool f3 = dsub(dabs(t0), hA) < dsub(dabs(t1), hB);
+        if (f3) {
+            t1 = copysign(hB, t1);
+            t0 = dadd(dmul(1.0, dadd(dadd(dmul(bx, A.cx), dmul(by, A.cy)), dmul(bz, A.cz))), dmul(d, t1));
+            if (dabs(t0) > hA) t0 = copysign(hA, t0);
+        } else {
+            t0 = copysign(hA, t0);
+            t1 = dadd(dmul(-1.0, dadd(dadd(dmul(bx, B.cx), dmul(by, B.cy)), dmul(bz, B.cz))), dmul(d, t0));
+            if (dabs(t1) > hB) t1 = copysign(hB, t1);
+        }
+    }
+    double px = dsub(dsub(dadd(A.x, dmul(t0, A.cx)), Bx), dmul(t1, B.cx));
+    double py = dsub(dsub(dadd(A.y, dmul(t0, A.cy)), By), dmul(t1, B.cy));
+    double pz = dsub(dsub(dadd(A.z, dmul(t0, A.cz)), Bz), dmul(t1, B.cz));
+    double dist = dsqrt(dadd(dadd(dmul(px, px), dmul(py, py)), dmul(pz, pz)));
+    if (Dxo) {
+        double qx = dsub(dsub(dadd(A.x, dmul(u0, A.cx)), Bx), dmul(u1, B.cx));
+        double qy = dsub(dsub(dadd(A.y, dmul(u0, A.cy)), By), dmul(u1, B.cy));
+        double qz = dsub(dsub(dadd(A.z, dmul(u0, A.cz)), Bz), dmul(u1, B.cz));
+        *Dxo = dsqrt(dadd(dadd(dmul(qx, qx), dmul(qy, qy)), dmul(qz, qz)));
+    }
+    if (t0o) *t0o = t0;
+    if (t1o) *t1o = t1;
+    if (u0o) *u0o = u0;
+    if (u1o) *u1o = u1;
+    return dist;
+}
+
+// (a_B + a_A) * scf + sep + eps, left to right (inc/intersection_dev.h:78).
+NF_HD double thresh_d(double aA, double aB, double scf, double sep, double eps) {
+    return dadd(dadd(dmul(dadd(aB, aA), scf), sep), eps);
+}
+
+// The same routine in plain FP32 (what an FP32-only build decides), for the
+// would-flip diagnostic of the precision form.
+__device__ __forceinline__ bool ref_hit_f32(const float4& pA, const float4& cA, const float4& pB,
+                                            const float4& cB, float sx, float sy, float sz,
+                                            float eps, float thr, bool typo) {
+    float Bx = pB.x + sx, By = pB.y + sy, Bz = pB.z + sz;
+    float bx = Bx - pA.x, by = By - pA.y, bz = Bz - pA.z;
+    float d = cA.x * cB.x + cA.y * cB.y + cA.z * cB.z;
+    float t0, t1;
+    if (1.0f - fabsf(d) > eps) {
+        float ax = d * cB.x - cA.x, ay = d * cB.y - cA.y, az = d * cB.z - cA.z;
+        t0 = ax * bx + ay * by + az * bz;
+        ax = cB.x - d * cA.x; ay = cB.y - d * cA.y; az = cB.z - d * cA.z;
+        t1 = ax * bx + ay * by + az * bz;
+        t0 /= d * d - 1.0f;
+        t1 /= d * d - 1.0f;
+    } else {
+        t0 = copysignf(pA.w * 0.5f, bx * cA.x + by * cA.y + bz * cA.z);
+        t1 = typo ? -(bx * cB.x + bx * cB.y + bx * cB.z) + d * t0 : -(bx * cB.x + by * cB.y + bz * cB.z) + d * t0;
+    }
+    float hA = pA.w * 0.5f, hB = pB.w * 0.5f;
+    bool f1 = fabsf(t0) <= hA + cA.w + eps, f2 = fabsf(t1) <= hB + cB.w + eps;
+    if (!(f1 && f2)) {
+        bool f3 = (fabsf(t0) - hA) < (fabsf(t1) - hB);
+        if (f3) {
+            t1 = copysignf(hB, t1);
+            t0 = (bx * cA.x + by * cA.y + bz * cA.z) + d * t1;
+            if (fabsf(t0) > hA) t0 = copysignf(hA, t0);
+        } else {
+            t0 = copysignf(hA, t0);
+            t1 = -(bx * cB.x + by * cB.y + bz * cB.z) + d * t0;
+            if (fabsf(t1) > hB) t1 = copysignf(hB, t1);
+        }
+    }
+    float px = pA.x + t0 * cA.x - Bx - t1 * cB.x;
+    float py = pA.y + t0 * cA.y - By - t1 * cB.y;
+    float pz = pA.z + t0 * cA.z - Bz - t1 * cB.z;
+    return sqrtf(px * px + py * py + pz * pz) < thr;
+}
+
+// Realisation owning slot s, given the prefix table off[0..R] (off[0] = 0).
+__device__ __forceinline__ int find_real(const uint32_t* off, int R, uint32_t s) {
+    int lo = 0, hi = R;
+    while (hi - lo > 1) {
+        int mid = (lo + hi) >> 1;
+        if (off[mid] <= s) lo = mid; else hi = mid;
+    }
+    return lo;
+}
+
+// ---------------------------------------------------------------------------
+// Warp-aggregated counters.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void warp_add_u64(unsigned long long* dst, unsigned long long v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0 && v) atomicAdd(dst, v);
+}
+
+}  // namespace nf

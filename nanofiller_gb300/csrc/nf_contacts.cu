@@ -1,0 +1,530 @@
+// nf_contacts.cu -- tunnelling-contact extraction, screening and electrode roles.
+//
+// Reference path replaced: collect_cunduct_data steps 1-5 (src/conductivity.cu:140-226)
+// = get_contact_counts / get_contact_arrays (src/get_contact_arrays.cu:12-140) on
+// core_cell_interact_kernel COUNT/RECORD (src/core_cell_interaction_kernel.cu:69-315),
+// check_screened_contacts + generate_virt_inclusions + VIRTUAL_CHECK
+// (src/conductivity.cu:430-528, inc/conductKernels.h:289-361,
+// src/check_screened_Interactions.cu:12-70), sort_contacts_by_role
+// (src/conductivity.cu:530-637), get_contact_distance / get_contact_surface
+// (src/get_contact_data.cu:28-230).
+//
+// One sweep replaces COUNT + scan + RECORD: every contact found is appended to a
+// record buffer (global atomic, sized from the previous count and re-run once
+// if it overflows), then records are counting-sorted by their lower rod id and
+// each rod's short run is ordered by (J, image). The pair rule is the
+// reference's: rod I tests rods J > I of the 27 neighbour cells, J shifted by
+// the cell's periodic image (upper triangle + image shift, :115, :249-259), so
+// a rod never meets its own image (sameFLG, :253).
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+
+#include "nf_engine.cuh"
+
+namespace nf {
+
+static inline unsigned grid_for(size_t n, unsigned b) { return (unsigned)((n + b - 1) / b); }
+
+// ---------------------------------------------------------------------------
+// Pair sweep.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_ct_pairs(const Real* __restrict__ reals, int R,
+                                                  const uint32_t* __restrict__ rodoff, uint32_t nsorted,
+                                                  const uint32_t* __restrict__ rstart, const float4* __restrict__ spos,
+                                                  const float4* __restrict__ sdir, const uint32_t* __restrict__ sid,
+                                                  Rec* __restrict__ rec, unsigned long long cap,
+                                                  unsigned long long* __restrict__ recn, uint32_t* __restrict__ rcnt,
+                                                  unsigned long long* __restrict__ ctr) {
+    uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
+    unsigned long long tests = 0, exact = 0, flips = 0;
+    if (q < nsorted) {
+        const uint32_t i = sid[q];
+        const float4 pA = spos[q], cA = sdir[q];
+        const int r = find_real(rodoff, R, i);
+        const Real& Re = reals[r];
+        const float epc = 1e-6f;  // DEV_PRECISION (inc/definitions.h:5)
+        int cc[3] = {cell_coord(Re, 0, pA.x), cell_coord(Re, 1, pA.y), cell_coord(Re, 2, pA.z)};
+        const RodD a = rodd(pA, cA);
+        uint32_t mine = 0;
+        for (int o = 0; o < 27; ++o) {
+            uint32_t cell;
+            int img[3];
+            if (!stencil(Re, cc, o, Re.per_con, &cell, img)) continue;
+            const float sx = img[0] * Re.L[0], sy = img[1] * Re.L[1], sz = img[2] * Re.L[2];
+            for (uint32_t p = rstart[cell], p1 = rstart[cell + 1]; p < p1; ++p) {
+                const uint32_t j = sid[p];
+                if (j <= i) continue;
+                const float4 pB = spos[p], cB = sdir[p];
+                ++tests;
+                const float thr = (cB.w + cA.w) + Re.cut + epc;
+                if (!maybe_near(pA, cA, pB, cB, sx, sy, sz, thr, epc, Re.slack)) continue;
+                ++exact;
+                const RodD b = rodd(pB, cB);
+                double t0, t1, u0, u1, Dx;
+                const double shx = img[0] * (double)Re.L[0], shy = img[1] * (double)Re.L[1],
+                             shz = img[2] * (double)Re.L[2];
+                double d = ref_distance_d(a, b, shx, shy, shz, (double)epc, false, &t0, &t1, &u0, &u1, &Dx);
+                bool h = d < thresh_d(a.a, b.a, 1.0, (double)Re.cut, (double)epc);
+                if (ref_hit_f32(pA, cA, pB, cB, sx, sy, sz, epc, thr, false) != h) ++flips;
+                if (!h) continue;
+                unsigned long long slot = atomicAdd(recn, 1ull);
+                ++mine;
+                if (slot < cap) {
+                    Rec x;
+                    x.i = i;
+                    x.j = j;
+                    x.img[0] = (int8_t)img[0];
+                    x.img[1] = (int8_t)img[1];
+                    x.img[2] = (int8_t)img[2];
+                    x.img[3] = 0;
+                    x.flags = 0;
+                    x.t0 = t0; x.t1 = t1; x.d = d; x.Dx = Dx; x.u0 = u0; x.u1 = u1;
+                    rec[slot] = x;
+                }
+            }
+        }
+        if (mine) atomicAdd(&rcnt[i], mine);
+    }
+    warp_add_u64(&ctr[C_CT_PAIRS], tests);
+    warp_add_u64(&ctr[C_CT_EXACT], exact);
+    warp_add_u64(&ctr[C_CT_FLIPS], flips);
+}
+
+__global__ void k_rec_scatter(uint32_t n, const Rec* __restrict__ rec, const uint32_t* __restrict__ rpos,
+                              uint32_t* __restrict__ rcur, Rec* __restrict__ out) {
+    uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= n) return;
+    Rec x = rec[q];
+    uint32_t dst = rpos[x.i] + atomicAdd(&rcur[x.i], 1u);
+    out[dst] = x;
+}
+
+__device__ __forceinline__ bool rec_less(const Rec& a, const Rec& b) {
+    if (a.j != b.j) return a.j < b.j;
+    for (int d = 2; d >= 0; --d)
+        if (a.img[d] != b.img[d]) return a.img[d] < b.img[d];
+    return false;
+}
+
+// Order each rod's run by (J, image z, y, x): insertion sort (runs are short).
+__global__ void k_rec_sort(uint32_t nslot, const uint32_t* __restrict__ rpos, const uint32_t* __restrict__ rcnt,
+                           Rec* __restrict__ rec) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nslot) return;
+    uint32_t b = rpos[i], n = rcnt[i];
+    for (uint32_t a = 1; a < n; ++a) {
+        Rec x = rec[b + a];
+        uint32_t k = a;
+        while (k > 0 && rec_less(x, rec[b + k - 1])) {
+            rec[b + k] = rec[b + k - 1];
+            --k;
+        }
+        rec[b + k] = x;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Screening: the segment between the two contact points (radius min(aI,aJ))
+// is a virtual rod; the contact is dropped if any real rod crosses its body
+// (if_intersects with separation 0, then body_intersect on the unclamped
+// parameter along the virtual rod; src/core_cell_interaction_kernel.cu:141-146).
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_screen(const Real* __restrict__ reals, int R,
+                                                const uint32_t* __restrict__ rodoff, uint32_t nrec,
+                                                Rec* __restrict__ rec, const float4* __restrict__ pos,
+                                                const float4* __restrict__ dir,
+                                                const uint32_t* __restrict__ rstart,
+                                                const float4* __restrict__ spos, const float4* __restrict__ sdir,
+                                                unsigned long long* __restrict__ ctr) {
+    uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
+    unsigned long long tests = 0, exact = 0;
+    if (q < nrec) {
+        Rec x = rec[q];
+        const int r = find_real(rodoff, R, x.i);
+        const Real& Re = reals[r];
+        const double eps = (double)1e-6f;
+        const RodD A = rodd(pos[x.i], dir[x.i]);
+        const RodD B = rodd(pos[x.j], dir[x.j]);
+        const double sh[3] = {x.img[0] * (double)Re.L[0], x.img[1] * (double)Re.L[1], x.img[2] * (double)Re.L[2]};
+        const double p0[3] = {dadd(A.x, dmul(x.t0, A.cx)), dadd(A.y, dmul(x.t0, A.cy)), dadd(A.z, dmul(x.t0, A.cz))};
+        const double p1[3] = {dadd(dadd(B.x, sh[0]), dmul(x.t1, B.cx)), dadd(dadd(B.y, sh[1]), dmul(x.t1, B.cy)),
+                              dadd(dadd(B.z, sh[2]), dmul(x.t1, B.cz))};
+        double vr[3], vc[3];
+        for (int d = 0; d < 3; ++d) {
+            vr[d] = dmul(dadd(p0[d], p1[d]), 0.5);
+            vc[d] = dsub(p1[d], p0[d]);
+        }
+        double vl = dsqrt(dadd(dadd(dmul(vc[0], vc[0]), dmul(vc[1], vc[1])), dmul(vc[2], vc[2])));
+        bool hit = false;
+        if (vl > 0) {
+            double inv = ddiv(1.0, vl);
+            for (int d = 0; d < 3; ++d) vc[d] = dmul(vc[d], inv);
+            const double va = fmin(A.a, B.a);
+            RodD V{vr[0], vr[1], vr[2], vc[0], vc[1], vc[2], vl, va};
+            double vw[3];
+            int cc[3];
+            for (int d = 0; d < 3; ++d) {
+                double xw = vr[d];
+                if (Re.per_con & (1 << d)) {
+                    xw = fmod(xw, (double)Re.L[d]);
+                    if (xw < 0) xw = dadd(xw, (double)Re.L[d]);
+                }
+                vw[d] = xw;
+                cc[d] = cell_coord(Re, d, (float)xw);
+            }
+            const float4 pV = make_float4((float)vr[0], (float)vr[1], (float)vr[2], (float)vl);
+            const float4 cV = make_float4((float)vc[0], (float)vc[1], (float)vc[2], (float)va);
+            const float epsf = 1e-6f;
+            for (int o = 0; o < 27 && !hit; ++o) {
+                uint32_t cell;
+                int img[3];
+                if (!stencil(Re, cc, o, Re.per_con, &cell, img)) continue;
+                double sv[3];
+                for (int d = 0; d < 3; ++d) sv[d] = dsub(dsub(vw[d], vr[d]), img[d] * (double)Re.L[d]);
+                const float svf[3] = {(float)sv[0], (float)sv[1], (float)sv[2]};
+                for (uint32_t p = rstart[cell], p1e = rstart[cell + 1]; p < p1e; ++p) {
+                    const float4 pR = spos[p], cR = sdir[p];
+                    ++tests;
+                    const float thr = (cV.w + cR.w) + epsf;
+                    if (!maybe_near(pR, cR, pV, cV, svf[0], svf[1], svf[2], thr, epsf, Re.slack)) continue;
+                    ++exact;
+                    const RodD Rr = rodd(pR, cR);
+                    double u1, t0, t1, u0;
+                    double d = ref_distance_d(Rr, V, sv[0], sv[1], sv[2], eps, false, &t0, &t1, &u0, &u1, nullptr);
+                    bool h = d < thresh_d(Rr.a, V.a, 1.0, 0.0, eps);
+                    if (h && dsub(ddiv(V.l, 2.0), dabs(u1)) > dadd(V.a, eps)) { hit = true; break; }
+                }
+            }
+        }
+        if (hit) rec[q].flags |= 1u;
+    }
+    warp_add_u64(&ctr[C_SCR_PAIRS], tests);
+    warp_add_u64(&ctr[C_SCR_EXACT], exact);
+}
+
+// ---------------------------------------------------------------------------
+// Contact area, surf_to_cylinder_capped (inc/intersect/intersect_cylinder_capped.h:204-293)
+// evaluated in FP64 for rod A and rod B shifted by sh.
+// ---------------------------------------------------------------------------
+__device__ double dot3(const double* u, const double* w) {
+    return dadd(dadd(dmul(u[0], w[0]), dmul(u[1], w[1])), dmul(u[2], w[2]));
+}
+
+__device__ double contact_area(const RodD& A, const RodD& B, const double sh[3], double Dtt_x, double t1u,
+                               double t2u, double rlim) {
+    const double PIv = 3.141593;
+    double l1 = A.l, l2 = B.l, a1 = A.a, a2 = B.a;
+    double c1[3] = {A.cx, A.cy, A.cz}, c2[3] = {B.cx, B.cy, B.cz};
+    double r1[3] = {A.x, A.y, A.z};
+    double r2[3] = {dadd(B.x, sh[0]), dadd(B.y, sh[1]), dadd(B.z, sh[2])};
+    double sg = copysign(1.0, dot3(c1, c2));
+    double c2p[3] = {dmul(c2[0], sg), dmul(c2[1], sg), dmul(c2[2], sg)};
+    double dr1 = 0.0, dr2 = 0.0;
+    double h1 = fmax(dsub(dsub(Dtt_x, a2), rlim), 0.0);
+    double h2 = fmax(dsub(dsub(Dtt_x, a1), rlim), 0.0);
+    if (h1 <= a1) dr1 = dmul(a1, dsqrt(dsub(1.0, dmul(ddiv(h1, a1), ddiv(h1, a1)))));
+    if (h2 <= a2) dr2 = dmul(a2, dsqrt(dsub(1.0, dmul(ddiv(h2, a2), ddiv(h2, a2)))));
+    double dr = fmin(dr1, dr2);
+    double S = dmul(dmul(PIv, dr), dr);
+    double t1 = t1u, t2 = t2u;
+    double d = dot3(c1, c2p);
+    double sng = dsqrt(fmax(dsub(1.0, dmul(d, d)), 0.0));
+    double hl1 = ddiv(l1, 2.0), hl2 = ddiv(l2, 2.0);
+    if (dabs(t1) < dsub(hl1, a1) && dabs(t2) < dsub(hl2, a2)) {
+        double ax1[3] = {dadd(c1[0], c2p[0]), dadd(c1[1], c2p[1]), dadd(c1[2], c2p[2])};
+        double n1 = dsqrt(dot3(ax1, ax1));
+        double in1 = ddiv(1.0, n1);
+        for (int i = 0; i < 3; ++i) ax1[i] = dmul(ax1[i], in1);
+        double csg = dsqrt(fmax(dsub(1.0, dmul(sng, sng)), 0.0));
+        double sngh = dsqrt(ddiv(dsub(1.0, csg), 2.0));
+        double t2p = copysign(t2, dot3(c1, c2));
+        double dt0p = (sngh > 1e-6 ? ddiv(dr2, sngh) : hl1);
+        double dt0m = dt0p;
+        double qv[3];
+        for (int i = 0; i < 3; ++i) qv[i] = dadd(r1[i], dmul(c1[i], dsub(hl1, t1)));
+        double dt1p = dot3(qv, ax1);
+        for (int i = 0; i < 3; ++i) qv[i] = dadd(r1[i], dmul(c1[i], dsub(-hl1, t1)));
+        double dt1m = dabs(dot3(qv, ax1));
+        for (int i = 0; i < 3; ++i) qv[i] = dadd(r2[i], dmul(c2p[i], dsub(hl2, t2p)));
+        double dt2p = dot3(qv, ax1);
+        for (int i = 0; i < 3; ++i) qv[i] = dadd(r2[i], dmul(c2p[i], dsub(-hl2, t2p)));
+        double dt2m = dabs(dot3(qv, ax1));
+        double Ap = fmax(dr, fmin(dt0p, fmin(dt1p, dt2p)));
+        double Am = fmax(dr, fmin(dt0m, fmin(dt1m, dt2m)));
+        S = fmax(S, dmul(dmul(dmul(0.5, PIv), dr), dadd(Ap, Am)));
+    }
+    if ((sng <= ddiv(fmax(a1, a2), fmin(l1, l2))) && (dabs(t1) <= dadd(hl1, a1) || dabs(t2) <= dadd(hl2, a2))) {
+        double b[3] = {dsub(r2[0], r1[0]), dsub(r2[1], r1[1]), dsub(r2[2], r1[2])};
+        double cb1 = dot3(c1, b), cb2 = dot3(c2, b);
+        double t1a = copysign(hl1, cb1), t1b = dmul(-1.0, copysign(hl1, cb1));
+        double t2a = copysign(hl2, cb2), t2b = dmul(-1.0, copysign(hl2, cb2));
+        double qv[3];
+        for (int i = 0; i < 3; ++i) qv[i] = dadd(r1[i], dmul(c1[i], t1a));
+        double t1ac = dot3(qv, c1);
+        for (int i = 0; i < 3; ++i) qv[i] = dadd(r1[i], dmul(c1[i], t1b));
+        double t1bc = dot3(qv, c1);
+        for (int i = 0; i < 3; ++i) qv[i] = dadd(dadd(b[i], r1[i]), dmul(c2[i], t2a));
+        double t2ac = dot3(qv, c1);
+        for (int i = 0; i < 3; ++i) qv[i] = dadd(dadd(b[i], r1[i]), dmul(c2[i], t2b));
+        double t2bc = dot3(qv, c1);
+        double p1c = cb1 > 0 ? fmin(t1ac, t2ac) : fmax(t1ac, t2ac);
+        double p2c = cb1 > 0 ? fmax(t1bc, t2bc) : fmin(t1bc, t2bc);
+        S = fmax(S, dmul(dmul(dabs(dsub(p2c, p1c)), 2.0), dr));
+    }
+    return S;
+}
+
+__device__ __forceinline__ double tunnel_g(const Real& Re, double gap) {
+    double ge = gap > Re.dc ? gap : Re.dc;
+    return Re.G0 * exp(-(ge - Re.dc) / Re.lambda);
+}
+
+// Per-realisation counts of unscreened / screened records.
+__global__ void k_rec_count(int R, const uint32_t* __restrict__ rodoff, uint32_t nrec, const Rec* __restrict__ rec,
+                            uint32_t* __restrict__ keepf, uint32_t* __restrict__ cnt /* 2R */) {
+    uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= nrec) return;
+    const Rec& x = rec[q];
+    int r = find_real(rodoff, R, x.i);
+    bool scr = x.flags & 1u;
+    keepf[q] = scr ? 0u : 1u;
+    atomicAdd(&cnt[2 * r + (scr ? 1 : 0)], 1u);
+}
+
+// Electrode flags per rod slot: plane electrodes at x_f = 0 (source) and x_f = L_f (sink).
+__global__ void k_elec(uint32_t nslot, int R, const uint32_t* __restrict__ rodoff, const uint32_t* __restrict__ dcount,
+                       const Real* __restrict__ reals, const float4* __restrict__ pos, const float4* __restrict__ dir,
+                       uint32_t* __restrict__ fsnk, uint32_t* __restrict__ fsrc, double* __restrict__ esnk /* D,t */,
+                       double* __restrict__ esrc, uint32_t* __restrict__ cnt /* 2R: snk, src */) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nslot) return;
+    int r = find_real(rodoff, R, i);
+    const Real& Re = reals[r];
+    fsnk[i] = 0;
+    fsrc[i] = 0;
+    if (i - rodoff[r] >= dcount[r] || Re.field_axis < 0) return;
+    const RodD A = rodd(pos[i], dir[i]);
+    const int f = Re.field_axis;
+    const double cf = f == 0 ? A.cx : (f == 1 ? A.cy : A.cz);
+    const double rf = f == 0 ? A.x : (f == 1 ? A.y : A.z);
+    const double half = ddiv(A.l, 2.0);
+    const double tlo = cf > 0 ? -half : half, thi = -tlo;
+    const double zlo = dadd(rf, dmul(tlo, cf)), zhi = dadd(rf, dmul(thi, cf));
+    const double lim = dadd((double)Re.cut, (double)1e-6f);
+    const double dsnk = dsub((double)Re.L[f], zhi);
+    if (dsub(dsnk, A.a) < lim) {
+        fsnk[i] = 1;
+        esnk[2 * i] = dsnk;
+        esnk[2 * i + 1] = thi;
+        atomicAdd(&cnt[2 * r], 1u);
+    }
+    if (dsub(zlo, A.a) < lim) {
+        fsrc[i] = 1;
+        esrc[2 * i] = zlo;
+        esrc[2 * i + 1] = tlo;
+        atomicAdd(&cnt[2 * r + 1], 1u);
+    }
+}
+
+// Final contact arrays, per realisation block [internal | sink | source].
+__global__ void k_final_internal(int R, const uint32_t* __restrict__ rodoff, uint32_t nrec,
+                                 const Rec* __restrict__ rec, const uint32_t* __restrict__ keepf,
+                                 const uint32_t* __restrict__ kscan, const uint32_t* __restrict__ rpos,
+                                 const unsigned long long* __restrict__ ctoff, const Real* __restrict__ reals,
+                                 const float4* __restrict__ pos, const float4* __restrict__ dir,
+                                 uint32_t* __restrict__ oI, uint32_t* __restrict__ oJ, double* __restrict__ ot0,
+                                 double* __restrict__ ot1, double* __restrict__ oD, double* __restrict__ oG,
+                                 double* __restrict__ oS, int8_t* __restrict__ oimg, uint32_t* __restrict__ oreal) {
+    uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= nrec || !keepf[q]) return;
+    const Rec x = rec[q];
+    int r = find_real(rodoff, R, x.i);
+    const Real& Re = reals[r];
+    uint32_t first = rpos[rodoff[r]];
+    unsigned long long dst = ctoff[r] + (kscan[q] - kscan[first]);
+    const RodD A = rodd(pos[x.i], dir[x.i]);
+    const RodD B = rodd(pos[x.j], dir[x.j]);
+    oI[dst] = x.i;
+    oJ[dst] = x.j;
+    ot0[dst] = x.t0;
+    ot1[dst] = x.t1;
+    oD[dst] = x.d;
+    oG[dst] = tunnel_g(Re, dsub(dsub(x.d, A.a), B.a));
+    const double sh[3] = {x.img[0] * (double)Re.L[0], x.img[1] * (double)Re.L[1], x.img[2] * (double)Re.L[2]};
+    oS[dst] = contact_area(A, B, sh, x.Dx, x.u0, x.u1, (double)Re.cut);
+    oimg[3 * dst + 0] = x.img[0];
+    oimg[3 * dst + 1] = x.img[1];
+    oimg[3 * dst + 2] = x.img[2];
+    oreal[dst] = (uint32_t)r;
+}
+
+__global__ void k_final_elec(uint32_t nslot, int R, const uint32_t* __restrict__ rodoff,
+                             const uint32_t* __restrict__ flag, const uint32_t* __restrict__ fscan,
+                             const double* __restrict__ e, const unsigned long long* __restrict__ base,
+                             uint32_t elec_id, const Real* __restrict__ reals, const float4* __restrict__ dir,
+                             uint32_t* __restrict__ oI, uint32_t* __restrict__ oJ, double* __restrict__ ot0,
+                             double* __restrict__ ot1, double* __restrict__ oD, double* __restrict__ oG,
+                             double* __restrict__ oS, int8_t* __restrict__ oimg, uint32_t* __restrict__ oreal) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nslot || !flag[i]) return;
+    int r = find_real(rodoff, R, i);
+    const Real& Re = reals[r];
+    unsigned long long dst = base[r] + (fscan[i] - fscan[rodoff[r]]);
+    double D = e[2 * i];
+    oI[dst] = i;
+    oJ[dst] = elec_id;
+    ot0[dst] = e[2 * i + 1];
+    ot1[dst] = 0.0;
+    oD[dst] = D;
+    oG[dst] = tunnel_g(Re, dsub(D, (double)dir[i].w));
+    oS[dst] = 0.0;
+    oimg[3 * dst] = oimg[3 * dst + 1] = oimg[3 * dst + 2] = 0;
+    oreal[dst] = (uint32_t)r;
+}
+
+// ---------------------------------------------------------------------------
+#define NF_CK(x)                                            \
+    do {                                                    \
+        cudaError_t e_ = (x);                               \
+        if (e_ != cudaSuccess) return cuda_fail(e_, #x);    \
+    } while (0)
+
+nf_status Engine::contacts() {
+    if (!cells_valid || rod_slots == 0) { err = "no rods: generate or set rods first"; return NF_ERR_STATE; }
+    cudaEvent_t e0, e1;
+    NF_CK(cudaEventCreate(&e0));
+    NF_CK(cudaEventCreate(&e1));
+    NF_CK(cudaEventRecord(e0, st));
+    const uint64_t nrods = total_rods();
+    const uint32_t nslot = (uint32_t)rod_slots;
+    // Sorted rods: the cell list covers exactly the valid rods.
+    NF_CK(cudaMemsetAsync(ctr.p + C_CT_PAIRS, 0, sizeof(unsigned long long) * (C_NCTR - C_CT_PAIRS), st));
+    NF_CK(rcnt.ensure(nslot + 1));
+    NF_CK(rpos.ensure(nslot + 1));
+    NF_CK(rcur.ensure(nslot + 1));
+    NF_CK(recn.ensure(2 * R + 2));
+    size_t cap = std::max<size_t>(rec.cap, std::max<size_t>(4096, 2 * nrods));
+    for (int attempt = 0; attempt < 2; ++attempt) {
+        NF_CK(rec.ensure(cap));
+        NF_CK(cudaMemsetAsync(rcnt.p, 0, sizeof(uint32_t) * (nslot + 1), st));
+        NF_CK(cudaMemsetAsync(recn.p, 0, sizeof(unsigned long long), st));
+        if (nrods)
+            k_ct_pairs<<<grid_for(nrods, 256), 256, 0, st>>>(dreal.p, R, rodoff.p, (uint32_t)nrods, rstart.p, spos.p,
+                                                            sdir.p, sid.p, rec.p, rec.cap, recn.p, rcnt.p, ctr.p);
+        NF_CK(cudaGetLastError());
+        unsigned long long n = 0;
+        NF_CK(cudaMemcpyAsync(&n, recn.p, sizeof(n), cudaMemcpyDeviceToHost, st));
+        NF_CK(cudaStreamSynchronize(st));
+        if (n <= rec.cap) { cap = n; break; }
+        if (attempt == 1) { err = "contact record buffer overflow"; return NF_ERR_OVERFLOW; }
+        cap = n + n / 8 + 64;
+    }
+    const uint32_t nrec = (uint32_t)cap;
+    NF_CK(rec2.ensure(nrec + 1));
+    nf_status s = scan_u32(rcnt.p, rpos.p, nslot + 1);
+    if (s != NF_OK) return s;
+    NF_CK(cudaMemsetAsync(rcur.p, 0, sizeof(uint32_t) * (nslot + 1), st));
+    if (nrec) {
+        k_rec_scatter<<<grid_for(nrec, 256), 256, 0, st>>>(nrec, rec.p, rpos.p, rcur.p, rec2.p);
+        NF_CK(cudaGetLastError());
+        k_rec_sort<<<grid_for(nslot, 256), 256, 0, st>>>(nslot, rpos.p, rcnt.p, rec2.p);
+        NF_CK(cudaGetLastError());
+        if (prm[0].screening) {
+            k_screen<<<grid_for(nrec, 256), 256, 0, st>>>(dreal.p, R, rodoff.p, nrec, rec2.p, pos.p, dir.p, rstart.p,
+                                                         spos.p, sdir.p, ctr.p);
+            NF_CK(cudaGetLastError());
+        }
+    }
+    // Counts per realisation.
+    NF_CK(u32tmp.ensure(4 * (size_t)R + 2 * (size_t)nrec + 4 * (size_t)nslot + 16));
+    uint32_t* cnt = u32tmp.p;                 // 4R: int, scr, snk, src
+    uint32_t* keepf = cnt + 4 * R;            // nrec + 1
+    uint32_t* kscan = keepf + nrec + 1;       // nrec + 1
+    uint32_t* fsnk = kscan + nrec + 1;        // nslot + 1
+    uint32_t* fsrc = fsnk + nslot + 1;
+    uint32_t* ssnk = fsrc + nslot + 1;
+    uint32_t* ssrc = ssnk + nslot + 1;
+    NF_CK(cudaMemsetAsync(cnt, 0, sizeof(uint32_t) * 4 * R, st));
+    NF_CK(cudaMemsetAsync(keepf, 0, sizeof(uint32_t) * (nrec + 1), st));
+    if (nrec) {
+        k_rec_count<<<grid_for(nrec, 256), 256, 0, st>>>(R, rodoff.p, nrec, rec2.p, keepf, cnt);
+        NF_CK(cudaGetLastError());
+    }
+    s = scan_u32(keepf, kscan, nrec + 1);
+    if (s != NF_OK) return s;
+    DBuf<double>& esnk = vsnk;  // reuse solve buffers as scratch (2 doubles per slot)
+    DBuf<double>& esrc = vsrc;
+    NF_CK(esnk.ensure(2 * (size_t)nslot + 2));
+    NF_CK(esrc.ensure(2 * (size_t)nslot + 2));
+    NF_CK(cudaMemsetAsync(fsnk + nslot, 0, sizeof(uint32_t), st));
+    NF_CK(cudaMemsetAsync(fsrc + nslot, 0, sizeof(uint32_t), st));
+    k_elec<<<grid_for(nslot, 256), 256, 0, st>>>(nslot, R, rodoff.p, dcount.p, dreal.p, pos.p, dir.p, fsnk, fsrc,
+                                                 esnk.p, esrc.p, cnt + 2 * R);
+    NF_CK(cudaGetLastError());
+    s = scan_u32(fsnk, ssnk, nslot + 1);
+    if (s != NF_OK) return s;
+    s = scan_u32(fsrc, ssrc, nslot + 1);
+    if (s != NF_OK) return s;
+    std::vector<uint32_t> hc(4 * R);
+    NF_CK(cudaMemcpyAsync(hc.data(), cnt, sizeof(uint32_t) * 4 * R, cudaMemcpyDeviceToHost, st));
+    NF_CK(cudaStreamSynchronize(st));
+    ct_int.assign(R, 0); ct_scr.assign(R, 0); ct_snk.assign(R, 0); ct_src.assign(R, 0);
+    ct_off.assign(R + 1, 0);
+    std::vector<unsigned long long> hoff(3 * R);
+    for (int r = 0; r < R; ++r) {
+        ct_int[r] = hc[2 * r]; ct_scr[r] = hc[2 * r + 1];
+        ct_snk[r] = hc[2 * R + 2 * r]; ct_src[r] = hc[2 * R + 2 * r + 1];
+        hoff[r] = ct_off[r];
+        hoff[R + r] = ct_off[r] + ct_int[r];
+        hoff[2 * R + r] = ct_off[r] + ct_int[r] + ct_snk[r];
+        ct_off[r + 1] = ct_off[r] + ct_int[r] + ct_snk[r] + ct_src[r];
+    }
+    const size_t ntot = ct_off[R];
+    NF_CK(cI.ensure(ntot + 1)); NF_CK(cJ.ensure(ntot + 1));
+    NF_CK(ct0.ensure(ntot + 1)); NF_CK(ct1.ensure(ntot + 1));
+    NF_CK(cD.ensure(ntot + 1)); NF_CK(cG.ensure(ntot + 1)); NF_CK(cS.ensure(ntot + 1));
+    NF_CK(cimg.ensure(3 * ntot + 3)); NF_CK(creal2.ensure(ntot + 1));
+    NF_CK(recn.ensure(3 * (size_t)R + 2));
+    unsigned long long* doff = recn.p;
+    NF_CK(cudaMemcpyAsync(doff, hoff.data(), sizeof(unsigned long long) * 3 * R, cudaMemcpyHostToDevice, st));
+    if (nrec) {
+        k_final_internal<<<grid_for(nrec, 256), 256, 0, st>>>(R, rodoff.p, nrec, rec2.p, keepf, kscan, rpos.p, doff,
+                                                             dreal.p, pos.p, dir.p, cI.p, cJ.p, ct0.p, ct1.p, cD.p,
+                                                             cG.p, cS.p, cimg.p, creal2.p);
+        NF_CK(cudaGetLastError());
+    }
+    k_final_elec<<<grid_for(nslot, 256), 256, 0, st>>>(nslot, R, rodoff.p, fsnk, ssnk, esnk.p, doff + R, NF_SNK_ELEC,
+                                                       dreal.p, dir.p, cI.p, cJ.p, ct0.p, ct1.p, cD.p, cG.p, cS.p,
+                                                       cimg.p, creal2.p);
+    NF_CK(cudaGetLastError());
+    k_final_elec<<<grid_for(nslot, 256), 256, 0, st>>>(nslot, R, rodoff.p, fsrc, ssrc, esrc.p, doff + 2 * R,
+                                                       NF_SRC_ELEC, dreal.p, dir.p, cI.p, cJ.p, ct0.p, ct1.p, cD.p,
+                                                       cG.p, cS.p, cimg.p, creal2.p);
+    NF_CK(cudaGetLastError());
+    NF_CK(cudaEventRecord(e1, st));
+    NF_CK(cudaEventSynchronize(e1));
+    float ms = 0;
+    NF_CK(cudaEventElapsedTime(&ms, e0, e1));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    unsigned long long hk[C_NCTR];
+    NF_CK(cudaMemcpy(hk, ctr.p, sizeof(hk), cudaMemcpyDeviceToHost));
+    std::memset(&cst, 0, sizeof(cst));
+    for (int r = 0; r < R; ++r) {
+        cst.contacts += ct_int[r];
+        cst.screened += ct_scr[r];
+        cst.n_sink += ct_snk[r];
+        cst.n_source += ct_src[r];
+    }
+    cst.pair_tests = hk[C_CT_PAIRS] + hk[C_SCR_PAIRS];
+    cst.exact_evals = hk[C_CT_EXACT] + hk[C_SCR_EXACT];
+    cst.fp32_would_flip = hk[C_CT_FLIPS];
+    cst.ms = ms;
+    contacts_valid = true;
+    solve_valid = false;
+    return NF_OK;
+}
+
+#undef NF_CK
+}  // namespace nf

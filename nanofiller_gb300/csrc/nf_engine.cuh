@@ -1,0 +1,162 @@
+// nf_engine.cuh -- per-handle device state of the GB300 path and the stage
+// entry points (generation, contacts, network solve, adjoint).
+//
+// Memory layout in HBM (all realisations of a batch side by side):
+//   rods   pos[N] float4 (x,y,z,l), dir[N] float4 (cx,cy,cz,a): 32 B per rod,
+//          SoA so a warp reads 512 contiguous bytes per field pair;
+//          realisation r owns slots [rod_off_r, rod_off_r + target_r).
+//   cells  one global cell index space; realisation r owns
+//          [cell_off_r, cell_off_r + ncell_r). A CSR (rstart) over the
+//          cell-sorted copy spos/sdir/sid is rebuilt by a counting sort
+//          (count, exclusive scan, scatter) after every round.
+//   round  candidates of one round are compacted (stream order) and binned by
+//          cell the same way; per-candidate state + a fixed-capacity list of
+//          earlier conflicting candidates.
+#pragma once
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "../../include/nanofiller_gb300.h"
+#include "nf_common.cuh"
+
+namespace nf {
+
+constexpr int kConflictCap = 32;  // earlier in-round conflicts kept per candidate
+
+enum CandState : uint8_t { ST_NONE = 0, ST_REJ_OLD = 1, ST_ALIVE = 2, ST_ACC = 3, ST_REJ_CONF = 4 };
+
+// Device counters (unsigned long long) in Engine::ctr.
+enum Ctr {
+    C_PAIR_TESTS = 0, C_EXACT, C_FLIPS, C_OVERFLOW, C_UNDECIDED,
+    C_CT_PAIRS, C_CT_EXACT, C_CT_FLIPS, C_CT_RECORDS, C_SCR_PAIRS, C_SCR_EXACT,
+    C_CG_ITERS, C_NCTR
+};
+
+template <class T>
+struct DBuf {
+    T* p = nullptr;
+    size_t cap = 0;
+    cudaError_t ensure(size_t n) {
+        if (n <= cap && p) return cudaSuccess;
+        if (p) cudaFree(p);
+        p = nullptr;
+        cap = 0;
+        size_t m = n < 1 ? 1 : n;
+        cudaError_t e = cudaMalloc((void**)&p, m * sizeof(T));
+        if (e == cudaSuccess) cap = m;
+        return e;
+    }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        cap = 0;
+    }
+};
+
+// One contact record before sorting / screening (64 B).
+struct Rec {
+    uint32_t i, j;      // global rod slots, i < j
+    int8_t img[4];      // image of j (x,y,z), pad
+    uint32_t flags;     // bit0: screened
+    double t0, t1, d, Dx, u0, u1;
+};
+
+struct Engine {
+    cudaStream_t st = 0;
+    int dev = 0;
+    int nsm = 0;
+    std::string err;
+
+    // realisations
+    int R = 0;
+    std::vector<nf_params> prm;
+    std::vector<Real> hreal;
+    DBuf<Real> dreal;
+    std::vector<std::vector<float>> hmesh;  // host copies of meshes (per realisation, may be empty)
+    DBuf<float> mesh;
+    uint32_t ncell = 0;
+
+    // rods
+    std::vector<uint32_t> count;     // accepted per realisation (host mirror)
+    std::vector<uint64_t> knext;     // next stream index per realisation
+    std::vector<uint64_t> drawn;     // stream indices consumed
+    std::vector<uint64_t> dens_acc;  // density-accepted up to the stop
+    std::vector<int> rounds_r;
+    uint64_t rod_slots = 0;
+    DBuf<float4> pos, dir;
+    DBuf<uint64_t> sidx;
+    DBuf<uint32_t> dcount;  // device copy of count
+    DBuf<uint32_t> rodoff;  // R+1 prefix of targets
+    DBuf<uint32_t> rstart, rcursor;
+    DBuf<float4> spos, sdir;
+    DBuf<uint32_t> sid;
+    bool cells_valid = false;
+
+    // round scratch
+    DBuf<uint32_t> coff, keep, kpos, ccount, cstart, ccursor, cperm, creal, ccell, ccnt, clist, accf, accpos;
+    DBuf<uint64_t> kbeg, csidx;
+    DBuf<float4> cpos, cdir;
+    DBuf<uint8_t> state;
+    DBuf<uint32_t> meta;   // per-realisation round metadata
+    DBuf<unsigned long long> ctr;
+    DBuf<unsigned char> cubtmp;
+    DBuf<uint32_t> u32tmp;
+
+    // contacts
+    DBuf<Rec> rec, rec2;
+    DBuf<uint32_t> rcnt, rpos, rcur;
+    DBuf<unsigned long long> recn;
+    size_t n_int = 0, n_snk = 0, n_src = 0, n_scr = 0;
+    DBuf<uint32_t> cI, cJ;       // final contacts (global slots; J may be an electrode id)
+    DBuf<double> ct0, ct1, cD, cG, cS;
+    DBuf<int8_t> cimg;
+    DBuf<uint32_t> creal2;       // realisation of each final contact
+    std::vector<uint64_t> ct_off;  // per realisation prefix of final contacts (host)
+    std::vector<uint64_t> ct_int, ct_snk, ct_src, ct_scr;
+    bool contacts_valid = false;
+    DBuf<uint32_t> eflag;
+
+    // solve
+    DBuf<double> vsrc, vsnk, volt;
+    DBuf<uint32_t> parent, cflag, aidx, rowp, col, deg;
+    DBuf<float> val32, diag32;
+    DBuf<double> val64, diag64, bvec, xvec;
+    DBuf<float> cgbuf;
+    DBuf<double> cgred;
+    std::vector<nf_solve_stats> solve_st;
+    bool solve_valid = false;
+
+    // stats
+    nf_gen_stats gst{};
+    nf_contact_stats cst{};
+
+    // --- set-up ------------------------------------------------------------
+    nf_status init(const nf_params* params, int n, const std::vector<const float*>& meshes);
+    nf_status set_density(int r, int nx, int ny, int nz, const float* values);
+    void release();
+    nf_status cuda_fail(cudaError_t e, const char* where);
+
+    // --- stages ------------------------------------------------------------
+    nf_status setup();
+    nf_status stream_dump(uint64_t k0, uint64_t n, float* host10);
+    nf_status inject(size_t n, const float4* hpos, const float4* hdir, const uint64_t* hsidx);
+    nf_status generate();
+    nf_status rebuild_cells();
+    nf_status contacts();
+    nf_status solve();
+    nf_status adjoint(int r, float* dG_dend, size_t cap, double* dlam, double* dg0);
+
+    // helpers
+    nf_status scan_u32(const uint32_t* in, uint32_t* out, size_t n);
+    uint64_t total_rods() const;
+};
+
+// Derived realisation descriptor (identical arithmetic to the oracle).
+Real make_real(const nf_params& p, const float* dmesh, int mn[3], double reach);
+double stage_reach(const nf_params& p);
+int64_t target_count(const nf_params& p);
+
+}  // namespace nf

@@ -1,0 +1,798 @@
+// nf_generate.cu -- seeded candidate stream, von Neumann density test and
+// cell-list hard-core rejection with sequential-insertion semantics.
+//
+// Reference path replaced: cudaMain / cudaGenStep (src/cudaMain.cu:61-161,
+// :219-351) with cuda_CNTgenerate_orient (inc/cuda_CNTgenerate.h:136-260),
+// cuda_InternalIsect_noLck, cuda_NewExtIsectLB_parted, cuda_OldExtIsectLB
+// (inc/intersection_kern.h:12-364) and cuda_renewOcc (inc/auxilary_kernels.h:11-26).
+//
+// Semantics: candidate k (stream order) is accepted iff its density variate
+// passes (u < rho(x)) and it hits no rod accepted before it; generation stops
+// at the target count or when the stream budget is spent. Each round draws a
+// block of stream indices per realisation and
+//   1. recomputes candidates, keeps those passing the density test (scan),
+//   2. bins them by cell (counting sort),
+//   3. tests each against every accepted rod in the 27 neighbour cells,
+//   4. records, for survivors, the earlier survivors of the same round they hit,
+//   5. resolves those in stream order (a candidate is rejected once an earlier
+//      neighbour is accepted and accepted once all earlier neighbours are
+//      rejected; monotone, so passes converge to the sequential answer),
+//   6. appends the accepted in stream order up to the target.
+// The reference instead kills a same-cell candidate on conflict with any later
+// candidate (inc/intersection_kern.h:69-72) and lets parity scheduling decide
+// cross-cell conflicts (:119-126); its result depends on launch order.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+
+#include <cub/device/device_scan.cuh>
+
+#include "nf_engine.cuh"
+
+namespace nf {
+
+// ---------------------------------------------------------------------------
+// Host-side derived parameters (same arithmetic as the oracle).
+// ---------------------------------------------------------------------------
+int64_t target_count(const nf_params& p) {
+    if (p.n_target > 0) return p.n_target;
+    double V = (double)p.box[0] * p.box[1] * p.box[2];
+    double El = p.l, Ea2 = (double)p.a * p.a;
+    if (p.len_mode == NF_SIZE_LOGNORMAL) {
+        double s = 0, w = 0;
+        for (int i = -6000; i <= 6000; ++i) {
+            double z = i * 1e-3, g = std::exp(-0.5 * z * z);
+            double v = p.l * std::exp(p.len_sigma_ln * z);
+            v = std::min(std::max(v, (double)p.len_min), (double)p.len_max);
+            s += g * v;
+            w += g;
+        }
+        El = s / w;
+    }
+    if (p.rad_mode == NF_SIZE_UNIFORM) {
+        double lo = p.rad_min, hi = p.rad_max;
+        Ea2 = (hi * hi + hi * lo + lo * lo) / 3.0;
+    }
+    double vinc = M_PI * Ea2 * El;
+    return (int64_t)std::ceil((double)p.vf * V / vinc);
+}
+
+static void size_bounds(const nf_params& p, double* lmax, double* amax) {
+    *lmax = (p.len_mode == NF_SIZE_LOGNORMAL) ? (double)p.len_max : (double)p.l;
+    *amax = (p.rad_mode == NF_SIZE_UNIFORM) ? (double)std::max(p.rad_min, p.rad_max) : (double)p.a;
+}
+
+// One cell grid serves all stages: its edge covers the widest pair reach of
+// the hard-core test, the contact test and the screening test.
+double stage_reach(const nf_params& p) {
+    double lmax, amax;
+    size_bounds(p, &lmax, &amax);
+    double eps = p.tol, epc = (double)1e-6f;
+    double h = lmax / 2 + amax + std::max(eps, epc);
+    double gen = 2 * h + ((2 * amax) * p.sc_frac + p.sep + eps);
+    double con = 2 * h + (2 * amax + p.stat_dist_lim + epc);
+    return std::max(gen, con);
+}
+
+Real make_real(const nf_params& p, const float* dmesh, int mn[3], double reach) {
+    Real R;
+    std::memset(&R, 0, sizeof(R));
+    for (int d = 0; d < 3; ++d) R.L[d] = p.box[d];
+    R.key[0] = (uint32_t)(p.seed & 0xffffffffu);
+    R.key[1] = (uint32_t)(p.seed >> 32);
+    R.orient = p.orient_mode;
+    R.len_mode = p.len_mode;
+    R.rad_mode = p.rad_mode;
+    R.kappa = p.vmf_kappa;
+    R.E2 = (p.orient_mode == NF_ORIENT_VMF) ? exp_nf(fmul(-2.0f, p.vmf_kappa)) : 0.0f;
+    R.rot = (p.pref_ort[0] != 0.0f) || (p.pref_ort[1] != 0.0f);
+    float cM, sM, cX, sX;
+    sincos_turns((float)((double)p.pref_ort[0] / (2.0 * 3.14159265358979323846)), &cM, &sM);
+    sincos_turns((float)((double)(-p.pref_ort[1]) / (2.0 * 3.14159265358979323846)), &cX, &sX);
+    // inc_rotation (inc/cuda_CNTgenerate.h:289-295), Mu = phi, Xi = -theta
+    R.m[0] = fmul(cM, cX);  R.m[1] = sM;   R.m[2] = fmul(-sX, cM);
+    R.m[3] = fmul(-sM, cX); R.m[4] = cM;   R.m[5] = fmul(sX, sM);
+    R.m[6] = sX;            R.m[7] = 0.0f; R.m[8] = cX;
+    R.l = p.l;
+    R.a = p.a;
+    R.sigma = p.len_sigma_ln;
+    R.lmin = p.len_min;
+    R.lmax = p.len_max;
+    R.rmin = p.rad_min;
+    R.rmax = p.rad_max;
+    R.mesh = dmesh;
+    for (int d = 0; d < 3; ++d) R.mn[d] = dmesh ? mn[d] : 0;
+    R.dflt = p.density_default;
+    double e = std::max(reach * 1.0001, (double)p.cell_edge);
+    for (int d = 0; d < 3; ++d) {
+        int c = (int)std::floor((double)p.box[d] / e);
+        R.n[d] = c < 1 ? 1 : c;
+        R.invE[d] = (float)((double)R.n[d] / (double)p.box[d]);
+    }
+    R.per_gen = p.gen_periodic & 7;
+    R.per_con = (p.gen_periodic & ~p.field_dir) & 7;
+    R.eps = p.tol;
+    R.scf = p.sc_frac;
+    R.sep = p.sep;
+    R.cut = p.stat_dist_lim;
+    R.typo = p.ref_parallel_typo;
+    float Lmax = std::max(p.box[0], std::max(p.box[1], p.box[2]));
+    R.slack = Lmax * 9.5367431640625e-07f;  // 2^-20 L: coordinate rounding
+    R.field_axis = p.field_dir == 1 ? 0 : (p.field_dir == 2 ? 1 : (p.field_dir == 4 ? 2 : -1));
+    R.G0 = p.G0;
+    R.lambda = p.lambda;
+    R.dc = p.d_c;
+    return R;
+}
+
+// ---------------------------------------------------------------------------
+// Kernels.
+// ---------------------------------------------------------------------------
+// Density test of every stream slot of the round.
+__global__ void k_stream_keep(const Real* __restrict__ reals, int R, const uint32_t* __restrict__ coff,
+                              const uint64_t* __restrict__ kbeg, uint32_t nslots, uint32_t* __restrict__ keep) {
+    uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= nslots) return;
+    int r = find_real(coff, R, s);
+    const Real& Re = reals[r];
+    uint64_t k = kbeg[r] + (s - coff[r]);
+    float4 p, d;
+    float u, rho;
+    candidate(Re, k, &p, &d, &u, &rho);
+    keep[s] = (u < rho) ? 1u : 0u;
+}
+
+// Compaction in stream order + cell counts.
+__global__ void k_compact(const Real* __restrict__ reals, int R, const uint32_t* __restrict__ coff,
+                          const uint64_t* __restrict__ kbeg, uint32_t nslots, const uint32_t* __restrict__ keep,
+                          const uint32_t* __restrict__ kpos, float4* __restrict__ cpos, float4* __restrict__ cdir,
+                          uint64_t* __restrict__ csidx, uint32_t* __restrict__ creal, uint32_t* __restrict__ ccell,
+                          uint32_t* __restrict__ ccount, uint8_t* __restrict__ state) {
+    uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= nslots || !keep[s]) return;
+    int r = find_real(coff, R, s);
+    const Real& Re = reals[r];
+    uint64_t k = kbeg[r] + (s - coff[r]);
+    float4 p, d;
+    float u, rho;
+    candidate(Re, k, &p, &d, &u, &rho);
+    uint32_t c = kpos[s];
+    cpos[c] = p;
+    cdir[c] = d;
+    csidx[c] = k;
+    creal[c] = (uint32_t)r;
+    uint32_t cell = cell_of(Re, p.x, p.y, p.z);
+    ccell[c] = cell;
+    state[c] = ST_NONE;
+    atomicAdd(&ccount[cell], 1u);
+}
+
+// Counting-sort scatter: perm[start[cell] + cursor] = id.
+__global__ void k_bin(uint32_t n, const uint32_t* __restrict__ ntot, const uint32_t* __restrict__ cellof,
+                      const uint32_t* __restrict__ start, uint32_t* __restrict__ cursor, uint32_t* __restrict__ perm) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    uint32_t m = ntot ? *ntot : n;
+    if (i >= m) return;
+    uint32_t cell = cellof[i];
+    uint32_t q = start[cell] + atomicAdd(&cursor[cell], 1u);
+    perm[q] = i;
+}
+
+// Candidate vs accepted rods of the 27 neighbour cells (cuda_OldExtIsectLB's job).
+__global__ void __launch_bounds__(256) k_old_test(const Real* __restrict__ reals, const uint32_t* __restrict__ ntot,
+                                                  const uint32_t* __restrict__ cperm, const float4* __restrict__ cpos,
+                                                  const float4* __restrict__ cdir, const uint32_t* __restrict__ creal,
+                                                  const uint32_t* __restrict__ rstart, const float4* __restrict__ spos,
+                                                  const float4* __restrict__ sdir, int have_rods,
+                                                  uint8_t* __restrict__ state, unsigned long long* __restrict__ ctr) {
+    uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    bool active = t < *ntot;
+    unsigned long long tests = 0, exact = 0, flips = 0;
+    if (active) {
+        uint32_t c = cperm[t];
+        const float4 pA = cpos[c], cA = cdir[c];
+        const Real& Re = reals[creal[c]];
+        bool hit = false;
+        if (have_rods) {
+            int cc[3] = {cell_coord(Re, 0, pA.x), cell_coord(Re, 1, pA.y), cell_coord(Re, 2, pA.z)};
+            const RodD a = rodd(pA, cA);
+            for (int o = 0; o < 27 && !hit; ++o) {
+                uint32_t cell;
+                int img[3];
+                if (!stencil(Re, cc, o, Re.per_gen, &cell, img)) continue;
+                const float sx = img[0] * Re.L[0], sy = img[1] * Re.L[1], sz = img[2] * Re.L[2];
+                const uint32_t b0 = rstart[cell], b1 = rstart[cell + 1];
+                for (uint32_t j = b0; j < b1; ++j) {
+                    const float4 pB = spos[j], cB = sdir[j];
+                    ++tests;
+                    const float thr = (cB.w + cA.w) * Re.scf + Re.sep + Re.eps;
+                    if (!maybe_near(pA, cA, pB, cB, sx, sy, sz, thr, Re.eps, Re.slack)) continue;
+                    ++exact;
+                    const RodD b = rodd(pB, cB);
+                    double d = ref_distance_d(a, b, img[0] * (double)Re.L[0], img[1] * (double)Re.L[1],
+                                              img[2] * (double)Re.L[2], (double)Re.eps, Re.typo != 0,
+                                              nullptr, nullptr, nullptr, nullptr, nullptr);
+                    bool h = d < thresh_d(a.a, b.a, (double)Re.scf, (double)Re.sep, (double)Re.eps);
+                    if (ref_hit_f32(pA, cA, pB, cB, sx, sy, sz, Re.eps, thr, Re.typo != 0) != h) ++flips;
+                    if (h) { hit = true; break; }
+                }
+            }
+        }
+        state[c] = hit ? ST_REJ_OLD : ST_ALIVE;
+    }
+    warp_add_u64(&ctr[C_PAIR_TESTS], tests);
+    warp_add_u64(&ctr[C_EXACT], exact);
+    warp_add_u64(&ctr[C_FLIPS], flips);
+}
+
+// Earlier surviving candidates of the same round that a survivor hits.
+__global__ void __launch_bounds__(256) k_conflicts(const Real* __restrict__ reals, const uint32_t* __restrict__ ntot,
+                                                   const uint32_t* __restrict__ cperm, const uint32_t* __restrict__ cstart,
+                                                   const float4* __restrict__ cpos, const float4* __restrict__ cdir,
+                                                   const uint64_t* __restrict__ csidx, const uint32_t* __restrict__ creal,
+                                                   const uint8_t* __restrict__ state, uint32_t* __restrict__ ccnt,
+                                                   uint32_t* __restrict__ clist, unsigned long long* __restrict__ ctr) {
+    uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    bool active = t < *ntot;
+    unsigned long long tests = 0, exact = 0, flips = 0;
+    if (active) {
+        uint32_t c = cperm[t];
+        uint32_t n = 0;
+        if (state[c] == ST_ALIVE) {
+            const float4 pA = cpos[c], cA = cdir[c];
+            const uint64_t kA = csidx[c];
+            const Real& Re = reals[creal[c]];
+            int cc[3] = {cell_coord(Re, 0, pA.x), cell_coord(Re, 1, pA.y), cell_coord(Re, 2, pA.z)};
+            const RodD a = rodd(pA, cA);
+            for (int o = 0; o < 27; ++o) {
+                uint32_t cell;
+                int img[3];
+                if (!stencil(Re, cc, o, Re.per_gen, &cell, img)) continue;
+                const float sx = img[0] * Re.L[0], sy = img[1] * Re.L[1], sz = img[2] * Re.L[2];
+                for (uint32_t q = cstart[cell], q1 = cstart[cell + 1]; q < q1; ++q) {
+                    uint32_t j = cperm[q];
+                    if (csidx[j] >= kA || state[j] != ST_ALIVE) continue;
+                    const float4 pB = cpos[j], cB = cdir[j];
+                    ++tests;
+                    const float thr = (cB.w + cA.w) * Re.scf + Re.sep + Re.eps;
+                    if (!maybe_near(pA, cA, pB, cB, sx, sy, sz, thr, Re.eps, Re.slack)) continue;
+                    ++exact;
+                    const RodD b = rodd(pB, cB);
+                    double d = ref_distance_d(a, b, img[0] * (double)Re.L[0], img[1] * (double)Re.L[1],
+                                              img[2] * (double)Re.L[2], (double)Re.eps, Re.typo != 0,
+                                              nullptr, nullptr, nullptr, nullptr, nullptr);
+                    bool h = d < thresh_d(a.a, b.a, (double)Re.scf, (double)Re.sep, (double)Re.eps);
+                    if (ref_hit_f32(pA, cA, pB, cB, sx, sy, sz, Re.eps, thr, Re.typo != 0) != h) ++flips;
+                    if (h) {
+                        if (n < (uint32_t)kConflictCap) clist[(size_t)c * kConflictCap + n] = j;
+                        ++n;
+                    }
+                }
+            }
+        }
+        ccnt[c] = n;
+        if (n > (uint32_t)kConflictCap) atomicAdd(&ctr[C_OVERFLOW], 1ull);
+    }
+    warp_add_u64(&ctr[C_PAIR_TESTS], tests);
+    warp_add_u64(&ctr[C_EXACT], exact);
+    warp_add_u64(&ctr[C_FLIPS], flips);
+}
+
+// One pass of the in-order resolution.
+__global__ void k_resolve(const uint32_t* __restrict__ ntot, uint8_t* state, const uint32_t* __restrict__ ccnt,
+                          const uint32_t* __restrict__ clist, unsigned long long* __restrict__ ctr) {
+    uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= *ntot) return;
+    volatile uint8_t* vs = state;
+    if (vs[c] != ST_ALIVE) return;
+    uint32_t n = ccnt[c];
+    bool any_acc = false, all_rej = true;
+    for (uint32_t e = 0; e < n; ++e) {
+        uint8_t s = vs[clist[(size_t)c * kConflictCap + e]];
+        if (s == ST_ACC) { any_acc = true; break; }
+        if (s == ST_ALIVE) all_rej = false;
+    }
+    if (any_acc) vs[c] = ST_REJ_CONF;
+    else if (all_rej) vs[c] = ST_ACC;
+    else atomicAdd(&ctr[C_UNDECIDED], 1ull);
+}
+
+__global__ void k_accflag(const uint32_t* __restrict__ ntot, uint32_t cap, const uint8_t* __restrict__ state,
+                          uint32_t* __restrict__ accf) {
+    uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= cap) return;
+    accf[c] = (c < *ntot && state[c] == ST_ACC) ? 1u : 0u;
+}
+
+// Per-realisation metadata of the round: meta[r*4 + {0:cfirst, 1:clast, 2:accbase, 3:acctot}].
+__global__ void k_meta(int R, const uint32_t* __restrict__ coff, const uint32_t* __restrict__ keep,
+                       const uint32_t* __restrict__ kpos, const uint32_t* __restrict__ accf,
+                       const uint32_t* __restrict__ accpos, uint32_t* __restrict__ meta) {
+    int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= R) return;
+    uint32_t s0 = coff[r], s1 = coff[r + 1];
+    uint32_t c0 = kpos[s0];
+    uint32_t c1 = (s1 > s0) ? kpos[s1 - 1] + keep[s1 - 1] : c0;
+    uint32_t a0 = (c1 > c0) ? accpos[c0] : 0u;
+    uint32_t a1 = (c1 > c0) ? accpos[c1 - 1] + accf[c1 - 1] : 0u;
+    meta[4 * r + 0] = c0;
+    meta[4 * r + 1] = c1;
+    meta[4 * r + 2] = a0;
+    meta[4 * r + 3] = a1 - a0;
+}
+
+// Append accepted candidates in stream order up to each target.
+// out[r*2 + {0: stream index+1 of the target-reaching rod, 1: density-accepted up to it}].
+__global__ void k_append(const uint32_t* __restrict__ ntot, const uint8_t* __restrict__ state,
+                         const uint32_t* __restrict__ creal, const uint32_t* __restrict__ accpos,
+                         const uint32_t* __restrict__ meta, const uint32_t* __restrict__ rodoff,
+                         const uint32_t* __restrict__ dcount, const Real* __restrict__ reals,
+                         const float4* __restrict__ cpos, const float4* __restrict__ cdir,
+                         const uint64_t* __restrict__ csidx, float4* __restrict__ pos, float4* __restrict__ dir,
+                         uint64_t* __restrict__ sidx, uint64_t* __restrict__ out) {
+    uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= *ntot || state[c] != ST_ACC) return;
+    uint32_t r = creal[c];
+    uint32_t rank = accpos[c] - meta[4 * r + 2];
+    uint32_t have = dcount[r];
+    uint32_t rem = reals[r].target - have;
+    if (rank >= rem) return;
+    uint32_t dst = rodoff[r] + have + rank;
+    pos[dst] = cpos[c];
+    dir[dst] = cdir[c];
+    sidx[dst] = csidx[c];
+    if (rank == rem - 1) {
+        out[2 * r + 0] = csidx[c] + 1;
+        out[2 * r + 1] = c - meta[4 * r + 0] + 1;
+    }
+}
+
+// Rod cell list: counts.
+__global__ void k_rod_count(uint32_t nslot, int R, const uint32_t* __restrict__ rodoff,
+                            const uint32_t* __restrict__ dcount, const Real* __restrict__ reals,
+                            const float4* __restrict__ pos, uint32_t* __restrict__ rcell,
+                            uint32_t* __restrict__ ccount) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nslot) return;
+    int r = find_real(rodoff, R, i);
+    if (i - rodoff[r] >= dcount[r]) { rcell[i] = 0xffffffffu; return; }
+    const Real& Re = reals[r];
+    float4 p = pos[i];
+    uint32_t cell = cell_of(Re, p.x, p.y, p.z);
+    rcell[i] = cell;
+    atomicAdd(&ccount[cell], 1u);
+}
+
+__global__ void k_rod_scatter(uint32_t nslot, const uint32_t* __restrict__ rcell, const uint32_t* __restrict__ start,
+                              uint32_t* __restrict__ cursor, const float4* __restrict__ pos,
+                              const float4* __restrict__ dir, float4* __restrict__ spos, float4* __restrict__ sdir,
+                              uint32_t* __restrict__ sid) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nslot) return;
+    uint32_t cell = rcell[i];
+    if (cell == 0xffffffffu) return;
+    uint32_t q = start[cell] + atomicAdd(&cursor[cell], 1u);
+    spos[q] = pos[i];
+    sdir[q] = dir[i];
+    sid[q] = i;
+}
+
+// ---------------------------------------------------------------------------
+// Host orchestration.
+// ---------------------------------------------------------------------------
+static inline unsigned grid_for(size_t n, unsigned b) { return (unsigned)((n + b - 1) / b); }
+
+nf_status Engine::cuda_fail(cudaError_t e, const char* where) {
+    err = std::string(where) + ": " + cudaGetErrorString(e);
+    return e == cudaErrorMemoryAllocation ? NF_ERR_ALLOC : NF_ERR_CUDA;
+}
+
+#define NF_CK(x)                                            \
+    do {                                                    \
+        cudaError_t e_ = (x);                               \
+        if (e_ != cudaSuccess) return cuda_fail(e_, #x);    \
+    } while (0)
+
+nf_status Engine::scan_u32(const uint32_t* in, uint32_t* out, size_t n) {
+    size_t bytes = 0;
+    NF_CK(cub::DeviceScan::ExclusiveSum(nullptr, bytes, in, out, (int)n, st));
+    NF_CK(cubtmp.ensure(bytes));
+    NF_CK(cub::DeviceScan::ExclusiveSum(cubtmp.p, bytes, in, out, (int)n, st));
+    return NF_OK;
+}
+
+uint64_t Engine::total_rods() const {
+    uint64_t t = 0;
+    for (uint32_t c : count) t += c;
+    return t;
+}
+
+nf_status Engine::init(const nf_params* params, int n, const std::vector<const float*>& meshes) {
+    R = n;
+    prm.assign(params, params + n);
+    NF_CK(cudaGetDevice(&dev));
+    NF_CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+    hmesh.assign(n, {});
+    for (int r = 0; r < n; ++r) {
+        const nf_params& p = prm[r];
+        if (meshes.size() > (size_t)r && meshes[r]) {
+            size_t m = (size_t)p.mesh_ext[0] * p.mesh_ext[1] * p.mesh_ext[2];
+            hmesh[r].assign(meshes[r], meshes[r] + m);
+        }
+    }
+    count.assign(n, 0);
+    knext.assign(n, 0);
+    drawn.assign(n, 0);
+    dens_acc.assign(n, 0);
+    rounds_r.assign(n, 0);
+    NF_CK(ctr.ensure(C_NCTR));
+    return NF_OK;
+}
+
+nf_status Engine::set_density(int r, int nx, int ny, int nz, const float* values) {
+    if (r < 0 || r >= R) return NF_ERR_PARAM;
+    prm[r].mesh_ext[0] = nx;
+    prm[r].mesh_ext[1] = ny;
+    prm[r].mesh_ext[2] = nz;
+    hmesh[r].assign(values, values + (size_t)nx * ny * nz);
+    return NF_OK;
+}
+
+void Engine::release() {
+    DBuf<float4>* f4[] = {&pos, &dir, &spos, &sdir, &cpos, &cdir};
+    for (auto* b : f4) b->release();
+    DBuf<uint32_t>* u32[] = {&dcount, &rodoff, &rstart, &rcursor, &sid, &coff, &keep, &kpos, &ccount,
+                             &cstart, &ccursor, &cperm, &creal, &ccell, &ccnt, &clist, &accf, &accpos,
+                             &meta, &u32tmp, &rcnt, &rpos, &rcur, &cI, &cJ, &creal2, &eflag, &parent,
+                             &cflag, &aidx, &rowp, &col, &deg};
+    for (auto* b : u32) b->release();
+    DBuf<uint64_t>* u64[] = {&sidx, &kbeg, &csidx};
+    for (auto* b : u64) b->release();
+    DBuf<double>* d64[] = {&ct0, &ct1, &cD, &cG, &cS, &vsrc, &vsnk, &volt, &val64, &diag64, &bvec, &xvec, &cgred};
+    for (auto* b : d64) b->release();
+    dreal.release(); mesh.release(); state.release(); ctr.release(); cubtmp.release();
+    rec.release(); rec2.release(); recn.release(); cimg.release();
+    val32.release(); diag32.release(); cgbuf.release();
+}
+
+nf_status Engine::rebuild_cells() {
+    NF_CK(cudaMemsetAsync(ccount.p, 0, sizeof(uint32_t) * (ncell + 1), st));
+    NF_CK(u32tmp.ensure(rod_slots + 1));
+    if (rod_slots) {
+        k_rod_count<<<grid_for(rod_slots, 256), 256, 0, st>>>((uint32_t)rod_slots, R, rodoff.p, dcount.p, dreal.p,
+                                                              pos.p, u32tmp.p, ccount.p);
+        NF_CK(cudaGetLastError());
+    }
+    nf_status s = scan_u32(ccount.p, rstart.p, ncell + 1);
+    if (s != NF_OK) return s;
+    NF_CK(cudaMemsetAsync(rcursor.p, 0, sizeof(uint32_t) * (ncell + 1), st));
+    if (rod_slots) {
+        k_rod_scatter<<<grid_for(rod_slots, 256), 256, 0, st>>>((uint32_t)rod_slots, u32tmp.p, rstart.p, rcursor.p,
+                                                                pos.p, dir.p, spos.p, sdir.p, sid.p);
+        NF_CK(cudaGetLastError());
+    }
+    cells_valid = true;
+    return NF_OK;
+}
+
+// Sets up grids, uploads meshes and realisation descriptors, sizes rod storage.
+static nf_status setup_reals(Engine& E) {
+    std::vector<uint32_t> mesh_off(E.R, 0);
+    size_t mtot = 0;
+    for (int r = 0; r < E.R; ++r) { mesh_off[r] = (uint32_t)mtot; mtot += E.hmesh[r].size(); }
+    cudaError_t e = E.mesh.ensure(mtot + 1);
+    if (e != cudaSuccess) return E.cuda_fail(e, "mesh alloc");
+    for (int r = 0; r < E.R; ++r)
+        if (!E.hmesh[r].empty()) {
+            e = cudaMemcpyAsync(E.mesh.p + mesh_off[r], E.hmesh[r].data(), E.hmesh[r].size() * sizeof(float),
+                                cudaMemcpyHostToDevice, E.st);
+            if (e != cudaSuccess) return E.cuda_fail(e, "mesh upload");
+        }
+    E.hreal.resize(E.R);
+    uint32_t coffs = 0;
+    uint64_t roff = 0;
+    std::vector<uint32_t> hrodoff(E.R + 1);
+    for (int r = 0; r < E.R; ++r) {
+        const nf_params& p = E.prm[r];
+        int mn[3] = {p.mesh_ext[0], p.mesh_ext[1], p.mesh_ext[2]};
+        const float* dm = E.hmesh[r].empty() ? nullptr : E.mesh.p + mesh_off[r];
+        Real Re = make_real(p, dm, mn, stage_reach(p));
+        Re.cell_off = coffs;
+        Re.ncell = (uint32_t)(Re.n[0] * Re.n[1] * Re.n[2]);
+        coffs += Re.ncell;
+        int64_t tgt = target_count(p);
+        if (tgt < 0 || tgt > 0x7fffffff) { E.err = "target count out of range"; return NF_ERR_PARAM; }
+        Re.target = (uint32_t)tgt;
+        Re.rod_off = (uint32_t)roff;
+        hrodoff[r] = (uint32_t)roff;
+        roff += Re.target;
+        if (roff > 0xffffff00ull) { E.err = "too many rods"; return NF_ERR_PARAM; }
+        E.hreal[r] = Re;
+    }
+    hrodoff[E.R] = (uint32_t)roff;
+    E.ncell = coffs;
+    E.rod_slots = roff;
+#define NF_CKS(x) do { cudaError_t e_ = (x); if (e_ != cudaSuccess) return E.cuda_fail(e_, #x); } while (0)
+    NF_CKS(E.dreal.ensure(E.R));
+    NF_CKS(cudaMemcpyAsync(E.dreal.p, E.hreal.data(), sizeof(Real) * E.R, cudaMemcpyHostToDevice, E.st));
+    NF_CKS(E.rodoff.ensure(E.R + 1));
+    NF_CKS(cudaMemcpyAsync(E.rodoff.p, hrodoff.data(), sizeof(uint32_t) * (E.R + 1), cudaMemcpyHostToDevice, E.st));
+    NF_CKS(E.pos.ensure(roff + 1));
+    NF_CKS(E.dir.ensure(roff + 1));
+    NF_CKS(E.sidx.ensure(roff + 1));
+    NF_CKS(E.spos.ensure(roff + 1));
+    NF_CKS(E.sdir.ensure(roff + 1));
+    NF_CKS(E.sid.ensure(roff + 1));
+    NF_CKS(E.dcount.ensure(E.R));
+    NF_CKS(E.rstart.ensure(E.ncell + 1));
+    NF_CKS(E.rcursor.ensure(E.ncell + 1));
+    NF_CKS(E.ccount.ensure(E.ncell + 1));
+    NF_CKS(E.cstart.ensure(E.ncell + 1));
+    NF_CKS(E.ccursor.ensure(E.ncell + 1));
+#undef NF_CKS
+    return NF_OK;
+}
+
+nf_status Engine::setup() { return setup_reals(*this); }
+
+__global__ void k_stream_dump(const Real* __restrict__ reals, uint64_t k0, uint64_t n, float* __restrict__ out) {
+    uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float4 p, d;
+    float u, rho;
+    candidate(reals[0], k0 + i, &p, &d, &u, &rho);
+    float* o = out + 10 * i;
+    o[0] = p.x; o[1] = p.y; o[2] = p.z; o[3] = d.x; o[4] = d.y; o[5] = d.z;
+    o[6] = p.w; o[7] = d.w; o[8] = u; o[9] = rho;
+}
+
+nf_status Engine::stream_dump(uint64_t k0, uint64_t n, float* host10) {
+    nf_status s = setup_reals(*this);
+    if (s != NF_OK) return s;
+    DBuf<float> o;
+    NF_CK(o.ensure(10 * n + 1));
+    if (n) k_stream_dump<<<grid_for(n, 256), 256, 0, st>>>(dreal.p, k0, n, o.p);
+    NF_CK(cudaGetLastError());
+    NF_CK(cudaMemcpyAsync(host10, o.p, sizeof(float) * 10 * n, cudaMemcpyDeviceToHost, st));
+    NF_CK(cudaStreamSynchronize(st));
+    o.release();
+    return NF_OK;
+}
+
+// Replace realisation 0's rods (e.g. read from output.bin); the target becomes n.
+nf_status Engine::inject(size_t n, const float4* hpos, const float4* hdir, const uint64_t* hsidx) {
+    if (R != 1) { err = "rods can be set on a single-realisation handle only"; return NF_ERR_STATE; }
+    prm[0].n_target = (int64_t)n;
+    nf_status s = setup_reals(*this);
+    if (s != NF_OK) return s;
+    if (n) {
+        NF_CK(cudaMemcpyAsync(pos.p, hpos, sizeof(float4) * n, cudaMemcpyHostToDevice, st));
+        NF_CK(cudaMemcpyAsync(dir.p, hdir, sizeof(float4) * n, cudaMemcpyHostToDevice, st));
+        if (hsidx) NF_CK(cudaMemcpyAsync(sidx.p, hsidx, sizeof(uint64_t) * n, cudaMemcpyHostToDevice, st));
+        else NF_CK(cudaMemsetAsync(sidx.p, 0xff, sizeof(uint64_t) * n, st));
+    }
+    count.assign(1, (uint32_t)n);
+    knext.assign(1, 0);
+    drawn.assign(1, 0);
+    dens_acc.assign(1, 0);
+    NF_CK(cudaMemcpyAsync(dcount.p, count.data(), sizeof(uint32_t), cudaMemcpyHostToDevice, st));
+    s = rebuild_cells();
+    if (s != NF_OK) return s;
+    contacts_valid = false;
+    solve_valid = false;
+    std::memset(&gst, 0, sizeof(gst));
+    gst.accepted = n;
+    gst.target = n;
+    gst.target_reached = 1;
+    NF_CK(cudaStreamSynchronize(st));
+    return NF_OK;
+}
+
+nf_status Engine::generate() {
+    nf_status s = setup_reals(*this);
+    if (s != NF_OK) return s;
+    cudaEvent_t e0, e1;
+    NF_CK(cudaEventCreate(&e0));
+    NF_CK(cudaEventCreate(&e1));
+    NF_CK(cudaEventRecord(e0, st));
+    std::fill(count.begin(), count.end(), 0u);
+    std::fill(knext.begin(), knext.end(), 0ull);
+    std::fill(drawn.begin(), drawn.end(), 0ull);
+    std::fill(dens_acc.begin(), dens_acc.end(), 0ull);
+    std::fill(rounds_r.begin(), rounds_r.end(), 0);
+    NF_CK(cudaMemsetAsync(dcount.p, 0, sizeof(uint32_t) * R, st));
+    NF_CK(cudaMemsetAsync(ctr.p, 0, sizeof(unsigned long long) * C_NCTR, st));
+    s = rebuild_cells();
+    if (s != NF_OK) return s;
+    contacts_valid = false;
+    solve_valid = false;
+
+    // Round sizing statistics.
+    std::vector<double> p_dens(R), alive_max(R);
+    for (int r = 0; r < R; ++r) {
+        const nf_params& p = prm[r];
+        double mean = p.density_default, peak = 1.0;
+        if (!hmesh[r].empty()) {
+            double sm = 0, mx = 0;
+            for (float v : hmesh[r]) { sm += v; mx = std::max(mx, (double)v); }
+            mean = sm / hmesh[r].size();
+            peak = mean > 0 ? std::max(1.0, mx / mean) : 1.0;
+        }
+        p_dens[r] = std::min(1.0, std::max(mean, 1e-3));
+        double lmax, amax;
+        size_bounds(p, &lmax, &amax);
+        double V = (double)p.box[0] * p.box[1] * p.box[2];
+        double vex = 0.5 * M_PI * lmax * lmax * (2 * amax + p.sep) + 1e-12;
+        // ~8 expected in-round conflicts per survivor at the density peak
+        alive_max[r] = std::max(4096.0, 8.0 * V / (vex * peak));
+    }
+    std::vector<uint32_t> hcoff(R + 1);
+    std::vector<uint64_t> hkbeg(R), hout(2 * R);
+    std::vector<uint32_t> hmeta(4 * R);
+    std::vector<uint64_t> c_round(R);
+    double scale = 1.0;
+    int rounds = 0;
+    const int max_rounds = 100000;
+    for (; rounds < max_rounds; ++rounds) {
+        uint64_t slots = 0;
+        int active = 0;
+        for (int r = 0; r < R; ++r) {
+            const nf_params& p = prm[r];
+            uint64_t c = 0;
+            uint32_t tgt = hreal[r].target;
+            if (count[r] < tgt && knext[r] < p.n_candidates) {
+                double acc_rate = p_dens[r];
+                if (knext[r] > 0 && dens_acc[r] > 0)
+                    acc_rate = ((double)dens_acc[r] / knext[r]) * std::max(0.02, (double)count[r] / dens_acc[r]);
+                double want = (tgt - count[r]) / std::max(acc_rate, 1e-6) * 1.2 + 256;
+                // survivors of the old-rod test per round stay near alive_max
+                double amax_c = alive_max[r] / std::max(acc_rate, 1e-6);
+                double cr = std::min(want, amax_c) * scale;
+                if (p.round_candidates > 0) cr = std::min(cr, (double)p.round_candidates);
+                c = (uint64_t)std::max(64.0, cr);
+                c = std::min<uint64_t>(c, p.n_candidates - knext[r]);
+                c = std::min<uint64_t>(c, 1u << 24);
+                ++active;
+            }
+            c_round[r] = c;
+            hcoff[r] = (uint32_t)slots;
+            hkbeg[r] = knext[r];
+            slots += c;
+        }
+        hcoff[R] = (uint32_t)slots;
+        if (!active) break;
+        // Buffers.
+        NF_CK(coff.ensure(R + 1));
+        NF_CK(kbeg.ensure(R));
+        NF_CK(keep.ensure(slots + 1));
+        NF_CK(kpos.ensure(slots + 1));
+        NF_CK(cpos.ensure(slots));
+        NF_CK(cdir.ensure(slots));
+        NF_CK(csidx.ensure(slots));
+        NF_CK(creal.ensure(slots));
+        NF_CK(ccell.ensure(slots));
+        NF_CK(cperm.ensure(slots));
+        NF_CK(state.ensure(slots));
+        NF_CK(ccnt.ensure(slots));
+        NF_CK(clist.ensure(slots * kConflictCap));
+        NF_CK(accf.ensure(slots + 1));
+        NF_CK(accpos.ensure(slots + 1));
+        NF_CK(meta.ensure(4 * R));
+        NF_CK(recn.ensure(2 * R + 2));
+        NF_CK(cudaMemcpyAsync(coff.p, hcoff.data(), sizeof(uint32_t) * (R + 1), cudaMemcpyHostToDevice, st));
+        NF_CK(cudaMemcpyAsync(kbeg.p, hkbeg.data(), sizeof(uint64_t) * R, cudaMemcpyHostToDevice, st));
+        const unsigned gs = grid_for(slots, 256);
+        k_stream_keep<<<gs, 256, 0, st>>>(dreal.p, R, coff.p, kbeg.p, (uint32_t)slots, keep.p);
+        NF_CK(cudaGetLastError());
+        NF_CK(cudaMemsetAsync(keep.p + slots, 0, sizeof(uint32_t), st));
+        s = scan_u32(keep.p, kpos.p, slots + 1);  // kpos[slots] = compacted total
+        if (s != NF_OK) return s;
+        uint32_t* ntot = kpos.p + slots;
+        NF_CK(cudaMemsetAsync(ccount.p, 0, sizeof(uint32_t) * (ncell + 1), st));
+        k_compact<<<gs, 256, 0, st>>>(dreal.p, R, coff.p, kbeg.p, (uint32_t)slots, keep.p, kpos.p, cpos.p, cdir.p,
+                                     csidx.p, creal.p, ccell.p, ccount.p, state.p);
+        NF_CK(cudaGetLastError());
+        s = scan_u32(ccount.p, cstart.p, ncell + 1);
+        if (s != NF_OK) return s;
+        NF_CK(cudaMemsetAsync(ccursor.p, 0, sizeof(uint32_t) * (ncell + 1), st));
+        k_bin<<<gs, 256, 0, st>>>((uint32_t)slots, ntot, ccell.p, cstart.p, ccursor.p, cperm.p);
+        NF_CK(cudaGetLastError());
+        k_old_test<<<gs, 256, 0, st>>>(dreal.p, ntot, cperm.p, cpos.p, cdir.p, creal.p, rstart.p, spos.p, sdir.p,
+                                       total_rods() > 0 ? 1 : 0, state.p, ctr.p);
+        NF_CK(cudaGetLastError());
+        NF_CK(cudaMemsetAsync(ctr.p + C_OVERFLOW, 0, sizeof(unsigned long long), st));
+        k_conflicts<<<gs, 256, 0, st>>>(dreal.p, ntot, cperm.p, cstart.p, cpos.p, cdir.p, csidx.p, creal.p, state.p,
+                                        ccnt.p, clist.p, ctr.p);
+        NF_CK(cudaGetLastError());
+        unsigned long long ovf = 0;
+        NF_CK(cudaMemcpyAsync(&ovf, ctr.p + C_OVERFLOW, sizeof(ovf), cudaMemcpyDeviceToHost, st));
+        NF_CK(cudaStreamSynchronize(st));
+        if (ovf) {  // too many in-round conflicts: redo the round with fewer candidates
+            scale *= 0.5;
+            if (scale < 1e-4) { err = "in-round conflict list overflow"; return NF_ERR_OVERFLOW; }
+            --rounds;
+            continue;
+        }
+        // Resolution passes (chains are short; bounded by the round size).
+        uint64_t passes = 0;
+        for (;;) {
+            NF_CK(cudaMemsetAsync(ctr.p + C_UNDECIDED, 0, sizeof(unsigned long long), st));
+            for (int q = 0; q < 4; ++q)
+                k_resolve<<<gs, 256, 0, st>>>(ntot, state.p, ccnt.p, clist.p, ctr.p);
+            NF_CK(cudaGetLastError());
+            passes += 4;
+            // The last pass's undecided count: re-zero then one more pass.
+            NF_CK(cudaMemsetAsync(ctr.p + C_UNDECIDED, 0, sizeof(unsigned long long), st));
+            k_resolve<<<gs, 256, 0, st>>>(ntot, state.p, ccnt.p, clist.p, ctr.p);
+            ++passes;
+            unsigned long long und = 0;
+            NF_CK(cudaMemcpyAsync(&und, ctr.p + C_UNDECIDED, sizeof(und), cudaMemcpyDeviceToHost, st));
+            NF_CK(cudaStreamSynchronize(st));
+            if (!und) break;
+            if (passes > slots + 8) { err = "conflict resolution did not converge"; return NF_ERR_TIMEOUT; }
+        }
+        // Append.
+        k_accflag<<<grid_for(slots + 1, 256), 256, 0, st>>>(ntot, (uint32_t)(slots + 1), state.p, accf.p);
+        NF_CK(cudaGetLastError());
+        s = scan_u32(accf.p, accpos.p, slots + 1);
+        if (s != NF_OK) return s;
+        k_meta<<<grid_for(R, 128), 128, 0, st>>>(R, coff.p, keep.p, kpos.p, accf.p, accpos.p, meta.p);
+        NF_CK(cudaGetLastError());
+        NF_CK(cudaMemsetAsync(recn.p, 0, sizeof(unsigned long long) * 2 * R, st));
+        k_append<<<gs, 256, 0, st>>>(ntot, state.p, creal.p, accpos.p, meta.p, rodoff.p, dcount.p, dreal.p, cpos.p,
+                                     cdir.p, csidx.p, pos.p, dir.p, sidx.p, (uint64_t*)recn.p);
+        NF_CK(cudaGetLastError());
+        NF_CK(cudaMemcpyAsync(hmeta.data(), meta.p, sizeof(uint32_t) * 4 * R, cudaMemcpyDeviceToHost, st));
+        NF_CK(cudaMemcpyAsync(hout.data(), recn.p, sizeof(uint64_t) * 2 * R, cudaMemcpyDeviceToHost, st));
+        NF_CK(cudaStreamSynchronize(st));
+        bool any_new = false;
+        for (int r = 0; r < R; ++r) {
+            if (!c_round[r]) continue;
+            ++rounds_r[r];
+            uint32_t rem = hreal[r].target - count[r];
+            uint32_t got = std::min(hmeta[4 * r + 3], rem);
+            uint32_t kept = hmeta[4 * r + 1] - hmeta[4 * r + 0];
+            if (got) any_new = true;
+            count[r] += got;
+            if (count[r] == hreal[r].target && got == rem && rem > 0) {
+                drawn[r] = hout[2 * r + 0];
+                dens_acc[r] += hout[2 * r + 1];
+            } else {
+                dens_acc[r] += kept;
+            }
+            knext[r] += c_round[r];
+            if (count[r] < hreal[r].target) drawn[r] = knext[r];
+        }
+        NF_CK(cudaMemcpyAsync(dcount.p, count.data(), sizeof(uint32_t) * R, cudaMemcpyHostToDevice, st));
+        if (any_new) {
+            s = rebuild_cells();
+            if (s != NF_OK) return s;
+        }
+        scale = std::min(1.0, scale * 2.0);
+    }
+    NF_CK(cudaEventRecord(e1, st));
+    NF_CK(cudaEventSynchronize(e1));
+    float ms = 0;
+    NF_CK(cudaEventElapsedTime(&ms, e0, e1));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    unsigned long long hc[C_NCTR];
+    NF_CK(cudaMemcpy(hc, ctr.p, sizeof(hc), cudaMemcpyDeviceToHost));
+    std::memset(&gst, 0, sizeof(gst));
+    for (int r = 0; r < R; ++r) {
+        gst.candidates_drawn += drawn[r];
+        gst.density_accepted += dens_acc[r];
+        gst.accepted += count[r];
+        gst.target += hreal[r].target;
+    }
+    gst.pair_tests = hc[C_PAIR_TESTS];
+    gst.exact_evals = hc[C_EXACT];
+    gst.fp32_would_flip = hc[C_FLIPS];
+    gst.rounds = rounds;
+    gst.target_reached = gst.accepted == gst.target;
+    gst.ms = ms;
+    return NF_OK;
+}
+
+#undef NF_CK
+}  // namespace nf

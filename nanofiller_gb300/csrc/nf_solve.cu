@@ -1,0 +1,523 @@
+// nf_solve.cu -- conductance network: assembly, mixed-precision solve, adjoint.
+//
+// Reference path replaced: the offline Kirchhoff tool (tools/kirchhoff/kirchhoff.py:
+// 211-269 with MKL DSS, tools/kirchhoff/lib/solver.cpp:185-269). Rods are nodes
+// (equipotential); a rod-rod contact is a conductance G = G0 exp(-(gap-d_c)/lambda),
+// gap floored at d_c (kirchhoff.py:146-148); electrode contacts enter in Norton
+// form: diag += G_src + G_snk, rhs = G_src (source at 1 V, sink at 0 V,
+// kirchhoff.py:239-242). G_eff = sum_i G_src,i (1 - V_i) (kirchhoff.py:269).
+//
+// Only rods whose connected component touches both electrodes carry current, so
+// only those are unknowns (the rest of the matrix is singular or irrelevant; the
+// reference floors empty rows at 1, kirchhoff.py:240).
+//
+// Solve: Jacobi-preconditioned CG in FP32 on the FP32 copy of the matrix, inside
+// iterative refinement whose residual b - K x is accumulated in FP64 from the
+// FP64 matrix. One CTA per realisation, all reductions block-deterministic.
+//
+// Adjoint: the Laplacian is self-adjoint, so dG_eff/dG_e = (V_i - V_j)^2 with
+// V_src = 1, V_snk = 0 (Thomson's principle); no second solve is needed.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+
+#include "nf_engine.cuh"
+
+namespace nf {
+
+static inline unsigned grid_for(size_t n, unsigned b) { return (unsigned)((n + b - 1) / b); }
+
+constexpr uint32_t kFindCap = 1u << 22;  // bound on union-find walks / CAS retries
+
+__device__ __forceinline__ uint32_t uf_find(uint32_t* parent, uint32_t x, uint32_t* err) {
+    uint32_t steps = 0;
+    while (true) {
+        uint32_t p = parent[x];
+        if (p == x) return x;
+        uint32_t g = parent[p];
+        if (g != p) atomicCAS(&parent[x], p, g);  // path halving
+        x = p;
+        if (++steps > kFindCap) { atomicExch(err, 1u); return x; }
+    }
+}
+
+__global__ void k_uf_init(uint32_t n, uint32_t* parent, uint32_t* flag) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    parent[i] = i;
+    flag[i] = 0;
+}
+
+__global__ void k_uf_union(uint32_t m, const uint32_t* __restrict__ I, const uint32_t* __restrict__ J,
+                           uint32_t* parent, uint32_t* err) {
+    uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= m) return;
+    uint32_t j = J[e];
+    if (j >= NF_SNK_ELEC) return;
+    uint32_t a = I[e], b = j;
+    for (uint32_t it = 0; it < kFindCap; ++it) {
+        a = uf_find(parent, a, err);
+        b = uf_find(parent, b, err);
+        if (a == b) return;
+        if (a < b) { uint32_t t = a; a = b; b = t; }
+        if (atomicCAS(&parent[a], a, b) == a) return;  // hook larger root under smaller
+    }
+    atomicExch(err, 1u);
+}
+
+__global__ void k_uf_flags(uint32_t m, const uint32_t* __restrict__ I, const uint32_t* __restrict__ J,
+                           uint32_t* parent, uint32_t* flag, uint32_t* err) {
+    uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= m) return;
+    uint32_t j = J[e];
+    if (j < NF_SNK_ELEC) return;
+    uint32_t r = uf_find(parent, I[e], err);
+    atomicOr(&flag[r], j == NF_SRC_ELEC ? 1u : 2u);
+}
+
+// Active (current-carrying) rods; per-rod source / sink conductance.
+__global__ void k_active(uint32_t n, uint32_t* parent, const uint32_t* __restrict__ flag, uint32_t* __restrict__ act,
+                         uint32_t* err) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    act[i] = flag[uf_find(parent, i, err)] == 3u ? 1u : 0u;
+}
+
+__global__ void k_elec_g(uint32_t m, const uint32_t* __restrict__ I, const uint32_t* __restrict__ J,
+                         const double* __restrict__ G, double* __restrict__ s, double* __restrict__ t) {
+    uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= m) return;
+    uint32_t j = J[e];
+    if (j == NF_SRC_ELEC) s[I[e]] = G[e];
+    else if (j == NF_SNK_ELEC) t[I[e]] = G[e];
+}
+
+__global__ void k_deg(uint32_t m, const uint32_t* __restrict__ I, const uint32_t* __restrict__ J,
+                      const uint32_t* __restrict__ act, const uint32_t* __restrict__ aidx, uint32_t* __restrict__ deg) {
+    uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= m) return;
+    uint32_t j = J[e];
+    if (j >= NF_SNK_ELEC) return;
+    uint32_t i = I[e];
+    if (!act[i]) return;  // both ends share a component
+    atomicAdd(&deg[aidx[i]], 1u);
+    atomicAdd(&deg[aidx[j]], 1u);
+}
+
+__global__ void k_fill(uint32_t m, const uint32_t* __restrict__ I, const uint32_t* __restrict__ J,
+                       const double* __restrict__ G, const uint32_t* __restrict__ act,
+                       const uint32_t* __restrict__ aidx, const uint32_t* __restrict__ rowp, uint32_t* __restrict__ cur,
+                       uint32_t* __restrict__ col, double* __restrict__ v64) {
+    uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= m) return;
+    uint32_t j = J[e];
+    if (j >= NF_SNK_ELEC) return;
+    uint32_t i = I[e];
+    if (!act[i]) return;
+    uint32_t a = aidx[i], b = aidx[j];
+    uint32_t qa = rowp[a] + atomicAdd(&cur[a], 1u);
+    uint32_t qb = rowp[b] + atomicAdd(&cur[b], 1u);
+    col[qa] = b; v64[qa] = -G[e];
+    col[qb] = a; v64[qb] = -G[e];
+}
+
+// Sort each row by column (deterministic SpMV order), diagonal, FP32 copies, rhs.
+__global__ void k_rows(uint32_t nslot, const uint32_t* __restrict__ act, const uint32_t* __restrict__ aidx,
+                       const uint32_t* __restrict__ rowp, uint32_t* __restrict__ col, double* __restrict__ v64,
+                       float* __restrict__ v32, const double* __restrict__ s, const double* __restrict__ t,
+                       double* __restrict__ d64, float* __restrict__ d32, double* __restrict__ b) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nslot || !act[i]) return;
+    uint32_t a = aidx[i];
+    uint32_t p0 = rowp[a], p1 = rowp[a + 1];
+    for (uint32_t k = p0 + 1; k < p1; ++k) {
+        uint32_t c = col[k];
+        double v = v64[k];
+        uint32_t q = k;
+        while (q > p0 && col[q - 1] > c) { col[q] = col[q - 1]; v64[q] = v64[q - 1]; --q; }
+        col[q] = c;
+        v64[q] = v;
+    }
+    double dg = 0.0;
+    for (uint32_t k = p0; k < p1; ++k) { dg -= v64[k]; v32[k] = (float)v64[k]; }
+    dg += s[i] + t[i];
+    d64[a] = dg;
+    d32[a] = (float)dg;
+    b[a] = s[i];
+}
+
+// ---------------------------------------------------------------------------
+// Block reductions (deterministic: fixed thread->row mapping and tree).
+// ---------------------------------------------------------------------------
+template <int NT>
+__device__ __forceinline__ double block_sum(double v, double* sh) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    __syncthreads();
+    if (l == 0) sh[w] = v;
+    __syncthreads();
+    if (w == 0) {
+        double x = (l < NT / 32) ? sh[l] : 0.0;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+        if (l == 0) sh[32] = x;
+    }
+    __syncthreads();
+    return sh[32];
+}
+
+template <int NT>
+__device__ __forceinline__ void block_sum2(float a, float b, double* sh, double* oa, double* ob) {
+    double x = a, y = b;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        x += __shfl_down_sync(0xffffffffu, x, o);
+        y += __shfl_down_sync(0xffffffffu, y, o);
+    }
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    __syncthreads();
+    if (l == 0) { sh[w] = x; sh[40 + w] = y; }
+    __syncthreads();
+    if (w == 0) {
+        double u = (l < NT / 32) ? sh[l] : 0.0, v = (l < NT / 32) ? sh[40 + l] : 0.0;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            u += __shfl_down_sync(0xffffffffu, u, o);
+            v += __shfl_down_sync(0xffffffffu, v, o);
+        }
+        if (l == 0) { sh[32] = u; sh[33] = v; }
+    }
+    __syncthreads();
+    *oa = sh[32];
+    *ob = sh[33];
+}
+
+struct CgOut {
+    double G, res;
+    int outer, inner, n;
+    int pad;
+};
+
+// One CTA per realisation. work: 4 float vectors (r, z, p, q) + e per active row.
+template <int NT>
+__global__ void __launch_bounds__(NT) k_cg(int R, const uint32_t* __restrict__ abase,
+                                           const uint32_t* __restrict__ rowp, const uint32_t* __restrict__ col,
+                                           const float* __restrict__ v32, const double* __restrict__ v64,
+                                           const float* __restrict__ d32, const double* __restrict__ d64,
+                                           const double* __restrict__ b, double* __restrict__ x,
+                                           double* __restrict__ r64, float* __restrict__ work, double tol,
+                                           int max_inner, CgOut* __restrict__ out) {
+    __shared__ double sh[96];
+    const int rr = blockIdx.x;
+    if (rr >= R) return;
+    const uint32_t base = abase[rr], n = abase[rr + 1] - base;
+    float* w_r = work + 5ull * base;
+    float* w_z = w_r + n;
+    float* w_p = w_z + n;
+    float* w_q = w_p + n;
+    float* w_e = w_q + n;
+    CgOut o{};
+    o.n = (int)n;
+    if (n == 0) {
+        if (threadIdx.x == 0) out[rr] = o;
+        return;
+    }
+    const double* bb = b + base;
+    double* xx = x + base;
+    double* rv = r64 + base;
+    const float* dd = d32 + base;
+    double part = 0.0;
+    for (uint32_t i = threadIdx.x; i < n; i += NT) {
+        xx[i] = 0.0;
+        rv[i] = bb[i];
+        part += bb[i] * bb[i];
+    }
+    const double bn = sqrt(block_sum<NT>(part, sh));
+    double rn = bn;
+    int inner_total = 0, outer = 0;
+    const float inner_tol = 1e-4f;
+    for (; outer < 40; ++outer) {
+        if (!(rn > tol * bn)) break;
+        const float sc = (float)(1.0 / rn);
+        float prz = 0.f, prr = 0.f;
+        for (uint32_t i = threadIdx.x; i < n; i += NT) {
+            float ri = (float)rv[i] * sc;
+            float zi = ri / dd[i];
+            w_r[i] = ri; w_z[i] = zi; w_p[i] = zi; w_e[i] = 0.f;
+            prz += ri * zi;
+            prr += ri * ri;
+        }
+        double rz, rr2;
+        block_sum2<NT>(prz, prr, sh, &rz, &rr2);
+        const double r0 = sqrt(rr2);
+        int it = 0;
+        for (; it < max_inner; ++it) {
+            __syncthreads();  // p complete
+            float ppq = 0.f;
+            for (uint32_t i = threadIdx.x; i < n; i += NT) {
+                const uint32_t g = base + i;
+                float acc = ((float)d64[g]) * w_p[i];
+                for (uint32_t k = rowp[g], k1 = rowp[g + 1]; k < k1; ++k) acc += v32[k] * w_p[col[k] - base];
+                w_q[i] = acc;
+                ppq += w_p[i] * acc;
+            }
+            const double pq = block_sum<NT>((double)ppq, sh);
+            if (!(pq > 0.0)) break;
+            const float alpha = (float)(rz / pq);
+            float qz = 0.f, qr = 0.f;
+            for (uint32_t i = threadIdx.x; i < n; i += NT) {
+                w_e[i] += alpha * w_p[i];
+                float ri = w_r[i] - alpha * w_q[i];
+                w_r[i] = ri;
+                float zi = ri / dd[i];
+                w_z[i] = zi;
+                qz += ri * zi;
+                qr += ri * ri;
+            }
+            double rz_new, rr_new;
+            block_sum2<NT>(qz, qr, sh, &rz_new, &rr_new);
+            if (sqrt(rr_new) <= inner_tol * r0) { ++it; break; }
+            const float beta = (float)(rz_new / rz);
+            rz = rz_new;
+            for (uint32_t i = threadIdx.x; i < n; i += NT) w_p[i] = w_z[i] + beta * w_p[i];
+        }
+        inner_total += it;
+        __syncthreads();
+        for (uint32_t i = threadIdx.x; i < n; i += NT) xx[i] += rn * (double)w_e[i];
+        __syncthreads();
+        // FP64 residual in row order.
+        part = 0.0;
+        for (uint32_t i = threadIdx.x; i < n; i += NT) {
+            const uint32_t g = base + i;
+            double acc = d64[g] * xx[i];
+            for (uint32_t k = rowp[g], k1 = rowp[g + 1]; k < k1; ++k) acc += v64[k] * xx[col[k] - base];
+            double ri = bb[i] - acc;
+            rv[i] = ri;
+            part += ri * ri;
+        }
+        rn = sqrt(block_sum<NT>(part, sh));
+        if (it == 0) break;  // no progress possible
+    }
+    part = 0.0;
+    for (uint32_t i = threadIdx.x; i < n; i += NT) part += bb[i] * (1.0 - xx[i]);
+    const double G = block_sum<NT>(part, sh);
+    if (threadIdx.x == 0) {
+        o.G = G;
+        o.res = bn > 0 ? rn / bn : 0.0;
+        o.outer = outer;
+        o.inner = inner_total;
+        out[rr] = o;
+    }
+}
+
+// Voltages per rod; outside the source-sink network, components touching only
+// the source sit at 1 V and all others at 0 V (no current flows there).
+__global__ void k_scatter_v(uint32_t nslot, const uint32_t* __restrict__ act, const uint32_t* __restrict__ aidx,
+                            const double* __restrict__ x, uint32_t* parent, const uint32_t* __restrict__ flag,
+                            double* __restrict__ volt, uint32_t* err) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nslot) return;
+    volt[i] = act[i] ? x[aidx[i]] : (flag[uf_find(parent, i, err)] == 1u ? 1.0 : 0.0);
+}
+
+#define NF_CK(x)                                            \
+    do {                                                    \
+        cudaError_t e_ = (x);                               \
+        if (e_ != cudaSuccess) return cuda_fail(e_, #x);    \
+    } while (0)
+
+nf_status Engine::solve() {
+    if (!contacts_valid) { err = "no contacts: run nf_contacts first"; return NF_ERR_STATE; }
+    cudaEvent_t e0, e1;
+    NF_CK(cudaEventCreate(&e0));
+    NF_CK(cudaEventCreate(&e1));
+    NF_CK(cudaEventRecord(e0, st));
+    const uint32_t nslot = (uint32_t)rod_slots;
+    const uint32_t m = (uint32_t)ct_off[R];
+    NF_CK(parent.ensure(nslot + 1));
+    NF_CK(cflag.ensure(nslot + 1));
+    NF_CK(aidx.ensure(nslot + 1));
+    NF_CK(eflag.ensure(nslot + 2));  // act[] + error word
+    NF_CK(vsrc.ensure(nslot + 1));
+    NF_CK(vsnk.ensure(nslot + 1));
+    NF_CK(volt.ensure(nslot + 1));
+    uint32_t* act = eflag.p;
+    uint32_t* errw = eflag.p + nslot + 1;
+    NF_CK(cudaMemsetAsync(errw, 0, sizeof(uint32_t), st));
+    NF_CK(cudaMemsetAsync(vsrc.p, 0, sizeof(double) * (nslot + 1), st));
+    NF_CK(cudaMemsetAsync(vsnk.p, 0, sizeof(double) * (nslot + 1), st));
+    NF_CK(cudaMemsetAsync(act + nslot, 0, sizeof(uint32_t), st));
+    k_uf_init<<<grid_for(nslot, 256), 256, 0, st>>>(nslot, parent.p, cflag.p);
+    if (m) {
+        k_uf_union<<<grid_for(m, 256), 256, 0, st>>>(m, cI.p, cJ.p, parent.p, errw);
+        k_uf_flags<<<grid_for(m, 256), 256, 0, st>>>(m, cI.p, cJ.p, parent.p, cflag.p, errw);
+        k_elec_g<<<grid_for(m, 256), 256, 0, st>>>(m, cI.p, cJ.p, cG.p, vsrc.p, vsnk.p);
+    }
+    k_active<<<grid_for(nslot, 256), 256, 0, st>>>(nslot, parent.p, cflag.p, act, errw);
+    NF_CK(cudaGetLastError());
+    nf_status s = scan_u32(act, aidx.p, nslot + 1);
+    if (s != NF_OK) return s;
+    // Active count per realisation: aidx at rod_off boundaries.
+    std::vector<uint32_t> hrodoff(R + 1), habase(R + 1);
+    for (int r = 0; r < R; ++r) hrodoff[r] = hreal[r].rod_off;
+    hrodoff[R] = nslot;
+    for (int r = 0; r <= R; ++r)
+        NF_CK(cudaMemcpyAsync(&habase[r], aidx.p + hrodoff[r], sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+    uint32_t herr = 0;
+    NF_CK(cudaMemcpyAsync(&herr, errw, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+    NF_CK(cudaStreamSynchronize(st));
+    if (herr) { err = "union-find walk exceeded its bound"; return NF_ERR_TIMEOUT; }
+    const uint32_t na = habase[R];
+    NF_CK(deg.ensure(na + 1));
+    NF_CK(rowp.ensure(na + 1));
+    NF_CK(cudaMemsetAsync(deg.p, 0, sizeof(uint32_t) * (na + 1), st));
+    if (m) k_deg<<<grid_for(m, 256), 256, 0, st>>>(m, cI.p, cJ.p, act, aidx.p, deg.p);
+    NF_CK(cudaGetLastError());
+    s = scan_u32(deg.p, rowp.p, na + 1);
+    if (s != NF_OK) return s;
+    uint32_t nnz = 0;
+    NF_CK(cudaMemcpyAsync(&nnz, rowp.p + na, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+    NF_CK(cudaStreamSynchronize(st));
+    NF_CK(col.ensure(nnz + 1));
+    NF_CK(val64.ensure(nnz + 1));
+    NF_CK(val32.ensure(nnz + 1));
+    NF_CK(diag64.ensure(na + 1));
+    NF_CK(diag32.ensure(na + 1));
+    NF_CK(bvec.ensure(na + 1));
+    NF_CK(xvec.ensure(na + 1));
+    NF_CK(cgred.ensure(na + 1));
+    NF_CK(cgbuf.ensure(5 * (size_t)na + 5));
+    NF_CK(cudaMemsetAsync(deg.p, 0, sizeof(uint32_t) * (na + 1), st));  // reuse as cursor
+    if (m) k_fill<<<grid_for(m, 256), 256, 0, st>>>(m, cI.p, cJ.p, cG.p, act, aidx.p, rowp.p, deg.p, col.p, val64.p);
+    k_rows<<<grid_for(nslot, 256), 256, 0, st>>>(nslot, act, aidx.p, rowp.p, col.p, val64.p, val32.p, vsrc.p,
+                                                 vsnk.p, diag64.p, diag32.p, bvec.p);
+    NF_CK(cudaGetLastError());
+    DBuf<uint32_t>& dab = rcur;  // per-realisation active base (R+1)
+    NF_CK(dab.ensure(R + 1));
+    NF_CK(cudaMemcpyAsync(dab.p, habase.data(), sizeof(uint32_t) * (R + 1), cudaMemcpyHostToDevice, st));
+    DBuf<CgOut> outs;
+    NF_CK(outs.ensure(R));
+    const double tol = prm[0].solve_tol > 0 ? prm[0].solve_tol : 1e-10;
+    const int max_inner = prm[0].solve_max_iter > 0 ? prm[0].solve_max_iter : 20000;
+    k_cg<512><<<R, 512, 0, st>>>(R, dab.p, rowp.p, col.p, val32.p, val64.p, diag32.p, diag64.p, bvec.p, xvec.p,
+                                 cgred.p, cgbuf.p, tol, max_inner, outs.p);
+    NF_CK(cudaGetLastError());
+    k_scatter_v<<<grid_for(nslot, 256), 256, 0, st>>>(nslot, act, aidx.p, xvec.p, parent.p, cflag.p, volt.p, errw);
+    NF_CK(cudaGetLastError());
+    std::vector<CgOut> ho(R);
+    NF_CK(cudaMemcpyAsync(ho.data(), outs.p, sizeof(CgOut) * R, cudaMemcpyDeviceToHost, st));
+    NF_CK(cudaEventRecord(e1, st));
+    NF_CK(cudaEventSynchronize(e1));
+    outs.release();
+    float ms = 0;
+    NF_CK(cudaEventElapsedTime(&ms, e0, e1));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    solve_st.assign(R, nf_solve_stats{});
+    bool conv = true;
+    for (int r = 0; r < R; ++r) {
+        nf_solve_stats& S = solve_st[r];
+        S.G_eff = ho[r].G;
+        S.residual = ho[r].res;
+        S.outer_iters = ho[r].outer;
+        S.inner_iters = ho[r].inner;
+        S.n_nodes = count[r];
+        S.n_active = habase[r + 1] - habase[r];
+        S.percolating = S.n_active > 0;
+        S.ms = ms;
+        if (S.n_active > 0 && !(S.residual <= tol)) conv = false;
+    }
+    solve_valid = true;
+    if (!conv) { err = "network solve did not reach its tolerance"; return NF_ERR_NOT_CONVERGED; }
+    return NF_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Adjoint.
+// ---------------------------------------------------------------------------
+__global__ void k_adjoint(uint32_t lo, uint32_t hi, uint32_t rod0, const Real* __restrict__ reals, uint32_t r,
+                          const uint32_t* __restrict__ I, const uint32_t* __restrict__ J,
+                          const double* __restrict__ t0, const double* __restrict__ t1, const double* __restrict__ D,
+                          const double* __restrict__ G, const int8_t* __restrict__ img,
+                          const float4* __restrict__ pos, const float4* __restrict__ dir,
+                          const double* __restrict__ V, double* __restrict__ grad, double* __restrict__ acc) {
+    uint32_t e = lo + blockIdx.x * blockDim.x + threadIdx.x;
+    double dl = 0.0, dg0 = 0.0;
+    if (e < hi) {
+        const Real& Re = reals[r];
+        const uint32_t i = I[e], j = J[e];
+        const float4 pA = pos[i], cA = dir[i];
+        double dv, gap;
+        if (j == NF_SRC_ELEC) { dv = 1.0 - V[i]; gap = D[e] - cA.w; }
+        else if (j == NF_SNK_ELEC) { dv = V[i]; gap = D[e] - cA.w; }
+        else { dv = V[i] - V[j]; gap = D[e] - cA.w - dir[j].w; }
+        const double w = dv * dv;
+        dg0 = w * G[e] / Re.G0;
+        const bool clamped = !(gap > Re.dc);
+        if (!clamped) {
+            dl = w * G[e] * (gap - Re.dc) / (Re.lambda * Re.lambda);
+            const double dGdD = -G[e] / Re.lambda * w;
+            const double uI = t0[e] / pA.w + 0.5;
+            double* gi = grad + 6ull * (i - rod0);
+            if (j >= NF_SNK_ELEC) {
+                const int f = Re.field_axis;
+                const double sg = (j == NF_SRC_ELEC) ? 1.0 : -1.0;
+                atomicAdd(&gi[f], dGdD * sg * (1.0 - uI));
+                atomicAdd(&gi[3 + f], dGdD * sg * uI);
+            } else {
+                const float4 pB = pos[j], cB = dir[j];
+                const double sh[3] = {img[3 * e] * (double)Re.L[0], img[3 * e + 1] * (double)Re.L[1],
+                                      img[3 * e + 2] * (double)Re.L[2]};
+                const double pa[3] = {pA.x + t0[e] * cA.x, pA.y + t0[e] * cA.y, pA.z + t0[e] * cA.z};
+                const double pb[3] = {(pB.x + sh[0]) + t1[e] * cB.x, (pB.y + sh[1]) + t1[e] * cB.y,
+                                      (pB.z + sh[2]) + t1[e] * cB.z};
+                const double uJ = t1[e] / pB.w + 0.5;
+                double* gj = grad + 6ull * (j - rod0);
+                for (int d = 0; d < 3; ++d) {
+                    const double gd = (pa[d] - pb[d]) / D[e] * dGdD;
+                    atomicAdd(&gi[d], gd * (1.0 - uI));
+                    atomicAdd(&gi[3 + d], gd * uI);
+                    atomicAdd(&gj[d], -gd * (1.0 - uJ));
+                    atomicAdd(&gj[3 + d], -gd * uJ);
+                }
+            }
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        dl += __shfl_down_sync(0xffffffffu, dl, o);
+        dg0 += __shfl_down_sync(0xffffffffu, dg0, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicAdd(&acc[0], dl);
+        atomicAdd(&acc[1], dg0);
+    }
+}
+
+nf_status Engine::adjoint(int r, float* dG_dend, size_t cap, double* dlam, double* dg0) {
+    if (!solve_valid) { err = "no solution: run nf_solve first"; return NF_ERR_STATE; }
+    if (r < 0 || r >= R) return NF_ERR_PARAM;
+    const uint32_t n = count[r];
+    if (dG_dend && cap < (size_t)n) { err = "gradient buffer too small"; return NF_ERR_CAPACITY; }
+    DBuf<double> g;
+    NF_CK(g.ensure(6ull * n + 2));
+    NF_CK(cudaMemsetAsync(g.p, 0, sizeof(double) * (6ull * n + 2), st));
+    const uint32_t lo = (uint32_t)ct_off[r], hi = (uint32_t)ct_off[r + 1];
+    if (hi > lo)
+        k_adjoint<<<grid_for(hi - lo, 256), 256, 0, st>>>(lo, hi, hreal[r].rod_off, dreal.p, (uint32_t)r, cI.p, cJ.p,
+                                                          ct0.p, ct1.p, cD.p, cG.p, cimg.p, pos.p, dir.p, volt.p, g.p,
+                                                          g.p + 6ull * n);
+    NF_CK(cudaGetLastError());
+    std::vector<double> h(6ull * n + 2);
+    NF_CK(cudaMemcpyAsync(h.data(), g.p, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, st));
+    NF_CK(cudaStreamSynchronize(st));
+    g.release();
+    if (dG_dend)
+        for (size_t k = 0; k < 6ull * n; ++k) dG_dend[k] = (float)h[k];
+    if (dlam) *dlam = h[6ull * n];
+    if (dg0) *dg0 = h[6ull * n + 1];
+    return NF_OK;
+}
+
+#undef NF_CK
+}  // namespace nf

@@ -1,0 +1,993 @@
+// nf_oracle.cpp -- CPU oracle of the NanoFiller hot path. TEST INFRASTRUCTURE:
+// loaded only by tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg.
+//
+// Build with -ffp-contract=off (oracle/Makefile): the FP64 decisions must be
+// reproducible operation-for-operation, so no multiply-add may be fused.
+//
+// Reference lines restated here (pyrlinum/NanoFiller):
+//   cnt_intersec_shr                inc/intersection_dev.h:10-80
+//   distance_cylinder_capped        inc/intersect/intersect_cylinder_capped.h:69-147
+//   if_intersects_cylinder_capped   inc/intersect/intersect_cylinder_capped.h:157-159
+//   body_intersect_cylinder_capped  inc/intersect/intersect_cylinder_capped.h:181-183
+//   surf_to_cylinder_capped         inc/intersect/intersect_cylinder_capped.h:204-293
+//   generate_virt_inclusions        inc/conductKernels.h:289-361
+//   stride2glbID_directed_uint      inc/memoryIO.h:70-85 (+ image shift stride2dspl :533-553)
+//   set_numCNT                      src/simPrms.cpp:987-1002
+//   get_elec_dmnID (electrode role) inc/conductivity.h:71-90 (plane form, see below)
+//   kirchhoff assembly, G_eff       tools/kirchhoff/kirchhoff.py:232-269
+#include "nf_oracle.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <numeric>
+#include <vector>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+namespace {
+
+// ---------------------------------------------------------------------------
+// Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11).
+// ---------------------------------------------------------------------------
+inline void philox(const uint32_t c_in[4], const uint32_t k_in[2], uint32_t o[4]) {
+    uint32_t c0 = c_in[0], c1 = c_in[1], c2 = c_in[2], c3 = c_in[3];
+    uint32_t k0 = k_in[0], k1 = k_in[1];
+    for (int r = 0; r < 10; ++r) {
+        uint64_t p0 = (uint64_t)0xD2511F53u * c0;
+        uint64_t p1 = (uint64_t)0xCD9E8D57u * c2;
+        uint32_t hi0 = (uint32_t)(p0 >> 32), lo0 = (uint32_t)p0;
+        uint32_t hi1 = (uint32_t)(p1 >> 32), lo1 = (uint32_t)p1;
+        uint32_t n0 = hi1 ^ c1 ^ k0, n1 = lo1, n2 = hi0 ^ c3 ^ k1, n3 = lo0;
+        c0 = n0; c1 = n1; c2 = n2; c3 = n3;
+        k0 += 0x9E3779B9u; k1 += 0xBB67AE85u;
+    }
+    o[0] = c0; o[1] = c1; o[2] = c2; o[3] = c3;
+}
+
+inline float uni(uint32_t u) { return (float)(u >> 8) * 5.9604644775390625e-08f; }
+
+inline uint32_t fbits(float f) { uint32_t b; std::memcpy(&b, &f, 4); return b; }
+inline float bitsf(uint32_t b) { float f; std::memcpy(&f, &b, 4); return f; }
+
+// sin/cos of 2*pi*t: quadrant reduction in turns (exact) + Taylor polynomials.
+inline void sincos_turns(float t, float* c, float* s) {
+    float t4 = t * 4.0f;
+    float q = std::floor(t4 + 0.5f);
+    float r = t4 - q;
+    float x = r * (float)(M_PI / 2.0);
+    float x2 = x * x;
+    float ps = (float)(1.0 / 362880.0);
+    ps = ps * x2 + (float)(-1.0 / 5040.0);
+    ps = ps * x2 + (float)(1.0 / 120.0);
+    ps = ps * x2 + (float)(-1.0 / 6.0);
+    float sn = x + (x * x2) * ps;
+    float pc = (float)(-1.0 / 3628800.0);
+    pc = pc * x2 + (float)(1.0 / 40320.0);
+    pc = pc * x2 + (float)(-1.0 / 720.0);
+    pc = pc * x2 + (float)(1.0 / 24.0);
+    pc = pc * x2 + -0.5f;
+    float cs = 1.0f + x2 * pc;
+    int qi = ((int)q) & 3;
+    switch (qi) {
+        case 0: *c = cs; *s = sn; break;
+        case 1: *c = -sn; *s = cs; break;
+        case 2: *c = -cs; *s = -sn; break;
+        default: *c = sn; *s = -cs; break;
+    }
+}
+
+// natural log via the atanh series of (m-1)/(m+1), m in [sqrt(1/2), sqrt(2)).
+inline float logf_nf(float v) {
+    uint32_t b = fbits(v);
+    int e = (int)((b >> 23) & 0xffu) - 127;
+    float m = bitsf((b & 0x007fffffu) | 0x3f800000u);
+    if (m > 1.41421354f) { m = m * 0.5f; e += 1; }
+    float s = (m - 1.0f) / (m + 1.0f);
+    float s2 = s * s;
+    float p = (float)(1.0 / 11.0);
+    p = p * s2 + (float)(1.0 / 9.0);
+    p = p * s2 + (float)(1.0 / 7.0);
+    p = p * s2 + (float)(1.0 / 5.0);
+    p = p * s2 + (float)(1.0 / 3.0);
+    float two_s = s + s;
+    float lm = two_s + two_s * (s2 * p);
+    return (float)e * (float)M_LN2 + lm;
+}
+
+// exp via Cody-Waite reduction by ln2 and a degree-8 Taylor polynomial.
+inline float expf_nf(float x) {
+    float kf = std::floor(x * (float)(1.0 / M_LN2) + 0.5f);
+    float r = (x - kf * 0.693145751953125f) - kf * 1.428606765330187e-06f;
+    float p = (float)(1.0 / 40320.0);
+    p = p * r + (float)(1.0 / 5040.0);
+    p = p * r + (float)(1.0 / 720.0);
+    p = p * r + (float)(1.0 / 120.0);
+    p = p * r + (float)(1.0 / 24.0);
+    p = p * r + (float)(1.0 / 6.0);
+    p = p * r + 0.5f;
+    p = p * r + 1.0f;
+    p = p * r + 1.0f;
+    int k = (int)kf;
+    if (k < -126) k = -126;
+    if (k > 127) k = 127;
+    return p * bitsf((uint32_t)(k + 127) << 23);
+}
+
+// ---------------------------------------------------------------------------
+// Derived stream constants (computed identically by the product's host code).
+// ---------------------------------------------------------------------------
+struct Stream {
+    float L[3];
+    uint32_t key[2];
+    int orient, len_mode, rad_mode;
+    float kappa, E2;
+    bool rot;
+    float m[9];
+    float l, a, sigma, lmin, lmax, rmin, rmax;
+    // density
+    const float* mesh;
+    int n[3];
+    float dflt;
+};
+
+Stream make_stream(const nf_params* p, const float* mesh, int nx, int ny, int nz) {
+    Stream S;
+    for (int d = 0; d < 3; ++d) S.L[d] = p->box[d];
+    S.key[0] = (uint32_t)(p->seed & 0xffffffffu);
+    S.key[1] = (uint32_t)(p->seed >> 32);
+    S.orient = p->orient_mode;
+    S.len_mode = p->len_mode;
+    S.rad_mode = p->rad_mode;
+    S.kappa = p->vmf_kappa;
+    S.E2 = (S.orient == NF_ORIENT_VMF) ? expf_nf(-2.0f * p->vmf_kappa) : 0.0f;
+    S.rot = (p->pref_ort[0] != 0.0f) || (p->pref_ort[1] != 0.0f);
+    float cM, sM, cX, sX;
+    sincos_turns((float)((double)p->pref_ort[0] / (2.0 * M_PI)), &cM, &sM);
+    sincos_turns((float)((double)(-p->pref_ort[1]) / (2.0 * M_PI)), &cX, &sX);
+    // inc_rotation, inc/cuda_CNTgenerate.h:289-295 (Mu = phi, Xi = -theta)
+    S.m[0] = cM * cX;  S.m[1] = sM;  S.m[2] = -sX * cM;
+    S.m[3] = -sM * cX; S.m[4] = cM;  S.m[5] = sX * sM;
+    S.m[6] = sX;       S.m[7] = 0.0f; S.m[8] = cX;
+    S.l = p->l; S.a = p->a;
+    S.sigma = p->len_sigma_ln; S.lmin = p->len_min; S.lmax = p->len_max;
+    S.rmin = p->rad_min; S.rmax = p->rad_max;
+    S.mesh = mesh;
+    S.n[0] = nx; S.n[1] = ny; S.n[2] = nz;
+    S.dflt = p->density_default;
+    return S;
+}
+
+inline float lerpf(float a, float b, float f) { return a + (b - a) * f; }
+
+float density(const Stream& S, float x, float y, float z) {
+    if (!S.mesh) return S.dflt;
+    float pos[3] = {x, y, z};
+    int i0[3], i1[3];
+    float f[3];
+    for (int d = 0; d < 3; ++d) {
+        float g = (pos[d] / S.L[d]) * (float)S.n[d] - 0.5f;
+        float fl = std::floor(g);
+        f[d] = g - fl;
+        int i = (int)fl;
+        i %= S.n[d];
+        if (i < 0) i += S.n[d];
+        i0[d] = i;
+        i1[d] = (i + 1 == S.n[d]) ? 0 : i + 1;
+    }
+    auto v = [&](int i, int j, int k) { return S.mesh[((size_t)i * S.n[1] + j) * S.n[2] + k]; };
+    float c00 = lerpf(v(i0[0], i0[1], i0[2]), v(i1[0], i0[1], i0[2]), f[0]);
+    float c10 = lerpf(v(i0[0], i1[1], i0[2]), v(i1[0], i1[1], i0[2]), f[0]);
+    float c01 = lerpf(v(i0[0], i0[1], i1[2]), v(i1[0], i0[1], i1[2]), f[0]);
+    float c11 = lerpf(v(i0[0], i1[1], i1[2]), v(i1[0], i1[1], i1[2]), f[0]);
+    float c0 = lerpf(c00, c10, f[1]);
+    float c1 = lerpf(c01, c11, f[1]);
+    return lerpf(c0, c1, f[2]);
+}
+
+// Candidate k: 10 floats x y z cx cy cz l a u rho.
+void candidate(const Stream& S, uint64_t k, float* o) {
+    uint32_t ctr[4] = {(uint32_t)k, (uint32_t)(k >> 32), 0u, 0u};
+    uint32_t A[4], B[4];
+    philox(ctr, S.key, A);
+    ctr[2] = 1u;
+    philox(ctr, S.key, B);
+    float x = uni(A[0]) * S.L[0];
+    float y = uni(A[1]) * S.L[1];
+    float z = uni(A[2]) * S.L[2];
+    float u = uni(A[3]);
+    float cz;
+    if (S.orient == NF_ORIENT_VMF) {
+        float w = 1.0f - uni(B[0]);
+        float v = w + (1.0f - w) * S.E2;
+        cz = 1.0f + logf_nf(v) / S.kappa;
+        if (cz < -1.0f) cz = -1.0f;
+        if (cz > 1.0f) cz = 1.0f;
+    } else {
+        cz = uni(B[0]) * 2.0f - 1.0f;
+    }
+    float cp, sp;
+    sincos_turns(uni(B[1]), &cp, &sp);
+    float sr = 1.0f - cz * cz;
+    float s = std::sqrt(sr > 0.0f ? sr : 0.0f);
+    float cx = s * cp, cy = s * sp;
+    if (S.rot) {
+        float rx = (S.m[0] * cx + S.m[1] * cy) + S.m[2] * cz;
+        float ry = (S.m[3] * cx + S.m[4] * cy) + S.m[5] * cz;
+        float rz = (S.m[6] * cx + S.m[7] * cy) + S.m[8] * cz;
+        cx = rx; cy = ry; cz = rz;
+    }
+    float len = S.l;
+    if (S.len_mode == NF_SIZE_LOGNORMAL) {
+        float cb, sb;
+        sincos_turns(uni(B[3]), &cb, &sb);
+        float g = std::sqrt(-2.0f * logf_nf(1.0f - uni(B[2]))) * cb;
+        len = S.l * expf_nf(S.sigma * g);
+        if (len < S.lmin) len = S.lmin;
+        if (len > S.lmax) len = S.lmax;
+    }
+    float rad = S.a;
+    if (S.rad_mode == NF_SIZE_UNIFORM) {
+        uint32_t C[4];
+        ctr[2] = 2u;
+        philox(ctr, S.key, C);
+        rad = S.rmin + (S.rmax - S.rmin) * uni(C[0]);
+    }
+    o[0] = x; o[1] = y; o[2] = z; o[3] = cx; o[4] = cy; o[5] = cz;
+    o[6] = len; o[7] = rad; o[8] = u; o[9] = density(S, x, y, z);
+}
+
+// ---------------------------------------------------------------------------
+// The reference routine, templated on the arithmetic type.
+// A in "registers", B in "shared memory" shifted by its periodic image.
+// ---------------------------------------------------------------------------
+template <typename T>
+struct RodT { T x, y, z, cx, cy, cz, l, a; };
+
+template <typename T>
+RodT<T> rodT(const nfo_rod& r) {
+    return RodT<T>{(T)r.x, (T)r.y, (T)r.z, (T)r.cx, (T)r.cy, (T)r.cz, (T)r.l, (T)r.a};
+}
+
+template <typename T>
+inline T tabs(T v) { return v < T(0) ? -v : v; }
+
+// Returns d; writes clamped t0,t1 and Dtt (perpendicular distance, unclamped t0,t1).
+template <typename T>
+T ref_distance(const RodT<T>& A, const RodT<T>& B0, T sx, T sy, T sz, T eps, bool typo,
+               T* t0o, T* t1o, T Dtt[3]) {
+    const T Bx = B0.x + sx, By = B0.y + sy, Bz = B0.z + sz;  // tarnsCNT
+    const T bx = Bx - A.x, by = By - A.y, bz = Bz - A.z;      // r2-r1
+    T d = A.cx * B0.cx + A.cy * B0.cy + A.cz * B0.cz;           // c1*c2
+    T t0, t1;
+    if (T(1) - tabs(d) > eps) {
+        T ax = d * B0.cx - A.cx, ay = d * B0.cy - A.cy, az = d * B0.cz - A.cz;
+        t0 = ax * bx + ay * by + az * bz;
+        ax = B0.cx - d * A.cx; ay = B0.cy - d * A.cy; az = B0.cz - d * A.cz;
+        t1 = ax * bx + ay * by + az * bz;
+        t0 = t0 / (d * d - T(1));
+        t1 = t1 / (d * d - T(1));
+    } else {
+        t0 = std::copysign(A.l / T(2), bx * A.cx + by * A.cy + bz * A.cz);
+        if (typo)
+            t1 = T(-1) * (bx * B0.cx + bx * B0.cy + bx * B0.cz) + d * t0;
+        else
+            t1 = T(-1) * (bx * B0.cx + by * B0.cy + bz * B0.cz) + d * t0;
+    }
+    const T u0 = t0, u1 = t1;
+    bool f1 = tabs(t0) <= (A.l / T(2) + A.a + eps);
+    bool f2 = tabs(t1) <= (B0.l / T(2) + B0.a + eps);
+    if (!(f1 && f2)) {
+        bool f3 = (tabs(t0) - A.l / T(2)) < (tabs(t1) - B0.l / T(2));
+        if (f3) {
+            t1 = std::copysign(B0.l / T(2), t1);
+            t0 = T(1) * (bx * A.cx + by * A.cy + bz * A.cz) + d * t1;
+            T len = A.l / T(2);
+            if (tabs(t0) > len) t0 = std::copysign(len, t0);
+        } else {
+            t0 = std::copysign(A.l / T(2), t0);
+            t1 = T(-1) * (bx * B0.cx + by * B0.cy + bz * B0.cz) + d * t0;
+            T len = B0.l / T(2);
+            if (tabs(t1) > len) t1 = std::copysign(len, t1);
+        }
+    }
+    T px = ((A.x + t0 * A.cx) - Bx) - t1 * B0.cx;
+    T py = ((A.y + t0 * A.cy) - By) - t1 * B0.cy;
+    T pz = ((A.z + t0 * A.cz) - Bz) - t1 * B0.cz;
+    T dist = std::sqrt(px * px + py * py + pz * pz);
+    T qx = ((A.x + u0 * A.cx) - Bx) - u1 * B0.cx;
+    T qy = ((A.y + u0 * A.cy) - By) - u1 * B0.cy;
+    T qz = ((A.z + u0 * A.cz) - Bz) - u1 * B0.cz;
+    Dtt[0] = std::sqrt(qx * qx + qy * qy + qz * qz);
+    Dtt[1] = u0;
+    Dtt[2] = u1;
+    *t0o = t0;
+    *t1o = t1;
+    return dist;
+}
+
+// threshold (a_B + a_A) * scf + sep + eps, left-to-right as in the reference.
+template <typename T>
+inline T thresh(T aA, T aB, T scf, T sep, T eps) { return (aB + aA) * scf + sep + eps; }
+
+// ---------------------------------------------------------------------------
+// Grid of cells with a 27-offset stencil and periodic images.
+// ---------------------------------------------------------------------------
+struct Grid {
+    int n[3];
+    float L[3];
+    int periodic;
+    double invE[3];
+    void init(const float Lb[3], int per, double reach, double min_edge) {
+        periodic = per;
+        double e = std::max(reach * 1.0001, min_edge);
+        for (int d = 0; d < 3; ++d) {
+            L[d] = Lb[d];
+            int c = (int)std::floor((double)Lb[d] / e);
+            n[d] = c < 1 ? 1 : c;
+            invE[d] = (double)n[d] / (double)Lb[d];
+        }
+    }
+    int coord(int d, float x) const {
+        int c = (int)std::floor((double)x * invE[d]);
+        if (c < 0) c = 0;
+        if (c >= n[d]) c = n[d] - 1;
+        return c;
+    }
+    int ncell() const { return n[0] * n[1] * n[2]; }
+};
+
+struct Reach {  // per-run parameters of one pair kind
+    double eps, scf, sep;
+    int typo;
+    int kind;
+};
+
+// d >= |b| - hA|cA| - hB|cB| (both points lie within h|c| of the centres), so
+// pairs beyond this bound cannot satisfy the test; FP64 slack 1e-9 relative.
+inline bool sphere_far(const RodT<double>& A, const RodT<double>& B, double sx, double sy,
+                       double sz, double thr, double eps) {
+    double bx = (B.x + sx) - A.x, by = (B.y + sy) - A.y, bz = (B.z + sz) - A.z;
+    double nA = std::sqrt(A.cx * A.cx + A.cy * A.cy + A.cz * A.cz);
+    double nB = std::sqrt(B.cx * B.cx + B.cy * B.cy + B.cz * B.cz);
+    double R = ((A.l / 2 + A.a + eps) * nA + (B.l / 2 + B.a + eps) * nB + thr) * (1.0 + 1e-9) + 1e-12;
+    return bx * bx + by * by + bz * bz > R * R;
+}
+
+// Hard-core test of candidate A against accepted B shifted by image.
+inline bool hc_hit(const RodT<double>& A, const RodT<double>& B, double sx, double sy, double sz,
+                   const nf_params* p, uint64_t* evals) {
+    double eps = (double)p->tol, scf = (double)p->sc_frac, sep = (double)p->sep;
+    if (!(A.l > 0)) return false;  // probe.l<=0
+    double thr = thresh<double>(A.a, B.a, scf, sep, eps);
+    if (sphere_far(A, B, sx, sy, sz, thr, eps)) return false;
+    if (evals) ++*evals;
+    double t0, t1, Dtt[3];
+    double d = ref_distance<double>(A, B, sx, sy, sz, eps, p->ref_parallel_typo != 0, &t0, &t1, Dtt);
+    return d < thr;
+}
+
+double gen_reach(const nf_params* p, double lmax, double amax) {
+    double eps = p->tol;
+    double h = lmax / 2 + amax + eps;
+    return 2 * h + ((2 * amax) * p->sc_frac + p->sep + eps);
+}
+
+void size_bounds(const nf_params* p, double* lmax, double* amax) {
+    *lmax = (p->len_mode == NF_SIZE_LOGNORMAL) ? (double)p->len_max : (double)p->l;
+    *amax = (p->rad_mode == NF_SIZE_UNIFORM) ? (double)std::max(p->rad_min, p->rad_max) : (double)p->a;
+}
+
+int64_t target_count(const nf_params* p) {
+    if (p->n_target > 0) return p->n_target;
+    double V = (double)p->box[0] * p->box[1] * p->box[2];
+    double El = p->l, Ea2 = (double)p->a * p->a;
+    if (p->len_mode == NF_SIZE_LOGNORMAL) {
+        // E[l] of the clipped lognormal by quadrature over the standard normal.
+        double s = 0, w = 0;
+        for (int i = -6000; i <= 6000; ++i) {
+            double z = i * 1e-3, g = std::exp(-0.5 * z * z);
+            double v = p->l * std::exp(p->len_sigma_ln * z);
+            v = std::min(std::max(v, (double)p->len_min), (double)p->len_max);
+            s += g * v; w += g;
+        }
+        El = s / w;
+    }
+    if (p->rad_mode == NF_SIZE_UNIFORM) {
+        double lo = p->rad_min, hi = p->rad_max;
+        Ea2 = (hi * hi + hi * lo + lo * lo) / 3.0;
+    }
+    double vinc = M_PI * Ea2 * El;
+    return (int64_t)std::ceil((double)p->vf * V / vinc);
+}
+
+struct CellList {
+    std::vector<std::vector<int64_t>> cells;
+};
+
+template <typename F>
+void for_stencil(const Grid& g, const int c[3], F&& f) {
+    for (int oz = -1; oz <= 1; ++oz)
+        for (int oy = -1; oy <= 1; ++oy)
+            for (int ox = -1; ox <= 1; ++ox) {
+                int o[3] = {ox, oy, oz}, q[3], img[3];
+                bool ok = true;
+                for (int d = 0; d < 3; ++d) {
+                    int v = c[d] + o[d];
+                    img[d] = 0;
+                    if (v < 0) {
+                        if (!(g.periodic & (1 << d))) { ok = false; break; }
+                        v += g.n[d]; img[d] = -1;
+                    } else if (v >= g.n[d]) {
+                        if (!(g.periodic & (1 << d))) { ok = false; break; }
+                        v -= g.n[d]; img[d] = 1;
+                    }
+                    q[d] = v;
+                }
+                if (!ok) continue;
+                int cell = q[0] + g.n[0] * (q[1] + g.n[1] * q[2]);
+                f(cell, img);
+            }
+}
+
+template <typename F>
+void for_images(int periodic, F&& f) {
+    for (int iz = -1; iz <= 1; ++iz)
+        for (int iy = -1; iy <= 1; ++iy)
+            for (int ix = -1; ix <= 1; ++ix) {
+                int img[3] = {ix, iy, iz};
+                bool ok = true;
+                for (int d = 0; d < 3; ++d)
+                    if (img[d] != 0 && !(periodic & (1 << d))) ok = false;
+                if (ok) f(img);
+            }
+}
+
+int nthreads_of(int n) {
+#ifdef _OPENMP
+    return n > 0 ? n : omp_get_max_threads();
+#else
+    (void)n;
+    return 1;
+#endif
+}
+
+// Union-find with path halving.
+struct DSU {
+    std::vector<int64_t> p;
+    explicit DSU(int64_t n) : p(n) { std::iota(p.begin(), p.end(), 0); }
+    int64_t find(int64_t x) {
+        while (p[x] != x) { p[x] = p[p[x]]; x = p[x]; }
+        return x;
+    }
+    void unite(int64_t a, int64_t b) {
+        a = find(a); b = find(b);
+        if (a == b) return;
+        if (a < b) std::swap(a, b);
+        p[a] = b;
+    }
+};
+
+}  // namespace
+
+// ===========================================================================
+extern "C" {
+
+void nfo_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]) {
+    philox(ctr, key, out);
+}
+void nfo_sincos_turns(float t, float* c, float* s) { sincos_turns(t, c, s); }
+float nfo_logf(float v) { return logf_nf(v); }
+float nfo_expf(float x) { return expf_nf(x); }
+
+int nfo_pair_eval(int use_double, int kind, const nfo_rod* A, const nfo_rod* B,
+                  const double shift[3], double eps, double scf, double thr_sep, int typo,
+                  double out[6]) {
+    if (use_double) {
+        RodT<double> a = rodT<double>(*A), b = rodT<double>(*B);
+        if (kind == 0 && !(a.l > 0)) { for (int i = 0; i < 6; ++i) out[i] = 0; return 0; }
+        double t0, t1, Dtt[3];
+        double d = ref_distance<double>(a, b, shift[0], shift[1], shift[2], eps,
+                                        kind == 0 && typo, &t0, &t1, Dtt);
+        out[0] = d; out[1] = t0; out[2] = t1; out[3] = Dtt[0]; out[4] = Dtt[1]; out[5] = Dtt[2];
+        return d < thresh<double>(a.a, b.a, scf, thr_sep, eps);
+    } else {
+        RodT<float> a = rodT<float>(*A), b = rodT<float>(*B);
+        if (kind == 0 && !(a.l > 0)) { for (int i = 0; i < 6; ++i) out[i] = 0; return 0; }
+        float t0, t1, Dtt[3];
+        float d = ref_distance<float>(a, b, (float)shift[0], (float)shift[1], (float)shift[2],
+                                      (float)eps, kind == 0 && typo, &t0, &t1, Dtt);
+        out[0] = d; out[1] = t0; out[2] = t1; out[3] = Dtt[0]; out[4] = Dtt[1]; out[5] = Dtt[2];
+        return d < thresh<float>(a.a, b.a, (float)scf, (float)thr_sep, (float)eps);
+    }
+}
+
+int nfo_screen_eval(const nfo_rod* A, const double vr[3], const double vc[3], double vl,
+                    double va, const double shift[3], double eps) {
+    RodT<double> a = rodT<double>(*A);
+    RodT<double> v{vr[0], vr[1], vr[2], vc[0], vc[1], vc[2], vl, va};
+    double t0, t1, Dtt[3];
+    double d = ref_distance<double>(a, v, shift[0], shift[1], shift[2], eps, false, &t0, &t1, Dtt);
+    // if_intersects (separation 0, soft_frac 1) and body_intersect on the virtual rod.
+    bool hit = d < thresh<double>(a.a, v.a, 1.0, 0.0, eps);
+    bool body = (v.l / 2.0 - tabs(Dtt[2])) > (v.a + eps);
+    return hit && body;
+}
+
+double nfo_contact_area(const nfo_rod* A, const nfo_rod* B, const double shift[3],
+                        double Dtt_x, double t1u, double t2u, double rlim) {
+    // surf_to_cylinder_capped in FP64 (A = probe, B = shifted partner).
+    const double PIv = 3.141593;  // PI of inc/vectorMath.h:7
+    double l1 = A->l, l2 = B->l, a1 = A->a, a2 = B->a;
+    double c1[3] = {A->cx, A->cy, A->cz}, c2[3] = {B->cx, B->cy, B->cz};
+    double r1[3] = {A->x, A->y, A->z};
+    double r2[3] = {B->x + shift[0], B->y + shift[1], B->z + shift[2]};
+    auto dot = [](const double* u, const double* w) { return u[0] * w[0] + u[1] * w[1] + u[2] * w[2]; };
+    double sg = std::copysign(1.0, dot(c1, c2));
+    double c2p[3] = {c2[0] * sg, c2[1] * sg, c2[2] * sg};
+    double dr1 = 0.0, dr2 = 0.0;
+    double h1 = std::max(Dtt_x - a2 - rlim, 0.0);
+    double h2 = std::max(Dtt_x - a1 - rlim, 0.0);
+    if (h1 <= a1) dr1 = a1 * std::sqrt(1 - (h1 / a1) * (h1 / a1));
+    if (h2 <= a2) dr2 = a2 * std::sqrt(1 - (h2 / a2) * (h2 / a2));
+    double dr = std::min(dr1, dr2);
+    double S = PIv * dr * dr;
+    double t1 = t1u, t2 = t2u;
+    double d = dot(c1, c2p);
+    double sng = std::sqrt(std::max(1 - d * d, 0.0));
+    if (tabs(t1) < (l1 / 2 - a1) && tabs(t2) < (l2 / 2 - a2)) {
+        double ax1[3] = {c1[0] + c2p[0], c1[1] + c2p[1], c1[2] + c2p[2]};
+        double n1 = std::sqrt(dot(ax1, ax1));
+        for (int i = 0; i < 3; ++i) ax1[i] *= 1.0 / n1;
+        double csg = std::sqrt(std::max(1 - sng * sng, 0.0));
+        double sngh = std::sqrt((1 - csg) / 2.0);
+        double t2p = std::copysign(t2, dot(c1, c2));
+        double dt0p = (sngh > 1e-6 ? dr2 / sngh : l1 / 2);
+        double dt0m = dt0p;
+        double q[3];
+        for (int i = 0; i < 3; ++i) q[i] = r1[i] + c1[i] * (l1 / 2 - t1);
+        double dt1p = dot(q, ax1);
+        for (int i = 0; i < 3; ++i) q[i] = r1[i] + c1[i] * (-l1 / 2 - t1);
+        double dt1m = tabs(dot(q, ax1));
+        for (int i = 0; i < 3; ++i) q[i] = r2[i] + c2p[i] * (l2 / 2 - t2p);
+        double dt2p = dot(q, ax1);
+        for (int i = 0; i < 3; ++i) q[i] = r2[i] + c2p[i] * (-l2 / 2 - t2p);
+        double dt2m = tabs(dot(q, ax1));
+        double Ap = std::max(dr, std::min(dt0p, std::min(dt1p, dt2p)));
+        double Am = std::max(dr, std::min(dt0m, std::min(dt1m, dt2m)));
+        S = std::max(S, 0.5 * PIv * dr * (Ap + Am));
+    }
+    if ((sng <= (std::max(a1, a2) / std::min(l1, l2))) && (tabs(t1) <= l1 / 2 + a1 || tabs(t2) <= l2 / 2 + a2)) {
+        double b[3] = {r2[0] - r1[0], r2[1] - r1[1], r2[2] - r1[2]};
+        double cb1 = dot(c1, b), cb2 = dot(c2, b);
+        double t1a = std::copysign(l1 / 2, cb1), t1b = -1 * std::copysign(l1 / 2, cb1);
+        double t2a = std::copysign(l2 / 2, cb2), t2b = -1 * std::copysign(l2 / 2, cb2);
+        double q[3];
+        for (int i = 0; i < 3; ++i) q[i] = r1[i] + c1[i] * t1a;
+        double t1ac = dot(q, c1);
+        for (int i = 0; i < 3; ++i) q[i] = r1[i] + c1[i] * t1b;
+        double t1bc = dot(q, c1);
+        for (int i = 0; i < 3; ++i) q[i] = b[i] + r1[i] + c2[i] * t2a;
+        double t2ac = dot(q, c1);
+        for (int i = 0; i < 3; ++i) q[i] = b[i] + r1[i] + c2[i] * t2b;
+        double t2bc = dot(q, c1);
+        double p1c = cb1 > 0 ? std::min(t1ac, t2ac) : std::max(t1ac, t2ac);
+        double p2c = cb1 > 0 ? std::max(t1bc, t2bc) : std::min(t1bc, t2bc);
+        S = std::max(S, tabs(p2c - p1c) * 2 * dr);
+    }
+    return S;
+}
+
+int nfo_candidates(const nf_params* p, const float* mesh, int nx, int ny, int nz, uint64_t k0,
+                   uint64_t n, float* out) {
+    if (!p || !out) return -1;
+    Stream S = make_stream(p, mesh, nx, ny, nz);
+    for (uint64_t i = 0; i < n; ++i) candidate(S, k0 + i, out + 10 * i);
+    return 0;
+}
+
+int64_t nfo_generate(const nf_params* p, const float* mesh, int nx, int ny, int nz,
+                     int nthreads, int64_t batch, int brute_force, int64_t cap, nfo_rod* rods,
+                     uint64_t* stream_index, uint64_t stats[3]) {
+    if (!p || !rods) return -1;
+    const int nt = nthreads_of(nthreads);
+    Stream S = make_stream(p, mesh, nx, ny, nz);
+    const int64_t target = target_count(p);
+    double lmax, amax;
+    size_bounds(p, &lmax, &amax);
+    Grid g;
+    g.init(p->box, p->gen_periodic, gen_reach(p, lmax, amax), p->cell_edge);
+    std::vector<std::vector<int64_t>> cells(g.ncell());
+    std::vector<RodT<double>> accD;
+    accD.reserve((size_t)std::max<int64_t>(target, 0));
+    int64_t acc = 0;
+    uint64_t k = 0, drawn = 0, dens_acc = 0, evals = 0;
+    const uint64_t budget = p->n_candidates;
+    if (batch < 1) batch = 1;
+    std::vector<float> cand;
+    std::vector<char> keep;
+    std::vector<uint64_t> ev_thread(nt, 0);
+    auto cell_of = [&](const RodT<double>& r, int c[3]) {
+        c[0] = g.coord(0, (float)r.x); c[1] = g.coord(1, (float)r.y); c[2] = g.coord(2, (float)r.z);
+    };
+    auto test_vs = [&](const RodT<double>& A, const std::vector<std::vector<int64_t>>& cl,
+                       const std::vector<RodT<double>>& pool, uint64_t* ev) -> bool {
+        if (brute_force) {
+            bool hit = false;
+            for (size_t j = 0; j < pool.size() && !hit; ++j)
+                for_images(g.periodic, [&](const int img[3]) {
+                    if (hit) return;
+                    if (hc_hit(A, pool[j], img[0] * (double)g.L[0], img[1] * (double)g.L[1],
+                               img[2] * (double)g.L[2], p, ev))
+                        hit = true;
+                });
+            return hit;
+        }
+        int c[3];
+        cell_of(A, c);
+        bool hit = false;
+        for_stencil(g, c, [&](int cell, const int img[3]) {
+            if (hit) return;
+            for (int64_t j : cl[cell]) {
+                if (hc_hit(A, pool[j], img[0] * (double)g.L[0], img[1] * (double)g.L[1],
+                           img[2] * (double)g.L[2], p, ev)) { hit = true; return; }
+            }
+        });
+        return hit;
+    };
+    while (k < budget && acc < target) {
+        uint64_t b = std::min<uint64_t>((uint64_t)batch, budget - k);
+        cand.assign(10 * b, 0.0f);
+        keep.assign(b, 0);
+        #pragma omp parallel for num_threads(nt) schedule(dynamic, 64)
+        for (int64_t i = 0; i < (int64_t)b; ++i) {
+            float* o = &cand[10 * i];
+            candidate(S, k + i, o);
+            if (!(o[8] < o[9])) continue;  // von Neumann: u < rho(x)
+            keep[i] = 1;
+            nfo_rod r{o[0], o[1], o[2], o[3], o[4], o[5], o[6], o[7]};
+            RodT<double> A = rodT<double>(r);
+#ifdef _OPENMP
+            int tid = omp_get_thread_num();
+#else
+            int tid = 0;
+#endif
+            if (test_vs(A, cells, accD, &ev_thread[tid])) keep[i] = 2;  // hit an accepted rod
+        }
+        // In-batch conflicts, resolved in stream order.
+        std::vector<std::vector<int64_t>> newcells(brute_force ? 0 : g.ncell());
+        std::vector<RodT<double>> newD;
+        std::vector<int64_t> touched;
+        uint64_t last = k + b;
+        for (uint64_t i = 0; i < b; ++i) {
+            if (keep[i] == 0) continue;
+            ++dens_acc;
+            if (keep[i] == 2) continue;
+            float* o = &cand[10 * i];
+            nfo_rod r{o[0], o[1], o[2], o[3], o[4], o[5], o[6], o[7]};
+            RodT<double> A = rodT<double>(r);
+            if (test_vs(A, newcells, newD, &evals)) continue;
+            if (acc >= cap) return -2;
+            rods[acc] = r;
+            if (stream_index) stream_index[acc] = k + i;
+            accD.push_back(A);
+            newD.push_back(A);
+            if (!brute_force) {
+                int c[3];
+                cell_of(A, c);
+                int cell = c[0] + g.n[0] * (c[1] + g.n[1] * c[2]);
+                cells[cell].push_back((int64_t)accD.size() - 1);
+                newcells[cell].push_back((int64_t)newD.size() - 1);
+            }
+            ++acc;
+            if (acc == target) { last = k + i + 1; break; }
+        }
+        drawn = last;
+        k += b;
+    }
+    if (acc < target) drawn = std::min<uint64_t>(k, budget);
+    for (uint64_t e : ev_thread) evals += e;
+    if (stats) { stats[0] = drawn; stats[1] = dens_acc; stats[2] = evals; }
+    return acc;
+}
+
+int64_t nfo_contacts(const nf_params* p, const nfo_rod* rods, int64_t n, int nthreads,
+                     int brute_force, int64_t cap, uint32_t* I, uint32_t* J, double* tI,
+                     double* tJ, double* D, double* G, double* S, int8_t* img, int64_t counts[4]) {
+    if (!p || (!rods && n > 0)) return -1;
+    const int nt = nthreads_of(nthreads);
+    const double eps = 1e-6f;  // DEV_PRECISION, inc/definitions.h:5
+    const double cut = p->stat_dist_lim;
+    const int per = p->gen_periodic & ~p->field_dir;  // peri_dir = 7 - dir
+    double lmax = 0, amax = 0;
+    for (int64_t i = 0; i < n; ++i) { lmax = std::max(lmax, (double)rods[i].l); amax = std::max(amax, (double)rods[i].a); }
+    Grid g;
+    double reach = 2 * (lmax / 2 + amax + eps) + (2 * amax + cut + eps);
+    g.init(p->box, per, reach, p->cell_edge);
+    std::vector<RodT<double>> R(n);
+    std::vector<std::vector<int64_t>> cells(g.ncell());
+    for (int64_t i = 0; i < n; ++i) {
+        R[i] = rodT<double>(rods[i]);
+        int c = g.coord(0, rods[i].x) + g.n[0] * (g.coord(1, rods[i].y) + g.n[1] * g.coord(2, rods[i].z));
+        cells[c].push_back(i);
+    }
+    struct Ct { uint32_t i, j; int8_t im[3]; double t0, t1, d, Dx, u0, u1; };
+    std::vector<std::vector<Ct>> per_t(nt);
+    #pragma omp parallel for num_threads(nt) schedule(dynamic, 16)
+    for (int64_t i = 0; i < n; ++i) {
+#ifdef _OPENMP
+        auto& out = per_t[omp_get_thread_num()];
+#else
+        auto& out = per_t[0];
+#endif
+        const RodT<double>& A = R[i];
+        auto test = [&](int64_t j, const int im[3]) {
+            if (j <= i) return;
+            const RodT<double>& B = R[j];
+            double sx = im[0] * (double)g.L[0], sy = im[1] * (double)g.L[1], sz = im[2] * (double)g.L[2];
+            double thr = thresh<double>(A.a, B.a, 1.0, cut, eps);
+            if (sphere_far(A, B, sx, sy, sz, thr, eps)) return;
+            double t0, t1, Dtt[3];
+            double d = ref_distance<double>(A, B, sx, sy, sz, eps, false, &t0, &t1, Dtt);
+            if (d < thr) {
+                Ct c{(uint32_t)i, (uint32_t)j, {(int8_t)im[0], (int8_t)im[1], (int8_t)im[2]}, t0, t1, d, Dtt[0], Dtt[1], Dtt[2]};
+                out.push_back(c);
+            }
+        };
+        if (brute_force) {
+            for (int64_t j = i + 1; j < n; ++j) for_images(per, [&](const int im[3]) { test(j, im); });
+        } else {
+            int c[3] = {g.coord(0, rods[i].x), g.coord(1, rods[i].y), g.coord(2, rods[i].z)};
+            for_stencil(g, c, [&](int cell, const int im[3]) { for (int64_t j : cells[cell]) test(j, im); });
+        }
+    }
+    std::vector<Ct> all;
+    for (auto& v : per_t) all.insert(all.end(), v.begin(), v.end());
+    std::sort(all.begin(), all.end(), [](const Ct& a, const Ct& b) {
+        if (a.i != b.i) return a.i < b.i;
+        if (a.j != b.j) return a.j < b.j;
+        for (int d = 2; d >= 0; --d) if (a.im[d] != b.im[d]) return a.im[d] < b.im[d];
+        return false;
+    });
+    // Screening by virtual inclusions (inc/conductKernels.h:289-361 and the
+    // VIRTUAL_CHECK mode of src/core_cell_interaction_kernel.cu:141-146).
+    std::vector<char> screened(all.size(), 0);
+    if (p->screening) {
+        double vreach = 2 * (lmax / 2 + amax + eps) + (2 * amax + eps);  // V shorter than a rod
+        Grid gs;
+        gs.init(p->box, per, vreach, p->cell_edge);
+        std::vector<std::vector<int64_t>> rc(gs.ncell());
+        for (int64_t i = 0; i < n; ++i)
+            rc[gs.coord(0, rods[i].x) + gs.n[0] * (gs.coord(1, rods[i].y) + gs.n[1] * gs.coord(2, rods[i].z))].push_back(i);
+        #pragma omp parallel for num_threads(nt) schedule(dynamic, 16)
+        for (int64_t q = 0; q < (int64_t)all.size(); ++q) {
+            const Ct& c = all[q];
+            const RodT<double>& A = R[c.i];
+            const RodT<double>& B = R[c.j];
+            double sh[3] = {c.im[0] * (double)g.L[0], c.im[1] * (double)g.L[1], c.im[2] * (double)g.L[2]};
+            double p0[3] = {A.x + c.t0 * A.cx, A.y + c.t0 * A.cy, A.z + c.t0 * A.cz};
+            double p1[3] = {(B.x + sh[0]) + c.t1 * B.cx, (B.y + sh[1]) + c.t1 * B.cy, (B.z + sh[2]) + c.t1 * B.cz};
+            double vr[3], vc[3];
+            for (int d = 0; d < 3; ++d) { vr[d] = (p0[d] + p1[d]) * 0.5; vc[d] = p1[d] - p0[d]; }
+            double vl = std::sqrt(vc[0] * vc[0] + vc[1] * vc[1] + vc[2] * vc[2]);
+            if (!(vl > 0)) continue;
+            for (int d = 0; d < 3; ++d) vc[d] = vc[d] * (1.0 / vl);
+            double va = std::min(A.a, B.a);
+            RodT<double> V{vr[0], vr[1], vr[2], vc[0], vc[1], vc[2], vl, va};
+            // Cell of V's centre, wrapped into the box on periodic axes.
+            int cc[3];
+            double vw[3];
+            for (int d = 0; d < 3; ++d) {
+                double x = vr[d];
+                if (per & (1 << d)) { x = std::fmod(x, (double)g.L[d]); if (x < 0) x += g.L[d]; }
+                vw[d] = x;
+                cc[d] = gs.coord(d, (float)x);
+            }
+            bool hit = false;
+            for_stencil(gs, cc, [&](int cell, const int im[3]) {
+                if (hit) return;
+                for (int64_t r : rc[cell]) {
+                    // real rod R[r] at image im relative to V's wrapped cell: the
+                    // virtual rod is moved by -(image) so the real rod stays in place.
+                    double sv[3];
+                    for (int d = 0; d < 3; ++d) sv[d] = (vw[d] - vr[d]) - im[d] * (double)gs.L[d];
+                    const RodT<double>& Rr = R[r];
+                    double thr = thresh<double>(Rr.a, V.a, 1.0, 0.0, eps);
+                    if (sphere_far(Rr, V, sv[0], sv[1], sv[2], thr, eps)) continue;
+                    double t0, t1, Dtt[3];
+                    double d = ref_distance<double>(Rr, V, sv[0], sv[1], sv[2], eps, false, &t0, &t1, Dtt);
+                    if (d < thr && (V.l / 2.0 - tabs(Dtt[2])) > (V.a + eps)) { hit = true; return; }
+                }
+            });
+            screened[q] = hit;
+        }
+    }
+    int64_t n_int = 0, n_scr = 0;
+    for (size_t q = 0; q < all.size(); ++q) (screened[q] ? n_scr : n_int)++;
+    // Electrode contacts: rods whose capsule comes within the cutoff of the
+    // planes x_f = 0 (source) and x_f = L_f (sink) of the field axis f.
+    std::vector<std::pair<uint32_t, double>> snk, src;  // (rod, D)
+    std::vector<double> snk_t, src_t;
+    int f = p->field_dir == 1 ? 0 : (p->field_dir == 2 ? 1 : (p->field_dir == 4 ? 2 : -1));
+    if (f >= 0) {
+        for (int64_t i = 0; i < n; ++i) {
+            const RodT<double>& A = R[i];
+            double cf = f == 0 ? A.cx : (f == 1 ? A.cy : A.cz);
+            double rf = f == 0 ? A.x : (f == 1 ? A.y : A.z);
+            double half = A.l / 2;
+            double tlo = cf > 0 ? -half : half;
+            double thi = -tlo;
+            double zlo = rf + tlo * cf, zhi = rf + thi * cf;
+            double Lf = g.L[f];
+            double dsnk = Lf - zhi;
+            if (dsnk - A.a < cut + eps) { snk.push_back({(uint32_t)i, dsnk}); snk_t.push_back(thi); }
+            if (zlo - A.a < cut + eps) { src.push_back({(uint32_t)i, zlo}); src_t.push_back(tlo); }
+        }
+    }
+    int64_t total = n_int + (int64_t)snk.size() + (int64_t)src.size();
+    if (counts) { counts[0] = n_int; counts[1] = n_scr; counts[2] = (int64_t)snk.size(); counts[3] = (int64_t)src.size(); }
+    if (total > cap || !I) return total;
+    const double G0 = p->G0, lam = p->lambda, dc = p->d_c;
+    auto gfun = [&](double gap) { double ge = gap > dc ? gap : dc; return G0 * std::exp(-(ge - dc) / lam); };
+    int64_t o = 0;
+    for (size_t q = 0; q < all.size(); ++q) {
+        if (screened[q]) continue;
+        const Ct& c = all[q];
+        I[o] = c.i; J[o] = c.j;
+        if (tI) tI[o] = c.t0;
+        if (tJ) tJ[o] = c.t1;
+        if (D) D[o] = c.d;
+        if (G) G[o] = gfun(c.d - R[c.i].a - R[c.j].a);
+        if (S) {
+            double sh[3] = {c.im[0] * (double)g.L[0], c.im[1] * (double)g.L[1], c.im[2] * (double)g.L[2]};
+            S[o] = nfo_contact_area(&rods[c.i], &rods[c.j], sh, c.Dx, c.u0, c.u1, cut);
+        }
+        if (img) for (int d = 0; d < 3; ++d) img[3 * o + d] = c.im[d];
+        ++o;
+    }
+    auto put_elec = [&](const std::vector<std::pair<uint32_t, double>>& v, const std::vector<double>& tv, uint32_t id) {
+        for (size_t q = 0; q < v.size(); ++q) {
+            I[o] = v[q].first; J[o] = id;
+            if (tI) tI[o] = tv[q];
+            if (tJ) tJ[o] = 0;
+            if (D) D[o] = v[q].second;
+            if (G) G[o] = gfun(v[q].second - R[v[q].first].a);
+            if (S) S[o] = 0;
+            if (img) for (int d = 0; d < 3; ++d) img[3 * o + d] = 0;
+            ++o;
+        }
+    };
+    put_elec(snk, snk_t, NF_SNK_ELEC);
+    put_elec(src, src_t, NF_SRC_ELEC);
+    return total;
+}
+
+double nfo_solve(int64_t n_rods, int64_t n_contacts, const uint32_t* I, const uint32_t* J,
+                 const double* G, double tol, int max_iter, double* v, double info[4]) {
+    std::vector<double> s(n_rods, 0.0), t(n_rods, 0.0);
+    DSU dsu(n_rods);
+    for (int64_t e = 0; e < n_contacts; ++e) {
+        if (J[e] == NF_SRC_ELEC) s[I[e]] += G[e];
+        else if (J[e] == NF_SNK_ELEC) t[I[e]] += G[e];
+        else dsu.unite(I[e], J[e]);
+    }
+    std::vector<char> hs(n_rods, 0), ht(n_rods, 0);
+    for (int64_t i = 0; i < n_rods; ++i) {
+        int64_t r = dsu.find(i);
+        if (s[i] > 0) hs[r] = 1;
+        if (t[i] > 0) ht[r] = 1;
+    }
+    std::vector<int64_t> idx(n_rods, -1);
+    int64_t m = 0;
+    for (int64_t i = 0; i < n_rods; ++i) {
+        int64_t r = dsu.find(i);
+        if (hs[r] && ht[r]) idx[i] = m++;
+    }
+    // Outside the source-sink network: components touching only the source sit
+    // at 1 V, all others at 0 V (no current flows there either way).
+    if (v) for (int64_t i = 0; i < n_rods; ++i) { int64_t r = dsu.find(i); v[i] = (hs[r] && !ht[r]) ? 1.0 : 0.0; }
+    if (info) { info[0] = 0; info[1] = (double)m; info[2] = m > 0; info[3] = 0; }
+    if (m == 0) return 0.0;
+    // CSR of K = L + diag(s + t) on active nodes.
+    std::vector<std::vector<std::pair<int64_t, double>>> rows(m);
+    std::vector<double> diag(m, 0.0), b(m, 0.0);
+    for (int64_t i = 0; i < n_rods; ++i) if (idx[i] >= 0) { diag[idx[i]] += s[i] + t[i]; b[idx[i]] = s[i]; }
+    for (int64_t e = 0; e < n_contacts; ++e) {
+        if (J[e] >= NF_SNK_ELEC) continue;
+        int64_t a = idx[I[e]], c = idx[J[e]];
+        if (a < 0) continue;
+        diag[a] += G[e]; diag[c] += G[e];
+        rows[a].push_back({c, -G[e]});
+        rows[c].push_back({a, -G[e]});
+    }
+    auto spmv = [&](const std::vector<double>& x, std::vector<double>& y) {
+        for (int64_t i = 0; i < m; ++i) {
+            double acc = diag[i] * x[i];
+            for (auto& kv : rows[i]) acc += kv.second * x[kv.first];
+            y[i] = acc;
+        }
+    };
+    std::vector<double> x(m, 0.0), r(b), z(m), pdir(m), q(m);
+    double bn = std::sqrt(std::inner_product(b.begin(), b.end(), b.begin(), 0.0));
+    for (int64_t i = 0; i < m; ++i) z[i] = r[i] / diag[i];
+    pdir = z;
+    double rz = std::inner_product(r.begin(), r.end(), z.begin(), 0.0);
+    int it = 0;
+    double rn = bn;
+    for (; it < max_iter && rn > tol * bn; ++it) {
+        spmv(pdir, q);
+        double alpha = rz / std::inner_product(pdir.begin(), pdir.end(), q.begin(), 0.0);
+        for (int64_t i = 0; i < m; ++i) { x[i] += alpha * pdir[i]; r[i] -= alpha * q[i]; }
+        if ((it + 1) % 50 == 0) {  // true residual now and then
+            spmv(x, q);
+            for (int64_t i = 0; i < m; ++i) r[i] = b[i] - q[i];
+        }
+        rn = std::sqrt(std::inner_product(r.begin(), r.end(), r.begin(), 0.0));
+        for (int64_t i = 0; i < m; ++i) z[i] = r[i] / diag[i];
+        double rz2 = std::inner_product(r.begin(), r.end(), z.begin(), 0.0);
+        double beta = rz2 / rz;
+        rz = rz2;
+        for (int64_t i = 0; i < m; ++i) pdir[i] = z[i] + beta * pdir[i];
+    }
+    spmv(x, q);
+    double res = 0;
+    for (int64_t i = 0; i < m; ++i) res += (b[i] - q[i]) * (b[i] - q[i]);
+    double Geff = 0;
+    for (int64_t i = 0; i < n_rods; ++i) {
+        if (idx[i] < 0) continue;
+        if (v) v[i] = x[idx[i]];
+        Geff += s[i] * (1.0 - x[idx[i]]);
+    }
+    if (info) { info[0] = it; info[3] = std::sqrt(res) / bn; }
+    return Geff;
+}
+
+void nfo_adjoint(const nf_params* p, const nfo_rod* rods, int64_t n_rods, int64_t n_contacts,
+                 const uint32_t* I, const uint32_t* J, const double* tI, const double* tJ,
+                 const double* D, const double* G, const int8_t* img, const double* v,
+                 double* dG_dend, double* dG_dlambda, double* dG_dG0) {
+    const double lam = p->lambda, dc = p->d_c, G0 = p->G0;
+    double dl = 0, dg0 = 0;
+    if (dG_dend) std::fill(dG_dend, dG_dend + 6 * n_rods, 0.0);
+    int f = p->field_dir == 1 ? 0 : (p->field_dir == 2 ? 1 : (p->field_dir == 4 ? 2 : -1));
+    for (int64_t e = 0; e < n_contacts; ++e) {
+        uint32_t i = I[e], j = J[e];
+        const nfo_rod& A = rods[i];
+        double dv, gap;
+        if (j == NF_SRC_ELEC) { dv = 1.0 - v[i]; gap = D[e] - A.a; }
+        else if (j == NF_SNK_ELEC) { dv = v[i]; gap = D[e] - A.a; }
+        else { dv = v[i] - v[j]; gap = D[e] - A.a - rods[j].a; }
+        double w = dv * dv;  // dG_eff/dG_e (self-adjoint network)
+        dg0 += w * G[e] / G0;
+        bool clamped = !(gap > dc);
+        if (!clamped) dl += w * G[e] * (gap - dc) / (lam * lam);
+        if (!dG_dend || clamped) continue;
+        double dGdD = -G[e] / lam * w;  // d/dD of G_e times dG_eff/dG_e
+        if (j >= NF_SNK_ELEC) {
+            // D = x_f of the lowest (source) / L - x_f of the highest (sink) axis end.
+            double sgn = (j == NF_SRC_ELEC) ? 1.0 : -1.0;
+            double uI = tI[e] / A.l + 0.5;
+            dG_dend[6 * i + f] += dGdD * sgn * (1.0 - uI);
+            dG_dend[6 * i + 3 + f] += dGdD * sgn * uI;
+            continue;
+        }
+        const nfo_rod& B = rods[j];
+        double sh[3] = {img[3 * e] * (double)p->box[0], img[3 * e + 1] * (double)p->box[1], img[3 * e + 2] * (double)p->box[2]};
+        double pa[3] = {A.x + tI[e] * A.cx, A.y + tI[e] * A.cy, A.z + tI[e] * A.cz};
+        double pb[3] = {(B.x + sh[0]) + tJ[e] * B.cx, (B.y + sh[1]) + tJ[e] * B.cy, (B.z + sh[2]) + tJ[e] * B.cz};
+        double uI = tI[e] / A.l + 0.5, uJ = tJ[e] / B.l + 0.5;
+        for (int d = 0; d < 3; ++d) {
+            double gd = (pa[d] - pb[d]) / D[e] * dGdD;
+            dG_dend[6 * i + d] += gd * (1.0 - uI);
+            dG_dend[6 * i + 3 + d] += gd * uI;
+            dG_dend[6 * j + d] -= gd * (1.0 - uJ);
+            dG_dend[6 * j + 3 + d] -= gd * uJ;
+        }
+    }
+    if (dG_dlambda) *dG_dlambda = dl;
+    if (dG_dG0) *dG_dG0 = dg0;
+}
+
+}  // extern "C"

@@ -1,0 +1,95 @@
+/*
+ * nf_oracle.h -- CPU oracle for the NanoFiller hot path (TEST INFRASTRUCTURE).
+ *
+ * This library is the checker: only the tests, __graft_entry__.smoke() and the
+ * CPU-baseline leg of bench.py load it. The product library never links it.
+ *
+ * It restates, in plain C++ evaluated in FP64 (or FP32 for pinning against the
+ * reference's own source), the reference's algorithm for:
+ *   - the hard-core predicate  cnt_intersec_shr      inc/intersection_dev.h:10-80
+ *   - the contact routine      distance_cylinder_capped
+ *                              inc/intersect/intersect_cylinder_capped.h:69-167
+ *   - the screening body test  body_intersect_cylinder_capped  (same file :181-191)
+ *   - the virtual inclusion    generate_virt_inclusions  inc/conductKernels.h:289-361
+ *   - the contact-area estimate surf_to_cylinder_capped (same file :204-293)
+ *   - the target count         simPrms::set_numCNT       src/simPrms.cpp:987-1002
+ *   - the Norton assembly and G_eff  tools/kirchhoff/kirchhoff.py:232-269
+ * plus the project-defined seeded candidate stream (Philox4x32-10, Salmon et al.
+ * 2011) and sequential insertion in stream order.
+ */
+#ifndef NF_ORACLE_H
+#define NF_ORACLE_H
+#include <stdint.h>
+#include "../include/nanofiller_gb300.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct nfo_rod { float x, y, z, cx, cy, cz, l, a; } nfo_rod;
+
+/* Philox4x32-10 block. */
+void nfo_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);
+
+/* Deterministic float math of the stream contract. */
+void nfo_sincos_turns(float t, float *c, float *s);
+float nfo_logf(float v);
+float nfo_expf(float x);
+
+/* Reference routine on one pair. kind 0: hard-core test (cnt_intersec_shr),
+ * kind 1: contact routine (distance_cylinder_capped). B is shifted by shift[]
+ * (its periodic image) before the test, as tarnsCNT does. use_double selects
+ * FP64 or FP32 evaluation. out = {d, t0, t1, Dtt.x, Dtt.y, Dtt.z}.
+ * thr_sep is `sep` (kind 0) or `separation` (kind 1); scf the soft-core fraction.
+ * Returns the hit decision. */
+int nfo_pair_eval(int use_double, int kind, const nfo_rod *A, const nfo_rod *B,
+                  const double shift[3], double eps, double scf, double thr_sep,
+                  int typo, double out[6]);
+
+/* Screening body test of a real rod A against a virtual rod given in FP64
+ * (centre, unit axis, length, radius). Returns 1 if the virtual rod is crossed. */
+int nfo_screen_eval(const nfo_rod *A, const double vr[3], const double vc[3],
+                    double vl, double va, const double shift[3], double eps);
+
+/* Contact area (surf_to_cylinder_capped) in FP64. */
+double nfo_contact_area(const nfo_rod *A, const nfo_rod *B, const double shift[3],
+                        double Dtt_x, double t0u, double t1u, double rlim);
+
+/* Candidate stream k0..k0+n-1: out[10*i + f], f = x y z cx cy cz l a u rho. */
+int nfo_candidates(const nf_params *p, const float *mesh, int nx, int ny, int nz,
+                   uint64_t k0, uint64_t n, float *out);
+
+/* Sequential insertion in stream order. batch>1 tests batches in parallel and
+ * resolves in-batch conflicts in index order (identical result).
+ * stats = {drawn, density_accepted, pair_evals}. Returns accepted count or <0. */
+int64_t nfo_generate(const nf_params *p, const float *mesh, int nx, int ny, int nz,
+                     int nthreads, int64_t batch, int brute_force, int64_t cap,
+                     nfo_rod *rods, uint64_t *stream_index, uint64_t stats[3]);
+
+/* Contacts: rod-rod (sorted I,J,image; screened ones removed), then sink, then
+ * source. counts = {internal, screened, sink, source}. Returns total or <0.
+ * Arrays sized cap. Electrode ids as in nanofiller_gb300.h. */
+int64_t nfo_contacts(const nf_params *p, const nfo_rod *rods, int64_t n, int nthreads,
+                     int brute_force, int64_t cap, uint32_t *I, uint32_t *J,
+                     double *tI, double *tJ, double *D, double *G, double *S,
+                     int8_t *img, int64_t counts[4]);
+
+/* Network solve by Jacobi-preconditioned CG in FP64 on the rods joined to both
+ * electrodes. v (n) receives voltages (1 on components touching only the source,
+ * 0 on other rods outside the network). info = {iters, n_active,
+ * percolating, residual}. Returns G_eff. */
+double nfo_solve(int64_t n_rods, int64_t n_contacts, const uint32_t *I,
+                 const uint32_t *J, const double *G, double tol, int max_iter,
+                 double *v, double info[4]);
+
+/* Adjoint: dG/d(endpoints) N x 6, dG/dlambda, dG/dG0 (FP64). */
+void nfo_adjoint(const nf_params *p, const nfo_rod *rods, int64_t n_rods,
+                 int64_t n_contacts, const uint32_t *I, const uint32_t *J,
+                 const double *tI, const double *tJ, const double *D,
+                 const double *G, const int8_t *img, const double *v,
+                 double *dG_dend, double *dG_dlambda, double *dG_dG0);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

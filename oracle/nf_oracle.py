@@ -1,0 +1,217 @@
+"""ctypes front end of the CPU oracle (TEST INFRASTRUCTURE).
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg import this
+module. It builds oracle/_build/libnf_oracle.so on first use (g++, no GPU) and
+exposes the oracle's restatement of the reference path on numpy arrays.
+
+Parameters travel as plain dicts of nf_params field names; the ctypes mirror of
+nf_params below follows include/nanofiller_gb300.h field for field.
+"""
+import ctypes as C
+import os
+import subprocess
+import threading
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libnf_oracle.so")
+_lock = threading.Lock()
+_lib = None
+
+SRC_ELEC = 0xFFFFFFFF
+SNK_ELEC = 0xFFFFFFFE
+
+
+class NfParams(C.Structure):
+    _fields_ = [
+        ("vf", C.c_float), ("vf_precision", C.c_float), ("box", C.c_float * 3),
+        ("mesh_ext", C.c_int32 * 3), ("density_file", C.c_char * 256),
+        ("pref_ort", C.c_float * 2), ("theta_med", C.c_float), ("theta_dev", C.c_float),
+        ("phi_med", C.c_float), ("phi_dev", C.c_float), ("l", C.c_float), ("a", C.c_float),
+        ("l_dev", C.c_float), ("a_dev", C.c_float), ("sep", C.c_float), ("sc_frac", C.c_float),
+        ("tol", C.c_float), ("stat_dist_lim", C.c_float), ("wrt_bin", C.c_int32),
+        ("self_align_step", C.c_int32), ("clust_flag", C.c_int32), ("reduce_flag", C.c_int32),
+        ("seed", C.c_uint64), ("n_candidates", C.c_uint64), ("n_target", C.c_int64),
+        ("gen_periodic", C.c_int32), ("field_dir", C.c_int32), ("orient_mode", C.c_int32),
+        ("vmf_kappa", C.c_float), ("len_mode", C.c_int32), ("len_sigma_ln", C.c_float),
+        ("len_min", C.c_float), ("len_max", C.c_float), ("rad_mode", C.c_int32),
+        ("rad_min", C.c_float), ("rad_max", C.c_float), ("density_default", C.c_float),
+        ("cell_edge", C.c_float), ("G0", C.c_double), ("lambda_", C.c_double), ("d_c", C.c_double),
+        ("ref_parallel_typo", C.c_int32), ("screening", C.c_int32),
+        ("round_candidates", C.c_int32), ("solve_max_iter", C.c_int32), ("solve_tol", C.c_double),
+    ]
+
+
+# Reference defaults (src/simPrms.cpp:22-117) plus project defaults.
+DEFAULTS = dict(
+    vf=0.05 / 100.0, vf_precision=0.05, box=(0.0, 0.0, 0.0), mesh_ext=(0, 0, 0), density_file=b"",
+    pref_ort=(0.0, 0.0), theta_med=0.0, theta_dev=-1.0, phi_med=0.0, phi_dev=-1.0,
+    l=4.0, a=0.010, l_dev=-1.0, a_dev=-1.0, sep=0.0, sc_frac=1.0, tol=1e-6, stat_dist_lim=0.015,
+    wrt_bin=0, self_align_step=0, clust_flag=0, reduce_flag=0,
+    seed=0, n_candidates=1 << 20, n_target=0, gen_periodic=7, field_dir=4, orient_mode=0,
+    vmf_kappa=0.0, len_mode=0, len_sigma_ln=0.0, len_min=0.0, len_max=0.0, rad_mode=0,
+    rad_min=0.0, rad_max=0.0, density_default=1.0, cell_edge=0.0, G0=1e-5, lambda_=0.00018,
+    d_c=0.00034, ref_parallel_typo=0, screening=1, round_candidates=0, solve_max_iter=20000,
+    solve_tol=1e-10,
+)
+
+
+def make_params(d):
+    p = NfParams()
+    full = dict(DEFAULTS)
+    full.update(d)
+    for k, v in full.items():
+        if k == "lambda":
+            k = "lambda_"
+        if isinstance(v, (tuple, list)):
+            arr = getattr(p, k)
+            for i, x in enumerate(v):
+                arr[i] = x
+        elif k == "density_file":
+            setattr(p, k, v if isinstance(v, bytes) else str(v).encode())
+        else:
+            setattr(p, k, v)
+    return p
+
+
+def build():
+    subprocess.run(["make", "-s", "-C", HERE], check=True)
+
+
+def lib():
+    global _lib
+    with _lock:
+        if _lib is None:
+            if not os.path.exists(LIB_PATH) or os.path.getmtime(LIB_PATH) < max(
+                    os.path.getmtime(os.path.join(HERE, f)) for f in ("nf_oracle.cpp", "nf_oracle.h")):
+                build()
+            L = C.CDLL(LIB_PATH)
+            P = C.POINTER
+            L.nfo_philox4x32_10.argtypes = [P(C.c_uint32), P(C.c_uint32), P(C.c_uint32)]
+            L.nfo_sincos_turns.argtypes = [C.c_float, P(C.c_float), P(C.c_float)]
+            L.nfo_logf.argtypes = [C.c_float]; L.nfo_logf.restype = C.c_float
+            L.nfo_expf.argtypes = [C.c_float]; L.nfo_expf.restype = C.c_float
+            L.nfo_pair_eval.argtypes = [C.c_int, C.c_int, C.c_void_p, C.c_void_p, P(C.c_double),
+                                        C.c_double, C.c_double, C.c_double, C.c_int, P(C.c_double)]
+            L.nfo_pair_eval.restype = C.c_int
+            L.nfo_screen_eval.argtypes = [C.c_void_p, P(C.c_double), P(C.c_double), C.c_double,
+                                          C.c_double, P(C.c_double), C.c_double]
+            L.nfo_candidates.argtypes = [P(NfParams), C.c_void_p, C.c_int, C.c_int, C.c_int,
+                                         C.c_uint64, C.c_uint64, C.c_void_p]
+            L.nfo_generate.argtypes = [P(NfParams), C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int,
+                                       C.c_int64, C.c_int, C.c_int64, C.c_void_p, C.c_void_p,
+                                       P(C.c_uint64)]
+            L.nfo_generate.restype = C.c_int64
+            L.nfo_contacts.argtypes = [P(NfParams), C.c_void_p, C.c_int64, C.c_int, C.c_int,
+                                       C.c_int64] + [C.c_void_p] * 8 + [P(C.c_int64)]
+            L.nfo_contacts.restype = C.c_int64
+            L.nfo_solve.argtypes = [C.c_int64, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p,
+                                    C.c_double, C.c_int, C.c_void_p, P(C.c_double)]
+            L.nfo_solve.restype = C.c_double
+            L.nfo_adjoint.argtypes = [P(NfParams), C.c_void_p, C.c_int64, C.c_int64] + \
+                [C.c_void_p] * 8 + [C.c_void_p, P(C.c_double), P(C.c_double)]
+            _lib = L
+    return _lib
+
+
+ROD_DTYPE = np.dtype([(f, np.float32) for f in ("x", "y", "z", "cx", "cy", "cz", "l", "a")])
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+def philox(ctr, key):
+    L = lib()
+    c = (C.c_uint32 * 4)(*ctr)
+    k = (C.c_uint32 * 2)(*key)
+    o = (C.c_uint32 * 4)()
+    L.nfo_philox4x32_10(c, k, o)
+    return list(o)
+
+
+def sincos_turns(t):
+    c, s = C.c_float(), C.c_float()
+    lib().nfo_sincos_turns(t, C.byref(c), C.byref(s))
+    return c.value, s.value
+
+
+def candidates(params, k0, n, mesh=None):
+    p = make_params(params)
+    out = np.zeros((n, 10), np.float32)
+    nx, ny, nz = mesh.shape if mesh is not None else (0, 0, 0)
+    m = None if mesh is None else np.ascontiguousarray(mesh, np.float32)
+    lib().nfo_candidates(C.byref(p), _ptr(m), nx, ny, nz, k0, n, _ptr(out))
+    return out
+
+
+def pair_eval(A, B, shift=(0.0, 0.0, 0.0), kind=1, use_double=True, eps=1e-6, scf=1.0,
+              thr_sep=0.0014, typo=False):
+    a = np.array([tuple(A)], ROD_DTYPE)
+    b = np.array([tuple(B)], ROD_DTYPE)
+    sh = (C.c_double * 3)(*shift)
+    out = (C.c_double * 6)()
+    hit = lib().nfo_pair_eval(int(use_double), kind, _ptr(a), _ptr(b), sh, eps, scf, thr_sep,
+                              int(typo), out)
+    return bool(hit), list(out)
+
+
+def generate(params, mesh=None, nthreads=0, batch=4096, brute_force=False, cap=None):
+    p = make_params(params)
+    if cap is None:
+        cap = int(params.get("n_target") or 0) or 4 * 10 ** 6
+    rods = np.zeros(cap, ROD_DTYPE)
+    idx = np.zeros(cap, np.uint64)
+    st = (C.c_uint64 * 3)()
+    nx, ny, nz = mesh.shape if mesh is not None else (0, 0, 0)
+    m = None if mesh is None else np.ascontiguousarray(mesh, np.float32)
+    n = lib().nfo_generate(C.byref(p), _ptr(m), nx, ny, nz, nthreads, batch, int(brute_force),
+                           cap, _ptr(rods), _ptr(idx), st)
+    if n < 0:
+        raise RuntimeError(f"nfo_generate failed ({n})")
+    return rods[:n].copy(), idx[:n].copy(), dict(drawn=st[0], density_accepted=st[1], exact_evals=st[2])
+
+
+def contacts(params, rods, nthreads=0, brute_force=False):
+    p = make_params(params)
+    rods = np.ascontiguousarray(rods, ROD_DTYPE)
+    cnt = (C.c_int64 * 4)()
+    L = lib()
+    need = L.nfo_contacts(C.byref(p), _ptr(rods), len(rods), nthreads, int(brute_force), 0,
+                          *([None] * 9), cnt)
+    if need < 0:
+        raise RuntimeError("nfo_contacts failed")
+    cap = max(int(need), 1)
+    out = dict(I=np.zeros(cap, np.uint32), J=np.zeros(cap, np.uint32), tI=np.zeros(cap),
+               tJ=np.zeros(cap), D=np.zeros(cap), G=np.zeros(cap), S=np.zeros(cap),
+               image=np.zeros((cap, 3), np.int8))
+    n = L.nfo_contacts(C.byref(p), _ptr(rods), len(rods), nthreads, int(brute_force), cap,
+                       _ptr(out["I"]), _ptr(out["J"]), _ptr(out["tI"]), _ptr(out["tJ"]),
+                       _ptr(out["D"]), _ptr(out["G"]), _ptr(out["S"]), _ptr(out["image"]), cnt)
+    out = {k: v[:n] for k, v in out.items()}
+    out["counts"] = dict(internal=cnt[0], screened=cnt[1], sink=cnt[2], source=cnt[3])
+    return out
+
+
+def solve(n_rods, ct, tol=1e-12, max_iter=200000):
+    v = np.zeros(n_rods)
+    info = (C.c_double * 4)()
+    I = np.ascontiguousarray(ct["I"], np.uint32)
+    J = np.ascontiguousarray(ct["J"], np.uint32)
+    G = np.ascontiguousarray(ct["G"], np.float64)
+    g = lib().nfo_solve(n_rods, len(I), _ptr(I), _ptr(J), _ptr(G), tol, max_iter, _ptr(v), info)
+    return g, v, dict(iters=info[0], n_active=int(info[1]), percolating=bool(info[2]), residual=info[3])
+
+
+def adjoint(params, rods, ct, v):
+    p = make_params(params)
+    rods = np.ascontiguousarray(rods, ROD_DTYPE)
+    n = len(rods)
+    g = np.zeros((n, 6))
+    dl, dg0 = C.c_double(), C.c_double()
+    arr = [np.ascontiguousarray(ct[k]) for k in ("I", "J", "tI", "tJ", "D", "G")]
+    img = np.ascontiguousarray(ct["image"], np.int8)
+    lib().nfo_adjoint(C.byref(p), _ptr(rods), n, len(arr[0]), *[_ptr(a) for a in arr], _ptr(img),
+                      _ptr(np.ascontiguousarray(v, np.float64)), _ptr(g), C.byref(dl), C.byref(dg0))
+    return g, dl.value, dg0.value
