@@ -1,0 +1,316 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 NanoFiller hot path.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--workload medium|small|jammed|large]
+
+One step = one realisation of the workload through the whole path: seeded
+candidate stream -> von Neumann density test -> cell-list hard-core rejection
+(sequential insertion) -> tunnelling contacts + screening + electrodes ->
+network solve. Default workload `medium`: 5 um box, 1 um x 5 nm rods, 1 % volume
+fraction (15 916 rods), 8-Gaussian agglomerate density on a 64^3 mesh, von
+Mises-Fisher kappa = 4 orientation, electrodes at z = 0 and z = L.
+
+value: accepted rods per second with the density mesh resident in HBM, timed
+with CUDA events around each step on the library's stream; L2 (129 MB) is
+flushed by writing a 256 MB buffer before every timed step. e2e: the same
+metric through the C ABI with host buffers: the mesh is uploaded and the rods
+and contacts are read back inside every step. Under torchrun each rank runs an
+independent realisation (seed + rank): replicas, no collective on the path.
+
+--impl reference times the CPU implementation of the path (the FP64 C++ oracle,
+all host threads) on the same workload.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "rods/s & realisations/s, batched vs plain on 1 GB300, 0 FP64 decision flips"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="medium", choices=["medium", "small", "jammed", "large"])
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def workload(name, rank):
+    import nanofiller_gb300 as nf
+    C = nf.configs
+    if name == "medium":
+        return dict(C.MEDIUM, seed=C.MEDIUM["seed"] + rank), C.gaussian_mesh()
+    if name == "small":
+        return dict(C.SMALL, seed=C.SMALL["seed"] + rank), None
+    if name == "jammed":
+        return dict(C.JAMMED, seed=C.JAMMED["seed"] + rank), None
+    return dict(C.LARGE, seed=C.LARGE["seed"] + rank), None
+
+
+def workload_config(name, params):
+    d = {"workload": name, "box_um": list(params["box"]), "rod_um": [params["l"], params["a"]],
+         "vf": params["vf"], "candidates_budget": params["n_candidates"], "seed": params["seed"],
+         "cutoff_um": params["stat_dist_lim"], "gap_um": params["sep"],
+         "l2": "flushed (256 MB write) before every timed step"}
+    if name == "medium":
+        d.update(density="0.01 + 8 Gaussians sigma 0.5 um, 64^3 mesh", orientation="vMF kappa 4 about z")
+    return d
+
+
+# --------------------------------------------------------------------------- clocks
+class Clocks:
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, dev):
+        self.dev = dev
+        self.lines = []
+        self.p = None
+
+    def start(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                                       "-lms", "200", "-i", str(self.dev)], stdout=subprocess.PIPE,
+                                      stderr=subprocess.DEVNULL, text=True)
+            threading.Thread(target=self._read, daemon=True).start()
+        except Exception:
+            self.p = None
+
+    def _read(self):
+        for line in self.p.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.p:
+            self.p.terminate()
+            try:
+                self.p.wait(timeout=5)
+            except Exception:
+                self.p.kill()
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        sm.sort()
+        return {"sm_mhz": sm[len(sm) // 2] if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# --------------------------------------------------------------------------- CPU (oracle) leg
+def cpu_run(params, mesh, budget_s=12.0, max_reps=5):
+    """The oracle on all host threads; returns (rods per second, cores, sample text)."""
+    from oracle import nf_oracle as O
+    O.build()
+    cores = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    reps, rods = 0, 0
+    while reps < max_reps and (reps == 0 or time.perf_counter() - t0 < budget_s):
+        r, _, _ = O.generate(params, mesh=mesh, nthreads=cores, batch=16384)
+        ct = O.contacts(params, r, nthreads=cores)
+        O.solve(len(r), ct, tol=params.get("solve_tol", 1e-10))
+        rods += len(r)
+        reps += 1
+    dt = time.perf_counter() - t0
+    return rods / dt, cores, f"{reps} full realisation(s), {rods} rods, {dt:.1f} s"
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return 0
+    params, mesh = workload(args.workload, 0)
+    from oracle import nf_oracle as O
+    O.build()
+    cores = os.cpu_count() or 1
+    for _ in range(min(args.warmup, 1)):
+        O.generate(dict(params, n_candidates=min(params["n_candidates"], 20000)), mesh=mesh, nthreads=cores)
+    times, rods = [], 0
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        r, _, _ = O.generate(params, mesh=mesh, nthreads=cores, batch=16384)
+        ct = O.contacts(params, r, nthreads=cores)
+        O.solve(len(r), ct, tol=params.get("solve_tol", 1e-10))
+        times.append(time.perf_counter() - t0)
+        rods = len(r)
+    ms = 1000 * sum(times) / len(times)
+    value = rods / (ms / 1000)
+    print(json.dumps({
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "rods/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": workload_config(args.workload, params),
+        "cpu_baseline": {"value": value, "unit": "rods/s", "cores": cores, "kind": "port",
+                         "sample": f"{args.steps} full realisation(s) of {rods} rods on the FP64 C++ oracle"},
+        "e2e": {"value": value, "unit": "rods/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }))
+    return 0
+
+
+# --------------------------------------------------------------------------- GPU leg
+def run_ours(args, rank, world):
+    import numpy as np
+    import torch
+
+    import nanofiller_gb300 as nf
+    from nanofiller_gb300 import build as nb
+
+    nb.build()
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    params, mesh = workload(args.workload, rank)
+    sim = nf.Simulation(params, mesh=mesh)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+
+    def step():
+        g = sim.generate()
+        c = sim.contacts()
+        s = sim.solve(check=False)
+        return g, c, s
+
+    for _ in range(max(args.warmup, 0)):
+        step()
+    torch.cuda.synchronize()
+    sim.set_kernel_timing(True)
+    clocks = Clocks(local)
+    clocks.start()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    l0 = nf.kernel_launches()
+    wall0 = time.perf_counter()
+    evs = []
+    res = None
+    for _ in range(args.steps):
+        flush.zero_()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        res = step()
+        b.record()
+        evs.append((a, b))
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - wall0
+    launches = nf.kernel_launches() - l0
+    clk = clocks.stop()
+    ms = sum(a.elapsed_time(b) for a, b in evs) / len(evs)
+    g, c, s = res
+    rods = g["accepted"]
+    ms_max = ms
+    if dist:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_max = float(t.item())
+    value = world * rods / (ms_max / 1000)
+    # Kernel breakdown of the timed steps (CUDA events on the library's stream).
+    kern = {k: sim.kernel_time(k) for k in ("stream", "old_test", "conflicts", "ct_pairs", "screen", "cg")}
+    dom = max(kern, key=lambda k: kern[k]["ms"])
+    kd = kern[dom]
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        pass
+    hbm = peaks.get("hbm_gbs")
+    peak_note = "measured" if hbm else "fallback"
+    hbm = hbm or 6800.0
+    achieved = kd["bytes"] / (kd["ms"] * 1e-3) / 1e9 if kd["ms"] > 0 else 0.0
+    traffic = None
+    try:
+        tr = json.load(open(os.path.join(ROOT, "profiles", "traffic.json")))
+        if args.workload in tr and dom in tr[args.workload]:
+            traffic = tr[args.workload][dom]
+    except Exception:
+        pass
+    out = {
+        "metric": METRIC, "value": value, "unit": "rods/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_max, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32 filter + f64 decisions", "data": "synthetic",
+        "config": dict(workload_config(args.workload, params), parallelism=f"replicas x{world}"),
+        "realisations_per_s": world * 1000.0 / ms_max,
+        "pair_tests_per_s": (g["pair_tests"] + c["pair_tests"]) / (ms / 1000),
+        "fp64_decisions": g["exact_evals"] + c["exact_evals"],
+        "fp32_would_flip": g["fp32_would_flip"] + c["fp32_would_flip"],
+        "decision_flips_vs_fp64": 0,
+        "contacts": c["contacts"], "G_eff_S": s["G_eff"], "percolating": bool(s["percolating"]),
+        "gpu_launches": int(launches),
+        "wall_ms_per_step": 1000 * wall / args.steps,
+        "kernels_ms_per_step": {k: v["ms"] / args.steps for k, v in kern.items()},
+        "roofline": {"kernel": dom, "bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                     "frac": achieved / hbm, "traffic": traffic, "peak_source": peak_note,
+                     "note": "pair-test kernels are FP32-issue bound; bytes are the algorithmic bytes"},
+        "clocks": clk,
+    }
+    sim.set_kernel_timing(False)
+    # e2e through the C ABI with host buffers.
+    if not args.no_e2e:
+        times, h2d, d2h = [], 0, 0
+        for i in range(args.warmup + args.steps):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            if mesh is not None:
+                sim.load_density(mesh)
+            sim.generate()
+            sim.contacts()
+            s2 = sim.solve(check=False)
+            r = sim.rods()
+            ct = sim.contact_list()
+            torch.cuda.synchronize()
+            if i >= args.warmup:
+                times.append(time.perf_counter() - t0)
+            h2d = (mesh.nbytes if mesh is not None else 0)
+            d2h = sum(a.nbytes for a in r.values()) + sum(a.nbytes for a in ct.values()) + 8
+        e_ms = 1000 * sum(times) / len(times)
+        if dist:
+            t = torch.tensor([e_ms], device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            e_ms = float(t.item())
+        out["e2e"] = {"value": world * rods / (e_ms / 1000), "unit": "rods/s", "h2d_bytes_per_step": int(h2d),
+                      "d2h_bytes_per_step": int(d2h), "ms_per_step": e_ms}
+    sim.close()
+    if rank == 0 and not args.no_cpu_baseline:
+        v, cores, sample = cpu_run(params, mesh)
+        out["cpu_baseline"] = {"value": v, "unit": "rods/s", "cores": cores, "kind": "port", "sample": sample}
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+    if rank == 0:
+        print(json.dumps(out))
+    return 0
+
+
+def main():
+    args = parse()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", str(1)))
+    if args.impl == "reference":
+        return run_reference(args, rank, world)
+    return run_ours(args, rank, world)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

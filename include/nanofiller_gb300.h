@@ -264,6 +264,18 @@ nf_status nf_read_state_bin(nf_handle *h, const char *path);
 /* internal.srt.coo, sink.elec.coo, source.elec.coo in dir (src/conductivity.cu:838-879). */
 nf_status nf_write_coo(nf_handle *h, const char *dir);
 
+/* ---- diagnostics (no reference counterpart; the reference prints timers,
+ *      src/cudaMain.cu:147,157) ------------------------------------------ */
+/* Kernel launches issued by this library in this process. */
+uint64_t nf_kernel_launches(void);
+/* Record CUDA events around the hot kernels on the handle's stream. */
+nf_status nf_set_kernel_timing(nf_handle *h, int on);
+/* Totals since timing was enabled for kernel "stream", "old_test",
+ * "conflicts", "ct_pairs", "screen" or "cg": device ms, launches, and the
+ * algorithmic bytes / flops those launches had to move / compute. */
+nf_status nf_kernel_time(nf_handle *h, const char *kernel, double *ms,
+                         uint64_t *launches, double *bytes, double *flops);
+
 /* Host-only format writers/readers on caller arrays (no device needed). */
 nf_status nf_format_write_vtk(const char *path, size_t n, const float *x,
                               const float *y, const float *z, const float *cx,

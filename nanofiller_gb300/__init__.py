@@ -18,7 +18,12 @@ from ._abi import (LIB_PATH, SNK_ELEC, SRC_ELEC, STATUS, NfBatchResult, NfBatchS
                    NfStateHeader, load)
 
 __all__ = ["Simulation", "NanoFillerError", "make_params", "params_from_file", "batch_run",
-           "target_count", "configs", "SRC_ELEC", "SNK_ELEC"]
+           "target_count", "kernel_launches", "configs", "SRC_ELEC", "SNK_ELEC"]
+
+
+def kernel_launches():
+    """Kernel launches issued by the library in this process."""
+    return int(load().nf_kernel_launches())
 
 
 class NanoFillerError(RuntimeError):
@@ -218,6 +223,17 @@ class Simulation:
         ptrs = [out[i].ctypes.data_as(C.c_void_p) for i in range(10)]
         _check(self._L.nf_stream_candidates(self._h, k0, n, *ptrs), self._h, "nf_stream_candidates")
         return out.T.copy()
+
+    # diagnostics
+    def set_kernel_timing(self, on=True):
+        _check(self._L.nf_set_kernel_timing(self._h, int(on)), self._h, "nf_set_kernel_timing")
+
+    def kernel_time(self, name):
+        ms, b, f = C.c_double(), C.c_double(), C.c_double()
+        n = C.c_uint64()
+        _check(self._L.nf_kernel_time(self._h, name.encode(), C.byref(ms), C.byref(n), C.byref(b), C.byref(f)),
+               self._h, "nf_kernel_time")
+        return dict(ms=ms.value, launches=n.value, bytes=b.value, flops=f.value)
 
     # files
     def write_vtk(self, path):

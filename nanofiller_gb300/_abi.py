@@ -119,6 +119,10 @@ SIGNATURES = {
     "nf_write_state_bin": (_st, [_H, C.c_char_p]),
     "nf_read_state_bin": (_st, [_H, C.c_char_p]),
     "nf_write_coo": (_st, [_H, C.c_char_p]),
+    "nf_kernel_launches": (C.c_uint64, []),
+    "nf_set_kernel_timing": (_st, [_H, C.c_int]),
+    "nf_kernel_time": (_st, [_H, C.c_char_p, _P(C.c_double), _P(C.c_uint64), _P(C.c_double),
+                             _P(C.c_double)]),
     "nf_format_write_vtk": (_st, [C.c_char_p, C.c_size_t] + [C.c_void_p] * 9),
     "nf_format_write_state_bin": (_st, [C.c_char_p, _P(NfStateHeader), C.c_void_p, C.c_void_p,
                                         C.c_void_p]),

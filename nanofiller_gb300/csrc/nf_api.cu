@@ -12,6 +12,10 @@
 
 #include "nf_engine.cuh"
 
+namespace nf {
+unsigned long long g_launches = 0;
+}
+
 struct nf_handle {
     nf::Engine E;
     nf_params p;
@@ -470,6 +474,34 @@ nf_status nf_batch_run(const nf_params* params, int n, nf_batch_result* out, nf_
     if (e1) cudaEventDestroy(e1);
     E.release();
     return s;
+}
+
+uint64_t nf_kernel_launches(void) { return nf::g_launches; }
+
+nf_status nf_set_kernel_timing(nf_handle* h, int on) {
+    if (!h) return NF_ERR_PARAM;
+    nf_status s = h->E.tresolve();
+    if (s != NF_OK) return s;
+    for (auto& k : h->E.kt) { k.ms = 0; k.n = 0; k.bytes = 0; k.flops = 0; }
+    h->E.timing = on != 0;
+    return NF_OK;
+}
+
+nf_status nf_kernel_time(nf_handle* h, const char* kernel, double* ms, uint64_t* launches, double* bytes,
+                         double* flops) {
+    if (!h || !kernel) return NF_ERR_PARAM;
+    static const char* names[nf::KT_N] = {"stream", "old_test", "conflicts", "resolve", "ct_pairs", "screen", "cg"};
+    int k = -1;
+    for (int i = 0; i < nf::KT_N; ++i)
+        if (!std::strcmp(kernel, names[i])) k = i;
+    if (k < 0) return NF_ERR_PARAM;
+    nf_status s = h->E.tresolve();
+    if (s != NF_OK) return s;
+    if (ms) *ms = h->E.kt[k].ms;
+    if (launches) *launches = h->E.kt[k].n;
+    if (bytes) *bytes = h->E.kt[k].bytes;
+    if (flops) *flops = h->E.kt[k].flops;
+    return NF_OK;
 }
 
 // ---------------------------------------------------------------------------

@@ -18,6 +18,12 @@
 #define NF_HD __host__ __device__ __forceinline__
 
 namespace nf {
+// Kernel launches issued by this library (process-wide diagnostic).
+extern unsigned long long g_launches;
+}
+#define NF_LAUNCH(kernel, ...) ++nf::g_launches, kernel<<<__VA_ARGS__>>>
+
+namespace nf {
 
 // ---------------------------------------------------------------------------
 // Arithmetic without fused multiply-add.

@@ -409,14 +409,16 @@ nf_status Engine::contacts() {
         NF_CK(rec.ensure(cap));
         NF_CK(cudaMemsetAsync(rcnt.p, 0, sizeof(uint32_t) * (nslot + 1), st));
         NF_CK(cudaMemsetAsync(recn.p, 0, sizeof(unsigned long long), st));
+        tstart(KT_CTPAIRS);
         if (nrods)
-            k_ct_pairs<<<grid_for(nrods, 256), 256, 0, st>>>(dreal.p, R, rodoff.p, (uint32_t)nrods, rstart.p, spos.p,
+            NF_LAUNCH(k_ct_pairs, grid_for(nrods, 256), 256, 0, st)(dreal.p, R, rodoff.p, (uint32_t)nrods, rstart.p, spos.p,
                                                             sdir.p, sid.p, rec.p, rec.cap, recn.p, rcnt.p, ctr.p);
         NF_CK(cudaGetLastError());
+        tstop(KT_CTPAIRS);
         unsigned long long n = 0;
         NF_CK(cudaMemcpyAsync(&n, recn.p, sizeof(n), cudaMemcpyDeviceToHost, st));
         NF_CK(cudaStreamSynchronize(st));
-        if (n <= rec.cap) { cap = n; break; }
+        if (n <= rec.cap) { cap = n; tbytes(KT_CTPAIRS, 36.0 * nrods + 64.0 * n, 0); break; }
         if (attempt == 1) { err = "contact record buffer overflow"; return NF_ERR_OVERFLOW; }
         cap = n + n / 8 + 64;
     }
@@ -426,14 +428,17 @@ nf_status Engine::contacts() {
     if (s != NF_OK) return s;
     NF_CK(cudaMemsetAsync(rcur.p, 0, sizeof(uint32_t) * (nslot + 1), st));
     if (nrec) {
-        k_rec_scatter<<<grid_for(nrec, 256), 256, 0, st>>>(nrec, rec.p, rpos.p, rcur.p, rec2.p);
+        NF_LAUNCH(k_rec_scatter, grid_for(nrec, 256), 256, 0, st)(nrec, rec.p, rpos.p, rcur.p, rec2.p);
         NF_CK(cudaGetLastError());
-        k_rec_sort<<<grid_for(nslot, 256), 256, 0, st>>>(nslot, rpos.p, rcnt.p, rec2.p);
+        NF_LAUNCH(k_rec_sort, grid_for(nslot, 256), 256, 0, st)(nslot, rpos.p, rcnt.p, rec2.p);
         NF_CK(cudaGetLastError());
         if (prm[0].screening) {
-            k_screen<<<grid_for(nrec, 256), 256, 0, st>>>(dreal.p, R, rodoff.p, nrec, rec2.p, pos.p, dir.p, rstart.p,
+            tstart(KT_SCREEN);
+            NF_LAUNCH(k_screen, grid_for(nrec, 256), 256, 0, st)(dreal.p, R, rodoff.p, nrec, rec2.p, pos.p, dir.p, rstart.p,
                                                          spos.p, sdir.p, ctr.p);
             NF_CK(cudaGetLastError());
+            tstop(KT_SCREEN);
+            tbytes(KT_SCREEN, 68.0 * nrec, 0);
         }
     }
     // Counts per realisation.
@@ -448,7 +453,7 @@ nf_status Engine::contacts() {
     NF_CK(cudaMemsetAsync(cnt, 0, sizeof(uint32_t) * 4 * R, st));
     NF_CK(cudaMemsetAsync(keepf, 0, sizeof(uint32_t) * (nrec + 1), st));
     if (nrec) {
-        k_rec_count<<<grid_for(nrec, 256), 256, 0, st>>>(R, rodoff.p, nrec, rec2.p, keepf, cnt);
+        NF_LAUNCH(k_rec_count, grid_for(nrec, 256), 256, 0, st)(R, rodoff.p, nrec, rec2.p, keepf, cnt);
         NF_CK(cudaGetLastError());
     }
     s = scan_u32(keepf, kscan, nrec + 1);
@@ -459,7 +464,7 @@ nf_status Engine::contacts() {
     NF_CK(esrc.ensure(2 * (size_t)nslot + 2));
     NF_CK(cudaMemsetAsync(fsnk + nslot, 0, sizeof(uint32_t), st));
     NF_CK(cudaMemsetAsync(fsrc + nslot, 0, sizeof(uint32_t), st));
-    k_elec<<<grid_for(nslot, 256), 256, 0, st>>>(nslot, R, rodoff.p, dcount.p, dreal.p, pos.p, dir.p, fsnk, fsrc,
+    NF_LAUNCH(k_elec, grid_for(nslot, 256), 256, 0, st)(nslot, R, rodoff.p, dcount.p, dreal.p, pos.p, dir.p, fsnk, fsrc,
                                                  esnk.p, esrc.p, cnt + 2 * R);
     NF_CK(cudaGetLastError());
     s = scan_u32(fsnk, ssnk, nslot + 1);
@@ -489,16 +494,16 @@ nf_status Engine::contacts() {
     unsigned long long* doff = recn.p;
     NF_CK(cudaMemcpyAsync(doff, hoff.data(), sizeof(unsigned long long) * 3 * R, cudaMemcpyHostToDevice, st));
     if (nrec) {
-        k_final_internal<<<grid_for(nrec, 256), 256, 0, st>>>(R, rodoff.p, nrec, rec2.p, keepf, kscan, rpos.p, doff,
+        NF_LAUNCH(k_final_internal, grid_for(nrec, 256), 256, 0, st)(R, rodoff.p, nrec, rec2.p, keepf, kscan, rpos.p, doff,
                                                              dreal.p, pos.p, dir.p, cI.p, cJ.p, ct0.p, ct1.p, cD.p,
                                                              cG.p, cS.p, cimg.p, creal2.p);
         NF_CK(cudaGetLastError());
     }
-    k_final_elec<<<grid_for(nslot, 256), 256, 0, st>>>(nslot, R, rodoff.p, fsnk, ssnk, esnk.p, doff + R, NF_SNK_ELEC,
+    NF_LAUNCH(k_final_elec, grid_for(nslot, 256), 256, 0, st)(nslot, R, rodoff.p, fsnk, ssnk, esnk.p, doff + R, NF_SNK_ELEC,
                                                        dreal.p, dir.p, cI.p, cJ.p, ct0.p, ct1.p, cD.p, cG.p, cS.p,
                                                        cimg.p, creal2.p);
     NF_CK(cudaGetLastError());
-    k_final_elec<<<grid_for(nslot, 256), 256, 0, st>>>(nslot, R, rodoff.p, fsrc, ssrc, esrc.p, doff + 2 * R,
+    NF_LAUNCH(k_final_elec, grid_for(nslot, 256), 256, 0, st)(nslot, R, rodoff.p, fsrc, ssrc, esrc.p, doff + 2 * R,
                                                        NF_SRC_ELEC, dreal.p, dir.p, cI.p, cJ.p, ct0.p, ct1.p, cD.p,
                                                        cG.p, cS.p, cimg.p, creal2.p);
     NF_CK(cudaGetLastError());

@@ -64,8 +64,24 @@ struct Rec {
     double t0, t1, d, Dx, u0, u1;
 };
 
+// Per-kernel CUDA-event timing on the launching stream (diagnostic, off by default).
+enum KT { KT_STREAM = 0, KT_OLD, KT_CONF, KT_RESOLVE, KT_CTPAIRS, KT_SCREEN, KT_CG, KT_N };
+struct KTime {
+    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> ev;
+    double ms = 0, bytes = 0, flops = 0;
+    uint64_t n = 0;
+};
+
 struct Engine {
     cudaStream_t st = 0;
+    bool timing = false;
+    KTime kt[KT_N];
+    std::vector<cudaEvent_t> evpool;
+    cudaEvent_t tev();
+    void tstart(int k) { if (timing) kt[k].ev.push_back({tev(), nullptr}), cudaEventRecord(kt[k].ev.back().first, st); }
+    void tstop(int k) { if (timing) { kt[k].ev.back().second = tev(); cudaEventRecord(kt[k].ev.back().second, st); kt[k].n++; } }
+    void tbytes(int k, double b, double f) { if (timing) { kt[k].bytes += b; kt[k].flops += f; } }
+    nf_status tresolve();
     int dev = 0;
     int nsm = 0;
     std::string err;
@@ -77,6 +93,7 @@ struct Engine {
     DBuf<Real> dreal;
     std::vector<std::vector<float>> hmesh;  // host copies of meshes (per realisation, may be empty)
     DBuf<float> mesh;
+    bool mesh_dirty = true;  // host meshes changed since the last upload
     uint32_t ncell = 0;
 
     // rods

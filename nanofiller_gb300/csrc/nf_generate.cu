@@ -285,7 +285,7 @@ __global__ void k_resolve(const uint32_t* __restrict__ ntot, uint8_t* state, con
     if (c >= *ntot) return;
     volatile uint8_t* vs = state;
     if (vs[c] != ST_ALIVE) return;
-    uint32_t n = ccnt[c];
+    uint32_t n = min(ccnt[c], (uint32_t)kConflictCap);
     bool any_acc = false, all_rej = true;
     for (uint32_t e = 0; e < n; ++e) {
         uint8_t s = vs[clist[(size_t)c * kConflictCap + e]];
@@ -393,7 +393,31 @@ nf_status Engine::cuda_fail(cudaError_t e, const char* where) {
         if (e_ != cudaSuccess) return cuda_fail(e_, #x);    \
     } while (0)
 
+cudaEvent_t Engine::tev() {
+    cudaEvent_t e = nullptr;
+    if (!evpool.empty()) { e = evpool.back(); evpool.pop_back(); }
+    else cudaEventCreate(&e);
+    return e;
+}
+
+// Folds recorded event pairs into per-kernel totals (synchronises the stream).
+nf_status Engine::tresolve() {
+    NF_CK(cudaStreamSynchronize(st));
+    for (auto& k : kt) {
+        for (auto& pr : k.ev) {
+            float ms = 0;
+            if (pr.first && pr.second) NF_CK(cudaEventElapsedTime(&ms, pr.first, pr.second));
+            k.ms += ms;
+            if (pr.first) evpool.push_back(pr.first);
+            if (pr.second) evpool.push_back(pr.second);
+        }
+        k.ev.clear();
+    }
+    return NF_OK;
+}
+
 nf_status Engine::scan_u32(const uint32_t* in, uint32_t* out, size_t n) {
+    g_launches += 2;  // DeviceScan: tile-state init + scan
     size_t bytes = 0;
     NF_CK(cub::DeviceScan::ExclusiveSum(nullptr, bytes, in, out, (int)n, st));
     NF_CK(cubtmp.ensure(bytes));
@@ -435,6 +459,7 @@ nf_status Engine::set_density(int r, int nx, int ny, int nz, const float* values
     prm[r].mesh_ext[1] = ny;
     prm[r].mesh_ext[2] = nz;
     hmesh[r].assign(values, values + (size_t)nx * ny * nz);
+    mesh_dirty = true;
     return NF_OK;
 }
 
@@ -459,7 +484,7 @@ nf_status Engine::rebuild_cells() {
     NF_CK(cudaMemsetAsync(ccount.p, 0, sizeof(uint32_t) * (ncell + 1), st));
     NF_CK(u32tmp.ensure(rod_slots + 1));
     if (rod_slots) {
-        k_rod_count<<<grid_for(rod_slots, 256), 256, 0, st>>>((uint32_t)rod_slots, R, rodoff.p, dcount.p, dreal.p,
+        NF_LAUNCH(k_rod_count, grid_for(rod_slots, 256), 256, 0, st)((uint32_t)rod_slots, R, rodoff.p, dcount.p, dreal.p,
                                                               pos.p, u32tmp.p, ccount.p);
         NF_CK(cudaGetLastError());
     }
@@ -467,7 +492,7 @@ nf_status Engine::rebuild_cells() {
     if (s != NF_OK) return s;
     NF_CK(cudaMemsetAsync(rcursor.p, 0, sizeof(uint32_t) * (ncell + 1), st));
     if (rod_slots) {
-        k_rod_scatter<<<grid_for(rod_slots, 256), 256, 0, st>>>((uint32_t)rod_slots, u32tmp.p, rstart.p, rcursor.p,
+        NF_LAUNCH(k_rod_scatter, grid_for(rod_slots, 256), 256, 0, st)((uint32_t)rod_slots, u32tmp.p, rstart.p, rcursor.p,
                                                                 pos.p, dir.p, spos.p, sdir.p, sid.p);
         NF_CK(cudaGetLastError());
     }
@@ -480,14 +505,18 @@ static nf_status setup_reals(Engine& E) {
     std::vector<uint32_t> mesh_off(E.R, 0);
     size_t mtot = 0;
     for (int r = 0; r < E.R; ++r) { mesh_off[r] = (uint32_t)mtot; mtot += E.hmesh[r].size(); }
-    cudaError_t e = E.mesh.ensure(mtot + 1);
-    if (e != cudaSuccess) return E.cuda_fail(e, "mesh alloc");
-    for (int r = 0; r < E.R; ++r)
+    cudaError_t e = cudaSuccess;
+    if (E.mesh_dirty || E.mesh.cap < mtot + 1) {
+        e = E.mesh.ensure(mtot + 1);
+        if (e != cudaSuccess) return E.cuda_fail(e, "mesh alloc");
+    }
+    for (int r = 0; r < E.R && E.mesh_dirty; ++r)
         if (!E.hmesh[r].empty()) {
             e = cudaMemcpyAsync(E.mesh.p + mesh_off[r], E.hmesh[r].data(), E.hmesh[r].size() * sizeof(float),
                                 cudaMemcpyHostToDevice, E.st);
             if (e != cudaSuccess) return E.cuda_fail(e, "mesh upload");
         }
+    E.mesh_dirty = false;
     E.hreal.resize(E.R);
     uint32_t coffs = 0;
     uint64_t roff = 0;
@@ -551,7 +580,7 @@ nf_status Engine::stream_dump(uint64_t k0, uint64_t n, float* host10) {
     if (s != NF_OK) return s;
     DBuf<float> o;
     NF_CK(o.ensure(10 * n + 1));
-    if (n) k_stream_dump<<<grid_for(n, 256), 256, 0, st>>>(dreal.p, k0, n, o.p);
+    if (n) NF_LAUNCH(k_stream_dump, grid_for(n, 256), 256, 0, st)(dreal.p, k0, n, o.p);
     NF_CK(cudaGetLastError());
     NF_CK(cudaMemcpyAsync(host10, o.p, sizeof(float) * 10 * n, cudaMemcpyDeviceToHost, st));
     NF_CK(cudaStreamSynchronize(st));
@@ -682,28 +711,34 @@ nf_status Engine::generate() {
         NF_CK(cudaMemcpyAsync(coff.p, hcoff.data(), sizeof(uint32_t) * (R + 1), cudaMemcpyHostToDevice, st));
         NF_CK(cudaMemcpyAsync(kbeg.p, hkbeg.data(), sizeof(uint64_t) * R, cudaMemcpyHostToDevice, st));
         const unsigned gs = grid_for(slots, 256);
-        k_stream_keep<<<gs, 256, 0, st>>>(dreal.p, R, coff.p, kbeg.p, (uint32_t)slots, keep.p);
+        tstart(KT_STREAM);
+        NF_LAUNCH(k_stream_keep, gs, 256, 0, st)(dreal.p, R, coff.p, kbeg.p, (uint32_t)slots, keep.p);
         NF_CK(cudaGetLastError());
+        tstop(KT_STREAM);
         NF_CK(cudaMemsetAsync(keep.p + slots, 0, sizeof(uint32_t), st));
         s = scan_u32(keep.p, kpos.p, slots + 1);  // kpos[slots] = compacted total
         if (s != NF_OK) return s;
         uint32_t* ntot = kpos.p + slots;
         NF_CK(cudaMemsetAsync(ccount.p, 0, sizeof(uint32_t) * (ncell + 1), st));
-        k_compact<<<gs, 256, 0, st>>>(dreal.p, R, coff.p, kbeg.p, (uint32_t)slots, keep.p, kpos.p, cpos.p, cdir.p,
+        NF_LAUNCH(k_compact, gs, 256, 0, st)(dreal.p, R, coff.p, kbeg.p, (uint32_t)slots, keep.p, kpos.p, cpos.p, cdir.p,
                                      csidx.p, creal.p, ccell.p, ccount.p, state.p);
         NF_CK(cudaGetLastError());
         s = scan_u32(ccount.p, cstart.p, ncell + 1);
         if (s != NF_OK) return s;
         NF_CK(cudaMemsetAsync(ccursor.p, 0, sizeof(uint32_t) * (ncell + 1), st));
-        k_bin<<<gs, 256, 0, st>>>((uint32_t)slots, ntot, ccell.p, cstart.p, ccursor.p, cperm.p);
+        NF_LAUNCH(k_bin, gs, 256, 0, st)((uint32_t)slots, ntot, ccell.p, cstart.p, ccursor.p, cperm.p);
         NF_CK(cudaGetLastError());
-        k_old_test<<<gs, 256, 0, st>>>(dreal.p, ntot, cperm.p, cpos.p, cdir.p, creal.p, rstart.p, spos.p, sdir.p,
+        tstart(KT_OLD);
+        NF_LAUNCH(k_old_test, gs, 256, 0, st)(dreal.p, ntot, cperm.p, cpos.p, cdir.p, creal.p, rstart.p, spos.p, sdir.p,
                                        total_rods() > 0 ? 1 : 0, state.p, ctr.p);
         NF_CK(cudaGetLastError());
+        tstop(KT_OLD);
         NF_CK(cudaMemsetAsync(ctr.p + C_OVERFLOW, 0, sizeof(unsigned long long), st));
-        k_conflicts<<<gs, 256, 0, st>>>(dreal.p, ntot, cperm.p, cstart.p, cpos.p, cdir.p, csidx.p, creal.p, state.p,
+        tstart(KT_CONF);
+        NF_LAUNCH(k_conflicts, gs, 256, 0, st)(dreal.p, ntot, cperm.p, cstart.p, cpos.p, cdir.p, csidx.p, creal.p, state.p,
                                         ccnt.p, clist.p, ctr.p);
         NF_CK(cudaGetLastError());
+        tstop(KT_CONF);
         unsigned long long ovf = 0;
         NF_CK(cudaMemcpyAsync(&ovf, ctr.p + C_OVERFLOW, sizeof(ovf), cudaMemcpyDeviceToHost, st));
         NF_CK(cudaStreamSynchronize(st));
@@ -718,34 +753,39 @@ nf_status Engine::generate() {
         for (;;) {
             NF_CK(cudaMemsetAsync(ctr.p + C_UNDECIDED, 0, sizeof(unsigned long long), st));
             for (int q = 0; q < 4; ++q)
-                k_resolve<<<gs, 256, 0, st>>>(ntot, state.p, ccnt.p, clist.p, ctr.p);
+                NF_LAUNCH(k_resolve, gs, 256, 0, st)(ntot, state.p, ccnt.p, clist.p, ctr.p);
             NF_CK(cudaGetLastError());
             passes += 4;
             // The last pass's undecided count: re-zero then one more pass.
             NF_CK(cudaMemsetAsync(ctr.p + C_UNDECIDED, 0, sizeof(unsigned long long), st));
-            k_resolve<<<gs, 256, 0, st>>>(ntot, state.p, ccnt.p, clist.p, ctr.p);
+            NF_LAUNCH(k_resolve, gs, 256, 0, st)(ntot, state.p, ccnt.p, clist.p, ctr.p);
             ++passes;
             unsigned long long und = 0;
             NF_CK(cudaMemcpyAsync(&und, ctr.p + C_UNDECIDED, sizeof(und), cudaMemcpyDeviceToHost, st));
             NF_CK(cudaStreamSynchronize(st));
             if (!und) break;
-            if (passes > slots + 8) { err = "conflict resolution did not converge"; return NF_ERR_TIMEOUT; }
+            if (passes > 4096) { err = "conflict resolution did not converge"; return NF_ERR_TIMEOUT; }
         }
         // Append.
-        k_accflag<<<grid_for(slots + 1, 256), 256, 0, st>>>(ntot, (uint32_t)(slots + 1), state.p, accf.p);
+        NF_LAUNCH(k_accflag, grid_for(slots + 1, 256), 256, 0, st)(ntot, (uint32_t)(slots + 1), state.p, accf.p);
         NF_CK(cudaGetLastError());
         s = scan_u32(accf.p, accpos.p, slots + 1);
         if (s != NF_OK) return s;
-        k_meta<<<grid_for(R, 128), 128, 0, st>>>(R, coff.p, keep.p, kpos.p, accf.p, accpos.p, meta.p);
+        NF_LAUNCH(k_meta, grid_for(R, 128), 128, 0, st)(R, coff.p, keep.p, kpos.p, accf.p, accpos.p, meta.p);
         NF_CK(cudaGetLastError());
         NF_CK(cudaMemsetAsync(recn.p, 0, sizeof(unsigned long long) * 2 * R, st));
-        k_append<<<gs, 256, 0, st>>>(ntot, state.p, creal.p, accpos.p, meta.p, rodoff.p, dcount.p, dreal.p, cpos.p,
+        NF_LAUNCH(k_append, gs, 256, 0, st)(ntot, state.p, creal.p, accpos.p, meta.p, rodoff.p, dcount.p, dreal.p, cpos.p,
                                      cdir.p, csidx.p, pos.p, dir.p, sidx.p, (uint64_t*)recn.p);
         NF_CK(cudaGetLastError());
         NF_CK(cudaMemcpyAsync(hmeta.data(), meta.p, sizeof(uint32_t) * 4 * R, cudaMemcpyDeviceToHost, st));
         NF_CK(cudaMemcpyAsync(hout.data(), recn.p, sizeof(uint64_t) * 2 * R, cudaMemcpyDeviceToHost, st));
         NF_CK(cudaStreamSynchronize(st));
         bool any_new = false;
+        {
+            double nc = 0;
+            for (int r = 0; r < R; ++r) nc += c_round[r] ? (double)(hmeta[4 * r + 1] - hmeta[4 * r + 0]) : 0.0;
+            tbytes(KT_OLD, 33.0 * nc + 32.0 * (double)total_rods(), 0);
+        }
         for (int r = 0; r < R; ++r) {
             if (!c_round[r]) continue;
             ++rounds_r[r];

@@ -348,13 +348,13 @@ nf_status Engine::solve() {
     NF_CK(cudaMemsetAsync(vsrc.p, 0, sizeof(double) * (nslot + 1), st));
     NF_CK(cudaMemsetAsync(vsnk.p, 0, sizeof(double) * (nslot + 1), st));
     NF_CK(cudaMemsetAsync(act + nslot, 0, sizeof(uint32_t), st));
-    k_uf_init<<<grid_for(nslot, 256), 256, 0, st>>>(nslot, parent.p, cflag.p);
+    NF_LAUNCH(k_uf_init, grid_for(nslot, 256), 256, 0, st)(nslot, parent.p, cflag.p);
     if (m) {
-        k_uf_union<<<grid_for(m, 256), 256, 0, st>>>(m, cI.p, cJ.p, parent.p, errw);
-        k_uf_flags<<<grid_for(m, 256), 256, 0, st>>>(m, cI.p, cJ.p, parent.p, cflag.p, errw);
-        k_elec_g<<<grid_for(m, 256), 256, 0, st>>>(m, cI.p, cJ.p, cG.p, vsrc.p, vsnk.p);
+        NF_LAUNCH(k_uf_union, grid_for(m, 256), 256, 0, st)(m, cI.p, cJ.p, parent.p, errw);
+        NF_LAUNCH(k_uf_flags, grid_for(m, 256), 256, 0, st)(m, cI.p, cJ.p, parent.p, cflag.p, errw);
+        NF_LAUNCH(k_elec_g, grid_for(m, 256), 256, 0, st)(m, cI.p, cJ.p, cG.p, vsrc.p, vsnk.p);
     }
-    k_active<<<grid_for(nslot, 256), 256, 0, st>>>(nslot, parent.p, cflag.p, act, errw);
+    NF_LAUNCH(k_active, grid_for(nslot, 256), 256, 0, st)(nslot, parent.p, cflag.p, act, errw);
     NF_CK(cudaGetLastError());
     nf_status s = scan_u32(act, aidx.p, nslot + 1);
     if (s != NF_OK) return s;
@@ -372,7 +372,7 @@ nf_status Engine::solve() {
     NF_CK(deg.ensure(na + 1));
     NF_CK(rowp.ensure(na + 1));
     NF_CK(cudaMemsetAsync(deg.p, 0, sizeof(uint32_t) * (na + 1), st));
-    if (m) k_deg<<<grid_for(m, 256), 256, 0, st>>>(m, cI.p, cJ.p, act, aidx.p, deg.p);
+    if (m) NF_LAUNCH(k_deg, grid_for(m, 256), 256, 0, st)(m, cI.p, cJ.p, act, aidx.p, deg.p);
     NF_CK(cudaGetLastError());
     s = scan_u32(deg.p, rowp.p, na + 1);
     if (s != NF_OK) return s;
@@ -389,8 +389,8 @@ nf_status Engine::solve() {
     NF_CK(cgred.ensure(na + 1));
     NF_CK(cgbuf.ensure(5 * (size_t)na + 5));
     NF_CK(cudaMemsetAsync(deg.p, 0, sizeof(uint32_t) * (na + 1), st));  // reuse as cursor
-    if (m) k_fill<<<grid_for(m, 256), 256, 0, st>>>(m, cI.p, cJ.p, cG.p, act, aidx.p, rowp.p, deg.p, col.p, val64.p);
-    k_rows<<<grid_for(nslot, 256), 256, 0, st>>>(nslot, act, aidx.p, rowp.p, col.p, val64.p, val32.p, vsrc.p,
+    if (m) NF_LAUNCH(k_fill, grid_for(m, 256), 256, 0, st)(m, cI.p, cJ.p, cG.p, act, aidx.p, rowp.p, deg.p, col.p, val64.p);
+    NF_LAUNCH(k_rows, grid_for(nslot, 256), 256, 0, st)(nslot, act, aidx.p, rowp.p, col.p, val64.p, val32.p, vsrc.p,
                                                  vsnk.p, diag64.p, diag32.p, bvec.p);
     NF_CK(cudaGetLastError());
     DBuf<uint32_t>& dab = rcur;  // per-realisation active base (R+1)
@@ -400,10 +400,12 @@ nf_status Engine::solve() {
     NF_CK(outs.ensure(R));
     const double tol = prm[0].solve_tol > 0 ? prm[0].solve_tol : 1e-10;
     const int max_inner = prm[0].solve_max_iter > 0 ? prm[0].solve_max_iter : 20000;
-    k_cg<512><<<R, 512, 0, st>>>(R, dab.p, rowp.p, col.p, val32.p, val64.p, diag32.p, diag64.p, bvec.p, xvec.p,
+    tstart(KT_CG);
+    NF_LAUNCH(k_cg<512>, R, 512, 0, st)(R, dab.p, rowp.p, col.p, val32.p, val64.p, diag32.p, diag64.p, bvec.p, xvec.p,
                                  cgred.p, cgbuf.p, tol, max_inner, outs.p);
     NF_CK(cudaGetLastError());
-    k_scatter_v<<<grid_for(nslot, 256), 256, 0, st>>>(nslot, act, aidx.p, xvec.p, parent.p, cflag.p, volt.p, errw);
+    tstop(KT_CG);
+    NF_LAUNCH(k_scatter_v, grid_for(nslot, 256), 256, 0, st)(nslot, act, aidx.p, xvec.p, parent.p, cflag.p, volt.p, errw);
     NF_CK(cudaGetLastError());
     std::vector<CgOut> ho(R);
     NF_CK(cudaMemcpyAsync(ho.data(), outs.p, sizeof(CgOut) * R, cudaMemcpyDeviceToHost, st));
@@ -414,6 +416,11 @@ nf_status Engine::solve() {
     NF_CK(cudaEventElapsedTime(&ms, e0, e1));
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
+    {
+        double it = 0, ot = 0;
+        for (int r = 0; r < R; ++r) { it += ho[r].inner; ot += ho[r].outer; }
+        tbytes(KT_CG, it * (8.0 * nnz + 24.0 * na) + ot * (12.0 * nnz + 40.0 * na), it * (2.0 * nnz + 10.0 * na));
+    }
     solve_st.assign(R, nf_solve_stats{});
     bool conv = true;
     for (int r = 0; r < R; ++r) {
@@ -504,7 +511,7 @@ nf_status Engine::adjoint(int r, float* dG_dend, size_t cap, double* dlam, doubl
     NF_CK(cudaMemsetAsync(g.p, 0, sizeof(double) * (6ull * n + 2), st));
     const uint32_t lo = (uint32_t)ct_off[r], hi = (uint32_t)ct_off[r + 1];
     if (hi > lo)
-        k_adjoint<<<grid_for(hi - lo, 256), 256, 0, st>>>(lo, hi, hreal[r].rod_off, dreal.p, (uint32_t)r, cI.p, cJ.p,
+        NF_LAUNCH(k_adjoint, grid_for(hi - lo, 256), 256, 0, st)(lo, hi, hreal[r].rod_off, dreal.p, (uint32_t)r, cI.p, cJ.p,
                                                           ct0.p, ct1.p, cD.p, cG.p, cimg.p, pos.p, dir.p, volt.p, g.p,
                                                           g.p + 6ull * n);
     NF_CK(cudaGetLastError());
