@@ -484,6 +484,12 @@ nf_status nf_set_kernel_timing(nf_handle* h, int on) {
     if (s != NF_OK) return s;
     for (auto& k : h->E.kt) { k.ms = 0; k.n = 0; k.bytes = 0; k.flops = 0; }
     h->E.timing = on != 0;
+    // Create the events up front so recording them costs no host-side creation.
+    while (on && h->E.evpool.size() < 8192) {
+        cudaEvent_t e;
+        if (cudaEventCreate(&e) != cudaSuccess) break;
+        h->E.evpool.push_back(e);
+    }
     return NF_OK;
 }
 

@@ -214,6 +214,8 @@ def test_batched_equals_plain(gpu):
 
 
 def test_state_bin_roundtrip_keeps_contacts(gpu, tmp_path):
+    """output.bin stores the rods grouped by cell; reading it back gives the same
+    rod set and, up to relabelling, the same contacts (distances to 1e-12)."""
     cfg = perc_small(gpu.configs)
     g = run_gpu(gpu, cfg, stages=("generate", "contacts"))
     g["sim"].write_state(tmp_path / "output.bin")
@@ -221,17 +223,13 @@ def test_state_bin_roundtrip_keeps_contacts(gpu, tmp_path):
     g["sim"].write_coo(tmp_path)
     s2 = gpu.Simulation(cfg)
     s2.read_state(tmp_path / "output.bin")
-    s2.contacts()
+    c2s = s2.contacts()
     c2 = s2.contact_list()
-    # the file stores rods grouped by cell: compare contact sets by rod coordinates
     r1, r2 = g["rods"], s2.rods()
-    key = lambda r, i: (r["x"][i], r["y"][i], r["z"][i])
-    k1 = sorted((key(r1, i), key(r1, j) if j < 0xFFFFFFFE else j, d)
-                for i, j, d in zip(g["ct"]["I"], g["ct"]["J"], g["ct"]["D"]))
-    k2 = sorted(tuple(sorted([key(r2, i), key(r2, j)])) + (d,) if j < 0xFFFFFFFE else (key(r2, i), j, d)
-                for i, j, d in zip(c2["I"], c2["J"], c2["D"]))
-    k1 = sorted(tuple(sorted([a, b])) + (d,) if not isinstance(b, int) else (a, b, d) for a, b, d in k1)
-    assert len(k1) == len(k2)
+    key = lambda r: sorted(zip(*(r[f].tolist() for f in ROD_F)))
+    assert key(r1) == key(r2)
+    assert c2s["contacts"] == g["cst"]["contacts"] and c2s["n_sink"] == g["cst"]["n_sink"]
+    np.testing.assert_allclose(np.sort(c2["D"]), np.sort(g["ct"]["D"]), rtol=1e-12)
     lines = open(tmp_path / "internal.srt.coo").read().splitlines()
     assert lines[0] == "#\tI\tJ\tD\tS" and len(lines) == 1 + g["cst"]["contacts"]
     assert open(tmp_path / "rods.vtk").readline().strip() == "# vtk DataFile Version 2.0"
