@@ -21,50 +21,65 @@
 #include <cstring>
 
 #include "nf_engine.cuh"
+#include "nf_tiles.cuh"
 
 namespace nf {
 
 static inline unsigned grid_for(size_t n, unsigned b) { return (unsigned)((n + b - 1) / b); }
 
 // ---------------------------------------------------------------------------
-// Pair sweep.
+// Pair sweep: one (rod chunk, stencil offset) per block, neighbour rods staged
+// in shared memory. Rod I records rods J > I (upper triangle).
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) k_ct_pairs(const Real* __restrict__ reals, int R,
-                                                  const uint32_t* __restrict__ rodoff, uint32_t nsorted,
-                                                  const uint32_t* __restrict__ rstart, const float4* __restrict__ spos,
-                                                  const float4* __restrict__ sdir, const uint32_t* __restrict__ sid,
-                                                  Rec* __restrict__ rec, unsigned long long cap,
-                                                  unsigned long long* __restrict__ recn, uint32_t* __restrict__ rcnt,
-                                                  unsigned long long* __restrict__ ctr) {
-    uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
+__global__ void __launch_bounds__(kTPB) k_ct_tiles(const Real* __restrict__ reals,
+                                                   const uint32_t* __restrict__ nchunk,
+                                                   const Chunk* __restrict__ chunks,
+                                                   const uint32_t* __restrict__ rstart,
+                                                   const float4* __restrict__ spos, const float4* __restrict__ sdir,
+                                                   const uint32_t* __restrict__ sid, Rec* __restrict__ rec,
+                                                   unsigned long long cap, unsigned long long* __restrict__ recn,
+                                                   uint32_t* __restrict__ rcnt, unsigned long long* __restrict__ ctr) {
+    __shared__ float4 tp[kTile], td[kTile];
+    __shared__ uint32_t ti[kTile];
+    const uint32_t ch = blockIdx.x;
+    if (ch >= *nchunk) return;
+    const Chunk C = chunks[ch];
+    const Real& Re = reals[C.real];
+    uint32_t nc;
+    int img[3];
+    if (!chunk_neighbour(Re, C.cell, (int)blockIdx.y, Re.per_con, &nc, img)) return;
+    const uint32_t t0 = rstart[nc], t1 = rstart[nc + 1];
+    if (t0 == t1) return;
+    const bool have = threadIdx.x < C.n;
+    const uint32_t q = C.first + threadIdx.x;
+    uint32_t i = 0;
+    float4 pA = make_float4(0, 0, 0, 0), cA = pA;
+    if (have) { i = sid[q]; pA = spos[q]; cA = sdir[q]; }
+    const float epc = 1e-6f;  // DEV_PRECISION (inc/definitions.h:5)
+    const float sx = img[0] * Re.L[0], sy = img[1] * Re.L[1], sz = img[2] * Re.L[2];
+    const double shx = img[0] * (double)Re.L[0], shy = img[1] * (double)Re.L[1], shz = img[2] * (double)Re.L[2];
     unsigned long long tests = 0, exact = 0, flips = 0;
-    if (q < nsorted) {
-        const uint32_t i = sid[q];
-        const float4 pA = spos[q], cA = sdir[q];
-        const int r = find_real(rodoff, R, i);
-        const Real& Re = reals[r];
-        const float epc = 1e-6f;  // DEV_PRECISION (inc/definitions.h:5)
-        int cc[3] = {cell_coord(Re, 0, pA.x), cell_coord(Re, 1, pA.y), cell_coord(Re, 2, pA.z)};
-        const RodD a = rodd(pA, cA);
-        uint32_t mine = 0;
-        for (int o = 0; o < 27; ++o) {
-            uint32_t cell;
-            int img[3];
-            if (!stencil(Re, cc, o, Re.per_con, &cell, img)) continue;
-            const float sx = img[0] * Re.L[0], sy = img[1] * Re.L[1], sz = img[2] * Re.L[2];
-            for (uint32_t p = rstart[cell], p1 = rstart[cell + 1]; p < p1; ++p) {
-                const uint32_t j = sid[p];
+    uint32_t mine = 0;
+    for (uint32_t base = t0; base < t1; base += kTile) {
+        const uint32_t m = min((uint32_t)kTile, t1 - base);
+        for (uint32_t k = threadIdx.x; k < m; k += kTPB) {
+            tp[k] = spos[base + k];
+            td[k] = sdir[base + k];
+            ti[k] = sid[base + k];
+        }
+        __syncthreads();
+        if (have) {
+            for (uint32_t k = 0; k < m; ++k) {
+                const uint32_t j = ti[k];
                 if (j <= i) continue;
-                const float4 pB = spos[p], cB = sdir[p];
+                const float4 pB = tp[k], cB = td[k];
                 ++tests;
                 const float thr = (cB.w + cA.w) + Re.cut + epc;
                 if (!maybe_near(pA, cA, pB, cB, sx, sy, sz, thr, epc, Re.slack)) continue;
                 ++exact;
-                const RodD b = rodd(pB, cB);
-                double t0, t1, u0, u1, Dx;
-                const double shx = img[0] * (double)Re.L[0], shy = img[1] * (double)Re.L[1],
-                             shz = img[2] * (double)Re.L[2];
-                double d = ref_distance_d(a, b, shx, shy, shz, (double)epc, false, &t0, &t1, &u0, &u1, &Dx);
+                const RodD a = rodd(pA, cA), b = rodd(pB, cB);
+                double t0d, t1d, u0, u1, Dx;
+                double d = ref_distance_d(a, b, shx, shy, shz, (double)epc, false, &t0d, &t1d, &u0, &u1, &Dx);
                 bool h = d < thresh_d(a.a, b.a, 1.0, (double)Re.cut, (double)epc);
                 if (ref_hit_f32(pA, cA, pB, cB, sx, sy, sz, epc, thr, false) != h) ++flips;
                 if (!h) continue;
@@ -79,13 +94,14 @@ __global__ void __launch_bounds__(256) k_ct_pairs(const Real* __restrict__ reals
                     x.img[2] = (int8_t)img[2];
                     x.img[3] = 0;
                     x.flags = 0;
-                    x.t0 = t0; x.t1 = t1; x.d = d; x.Dx = Dx; x.u0 = u0; x.u1 = u1;
+                    x.t0 = t0d; x.t1 = t1d; x.d = d; x.Dx = Dx; x.u0 = u0; x.u1 = u1;
                     rec[slot] = x;
                 }
             }
         }
-        if (mine) atomicAdd(&rcnt[i], mine);
+        __syncthreads();
     }
+    if (mine) atomicAdd(&rcnt[i], mine);
     warp_add_u64(&ctr[C_CT_PAIRS], tests);
     warp_add_u64(&ctr[C_CT_EXACT], exact);
     warp_add_u64(&ctr[C_CT_FLIPS], flips);
@@ -129,75 +145,131 @@ __global__ void k_rec_sort(uint32_t nslot, const uint32_t* __restrict__ rpos, co
 // is a virtual rod; the contact is dropped if any real rod crosses its body
 // (if_intersects with separation 0, then body_intersect on the unclamped
 // parameter along the virtual rod; src/core_cell_interaction_kernel.cu:141-146).
+// k_virt builds the virtual rods (FP64 record + FP32 copy) and bins them by
+// the cell of their centre wrapped into the box; k_scr_tiles tests them.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) k_screen(const Real* __restrict__ reals, int R,
-                                                const uint32_t* __restrict__ rodoff, uint32_t nrec,
-                                                Rec* __restrict__ rec, const float4* __restrict__ pos,
-                                                const float4* __restrict__ dir,
-                                                const uint32_t* __restrict__ rstart,
-                                                const float4* __restrict__ spos, const float4* __restrict__ sdir,
-                                                unsigned long long* __restrict__ ctr) {
+constexpr int kVD = 11;  // doubles per virtual rod: x y z cx cy cz l a, wrap shift x y z
+
+__global__ void k_virt(int R, const uint32_t* __restrict__ rodoff, uint32_t nrec, const Rec* __restrict__ rec,
+                       const float4* __restrict__ pos, const float4* __restrict__ dir,
+                       const Real* __restrict__ reals, double* __restrict__ vd, float4* __restrict__ vpf,
+                       float4* __restrict__ vdf, uint32_t* __restrict__ vcell, uint32_t* __restrict__ vcount) {
     uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
-    unsigned long long tests = 0, exact = 0;
-    if (q < nrec) {
-        Rec x = rec[q];
-        const int r = find_real(rodoff, R, x.i);
-        const Real& Re = reals[r];
-        const double eps = (double)1e-6f;
-        const RodD A = rodd(pos[x.i], dir[x.i]);
-        const RodD B = rodd(pos[x.j], dir[x.j]);
-        const double sh[3] = {x.img[0] * (double)Re.L[0], x.img[1] * (double)Re.L[1], x.img[2] * (double)Re.L[2]};
-        const double p0[3] = {dadd(A.x, dmul(x.t0, A.cx)), dadd(A.y, dmul(x.t0, A.cy)), dadd(A.z, dmul(x.t0, A.cz))};
-        const double p1[3] = {dadd(dadd(B.x, sh[0]), dmul(x.t1, B.cx)), dadd(dadd(B.y, sh[1]), dmul(x.t1, B.cy)),
-                              dadd(dadd(B.z, sh[2]), dmul(x.t1, B.cz))};
-        double vr[3], vc[3];
+    if (q >= nrec) return;
+    const Rec x = rec[q];
+    const int r = find_real(rodoff, R, x.i);
+    const Real& Re = reals[r];
+    const RodD A = rodd(pos[x.i], dir[x.i]);
+    const RodD B = rodd(pos[x.j], dir[x.j]);
+    const double sh[3] = {x.img[0] * (double)Re.L[0], x.img[1] * (double)Re.L[1], x.img[2] * (double)Re.L[2]};
+    const double p0[3] = {dadd(A.x, dmul(x.t0, A.cx)), dadd(A.y, dmul(x.t0, A.cy)), dadd(A.z, dmul(x.t0, A.cz))};
+    const double p1[3] = {dadd(dadd(B.x, sh[0]), dmul(x.t1, B.cx)), dadd(dadd(B.y, sh[1]), dmul(x.t1, B.cy)),
+                          dadd(dadd(B.z, sh[2]), dmul(x.t1, B.cz))};
+    double vr[3], vc[3];
+    for (int d = 0; d < 3; ++d) {
+        vr[d] = dmul(dadd(p0[d], p1[d]), 0.5);
+        vc[d] = dsub(p1[d], p0[d]);
+    }
+    double vl = dsqrt(dadd(dadd(dmul(vc[0], vc[0]), dmul(vc[1], vc[1])), dmul(vc[2], vc[2])));
+    if (!(vl > 0)) { vcell[q] = 0xffffffffu; return; }
+    double inv = ddiv(1.0, vl);
+    for (int d = 0; d < 3; ++d) vc[d] = dmul(vc[d], inv);
+    const double va = fmin(A.a, B.a);
+    double vw[3];
+    for (int d = 0; d < 3; ++d) {
+        double xw = vr[d];
+        if (Re.per_con & (1 << d)) {
+            xw = fmod(xw, (double)Re.L[d]);
+            if (xw < 0) xw = dadd(xw, (double)Re.L[d]);
+        }
+        vw[d] = xw;
+    }
+    double* o = vd + (size_t)kVD * q;
+    o[0] = vr[0]; o[1] = vr[1]; o[2] = vr[2];
+    o[3] = vc[0]; o[4] = vc[1]; o[5] = vc[2];
+    o[6] = vl; o[7] = va;
+    o[8] = dsub(vw[0], vr[0]); o[9] = dsub(vw[1], vr[1]); o[10] = dsub(vw[2], vr[2]);
+    vpf[q] = make_float4((float)vr[0], (float)vr[1], (float)vr[2], (float)vl);
+    vdf[q] = make_float4((float)vc[0], (float)vc[1], (float)vc[2], (float)va);
+    const uint32_t cell = cell_of(Re, (float)vw[0], (float)vw[1], (float)vw[2]);
+    vcell[q] = cell;
+    atomicAdd(&vcount[cell], 1u);
+}
+
+__global__ void k_vbin(uint32_t n, const uint32_t* __restrict__ cellof, const uint32_t* __restrict__ start,
+                       uint32_t* __restrict__ cursor, uint32_t* __restrict__ perm) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    uint32_t cell = cellof[i];
+    if (cell == 0xffffffffu) return;  // zero-length segment: never screened
+    perm[start[cell] + atomicAdd(&cursor[cell], 1u)] = i;
+}
+
+__global__ void __launch_bounds__(kTPB) k_scr_tiles(const Real* __restrict__ reals,
+                                                    const uint32_t* __restrict__ nchunk,
+                                                    const Chunk* __restrict__ chunks,
+                                                    const uint32_t* __restrict__ vperm,
+                                                    const double* __restrict__ vd, const float4* __restrict__ vpf,
+                                                    const float4* __restrict__ vdf,
+                                                    const uint32_t* __restrict__ rstart,
+                                                    const float4* __restrict__ spos, const float4* __restrict__ sdir,
+                                                    Rec* rec, unsigned long long* __restrict__ ctr) {
+    __shared__ float4 tp[kTile], td[kTile];
+    const uint32_t ch = blockIdx.x;
+    if (ch >= *nchunk) return;
+    const Chunk C = chunks[ch];
+    const Real& Re = reals[C.real];
+    uint32_t nc;
+    int img[3];
+    if (!chunk_neighbour(Re, C.cell, (int)blockIdx.y, Re.per_con, &nc, img)) return;
+    const uint32_t t0 = rstart[nc], t1 = rstart[nc + 1];
+    if (t0 == t1) return;
+    const bool have = threadIdx.x < C.n;
+    const uint32_t id = have ? vperm[C.first + threadIdx.x] : 0u;
+    volatile uint32_t* vflag = have ? &rec[id].flags : nullptr;
+    RodD V{};
+    double sv[3] = {0, 0, 0};
+    float4 pV = make_float4(0, 0, 0, 0), cV = pV;
+    float svf[3] = {0, 0, 0};
+    bool alive = have && !(*vflag & 1u);
+    if (have) {
+        const double* o = vd + (size_t)kVD * id;
+        V = RodD{o[0], o[1], o[2], o[3], o[4], o[5], o[6], o[7]};
         for (int d = 0; d < 3; ++d) {
-            vr[d] = dmul(dadd(p0[d], p1[d]), 0.5);
-            vc[d] = dsub(p1[d], p0[d]);
+            sv[d] = dsub(o[8 + d], img[d] * (double)Re.L[d]);
+            svf[d] = (float)sv[d];
         }
-        double vl = dsqrt(dadd(dadd(dmul(vc[0], vc[0]), dmul(vc[1], vc[1])), dmul(vc[2], vc[2])));
-        bool hit = false;
-        if (vl > 0) {
-            double inv = ddiv(1.0, vl);
-            for (int d = 0; d < 3; ++d) vc[d] = dmul(vc[d], inv);
-            const double va = fmin(A.a, B.a);
-            RodD V{vr[0], vr[1], vr[2], vc[0], vc[1], vc[2], vl, va};
-            double vw[3];
-            int cc[3];
-            for (int d = 0; d < 3; ++d) {
-                double xw = vr[d];
-                if (Re.per_con & (1 << d)) {
-                    xw = fmod(xw, (double)Re.L[d]);
-                    if (xw < 0) xw = dadd(xw, (double)Re.L[d]);
-                }
-                vw[d] = xw;
-                cc[d] = cell_coord(Re, d, (float)xw);
-            }
-            const float4 pV = make_float4((float)vr[0], (float)vr[1], (float)vr[2], (float)vl);
-            const float4 cV = make_float4((float)vc[0], (float)vc[1], (float)vc[2], (float)va);
-            const float epsf = 1e-6f;
-            for (int o = 0; o < 27 && !hit; ++o) {
-                uint32_t cell;
-                int img[3];
-                if (!stencil(Re, cc, o, Re.per_con, &cell, img)) continue;
-                double sv[3];
-                for (int d = 0; d < 3; ++d) sv[d] = dsub(dsub(vw[d], vr[d]), img[d] * (double)Re.L[d]);
-                const float svf[3] = {(float)sv[0], (float)sv[1], (float)sv[2]};
-                for (uint32_t p = rstart[cell], p1e = rstart[cell + 1]; p < p1e; ++p) {
-                    const float4 pR = spos[p], cR = sdir[p];
-                    ++tests;
-                    const float thr = (cV.w + cR.w) + epsf;
-                    if (!maybe_near(pR, cR, pV, cV, svf[0], svf[1], svf[2], thr, epsf, Re.slack)) continue;
-                    ++exact;
-                    const RodD Rr = rodd(pR, cR);
-                    double u1, t0, t1, u0;
-                    double d = ref_distance_d(Rr, V, sv[0], sv[1], sv[2], eps, false, &t0, &t1, &u0, &u1, nullptr);
-                    bool h = d < thresh_d(Rr.a, V.a, 1.0, 0.0, eps);
-                    if (h && dsub(ddiv(V.l, 2.0), dabs(u1)) > dadd(V.a, eps)) { hit = true; break; }
+        pV = vpf[id];
+        cV = vdf[id];
+    }
+    const double eps = (double)1e-6f;
+    const float epsf = 1e-6f;
+    unsigned long long tests = 0, exact = 0;
+    for (uint32_t base = t0; base < t1; base += kTile) {
+        if (!__syncthreads_or(alive)) break;
+        const uint32_t m = min((uint32_t)kTile, t1 - base);
+        for (uint32_t k = threadIdx.x; k < m; k += kTPB) { tp[k] = spos[base + k]; td[k] = sdir[base + k]; }
+        __syncthreads();
+        if (alive) {
+            for (uint32_t k = 0; k < m; ++k) {
+                const float4 pR = tp[k], cR = td[k];
+                ++tests;
+                const float thr = (cV.w + cR.w) + epsf;
+                if (!maybe_near(pR, cR, pV, cV, svf[0], svf[1], svf[2], thr, epsf, Re.slack)) continue;
+                ++exact;
+                const RodD Rr = rodd(pR, cR);
+                double u1, t0d, t1d, u0;
+                double d = ref_distance_d(Rr, V, sv[0], sv[1], sv[2], eps, false, &t0d, &t1d, &u0, &u1, nullptr);
+                bool h = d < thresh_d(Rr.a, V.a, 1.0, 0.0, eps);
+                if (h && dsub(ddiv(V.l, 2.0), dabs(u1)) > dadd(V.a, eps)) {
+                    atomicOr(&rec[id].flags, 1u);
+                    alive = false;
+                    break;
                 }
             }
+            if (alive && (*vflag & 1u)) alive = false;  // decided by another block
         }
-        if (hit) rec[q].flags |= 1u;
+        __syncthreads();
     }
     warp_add_u64(&ctr[C_SCR_PAIRS], tests);
     warp_add_u64(&ctr[C_SCR_EXACT], exact);
@@ -405,14 +477,17 @@ nf_status Engine::contacts() {
     NF_CK(rcur.ensure(nslot + 1));
     NF_CK(recn.ensure(2 * R + 2));
     size_t cap = std::max<size_t>(rec.cap, std::max<size_t>(4096, 2 * nrods));
+    nf_status s = build_chunks(rstart.p, nrods);
+    if (s != NF_OK) return s;
+    const dim3 tg(grid_for(nrods, kTPB) + ncell, 27);
     for (int attempt = 0; attempt < 2; ++attempt) {
         NF_CK(rec.ensure(cap));
         NF_CK(cudaMemsetAsync(rcnt.p, 0, sizeof(uint32_t) * (nslot + 1), st));
         NF_CK(cudaMemsetAsync(recn.p, 0, sizeof(unsigned long long), st));
         tstart(KT_CTPAIRS);
         if (nrods)
-            NF_LAUNCH(k_ct_pairs, grid_for(nrods, 256), 256, 0, st)(dreal.p, R, rodoff.p, (uint32_t)nrods, rstart.p, spos.p,
-                                                            sdir.p, sid.p, rec.p, rec.cap, recn.p, rcnt.p, ctr.p);
+            NF_LAUNCH(k_ct_tiles, tg, kTPB, 0, st)(dreal.p, choff.p + ncell, chunks.p, rstart.p, spos.p, sdir.p, sid.p,
+                                                   rec.p, rec.cap, recn.p, rcnt.p, ctr.p);
         NF_CK(cudaGetLastError());
         tstop(KT_CTPAIRS);
         unsigned long long n = 0;
@@ -424,7 +499,7 @@ nf_status Engine::contacts() {
     }
     const uint32_t nrec = (uint32_t)cap;
     NF_CK(rec2.ensure(nrec + 1));
-    nf_status s = scan_u32(rcnt.p, rpos.p, nslot + 1);
+    s = scan_u32(rcnt.p, rpos.p, nslot + 1);
     if (s != NF_OK) return s;
     NF_CK(cudaMemsetAsync(rcur.p, 0, sizeof(uint32_t) * (nslot + 1), st));
     if (nrec) {
@@ -433,12 +508,31 @@ nf_status Engine::contacts() {
         NF_LAUNCH(k_rec_sort, grid_for(nslot, 256), 256, 0, st)(nslot, rpos.p, rcnt.p, rec2.p);
         NF_CK(cudaGetLastError());
         if (prm[0].screening) {
+            NF_CK(vdbl.ensure((size_t)kVD * nrec));
+            NF_CK(vpf.ensure(nrec));
+            NF_CK(vdf.ensure(nrec));
+            NF_CK(vcell.ensure(nrec));
+            NF_CK(vperm.ensure(nrec));
+            NF_CK(vstart.ensure(ncell + 1));
+            NF_CK(vcur.ensure(ncell + 1));
+            NF_CK(cudaMemsetAsync(vcur.p, 0, sizeof(uint32_t) * (ncell + 1), st));
             tstart(KT_SCREEN);
-            NF_LAUNCH(k_screen, grid_for(nrec, 256), 256, 0, st)(dreal.p, R, rodoff.p, nrec, rec2.p, pos.p, dir.p, rstart.p,
-                                                         spos.p, sdir.p, ctr.p);
+            NF_LAUNCH(k_virt, grid_for(nrec, 256), 256, 0, st)(R, rodoff.p, nrec, rec2.p, pos.p, dir.p, dreal.p, vdbl.p,
+                                                               vpf.p, vdf.p, vcell.p, vcur.p);
+            NF_CK(cudaGetLastError());
+            s = scan_u32(vcur.p, vstart.p, ncell + 1);
+            if (s != NF_OK) return s;
+            NF_CK(cudaMemsetAsync(vcur.p, 0, sizeof(uint32_t) * (ncell + 1), st));
+            NF_LAUNCH(k_vbin, grid_for(nrec, 256), 256, 0, st)(nrec, vcell.p, vstart.p, vcur.p, vperm.p);
+            NF_CK(cudaGetLastError());
+            s = build_chunks(vstart.p, nrec);
+            if (s != NF_OK) return s;
+            const dim3 vg(grid_for(nrec, kTPB) + ncell, 27);
+            NF_LAUNCH(k_scr_tiles, vg, kTPB, 0, st)(dreal.p, choff.p + ncell, chunks.p, vperm.p, vdbl.p, vpf.p, vdf.p,
+                                                    rstart.p, spos.p, sdir.p, rec2.p, ctr.p);
             NF_CK(cudaGetLastError());
             tstop(KT_SCREEN);
-            tbytes(KT_SCREEN, 68.0 * nrec, 0);
+            tbytes(KT_SCREEN, 64.0 * nrec + 32.0 * nrods, 0);
         }
     }
     // Counts per realisation.

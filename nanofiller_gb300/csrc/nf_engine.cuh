@@ -21,6 +21,7 @@
 
 #include "../../include/nanofiller_gb300.h"
 #include "nf_common.cuh"
+#include "nf_tiles.cuh"
 
 namespace nf {
 
@@ -116,6 +117,9 @@ struct Engine {
     DBuf<uint32_t> coff, keep, kpos, ccount, cstart, ccursor, cperm, creal, ccell, ccnt, clist, accf, accpos;
     DBuf<uint64_t> kbeg, csidx;
     DBuf<float4> cpos, cdir;
+    DBuf<float4> gpos, gdir;     // candidates in cell order
+    DBuf<Chunk> chunks;          // (cell, probe range) work table of the pair kernels
+    DBuf<uint32_t> nch, choff, celloff;
     DBuf<uint8_t> state;
     DBuf<uint32_t> meta;   // per-realisation round metadata
     DBuf<unsigned long long> ctr;
@@ -135,6 +139,11 @@ struct Engine {
     std::vector<uint64_t> ct_int, ct_snk, ct_src, ct_scr;
     bool contacts_valid = false;
     DBuf<uint32_t> eflag;
+    // virtual rods of the screening test: FP32 copies for the filter, FP64
+    // record (x,y,z,cx,cy,cz,l,a, wrap shift x,y,z), cell binning
+    DBuf<float4> vpf, vdf;
+    DBuf<double> vdbl;
+    DBuf<uint32_t> vcell, vperm, vstart, vcur;
 
     // solve
     DBuf<double> vsrc, vsnk, volt;
@@ -168,6 +177,7 @@ struct Engine {
 
     // helpers
     nf_status scan_u32(const uint32_t* in, uint32_t* out, size_t n);
+    nf_status build_chunks(const uint32_t* pstart, size_t nprobes);
     uint64_t total_rods() const;
 };
 

@@ -28,6 +28,7 @@
 #include <cub/device/device_scan.cuh>
 
 #include "nf_engine.cuh"
+#include "nf_tiles.cuh"
 
 namespace nf {
 
@@ -163,7 +164,7 @@ __global__ void k_compact(const Real* __restrict__ reals, int R, const uint32_t*
     creal[c] = (uint32_t)r;
     uint32_t cell = cell_of(Re, p.x, p.y, p.z);
     ccell[c] = cell;
-    state[c] = ST_NONE;
+    state[c] = ST_ALIVE;
     atomicAdd(&ccount[cell], 1u);
 }
 
@@ -178,104 +179,135 @@ __global__ void k_bin(uint32_t n, const uint32_t* __restrict__ ntot, const uint3
     perm[q] = i;
 }
 
-// Candidate vs accepted rods of the 27 neighbour cells (cuda_OldExtIsectLB's job).
-__global__ void __launch_bounds__(256) k_old_test(const Real* __restrict__ reals, const uint32_t* __restrict__ ntot,
-                                                  const uint32_t* __restrict__ cperm, const float4* __restrict__ cpos,
-                                                  const float4* __restrict__ cdir, const uint32_t* __restrict__ creal,
-                                                  const uint32_t* __restrict__ rstart, const float4* __restrict__ spos,
-                                                  const float4* __restrict__ sdir, int have_rods,
-                                                  uint8_t* __restrict__ state, unsigned long long* __restrict__ ctr) {
-    uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-    bool active = t < *ntot;
+// Candidate vs accepted rods of one neighbour cell (cuda_OldExtIsectLB's job),
+// one (candidate chunk, stencil offset) per block, targets staged in shared memory.
+__global__ void __launch_bounds__(kTPB) k_old_tiles(const Real* __restrict__ reals,
+                                                    const uint32_t* __restrict__ nchunk,
+                                                    const Chunk* __restrict__ chunks,
+                                                    const uint32_t* __restrict__ cperm,
+                                                    const float4* __restrict__ gpos, const float4* __restrict__ gdir,
+                                                    const uint32_t* __restrict__ rstart,
+                                                    const float4* __restrict__ spos, const float4* __restrict__ sdir,
+                                                    uint8_t* state, unsigned long long* __restrict__ ctr) {
+    __shared__ float4 tp[kTile], td[kTile];
+    const uint32_t ch = blockIdx.x;
+    if (ch >= *nchunk) return;
+    const Chunk C = chunks[ch];
+    const Real& Re = reals[C.real];
+    uint32_t nc;
+    int img[3];
+    if (!chunk_neighbour(Re, C.cell, (int)blockIdx.y, Re.per_gen, &nc, img)) return;
+    const uint32_t t0 = rstart[nc], t1 = rstart[nc + 1];
+    if (t0 == t1) return;
+    volatile uint8_t* vst = state;
+    const bool have = threadIdx.x < C.n;
+    const uint32_t q = C.first + threadIdx.x;
+    const uint32_t cid = have ? cperm[q] : 0u;
+    float4 pA = make_float4(0, 0, 0, 0), cA = pA;
+    if (have) { pA = gpos[q]; cA = gdir[q]; }
+    bool alive = have && vst[cid] != ST_REJ_OLD;
+    const float sx = img[0] * Re.L[0], sy = img[1] * Re.L[1], sz = img[2] * Re.L[2];
+    const double shx = img[0] * (double)Re.L[0], shy = img[1] * (double)Re.L[1], shz = img[2] * (double)Re.L[2];
     unsigned long long tests = 0, exact = 0, flips = 0;
-    if (active) {
-        uint32_t c = cperm[t];
-        const float4 pA = cpos[c], cA = cdir[c];
-        const Real& Re = reals[creal[c]];
-        bool hit = false;
-        if (have_rods) {
-            int cc[3] = {cell_coord(Re, 0, pA.x), cell_coord(Re, 1, pA.y), cell_coord(Re, 2, pA.z)};
-            const RodD a = rodd(pA, cA);
-            for (int o = 0; o < 27 && !hit; ++o) {
-                uint32_t cell;
-                int img[3];
-                if (!stencil(Re, cc, o, Re.per_gen, &cell, img)) continue;
-                const float sx = img[0] * Re.L[0], sy = img[1] * Re.L[1], sz = img[2] * Re.L[2];
-                const uint32_t b0 = rstart[cell], b1 = rstart[cell + 1];
-                for (uint32_t j = b0; j < b1; ++j) {
-                    const float4 pB = spos[j], cB = sdir[j];
-                    ++tests;
-                    const float thr = (cB.w + cA.w) * Re.scf + Re.sep + Re.eps;
-                    if (!maybe_near(pA, cA, pB, cB, sx, sy, sz, thr, Re.eps, Re.slack)) continue;
-                    ++exact;
-                    const RodD b = rodd(pB, cB);
-                    double d = ref_distance_d(a, b, img[0] * (double)Re.L[0], img[1] * (double)Re.L[1],
-                                              img[2] * (double)Re.L[2], (double)Re.eps, Re.typo != 0,
-                                              nullptr, nullptr, nullptr, nullptr, nullptr);
-                    bool h = d < thresh_d(a.a, b.a, (double)Re.scf, (double)Re.sep, (double)Re.eps);
-                    if (ref_hit_f32(pA, cA, pB, cB, sx, sy, sz, Re.eps, thr, Re.typo != 0) != h) ++flips;
-                    if (h) { hit = true; break; }
-                }
+    for (uint32_t base = t0; base < t1; base += kTile) {
+        if (!__syncthreads_or(alive)) break;
+        const uint32_t m = min((uint32_t)kTile, t1 - base);
+        for (uint32_t k = threadIdx.x; k < m; k += kTPB) { tp[k] = spos[base + k]; td[k] = sdir[base + k]; }
+        __syncthreads();
+        if (alive) {
+            for (uint32_t k = 0; k < m; ++k) {
+                const float4 pB = tp[k], cB = td[k];
+                ++tests;
+                const float thr = (cB.w + cA.w) * Re.scf + Re.sep + Re.eps;
+                if (!maybe_near(pA, cA, pB, cB, sx, sy, sz, thr, Re.eps, Re.slack)) continue;
+                ++exact;
+                const RodD a = rodd(pA, cA), b = rodd(pB, cB);
+                double d = ref_distance_d(a, b, shx, shy, shz, (double)Re.eps, Re.typo != 0, nullptr, nullptr,
+                                          nullptr, nullptr, nullptr);
+                bool h = d < thresh_d(a.a, b.a, (double)Re.scf, (double)Re.sep, (double)Re.eps);
+                if (ref_hit_f32(pA, cA, pB, cB, sx, sy, sz, Re.eps, thr, Re.typo != 0) != h) ++flips;
+                if (h) { vst[cid] = ST_REJ_OLD; alive = false; break; }
             }
+            if (alive && vst[cid] == ST_REJ_OLD) alive = false;  // decided by another block
         }
-        state[c] = hit ? ST_REJ_OLD : ST_ALIVE;
+        __syncthreads();
     }
     warp_add_u64(&ctr[C_PAIR_TESTS], tests);
     warp_add_u64(&ctr[C_EXACT], exact);
     warp_add_u64(&ctr[C_FLIPS], flips);
 }
 
-// Earlier surviving candidates of the same round that a survivor hits.
-__global__ void __launch_bounds__(256) k_conflicts(const Real* __restrict__ reals, const uint32_t* __restrict__ ntot,
-                                                   const uint32_t* __restrict__ cperm, const uint32_t* __restrict__ cstart,
-                                                   const float4* __restrict__ cpos, const float4* __restrict__ cdir,
-                                                   const uint64_t* __restrict__ csidx, const uint32_t* __restrict__ creal,
-                                                   const uint8_t* __restrict__ state, uint32_t* __restrict__ ccnt,
-                                                   uint32_t* __restrict__ clist, unsigned long long* __restrict__ ctr) {
-    uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-    bool active = t < *ntot;
-    unsigned long long tests = 0, exact = 0, flips = 0;
-    if (active) {
-        uint32_t c = cperm[t];
-        uint32_t n = 0;
-        if (state[c] == ST_ALIVE) {
-            const float4 pA = cpos[c], cA = cdir[c];
-            const uint64_t kA = csidx[c];
-            const Real& Re = reals[creal[c]];
-            int cc[3] = {cell_coord(Re, 0, pA.x), cell_coord(Re, 1, pA.y), cell_coord(Re, 2, pA.z)};
-            const RodD a = rodd(pA, cA);
-            for (int o = 0; o < 27; ++o) {
-                uint32_t cell;
-                int img[3];
-                if (!stencil(Re, cc, o, Re.per_gen, &cell, img)) continue;
-                const float sx = img[0] * Re.L[0], sy = img[1] * Re.L[1], sz = img[2] * Re.L[2];
-                for (uint32_t q = cstart[cell], q1 = cstart[cell + 1]; q < q1; ++q) {
-                    uint32_t j = cperm[q];
-                    if (csidx[j] >= kA || state[j] != ST_ALIVE) continue;
-                    const float4 pB = cpos[j], cB = cdir[j];
+// Earlier surviving candidates of one neighbour cell that a survivor hits.
+__global__ void __launch_bounds__(kTPB) k_conf_tiles(const Real* __restrict__ reals,
+                                                     const uint32_t* __restrict__ nchunk,
+                                                     const Chunk* __restrict__ chunks,
+                                                     const uint32_t* __restrict__ cperm,
+                                                     const uint32_t* __restrict__ cstart,
+                                                     const float4* __restrict__ gpos, const float4* __restrict__ gdir,
+                                                     const uint64_t* __restrict__ csidx,
+                                                     const uint8_t* __restrict__ state, uint32_t* __restrict__ ccnt,
+                                                     uint32_t* __restrict__ clist, unsigned long long* __restrict__ ctr) {
+    __shared__ float4 tp[kTile], td[kTile];
+    __shared__ uint64_t tk[kTile];
+    __shared__ uint32_t ti[kTile];
+    const uint32_t ch = blockIdx.x;
+    if (ch >= *nchunk) return;
+    const Chunk C = chunks[ch];
+    const Real& Re = reals[C.real];
+    uint32_t nc;
+    int img[3];
+    if (!chunk_neighbour(Re, C.cell, (int)blockIdx.y, Re.per_gen, &nc, img)) return;
+    const uint32_t t0 = cstart[nc], t1 = cstart[nc + 1];
+    if (t0 == t1) return;
+    const bool have = threadIdx.x < C.n;
+    const uint32_t q = C.first + threadIdx.x;
+    const uint32_t cid = have ? cperm[q] : 0u;
+    float4 pA = make_float4(0, 0, 0, 0), cA = pA;
+    uint64_t kA = 0;
+    bool alive = have && state[cid] == ST_ALIVE;
+    if (alive) { pA = gpos[q]; cA = gdir[q]; kA = csidx[cid]; }
+    const float sx = img[0] * Re.L[0], sy = img[1] * Re.L[1], sz = img[2] * Re.L[2];
+    const double shx = img[0] * (double)Re.L[0], shy = img[1] * (double)Re.L[1], shz = img[2] * (double)Re.L[2];
+    unsigned long long tests = 0, exact = 0, flips = 0, ovf = 0;
+    if (__syncthreads_or(alive)) {
+        for (uint32_t base = t0; base < t1; base += kTile) {
+            const uint32_t m = min((uint32_t)kTile, t1 - base);
+            for (uint32_t k = threadIdx.x; k < m; k += kTPB) {
+                const uint32_t j = cperm[base + k];
+                tp[k] = gpos[base + k];
+                td[k] = gdir[base + k];
+                ti[k] = j;
+                // only earlier survivors matter: fold both conditions into the key
+                tk[k] = state[j] == ST_ALIVE ? csidx[j] : ~0ull;
+            }
+            __syncthreads();
+            if (alive) {
+                for (uint32_t k = 0; k < m; ++k) {
+                    if (tk[k] >= kA) continue;
+                    const float4 pB = tp[k], cB = td[k];
                     ++tests;
                     const float thr = (cB.w + cA.w) * Re.scf + Re.sep + Re.eps;
                     if (!maybe_near(pA, cA, pB, cB, sx, sy, sz, thr, Re.eps, Re.slack)) continue;
                     ++exact;
-                    const RodD b = rodd(pB, cB);
-                    double d = ref_distance_d(a, b, img[0] * (double)Re.L[0], img[1] * (double)Re.L[1],
-                                              img[2] * (double)Re.L[2], (double)Re.eps, Re.typo != 0,
-                                              nullptr, nullptr, nullptr, nullptr, nullptr);
+                    const RodD a = rodd(pA, cA), b = rodd(pB, cB);
+                    double d = ref_distance_d(a, b, shx, shy, shz, (double)Re.eps, Re.typo != 0, nullptr,
+                                              nullptr, nullptr, nullptr, nullptr);
                     bool h = d < thresh_d(a.a, b.a, (double)Re.scf, (double)Re.sep, (double)Re.eps);
                     if (ref_hit_f32(pA, cA, pB, cB, sx, sy, sz, Re.eps, thr, Re.typo != 0) != h) ++flips;
                     if (h) {
-                        if (n < (uint32_t)kConflictCap) clist[(size_t)c * kConflictCap + n] = j;
-                        ++n;
+                        uint32_t slot = atomicAdd(&ccnt[cid], 1u);
+                        if (slot < (uint32_t)kConflictCap) clist[(size_t)cid * kConflictCap + slot] = ti[k];
+                        else ++ovf;
                     }
                 }
             }
+            __syncthreads();
         }
-        ccnt[c] = n;
-        if (n > (uint32_t)kConflictCap) atomicAdd(&ctr[C_OVERFLOW], 1ull);
     }
     warp_add_u64(&ctr[C_PAIR_TESTS], tests);
     warp_add_u64(&ctr[C_EXACT], exact);
     warp_add_u64(&ctr[C_FLIPS], flips);
+    warp_add_u64(&ctr[C_OVERFLOW], ovf);
 }
 
 // One pass of the in-order resolution.
@@ -416,6 +448,33 @@ nf_status Engine::tresolve() {
     return NF_OK;
 }
 
+__global__ void k_gather_pd(uint32_t n, const uint32_t* __restrict__ ntot, const uint32_t* __restrict__ perm,
+                            const float4* __restrict__ pos, const float4* __restrict__ dir,
+                            float4* __restrict__ opos, float4* __restrict__ odir) {
+    uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
+    uint32_t m = ntot ? *ntot : n;
+    if (q >= m) return;
+    uint32_t i = perm[q];
+    opos[q] = pos[i];
+    odir[q] = dir[i];
+}
+
+// Chunk table over the cell CSR pstart (ncell + 1 entries); the chunk total is
+// left on the device at choff[ncell].
+nf_status Engine::build_chunks(const uint32_t* pstart, size_t nprobes) {
+    NF_CK(nch.ensure(ncell + 1));
+    NF_CK(choff.ensure(ncell + 1));
+    NF_LAUNCH(k_chunk_count, grid_for(ncell + 1, 256), 256, 0, st)(ncell, pstart, nch.p);
+    NF_CK(cudaGetLastError());
+    nf_status s = scan_u32(nch.p, choff.p, ncell + 1);
+    if (s != NF_OK) return s;
+    // Upper bound on chunks: all probes over kTPB plus one partial chunk per cell.
+    NF_CK(chunks.ensure((size_t)ncell + nprobes / kTPB + 1));
+    NF_LAUNCH(k_chunk_fill, grid_for(ncell, 256), 256, 0, st)(ncell, R, celloff.p, pstart, choff.p, chunks.p);
+    NF_CK(cudaGetLastError());
+    return NF_OK;
+}
+
 nf_status Engine::scan_u32(const uint32_t* in, uint32_t* out, size_t n) {
     g_launches += 2;  // DeviceScan: tile-state init + scan
     size_t bytes = 0;
@@ -464,9 +523,10 @@ nf_status Engine::set_density(int r, int nx, int ny, int nz, const float* values
 }
 
 void Engine::release() {
-    DBuf<float4>* f4[] = {&pos, &dir, &spos, &sdir, &cpos, &cdir};
+    DBuf<float4>* f4[] = {&pos, &dir, &spos, &sdir, &cpos, &cdir, &gpos, &gdir, &vpf, &vdf};
     for (auto* b : f4) b->release();
-    DBuf<uint32_t>* u32[] = {&dcount, &rodoff, &rstart, &rcursor, &sid, &coff, &keep, &kpos, &ccount,
+    DBuf<uint32_t>* u32[] = {&nch, &choff, &celloff, &vcell, &vperm, &vstart, &vcur,
+                             &dcount, &rodoff, &rstart, &rcursor, &sid, &coff, &keep, &kpos, &ccount,
                              &cstart, &ccursor, &cperm, &creal, &ccell, &ccnt, &clist, &accf, &accpos,
                              &meta, &u32tmp, &rcnt, &rpos, &rcur, &cI, &cJ, &creal2, &eflag, &parent,
                              &cflag, &aidx, &rowp, &col, &deg};
@@ -475,7 +535,8 @@ void Engine::release() {
     for (auto* b : u64) b->release();
     DBuf<double>* d64[] = {&ct0, &ct1, &cD, &cG, &cS, &vsrc, &vsnk, &volt, &val64, &diag64, &bvec, &xvec, &cgred};
     for (auto* b : d64) b->release();
-    dreal.release(); mesh.release(); state.release(); ctr.release(); cubtmp.release();
+    dreal.release(); mesh.release(); state.release(); ctr.release(); cubtmp.release(); chunks.release();
+    vdbl.release();
     rec.release(); rec2.release(); recn.release(); cimg.release();
     val32.release(); diag32.release(); cgbuf.release();
 }
@@ -542,6 +603,11 @@ static nf_status setup_reals(Engine& E) {
     E.ncell = coffs;
     E.rod_slots = roff;
 #define NF_CKS(x) do { cudaError_t e_ = (x); if (e_ != cudaSuccess) return E.cuda_fail(e_, #x); } while (0)
+    std::vector<uint32_t> hcelloff(E.R + 1);
+    for (int r = 0; r < E.R; ++r) hcelloff[r] = E.hreal[r].cell_off;
+    hcelloff[E.R] = E.ncell;
+    NF_CKS(E.celloff.ensure(E.R + 1));
+    NF_CKS(cudaMemcpyAsync(E.celloff.p, hcelloff.data(), sizeof(uint32_t) * (E.R + 1), cudaMemcpyHostToDevice, E.st));
     NF_CKS(E.dreal.ensure(E.R));
     NF_CKS(cudaMemcpyAsync(E.dreal.p, E.hreal.data(), sizeof(Real) * E.R, cudaMemcpyHostToDevice, E.st));
     NF_CKS(E.rodoff.ensure(E.R + 1));
@@ -701,6 +767,8 @@ nf_status Engine::generate() {
         NF_CK(creal.ensure(slots));
         NF_CK(ccell.ensure(slots));
         NF_CK(cperm.ensure(slots));
+        NF_CK(gpos.ensure(slots));
+        NF_CK(gdir.ensure(slots));
         NF_CK(state.ensure(slots));
         NF_CK(ccnt.ensure(slots));
         NF_CK(clist.ensure(slots * kConflictCap));
@@ -728,15 +796,23 @@ nf_status Engine::generate() {
         NF_CK(cudaMemsetAsync(ccursor.p, 0, sizeof(uint32_t) * (ncell + 1), st));
         NF_LAUNCH(k_bin, gs, 256, 0, st)((uint32_t)slots, ntot, ccell.p, cstart.p, ccursor.p, cperm.p);
         NF_CK(cudaGetLastError());
+        // Cell-sorted candidate copy and the chunk table of this round.
+        NF_LAUNCH(k_gather_pd, gs, 256, 0, st)((uint32_t)slots, ntot, cperm.p, cpos.p, cdir.p, gpos.p, gdir.p);
+        NF_CK(cudaGetLastError());
+        s = build_chunks(cstart.p, slots);
+        if (s != NF_OK) return s;
+        const dim3 tg(grid_for(slots, kTPB) + (unsigned)std::min<uint64_t>(ncell, slots), 27);
         tstart(KT_OLD);
-        NF_LAUNCH(k_old_test, gs, 256, 0, st)(dreal.p, ntot, cperm.p, cpos.p, cdir.p, creal.p, rstart.p, spos.p, sdir.p,
-                                       total_rods() > 0 ? 1 : 0, state.p, ctr.p);
+        if (total_rods() > 0)
+            NF_LAUNCH(k_old_tiles, tg, kTPB, 0, st)(dreal.p, choff.p + ncell, chunks.p, cperm.p, gpos.p, gdir.p,
+                                                    rstart.p, spos.p, sdir.p, state.p, ctr.p);
         NF_CK(cudaGetLastError());
         tstop(KT_OLD);
         NF_CK(cudaMemsetAsync(ctr.p + C_OVERFLOW, 0, sizeof(unsigned long long), st));
+        NF_CK(cudaMemsetAsync(ccnt.p, 0, sizeof(uint32_t) * slots, st));
         tstart(KT_CONF);
-        NF_LAUNCH(k_conflicts, gs, 256, 0, st)(dreal.p, ntot, cperm.p, cstart.p, cpos.p, cdir.p, csidx.p, creal.p, state.p,
-                                        ccnt.p, clist.p, ctr.p);
+        NF_LAUNCH(k_conf_tiles, tg, kTPB, 0, st)(dreal.p, choff.p + ncell, chunks.p, cperm.p, cstart.p, gpos.p,
+                                                 gdir.p, csidx.p, state.p, ccnt.p, clist.p, ctr.p);
         NF_CK(cudaGetLastError());
         tstop(KT_CONF);
         unsigned long long ovf = 0;

@@ -1,0 +1,79 @@
+// nf_tiles.cuh -- work decomposition of the cell-pair kernels.
+//
+// Probes (candidates, rods or virtual rods) are binned by cell (CSR pstart).
+// A chunk is up to kTPB probes of one cell; a block of the pair kernels takes
+// one (chunk, stencil offset) pair: it owns one neighbour cell of one probe
+// chunk, streams that cell's targets through shared memory in tiles of kTile,
+// and every thread tests its probe against each staged target (all threads read
+// the same shared-memory word: broadcast, no bank conflict). The 27 offsets of a
+// chunk run as 27 independent blocks, so a dense cell fills many SMs, and a
+// probe decided in one block is skipped by the others at the next tile.
+#pragma once
+#include <cstdint>
+
+#include "nf_common.cuh"
+
+namespace nf {
+
+constexpr int kTPB = 128;   // probes per chunk = threads per block
+constexpr int kTile = 256;  // targets staged per shared-memory tile
+
+struct Chunk {
+    uint32_t cell;   // global cell id of the probes
+    uint32_t first;  // first probe (index into the cell-sorted probe order)
+    uint32_t n;      // probes in the chunk (<= kTPB)
+    uint32_t real;   // realisation of the cell
+};
+
+// Number of chunks per cell.
+static __global__ void k_chunk_count(uint32_t ncell, const uint32_t* __restrict__ pstart, uint32_t* __restrict__ nch) {
+    uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c > ncell) return;
+    if (c == ncell) { nch[c] = 0; return; }
+    uint32_t n = pstart[c + 1] - pstart[c];
+    nch[c] = (n + kTPB - 1) / kTPB;
+}
+
+static __global__ void k_chunk_fill(uint32_t ncell, int R, const uint32_t* __restrict__ celloff,
+                             const uint32_t* __restrict__ pstart, const uint32_t* __restrict__ choff,
+                             Chunk* __restrict__ chunks) {
+    uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= ncell) return;
+    uint32_t b = pstart[c], n = pstart[c + 1] - b, k0 = choff[c];
+    uint32_t r = (uint32_t)find_real(celloff, R, c);
+    for (uint32_t k = 0; k * kTPB < n; ++k) {
+        Chunk ch;
+        ch.cell = c;
+        ch.first = b + k * kTPB;
+        ch.n = min((uint32_t)kTPB, n - k * kTPB);
+        ch.real = r;
+        chunks[k0 + k] = ch;
+    }
+}
+
+// Decode the stencil neighbour of chunk cell `cell` (global id) for offset o.
+__device__ __forceinline__ bool chunk_neighbour(const Real& Re, uint32_t cell, int o, int per, uint32_t* nc,
+                                                int img[3]) {
+    uint32_t loc = cell - Re.cell_off;
+    int c[3];
+    c[0] = (int)(loc % (uint32_t)Re.n[0]);
+    c[1] = (int)((loc / (uint32_t)Re.n[0]) % (uint32_t)Re.n[1]);
+    c[2] = (int)(loc / ((uint32_t)Re.n[0] * (uint32_t)Re.n[1]));
+    return stencil(Re, c, o, per, nc, img);
+}
+
+// Gather rows of (pos, dir, payload) into cell-sorted order.
+template <class P>
+static __global__ void k_gather(uint32_t n, const uint32_t* __restrict__ ntot, const uint32_t* __restrict__ perm,
+                         const float4* __restrict__ pos, const float4* __restrict__ dir, const P* __restrict__ pay,
+                         float4* __restrict__ opos, float4* __restrict__ odir, P* __restrict__ opay) {
+    uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
+    uint32_t m = ntot ? *ntot : n;
+    if (q >= m) return;
+    uint32_t i = perm[q];
+    opos[q] = pos[i];
+    odir[q] = dir[i];
+    opay[q] = pay[i];
+}
+
+}  // namespace nf
