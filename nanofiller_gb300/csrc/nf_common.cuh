@@ -290,22 +290,31 @@ NF_HD bool stencil(const Real& R, const int c[3], int o, int per, uint32_t* cell
 }
 
 // ---------------------------------------------------------------------------
-// FP32 conservative filter. The reference's points lie within (l/2+a+eps)|c|
-// of each centre and on the axis lines, so
-//   d >= |b| - hA - hB   and   d >= |(cA x cB) . b| / |cA x cB|.
-// A pair is "far" when either bound, evaluated in FP32 with error margins
-// (relative 2e-6 / 2e-4, absolute `slack` for coordinate rounding), clears
-// the threshold. Far pairs cannot satisfy d < thr in any precision; the rest
-// go to the FP64 routine.
+// FP32 conservative filter. The reference's points lie on the two axis lines,
+// within (l/2 + a + eps)|c| of each centre, so d is bounded below by
+//   (1) the centre distance minus both half-reaches (bounding spheres),
+//   (2) the distance of the two lines, |(cA x cB) . b| / |cA x cB|,
+//   (3) the gap of the projections of the two segments onto cA, and onto cB
+//       (projection is 1-Lipschitz: a separating-axis bound).
+// A pair is "far" when one bound, evaluated in FP32 with error margins
+// (relative 2e-6 .. 2e-4, absolute `slack` for coordinate rounding), clears the
+// threshold; far pairs cannot satisfy d < thr in any precision. The rest go to
+// the FP64 routine.
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ bool maybe_near(const float4& pA, const float4& cA, const float4& pB,
-                                           const float4& cB, float sx, float sy, float sz,
-                                           float thr, float eps, float slack) {
+NF_HD bool maybe_near(const float4& pA, const float4& cA, const float4& pB, const float4& cB, float sx, float sy,
+                      float sz, float thr, float eps, float slack) {
     float bx = (pB.x + sx) - pA.x, by = (pB.y + sy) - pA.y, bz = (pB.z + sz) - pA.z;
     float hA = pA.w * 0.5f + cA.w + eps, hB = pB.w * 0.5f + cB.w + eps;
     float Rr = (hA + hB + thr) * 1.000002f + slack;
     float bb = bx * bx + by * by + bz * bz;
     if (bb > Rr * Rr) return false;
+    float err = 4e-6f * (1.0f + sqrtf(bb)) + slack;
+    float thr_s = thr * 1.0002f;
+    float dcc = fabsf(cA.x * cB.x + cA.y * cB.y + cA.z * cB.z);
+    float pa = fabsf(bx * cA.x + by * cA.y + bz * cA.z);
+    if (pa - (hA + hB * dcc) * 1.00001f - err > thr_s) return false;
+    float pb = fabsf(bx * cB.x + by * cB.y + bz * cB.z);
+    if (pb - (hB + hA * dcc) * 1.00001f - err > thr_s) return false;
     float nx = cA.y * cB.z - cA.z * cB.y;
     float ny = cA.z * cB.x - cA.x * cB.z;
     float nz = cA.x * cB.y - cA.y * cB.x;
@@ -313,9 +322,38 @@ __device__ __forceinline__ bool maybe_near(const float4& pA, const float4& cA, c
     if (nn > 1e-4f) {
         float nb = fabsf(nx * bx + ny * by + nz * bz);
         float s = sqrtf(nn);
-        if (nb - 4e-6f * (1.0f + sqrtf(bb)) - slack > thr * s * 1.0002f) return false;
+        if (nb - err > thr_s * s) return false;
     }
     return true;
+}
+
+// FP32 certificate of a hit. When the reference routine takes its
+// non-parallel branch and leaves both parameters unclamped (|t| <= l/2 + a + eps
+// for both rods), its points are the feet of the common perpendicular and d is
+// exactly the distance of the two lines. The certificate demands margins that
+// exceed the FP32 error of every quantity involved: |c1.c2| <= 0.995 (so
+// |d^2 - 1| >= 0.0099 and the branch is far from the 1e-6 parallel test), both
+// |t| at least dt inside their limits, and the line distance at least err
+// below the threshold. Certified pairs are hits in FP64 as well.
+NF_HD bool certain_hit(const float4& pA, const float4& cA, const float4& pB, const float4& cB, float sx, float sy,
+                       float sz, float thr, float eps, float slack) {
+    float bx = (pB.x + sx) - pA.x, by = (pB.y + sy) - pA.y, bz = (pB.z + sz) - pA.z;
+    float d = cA.x * cB.x + cA.y * cB.y + cA.z * cB.z;
+    if (fabsf(d) > 0.995f) return false;
+    float den = d * d - 1.0f;
+    float nb = sqrtf(bx * bx + by * by + bz * bz);
+    float t0 = ((d * cB.x - cA.x) * bx + (d * cB.y - cA.y) * by + (d * cB.z - cA.z) * bz) / den;
+    float t1 = ((cB.x - d * cA.x) * bx + (cB.y - d * cA.y) * by + (cB.z - d * cA.z) * bz) / den;
+    float dt = (2e-5f * (1.0f + nb) + 2.0f * slack) / fabsf(den);
+    if (fabsf(t0) + dt >= (pA.w * 0.5f + cA.w + eps) * 0.99999f) return false;
+    if (fabsf(t1) + dt >= (pB.w * 0.5f + cB.w + eps) * 0.99999f) return false;
+    float nx = cA.y * cB.z - cA.z * cB.y;
+    float ny = cA.z * cB.x - cA.x * cB.z;
+    float nz = cA.x * cB.y - cA.y * cB.x;
+    float s = sqrtf(nx * nx + ny * ny + nz * nz);
+    float ld = fabsf(nx * bx + ny * by + nz * bz) / s;
+    float err = (4e-6f * (1.0f + nb) + slack) / s + 1e-6f * ld;
+    return ld + err < thr * 0.9998f;
 }
 
 // ---------------------------------------------------------------------------

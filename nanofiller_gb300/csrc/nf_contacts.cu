@@ -29,16 +29,17 @@ static inline unsigned grid_for(size_t n, unsigned b) { return (unsigned)((n + b
 
 // ---------------------------------------------------------------------------
 // Pair sweep: one (rod chunk, stencil offset) per block, neighbour rods staged
-// in shared memory. Rod I records rods J > I (upper triangle).
+// in shared memory. Rod I considers rods J > I (upper triangle); pairs the FP32
+// filter cannot rule out are queued (probe, target = sorted rod indices) and
+// recorded by k_ct_exact from their FP64 evaluation.
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(kTPB) k_ct_tiles(const Real* __restrict__ reals,
                                                    const uint32_t* __restrict__ nchunk,
                                                    const Chunk* __restrict__ chunks,
                                                    const uint32_t* __restrict__ rstart,
                                                    const float4* __restrict__ spos, const float4* __restrict__ sdir,
-                                                   const uint32_t* __restrict__ sid, Rec* __restrict__ rec,
-                                                   unsigned long long cap, unsigned long long* __restrict__ recn,
-                                                   uint32_t* __restrict__ rcnt, unsigned long long* __restrict__ ctr) {
+                                                   const uint32_t* __restrict__ sid, unsigned long long* __restrict__ xq,
+                                                   unsigned long long xcap, unsigned long long* __restrict__ ctr) {
     __shared__ float4 tp[kTile], td[kTile];
     __shared__ uint32_t ti[kTile];
     const uint32_t ch = blockIdx.x;
@@ -57,9 +58,7 @@ __global__ void __launch_bounds__(kTPB) k_ct_tiles(const Real* __restrict__ real
     if (have) { i = sid[q]; pA = spos[q]; cA = sdir[q]; }
     const float epc = 1e-6f;  // DEV_PRECISION (inc/definitions.h:5)
     const float sx = img[0] * Re.L[0], sy = img[1] * Re.L[1], sz = img[2] * Re.L[2];
-    const double shx = img[0] * (double)Re.L[0], shy = img[1] * (double)Re.L[1], shz = img[2] * (double)Re.L[2];
-    unsigned long long tests = 0, exact = 0, flips = 0;
-    uint32_t mine = 0;
+    unsigned long long tests = 0;
     for (uint32_t base = t0; base < t1; base += kTile) {
         const uint32_t m = min((uint32_t)kTile, t1 - base);
         for (uint32_t k = threadIdx.x; k < m; k += kTPB) {
@@ -70,39 +69,63 @@ __global__ void __launch_bounds__(kTPB) k_ct_tiles(const Real* __restrict__ real
         __syncthreads();
         if (have) {
             for (uint32_t k = 0; k < m; ++k) {
-                const uint32_t j = ti[k];
-                if (j <= i) continue;
+                if (ti[k] <= i) continue;
                 const float4 pB = tp[k], cB = td[k];
                 ++tests;
                 const float thr = (cB.w + cA.w) + Re.cut + epc;
                 if (!maybe_near(pA, cA, pB, cB, sx, sy, sz, thr, epc, Re.slack)) continue;
-                ++exact;
-                const RodD a = rodd(pA, cA), b = rodd(pB, cB);
-                double t0d, t1d, u0, u1, Dx;
-                double d = ref_distance_d(a, b, shx, shy, shz, (double)epc, false, &t0d, &t1d, &u0, &u1, &Dx);
-                bool h = d < thresh_d(a.a, b.a, 1.0, (double)Re.cut, (double)epc);
-                if (ref_hit_f32(pA, cA, pB, cB, sx, sy, sz, epc, thr, false) != h) ++flips;
-                if (!h) continue;
-                unsigned long long slot = atomicAdd(recn, 1ull);
-                ++mine;
-                if (slot < cap) {
-                    Rec x;
-                    x.i = i;
-                    x.j = j;
-                    x.img[0] = (int8_t)img[0];
-                    x.img[1] = (int8_t)img[1];
-                    x.img[2] = (int8_t)img[2];
-                    x.img[3] = 0;
-                    x.flags = 0;
-                    x.t0 = t0d; x.t1 = t1d; x.d = d; x.Dx = Dx; x.u0 = u0; x.u1 = u1;
-                    rec[slot] = x;
-                }
+                xq_push(xq, xcap, &ctr[C_XQ], xq_pack(q, base + k, img));
             }
         }
         __syncthreads();
     }
-    if (mine) atomicAdd(&rcnt[i], mine);
     warp_add_u64(&ctr[C_CT_PAIRS], tests);
+}
+
+__global__ void __launch_bounds__(256) k_ct_exact(const Real* __restrict__ reals, int R,
+                                                  const uint32_t* __restrict__ rodoff,
+                                                  const unsigned long long* __restrict__ xq,
+                                                  const unsigned long long* __restrict__ count, unsigned long long xcap,
+                                                  const float4* __restrict__ spos, const float4* __restrict__ sdir,
+                                                  const uint32_t* __restrict__ sid, Rec* __restrict__ rec,
+                                                  unsigned long long cap, unsigned long long* __restrict__ recn,
+                                                  uint32_t* __restrict__ rcnt, unsigned long long* __restrict__ ctr) {
+    const unsigned long long n = min(*count, xcap);
+    const float epc = 1e-6f;
+    unsigned long long exact = 0, flips = 0;
+    for (unsigned long long e = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; e < n;
+         e += (unsigned long long)gridDim.x * blockDim.x) {
+        uint32_t q, p;
+        int img[3];
+        xq_unpack(xq[e], &q, &p, img);
+        const uint32_t i = sid[q], j = sid[p];
+        const Real& Re = reals[find_real(rodoff, R, i)];
+        const float4 pA = spos[q], cA = sdir[q], pB = spos[p], cB = sdir[p];
+        ++exact;
+        const RodD a = rodd(pA, cA), b = rodd(pB, cB);
+        double t0d, t1d, u0, u1, Dx;
+        double d = ref_distance_d(a, b, img[0] * (double)Re.L[0], img[1] * (double)Re.L[1],
+                                  img[2] * (double)Re.L[2], (double)epc, false, &t0d, &t1d, &u0, &u1, &Dx);
+        bool h = d < thresh_d(a.a, b.a, 1.0, (double)Re.cut, (double)epc);
+        const float thr = (cB.w + cA.w) + Re.cut + epc;
+        if (ref_hit_f32(pA, cA, pB, cB, img[0] * Re.L[0], img[1] * Re.L[1], img[2] * Re.L[2], epc, thr, false) != h)
+            ++flips;
+        if (!h) continue;
+        unsigned long long slot = atomicAdd(recn, 1ull);
+        atomicAdd(&rcnt[i], 1u);
+        if (slot < cap) {
+            Rec x;
+            x.i = i;
+            x.j = j;
+            x.img[0] = (int8_t)img[0];
+            x.img[1] = (int8_t)img[1];
+            x.img[2] = (int8_t)img[2];
+            x.img[3] = 0;
+            x.flags = 0;
+            x.t0 = t0d; x.t1 = t1d; x.d = d; x.Dx = Dx; x.u0 = u0; x.u1 = u1;
+            rec[slot] = x;
+        }
+    }
     warp_add_u64(&ctr[C_CT_EXACT], exact);
     warp_add_u64(&ctr[C_CT_FLIPS], flips);
 }
@@ -213,7 +236,8 @@ __global__ void __launch_bounds__(kTPB) k_scr_tiles(const Real* __restrict__ rea
                                                     const float4* __restrict__ vdf,
                                                     const uint32_t* __restrict__ rstart,
                                                     const float4* __restrict__ spos, const float4* __restrict__ sdir,
-                                                    Rec* rec, unsigned long long* __restrict__ ctr) {
+                                                    unsigned long long* __restrict__ xq, unsigned long long xcap,
+                                                    unsigned long long* __restrict__ ctr) {
     __shared__ float4 tp[kTile], td[kTile];
     const uint32_t ch = blockIdx.x;
     if (ch >= *nchunk) return;
@@ -226,52 +250,63 @@ __global__ void __launch_bounds__(kTPB) k_scr_tiles(const Real* __restrict__ rea
     if (t0 == t1) return;
     const bool have = threadIdx.x < C.n;
     const uint32_t id = have ? vperm[C.first + threadIdx.x] : 0u;
-    volatile uint32_t* vflag = have ? &rec[id].flags : nullptr;
-    RodD V{};
-    double sv[3] = {0, 0, 0};
     float4 pV = make_float4(0, 0, 0, 0), cV = pV;
     float svf[3] = {0, 0, 0};
-    bool alive = have && !(*vflag & 1u);
     if (have) {
         const double* o = vd + (size_t)kVD * id;
-        V = RodD{o[0], o[1], o[2], o[3], o[4], o[5], o[6], o[7]};
-        for (int d = 0; d < 3; ++d) {
-            sv[d] = dsub(o[8 + d], img[d] * (double)Re.L[d]);
-            svf[d] = (float)sv[d];
-        }
+        for (int d = 0; d < 3; ++d) svf[d] = (float)dsub(o[8 + d], img[d] * (double)Re.L[d]);
         pV = vpf[id];
         cV = vdf[id];
     }
-    const double eps = (double)1e-6f;
     const float epsf = 1e-6f;
-    unsigned long long tests = 0, exact = 0;
+    unsigned long long tests = 0;
     for (uint32_t base = t0; base < t1; base += kTile) {
-        if (!__syncthreads_or(alive)) break;
         const uint32_t m = min((uint32_t)kTile, t1 - base);
         for (uint32_t k = threadIdx.x; k < m; k += kTPB) { tp[k] = spos[base + k]; td[k] = sdir[base + k]; }
         __syncthreads();
-        if (alive) {
+        if (have) {
             for (uint32_t k = 0; k < m; ++k) {
                 const float4 pR = tp[k], cR = td[k];
                 ++tests;
                 const float thr = (cV.w + cR.w) + epsf;
                 if (!maybe_near(pR, cR, pV, cV, svf[0], svf[1], svf[2], thr, epsf, Re.slack)) continue;
-                ++exact;
-                const RodD Rr = rodd(pR, cR);
-                double u1, t0d, t1d, u0;
-                double d = ref_distance_d(Rr, V, sv[0], sv[1], sv[2], eps, false, &t0d, &t1d, &u0, &u1, nullptr);
-                bool h = d < thresh_d(Rr.a, V.a, 1.0, 0.0, eps);
-                if (h && dsub(ddiv(V.l, 2.0), dabs(u1)) > dadd(V.a, eps)) {
-                    atomicOr(&rec[id].flags, 1u);
-                    alive = false;
-                    break;
-                }
+                xq_push(xq, xcap, &ctr[C_XQ], xq_pack(id, base + k, img));
             }
-            if (alive && (*vflag & 1u)) alive = false;  // decided by another block
         }
         __syncthreads();
     }
     warp_add_u64(&ctr[C_SCR_PAIRS], tests);
+}
+
+__global__ void __launch_bounds__(256) k_scr_exact(const Real* __restrict__ reals, int R,
+                                                   const uint32_t* __restrict__ rodoff,
+                                                   const unsigned long long* __restrict__ xq,
+                                                   const unsigned long long* __restrict__ count, unsigned long long xcap,
+                                                   const double* __restrict__ vd, const float4* __restrict__ spos,
+                                                   const float4* __restrict__ sdir, Rec* rec,
+                                                   unsigned long long* __restrict__ ctr) {
+    const unsigned long long n = min(*count, xcap);
+    const double eps = (double)1e-6f;
+    unsigned long long exact = 0;
+    for (unsigned long long e = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; e < n;
+         e += (unsigned long long)gridDim.x * blockDim.x) {
+        uint32_t id, p;
+        int img[3];
+        xq_unpack(xq[e], &id, &p, img);
+        volatile uint32_t* vflag = &rec[id].flags;
+        if (*vflag & 1u) continue;
+        const Real& Re = reals[find_real(rodoff, R, rec[id].i)];
+        const double* o = vd + (size_t)kVD * id;
+        const RodD V{o[0], o[1], o[2], o[3], o[4], o[5], o[6], o[7]};
+        double sv[3];
+        for (int d = 0; d < 3; ++d) sv[d] = dsub(o[8 + d], img[d] * (double)Re.L[d]);
+        const RodD Rr = rodd(spos[p], sdir[p]);
+        ++exact;
+        double u1, t0d, t1d, u0;
+        double d = ref_distance_d(Rr, V, sv[0], sv[1], sv[2], eps, false, &t0d, &t1d, &u0, &u1, nullptr);
+        bool h = d < thresh_d(Rr.a, V.a, 1.0, 0.0, eps);
+        if (h && dsub(ddiv(V.l, 2.0), dabs(u1)) > dadd(V.a, eps)) atomicOr(&rec[id].flags, 1u);
+    }
     warp_add_u64(&ctr[C_SCR_EXACT], exact);
 }
 
@@ -480,22 +515,31 @@ nf_status Engine::contacts() {
     nf_status s = build_chunks(rstart.p, nrods);
     if (s != NF_OK) return s;
     const dim3 tg(grid_for(nrods, kTPB) + ncell, 27);
-    for (int attempt = 0; attempt < 2; ++attempt) {
+    const unsigned xg = (unsigned)(4 * nsm);
+    for (int attempt = 0; attempt < 4; ++attempt) {
         NF_CK(rec.ensure(cap));
+        NF_CK(xq.ensure(xq_cap));
         NF_CK(cudaMemsetAsync(rcnt.p, 0, sizeof(uint32_t) * (nslot + 1), st));
         NF_CK(cudaMemsetAsync(recn.p, 0, sizeof(unsigned long long), st));
+        NF_CK(cudaMemsetAsync(ctr.p + C_XQ, 0, sizeof(unsigned long long), st));
         tstart(KT_CTPAIRS);
-        if (nrods)
+        if (nrods) {
             NF_LAUNCH(k_ct_tiles, tg, kTPB, 0, st)(dreal.p, choff.p + ncell, chunks.p, rstart.p, spos.p, sdir.p, sid.p,
-                                                   rec.p, rec.cap, recn.p, rcnt.p, ctr.p);
+                                                   xq.p, xq.cap, ctr.p);
+            NF_CK(cudaGetLastError());
+            NF_LAUNCH(k_ct_exact, xg, 256, 0, st)(dreal.p, R, rodoff.p, xq.p, ctr.p + C_XQ, xq.cap, spos.p, sdir.p,
+                                                  sid.p, rec.p, rec.cap, recn.p, rcnt.p, ctr.p);
+        }
         NF_CK(cudaGetLastError());
         tstop(KT_CTPAIRS);
-        unsigned long long n = 0;
-        NF_CK(cudaMemcpyAsync(&n, recn.p, sizeof(n), cudaMemcpyDeviceToHost, st));
+        unsigned long long hv[2] = {0, 0};
+        NF_CK(cudaMemcpyAsync(&hv[0], recn.p, sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
+        NF_CK(cudaMemcpyAsync(&hv[1], ctr.p + C_XQ, sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
         NF_CK(cudaStreamSynchronize(st));
-        if (n <= rec.cap) { cap = n; tbytes(KT_CTPAIRS, 36.0 * nrods + 64.0 * n, 0); break; }
-        if (attempt == 1) { err = "contact record buffer overflow"; return NF_ERR_OVERFLOW; }
-        cap = n + n / 8 + 64;
+        if (hv[1] > xq.cap) { xq_cap = (size_t)(hv[1] * 1.25) + 1024; continue; }
+        if (hv[0] <= rec.cap) { cap = hv[0]; tbytes(KT_CTPAIRS, 36.0 * nrods + 64.0 * hv[0], 0); break; }
+        cap = hv[0] + hv[0] / 8 + 64;
+        if (attempt == 3) { err = "contact record buffer overflow"; return NF_ERR_OVERFLOW; }
     }
     const uint32_t nrec = (uint32_t)cap;
     NF_CK(rec2.ensure(nrec + 1));
@@ -528,9 +572,22 @@ nf_status Engine::contacts() {
             s = build_chunks(vstart.p, nrec);
             if (s != NF_OK) return s;
             const dim3 vg(grid_for(nrec, kTPB) + ncell, 27);
-            NF_LAUNCH(k_scr_tiles, vg, kTPB, 0, st)(dreal.p, choff.p + ncell, chunks.p, vperm.p, vdbl.p, vpf.p, vdf.p,
-                                                    rstart.p, spos.p, sdir.p, rec2.p, ctr.p);
-            NF_CK(cudaGetLastError());
+            for (int attempt = 0; attempt < 3; ++attempt) {
+                NF_CK(xq.ensure(xq_cap));
+                NF_CK(cudaMemsetAsync(ctr.p + C_XQ, 0, sizeof(unsigned long long), st));
+                NF_LAUNCH(k_scr_tiles, vg, kTPB, 0, st)(dreal.p, choff.p + ncell, chunks.p, vperm.p, vdbl.p, vpf.p,
+                                                        vdf.p, rstart.p, spos.p, sdir.p, xq.p, xq.cap, ctr.p);
+                NF_CK(cudaGetLastError());
+                NF_LAUNCH(k_scr_exact, xg, 256, 0, st)(dreal.p, R, rodoff.p, xq.p, ctr.p + C_XQ, xq.cap, vdbl.p,
+                                                       spos.p, sdir.p, rec2.p, ctr.p);
+                NF_CK(cudaGetLastError());
+                unsigned long long nq = 0;
+                NF_CK(cudaMemcpyAsync(&nq, ctr.p + C_XQ, sizeof(nq), cudaMemcpyDeviceToHost, st));
+                NF_CK(cudaStreamSynchronize(st));
+                if (nq <= xq.cap) break;
+                xq_cap = (size_t)(nq * 1.25) + 1024;  // screening flags are idempotent: rerun
+                if (attempt == 2) { err = "screening queue overflow"; return NF_ERR_OVERFLOW; }
+            }
             tstop(KT_SCREEN);
             tbytes(KT_SCREEN, 64.0 * nrec + 32.0 * nrods, 0);
         }

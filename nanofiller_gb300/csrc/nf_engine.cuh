@@ -33,7 +33,7 @@ enum CandState : uint8_t { ST_NONE = 0, ST_REJ_OLD = 1, ST_ALIVE = 2, ST_ACC = 3
 enum Ctr {
     C_PAIR_TESTS = 0, C_EXACT, C_FLIPS, C_OVERFLOW, C_UNDECIDED,
     C_CT_PAIRS, C_CT_EXACT, C_CT_FLIPS, C_CT_RECORDS, C_SCR_PAIRS, C_SCR_EXACT,
-    C_CG_ITERS, C_NCTR
+    C_CG_ITERS, C_XQ_OLD, C_XQ_CONF, C_XQ, C_CERT, C_NCTR
 };
 
 template <class T>
@@ -119,6 +119,8 @@ struct Engine {
     DBuf<float4> cpos, cdir;
     DBuf<float4> gpos, gdir;     // candidates in cell order
     DBuf<Chunk> chunks;          // (cell, probe range) work table of the pair kernels
+    DBuf<unsigned long long> xq, xq2;  // exact queues (pairs left to FP64)
+    size_t xq_cap = 1 << 16;
     DBuf<uint32_t> nch, choff, celloff;
     DBuf<uint8_t> state;
     DBuf<uint32_t> meta;   // per-realisation round metadata

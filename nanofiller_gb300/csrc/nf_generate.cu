@@ -180,7 +180,9 @@ __global__ void k_bin(uint32_t n, const uint32_t* __restrict__ ntot, const uint3
 }
 
 // Candidate vs accepted rods of one neighbour cell (cuda_OldExtIsectLB's job),
-// one (candidate chunk, stencil offset) per block, targets staged in shared memory.
+// one (candidate chunk, stencil offset) per block, targets staged in shared
+// memory. Far pairs are dropped and clear hits decided in FP32; the rest go to
+// the exact queue (probe = compact candidate id, target = sorted rod index).
 __global__ void __launch_bounds__(kTPB) k_old_tiles(const Real* __restrict__ reals,
                                                     const uint32_t* __restrict__ nchunk,
                                                     const Chunk* __restrict__ chunks,
@@ -188,7 +190,8 @@ __global__ void __launch_bounds__(kTPB) k_old_tiles(const Real* __restrict__ rea
                                                     const float4* __restrict__ gpos, const float4* __restrict__ gdir,
                                                     const uint32_t* __restrict__ rstart,
                                                     const float4* __restrict__ spos, const float4* __restrict__ sdir,
-                                                    uint8_t* state, unsigned long long* __restrict__ ctr) {
+                                                    uint8_t* state, unsigned long long* __restrict__ xq,
+                                                    unsigned long long xcap, unsigned long long* __restrict__ ctr) {
     __shared__ float4 tp[kTile], td[kTile];
     const uint32_t ch = blockIdx.x;
     if (ch >= *nchunk) return;
@@ -207,8 +210,7 @@ __global__ void __launch_bounds__(kTPB) k_old_tiles(const Real* __restrict__ rea
     if (have) { pA = gpos[q]; cA = gdir[q]; }
     bool alive = have && vst[cid] != ST_REJ_OLD;
     const float sx = img[0] * Re.L[0], sy = img[1] * Re.L[1], sz = img[2] * Re.L[2];
-    const double shx = img[0] * (double)Re.L[0], shy = img[1] * (double)Re.L[1], shz = img[2] * (double)Re.L[2];
-    unsigned long long tests = 0, exact = 0, flips = 0;
+    unsigned long long tests = 0, cert = 0;
     for (uint32_t base = t0; base < t1; base += kTile) {
         if (!__syncthreads_or(alive)) break;
         const uint32_t m = min((uint32_t)kTile, t1 - base);
@@ -220,24 +222,59 @@ __global__ void __launch_bounds__(kTPB) k_old_tiles(const Real* __restrict__ rea
                 ++tests;
                 const float thr = (cB.w + cA.w) * Re.scf + Re.sep + Re.eps;
                 if (!maybe_near(pA, cA, pB, cB, sx, sy, sz, thr, Re.eps, Re.slack)) continue;
-                ++exact;
-                const RodD a = rodd(pA, cA), b = rodd(pB, cB);
-                double d = ref_distance_d(a, b, shx, shy, shz, (double)Re.eps, Re.typo != 0, nullptr, nullptr,
-                                          nullptr, nullptr, nullptr);
-                bool h = d < thresh_d(a.a, b.a, (double)Re.scf, (double)Re.sep, (double)Re.eps);
-                if (ref_hit_f32(pA, cA, pB, cB, sx, sy, sz, Re.eps, thr, Re.typo != 0) != h) ++flips;
-                if (h) { vst[cid] = ST_REJ_OLD; alive = false; break; }
+                if (!Re.typo && certain_hit(pA, cA, pB, cB, sx, sy, sz, thr, Re.eps, Re.slack)) {
+                    ++cert;
+                    vst[cid] = ST_REJ_OLD;
+                    alive = false;
+                    break;
+                }
+                xq_push(xq, xcap, &ctr[C_XQ_OLD], xq_pack(cid, base + k, img));
             }
             if (alive && vst[cid] == ST_REJ_OLD) alive = false;  // decided by another block
         }
         __syncthreads();
     }
     warp_add_u64(&ctr[C_PAIR_TESTS], tests);
+    warp_add_u64(&ctr[C_CERT], cert);
+}
+
+// FP64 decisions of the queued (candidate, accepted rod) pairs.
+__global__ void __launch_bounds__(256) k_old_exact(const Real* __restrict__ reals,
+                                                   const unsigned long long* __restrict__ xq,
+                                                   const unsigned long long* __restrict__ count,
+                                                   unsigned long long cap, const float4* __restrict__ cpos,
+                                                   const float4* __restrict__ cdir, const uint32_t* __restrict__ creal,
+                                                   const float4* __restrict__ spos, const float4* __restrict__ sdir,
+                                                   uint8_t* state, unsigned long long* __restrict__ ctr) {
+    const unsigned long long n = min(*count, cap);
+    volatile uint8_t* vst = state;
+    unsigned long long exact = 0, flips = 0;
+    for (unsigned long long e = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; e < n;
+         e += (unsigned long long)gridDim.x * blockDim.x) {
+        uint32_t cid, j;
+        int img[3];
+        xq_unpack(xq[e], &cid, &j, img);
+        if (vst[cid] == ST_REJ_OLD) continue;
+        const Real& Re = reals[creal[cid]];
+        const float4 pA = cpos[cid], cA = cdir[cid], pB = spos[j], cB = sdir[j];
+        ++exact;
+        const RodD a = rodd(pA, cA), b = rodd(pB, cB);
+        double d = ref_distance_d(a, b, img[0] * (double)Re.L[0], img[1] * (double)Re.L[1],
+                                  img[2] * (double)Re.L[2], (double)Re.eps, Re.typo != 0, nullptr, nullptr,
+                                  nullptr, nullptr, nullptr);
+        bool h = d < thresh_d(a.a, b.a, (double)Re.scf, (double)Re.sep, (double)Re.eps);
+        const float thr = (cB.w + cA.w) * Re.scf + Re.sep + Re.eps;
+        if (ref_hit_f32(pA, cA, pB, cB, img[0] * Re.L[0], img[1] * Re.L[1], img[2] * Re.L[2], Re.eps, thr,
+                        Re.typo != 0) != h)
+            ++flips;
+        if (h) vst[cid] = ST_REJ_OLD;
+    }
     warp_add_u64(&ctr[C_EXACT], exact);
     warp_add_u64(&ctr[C_FLIPS], flips);
 }
 
 // Earlier surviving candidates of one neighbour cell that a survivor hits.
+// Certified hits are listed directly, uncertain pairs queued (target = compact id).
 __global__ void __launch_bounds__(kTPB) k_conf_tiles(const Real* __restrict__ reals,
                                                      const uint32_t* __restrict__ nchunk,
                                                      const Chunk* __restrict__ chunks,
@@ -246,7 +283,8 @@ __global__ void __launch_bounds__(kTPB) k_conf_tiles(const Real* __restrict__ re
                                                      const float4* __restrict__ gpos, const float4* __restrict__ gdir,
                                                      const uint64_t* __restrict__ csidx,
                                                      const uint8_t* __restrict__ state, uint32_t* __restrict__ ccnt,
-                                                     uint32_t* __restrict__ clist, unsigned long long* __restrict__ ctr) {
+                                                     uint32_t* __restrict__ clist, unsigned long long* __restrict__ xq,
+                                                     unsigned long long xcap, unsigned long long* __restrict__ ctr) {
     __shared__ float4 tp[kTile], td[kTile];
     __shared__ uint64_t tk[kTile];
     __shared__ uint32_t ti[kTile];
@@ -267,8 +305,7 @@ __global__ void __launch_bounds__(kTPB) k_conf_tiles(const Real* __restrict__ re
     bool alive = have && state[cid] == ST_ALIVE;
     if (alive) { pA = gpos[q]; cA = gdir[q]; kA = csidx[cid]; }
     const float sx = img[0] * Re.L[0], sy = img[1] * Re.L[1], sz = img[2] * Re.L[2];
-    const double shx = img[0] * (double)Re.L[0], shy = img[1] * (double)Re.L[1], shz = img[2] * (double)Re.L[2];
-    unsigned long long tests = 0, exact = 0, flips = 0, ovf = 0;
+    unsigned long long tests = 0, ovf = 0, cert = 0;
     if (__syncthreads_or(alive)) {
         for (uint32_t base = t0; base < t1; base += kTile) {
             const uint32_t m = min((uint32_t)kTile, t1 - base);
@@ -288,16 +325,13 @@ __global__ void __launch_bounds__(kTPB) k_conf_tiles(const Real* __restrict__ re
                     ++tests;
                     const float thr = (cB.w + cA.w) * Re.scf + Re.sep + Re.eps;
                     if (!maybe_near(pA, cA, pB, cB, sx, sy, sz, thr, Re.eps, Re.slack)) continue;
-                    ++exact;
-                    const RodD a = rodd(pA, cA), b = rodd(pB, cB);
-                    double d = ref_distance_d(a, b, shx, shy, shz, (double)Re.eps, Re.typo != 0, nullptr,
-                                              nullptr, nullptr, nullptr, nullptr);
-                    bool h = d < thresh_d(a.a, b.a, (double)Re.scf, (double)Re.sep, (double)Re.eps);
-                    if (ref_hit_f32(pA, cA, pB, cB, sx, sy, sz, Re.eps, thr, Re.typo != 0) != h) ++flips;
-                    if (h) {
+                    if (!Re.typo && certain_hit(pA, cA, pB, cB, sx, sy, sz, thr, Re.eps, Re.slack)) {
+                        ++cert;
                         uint32_t slot = atomicAdd(&ccnt[cid], 1u);
                         if (slot < (uint32_t)kConflictCap) clist[(size_t)cid * kConflictCap + slot] = ti[k];
                         else ++ovf;
+                    } else {
+                        xq_push(xq, xcap, &ctr[C_XQ_CONF], xq_pack(cid, ti[k], img));
                     }
                 }
             }
@@ -305,6 +339,42 @@ __global__ void __launch_bounds__(kTPB) k_conf_tiles(const Real* __restrict__ re
         }
     }
     warp_add_u64(&ctr[C_PAIR_TESTS], tests);
+    warp_add_u64(&ctr[C_OVERFLOW], ovf);
+    warp_add_u64(&ctr[C_CERT], cert);
+}
+
+__global__ void __launch_bounds__(256) k_conf_exact(const Real* __restrict__ reals,
+                                                    const unsigned long long* __restrict__ xq,
+                                                    const unsigned long long* __restrict__ count,
+                                                    unsigned long long cap, const float4* __restrict__ cpos,
+                                                    const float4* __restrict__ cdir, const uint32_t* __restrict__ creal,
+                                                    uint32_t* __restrict__ ccnt, uint32_t* __restrict__ clist,
+                                                    unsigned long long* __restrict__ ctr) {
+    const unsigned long long n = min(*count, cap);
+    unsigned long long exact = 0, flips = 0, ovf = 0;
+    for (unsigned long long e = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; e < n;
+         e += (unsigned long long)gridDim.x * blockDim.x) {
+        uint32_t cid, j;
+        int img[3];
+        xq_unpack(xq[e], &cid, &j, img);
+        const Real& Re = reals[creal[cid]];
+        const float4 pA = cpos[cid], cA = cdir[cid], pB = cpos[j], cB = cdir[j];
+        ++exact;
+        const RodD a = rodd(pA, cA), b = rodd(pB, cB);
+        double d = ref_distance_d(a, b, img[0] * (double)Re.L[0], img[1] * (double)Re.L[1],
+                                  img[2] * (double)Re.L[2], (double)Re.eps, Re.typo != 0, nullptr, nullptr,
+                                  nullptr, nullptr, nullptr);
+        bool h = d < thresh_d(a.a, b.a, (double)Re.scf, (double)Re.sep, (double)Re.eps);
+        const float thr = (cB.w + cA.w) * Re.scf + Re.sep + Re.eps;
+        if (ref_hit_f32(pA, cA, pB, cB, img[0] * Re.L[0], img[1] * Re.L[1], img[2] * Re.L[2], Re.eps, thr,
+                        Re.typo != 0) != h)
+            ++flips;
+        if (h) {
+            uint32_t slot = atomicAdd(&ccnt[cid], 1u);
+            if (slot < (uint32_t)kConflictCap) clist[(size_t)cid * kConflictCap + slot] = j;
+            else ++ovf;
+        }
+    }
     warp_add_u64(&ctr[C_EXACT], exact);
     warp_add_u64(&ctr[C_FLIPS], flips);
     warp_add_u64(&ctr[C_OVERFLOW], ovf);
@@ -802,23 +872,40 @@ nf_status Engine::generate() {
         s = build_chunks(cstart.p, slots);
         if (s != NF_OK) return s;
         const dim3 tg(grid_for(slots, kTPB) + (unsigned)std::min<uint64_t>(ncell, slots), 27);
+        const unsigned xg = (unsigned)(4 * nsm);
+        NF_CK(xq.ensure(xq_cap));
+        NF_CK(xq2.ensure(xq_cap));
+        NF_CK(cudaMemsetAsync(ctr.p + C_XQ_OLD, 0, 2 * sizeof(unsigned long long), st));
         tstart(KT_OLD);
-        if (total_rods() > 0)
+        if (total_rods() > 0) {
             NF_LAUNCH(k_old_tiles, tg, kTPB, 0, st)(dreal.p, choff.p + ncell, chunks.p, cperm.p, gpos.p, gdir.p,
-                                                    rstart.p, spos.p, sdir.p, state.p, ctr.p);
+                                                    rstart.p, spos.p, sdir.p, state.p, xq.p, xq.cap, ctr.p);
+            NF_CK(cudaGetLastError());
+            NF_LAUNCH(k_old_exact, xg, 256, 0, st)(dreal.p, xq.p, ctr.p + C_XQ_OLD, xq.cap, cpos.p, cdir.p, creal.p,
+                                                   spos.p, sdir.p, state.p, ctr.p);
+        }
         NF_CK(cudaGetLastError());
         tstop(KT_OLD);
         NF_CK(cudaMemsetAsync(ctr.p + C_OVERFLOW, 0, sizeof(unsigned long long), st));
         NF_CK(cudaMemsetAsync(ccnt.p, 0, sizeof(uint32_t) * slots, st));
         tstart(KT_CONF);
         NF_LAUNCH(k_conf_tiles, tg, kTPB, 0, st)(dreal.p, choff.p + ncell, chunks.p, cperm.p, cstart.p, gpos.p,
-                                                 gdir.p, csidx.p, state.p, ccnt.p, clist.p, ctr.p);
+                                                 gdir.p, csidx.p, state.p, ccnt.p, clist.p, xq2.p, xq2.cap, ctr.p);
+        NF_CK(cudaGetLastError());
+        NF_LAUNCH(k_conf_exact, xg, 256, 0, st)(dreal.p, xq2.p, ctr.p + C_XQ_CONF, xq2.cap, cpos.p, cdir.p, creal.p,
+                                                ccnt.p, clist.p, ctr.p);
         NF_CK(cudaGetLastError());
         tstop(KT_CONF);
-        unsigned long long ovf = 0;
-        NF_CK(cudaMemcpyAsync(&ovf, ctr.p + C_OVERFLOW, sizeof(ovf), cudaMemcpyDeviceToHost, st));
+        unsigned long long hv[3] = {0, 0, 0};  // conflict overflow, old queue, conflict queue
+        NF_CK(cudaMemcpyAsync(&hv[0], ctr.p + C_OVERFLOW, sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
+        NF_CK(cudaMemcpyAsync(&hv[1], ctr.p + C_XQ_OLD, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
         NF_CK(cudaStreamSynchronize(st));
-        if (ovf) {  // too many in-round conflicts: redo the round with fewer candidates
+        if (hv[1] > xq.cap || hv[2] > xq2.cap) {  // exact queue too small: grow it and redo the round
+            xq_cap = (size_t)(std::max(hv[1], hv[2]) * 1.25) + 1024;
+            --rounds;
+            continue;
+        }
+        if (hv[0]) {  // too many in-round conflicts: redo the round with fewer candidates
             scale *= 0.5;
             if (scale < 1e-4) { err = "in-round conflict list overflow"; return NF_ERR_OVERFLOW; }
             --rounds;
@@ -904,6 +991,7 @@ nf_status Engine::generate() {
     gst.pair_tests = hc[C_PAIR_TESTS];
     gst.exact_evals = hc[C_EXACT];
     gst.fp32_would_flip = hc[C_FLIPS];
+    gst.exact_evals = hc[C_EXACT];
     gst.rounds = rounds;
     gst.target_reached = gst.accepted == gst.target;
     gst.ms = ms;

@@ -11,6 +11,8 @@
 #pragma once
 #include <cstdint>
 
+#include <cooperative_groups.h>
+
 #include "nf_common.cuh"
 
 namespace nf {
@@ -60,6 +62,39 @@ __device__ __forceinline__ bool chunk_neighbour(const Real& Re, uint32_t cell, i
     c[1] = (int)((loc / (uint32_t)Re.n[0]) % (uint32_t)Re.n[1]);
     c[2] = (int)(loc / ((uint32_t)Re.n[0] * (uint32_t)Re.n[1]));
     return stencil(Re, c, o, per, nc, img);
+}
+
+// ---------------------------------------------------------------------------
+// Exact queue: pairs the FP32 filter could not decide are appended here and
+// evaluated afterwards in FP64 by full warps (on GB300 an FP64 warp
+// instruction costs the same with 1 or 32 active lanes). Entry layout:
+// probe (32 bits) | target (26 bits) | image of the target (3 x 2 bits).
+// ---------------------------------------------------------------------------
+constexpr uint32_t kXqTargetBits = 26;
+
+__device__ __forceinline__ unsigned long long xq_pack(uint32_t probe, uint32_t target, const int img[3]) {
+    uint32_t im = (uint32_t)(img[0] + 1) | ((uint32_t)(img[1] + 1) << 2) | ((uint32_t)(img[2] + 1) << 4);
+    return ((unsigned long long)probe << 32) | ((unsigned long long)target << 6) | im;
+}
+
+__device__ __forceinline__ void xq_unpack(unsigned long long e, uint32_t* probe, uint32_t* target, int img[3]) {
+    *probe = (uint32_t)(e >> 32);
+    *target = (uint32_t)((e >> 6) & ((1u << kXqTargetBits) - 1u));
+    img[0] = (int)(e & 3u) - 1;
+    img[1] = (int)((e >> 2) & 3u) - 1;
+    img[2] = (int)((e >> 4) & 3u) - 1;
+}
+
+// Append from divergent code: one atomic per coalesced group of lanes.
+__device__ __forceinline__ void xq_push(unsigned long long* q, unsigned long long cap, unsigned long long* count,
+                                        unsigned long long e) {
+    namespace cg = cooperative_groups;
+    cg::coalesced_group g = cg::coalesced_threads();
+    unsigned long long base = 0;
+    if (g.thread_rank() == 0) base = atomicAdd(count, (unsigned long long)g.size());
+    base = g.shfl(base, 0);
+    unsigned long long slot = base + g.thread_rank();
+    if (slot < cap) q[slot] = e;
 }
 
 // Gather rows of (pos, dir, payload) into cell-sorted order.
