@@ -327,6 +327,14 @@ NF_HD bool maybe_near(const float4& pA, const float4& cA, const float4& pB, cons
     return true;
 }
 
+// The sphere bound of maybe_near with the probe's terms hoisted: hAs = hA +
+// thr-part of A, evaluated once per probe; hB and aB staged with the target.
+// Same inequality as the first test of maybe_near (conservative).
+NF_HD bool sphere_far(float bx, float by, float bz, float hA_plus, float hB, float aB, float scf, float slack) {
+    float Rr = (hA_plus + hB + aB * scf) * 1.000002f + slack;
+    return bx * bx + by * by + bz * bz > Rr * Rr;
+}
+
 // FP32 certificate of a hit. When the reference routine takes its
 // non-parallel branch and leaves both parameters unclamped (|t| <= l/2 + a + eps
 // for both rods), its points are the feet of the common perpendicular and d is

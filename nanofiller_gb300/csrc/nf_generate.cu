@@ -217,9 +217,16 @@ __global__ void __launch_bounds__(kTPB) k_old_tiles(const Real* __restrict__ rea
         for (uint32_t k = threadIdx.x; k < m; k += kTPB) { tp[k] = spos[base + k]; td[k] = sdir[base + k]; }
         __syncthreads();
         if (alive) {
+            // probe terms of the sphere bound: hA + aA*scf + sep + eps
+            const float hAp = pA.w * 0.5f + cA.w + Re.eps + cA.w * Re.scf + Re.sep + Re.eps;
+            const float ax = pA.x - sx, ay = pA.y - sy, az = pA.z - sz;
+            tests += m;
+#pragma unroll 4
             for (uint32_t k = 0; k < m; ++k) {
                 const float4 pB = tp[k], cB = td[k];
-                ++tests;
+                if (sphere_far(pB.x - ax, pB.y - ay, pB.z - az, hAp, pB.w * 0.5f + cB.w + Re.eps, cB.w, Re.scf,
+                               Re.slack))
+                    continue;
                 const float thr = (cB.w + cA.w) * Re.scf + Re.sep + Re.eps;
                 if (!maybe_near(pA, cA, pB, cB, sx, sy, sz, thr, Re.eps, Re.slack)) continue;
                 if (!Re.typo && certain_hit(pA, cA, pB, cB, sx, sy, sz, thr, Re.eps, Re.slack)) {
@@ -319,10 +326,15 @@ __global__ void __launch_bounds__(kTPB) k_conf_tiles(const Real* __restrict__ re
             }
             __syncthreads();
             if (alive) {
+                const float hAp = pA.w * 0.5f + cA.w + Re.eps + cA.w * Re.scf + Re.sep + Re.eps;
+                const float ax = pA.x - sx, ay = pA.y - sy, az = pA.z - sz;
                 for (uint32_t k = 0; k < m; ++k) {
                     if (tk[k] >= kA) continue;
                     const float4 pB = tp[k], cB = td[k];
                     ++tests;
+                    if (sphere_far(pB.x - ax, pB.y - ay, pB.z - az, hAp, pB.w * 0.5f + cB.w + Re.eps, cB.w, Re.scf,
+                                   Re.slack))
+                        continue;
                     const float thr = (cB.w + cA.w) * Re.scf + Re.sep + Re.eps;
                     if (!maybe_near(pA, cA, pB, cB, sx, sy, sz, thr, Re.eps, Re.slack)) continue;
                     if (!Re.typo && certain_hit(pA, cA, pB, cB, sx, sy, sz, thr, Re.eps, Re.slack)) {
@@ -788,8 +800,9 @@ nf_status Engine::generate() {
         size_bounds(p, &lmax, &amax);
         double V = (double)p.box[0] * p.box[1] * p.box[2];
         double vex = 0.5 * M_PI * lmax * lmax * (2 * amax + p.sep) + 1e-12;
-        // ~8 expected in-round conflicts per survivor at the density peak
-        alive_max[r] = std::max(4096.0, 8.0 * V / (vex * peak));
+        // ~32 expected in-round conflicts per survivor at the density peak
+        // (a conflict list overflow redoes the round at half size)
+        alive_max[r] = std::max(8192.0, 32.0 * V / (vex * peak));
     }
     std::vector<uint32_t> hcoff(R + 1);
     std::vector<uint64_t> hkbeg(R), hout(2 * R);
@@ -896,38 +909,40 @@ nf_status Engine::generate() {
                                                 ccnt.p, clist.p, ctr.p);
         NF_CK(cudaGetLastError());
         tstop(KT_CONF);
-        unsigned long long hv[3] = {0, 0, 0};  // conflict overflow, old queue, conflict queue
-        NF_CK(cudaMemcpyAsync(&hv[0], ctr.p + C_OVERFLOW, sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
-        NF_CK(cudaMemcpyAsync(&hv[1], ctr.p + C_XQ_OLD, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
-        NF_CK(cudaStreamSynchronize(st));
-        if (hv[1] > xq.cap || hv[2] > xq2.cap) {  // exact queue too small: grow it and redo the round
-            xq_cap = (size_t)(std::max(hv[1], hv[2]) * 1.25) + 1024;
-            --rounds;
-            continue;
-        }
-        if (hv[0]) {  // too many in-round conflicts: redo the round with fewer candidates
-            scale *= 0.5;
-            if (scale < 1e-4) { err = "in-round conflict list overflow"; return NF_ERR_OVERFLOW; }
-            --rounds;
-            continue;
-        }
-        // Resolution passes (chains are short; bounded by the round size).
+        // Resolution passes (chains are short), then one read-back of the
+        // overflow / queue / undecided counters.
         uint64_t passes = 0;
+        bool redo = false;
         for (;;) {
-            NF_CK(cudaMemsetAsync(ctr.p + C_UNDECIDED, 0, sizeof(unsigned long long), st));
-            for (int q = 0; q < 4; ++q)
+            for (int q = 0; q < 3; ++q)
                 NF_LAUNCH(k_resolve, gs, 256, 0, st)(ntot, state.p, ccnt.p, clist.p, ctr.p);
-            NF_CK(cudaGetLastError());
-            passes += 4;
-            // The last pass's undecided count: re-zero then one more pass.
             NF_CK(cudaMemsetAsync(ctr.p + C_UNDECIDED, 0, sizeof(unsigned long long), st));
             NF_LAUNCH(k_resolve, gs, 256, 0, st)(ntot, state.p, ccnt.p, clist.p, ctr.p);
-            ++passes;
-            unsigned long long und = 0;
-            NF_CK(cudaMemcpyAsync(&und, ctr.p + C_UNDECIDED, sizeof(und), cudaMemcpyDeviceToHost, st));
+            NF_CK(cudaGetLastError());
+            passes += 4;
+            unsigned long long hv[4] = {0, 0, 0, 0};  // conflict overflow, undecided, old queue, conflict queue
+            NF_CK(cudaMemcpyAsync(&hv[0], ctr.p + C_OVERFLOW, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                                  st));
+            NF_CK(cudaMemcpyAsync(&hv[2], ctr.p + C_XQ_OLD, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                                  st));
             NF_CK(cudaStreamSynchronize(st));
-            if (!und) break;
+            if (hv[2] > xq.cap || hv[3] > xq2.cap) {  // exact queue too small: grow it and redo the round
+                xq_cap = (size_t)(std::max(hv[2], hv[3]) * 1.25) + 1024;
+                redo = true;
+                break;
+            }
+            if (hv[0]) {  // too many in-round conflicts: redo the round with fewer candidates
+                scale *= 0.5;
+                if (scale < 1e-4) { err = "in-round conflict list overflow"; return NF_ERR_OVERFLOW; }
+                redo = true;
+                break;
+            }
+            if (!hv[1]) break;
             if (passes > 4096) { err = "conflict resolution did not converge"; return NF_ERR_TIMEOUT; }
+        }
+        if (redo) {
+            --rounds;
+            continue;
         }
         // Append.
         NF_LAUNCH(k_accflag, grid_for(slots + 1, 256), 256, 0, st)(ntot, (uint32_t)(slots + 1), state.p, accf.p);
