@@ -800,9 +800,9 @@ nf_status Engine::generate() {
         size_bounds(p, &lmax, &amax);
         double V = (double)p.box[0] * p.box[1] * p.box[2];
         double vex = 0.5 * M_PI * lmax * lmax * (2 * amax + p.sep) + 1e-12;
-        // ~32 expected in-round conflicts per survivor at the density peak
+        // ~8 expected in-round conflicts per survivor at the density peak
         // (a conflict list overflow redoes the round at half size)
-        alive_max[r] = std::max(8192.0, 32.0 * V / (vex * peak));
+        alive_max[r] = std::max(4096.0, 8.0 * V / (vex * peak));
     }
     std::vector<uint32_t> hcoff(R + 1);
     std::vector<uint64_t> hkbeg(R), hout(2 * R);
