@@ -221,7 +221,6 @@ __global__ void __launch_bounds__(kTPB) k_old_tiles(const Real* __restrict__ rea
             const float hAp = pA.w * 0.5f + cA.w + Re.eps + cA.w * Re.scf + Re.sep + Re.eps;
             const float ax = pA.x - sx, ay = pA.y - sy, az = pA.z - sz;
             tests += m;
-#pragma unroll 4
             for (uint32_t k = 0; k < m; ++k) {
                 const float4 pB = tp[k], cB = td[k];
                 if (sphere_far(pB.x - ax, pB.y - ay, pB.z - az, hAp, pB.w * 0.5f + cB.w + Re.eps, cB.w, Re.scf,
@@ -821,7 +820,7 @@ nf_status Engine::generate() {
             if (count[r] < tgt && knext[r] < p.n_candidates) {
                 double acc_rate = p_dens[r];
                 if (knext[r] > 0 && dens_acc[r] > 0)
-                    acc_rate = ((double)dens_acc[r] / knext[r]) * std::max(0.02, (double)count[r] / dens_acc[r]);
+                    acc_rate = ((double)dens_acc[r] / knext[r]) * std::max(1e-6, (double)count[r] / dens_acc[r]);
                 double want = (tgt - count[r]) / std::max(acc_rate, 1e-6) * 1.2 + 256;
                 // survivors of the old-rod test per round stay near alive_max
                 double amax_c = alive_max[r] / std::max(acc_rate, 1e-6);
