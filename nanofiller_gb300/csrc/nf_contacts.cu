@@ -40,44 +40,55 @@ __global__ void __launch_bounds__(kTPB) k_ct_tiles(const Real* __restrict__ real
                                                    const float4* __restrict__ spos, const float4* __restrict__ sdir,
                                                    const uint32_t* __restrict__ sid, unsigned long long* __restrict__ xq,
                                                    unsigned long long xcap, unsigned long long* __restrict__ ctr) {
-    __shared__ float4 tp[kTile], td[kTile];
-    __shared__ uint32_t ti[kTile];
-    const uint32_t ch = blockIdx.x;
-    if (ch >= *nchunk) return;
-    const Chunk C = chunks[ch];
-    const Real& Re = reals[C.real];
+    __shared__ WarpTile tiles[kTPB / 32];
+    __shared__ uint32_t tid_[kTPB / 32][kWT];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint32_t ch = blockIdx.x * (kTPB / 32) + w;
+    const float epc = 1e-6f;  // DEV_PRECISION (inc/definitions.h:5)
+    unsigned long long tests = 0;
     uint32_t nc;
     int img[3];
-    if (!chunk_neighbour(Re, C.cell, (int)blockIdx.y, Re.per_con, &nc, img)) return;
-    const uint32_t t0 = rstart[nc], t1 = rstart[nc + 1];
-    if (t0 == t1) return;
-    const bool have = threadIdx.x < C.n;
-    const uint32_t q = C.first + threadIdx.x;
-    uint32_t i = 0;
-    float4 pA = make_float4(0, 0, 0, 0), cA = pA;
-    if (have) { i = sid[q]; pA = spos[q]; cA = sdir[q]; }
-    const float epc = 1e-6f;  // DEV_PRECISION (inc/definitions.h:5)
-    const float sx = img[0] * Re.L[0], sy = img[1] * Re.L[1], sz = img[2] * Re.L[2];
-    unsigned long long tests = 0;
-    for (uint32_t base = t0; base < t1; base += kTile) {
-        const uint32_t m = min((uint32_t)kTile, t1 - base);
-        for (uint32_t k = threadIdx.x; k < m; k += kTPB) {
-            tp[k] = spos[base + k];
-            td[k] = sdir[base + k];
-            ti[k] = sid[base + k];
-        }
-        __syncthreads();
-        if (have) {
-            for (uint32_t k = 0; k < m; ++k) {
-                if (ti[k] <= i) continue;
-                const float4 pB = tp[k], cB = td[k];
-                ++tests;
-                const float thr = (cB.w + cA.w) + Re.cut + epc;
-                if (!maybe_near(pA, cA, pB, cB, sx, sy, sz, thr, epc, Re.slack)) continue;
-                xq_push(xq, xcap, &ctr[C_XQ], xq_pack(q, base + k, img));
+    const Chunk C = ch < *nchunk ? chunks[ch] : Chunk{0, 0, 0, 0};
+    const Real& Re = reals[C.real];
+    if (C.n && chunk_neighbour(Re, C.cell, (int)blockIdx.y, Re.per_con, &nc, img)) {
+        const uint32_t t0 = rstart[nc], t1 = rstart[nc + 1];
+        const bool have = (uint32_t)lane < C.n;
+        const uint32_t q = C.first + lane;
+        uint32_t i = 0;
+        float4 pA = make_float4(0, 0, 0, 0), cA = pA;
+        if (have) { i = sid[q]; pA = spos[q]; cA = sdir[q]; }
+        const float sx = img[0] * Re.L[0], sy = img[1] * Re.L[1], sz = img[2] * Re.L[2];
+        const float ax = pA.x - sx, ay = pA.y - sy, az = pA.z - sz;
+        const float hAp = pA.w * 0.5f + cA.w + epc + cA.w + Re.cut + epc;
+        WarpTile& T = tiles[w];
+        for (uint32_t base = t0; base < t1; base += kWT) {
+            const uint32_t k = base + lane;
+            if (k < t1) {
+                const float4 p = spos[k], c = sdir[k];
+                T.l[lane] = p.w;
+                T.p[lane] = make_float4(p.x, p.y, p.z, p.w * 0.5f + c.w + epc + c.w);
+                T.c[lane] = c;
+                tid_[w][lane] = sid[k];
             }
+            __syncwarp();
+            const uint32_t m = min((uint32_t)kWT, t1 - base);
+            if (have) {
+                for (uint32_t j = 0; j < m; ++j) {
+                    if (tid_[w][j] <= i) continue;  // each unordered pair once (J > I)
+                    ++tests;
+                    const float4 tq = T.p[j];
+                    const float bx = tq.x - ax, by = tq.y - ay, bz = tq.z - az;
+                    const float Rr = (hAp + tq.w) * 1.000002f + Re.slack;
+                    if (bx * bx + by * by + bz * bz > Rr * Rr) continue;
+                    const float4 cB = T.c[j];
+                    const float4 pB = make_float4(tq.x, tq.y, tq.z, T.l[j]);
+                    const float thr = (cB.w + cA.w) + Re.cut + epc;
+                    if (!maybe_near(pA, cA, pB, cB, sx, sy, sz, thr, epc, Re.slack)) continue;
+                    xq_push(xq, xcap, &ctr[C_XQ], xq_pack(q, base + j, img));
+                }
+            }
+            __syncwarp();
         }
-        __syncthreads();
     }
     warp_add_u64(&ctr[C_CT_PAIRS], tests);
 }
@@ -238,42 +249,47 @@ __global__ void __launch_bounds__(kTPB) k_scr_tiles(const Real* __restrict__ rea
                                                     const float4* __restrict__ spos, const float4* __restrict__ sdir,
                                                     unsigned long long* __restrict__ xq, unsigned long long xcap,
                                                     unsigned long long* __restrict__ ctr) {
-    __shared__ float4 tp[kTile], td[kTile];
-    const uint32_t ch = blockIdx.x;
-    if (ch >= *nchunk) return;
-    const Chunk C = chunks[ch];
-    const Real& Re = reals[C.real];
-    uint32_t nc;
-    int img[3];
-    if (!chunk_neighbour(Re, C.cell, (int)blockIdx.y, Re.per_con, &nc, img)) return;
-    const uint32_t t0 = rstart[nc], t1 = rstart[nc + 1];
-    if (t0 == t1) return;
-    const bool have = threadIdx.x < C.n;
-    const uint32_t id = have ? vperm[C.first + threadIdx.x] : 0u;
-    float4 pV = make_float4(0, 0, 0, 0), cV = pV;
-    float svf[3] = {0, 0, 0};
-    if (have) {
-        const double* o = vd + (size_t)kVD * id;
-        for (int d = 0; d < 3; ++d) svf[d] = (float)dsub(o[8 + d], img[d] * (double)Re.L[d]);
-        pV = vpf[id];
-        cV = vdf[id];
-    }
+    __shared__ WarpTile tiles[kTPB / 32];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint32_t ch = blockIdx.x * (kTPB / 32) + w;
     const float epsf = 1e-6f;
     unsigned long long tests = 0;
-    for (uint32_t base = t0; base < t1; base += kTile) {
-        const uint32_t m = min((uint32_t)kTile, t1 - base);
-        for (uint32_t k = threadIdx.x; k < m; k += kTPB) { tp[k] = spos[base + k]; td[k] = sdir[base + k]; }
-        __syncthreads();
+    uint32_t nc;
+    int img[3];
+    const Chunk C = ch < *nchunk ? chunks[ch] : Chunk{0, 0, 0, 0};
+    const Real& Re = reals[C.real];
+    if (C.n && chunk_neighbour(Re, C.cell, (int)blockIdx.y, Re.per_con, &nc, img)) {
+        const uint32_t t0 = rstart[nc], t1 = rstart[nc + 1];
+        const bool have = (uint32_t)lane < C.n;
+        const uint32_t id = have ? vperm[C.first + lane] : 0u;
+        float4 pV = make_float4(0, 0, 0, 0), cV = pV;
+        float svf[3] = {0, 0, 0};
         if (have) {
-            for (uint32_t k = 0; k < m; ++k) {
-                const float4 pR = tp[k], cR = td[k];
-                ++tests;
-                const float thr = (cV.w + cR.w) + epsf;
-                if (!maybe_near(pR, cR, pV, cV, svf[0], svf[1], svf[2], thr, epsf, Re.slack)) continue;
-                xq_push(xq, xcap, &ctr[C_XQ], xq_pack(id, base + k, img));
-            }
+            const double* o = vd + (size_t)kVD * id;
+            for (int d = 0; d < 3; ++d) svf[d] = (float)dsub(o[8 + d], img[d] * (double)Re.L[d]);
+            pV = vpf[id];
+            cV = vdf[id];
         }
-        __syncthreads();
+        WarpTile& T = tiles[w];
+        for (uint32_t base = t0; base < t1; base += kWT) {
+            const uint32_t k = base + lane;
+            if (k < t1) {
+                T.p[lane] = spos[k];
+                T.c[lane] = sdir[k];
+            }
+            __syncwarp();
+            const uint32_t m = min((uint32_t)kWT, t1 - base);
+            if (have) {
+                tests += m;
+                for (uint32_t j = 0; j < m; ++j) {
+                    const float4 pR = T.p[j], cR = T.c[j];
+                    const float thr = (cV.w + cR.w) + epsf;
+                    if (!maybe_near(pR, cR, pV, cV, svf[0], svf[1], svf[2], thr, epsf, Re.slack)) continue;
+                    xq_push(xq, xcap, &ctr[C_XQ], xq_pack(id, base + j, img));
+                }
+            }
+            __syncwarp();
+        }
     }
     warp_add_u64(&ctr[C_SCR_PAIRS], tests);
 }
@@ -514,7 +530,7 @@ nf_status Engine::contacts() {
     size_t cap = std::max<size_t>(rec.cap, std::max<size_t>(4096, 2 * nrods));
     nf_status s = build_chunks(rstart.p, nrods);
     if (s != NF_OK) return s;
-    const dim3 tg(grid_for(nrods, kTPB) + ncell, 27);
+    const dim3 tg(grid_for((uint64_t)nrods / kWC + ncell + 1, kTPB / 32), 27);
     const unsigned xg = (unsigned)(4 * nsm);
     for (int attempt = 0; attempt < 4; ++attempt) {
         NF_CK(rec.ensure(cap));
@@ -571,7 +587,7 @@ nf_status Engine::contacts() {
             NF_CK(cudaGetLastError());
             s = build_chunks(vstart.p, nrec);
             if (s != NF_OK) return s;
-            const dim3 vg(grid_for(nrec, kTPB) + ncell, 27);
+            const dim3 vg(grid_for((uint64_t)nrec / kWC + ncell + 1, kTPB / 32), 27);
             for (int attempt = 0; attempt < 3; ++attempt) {
                 NF_CK(xq.ensure(xq_cap));
                 NF_CK(cudaMemsetAsync(ctr.p + C_XQ, 0, sizeof(unsigned long long), st));

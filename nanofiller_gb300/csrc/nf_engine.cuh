@@ -118,6 +118,9 @@ struct Engine {
     DBuf<uint64_t> kbeg, csidx;
     DBuf<float4> cpos, cdir;
     DBuf<float4> gpos, gdir;     // candidates in cell order
+    DBuf<float4> apos, adir;     // survivors of the old-rod test in cell order
+    DBuf<uint64_t> akey;         // their stream indices
+    DBuf<uint32_t> aperm, astart;
     DBuf<Chunk> chunks;          // (cell, probe range) work table of the pair kernels
     DBuf<unsigned long long> xq, xq2;  // exact queues (pairs left to FP64)
     size_t xq_cap = 1 << 16;

@@ -179,9 +179,11 @@ __global__ void k_bin(uint32_t n, const uint32_t* __restrict__ ntot, const uint3
     perm[q] = i;
 }
 
-// Candidate vs accepted rods of one neighbour cell (cuda_OldExtIsectLB's job),
-// one (candidate chunk, stencil offset) per block, targets staged in shared
-// memory. Far pairs are dropped and clear hits decided in FP32; the rest go to
+// Candidate vs accepted rods of one neighbour cell (cuda_OldExtIsectLB's job).
+// One warp per (chunk of <= 32 candidates of a cell, stencil offset); the
+// warp stages the neighbour cell's rods 32 at a time in its own shared-memory
+// tile and every lane tests its candidate against each staged rod (broadcast
+// reads). Far pairs are dropped and clear hits decided in FP32; the rest go to
 // the exact queue (probe = compact candidate id, target = sorted rod index).
 __global__ void __launch_bounds__(kTPB) k_old_tiles(const Real* __restrict__ reals,
                                                     const uint32_t* __restrict__ nchunk,
@@ -192,53 +194,61 @@ __global__ void __launch_bounds__(kTPB) k_old_tiles(const Real* __restrict__ rea
                                                     const float4* __restrict__ spos, const float4* __restrict__ sdir,
                                                     uint8_t* state, unsigned long long* __restrict__ xq,
                                                     unsigned long long xcap, unsigned long long* __restrict__ ctr) {
-    __shared__ float4 tp[kTile], td[kTile];
-    const uint32_t ch = blockIdx.x;
-    if (ch >= *nchunk) return;
-    const Chunk C = chunks[ch];
-    const Real& Re = reals[C.real];
+    __shared__ WarpTile tiles[kTPB / 32];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint32_t ch = blockIdx.x * (kTPB / 32) + w;
+    unsigned long long tests = 0, cert = 0;
     uint32_t nc;
     int img[3];
-    if (!chunk_neighbour(Re, C.cell, (int)blockIdx.y, Re.per_gen, &nc, img)) return;
-    const uint32_t t0 = rstart[nc], t1 = rstart[nc + 1];
-    if (t0 == t1) return;
-    volatile uint8_t* vst = state;
-    const bool have = threadIdx.x < C.n;
-    const uint32_t q = C.first + threadIdx.x;
-    const uint32_t cid = have ? cperm[q] : 0u;
-    float4 pA = make_float4(0, 0, 0, 0), cA = pA;
-    if (have) { pA = gpos[q]; cA = gdir[q]; }
-    bool alive = have && vst[cid] != ST_REJ_OLD;
-    const float sx = img[0] * Re.L[0], sy = img[1] * Re.L[1], sz = img[2] * Re.L[2];
-    unsigned long long tests = 0, cert = 0;
-    for (uint32_t base = t0; base < t1; base += kTile) {
-        if (!__syncthreads_or(alive)) break;
-        const uint32_t m = min((uint32_t)kTile, t1 - base);
-        for (uint32_t k = threadIdx.x; k < m; k += kTPB) { tp[k] = spos[base + k]; td[k] = sdir[base + k]; }
-        __syncthreads();
-        if (alive) {
-            // probe terms of the sphere bound: hA + aA*scf + sep + eps
-            const float hAp = pA.w * 0.5f + cA.w + Re.eps + cA.w * Re.scf + Re.sep + Re.eps;
-            const float ax = pA.x - sx, ay = pA.y - sy, az = pA.z - sz;
-            tests += m;
-            for (uint32_t k = 0; k < m; ++k) {
-                const float4 pB = tp[k], cB = td[k];
-                if (sphere_far(pB.x - ax, pB.y - ay, pB.z - az, hAp, pB.w * 0.5f + cB.w + Re.eps, cB.w, Re.scf,
-                               Re.slack))
-                    continue;
-                const float thr = (cB.w + cA.w) * Re.scf + Re.sep + Re.eps;
-                if (!maybe_near(pA, cA, pB, cB, sx, sy, sz, thr, Re.eps, Re.slack)) continue;
-                if (!Re.typo && certain_hit(pA, cA, pB, cB, sx, sy, sz, thr, Re.eps, Re.slack)) {
-                    ++cert;
-                    vst[cid] = ST_REJ_OLD;
-                    alive = false;
-                    break;
-                }
-                xq_push(xq, xcap, &ctr[C_XQ_OLD], xq_pack(cid, base + k, img));
+    const Chunk C = ch < *nchunk ? chunks[ch] : Chunk{0, 0, 0, 0};
+    const Real& Re = reals[C.real];
+    if (C.n && chunk_neighbour(Re, C.cell, (int)blockIdx.y, Re.per_gen, &nc, img)) {
+        const uint32_t t0 = rstart[nc], t1 = rstart[nc + 1];
+        volatile uint8_t* vst = state;
+        const bool have = (uint32_t)lane < C.n;
+        const uint32_t q = C.first + lane;
+        const uint32_t cid = have ? cperm[q] : 0u;
+        float4 pA = make_float4(0, 0, 0, 0), cA = pA;
+        if (have) { pA = gpos[q]; cA = gdir[q]; }
+        bool alive = have && vst[cid] != ST_REJ_OLD;
+        const float sx = img[0] * Re.L[0], sy = img[1] * Re.L[1], sz = img[2] * Re.L[2];
+        const float ax = pA.x - sx, ay = pA.y - sy, az = pA.z - sz;
+        const float hAp = pA.w * 0.5f + cA.w + Re.eps + cA.w * Re.scf + Re.sep + Re.eps;
+        WarpTile& T = tiles[w];
+        for (uint32_t base = t0; base < t1; base += kWT) {
+            if (!__any_sync(0xffffffffu, alive)) break;
+            const uint32_t k = base + lane;
+            if (k < t1) {
+                const float4 p = spos[k], c = sdir[k];
+                T.l[lane] = p.w;
+                T.p[lane] = make_float4(p.x, p.y, p.z, p.w * 0.5f + c.w + Re.eps + c.w * Re.scf);
+                T.c[lane] = c;
             }
-            if (alive && vst[cid] == ST_REJ_OLD) alive = false;  // decided by another block
+            __syncwarp();
+            const uint32_t m = min((uint32_t)kWT, t1 - base);
+            if (alive) {
+                tests += m;
+                for (uint32_t j = 0; j < m; ++j) {
+                    const float4 tq = T.p[j];
+                    const float bx = tq.x - ax, by = tq.y - ay, bz = tq.z - az;
+                    const float Rr = (hAp + tq.w) * 1.000002f + Re.slack;
+                    if (bx * bx + by * by + bz * bz > Rr * Rr) continue;
+                    const float4 cB = T.c[j];
+                    const float4 pB = make_float4(tq.x, tq.y, tq.z, T.l[j]);
+                    const float thr = (cB.w + cA.w) * Re.scf + Re.sep + Re.eps;
+                    if (!maybe_near(pA, cA, pB, cB, sx, sy, sz, thr, Re.eps, Re.slack)) continue;
+                    if (!Re.typo && certain_hit(pA, cA, pB, cB, sx, sy, sz, thr, Re.eps, Re.slack)) {
+                        ++cert;
+                        vst[cid] = ST_REJ_OLD;
+                        alive = false;
+                        break;
+                    }
+                    xq_push(xq, xcap, &ctr[C_XQ_OLD], xq_pack(cid, base + j, img));
+                }
+                if (alive && vst[cid] == ST_REJ_OLD) alive = false;  // decided by another warp
+            }
+            __syncwarp();
         }
-        __syncthreads();
     }
     warp_add_u64(&ctr[C_PAIR_TESTS], tests);
     warp_add_u64(&ctr[C_CERT], cert);
@@ -279,74 +289,104 @@ __global__ void __launch_bounds__(256) k_old_exact(const Real* __restrict__ real
     warp_add_u64(&ctr[C_FLIPS], flips);
 }
 
-// Earlier surviving candidates of one neighbour cell that a survivor hits.
-// Certified hits are listed directly, uncertain pairs queued (target = compact id).
+// Survivors of the old-rod test, binned by cell (stream order is kept in the
+// per-candidate key): the in-round conflict sweep runs over these only.
+__global__ void k_alive_count(uint32_t n, const uint32_t* __restrict__ ntot, const uint32_t* __restrict__ cperm,
+                              const uint8_t* __restrict__ state, const uint32_t* __restrict__ ccell,
+                              uint32_t* __restrict__ acount) {
+    uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= *ntot) return;
+    uint32_t cid = cperm[q];
+    if (state[cid] == ST_ALIVE) atomicAdd(&acount[ccell[cid]], 1u);
+}
+
+__global__ void k_alive_bin(uint32_t n, const uint32_t* __restrict__ ntot, const uint32_t* __restrict__ cperm,
+                            const uint8_t* __restrict__ state, const uint32_t* __restrict__ ccell,
+                            const uint32_t* __restrict__ astart, uint32_t* __restrict__ acur,
+                            const float4* __restrict__ gpos, const float4* __restrict__ gdir,
+                            const uint64_t* __restrict__ csidx, uint32_t* __restrict__ aperm,
+                            float4* __restrict__ apos, float4* __restrict__ adir, uint64_t* __restrict__ akey) {
+    uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= *ntot) return;
+    uint32_t cid = cperm[q];
+    if (state[cid] != ST_ALIVE) return;
+    uint32_t cell = ccell[cid];
+    uint32_t d = astart[cell] + atomicAdd(&acur[cell], 1u);
+    aperm[d] = cid;
+    apos[d] = gpos[q];
+    adir[d] = gdir[q];
+    akey[d] = csidx[cid];
+}
+
+// Earlier survivors of one neighbour cell that a survivor hits (one warp per
+// (survivor chunk, offset)). Certified hits are listed directly, uncertain
+// pairs queued (target = compact candidate id).
 __global__ void __launch_bounds__(kTPB) k_conf_tiles(const Real* __restrict__ reals,
                                                      const uint32_t* __restrict__ nchunk,
                                                      const Chunk* __restrict__ chunks,
-                                                     const uint32_t* __restrict__ cperm,
-                                                     const uint32_t* __restrict__ cstart,
-                                                     const float4* __restrict__ gpos, const float4* __restrict__ gdir,
-                                                     const uint64_t* __restrict__ csidx,
-                                                     const uint8_t* __restrict__ state, uint32_t* __restrict__ ccnt,
+                                                     const uint32_t* __restrict__ aperm,
+                                                     const uint32_t* __restrict__ astart,
+                                                     const float4* __restrict__ apos, const float4* __restrict__ adir,
+                                                     const uint64_t* __restrict__ akey, uint32_t* __restrict__ ccnt,
                                                      uint32_t* __restrict__ clist, unsigned long long* __restrict__ xq,
                                                      unsigned long long xcap, unsigned long long* __restrict__ ctr) {
-    __shared__ float4 tp[kTile], td[kTile];
-    __shared__ uint64_t tk[kTile];
-    __shared__ uint32_t ti[kTile];
-    const uint32_t ch = blockIdx.x;
-    if (ch >= *nchunk) return;
-    const Chunk C = chunks[ch];
-    const Real& Re = reals[C.real];
+    __shared__ WarpTile tiles[kTPB / 32];
+    __shared__ uint64_t tkey[kTPB / 32][kWT];
+    __shared__ uint32_t tid_[kTPB / 32][kWT];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint32_t ch = blockIdx.x * (kTPB / 32) + w;
+    unsigned long long tests = 0, ovf = 0, cert = 0;
     uint32_t nc;
     int img[3];
-    if (!chunk_neighbour(Re, C.cell, (int)blockIdx.y, Re.per_gen, &nc, img)) return;
-    const uint32_t t0 = cstart[nc], t1 = cstart[nc + 1];
-    if (t0 == t1) return;
-    const bool have = threadIdx.x < C.n;
-    const uint32_t q = C.first + threadIdx.x;
-    const uint32_t cid = have ? cperm[q] : 0u;
-    float4 pA = make_float4(0, 0, 0, 0), cA = pA;
-    uint64_t kA = 0;
-    bool alive = have && state[cid] == ST_ALIVE;
-    if (alive) { pA = gpos[q]; cA = gdir[q]; kA = csidx[cid]; }
-    const float sx = img[0] * Re.L[0], sy = img[1] * Re.L[1], sz = img[2] * Re.L[2];
-    unsigned long long tests = 0, ovf = 0, cert = 0;
-    if (__syncthreads_or(alive)) {
-        for (uint32_t base = t0; base < t1; base += kTile) {
-            const uint32_t m = min((uint32_t)kTile, t1 - base);
-            for (uint32_t k = threadIdx.x; k < m; k += kTPB) {
-                const uint32_t j = cperm[base + k];
-                tp[k] = gpos[base + k];
-                td[k] = gdir[base + k];
-                ti[k] = j;
-                // only earlier survivors matter: fold both conditions into the key
-                tk[k] = state[j] == ST_ALIVE ? csidx[j] : ~0ull;
+    const Chunk C = ch < *nchunk ? chunks[ch] : Chunk{0, 0, 0, 0};
+    const Real& Re = reals[C.real];
+    if (C.n && chunk_neighbour(Re, C.cell, (int)blockIdx.y, Re.per_gen, &nc, img)) {
+        const uint32_t t0 = astart[nc], t1 = astart[nc + 1];
+        const bool have = (uint32_t)lane < C.n;
+        const uint32_t q = C.first + lane;
+        const uint32_t cid = have ? aperm[q] : 0u;
+        float4 pA = make_float4(0, 0, 0, 0), cA = pA;
+        uint64_t kA = 0;
+        if (have) { pA = apos[q]; cA = adir[q]; kA = akey[q]; }
+        const float sx = img[0] * Re.L[0], sy = img[1] * Re.L[1], sz = img[2] * Re.L[2];
+        const float ax = pA.x - sx, ay = pA.y - sy, az = pA.z - sz;
+        const float hAp = pA.w * 0.5f + cA.w + Re.eps + cA.w * Re.scf + Re.sep + Re.eps;
+        WarpTile& T = tiles[w];
+        for (uint32_t base = t0; base < t1; base += kWT) {
+            const uint32_t k = base + lane;
+            if (k < t1) {
+                const float4 p = apos[k], c = adir[k];
+                T.l[lane] = p.w;
+                T.p[lane] = make_float4(p.x, p.y, p.z, p.w * 0.5f + c.w + Re.eps + c.w * Re.scf);
+                T.c[lane] = c;
+                tkey[w][lane] = akey[k];
+                tid_[w][lane] = aperm[k];
             }
-            __syncthreads();
-            if (alive) {
-                const float hAp = pA.w * 0.5f + cA.w + Re.eps + cA.w * Re.scf + Re.sep + Re.eps;
-                const float ax = pA.x - sx, ay = pA.y - sy, az = pA.z - sz;
-                for (uint32_t k = 0; k < m; ++k) {
-                    if (tk[k] >= kA) continue;
-                    const float4 pB = tp[k], cB = td[k];
+            __syncwarp();
+            const uint32_t m = min((uint32_t)kWT, t1 - base);
+            if (have) {
+                for (uint32_t j = 0; j < m; ++j) {
+                    if (tkey[w][j] >= kA) continue;  // earlier survivors only
                     ++tests;
-                    if (sphere_far(pB.x - ax, pB.y - ay, pB.z - az, hAp, pB.w * 0.5f + cB.w + Re.eps, cB.w, Re.scf,
-                                   Re.slack))
-                        continue;
+                    const float4 tq = T.p[j];
+                    const float bx = tq.x - ax, by = tq.y - ay, bz = tq.z - az;
+                    const float Rr = (hAp + tq.w) * 1.000002f + Re.slack;
+                    if (bx * bx + by * by + bz * bz > Rr * Rr) continue;
+                    const float4 cB = T.c[j];
+                    const float4 pB = make_float4(tq.x, tq.y, tq.z, T.l[j]);
                     const float thr = (cB.w + cA.w) * Re.scf + Re.sep + Re.eps;
                     if (!maybe_near(pA, cA, pB, cB, sx, sy, sz, thr, Re.eps, Re.slack)) continue;
                     if (!Re.typo && certain_hit(pA, cA, pB, cB, sx, sy, sz, thr, Re.eps, Re.slack)) {
                         ++cert;
                         uint32_t slot = atomicAdd(&ccnt[cid], 1u);
-                        if (slot < (uint32_t)kConflictCap) clist[(size_t)cid * kConflictCap + slot] = ti[k];
+                        if (slot < (uint32_t)kConflictCap) clist[(size_t)cid * kConflictCap + slot] = tid_[w][j];
                         else ++ovf;
                     } else {
-                        xq_push(xq, xcap, &ctr[C_XQ_CONF], xq_pack(cid, ti[k], img));
+                        xq_push(xq, xcap, &ctr[C_XQ_CONF], xq_pack(cid, tid_[w][j], img));
                     }
                 }
             }
-            __syncthreads();
+            __syncwarp();
         }
     }
     warp_add_u64(&ctr[C_PAIR_TESTS], tests);
@@ -549,8 +589,8 @@ nf_status Engine::build_chunks(const uint32_t* pstart, size_t nprobes) {
     NF_CK(cudaGetLastError());
     nf_status s = scan_u32(nch.p, choff.p, ncell + 1);
     if (s != NF_OK) return s;
-    // Upper bound on chunks: all probes over kTPB plus one partial chunk per cell.
-    NF_CK(chunks.ensure((size_t)ncell + nprobes / kTPB + 1));
+    // Upper bound on chunks: all probes over kWC plus one partial chunk per cell.
+    NF_CK(chunks.ensure((size_t)ncell + nprobes / kWC + 1));
     NF_LAUNCH(k_chunk_fill, grid_for(ncell, 256), 256, 0, st)(ncell, R, celloff.p, pstart, choff.p, chunks.p);
     NF_CK(cudaGetLastError());
     return NF_OK;
@@ -604,15 +644,15 @@ nf_status Engine::set_density(int r, int nx, int ny, int nz, const float* values
 }
 
 void Engine::release() {
-    DBuf<float4>* f4[] = {&pos, &dir, &spos, &sdir, &cpos, &cdir, &gpos, &gdir, &vpf, &vdf};
+    DBuf<float4>* f4[] = {&pos, &dir, &spos, &sdir, &cpos, &cdir, &gpos, &gdir, &vpf, &vdf, &apos, &adir};
     for (auto* b : f4) b->release();
-    DBuf<uint32_t>* u32[] = {&nch, &choff, &celloff, &vcell, &vperm, &vstart, &vcur,
+    DBuf<uint32_t>* u32[] = {&nch, &choff, &celloff, &vcell, &vperm, &vstart, &vcur, &aperm, &astart,
                              &dcount, &rodoff, &rstart, &rcursor, &sid, &coff, &keep, &kpos, &ccount,
                              &cstart, &ccursor, &cperm, &creal, &ccell, &ccnt, &clist, &accf, &accpos,
                              &meta, &u32tmp, &rcnt, &rpos, &rcur, &cI, &cJ, &creal2, &eflag, &parent,
                              &cflag, &aidx, &rowp, &col, &deg};
     for (auto* b : u32) b->release();
-    DBuf<uint64_t>* u64[] = {&sidx, &kbeg, &csidx};
+    DBuf<uint64_t>* u64[] = {&sidx, &kbeg, &csidx, &akey};
     for (auto* b : u64) b->release();
     DBuf<double>* d64[] = {&ct0, &ct1, &cD, &cG, &cS, &vsrc, &vsnk, &volt, &val64, &diag64, &bvec, &xvec, &cgred};
     for (auto* b : d64) b->release();
@@ -851,6 +891,11 @@ nf_status Engine::generate() {
         NF_CK(cperm.ensure(slots));
         NF_CK(gpos.ensure(slots));
         NF_CK(gdir.ensure(slots));
+        NF_CK(apos.ensure(slots));
+        NF_CK(adir.ensure(slots));
+        NF_CK(akey.ensure(slots));
+        NF_CK(aperm.ensure(slots));
+        NF_CK(astart.ensure(ncell + 1));
         NF_CK(state.ensure(slots));
         NF_CK(ccnt.ensure(slots));
         NF_CK(clist.ensure(slots * kConflictCap));
@@ -883,7 +928,7 @@ nf_status Engine::generate() {
         NF_CK(cudaGetLastError());
         s = build_chunks(cstart.p, slots);
         if (s != NF_OK) return s;
-        const dim3 tg(grid_for(slots, kTPB) + (unsigned)std::min<uint64_t>(ncell, slots), 27);
+        const dim3 tg(grid_for(slots / kWC + (uint64_t)ncell + 1, kTPB / 32), 27);
         const unsigned xg = (unsigned)(4 * nsm);
         NF_CK(xq.ensure(xq_cap));
         NF_CK(xq2.ensure(xq_cap));
@@ -898,11 +943,23 @@ nf_status Engine::generate() {
         }
         NF_CK(cudaGetLastError());
         tstop(KT_OLD);
+        // Survivors binned by cell.
+        NF_CK(cudaMemsetAsync(ccursor.p, 0, sizeof(uint32_t) * (ncell + 1), st));
+        NF_LAUNCH(k_alive_count, gs, 256, 0, st)((uint32_t)slots, ntot, cperm.p, state.p, ccell.p, ccursor.p);
+        NF_CK(cudaGetLastError());
+        s = scan_u32(ccursor.p, astart.p, ncell + 1);
+        if (s != NF_OK) return s;
+        NF_CK(cudaMemsetAsync(ccursor.p, 0, sizeof(uint32_t) * (ncell + 1), st));
+        NF_LAUNCH(k_alive_bin, gs, 256, 0, st)((uint32_t)slots, ntot, cperm.p, state.p, ccell.p, astart.p, ccursor.p,
+                                               gpos.p, gdir.p, csidx.p, aperm.p, apos.p, adir.p, akey.p);
+        NF_CK(cudaGetLastError());
+        s = build_chunks(astart.p, slots);
+        if (s != NF_OK) return s;
         NF_CK(cudaMemsetAsync(ctr.p + C_OVERFLOW, 0, sizeof(unsigned long long), st));
         NF_CK(cudaMemsetAsync(ccnt.p, 0, sizeof(uint32_t) * slots, st));
         tstart(KT_CONF);
-        NF_LAUNCH(k_conf_tiles, tg, kTPB, 0, st)(dreal.p, choff.p + ncell, chunks.p, cperm.p, cstart.p, gpos.p,
-                                                 gdir.p, csidx.p, state.p, ccnt.p, clist.p, xq2.p, xq2.cap, ctr.p);
+        NF_LAUNCH(k_conf_tiles, tg, kTPB, 0, st)(dreal.p, choff.p + ncell, chunks.p, aperm.p, astart.p, apos.p,
+                                                 adir.p, akey.p, ccnt.p, clist.p, xq2.p, xq2.cap, ctr.p);
         NF_CK(cudaGetLastError());
         NF_LAUNCH(k_conf_exact, xg, 256, 0, st)(dreal.p, xq2.p, ctr.p + C_XQ_CONF, xq2.cap, cpos.p, cdir.p, creal.p,
                                                 ccnt.p, clist.p, ctr.p);

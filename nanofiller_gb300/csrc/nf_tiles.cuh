@@ -1,13 +1,15 @@
 // nf_tiles.cuh -- work decomposition of the cell-pair kernels.
 //
 // Probes (candidates, rods or virtual rods) are binned by cell (CSR pstart).
-// A chunk is up to kTPB probes of one cell; a block of the pair kernels takes
-// one (chunk, stencil offset) pair: it owns one neighbour cell of one probe
-// chunk, streams that cell's targets through shared memory in tiles of kTile,
-// and every thread tests its probe against each staged target (all threads read
-// the same shared-memory word: broadcast, no bank conflict). The 27 offsets of a
-// chunk run as 27 independent blocks, so a dense cell fills many SMs, and a
-// probe decided in one block is skipped by the others at the next tile.
+// A chunk is up to kWC = 32 probes of one cell, one per lane of a warp; a warp
+// of the pair kernels takes one (chunk, stencil offset) pair: it owns one
+// neighbour cell of one probe chunk, stages that cell's targets 32 at a time
+// in a warp-private shared-memory tile (one coalesced load per lane), and
+// every lane tests its probe against each staged target (all lanes read the
+// same shared-memory word: broadcast, no bank conflict). Warps only meet at
+// __syncwarp, so a warp whose cell is sparse or whose probes are all decided
+// retires without waiting for the other warps of its block. The 27 offsets of
+// a chunk run as 27 independent warps, so a dense cell fills many SMs.
 #pragma once
 #include <cstdint>
 
@@ -17,13 +19,22 @@
 
 namespace nf {
 
-constexpr int kTPB = 128;   // probes per chunk = threads per block
-constexpr int kTile = 256;  // targets staged per shared-memory tile
+constexpr int kTPB = 128;   // threads per block of the pair kernels (4 independent warps)
+constexpr int kWC = 32;     // probes per chunk: one warp per (chunk, neighbour cell)
+constexpr int kWT = 32;     // targets per warp-private shared-memory tile
+
+// Warp-private staging of one tile of targets: position with the target's
+// sphere term folded into .w (l/2 + a + eps + a*scf), axis + radius, length.
+struct WarpTile {
+    float4 p[kWT];
+    float4 c[kWT];
+    float l[kWT];
+};
 
 struct Chunk {
     uint32_t cell;   // global cell id of the probes
     uint32_t first;  // first probe (index into the cell-sorted probe order)
-    uint32_t n;      // probes in the chunk (<= kTPB)
+    uint32_t n;      // probes in the chunk (<= kWC)
     uint32_t real;   // realisation of the cell
 };
 
@@ -33,7 +44,7 @@ static __global__ void k_chunk_count(uint32_t ncell, const uint32_t* __restrict_
     if (c > ncell) return;
     if (c == ncell) { nch[c] = 0; return; }
     uint32_t n = pstart[c + 1] - pstart[c];
-    nch[c] = (n + kTPB - 1) / kTPB;
+    nch[c] = (n + kWC - 1) / kWC;
 }
 
 static __global__ void k_chunk_fill(uint32_t ncell, int R, const uint32_t* __restrict__ celloff,
@@ -43,11 +54,11 @@ static __global__ void k_chunk_fill(uint32_t ncell, int R, const uint32_t* __res
     if (c >= ncell) return;
     uint32_t b = pstart[c], n = pstart[c + 1] - b, k0 = choff[c];
     uint32_t r = (uint32_t)find_real(celloff, R, c);
-    for (uint32_t k = 0; k * kTPB < n; ++k) {
+    for (uint32_t k = 0; k * kWC < n; ++k) {
         Chunk ch;
         ch.cell = c;
-        ch.first = b + k * kTPB;
-        ch.n = min((uint32_t)kTPB, n - k * kTPB);
+        ch.first = b + k * kWC;
+        ch.n = min((uint32_t)kWC, n - k * kWC);
         ch.real = r;
         chunks[k0 + k] = ch;
     }
