@@ -227,6 +227,28 @@ nf_status nf_stream_candidates(nf_handle *h, uint64_t k0, uint64_t n,
                                float *x, float *y, float *z, float *cx,
                                float *cy, float *cz, float *l, float *a,
                                float *u, float *rho);
+/* Same candidates as nf_stream_candidates, through a call that allocates
+ * nothing (no reference counterpart). For callers that may not allocate
+ * while they run: a host framework that has handed all free device memory
+ * to its own caching allocator, or a checker that samples the stream while
+ * nf_generate runs on another stream of the same device and must not stall
+ * it (cudaFree synchronises the whole device). The staging buffer is a
+ * fixed device array of NF_NOALLOC_MAX_CANDIDATES x 10 floats (2.5 MiB)
+ * inside the library; n above NF_NOALLOC_MAX_CANDIDATES returns
+ * NF_ERR_CAPACITY. Nothing in that array needs to start at zero: each call
+ * writes every value it copies out. The first call on each device looks up
+ * the array's device address (cudaGetSymbolAddress, which may load the
+ * library's device code): make that first call before any stream capture
+ * begins. Calls on the same device share the array, so two calls in flight
+ * at once (different streams or host threads) race: serialise them. A handle
+ * with a density mesh must have uploaded it first (nf_generate or
+ * nf_stream_candidates after nf_create / nf_load_density), else
+ * NF_ERR_STATE; the current device must be the handle's. */
+#define NF_NOALLOC_MAX_CANDIDATES 65536u
+nf_status nf_stream_candidates_noalloc(nf_handle *h, uint64_t k0, uint64_t n,
+                                       float *x, float *y, float *z, float *cx,
+                                       float *cy, float *cz, float *l, float *a,
+                                       float *u, float *rho);
 /* Copy the accepted rods out (simPrms::asmbl_cnt_data, src/simPrms.cpp:329-391). */
 nf_status nf_get_rods(nf_handle *h, nf_rods *out);
 /* Replace the rod set (inject, e.g. from output.bin; stream_index may be NULL). */

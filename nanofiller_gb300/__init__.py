@@ -224,6 +224,16 @@ class Simulation:
         _check(self._L.nf_stream_candidates(self._h, k0, n, *ptrs), self._h, "nf_stream_candidates")
         return out.T.copy()
 
+    def stream_noalloc(self, k0, n):
+        """Same rows as stream(k0, n) through nf_stream_candidates_noalloc,
+        which stages in a fixed device array (n <= 65536) and allocates no
+        device memory."""
+        out = np.zeros((10, n), np.float32)
+        ptrs = [out[i].ctypes.data_as(C.c_void_p) for i in range(10)]
+        _check(self._L.nf_stream_candidates_noalloc(self._h, k0, n, *ptrs), self._h,
+               "nf_stream_candidates_noalloc")
+        return out.T.copy()
+
     # diagnostics
     def set_kernel_timing(self, on=True):
         _check(self._L.nf_set_kernel_timing(self._h, int(on)), self._h, "nf_set_kernel_timing")

@@ -107,6 +107,7 @@ SIGNATURES = {
     "nf_read_density_file": (_st, [C.c_char_p, _P(C.c_int), _P(C.c_float), C.c_void_p, C.c_size_t]),
     "nf_generate": (_st, [_H, _P(NfGenStats)]),
     "nf_stream_candidates": (_st, [_H, C.c_uint64, C.c_uint64] + [C.c_void_p] * 10),
+    "nf_stream_candidates_noalloc": (_st, [_H, C.c_uint64, C.c_uint64] + [C.c_void_p] * 10),
     "nf_get_rods": (_st, [_H, _P(NfRods)]),
     "nf_set_rods": (_st, [_H, _P(NfRods)]),
     "nf_contacts": (_st, [_H, _P(NfContactStats)]),

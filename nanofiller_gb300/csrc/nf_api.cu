@@ -1,6 +1,7 @@
 // nf_api.cu -- the C ABI (include/nanofiller_gb300.h) over the GB300 engine,
 // the reference keyword parser and the reference file formats.
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -731,3 +732,85 @@ nf_status nf_write_coo(nf_handle* h, const char* dir) {
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Candidate dump without allocation (nf_stream_candidates_noalloc; no
+// reference counterpart). The allocating dump stages its output in a device
+// buffer it allocates and frees per call; this variant stages it in one fixed
+// device array of this translation unit and takes the realisation descriptor
+// as a kernel argument, so the call itself allocates no device or host memory.
+// ---------------------------------------------------------------------------
+namespace {
+
+constexpr uint32_t kNoAllocMax = NF_NOALLOC_MAX_CANDIDATES;
+constexpr int kNoAllocDevices = 64;  // device ordinals served by the address cache
+
+// Field-major staging: field f of candidate i at [f * kNoAllocMax + i]
+// (10 fields x 65536 candidates x 4 B = 2.5 MiB). Nothing here needs to start
+// at zero: a call writes all 10 * n values before it copies them out.
+static __device__ __align__(256) float g_noalloc_stage[10 * kNoAllocMax];
+
+// Device address of g_noalloc_stage per device ordinal, looked up by the first
+// call on that device (concurrent first calls store the same value).
+std::atomic<float*> g_noalloc_addr[kNoAllocDevices];
+
+__global__ void k_stream_dump_static(const nf::Real Re, uint64_t k0, uint32_t n, float* __restrict__ out) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float4 p, d;
+    float u, rho;
+    nf::candidate(Re, k0 + i, &p, &d, &u, &rho);
+    const float v[10] = {p.x, p.y, p.z, d.x, d.y, d.z, p.w, d.w, u, rho};
+    for (int f = 0; f < 10; ++f) out[(size_t)f * kNoAllocMax + i] = v[f];
+}
+
+}  // namespace
+
+extern "C" nf_status nf_stream_candidates_noalloc(nf_handle* h, uint64_t k0, uint64_t n, float* x, float* y, float* z,
+                                                  float* cx, float* cy, float* cz, float* l, float* a, float* u,
+                                                  float* rho) {
+    if (!h) return NF_ERR_PARAM;
+    nf::Engine& E = h->E;
+    if (n > kNoAllocMax)
+        return fail(h, NF_ERR_CAPACITY, "nf_stream_candidates_noalloc: n exceeds the fixed staging array of "
+                                        "NF_NOALLOC_MAX_CANDIDATES = 65536 candidates");
+    int dev = -1;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return E.cuda_fail(e, "cudaGetDevice");
+    if (dev != E.dev) return fail(h, NF_ERR_STATE, "nf_stream_candidates_noalloc: current device is not the handle's");
+    if (dev < 0 || dev >= kNoAllocDevices)
+        return fail(h, NF_ERR_PARAM, "nf_stream_candidates_noalloc: device ordinal above 63");
+    float* stage = g_noalloc_addr[dev].load(std::memory_order_acquire);
+    if (!stage) {
+        void* addr = nullptr;
+        e = cudaGetSymbolAddress(&addr, g_noalloc_stage);
+        if (e != cudaSuccess) return E.cuda_fail(e, "cudaGetSymbolAddress(staging array)");
+        stage = static_cast<float*>(addr);
+        g_noalloc_addr[dev].store(stage, std::memory_order_release);
+    }
+    // Same descriptor as the allocating dump builds for realisation 0.
+    const nf_params& p = E.prm[0];
+    const float* dmesh = nullptr;
+    if (!E.hmesh[0].empty()) {
+        if (E.mesh_dirty || E.hreal.empty())
+            return fail(h, NF_ERR_STATE, "nf_stream_candidates_noalloc: the density mesh is not on the device yet "
+                                         "(nf_generate or nf_stream_candidates uploads it)");
+        dmesh = E.hreal[0].mesh;
+    }
+    int mn[3] = {p.mesh_ext[0], p.mesh_ext[1], p.mesh_ext[2]};
+    const nf::Real Re = nf::make_real(p, dmesh, mn, nf::stage_reach(p));
+    if (n) {
+        NF_LAUNCH(k_stream_dump_static, (unsigned)((n + 255) / 256), 256, 0, E.st)(Re, k0, (uint32_t)n, stage);
+        e = cudaGetLastError();
+        if (e != cudaSuccess) return E.cuda_fail(e, "k_stream_dump_static");
+    }
+    float* dst[10] = {x, y, z, cx, cy, cz, l, a, u, rho};
+    for (int f = 0; f < 10 && n; ++f) {
+        if (!dst[f]) continue;
+        e = cudaMemcpyAsync(dst[f], stage + (size_t)f * kNoAllocMax, sizeof(float) * n, cudaMemcpyDeviceToHost, E.st);
+        if (e != cudaSuccess) return E.cuda_fail(e, "nf_stream_candidates_noalloc copy-out");
+    }
+    e = cudaStreamSynchronize(E.st);
+    if (e != cudaSuccess) return E.cuda_fail(e, "nf_stream_candidates_noalloc");
+    return NF_OK;
+}
