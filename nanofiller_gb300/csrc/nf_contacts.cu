@@ -34,36 +34,35 @@ static inline unsigned grid_for(size_t n, unsigned b) { return (unsigned)((n + b
 // recorded by k_ct_exact from their FP64 evaluation.
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(kTPB) k_ct_tiles(const Real* __restrict__ reals,
-                                                   const uint32_t* __restrict__ nchunk,
-                                                   const Chunk* __restrict__ chunks,
-                                                   const uint32_t* __restrict__ rstart,
+                                                   const uint32_t* __restrict__ nitems, uint32_t icap,
+                                                   const Item* __restrict__ items,
                                                    const float4* __restrict__ spos, const float4* __restrict__ sdir,
                                                    const uint32_t* __restrict__ sid, unsigned long long* __restrict__ xq,
                                                    unsigned long long xcap, unsigned long long* __restrict__ ctr) {
     __shared__ WarpTile tiles[kTPB / 32];
     __shared__ uint32_t tid_[kTPB / 32][kWT];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const uint32_t ch = blockIdx.x * (kTPB / 32) + w;
+    WarpTile& T = tiles[w];
     const float epc = 1e-6f;  // DEV_PRECISION (inc/definitions.h:5)
     unsigned long long tests = 0;
-    uint32_t nc;
-    int img[3];
-    const Chunk C = ch < *nchunk ? chunks[ch] : Chunk{0, 0, 0, 0};
-    const Real& Re = reals[C.real];
-    if (C.n && chunk_neighbour(Re, C.cell, (int)blockIdx.y, Re.per_con, &nc, img)) {
-        const uint32_t t0 = rstart[nc], t1 = rstart[nc + 1];
-        const bool have = (uint32_t)lane < C.n;
-        const uint32_t q = C.first + lane;
+    const uint32_t n = min(*nitems, icap);
+    for (uint32_t it = blockIdx.x * (kTPB / 32) + w; it < n; it += gridDim.x * (kTPB / 32)) {
+        const Item I = items[it];
+        uint32_t np, nt;
+        int img[3];
+        item_unpack(I, &np, &nt, img);
+        const Real& Re = reals[I.real];
+        const bool have = (uint32_t)lane < np;
+        const uint32_t q = I.pfirst + lane;
         uint32_t i = 0;
         float4 pA = make_float4(0, 0, 0, 0), cA = pA;
         if (have) { i = sid[q]; pA = spos[q]; cA = sdir[q]; }
         const float sx = img[0] * Re.L[0], sy = img[1] * Re.L[1], sz = img[2] * Re.L[2];
         const float ax = pA.x - sx, ay = pA.y - sy, az = pA.z - sz;
         const float hAp = pA.w * 0.5f + cA.w + epc + cA.w + Re.cut + epc;
-        WarpTile& T = tiles[w];
-        for (uint32_t base = t0; base < t1; base += kWT) {
-            const uint32_t k = base + lane;
-            if (k < t1) {
+        for (uint32_t b = 0; b < nt; b += kWT) {
+            if (b + lane < nt) {
+                const uint32_t k = I.tfirst + b + lane;
                 const float4 p = spos[k], c = sdir[k];
                 T.l[lane] = p.w;
                 T.p[lane] = make_float4(p.x, p.y, p.z, p.w * 0.5f + c.w + epc + c.w);
@@ -71,7 +70,7 @@ __global__ void __launch_bounds__(kTPB) k_ct_tiles(const Real* __restrict__ real
                 tid_[w][lane] = sid[k];
             }
             __syncwarp();
-            const uint32_t m = min((uint32_t)kWT, t1 - base);
+            const uint32_t m = min((uint32_t)kWT, nt - b);
             if (have) {
                 for (uint32_t j = 0; j < m; ++j) {
                     if (tid_[w][j] <= i) continue;  // each unordered pair once (J > I)
@@ -84,7 +83,7 @@ __global__ void __launch_bounds__(kTPB) k_ct_tiles(const Real* __restrict__ real
                     const float4 pB = make_float4(tq.x, tq.y, tq.z, T.l[j]);
                     const float thr = (cB.w + cA.w) + Re.cut + epc;
                     if (!maybe_near(pA, cA, pB, cB, sx, sy, sz, thr, epc, Re.slack)) continue;
-                    xq_push(xq, xcap, &ctr[C_XQ], xq_pack(q, base + j, img));
+                    xq_push(xq, xcap, &ctr[C_XQ], xq_pack(q, I.tfirst + b + j, img));
                 }
             }
             __syncwarp();
@@ -240,28 +239,28 @@ __global__ void k_vbin(uint32_t n, const uint32_t* __restrict__ cellof, const ui
 }
 
 __global__ void __launch_bounds__(kTPB) k_scr_tiles(const Real* __restrict__ reals,
-                                                    const uint32_t* __restrict__ nchunk,
-                                                    const Chunk* __restrict__ chunks,
+                                                    const uint32_t* __restrict__ nitems, uint32_t icap,
+                                                    const Item* __restrict__ items,
                                                     const uint32_t* __restrict__ vperm,
                                                     const double* __restrict__ vd, const float4* __restrict__ vpf,
                                                     const float4* __restrict__ vdf,
-                                                    const uint32_t* __restrict__ rstart,
                                                     const float4* __restrict__ spos, const float4* __restrict__ sdir,
                                                     unsigned long long* __restrict__ xq, unsigned long long xcap,
                                                     unsigned long long* __restrict__ ctr) {
     __shared__ WarpTile tiles[kTPB / 32];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const uint32_t ch = blockIdx.x * (kTPB / 32) + w;
+    WarpTile& T = tiles[w];
     const float epsf = 1e-6f;
     unsigned long long tests = 0;
-    uint32_t nc;
-    int img[3];
-    const Chunk C = ch < *nchunk ? chunks[ch] : Chunk{0, 0, 0, 0};
-    const Real& Re = reals[C.real];
-    if (C.n && chunk_neighbour(Re, C.cell, (int)blockIdx.y, Re.per_con, &nc, img)) {
-        const uint32_t t0 = rstart[nc], t1 = rstart[nc + 1];
-        const bool have = (uint32_t)lane < C.n;
-        const uint32_t id = have ? vperm[C.first + lane] : 0u;
+    const uint32_t n = min(*nitems, icap);
+    for (uint32_t it = blockIdx.x * (kTPB / 32) + w; it < n; it += gridDim.x * (kTPB / 32)) {
+        const Item I = items[it];
+        uint32_t np, nt;
+        int img[3];
+        item_unpack(I, &np, &nt, img);
+        const Real& Re = reals[I.real];
+        const bool have = (uint32_t)lane < np;
+        const uint32_t id = have ? vperm[I.pfirst + lane] : 0u;
         float4 pV = make_float4(0, 0, 0, 0), cV = pV;
         float svf[3] = {0, 0, 0};
         if (have) {
@@ -270,22 +269,20 @@ __global__ void __launch_bounds__(kTPB) k_scr_tiles(const Real* __restrict__ rea
             pV = vpf[id];
             cV = vdf[id];
         }
-        WarpTile& T = tiles[w];
-        for (uint32_t base = t0; base < t1; base += kWT) {
-            const uint32_t k = base + lane;
-            if (k < t1) {
-                T.p[lane] = spos[k];
-                T.c[lane] = sdir[k];
+        for (uint32_t b = 0; b < nt; b += kWT) {
+            if (b + lane < nt) {
+                T.p[lane] = spos[I.tfirst + b + lane];
+                T.c[lane] = sdir[I.tfirst + b + lane];
             }
             __syncwarp();
-            const uint32_t m = min((uint32_t)kWT, t1 - base);
+            const uint32_t m = min((uint32_t)kWT, nt - b);
             if (have) {
                 tests += m;
                 for (uint32_t j = 0; j < m; ++j) {
                     const float4 pR = T.p[j], cR = T.c[j];
                     const float thr = (cV.w + cR.w) + epsf;
                     if (!maybe_near(pR, cR, pV, cV, svf[0], svf[1], svf[2], thr, epsf, Re.slack)) continue;
-                    xq_push(xq, xcap, &ctr[C_XQ], xq_pack(id, base + j, img));
+                    xq_push(xq, xcap, &ctr[C_XQ], xq_pack(id, I.tfirst + b + j, img));
                 }
             }
             __syncwarp();
@@ -528,11 +525,15 @@ nf_status Engine::contacts() {
     NF_CK(rcur.ensure(nslot + 1));
     NF_CK(recn.ensure(2 * R + 2));
     size_t cap = std::max<size_t>(rec.cap, std::max<size_t>(4096, 2 * nrods));
-    nf_status s = build_chunks(rstart.p, nrods);
-    if (s != NF_OK) return s;
-    const dim3 tg(grid_for((uint64_t)nrods / kWC + ncell + 1, kTPB / 32), 27);
+    nf_status s = NF_OK;
     const unsigned xg = (unsigned)(4 * nsm);
-    for (int attempt = 0; attempt < 4; ++attempt) {
+    bool items_ok = false, done = false;
+    for (int attempt = 0; attempt < 5 && !done; ++attempt) {
+        if (!items_ok) {
+            NF_CK(cudaMemsetAsync(ctr.p + C_ITEMS, 0, sizeof(unsigned long long), st));
+            s = build_items(rstart.p, rstart.p, 1);
+            if (s != NF_OK) return s;
+        }
         NF_CK(rec.ensure(cap));
         NF_CK(xq.ensure(xq_cap));
         NF_CK(cudaMemsetAsync(rcnt.p, 0, sizeof(uint32_t) * (nslot + 1), st));
@@ -540,23 +541,26 @@ nf_status Engine::contacts() {
         NF_CK(cudaMemsetAsync(ctr.p + C_XQ, 0, sizeof(unsigned long long), st));
         tstart(KT_CTPAIRS);
         if (nrods) {
-            NF_LAUNCH(k_ct_tiles, tg, kTPB, 0, st)(dreal.p, choff.p + ncell, chunks.p, rstart.p, spos.p, sdir.p, sid.p,
-                                                   xq.p, xq.cap, ctr.p);
+            NF_LAUNCH(k_ct_tiles, persistent_grid(k_ct_tiles), kTPB, 0, st)(dreal.p, item_count(), (uint32_t)items.cap, items.p, spos.p, sdir.p,
+                                                   sid.p, xq.p, xq.cap, ctr.p);
             NF_CK(cudaGetLastError());
             NF_LAUNCH(k_ct_exact, xg, 256, 0, st)(dreal.p, R, rodoff.p, xq.p, ctr.p + C_XQ, xq.cap, spos.p, sdir.p,
                                                   sid.p, rec.p, rec.cap, recn.p, rcnt.p, ctr.p);
         }
         NF_CK(cudaGetLastError());
         tstop(KT_CTPAIRS);
-        unsigned long long hv[2] = {0, 0};
+        unsigned long long hv[3] = {0, 0, 0};
         NF_CK(cudaMemcpyAsync(&hv[0], recn.p, sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
         NF_CK(cudaMemcpyAsync(&hv[1], ctr.p + C_XQ, sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
+        NF_CK(cudaMemcpyAsync(&hv[2], ctr.p + C_ITEMS, sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
         NF_CK(cudaStreamSynchronize(st));
+        if (hv[2] > items.cap) { it_cap = (size_t)(hv[2] * 1.25) + 4096; items_ok = false; continue; }
+        items_ok = true;
         if (hv[1] > xq.cap) { xq_cap = (size_t)(hv[1] * 1.25) + 1024; continue; }
-        if (hv[0] <= rec.cap) { cap = hv[0]; tbytes(KT_CTPAIRS, 36.0 * nrods + 64.0 * hv[0], 0); break; }
-        cap = hv[0] + hv[0] / 8 + 64;
-        if (attempt == 3) { err = "contact record buffer overflow"; return NF_ERR_OVERFLOW; }
+        if (hv[0] <= rec.cap) { cap = hv[0]; tbytes(KT_CTPAIRS, 36.0 * nrods + 64.0 * hv[0], 0); done = true; }
+        else cap = hv[0] + hv[0] / 8 + 64;
     }
+    if (!done) { err = "contact work list, queue or record buffer overflow"; return NF_ERR_OVERFLOW; }
     const uint32_t nrec = (uint32_t)cap;
     NF_CK(rec2.ensure(nrec + 1));
     s = scan_u32(rcnt.p, rpos.p, nslot + 1);
@@ -585,25 +589,32 @@ nf_status Engine::contacts() {
             NF_CK(cudaMemsetAsync(vcur.p, 0, sizeof(uint32_t) * (ncell + 1), st));
             NF_LAUNCH(k_vbin, grid_for(nrec, 256), 256, 0, st)(nrec, vcell.p, vstart.p, vcur.p, vperm.p);
             NF_CK(cudaGetLastError());
-            s = build_chunks(vstart.p, nrec);
-            if (s != NF_OK) return s;
-            const dim3 vg(grid_for((uint64_t)nrec / kWC + ncell + 1, kTPB / 32), 27);
-            for (int attempt = 0; attempt < 3; ++attempt) {
+            bool vitems_ok = false, vdone = false;
+            for (int attempt = 0; attempt < 4 && !vdone; ++attempt) {
+                if (!vitems_ok) {
+                    NF_CK(cudaMemsetAsync(ctr.p + C_ITEMS, 0, sizeof(unsigned long long), st));
+                    s = build_items(vstart.p, rstart.p, 1);
+                    if (s != NF_OK) return s;
+                }
                 NF_CK(xq.ensure(xq_cap));
                 NF_CK(cudaMemsetAsync(ctr.p + C_XQ, 0, sizeof(unsigned long long), st));
-                NF_LAUNCH(k_scr_tiles, vg, kTPB, 0, st)(dreal.p, choff.p + ncell, chunks.p, vperm.p, vdbl.p, vpf.p,
-                                                        vdf.p, rstart.p, spos.p, sdir.p, xq.p, xq.cap, ctr.p);
+                NF_LAUNCH(k_scr_tiles, persistent_grid(k_scr_tiles), kTPB, 0, st)(dreal.p, item_count(), (uint32_t)items.cap, items.p, vperm.p, vdbl.p,
+                                                        vpf.p, vdf.p, spos.p, sdir.p, xq.p, xq.cap, ctr.p);
                 NF_CK(cudaGetLastError());
                 NF_LAUNCH(k_scr_exact, xg, 256, 0, st)(dreal.p, R, rodoff.p, xq.p, ctr.p + C_XQ, xq.cap, vdbl.p,
                                                        spos.p, sdir.p, rec2.p, ctr.p);
                 NF_CK(cudaGetLastError());
-                unsigned long long nq = 0;
-                NF_CK(cudaMemcpyAsync(&nq, ctr.p + C_XQ, sizeof(nq), cudaMemcpyDeviceToHost, st));
+                unsigned long long nq[2] = {0, 0};
+                NF_CK(cudaMemcpyAsync(&nq[0], ctr.p + C_XQ, sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
+                NF_CK(cudaMemcpyAsync(&nq[1], ctr.p + C_ITEMS, sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                                      st));
                 NF_CK(cudaStreamSynchronize(st));
-                if (nq <= xq.cap) break;
-                xq_cap = (size_t)(nq * 1.25) + 1024;  // screening flags are idempotent: rerun
-                if (attempt == 2) { err = "screening queue overflow"; return NF_ERR_OVERFLOW; }
+                // Screening flags are idempotent: an incomplete pass is simply rerun.
+                if (nq[1] > items.cap) { it_cap = (size_t)(nq[1] * 1.25) + 4096; vitems_ok = false; }
+                else if (nq[0] > xq.cap) { vitems_ok = true; xq_cap = (size_t)(nq[0] * 1.25) + 1024; }
+                else vdone = true;
             }
+            if (!vdone) { err = "screening work list or queue overflow"; return NF_ERR_OVERFLOW; }
             tstop(KT_SCREEN);
             tbytes(KT_SCREEN, 64.0 * nrec + 32.0 * nrods, 0);
         }

@@ -33,7 +33,7 @@ enum CandState : uint8_t { ST_NONE = 0, ST_REJ_OLD = 1, ST_ALIVE = 2, ST_ACC = 3
 enum Ctr {
     C_PAIR_TESTS = 0, C_EXACT, C_FLIPS, C_OVERFLOW, C_UNDECIDED,
     C_CT_PAIRS, C_CT_EXACT, C_CT_FLIPS, C_CT_RECORDS, C_SCR_PAIRS, C_SCR_EXACT,
-    C_CG_ITERS, C_XQ_OLD, C_XQ_CONF, C_XQ, C_CERT, C_NCTR
+    C_CG_ITERS, C_XQ_OLD, C_XQ_CONF, C_XQ, C_CERT, C_ITEMS, C_NCTR
 };
 
 template <class T>
@@ -121,10 +121,11 @@ struct Engine {
     DBuf<float4> apos, adir;     // survivors of the old-rod test in cell order
     DBuf<uint64_t> akey;         // their stream indices
     DBuf<uint32_t> aperm, astart;
-    DBuf<Chunk> chunks;          // (cell, probe range) work table of the pair kernels
+    DBuf<Item> items;            // work list of the pair kernels
+    size_t it_cap = 1 << 20;     // its capacity (grown on overflow)
     DBuf<unsigned long long> xq, xq2;  // exact queues (pairs left to FP64)
     size_t xq_cap = 1 << 16;
-    DBuf<uint32_t> nch, choff, celloff;
+    DBuf<uint32_t> icnt, ioff, celloff;
     DBuf<uint8_t> state;
     DBuf<uint32_t> meta;   // per-realisation round metadata
     DBuf<unsigned long long> ctr;
@@ -182,7 +183,20 @@ struct Engine {
 
     // helpers
     nf_status scan_u32(const uint32_t* in, uint32_t* out, size_t n);
-    nf_status build_chunks(const uint32_t* pstart, size_t nprobes);
+    // Work list of (probe chunk, offset, target segment) items; the item
+    // count lands in ioff[ncell * 27] and its maximum over calls in ctr[C_ITEMS].
+    nf_status build_items(const uint32_t* pstart, const uint32_t* tstart, int stage);
+    // Device address of the item count of the last build_items (read it after
+    // that call: build_items may reallocate ioff).
+    const uint32_t* item_count() const { return ioff.p + (size_t)ncell * 27; }
+    // Persistent grid of a pair kernel: as many kTPB-thread blocks as fit on
+    // the device at once.
+    template <class K>
+    unsigned persistent_grid(K kernel) const {
+        int nb = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kernel, kTPB, 0) != cudaSuccess || nb < 1) nb = 1;
+        return (unsigned)(nsm * nb);
+    }
     uint64_t total_rods() const;
 };
 

@@ -179,34 +179,34 @@ __global__ void k_bin(uint32_t n, const uint32_t* __restrict__ ntot, const uint3
     perm[q] = i;
 }
 
-// Candidate vs accepted rods of one neighbour cell (cuda_OldExtIsectLB's job).
-// One warp per (chunk of <= 32 candidates of a cell, stencil offset); the
-// warp stages the neighbour cell's rods 32 at a time in its own shared-memory
-// tile and every lane tests its candidate against each staged rod (broadcast
-// reads). Far pairs are dropped and clear hits decided in FP32; the rest go to
-// the exact queue (probe = compact candidate id, target = sorted rod index).
+// Candidate vs accepted rods of one neighbour cell (cuda_OldExtIsectLB's job),
+// over the work list: each item is up to 32 candidates of a cell against up to
+// kSeg rods of one neighbour cell. Far pairs are dropped and clear hits decided
+// in FP32 (the candidate is rejected at once and skipped by every other item
+// at its next tile); the rest go to the exact queue (probe = compact candidate
+// id, target = sorted rod index).
 __global__ void __launch_bounds__(kTPB) k_old_tiles(const Real* __restrict__ reals,
-                                                    const uint32_t* __restrict__ nchunk,
-                                                    const Chunk* __restrict__ chunks,
+                                                    const uint32_t* __restrict__ nitems, uint32_t icap,
+                                                    const Item* __restrict__ items,
                                                     const uint32_t* __restrict__ cperm,
                                                     const float4* __restrict__ gpos, const float4* __restrict__ gdir,
-                                                    const uint32_t* __restrict__ rstart,
                                                     const float4* __restrict__ spos, const float4* __restrict__ sdir,
                                                     uint8_t* state, unsigned long long* __restrict__ xq,
                                                     unsigned long long xcap, unsigned long long* __restrict__ ctr) {
     __shared__ WarpTile tiles[kTPB / 32];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const uint32_t ch = blockIdx.x * (kTPB / 32) + w;
+    WarpTile& T = tiles[w];
+    volatile uint8_t* vst = state;
     unsigned long long tests = 0, cert = 0;
-    uint32_t nc;
-    int img[3];
-    const Chunk C = ch < *nchunk ? chunks[ch] : Chunk{0, 0, 0, 0};
-    const Real& Re = reals[C.real];
-    if (C.n && chunk_neighbour(Re, C.cell, (int)blockIdx.y, Re.per_gen, &nc, img)) {
-        const uint32_t t0 = rstart[nc], t1 = rstart[nc + 1];
-        volatile uint8_t* vst = state;
-        const bool have = (uint32_t)lane < C.n;
-        const uint32_t q = C.first + lane;
+    const uint32_t n = min(*nitems, icap);
+    for (uint32_t it = blockIdx.x * (kTPB / 32) + w; it < n; it += gridDim.x * (kTPB / 32)) {
+        const Item I = items[it];
+        uint32_t np, nt;
+        int img[3];
+        item_unpack(I, &np, &nt, img);
+        const Real& Re = reals[I.real];
+        const bool have = (uint32_t)lane < np;
+        const uint32_t q = I.pfirst + lane;
         const uint32_t cid = have ? cperm[q] : 0u;
         float4 pA = make_float4(0, 0, 0, 0), cA = pA;
         if (have) { pA = gpos[q]; cA = gdir[q]; }
@@ -214,18 +214,17 @@ __global__ void __launch_bounds__(kTPB) k_old_tiles(const Real* __restrict__ rea
         const float sx = img[0] * Re.L[0], sy = img[1] * Re.L[1], sz = img[2] * Re.L[2];
         const float ax = pA.x - sx, ay = pA.y - sy, az = pA.z - sz;
         const float hAp = pA.w * 0.5f + cA.w + Re.eps + cA.w * Re.scf + Re.sep + Re.eps;
-        WarpTile& T = tiles[w];
-        for (uint32_t base = t0; base < t1; base += kWT) {
+        for (uint32_t b = 0; b < nt; b += kWT) {
             if (!__any_sync(0xffffffffu, alive)) break;
-            const uint32_t k = base + lane;
-            if (k < t1) {
+            if (b + lane < nt) {
+                const uint32_t k = I.tfirst + b + lane;
                 const float4 p = spos[k], c = sdir[k];
                 T.l[lane] = p.w;
                 T.p[lane] = make_float4(p.x, p.y, p.z, p.w * 0.5f + c.w + Re.eps + c.w * Re.scf);
                 T.c[lane] = c;
             }
             __syncwarp();
-            const uint32_t m = min((uint32_t)kWT, t1 - base);
+            const uint32_t m = min((uint32_t)kWT, nt - b);
             if (alive) {
                 tests += m;
                 for (uint32_t j = 0; j < m; ++j) {
@@ -243,9 +242,9 @@ __global__ void __launch_bounds__(kTPB) k_old_tiles(const Real* __restrict__ rea
                         alive = false;
                         break;
                     }
-                    xq_push(xq, xcap, &ctr[C_XQ_OLD], xq_pack(cid, base + j, img));
+                    xq_push(xq, xcap, &ctr[C_XQ_OLD], xq_pack(cid, I.tfirst + b + j, img));
                 }
-                if (alive && vst[cid] == ST_REJ_OLD) alive = false;  // decided by another warp
+                if (alive && vst[cid] == ST_REJ_OLD) alive = false;  // decided by another item
             }
             __syncwarp();
         }
@@ -318,14 +317,13 @@ __global__ void k_alive_bin(uint32_t n, const uint32_t* __restrict__ ntot, const
     akey[d] = csidx[cid];
 }
 
-// Earlier survivors of one neighbour cell that a survivor hits (one warp per
-// (survivor chunk, offset)). Certified hits are listed directly, uncertain
+// Earlier survivors of one neighbour cell that a survivor hits, over the work
+// list of the survivor cells. Certified hits are listed directly, uncertain
 // pairs queued (target = compact candidate id).
 __global__ void __launch_bounds__(kTPB) k_conf_tiles(const Real* __restrict__ reals,
-                                                     const uint32_t* __restrict__ nchunk,
-                                                     const Chunk* __restrict__ chunks,
+                                                     const uint32_t* __restrict__ nitems, uint32_t icap,
+                                                     const Item* __restrict__ items,
                                                      const uint32_t* __restrict__ aperm,
-                                                     const uint32_t* __restrict__ astart,
                                                      const float4* __restrict__ apos, const float4* __restrict__ adir,
                                                      const uint64_t* __restrict__ akey, uint32_t* __restrict__ ccnt,
                                                      uint32_t* __restrict__ clist, unsigned long long* __restrict__ xq,
@@ -334,16 +332,17 @@ __global__ void __launch_bounds__(kTPB) k_conf_tiles(const Real* __restrict__ re
     __shared__ uint64_t tkey[kTPB / 32][kWT];
     __shared__ uint32_t tid_[kTPB / 32][kWT];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const uint32_t ch = blockIdx.x * (kTPB / 32) + w;
+    WarpTile& T = tiles[w];
     unsigned long long tests = 0, ovf = 0, cert = 0;
-    uint32_t nc;
-    int img[3];
-    const Chunk C = ch < *nchunk ? chunks[ch] : Chunk{0, 0, 0, 0};
-    const Real& Re = reals[C.real];
-    if (C.n && chunk_neighbour(Re, C.cell, (int)blockIdx.y, Re.per_gen, &nc, img)) {
-        const uint32_t t0 = astart[nc], t1 = astart[nc + 1];
-        const bool have = (uint32_t)lane < C.n;
-        const uint32_t q = C.first + lane;
+    const uint32_t n = min(*nitems, icap);
+    for (uint32_t it = blockIdx.x * (kTPB / 32) + w; it < n; it += gridDim.x * (kTPB / 32)) {
+        const Item I = items[it];
+        uint32_t np, nt;
+        int img[3];
+        item_unpack(I, &np, &nt, img);
+        const Real& Re = reals[I.real];
+        const bool have = (uint32_t)lane < np;
+        const uint32_t q = I.pfirst + lane;
         const uint32_t cid = have ? aperm[q] : 0u;
         float4 pA = make_float4(0, 0, 0, 0), cA = pA;
         uint64_t kA = 0;
@@ -351,10 +350,9 @@ __global__ void __launch_bounds__(kTPB) k_conf_tiles(const Real* __restrict__ re
         const float sx = img[0] * Re.L[0], sy = img[1] * Re.L[1], sz = img[2] * Re.L[2];
         const float ax = pA.x - sx, ay = pA.y - sy, az = pA.z - sz;
         const float hAp = pA.w * 0.5f + cA.w + Re.eps + cA.w * Re.scf + Re.sep + Re.eps;
-        WarpTile& T = tiles[w];
-        for (uint32_t base = t0; base < t1; base += kWT) {
-            const uint32_t k = base + lane;
-            if (k < t1) {
+        for (uint32_t b = 0; b < nt; b += kWT) {
+            if (b + lane < nt) {
+                const uint32_t k = I.tfirst + b + lane;
                 const float4 p = apos[k], c = adir[k];
                 T.l[lane] = p.w;
                 T.p[lane] = make_float4(p.x, p.y, p.z, p.w * 0.5f + c.w + Re.eps + c.w * Re.scf);
@@ -363,7 +361,7 @@ __global__ void __launch_bounds__(kTPB) k_conf_tiles(const Real* __restrict__ re
                 tid_[w][lane] = aperm[k];
             }
             __syncwarp();
-            const uint32_t m = min((uint32_t)kWT, t1 - base);
+            const uint32_t m = min((uint32_t)kWT, nt - b);
             if (have) {
                 for (uint32_t j = 0; j < m; ++j) {
                     if (tkey[w][j] >= kA) continue;  // earlier survivors only
@@ -580,18 +578,20 @@ __global__ void k_gather_pd(uint32_t n, const uint32_t* __restrict__ ntot, const
     odir[q] = dir[i];
 }
 
-// Chunk table over the cell CSR pstart (ncell + 1 entries); the chunk total is
-// left on the device at choff[ncell].
-nf_status Engine::build_chunks(const uint32_t* pstart, size_t nprobes) {
-    NF_CK(nch.ensure(ncell + 1));
-    NF_CK(choff.ensure(ncell + 1));
-    NF_LAUNCH(k_chunk_count, grid_for(ncell + 1, 256), 256, 0, st)(ncell, pstart, nch.p);
+// Work list of one pair sweep: probes binned by pstart against targets binned
+// by tstart, with the periodic flags of the stage (0 generation, 1 contacts).
+nf_status Engine::build_items(const uint32_t* pstart, const uint32_t* tstart, int stage) {
+    const size_t n27 = (size_t)ncell * 27;
+    NF_CK(icnt.ensure(n27 + 1));
+    NF_CK(ioff.ensure(n27 + 1));
+    NF_CK(items.ensure(it_cap));
+    NF_LAUNCH(k_item_count, grid_for(n27 + 1, 256), 256, 0, st)(ncell, R, celloff.p, dreal.p, stage, pstart, tstart,
+                                                                 icnt.p);
     NF_CK(cudaGetLastError());
-    nf_status s = scan_u32(nch.p, choff.p, ncell + 1);
+    nf_status s = scan_u32(icnt.p, ioff.p, n27 + 1);
     if (s != NF_OK) return s;
-    // Upper bound on chunks: all probes over kWC plus one partial chunk per cell.
-    NF_CK(chunks.ensure((size_t)ncell + nprobes / kWC + 1));
-    NF_LAUNCH(k_chunk_fill, grid_for(ncell, 256), 256, 0, st)(ncell, R, celloff.p, pstart, choff.p, chunks.p);
+    NF_LAUNCH(k_item_fill, grid_for(n27, 256), 256, 0, st)(ncell, R, celloff.p, dreal.p, stage, pstart, tstart, ioff.p,
+                                                           items.p, (uint32_t)items.cap, ctr.p + C_ITEMS);
     NF_CK(cudaGetLastError());
     return NF_OK;
 }
@@ -646,7 +646,7 @@ nf_status Engine::set_density(int r, int nx, int ny, int nz, const float* values
 void Engine::release() {
     DBuf<float4>* f4[] = {&pos, &dir, &spos, &sdir, &cpos, &cdir, &gpos, &gdir, &vpf, &vdf, &apos, &adir};
     for (auto* b : f4) b->release();
-    DBuf<uint32_t>* u32[] = {&nch, &choff, &celloff, &vcell, &vperm, &vstart, &vcur, &aperm, &astart,
+    DBuf<uint32_t>* u32[] = {&icnt, &ioff, &celloff, &vcell, &vperm, &vstart, &vcur, &aperm, &astart,
                              &dcount, &rodoff, &rstart, &rcursor, &sid, &coff, &keep, &kpos, &ccount,
                              &cstart, &ccursor, &cperm, &creal, &ccell, &ccnt, &clist, &accf, &accpos,
                              &meta, &u32tmp, &rcnt, &rpos, &rcur, &cI, &cJ, &creal2, &eflag, &parent,
@@ -656,7 +656,7 @@ void Engine::release() {
     for (auto* b : u64) b->release();
     DBuf<double>* d64[] = {&ct0, &ct1, &cD, &cG, &cS, &vsrc, &vsnk, &volt, &val64, &diag64, &bvec, &xvec, &cgred};
     for (auto* b : d64) b->release();
-    dreal.release(); mesh.release(); state.release(); ctr.release(); cubtmp.release(); chunks.release();
+    dreal.release(); mesh.release(); state.release(); ctr.release(); cubtmp.release(); items.release();
     vdbl.release();
     rec.release(); rec2.release(); recn.release(); cimg.release();
     val32.release(); diag32.release(); cgbuf.release();
@@ -926,17 +926,17 @@ nf_status Engine::generate() {
         // Cell-sorted candidate copy and the chunk table of this round.
         NF_LAUNCH(k_gather_pd, gs, 256, 0, st)((uint32_t)slots, ntot, cperm.p, cpos.p, cdir.p, gpos.p, gdir.p);
         NF_CK(cudaGetLastError());
-        s = build_chunks(cstart.p, slots);
+        NF_CK(cudaMemsetAsync(ctr.p + C_ITEMS, 0, sizeof(unsigned long long), st));
+        s = build_items(cstart.p, rstart.p, 0);
         if (s != NF_OK) return s;
-        const dim3 tg(grid_for(slots / kWC + (uint64_t)ncell + 1, kTPB / 32), 27);
         const unsigned xg = (unsigned)(4 * nsm);
         NF_CK(xq.ensure(xq_cap));
         NF_CK(xq2.ensure(xq_cap));
         NF_CK(cudaMemsetAsync(ctr.p + C_XQ_OLD, 0, 2 * sizeof(unsigned long long), st));
         tstart(KT_OLD);
         if (total_rods() > 0) {
-            NF_LAUNCH(k_old_tiles, tg, kTPB, 0, st)(dreal.p, choff.p + ncell, chunks.p, cperm.p, gpos.p, gdir.p,
-                                                    rstart.p, spos.p, sdir.p, state.p, xq.p, xq.cap, ctr.p);
+            NF_LAUNCH(k_old_tiles, persistent_grid(k_old_tiles), kTPB, 0, st)(dreal.p, item_count(), (uint32_t)items.cap, items.p, cperm.p, gpos.p,
+                                                    gdir.p, spos.p, sdir.p, state.p, xq.p, xq.cap, ctr.p);
             NF_CK(cudaGetLastError());
             NF_LAUNCH(k_old_exact, xg, 256, 0, st)(dreal.p, xq.p, ctr.p + C_XQ_OLD, xq.cap, cpos.p, cdir.p, creal.p,
                                                    spos.p, sdir.p, state.p, ctr.p);
@@ -953,12 +953,12 @@ nf_status Engine::generate() {
         NF_LAUNCH(k_alive_bin, gs, 256, 0, st)((uint32_t)slots, ntot, cperm.p, state.p, ccell.p, astart.p, ccursor.p,
                                                gpos.p, gdir.p, csidx.p, aperm.p, apos.p, adir.p, akey.p);
         NF_CK(cudaGetLastError());
-        s = build_chunks(astart.p, slots);
+        s = build_items(astart.p, astart.p, 0);
         if (s != NF_OK) return s;
         NF_CK(cudaMemsetAsync(ctr.p + C_OVERFLOW, 0, sizeof(unsigned long long), st));
         NF_CK(cudaMemsetAsync(ccnt.p, 0, sizeof(uint32_t) * slots, st));
         tstart(KT_CONF);
-        NF_LAUNCH(k_conf_tiles, tg, kTPB, 0, st)(dreal.p, choff.p + ncell, chunks.p, aperm.p, astart.p, apos.p,
+        NF_LAUNCH(k_conf_tiles, persistent_grid(k_conf_tiles), kTPB, 0, st)(dreal.p, item_count(), (uint32_t)items.cap, items.p, aperm.p, apos.p,
                                                  adir.p, akey.p, ccnt.p, clist.p, xq2.p, xq2.cap, ctr.p);
         NF_CK(cudaGetLastError());
         NF_LAUNCH(k_conf_exact, xg, 256, 0, st)(dreal.p, xq2.p, ctr.p + C_XQ_CONF, xq2.cap, cpos.p, cdir.p, creal.p,
@@ -976,12 +976,19 @@ nf_status Engine::generate() {
             NF_LAUNCH(k_resolve, gs, 256, 0, st)(ntot, state.p, ccnt.p, clist.p, ctr.p);
             NF_CK(cudaGetLastError());
             passes += 4;
-            unsigned long long hv[4] = {0, 0, 0, 0};  // conflict overflow, undecided, old queue, conflict queue
+            static_assert(C_UNDECIDED == C_OVERFLOW + 1 && C_ITEMS == C_XQ_OLD + 4, "read-back layout");
+            // conflict overflow, undecided, old queue, conflict queue, (C_XQ, C_CERT), work items
+            unsigned long long hv[7] = {0, 0, 0, 0, 0, 0, 0};
             NF_CK(cudaMemcpyAsync(&hv[0], ctr.p + C_OVERFLOW, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
                                   st));
-            NF_CK(cudaMemcpyAsync(&hv[2], ctr.p + C_XQ_OLD, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+            NF_CK(cudaMemcpyAsync(&hv[2], ctr.p + C_XQ_OLD, 5 * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
                                   st));
             NF_CK(cudaStreamSynchronize(st));
+            if (hv[6] > items.cap) {  // work list too small: grow it and redo the round
+                it_cap = (size_t)(hv[6] * 1.25) + 4096;
+                redo = true;
+                break;
+            }
             if (hv[2] > xq.cap || hv[3] > xq2.cap) {  // exact queue too small: grow it and redo the round
                 xq_cap = (size_t)(std::max(hv[2], hv[3]) * 1.25) + 1024;
                 redo = true;

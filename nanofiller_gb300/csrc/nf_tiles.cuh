@@ -1,15 +1,16 @@
 // nf_tiles.cuh -- work decomposition of the cell-pair kernels.
 //
-// Probes (candidates, rods or virtual rods) are binned by cell (CSR pstart).
-// A chunk is up to kWC = 32 probes of one cell, one per lane of a warp; a warp
-// of the pair kernels takes one (chunk, stencil offset) pair: it owns one
-// neighbour cell of one probe chunk, stages that cell's targets 32 at a time
-// in a warp-private shared-memory tile (one coalesced load per lane), and
-// every lane tests its probe against each staged target (all lanes read the
-// same shared-memory word: broadcast, no bank conflict). Warps only meet at
-// __syncwarp, so a warp whose cell is sparse or whose probes are all decided
-// retires without waiting for the other warps of its block. The 27 offsets of
-// a chunk run as 27 independent warps, so a dense cell fills many SMs.
+// Probes (candidates, rods or virtual rods) and targets are binned by cell
+// (CSR pstart / tstart). The pair kernels run over a work list built on the
+// device: one item per (probe chunk of <= kWC = 32 probes of a cell, stencil
+// offset, segment of <= kSeg targets of the neighbour cell), so no item is
+// longer than kSeg targets whatever the density, and empty neighbours (open
+// boundaries, empty cells) produce no items. A persistent grid of 4-warp
+// blocks strides over the items; a warp takes one item, each lane holds one
+// probe, the warp stages the segment's targets 32 at a time in its own
+// shared-memory tile (one coalesced load per lane) and every lane tests its
+// probe against each staged target (broadcast reads, no bank conflict).
+// Warps only meet at __syncwarp.
 #pragma once
 #include <cstdint>
 
@@ -20,59 +21,95 @@
 namespace nf {
 
 constexpr int kTPB = 128;   // threads per block of the pair kernels (4 independent warps)
-constexpr int kWC = 32;     // probes per chunk: one warp per (chunk, neighbour cell)
+constexpr int kWC = 32;     // probes per item: one per lane
 constexpr int kWT = 32;     // targets per warp-private shared-memory tile
+constexpr int kSeg = 128;   // targets per item at most
 
 // Warp-private staging of one tile of targets: position with the target's
-// sphere term folded into .w (l/2 + a + eps + a*scf), axis + radius, length.
+// sphere term folded into .w, axis + radius, length.
 struct WarpTile {
     float4 p[kWT];
     float4 c[kWT];
     float l[kWT];
 };
 
-struct Chunk {
-    uint32_t cell;   // global cell id of the probes
-    uint32_t first;  // first probe (index into the cell-sorted probe order)
-    uint32_t n;      // probes in the chunk (<= kWC)
-    uint32_t real;   // realisation of the cell
+// One work item: probes [pfirst, pfirst + np) of one cell (cell-sorted probe
+// order) against targets [tfirst, tfirst + nt) of one neighbour cell seen
+// through periodic image img. pack = np | nt << 6 | image code << 15.
+struct Item {
+    uint32_t pfirst, tfirst, real, pack;
 };
 
-// Number of chunks per cell.
-static __global__ void k_chunk_count(uint32_t ncell, const uint32_t* __restrict__ pstart, uint32_t* __restrict__ nch) {
-    uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c > ncell) return;
-    if (c == ncell) { nch[c] = 0; return; }
-    uint32_t n = pstart[c + 1] - pstart[c];
-    nch[c] = (n + kWC - 1) / kWC;
+__device__ __forceinline__ void item_unpack(const Item& I, uint32_t* np, uint32_t* nt, int img[3]) {
+    *np = I.pack & 63u;
+    *nt = (I.pack >> 6) & 511u;
+    const uint32_t im = I.pack >> 15;
+    img[0] = (int)(im & 3u) - 1;
+    img[1] = (int)((im >> 2) & 3u) - 1;
+    img[2] = (int)((im >> 4) & 3u) - 1;
 }
 
-static __global__ void k_chunk_fill(uint32_t ncell, int R, const uint32_t* __restrict__ celloff,
-                             const uint32_t* __restrict__ pstart, const uint32_t* __restrict__ choff,
-                             Chunk* __restrict__ chunks) {
-    uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= ncell) return;
-    uint32_t b = pstart[c], n = pstart[c + 1] - b, k0 = choff[c];
-    uint32_t r = (uint32_t)find_real(celloff, R, c);
-    for (uint32_t k = 0; k * kWC < n; ++k) {
-        Chunk ch;
-        ch.cell = c;
-        ch.first = b + k * kWC;
-        ch.n = min((uint32_t)kWC, n - k * kWC);
-        ch.real = r;
-        chunks[k0 + k] = ch;
+// Stage selector of the periodic flags: 0 = generation, 1 = contacts.
+__device__ __forceinline__ int stage_per(const Real& Re, int stage) { return stage ? Re.per_con : Re.per_gen; }
+
+// Items of (cell c, offset o) for t = c * 27 + o; t == ncell * 27 writes 0.
+static __global__ void k_item_count(uint32_t ncell, int R, const uint32_t* __restrict__ celloff,
+                                    const Real* __restrict__ reals, int stage, const uint32_t* __restrict__ pstart,
+                                    const uint32_t* __restrict__ tstart, uint32_t* __restrict__ icnt) {
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t nt27 = ncell * 27u;
+    if (t > nt27) return;
+    if (t == nt27) { icnt[t] = 0; return; }
+    const uint32_t c = t / 27u;
+    const int o = (int)(t % 27u);
+    const uint32_t np = pstart[c + 1] - pstart[c];
+    uint32_t n = 0;
+    if (np) {
+        const Real& Re = reals[find_real(celloff, R, c)];
+        const uint32_t loc = c - Re.cell_off;
+        const int cc[3] = {(int)(loc % (uint32_t)Re.n[0]), (int)((loc / (uint32_t)Re.n[0]) % (uint32_t)Re.n[1]),
+                           (int)(loc / ((uint32_t)Re.n[0] * (uint32_t)Re.n[1]))};
+        uint32_t nc;
+        int img[3];
+        if (stencil(Re, cc, o, stage_per(Re, stage), &nc, img)) {
+            const uint32_t nt = tstart[nc + 1] - tstart[nc];
+            n = ((np + kWC - 1) / kWC) * ((nt + kSeg - 1) / kSeg);
+        }
     }
+    icnt[t] = n;
 }
 
-// Decode the stencil neighbour of chunk cell `cell` (global id) for offset o.
-__device__ __forceinline__ bool chunk_neighbour(const Real& Re, uint32_t cell, int o, int per, uint32_t* nc,
-                                                int img[3]) {
-    uint32_t loc = cell - Re.cell_off;
-    int c[3];
-    c[0] = (int)(loc % (uint32_t)Re.n[0]);
-    c[1] = (int)((loc / (uint32_t)Re.n[0]) % (uint32_t)Re.n[1]);
-    c[2] = (int)(loc / ((uint32_t)Re.n[0] * (uint32_t)Re.n[1]));
-    return stencil(Re, c, o, per, nc, img);
+static __global__ void k_item_fill(uint32_t ncell, int R, const uint32_t* __restrict__ celloff,
+                                   const Real* __restrict__ reals, int stage, const uint32_t* __restrict__ pstart,
+                                   const uint32_t* __restrict__ tstart, const uint32_t* __restrict__ ioff,
+                                   Item* __restrict__ items, uint32_t cap, unsigned long long* __restrict__ imax) {
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t == 0) atomicMax(imax, (unsigned long long)ioff[ncell * 27u]);
+    if (t >= ncell * 27u) return;
+    uint32_t k = ioff[t];
+    const uint32_t kend = ioff[t + 1];
+    if (k == kend) return;
+    const uint32_t c = t / 27u;
+    const int o = (int)(t % 27u);
+    const int r = find_real(celloff, R, c);
+    const Real& Re = reals[r];
+    const uint32_t loc = c - Re.cell_off;
+    const int cc[3] = {(int)(loc % (uint32_t)Re.n[0]), (int)((loc / (uint32_t)Re.n[0]) % (uint32_t)Re.n[1]),
+                       (int)(loc / ((uint32_t)Re.n[0] * (uint32_t)Re.n[1]))};
+    uint32_t nc;
+    int img[3];
+    stencil(Re, cc, o, stage_per(Re, stage), &nc, img);
+    const uint32_t p0 = pstart[c], np = pstart[c + 1] - p0;
+    const uint32_t t0 = tstart[nc], nt = tstart[nc + 1] - t0;
+    const uint32_t im = (uint32_t)(img[0] + 1) | ((uint32_t)(img[1] + 1) << 2) | ((uint32_t)(img[2] + 1) << 4);
+    for (uint32_t a = 0; a < np && k < kend; a += kWC) {
+        const uint32_t pa = min((uint32_t)kWC, np - a);
+        for (uint32_t b = 0; b < nt && k < kend; b += kSeg, ++k) {
+            if (k >= cap) return;
+            const uint32_t tb = min((uint32_t)kSeg, nt - b);
+            items[k] = Item{p0 + a, t0 + b, (uint32_t)r, pa | (tb << 6) | (im << 15)};
+        }
+    }
 }
 
 // ---------------------------------------------------------------------------
