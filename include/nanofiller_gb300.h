@@ -105,7 +105,7 @@ typedef struct nf_params {
     int32_t ref_parallel_typo; /* REF_PARALLEL_TYPO: hard-core parallel branch as in
                                   inc/intersection_dev.h:51                 */
     int32_t screening;      /* SCREENING: drop contacts crossed by a rod     */
-    int32_t round_candidates; /* ROUND_CANDIDATES: 0 -> adaptive             */
+    int32_t round_candidates; /* ROUND_CANDIDATES: candidates per round; 0 -> adaptive */
     int32_t solve_max_iter; /* SOLVE_MAX_ITER (inner FP32 CG iterations)     */
     double solve_tol;       /* SOLVE_TOL: FP64 relative residual             */
 } nf_params;

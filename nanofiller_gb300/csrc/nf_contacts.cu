@@ -39,14 +39,18 @@ __global__ void __launch_bounds__(kTPB) k_ct_tiles(const Real* __restrict__ real
                                                    const float4* __restrict__ spos, const float4* __restrict__ sdir,
                                                    const uint32_t* __restrict__ sid, unsigned long long* __restrict__ xq,
                                                    unsigned long long xcap, unsigned long long* __restrict__ ctr) {
-    __shared__ WarpTile tiles[kTPB / 32];
-    __shared__ uint32_t tid_[kTPB / 32][kWT];
+    constexpr int kW = kTPB / 32;
+    __shared__ WarpTile tiles[kW];
+    __shared__ uint32_t tid_[kW][kWT];
+    __shared__ float4 ppos[kW][32], pdir[kW][32];
+    __shared__ uint16_t pq[kW][kPQ];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const unsigned lt = (1u << lane) - 1u;
     WarpTile& T = tiles[w];
     const float epc = 1e-6f;  // DEV_PRECISION (inc/definitions.h:5)
     unsigned long long tests = 0;
     const uint32_t n = min(*nitems, icap);
-    for (uint32_t it = blockIdx.x * (kTPB / 32) + w; it < n; it += gridDim.x * (kTPB / 32)) {
+    for (uint32_t it = blockIdx.x * kW + w; it < n; it += gridDim.x * kW) {
         const Item I = items[it];
         uint32_t np, nt;
         int img[3];
@@ -57,9 +61,27 @@ __global__ void __launch_bounds__(kTPB) k_ct_tiles(const Real* __restrict__ real
         uint32_t i = 0;
         float4 pA = make_float4(0, 0, 0, 0), cA = pA;
         if (have) { i = sid[q]; pA = spos[q]; cA = sdir[q]; }
+        __syncwarp();
+        ppos[w][lane] = pA;
+        pdir[w][lane] = cA;
         const float sx = img[0] * Re.L[0], sy = img[1] * Re.L[1], sz = img[2] * Re.L[2];
         const float ax = pA.x - sx, ay = pA.y - sy, az = pA.z - sz;
         const float hAp = pA.w * 0.5f + cA.w + epc + cA.w + Re.cut + epc;
+        auto batch = [&](int from, int cnt, uint32_t base) {
+            __syncwarp();
+            if (lane < cnt) {
+                const uint16_t e = pq[w][from + lane];
+                const int pl = e >> 5;
+                const uint32_t t = e & 31u;
+                const float4 qA = ppos[w][pl], dA = pdir[w][pl];
+                const float4 tq = T.p[t], cB = T.c[t];
+                const float4 pB = make_float4(tq.x, tq.y, tq.z, T.l[t]);
+                const float thr = (cB.w + dA.w) + Re.cut + epc;
+                if (maybe_near(qA, dA, pB, cB, sx, sy, sz, thr, epc, Re.slack))
+                    xq_push(xq, xcap, &ctr[C_XQ], xq_pack(I.pfirst + pl, base + t, img));
+            }
+            __syncwarp();
+        };
         for (uint32_t b = 0; b < nt; b += kWT) {
             if (b + lane < nt) {
                 const uint32_t k = I.tfirst + b + lane;
@@ -71,21 +93,25 @@ __global__ void __launch_bounds__(kTPB) k_ct_tiles(const Real* __restrict__ real
             }
             __syncwarp();
             const uint32_t m = min((uint32_t)kWT, nt - b);
-            if (have) {
-                for (uint32_t j = 0; j < m; ++j) {
-                    if (tid_[w][j] <= i) continue;  // each unordered pair once (J > I)
+            int qn = 0;
+            for (uint32_t j = 0; j < m; ++j) {
+                bool pass = false;
+                if (have && tid_[w][j] > i) {  // each unordered pair once (J > I)
                     ++tests;
                     const float4 tq = T.p[j];
                     const float bx = tq.x - ax, by = tq.y - ay, bz = tq.z - az;
                     const float Rr = (hAp + tq.w) * 1.000002f + Re.slack;
-                    if (bx * bx + by * by + bz * bz > Rr * Rr) continue;
-                    const float4 cB = T.c[j];
-                    const float4 pB = make_float4(tq.x, tq.y, tq.z, T.l[j]);
-                    const float thr = (cB.w + cA.w) + Re.cut + epc;
-                    if (!maybe_near(pA, cA, pB, cB, sx, sy, sz, thr, epc, Re.slack)) continue;
-                    xq_push(xq, xcap, &ctr[C_XQ], xq_pack(q, I.tfirst + b + j, img));
+                    pass = bx * bx + by * by + bz * bz <= Rr * Rr;
+                }
+                const unsigned bal = __ballot_sync(0xffffffffu, pass);
+                if (pass) pq[w][qn + __popc(bal & lt)] = pq_entry(lane, j);
+                qn += __popc(bal);
+                if (qn >= 32) {
+                    qn -= 32;
+                    batch(qn, 32, I.tfirst + b);
                 }
             }
+            if (qn) batch(0, qn, I.tfirst + b);
             __syncwarp();
         }
     }
@@ -531,7 +557,7 @@ nf_status Engine::contacts() {
     for (int attempt = 0; attempt < 5 && !done; ++attempt) {
         if (!items_ok) {
             NF_CK(cudaMemsetAsync(ctr.p + C_ITEMS, 0, sizeof(unsigned long long), st));
-            s = build_items(rstart.p, rstart.p, 1);
+            s = build_items(rstart.p, rstart.p, 1, nrods, nrods);
             if (s != NF_OK) return s;
         }
         NF_CK(rec.ensure(cap));
@@ -593,7 +619,7 @@ nf_status Engine::contacts() {
             for (int attempt = 0; attempt < 4 && !vdone; ++attempt) {
                 if (!vitems_ok) {
                     NF_CK(cudaMemsetAsync(ctr.p + C_ITEMS, 0, sizeof(unsigned long long), st));
-                    s = build_items(vstart.p, rstart.p, 1);
+                    s = build_items(vstart.p, rstart.p, 1, nrec, nrods);
                     if (s != NF_OK) return s;
                 }
                 NF_CK(xq.ensure(xq_cap));

@@ -185,7 +185,8 @@ struct Engine {
     nf_status scan_u32(const uint32_t* in, uint32_t* out, size_t n);
     // Work list of (probe chunk, offset, target segment) items; the item
     // count lands in ioff[ncell * 27] and its maximum over calls in ctr[C_ITEMS].
-    nf_status build_items(const uint32_t* pstart, const uint32_t* tstart, int stage);
+    // np / nt: probes and targets in all cells, for the first capacity guess.
+    nf_status build_items(const uint32_t* pstart, const uint32_t* tstart, int stage, uint64_t np, uint64_t nt);
     // Device address of the item count of the last build_items (read it after
     // that call: build_items may reallocate ioff).
     const uint32_t* item_count() const { return ioff.p + (size_t)ncell * 27; }

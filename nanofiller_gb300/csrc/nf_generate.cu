@@ -181,10 +181,11 @@ __global__ void k_bin(uint32_t n, const uint32_t* __restrict__ ntot, const uint3
 
 // Candidate vs accepted rods of one neighbour cell (cuda_OldExtIsectLB's job),
 // over the work list: each item is up to 32 candidates of a cell against up to
-// kSeg rods of one neighbour cell. Far pairs are dropped and clear hits decided
-// in FP32 (the candidate is rejected at once and skipped by every other item
-// at its next tile); the rest go to the exact queue (probe = compact candidate
-// id, target = sorted rod index).
+// kSeg rods of one neighbour cell. Each lane runs the sphere pre-test of its
+// candidate against every staged rod; passing pairs are evaluated in full-warp
+// batches: far pairs dropped, clear hits decided in FP32 (the candidate is
+// rejected at once and skipped by every other item at its next tile), the
+// rest queued for FP64 (probe = compact candidate id, target = sorted rod).
 __global__ void __launch_bounds__(kTPB) k_old_tiles(const Real* __restrict__ reals,
                                                     const uint32_t* __restrict__ nitems, uint32_t icap,
                                                     const Item* __restrict__ items,
@@ -193,13 +194,18 @@ __global__ void __launch_bounds__(kTPB) k_old_tiles(const Real* __restrict__ rea
                                                     const float4* __restrict__ spos, const float4* __restrict__ sdir,
                                                     uint8_t* state, unsigned long long* __restrict__ xq,
                                                     unsigned long long xcap, unsigned long long* __restrict__ ctr) {
-    __shared__ WarpTile tiles[kTPB / 32];
+    constexpr int kW = kTPB / 32;
+    __shared__ WarpTile tiles[kW];
+    __shared__ float4 ppos[kW][32], pdir[kW][32];
+    __shared__ uint32_t pcid[kW][32];
+    __shared__ uint16_t pq[kW][kPQ];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const unsigned lt = (1u << lane) - 1u;
     WarpTile& T = tiles[w];
     volatile uint8_t* vst = state;
     unsigned long long tests = 0, cert = 0;
     const uint32_t n = min(*nitems, icap);
-    for (uint32_t it = blockIdx.x * (kTPB / 32) + w; it < n; it += gridDim.x * (kTPB / 32)) {
+    for (uint32_t it = blockIdx.x * kW + w; it < n; it += gridDim.x * kW) {
         const Item I = items[it];
         uint32_t np, nt;
         int img[3];
@@ -211,9 +217,43 @@ __global__ void __launch_bounds__(kTPB) k_old_tiles(const Real* __restrict__ rea
         float4 pA = make_float4(0, 0, 0, 0), cA = pA;
         if (have) { pA = gpos[q]; cA = gdir[q]; }
         bool alive = have && vst[cid] != ST_REJ_OLD;
+        __syncwarp();
+        ppos[w][lane] = pA;
+        pdir[w][lane] = cA;
+        pcid[w][lane] = cid;
         const float sx = img[0] * Re.L[0], sy = img[1] * Re.L[1], sz = img[2] * Re.L[2];
         const float ax = pA.x - sx, ay = pA.y - sy, az = pA.z - sz;
         const float hAp = pA.w * 0.5f + cA.w + Re.eps + cA.w * Re.scf + Re.sep + Re.eps;
+        unsigned dead = 0;  // probe lanes decided during this item (warp-uniform)
+        // Full-warp evaluation of stack entries [from, from + cnt).
+        auto batch = [&](int from, int cnt, uint32_t base) {
+            __syncwarp();
+            bool hit = false;
+            int pl = 0;
+            if (lane < cnt) {
+                const uint16_t e = pq[w][from + lane];
+                pl = e >> 5;
+                const uint32_t t = e & 31u;
+                if (!((dead >> pl) & 1u)) {
+                    const float4 qA = ppos[w][pl], dA = pdir[w][pl];
+                    const float4 tq = T.p[t], cB = T.c[t];
+                    const float4 pB = make_float4(tq.x, tq.y, tq.z, T.l[t]);
+                    const float thr = (cB.w + dA.w) * Re.scf + Re.sep + Re.eps;
+                    if (maybe_near(qA, dA, pB, cB, sx, sy, sz, thr, Re.eps, Re.slack)) {
+                        const uint32_t c = pcid[w][pl];
+                        if (!Re.typo && certain_hit(qA, dA, pB, cB, sx, sy, sz, thr, Re.eps, Re.slack)) {
+                            hit = true;
+                            ++cert;
+                            vst[c] = ST_REJ_OLD;
+                        } else {
+                            xq_push(xq, xcap, &ctr[C_XQ_OLD], xq_pack(c, base + t, img));
+                        }
+                    }
+                }
+            }
+            dead |= __reduce_or_sync(0xffffffffu, hit ? (1u << pl) : 0u);
+            __syncwarp();
+        };
         for (uint32_t b = 0; b < nt; b += kWT) {
             if (!__any_sync(0xffffffffu, alive)) break;
             if (b + lane < nt) {
@@ -225,27 +265,28 @@ __global__ void __launch_bounds__(kTPB) k_old_tiles(const Real* __restrict__ rea
             }
             __syncwarp();
             const uint32_t m = min((uint32_t)kWT, nt - b);
-            if (alive) {
-                tests += m;
-                for (uint32_t j = 0; j < m; ++j) {
+            int qn = 0;
+            if (alive) tests += m;
+            for (uint32_t j = 0; j < m; ++j) {
+                bool pass = false;
+                if (alive) {
                     const float4 tq = T.p[j];
                     const float bx = tq.x - ax, by = tq.y - ay, bz = tq.z - az;
                     const float Rr = (hAp + tq.w) * 1.000002f + Re.slack;
-                    if (bx * bx + by * by + bz * bz > Rr * Rr) continue;
-                    const float4 cB = T.c[j];
-                    const float4 pB = make_float4(tq.x, tq.y, tq.z, T.l[j]);
-                    const float thr = (cB.w + cA.w) * Re.scf + Re.sep + Re.eps;
-                    if (!maybe_near(pA, cA, pB, cB, sx, sy, sz, thr, Re.eps, Re.slack)) continue;
-                    if (!Re.typo && certain_hit(pA, cA, pB, cB, sx, sy, sz, thr, Re.eps, Re.slack)) {
-                        ++cert;
-                        vst[cid] = ST_REJ_OLD;
-                        alive = false;
-                        break;
-                    }
-                    xq_push(xq, xcap, &ctr[C_XQ_OLD], xq_pack(cid, I.tfirst + b + j, img));
+                    pass = bx * bx + by * by + bz * bz <= Rr * Rr;
                 }
-                if (alive && vst[cid] == ST_REJ_OLD) alive = false;  // decided by another item
+                const unsigned bal = __ballot_sync(0xffffffffu, pass);
+                if (pass) pq[w][qn + __popc(bal & lt)] = pq_entry(lane, j);
+                qn += __popc(bal);
+                if (qn >= 32) {
+                    qn -= 32;
+                    batch(qn, 32, I.tfirst + b);
+                    if ((dead >> lane) & 1u) alive = false;
+                }
             }
+            if (qn) batch(0, qn, I.tfirst + b);
+            if ((dead >> lane) & 1u) alive = false;
+            if (alive && vst[cid] == ST_REJ_OLD) alive = false;  // decided by another item
             __syncwarp();
         }
     }
@@ -318,8 +359,9 @@ __global__ void k_alive_bin(uint32_t n, const uint32_t* __restrict__ ntot, const
 }
 
 // Earlier survivors of one neighbour cell that a survivor hits, over the work
-// list of the survivor cells. Certified hits are listed directly, uncertain
-// pairs queued (target = compact candidate id).
+// list of the survivor cells (sphere pre-test per lane, full-warp batches of
+// the passing pairs). Certified hits are listed directly, uncertain pairs
+// queued (target = compact candidate id).
 __global__ void __launch_bounds__(kTPB) k_conf_tiles(const Real* __restrict__ reals,
                                                      const uint32_t* __restrict__ nitems, uint32_t icap,
                                                      const Item* __restrict__ items,
@@ -328,14 +370,19 @@ __global__ void __launch_bounds__(kTPB) k_conf_tiles(const Real* __restrict__ re
                                                      const uint64_t* __restrict__ akey, uint32_t* __restrict__ ccnt,
                                                      uint32_t* __restrict__ clist, unsigned long long* __restrict__ xq,
                                                      unsigned long long xcap, unsigned long long* __restrict__ ctr) {
-    __shared__ WarpTile tiles[kTPB / 32];
-    __shared__ uint64_t tkey[kTPB / 32][kWT];
-    __shared__ uint32_t tid_[kTPB / 32][kWT];
+    constexpr int kW = kTPB / 32;
+    __shared__ WarpTile tiles[kW];
+    __shared__ uint64_t tkey[kW][kWT];
+    __shared__ uint32_t tid_[kW][kWT];
+    __shared__ float4 ppos[kW][32], pdir[kW][32];
+    __shared__ uint32_t pcid[kW][32];
+    __shared__ uint16_t pq[kW][kPQ];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const unsigned lt = (1u << lane) - 1u;
     WarpTile& T = tiles[w];
     unsigned long long tests = 0, ovf = 0, cert = 0;
     const uint32_t n = min(*nitems, icap);
-    for (uint32_t it = blockIdx.x * (kTPB / 32) + w; it < n; it += gridDim.x * (kTPB / 32)) {
+    for (uint32_t it = blockIdx.x * kW + w; it < n; it += gridDim.x * kW) {
         const Item I = items[it];
         uint32_t np, nt;
         int img[3];
@@ -347,9 +394,37 @@ __global__ void __launch_bounds__(kTPB) k_conf_tiles(const Real* __restrict__ re
         float4 pA = make_float4(0, 0, 0, 0), cA = pA;
         uint64_t kA = 0;
         if (have) { pA = apos[q]; cA = adir[q]; kA = akey[q]; }
+        __syncwarp();
+        ppos[w][lane] = pA;
+        pdir[w][lane] = cA;
+        pcid[w][lane] = cid;
         const float sx = img[0] * Re.L[0], sy = img[1] * Re.L[1], sz = img[2] * Re.L[2];
         const float ax = pA.x - sx, ay = pA.y - sy, az = pA.z - sz;
         const float hAp = pA.w * 0.5f + cA.w + Re.eps + cA.w * Re.scf + Re.sep + Re.eps;
+        auto batch = [&](int from, int cnt) {
+            __syncwarp();
+            if (lane < cnt) {
+                const uint16_t e = pq[w][from + lane];
+                const int pl = e >> 5;
+                const uint32_t t = e & 31u;
+                const float4 qA = ppos[w][pl], dA = pdir[w][pl];
+                const float4 tq = T.p[t], cB = T.c[t];
+                const float4 pB = make_float4(tq.x, tq.y, tq.z, T.l[t]);
+                const float thr = (cB.w + dA.w) * Re.scf + Re.sep + Re.eps;
+                if (maybe_near(qA, dA, pB, cB, sx, sy, sz, thr, Re.eps, Re.slack)) {
+                    const uint32_t c = pcid[w][pl];
+                    if (!Re.typo && certain_hit(qA, dA, pB, cB, sx, sy, sz, thr, Re.eps, Re.slack)) {
+                        ++cert;
+                        uint32_t slot = atomicAdd(&ccnt[c], 1u);
+                        if (slot < (uint32_t)kConflictCap) clist[(size_t)c * kConflictCap + slot] = tid_[w][t];
+                        else ++ovf;
+                    } else {
+                        xq_push(xq, xcap, &ctr[C_XQ_CONF], xq_pack(c, tid_[w][t], img));
+                    }
+                }
+            }
+            __syncwarp();
+        };
         for (uint32_t b = 0; b < nt; b += kWT) {
             if (b + lane < nt) {
                 const uint32_t k = I.tfirst + b + lane;
@@ -362,28 +437,25 @@ __global__ void __launch_bounds__(kTPB) k_conf_tiles(const Real* __restrict__ re
             }
             __syncwarp();
             const uint32_t m = min((uint32_t)kWT, nt - b);
-            if (have) {
-                for (uint32_t j = 0; j < m; ++j) {
-                    if (tkey[w][j] >= kA) continue;  // earlier survivors only
+            int qn = 0;
+            for (uint32_t j = 0; j < m; ++j) {
+                bool pass = false;
+                if (have && tkey[w][j] < kA) {  // earlier survivors only
                     ++tests;
                     const float4 tq = T.p[j];
                     const float bx = tq.x - ax, by = tq.y - ay, bz = tq.z - az;
                     const float Rr = (hAp + tq.w) * 1.000002f + Re.slack;
-                    if (bx * bx + by * by + bz * bz > Rr * Rr) continue;
-                    const float4 cB = T.c[j];
-                    const float4 pB = make_float4(tq.x, tq.y, tq.z, T.l[j]);
-                    const float thr = (cB.w + cA.w) * Re.scf + Re.sep + Re.eps;
-                    if (!maybe_near(pA, cA, pB, cB, sx, sy, sz, thr, Re.eps, Re.slack)) continue;
-                    if (!Re.typo && certain_hit(pA, cA, pB, cB, sx, sy, sz, thr, Re.eps, Re.slack)) {
-                        ++cert;
-                        uint32_t slot = atomicAdd(&ccnt[cid], 1u);
-                        if (slot < (uint32_t)kConflictCap) clist[(size_t)cid * kConflictCap + slot] = tid_[w][j];
-                        else ++ovf;
-                    } else {
-                        xq_push(xq, xcap, &ctr[C_XQ_CONF], xq_pack(cid, tid_[w][j], img));
-                    }
+                    pass = bx * bx + by * by + bz * bz <= Rr * Rr;
+                }
+                const unsigned bal = __ballot_sync(0xffffffffu, pass);
+                if (pass) pq[w][qn + __popc(bal & lt)] = pq_entry(lane, j);
+                qn += __popc(bal);
+                if (qn >= 32) {
+                    qn -= 32;
+                    batch(qn, 32);
                 }
             }
+            if (qn) batch(0, qn);
             __syncwarp();
         }
     }
@@ -580,10 +652,14 @@ __global__ void k_gather_pd(uint32_t n, const uint32_t* __restrict__ ntot, const
 
 // Work list of one pair sweep: probes binned by pstart against targets binned
 // by tstart, with the periodic flags of the stage (0 generation, 1 contacts).
-nf_status Engine::build_items(const uint32_t* pstart, const uint32_t* tstart, int stage) {
+nf_status Engine::build_items(const uint32_t* pstart, const uint32_t* tstart, int stage, uint64_t np, uint64_t nt) {
     const size_t n27 = (size_t)ncell * 27;
     NF_CK(icnt.ensure(n27 + 1));
     NF_CK(ioff.ensure(n27 + 1));
+    // Items of evenly spread probes and targets, with a quarter of headroom; a
+    // work list that still overflows is grown and its pass redone.
+    const double guess = 27.0 * ((double)np / kWC + ncell) * (1.0 + (double)nt / ((double)ncell * kSeg)) * 1.25;
+    it_cap = std::max(it_cap, (size_t)std::min(guess, 4.0e8));
     NF_CK(items.ensure(it_cap));
     NF_LAUNCH(k_item_count, grid_for(n27 + 1, 256), 256, 0, st)(ncell, R, celloff.p, dreal.p, stage, pstart, tstart,
                                                                  icnt.p);
@@ -804,6 +880,10 @@ nf_status Engine::inject(size_t n, const float4* hpos, const float4* hdir, const
     return NF_OK;
 }
 
+// Candidates of one round over all realisations at most (~300 B of device
+// memory per candidate slot).
+constexpr uint64_t kRoundSlotCap = 1ull << 24;
+
 nf_status Engine::generate() {
     nf_status s = setup_reals(*this);
     if (s != NF_OK) return s;
@@ -847,6 +927,7 @@ nf_status Engine::generate() {
     std::vector<uint64_t> hkbeg(R), hout(2 * R);
     std::vector<uint32_t> hmeta(4 * R);
     std::vector<uint64_t> c_round(R);
+    std::vector<double> last_rate(R, 1.0);  // accepted / drawn in the last round
     double scale = 1.0;
     int rounds = 0;
     const int max_rounds = 100000;
@@ -858,14 +939,20 @@ nf_status Engine::generate() {
             uint64_t c = 0;
             uint32_t tgt = hreal[r].target;
             if (count[r] < tgt && knext[r] < p.n_candidates) {
-                double acc_rate = p_dens[r];
-                if (knext[r] > 0 && dens_acc[r] > 0)
-                    acc_rate = ((double)dens_acc[r] / knext[r]) * std::max(1e-6, (double)count[r] / dens_acc[r]);
-                double want = (tgt - count[r]) / std::max(acc_rate, 1e-6) * 1.2 + 256;
-                // survivors of the old-rod test per round stay near alive_max
-                double amax_c = alive_max[r] / std::max(acc_rate, 1e-6);
-                double cr = std::min(want, amax_c) * scale;
-                if (p.round_candidates > 0) cr = std::min(cr, (double)p.round_candidates);
+                // Acceptance per candidate: the density acceptance before the
+                // first round, then the last round's own rate (the rate only
+                // falls as the box fills, so the cumulative rate would
+                // overestimate it). Rounds draw twice the expected need: extra
+                // candidates cost sweep work, a short round costs a round.
+                const double acc_rate = rounds_r[r] > 0 ? last_rate[r] : p_dens[r];
+                double want = (tgt - count[r]) / std::max(acc_rate, 1e-6) * 2.0 + 256;
+                // Survivors of the old-rod test per round: at most alive_max
+                // (bounds the conflict lists) and at most about the rods already
+                // placed (in-round conflict work grows with the square of the
+                // survivors, the old-rod work only with survivors x rods).
+                const double grow = std::max({4096.0, (double)count[r], 0.5 * tgt});
+                double amax_c = std::min(alive_max[r], grow) / std::max(acc_rate, 1e-6);
+                double cr = std::min(want, p.round_candidates > 0 ? (double)p.round_candidates : amax_c) * scale;
                 c = (uint64_t)std::max(64.0, cr);
                 c = std::min<uint64_t>(c, p.n_candidates - knext[r]);
                 c = std::min<uint64_t>(c, 1u << 24);
@@ -875,6 +962,16 @@ nf_status Engine::generate() {
             hcoff[r] = (uint32_t)slots;
             hkbeg[r] = knext[r];
             slots += c;
+        }
+        if (slots > kRoundSlotCap) {  // bound the round's memory: scale every realisation down
+            const double f = (double)kRoundSlotCap / (double)slots;
+            slots = 0;
+            for (int r = 0; r < R; ++r) {
+                if (c_round[r]) c_round[r] = std::max<uint64_t>(std::min<uint64_t>(64, c_round[r]),
+                                                                (uint64_t)(c_round[r] * f));
+                hcoff[r] = (uint32_t)slots;
+                slots += c_round[r];
+            }
         }
         hcoff[R] = (uint32_t)slots;
         if (!active) break;
@@ -927,9 +1024,10 @@ nf_status Engine::generate() {
         NF_LAUNCH(k_gather_pd, gs, 256, 0, st)((uint32_t)slots, ntot, cperm.p, cpos.p, cdir.p, gpos.p, gdir.p);
         NF_CK(cudaGetLastError());
         NF_CK(cudaMemsetAsync(ctr.p + C_ITEMS, 0, sizeof(unsigned long long), st));
-        s = build_items(cstart.p, rstart.p, 0);
+        s = build_items(cstart.p, rstart.p, 0, slots, total_rods());
         if (s != NF_OK) return s;
         const unsigned xg = (unsigned)(4 * nsm);
+        xq_cap = std::max(xq_cap, (size_t)(slots / 8));  // first guess; grown and redone on overflow
         NF_CK(xq.ensure(xq_cap));
         NF_CK(xq2.ensure(xq_cap));
         NF_CK(cudaMemsetAsync(ctr.p + C_XQ_OLD, 0, 2 * sizeof(unsigned long long), st));
@@ -953,7 +1051,7 @@ nf_status Engine::generate() {
         NF_LAUNCH(k_alive_bin, gs, 256, 0, st)((uint32_t)slots, ntot, cperm.p, state.p, ccell.p, astart.p, ccursor.p,
                                                gpos.p, gdir.p, csidx.p, aperm.p, apos.p, adir.p, akey.p);
         NF_CK(cudaGetLastError());
-        s = build_items(astart.p, astart.p, 0);
+        s = build_items(astart.p, astart.p, 0, slots, slots);
         if (s != NF_OK) return s;
         NF_CK(cudaMemsetAsync(ctr.p + C_OVERFLOW, 0, sizeof(unsigned long long), st));
         NF_CK(cudaMemsetAsync(ccnt.p, 0, sizeof(uint32_t) * slots, st));
@@ -1030,6 +1128,7 @@ nf_status Engine::generate() {
         for (int r = 0; r < R; ++r) {
             if (!c_round[r]) continue;
             ++rounds_r[r];
+            last_rate[r] = std::max(1e-7, (double)hmeta[4 * r + 3] / (double)c_round[r]);
             uint32_t rem = hreal[r].target - count[r];
             uint32_t got = std::min(hmeta[4 * r + 3], rem);
             uint32_t kept = hmeta[4 * r + 1] - hmeta[4 * r + 0];

@@ -25,6 +25,16 @@ constexpr int kWC = 32;     // probes per item: one per lane
 constexpr int kWT = 32;     // targets per warp-private shared-memory tile
 constexpr int kSeg = 128;   // targets per item at most
 
+// Pairs that pass the per-lane sphere pre-test are pushed on a per-warp
+// stack of (probe lane, target slot) entries and evaluated 32 at a time by
+// the full warp, so the long filter path (maybe_near, certain_hit) runs with
+// every lane busy instead of once per passing lane.
+constexpr int kPQ = 64;  // stack capacity: < 32 pending + one push of <= 32
+
+__device__ __forceinline__ uint16_t pq_entry(int probe_lane, uint32_t slot) {
+    return (uint16_t)(((uint32_t)probe_lane << 5) | slot);
+}
+
 // Warp-private staging of one tile of targets: position with the target's
 // sphere term folded into .w, axis + radius, length.
 struct WarpTile {
