@@ -43,9 +43,9 @@ __global__ void __launch_bounds__(kTPB) k_ct_tiles(const Real* __restrict__ real
     __shared__ WarpTile tiles[kW];
     __shared__ uint32_t tid_[kW][kWT];
     __shared__ float4 ppos[kW][32], pdir[kW][32];
-    __shared__ uint16_t pq[kW][kPQ];
+    __shared__ int msp[kW][32];
+    __shared__ uint32_t msm[kW][32];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const unsigned lt = (1u << lane) - 1u;
     WarpTile& T = tiles[w];
     const float epc = 1e-6f;  // DEV_PRECISION (inc/definitions.h:5)
     unsigned long long tests = 0;
@@ -58,7 +58,7 @@ __global__ void __launch_bounds__(kTPB) k_ct_tiles(const Real* __restrict__ real
         const Real& Re = reals[I.real];
         const bool have = (uint32_t)lane < np;
         const uint32_t q = I.pfirst + lane;
-        uint32_t i = 0;
+        uint32_t i = 0xffffffffu;
         float4 pA = make_float4(0, 0, 0, 0), cA = pA;
         if (have) { i = sid[q]; pA = spos[q]; cA = sdir[q]; }
         __syncwarp();
@@ -66,52 +66,48 @@ __global__ void __launch_bounds__(kTPB) k_ct_tiles(const Real* __restrict__ real
         pdir[w][lane] = cA;
         const float sx = img[0] * Re.L[0], sy = img[1] * Re.L[1], sz = img[2] * Re.L[2];
         const float ax = pA.x - sx, ay = pA.y - sy, az = pA.z - sz;
-        const float hAp = pA.w * 0.5f + cA.w + epc + cA.w + Re.cut + epc;
-        auto batch = [&](int from, int cnt, uint32_t base) {
+        const float hA2 = (pA.w * 0.5f + cA.w + epc + cA.w + Re.cut + epc) * 1.000002f + Re.slack;
+        for (uint32_t b = 0; b < nt; b += kWT) {
+            const uint32_t m = min((uint32_t)kWT, nt - b);
+            if ((uint32_t)lane < m) {
+                const uint32_t k = I.tfirst + b + lane;
+                const float4 p = spos[k], c = sdir[k];
+                T.l[lane] = p.w;
+                T.p[lane] = make_float4(p.x, p.y, p.z, (p.w * 0.5f + c.w + epc + c.w) * 1.000002f);
+                T.c[lane] = c;
+                tid_[w][lane] = sid[k];
+            } else {
+                T.p[lane] = make_float4(kFar, kFar, kFar, 0.0f);
+                tid_[w][lane] = 0u;
+            }
             __syncwarp();
-            if (lane < cnt) {
-                const uint16_t e = pq[w][from + lane];
-                const int pl = e >> 5;
-                const uint32_t t = e & 31u;
+            uint32_t mask = 0, umask = 0;  // marked pairs; pairs with J > I
+            if (have) {
+                const uint32_t m8 = (m + 7u) & ~7u;
+                for (uint32_t j0 = 0; j0 < m8; j0 += 8) {
+#pragma unroll
+                    for (uint32_t jj = 0; jj < 8; ++jj) {
+                        const uint32_t j = j0 + jj;
+                        const float4 tq = T.p[j];
+                        const float bx = tq.x - ax, by = tq.y - ay, bz = tq.z - az;
+                        const float Rr = hA2 + tq.w;
+                        const uint32_t bit = tid_[w][j] > i ? (1u << j) : 0u;  // each unordered pair once
+                        umask |= bit;
+                        if (bx * bx + by * by + bz * bz <= Rr * Rr) mask |= bit;
+                    }
+                }
+                tests += __popc(umask);
+            }
+            const uint32_t base = I.tfirst + b;
+            for_marked_pairs(mask, lane, msp[w], msm[w], [&](bool valid, int pl, int t) {
+                if (!valid) return;
                 const float4 qA = ppos[w][pl], dA = pdir[w][pl];
                 const float4 tq = T.p[t], cB = T.c[t];
                 const float4 pB = make_float4(tq.x, tq.y, tq.z, T.l[t]);
                 const float thr = (cB.w + dA.w) + Re.cut + epc;
                 if (maybe_near(qA, dA, pB, cB, sx, sy, sz, thr, epc, Re.slack))
                     xq_push(xq, xcap, &ctr[C_XQ], xq_pack(I.pfirst + pl, base + t, img));
-            }
-            __syncwarp();
-        };
-        for (uint32_t b = 0; b < nt; b += kWT) {
-            if (b + lane < nt) {
-                const uint32_t k = I.tfirst + b + lane;
-                const float4 p = spos[k], c = sdir[k];
-                T.l[lane] = p.w;
-                T.p[lane] = make_float4(p.x, p.y, p.z, p.w * 0.5f + c.w + epc + c.w);
-                T.c[lane] = c;
-                tid_[w][lane] = sid[k];
-            }
-            __syncwarp();
-            const uint32_t m = min((uint32_t)kWT, nt - b);
-            int qn = 0;
-            for (uint32_t j = 0; j < m; ++j) {
-                bool pass = false;
-                if (have && tid_[w][j] > i) {  // each unordered pair once (J > I)
-                    ++tests;
-                    const float4 tq = T.p[j];
-                    const float bx = tq.x - ax, by = tq.y - ay, bz = tq.z - az;
-                    const float Rr = (hAp + tq.w) * 1.000002f + Re.slack;
-                    pass = bx * bx + by * by + bz * bz <= Rr * Rr;
-                }
-                const unsigned bal = __ballot_sync(0xffffffffu, pass);
-                if (pass) pq[w][qn + __popc(bal & lt)] = pq_entry(lane, j);
-                qn += __popc(bal);
-                if (qn >= 32) {
-                    qn -= 32;
-                    batch(qn, 32, I.tfirst + b);
-                }
-            }
-            if (qn) batch(0, qn, I.tfirst + b);
+            });
             __syncwarp();
         }
     }

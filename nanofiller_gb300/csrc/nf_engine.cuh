@@ -119,7 +119,6 @@ struct Engine {
     DBuf<float4> cpos, cdir;
     DBuf<float4> gpos, gdir;     // candidates in cell order
     DBuf<float4> apos, adir;     // survivors of the old-rod test in cell order
-    DBuf<uint64_t> akey;         // their stream indices
     DBuf<uint32_t> aperm, astart;
     DBuf<Item> items;            // work list of the pair kernels
     size_t it_cap = 1 << 20;     // its capacity (grown on overflow)

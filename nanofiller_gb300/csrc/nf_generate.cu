@@ -181,9 +181,9 @@ __global__ void k_bin(uint32_t n, const uint32_t* __restrict__ ntot, const uint3
 
 // Candidate vs accepted rods of one neighbour cell (cuda_OldExtIsectLB's job),
 // over the work list: each item is up to 32 candidates of a cell against up to
-// kSeg rods of one neighbour cell. Each lane runs the sphere pre-test of its
-// candidate against every staged rod; passing pairs are evaluated in full-warp
-// batches: far pairs dropped, clear hits decided in FP32 (the candidate is
+// kSeg rods of one neighbour cell. Each lane marks the staged rods that pass
+// the sphere pre-test of its candidate; the marked pairs are evaluated by the
+// whole warp: far pairs dropped, clear hits decided in FP32 (the candidate is
 // rejected at once and skipped by every other item at its next tile), the
 // rest queued for FP64 (probe = compact candidate id, target = sorted rod).
 __global__ void __launch_bounds__(kTPB) k_old_tiles(const Real* __restrict__ reals,
@@ -198,9 +198,9 @@ __global__ void __launch_bounds__(kTPB) k_old_tiles(const Real* __restrict__ rea
     __shared__ WarpTile tiles[kW];
     __shared__ float4 ppos[kW][32], pdir[kW][32];
     __shared__ uint32_t pcid[kW][32];
-    __shared__ uint16_t pq[kW][kPQ];
+    __shared__ int msp[kW][32];
+    __shared__ uint32_t msm[kW][32];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const unsigned lt = (1u << lane) - 1u;
     WarpTile& T = tiles[w];
     volatile uint8_t* vst = state;
     unsigned long long tests = 0, cert = 0;
@@ -223,18 +223,39 @@ __global__ void __launch_bounds__(kTPB) k_old_tiles(const Real* __restrict__ rea
         pcid[w][lane] = cid;
         const float sx = img[0] * Re.L[0], sy = img[1] * Re.L[1], sz = img[2] * Re.L[2];
         const float ax = pA.x - sx, ay = pA.y - sy, az = pA.z - sz;
-        const float hAp = pA.w * 0.5f + cA.w + Re.eps + cA.w * Re.scf + Re.sep + Re.eps;
+        const float hA2 = (pA.w * 0.5f + cA.w + Re.eps + cA.w * Re.scf + Re.sep + Re.eps) * 1.000002f + Re.slack;
         unsigned dead = 0;  // probe lanes decided during this item (warp-uniform)
-        // Full-warp evaluation of stack entries [from, from + cnt).
-        auto batch = [&](int from, int cnt, uint32_t base) {
+        for (uint32_t b = 0; b < nt; b += kWT) {
+            if (!__any_sync(0xffffffffu, alive)) break;
+            const uint32_t m = min((uint32_t)kWT, nt - b);
+            if ((uint32_t)lane < m) {
+                const uint32_t k = I.tfirst + b + lane;
+                const float4 p = spos[k], c = sdir[k];
+                T.l[lane] = p.w;
+                T.p[lane] = make_float4(p.x, p.y, p.z, (p.w * 0.5f + c.w + Re.eps + c.w * Re.scf) * 1.000002f);
+                T.c[lane] = c;
+            } else {
+                T.p[lane] = make_float4(kFar, kFar, kFar, 0.0f);
+            }
             __syncwarp();
-            bool hit = false;
-            int pl = 0;
-            if (lane < cnt) {
-                const uint16_t e = pq[w][from + lane];
-                pl = e >> 5;
-                const uint32_t t = e & 31u;
-                if (!((dead >> pl) & 1u)) {
+            uint32_t mask = 0;
+            if (alive) {
+                tests += m;
+                const uint32_t m8 = (m + 7u) & ~7u;
+                for (uint32_t j0 = 0; j0 < m8; j0 += 8) {
+#pragma unroll
+                    for (uint32_t jj = 0; jj < 8; ++jj) {
+                        const float4 tq = T.p[j0 + jj];
+                        const float bx = tq.x - ax, by = tq.y - ay, bz = tq.z - az;
+                        const float Rr = hA2 + tq.w;
+                        if (bx * bx + by * by + bz * bz <= Rr * Rr) mask |= 1u << (j0 + jj);
+                    }
+                }
+            }
+            const uint32_t base = I.tfirst + b;
+            for_marked_pairs(mask, lane, msp[w], msm[w], [&](bool valid, int pl, int t) {
+                bool hit = false;
+                if (valid && !((dead >> pl) & 1u)) {
                     const float4 qA = ppos[w][pl], dA = pdir[w][pl];
                     const float4 tq = T.p[t], cB = T.c[t];
                     const float4 pB = make_float4(tq.x, tq.y, tq.z, T.l[t]);
@@ -250,41 +271,8 @@ __global__ void __launch_bounds__(kTPB) k_old_tiles(const Real* __restrict__ rea
                         }
                     }
                 }
-            }
-            dead |= __reduce_or_sync(0xffffffffu, hit ? (1u << pl) : 0u);
-            __syncwarp();
-        };
-        for (uint32_t b = 0; b < nt; b += kWT) {
-            if (!__any_sync(0xffffffffu, alive)) break;
-            if (b + lane < nt) {
-                const uint32_t k = I.tfirst + b + lane;
-                const float4 p = spos[k], c = sdir[k];
-                T.l[lane] = p.w;
-                T.p[lane] = make_float4(p.x, p.y, p.z, p.w * 0.5f + c.w + Re.eps + c.w * Re.scf);
-                T.c[lane] = c;
-            }
-            __syncwarp();
-            const uint32_t m = min((uint32_t)kWT, nt - b);
-            int qn = 0;
-            if (alive) tests += m;
-            for (uint32_t j = 0; j < m; ++j) {
-                bool pass = false;
-                if (alive) {
-                    const float4 tq = T.p[j];
-                    const float bx = tq.x - ax, by = tq.y - ay, bz = tq.z - az;
-                    const float Rr = (hAp + tq.w) * 1.000002f + Re.slack;
-                    pass = bx * bx + by * by + bz * bz <= Rr * Rr;
-                }
-                const unsigned bal = __ballot_sync(0xffffffffu, pass);
-                if (pass) pq[w][qn + __popc(bal & lt)] = pq_entry(lane, j);
-                qn += __popc(bal);
-                if (qn >= 32) {
-                    qn -= 32;
-                    batch(qn, 32, I.tfirst + b);
-                    if ((dead >> lane) & 1u) alive = false;
-                }
-            }
-            if (qn) batch(0, qn, I.tfirst + b);
+                dead |= __reduce_or_sync(0xffffffffu, hit ? (1u << pl) : 0u);
+            });
             if ((dead >> lane) & 1u) alive = false;
             if (alive && vst[cid] == ST_REJ_OLD) alive = false;  // decided by another item
             __syncwarp();
@@ -344,8 +332,8 @@ __global__ void k_alive_bin(uint32_t n, const uint32_t* __restrict__ ntot, const
                             const uint8_t* __restrict__ state, const uint32_t* __restrict__ ccell,
                             const uint32_t* __restrict__ astart, uint32_t* __restrict__ acur,
                             const float4* __restrict__ gpos, const float4* __restrict__ gdir,
-                            const uint64_t* __restrict__ csidx, uint32_t* __restrict__ aperm,
-                            float4* __restrict__ apos, float4* __restrict__ adir, uint64_t* __restrict__ akey) {
+                            uint32_t* __restrict__ aperm, float4* __restrict__ apos,
+                            float4* __restrict__ adir) {
     uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= *ntot) return;
     uint32_t cid = cperm[q];
@@ -355,30 +343,29 @@ __global__ void k_alive_bin(uint32_t n, const uint32_t* __restrict__ ntot, const
     aperm[d] = cid;
     apos[d] = gpos[q];
     adir[d] = gdir[q];
-    akey[d] = csidx[cid];
 }
 
 // Earlier survivors of one neighbour cell that a survivor hits, over the work
-// list of the survivor cells (sphere pre-test per lane, full-warp batches of
-// the passing pairs). Certified hits are listed directly, uncertain pairs
-// queued (target = compact candidate id).
+// list of the survivor cells (sphere marks per lane, full-warp evaluation of
+// the marked pairs). Compact candidate ids follow stream order within a
+// realisation, so "earlier" is a smaller id. Certified hits are listed
+// directly, uncertain pairs queued (target = compact candidate id).
 __global__ void __launch_bounds__(kTPB) k_conf_tiles(const Real* __restrict__ reals,
                                                      const uint32_t* __restrict__ nitems, uint32_t icap,
                                                      const Item* __restrict__ items,
                                                      const uint32_t* __restrict__ aperm,
                                                      const float4* __restrict__ apos, const float4* __restrict__ adir,
-                                                     const uint64_t* __restrict__ akey, uint32_t* __restrict__ ccnt,
-                                                     uint32_t* __restrict__ clist, unsigned long long* __restrict__ xq,
-                                                     unsigned long long xcap, unsigned long long* __restrict__ ctr) {
+                                                     uint32_t* __restrict__ ccnt, uint32_t* __restrict__ clist,
+                                                     unsigned long long* __restrict__ xq, unsigned long long xcap,
+                                                     unsigned long long* __restrict__ ctr) {
     constexpr int kW = kTPB / 32;
     __shared__ WarpTile tiles[kW];
-    __shared__ uint64_t tkey[kW][kWT];
     __shared__ uint32_t tid_[kW][kWT];
     __shared__ float4 ppos[kW][32], pdir[kW][32];
     __shared__ uint32_t pcid[kW][32];
-    __shared__ uint16_t pq[kW][kPQ];
+    __shared__ int msp[kW][32];
+    __shared__ uint32_t msm[kW][32];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const unsigned lt = (1u << lane) - 1u;
     WarpTile& T = tiles[w];
     unsigned long long tests = 0, ovf = 0, cert = 0;
     const uint32_t n = min(*nitems, icap);
@@ -392,21 +379,47 @@ __global__ void __launch_bounds__(kTPB) k_conf_tiles(const Real* __restrict__ re
         const uint32_t q = I.pfirst + lane;
         const uint32_t cid = have ? aperm[q] : 0u;
         float4 pA = make_float4(0, 0, 0, 0), cA = pA;
-        uint64_t kA = 0;
-        if (have) { pA = apos[q]; cA = adir[q]; kA = akey[q]; }
+        if (have) { pA = apos[q]; cA = adir[q]; }
         __syncwarp();
         ppos[w][lane] = pA;
         pdir[w][lane] = cA;
         pcid[w][lane] = cid;
         const float sx = img[0] * Re.L[0], sy = img[1] * Re.L[1], sz = img[2] * Re.L[2];
         const float ax = pA.x - sx, ay = pA.y - sy, az = pA.z - sz;
-        const float hAp = pA.w * 0.5f + cA.w + Re.eps + cA.w * Re.scf + Re.sep + Re.eps;
-        auto batch = [&](int from, int cnt) {
+        const float hA2 = (pA.w * 0.5f + cA.w + Re.eps + cA.w * Re.scf + Re.sep + Re.eps) * 1.000002f + Re.slack;
+        for (uint32_t b = 0; b < nt; b += kWT) {
+            const uint32_t m = min((uint32_t)kWT, nt - b);
+            if ((uint32_t)lane < m) {
+                const uint32_t k = I.tfirst + b + lane;
+                const float4 p = apos[k], c = adir[k];
+                T.l[lane] = p.w;
+                T.p[lane] = make_float4(p.x, p.y, p.z, (p.w * 0.5f + c.w + Re.eps + c.w * Re.scf) * 1.000002f);
+                T.c[lane] = c;
+                tid_[w][lane] = aperm[k];
+            } else {
+                T.p[lane] = make_float4(kFar, kFar, kFar, 0.0f);
+                tid_[w][lane] = 0xffffffffu;
+            }
             __syncwarp();
-            if (lane < cnt) {
-                const uint16_t e = pq[w][from + lane];
-                const int pl = e >> 5;
-                const uint32_t t = e & 31u;
+            uint32_t mask = 0, emask = 0;  // marked pairs; earlier survivors
+            if (have) {
+                const uint32_t m8 = (m + 7u) & ~7u;
+                for (uint32_t j0 = 0; j0 < m8; j0 += 8) {
+#pragma unroll
+                    for (uint32_t jj = 0; jj < 8; ++jj) {
+                        const uint32_t j = j0 + jj;
+                        const float4 tq = T.p[j];
+                        const float bx = tq.x - ax, by = tq.y - ay, bz = tq.z - az;
+                        const float Rr = hA2 + tq.w;
+                        const uint32_t bit = tid_[w][j] < cid ? (1u << j) : 0u;
+                        emask |= bit;
+                        if (bx * bx + by * by + bz * bz <= Rr * Rr) mask |= bit;
+                    }
+                }
+                tests += __popc(emask);
+            }
+            for_marked_pairs(mask, lane, msp[w], msm[w], [&](bool valid, int pl, int t) {
+                if (!valid) return;
                 const float4 qA = ppos[w][pl], dA = pdir[w][pl];
                 const float4 tq = T.p[t], cB = T.c[t];
                 const float4 pB = make_float4(tq.x, tq.y, tq.z, T.l[t]);
@@ -422,40 +435,7 @@ __global__ void __launch_bounds__(kTPB) k_conf_tiles(const Real* __restrict__ re
                         xq_push(xq, xcap, &ctr[C_XQ_CONF], xq_pack(c, tid_[w][t], img));
                     }
                 }
-            }
-            __syncwarp();
-        };
-        for (uint32_t b = 0; b < nt; b += kWT) {
-            if (b + lane < nt) {
-                const uint32_t k = I.tfirst + b + lane;
-                const float4 p = apos[k], c = adir[k];
-                T.l[lane] = p.w;
-                T.p[lane] = make_float4(p.x, p.y, p.z, p.w * 0.5f + c.w + Re.eps + c.w * Re.scf);
-                T.c[lane] = c;
-                tkey[w][lane] = akey[k];
-                tid_[w][lane] = aperm[k];
-            }
-            __syncwarp();
-            const uint32_t m = min((uint32_t)kWT, nt - b);
-            int qn = 0;
-            for (uint32_t j = 0; j < m; ++j) {
-                bool pass = false;
-                if (have && tkey[w][j] < kA) {  // earlier survivors only
-                    ++tests;
-                    const float4 tq = T.p[j];
-                    const float bx = tq.x - ax, by = tq.y - ay, bz = tq.z - az;
-                    const float Rr = (hAp + tq.w) * 1.000002f + Re.slack;
-                    pass = bx * bx + by * by + bz * bz <= Rr * Rr;
-                }
-                const unsigned bal = __ballot_sync(0xffffffffu, pass);
-                if (pass) pq[w][qn + __popc(bal & lt)] = pq_entry(lane, j);
-                qn += __popc(bal);
-                if (qn >= 32) {
-                    qn -= 32;
-                    batch(qn, 32);
-                }
-            }
-            if (qn) batch(0, qn);
+            });
             __syncwarp();
         }
     }
@@ -728,7 +708,7 @@ void Engine::release() {
                              &meta, &u32tmp, &rcnt, &rpos, &rcur, &cI, &cJ, &creal2, &eflag, &parent,
                              &cflag, &aidx, &rowp, &col, &deg};
     for (auto* b : u32) b->release();
-    DBuf<uint64_t>* u64[] = {&sidx, &kbeg, &csidx, &akey};
+    DBuf<uint64_t>* u64[] = {&sidx, &kbeg, &csidx};
     for (auto* b : u64) b->release();
     DBuf<double>* d64[] = {&ct0, &ct1, &cD, &cG, &cS, &vsrc, &vsnk, &volt, &val64, &diag64, &bvec, &xvec, &cgred};
     for (auto* b : d64) b->release();
@@ -990,7 +970,6 @@ nf_status Engine::generate() {
         NF_CK(gdir.ensure(slots));
         NF_CK(apos.ensure(slots));
         NF_CK(adir.ensure(slots));
-        NF_CK(akey.ensure(slots));
         NF_CK(aperm.ensure(slots));
         NF_CK(astart.ensure(ncell + 1));
         NF_CK(state.ensure(slots));
@@ -1049,7 +1028,7 @@ nf_status Engine::generate() {
         if (s != NF_OK) return s;
         NF_CK(cudaMemsetAsync(ccursor.p, 0, sizeof(uint32_t) * (ncell + 1), st));
         NF_LAUNCH(k_alive_bin, gs, 256, 0, st)((uint32_t)slots, ntot, cperm.p, state.p, ccell.p, astart.p, ccursor.p,
-                                               gpos.p, gdir.p, csidx.p, aperm.p, apos.p, adir.p, akey.p);
+                                               gpos.p, gdir.p, aperm.p, apos.p, adir.p);
         NF_CK(cudaGetLastError());
         s = build_items(astart.p, astart.p, 0, slots, slots);
         if (s != NF_OK) return s;
@@ -1057,7 +1036,7 @@ nf_status Engine::generate() {
         NF_CK(cudaMemsetAsync(ccnt.p, 0, sizeof(uint32_t) * slots, st));
         tstart(KT_CONF);
         NF_LAUNCH(k_conf_tiles, persistent_grid(k_conf_tiles), kTPB, 0, st)(dreal.p, item_count(), (uint32_t)items.cap, items.p, aperm.p, apos.p,
-                                                 adir.p, akey.p, ccnt.p, clist.p, xq2.p, xq2.cap, ctr.p);
+                                                 adir.p, ccnt.p, clist.p, xq2.p, xq2.cap, ctr.p);
         NF_CK(cudaGetLastError());
         NF_LAUNCH(k_conf_exact, xg, 256, 0, st)(dreal.p, xq2.p, ctr.p + C_XQ_CONF, xq2.cap, cpos.p, cdir.p, creal.p,
                                                 ccnt.p, clist.p, ctr.p);

@@ -25,14 +25,47 @@ constexpr int kWC = 32;     // probes per item: one per lane
 constexpr int kWT = 32;     // targets per warp-private shared-memory tile
 constexpr int kSeg = 128;   // targets per item at most
 
-// Pairs that pass the per-lane sphere pre-test are pushed on a per-warp
-// stack of (probe lane, target slot) entries and evaluated 32 at a time by
-// the full warp, so the long filter path (maybe_near, certain_hit) runs with
-// every lane busy instead of once per passing lane.
-constexpr int kPQ = 64;  // stack capacity: < 32 pending + one push of <= 32
+// Pairs that pass the per-lane sphere pre-test are marked in a 32-bit mask
+// per lane (bit j = staged target j); after the tile the marked pairs are
+// handed out 32 at a time to the whole warp, so the long filter path
+// (maybe_near, certain_hit) runs with every lane busy. A far-away position
+// pads the tile beyond its last target, so the marking loop needs no bound.
+constexpr float kFar = 1.0e30f;
 
-__device__ __forceinline__ uint16_t pq_entry(int probe_lane, uint32_t slot) {
-    return (uint16_t)(((uint32_t)probe_lane << 5) | slot);
+// Calls f(valid, probe_lane, slot) once per group of up to 32 marked pairs
+// (warp-uniform; f must be called by all lanes). sp / sm: 32-word scratch.
+template <class F>
+__device__ __forceinline__ void for_marked_pairs(uint32_t mask, int lane, int* sp, uint32_t* sm, F&& f) {
+    const int cnt = __popc(mask);
+    int incl = cnt;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int v = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += v;
+    }
+    const int total = __shfl_sync(0xffffffffu, incl, 31);
+    if (total == 0) return;
+    sp[lane] = incl - cnt;
+    sm[lane] = mask;
+    __syncwarp();
+    for (int base = 0; base < total; base += 32) {
+        const int g = base + lane;
+        const bool valid = g < total;
+        int pl = 0, t = 0;
+        if (valid) {
+            // owner lane: the last lane whose exclusive prefix is <= g
+            int src = 0;
+#pragma unroll
+            for (int step = 16; step; step >>= 1)
+                if (sp[src + step] <= g) src += step;
+            uint32_t m = sm[src];
+            for (int k = g - sp[src]; k > 0; --k) m &= m - 1u;
+            pl = src;
+            t = __ffs(m) - 1;
+        }
+        f(valid, pl, t);
+    }
+    __syncwarp();
 }
 
 // Warp-private staging of one tile of targets: position with the target's
