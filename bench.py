@@ -350,6 +350,23 @@ def run_ours(args, rank, world):
         "clocks": clk,
     }
     sim.set_kernel_timing(False)
+    if s["percolating"]:
+        # Differentiation form: the adjoint (gradient w.r.t. all endpoints, lambda,
+        # G0, copied to the host) against one forward network solve.
+        ts, ta = [], []
+        for _ in range(5):
+            a, b, c = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+            a.record()
+            sim.solve(check=False)
+            b.record()
+            sim.adjoint()
+            c.record()
+            torch.cuda.synchronize()
+            ts.append(a.elapsed_time(b))
+            ta.append(b.elapsed_time(c))
+        ts.sort()
+        ta.sort()
+        out["adjoint"] = {"solve_ms": ts[2], "adjoint_ms": ta[2], "adjoint_over_solve": ta[2] / ts[2]}
     # e2e through the C ABI with host buffers.
     if not args.no_e2e:
         times, h2d, d2h = [], 0, 0

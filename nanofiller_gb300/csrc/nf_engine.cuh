@@ -186,6 +186,10 @@ struct Engine {
     // count lands in ioff[ncell * 27] and its maximum over calls in ctr[C_ITEMS].
     // np / nt: probes and targets in all cells, for the first capacity guess.
     nf_status build_items(const uint32_t* pstart, const uint32_t* tstart, int stage, uint64_t np, uint64_t nt);
+    // Pinned host block for the per-round read-backs.
+    uint8_t* hpin = nullptr;
+    size_t hpin_cap = 0;
+    nf_status ensure_pinned(size_t bytes);
     // Device address of the item count of the last build_items (read it after
     // that call: build_items may reallocate ioff).
     const uint32_t* item_count() const { return ioff.p + (size_t)ncell * 27; }

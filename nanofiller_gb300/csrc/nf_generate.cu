@@ -632,6 +632,16 @@ __global__ void k_gather_pd(uint32_t n, const uint32_t* __restrict__ ntot, const
 
 // Work list of one pair sweep: probes binned by pstart against targets binned
 // by tstart, with the periodic flags of the stage (0 generation, 1 contacts).
+nf_status Engine::ensure_pinned(size_t bytes) {
+    if (bytes <= hpin_cap) return NF_OK;
+    if (hpin) cudaFreeHost(hpin);
+    hpin = nullptr;
+    hpin_cap = 0;
+    NF_CK(cudaMallocHost(reinterpret_cast<void**>(&hpin), bytes));
+    hpin_cap = bytes;
+    return NF_OK;
+}
+
 nf_status Engine::build_items(const uint32_t* pstart, const uint32_t* tstart, int stage, uint64_t np, uint64_t nt) {
     const size_t n27 = (size_t)ncell * 27;
     NF_CK(icnt.ensure(n27 + 1));
@@ -646,13 +656,56 @@ nf_status Engine::build_items(const uint32_t* pstart, const uint32_t* tstart, in
     NF_CK(cudaGetLastError());
     nf_status s = scan_u32(icnt.p, ioff.p, n27 + 1);
     if (s != NF_OK) return s;
-    NF_LAUNCH(k_item_fill, grid_for(n27, 256), 256, 0, st)(ncell, R, celloff.p, dreal.p, stage, pstart, tstart, ioff.p,
+    NF_LAUNCH(k_item_fill, grid_for(n27 * 32, 256), 256, 0, st)(ncell, R, celloff.p, dreal.p, stage, pstart, tstart, ioff.p,
                                                            items.p, (uint32_t)items.cap, ctr.p + C_ITEMS);
     NF_CK(cudaGetLastError());
     return NF_OK;
 }
 
+// Exclusive scan of up to kSmallScan values in one block: each thread sums a
+// contiguous run, the block scans the run totals, each thread writes its run.
+// Reads each value before writing its own slot, so in == out is allowed.
+constexpr size_t kSmallScan = 1 << 13;
+
+__global__ void __launch_bounds__(1024) k_scan_small(const uint32_t* in, uint32_t* out, uint32_t n) {
+    __shared__ uint32_t wsum[32];
+    const uint32_t per = (n + 1023u) / 1024u;
+    const uint32_t b = threadIdx.x * per, e = min(n, b + per);
+    uint32_t sum = 0;
+    for (uint32_t i = b; i < e; ++i) sum += in[i];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    uint32_t incl = sum;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t v = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += v;
+    }
+    if (lane == 31) wsum[w] = incl;
+    __syncthreads();
+    if (w == 0) {
+        uint32_t t = wsum[lane], ti = t;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t v = __shfl_up_sync(0xffffffffu, ti, o);
+            if (lane >= o) ti += v;
+        }
+        wsum[lane] = ti - t;  // exclusive prefix of the warp totals
+    }
+    __syncthreads();
+    uint32_t run = wsum[w] + incl - sum;
+    for (uint32_t i = b; i < e; ++i) {
+        const uint32_t v = in[i];
+        out[i] = run;
+        run += v;
+    }
+}
+
 nf_status Engine::scan_u32(const uint32_t* in, uint32_t* out, size_t n) {
+    if (n <= kSmallScan) {
+        NF_LAUNCH(k_scan_small, 1, 1024, 0, st)(in, out, (uint32_t)n);
+        NF_CK(cudaGetLastError());
+        return NF_OK;
+    }
     g_launches += 2;  // DeviceScan: tile-state init + scan
     size_t bytes = 0;
     NF_CK(cub::DeviceScan::ExclusiveSum(nullptr, bytes, in, out, (int)n, st));
@@ -712,6 +765,9 @@ void Engine::release() {
     for (auto* b : u64) b->release();
     DBuf<double>* d64[] = {&ct0, &ct1, &cD, &cG, &cS, &vsrc, &vsnk, &volt, &val64, &diag64, &bvec, &xvec, &cgred};
     for (auto* b : d64) b->release();
+    if (hpin) cudaFreeHost(hpin);
+    hpin = nullptr;
+    hpin_cap = 0;
     dreal.release(); mesh.release(); state.release(); ctr.release(); cubtmp.release(); items.release();
     vdbl.release();
     rec.release(); rec2.release(); recn.release(); cimg.release();
@@ -904,8 +960,7 @@ nf_status Engine::generate() {
         alive_max[r] = std::max(4096.0, 8.0 * V / (vex * peak));
     }
     std::vector<uint32_t> hcoff(R + 1);
-    std::vector<uint64_t> hkbeg(R), hout(2 * R);
-    std::vector<uint32_t> hmeta(4 * R);
+    std::vector<uint64_t> hkbeg(R);
     std::vector<uint64_t> c_round(R);
     std::vector<double> last_rate(R, 1.0);  // accepted / drawn in the last round
     double scale = 1.0;
@@ -1042,10 +1097,20 @@ nf_status Engine::generate() {
                                                 ccnt.p, clist.p, ctr.p);
         NF_CK(cudaGetLastError());
         tstop(KT_CONF);
-        // Resolution passes (chains are short), then one read-back of the
-        // overflow / queue / undecided counters.
+        // Resolution passes (chains are short), then the append, optimistic
+        // until one read-back of the counters shows that every candidate was
+        // decided; otherwise more passes and a fresh append (it is idempotent:
+        // the device rod counts change only after the read-back).
+        static_assert(C_UNDECIDED == C_OVERFLOW + 1 && C_ITEMS == C_XQ_OLD + 4, "read-back layout");
         uint64_t passes = 0;
         bool redo = false;
+        // pinned read-back block: [0..1] overflow, undecided; [2..6] old queue,
+        // conflict queue, (C_XQ, C_CERT), work items; then recn (2R u64), meta (4R u32)
+        s = ensure_pinned(sizeof(unsigned long long) * (7 + 2 * (size_t)R) + sizeof(uint32_t) * 4 * (size_t)R);
+        if (s != NF_OK) return s;
+        unsigned long long* hv = reinterpret_cast<unsigned long long*>(hpin);
+        uint64_t* hout = reinterpret_cast<uint64_t*>(hv + 7);
+        uint32_t* hmeta = reinterpret_cast<uint32_t*>(hout + 2 * R);
         for (;;) {
             for (int q = 0; q < 3; ++q)
                 NF_LAUNCH(k_resolve, gs, 256, 0, st)(ntot, state.p, ccnt.p, clist.p, ctr.p);
@@ -1053,13 +1118,22 @@ nf_status Engine::generate() {
             NF_LAUNCH(k_resolve, gs, 256, 0, st)(ntot, state.p, ccnt.p, clist.p, ctr.p);
             NF_CK(cudaGetLastError());
             passes += 4;
-            static_assert(C_UNDECIDED == C_OVERFLOW + 1 && C_ITEMS == C_XQ_OLD + 4, "read-back layout");
-            // conflict overflow, undecided, old queue, conflict queue, (C_XQ, C_CERT), work items
-            unsigned long long hv[7] = {0, 0, 0, 0, 0, 0, 0};
+            NF_LAUNCH(k_accflag, grid_for(slots + 1, 256), 256, 0, st)(ntot, (uint32_t)(slots + 1), state.p, accf.p);
+            NF_CK(cudaGetLastError());
+            s = scan_u32(accf.p, accpos.p, slots + 1);
+            if (s != NF_OK) return s;
+            NF_LAUNCH(k_meta, grid_for(R, 128), 128, 0, st)(R, coff.p, keep.p, kpos.p, accf.p, accpos.p, meta.p);
+            NF_CK(cudaGetLastError());
+            NF_CK(cudaMemsetAsync(recn.p, 0, sizeof(unsigned long long) * 2 * R, st));
+            NF_LAUNCH(k_append, gs, 256, 0, st)(ntot, state.p, creal.p, accpos.p, meta.p, rodoff.p, dcount.p, dreal.p,
+                                                cpos.p, cdir.p, csidx.p, pos.p, dir.p, sidx.p, (uint64_t*)recn.p);
+            NF_CK(cudaGetLastError());
             NF_CK(cudaMemcpyAsync(&hv[0], ctr.p + C_OVERFLOW, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
                                   st));
             NF_CK(cudaMemcpyAsync(&hv[2], ctr.p + C_XQ_OLD, 5 * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
                                   st));
+            NF_CK(cudaMemcpyAsync(hout, recn.p, sizeof(uint64_t) * 2 * R, cudaMemcpyDeviceToHost, st));
+            NF_CK(cudaMemcpyAsync(hmeta, meta.p, sizeof(uint32_t) * 4 * R, cudaMemcpyDeviceToHost, st));
             NF_CK(cudaStreamSynchronize(st));
             if (hv[6] > items.cap) {  // work list too small: grow it and redo the round
                 it_cap = (size_t)(hv[6] * 1.25) + 4096;
@@ -1084,20 +1158,6 @@ nf_status Engine::generate() {
             --rounds;
             continue;
         }
-        // Append.
-        NF_LAUNCH(k_accflag, grid_for(slots + 1, 256), 256, 0, st)(ntot, (uint32_t)(slots + 1), state.p, accf.p);
-        NF_CK(cudaGetLastError());
-        s = scan_u32(accf.p, accpos.p, slots + 1);
-        if (s != NF_OK) return s;
-        NF_LAUNCH(k_meta, grid_for(R, 128), 128, 0, st)(R, coff.p, keep.p, kpos.p, accf.p, accpos.p, meta.p);
-        NF_CK(cudaGetLastError());
-        NF_CK(cudaMemsetAsync(recn.p, 0, sizeof(unsigned long long) * 2 * R, st));
-        NF_LAUNCH(k_append, gs, 256, 0, st)(ntot, state.p, creal.p, accpos.p, meta.p, rodoff.p, dcount.p, dreal.p, cpos.p,
-                                     cdir.p, csidx.p, pos.p, dir.p, sidx.p, (uint64_t*)recn.p);
-        NF_CK(cudaGetLastError());
-        NF_CK(cudaMemcpyAsync(hmeta.data(), meta.p, sizeof(uint32_t) * 4 * R, cudaMemcpyDeviceToHost, st));
-        NF_CK(cudaMemcpyAsync(hout.data(), recn.p, sizeof(uint64_t) * 2 * R, cudaMemcpyDeviceToHost, st));
-        NF_CK(cudaStreamSynchronize(st));
         bool any_new = false;
         {
             double nc = 0;

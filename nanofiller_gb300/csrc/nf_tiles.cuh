@@ -122,16 +122,18 @@ static __global__ void k_item_count(uint32_t ncell, int R, const uint32_t* __res
     icnt[t] = n;
 }
 
+// One warp per (cell, offset): lane r writes items r, r + 32, ... of the pair
+// (item index = probe chunk * segments + target segment).
 static __global__ void k_item_fill(uint32_t ncell, int R, const uint32_t* __restrict__ celloff,
                                    const Real* __restrict__ reals, int stage, const uint32_t* __restrict__ pstart,
                                    const uint32_t* __restrict__ tstart, const uint32_t* __restrict__ ioff,
                                    Item* __restrict__ items, uint32_t cap, unsigned long long* __restrict__ imax) {
-    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t == 0) atomicMax(imax, (unsigned long long)ioff[ncell * 27u]);
+    const uint32_t gt = blockIdx.x * blockDim.x + threadIdx.x;
+    if (gt == 0) atomicMax(imax, (unsigned long long)ioff[ncell * 27u]);
+    const uint32_t t = gt >> 5, lane = gt & 31u;
     if (t >= ncell * 27u) return;
-    uint32_t k = ioff[t];
-    const uint32_t kend = ioff[t + 1];
-    if (k == kend) return;
+    const uint32_t k0 = ioff[t], kend = ioff[t + 1];
+    if (k0 == kend) return;
     const uint32_t c = t / 27u;
     const int o = (int)(t % 27u);
     const int r = find_real(celloff, R, c);
@@ -144,14 +146,13 @@ static __global__ void k_item_fill(uint32_t ncell, int R, const uint32_t* __rest
     stencil(Re, cc, o, stage_per(Re, stage), &nc, img);
     const uint32_t p0 = pstart[c], np = pstart[c + 1] - p0;
     const uint32_t t0 = tstart[nc], nt = tstart[nc + 1] - t0;
+    const uint32_t nseg = (nt + kSeg - 1) / kSeg;
     const uint32_t im = (uint32_t)(img[0] + 1) | ((uint32_t)(img[1] + 1) << 2) | ((uint32_t)(img[2] + 1) << 4);
-    for (uint32_t a = 0; a < np && k < kend; a += kWC) {
-        const uint32_t pa = min((uint32_t)kWC, np - a);
-        for (uint32_t b = 0; b < nt && k < kend; b += kSeg, ++k) {
-            if (k >= cap) return;
-            const uint32_t tb = min((uint32_t)kSeg, nt - b);
-            items[k] = Item{p0 + a, t0 + b, (uint32_t)r, pa | (tb << 6) | (im << 15)};
-        }
+    for (uint32_t k = k0 + lane; k < kend && k < cap; k += 32) {
+        const uint32_t idx = k - k0;
+        const uint32_t a = (idx / nseg) * kWC, b = (idx % nseg) * kSeg;
+        const uint32_t pa = min((uint32_t)kWC, np - a), tb = min((uint32_t)kSeg, nt - b);
+        items[k] = Item{p0 + a, t0 + b, (uint32_t)r, pa | (tb << 6) | (im << 15)};
     }
 }
 
