@@ -580,6 +580,29 @@ double nfo_contact_area(const nfo_rod* A, const nfo_rod* B, const double shift[3
     return S;
 }
 
+int64_t nfo_first_hits(const nf_params* p, const nfo_rod* probes, const uint64_t* k, int64_t m,
+                       const nfo_rod* rods, const uint64_t* sidx, int64_t n, int nthreads, int64_t* out) {
+    if (!p || (m && (!probes || !k || !out)) || (n && (!rods || !sidx))) return -1;
+    const int nt = nthreads_of(nthreads);
+    std::vector<RodT<double>> R(n);
+    for (int64_t j = 0; j < n; ++j) R[j] = rodT<double>(rods[j]);
+    const double L[3] = {(double)p->box[0], (double)p->box[1], (double)p->box[2]};
+    #pragma omp parallel for num_threads(nt) schedule(dynamic, 1)
+    for (int64_t i = 0; i < m; ++i) {
+        const RodT<double> A = rodT<double>(probes[i]);
+        int64_t first = -1;
+        for (int64_t j = 0; j < n && first < 0; ++j) {
+            if (sidx[j] >= k[i]) continue;
+            for_images(p->gen_periodic & 7, [&](const int img[3]) {
+                if (first < 0 && hc_hit(A, R[j], img[0] * L[0], img[1] * L[1], img[2] * L[2], p, nullptr))
+                    first = j;
+            });
+        }
+        out[i] = first;
+    }
+    return m;
+}
+
 int nfo_candidates(const nf_params* p, const float* mesh, int nx, int ny, int nz, uint64_t k0,
                    uint64_t n, float* out) {
     if (!p || !out) return -1;

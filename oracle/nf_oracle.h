@@ -55,6 +55,12 @@ int nfo_screen_eval(const nfo_rod *A, const double vr[3], const double vc[3],
 double nfo_contact_area(const nfo_rod *A, const nfo_rod *B, const double shift[3],
                         double Dtt_x, double t0u, double t1u, double rlim);
 
+/* Brute force over all images: for each probe i, the first rod j (array order)
+ * with sidx[j] < k[i] that the probe hits in the FP64 hard-core test of the
+ * generation stage, or -1. For checking accepted / rejected decisions. */
+int64_t nfo_first_hits(const nf_params *p, const nfo_rod *probes, const uint64_t *k, int64_t m,
+                       const nfo_rod *rods, const uint64_t *sidx, int64_t n, int nthreads, int64_t *out);
+
 /* Candidate stream k0..k0+n-1: out[10*i + f], f = x y z cx cy cz l a u rho. */
 int nfo_candidates(const nf_params *p, const float *mesh, int nx, int ny, int nz,
                    uint64_t k0, uint64_t n, float *out);

@@ -106,6 +106,9 @@ def lib():
             L.nfo_contacts.argtypes = [P(NfParams), C.c_void_p, C.c_int64, C.c_int, C.c_int,
                                        C.c_int64] + [C.c_void_p] * 8 + [P(C.c_int64)]
             L.nfo_contacts.restype = C.c_int64
+            L.nfo_first_hits.argtypes = [P(NfParams), C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p,
+                                         C.c_int64, C.c_int, C.c_void_p]
+            L.nfo_first_hits.restype = C.c_int64
             L.nfo_solve.argtypes = [C.c_int64, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p,
                                     C.c_double, C.c_int, C.c_void_p, P(C.c_double)]
             L.nfo_solve.restype = C.c_double
@@ -155,6 +158,22 @@ def pair_eval(A, B, shift=(0.0, 0.0, 0.0), kind=1, use_double=True, eps=1e-6, sc
     hit = lib().nfo_pair_eval(int(use_double), kind, _ptr(a), _ptr(b), sh, eps, scf, thr_sep,
                               int(typo), out)
     return bool(hit), list(out)
+
+
+def first_hits(params, probes, k, rods, stream_index, nthreads=0):
+    """For each probe (rod record) with stream index k: the first accepted rod
+    with a smaller stream index that it hits (FP64, all images), or -1."""
+    p = make_params(params)
+    probes = np.ascontiguousarray(probes, ROD_DTYPE)
+    rods = np.ascontiguousarray(rods, ROD_DTYPE)
+    k = np.ascontiguousarray(k, np.uint64)
+    si = np.ascontiguousarray(stream_index, np.uint64)
+    out = np.zeros(len(probes), np.int64)
+    r = lib().nfo_first_hits(C.byref(p), _ptr(probes), _ptr(k), len(probes), _ptr(rods), _ptr(si), len(rods),
+                             nthreads, _ptr(out))
+    if r < 0:
+        raise RuntimeError("nfo_first_hits failed")
+    return out
 
 
 def generate(params, mesh=None, nthreads=0, batch=4096, brute_force=False, cap=None):

@@ -212,14 +212,14 @@ def test_autograd_function_wraps_the_adjoint(gpu, network):
     g0 = torch.tensor(base["G0"], dtype=torch.float64, requires_grad=True)
     G = Geff.apply(ends, lam, g0)
     (2.0 * G).backward()
-    assert float(G) > 0
+    assert float(G.detach()) > 0
     # the same network computed directly gives the same value and gradient
     with gpu.Simulation(base) as sim:
         sim.set_rods(rods_from_endpoints(E0, a))
         sim.contacts()
         s = sim.solve()
         g, dl, dg0 = sim.adjoint()
-    assert float(G) == pytest.approx(s["G_eff"], rel=1e-12)
+    assert float(G.detach()) == pytest.approx(s["G_eff"], rel=1e-12)
     np.testing.assert_array_equal(ends.grad.numpy(), 2.0 * g.astype(np.float64))
     assert float(lam.grad) == pytest.approx(2.0 * dl, rel=1e-12)
     assert float(g0.grad) == pytest.approx(2.0 * dg0, rel=1e-12)
