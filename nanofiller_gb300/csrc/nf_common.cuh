@@ -156,9 +156,11 @@ struct Real {
     const float* mesh;
     int32_t mn[3];
     float dflt;
-    // cell grid (shared by generation, contacts and screening)
+    // cell grid (shared by generation, contacts and screening); every pair
+    // within reach is at most S cells apart along each axis
     int32_t n[3];
     float invE[3];
+    int32_t S;
     int32_t per_gen, per_con;
     uint32_t cell_off, ncell;
     // rods
@@ -266,27 +268,46 @@ NF_HD uint32_t cell_of(const Real& R, float x, float y, float z) {
     return R.cell_off + (uint32_t)(cx + R.n[0] * (cy + R.n[1] * cz));
 }
 
-// Neighbour of cell (c) by offset o in {-1,0,1}^3 under periodic mask `per`.
-// Returns false when the offset leaves an open axis; img = periodic image of
-// the neighbour cell relative to the box (the stride2dspl shift).
-NF_HD bool stencil(const Real& R, const int c[3], int o, int per, uint32_t* cell, int img[3]) {
-    int off[3] = {o % 3 - 1, (o / 3) % 3 - 1, o / 9 - 1};
-    int q[3];
+// Row r of the (2S+1)^2 rows of the stencil of cell c: the cells at
+// (c.x - S .. c.x + S, c.y + dy, c.z + dz). Along x the row is split where it
+// wraps, into at most 3 runs of consecutive cells, each with one periodic image.
+// Returns the number of runs (0 when the row leaves an open axis).
+struct Run {
+    uint32_t lo, hi;  // global ids of the first and last cell of the run
+    int img[3];
+};
+
+NF_HD int stencil_row(const Real& R, const int c[3], int r, int per, Run run[3]) {
+    const int w = 2 * R.S + 1;
+    if (r >= w * w) return 0;
+    int q[3], im[3] = {0, 0, 0};
+    const int off[3] = {0, r % w - R.S, r / w - R.S};
 #pragma unroll
-    for (int d = 0; d < 3; ++d) {
+    for (int d = 1; d < 3; ++d) {
         int v = c[d] + off[d];
-        img[d] = 0;
         if (v < 0) {
-            if (!(per & (1 << d))) return false;
-            v += R.n[d]; img[d] = -1;
+            if (!(per & (1 << d))) return 0;
+            v += R.n[d]; im[d] = -1;
         } else if (v >= R.n[d]) {
-            if (!(per & (1 << d))) return false;
-            v -= R.n[d]; img[d] = 1;
+            if (!(per & (1 << d))) return 0;
+            v -= R.n[d]; im[d] = 1;
         }
         q[d] = v;
     }
-    *cell = R.cell_off + (uint32_t)(q[0] + R.n[0] * (q[1] + R.n[1] * q[2]));
-    return true;
+    const uint32_t base = R.cell_off + (uint32_t)(R.n[0] * (q[1] + R.n[1] * q[2]));
+    const int nx = R.n[0], x0 = c[0] - R.S, x1 = c[0] + R.S;
+    const bool px = (per & 1) != 0;
+    int k = 0;
+    auto put = [&](int lo, int hi, int ix) {
+        run[k].lo = base + (uint32_t)lo;
+        run[k].hi = base + (uint32_t)hi;
+        run[k].img[0] = ix; run[k].img[1] = im[1]; run[k].img[2] = im[2];
+        ++k;
+    };
+    if (px && x0 < 0) put(x0 + nx, nx - 1, -1);
+    put(x0 < 0 ? 0 : x0, x1 >= nx ? nx - 1 : x1, 0);
+    if (px && x1 >= nx) put(0, x1 - nx, 1);
+    return k;
 }
 
 // ---------------------------------------------------------------------------
@@ -325,6 +346,23 @@ NF_HD bool maybe_near(const float4& pA, const float4& cA, const float4& pB, cons
         if (nb - err > thr_s * s) return false;
     }
     return true;
+}
+
+// The line-distance test of maybe_near on its own (same expressions, so
+// line_far() true implies maybe_near() false): the two infinite axis lines are
+// certainly farther apart than thr. Near-parallel pairs are never far here.
+NF_HD bool line_far(const float4& pA, const float4& cA, const float4& pB, const float4& cB, float sx, float sy,
+                    float sz, float thr, float slack) {
+    float bx = (pB.x + sx) - pA.x, by = (pB.y + sy) - pA.y, bz = (pB.z + sz) - pA.z;
+    float bb = bx * bx + by * by + bz * bz;
+    float nx = cA.y * cB.z - cA.z * cB.y;
+    float ny = cA.z * cB.x - cA.x * cB.z;
+    float nz = cA.x * cB.y - cA.y * cB.x;
+    float nn = nx * nx + ny * ny + nz * nz;
+    if (!(nn > 1e-4f)) return false;
+    float err = 4e-6f * (1.0f + sqrtf(bb)) + slack;
+    float nb = fabsf(nx * bx + ny * by + nz * bz);
+    return nb - err > thr * 1.0002f * sqrtf(nn);
 }
 
 // The sphere bound of maybe_near with the probe's terms hoisted: hAs = hA +

@@ -45,6 +45,7 @@ __global__ void __launch_bounds__(kTPB) k_ct_tiles(const Real* __restrict__ real
     __shared__ float4 ppos[kW][32], pdir[kW][32];
     __shared__ int msp[kW][32];
     __shared__ uint32_t msm[kW][32];
+    __shared__ uint16_t mq2[kW][64];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     WarpTile& T = tiles[w];
     const float epc = 1e-6f;  // DEV_PRECISION (inc/definitions.h:5)
@@ -99,7 +100,12 @@ __global__ void __launch_bounds__(kTPB) k_ct_tiles(const Real* __restrict__ real
                 tests += __popc(umask);
             }
             const uint32_t base = I.tfirst + b;
-            for_marked_pairs(mask, lane, msp[w], msm[w], [&](bool valid, int pl, int t) {
+            auto keep = [&](int pl, int t) {
+                const float4 dA = pdir[w][pl], tq = T.p[t], cB = T.c[t];
+                const float4 pB = make_float4(tq.x, tq.y, tq.z, T.l[t]);
+                return !line_far(ppos[w][pl], dA, pB, cB, sx, sy, sz, (cB.w + dA.w) + Re.cut + epc, Re.slack);
+            };
+            for_marked_pairs(mask, lane, msp[w], msm[w], mq2[w], keep, [&](bool valid, int pl, int t) {
                 if (!valid) return;
                 const float4 qA = ppos[w][pl], dA = pdir[w][pl];
                 const float4 tq = T.p[t], cB = T.c[t];

@@ -192,7 +192,7 @@ struct Engine {
     nf_status ensure_pinned(size_t bytes);
     // Device address of the item count of the last build_items (read it after
     // that call: build_items may reallocate ioff).
-    const uint32_t* item_count() const { return ioff.p + (size_t)ncell * 27; }
+    const uint32_t* item_count() const { return ioff.p + (size_t)ncell * kRows; }
     // Persistent grid of a pair kernel: as many kTPB-thread blocks as fit on
     // the device at once.
     template <class K>

@@ -104,14 +104,26 @@ Real make_real(const nf_params& p, const float* dmesh, int mn[3], double reach) 
     R.mesh = dmesh;
     for (int d = 0; d < 3; ++d) R.mn[d] = dmesh ? mn[d] : 0;
     R.dflt = p.density_default;
-    double e = std::max(reach * 1.0001, (double)p.cell_edge);
-    for (int d = 0; d < 3; ++d) {
-        int c = (int)std::floor((double)p.box[d] / e);
-        R.n[d] = c < 1 ? 1 : c;
-        R.invE[d] = (float)((double)R.n[d] / (double)p.box[d]);
-    }
     R.per_gen = p.gen_periodic & 7;
     R.per_con = (p.gen_periodic & ~p.field_dir) & 7;
+    // Cells of edge >= reach / S with a stencil of radius S. S = 2 tests about
+    // 125 (reach/2)^3 of volume per probe instead of 27 reach^3 for S = 1; a
+    // periodic axis needs at least S cells so that images stay within +-1.
+    auto grid = [&](int S) {
+        const double e = std::max(reach * 1.0001 / S, (double)p.cell_edge);
+        double emin = 1e300;
+        for (int d = 0; d < 3; ++d) {
+            int c = (int)std::floor((double)p.box[d] / e);
+            R.n[d] = c < 1 ? 1 : c;
+            R.invE[d] = (float)((double)R.n[d] / (double)p.box[d]);
+            emin = std::min(emin, (double)p.box[d] / R.n[d]);
+        }
+        R.S = std::max(1, (int)std::ceil(reach * 1.0001 / emin - 1e-9));
+        for (int d = 0; d < 3; ++d)
+            if (((R.per_gen | R.per_con) >> d & 1) && R.n[d] < R.S) return false;
+        return R.S <= kStencilMax;
+    };
+    if (!grid(2)) grid(1);
     R.eps = p.tol;
     R.scf = p.sc_frac;
     R.sep = p.sep;
@@ -200,6 +212,7 @@ __global__ void __launch_bounds__(kTPB) k_old_tiles(const Real* __restrict__ rea
     __shared__ uint32_t pcid[kW][32];
     __shared__ int msp[kW][32];
     __shared__ uint32_t msm[kW][32];
+    __shared__ uint16_t mq2[kW][64];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     WarpTile& T = tiles[w];
     volatile uint8_t* vst = state;
@@ -253,7 +266,14 @@ __global__ void __launch_bounds__(kTPB) k_old_tiles(const Real* __restrict__ rea
                 }
             }
             const uint32_t base = I.tfirst + b;
-            for_marked_pairs(mask, lane, msp[w], msm[w], [&](bool valid, int pl, int t) {
+            auto keep = [&](int pl, int t) {
+                if ((dead >> pl) & 1u) return false;
+                const float4 dA = pdir[w][pl], tq = T.p[t], cB = T.c[t];
+                const float4 pB = make_float4(tq.x, tq.y, tq.z, T.l[t]);
+                return !line_far(ppos[w][pl], dA, pB, cB, sx, sy, sz, (cB.w + dA.w) * Re.scf + Re.sep + Re.eps,
+                                 Re.slack);
+            };
+            for_marked_pairs(mask, lane, msp[w], msm[w], mq2[w], keep, [&](bool valid, int pl, int t) {
                 bool hit = false;
                 if (valid && !((dead >> pl) & 1u)) {
                     const float4 qA = ppos[w][pl], dA = pdir[w][pl];
@@ -365,6 +385,7 @@ __global__ void __launch_bounds__(kTPB) k_conf_tiles(const Real* __restrict__ re
     __shared__ uint32_t pcid[kW][32];
     __shared__ int msp[kW][32];
     __shared__ uint32_t msm[kW][32];
+    __shared__ uint16_t mq2[kW][64];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     WarpTile& T = tiles[w];
     unsigned long long tests = 0, ovf = 0, cert = 0;
@@ -418,7 +439,13 @@ __global__ void __launch_bounds__(kTPB) k_conf_tiles(const Real* __restrict__ re
                 }
                 tests += __popc(emask);
             }
-            for_marked_pairs(mask, lane, msp[w], msm[w], [&](bool valid, int pl, int t) {
+            auto keep = [&](int pl, int t) {
+                const float4 dA = pdir[w][pl], tq = T.p[t], cB = T.c[t];
+                const float4 pB = make_float4(tq.x, tq.y, tq.z, T.l[t]);
+                return !line_far(ppos[w][pl], dA, pB, cB, sx, sy, sz, (cB.w + dA.w) * Re.scf + Re.sep + Re.eps,
+                                 Re.slack);
+            };
+            for_marked_pairs(mask, lane, msp[w], msm[w], mq2[w], keep, [&](bool valid, int pl, int t) {
                 if (!valid) return;
                 const float4 qA = ppos[w][pl], dA = pdir[w][pl];
                 const float4 tq = T.p[t], cB = T.c[t];
@@ -643,12 +670,12 @@ nf_status Engine::ensure_pinned(size_t bytes) {
 }
 
 nf_status Engine::build_items(const uint32_t* pstart, const uint32_t* tstart, int stage, uint64_t np, uint64_t nt) {
-    const size_t n27 = (size_t)ncell * 27;
+    const size_t n27 = (size_t)ncell * kRows;
     NF_CK(icnt.ensure(n27 + 1));
     NF_CK(ioff.ensure(n27 + 1));
     // Items of evenly spread probes and targets, with a quarter of headroom; a
     // work list that still overflows is grown and its pass redone.
-    const double guess = 27.0 * ((double)np / kWC + ncell) * (1.0 + (double)nt / ((double)ncell * kSeg)) * 1.25;
+    const double guess = 25.0 * ((double)np / kWC + ncell) * (1.0 + 5.0 * (double)nt / ((double)ncell * kSeg)) * 1.25;
     it_cap = std::max(it_cap, (size_t)std::min(guess, 4.0e8));
     NF_CK(items.ensure(it_cap));
     NF_LAUNCH(k_item_count, grid_for(n27 + 1, 256), 256, 0, st)(ncell, R, celloff.p, dreal.p, stage, pstart, tstart,

@@ -32,10 +32,15 @@ constexpr int kSeg = 128;   // targets per item at most
 // pads the tile beyond its last target, so the marking loop needs no bound.
 constexpr float kFar = 1.0e30f;
 
-// Calls f(valid, probe_lane, slot) once per group of up to 32 marked pairs
-// (warp-uniform; f must be called by all lanes). sp / sm: 32-word scratch.
-template <class F>
-__device__ __forceinline__ void for_marked_pairs(uint32_t mask, int lane, int* sp, uint32_t* sm, F&& f) {
+// Hands the marked pairs of a tile to the warp in two stages. Stage 1: 32 at a
+// time, keep(probe_lane, slot) runs a cheap rejection (one lane per pair).
+// Stage 2: the pairs kept are gathered in a second per-warp list q2 (64 entries)
+// and eval(valid, probe_lane, slot) runs on 32 of them at a time, so the long
+// evaluation also runs with every lane busy. eval is called by all lanes
+// (valid false on idle ones). sp / sm: 32-word scratch.
+template <class K, class F>
+__device__ __forceinline__ void for_marked_pairs(uint32_t mask, int lane, int* sp, uint32_t* sm, uint16_t* q2,
+                                                 K&& keep, F&& eval) {
     const int cnt = __popc(mask);
     int incl = cnt;
 #pragma unroll
@@ -45,14 +50,16 @@ __device__ __forceinline__ void for_marked_pairs(uint32_t mask, int lane, int* s
     }
     const int total = __shfl_sync(0xffffffffu, incl, 31);
     if (total == 0) return;
+    const unsigned lt = (1u << lane) - 1u;
     sp[lane] = incl - cnt;
     sm[lane] = mask;
     __syncwarp();
+    int n2 = 0;
     for (int base = 0; base < total; base += 32) {
         const int g = base + lane;
-        const bool valid = g < total;
+        bool kept = false;
         int pl = 0, t = 0;
-        if (valid) {
+        if (g < total) {
             // owner lane: the last lane whose exclusive prefix is <= g
             int src = 0;
 #pragma unroll
@@ -62,8 +69,24 @@ __device__ __forceinline__ void for_marked_pairs(uint32_t mask, int lane, int* s
             for (int k = g - sp[src]; k > 0; --k) m &= m - 1u;
             pl = src;
             t = __ffs(m) - 1;
+            kept = keep(pl, t);
         }
-        f(valid, pl, t);
+        const unsigned bal = __ballot_sync(0xffffffffu, kept);
+        if (kept) q2[n2 + __popc(bal & lt)] = (uint16_t)((pl << 5) | t);
+        n2 += __popc(bal);
+        if (n2 >= 32) {
+            __syncwarp();
+            n2 -= 32;
+            const uint16_t e = q2[n2 + lane];
+            eval(true, e >> 5, e & 31);
+            __syncwarp();
+        }
+    }
+    if (n2) {
+        __syncwarp();
+        const bool v = lane < n2;
+        const uint16_t e = v ? q2[lane] : (uint16_t)0;
+        eval(v, e >> 5, e & 31);
     }
     __syncwarp();
 }
@@ -95,64 +118,80 @@ __device__ __forceinline__ void item_unpack(const Item& I, uint32_t* np, uint32_
 // Stage selector of the periodic flags: 0 = generation, 1 = contacts.
 __device__ __forceinline__ int stage_per(const Real& Re, int stage) { return stage ? Re.per_con : Re.per_gen; }
 
-// Items of (cell c, offset o) for t = c * 27 + o; t == ncell * 27 writes 0.
+constexpr int kStencilMax = 2;                                  // largest stencil radius
+constexpr int kRows = (2 * kStencilMax + 1) * (2 * kStencilMax + 1);  // rows per cell
+
+__device__ __forceinline__ void cell_xyz(const Real& Re, uint32_t c, int cc[3]) {
+    const uint32_t loc = c - Re.cell_off;
+    cc[0] = (int)(loc % (uint32_t)Re.n[0]);
+    cc[1] = (int)((loc / (uint32_t)Re.n[0]) % (uint32_t)Re.n[1]);
+    cc[2] = (int)(loc / ((uint32_t)Re.n[0] * (uint32_t)Re.n[1]));
+}
+
+// Items of (cell c, stencil row r) for t = c * kRows + r: probe chunks of the
+// cell times target segments of every run of the row; t == ncell * kRows writes 0.
 static __global__ void k_item_count(uint32_t ncell, int R, const uint32_t* __restrict__ celloff,
                                     const Real* __restrict__ reals, int stage, const uint32_t* __restrict__ pstart,
                                     const uint32_t* __restrict__ tstart, uint32_t* __restrict__ icnt) {
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-    const uint32_t nt27 = ncell * 27u;
+    const uint32_t nt27 = ncell * (uint32_t)kRows;
     if (t > nt27) return;
     if (t == nt27) { icnt[t] = 0; return; }
-    const uint32_t c = t / 27u;
-    const int o = (int)(t % 27u);
+    const uint32_t c = t / kRows;
+    const int r = (int)(t % kRows);
     const uint32_t np = pstart[c + 1] - pstart[c];
     uint32_t n = 0;
     if (np) {
         const Real& Re = reals[find_real(celloff, R, c)];
-        const uint32_t loc = c - Re.cell_off;
-        const int cc[3] = {(int)(loc % (uint32_t)Re.n[0]), (int)((loc / (uint32_t)Re.n[0]) % (uint32_t)Re.n[1]),
-                           (int)(loc / ((uint32_t)Re.n[0] * (uint32_t)Re.n[1]))};
-        uint32_t nc;
-        int img[3];
-        if (stencil(Re, cc, o, stage_per(Re, stage), &nc, img)) {
-            const uint32_t nt = tstart[nc + 1] - tstart[nc];
-            n = ((np + kWC - 1) / kWC) * ((nt + kSeg - 1) / kSeg);
-        }
+        int cc[3];
+        cell_xyz(Re, c, cc);
+        Run run[3];
+        const int k = stencil_row(Re, cc, r, stage_per(Re, stage), run);
+        uint32_t segs = 0;
+        for (int q = 0; q < k; ++q) segs += (tstart[run[q].hi + 1] - tstart[run[q].lo] + kSeg - 1) / kSeg;
+        n = ((np + kWC - 1) / kWC) * segs;
     }
     icnt[t] = n;
 }
 
-// One warp per (cell, offset): lane r writes items r, r + 32, ... of the pair
-// (item index = probe chunk * segments + target segment).
+// One warp per (cell, row): lane i writes items i, i + 32, ... of the pair
+// (item index = probe chunk * segments of the row + segment).
 static __global__ void k_item_fill(uint32_t ncell, int R, const uint32_t* __restrict__ celloff,
                                    const Real* __restrict__ reals, int stage, const uint32_t* __restrict__ pstart,
                                    const uint32_t* __restrict__ tstart, const uint32_t* __restrict__ ioff,
                                    Item* __restrict__ items, uint32_t cap, unsigned long long* __restrict__ imax) {
     const uint32_t gt = blockIdx.x * blockDim.x + threadIdx.x;
-    if (gt == 0) atomicMax(imax, (unsigned long long)ioff[ncell * 27u]);
+    if (gt == 0) atomicMax(imax, (unsigned long long)ioff[ncell * (uint32_t)kRows]);
     const uint32_t t = gt >> 5, lane = gt & 31u;
-    if (t >= ncell * 27u) return;
+    if (t >= ncell * (uint32_t)kRows) return;
     const uint32_t k0 = ioff[t], kend = ioff[t + 1];
     if (k0 == kend) return;
-    const uint32_t c = t / 27u;
-    const int o = (int)(t % 27u);
-    const int r = find_real(celloff, R, c);
-    const Real& Re = reals[r];
-    const uint32_t loc = c - Re.cell_off;
-    const int cc[3] = {(int)(loc % (uint32_t)Re.n[0]), (int)((loc / (uint32_t)Re.n[0]) % (uint32_t)Re.n[1]),
-                       (int)(loc / ((uint32_t)Re.n[0] * (uint32_t)Re.n[1]))};
-    uint32_t nc;
-    int img[3];
-    stencil(Re, cc, o, stage_per(Re, stage), &nc, img);
+    const uint32_t c = t / kRows;
+    const int r = (int)(t % kRows);
+    const int ri = find_real(celloff, R, c);
+    const Real& Re = reals[ri];
+    int cc[3];
+    cell_xyz(Re, c, cc);
+    Run run[3];
+    const int nr = stencil_row(Re, cc, r, stage_per(Re, stage), run);
+    uint32_t t0[3], nt[3], sg[3], segs = 0, im[3];
+    for (int q = 0; q < nr; ++q) {
+        t0[q] = tstart[run[q].lo];
+        nt[q] = tstart[run[q].hi + 1] - t0[q];
+        sg[q] = (nt[q] + kSeg - 1) / kSeg;
+        segs += sg[q];
+        im[q] = (uint32_t)(run[q].img[0] + 1) | ((uint32_t)(run[q].img[1] + 1) << 2) |
+                ((uint32_t)(run[q].img[2] + 1) << 4);
+    }
     const uint32_t p0 = pstart[c], np = pstart[c + 1] - p0;
-    const uint32_t t0 = tstart[nc], nt = tstart[nc + 1] - t0;
-    const uint32_t nseg = (nt + kSeg - 1) / kSeg;
-    const uint32_t im = (uint32_t)(img[0] + 1) | ((uint32_t)(img[1] + 1) << 2) | ((uint32_t)(img[2] + 1) << 4);
     for (uint32_t k = k0 + lane; k < kend && k < cap; k += 32) {
         const uint32_t idx = k - k0;
-        const uint32_t a = (idx / nseg) * kWC, b = (idx % nseg) * kSeg;
-        const uint32_t pa = min((uint32_t)kWC, np - a), tb = min((uint32_t)kSeg, nt - b);
-        items[k] = Item{p0 + a, t0 + b, (uint32_t)r, pa | (tb << 6) | (im << 15)};
+        const uint32_t a = (idx / segs) * kWC;
+        uint32_t s = idx % segs, q = 0;
+        while (s >= sg[q]) s -= sg[q++];
+        const uint32_t b = s * kSeg;
+        const uint32_t pa = min((uint32_t)kWC, np - a), tb = min((uint32_t)kSeg, nt[q] - b);
+        items[k] = Item{p0 + a, t0[q] + b, (uint32_t)ri, pa | (tb << 6) | (im[q] << 15)};
     }
 }
 
