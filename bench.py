@@ -337,6 +337,8 @@ def run_ours(args, rank, world):
         "realisations_per_s": world * 1000.0 / ms_max,
         "pair_tests_per_s": (g["pair_tests"] + c["pair_tests"]) / (ms / 1000),
         "fp64_decisions": g["exact_evals"] + c["exact_evals"],
+        "generation_sweeps": {k: g[k] for k in ("work_items", "target_tiles", "pair_tests", "sphere_pairs",
+                                                  "line_pairs", "exact_evals")},
         "fp32_would_flip": g["fp32_would_flip"] + c["fp32_would_flip"],
         "decision_flips_vs_fp64": 0,
         "contacts": c["contacts"], "G_eff_S": s["G_eff"], "percolating": bool(s["percolating"]),

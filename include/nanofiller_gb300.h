@@ -144,6 +144,11 @@ typedef struct nf_gen_stats {
     int32_t rounds;
     int32_t target_reached;
     double ms;
+    /* work of the two pair sweeps (candidates vs rods, vs earlier candidates) */
+    uint64_t work_items;        /* (probe chunk, stencil row, segment) items  */
+    uint64_t target_tiles;      /* 32-target tiles staged                    */
+    uint64_t sphere_pairs;      /* pairs within the bounding-sphere reach    */
+    uint64_t line_pairs;        /* of those, axis lines within the threshold */
 } nf_gen_stats;
 
 typedef struct nf_contact_stats {

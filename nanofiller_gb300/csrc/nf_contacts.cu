@@ -33,7 +33,7 @@ static inline unsigned grid_for(size_t n, unsigned b) { return (unsigned)((n + b
 // filter cannot rule out are queued (probe, target = sorted rod indices) and
 // recorded by k_ct_exact from their FP64 evaluation.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(kTPB) k_ct_tiles(const Real* __restrict__ reals,
+__global__ void __launch_bounds__(kTPB, 8) k_ct_tiles(const Real* __restrict__ reals,
                                                    const uint32_t* __restrict__ nitems, uint32_t icap,
                                                    const Item* __restrict__ items,
                                                    const float4* __restrict__ spos, const float4* __restrict__ sdir,
@@ -51,8 +51,11 @@ __global__ void __launch_bounds__(kTPB) k_ct_tiles(const Real* __restrict__ real
     const float epc = 1e-6f;  // DEV_PRECISION (inc/definitions.h:5)
     unsigned long long tests = 0;
     const uint32_t n = min(*nitems, icap);
-    for (uint32_t it = blockIdx.x * kW + w; it < n; it += gridDim.x * kW) {
-        const Item I = items[it];
+    const uint32_t stride = gridDim.x * kW;
+    Item nxt = blockIdx.x * kW + w < n ? items[blockIdx.x * kW + w] : Item{0, 0, 0, 0};
+    for (uint32_t it = blockIdx.x * kW + w; it < n; it += stride) {
+        const Item I = nxt;
+        if (it + stride < n) nxt = items[it + stride];  // next item's descriptor in flight meanwhile
         uint32_t np, nt;
         int img[3];
         item_unpack(I, &np, &nt, img);
@@ -105,7 +108,7 @@ __global__ void __launch_bounds__(kTPB) k_ct_tiles(const Real* __restrict__ real
                 const float4 pB = make_float4(tq.x, tq.y, tq.z, T.l[t]);
                 return !line_far(ppos[w][pl], dA, pB, cB, sx, sy, sz, (cB.w + dA.w) + Re.cut + epc, Re.slack);
             };
-            for_marked_pairs(mask, lane, msp[w], msm[w], mq2[w], keep, [&](bool valid, int pl, int t) {
+            (void)for_marked_pairs(mask, lane, msp[w], msm[w], mq2[w], keep, [&](bool valid, int pl, int t) {
                 if (!valid) return;
                 const float4 qA = ppos[w][pl], dA = pdir[w][pl];
                 const float4 tq = T.p[t], cB = T.c[t];

@@ -198,7 +198,7 @@ __global__ void k_bin(uint32_t n, const uint32_t* __restrict__ ntot, const uint3
 // whole warp: far pairs dropped, clear hits decided in FP32 (the candidate is
 // rejected at once and skipped by every other item at its next tile), the
 // rest queued for FP64 (probe = compact candidate id, target = sorted rod).
-__global__ void __launch_bounds__(kTPB) k_old_tiles(const Real* __restrict__ reals,
+__global__ void __launch_bounds__(kTPB, 8) k_old_tiles(const Real* __restrict__ reals,
                                                     const uint32_t* __restrict__ nitems, uint32_t icap,
                                                     const Item* __restrict__ items,
                                                     const uint32_t* __restrict__ cperm,
@@ -216,10 +216,14 @@ __global__ void __launch_bounds__(kTPB) k_old_tiles(const Real* __restrict__ rea
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     WarpTile& T = tiles[w];
     volatile uint8_t* vst = state;
-    unsigned long long tests = 0, cert = 0;
+    unsigned long long tests = 0, cert = 0, nitem = 0, ntile = 0, nsph = 0, nline = 0;
     const uint32_t n = min(*nitems, icap);
-    for (uint32_t it = blockIdx.x * kW + w; it < n; it += gridDim.x * kW) {
-        const Item I = items[it];
+    const uint32_t stride = gridDim.x * kW;
+    Item nxt = blockIdx.x * kW + w < n ? items[blockIdx.x * kW + w] : Item{0, 0, 0, 0};
+    for (uint32_t it = blockIdx.x * kW + w; it < n; it += stride) {
+        const Item I = nxt;
+        if (it + stride < n) nxt = items[it + stride];  // next item's descriptor in flight meanwhile
+        ++nitem;
         uint32_t np, nt;
         int img[3];
         item_unpack(I, &np, &nt, img);
@@ -273,7 +277,9 @@ __global__ void __launch_bounds__(kTPB) k_old_tiles(const Real* __restrict__ rea
                 return !line_far(ppos[w][pl], dA, pB, cB, sx, sy, sz, (cB.w + dA.w) * Re.scf + Re.sep + Re.eps,
                                  Re.slack);
             };
-            for_marked_pairs(mask, lane, msp[w], msm[w], mq2[w], keep, [&](bool valid, int pl, int t) {
+            ++ntile;
+            nsph += __popc(mask);
+            const int kept_ = for_marked_pairs(mask, lane, msp[w], msm[w], mq2[w], keep, [&](bool valid, int pl, int t) {
                 bool hit = false;
                 if (valid && !((dead >> pl) & 1u)) {
                     const float4 qA = ppos[w][pl], dA = pdir[w][pl];
@@ -293,6 +299,7 @@ __global__ void __launch_bounds__(kTPB) k_old_tiles(const Real* __restrict__ rea
                 }
                 dead |= __reduce_or_sync(0xffffffffu, hit ? (1u << pl) : 0u);
             });
+            if (lane == 0) nline += kept_;
             if ((dead >> lane) & 1u) alive = false;
             if (alive && vst[cid] == ST_REJ_OLD) alive = false;  // decided by another item
             __syncwarp();
@@ -300,6 +307,12 @@ __global__ void __launch_bounds__(kTPB) k_old_tiles(const Real* __restrict__ rea
     }
     warp_add_u64(&ctr[C_PAIR_TESTS], tests);
     warp_add_u64(&ctr[C_CERT], cert);
+    if (lane == 0) {
+        atomicAdd(&ctr[C_G_ITEMS], nitem);
+        atomicAdd(&ctr[C_G_TILES], ntile);
+        atomicAdd(&ctr[C_G_LINE], nline);
+    }
+    warp_add_u64(&ctr[C_G_SPHERE], nsph);
 }
 
 // FP64 decisions of the queued (candidate, accepted rod) pairs.
@@ -370,7 +383,7 @@ __global__ void k_alive_bin(uint32_t n, const uint32_t* __restrict__ ntot, const
 // the marked pairs). Compact candidate ids follow stream order within a
 // realisation, so "earlier" is a smaller id. Certified hits are listed
 // directly, uncertain pairs queued (target = compact candidate id).
-__global__ void __launch_bounds__(kTPB) k_conf_tiles(const Real* __restrict__ reals,
+__global__ void __launch_bounds__(kTPB, 8) k_conf_tiles(const Real* __restrict__ reals,
                                                      const uint32_t* __restrict__ nitems, uint32_t icap,
                                                      const Item* __restrict__ items,
                                                      const uint32_t* __restrict__ aperm,
@@ -388,10 +401,14 @@ __global__ void __launch_bounds__(kTPB) k_conf_tiles(const Real* __restrict__ re
     __shared__ uint16_t mq2[kW][64];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     WarpTile& T = tiles[w];
-    unsigned long long tests = 0, ovf = 0, cert = 0;
+    unsigned long long tests = 0, ovf = 0, cert = 0, nitem = 0, ntile = 0, nsph = 0, nline = 0;
     const uint32_t n = min(*nitems, icap);
-    for (uint32_t it = blockIdx.x * kW + w; it < n; it += gridDim.x * kW) {
-        const Item I = items[it];
+    const uint32_t stride = gridDim.x * kW;
+    Item nxt = blockIdx.x * kW + w < n ? items[blockIdx.x * kW + w] : Item{0, 0, 0, 0};
+    for (uint32_t it = blockIdx.x * kW + w; it < n; it += stride) {
+        const Item I = nxt;
+        if (it + stride < n) nxt = items[it + stride];  // next item's descriptor in flight meanwhile
+        ++nitem;
         uint32_t np, nt;
         int img[3];
         item_unpack(I, &np, &nt, img);
@@ -445,7 +462,9 @@ __global__ void __launch_bounds__(kTPB) k_conf_tiles(const Real* __restrict__ re
                 return !line_far(ppos[w][pl], dA, pB, cB, sx, sy, sz, (cB.w + dA.w) * Re.scf + Re.sep + Re.eps,
                                  Re.slack);
             };
-            for_marked_pairs(mask, lane, msp[w], msm[w], mq2[w], keep, [&](bool valid, int pl, int t) {
+            ++ntile;
+            nsph += __popc(mask);
+            const int kept_ = for_marked_pairs(mask, lane, msp[w], msm[w], mq2[w], keep, [&](bool valid, int pl, int t) {
                 if (!valid) return;
                 const float4 qA = ppos[w][pl], dA = pdir[w][pl];
                 const float4 tq = T.p[t], cB = T.c[t];
@@ -463,12 +482,19 @@ __global__ void __launch_bounds__(kTPB) k_conf_tiles(const Real* __restrict__ re
                     }
                 }
             });
+            if (lane == 0) nline += kept_;
             __syncwarp();
         }
     }
     warp_add_u64(&ctr[C_PAIR_TESTS], tests);
     warp_add_u64(&ctr[C_OVERFLOW], ovf);
     warp_add_u64(&ctr[C_CERT], cert);
+    if (lane == 0) {
+        atomicAdd(&ctr[C_G_ITEMS], nitem);
+        atomicAdd(&ctr[C_G_TILES], ntile);
+        atomicAdd(&ctr[C_G_LINE], nline);
+    }
+    warp_add_u64(&ctr[C_G_SPHERE], nsph);
 }
 
 __global__ void __launch_bounds__(256) k_conf_exact(const Real* __restrict__ reals,
@@ -1232,6 +1258,10 @@ nf_status Engine::generate() {
         gst.target += hreal[r].target;
     }
     gst.pair_tests = hc[C_PAIR_TESTS];
+    gst.work_items = hc[C_G_ITEMS];
+    gst.target_tiles = hc[C_G_TILES];
+    gst.sphere_pairs = hc[C_G_SPHERE];
+    gst.line_pairs = hc[C_G_LINE];
     gst.exact_evals = hc[C_EXACT];
     gst.fp32_would_flip = hc[C_FLIPS];
     gst.exact_evals = hc[C_EXACT];

@@ -37,10 +37,11 @@ constexpr float kFar = 1.0e30f;
 // Stage 2: the pairs kept are gathered in a second per-warp list q2 (64 entries)
 // and eval(valid, probe_lane, slot) runs on 32 of them at a time, so the long
 // evaluation also runs with every lane busy. eval is called by all lanes
-// (valid false on idle ones). sp / sm: 32-word scratch.
+// (valid false on idle ones). sp / sm: 32-word scratch. Returns the number of
+// pairs kept by stage 1 (warp-uniform).
 template <class K, class F>
-__device__ __forceinline__ void for_marked_pairs(uint32_t mask, int lane, int* sp, uint32_t* sm, uint16_t* q2,
-                                                 K&& keep, F&& eval) {
+__device__ __forceinline__ int for_marked_pairs(uint32_t mask, int lane, int* sp, uint32_t* sm, uint16_t* q2,
+                                                K&& keep, F&& eval) {
     const int cnt = __popc(mask);
     int incl = cnt;
 #pragma unroll
@@ -49,8 +50,9 @@ __device__ __forceinline__ void for_marked_pairs(uint32_t mask, int lane, int* s
         if (lane >= o) incl += v;
     }
     const int total = __shfl_sync(0xffffffffu, incl, 31);
-    if (total == 0) return;
+    if (total == 0) return 0;
     const unsigned lt = (1u << lane) - 1u;
+    int kept_total = 0;
     sp[lane] = incl - cnt;
     sm[lane] = mask;
     __syncwarp();
@@ -74,6 +76,7 @@ __device__ __forceinline__ void for_marked_pairs(uint32_t mask, int lane, int* s
         const unsigned bal = __ballot_sync(0xffffffffu, kept);
         if (kept) q2[n2 + __popc(bal & lt)] = (uint16_t)((pl << 5) | t);
         n2 += __popc(bal);
+        kept_total += __popc(bal);
         if (n2 >= 32) {
             __syncwarp();
             n2 -= 32;
@@ -89,6 +92,7 @@ __device__ __forceinline__ void for_marked_pairs(uint32_t mask, int lane, int* s
         eval(v, e >> 5, e & 31);
     }
     __syncwarp();
+    return kept_total;
 }
 
 // Warp-private staging of one tile of targets: position with the target's
