@@ -33,7 +33,7 @@ static inline unsigned grid_for(size_t n, unsigned b) { return (unsigned)((n + b
 // filter cannot rule out are queued (probe, target = sorted rod indices) and
 // recorded by k_ct_exact from their FP64 evaluation.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(kTPB, 8) k_ct_tiles(const Real* __restrict__ reals,
+__global__ void __launch_bounds__(kTPB, 6) k_ct_tiles(const Real* __restrict__ reals,
                                                    const uint32_t* __restrict__ nitems, uint32_t icap,
                                                    const Item* __restrict__ items,
                                                    const float4* __restrict__ spos, const float4* __restrict__ sdir,

@@ -198,7 +198,7 @@ __global__ void k_bin(uint32_t n, const uint32_t* __restrict__ ntot, const uint3
 // whole warp: far pairs dropped, clear hits decided in FP32 (the candidate is
 // rejected at once and skipped by every other item at its next tile), the
 // rest queued for FP64 (probe = compact candidate id, target = sorted rod).
-__global__ void __launch_bounds__(kTPB, 8) k_old_tiles(const Real* __restrict__ reals,
+__global__ void __launch_bounds__(kTPB, 6) k_old_tiles(const Real* __restrict__ reals,
                                                     const uint32_t* __restrict__ nitems, uint32_t icap,
                                                     const Item* __restrict__ items,
                                                     const uint32_t* __restrict__ cperm,
@@ -383,7 +383,7 @@ __global__ void k_alive_bin(uint32_t n, const uint32_t* __restrict__ ntot, const
 // the marked pairs). Compact candidate ids follow stream order within a
 // realisation, so "earlier" is a smaller id. Certified hits are listed
 // directly, uncertain pairs queued (target = compact candidate id).
-__global__ void __launch_bounds__(kTPB, 8) k_conf_tiles(const Real* __restrict__ reals,
+__global__ void __launch_bounds__(kTPB, 6) k_conf_tiles(const Real* __restrict__ reals,
                                                      const uint32_t* __restrict__ nitems, uint32_t icap,
                                                      const Item* __restrict__ items,
                                                      const uint32_t* __restrict__ aperm,
