@@ -33,7 +33,7 @@ enum CandState : uint8_t { ST_NONE = 0, ST_REJ_OLD = 1, ST_ALIVE = 2, ST_ACC = 3
 enum Ctr {
     C_PAIR_TESTS = 0, C_EXACT, C_FLIPS, C_OVERFLOW, C_UNDECIDED,
     C_CT_PAIRS, C_CT_EXACT, C_CT_FLIPS, C_CT_RECORDS, C_SCR_PAIRS, C_SCR_EXACT,
-    C_CG_ITERS, C_XQ_OLD, C_XQ_CONF, C_XQ, C_CERT, C_ITEMS, C_G_ITEMS, C_G_TILES, C_G_SPHERE, C_G_LINE, C_NCTR
+    C_CG_ITERS, C_XQ_OLD, C_XQ_CONF, C_XQ, C_CERT, C_ITEMS, C_G_ITEMS, C_G_TILES, C_G_SPHERE, C_G_LINE, C_XQ_MARK, C_NCTR
 };
 
 template <class T>
@@ -185,7 +185,9 @@ struct Engine {
     // Work list of (probe chunk, offset, target segment) items; the item
     // count lands in ioff[ncell * 27] and its maximum over calls in ctr[C_ITEMS].
     // np / nt: probes and targets in all cells, for the first capacity guess.
-    nf_status build_items(const uint32_t* pstart, const uint32_t* tstart, int stage, uint64_t np, uint64_t nt);
+    // ring: 0 all stencil rows, 1 the inner rows (|dy|, |dz| <= 1), 2 the others.
+    nf_status build_items(const uint32_t* pstart, const uint32_t* tstart, int stage, uint64_t np, uint64_t nt,
+                          int ring = 0);
     // Pinned host block for the per-round read-backs.
     uint8_t* hpin = nullptr;
     size_t hpin_cap = 0;

@@ -318,15 +318,17 @@ __global__ void __launch_bounds__(kTPB, 6) k_old_tiles(const Real* __restrict__ 
 // FP64 decisions of the queued (candidate, accepted rod) pairs.
 __global__ void __launch_bounds__(256) k_old_exact(const Real* __restrict__ reals,
                                                    const unsigned long long* __restrict__ xq,
+                                                   const unsigned long long* __restrict__ first,
                                                    const unsigned long long* __restrict__ count,
                                                    unsigned long long cap, const float4* __restrict__ cpos,
                                                    const float4* __restrict__ cdir, const uint32_t* __restrict__ creal,
                                                    const float4* __restrict__ spos, const float4* __restrict__ sdir,
                                                    uint8_t* state, unsigned long long* __restrict__ ctr) {
     const unsigned long long n = min(*count, cap);
+    const unsigned long long e0 = first ? min(*first, cap) : 0ull;
     volatile uint8_t* vst = state;
     unsigned long long exact = 0, flips = 0;
-    for (unsigned long long e = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; e < n;
+    for (unsigned long long e = e0 + blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; e < n;
          e += (unsigned long long)gridDim.x * blockDim.x) {
         uint32_t cid, j;
         int img[3];
@@ -695,7 +697,8 @@ nf_status Engine::ensure_pinned(size_t bytes) {
     return NF_OK;
 }
 
-nf_status Engine::build_items(const uint32_t* pstart, const uint32_t* tstart, int stage, uint64_t np, uint64_t nt) {
+nf_status Engine::build_items(const uint32_t* pstart, const uint32_t* tstart, int stage, uint64_t np, uint64_t nt,
+                              int ring) {
     const size_t n27 = (size_t)ncell * kRows;
     NF_CK(icnt.ensure(n27 + 1));
     NF_CK(ioff.ensure(n27 + 1));
@@ -704,12 +707,12 @@ nf_status Engine::build_items(const uint32_t* pstart, const uint32_t* tstart, in
     const double guess = 25.0 * ((double)np / kWC + ncell) * (1.0 + 5.0 * (double)nt / ((double)ncell * kSeg)) * 1.25;
     it_cap = std::max(it_cap, (size_t)std::min(guess, 4.0e8));
     NF_CK(items.ensure(it_cap));
-    NF_LAUNCH(k_item_count, grid_for(n27 + 1, 256), 256, 0, st)(ncell, R, celloff.p, dreal.p, stage, pstart, tstart,
-                                                                 icnt.p);
+    NF_LAUNCH(k_item_count, grid_for(n27 + 1, 256), 256, 0, st)(ncell, R, celloff.p, dreal.p, stage, ring, pstart,
+                                                                 tstart, icnt.p);
     NF_CK(cudaGetLastError());
     nf_status s = scan_u32(icnt.p, ioff.p, n27 + 1);
     if (s != NF_OK) return s;
-    NF_LAUNCH(k_item_fill, grid_for(n27 * 32, 256), 256, 0, st)(ncell, R, celloff.p, dreal.p, stage, pstart, tstart, ioff.p,
+    NF_LAUNCH(k_item_fill, grid_for(n27 * 32, 256), 256, 0, st)(ncell, R, celloff.p, dreal.p, stage, ring, pstart, tstart, ioff.p,
                                                            items.p, (uint32_t)items.cap, ctr.p + C_ITEMS);
     NF_CK(cudaGetLastError());
     return NF_OK;
@@ -1110,34 +1113,66 @@ nf_status Engine::generate() {
         // Cell-sorted candidate copy and the chunk table of this round.
         NF_LAUNCH(k_gather_pd, gs, 256, 0, st)((uint32_t)slots, ntot, cperm.p, cpos.p, cdir.p, gpos.p, gdir.p);
         NF_CK(cudaGetLastError());
+        // The old-rod test runs in two phases when the grid has outer stencil
+        // rows and the round is heavy: every candidate against the inner rows
+        // (|dy|, |dz| <= 1: a third of the volume, most of the hits), then only
+        // the survivors, packed densely again, against the outer rows. Same
+        // decisions as one pass; the second pass costs a binning, a work list and
+        // two launches (~0.1 ms), repaid once candidates x rods passes ~1e10.
+        bool outer_rows = false;
+        double work = 0;
+        for (int r = 0; r < R; ++r) {
+            outer_rows |= c_round[r] && hreal[r].S > 1;
+            work += (double)c_round[r] * (double)count[r];
+        }
+        const bool two_phase = outer_rows && work > 1e10;
         NF_CK(cudaMemsetAsync(ctr.p + C_ITEMS, 0, sizeof(unsigned long long), st));
-        s = build_items(cstart.p, rstart.p, 0, slots, total_rods());
+        s = build_items(cstart.p, rstart.p, 0, slots, total_rods(), two_phase ? 1 : 0);
         if (s != NF_OK) return s;
         const unsigned xg = (unsigned)(4 * nsm);
         xq_cap = std::max(xq_cap, (size_t)(slots / 8));  // first guess; grown and redone on overflow
         NF_CK(xq.ensure(xq_cap));
         NF_CK(xq2.ensure(xq_cap));
         NF_CK(cudaMemsetAsync(ctr.p + C_XQ_OLD, 0, 2 * sizeof(unsigned long long), st));
+        // Survivors of the candidates in cell order (aperm / apos / adir, CSR astart).
+        auto bin_survivors = [&]() -> nf_status {
+            NF_CK(cudaMemsetAsync(ccursor.p, 0, sizeof(uint32_t) * (ncell + 1), st));
+            NF_LAUNCH(k_alive_count, gs, 256, 0, st)((uint32_t)slots, ntot, cperm.p, state.p, ccell.p, ccursor.p);
+            NF_CK(cudaGetLastError());
+            nf_status s2 = scan_u32(ccursor.p, astart.p, ncell + 1);
+            if (s2 != NF_OK) return s2;
+            NF_CK(cudaMemsetAsync(ccursor.p, 0, sizeof(uint32_t) * (ncell + 1), st));
+            NF_LAUNCH(k_alive_bin, gs, 256, 0, st)((uint32_t)slots, ntot, cperm.p, state.p, ccell.p, astart.p,
+                                                   ccursor.p, gpos.p, gdir.p, aperm.p, apos.p, adir.p);
+            NF_CK(cudaGetLastError());
+            return NF_OK;
+        };
         tstart(KT_OLD);
         if (total_rods() > 0) {
             NF_LAUNCH(k_old_tiles, persistent_grid(k_old_tiles), kTPB, 0, st)(dreal.p, item_count(), (uint32_t)items.cap, items.p, cperm.p, gpos.p,
                                                     gdir.p, spos.p, sdir.p, state.p, xq.p, xq.cap, ctr.p);
             NF_CK(cudaGetLastError());
-            NF_LAUNCH(k_old_exact, xg, 256, 0, st)(dreal.p, xq.p, ctr.p + C_XQ_OLD, xq.cap, cpos.p, cdir.p, creal.p,
-                                                   spos.p, sdir.p, state.p, ctr.p);
+            NF_LAUNCH(k_old_exact, xg, 256, 0, st)(dreal.p, xq.p, nullptr, ctr.p + C_XQ_OLD, xq.cap, cpos.p, cdir.p,
+                                                   creal.p, spos.p, sdir.p, state.p, ctr.p);
         }
         NF_CK(cudaGetLastError());
+        if (two_phase) {
+            NF_CK(cudaMemcpyAsync(ctr.p + C_XQ_MARK, ctr.p + C_XQ_OLD, sizeof(unsigned long long),
+                                  cudaMemcpyDeviceToDevice, st));
+            s = bin_survivors();
+            if (s != NF_OK) return s;
+            s = build_items(astart.p, rstart.p, 0, slots, total_rods(), 2);
+            if (s != NF_OK) return s;
+            NF_LAUNCH(k_old_tiles, persistent_grid(k_old_tiles), kTPB, 0, st)(dreal.p, item_count(), (uint32_t)items.cap, items.p, aperm.p, apos.p,
+                                                    adir.p, spos.p, sdir.p, state.p, xq.p, xq.cap, ctr.p);
+            NF_CK(cudaGetLastError());
+            NF_LAUNCH(k_old_exact, xg, 256, 0, st)(dreal.p, xq.p, ctr.p + C_XQ_MARK, ctr.p + C_XQ_OLD, xq.cap,
+                                                   cpos.p, cdir.p, creal.p, spos.p, sdir.p, state.p, ctr.p);
+            NF_CK(cudaGetLastError());
+        }
         tstop(KT_OLD);
-        // Survivors binned by cell.
-        NF_CK(cudaMemsetAsync(ccursor.p, 0, sizeof(uint32_t) * (ncell + 1), st));
-        NF_LAUNCH(k_alive_count, gs, 256, 0, st)((uint32_t)slots, ntot, cperm.p, state.p, ccell.p, ccursor.p);
-        NF_CK(cudaGetLastError());
-        s = scan_u32(ccursor.p, astart.p, ncell + 1);
+        s = bin_survivors();
         if (s != NF_OK) return s;
-        NF_CK(cudaMemsetAsync(ccursor.p, 0, sizeof(uint32_t) * (ncell + 1), st));
-        NF_LAUNCH(k_alive_bin, gs, 256, 0, st)((uint32_t)slots, ntot, cperm.p, state.p, ccell.p, astart.p, ccursor.p,
-                                               gpos.p, gdir.p, aperm.p, apos.p, adir.p);
-        NF_CK(cudaGetLastError());
         s = build_items(astart.p, astart.p, 0, slots, slots);
         if (s != NF_OK) return s;
         NF_CK(cudaMemsetAsync(ctr.p + C_OVERFLOW, 0, sizeof(unsigned long long), st));

@@ -132,11 +132,22 @@ __device__ __forceinline__ void cell_xyz(const Real& Re, uint32_t c, int cc[3]) 
     cc[2] = (int)(loc / ((uint32_t)Re.n[0] * (uint32_t)Re.n[1]));
 }
 
+// Row r of a radius-S stencil belongs to ring 1 (|dy|, |dz| <= 1) or ring 2;
+// ring 0 selects every row.
+__device__ __forceinline__ bool row_in_ring(const Real& Re, int r, int ring) {
+    if (ring == 0) return true;
+    const int w = 2 * Re.S + 1;
+    const int dy = r % w - Re.S, dz = r / w - Re.S;
+    const bool inner = dy >= -1 && dy <= 1 && dz >= -1 && dz <= 1;
+    return ring == 1 ? inner : !inner;
+}
+
 // Items of (cell c, stencil row r) for t = c * kRows + r: probe chunks of the
 // cell times target segments of every run of the row; t == ncell * kRows writes 0.
 static __global__ void k_item_count(uint32_t ncell, int R, const uint32_t* __restrict__ celloff,
-                                    const Real* __restrict__ reals, int stage, const uint32_t* __restrict__ pstart,
-                                    const uint32_t* __restrict__ tstart, uint32_t* __restrict__ icnt) {
+                                    const Real* __restrict__ reals, int stage, int ring,
+                                    const uint32_t* __restrict__ pstart, const uint32_t* __restrict__ tstart,
+                                    uint32_t* __restrict__ icnt) {
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t nt27 = ncell * (uint32_t)kRows;
     if (t > nt27) return;
@@ -150,7 +161,7 @@ static __global__ void k_item_count(uint32_t ncell, int R, const uint32_t* __res
         int cc[3];
         cell_xyz(Re, c, cc);
         Run run[3];
-        const int k = stencil_row(Re, cc, r, stage_per(Re, stage), run);
+        const int k = row_in_ring(Re, r, ring) ? stencil_row(Re, cc, r, stage_per(Re, stage), run) : 0;
         uint32_t segs = 0;
         for (int q = 0; q < k; ++q) segs += (tstart[run[q].hi + 1] - tstart[run[q].lo] + kSeg - 1) / kSeg;
         n = ((np + kWC - 1) / kWC) * segs;
@@ -161,7 +172,7 @@ static __global__ void k_item_count(uint32_t ncell, int R, const uint32_t* __res
 // One warp per (cell, row): lane i writes items i, i + 32, ... of the pair
 // (item index = probe chunk * segments of the row + segment).
 static __global__ void k_item_fill(uint32_t ncell, int R, const uint32_t* __restrict__ celloff,
-                                   const Real* __restrict__ reals, int stage, const uint32_t* __restrict__ pstart,
+                                   const Real* __restrict__ reals, int stage, int ring, const uint32_t* __restrict__ pstart,
                                    const uint32_t* __restrict__ tstart, const uint32_t* __restrict__ ioff,
                                    Item* __restrict__ items, uint32_t cap, unsigned long long* __restrict__ imax) {
     const uint32_t gt = blockIdx.x * blockDim.x + threadIdx.x;
@@ -177,7 +188,7 @@ static __global__ void k_item_fill(uint32_t ncell, int R, const uint32_t* __rest
     int cc[3];
     cell_xyz(Re, c, cc);
     Run run[3];
-    const int nr = stencil_row(Re, cc, r, stage_per(Re, stage), run);
+    const int nr = row_in_ring(Re, r, ring) ? stencil_row(Re, cc, r, stage_per(Re, stage), run) : 0;
     uint32_t t0[3], nt[3], sg[3], segs = 0, im[3];
     for (int q = 0; q < nr; ++q) {
         t0[q] = tstart[run[q].lo];
