@@ -1,7 +1,8 @@
 """Builds libnanofiller_gb300.so (sm_103a) in-tree, in nanofiller_gb300/_build/.
 
 Each .cu translation unit is compiled in parallel with nvcc, then linked into one
-shared library with a static CUDA runtime. Host code is compiled with
+shared library with a static CUDA runtime; the command-line front end
+(_build/nanofiller, cli/nanofiller.cpp) is linked against it. Host code is compiled with
 -ffp-contract=off so the host half of the seeded stream matches the device bits
 on x86-64 and aarch64 alike.
 """
@@ -15,6 +16,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 SRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libnanofiller_gb300.so")
+CLI = os.path.join(OUT, "nanofiller")
 SOURCES = ["nf_generate.cu", "nf_contacts.cu", "nf_solve.cu", "nf_api.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
@@ -36,10 +38,11 @@ def _flags(verbose_ptxas=False):
 
 
 def _stale():
-    if not os.path.exists(LIB):
+    if not os.path.exists(LIB) or not os.path.exists(CLI):
         return True
-    t = os.path.getmtime(LIB)
+    t = min(os.path.getmtime(LIB), os.path.getmtime(CLI))
     deps = [os.path.join(SRC, f) for f in os.listdir(SRC)]
+    deps.append(os.path.join(HERE, "cli", "nanofiller.cpp"))
     deps.append(os.path.join(HERE, "..", "include", "nanofiller_gb300.h"))
     deps.append(os.path.abspath(__file__))
     return any(os.path.getmtime(d) > t for d in deps)
@@ -72,6 +75,15 @@ def build(force=False, verbose_ptxas=False, jobs=None):
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stderr}")
     os.replace(tmp, LIB)
+    # Command-line front end, linked against the library next to it.
+    cxx = shutil.which("g++") or "g++"
+    cmd = [cxx, "-O2", "-std=c++17", "-I", os.path.join(HERE, "..", "include"),
+           os.path.join(HERE, "cli", "nanofiller.cpp"), "-o", CLI + ".tmp", "-L", OUT,
+           "-l:libnanofiller_gb300.so", "-Wl,-rpath,$ORIGIN"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"command-line front end failed to build:\n{r.stderr}")
+    os.replace(CLI + ".tmp", CLI)
     return LIB
 
 

@@ -1,0 +1,174 @@
+// nanofiller.cpp -- command-line front end over the C ABI, with the verb syntax
+// of the reference's NanoFiller binary (src/NanoFiller.cpp:37-162):
+//
+//   nanofiller <parameter file> [generate] [verb ...]
+//
+// `generate` draws the rods (nf_generate; output.bin is written when WRT_BIN is
+// set); without it the rods are read from output.bin in the working directory.
+// Verbs on this path:
+//   write_vtk             output.vtk (write_CNTvtk layout)
+//   expand <dir>          field axis of the electrodes (1 = x, 2 = y, 4 = z); the
+//                         electrodes are the two faces of that axis
+//   stat_conduct <dir>    contacts with screening and electrode roles, written as
+//                         internal.srt.coo, sink.elec.coo, source.elec.coo, then
+//                         the network solve (G_eff printed)
+// The reference's other verbs (plot, reduce, stat_nematic, stat_phitheta,
+// stat_mutangle, stat_exclsurf, stat_contacts, stat_vdw, write_ort, write_lmp,
+// stat_conduct ... internal) are not part of this path: they are reported and
+// the program exits with status 2 before any work. Every error exits non-zero
+// with the library's message.
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "nanofiller_gb300.h"
+
+namespace {
+
+const double kPi = 3.14159265358979323846;
+
+int fail(nf_handle* h, nf_status s, const char* what) {
+    char msg[512] = "";
+    if (h) nf_last_error(h, msg, sizeof msg);
+    std::fprintf(stderr, "nanofiller: %s: %s%s%s\n", what, nf_status_string(s), msg[0] ? ": " : "", msg);
+    return 1;
+}
+
+struct Verb {
+    std::string name;
+    int dir;
+};
+
+bool not_on_path(const std::string& v) {
+    static const char* other[] = {"plot", "reduce", "stat_nematic", "stat_phitheta", "stat_mutangle",
+                                  "stat_exclsurf", "stat_contacts", "stat_vdw", "write_ort", "write_lmp"};
+    for (const char* o : other)
+        if (v == o) return true;
+    return false;
+}
+
+int parse_dir(const char* s, int* dir) {
+    char* end = nullptr;
+    long d = std::strtol(s, &end, 10);
+    if (!end || *end || (d != 1 && d != 2 && d != 4)) return 0;
+    *dir = (int)d;
+    return 1;
+}
+
+}  // namespace
+
+int main(int argc, char** argv) {
+    if (argc < 3) {
+        std::fprintf(stderr,
+                     "usage: nanofiller <parameter file> [generate] [write_vtk] [expand <dir>] "
+                     "[stat_conduct <dir>]\n");
+        return 1;
+    }
+    // Verbs first, so that a command line this path cannot run does no work.
+    bool generate = std::strcmp(argv[2], "generate") == 0;
+    std::vector<Verb> verbs;
+    int field_dir = 0;
+    for (int a = generate ? 3 : 2; a < argc; ++a) {
+        std::string v = argv[a];
+        if (v == "write_vtk") {
+            verbs.push_back({v, 0});
+        } else if (v == "expand" || v == "stat_conduct") {
+            int d = 0;
+            if (a + 1 >= argc || !parse_dir(argv[a + 1], &d)) {
+                std::fprintf(stderr, "nanofiller: %s needs a direction 1, 2 or 4\n", v.c_str());
+                return 1;
+            }
+            ++a;
+            if (v == "stat_conduct" && a + 1 < argc && std::strcmp(argv[a + 1], "internal") == 0) {
+                std::fprintf(stderr, "nanofiller: stat_conduct ... internal (intra-rod resistor network) "
+                                     "is not part of this path\n");
+                return 2;
+            }
+            if (field_dir && field_dir != d) {
+                std::fprintf(stderr, "nanofiller: conflicting directions %d and %d\n", field_dir, d);
+                return 1;
+            }
+            field_dir = d;
+            verbs.push_back({v, d});
+        } else if (not_on_path(v)) {
+            std::fprintf(stderr, "nanofiller: verb '%s' is not part of this path\n", v.c_str());
+            return 2;
+        } else {
+            std::fprintf(stderr, "nanofiller: unknown verb '%s'\n", v.c_str());
+            return 1;
+        }
+    }
+
+    nf_params p;
+    nf_params_default(&p);
+    int unknown = 0;
+    nf_status s = nf_params_from_file(argv[1], &p, &unknown);
+    if (s != NF_OK) return fail(nullptr, s, argv[1]);
+    if (unknown) std::fprintf(stderr, "nanofiller: %d unknown key(s) in %s ignored\n", unknown, argv[1]);
+    if (field_dir) p.field_dir = field_dir;
+
+    nf_handle* h = nullptr;
+    s = nf_create(&p, &h);
+    if (s != NF_OK) return fail(nullptr, s, "nf_create");
+    int rc = 0;
+    if (generate) {
+        nf_gen_stats g;
+        s = nf_generate(h, &g);
+        if (s != NF_OK) { rc = fail(h, s, "generate"); goto done; }
+        std::printf("%llu inclusions generated from %llu candidates in %.3f ms\n",
+                    (unsigned long long)g.accepted, (unsigned long long)g.candidates_drawn, g.ms);
+        if (p.wrt_bin) {
+            s = nf_write_state_bin(h, "output.bin");
+            if (s != NF_OK) { rc = fail(h, s, "output.bin"); goto done; }
+        }
+    } else {
+        s = nf_read_state_bin(h, "output.bin");
+        if (s != NF_OK) { rc = fail(h, s, "output.bin"); goto done; }
+    }
+    {
+        // Volume fraction of the rods as cylinders without caps (get_VolFrac,
+        // src/simPrms.cpp:1026-1030).
+        nf_rods r;
+        std::memset(&r, 0, sizeof r);
+        s = nf_get_rods(h, &r);
+        if (s != NF_OK && s != NF_ERR_CAPACITY) { rc = fail(h, s, "rods"); goto done; }
+        std::vector<float> l(r.count), a(r.count);
+        r.capacity = r.count;
+        r.l = l.data();
+        r.a = a.data();
+        s = nf_get_rods(h, &r);
+        if (s != NF_OK) { rc = fail(h, s, "rods"); goto done; }
+        double vol = 0;
+        for (size_t i = 0; i < r.count; ++i) vol += kPi * (double)a[i] * a[i] * l[i];
+        std::printf("Volume fraction of %5.2f percent is achieved\n",
+                    100.0 * vol / ((double)p.box[0] * p.box[1] * p.box[2]));
+    }
+    for (const Verb& v : verbs) {
+        if (v.name == "write_vtk") {
+            s = nf_write_vtk(h, "output.vtk");
+            if (s != NF_OK) { rc = fail(h, s, "write_vtk"); goto done; }
+        } else if (v.name == "stat_conduct") {
+            nf_contact_stats c;
+            s = nf_contacts(h, &c);
+            if (s != NF_OK) { rc = fail(h, s, "contacts"); goto done; }
+            s = nf_write_coo(h, ".");
+            if (s != NF_OK) { rc = fail(h, s, "coo files"); goto done; }
+            std::printf("%llu contacts (%llu screened), %llu to the source, %llu to the sink\n",
+                        (unsigned long long)c.contacts, (unsigned long long)c.screened,
+                        (unsigned long long)c.n_source, (unsigned long long)c.n_sink);
+            nf_solve_stats so;
+            s = nf_solve(h, &so);
+            if (s != NF_OK && s != NF_ERR_NOT_CONVERGED) { rc = fail(h, s, "solve"); goto done; }
+            std::printf("G_eff = %.9e S (%lld of %lld rods in the network, residual %.3e)\n", so.G_eff,
+                        (long long)so.n_active, (long long)so.n_nodes, so.residual);
+            if (s == NF_ERR_NOT_CONVERGED) { rc = fail(h, s, "solve"); goto done; }
+        }
+        // expand only sets the field axis, applied before nf_create.
+    }
+done:
+    nf_destroy(h);
+    return rc;
+}
