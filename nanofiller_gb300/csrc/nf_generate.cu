@@ -536,23 +536,32 @@ __global__ void __launch_bounds__(256) k_conf_exact(const Real* __restrict__ rea
     warp_add_u64(&ctr[C_OVERFLOW], ovf);
 }
 
-// One pass of the in-order resolution.
+// In-order resolution: a surviving candidate is rejected once one of its
+// earlier conflicts is accepted and accepted once all of them are rejected.
+// States only move from ST_ALIVE to a final state, so the passes need no grid
+// barrier: a thread re-reads its conflicts up to `passes` times (with a short
+// pause for the other threads to decide), and a candidate still open after
+// that is counted in C_UNDECIDED (a count that is too high only costs the
+// host another launch).
 __global__ void k_resolve(const uint32_t* __restrict__ ntot, uint8_t* state, const uint32_t* __restrict__ ccnt,
-                          const uint32_t* __restrict__ clist, unsigned long long* __restrict__ ctr) {
+                          const uint32_t* __restrict__ clist, unsigned long long* __restrict__ ctr, int passes) {
     uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= *ntot) return;
     volatile uint8_t* vs = state;
     if (vs[c] != ST_ALIVE) return;
-    uint32_t n = min(ccnt[c], (uint32_t)kConflictCap);
-    bool any_acc = false, all_rej = true;
-    for (uint32_t e = 0; e < n; ++e) {
-        uint8_t s = vs[clist[(size_t)c * kConflictCap + e]];
-        if (s == ST_ACC) { any_acc = true; break; }
-        if (s == ST_ALIVE) all_rej = false;
+    const uint32_t n = min(ccnt[c], (uint32_t)kConflictCap);
+    for (int p = 0; p < passes; ++p) {
+        bool any_acc = false, all_rej = true;
+        for (uint32_t e = 0; e < n; ++e) {
+            uint8_t s = vs[clist[(size_t)c * kConflictCap + e]];
+            if (s == ST_ACC) { any_acc = true; break; }
+            if (s == ST_ALIVE) all_rej = false;
+        }
+        if (any_acc) { vs[c] = ST_REJ_CONF; return; }
+        if (all_rej) { vs[c] = ST_ACC; return; }
+        __nanosleep(200);
     }
-    if (any_acc) vs[c] = ST_REJ_CONF;
-    else if (all_rej) vs[c] = ST_ACC;
-    else atomicAdd(&ctr[C_UNDECIDED], 1ull);
+    atomicAdd(&ctr[C_UNDECIDED], 1ull);
 }
 
 __global__ void k_accflag(const uint32_t* __restrict__ ntot, uint32_t cap, const uint8_t* __restrict__ state,
@@ -1200,12 +1209,10 @@ nf_status Engine::generate() {
         uint64_t* hout = reinterpret_cast<uint64_t*>(hv + 7);
         uint32_t* hmeta = reinterpret_cast<uint32_t*>(hout + 2 * R);
         for (;;) {
-            for (int q = 0; q < 3; ++q)
-                NF_LAUNCH(k_resolve, gs, 256, 0, st)(ntot, state.p, ccnt.p, clist.p, ctr.p);
             NF_CK(cudaMemsetAsync(ctr.p + C_UNDECIDED, 0, sizeof(unsigned long long), st));
-            NF_LAUNCH(k_resolve, gs, 256, 0, st)(ntot, state.p, ccnt.p, clist.p, ctr.p);
+            NF_LAUNCH(k_resolve, gs, 256, 0, st)(ntot, state.p, ccnt.p, clist.p, ctr.p, 16);
             NF_CK(cudaGetLastError());
-            passes += 4;
+            passes += 16;
             NF_LAUNCH(k_accflag, grid_for(slots + 1, 256), 256, 0, st)(ntot, (uint32_t)(slots + 1), state.p, accf.p);
             NF_CK(cudaGetLastError());
             s = scan_u32(accf.p, accpos.p, slots + 1);
