@@ -721,8 +721,10 @@ nf_status Engine::build_items(const uint32_t* pstart, const uint32_t* tstart, in
     NF_CK(cudaGetLastError());
     nf_status s = scan_u32(icnt.p, ioff.p, n27 + 1);
     if (s != NF_OK) return s;
-    NF_LAUNCH(k_item_fill, grid_for(n27 * 32, 256), 256, 0, st)(ncell, R, celloff.p, dreal.p, stage, ring, pstart, tstart, ioff.p,
-                                                           items.p, (uint32_t)items.cap, ctr.p + C_ITEMS);
+    // pairs per warp: 1 while pairs are few enough to give each its own warp
+    const size_t per = n27 <= ((size_t)1 << 20) ? 1 : 32;
+    NF_LAUNCH(k_item_fill, grid_for((n27 + per - 1) / per * 32, 256), 256, 0, st)(ncell, R, celloff.p, dreal.p, stage, ring, pstart, tstart, ioff.p,
+                                                           items.p, (uint32_t)items.cap, ctr.p + C_ITEMS, (uint32_t)per);
     NF_CK(cudaGetLastError());
     return NF_OK;
 }

@@ -169,44 +169,56 @@ static __global__ void k_item_count(uint32_t ncell, int R, const uint32_t* __res
     icnt[t] = n;
 }
 
-// One warp per (cell, row): lane i writes items i, i + 32, ... of the pair
-// (item index = probe chunk * segments of the row + segment).
+// One warp per `per` consecutive (cell, row) pairs (per = 1, 2, ..., 32): the
+// warp takes the pairs that have items one after the other, and lane i writes
+// items i, i + 32, ... of each (item index = probe chunk * segments of the row
+// + segment). With many small realisations in one launch most pairs are empty
+// and per = 32 lets them cost one load and a ballot; with few, busy pairs
+// per = 1 keeps one warp per pair.
 static __global__ void k_item_fill(uint32_t ncell, int R, const uint32_t* __restrict__ celloff,
                                    const Real* __restrict__ reals, int stage, int ring, const uint32_t* __restrict__ pstart,
                                    const uint32_t* __restrict__ tstart, const uint32_t* __restrict__ ioff,
-                                   Item* __restrict__ items, uint32_t cap, unsigned long long* __restrict__ imax) {
+                                   Item* __restrict__ items, uint32_t cap, unsigned long long* __restrict__ imax,
+                                   uint32_t per) {
     const uint32_t gt = blockIdx.x * blockDim.x + threadIdx.x;
     if (gt == 0) atomicMax(imax, (unsigned long long)ioff[ncell * (uint32_t)kRows]);
-    const uint32_t t = gt >> 5, lane = gt & 31u;
-    if (t >= ncell * (uint32_t)kRows) return;
-    const uint32_t k0 = ioff[t], kend = ioff[t + 1];
-    if (k0 == kend) return;
-    const uint32_t c = t / kRows;
-    const int r = (int)(t % kRows);
-    const int ri = find_real(celloff, R, c);
-    const Real& Re = reals[ri];
-    int cc[3];
-    cell_xyz(Re, c, cc);
-    Run run[3];
-    const int nr = row_in_ring(Re, r, ring) ? stencil_row(Re, cc, r, stage_per(Re, stage), run) : 0;
-    uint32_t t0[3], nt[3], sg[3], segs = 0, im[3];
-    for (int q = 0; q < nr; ++q) {
-        t0[q] = tstart[run[q].lo];
-        nt[q] = tstart[run[q].hi + 1] - t0[q];
-        sg[q] = (nt[q] + kSeg - 1) / kSeg;
-        segs += sg[q];
-        im[q] = (uint32_t)(run[q].img[0] + 1) | ((uint32_t)(run[q].img[1] + 1) << 2) |
-                ((uint32_t)(run[q].img[2] + 1) << 4);
-    }
-    const uint32_t p0 = pstart[c], np = pstart[c + 1] - p0;
-    for (uint32_t k = k0 + lane; k < kend && k < cap; k += 32) {
-        const uint32_t idx = k - k0;
-        const uint32_t a = (idx / segs) * kWC;
-        uint32_t s = idx % segs, q = 0;
-        while (s >= sg[q]) s -= sg[q++];
-        const uint32_t b = s * kSeg;
-        const uint32_t pa = min((uint32_t)kWC, np - a), tb = min((uint32_t)kSeg, nt[q] - b);
-        items[k] = Item{p0 + a, t0[q] + b, (uint32_t)ri, pa | (tb << 6) | (im[q] << 15)};
+    const uint32_t npair = ncell * (uint32_t)kRows;
+    const uint32_t lane = gt & 31u, first = (gt >> 5) * per, t_own = first + lane;
+    uint32_t k0_own = 0, kend_own = 0;
+    if (lane < per && t_own < npair) { k0_own = ioff[t_own]; kend_own = ioff[t_own + 1]; }
+    unsigned todo = __ballot_sync(0xffffffffu, kend_own > k0_own);
+    while (todo) {
+        const int src = __ffs(todo) - 1;
+        todo &= todo - 1u;
+        const uint32_t t = first + (uint32_t)src;
+        const uint32_t k0 = __shfl_sync(0xffffffffu, k0_own, src), kend = __shfl_sync(0xffffffffu, kend_own, src);
+        const uint32_t c = t / kRows;
+        const int r = (int)(t % kRows);
+        const int ri = find_real(celloff, R, c);
+        const Real& Re = reals[ri];
+        int cc[3];
+        cell_xyz(Re, c, cc);
+        Run run[3];
+        const int nr = row_in_ring(Re, r, ring) ? stencil_row(Re, cc, r, stage_per(Re, stage), run) : 0;
+        uint32_t t0[3], nt[3], sg[3], segs = 0, im[3];
+        for (int q = 0; q < nr; ++q) {
+            t0[q] = tstart[run[q].lo];
+            nt[q] = tstart[run[q].hi + 1] - t0[q];
+            sg[q] = (nt[q] + kSeg - 1) / kSeg;
+            segs += sg[q];
+            im[q] = (uint32_t)(run[q].img[0] + 1) | ((uint32_t)(run[q].img[1] + 1) << 2) |
+                    ((uint32_t)(run[q].img[2] + 1) << 4);
+        }
+        const uint32_t p0 = pstart[c], np = pstart[c + 1] - p0;
+        for (uint32_t k = k0 + lane; k < kend && k < cap; k += 32) {
+            const uint32_t idx = k - k0;
+            const uint32_t a = (idx / segs) * kWC;
+            uint32_t s = idx % segs, q = 0;
+            while (s >= sg[q]) s -= sg[q++];
+            const uint32_t b = s * kSeg;
+            const uint32_t pa = min((uint32_t)kWC, np - a), tb = min((uint32_t)kSeg, nt[q] - b);
+            items[k] = Item{p0 + a, t0[q] + b, (uint32_t)ri, pa | (tb << 6) | (im[q] << 15)};
+        }
     }
 }
 
