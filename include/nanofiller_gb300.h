@@ -108,6 +108,14 @@ typedef struct nf_params {
     int32_t round_candidates; /* ROUND_CANDIDATES: candidates per round; 0 -> adaptive */
     int32_t solve_max_iter; /* SOLVE_MAX_ITER (inner FP32 CG iterations)     */
     double solve_tol;       /* SOLVE_TOL: FP64 relative residual             */
+    /* --- tuning: speed only, results never depend on these --- */
+    int32_t stencil_radius; /* STENCIL_RADIUS: cells of edge >= reach / r and a
+                               (2r+1)^3 stencil; 0 -> 2 where the box allows  */
+    float round_overshoot;  /* ROUND_OVERSHOOT: candidates drawn per round over
+                               the expected need; 0 -> 2                      */
+    double two_phase_work;  /* TWO_PHASE_WORK: candidates x rods of a round
+                               above which the old-rod test runs in two
+                               phases; 0 -> 1e10, < 0 -> never                */
 } nf_params;
 
 /* Rods, structure of arrays, caller-owned host buffers. Any array may be NULL. */
@@ -290,6 +298,22 @@ nf_status nf_write_state_bin(nf_handle *h, const char *path);
 nf_status nf_read_state_bin(nf_handle *h, const char *path);
 /* internal.srt.coo, sink.elec.coo, source.elec.coo in dir (src/conductivity.cu:838-879). */
 nf_status nf_write_coo(nf_handle *h, const char *dir);
+
+/* ---- autotuner (no reference counterpart) -------------------------------- */
+/* Times full generations of the handle's realisation under candidate values
+ * of stencil_radius, round_overshoot and two_phase_work (one coordinate at a
+ * time, each trial run twice and timed on the second) and keeps the fastest
+ * in the handle's parameters. The accepted set does not depend on them: the
+ * handle ends holding the rods nf_generate gives. out may be NULL. */
+typedef struct nf_tune_result {
+    int32_t stencil_radius;
+    float round_overshoot;
+    double two_phase_work;
+    double ms_first;        /* generation time with the settings on entry   */
+    double ms_best;         /* with the settings chosen                     */
+    int32_t trials;
+} nf_tune_result;
+nf_status nf_autotune(nf_handle *h, nf_tune_result *out);
 
 /* ---- diagnostics (no reference counterpart; the reference prints timers,
  *      src/cudaMain.cu:147,157) ------------------------------------------ */

@@ -15,7 +15,7 @@ import numpy as np
 from . import configs  # noqa: F401
 from ._abi import (LIB_PATH, SNK_ELEC, SRC_ELEC, STATUS, NfBatchResult, NfBatchStats,  # noqa: F401
                    NfContactList, NfContactStats, NfGenStats, NfParams, NfRods, NfSolveStats,
-                   NfStateHeader, load)
+                   NfStateHeader, NfTuneResult, load)
 
 __all__ = ["Simulation", "NanoFillerError", "make_params", "params_from_file", "batch_run",
            "target_count", "kernel_launches", "configs", "SRC_ELEC", "SNK_ELEC"]
@@ -223,6 +223,13 @@ class Simulation:
         ptrs = [out[i].ctypes.data_as(C.c_void_p) for i in range(10)]
         _check(self._L.nf_stream_candidates(self._h, k0, n, *ptrs), self._h, "nf_stream_candidates")
         return out.T.copy()
+
+    def autotune(self):
+        """Pick stencil_radius, round_overshoot and two_phase_work by timing
+        generations (nf_autotune); the handle keeps the fastest settings."""
+        r = NfTuneResult()
+        _check(self._L.nf_autotune(self._h, C.byref(r)), self._h, "nf_autotune")
+        return {k: getattr(r, k) for k, _ in r._fields_}
 
     def stream_noalloc(self, k0, n):
         """Same rows as stream(k0, n) through nf_stream_candidates_noalloc,

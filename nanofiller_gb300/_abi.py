@@ -37,6 +37,7 @@ class NfParams(C.Structure):
         ("cell_edge", C.c_float), ("G0", C.c_double), ("lambda_", C.c_double), ("d_c", C.c_double),
         ("ref_parallel_typo", C.c_int32), ("screening", C.c_int32),
         ("round_candidates", C.c_int32), ("solve_max_iter", C.c_int32), ("solve_tol", C.c_double),
+        ("stencil_radius", C.c_int32), ("round_overshoot", C.c_float), ("two_phase_work", C.c_double),
     ]
 
 
@@ -78,6 +79,11 @@ class NfSolveStats(C.Structure):
 class NfBatchResult(C.Structure):
     _fields_ = [("accepted", C.c_uint64), ("contacts", C.c_uint64), ("G_eff", C.c_double),
                 ("residual", C.c_double), ("percolating", C.c_int32), ("status", C.c_int32)]
+
+
+class NfTuneResult(C.Structure):
+    _fields_ = [("stencil_radius", C.c_int32), ("round_overshoot", C.c_float), ("two_phase_work", C.c_double),
+                ("ms_first", C.c_double), ("ms_best", C.c_double), ("trials", C.c_int32)]
 
 
 class NfBatchStats(C.Structure):
@@ -124,6 +130,7 @@ SIGNATURES = {
     "nf_write_coo": (_st, [_H, C.c_char_p]),
     "nf_kernel_launches": (C.c_uint64, []),
     "nf_set_kernel_timing": (_st, [_H, C.c_int]),
+    "nf_autotune": (_st, [_H, _P(NfTuneResult)]),
     "nf_kernel_time": (_st, [_H, C.c_char_p, _P(C.c_double), _P(C.c_uint64), _P(C.c_double),
                              _P(C.c_double)]),
     "nf_format_write_vtk": (_st, [C.c_char_p, C.c_size_t] + [C.c_void_p] * 9),

@@ -66,6 +66,9 @@ nf_status validate(const nf_params& p, std::string* why) {
         *why = "RAD_RANGE lo hi required for uniform radii"; return NF_ERR_PARAM;
     }
     if (!(p.lambda > 0) || !(p.G0 > 0)) { *why = "tunnelling law needs G0 > 0 and lambda > 0"; return NF_ERR_PARAM; }
+    if (p.stencil_radius < 0 || p.stencil_radius > 2 || !(p.round_overshoot >= 0) || p.two_phase_work != p.two_phase_work) {
+        *why = "STENCIL_RADIUS must be 0, 1 or 2 and ROUND_OVERSHOOT >= 0"; return NF_ERR_PARAM;
+    }
     double reach = nf::stage_reach(p);
     for (int d = 0; d < 3; ++d)
         if ((p.gen_periodic >> d & 1) && p.box[d] < reach) {
@@ -207,6 +210,9 @@ nf_status nf_params_from_file(const char* path, nf_params* p, int* n_unknown) {
         else if (key == "ROUND_CANDIDATES") in >> p->round_candidates;
         else if (key == "SOLVE_MAX_ITER") in >> p->solve_max_iter;
         else if (key == "SOLVE_TOL") in >> p->solve_tol;
+        else if (key == "STENCIL_RADIUS") in >> p->stencil_radius;
+        else if (key == "ROUND_OVERSHOOT") in >> p->round_overshoot;
+        else if (key == "TWO_PHASE_WORK") in >> p->two_phase_work;
         else ++unknown;  // the reference prints "UNRECOGNISED STRING FOUND" and continues
     }
     if (n_unknown) *n_unknown = unknown;
@@ -292,6 +298,65 @@ nf_status nf_generate(nf_handle* h, nf_gen_stats* stats) {
     nf_status s = h->E.generate();
     if (stats) *stats = h->E.gst;
     return s;
+}
+
+nf_status nf_autotune(nf_handle* h, nf_tune_result* out) {
+    if (!h) return NF_ERR_PARAM;
+    nf::Engine& E = h->E;
+    if (E.R != 1) return fail(h, NF_ERR_STATE, "the autotuner runs on a single-realisation handle");
+    int trials = 0;
+    // Generation time under q: one untimed run (buffers grow to the new sizes),
+    // then one timed run (CUDA events inside nf_generate).
+    auto time_of = [&](const nf_params& q, double* ms) -> nf_status {
+        E.prm[0] = q;
+        h->p = q;
+        nf_status s = E.generate();
+        if (s == NF_OK) s = E.generate();
+        if (s != NF_OK) return s;
+        *ms = E.gst.ms;
+        ++trials;
+        return NF_OK;
+    };
+    nf_params best = h->p;
+    double t_best = 0;
+    nf_status s = time_of(best, &t_best);
+    if (s != NF_OK) return s;
+    const double ms_first = t_best;
+    auto try_value = [&](auto set, auto value) -> nf_status {
+        nf_params q = best;
+        set(q, value);
+        double t = 0;
+        nf_status st = time_of(q, &t);
+        if (st != NF_OK) return st;
+        if (t < t_best) { t_best = t; best = q; }
+        return NF_OK;
+    };
+    for (int r : {1, 2}) {
+        s = try_value([](nf_params& q, int v) { q.stencil_radius = v; }, r);
+        if (s != NF_OK) return s;
+    }
+    for (float f : {1.5f, 2.0f, 3.0f}) {
+        s = try_value([](nf_params& q, float v) { q.round_overshoot = v; }, f);
+        if (s != NF_OK) return s;
+    }
+    for (double w : {1e9, 1e10, -1.0}) {
+        s = try_value([](nf_params& q, double v) { q.two_phase_work = v; }, w);
+        if (s != NF_OK) return s;
+    }
+    // Leave the handle generated under the chosen settings.
+    E.prm[0] = best;
+    h->p = best;
+    s = E.generate();
+    if (s != NF_OK) return s;
+    if (out) {
+        out->stencil_radius = best.stencil_radius;
+        out->round_overshoot = best.round_overshoot;
+        out->two_phase_work = best.two_phase_work;
+        out->ms_first = ms_first;
+        out->ms_best = t_best;
+        out->trials = trials;
+    }
+    return NF_OK;
 }
 
 nf_status nf_stream_candidates(nf_handle* h, uint64_t k0, uint64_t n, float* x, float* y, float* z, float* cx,

@@ -123,7 +123,7 @@ Real make_real(const nf_params& p, const float* dmesh, int mn[3], double reach) 
             if (((R.per_gen | R.per_con) >> d & 1) && R.n[d] < R.S) return false;
         return R.S <= kStencilMax;
     };
-    if (!grid(2)) grid(1);
+    if (p.stencil_radius == 1 || !grid(2)) grid(1);
     R.eps = p.tol;
     R.scf = p.sc_frac;
     R.sep = p.sep;
@@ -1044,10 +1044,12 @@ nf_status Engine::generate() {
                 // Acceptance per candidate: the density acceptance before the
                 // first round, then the last round's own rate (the rate only
                 // falls as the box fills, so the cumulative rate would
-                // overestimate it). Rounds draw twice the expected need: extra
-                // candidates cost sweep work, a short round costs a round.
+                // overestimate it). Rounds draw round_overshoot (2 by default)
+                // times the expected need: extra candidates cost sweep work, a
+                // short round costs a round.
                 const double acc_rate = rounds_r[r] > 0 ? last_rate[r] : p_dens[r];
-                double want = (tgt - count[r]) / std::max(acc_rate, 1e-6) * 2.0 + 256;
+                const double over = p.round_overshoot > 0 ? (double)p.round_overshoot : 2.0;
+                double want = (tgt - count[r]) / std::max(acc_rate, 1e-6) * over + 256;
                 // Survivors of the old-rod test per round: at most alive_max
                 // (bounds the conflict lists) and at most the target count
                 // (in-round conflict work grows with the square of the
@@ -1137,7 +1139,8 @@ nf_status Engine::generate() {
             outer_rows |= c_round[r] && hreal[r].S > 1;
             work += (double)c_round[r] * (double)count[r];
         }
-        const bool two_phase = outer_rows && work > 1e10;
+        const double two_work = prm[0].two_phase_work != 0 ? prm[0].two_phase_work : 1e10;
+        const bool two_phase = outer_rows && two_work >= 0 && work > two_work;
         NF_CK(cudaMemsetAsync(ctr.p + C_ITEMS, 0, sizeof(unsigned long long), st));
         s = build_items(cstart.p, rstart.p, 0, slots, total_rods(), two_phase ? 1 : 0);
         if (s != NF_OK) return s;

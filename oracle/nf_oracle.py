@@ -40,6 +40,7 @@ class NfParams(C.Structure):
         ("cell_edge", C.c_float), ("G0", C.c_double), ("lambda_", C.c_double), ("d_c", C.c_double),
         ("ref_parallel_typo", C.c_int32), ("screening", C.c_int32),
         ("round_candidates", C.c_int32), ("solve_max_iter", C.c_int32), ("solve_tol", C.c_double),
+        ("stencil_radius", C.c_int32), ("round_overshoot", C.c_float), ("two_phase_work", C.c_double),
     ]
 
 
@@ -53,7 +54,7 @@ DEFAULTS = dict(
     vmf_kappa=0.0, len_mode=0, len_sigma_ln=0.0, len_min=0.0, len_max=0.0, rad_mode=0,
     rad_min=0.0, rad_max=0.0, density_default=1.0, cell_edge=0.0, G0=1e-5, lambda_=0.00018,
     d_c=0.00034, ref_parallel_typo=0, screening=1, round_candidates=0, solve_max_iter=20000,
-    solve_tol=1e-10,
+    solve_tol=1e-10, stencil_radius=0, round_overshoot=0.0, two_phase_work=0.0,
 )
 
 

@@ -1,0 +1,67 @@
+"""Tuning settings change speed only: every value of stencil_radius,
+round_overshoot and two_phase_work gives the oracle's accepted set and contact
+list bit for bit (two_phase_work = 1 forces the two-phase old-rod test on every
+round, which the default threshold keeps for heavy rounds only), and
+nf_autotune leaves the handle holding the same rods."""
+import numpy as np
+import pytest
+
+from conftest import rods_struct
+
+pytestmark = pytest.mark.gpu
+
+ROD_F = ("x", "y", "z", "cx", "cy", "cz", "l", "a")
+
+SETTINGS = [dict(stencil_radius=1), dict(stencil_radius=2), dict(round_overshoot=1.5),
+            dict(round_overshoot=3.0), dict(two_phase_work=1.0), dict(two_phase_work=-1.0),
+            dict(stencil_radius=1, two_phase_work=1.0)]
+
+
+@pytest.fixture(scope="module")
+def medium_oracle(gpu, oracle):
+    cfg = dict(gpu.configs.MEDIUM)
+    mesh = gpu.configs.gaussian_mesh()
+    rods_o, idx_o, _ = oracle.generate(cfg, mesh=mesh, batch=16384)
+    return cfg, mesh, rods_o, idx_o, oracle.contacts(cfg, rods_o)
+
+
+def check(sim, rods_o, idx_o, co):
+    r = sim.rods()
+    assert np.array_equal(r["stream_index"], idx_o)
+    for f in ROD_F:
+        assert np.array_equal(r[f], rods_o[f]), f
+    ct = sim.contact_list()
+    assert np.array_equal(ct["I"], co["I"]) and np.array_equal(ct["J"], co["J"])
+    assert np.array_equal(ct["D"], co["D"]) and np.array_equal(ct["image"], co["image"])
+
+
+@pytest.mark.parametrize("setting", SETTINGS, ids=lambda d: ",".join(f"{k}={v}" for k, v in d.items()))
+def test_settings_do_not_change_results(gpu, medium_oracle, setting):
+    cfg, mesh, rods_o, idx_o, co = medium_oracle
+    with gpu.Simulation(dict(cfg, **setting), mesh=mesh) as sim:
+        g = sim.generate()
+        sim.contacts()
+        check(sim, rods_o, idx_o, co)
+        if setting.get("two_phase_work", 0) > 0:
+            assert g["work_items"] > 0
+
+
+def test_autotune_keeps_results(gpu, medium_oracle):
+    cfg, mesh, rods_o, idx_o, co = medium_oracle
+    with gpu.Simulation(cfg, mesh=mesh) as sim:
+        t = sim.autotune()
+        assert t["trials"] == 9
+        assert 0 < t["ms_best"] <= t["ms_first"] * 1.05
+        assert t["stencil_radius"] in (0, 1, 2) and t["round_overshoot"] in (0.0, 1.5, 2.0, 3.0)
+        sim.contacts()
+        check(sim, rods_o, idx_o, co)
+        # the chosen settings stay on the handle
+        g = sim.generate()
+        assert g["accepted"] == len(idx_o)
+
+
+def test_tuning_parameters_validated(gpu):
+    for bad in (dict(stencil_radius=3), dict(round_overshoot=-1.0)):
+        with pytest.raises(gpu.NanoFillerError) as e:
+            gpu.Simulation(dict(gpu.configs.SMALL, **bad))
+        assert e.value.status == 1
