@@ -116,6 +116,11 @@ typedef struct nf_params {
     double two_phase_work;  /* TWO_PHASE_WORK: candidates x rods of a round
                                above which the old-rod test runs in two
                                phases; 0 -> 1e10, < 0 -> never                */
+    /* --- intra-rod resistor network (stat_conduct ... internal) --- */
+    double rod_sigma;       /* ROD_CONDUCTIVITY (S/um): a rod segment between
+                               contact points conducts rod_sigma pi a / L with
+                               L = dt / a (tools/kirchhoff/kirchhoff.py:90-95,
+                               s0 = 6.7e7 S/m = 67 S/um, the default)       */
 } nf_params;
 
 /* Rods, structure of arrays, caller-owned host buffers. Any array may be NULL. */
@@ -172,7 +177,7 @@ typedef struct nf_solve_stats {
     double residual;            /* final ||b - K v|| / ||b|| in FP64       */
     int32_t outer_iters;        /* FP64 refinement steps                   */
     int32_t inner_iters;        /* FP32 CG iterations, all steps           */
-    int64_t n_nodes;            /* rods in the network                     */
+    int64_t n_nodes;            /* rods, or nodes of the internal network  */
     int64_t n_active;           /* unknowns: rods linked to both electrodes*/
     int32_t percolating;        /* a path joins source and sink            */
     double ms;
@@ -278,6 +283,38 @@ nf_status nf_get_contacts(nf_handle *h, nf_contact_list *out);
 nf_status nf_solve(nf_handle *h, nf_solve_stats *stats);
 /* Node voltages (rods; 0 for rods outside the source-sink network). */
 nf_status nf_get_voltages(nf_handle *h, double *v, size_t capacity);
+
+/* ---- intra-rod resistor network (stat_conduct dir internal:
+ *      src/conductivity.cu:228-416,639-836, src/adjacency_graph.cu:57-219,
+ *      tools/kirchhoff/kirchhoff.py:90-95) ------------------------------- */
+/* Builds the node network from the current contacts: every contact end is a
+ * node (rod, t); a node no more than one radius past its predecessor on the
+ * rod merges into it (mean t); consecutive nodes of a rod are joined by a rod
+ * segment of conductance rod_sigma pi a / L, L = dt / a. Until the next
+ * nf_contacts or nf_generate, nf_solve solves this network (nf_get_voltages
+ * then returns node voltages) and nf_adjoint reports NF_ERR_UNSUPPORTED. */
+typedef struct nf_internal_stats {
+    uint64_t contact_ends;      /* nodes before merging                       */
+    uint64_t nodes;             /* nodes after merging                        */
+    uint64_t segments;          /* rod segments                               */
+} nf_internal_stats;
+nf_status nf_internal_network(nf_handle *h, nf_internal_stats *stats);
+/* The node network: nodes ordered by (rod, t); segments (i, j = i + 1, L, G);
+ * every contact's two nodes in nf_get_contacts order (j keeps the electrode
+ * id of electrode contacts). Any array may be NULL; counts are always set. */
+typedef struct nf_internal_net {
+    size_t capacity;        /* in: entries every non-NULL array holds        */
+    size_t n_nodes, n_segments, n_edges;
+    uint32_t *node_rod;
+    double *node_t;
+    uint32_t *seg_i, *seg_j;
+    double *seg_l, *seg_g;
+    uint32_t *edge_i, *edge_j;
+} nf_internal_net;
+nf_status nf_get_internal_network(nf_handle *h, nf_internal_net *out);
+/* Nodes.tbl.dat, segment.LA.coo, internal.DS.coo, sink.DS.coo, source.DS.coo
+ * in dir (save_coo layouts, src/conductivity.cu:881-930). */
+nf_status nf_write_internal_coo(nf_handle *h, const char *dir);
 
 /* ---- adjoint (no reference counterpart) ------------------------------- */
 /* dG_eff/d(endpoints) as N x 6 (e0.xyz, e1.xyz with e0/1 = r -/+ l/2 c),

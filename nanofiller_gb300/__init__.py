@@ -15,7 +15,7 @@ import numpy as np
 from . import configs  # noqa: F401
 from ._abi import (LIB_PATH, SNK_ELEC, SRC_ELEC, STATUS, NfBatchResult, NfBatchStats,  # noqa: F401
                    NfContactList, NfContactStats, NfGenStats, NfParams, NfRods, NfSolveStats,
-                   NfStateHeader, NfTuneResult, load)
+                   NfInternalNet, NfInternalStats, NfStateHeader, NfTuneResult, load)
 
 __all__ = ["Simulation", "NanoFillerError", "make_params", "params_from_file", "batch_run",
            "target_count", "kernel_launches", "configs", "SRC_ELEC", "SNK_ELEC"]
@@ -94,6 +94,7 @@ class Simulation:
 
     def __init__(self, params, mesh=None, stream=None):
         self._L = load()
+        self._nv = None  # voltage count of the last solve
         self.params = make_params(params)
         h = C.c_void_p()
         _check(self._L.nf_create(C.byref(self.params), C.byref(h)), what="nf_create")
@@ -144,6 +145,7 @@ class Simulation:
             _check(st, self._h, "nf_solve")
         out = {k: getattr(s, k) for k, _ in s._fields_}
         out["status"] = st
+        self._nv = int(s.n_nodes) if st == 0 else None
         return out
 
     def adjoint(self):
@@ -213,7 +215,9 @@ class Simulation:
         return out
 
     def voltages(self):
-        n = self.n_rods()
+        """Voltages of the last solve: one per rod, or one per node of the
+        internal network when that was solved."""
+        n = self._nv if self._nv is not None else self.n_rods()
         v = np.zeros(n)
         _check(self._L.nf_get_voltages(self._h, v.ctypes.data_as(C.c_void_p), n), self._h, "nf_get_voltages")
         return v
@@ -223,6 +227,30 @@ class Simulation:
         ptrs = [out[i].ctypes.data_as(C.c_void_p) for i in range(10)]
         _check(self._L.nf_stream_candidates(self._h, k0, n, *ptrs), self._h, "nf_stream_candidates")
         return out.T.copy()
+
+    def internal_network(self):
+        """Build the intra-rod resistor network from the current contacts
+        (nf_internal_network); nf_solve then solves it."""
+        st = NfInternalStats()
+        _check(self._L.nf_internal_network(self._h, C.byref(st)), self._h, "nf_internal_network")
+        return {k: getattr(st, k) for k, _ in st._fields_}
+
+    def internal_net(self):
+        """Nodes, segments and contact-end nodes of the internal network."""
+        q = NfInternalNet()
+        _check(self._L.nf_get_internal_network(self._h, C.byref(q)), self._h, "nf_get_internal_network")
+        nn, ns, ne = q.n_nodes, q.n_segments, q.n_edges
+        out = dict(node_rod=np.zeros(nn, np.uint32), node_t=np.zeros(nn), seg_i=np.zeros(ns, np.uint32),
+                   seg_j=np.zeros(ns, np.uint32), seg_l=np.zeros(ns), seg_g=np.zeros(ns),
+                   edge_i=np.zeros(ne, np.uint32), edge_j=np.zeros(ne, np.uint32))
+        q.capacity = max(nn, ns, ne, 1)
+        for k, a in out.items():
+            setattr(q, k, a.ctypes.data_as(C.c_void_p))
+        _check(self._L.nf_get_internal_network(self._h, C.byref(q)), self._h, "nf_get_internal_network")
+        return out
+
+    def write_internal_coo(self, path):
+        _check(self._L.nf_write_internal_coo(self._h, str(path).encode()), self._h, "nf_write_internal_coo")
 
     def autotune(self):
         """Pick stencil_radius, round_overshoot and two_phase_work by timing

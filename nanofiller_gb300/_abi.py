@@ -38,6 +38,7 @@ class NfParams(C.Structure):
         ("ref_parallel_typo", C.c_int32), ("screening", C.c_int32),
         ("round_candidates", C.c_int32), ("solve_max_iter", C.c_int32), ("solve_tol", C.c_double),
         ("stencil_radius", C.c_int32), ("round_overshoot", C.c_float), ("two_phase_work", C.c_double),
+        ("rod_sigma", C.c_double),
     ]
 
 
@@ -79,6 +80,17 @@ class NfSolveStats(C.Structure):
 class NfBatchResult(C.Structure):
     _fields_ = [("accepted", C.c_uint64), ("contacts", C.c_uint64), ("G_eff", C.c_double),
                 ("residual", C.c_double), ("percolating", C.c_int32), ("status", C.c_int32)]
+
+
+class NfInternalStats(C.Structure):
+    _fields_ = [("contact_ends", C.c_uint64), ("nodes", C.c_uint64), ("segments", C.c_uint64)]
+
+
+class NfInternalNet(C.Structure):
+    _fields_ = [("capacity", C.c_size_t), ("n_nodes", C.c_size_t), ("n_segments", C.c_size_t),
+                ("n_edges", C.c_size_t), ("node_rod", C.c_void_p), ("node_t", C.c_void_p), ("seg_i", C.c_void_p),
+                ("seg_j", C.c_void_p), ("seg_l", C.c_void_p), ("seg_g", C.c_void_p), ("edge_i", C.c_void_p),
+                ("edge_j", C.c_void_p)]
 
 
 class NfTuneResult(C.Structure):
@@ -131,6 +143,9 @@ SIGNATURES = {
     "nf_kernel_launches": (C.c_uint64, []),
     "nf_set_kernel_timing": (_st, [_H, C.c_int]),
     "nf_autotune": (_st, [_H, _P(NfTuneResult)]),
+    "nf_internal_network": (_st, [_H, _P(NfInternalStats)]),
+    "nf_get_internal_network": (_st, [_H, _P(NfInternalNet)]),
+    "nf_write_internal_coo": (_st, [_H, C.c_char_p]),
     "nf_kernel_time": (_st, [_H, C.c_char_p, _P(C.c_double), _P(C.c_uint64), _P(C.c_double),
                              _P(C.c_double)]),
     "nf_format_write_vtk": (_st, [C.c_char_p, C.c_size_t] + [C.c_void_p] * 9),

@@ -12,11 +12,16 @@
 //   stat_conduct <dir>    contacts with screening and electrode roles, written as
 //                         internal.srt.coo, sink.elec.coo, source.elec.coo, then
 //                         the network solve (G_eff printed)
+//   stat_conduct <dir> internal
+//                         the same with the intra-rod resistor network: nodes at
+//                         the contact points, rod segments between them, written
+//                         as Nodes.tbl.dat, segment.LA.coo, internal.DS.coo,
+//                         sink.DS.coo, source.DS.coo, then the node-network solve
 // The reference's other verbs (plot, reduce, stat_nematic, stat_phitheta,
-// stat_mutangle, stat_exclsurf, stat_contacts, stat_vdw, write_ort, write_lmp,
-// stat_conduct ... internal) are not part of this path: they are reported and
-// the program exits with status 2 before any work. Every error exits non-zero
-// with the library's message.
+// stat_mutangle, stat_exclsurf, stat_contacts, stat_vdw, write_ort, write_lmp)
+// are not part of this path: they are reported and the program exits with
+// status 2 before any work. Every error exits non-zero with the library's
+// message.
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -40,6 +45,7 @@ int fail(nf_handle* h, nf_status s, const char* what) {
 struct Verb {
     std::string name;
     int dir;
+    bool internal;
 };
 
 bool not_on_path(const std::string& v) {
@@ -74,7 +80,7 @@ int main(int argc, char** argv) {
     for (int a = generate ? 3 : 2; a < argc; ++a) {
         std::string v = argv[a];
         if (v == "write_vtk") {
-            verbs.push_back({v, 0});
+            verbs.push_back({v, 0, false});
         } else if (v == "expand" || v == "stat_conduct") {
             int d = 0;
             if (a + 1 >= argc || !parse_dir(argv[a + 1], &d)) {
@@ -82,17 +88,17 @@ int main(int argc, char** argv) {
                 return 1;
             }
             ++a;
+            bool internal = false;
             if (v == "stat_conduct" && a + 1 < argc && std::strcmp(argv[a + 1], "internal") == 0) {
-                std::fprintf(stderr, "nanofiller: stat_conduct ... internal (intra-rod resistor network) "
-                                     "is not part of this path\n");
-                return 2;
+                internal = true;
+                ++a;
             }
             if (field_dir && field_dir != d) {
                 std::fprintf(stderr, "nanofiller: conflicting directions %d and %d\n", field_dir, d);
                 return 1;
             }
             field_dir = d;
-            verbs.push_back({v, d});
+            verbs.push_back({v, d, internal});
         } else if (not_on_path(v)) {
             std::fprintf(stderr, "nanofiller: verb '%s' is not part of this path\n", v.c_str());
             return 2;
@@ -154,15 +160,25 @@ int main(int argc, char** argv) {
             nf_contact_stats c;
             s = nf_contacts(h, &c);
             if (s != NF_OK) { rc = fail(h, s, "contacts"); goto done; }
-            s = nf_write_coo(h, ".");
-            if (s != NF_OK) { rc = fail(h, s, "coo files"); goto done; }
             std::printf("%llu contacts (%llu screened), %llu to the source, %llu to the sink\n",
                         (unsigned long long)c.contacts, (unsigned long long)c.screened,
                         (unsigned long long)c.n_source, (unsigned long long)c.n_sink);
+            if (v.internal) {
+                nf_internal_stats is;
+                s = nf_internal_network(h, &is);
+                if (s != NF_OK) { rc = fail(h, s, "internal network"); goto done; }
+                s = nf_write_internal_coo(h, ".");
+                if (s != NF_OK) { rc = fail(h, s, "internal network files"); goto done; }
+                std::printf("%llu nodes (%llu contact ends), %llu rod segments\n", (unsigned long long)is.nodes,
+                            (unsigned long long)is.contact_ends, (unsigned long long)is.segments);
+            } else {
+                s = nf_write_coo(h, ".");
+                if (s != NF_OK) { rc = fail(h, s, "coo files"); goto done; }
+            }
             nf_solve_stats so;
             s = nf_solve(h, &so);
             if (s != NF_OK && s != NF_ERR_NOT_CONVERGED) { rc = fail(h, s, "solve"); goto done; }
-            std::printf("G_eff = %.9e S (%lld of %lld rods in the network, residual %.3e)\n", so.G_eff,
+            std::printf("G_eff = %.9e S (%lld of %lld nodes in the network, residual %.3e)\n", so.G_eff,
                         (long long)so.n_active, (long long)so.n_nodes, so.residual);
             if (s == NF_ERR_NOT_CONVERGED) { rc = fail(h, s, "solve"); goto done; }
         }

@@ -69,6 +69,7 @@ nf_status validate(const nf_params& p, std::string* why) {
     if (p.stencil_radius < 0 || p.stencil_radius > 2 || !(p.round_overshoot >= 0) || p.two_phase_work != p.two_phase_work) {
         *why = "STENCIL_RADIUS must be 0, 1 or 2 and ROUND_OVERSHOOT >= 0"; return NF_ERR_PARAM;
     }
+    if (!(p.rod_sigma > 0)) { *why = "ROD_CONDUCTIVITY must be positive"; return NF_ERR_PARAM; }
     double reach = nf::stage_reach(p);
     for (int d = 0; d < 3; ++d)
         if ((p.gen_periodic >> d & 1) && p.box[d] < reach) {
@@ -132,6 +133,7 @@ nf_status nf_params_default(nf_params* p) {
     p->d_c = 0.34e-3;
     p->screening = 1;
     p->solve_max_iter = 20000;
+    p->rod_sigma = 67.0;  // 6.7e7 S/m (tools/kirchhoff/kirchhoff.py:68)
     p->solve_tol = 1e-10;
     return NF_OK;
 }
@@ -213,6 +215,7 @@ nf_status nf_params_from_file(const char* path, nf_params* p, int* n_unknown) {
         else if (key == "STENCIL_RADIUS") in >> p->stencil_radius;
         else if (key == "ROUND_OVERSHOOT") in >> p->round_overshoot;
         else if (key == "TWO_PHASE_WORK") in >> p->two_phase_work;
+        else if (key == "ROD_CONDUCTIVITY") in >> p->rod_sigma;
         else ++unknown;  // the reference prints "UNRECOGNISED STRING FOUND" and continues
     }
     if (n_unknown) *n_unknown = unknown;
@@ -466,7 +469,7 @@ nf_status nf_get_voltages(nf_handle* h, double* v, size_t capacity) {
     if (!h || !v) return NF_ERR_PARAM;
     nf::Engine& E = h->E;
     if (!E.solve_valid) return fail(h, NF_ERR_STATE, "no solution");
-    size_t n = E.count[0];
+    size_t n = E.int_valid ? E.int_count[0] : E.count[0];
     if (capacity < n) return NF_ERR_CAPACITY;
     cudaError_t e = cudaMemcpyAsync(v, E.volt.p, sizeof(double) * n, cudaMemcpyDeviceToHost, E.st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(E.st);
@@ -476,7 +479,115 @@ nf_status nf_get_voltages(nf_handle* h, double* v, size_t capacity) {
 
 nf_status nf_adjoint(nf_handle* h, float* dG_dend, size_t capacity, double* dG_dlambda, double* dG_dG0) {
     if (!h) return NF_ERR_PARAM;
+    if (h->E.int_valid)
+        return fail(h, NF_ERR_UNSUPPORTED, "the adjoint covers the contact network (run nf_contacts again)");
     return h->E.adjoint(0, dG_dend, capacity, dG_dlambda, dG_dG0);
+}
+
+nf_status nf_internal_network(nf_handle* h, nf_internal_stats* stats) {
+    if (!h) return NF_ERR_PARAM;
+    nf::Engine& E = h->E;
+    if (E.R != 1) return fail(h, NF_ERR_STATE, "the internal network is built on a single-realisation handle");
+    nf_status s = E.internal_network();
+    if (s != NF_OK) return s;
+    if (stats) {
+        stats->contact_ends = E.int_full;
+        stats->nodes = E.int_nodes;
+        stats->segments = E.int_segs;
+    }
+    return NF_OK;
+}
+
+nf_status nf_get_internal_network(nf_handle* h, nf_internal_net* out) {
+    if (!h || !out) return NF_ERR_PARAM;
+    nf::Engine& E = h->E;
+    if (!E.int_valid) return fail(h, NF_ERR_STATE, "no internal network: run nf_internal_network first");
+    const size_t nn = E.int_nodes, ns = E.int_segs, ne = E.ct_off[1];
+    out->n_nodes = nn;
+    out->n_segments = ns;
+    out->n_edges = ne;
+    const size_t need = std::max(nn, std::max(ns, ne));
+    const bool any = out->node_rod || out->node_t || out->seg_i || out->seg_j || out->seg_l || out->seg_g ||
+                     out->edge_i || out->edge_j;
+    if (!any) return NF_OK;
+    if (out->capacity < need) return NF_ERR_CAPACITY;
+    struct Copy { void* dst; const void* src; size_t bytes; };
+    const Copy cp[] = {{out->node_rod, E.inrod.p, 4 * nn}, {out->node_t, E.int_t.p, 8 * nn},
+                       {out->seg_i, E.ieI.p + ne, 4 * ns}, {out->seg_j, E.ieJ.p + ne, 4 * ns},
+                       {out->seg_l, E.iseg_l.p, 8 * ns}, {out->seg_g, E.ieG.p + ne, 8 * ns},
+                       {out->edge_i, E.ieI.p, 4 * ne}, {out->edge_j, E.ieJ.p, 4 * ne}};
+    cudaError_t e = cudaSuccess;
+    for (const Copy& c : cp)
+        if (c.dst && c.bytes && e == cudaSuccess) e = cudaMemcpyAsync(c.dst, c.src, c.bytes, cudaMemcpyDeviceToHost, E.st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(E.st);
+    if (e != cudaSuccess) return E.cuda_fail(e, "nf_get_internal_network");
+    return NF_OK;
+}
+
+nf_status nf_write_internal_coo(nf_handle* h, const char* dir) {
+    if (!h || !dir) return NF_ERR_PARAM;
+    nf::Engine& E = h->E;
+    if (!E.int_valid) return fail(h, NF_ERR_STATE, "no internal network: run nf_internal_network first");
+    nf_internal_net net{};
+    nf_status s = nf_get_internal_network(h, &net);
+    if (s != NF_OK) return s;
+    const size_t nn = net.n_nodes, ns = net.n_segments, ne = net.n_edges;
+    std::vector<uint32_t> nrod(nn), si(ns), sj(ns), ei(ne), ej(ne);
+    std::vector<double> nt(nn), sl(ns), sg(ns);
+    net.capacity = std::max(nn, std::max(ns, ne));
+    net.node_rod = nrod.data(); net.node_t = nt.data();
+    net.seg_i = si.data(); net.seg_j = sj.data(); net.seg_l = sl.data(); net.seg_g = sg.data();
+    net.edge_i = ei.data(); net.edge_j = ej.data();
+    if (net.capacity && (s = nf_get_internal_network(h, &net)) != NF_OK) return s;
+    std::vector<uint32_t> I(ne), J(ne);
+    std::vector<double> D(ne), S(ne);
+    nf_contact_list c{};
+    c.capacity = ne;
+    c.I = I.data(); c.J = J.data(); c.D = D.data(); c.S = S.data();
+    if ((s = nf_get_contacts(h, &c)) != NF_OK) return s;
+    std::vector<float> rad(E.count[0]);
+    nf_rods r{};
+    r.capacity = rad.size();
+    r.a = rad.data();
+    if ((s = nf_get_rods(h, &r)) != NF_OK) return s;
+    auto open = [&](const char* name, const char* header, std::ofstream& o) {
+        o.open(std::string(dir) + "/" + name);
+        if (o.is_open()) o << header;
+        return o.is_open();
+    };
+    std::ofstream o;
+    // Nodes.tbl.dat: node, rod, t (save_coo with one data column)
+    if (!open("Nodes.tbl.dat", "#\tI\tJ\tData\n", o)) return NF_ERR_IO;
+    for (size_t k = 0; k < nn; ++k) o << "\t" << k << "\t" << nrod[k] << "\t" << (float)nt[k] << "\n";
+    if (!o.good()) return NF_ERR_IO;
+    o.close();
+    // segment.LA.coo: i, j, L, a
+    if (!open("segment.LA.coo", "#\tI\tJ\tData1\tData2\n", o)) return NF_ERR_IO;
+    for (size_t k = 0; k < ns; ++k)
+        o << "\t" << si[k] << "\t" << sj[k] << "\t" << (float)sl[k] << "\t" << rad[nrod[si[k]]] << "\n";
+    if (!o.good()) return NF_ERR_IO;
+    o.close();
+    // internal / sink / source .DS.coo: node pairs with D and S, each block sorted
+    // by its node pair (electrode contacts written as (electrode id, node)).
+    const size_t nint = E.ct_int[0], nsnk = E.ct_snk[0];
+    const size_t b[4] = {0, nint, nint + nsnk, ne};
+    const char* names[3] = {"internal.DS.coo", "sink.DS.coo", "source.DS.coo"};
+    for (int f = 0; f < 3; ++f) {
+        std::vector<size_t> ord;
+        for (size_t q = b[f]; q < b[f + 1]; ++q) ord.push_back(q);
+        auto key = [&](size_t q) {
+            return f == 0 ? std::make_pair(ei[q], ej[q]) : std::make_pair(ej[q], ei[q]);
+        };
+        std::stable_sort(ord.begin(), ord.end(), [&](size_t x, size_t y) { return key(x) < key(y); });
+        if (!open(names[f], "#\tI\tJ\tData1\tData2\n", o)) return NF_ERR_IO;
+        for (size_t q : ord) {
+            const std::pair<uint32_t, uint32_t> k = key(q);
+            o << "\t" << k.first << "\t" << k.second << "\t" << (float)D[q] << "\t" << (float)S[q] << "\n";
+        }
+        if (!o.good()) return NF_ERR_IO;
+        o.close();
+    }
+    return NF_OK;
 }
 
 nf_status nf_batch_run(const nf_params* params, int n, nf_batch_result* out, nf_batch_stats* stats) {

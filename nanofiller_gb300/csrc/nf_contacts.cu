@@ -737,6 +737,7 @@ nf_status Engine::contacts() {
     cst.ms = ms;
     contacts_valid = true;
     solve_valid = false;
+    int_valid = false;
     return NF_OK;
 }
 

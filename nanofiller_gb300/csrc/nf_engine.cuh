@@ -153,8 +153,8 @@ struct Engine {
     // solve
     DBuf<double> vsrc, vsnk, volt;
     DBuf<uint32_t> parent, cflag, aidx, rowp, col, deg;
-    DBuf<float> val32, diag32;
-    DBuf<double> val64, diag64, bvec, xvec;
+    DBuf<float> val32, diag32, chain32;
+    DBuf<double> val64, diag64, bvec, xvec, cdiag, chain64;
     DBuf<float> cgbuf;
     DBuf<double> cgred;
     std::vector<nf_solve_stats> solve_st;
@@ -178,6 +178,19 @@ struct Engine {
     nf_status rebuild_cells();
     nf_status contacts();
     nf_status solve();
+    // Edges [0, mc) are general; edges [mc, m) are chain links joining node i
+    // to node i + 1 of the same rod (rod segments of the internal network).
+    nf_status solve_graph(uint32_t n, const std::vector<uint32_t>& off, const std::vector<uint32_t>& nodes, uint32_t mc,
+                          uint32_t m, const uint32_t* eI, const uint32_t* eJ, const double* eG);
+    // Intra-rod resistor network (nodes = contact points, merged closer than a
+    // radius; edges = contacts + rod segments); nf_solve uses it while int_valid.
+    nf_status internal_network();
+    bool int_valid = false;
+    uint64_t int_nodes = 0, int_edges = 0, int_segs = 0, int_full = 0;
+    std::vector<uint32_t> int_off, int_count;     // per realisation node ranges
+    DBuf<uint32_t> inrod, ieI, ieJ, ivals, ivals2, inew, igid, islot;
+    DBuf<double> int_t, ieG, iseg_l;
+    DBuf<unsigned long long> ikeys, ikeys2;
     nf_status adjoint(int r, float* dG_dend, size_t cap, double* dlam, double* dg0);
 
     // helpers

@@ -822,7 +822,7 @@ nf_status Engine::set_density(int r, int nx, int ny, int nz, const float* values
 void Engine::release() {
     DBuf<float4>* f4[] = {&pos, &dir, &spos, &sdir, &cpos, &cdir, &gpos, &gdir, &vpf, &vdf, &apos, &adir};
     for (auto* b : f4) b->release();
-    DBuf<uint32_t>* u32[] = {&icnt, &ioff, &celloff, &vcell, &vperm, &vstart, &vcur, &aperm, &astart,
+    DBuf<uint32_t>* u32[] = {&inrod, &ieI, &ieJ, &ivals, &ivals2, &inew, &igid, &islot, &icnt, &ioff, &celloff, &vcell, &vperm, &vstart, &vcur, &aperm, &astart,
                              &dcount, &rodoff, &rstart, &rcursor, &sid, &coff, &keep, &kpos, &ccount,
                              &cstart, &ccursor, &cperm, &creal, &ccell, &ccnt, &clist, &accf, &accpos,
                              &meta, &u32tmp, &rcnt, &rpos, &rcur, &cI, &cJ, &creal2, &eflag, &parent,
@@ -830,7 +830,9 @@ void Engine::release() {
     for (auto* b : u32) b->release();
     DBuf<uint64_t>* u64[] = {&sidx, &kbeg, &csidx};
     for (auto* b : u64) b->release();
-    DBuf<double>* d64[] = {&ct0, &ct1, &cD, &cG, &cS, &vsrc, &vsnk, &volt, &val64, &diag64, &bvec, &xvec, &cgred};
+    ikeys.release(); ikeys2.release();
+    DBuf<double>* d64[] = {&ct0, &ct1, &cD, &cG, &cS, &vsrc, &vsnk, &volt, &val64, &diag64, &bvec, &xvec, &cgred,
+                           &cdiag, &chain64, &int_t, &ieG, &iseg_l};
     for (auto* b : d64) b->release();
     if (hpin) cudaFreeHost(hpin);
     hpin = nullptr;
@@ -838,7 +840,7 @@ void Engine::release() {
     dreal.release(); mesh.release(); state.release(); ctr.release(); cubtmp.release(); items.release();
     vdbl.release();
     rec.release(); rec2.release(); recn.release(); cimg.release();
-    val32.release(); diag32.release(); cgbuf.release();
+    val32.release(); diag32.release(); chain32.release(); cgbuf.release();
 }
 
 nf_status Engine::rebuild_cells() {
@@ -975,6 +977,7 @@ nf_status Engine::inject(size_t n, const float4* hpos, const float4* hdir, const
     if (s != NF_OK) return s;
     contacts_valid = false;
     solve_valid = false;
+    int_valid = false;
     std::memset(&gst, 0, sizeof(gst));
     gst.accepted = n;
     gst.target = n;
@@ -1005,6 +1008,7 @@ nf_status Engine::generate() {
     if (s != NF_OK) return s;
     contacts_valid = false;
     solve_valid = false;
+    int_valid = false;
 
     // Round sizing statistics.
     std::vector<double> p_dens(R), alive_max(R);

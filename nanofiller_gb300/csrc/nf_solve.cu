@@ -11,9 +11,22 @@
 // only those are unknowns (the rest of the matrix is singular or irrelevant; the
 // reference floors empty rows at 1, kirchhoff.py:240).
 //
-// Solve: Jacobi-preconditioned CG in FP32 on the FP32 copy of the matrix, inside
+// Solve: preconditioned CG in FP32 on the FP32 copy of the matrix, inside
 // iterative refinement whose residual b - K x is accumulated in FP64 from the
 // FP64 matrix. One CTA per realisation, all reductions block-deterministic.
+// K is applied as a Laplacian, (K x)_i = e_i x_i + sum_j G_ij (x_i - x_j) with
+// e_i the electrode conductance, so that strong edges between nearly
+// equipotential nodes do not cancel against the diagonal.
+//
+// Preconditioner: block Jacobi over chains. In the intra-rod network the nodes
+// of a rod are consecutive and joined by rod segments that conduct 1e3-1e9 times
+// better than a tunnelling contact; each such chain is solved exactly as a
+// tridiagonal system (Thomas algorithm) whose diagonal also carries the
+// node's contact and electrode conductances. A rod-level network has chains of
+// one node, where this is plain Jacobi. The LDL^T pivots are formed as
+// w_k = g_k + gamma_k, gamma_k = c_k + g_{k-1} gamma_{k-1} / (g_{k-1} + gamma_{k-1})
+// (g: segment conductance to the next node, c: the node's other conductances),
+// a sum of positive terms with no cancellation.
 //
 // Adjoint: the Laplacian is self-adjoint, so dG_eff/dG_e = (V_i - V_j)^2 with
 // V_src = 1, V_snk = 0 (Thomson's principle); no second solve is needed.
@@ -117,15 +130,34 @@ __global__ void k_fill(uint32_t m, const uint32_t* __restrict__ I, const uint32_
     uint32_t a = aidx[i], b = aidx[j];
     uint32_t qa = rowp[a] + atomicAdd(&cur[a], 1u);
     uint32_t qb = rowp[b] + atomicAdd(&cur[b], 1u);
-    col[qa] = b; v64[qa] = -G[e];
-    col[qb] = a; v64[qb] = -G[e];
+    col[qa] = b; v64[qa] = G[e];
+    col[qb] = a; v64[qb] = G[e];
 }
 
-// Sort each row by column (deterministic SpMV order), diagonal, FP32 copies, rhs.
+// Chain links (edges [mc, m)): node j = i + 1 of the same rod, both active or
+// neither. gr[a] links row a to row a + 1, gl[a + 1] the same link seen from
+// below.
+__global__ void k_chain_links(uint32_t mc, uint32_t m, const uint32_t* __restrict__ I,
+                              const uint32_t* __restrict__ J, const double* __restrict__ G,
+                              const uint32_t* __restrict__ act, const uint32_t* __restrict__ aidx,
+                              double* __restrict__ gl, double* __restrict__ gr, uint32_t* err) {
+    uint32_t e = mc + blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= m) return;
+    const uint32_t i = I[e], j = J[e];
+    if (!act[i]) return;
+    const uint32_t a = aidx[i];
+    if (j != i + 1 || !act[j] || aidx[j] != a + 1) { atomicExch(err, 2u); return; }
+    gr[a] = G[e];
+    gl[a + 1] = G[e];
+}
+
+// Sort each row by column (deterministic SpMV order), FP32 copies, electrode
+// conductance e = s + t, the row's non-chain conductance c = e + sum_k G_k, rhs.
 __global__ void k_rows(uint32_t nslot, const uint32_t* __restrict__ act, const uint32_t* __restrict__ aidx,
                        const uint32_t* __restrict__ rowp, uint32_t* __restrict__ col, double* __restrict__ v64,
                        float* __restrict__ v32, const double* __restrict__ s, const double* __restrict__ t,
-                       double* __restrict__ d64, float* __restrict__ d32, double* __restrict__ b) {
+                       double* __restrict__ e64, float* __restrict__ e32, double* __restrict__ c64,
+                       double* __restrict__ b) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nslot || !act[i]) return;
     uint32_t a = aidx[i];
@@ -138,12 +170,42 @@ __global__ void k_rows(uint32_t nslot, const uint32_t* __restrict__ act, const u
         col[q] = c;
         v64[q] = v;
     }
-    double dg = 0.0;
-    for (uint32_t k = p0; k < p1; ++k) { dg -= v64[k]; v32[k] = (float)v64[k]; }
-    dg += s[i] + t[i];
-    d64[a] = dg;
-    d32[a] = (float)dg;
+    const double el = s[i] + t[i];
+    double c = el;
+    for (uint32_t k = p0; k < p1; ++k) { c += v64[k]; v32[k] = (float)v64[k]; }
+    e64[a] = el;
+    e32[a] = (float)el;
+    c64[a] = c;
     b[a] = s[i];
+}
+
+// Tridiagonal factors per chain, from its first row (gl == 0): FP32 copies of
+// the links, the forward multipliers mlo_k = g_{k-1} / w_{k-1} and 1 / w_k.
+// ch32 layout: [gl | gr | mlo | iw], na entries each.
+__global__ void k_chain_factor(uint32_t na, const double* __restrict__ gl, const double* __restrict__ gr,
+                               const double* __restrict__ c64, float* __restrict__ ch32) {
+    const uint32_t a = blockIdx.x * blockDim.x + threadIdx.x;
+    if (a >= na || gl[a] > 0.0) return;
+    float* gl32 = ch32;
+    float* gr32 = ch32 + na;
+    float* mlo = ch32 + 2ull * na;
+    float* iw = ch32 + 3ull * na;
+    double gam = c64[a];
+    uint32_t k = a;
+    gl32[a] = 0.f;
+    mlo[a] = 0.f;
+    while (true) {
+        const double g = gr[k];
+        const double w = g + gam;
+        iw[k] = w > 0.0 ? (float)(1.0 / w) : 0.f;
+        gr32[k] = (float)g;
+        if (!(g > 0.0) || k + 1 >= na) break;
+        const uint32_t k1 = k + 1;
+        gl32[k1] = (float)g;
+        mlo[k1] = (float)(g / w);
+        gam = c64[k1] + g * gam / (g + gam);
+        k = k1;
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -199,15 +261,50 @@ struct CgOut {
     int pad;
 };
 
-// One CTA per realisation. work: 4 float vectors (r, z, p, q) + e per active row.
+// z = M^-1 r on this thread's chains (rows i with gl[i] == 0 start one): a
+// forward sweep y_k = r_k + mlo_k y_{k-1}, then z_k = (y_k + g_k z_{k+1}) / w_k.
+// Accumulates r.z and r.r over the chain's rows.
+__device__ __forceinline__ void chain_precond(uint32_t n, const float* __restrict__ gl, const float* __restrict__ gr,
+                                              const float* __restrict__ mlo, const float* __restrict__ iw,
+                                              const float* __restrict__ r, float* __restrict__ z, uint32_t stride,
+                                              float* rz, float* rr) {
+    for (uint32_t i = threadIdx.x; i < n; i += stride) {
+        if (gl[i] != 0.f) continue;
+        uint32_t k = i;
+        float y = r[k];
+        z[k] = y;
+        while (gr[k] > 0.f && k + 1 < n) {
+            ++k;
+            y = r[k] + mlo[k] * y;
+            z[k] = y;
+        }
+        float zk = y * iw[k];
+        z[k] = zk;
+        *rz += r[k] * zk;
+        *rr += r[k] * r[k];
+        while (k > i) {
+            --k;
+            zk = (z[k] + gr[k] * zk) * iw[k];
+            z[k] = zk;
+            *rz += r[k] * zk;
+            *rr += r[k] * r[k];
+        }
+    }
+}
+
+// One CTA per realisation. work: 5 float vectors (r, z, p, q, e) per active row.
+// e64 / e32: electrode conductance per row; CSR values are the conductances
+// G > 0; ch64 = [gl | gr] and ch32 = [gl | gr | mlo | iw] hold the chain links
+// and factors (na rows each) when chains != 0.
 template <int NT>
 __global__ void __launch_bounds__(NT) k_cg(int R, const uint32_t* __restrict__ abase,
                                            const uint32_t* __restrict__ rowp, const uint32_t* __restrict__ col,
                                            const float* __restrict__ v32, const double* __restrict__ v64,
-                                           const float* __restrict__ d32, const double* __restrict__ d64,
-                                           const double* __restrict__ b, double* __restrict__ x,
-                                           double* __restrict__ r64, float* __restrict__ work, double tol,
-                                           int max_inner, CgOut* __restrict__ out) {
+                                           const float* __restrict__ e32, const double* __restrict__ e64,
+                                           const double* __restrict__ ch64, const float* __restrict__ ch32,
+                                           uint32_t na, int chains, const double* __restrict__ b,
+                                           double* __restrict__ x, double* __restrict__ r64, float* __restrict__ work,
+                                           double tol, int max_inner, CgOut* __restrict__ out) {
     __shared__ double sh[96];
     const int rr = blockIdx.x;
     if (rr >= R) return;
@@ -226,7 +323,12 @@ __global__ void __launch_bounds__(NT) k_cg(int R, const uint32_t* __restrict__ a
     const double* bb = b + base;
     double* xx = x + base;
     double* rv = r64 + base;
-    const float* dd = d32 + base;
+    const float* gl32 = ch32 + base;
+    const float* gr32 = ch32 + na + base;
+    const float* mlo = ch32 + 2ull * na + base;
+    const float* iw = ch32 + 3ull * na + base;
+    const double* gl64 = ch64 + base;
+    const double* gr64 = ch64 + na + base;
     double part = 0.0;
     for (uint32_t i = threadIdx.x; i < n; i += NT) {
         xx[i] = 0.0;
@@ -242,14 +344,23 @@ __global__ void __launch_bounds__(NT) k_cg(int R, const uint32_t* __restrict__ a
         const float sc = (float)(1.0 / rn);
         float prz = 0.f, prr = 0.f;
         for (uint32_t i = threadIdx.x; i < n; i += NT) {
-            float ri = (float)rv[i] * sc;
-            float zi = ri / dd[i];
-            w_r[i] = ri; w_z[i] = zi; w_p[i] = zi; w_e[i] = 0.f;
-            prz += ri * zi;
-            prr += ri * ri;
+            const float ri = (float)rv[i] * sc;
+            w_r[i] = ri;
+            w_e[i] = 0.f;
+            if (!chains) {
+                const float zi = ri * iw[i];
+                w_z[i] = zi;
+                prz += ri * zi;
+                prr += ri * ri;
+            }
+        }
+        if (chains) {
+            __syncthreads();  // r complete
+            chain_precond(n, gl32, gr32, mlo, iw, w_r, w_z, NT, &prz, &prr);
         }
         double rz, rr2;
         block_sum2<NT>(prz, prr, sh, &rz, &rr2);
+        for (uint32_t i = threadIdx.x; i < n; i += NT) w_p[i] = w_z[i];
         const double r0 = sqrt(rr2);
         int it = 0;
         for (; it < max_inner; ++it) {
@@ -257,10 +368,16 @@ __global__ void __launch_bounds__(NT) k_cg(int R, const uint32_t* __restrict__ a
             float ppq = 0.f;
             for (uint32_t i = threadIdx.x; i < n; i += NT) {
                 const uint32_t g = base + i;
-                float acc = ((float)d64[g]) * w_p[i];
-                for (uint32_t k = rowp[g], k1 = rowp[g + 1]; k < k1; ++k) acc += v32[k] * w_p[col[k] - base];
+                const float pi = w_p[i];
+                float acc = e32[g] * pi;
+                for (uint32_t k = rowp[g], k1 = rowp[g + 1]; k < k1; ++k) acc += v32[k] * (pi - w_p[col[k] - base]);
+                if (chains) {
+                    const float a = gl32[i], c = gr32[i];
+                    if (a != 0.f) acc += a * (pi - w_p[i - 1]);
+                    if (c != 0.f) acc += c * (pi - w_p[i + 1]);
+                }
                 w_q[i] = acc;
-                ppq += w_p[i] * acc;
+                ppq += pi * acc;
             }
             const double pq = block_sum<NT>((double)ppq, sh);
             if (!(pq > 0.0)) break;
@@ -268,12 +385,18 @@ __global__ void __launch_bounds__(NT) k_cg(int R, const uint32_t* __restrict__ a
             float qz = 0.f, qr = 0.f;
             for (uint32_t i = threadIdx.x; i < n; i += NT) {
                 w_e[i] += alpha * w_p[i];
-                float ri = w_r[i] - alpha * w_q[i];
+                const float ri = w_r[i] - alpha * w_q[i];
                 w_r[i] = ri;
-                float zi = ri / dd[i];
-                w_z[i] = zi;
-                qz += ri * zi;
-                qr += ri * ri;
+                if (!chains) {
+                    const float zi = ri * iw[i];
+                    w_z[i] = zi;
+                    qz += ri * zi;
+                    qr += ri * ri;
+                }
+            }
+            if (chains) {
+                __syncthreads();  // r complete
+                chain_precond(n, gl32, gr32, mlo, iw, w_r, w_z, NT, &qz, &qr);
             }
             double rz_new, rr_new;
             block_sum2<NT>(qz, qr, sh, &rz_new, &rr_new);
@@ -290,9 +413,15 @@ __global__ void __launch_bounds__(NT) k_cg(int R, const uint32_t* __restrict__ a
         part = 0.0;
         for (uint32_t i = threadIdx.x; i < n; i += NT) {
             const uint32_t g = base + i;
-            double acc = d64[g] * xx[i];
-            for (uint32_t k = rowp[g], k1 = rowp[g + 1]; k < k1; ++k) acc += v64[k] * xx[col[k] - base];
-            double ri = bb[i] - acc;
+            const double xi = xx[i];
+            double acc = e64[g] * xi;
+            for (uint32_t k = rowp[g], k1 = rowp[g + 1]; k < k1; ++k) acc += v64[k] * (xi - xx[col[k] - base]);
+            if (chains) {
+                const double a = gl64[i], c = gr64[i];
+                if (a != 0.0) acc += a * (xi - xx[i - 1]);
+                if (c != 0.0) acc += c * (xi - xx[i + 1]);
+            }
+            const double ri = bb[i] - acc;
             rv[i] = ri;
             part += ri * ri;
         }
@@ -329,12 +458,29 @@ __global__ void k_scatter_v(uint32_t nslot, const uint32_t* __restrict__ act, co
 
 nf_status Engine::solve() {
     if (!contacts_valid) { err = "no contacts: run nf_contacts first"; return NF_ERR_STATE; }
+    if (int_valid)
+        return solve_graph((uint32_t)int_nodes, int_off, int_count, (uint32_t)(int_edges - int_segs),
+                           (uint32_t)int_edges, ieI.p, ieJ.p, ieG.p);
+    std::vector<uint32_t> off(R + 1), nodes(R);
+    for (int r = 0; r < R; ++r) { off[r] = hreal[r].rod_off; nodes[r] = count[r]; }
+    off[R] = (uint32_t)rod_slots;
+    return solve_graph((uint32_t)rod_slots, off, nodes, (uint32_t)ct_off[R], (uint32_t)ct_off[R], cI.p, cJ.p, cG.p);
+}
+
+// Laplacian solve on a graph of n nodes (realisation r owns nodes
+// [off[r], off[r+1]), nodes[r] of them real) and m edges (I, J, G); J may be
+// NF_SRC_ELEC / NF_SNK_ELEC. Edges [mc, m) are chain links (J = I + 1, same
+// rod). Node voltages land in volt.
+nf_status Engine::solve_graph(uint32_t n, const std::vector<uint32_t>& off, const std::vector<uint32_t>& nodes,
+                              uint32_t mc, uint32_t m, const uint32_t* eI, const uint32_t* eJ, const double* eG) {
     cudaEvent_t e0, e1;
     NF_CK(cudaEventCreate(&e0));
     NF_CK(cudaEventCreate(&e1));
     NF_CK(cudaEventRecord(e0, st));
-    const uint32_t nslot = (uint32_t)rod_slots;
-    const uint32_t m = (uint32_t)ct_off[R];
+    const uint32_t nslot = n;
+    const uint32_t* cIp = eI;
+    const uint32_t* cJp = eJ;
+    const double* cGp = eG;
     NF_CK(parent.ensure(nslot + 1));
     NF_CK(cflag.ensure(nslot + 1));
     NF_CK(aidx.ensure(nslot + 1));
@@ -350,20 +496,18 @@ nf_status Engine::solve() {
     NF_CK(cudaMemsetAsync(act + nslot, 0, sizeof(uint32_t), st));
     NF_LAUNCH(k_uf_init, grid_for(nslot, 256), 256, 0, st)(nslot, parent.p, cflag.p);
     if (m) {
-        NF_LAUNCH(k_uf_union, grid_for(m, 256), 256, 0, st)(m, cI.p, cJ.p, parent.p, errw);
-        NF_LAUNCH(k_uf_flags, grid_for(m, 256), 256, 0, st)(m, cI.p, cJ.p, parent.p, cflag.p, errw);
-        NF_LAUNCH(k_elec_g, grid_for(m, 256), 256, 0, st)(m, cI.p, cJ.p, cG.p, vsrc.p, vsnk.p);
+        NF_LAUNCH(k_uf_union, grid_for(m, 256), 256, 0, st)(m, cIp, cJp, parent.p, errw);
+        NF_LAUNCH(k_uf_flags, grid_for(m, 256), 256, 0, st)(m, cIp, cJp, parent.p, cflag.p, errw);
+        NF_LAUNCH(k_elec_g, grid_for(m, 256), 256, 0, st)(m, cIp, cJp, cGp, vsrc.p, vsnk.p);
     }
     NF_LAUNCH(k_active, grid_for(nslot, 256), 256, 0, st)(nslot, parent.p, cflag.p, act, errw);
     NF_CK(cudaGetLastError());
     nf_status s = scan_u32(act, aidx.p, nslot + 1);
     if (s != NF_OK) return s;
-    // Active count per realisation: aidx at rod_off boundaries.
-    std::vector<uint32_t> hrodoff(R + 1), habase(R + 1);
-    for (int r = 0; r < R; ++r) hrodoff[r] = hreal[r].rod_off;
-    hrodoff[R] = nslot;
+    // Active count per realisation: aidx at the node-range boundaries.
+    std::vector<uint32_t> habase(R + 1);
     for (int r = 0; r <= R; ++r)
-        NF_CK(cudaMemcpyAsync(&habase[r], aidx.p + hrodoff[r], sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+        NF_CK(cudaMemcpyAsync(&habase[r], aidx.p + off[r], sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
     uint32_t herr = 0;
     NF_CK(cudaMemcpyAsync(&herr, errw, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
     NF_CK(cudaStreamSynchronize(st));
@@ -372,26 +516,39 @@ nf_status Engine::solve() {
     NF_CK(deg.ensure(na + 1));
     NF_CK(rowp.ensure(na + 1));
     NF_CK(cudaMemsetAsync(deg.p, 0, sizeof(uint32_t) * (na + 1), st));
-    if (m) NF_LAUNCH(k_deg, grid_for(m, 256), 256, 0, st)(m, cI.p, cJ.p, act, aidx.p, deg.p);
+    if (mc) NF_LAUNCH(k_deg, grid_for(mc, 256), 256, 0, st)(mc, cIp, cJp, act, aidx.p, deg.p);
+    NF_CK(cudaGetLastError());
+    const bool chains = m > mc;
+    NF_CK(chain64.ensure(2ull * na + 2));
+    NF_CK(chain32.ensure(4ull * na + 4));
+    NF_CK(cudaMemsetAsync(chain64.p, 0, sizeof(double) * (2ull * na + 2), st));
+    if (chains)
+        NF_LAUNCH(k_chain_links, grid_for(m - mc, 256), 256, 0, st)(mc, m, cIp, cJp, cGp, act, aidx.p, chain64.p,
+                                                                   chain64.p + na, errw);
     NF_CK(cudaGetLastError());
     s = scan_u32(deg.p, rowp.p, na + 1);
     if (s != NF_OK) return s;
     uint32_t nnz = 0;
     NF_CK(cudaMemcpyAsync(&nnz, rowp.p + na, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+    NF_CK(cudaMemcpyAsync(&herr, errw, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
     NF_CK(cudaStreamSynchronize(st));
+    if (herr) { err = "chain link between non-consecutive active nodes"; return NF_ERR_STATE; }
     NF_CK(col.ensure(nnz + 1));
     NF_CK(val64.ensure(nnz + 1));
     NF_CK(val32.ensure(nnz + 1));
     NF_CK(diag64.ensure(na + 1));
     NF_CK(diag32.ensure(na + 1));
+    NF_CK(cdiag.ensure(na + 1));
     NF_CK(bvec.ensure(na + 1));
     NF_CK(xvec.ensure(na + 1));
     NF_CK(cgred.ensure(na + 1));
     NF_CK(cgbuf.ensure(5 * (size_t)na + 5));
     NF_CK(cudaMemsetAsync(deg.p, 0, sizeof(uint32_t) * (na + 1), st));  // reuse as cursor
-    if (m) NF_LAUNCH(k_fill, grid_for(m, 256), 256, 0, st)(m, cI.p, cJ.p, cG.p, act, aidx.p, rowp.p, deg.p, col.p, val64.p);
+    if (mc) NF_LAUNCH(k_fill, grid_for(mc, 256), 256, 0, st)(mc, cIp, cJp, cGp, act, aidx.p, rowp.p, deg.p, col.p, val64.p);
     NF_LAUNCH(k_rows, grid_for(nslot, 256), 256, 0, st)(nslot, act, aidx.p, rowp.p, col.p, val64.p, val32.p, vsrc.p,
-                                                 vsnk.p, diag64.p, diag32.p, bvec.p);
+                                                 vsnk.p, diag64.p, diag32.p, cdiag.p, bvec.p);
+    if (na)
+        NF_LAUNCH(k_chain_factor, grid_for(na, 256), 256, 0, st)(na, chain64.p, chain64.p + na, cdiag.p, chain32.p);
     NF_CK(cudaGetLastError());
     DBuf<uint32_t>& dab = rcur;  // per-realisation active base (R+1)
     NF_CK(dab.ensure(R + 1));
@@ -401,8 +558,9 @@ nf_status Engine::solve() {
     const double tol = prm[0].solve_tol > 0 ? prm[0].solve_tol : 1e-10;
     const int max_inner = prm[0].solve_max_iter > 0 ? prm[0].solve_max_iter : 20000;
     tstart(KT_CG);
-    NF_LAUNCH(k_cg<512>, R, 512, 0, st)(R, dab.p, rowp.p, col.p, val32.p, val64.p, diag32.p, diag64.p, bvec.p, xvec.p,
-                                 cgred.p, cgbuf.p, tol, max_inner, outs.p);
+    NF_LAUNCH(k_cg<512>, R, 512, 0, st)(R, dab.p, rowp.p, col.p, val32.p, val64.p, diag32.p, diag64.p, chain64.p,
+                                 chain32.p, na, chains ? 1 : 0, bvec.p, xvec.p, cgred.p, cgbuf.p, tol, max_inner,
+                                 outs.p);
     NF_CK(cudaGetLastError());
     tstop(KT_CG);
     NF_LAUNCH(k_scatter_v, grid_for(nslot, 256), 256, 0, st)(nslot, act, aidx.p, xvec.p, parent.p, cflag.p, volt.p, errw);
@@ -429,7 +587,7 @@ nf_status Engine::solve() {
         S.residual = ho[r].res;
         S.outer_iters = ho[r].outer;
         S.inner_iters = ho[r].inner;
-        S.n_nodes = count[r];
+        S.n_nodes = nodes[r];
         S.n_active = habase[r + 1] - habase[r];
         S.percolating = S.n_active > 0;
         S.ms = ms;

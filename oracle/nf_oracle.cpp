@@ -887,6 +887,83 @@ int64_t nfo_contacts(const nf_params* p, const nfo_rod* rods, int64_t n, int nth
     return total;
 }
 
+// Intra-rod resistor network (the `stat_conduct ... internal` mode):
+// get_node_relations (src/conductivity.cu:639-754), get_internal_conduct and
+// get_segment_length (:756-836, src/get_contact_data.cu:235-297),
+// remove_redundant_nodes / reduce_node_tbl / recalculate_segments
+// (src/adjacency_graph.cu:57-219), segment conductance s0 pi a / L
+// (tools/kirchhoff/kirchhoff.py:90-95). Node positions t are the FP64 contact
+// parameters; nodes are ordered by (rod, float(t)), ties in contact order.
+static uint32_t ordered_bits(float f) {
+    uint32_t u;
+    std::memcpy(&u, &f, 4);
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+
+int64_t nfo_internal_network(const nf_params* p, const nfo_rod* rods, int64_t n_rods, int64_t m,
+                             const uint32_t* I, const uint32_t* J, const double* tI, const double* tJ,
+                             int64_t cap, uint32_t* node_rod, double* node_t, uint32_t* seg_i, uint32_t* seg_j,
+                             double* seg_l, double* seg_g, uint32_t* edge_i, uint32_t* edge_j, int64_t counts[3]) {
+    if (!p || (m && (!I || !J || !tI || !tJ))) return -1;
+    // slots 2e (rod I at tI) and 2e + 1 (rod J at tJ, internal contacts only)
+    std::vector<std::pair<uint64_t, int64_t>> key;
+    key.reserve(2 * m);
+    for (int64_t e = 0; e < m; ++e) {
+        key.push_back({((uint64_t)I[e] << 32) | ordered_bits((float)tI[e]), 2 * e});
+        if (J[e] < NF_SNK_ELEC) key.push_back({((uint64_t)J[e] << 32) | ordered_bits((float)tJ[e]), 2 * e + 1});
+    }
+    std::stable_sort(key.begin(), key.end(),
+                     [](const std::pair<uint64_t, int64_t>& a, const std::pair<uint64_t, int64_t>& b) {
+                         return a.first < b.first;
+                     });
+    const int64_t nfull = (int64_t)key.size();
+    auto rod_of = [&](int64_t k) { return (uint32_t)(key[k].first >> 32); };
+    auto t_of = [&](int64_t k) { int64_t sl = key[k].second; return (sl & 1) ? tJ[sl >> 1] : tI[sl >> 1]; };
+    // A node merges into its predecessor on the same rod when the segment
+    // between them is no longer than one radius (L = dt / a <= 1).
+    std::vector<int64_t> group(nfull);
+    int64_t ng = 0;
+    for (int64_t k = 0; k < nfull; ++k) {
+        bool merged = k > 0 && rod_of(k) == rod_of(k - 1) &&
+                      (t_of(k) - t_of(k - 1)) / (double)rods[rod_of(k)].a <= 1.0;
+        group[k] = merged ? ng - 1 : ng++;
+    }
+    if (ng > cap) return -2;
+    std::vector<double> tsum(ng, 0.0);
+    std::vector<int64_t> cnt(ng, 0);
+    for (int64_t k = 0; k < nfull; ++k) { tsum[group[k]] += t_of(k); ++cnt[group[k]]; }
+    for (int64_t k = 0; k < nfull; ++k) {
+        node_rod[group[k]] = rod_of(k);
+        node_t[group[k]] = tsum[group[k]] / (double)cnt[group[k]];
+    }
+    // contact ends -> nodes
+    std::vector<uint32_t> node_of_slot(2 * m, 0xFFFFFFFFu);
+    for (int64_t k = 0; k < nfull; ++k) node_of_slot[key[k].second] = (uint32_t)group[k];
+    for (int64_t e = 0; e < m; ++e) {
+        edge_i[e] = node_of_slot[2 * e];
+        edge_j[e] = J[e] < NF_SNK_ELEC ? node_of_slot[2 * e + 1] : J[e];
+    }
+    // segments between consecutive nodes of a rod
+    int64_t ns = 0;
+    const double PIv = 3.14159265358979323846;
+    for (int64_t g = 0; g + 1 < ng; ++g) {
+        if (node_rod[g] != node_rod[g + 1]) continue;
+        if (ns >= cap) return -2;
+        const double a = (double)rods[node_rod[g]].a;
+        const double L = (node_t[g + 1] - node_t[g]) / a;
+        seg_i[ns] = (uint32_t)g;
+        seg_j[ns] = (uint32_t)(g + 1);
+        seg_l[ns] = L;
+        seg_g[ns] = p->rod_sigma * PIv * a / L;
+        ++ns;
+    }
+    (void)n_rods;
+    counts[0] = ng;
+    counts[1] = ns;
+    counts[2] = nfull;
+    return ng;
+}
+
 double nfo_solve(int64_t n_rods, int64_t n_contacts, const uint32_t* I, const uint32_t* J,
                  const double* G, double tol, int max_iter, double* v, double info[4]) {
     std::vector<double> s(n_rods, 0.0), t(n_rods, 0.0);

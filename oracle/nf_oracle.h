@@ -61,6 +61,17 @@ double nfo_contact_area(const nfo_rod *A, const nfo_rod *B, const double shift[3
 int64_t nfo_first_hits(const nf_params *p, const nfo_rod *probes, const uint64_t *k, int64_t m,
                        const nfo_rod *rods, const uint64_t *sidx, int64_t n, int nthreads, int64_t *out);
 
+/* Intra-rod resistor network from a contact list (I, J, tI, tJ; electrode
+ * contacts carry J = NF_SRC_ELEC / NF_SNK_ELEC): merged nodes (rod, t),
+ * segments between consecutive nodes of a rod (L = dt / a, conductance
+ * rod_sigma pi a / L) and each contact's two node ids (edge_j keeps the
+ * electrode id). Arrays sized cap (edge arrays m). counts = {nodes, segments,
+ * nodes before merging}. Returns the node count, -2 when cap is too small. */
+int64_t nfo_internal_network(const nf_params *p, const nfo_rod *rods, int64_t n_rods, int64_t m,
+                             const uint32_t *I, const uint32_t *J, const double *tI, const double *tJ,
+                             int64_t cap, uint32_t *node_rod, double *node_t, uint32_t *seg_i, uint32_t *seg_j,
+                             double *seg_l, double *seg_g, uint32_t *edge_i, uint32_t *edge_j, int64_t counts[3]);
+
 /* Candidate stream k0..k0+n-1: out[10*i + f], f = x y z cx cy cz l a u rho. */
 int nfo_candidates(const nf_params *p, const float *mesh, int nx, int ny, int nz,
                    uint64_t k0, uint64_t n, float *out);

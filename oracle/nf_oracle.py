@@ -41,6 +41,7 @@ class NfParams(C.Structure):
         ("ref_parallel_typo", C.c_int32), ("screening", C.c_int32),
         ("round_candidates", C.c_int32), ("solve_max_iter", C.c_int32), ("solve_tol", C.c_double),
         ("stencil_radius", C.c_int32), ("round_overshoot", C.c_float), ("two_phase_work", C.c_double),
+        ("rod_sigma", C.c_double),
     ]
 
 
@@ -54,7 +55,7 @@ DEFAULTS = dict(
     vmf_kappa=0.0, len_mode=0, len_sigma_ln=0.0, len_min=0.0, len_max=0.0, rad_mode=0,
     rad_min=0.0, rad_max=0.0, density_default=1.0, cell_edge=0.0, G0=1e-5, lambda_=0.00018,
     d_c=0.00034, ref_parallel_typo=0, screening=1, round_candidates=0, solve_max_iter=20000,
-    solve_tol=1e-10, stencil_radius=0, round_overshoot=0.0, two_phase_work=0.0,
+    solve_tol=1e-10, stencil_radius=0, round_overshoot=0.0, two_phase_work=0.0, rod_sigma=67.0,
 )
 
 
@@ -110,6 +111,9 @@ def lib():
             L.nfo_first_hits.argtypes = [P(NfParams), C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p,
                                          C.c_int64, C.c_int, C.c_void_p]
             L.nfo_first_hits.restype = C.c_int64
+            L.nfo_internal_network.argtypes = [P(NfParams), C.c_void_p, C.c_int64, C.c_int64] + [C.c_void_p] * 4 + \
+                [C.c_int64] + [C.c_void_p] * 8 + [P(C.c_int64)]
+            L.nfo_internal_network.restype = C.c_int64
             L.nfo_solve.argtypes = [C.c_int64, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p,
                                     C.c_double, C.c_int, C.c_void_p, P(C.c_double)]
             L.nfo_solve.restype = C.c_double
@@ -175,6 +179,82 @@ def first_hits(params, probes, k, rods, stream_index, nthreads=0):
     if r < 0:
         raise RuntimeError("nfo_first_hits failed")
     return out
+
+
+def internal_network(params, rods, ct):
+    """Nodes, segments and node-level edges of the intra-rod resistor network."""
+    p = make_params(params)
+    rods = np.ascontiguousarray(rods, ROD_DTYPE)
+    m = len(ct["I"])
+    arr = [np.ascontiguousarray(ct["I"], np.uint32), np.ascontiguousarray(ct["J"], np.uint32),
+           np.ascontiguousarray(ct["tI"], np.float64), np.ascontiguousarray(ct["tJ"], np.float64)]
+    cap = 2 * m + 1
+    out = dict(node_rod=np.zeros(cap, np.uint32), node_t=np.zeros(cap), seg_i=np.zeros(cap, np.uint32),
+               seg_j=np.zeros(cap, np.uint32), seg_l=np.zeros(cap), seg_g=np.zeros(cap),
+               edge_i=np.zeros(m, np.uint32), edge_j=np.zeros(m, np.uint32))
+    cnt = (C.c_int64 * 3)()
+    r = lib().nfo_internal_network(C.byref(p), _ptr(rods), len(rods), m, *[_ptr(a) for a in arr], cap,
+                                   *[_ptr(out[k]) for k in ("node_rod", "node_t", "seg_i", "seg_j", "seg_l",
+                                                            "seg_g", "edge_i", "edge_j")], cnt)
+    if r < 0:
+        raise RuntimeError(f"nfo_internal_network failed ({r})")
+    n, ns = cnt[0], cnt[1]
+    for k in ("node_rod", "node_t"):
+        out[k] = out[k][:n]
+    for k in ("seg_i", "seg_j", "seg_l", "seg_g"):
+        out[k] = out[k][:ns]
+    out["nodes_before_merge"] = cnt[2]
+    return out
+
+
+def solve_internal(net, ct):
+    """G_eff of the node network (contact edges between nodes plus rod
+    segments) by a direct sparse LU factorisation in FP64, as the reference's
+    Kirchhoff tool solves its network (tools/kirchhoff/kirchhoff.py:211-269,
+    MKL DSS): Norton electrodes (source 1 V, sink 0 V), unknowns only in
+    components that touch both electrodes; outside them a component touching
+    only the source sits at 1 V, any other at 0 V.
+    Returns (G_eff, node voltages, info) like solve()."""
+    import scipy.sparse as sp
+    import scipy.sparse.csgraph as csg
+    import scipy.sparse.linalg as spl
+    n = len(net["node_rod"])
+    I = np.concatenate([net["edge_i"], net["seg_i"]]).astype(np.int64)
+    J = np.concatenate([net["edge_j"], net["seg_j"]]).astype(np.int64)
+    G = np.concatenate([np.asarray(ct["G"], np.float64), net["seg_g"]])
+    rr = J < SNK_ELEC
+    src, snk = J == SRC_ELEC, J == SNK_ELEC
+    s = np.zeros(n)
+    t = np.zeros(n)
+    np.add.at(s, I[src], G[src])
+    np.add.at(t, I[snk], G[snk])
+    A = sp.coo_matrix((np.ones(int(rr.sum())), (I[rr], J[rr])), shape=(n, n))
+    ncomp, lab = csg.connected_components(A, directed=False)
+    hs = np.zeros(ncomp, bool)
+    ht = np.zeros(ncomp, bool)
+    hs[lab[I[src]]] = True
+    ht[lab[I[snk]]] = True
+    act = (hs & ht)[lab]
+    v = (hs & ~ht)[lab].astype(np.float64)
+    na = int(act.sum())
+    info = dict(iters=0, n_active=na, percolating=na > 0, residual=0.0)
+    if na == 0:
+        return 0.0, v, info
+    idx = -np.ones(n, np.int64)
+    idx[act] = np.arange(na)
+    e = rr & act[I]
+    a, c, g = idx[I[e]], idx[J[e]], G[e]
+    diag = s[act] + t[act]
+    np.add.at(diag, a, g)
+    np.add.at(diag, c, g)
+    K = sp.coo_matrix((np.concatenate([diag, -g, -g]),
+                       (np.concatenate([np.arange(na), a, c]), np.concatenate([np.arange(na), c, a]))),
+                      shape=(na, na)).tocsc()
+    b = s[act]
+    x = spl.spsolve(K, b)
+    info["residual"] = float(np.linalg.norm(b - K @ x) / np.linalg.norm(b))
+    v[act] = x
+    return float(np.sum(b * (1.0 - x))), v, info
 
 
 def generate(params, mesh=None, nthreads=0, batch=4096, brute_force=False, cap=None):

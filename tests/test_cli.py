@@ -44,8 +44,6 @@ def test_cli_usage_and_verbs_without_gpu(lib, tmp_path):
     (tmp_path / "in.txt").write_text(SMALL_KEYS)
     r = run(exe, ["in.txt", "generate", "stat_nematic"], tmp_path)
     assert r.returncode == 2 and "not part of this path" in r.stderr
-    r = run(exe, ["in.txt", "generate", "stat_conduct", "4", "internal"], tmp_path)
-    assert r.returncode == 2 and "internal" in r.stderr
     r = run(exe, ["in.txt", "generate", "stat_conduct", "3"], tmp_path)
     assert r.returncode == 1 and "direction" in r.stderr
     r = run(exe, ["in.txt", "generate", "bogus"], tmp_path)
@@ -81,3 +79,28 @@ def test_cli_run_matches_library(gpu, tmp_path):
     r = run(exe, ["in.txt", "write_vtk"], a)
     assert r.returncode == 0, r.stderr
     assert (a / "output.vtk").read_bytes() == (b / "output.vtk").read_bytes()
+
+
+@pytest.mark.gpu
+def test_cli_internal_network_matches_library(gpu, tmp_path):
+    exe = cli(gpu)
+    a, b = tmp_path / "cli", tmp_path / "lib"
+    a.mkdir()
+    b.mkdir()
+    (a / "in.txt").write_text(SMALL_KEYS)
+    r = run(exe, ["in.txt", "generate", "stat_conduct", "4", "internal"], a)
+    assert r.returncode == 0, r.stderr
+    assert "rod segments" in r.stdout and "G_eff" in r.stdout
+    params, _ = gpu.params_from_file(a / "in.txt")
+    params["field_dir"] = 4
+    with gpu.Simulation(params) as sim:
+        sim.generate()
+        sim.contacts()
+        st = sim.internal_network()
+        sim.write_internal_coo(b)
+        sol = sim.solve(check=False)
+    assert f"{st['nodes']} nodes ({st['contact_ends']} contact ends), {st['segments']} rod segments" in r.stdout
+    assert f"G_eff = {sol['G_eff']:.9e} S" in r.stdout
+    for f in ("Nodes.tbl.dat", "segment.LA.coo", "internal.DS.coo", "sink.DS.coo", "source.DS.coo"):
+        assert (a / f).read_bytes() == (b / f).read_bytes(), f
+    assert not (a / "internal.srt.coo").exists()
