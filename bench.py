@@ -71,7 +71,50 @@ def workload_config(name, params):
 
 
 # --------------------------------------------------------------------------- clocks
+class Nvml:
+    """Read-only NVML queries through the driver's libnvidia-ml (ctypes): the
+    SM clock, its maximum and the clock-event reason mask. Nothing is set."""
+    # reason bits of nvmlClocksEventReason* (nvml.h)
+    BITS = {"sw_power_cap": 0x4, "hw_slowdown": 0x8, "sw_thermal_slowdown": 0x20,
+            "hw_thermal_slowdown": 0x40, "hw_power_brake_slowdown": 0x80}
+
+    def __init__(self, dev):
+        import ctypes as C
+        self.C = C
+        L = C.CDLL("libnvidia-ml.so.1")
+        if L.nvmlInit_v2() != 0:
+            raise RuntimeError("nvmlInit failed")
+        self.L = L
+        self.h = C.c_void_p()
+        uuid = None
+        try:
+            import torch
+            u = getattr(torch.cuda.get_device_properties(dev), "uuid", None)
+            if u is not None:
+                uuid = ("GPU-" + str(u)).encode()
+        except Exception:
+            uuid = None
+        if uuid is None or L.nvmlDeviceGetHandleByUUID(uuid, C.byref(self.h)) != 0:
+            if L.nvmlDeviceGetHandleByIndex_v2(dev, C.byref(self.h)) != 0:
+                raise RuntimeError("no NVML handle")
+        self.reasons_fn = getattr(L, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+            L.nvmlDeviceGetCurrentClocksThrottleReasons
+        v = C.c_uint()
+        self.max_sm = float(v.value) if L.nvmlDeviceGetMaxClockInfo(self.h, 1, C.byref(v)) == 0 else None
+
+    def sample(self):
+        C = self.C
+        v, r = C.c_uint(), C.c_ulonglong()
+        if self.L.nvmlDeviceGetClockInfo(self.h, 1, C.byref(v)) != 0:
+            return None
+        self.reasons_fn(self.h, C.byref(r))
+        return float(v.value), int(r.value)
+
+
 class Clocks:
+    """SM clock and throttle reasons during the timed window: NVML polled every
+    5 ms from a thread while the window is open (a window of a few tens of ms
+    still gets samples), and the nvidia-smi sampler line beside it."""
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
          "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
@@ -80,6 +123,13 @@ class Clocks:
         self.dev = dev
         self.lines = []
         self.p = None
+        self.nv = []
+        self.open = False
+        self.done = False
+        try:
+            self.nvml = Nvml(dev)
+        except Exception:
+            self.nvml = None
 
     def start(self):
         try:
@@ -89,17 +139,30 @@ class Clocks:
             threading.Thread(target=self._read, daemon=True).start()
         except Exception:
             self.p = None
+        if self.nvml:
+            threading.Thread(target=self._poll, daemon=True).start()
 
     def _read(self):
         for line in self.p.stdout:
             self.lines.append(line.strip())
 
+    def _poll(self):
+        while not self.done:
+            if self.open:
+                s = self.nvml.sample()
+                if s:
+                    self.nv.append(s)
+            time.sleep(0.005)
+
     def mark(self):
         """Start of the timed window: samples before it (the sampler's own
         start-up overlaps the warm-up steps) are not used."""
         self.first = len(self.lines)
+        self.open = True
 
     def stop(self):
+        self.open = False
+        self.done = True
         if self.p:
             self.p.terminate()
             try:
@@ -121,9 +184,17 @@ class Clocks:
             for n, v in zip(names, f[5:9]):
                 if v.lower().startswith("active"):
                     reasons.add(n)
+        smi = len(sm)
+        for mhz, mask in self.nv:
+            sm.append(mhz)
+            for n, bit in Nvml.BITS.items():
+                if mask & bit:
+                    reasons.add(n)
+        if mx is None and self.nvml:
+            mx = self.nvml.max_sm
         sm.sort()
         return {"sm_mhz": sm[len(sm) // 2] if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
-                "samples": len(sm)}
+                "samples": len(sm), "samples_nvidia_smi": smi, "samples_nvml": len(self.nv)}
 
 
 # --------------------------------------------------------------------------- CPU (oracle) leg
