@@ -316,6 +316,86 @@ nf_status nf_get_internal_network(nf_handle *h, nf_internal_net *out);
  * in dir (save_coo layouts, src/conductivity.cu:881-930). */
 nf_status nf_write_internal_coo(nf_handle *h, const char *dir);
 
+/* ---- AC admittance spectrum (tools/kirchhoff/kirchhoff.py) ------------ */
+/* The offline Kirchhoff tool's impedance sweep, restated: every edge gets the
+ * scaled admittance Y = G + i (omega / omega0) C, with
+ *   rod segment (L in radii, radius a):  G = sigma pi a / L * R0, C = 0
+ *                                          (sigma = nf_params.rod_sigma)
+ *   contact (axis distance D, area S):    d = max(D - 2 r_cnt, delta_min),
+ *     S clamped to [pi r_cnt^2, 2 r_cnt l_cnt]; dropped unless d < delta_eff;
+ *     G = (S / S_min) / (exp(B (d - delta_min)) d / delta_min) if d <= delta_tun
+ *     else 0; C = (S / S_min) / (d / delta_min), 0 if below c_min
+ * with A, B, R0 = A exp(B delta_min) delta_min / S_min, C0 = eps0 eps_r S_min /
+ * delta_min and omega0 = 1 / (R0 C0) from the barrier phi (kirchhoff.py:
+ * 55-116). Source at 1, sink at 0 (Norton form); I = sum over source
+ * contacts of Y_src (1 - V), Z = R0 L_box / I (kirchhoff.py:211-286). Lengths
+ * in um. One complex-symmetric solve per frequency, all frequencies of a call
+ * in one launch (a CTA each). */
+typedef struct nf_ac_params {
+    double r_cnt;       /* um: radius of the gap correction and of S_min (4.75e-3) */
+    double l_cnt;       /* um: S_max = 2 r_cnt l_cnt (1.5) */
+    double phi_ev;      /* barrier height, eV (3.5) */
+    double eps_r;       /* relative permittivity of the matrix (2.9) */
+    double delta_min;   /* um: gap floor (0.34e-3) */
+    double delta_tun;   /* um: tunnelling range (1.1e-3) */
+    double delta_eff;   /* um: electrostatic range R_cut; farther contacts dropped */
+    double c_min;       /* scaled capacitances below it are 0 (0.005) */
+    double l_box;       /* um: impedance scale Z = R0 l_box / I */
+    int32_t own_radii;  /* 0: gap D - 2 r_cnt for every contact (the tool);
+                           1: D - a_I - a_J, electrode contacts D - a_I (the
+                           handle's own network with plane electrodes) */
+    int32_t pad;
+    double tol;         /* relative FP64 residual per frequency (1e-10) */
+} nf_ac_params;
+
+typedef struct nf_ac_point {
+    double freq;        /* Hz */
+    double i_re, i_im;  /* I in units of 1 / R0 */
+    double z_re, z_im;  /* R0 l_box Re(1/I) and -R0 l_box Im(1/I), the
+                           columns of impedance_rRC.<patch>.dat */
+    double rms;         /* || K V - b ||_2 (the tool's RMS column) */
+    double residual;    /* || K V - b || / || b ||; converged when <= tol */
+    double i_err;       /* |V^T (b - K V)|: first-order error of I (K is
+                           symmetric, so dI = b^T K^-1 r); the solve runs to
+                           the FP64 rounding floor, so i_err / |I| says how
+                           many digits of I are resolved */
+    int32_t iters;      /* inner iterations */
+    int32_t converged;
+} nf_ac_point;
+
+typedef struct nf_ac_stats {
+    uint64_t n_nodes, n_active, n_contacts, n_kept, n_segments;
+    double R0, C0, omega0;  /* ohm, F, rad/s */
+    double ms;              /* device time of the call */
+} nf_ac_stats;
+
+/* A network given on the host (the tool's input files): nodes 0..n_nodes-1,
+ * segments (i, j = i + 1 of the same rod, L in radii, radius a in um),
+ * contacts (i, j node or NF_SRC_ELEC / NF_SNK_ELEC, axis distance D in um,
+ * area S in um^2). */
+typedef struct nf_ac_net {
+    uint64_t n_nodes;
+    uint64_t n_segments;
+    const uint32_t *seg_i, *seg_j;
+    const double *seg_l, *seg_a;
+    uint64_t n_contacts;
+    const uint32_t *ct_i, *ct_j;
+    const double *ct_d, *ct_s;
+} nf_ac_net;
+
+void nf_ac_params_default(nf_ac_params *p);
+/* The tool's frequency grid (Hz): 10^(log_df x + logF_min), logF in [-2, 14],
+ * split into n_patch patches of ceil(N / n_patch) points (kirchhoff.py:72-79,
+ * 176). Returns the count; writes at most capacity values. */
+size_t nf_ac_frequencies(double log_df, int n_patch, int patch_id, double *freq, size_t capacity);
+/* net == NULL: the handle's own network (the intra-rod network after
+ * nf_internal_network, else the rod-level contact network; one realisation).
+ * Otherwise the given host network; h then only supplies the stream, the
+ * device workspace and rod_sigma. Returns NF_ERR_NOT_CONVERGED if a
+ * frequency missed tol (all points are still filled). */
+nf_status nf_ac_spectrum(nf_handle *h, const nf_ac_net *net, const nf_ac_params *p, const double *freq,
+                         size_t n_freq, nf_ac_point *out, nf_ac_stats *stats);
+
 /* ---- adjoint (no reference counterpart) ------------------------------- */
 /* dG_eff/d(endpoints) as N x 6 (e0.xyz, e1.xyz with e0/1 = r -/+ l/2 c),
  * dG_eff/dlambda and dG_eff/dG0, contact topology held fixed. */

@@ -15,10 +15,12 @@ import numpy as np
 from . import configs  # noqa: F401
 from ._abi import (LIB_PATH, SNK_ELEC, SRC_ELEC, STATUS, NfBatchResult, NfBatchStats,  # noqa: F401
                    NfContactList, NfContactStats, NfGenStats, NfParams, NfRods, NfSolveStats,
-                   NfInternalNet, NfInternalStats, NfStateHeader, NfTuneResult, load)
+                   NfInternalNet, NfInternalStats, NfStateHeader, NfTuneResult, NfAcNet, NfAcParams,
+                   NfAcPoint, NfAcStats, load)
 
 __all__ = ["Simulation", "NanoFillerError", "make_params", "params_from_file", "batch_run",
-           "target_count", "kernel_launches", "configs", "SRC_ELEC", "SNK_ELEC"]
+           "target_count", "kernel_launches", "configs", "SRC_ELEC", "SNK_ELEC", "ac_params", "ac_frequencies",
+           "write_impedance", "write_kirchhoff_log"]
 
 
 def kernel_launches():
@@ -269,6 +271,38 @@ class Simulation:
                "nf_stream_candidates_noalloc")
         return out.T.copy()
 
+    def ac_spectrum(self, freq, net=None, check=True, **ac):
+        """AC admittance spectrum (nf_ac_spectrum) at the frequencies freq
+        (Hz) of the handle's network (net=None: the intra-rod network after
+        internal_network(), else the rod-level one) or of a host network
+        given as a dict (n_nodes, seg_i, seg_j, seg_l, seg_a, ct_i, ct_j,
+        ct_d, ct_s). Keyword arguments override nf_ac_params fields.
+        Returns a dict of per-frequency arrays plus 'stats' and 'status'."""
+        f = np.ascontiguousarray(freq, np.float64)
+        pts = (NfAcPoint * max(len(f), 1))()
+        st = NfAcStats()
+        keep = []
+        pn = None
+        if net is not None:
+            q = NfAcNet()
+            q.n_nodes = int(net["n_nodes"])
+            for k, t in (("seg_i", np.uint32), ("seg_j", np.uint32), ("seg_l", np.float64), ("seg_a", np.float64),
+                         ("ct_i", np.uint32), ("ct_j", np.uint32), ("ct_d", np.float64), ("ct_s", np.float64)):
+                a = np.ascontiguousarray(net.get(k, np.zeros(0)), t)
+                keep.append(a)
+                setattr(q, k, a.ctypes.data_as(C.c_void_p) if len(a) else None)
+            q.n_segments = len(keep[0])
+            q.n_contacts = len(keep[4])
+            pn = C.byref(q)
+        rc = self._L.nf_ac_spectrum(self._h, pn, C.byref(ac_params(**ac)), f.ctypes.data_as(C.c_void_p), len(f),
+                                    C.cast(pts, C.c_void_p), C.byref(st))
+        if check:
+            _check(rc, self._h, "nf_ac_spectrum")
+        out = {k: np.array([getattr(pts[i], k) for i in range(len(f))]) for k, _ in NfAcPoint._fields_}
+        out["stats"] = {k: getattr(st, k) for k, _ in st._fields_}
+        out["status"] = rc
+        return out
+
     # diagnostics
     def set_kernel_timing(self, on=True):
         _check(self._L.nf_set_kernel_timing(self._h, int(on)), self._h, "nf_set_kernel_timing")
@@ -304,3 +338,41 @@ def batch_run(param_list):
     _check(L.nf_batch_run(arr, n, res, C.byref(st)), what="nf_batch_run")
     out = [{k: getattr(r, k) for k, _ in r._fields_} for r in res]
     return out, {k: getattr(st, k) for k, _ in st._fields_}
+
+
+def ac_params(**kw):
+    """nf_ac_params with the Kirchhoff tool's defaults, fields overridden by kw."""
+    p = NfAcParams()
+    load().nf_ac_params_default(C.byref(p))
+    for k, v in kw.items():
+        if k not in dict(NfAcParams._fields_):
+            raise KeyError(k)
+        setattr(p, k, v)
+    return p
+
+
+def ac_frequencies(log_df, n_patch=1, patch_id=0):
+    """The Kirchhoff tool's frequency grid (Hz) for one patch (nf_ac_frequencies)."""
+    L = load()
+    n = L.nf_ac_frequencies(log_df, n_patch, patch_id, None, 0)
+    f = np.zeros(n)
+    L.nf_ac_frequencies(log_df, n_patch, patch_id, f.ctypes.data_as(C.c_void_p), n)
+    return f
+
+
+def write_impedance(path, spec):
+    """impedance_rRC.<patch>.dat: frequency, Re Z, -Im Z, RMS per line, as the
+    Kirchhoff tool's numpy.savetxt writes it (tools/kirchhoff/kirchhoff.py:284-286)."""
+    np.savetxt(path, np.c_[spec["freq"], spec["z_re"], spec["z_im"], spec["rms"]])
+
+
+def write_kirchhoff_log(path, spec, elapsed=None):
+    """kirchhoff.<patch>.log with the tool's header and line format
+    (tools/kirchhoff/kirchhoff.py:220-222,273-280)."""
+    n = len(spec["freq"])
+    el = np.zeros(n) if elapsed is None else np.broadcast_to(np.asarray(elapsed, float), (n,))
+    with open(path, "w") as f:
+        f.write("# Frequency\tZ_real\t(-1)Z_imag\tConverged\tRMSD\tElapsed\n")
+        for i in range(n):
+            f.write("{:>10.3e}\t{:>10.3e}\t{:>10.3e}\t{:>d}\t{:>10.3e}\t{:>10.3f}\n".format(
+                spec["freq"][i], spec["z_re"][i], spec["z_im"][i], int(spec["converged"][i]), spec["rms"][i], el[i]))

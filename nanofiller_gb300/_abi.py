@@ -93,6 +93,31 @@ class NfInternalNet(C.Structure):
                 ("edge_j", C.c_void_p)]
 
 
+class NfAcParams(C.Structure):
+    _fields_ = [("r_cnt", C.c_double), ("l_cnt", C.c_double), ("phi_ev", C.c_double), ("eps_r", C.c_double),
+                ("delta_min", C.c_double), ("delta_tun", C.c_double), ("delta_eff", C.c_double),
+                ("c_min", C.c_double), ("l_box", C.c_double), ("own_radii", C.c_int32), ("pad", C.c_int32),
+                ("tol", C.c_double)]
+
+
+class NfAcPoint(C.Structure):
+    _fields_ = [("freq", C.c_double), ("i_re", C.c_double), ("i_im", C.c_double), ("z_re", C.c_double),
+                ("z_im", C.c_double), ("rms", C.c_double), ("residual", C.c_double), ("i_err", C.c_double),
+                ("iters", C.c_int32), ("converged", C.c_int32)]
+
+
+class NfAcStats(C.Structure):
+    _fields_ = [("n_nodes", C.c_uint64), ("n_active", C.c_uint64), ("n_contacts", C.c_uint64),
+                ("n_kept", C.c_uint64), ("n_segments", C.c_uint64), ("R0", C.c_double), ("C0", C.c_double),
+                ("omega0", C.c_double), ("ms", C.c_double)]
+
+
+class NfAcNet(C.Structure):
+    _fields_ = [("n_nodes", C.c_uint64), ("n_segments", C.c_uint64), ("seg_i", C.c_void_p), ("seg_j", C.c_void_p),
+                ("seg_l", C.c_void_p), ("seg_a", C.c_void_p), ("n_contacts", C.c_uint64), ("ct_i", C.c_void_p),
+                ("ct_j", C.c_void_p), ("ct_d", C.c_void_p), ("ct_s", C.c_void_p)]
+
+
 class NfTuneResult(C.Structure):
     _fields_ = [("stencil_radius", C.c_int32), ("round_overshoot", C.c_float), ("two_phase_work", C.c_double),
                 ("ms_first", C.c_double), ("ms_best", C.c_double), ("trials", C.c_int32)]
@@ -146,6 +171,10 @@ SIGNATURES = {
     "nf_internal_network": (_st, [_H, _P(NfInternalStats)]),
     "nf_get_internal_network": (_st, [_H, _P(NfInternalNet)]),
     "nf_write_internal_coo": (_st, [_H, C.c_char_p]),
+    "nf_ac_params_default": (None, [_P(NfAcParams)]),
+    "nf_ac_frequencies": (C.c_size_t, [C.c_double, C.c_int, C.c_int, C.c_void_p, C.c_size_t]),
+    "nf_ac_spectrum": (_st, [_H, _P(NfAcNet), _P(NfAcParams), C.c_void_p, C.c_size_t, C.c_void_p,
+                             _P(NfAcStats)]),
     "nf_kernel_time": (_st, [_H, C.c_char_p, _P(C.c_double), _P(C.c_uint64), _P(C.c_double),
                              _P(C.c_double)]),
     "nf_format_write_vtk": (_st, [C.c_char_p, C.c_size_t] + [C.c_void_p] * 9),

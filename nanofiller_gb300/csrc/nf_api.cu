@@ -590,6 +590,71 @@ nf_status nf_write_internal_coo(nf_handle* h, const char* dir) {
     return NF_OK;
 }
 
+void nf_ac_params_default(nf_ac_params* p) {
+    if (!p) return;
+    *p = nf_ac_params{};
+    // the constants of tools/kirchhoff/kirchhoff.py:55-68 (lengths in um)
+    p->r_cnt = 4.75e-3;
+    p->l_cnt = 1.5;
+    p->phi_ev = 3.5;
+    p->eps_r = 2.9;
+    p->delta_min = 0.34e-3;
+    p->delta_tun = 1.1e-3;
+    p->delta_eff = 50e-3;
+    p->c_min = 0.005;
+    p->l_box = 1.0;
+    p->own_radii = 0;
+    p->tol = 1e-10;
+}
+
+size_t nf_ac_frequencies(double log_df, int n_patch, int patch_id, double* freq, size_t capacity) {
+    if (!(log_df > 0) || n_patch < 1 || patch_id < 0 || patch_id >= n_patch) return 0;
+    // kirchhoff.py:72-79,176: N = int(16 / log_df) + 1 points from 10^-2 Hz,
+    // patch = ceil(N / n_patch) points from logF_min = -2 + patch_id patch log_df
+    const long nf = (long)((14.0 - (-2.0)) / log_df) + 1;
+    const long patch = (long)std::ceil(nf * 1.0 / n_patch);
+    const double lo = -2.0 + patch_id * patch * log_df;
+    for (long x = 0; x < patch && (size_t)x < capacity; ++x)
+        if (freq) freq[x] = std::pow(10.0, log_df * x + lo);
+    return (size_t)patch;
+}
+
+nf_status nf_ac_spectrum(nf_handle* h, const nf_ac_net* net, const nf_ac_params* p, const double* freq,
+                         size_t n_freq, nf_ac_point* out, nf_ac_stats* stats) {
+    if (!h || !p || (n_freq && (!freq || !out))) return NF_ERR_PARAM;
+    nf::Engine& E = h->E;
+    if (!(p->r_cnt > 0) || !(p->l_cnt > 0) || !(p->phi_ev > 0) || !(p->eps_r > 0) || !(p->delta_min > 0) ||
+        !(p->delta_tun >= 0) || !(p->delta_eff > 0) || !(p->c_min >= 0) || !(p->l_box > 0) ||
+        (p->own_radii != 0 && p->own_radii != 1))
+        return fail(h, NF_ERR_PARAM, "AC parameters out of range");
+    for (size_t f = 0; f < n_freq; ++f)
+        if (!(freq[f] > 0) || !std::isfinite(freq[f])) return fail(h, NF_ERR_PARAM, "frequencies must be positive");
+    if (!net) {
+        if (E.R != 1) return fail(h, NF_ERR_STATE, "the AC spectrum runs on a single-realisation handle");
+        if (!E.contacts_valid) return fail(h, NF_ERR_STATE, "no contacts: run nf_contacts first");
+    } else {
+        if (p->own_radii) return fail(h, NF_ERR_PARAM, "own_radii needs the handle's own network");
+        const uint64_t n = net->n_nodes;
+        if (n == 0 || n >= NF_SNK_ELEC) return fail(h, NF_ERR_PARAM, "n_nodes out of range");
+        if ((net->n_segments && (!net->seg_i || !net->seg_j || !net->seg_l || !net->seg_a)) ||
+            (net->n_contacts && (!net->ct_i || !net->ct_j || !net->ct_d || !net->ct_s)))
+            return fail(h, NF_ERR_PARAM, "null network array");
+        if (net->n_segments + net->n_contacts >= (1ull << 31)) return fail(h, NF_ERR_PARAM, "network too large");
+        for (uint64_t s = 0; s < net->n_segments; ++s)
+            if (net->seg_i[s] >= n || net->seg_j[s] >= n || net->seg_i[s] == net->seg_j[s] ||
+                !(net->seg_l[s] > 0) || !(net->seg_a[s] > 0))
+                return fail(h, NF_ERR_PARAM, "segment out of range");
+        for (uint64_t c = 0; c < net->n_contacts; ++c) {
+            const uint32_t j = net->ct_j[c];
+            if (net->ct_i[c] >= n || (j >= n && j < NF_SNK_ELEC) || j == net->ct_i[c] || !std::isfinite(net->ct_d[c]) ||
+                !std::isfinite(net->ct_s[c]))
+                return fail(h, NF_ERR_PARAM, "contact out of range");
+        }
+    }
+    if (n_freq == 0) return NF_OK;
+    return E.ac_spectrum(net, *p, freq, n_freq, out, stats);
+}
+
 nf_status nf_batch_run(const nf_params* params, int n, nf_batch_result* out, nf_batch_stats* stats) {
     if (!params || n <= 0 || !out) return NF_ERR_PARAM;
     int ndev = 0;

@@ -57,6 +57,19 @@ struct DBuf {
     }
 };
 
+// Two CUDA events, destroyed with the object (early returns included).
+struct EventPair {
+    cudaEvent_t a = nullptr, b = nullptr;
+    cudaError_t create() {
+        cudaError_t e = cudaEventCreate(&a);
+        return e == cudaSuccess ? cudaEventCreate(&b) : e;
+    }
+    ~EventPair() {
+        if (a) cudaEventDestroy(a);
+        if (b) cudaEventDestroy(b);
+    }
+};
+
 // One contact record before sorting / screening (64 B).
 struct Rec {
     uint32_t i, j;      // global rod slots, i < j
@@ -155,6 +168,8 @@ struct Engine {
     DBuf<uint32_t> parent, cflag, aidx, rowp, col, deg;
     DBuf<float> val32, diag32, chain32;
     DBuf<double> val64, diag64, bvec, xvec, cdiag, chain64;
+    DBuf<double> valC64, diagC64, cdiagC, bvecC;  // capacitive parts (admittance form)
+    DBuf<double> acG, acC, acchi;                 // scaled edge admittances of an AC call, start chi
     DBuf<float> cgbuf;
     DBuf<double> cgred;
     std::vector<nf_solve_stats> solve_st;
@@ -178,6 +193,18 @@ struct Engine {
     nf_status rebuild_cells();
     nf_status contacts();
     nf_status solve();
+    // Active-set CSR system of a graph (shared by the DC and AC solves).
+    struct Asm {
+        uint32_t na = 0, nnz = 0;
+        bool chains = false;
+        std::vector<uint32_t> habase;  // active base per realisation
+    };
+    nf_status assemble(uint32_t n, const std::vector<uint32_t>& off, uint32_t mc, uint32_t m, const uint32_t* eI,
+                       const uint32_t* eJ, const double* eG, const double* eC, Asm* out);
+    // AC admittance spectrum of the handle's network (net == nullptr) or of a
+    // host-given network.
+    nf_status ac_spectrum(const nf_ac_net* net, const nf_ac_params& p, const double* freq, size_t nfreq,
+                          nf_ac_point* out, nf_ac_stats* stats);
     // Edges [0, mc) are general; edges [mc, m) are chain links joining node i
     // to node i + 1 of the same rod (rod segments of the internal network).
     nf_status solve_graph(uint32_t n, const std::vector<uint32_t>& off, const std::vector<uint32_t>& nodes, uint32_t mc,

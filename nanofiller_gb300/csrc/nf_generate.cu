@@ -832,7 +832,7 @@ void Engine::release() {
     for (auto* b : u64) b->release();
     ikeys.release(); ikeys2.release();
     DBuf<double>* d64[] = {&ct0, &ct1, &cD, &cG, &cS, &vsrc, &vsnk, &volt, &val64, &diag64, &bvec, &xvec, &cgred,
-                           &cdiag, &chain64, &int_t, &ieG, &iseg_l};
+                           &cdiag, &chain64, &valC64, &diagC64, &cdiagC, &bvecC, &acG, &acC, &acchi, &int_t, &ieG, &iseg_l};
     for (auto* b : d64) b->release();
     if (hpin) cudaFreeHost(hpin);
     hpin = nullptr;

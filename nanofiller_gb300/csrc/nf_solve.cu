@@ -35,24 +35,11 @@
 #include <cstring>
 
 #include "nf_engine.cuh"
+#include "nf_graph.cuh"
 
 namespace nf {
 
 static inline unsigned grid_for(size_t n, unsigned b) { return (unsigned)((n + b - 1) / b); }
-
-constexpr uint32_t kFindCap = 1u << 22;  // bound on union-find walks / CAS retries
-
-__device__ __forceinline__ uint32_t uf_find(uint32_t* parent, uint32_t x, uint32_t* err) {
-    uint32_t steps = 0;
-    while (true) {
-        uint32_t p = parent[x];
-        if (p == x) return x;
-        uint32_t g = parent[p];
-        if (g != p) atomicCAS(&parent[x], p, g);  // path halving
-        x = p;
-        if (++steps > kFindCap) { atomicExch(err, 1u); return x; }
-    }
-}
 
 __global__ void k_uf_init(uint32_t n, uint32_t* parent, uint32_t* flag) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -61,12 +48,19 @@ __global__ void k_uf_init(uint32_t n, uint32_t* parent, uint32_t* flag) {
     flag[i] = 0;
 }
 
+// An edge conducts unless the admittance form gives it G = C = 0 (an AC
+// contact beyond the electrostatic range); without C every edge conducts.
+__device__ __forceinline__ bool edge_on(const double* G, const double* C, uint32_t e) {
+    return !C || G[e] > 0.0 || C[e] > 0.0;
+}
+
 __global__ void k_uf_union(uint32_t m, const uint32_t* __restrict__ I, const uint32_t* __restrict__ J,
-                           uint32_t* parent, uint32_t* err) {
+                           const double* __restrict__ G, const double* __restrict__ C, uint32_t* parent,
+                           uint32_t* err) {
     uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= m) return;
     uint32_t j = J[e];
-    if (j >= NF_SNK_ELEC) return;
+    if (j >= NF_SNK_ELEC || !edge_on(G, C, e)) return;
     uint32_t a = I[e], b = j;
     for (uint32_t it = 0; it < kFindCap; ++it) {
         a = uf_find(parent, a, err);
@@ -79,11 +73,12 @@ __global__ void k_uf_union(uint32_t m, const uint32_t* __restrict__ I, const uin
 }
 
 __global__ void k_uf_flags(uint32_t m, const uint32_t* __restrict__ I, const uint32_t* __restrict__ J,
-                           uint32_t* parent, uint32_t* flag, uint32_t* err) {
+                           const double* __restrict__ G, const double* __restrict__ C, uint32_t* parent,
+                           uint32_t* flag, uint32_t* err) {
     uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= m) return;
     uint32_t j = J[e];
-    if (j < NF_SNK_ELEC) return;
+    if (j < NF_SNK_ELEC || !edge_on(G, C, e)) return;
     uint32_t r = uf_find(parent, I[e], err);
     atomicOr(&flag[r], j == NF_SRC_ELEC ? 1u : 2u);
 }
@@ -96,21 +91,30 @@ __global__ void k_active(uint32_t n, uint32_t* parent, const uint32_t* __restric
     act[i] = flag[uf_find(parent, i, err)] == 3u ? 1u : 0u;
 }
 
+// Electrode admittance per node (s: source, t: sink; sC, tC the capacitive
+// parts when C is given).
 __global__ void k_elec_g(uint32_t m, const uint32_t* __restrict__ I, const uint32_t* __restrict__ J,
-                         const double* __restrict__ G, double* __restrict__ s, double* __restrict__ t) {
+                         const double* __restrict__ G, const double* __restrict__ C, double* __restrict__ s,
+                         double* __restrict__ t, double* __restrict__ sC, double* __restrict__ tC) {
     uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= m) return;
     uint32_t j = J[e];
-    if (j == NF_SRC_ELEC) s[I[e]] = G[e];
-    else if (j == NF_SNK_ELEC) t[I[e]] = G[e];
+    if (j == NF_SRC_ELEC) {
+        s[I[e]] = G[e];
+        if (C) sC[I[e]] = C[e];
+    } else if (j == NF_SNK_ELEC) {
+        t[I[e]] = G[e];
+        if (C) tC[I[e]] = C[e];
+    }
 }
 
 __global__ void k_deg(uint32_t m, const uint32_t* __restrict__ I, const uint32_t* __restrict__ J,
-                      const uint32_t* __restrict__ act, const uint32_t* __restrict__ aidx, uint32_t* __restrict__ deg) {
+                      const double* __restrict__ G, const double* __restrict__ C, const uint32_t* __restrict__ act,
+                      const uint32_t* __restrict__ aidx, uint32_t* __restrict__ deg) {
     uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= m) return;
     uint32_t j = J[e];
-    if (j >= NF_SNK_ELEC) return;
+    if (j >= NF_SNK_ELEC || !edge_on(G, C, e)) return;
     uint32_t i = I[e];
     if (!act[i]) return;  // both ends share a component
     atomicAdd(&deg[aidx[i]], 1u);
@@ -118,13 +122,13 @@ __global__ void k_deg(uint32_t m, const uint32_t* __restrict__ I, const uint32_t
 }
 
 __global__ void k_fill(uint32_t m, const uint32_t* __restrict__ I, const uint32_t* __restrict__ J,
-                       const double* __restrict__ G, const uint32_t* __restrict__ act,
+                       const double* __restrict__ G, const double* __restrict__ C, const uint32_t* __restrict__ act,
                        const uint32_t* __restrict__ aidx, const uint32_t* __restrict__ rowp, uint32_t* __restrict__ cur,
-                       uint32_t* __restrict__ col, double* __restrict__ v64) {
+                       uint32_t* __restrict__ col, double* __restrict__ v64, double* __restrict__ vC64) {
     uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= m) return;
     uint32_t j = J[e];
-    if (j >= NF_SNK_ELEC) return;
+    if (j >= NF_SNK_ELEC || !edge_on(G, C, e)) return;
     uint32_t i = I[e];
     if (!act[i]) return;
     uint32_t a = aidx[i], b = aidx[j];
@@ -132,43 +136,63 @@ __global__ void k_fill(uint32_t m, const uint32_t* __restrict__ I, const uint32_
     uint32_t qb = rowp[b] + atomicAdd(&cur[b], 1u);
     col[qa] = b; v64[qa] = G[e];
     col[qb] = a; v64[qb] = G[e];
+    if (C) { vC64[qa] = C[e]; vC64[qb] = C[e]; }
 }
 
 // Chain links (edges [mc, m)): node j = i + 1 of the same rod, both active or
 // neither. gr[a] links row a to row a + 1, gl[a + 1] the same link seen from
 // below.
+// With C, the capacitive parts go to glC / grC (ch64 + 2 na, + 3 na).
 __global__ void k_chain_links(uint32_t mc, uint32_t m, const uint32_t* __restrict__ I,
                               const uint32_t* __restrict__ J, const double* __restrict__ G,
-                              const uint32_t* __restrict__ act, const uint32_t* __restrict__ aidx,
-                              double* __restrict__ gl, double* __restrict__ gr, uint32_t* err) {
+                              const double* __restrict__ C, const uint32_t* __restrict__ act,
+                              const uint32_t* __restrict__ aidx, uint32_t na, double* __restrict__ ch64,
+                              uint32_t* err) {
     uint32_t e = mc + blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= m) return;
     const uint32_t i = I[e], j = J[e];
-    if (!act[i]) return;
+    if (!act[i] || !edge_on(G, C, e)) return;
     const uint32_t a = aidx[i];
     if (j != i + 1 || !act[j] || aidx[j] != a + 1) { atomicExch(err, 2u); return; }
-    gr[a] = G[e];
-    gl[a + 1] = G[e];
+    ch64[a + na] = G[e];
+    ch64[a + 1] = G[e];
+    if (C) {
+        ch64[3ull * na + a] = C[e];
+        ch64[2ull * na + a + 1] = C[e];
+    }
 }
 
-// Sort each row by column (deterministic SpMV order), FP32 copies, electrode
-// conductance e = s + t, the row's non-chain conductance c = e + sum_k G_k, rhs.
+// Sort each row by (column, G, C) (deterministic SpMV order whatever order the
+// atomics filled it in), FP32 copies, electrode conductance e = s + t, the
+// row's non-chain conductance c = e + sum_k G_k, rhs b = s; with C the same
+// for the capacitive parts (eC, cC, bC).
 __global__ void k_rows(uint32_t nslot, const uint32_t* __restrict__ act, const uint32_t* __restrict__ aidx,
                        const uint32_t* __restrict__ rowp, uint32_t* __restrict__ col, double* __restrict__ v64,
-                       float* __restrict__ v32, const double* __restrict__ s, const double* __restrict__ t,
+                       double* __restrict__ vC64, float* __restrict__ v32, const double* __restrict__ s,
+                       const double* __restrict__ t, const double* __restrict__ sC, const double* __restrict__ tC,
                        double* __restrict__ e64, float* __restrict__ e32, double* __restrict__ c64,
-                       double* __restrict__ b) {
+                       double* __restrict__ b, double* __restrict__ eC64, double* __restrict__ cC64,
+                       double* __restrict__ bC) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nslot || !act[i]) return;
     uint32_t a = aidx[i];
     uint32_t p0 = rowp[a], p1 = rowp[a + 1];
+    const bool ac = vC64 != nullptr;
     for (uint32_t k = p0 + 1; k < p1; ++k) {
-        uint32_t c = col[k];
-        double v = v64[k];
+        const uint32_t c = col[k];
+        const double v = v64[k], w = ac ? vC64[k] : 0.0;
         uint32_t q = k;
-        while (q > p0 && col[q - 1] > c) { col[q] = col[q - 1]; v64[q] = v64[q - 1]; --q; }
+        while (q > p0) {
+            const uint32_t cp = col[q - 1];
+            const double vp = v64[q - 1], wp = ac ? vC64[q - 1] : 0.0;
+            if (!(cp > c || (cp == c && (vp > v || (vp == v && wp > w))))) break;
+            col[q] = cp; v64[q] = vp;
+            if (ac) vC64[q] = wp;
+            --q;
+        }
         col[q] = c;
         v64[q] = v;
+        if (ac) vC64[q] = w;
     }
     const double el = s[i] + t[i];
     double c = el;
@@ -177,6 +201,14 @@ __global__ void k_rows(uint32_t nslot, const uint32_t* __restrict__ act, const u
     e32[a] = (float)el;
     c64[a] = c;
     b[a] = s[i];
+    if (ac) {
+        const double elC = sC[i] + tC[i];
+        double cc = elC;
+        for (uint32_t k = p0; k < p1; ++k) cc += vC64[k];
+        eC64[a] = elC;
+        cC64[a] = cc;
+        bC[a] = sC[i];
+    }
 }
 
 // Tridiagonal factors per chain, from its first row (gl == 0): FP32 copies of
@@ -206,53 +238,6 @@ __global__ void k_chain_factor(uint32_t na, const double* __restrict__ gl, const
         gam = c64[k1] + g * gam / (g + gam);
         k = k1;
     }
-}
-
-// ---------------------------------------------------------------------------
-// Block reductions (deterministic: fixed thread->row mapping and tree).
-// ---------------------------------------------------------------------------
-template <int NT>
-__device__ __forceinline__ double block_sum(double v, double* sh) {
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
-    __syncthreads();
-    if (l == 0) sh[w] = v;
-    __syncthreads();
-    if (w == 0) {
-        double x = (l < NT / 32) ? sh[l] : 0.0;
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
-        if (l == 0) sh[32] = x;
-    }
-    __syncthreads();
-    return sh[32];
-}
-
-template <int NT>
-__device__ __forceinline__ void block_sum2(float a, float b, double* sh, double* oa, double* ob) {
-    double x = a, y = b;
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        x += __shfl_down_sync(0xffffffffu, x, o);
-        y += __shfl_down_sync(0xffffffffu, y, o);
-    }
-    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
-    __syncthreads();
-    if (l == 0) { sh[w] = x; sh[40 + w] = y; }
-    __syncthreads();
-    if (w == 0) {
-        double u = (l < NT / 32) ? sh[l] : 0.0, v = (l < NT / 32) ? sh[40 + l] : 0.0;
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            u += __shfl_down_sync(0xffffffffu, u, o);
-            v += __shfl_down_sync(0xffffffffu, v, o);
-        }
-        if (l == 0) { sh[32] = u; sh[33] = v; }
-    }
-    __syncthreads();
-    *oa = sh[32];
-    *ob = sh[33];
 }
 
 struct CgOut {
@@ -467,64 +452,65 @@ nf_status Engine::solve() {
     return solve_graph((uint32_t)rod_slots, off, nodes, (uint32_t)ct_off[R], (uint32_t)ct_off[R], cI.p, cJ.p, cG.p);
 }
 
-// Laplacian solve on a graph of n nodes (realisation r owns nodes
-// [off[r], off[r+1]), nodes[r] of them real) and m edges (I, J, G); J may be
-// NF_SRC_ELEC / NF_SNK_ELEC. Edges [mc, m) are chain links (J = I + 1, same
-// rod). Node voltages land in volt.
-nf_status Engine::solve_graph(uint32_t n, const std::vector<uint32_t>& off, const std::vector<uint32_t>& nodes,
-                              uint32_t mc, uint32_t m, const uint32_t* eI, const uint32_t* eJ, const double* eG) {
-    cudaEvent_t e0, e1;
-    NF_CK(cudaEventCreate(&e0));
-    NF_CK(cudaEventCreate(&e1));
-    NF_CK(cudaEventRecord(e0, st));
+// Active-set system of a graph of n nodes (realisation r owns nodes
+// [off[r], off[r+1])) and m edges (I, J, G[, C]); J may be NF_SRC_ELEC /
+// NF_SNK_ELEC; edges [mc, m) are chain links (J = I + 1, same rod). Only nodes
+// whose component touches both electrodes are unknowns. With C (admittance
+// form) an edge with G = C = 0 is absent, and the capacitive parts are
+// assembled beside the conductances (valC64, diagC64, cdiagC, bvecC, chain64
+// [gl | gr | glC | grC]).
+nf_status Engine::assemble(uint32_t n, const std::vector<uint32_t>& off, uint32_t mc, uint32_t m,
+                           const uint32_t* eI, const uint32_t* eJ, const double* eG, const double* eC, Asm* out) {
+    const int RR = (int)off.size() - 1;
     const uint32_t nslot = n;
-    const uint32_t* cIp = eI;
-    const uint32_t* cJp = eJ;
-    const double* cGp = eG;
+    const bool ac = eC != nullptr;
     NF_CK(parent.ensure(nslot + 1));
     NF_CK(cflag.ensure(nslot + 1));
     NF_CK(aidx.ensure(nslot + 1));
     NF_CK(eflag.ensure(nslot + 2));  // act[] + error word
-    NF_CK(vsrc.ensure(nslot + 1));
-    NF_CK(vsnk.ensure(nslot + 1));
-    NF_CK(volt.ensure(nslot + 1));
+    NF_CK(vsrc.ensure(2ull * nslot + 2));  // [s | sC]
+    NF_CK(vsnk.ensure(2ull * nslot + 2));  // [t | tC]
     uint32_t* act = eflag.p;
     uint32_t* errw = eflag.p + nslot + 1;
+    double* sC = vsrc.p + nslot + 1;
+    double* tC = vsnk.p + nslot + 1;
     NF_CK(cudaMemsetAsync(errw, 0, sizeof(uint32_t), st));
-    NF_CK(cudaMemsetAsync(vsrc.p, 0, sizeof(double) * (nslot + 1), st));
-    NF_CK(cudaMemsetAsync(vsnk.p, 0, sizeof(double) * (nslot + 1), st));
+    NF_CK(cudaMemsetAsync(vsrc.p, 0, sizeof(double) * (2ull * nslot + 2), st));
+    NF_CK(cudaMemsetAsync(vsnk.p, 0, sizeof(double) * (2ull * nslot + 2), st));
     NF_CK(cudaMemsetAsync(act + nslot, 0, sizeof(uint32_t), st));
     NF_LAUNCH(k_uf_init, grid_for(nslot, 256), 256, 0, st)(nslot, parent.p, cflag.p);
     if (m) {
-        NF_LAUNCH(k_uf_union, grid_for(m, 256), 256, 0, st)(m, cIp, cJp, parent.p, errw);
-        NF_LAUNCH(k_uf_flags, grid_for(m, 256), 256, 0, st)(m, cIp, cJp, parent.p, cflag.p, errw);
-        NF_LAUNCH(k_elec_g, grid_for(m, 256), 256, 0, st)(m, cIp, cJp, cGp, vsrc.p, vsnk.p);
+        NF_LAUNCH(k_uf_union, grid_for(m, 256), 256, 0, st)(m, eI, eJ, eG, eC, parent.p, errw);
+        NF_LAUNCH(k_uf_flags, grid_for(m, 256), 256, 0, st)(m, eI, eJ, eG, eC, parent.p, cflag.p, errw);
+        NF_LAUNCH(k_elec_g, grid_for(m, 256), 256, 0, st)(m, eI, eJ, eG, eC, vsrc.p, vsnk.p, sC, tC);
     }
     NF_LAUNCH(k_active, grid_for(nslot, 256), 256, 0, st)(nslot, parent.p, cflag.p, act, errw);
     NF_CK(cudaGetLastError());
     nf_status s = scan_u32(act, aidx.p, nslot + 1);
     if (s != NF_OK) return s;
     // Active count per realisation: aidx at the node-range boundaries.
-    std::vector<uint32_t> habase(R + 1);
-    for (int r = 0; r <= R; ++r)
-        NF_CK(cudaMemcpyAsync(&habase[r], aidx.p + off[r], sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+    out->habase.assign(RR + 1, 0);
+    for (int r = 0; r <= RR; ++r)
+        NF_CK(cudaMemcpyAsync(&out->habase[r], aidx.p + off[r], sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
     uint32_t herr = 0;
     NF_CK(cudaMemcpyAsync(&herr, errw, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
     NF_CK(cudaStreamSynchronize(st));
     if (herr) { err = "union-find walk exceeded its bound"; return NF_ERR_TIMEOUT; }
-    const uint32_t na = habase[R];
+    const uint32_t na = out->habase[RR];
+    out->na = na;
     NF_CK(deg.ensure(na + 1));
     NF_CK(rowp.ensure(na + 1));
     NF_CK(cudaMemsetAsync(deg.p, 0, sizeof(uint32_t) * (na + 1), st));
-    if (mc) NF_LAUNCH(k_deg, grid_for(mc, 256), 256, 0, st)(mc, cIp, cJp, act, aidx.p, deg.p);
+    if (mc) NF_LAUNCH(k_deg, grid_for(mc, 256), 256, 0, st)(mc, eI, eJ, eG, eC, act, aidx.p, deg.p);
     NF_CK(cudaGetLastError());
-    const bool chains = m > mc;
-    NF_CK(chain64.ensure(2ull * na + 2));
+    out->chains = m > mc;
+    const size_t nch = (ac ? 4ull : 2ull) * na + 4;
+    NF_CK(chain64.ensure(nch));
     NF_CK(chain32.ensure(4ull * na + 4));
-    NF_CK(cudaMemsetAsync(chain64.p, 0, sizeof(double) * (2ull * na + 2), st));
-    if (chains)
-        NF_LAUNCH(k_chain_links, grid_for(m - mc, 256), 256, 0, st)(mc, m, cIp, cJp, cGp, act, aidx.p, chain64.p,
-                                                                   chain64.p + na, errw);
+    NF_CK(cudaMemsetAsync(chain64.p, 0, sizeof(double) * nch, st));
+    if (out->chains)
+        NF_LAUNCH(k_chain_links, grid_for(m - mc, 256), 256, 0, st)(mc, m, eI, eJ, eG, eC, act, aidx.p, na, chain64.p,
+                                                                   errw);
     NF_CK(cudaGetLastError());
     s = scan_u32(deg.p, rowp.p, na + 1);
     if (s != NF_OK) return s;
@@ -533,6 +519,7 @@ nf_status Engine::solve_graph(uint32_t n, const std::vector<uint32_t>& off, cons
     NF_CK(cudaMemcpyAsync(&herr, errw, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
     NF_CK(cudaStreamSynchronize(st));
     if (herr) { err = "chain link between non-consecutive active nodes"; return NF_ERR_STATE; }
+    out->nnz = nnz;
     NF_CK(col.ensure(nnz + 1));
     NF_CK(val64.ensure(nnz + 1));
     NF_CK(val32.ensure(nnz + 1));
@@ -540,26 +527,53 @@ nf_status Engine::solve_graph(uint32_t n, const std::vector<uint32_t>& off, cons
     NF_CK(diag32.ensure(na + 1));
     NF_CK(cdiag.ensure(na + 1));
     NF_CK(bvec.ensure(na + 1));
+    if (ac) {
+        NF_CK(valC64.ensure(nnz + 1));
+        NF_CK(diagC64.ensure(na + 1));
+        NF_CK(cdiagC.ensure(na + 1));
+        NF_CK(bvecC.ensure(na + 1));
+    }
+    NF_CK(cudaMemsetAsync(deg.p, 0, sizeof(uint32_t) * (na + 1), st));  // reuse as cursor
+    if (mc)
+        NF_LAUNCH(k_fill, grid_for(mc, 256), 256, 0, st)(mc, eI, eJ, eG, eC, act, aidx.p, rowp.p, deg.p, col.p,
+                                                         val64.p, ac ? valC64.p : nullptr);
+    NF_LAUNCH(k_rows, grid_for(nslot, 256), 256, 0, st)(nslot, act, aidx.p, rowp.p, col.p, val64.p,
+                                                 ac ? valC64.p : nullptr, val32.p, vsrc.p, vsnk.p, sC, tC, diag64.p,
+                                                 diag32.p, cdiag.p, bvec.p, ac ? diagC64.p : nullptr,
+                                                 ac ? cdiagC.p : nullptr, ac ? bvecC.p : nullptr);
+    NF_CK(cudaGetLastError());
+    return NF_OK;
+}
+
+// Laplacian solve on the graph (see assemble); node voltages land in volt.
+nf_status Engine::solve_graph(uint32_t n, const std::vector<uint32_t>& off, const std::vector<uint32_t>& nodes,
+                              uint32_t mc, uint32_t m, const uint32_t* eI, const uint32_t* eJ, const double* eG) {
+    EventPair ev;
+    NF_CK(ev.create());
+    NF_CK(cudaEventRecord(ev.a, st));
+    Asm A;
+    nf_status s = assemble(n, off, mc, m, eI, eJ, eG, nullptr, &A);
+    if (s != NF_OK) return s;
+    const uint32_t nslot = n, na = A.na, nnz = A.nnz;
+    uint32_t* act = eflag.p;
+    uint32_t* errw = eflag.p + nslot + 1;
+    NF_CK(volt.ensure(nslot + 1));
     NF_CK(xvec.ensure(na + 1));
     NF_CK(cgred.ensure(na + 1));
     NF_CK(cgbuf.ensure(5 * (size_t)na + 5));
-    NF_CK(cudaMemsetAsync(deg.p, 0, sizeof(uint32_t) * (na + 1), st));  // reuse as cursor
-    if (mc) NF_LAUNCH(k_fill, grid_for(mc, 256), 256, 0, st)(mc, cIp, cJp, cGp, act, aidx.p, rowp.p, deg.p, col.p, val64.p);
-    NF_LAUNCH(k_rows, grid_for(nslot, 256), 256, 0, st)(nslot, act, aidx.p, rowp.p, col.p, val64.p, val32.p, vsrc.p,
-                                                 vsnk.p, diag64.p, diag32.p, cdiag.p, bvec.p);
     if (na)
         NF_LAUNCH(k_chain_factor, grid_for(na, 256), 256, 0, st)(na, chain64.p, chain64.p + na, cdiag.p, chain32.p);
     NF_CK(cudaGetLastError());
     DBuf<uint32_t>& dab = rcur;  // per-realisation active base (R+1)
     NF_CK(dab.ensure(R + 1));
-    NF_CK(cudaMemcpyAsync(dab.p, habase.data(), sizeof(uint32_t) * (R + 1), cudaMemcpyHostToDevice, st));
+    NF_CK(cudaMemcpyAsync(dab.p, A.habase.data(), sizeof(uint32_t) * (R + 1), cudaMemcpyHostToDevice, st));
     DBuf<CgOut> outs;
     NF_CK(outs.ensure(R));
     const double tol = prm[0].solve_tol > 0 ? prm[0].solve_tol : 1e-10;
     const int max_inner = prm[0].solve_max_iter > 0 ? prm[0].solve_max_iter : 20000;
     tstart(KT_CG);
     NF_LAUNCH(k_cg<512>, R, 512, 0, st)(R, dab.p, rowp.p, col.p, val32.p, val64.p, diag32.p, diag64.p, chain64.p,
-                                 chain32.p, na, chains ? 1 : 0, bvec.p, xvec.p, cgred.p, cgbuf.p, tol, max_inner,
+                                 chain32.p, na, A.chains ? 1 : 0, bvec.p, xvec.p, cgred.p, cgbuf.p, tol, max_inner,
                                  outs.p);
     NF_CK(cudaGetLastError());
     tstop(KT_CG);
@@ -567,13 +581,11 @@ nf_status Engine::solve_graph(uint32_t n, const std::vector<uint32_t>& off, cons
     NF_CK(cudaGetLastError());
     std::vector<CgOut> ho(R);
     NF_CK(cudaMemcpyAsync(ho.data(), outs.p, sizeof(CgOut) * R, cudaMemcpyDeviceToHost, st));
-    NF_CK(cudaEventRecord(e1, st));
-    NF_CK(cudaEventSynchronize(e1));
+    NF_CK(cudaEventRecord(ev.b, st));
+    NF_CK(cudaEventSynchronize(ev.b));
     outs.release();
     float ms = 0;
-    NF_CK(cudaEventElapsedTime(&ms, e0, e1));
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
+    NF_CK(cudaEventElapsedTime(&ms, ev.a, ev.b));
     {
         double it = 0, ot = 0;
         for (int r = 0; r < R; ++r) { it += ho[r].inner; ot += ho[r].outer; }
@@ -588,7 +600,7 @@ nf_status Engine::solve_graph(uint32_t n, const std::vector<uint32_t>& off, cons
         S.outer_iters = ho[r].outer;
         S.inner_iters = ho[r].inner;
         S.n_nodes = nodes[r];
-        S.n_active = habase[r + 1] - habase[r];
+        S.n_active = A.habase[r + 1] - A.habase[r];
         S.percolating = S.n_active > 0;
         S.ms = ms;
         if (S.n_active > 0 && !(S.residual <= tol)) conv = false;

@@ -207,6 +207,46 @@ def internal_network(params, rods, ct):
     return out
 
 
+def _laplacian_solve(na, a, c, y, el, b, steps=6, x0=None):
+    """Solve (diag(el) + Laplacian of the edges (a, c, y)) x = b by sparse LU
+    with iterative refinement. The residual is formed in difference form,
+    el_i x_i + sum_j y_ij (x_i - x_j), which does not cancel when strong edges
+    (rod segments, 1e4-1e12 times a contact) join nearly equipotential nodes;
+    plain LU loses that many digits in its pivots. With x0 the solve is for
+    the deviation x = x0 - V of the solution V from x0: K x = K x0 - b, the
+    right-hand side formed in difference form; x is returned (V = x0 - x).
+    Returns (x, ||b - K V||)."""
+    import scipy.sparse as sp
+    import scipy.sparse.linalg as spl
+    diag = np.array(el, dtype=np.result_type(el, y))
+    np.add.at(diag, a, y)
+    np.add.at(diag, c, y)
+    K = sp.coo_matrix((np.concatenate([diag, -y, -y]),
+                       (np.concatenate([np.arange(na), a, c]), np.concatenate([np.arange(na), c, a]))),
+                      shape=(na, na)).tocsc()
+    lu = spl.splu(K)
+
+    def kmul(x):
+        kx = el * x
+        d = y * (x[a] - x[c])
+        np.add.at(kx, a, d)
+        np.add.at(kx, c, -d)
+        return kx
+    rhs = b if x0 is None else kmul(np.asarray(x0, diag.dtype)) - b  # K x0 - b
+    x = lu.solve(rhs)
+    r = rhs - kmul(x)
+    for _ in range(steps):
+        x = x + lu.solve(r)
+        r2 = rhs - kmul(x)
+        if not np.linalg.norm(r2) < np.linalg.norm(r):
+            r = r2
+            break
+        r = r2
+    _laplacian_solve.rhs_norm = float(np.linalg.norm(rhs))
+    _laplacian_solve.last_r = r
+    return x, float(np.linalg.norm(r))
+
+
 def solve_internal(net, ct):
     """G_eff of the node network (contact edges between nodes plus rod
     segments) by a direct sparse LU factorisation in FP64, as the reference's
@@ -214,10 +254,10 @@ def solve_internal(net, ct):
     MKL DSS): Norton electrodes (source 1 V, sink 0 V), unknowns only in
     components that touch both electrodes; outside them a component touching
     only the source sits at 1 V, any other at 0 V.
+    The LU solve is refined (_laplacian_solve).
     Returns (G_eff, node voltages, info) like solve()."""
     import scipy.sparse as sp
     import scipy.sparse.csgraph as csg
-    import scipy.sparse.linalg as spl
     n = len(net["node_rod"])
     I = np.concatenate([net["edge_i"], net["seg_i"]]).astype(np.int64)
     J = np.concatenate([net["edge_j"], net["seg_j"]]).astype(np.int64)
@@ -243,16 +283,9 @@ def solve_internal(net, ct):
     idx = -np.ones(n, np.int64)
     idx[act] = np.arange(na)
     e = rr & act[I]
-    a, c, g = idx[I[e]], idx[J[e]], G[e]
-    diag = s[act] + t[act]
-    np.add.at(diag, a, g)
-    np.add.at(diag, c, g)
-    K = sp.coo_matrix((np.concatenate([diag, -g, -g]),
-                       (np.concatenate([np.arange(na), a, c]), np.concatenate([np.arange(na), c, a]))),
-                      shape=(na, na)).tocsc()
     b = s[act]
-    x = spl.spsolve(K, b)
-    info["residual"] = float(np.linalg.norm(b - K @ x) / np.linalg.norm(b))
+    x, res = _laplacian_solve(na, idx[I[e]], idx[J[e]], G[e], s[act] + t[act], b)
+    info["residual"] = res / float(np.linalg.norm(b))
     v[act] = x
     return float(np.sum(b * (1.0 - x))), v, info
 
@@ -315,3 +348,151 @@ def adjoint(params, rods, ct, v):
     lib().nfo_adjoint(C.byref(p), _ptr(rods), n, len(arr[0]), *[_ptr(a) for a in arr], _ptr(img),
                       _ptr(np.ascontiguousarray(v, np.float64)), _ptr(g), C.byref(dl), C.byref(dg0))
     return g, dl.value, dg0.value
+
+
+# ---------------------------------------------------------------------------
+# AC admittance spectrum: the offline Kirchhoff tool's sweep
+# (tools/kirchhoff/kirchhoff.py:55-286) restated in Python 3 / numpy / scipy.
+# ---------------------------------------------------------------------------
+AC_DEFAULTS = dict(r_cnt=4.75e-3, l_cnt=1.5, phi_ev=3.5, eps_r=2.9, delta_min=0.34e-3, delta_tun=1.1e-3,
+                   delta_eff=50e-3, c_min=0.005, l_box=1.0, own_radii=0)
+
+
+def ac_scales(p):
+    """A, B, R0, C0, omega0, S_min, S_max of kirchhoff.py:66-88 (SI units)."""
+    from scipy import constants as K
+    p = dict(AC_DEFAULTS, **p)
+    rc = p["r_cnt"] * 1e-6
+    dmin = p["delta_min"] * 1e-6
+    smin = np.pi * rc * rc
+    smax = p["l_cnt"] * 1e-6 * 2 * rc
+    phi = p["phi_ev"] * K.eV
+    A = 1.0 / np.sqrt(2 * K.m_e * phi) * (K.h / K.e) ** 2
+    B = 4 * np.pi / K.h * np.sqrt(2 * K.m_e * phi)
+    R0 = A * np.exp(B * dmin) * dmin / smin
+    C0 = K.epsilon_0 * p["eps_r"] * smin / dmin
+    return dict(A=A, B=B, R0=R0, C0=C0, omega0=1.0 / (R0 * C0), smin=smin, smax=smax)
+
+
+def ac_admittances(net, p, rod_sigma=67.0, radii=None):
+    """Scaled (G, C) per contact and G per segment (kirchhoff.py:90-116,139-206).
+    radii: (a_I, a_J) per contact in um for own_radii=1 (a_J = 0 at electrodes)."""
+    p = dict(AC_DEFAULTS, **p)
+    s = ac_scales(p)
+    D = np.asarray(net["ct_d"], np.float64)
+    S = np.asarray(net["ct_s"], np.float64)
+    if p["own_radii"]:
+        d = D * 1e-6 - (radii[0] + radii[1]) * 1e-6
+    else:
+        d = D * 1e-6 - 2 * p["r_cnt"] * 1e-6
+    dmin = p["delta_min"] * 1e-6
+    d = np.where(d > dmin, d, dmin)
+    S = S * 1e-12
+    S = np.where(S > s["smin"], S, s["smin"])
+    S = np.where(S <= s["smax"], S, s["smax"])
+    keep = d < p["delta_eff"] * 1e-6
+    sr, dr = S / s["smin"], d / dmin
+    tun = d <= p["delta_tun"] * 1e-6
+    G = np.zeros(len(d))
+    G[tun] = 1.0 / (np.exp(s["B"] * (d[tun] - dmin)) * dr[tun] / sr[tun])
+    Cc = sr / dr
+    Cc = np.where(Cc < p["c_min"], 0.0, Cc)
+    G = np.where(keep, G, 0.0)
+    Cc = np.where(keep, Cc, 0.0)
+    a = np.asarray(net["seg_a"], np.float64)
+    L = np.asarray(net["seg_l"], np.float64)
+    Gs = rod_sigma * np.pi * a / L * s["R0"]
+    return G, Cc, Gs, s
+
+
+def ac_spectrum(net, freq, p=None, rod_sigma=67.0, radii=None):
+    """Complex current I, impedance columns and RMS per frequency; unknowns
+    are the nodes whose component (edges with G > 0 or C > 0) touches both
+    electrodes, solved by sparse LU per frequency (kirchhoff.py:224-286,
+    solver_type 0) with refinement (_laplacian_solve). The solve runs on
+    x = chi - V, chi = 1 on the resistive clusters (G > 0 edges) tied to the
+    source by a resistive contact and 0 elsewhere: where the resistive network
+    does not join the electrodes, the low-frequency current is ~1e-14 of the
+    electrode admittances and 1 - V near the source is below what V carries in
+    FP64; x carries it. I = sum_i b_i (1 - chi_i + x_i)."""
+    import scipy.sparse as sp
+    import scipy.sparse.csgraph as csg
+    p = dict(AC_DEFAULTS, **(p or {}))
+    G, Cc, Gs, s = ac_admittances(net, p, rod_sigma, radii)
+    n = int(net["n_nodes"])
+    I = np.concatenate([np.asarray(net["ct_i"], np.int64), np.asarray(net["seg_i"], np.int64)])
+    J = np.concatenate([np.asarray(net["ct_j"], np.int64), np.asarray(net["seg_j"], np.int64)])
+    EG = np.concatenate([G, Gs])
+    EC = np.concatenate([Cc, np.zeros(len(Gs))])
+    on = (EG > 0) | (EC > 0)
+    rr = (J < SNK_ELEC) & on
+    src, snk = (J == SRC_ELEC) & on, (J == SNK_ELEC) & on
+    A = sp.coo_matrix((np.ones(int(rr.sum())), (I[rr], J[rr])), shape=(n, n))
+    ncomp, lab = csg.connected_components(A, directed=False)
+    hs = np.zeros(ncomp, bool)
+    ht = np.zeros(ncomp, bool)
+    hs[lab[I[src]]] = True
+    ht[lab[I[snk]]] = True
+    act = (hs & ht)[lab]
+    na = int(act.sum())
+    idx = -np.ones(n, np.int64)
+    idx[act] = np.arange(na)
+    e = rr & act[I]
+    a, c = idx[I[e]], idx[J[e]]
+    # chi: resistive clusters with a resistive source contact
+    res = rr & (EG > 0)
+    Ar = sp.coo_matrix((np.ones(int(res.sum())), (I[res], J[res])), shape=(n, n))
+    _, labr = csg.connected_components(Ar, directed=False)
+    srcr = src & (EG > 0)
+    chi_all = np.isin(labr, np.unique(labr[I[srcr]])).astype(np.float64)
+    chi = chi_all[act]
+    out = {k: np.zeros(len(freq)) for k in ("i_re", "i_im", "z_re", "z_im", "rms", "residual", "i_err")}
+    out["converged"] = np.ones(len(freq), bool)
+    out["freq"] = np.asarray(freq, np.float64)
+    zs = s["R0"] * p["l_box"] * 1e-6
+    for fi, f in enumerate(out["freq"]):
+        w = 2 * np.pi * f / s["omega0"]
+        Y = EG + 1j * w * EC
+        if na == 0:
+            out["z_re"][fi] = out["z_im"][fi] = np.inf
+            continue
+        bs = np.zeros(na, complex)
+        bt = np.zeros(na, complex)
+        np.add.at(bs, idx[I[src & act[I]]], Y[src & act[I]])
+        np.add.at(bt, idx[I[snk & act[I]]], Y[snk & act[I]])
+        x, rms = _laplacian_solve(na, a, c, Y[e], bs + bt, bs, x0=chi.astype(complex))
+        cur = np.sum(bs * ((1.0 - chi) + x))  # 1 - V = 1 - chi + x
+        cn = _laplacian_solve.rhs_norm
+        out["residual"][fi] = rms / cn if cn > 0 else 0.0
+        out["converged"][fi] = out["residual"][fi] <= 1e-9
+        # first-order error of I: V^T r, V = chi - x, r the residual of x
+        out["i_err"][fi] = abs(np.sum((chi - x) * _laplacian_solve.last_r))
+        out["i_re"][fi], out["i_im"][fi] = cur.real, cur.imag
+        out["rms"][fi] = rms
+        zi = zs / cur
+        out["z_re"][fi], out["z_im"][fi] = zi.real, -zi.imag
+    out["n_active"] = na
+    out["scales"] = s
+    return out
+
+
+def read_kirchhoff_inputs(directory, names=("segment.La.dat", "internal.DS.dat", "source.DS.dat", "sink.DS.dat")):
+    """The tool's four input tables (kirchhoff.py:118-138): segments (I, J, L,
+    a), internal contacts (I, J, D, S), source / sink contacts with the node in
+    column 1. Returns a host network dict."""
+    seg, internal, src, snk = (os.path.join(directory, x) for x in names)
+
+    def table(path, cols):
+        arr = np.loadtxt(path, skiprows=1, usecols=cols, ndmin=2)
+        return arr.reshape(-1, len(cols))
+    sg = table(seg, (0, 1, 2, 3))
+    it = table(internal, (0, 1, 2, 3))
+    so = table(src, (1, 2, 3))
+    si = table(snk, (1, 2, 3))
+    ct_i = np.concatenate([it[:, 0], so[:, 0], si[:, 0]]).astype(np.uint32)
+    ct_j = np.concatenate([it[:, 1], np.full(len(so), SRC_ELEC), np.full(len(si), SNK_ELEC)]).astype(np.uint32)
+    nodes = np.concatenate([sg[:, 0], sg[:, 1], it[:, 0], it[:, 1], so[:, 0], si[:, 0]])
+    return dict(n_nodes=int(nodes.max()) + 1 if len(nodes) else 0,
+                seg_i=sg[:, 0].astype(np.uint32), seg_j=sg[:, 1].astype(np.uint32), seg_l=sg[:, 2], seg_a=sg[:, 3],
+                ct_i=ct_i, ct_j=ct_j, ct_d=np.concatenate([it[:, 2], so[:, 1], si[:, 1]]),
+                ct_s=np.concatenate([it[:, 3], so[:, 2], si[:, 2]]))
