@@ -316,6 +316,25 @@ nf_status nf_get_internal_network(nf_handle *h, nf_internal_net *out);
  * in dir (save_coo layouts, src/conductivity.cu:881-930). */
 nf_status nf_write_internal_coo(nf_handle *h, const char *dir);
 
+/* ---- dead-end pruning: the `reduce` verb (src/NanoFiller.cpp:71-91) ---- */
+/* Replaces the reference's reduce loop (reduce(), src/conductivity.cu:79-138;
+ * contact_count_kernel_full / reductKernel, inc/conductKernels.h:39-162):
+ * contacts within stat_dist_lim are counted per rod without screening
+ * (electrode contacts count, electrodes are never removed), every rod with
+ * fewer than min_contacts goes, and the count repeats until nothing goes.
+ * The handle keeps the surviving rods in their order (stream indices kept);
+ * contacts and solutions are dropped. */
+typedef struct nf_reduce_stats {
+    uint64_t rods_before;
+    uint64_t rods_after;
+    uint64_t contacts;      /* unscreened contacts of the first count */
+    int32_t rounds;         /* passes that removed rods */
+    int32_t min_contacts;
+    double ms;
+} nf_reduce_stats;
+
+nf_status nf_reduce(nf_handle *h, int32_t min_contacts, nf_reduce_stats *stats);
+
 /* ---- AC admittance spectrum (tools/kirchhoff/kirchhoff.py) ------------ */
 /* The offline Kirchhoff tool's impedance sweep, restated: every edge gets the
  * scaled admittance Y = G + i (omega / omega0) C, with

@@ -16,7 +16,7 @@ from . import configs  # noqa: F401
 from ._abi import (LIB_PATH, SNK_ELEC, SRC_ELEC, STATUS, NfBatchResult, NfBatchStats,  # noqa: F401
                    NfContactList, NfContactStats, NfGenStats, NfParams, NfRods, NfSolveStats,
                    NfInternalNet, NfInternalStats, NfStateHeader, NfTuneResult, NfAcNet, NfAcParams,
-                   NfAcPoint, NfAcStats, load)
+                   NfAcPoint, NfAcStats, NfReduceStats, load)
 
 __all__ = ["Simulation", "NanoFillerError", "make_params", "params_from_file", "batch_run",
            "target_count", "kernel_launches", "configs", "SRC_ELEC", "SNK_ELEC", "ac_params", "ac_frequencies",
@@ -270,6 +270,13 @@ class Simulation:
         _check(self._L.nf_stream_candidates_noalloc(self._h, k0, n, *ptrs), self._h,
                "nf_stream_candidates_noalloc")
         return out.T.copy()
+
+    def reduce(self, min_contacts=2):
+        """Dead-end pruning (nf_reduce): keep the rods with at least
+        min_contacts unscreened contacts, repeatedly; electrodes stay."""
+        st = NfReduceStats()
+        _check(self._L.nf_reduce(self._h, min_contacts, C.byref(st)), self._h, "nf_reduce")
+        return {k: getattr(st, k) for k, _ in st._fields_}
 
     def ac_spectrum(self, freq, net=None, check=True, **ac):
         """AC admittance spectrum (nf_ac_spectrum) at the frequencies freq

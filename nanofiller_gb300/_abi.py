@@ -93,6 +93,11 @@ class NfInternalNet(C.Structure):
                 ("edge_j", C.c_void_p)]
 
 
+class NfReduceStats(C.Structure):
+    _fields_ = [("rods_before", C.c_uint64), ("rods_after", C.c_uint64), ("contacts", C.c_uint64),
+                ("rounds", C.c_int32), ("min_contacts", C.c_int32), ("ms", C.c_double)]
+
+
 class NfAcParams(C.Structure):
     _fields_ = [("r_cnt", C.c_double), ("l_cnt", C.c_double), ("phi_ev", C.c_double), ("eps_r", C.c_double),
                 ("delta_min", C.c_double), ("delta_tun", C.c_double), ("delta_eff", C.c_double),
@@ -171,6 +176,7 @@ SIGNATURES = {
     "nf_internal_network": (_st, [_H, _P(NfInternalStats)]),
     "nf_get_internal_network": (_st, [_H, _P(NfInternalNet)]),
     "nf_write_internal_coo": (_st, [_H, C.c_char_p]),
+    "nf_reduce": (_st, [_H, C.c_int32, _P(NfReduceStats)]),
     "nf_ac_params_default": (None, [_P(NfAcParams)]),
     "nf_ac_frequencies": (C.c_size_t, [C.c_double, C.c_int, C.c_int, C.c_void_p, C.c_size_t]),
     "nf_ac_spectrum": (_st, [_H, _P(NfAcNet), _P(NfAcParams), C.c_void_p, C.c_size_t, C.c_void_p,

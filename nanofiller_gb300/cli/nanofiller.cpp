@@ -17,7 +17,10 @@
 //                         the contact points, rod segments between them, written
 //                         as Nodes.tbl.dat, segment.LA.coo, internal.DS.coo,
 //                         sink.DS.coo, source.DS.coo, then the node-network solve
-// The reference's other verbs (plot, reduce, stat_nematic, stat_phitheta,
+//   reduce <dir>          dead-end pruning: rods with fewer than 2 contacts
+//                         within STAT_DIST_LIM (unscreened, electrodes count)
+//                         are removed until none is; reduced.bin with WRT_BIN 1
+// The reference's other verbs (plot, stat_nematic, stat_phitheta,
 // stat_mutangle, stat_exclsurf, stat_contacts, stat_vdw, write_ort, write_lmp)
 // are not part of this path: they are reported and the program exits with
 // status 2 before any work. Every error exits non-zero with the library's
@@ -49,7 +52,7 @@ struct Verb {
 };
 
 bool not_on_path(const std::string& v) {
-    static const char* other[] = {"plot", "reduce", "stat_nematic", "stat_phitheta", "stat_mutangle",
+    static const char* other[] = {"plot", "stat_nematic", "stat_phitheta", "stat_mutangle",
                                   "stat_exclsurf", "stat_contacts", "stat_vdw", "write_ort", "write_lmp"};
     for (const char* o : other)
         if (v == o) return true;
@@ -81,7 +84,7 @@ int main(int argc, char** argv) {
         std::string v = argv[a];
         if (v == "write_vtk") {
             verbs.push_back({v, 0, false});
-        } else if (v == "expand" || v == "stat_conduct") {
+        } else if (v == "expand" || v == "stat_conduct" || v == "reduce") {
             int d = 0;
             if (a + 1 >= argc || !parse_dir(argv[a + 1], &d)) {
                 std::fprintf(stderr, "nanofiller: %s needs a direction 1, 2 or 4\n", v.c_str());
@@ -156,6 +159,21 @@ int main(int argc, char** argv) {
         if (v.name == "write_vtk") {
             s = nf_write_vtk(h, "output.vtk");
             if (s != NF_OK) { rc = fail(h, s, "write_vtk"); goto done; }
+        } else if (v.name == "reduce") {
+            // src/NanoFiller.cpp:71-91: min_cont = 2, then reduced.bin
+            const int min_cont = 2;
+            std::printf("Eliminating inclusions with less then %d contacts up to %f um:\n", min_cont,
+                        p.stat_dist_lim);
+            nf_reduce_stats rs;
+            s = nf_reduce(h, min_cont, &rs);
+            if (s != NF_OK) { rc = fail(h, s, "reduce"); goto done; }
+            std::printf("Inclusions remained: %llu of %llu after %d pass(es), %.3f ms\n",
+                        (unsigned long long)rs.rods_after, (unsigned long long)rs.rods_before, rs.rounds + 1,
+                        rs.ms);
+            if (p.wrt_bin) {
+                s = nf_write_state_bin(h, "reduced.bin");
+                if (s != NF_OK) { rc = fail(h, s, "reduced.bin"); goto done; }
+            }
         } else if (v.name == "stat_conduct") {
             nf_contact_stats c;
             s = nf_contacts(h, &c);

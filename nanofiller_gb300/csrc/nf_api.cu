@@ -590,6 +590,15 @@ nf_status nf_write_internal_coo(nf_handle* h, const char* dir) {
     return NF_OK;
 }
 
+nf_status nf_reduce(nf_handle* h, int32_t min_contacts, nf_reduce_stats* stats) {
+    if (!h) return NF_ERR_PARAM;
+    if (min_contacts < 0) return fail(h, NF_ERR_PARAM, "min_contacts must be >= 0");
+    nf_reduce_stats st{};
+    nf_status s = h->E.prune(min_contacts, &st);
+    if (stats) *stats = st;
+    return s;
+}
+
 void nf_ac_params_default(nf_ac_params* p) {
     if (!p) return;
     *p = nf_ac_params{};

@@ -201,6 +201,9 @@ struct Engine {
     };
     nf_status assemble(uint32_t n, const std::vector<uint32_t>& off, uint32_t mc, uint32_t m, const uint32_t* eI,
                        const uint32_t* eJ, const double* eG, const double* eC, Asm* out);
+    // Dead-end pruning (the reference's reduce): keep the min_cont-core of the
+    // unscreened contact graph, electrodes kept.
+    nf_status prune(int min_cont, nf_reduce_stats* out);
     // AC admittance spectrum of the handle's network (net == nullptr) or of a
     // host-given network.
     nf_status ac_spectrum(const nf_ac_net* net, const nf_ac_params& p, const double* freq, size_t nfreq,

@@ -496,3 +496,26 @@ def read_kirchhoff_inputs(directory, names=("segment.La.dat", "internal.DS.dat",
                 seg_i=sg[:, 0].astype(np.uint32), seg_j=sg[:, 1].astype(np.uint32), seg_l=sg[:, 2], seg_a=sg[:, 3],
                 ct_i=ct_i, ct_j=ct_j, ct_d=np.concatenate([it[:, 2], so[:, 1], si[:, 1]]),
                 ct_s=np.concatenate([it[:, 3], so[:, 2], si[:, 2]]))
+
+
+def prune(n_rods, ct, min_contacts=2):
+    """Dead-end pruning of the reference's reduce verb (src/NanoFiller.cpp:71-91,
+    src/conductivity.cu:79-138, inc/conductKernels.h:39-162): contacts per
+    rod among the rods still present (an electrode contact counts, electrodes
+    stay), every rod below min_contacts removed in the same pass, passes
+    repeated until one removes nothing. Returns (keep mask, passes that
+    removed rods)."""
+    I = np.asarray(ct["I"], np.int64)
+    J = np.asarray(ct["J"], np.int64)
+    alive = np.ones(n_rods, bool)
+    elec = J >= SNK_ELEC
+    Jr = np.where(elec, 0, J)
+    rounds = 0
+    while True:
+        on = alive[I] & (elec | alive[Jr])
+        deg = np.bincount(I[on], minlength=n_rods) + np.bincount(Jr[on & ~elec], minlength=n_rods)
+        drop = alive & (deg < min_contacts)
+        if not drop.any():
+            return alive, rounds
+        alive &= ~drop
+        rounds += 1
