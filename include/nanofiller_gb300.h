@@ -335,6 +335,44 @@ typedef struct nf_reduce_stats {
 
 nf_status nf_reduce(nf_handle *h, int32_t min_contacts, nf_reduce_stats *stats);
 
+/* ---- statistics and writers (src/NanoFiller.cpp:92-147) -------------- */
+/* stat_nematic (get_nematic_order, src/statistics_collection.cu:589-638):
+ * S = sum P2(c . axis) / N over the rods (unit axis; the verb uses z). */
+nf_status nf_stat_nematic(nf_handle *h, const double axis[3], double *S);
+/* stat_phitheta (collect_PhiTheta_distr, src/statistics_collection.cu:
+ * 769-863): histogram of rod directions, bins_phi x bins_theta over
+ * [0, pi] x [0, pi], phi fastest; the verb uses 32 x 32 and writes rho.dat. */
+nf_status nf_stat_phitheta(nf_handle *h, int32_t bins_phi, int32_t bins_theta, uint64_t *hist);
+/* stat_contacts and stat_mutangle (collect_CntctPerInc :463-586,
+ * collect_1D_statDistr_weightedFloat :640-767): over the unscreened
+ * rod-rod contacts within STAT_DIST_LIM, contacts per rod (both ends) and the
+ * histogram of mutual angles acos|c_i . c_j| of the pairs whose closest
+ * points are interior to both rods, bins of (pi + TOL) / 2 / bins; the verb
+ * uses 32 bins and writes gamma.dat. If the handle's contacts are screened
+ * ones, an unscreened sweep replaces them and they are dropped afterwards.
+ * hist (bins) and per_rod (capacity >= rods) may be NULL. */
+typedef struct nf_pair_stats {
+    uint64_t rods;
+    uint64_t pairs;          /* rod-rod contacts */
+    uint64_t contacts_total; /* sum over rods of their contacts (2 x pairs) */
+    uint64_t angle_pairs;    /* pairs in the mutual-angle histogram */
+    uint32_t max_per_rod;
+    uint32_t pad;
+    double mean_per_rod;
+} nf_pair_stats;
+nf_status nf_stat_pairs(nf_handle *h, int32_t bins, uint64_t *hist, uint32_t *per_rod, size_t capacity,
+                        nf_pair_stats *stats);
+/* write_ort (write_CNT_ORTvtk, src/IO.cpp:77-97): rod directions as VTK points. */
+nf_status nf_write_ort_vtk(nf_handle *h, const char *path);
+/* write_lmp (write_CNTlmp, src/IO.cpp:99-146): LAMMPS data file of
+ * ellipsoids (length l + 2a, width 2a, quaternion from x to the rod axis);
+ * density per particle as the reference's simPrms density (4.579). */
+nf_status nf_write_lmp(nf_handle *h, const char *path, double density);
+/* The verbs' histogram files: rho.dat (write_Mathematica2Di, src/IO.cpp) and
+ * gamma.dat (write_mat, src/IO.cpp). Host-only. */
+nf_status nf_format_write_rho(const char *path, int32_t bins_phi, int32_t bins_theta, const uint64_t *hist);
+nf_status nf_format_write_gamma(const char *path, int32_t bins, const uint64_t *hist);
+
 /* ---- AC admittance spectrum (tools/kirchhoff/kirchhoff.py) ------------ */
 /* The offline Kirchhoff tool's impedance sweep, restated: every edge gets the
  * scaled admittance Y = G + i (omega / omega0) C, with

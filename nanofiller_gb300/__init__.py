@@ -16,7 +16,7 @@ from . import configs  # noqa: F401
 from ._abi import (LIB_PATH, SNK_ELEC, SRC_ELEC, STATUS, NfBatchResult, NfBatchStats,  # noqa: F401
                    NfContactList, NfContactStats, NfGenStats, NfParams, NfRods, NfSolveStats,
                    NfInternalNet, NfInternalStats, NfStateHeader, NfTuneResult, NfAcNet, NfAcParams,
-                   NfAcPoint, NfAcStats, NfReduceStats, load)
+                   NfAcPoint, NfAcStats, NfPairStats, NfReduceStats, load)
 
 __all__ = ["Simulation", "NanoFillerError", "make_params", "params_from_file", "batch_run",
            "target_count", "kernel_launches", "configs", "SRC_ELEC", "SNK_ELEC", "ac_params", "ac_frequencies",
@@ -278,6 +278,42 @@ class Simulation:
         _check(self._L.nf_reduce(self._h, min_contacts, C.byref(st)), self._h, "nf_reduce")
         return {k: getattr(st, k) for k, _ in st._fields_}
 
+    # statistics (the reference's stat_* verbs)
+    def nematic(self, axis=(0.0, 0.0, 1.0)):
+        """Nematic order parameter S = <P2(c . axis)> (nf_stat_nematic)."""
+        ax = np.ascontiguousarray(axis, np.float64)
+        S = C.c_double()
+        _check(self._L.nf_stat_nematic(self._h, ax.ctypes.data_as(C.c_void_p), C.byref(S)), self._h,
+               "nf_stat_nematic")
+        return S.value
+
+    def phitheta(self, bins_phi=32, bins_theta=32):
+        """Histogram of rod directions, shape (bins_theta, bins_phi) (nf_stat_phitheta)."""
+        h = np.zeros((bins_theta, bins_phi), np.uint64)
+        _check(self._L.nf_stat_phitheta(self._h, bins_phi, bins_theta, h.ctypes.data_as(C.c_void_p)), self._h,
+               "nf_stat_phitheta")
+        return h
+
+    def pair_stats(self, bins=32):
+        """Contacts per rod and the mutual-angle histogram over the unscreened
+        rod-rod contacts (nf_stat_pairs)."""
+        n = self.n_rods()
+        h = np.zeros(bins, np.uint64)
+        per = np.zeros(max(n, 1), np.uint32)
+        st = NfPairStats()
+        _check(self._L.nf_stat_pairs(self._h, bins, h.ctypes.data_as(C.c_void_p), per.ctypes.data_as(C.c_void_p),
+                                     len(per), C.byref(st)), self._h, "nf_stat_pairs")
+        out = {k: getattr(st, k) for k, _ in st._fields_}
+        out["hist"] = h
+        out["per_rod"] = per[:n]
+        return out
+
+    def write_ort(self, path):
+        _check(self._L.nf_write_ort_vtk(self._h, str(path).encode()), self._h, "nf_write_ort_vtk")
+
+    def write_lmp(self, path, density=4.579):
+        _check(self._L.nf_write_lmp(self._h, str(path).encode(), density), self._h, "nf_write_lmp")
+
     def ac_spectrum(self, freq, net=None, check=True, **ac):
         """AC admittance spectrum (nf_ac_spectrum) at the frequencies freq
         (Hz) of the handle's network (net=None: the intra-rod network after
@@ -383,3 +419,17 @@ def write_kirchhoff_log(path, spec, elapsed=None):
         for i in range(n):
             f.write("{:>10.3e}\t{:>10.3e}\t{:>10.3e}\t{:>d}\t{:>10.3e}\t{:>10.3f}\n".format(
                 spec["freq"][i], spec["z_re"][i], spec["z_im"][i], int(spec["converged"][i]), spec["rms"][i], el[i]))
+
+
+def write_rho(path, hist):
+    """rho.dat of the stat_phitheta verb; hist shaped (bins_theta, bins_phi)."""
+    h = np.ascontiguousarray(hist, np.uint64)
+    _check(load().nf_format_write_rho(str(path).encode(), h.shape[1], h.shape[0], h.ctypes.data_as(C.c_void_p)),
+           what="nf_format_write_rho")
+
+
+def write_gamma(path, hist):
+    """gamma.dat of the stat_mutangle verb."""
+    h = np.ascontiguousarray(hist, np.uint64)
+    _check(load().nf_format_write_gamma(str(path).encode(), len(h), h.ctypes.data_as(C.c_void_p)),
+           what="nf_format_write_gamma")

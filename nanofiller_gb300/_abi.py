@@ -98,6 +98,12 @@ class NfReduceStats(C.Structure):
                 ("rounds", C.c_int32), ("min_contacts", C.c_int32), ("ms", C.c_double)]
 
 
+class NfPairStats(C.Structure):
+    _fields_ = [("rods", C.c_uint64), ("pairs", C.c_uint64), ("contacts_total", C.c_uint64),
+                ("angle_pairs", C.c_uint64), ("max_per_rod", C.c_uint32), ("pad", C.c_uint32),
+                ("mean_per_rod", C.c_double)]
+
+
 class NfAcParams(C.Structure):
     _fields_ = [("r_cnt", C.c_double), ("l_cnt", C.c_double), ("phi_ev", C.c_double), ("eps_r", C.c_double),
                 ("delta_min", C.c_double), ("delta_tun", C.c_double), ("delta_eff", C.c_double),
@@ -177,6 +183,13 @@ SIGNATURES = {
     "nf_get_internal_network": (_st, [_H, _P(NfInternalNet)]),
     "nf_write_internal_coo": (_st, [_H, C.c_char_p]),
     "nf_reduce": (_st, [_H, C.c_int32, _P(NfReduceStats)]),
+    "nf_stat_nematic": (_st, [_H, C.c_void_p, _P(C.c_double)]),
+    "nf_stat_phitheta": (_st, [_H, C.c_int32, C.c_int32, C.c_void_p]),
+    "nf_stat_pairs": (_st, [_H, C.c_int32, C.c_void_p, C.c_void_p, C.c_size_t, _P(NfPairStats)]),
+    "nf_write_ort_vtk": (_st, [_H, C.c_char_p]),
+    "nf_write_lmp": (_st, [_H, C.c_char_p, C.c_double]),
+    "nf_format_write_rho": (_st, [C.c_char_p, C.c_int32, C.c_int32, C.c_void_p]),
+    "nf_format_write_gamma": (_st, [C.c_char_p, C.c_int32, C.c_void_p]),
     "nf_ac_params_default": (None, [_P(NfAcParams)]),
     "nf_ac_frequencies": (C.c_size_t, [C.c_double, C.c_int, C.c_int, C.c_void_p, C.c_size_t]),
     "nf_ac_spectrum": (_st, [_H, _P(NfAcNet), _P(NfAcParams), C.c_void_p, C.c_size_t, C.c_void_p,

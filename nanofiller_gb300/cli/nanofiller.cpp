@@ -20,9 +20,15 @@
 //   reduce <dir>          dead-end pruning: rods with fewer than 2 contacts
 //                         within STAT_DIST_LIM (unscreened, electrodes count)
 //                         are removed until none is; reduced.bin with WRT_BIN 1
-// The reference's other verbs (plot, stat_nematic, stat_phitheta,
-// stat_mutangle, stat_exclsurf, stat_contacts, stat_vdw, write_ort, write_lmp)
-// are not part of this path: they are reported and the program exits with
+//   stat_nematic          nematic order parameter about z, printed
+//   stat_phitheta         32 x 32 histogram of rod directions, rho.dat
+//   stat_mutangle         32-bin histogram of mutual angles of contacting rods
+//                         (closest points interior to both), gamma.dat
+//   stat_contacts         contacts per rod within STAT_DIST_LIM: total, mean, max
+//   write_ort             rod directions as VTK points, orient.vtk
+//   write_lmp             LAMMPS ellipsoid data, output.lmp.data
+// The reference's other verbs (plot, stat_exclsurf, stat_vdw) are not part of
+// this path: they are reported and the program exits with
 // status 2 before any work. Every error exits non-zero with the library's
 // message.
 #include <cmath>
@@ -52,8 +58,7 @@ struct Verb {
 };
 
 bool not_on_path(const std::string& v) {
-    static const char* other[] = {"plot", "stat_nematic", "stat_phitheta", "stat_mutangle",
-                                  "stat_exclsurf", "stat_contacts", "stat_vdw", "write_ort", "write_lmp"};
+    static const char* other[] = {"plot", "stat_exclsurf", "stat_vdw"};
     for (const char* o : other)
         if (v == o) return true;
     return false;
@@ -82,7 +87,8 @@ int main(int argc, char** argv) {
     int field_dir = 0;
     for (int a = generate ? 3 : 2; a < argc; ++a) {
         std::string v = argv[a];
-        if (v == "write_vtk") {
+        if (v == "write_vtk" || v == "stat_nematic" || v == "stat_phitheta" || v == "stat_mutangle" ||
+            v == "stat_contacts" || v == "write_ort" || v == "write_lmp") {
             verbs.push_back({v, 0, false});
         } else if (v == "expand" || v == "stat_conduct" || v == "reduce") {
             int d = 0;
@@ -159,6 +165,38 @@ int main(int argc, char** argv) {
         if (v.name == "write_vtk") {
             s = nf_write_vtk(h, "output.vtk");
             if (s != NF_OK) { rc = fail(h, s, "write_vtk"); goto done; }
+        } else if (v.name == "stat_nematic") {
+            const double z[3] = {0.0, 0.0, 1.0};
+            double S = 0;
+            s = nf_stat_nematic(h, z, &S);
+            if (s != NF_OK) { rc = fail(h, s, "stat_nematic"); goto done; }
+            std::printf("Estimated nematic order parameter: %f\n", S);
+        } else if (v.name == "stat_phitheta") {
+            std::vector<uint64_t> hist(32 * 32);
+            s = nf_stat_phitheta(h, 32, 32, hist.data());
+            if (s == NF_OK) s = nf_format_write_rho("rho.dat", 32, 32, hist.data());
+            if (s != NF_OK) { rc = fail(h, s, "stat_phitheta"); goto done; }
+            std::printf("file rho.dat created!\n");
+        } else if (v.name == "stat_mutangle" || v.name == "stat_contacts") {
+            std::vector<uint64_t> hist(32);
+            nf_pair_stats ps;
+            s = nf_stat_pairs(h, 32, hist.data(), nullptr, 0, &ps);
+            if (s != NF_OK) { rc = fail(h, s, v.name.c_str()); goto done; }
+            if (v.name == "stat_mutangle") {
+                s = nf_format_write_gamma("gamma.dat", 32, hist.data());
+                if (s != NF_OK) { rc = fail(h, s, "gamma.dat"); goto done; }
+                std::printf("accumulated counts %llu\n", (unsigned long long)ps.angle_pairs);
+            } else {
+                std::printf(" Total number of contacts per inclusion: %llu / %llu = %f \n",
+                            (unsigned long long)ps.contacts_total, (unsigned long long)ps.rods, ps.mean_per_rod);
+                std::printf("Maximum number of contacts per inclusion: %u \n", ps.max_per_rod);
+            }
+        } else if (v.name == "write_ort") {
+            s = nf_write_ort_vtk(h, "orient.vtk");
+            if (s != NF_OK) { rc = fail(h, s, "write_ort"); goto done; }
+        } else if (v.name == "write_lmp") {
+            s = nf_write_lmp(h, "output.lmp.data", 4.579);  // simPrms density (src/simPrms.cpp:27)
+            if (s != NF_OK) { rc = fail(h, s, "write_lmp"); goto done; }
         } else if (v.name == "reduce") {
             // src/NanoFiller.cpp:71-91: min_cont = 2, then reduced.bin
             const int min_cont = 2;

@@ -599,6 +599,112 @@ nf_status nf_reduce(nf_handle* h, int32_t min_contacts, nf_reduce_stats* stats) 
     return s;
 }
 
+nf_status nf_stat_nematic(nf_handle* h, const double axis[3], double* S) {
+    if (!h || !axis || !S) return NF_ERR_PARAM;
+    return h->E.stat_nematic(axis, S);
+}
+
+nf_status nf_stat_phitheta(nf_handle* h, int32_t bins_phi, int32_t bins_theta, uint64_t* hist) {
+    if (!h || !hist) return NF_ERR_PARAM;
+    return h->E.stat_phitheta(bins_phi, bins_theta, hist);
+}
+
+nf_status nf_stat_pairs(nf_handle* h, int32_t bins, uint64_t* hist, uint32_t* per_rod, size_t capacity,
+                        nf_pair_stats* stats) {
+    if (!h) return NF_ERR_PARAM;
+    return h->E.stat_pairs(bins, hist, per_rod, capacity, stats);
+}
+
+namespace {
+// Rods of realisation 0 on the host.
+nf_status host_rods(nf_handle* h, std::vector<float>* f) {
+    nf_rods r{};
+    nf_status s = nf_get_rods(h, &r);
+    if (s != NF_OK && s != NF_ERR_CAPACITY) return s;
+    const size_t n = r.count;
+    for (int k = 0; k < 8; ++k) f[k].assign(n, 0.f);
+    r.capacity = n;
+    r.x = f[0].data(); r.y = f[1].data(); r.z = f[2].data();
+    r.cx = f[3].data(); r.cy = f[4].data(); r.cz = f[5].data();
+    r.l = f[6].data(); r.a = f[7].data();
+    return nf_get_rods(h, &r);
+}
+}  // namespace
+
+nf_status nf_write_ort_vtk(nf_handle* h, const char* path) {
+    if (!h || !path) return NF_ERR_PARAM;
+    std::vector<float> f[8];
+    nf_status s = host_rods(h, f);
+    if (s != NF_OK) return s;
+    std::ofstream o(path, std::ios::out | std::ios::trunc);
+    if (!o) return fail(h, NF_ERR_IO, path);
+    const size_t n = f[0].size();
+    o << "# vtk DataFile Version 2.0" << std::endl << "CUDA generated CNTs" << std::endl << "ASCII" << std::endl
+      << "DATASET UNSTRUCTURED_GRID" << std::endl << "POINTS " << n << " float" << std::endl;
+    for (size_t i = 0; i < n; ++i)
+        o << std::setw(15) << std::setprecision(6) << f[3][i] << std::setw(15) << std::setprecision(6) << f[4][i]
+          << std::setw(15) << std::setprecision(6) << f[5][i] << std::endl;
+    return o.good() ? NF_OK : fail(h, NF_ERR_IO, path);
+}
+
+nf_status nf_write_lmp(nf_handle* h, const char* path, double density) {
+    if (!h || !path) return NF_ERR_PARAM;
+    std::vector<float> f[8];
+    nf_status s = host_rods(h, f);
+    if (s != NF_OK) return s;
+    std::ofstream o(path, std::ios::out | std::ios::trunc);
+    if (!o) return fail(h, NF_ERR_IO, path);
+    const size_t n = f[0].size();
+    const float* box = h->E.prm[0].box;
+    o << "CUDA generated aspherical particles" << std::endl << std::endl << n << " atoms" << std::endl
+      << 1 << " atom types" << std::endl << n << " ellipsoids" << std::endl << std::endl
+      << 0.0f << ' ' << box[0] << " xlo xhi" << std::endl << 0.0f << ' ' << box[1] << " ylo yhi" << std::endl
+      << 0.0f << ' ' << box[2] << " zlo zhi" << std::endl << std::endl << "Atoms" << std::endl << std::endl;
+    for (size_t i = 0; i < n; ++i)
+        o << i + 1 << ' ' << 1 << ' ' << 1 << ' ' << (float)density << std::setw(12) << std::setprecision(6)
+          << f[0][i] << std::setw(12) << std::setprecision(6) << f[1][i] << std::setw(12) << std::setprecision(6)
+          << f[2][i] << std::endl;
+    o << std::endl << "Ellipsoids" << std::endl << std::endl;
+    // quaternion of the rotation from x to c: axis (0, -cz, cy), angle acos(cx)
+    for (size_t i = 0; i < n; ++i) {
+        const float cx = f[3][i], cy = f[4][i], cz = f[5][i], l = f[6][i], a = f[7][i];
+        const float sh = sqrtf((1 - cx) / 2);
+        o << i + 1 << std::setw(12) << std::setprecision(6) << l + 2 * a << std::setw(12) << std::setprecision(6)
+          << 2 * a << std::setw(12) << std::setprecision(6) << 2 * a << std::setw(15) << std::setprecision(6)
+          << sqrtf((1 + cx) / 2) << std::setw(15) << std::setprecision(6) << 0.0f << std::setw(15)
+          << std::setprecision(6) << -cz * sh << std::setw(15) << std::setprecision(6) << +cy * sh << std::endl;
+    }
+    return o.good() ? NF_OK : fail(h, NF_ERR_IO, path);
+}
+
+nf_status nf_format_write_rho(const char* path, int32_t bx, int32_t by, const uint64_t* hist) {
+    if (!path || !hist || bx <= 0 || by <= 0) return NF_ERR_PARAM;
+    std::ofstream o(path, std::ios::out | std::ios::trunc);
+    if (!o) return NF_ERR_IO;
+    o << "rho = {";
+    for (int j = 0; j < by; ++j) {
+        o << "\t{";
+        for (int i = 0; i < bx; ++i) {
+            o << std::setw(12) << hist[i + (size_t)j * bx];
+            if (i != bx - 1) o << ",";
+        }
+        o << "}";
+        if (j != by - 1) o << "," << std::endl << "\t";
+    }
+    o << "}";
+    return o.good() ? NF_OK : NF_ERR_IO;
+}
+
+nf_status nf_format_write_gamma(const char* path, int32_t bins, const uint64_t* hist) {
+    if (!path || !hist || bins <= 0) return NF_ERR_PARAM;
+    std::ofstream o(path, std::ios::out | std::ios::trunc);
+    if (!o) return NF_ERR_IO;
+    o << "gamma={\t";
+    for (int i = 0; i < bins - 1; ++i) o << std::setw(10) << std::setprecision(7) << (double)hist[i] << "," << std::endl;
+    o << std::setw(10) << std::setprecision(7) << (double)hist[bins - 1] << "\t}" << std::endl;
+    return o.good() ? NF_OK : NF_ERR_IO;
+}
+
 void nf_ac_params_default(nf_ac_params* p) {
     if (!p) return;
     *p = nf_ac_params{};

@@ -736,6 +736,7 @@ nf_status Engine::contacts() {
     cst.fp32_would_flip = hk[C_CT_FLIPS];
     cst.ms = ms;
     contacts_valid = true;
+    contacts_screened = prm[0].screening != 0;
     solve_valid = false;
     int_valid = false;
     return NF_OK;

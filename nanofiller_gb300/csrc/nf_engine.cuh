@@ -156,6 +156,7 @@ struct Engine {
     std::vector<uint64_t> ct_off;  // per realisation prefix of final contacts (host)
     std::vector<uint64_t> ct_int, ct_snk, ct_src, ct_scr;
     bool contacts_valid = false;
+    bool contacts_screened = false;  // the current list had screened contacts removed
     DBuf<uint32_t> eflag;
     // virtual rods of the screening test: FP32 copies for the filter, FP64
     // record (x,y,z,cx,cy,cz,l,a, wrap shift x,y,z), cell binning
@@ -201,6 +202,13 @@ struct Engine {
     };
     nf_status assemble(uint32_t n, const std::vector<uint32_t>& off, uint32_t mc, uint32_t m, const uint32_t* eI,
                        const uint32_t* eJ, const double* eG, const double* eC, Asm* out);
+    // Unscreened contact list for the statistics (the reference counts every
+    // pair within the cutoff); *recomputed tells whether the handle's list
+    // was replaced.
+    nf_status unscreened_contacts(bool* recomputed);
+    nf_status stat_nematic(const double axis[3], double* S);
+    nf_status stat_phitheta(int bins_phi, int bins_theta, uint64_t* hist);
+    nf_status stat_pairs(int bins, uint64_t* hist, uint32_t* per_rod, size_t capacity, nf_pair_stats* out);
     // Dead-end pruning (the reference's reduce): keep the min_cont-core of the
     // unscreened contact graph, electrodes kept.
     nf_status prune(int min_cont, nf_reduce_stats* out);

@@ -519,3 +519,62 @@ def prune(n_rods, ct, min_contacts=2):
             return alive, rounds
         alive &= ~drop
         rounds += 1
+
+
+# ---------------------------------------------------------------------------
+# Statistics of the stat_* verbs (src/statistics_collection.cu), restated.
+# ---------------------------------------------------------------------------
+def nematic(rods, axis=(0.0, 0.0, 1.0)):
+    """sum P2(c . n) / N, rods with a direction component <= -1 + 1e-6 left out
+    of the sum (nematic_func, statistics_collection.cu:589-614)."""
+    n = np.asarray(axis, np.float64)
+    n = n / np.linalg.norm(n)
+    c = np.stack([rods["cx"], rods["cy"], rods["cz"]], 1)
+    lim = np.float32(-1.0) + np.float32(1e-6)
+    ok = np.all(c > lim, axis=1)
+    ct = c.astype(np.float64) @ n
+    return float(np.sum(np.where(ok, (3 * ct * ct - 1) / 2, 0.0)) / len(ct)) if len(ct) else 0.0
+
+
+def phitheta(rods, bx=32, by=32):
+    """Direction histogram (bins_theta, bins_phi) (statKernel_ANGL,
+    inc/statKernel_ANGL.h:57-63); phi = pi or theta = pi in the last bin."""
+    cz = np.clip(np.asarray(rods["cz"], np.float64), -1, 1)
+    cx = np.asarray(rods["cx"], np.float64)
+    theta = np.arccos(cz)
+    mid = (theta > 1e-3) & (theta < np.pi - 1e-3)
+    phi = np.zeros(len(cz))
+    phi[mid] = np.arccos(np.clip(cx[mid] / np.sqrt(1 - cz[mid] * cz[mid]), -1, 1))
+    ip = np.clip(np.floor(phi / (np.pi / bx)).astype(np.int64), 0, bx - 1)
+    it = np.clip(np.floor(theta / (np.pi / by)).astype(np.int64), 0, by - 1)
+    h = np.zeros((by, bx), np.uint64)
+    np.add.at(h, (it, ip), 1)
+    return h
+
+
+def pair_stats(params, rods, ct, bins=32):
+    """Contacts per rod (rod-rod, both ends) and the mutual-angle histogram of
+    the pairs with interior closest points and axis gap below stat_dist_lim
+    (statKernel_CntctPerInc and statKernel_MUT_ANGLE_weightedFloat,
+    inc/statKernel_MUT.h:26-131,452-512), from the oracle's unscreened
+    contacts."""
+    p = make_params(params)
+    n = len(rods)
+    I = np.asarray(ct["I"], np.int64)
+    J = np.asarray(ct["J"], np.int64)
+    rr = J < SNK_ELEC
+    I, J = I[rr], J[rr]
+    per = np.bincount(I, minlength=n) + np.bincount(J, minlength=n)
+    l = rods["l"].astype(np.float64)
+    a = rods["a"].astype(np.float64)
+    tI, tJ, D = np.asarray(ct["tI"])[rr], np.asarray(ct["tJ"])[rr], np.asarray(ct["D"])[rr]
+    interior = (np.abs(tI) < l[I] / 2) & (np.abs(tJ) < l[J] / 2)
+    near = (D - a[I] - a[J]) < float(p.stat_dist_lim)
+    sel = interior & near
+    c = np.stack([rods["cx"], rods["cy"], rods["cz"]], 1).astype(np.float64)
+    dot = np.sum(c[I[sel]] * c[J[sel]], axis=1)
+    g = np.arccos(np.minimum(np.abs(dot), 1.0))
+    step = ((np.pi + float(p.tol)) / 2.0) / bins
+    b = np.floor(g / step).astype(np.int64) % bins
+    hist = np.bincount(b, minlength=bins).astype(np.uint64)
+    return dict(per_rod=per.astype(np.uint32), hist=hist, pairs=int(rr.sum()))

@@ -42,7 +42,7 @@ def test_cli_usage_and_verbs_without_gpu(lib, tmp_path):
     r = run(exe, [], tmp_path)
     assert r.returncode == 1 and "usage" in r.stderr
     (tmp_path / "in.txt").write_text(SMALL_KEYS)
-    r = run(exe, ["in.txt", "generate", "stat_nematic"], tmp_path)
+    r = run(exe, ["in.txt", "generate", "stat_vdw"], tmp_path)
     assert r.returncode == 2 and "not part of this path" in r.stderr
     r = run(exe, ["in.txt", "generate", "stat_conduct", "3"], tmp_path)
     assert r.returncode == 1 and "direction" in r.stderr
