@@ -509,12 +509,12 @@ nf_status Engine::ac_spectrum(const nf_ac_net* net, const nf_ac_params& P, const
     {
         uint32_t* act = eflag.p;
         uint32_t* errw = eflag.p + n + 1;
-        NF_LAUNCH(k_uf_init, grid_for(n, 256), 256, 0, st)(n, parent.p, cflag.p);
+        if (n) NF_LAUNCH(k_uf_init, grid_for(n, 256), 256, 0, st)(n, parent.p, cflag.p);
         if (m) {
             NF_LAUNCH(k_uf_union, grid_for(m, 256), 256, 0, st)(m, eI, eJ, acG.p, acG.p, parent.p, errw);
             NF_LAUNCH(k_uf_flags, grid_for(m, 256), 256, 0, st)(m, eI, eJ, acG.p, acG.p, parent.p, cflag.p, errw);
         }
-        NF_LAUNCH(k_ac_chi, grid_for(n, 256), 256, 0, st)(n, act, aidx.p, parent.p, cflag.p, acchi.p, errw);
+        if (n) NF_LAUNCH(k_ac_chi, grid_for(n, 256), 256, 0, st)(n, act, aidx.p, parent.p, cflag.p, acchi.p, errw);
         NF_CK(cudaGetLastError());
         uint32_t herr = 0;
         NF_CK(cudaMemcpyAsync(&herr, errw, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));

@@ -478,13 +478,13 @@ nf_status Engine::assemble(uint32_t n, const std::vector<uint32_t>& off, uint32_
     NF_CK(cudaMemsetAsync(vsrc.p, 0, sizeof(double) * (2ull * nslot + 2), st));
     NF_CK(cudaMemsetAsync(vsnk.p, 0, sizeof(double) * (2ull * nslot + 2), st));
     NF_CK(cudaMemsetAsync(act + nslot, 0, sizeof(uint32_t), st));
-    NF_LAUNCH(k_uf_init, grid_for(nslot, 256), 256, 0, st)(nslot, parent.p, cflag.p);
+    if (nslot) NF_LAUNCH(k_uf_init, grid_for(nslot, 256), 256, 0, st)(nslot, parent.p, cflag.p);
     if (m) {
         NF_LAUNCH(k_uf_union, grid_for(m, 256), 256, 0, st)(m, eI, eJ, eG, eC, parent.p, errw);
         NF_LAUNCH(k_uf_flags, grid_for(m, 256), 256, 0, st)(m, eI, eJ, eG, eC, parent.p, cflag.p, errw);
         NF_LAUNCH(k_elec_g, grid_for(m, 256), 256, 0, st)(m, eI, eJ, eG, eC, vsrc.p, vsnk.p, sC, tC);
     }
-    NF_LAUNCH(k_active, grid_for(nslot, 256), 256, 0, st)(nslot, parent.p, cflag.p, act, errw);
+    if (nslot) NF_LAUNCH(k_active, grid_for(nslot, 256), 256, 0, st)(nslot, parent.p, cflag.p, act, errw);
     NF_CK(cudaGetLastError());
     nf_status s = scan_u32(act, aidx.p, nslot + 1);
     if (s != NF_OK) return s;
@@ -537,7 +537,8 @@ nf_status Engine::assemble(uint32_t n, const std::vector<uint32_t>& off, uint32_
     if (mc)
         NF_LAUNCH(k_fill, grid_for(mc, 256), 256, 0, st)(mc, eI, eJ, eG, eC, act, aidx.p, rowp.p, deg.p, col.p,
                                                          val64.p, ac ? valC64.p : nullptr);
-    NF_LAUNCH(k_rows, grid_for(nslot, 256), 256, 0, st)(nslot, act, aidx.p, rowp.p, col.p, val64.p,
+    if (nslot)
+        NF_LAUNCH(k_rows, grid_for(nslot, 256), 256, 0, st)(nslot, act, aidx.p, rowp.p, col.p, val64.p,
                                                  ac ? valC64.p : nullptr, val32.p, vsrc.p, vsnk.p, sC, tC, diag64.p,
                                                  diag32.p, cdiag.p, bvec.p, ac ? diagC64.p : nullptr,
                                                  ac ? cdiagC.p : nullptr, ac ? bvecC.p : nullptr);
@@ -577,7 +578,9 @@ nf_status Engine::solve_graph(uint32_t n, const std::vector<uint32_t>& off, cons
                                  outs.p);
     NF_CK(cudaGetLastError());
     tstop(KT_CG);
-    NF_LAUNCH(k_scatter_v, grid_for(nslot, 256), 256, 0, st)(nslot, act, aidx.p, xvec.p, parent.p, cflag.p, volt.p, errw);
+    if (nslot)
+        NF_LAUNCH(k_scatter_v, grid_for(nslot, 256), 256, 0, st)(nslot, act, aidx.p, xvec.p, parent.p, cflag.p, volt.p,
+                                                                 errw);
     NF_CK(cudaGetLastError());
     std::vector<CgOut> ho(R);
     NF_CK(cudaMemcpyAsync(ho.data(), outs.p, sizeof(CgOut) * R, cudaMemcpyDeviceToHost, st));
