@@ -121,6 +121,16 @@ typedef struct nf_params {
                                contact points conducts rod_sigma pi a / L with
                                L = dt / a (tools/kirchhoff/kirchhoff.py:90-95,
                                s0 = 6.7e7 S/m = 67 S/um, the default)       */
+    /* --- electrodes --- */
+    int32_t elec_buffer;    /* ELEC_BUFFER: 0 (default) electrodes are the two
+                               planes of the field axis; 1 the reference's
+                               `expand` buffer layers (src/simPrms.cpp:744-852):
+                               periodic images of the rods beyond each face,
+                               every contact with an image below the box is a
+                               source contact and above it a sink contact
+                               (get_elec_dmnID, inc/conductivity.h:71-90), one
+                               per image rod                                 */
+    int32_t pad_end;
 } nf_params;
 
 /* Rods, structure of arrays, caller-owned host buffers. Any array may be NULL. */

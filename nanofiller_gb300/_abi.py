@@ -39,6 +39,7 @@ class NfParams(C.Structure):
         ("round_candidates", C.c_int32), ("solve_max_iter", C.c_int32), ("solve_tol", C.c_double),
         ("stencil_radius", C.c_int32), ("round_overshoot", C.c_float), ("two_phase_work", C.c_double),
         ("rod_sigma", C.c_double),
+        ("elec_buffer", C.c_int32), ("pad_end", C.c_int32),
     ]
 
 

@@ -70,6 +70,7 @@ nf_status validate(const nf_params& p, std::string* why) {
         *why = "STENCIL_RADIUS must be 0, 1 or 2 and ROUND_OVERSHOOT >= 0"; return NF_ERR_PARAM;
     }
     if (!(p.rod_sigma > 0)) { *why = "ROD_CONDUCTIVITY must be positive"; return NF_ERR_PARAM; }
+    if (p.elec_buffer != 0 && p.elec_buffer != 1) { *why = "ELEC_BUFFER must be 0 or 1"; return NF_ERR_PARAM; }
     double reach = nf::stage_reach(p);
     for (int d = 0; d < 3; ++d)
         if ((p.gen_periodic >> d & 1) && p.box[d] < reach) {
@@ -216,6 +217,7 @@ nf_status nf_params_from_file(const char* path, nf_params* p, int* n_unknown) {
         else if (key == "ROUND_OVERSHOOT") in >> p->round_overshoot;
         else if (key == "TWO_PHASE_WORK") in >> p->two_phase_work;
         else if (key == "ROD_CONDUCTIVITY") in >> p->rod_sigma;
+        else if (key == "ELEC_BUFFER") in >> p->elec_buffer;
         else ++unknown;  // the reference prints "UNRECOGNISED STRING FOUND" and continues
     }
     if (n_unknown) *n_unknown = unknown;
@@ -481,6 +483,8 @@ nf_status nf_adjoint(nf_handle* h, float* dG_dend, size_t capacity, double* dG_d
     if (!h) return NF_ERR_PARAM;
     if (h->E.int_valid)
         return fail(h, NF_ERR_UNSUPPORTED, "the adjoint covers the contact network (run nf_contacts again)");
+    if (h->E.prm[0].elec_buffer && h->E.prm[0].field_dir)
+        return fail(h, NF_ERR_UNSUPPORTED, "the adjoint covers plane electrodes (ELEC_BUFFER 0)");
     return h->E.adjoint(0, dG_dend, capacity, dG_dlambda, dG_dG0);
 }
 
@@ -775,6 +779,10 @@ nf_status nf_batch_run(const nf_params* params, int n, nf_batch_result* out, nf_
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return NF_ERR_NO_DEVICE;
     std::vector<nf_params> ps(params, params + n);
+    for (int r = 1; r < n; ++r)  // one electrode model and field axis per engine when buffer layers are used
+        if ((ps[r].elec_buffer || ps[0].elec_buffer) &&
+            (ps[r].elec_buffer != ps[0].elec_buffer || ps[r].field_dir != ps[0].field_dir))
+            return NF_ERR_PARAM;
     std::vector<std::vector<float>> meshes(n);
     std::vector<const float*> mp(n, nullptr);
     for (int r = 0; r < n; ++r) {

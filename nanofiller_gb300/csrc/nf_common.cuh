@@ -170,6 +170,7 @@ struct Real {
     int32_t typo;
     float slack;            // FP32 filter: absolute slack for coordinate rounding
     int32_t field_axis;     // 0,1,2 or -1
+    int32_t ebuf;           // electrodes are buffer layers of images (else planes)
     double G0, lambda, dc;
 };
 

@@ -20,6 +20,8 @@
 #include <cmath>
 #include <cstring>
 
+#include <cub/device/device_radix_sort.cuh>
+
 #include "nf_engine.cuh"
 #include "nf_tiles.cuh"
 
@@ -431,16 +433,78 @@ __device__ __forceinline__ double tunnel_g(const Real& Re, double gap) {
     return Re.G0 * exp(-(ge - Re.dc) / Re.lambda);
 }
 
-// Per-realisation counts of unscreened / screened records.
+// Per-realisation counts of unscreened / screened records. With buffer-layer
+// electrodes (faxis >= 0) a kept record whose partner is an image across the
+// field axis is not internal: it becomes one sink and one source contact
+// (xf = 1; cnt[2R + 2r], cnt[2R + 2r + 1]).
 __global__ void k_rec_count(int R, const uint32_t* __restrict__ rodoff, uint32_t nrec, const Rec* __restrict__ rec,
-                            uint32_t* __restrict__ keepf, uint32_t* __restrict__ cnt /* 2R */) {
+                            int faxis, uint32_t* __restrict__ keepf, uint32_t* __restrict__ xf,
+                            uint32_t* __restrict__ cnt /* 4R */) {
     uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= nrec) return;
     const Rec& x = rec[q];
     int r = find_real(rodoff, R, x.i);
     bool scr = x.flags & 1u;
-    keepf[q] = scr ? 0u : 1u;
-    atomicAdd(&cnt[2 * r + (scr ? 1 : 0)], 1u);
+    const bool cross = !scr && faxis >= 0 && x.img[faxis] != 0;
+    keepf[q] = (scr || cross) ? 0u : 1u;
+    if (xf) xf[q] = cross ? 1u : 0u;
+    if (cross) {
+        atomicAdd(&cnt[2 * R + 2 * r], 1u);
+        atomicAdd(&cnt[2 * R + 2 * r + 1], 1u);
+    } else {
+        atomicAdd(&cnt[2 * r + (scr ? 1 : 0)], 1u);
+    }
+}
+
+// Buffer-layer electrode contacts of the cross records: the rod whose partner
+// image lies below the box (img < 0 from i's side, > 0 from j's side) touches
+// the source layer, the other rod the sink layer. Keys (rod, partner) for a
+// stable sort; values the record index.
+__global__ void k_buf_emit(uint32_t nrec, const Rec* __restrict__ rec, const uint32_t* __restrict__ xf,
+                           const uint32_t* __restrict__ xpos, int faxis, uint32_t nx,
+                           unsigned long long* __restrict__ key, uint32_t* __restrict__ val) {
+    uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= nrec || !xf[q]) return;
+    const Rec& x = rec[q];
+    const uint32_t k = xpos[q];
+    const bool below = x.img[faxis] < 0;  // j's image below: i touches the source layer
+    const uint32_t src = below ? x.i : x.j, snk = below ? x.j : x.i;
+    key[k] = ((unsigned long long)snk << 32) | (below ? x.i : x.j);            // sink list [0, nx)
+    val[k] = q;
+    key[nx + k] = ((unsigned long long)src << 32) | (below ? x.j : x.i);       // source list [nx, 2 nx)
+    val[nx + k] = q;
+}
+
+// Final sink or source block of the buffer-layer contacts, from the sorted
+// (rod, partner) list: realisation r's entries start at start[r].
+__global__ void k_final_buf(uint32_t n, const unsigned long long* __restrict__ key, const uint32_t* __restrict__ val,
+                            const Rec* __restrict__ rec, int R, const uint32_t* __restrict__ rodoff,
+                            const uint32_t* __restrict__ start, const unsigned long long* __restrict__ base,
+                            uint32_t elec_id, const Real* __restrict__ reals, const float4* __restrict__ pos,
+                            const float4* __restrict__ dir, uint32_t* __restrict__ oI, uint32_t* __restrict__ oJ,
+                            double* __restrict__ ot0, double* __restrict__ ot1, double* __restrict__ oD,
+                            double* __restrict__ oG, double* __restrict__ oS, int8_t* __restrict__ oimg,
+                            uint32_t* __restrict__ oreal) {
+    const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    const Rec x = rec[val[p]];
+    const uint32_t rod = (uint32_t)(key[p] >> 32);
+    const int r = find_real(rodoff, R, rod);
+    const Real& Re = reals[r];
+    const unsigned long long dst = base[r] + (p - start[r]);
+    const bool iside = rod == x.i;
+    const RodD A = rodd(pos[x.i], dir[x.i]);
+    const RodD B = rodd(pos[x.j], dir[x.j]);
+    oI[dst] = rod;
+    oJ[dst] = elec_id;
+    ot0[dst] = iside ? x.t0 : x.t1;
+    ot1[dst] = iside ? x.t1 : x.t0;
+    oD[dst] = x.d;
+    oG[dst] = tunnel_g(Re, dsub(dsub(x.d, A.a), B.a));
+    const double sh[3] = {x.img[0] * (double)Re.L[0], x.img[1] * (double)Re.L[1], x.img[2] * (double)Re.L[2]};
+    oS[dst] = contact_area(A, B, sh, x.Dx, x.u0, x.u1, (double)Re.cut);
+    for (int d = 0; d < 3; ++d) oimg[3 * dst + d] = (int8_t)(iside ? x.img[d] : -x.img[d]);
+    oreal[dst] = (uint32_t)r;
 }
 
 // Electrode flags per rod slot: plane electrodes at x_f = 0 (source) and x_f = L_f (sink).
@@ -659,27 +723,44 @@ nf_status Engine::contacts() {
     uint32_t* fsrc = fsnk + nslot + 1;
     uint32_t* ssnk = fsrc + nslot + 1;
     uint32_t* ssrc = ssnk + nslot + 1;
+    // buffer-layer electrodes: the field axis of realisation 0 (every
+    // realisation of a handle shares the electrode model and the field axis)
+    const int faxis = hreal[0].ebuf ? hreal[0].field_axis : -1;
+    DBuf<uint32_t>& xflag = ivals;  // reuse the intra-rod network's scratch
+    DBuf<uint32_t>& xpos = ivals2;
+    if (faxis >= 0) {
+        NF_CK(xflag.ensure(nrec + 1));
+        NF_CK(xpos.ensure(nrec + 1));
+        NF_CK(cudaMemsetAsync(xflag.p, 0, sizeof(uint32_t) * (nrec + 1), st));
+    }
     NF_CK(cudaMemsetAsync(cnt, 0, sizeof(uint32_t) * 4 * R, st));
     NF_CK(cudaMemsetAsync(keepf, 0, sizeof(uint32_t) * (nrec + 1), st));
     if (nrec) {
-        NF_LAUNCH(k_rec_count, grid_for(nrec, 256), 256, 0, st)(R, rodoff.p, nrec, rec2.p, keepf, cnt);
+        NF_LAUNCH(k_rec_count, grid_for(nrec, 256), 256, 0, st)(R, rodoff.p, nrec, rec2.p, faxis, keepf,
+                                                                 faxis >= 0 ? xflag.p : nullptr, cnt);
         NF_CK(cudaGetLastError());
     }
     s = scan_u32(keepf, kscan, nrec + 1);
     if (s != NF_OK) return s;
+    if (faxis >= 0) {
+        s = scan_u32(xflag.p, xpos.p, nrec + 1);
+        if (s != NF_OK) return s;
+    }
     DBuf<double>& esnk = vsnk;  // reuse solve buffers as scratch (2 doubles per slot)
     DBuf<double>& esrc = vsrc;
     NF_CK(esnk.ensure(2 * (size_t)nslot + 2));
     NF_CK(esrc.ensure(2 * (size_t)nslot + 2));
     NF_CK(cudaMemsetAsync(fsnk + nslot, 0, sizeof(uint32_t), st));
     NF_CK(cudaMemsetAsync(fsrc + nslot, 0, sizeof(uint32_t), st));
-    NF_LAUNCH(k_elec, grid_for(nslot, 256), 256, 0, st)(nslot, R, rodoff.p, dcount.p, dreal.p, pos.p, dir.p, fsnk, fsrc,
-                                                 esnk.p, esrc.p, cnt + 2 * R);
-    NF_CK(cudaGetLastError());
-    s = scan_u32(fsnk, ssnk, nslot + 1);
-    if (s != NF_OK) return s;
-    s = scan_u32(fsrc, ssrc, nslot + 1);
-    if (s != NF_OK) return s;
+    if (faxis < 0) {  // plane electrodes
+        NF_LAUNCH(k_elec, grid_for(nslot, 256), 256, 0, st)(nslot, R, rodoff.p, dcount.p, dreal.p, pos.p, dir.p, fsnk,
+                                                            fsrc, esnk.p, esrc.p, cnt + 2 * R);
+        NF_CK(cudaGetLastError());
+        s = scan_u32(fsnk, ssnk, nslot + 1);
+        if (s != NF_OK) return s;
+        s = scan_u32(fsrc, ssrc, nslot + 1);
+        if (s != NF_OK) return s;
+    }
     std::vector<uint32_t> hc(4 * R);
     NF_CK(cudaMemcpyAsync(hc.data(), cnt, sizeof(uint32_t) * 4 * R, cudaMemcpyDeviceToHost, st));
     NF_CK(cudaStreamSynchronize(st));
@@ -708,14 +789,52 @@ nf_status Engine::contacts() {
                                                              cG.p, cS.p, cimg.p, creal2.p);
         NF_CK(cudaGetLastError());
     }
-    NF_LAUNCH(k_final_elec, grid_for(nslot, 256), 256, 0, st)(nslot, R, rodoff.p, fsnk, ssnk, esnk.p, doff + R, NF_SNK_ELEC,
-                                                       dreal.p, dir.p, cI.p, cJ.p, ct0.p, ct1.p, cD.p, cG.p, cS.p,
-                                                       cimg.p, creal2.p);
-    NF_CK(cudaGetLastError());
-    NF_LAUNCH(k_final_elec, grid_for(nslot, 256), 256, 0, st)(nslot, R, rodoff.p, fsrc, ssrc, esrc.p, doff + 2 * R,
-                                                       NF_SRC_ELEC, dreal.p, dir.p, cI.p, cJ.p, ct0.p, ct1.p, cD.p,
-                                                       cG.p, cS.p, cimg.p, creal2.p);
-    NF_CK(cudaGetLastError());
+    if (faxis < 0) {
+        NF_LAUNCH(k_final_elec, grid_for(nslot, 256), 256, 0, st)(nslot, R, rodoff.p, fsnk, ssnk, esnk.p, doff + R,
+                                                                  NF_SNK_ELEC, dreal.p, dir.p, cI.p, cJ.p, ct0.p,
+                                                                  ct1.p, cD.p, cG.p, cS.p, cimg.p, creal2.p);
+        NF_CK(cudaGetLastError());
+        NF_LAUNCH(k_final_elec, grid_for(nslot, 256), 256, 0, st)(nslot, R, rodoff.p, fsrc, ssrc, esrc.p, doff + 2 * R,
+                                                                  NF_SRC_ELEC, dreal.p, dir.p, cI.p, cJ.p, ct0.p,
+                                                                  ct1.p, cD.p, cG.p, cS.p, cimg.p, creal2.p);
+        NF_CK(cudaGetLastError());
+    } else {
+        // buffer layers: one sink and one source contact per cross record,
+        // each list sorted by (rod, partner), ties in record order (stable)
+        uint32_t nx = 0;
+        std::vector<uint32_t> start(R + 1, 0);
+        for (int r = 0; r < R; ++r) { start[r] = nx; nx += ct_snk[r]; }
+        start[R] = nx;
+        if (nx) {
+            NF_CK(ikeys.ensure(2ull * nx));
+            NF_CK(ikeys2.ensure(2ull * nx));
+            NF_CK(inew.ensure(2ull * nx));
+            NF_CK(igid.ensure(2ull * nx));
+            NF_LAUNCH(k_buf_emit, grid_for(nrec, 256), 256, 0, st)(nrec, rec2.p, xflag.p, xpos.p, faxis, nx, ikeys.p,
+                                                                  inew.p);
+            NF_CK(cudaGetLastError());
+            for (int h = 0; h < 2; ++h) {
+                size_t bytes = 0;
+                NF_CK(cub::DeviceRadixSort::SortPairs(nullptr, bytes, ikeys.p + h * nx, ikeys2.p + h * nx,
+                                                      inew.p + h * nx, igid.p + h * nx, (int)nx, 0, 64, st));
+                NF_CK(cubtmp.ensure(bytes));
+                NF_CK(cub::DeviceRadixSort::SortPairs(cubtmp.p, bytes, ikeys.p + h * nx, ikeys2.p + h * nx,
+                                                      inew.p + h * nx, igid.p + h * nx, (int)nx, 0, 64, st));
+                g_launches += 1;
+            }
+            DBuf<uint32_t>& dstart = rcur;  // free again: the record scatter is done
+            NF_CK(dstart.ensure(R + 1));
+            NF_CK(cudaMemcpyAsync(dstart.p, start.data(), sizeof(uint32_t) * (R + 1), cudaMemcpyHostToDevice, st));
+            for (int h = 0; h < 2; ++h) {
+                NF_LAUNCH(k_final_buf, grid_for(nx, 256), 256, 0, st)(
+                    nx, ikeys2.p + h * nx, igid.p + h * nx, rec2.p, R, rodoff.p, dstart.p, doff + (h ? 2 * R : R),
+                    h ? NF_SRC_ELEC : NF_SNK_ELEC, dreal.p, pos.p, dir.p, cI.p, cJ.p, ct0.p, ct1.p, cD.p, cG.p, cS.p,
+                    cimg.p, creal2.p);
+                NF_CK(cudaGetLastError());
+            }
+            NF_CK(cudaStreamSynchronize(st));  // the host start[] copy is in flight until here
+        }
+    }
     NF_CK(cudaEventRecord(e1, st));
     NF_CK(cudaEventSynchronize(e1));
     float ms = 0;

@@ -171,6 +171,7 @@ struct Engine {
     DBuf<double> val64, diag64, bvec, xvec, cdiag, chain64;
     DBuf<double> valC64, diagC64, cdiagC, bvecC;  // capacitive parts (admittance form)
     DBuf<double> acG, acC, acchi;                 // scaled edge admittances of an AC call, start chi
+    DBuf<uint32_t> ecnt, eoff, elist;             // electrode edges per node (network assembly)
     DBuf<float> cgbuf;
     DBuf<double> cgred;
     std::vector<nf_solve_stats> solve_st;

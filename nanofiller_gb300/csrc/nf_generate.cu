@@ -105,7 +105,10 @@ Real make_real(const nf_params& p, const float* dmesh, int mn[3], double reach) 
     for (int d = 0; d < 3; ++d) R.mn[d] = dmesh ? mn[d] : 0;
     R.dflt = p.density_default;
     R.per_gen = p.gen_periodic & 7;
-    R.per_con = (p.gen_periodic & ~p.field_dir) & 7;
+    // contacts: the field axis is open with plane electrodes, periodic with
+    // buffer-layer electrodes (their rods are the images beyond each face)
+    R.per_con = (p.elec_buffer ? (p.gen_periodic | p.field_dir) : (p.gen_periodic & ~p.field_dir)) & 7;
+    R.ebuf = p.elec_buffer && p.field_dir ? 1 : 0;
     // Cells of edge >= reach / S with a stencil of radius S. S = 2 tests about
     // 125 (reach/2)^3 of volume per probe instead of 27 reach^3 for S = 1; a
     // periodic axis needs at least S cells so that images stay within +-1.
@@ -826,7 +829,7 @@ void Engine::release() {
                              &dcount, &rodoff, &rstart, &rcursor, &sid, &coff, &keep, &kpos, &ccount,
                              &cstart, &ccursor, &cperm, &creal, &ccell, &ccnt, &clist, &accf, &accpos,
                              &meta, &u32tmp, &rcnt, &rpos, &rcur, &cI, &cJ, &creal2, &eflag, &parent,
-                             &cflag, &aidx, &rowp, &col, &deg};
+                             &cflag, &aidx, &rowp, &col, &deg, &ecnt, &eoff, &elist};
     for (auto* b : u32) b->release();
     DBuf<uint64_t>* u64[] = {&sidx, &kbeg, &csidx};
     for (auto* b : u64) b->release();

@@ -92,20 +92,48 @@ __global__ void k_active(uint32_t n, uint32_t* parent, const uint32_t* __restric
 }
 
 // Electrode admittance per node (s: source, t: sink; sC, tC the capacitive
-// parts when C is given).
-__global__ void k_elec_g(uint32_t m, const uint32_t* __restrict__ I, const uint32_t* __restrict__ J,
-                         const double* __restrict__ G, const double* __restrict__ C, double* __restrict__ s,
-                         double* __restrict__ t, double* __restrict__ sC, double* __restrict__ tC) {
+// parts when C is given), summed over the node's electrode edges in edge
+// order: a node may carry several (buffer-layer electrodes give one contact
+// per image rod), so the edges are listed per node, sorted and added in order.
+__global__ void k_edeg(uint32_t m, const uint32_t* __restrict__ I, const uint32_t* __restrict__ J,
+                       const double* __restrict__ G, const double* __restrict__ C, uint32_t* __restrict__ ecnt) {
     uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;
-    if (e >= m) return;
-    uint32_t j = J[e];
-    if (j == NF_SRC_ELEC) {
-        s[I[e]] = G[e];
-        if (C) sC[I[e]] = C[e];
-    } else if (j == NF_SNK_ELEC) {
-        t[I[e]] = G[e];
-        if (C) tC[I[e]] = C[e];
+    if (e >= m || J[e] < NF_SNK_ELEC || !edge_on(G, C, e)) return;
+    atomicAdd(&ecnt[I[e]], 1u);
+}
+
+__global__ void k_efill(uint32_t m, const uint32_t* __restrict__ I, const uint32_t* __restrict__ J,
+                        const double* __restrict__ G, const double* __restrict__ C, const uint32_t* __restrict__ eoff,
+                        uint32_t* __restrict__ ecur, uint32_t* __restrict__ elist) {
+    uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= m || J[e] < NF_SNK_ELEC || !edge_on(G, C, e)) return;
+    const uint32_t i = I[e];
+    elist[eoff[i] + atomicAdd(&ecur[i], 1u)] = e;
+}
+
+__global__ void k_esum(uint32_t n, const uint32_t* __restrict__ eoff, uint32_t* __restrict__ elist,
+                       const uint32_t* __restrict__ J, const double* __restrict__ G, const double* __restrict__ C,
+                       double* __restrict__ s, double* __restrict__ t, double* __restrict__ sC,
+                       double* __restrict__ tC) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint32_t p0 = eoff[i], p1 = eoff[i + 1];
+    if (p0 == p1) return;
+    for (uint32_t k = p0 + 1; k < p1; ++k) {
+        const uint32_t v = elist[k];
+        uint32_t q = k;
+        while (q > p0 && elist[q - 1] > v) { elist[q] = elist[q - 1]; --q; }
+        elist[q] = v;
     }
+    double gs = 0.0, gt = 0.0, cs = 0.0, ct = 0.0;
+    for (uint32_t k = p0; k < p1; ++k) {
+        const uint32_t e = elist[k];
+        if (J[e] == NF_SRC_ELEC) { gs += G[e]; if (C) cs += C[e]; }
+        else { gt += G[e]; if (C) ct += C[e]; }
+    }
+    s[i] = gs;
+    t[i] = gt;
+    if (C) { sC[i] = cs; tC[i] = ct; }
 }
 
 __global__ void k_deg(uint32_t m, const uint32_t* __restrict__ I, const uint32_t* __restrict__ J,
@@ -482,8 +510,23 @@ nf_status Engine::assemble(uint32_t n, const std::vector<uint32_t>& off, uint32_
     if (m) {
         NF_LAUNCH(k_uf_union, grid_for(m, 256), 256, 0, st)(m, eI, eJ, eG, eC, parent.p, errw);
         NF_LAUNCH(k_uf_flags, grid_for(m, 256), 256, 0, st)(m, eI, eJ, eG, eC, parent.p, cflag.p, errw);
-        NF_LAUNCH(k_elec_g, grid_for(m, 256), 256, 0, st)(m, eI, eJ, eG, eC, vsrc.p, vsnk.p, sC, tC);
     }
+    // electrode admittance per node
+    NF_CK(ecnt.ensure(nslot + 1));
+    NF_CK(eoff.ensure(nslot + 1));
+    NF_CK(elist.ensure((size_t)m + 1));
+    NF_CK(cudaMemsetAsync(ecnt.p, 0, sizeof(uint32_t) * (nslot + 1), st));
+    if (m) NF_LAUNCH(k_edeg, grid_for(m, 256), 256, 0, st)(m, eI, eJ, eG, eC, ecnt.p);
+    NF_CK(cudaGetLastError());
+    {
+        nf_status se = scan_u32(ecnt.p, eoff.p, nslot + 1);
+        if (se != NF_OK) return se;
+    }
+    NF_CK(cudaMemsetAsync(ecnt.p, 0, sizeof(uint32_t) * (nslot + 1), st));  // reuse as cursor
+    if (m) NF_LAUNCH(k_efill, grid_for(m, 256), 256, 0, st)(m, eI, eJ, eG, eC, eoff.p, ecnt.p, elist.p);
+    if (nslot)
+        NF_LAUNCH(k_esum, grid_for(nslot, 256), 256, 0, st)(nslot, eoff.p, elist.p, eJ, eG, eC, vsrc.p, vsnk.p, sC, tC);
+    NF_CK(cudaGetLastError());
     if (nslot) NF_LAUNCH(k_active, grid_for(nslot, 256), 256, 0, st)(nslot, parent.p, cflag.p, act, errw);
     NF_CK(cudaGetLastError());
     nf_status s = scan_u32(act, aidx.p, nslot + 1);

@@ -723,7 +723,11 @@ int64_t nfo_contacts(const nf_params* p, const nfo_rod* rods, int64_t n, int nth
     const int nt = nthreads_of(nthreads);
     const double eps = 1e-6f;  // DEV_PRECISION, inc/definitions.h:5
     const double cut = p->stat_dist_lim;
-    const int per = p->gen_periodic & ~p->field_dir;  // peri_dir = 7 - dir
+    // peri_dir = 7 - dir; with buffer-layer electrodes the field axis is
+    // periodic too: its images are the electrode layers
+    const int fax = p->field_dir == 1 ? 0 : (p->field_dir == 2 ? 1 : (p->field_dir == 4 ? 2 : -1));
+    const bool buf = p->elec_buffer && fax >= 0;
+    const int per = buf ? ((p->gen_periodic | p->field_dir) & 7) : (p->gen_periodic & ~p->field_dir);
     double lmax = 0, amax = 0;
     for (int64_t i = 0; i < n; ++i) { lmax = std::max(lmax, (double)rods[i].l); amax = std::max(amax, (double)rods[i].a); }
     Grid g;
@@ -827,14 +831,36 @@ int64_t nfo_contacts(const nf_params* p, const nfo_rod* rods, int64_t n, int nth
             screened[q] = hit;
         }
     }
+    // Buffer-layer electrodes (expand, src/simPrms.cpp:744-852, roles by
+    // get_elec_dmnID, inc/conductivity.h:71-90): a kept pair whose partner is
+    // an image across the field axis gives the rod whose partner lies below
+    // the box a source contact and the other rod a sink contact.
+    struct BufCt { uint32_t rod, partner; size_t q; bool iside; };
+    std::vector<BufCt> bsnk, bsrc;
+    std::vector<char> cross(all.size(), 0);
+    if (buf)
+        for (size_t q = 0; q < all.size(); ++q) {
+            if (screened[q] || all[q].im[fax] == 0) continue;
+            cross[q] = 1;
+            const bool below = all[q].im[fax] < 0;
+            bsrc.push_back({below ? all[q].i : all[q].j, below ? all[q].j : all[q].i, q, below});
+            bsnk.push_back({below ? all[q].j : all[q].i, below ? all[q].i : all[q].j, q, !below});
+        }
+    auto bless = [](const BufCt& a, const BufCt& b) {
+        if (a.rod != b.rod) return a.rod < b.rod;
+        if (a.partner != b.partner) return a.partner < b.partner;
+        return a.q < b.q;
+    };
+    std::sort(bsnk.begin(), bsnk.end(), bless);
+    std::sort(bsrc.begin(), bsrc.end(), bless);
     int64_t n_int = 0, n_scr = 0;
-    for (size_t q = 0; q < all.size(); ++q) (screened[q] ? n_scr : n_int)++;
+    for (size_t q = 0; q < all.size(); ++q) if (!cross[q]) (screened[q] ? n_scr : n_int)++;
     // Electrode contacts: rods whose capsule comes within the cutoff of the
     // planes x_f = 0 (source) and x_f = L_f (sink) of the field axis f.
     std::vector<std::pair<uint32_t, double>> snk, src;  // (rod, D)
     std::vector<double> snk_t, src_t;
-    int f = p->field_dir == 1 ? 0 : (p->field_dir == 2 ? 1 : (p->field_dir == 4 ? 2 : -1));
-    if (f >= 0) {
+    int f = fax;
+    if (f >= 0 && !buf) {
         for (int64_t i = 0; i < n; ++i) {
             const RodT<double>& A = R[i];
             double cf = f == 0 ? A.cx : (f == 1 ? A.cy : A.cz);
@@ -849,14 +875,15 @@ int64_t nfo_contacts(const nf_params* p, const nfo_rod* rods, int64_t n, int nth
             if (zlo - A.a < cut + eps) { src.push_back({(uint32_t)i, zlo}); src_t.push_back(tlo); }
         }
     }
-    int64_t total = n_int + (int64_t)snk.size() + (int64_t)src.size();
-    if (counts) { counts[0] = n_int; counts[1] = n_scr; counts[2] = (int64_t)snk.size(); counts[3] = (int64_t)src.size(); }
+    const int64_t nsnk = (int64_t)(buf ? bsnk.size() : snk.size()), nsrc = (int64_t)(buf ? bsrc.size() : src.size());
+    int64_t total = n_int + nsnk + nsrc;
+    if (counts) { counts[0] = n_int; counts[1] = n_scr; counts[2] = nsnk; counts[3] = nsrc; }
     if (total > cap || !I) return total;
     const double G0 = p->G0, lam = p->lambda, dc = p->d_c;
     auto gfun = [&](double gap) { double ge = gap > dc ? gap : dc; return G0 * std::exp(-(ge - dc) / lam); };
     int64_t o = 0;
     for (size_t q = 0; q < all.size(); ++q) {
-        if (screened[q]) continue;
+        if (screened[q] || cross[q]) continue;
         const Ct& c = all[q];
         I[o] = c.i; J[o] = c.j;
         if (tI) tI[o] = c.t0;
@@ -882,8 +909,29 @@ int64_t nfo_contacts(const nf_params* p, const nfo_rod* rods, int64_t n, int nth
             ++o;
         }
     };
-    put_elec(snk, snk_t, NF_SNK_ELEC);
-    put_elec(src, src_t, NF_SRC_ELEC);
+    auto put_buf = [&](const std::vector<BufCt>& v, uint32_t id) {
+        for (const BufCt& b : v) {
+            const Ct& c = all[b.q];
+            I[o] = b.rod; J[o] = id;
+            if (tI) tI[o] = b.iside ? c.t0 : c.t1;
+            if (tJ) tJ[o] = b.iside ? c.t1 : c.t0;
+            if (D) D[o] = c.d;
+            if (G) G[o] = gfun(c.d - R[c.i].a - R[c.j].a);
+            if (S) {
+                double sh[3] = {c.im[0] * (double)g.L[0], c.im[1] * (double)g.L[1], c.im[2] * (double)g.L[2]};
+                S[o] = nfo_contact_area(&rods[c.i], &rods[c.j], sh, c.Dx, c.u0, c.u1, cut);
+            }
+            if (img) for (int d = 0; d < 3; ++d) img[3 * o + d] = (int8_t)(b.iside ? c.im[d] : -c.im[d]);
+            ++o;
+        }
+    };
+    if (buf) {
+        put_buf(bsnk, NF_SNK_ELEC);
+        put_buf(bsrc, NF_SRC_ELEC);
+    } else {
+        put_elec(snk, snk_t, NF_SNK_ELEC);
+        put_elec(src, src_t, NF_SRC_ELEC);
+    }
     return total;
 }
 

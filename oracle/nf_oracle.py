@@ -42,6 +42,7 @@ class NfParams(C.Structure):
         ("round_candidates", C.c_int32), ("solve_max_iter", C.c_int32), ("solve_tol", C.c_double),
         ("stencil_radius", C.c_int32), ("round_overshoot", C.c_float), ("two_phase_work", C.c_double),
         ("rod_sigma", C.c_double),
+        ("elec_buffer", C.c_int32), ("pad_end", C.c_int32),
     ]
 
 
@@ -55,7 +56,7 @@ DEFAULTS = dict(
     vmf_kappa=0.0, len_mode=0, len_sigma_ln=0.0, len_min=0.0, len_max=0.0, rad_mode=0,
     rad_min=0.0, rad_max=0.0, density_default=1.0, cell_edge=0.0, G0=1e-5, lambda_=0.00018,
     d_c=0.00034, ref_parallel_typo=0, screening=1, round_candidates=0, solve_max_iter=20000,
-    solve_tol=1e-10, stencil_radius=0, round_overshoot=0.0, two_phase_work=0.0, rod_sigma=67.0,
+    solve_tol=1e-10, stencil_radius=0, round_overshoot=0.0, two_phase_work=0.0, rod_sigma=67.0, elec_buffer=0,
 )
 
 
