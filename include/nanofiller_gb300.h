@@ -326,6 +326,14 @@ nf_status nf_get_internal_network(nf_handle *h, nf_internal_net *out);
  * in dir (save_coo layouts, src/conductivity.cu:881-930). */
 nf_status nf_write_internal_coo(nf_handle *h, const char *dir);
 
+/* ---- orientation law at run time ------------------------------------- */
+/* The orientation keywords of simPrms (ORIENT, VMF_KAPPA, PREF_ORT_PHI,
+ * PREF_ORT_THETA; src/simPrms.cpp:212-327) for the candidates drawn after
+ * this call, in every realisation of the handle: NF_ORIENT_ISOTROPIC, or
+ * NF_ORIENT_VMF with concentration kappa > 0 about the preferred axis
+ * (pref_phi, pref_theta) in radians. Rods already accepted stay. */
+nf_status nf_set_orientation(nf_handle *h, int32_t mode, float kappa, float pref_phi, float pref_theta);
+
 /* ---- dead-end pruning: the `reduce` verb (src/NanoFiller.cpp:71-91) ---- */
 /* Replaces the reference's reduce loop (reduce(), src/conductivity.cu:79-138;
  * contact_count_kernel_full / reductKernel, inc/conductKernels.h:39-162):

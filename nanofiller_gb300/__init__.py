@@ -271,6 +271,13 @@ class Simulation:
                "nf_stream_candidates_noalloc")
         return out.T.copy()
 
+    def set_orientation(self, mode, kappa=1.0, pref_phi=0.0, pref_theta=0.0):
+        """Orientation law of the candidates drawn from now on (nf_set_orientation):
+        mode 0 isotropic, 1 von Mises-Fisher with concentration kappa about the
+        axis (pref_phi, pref_theta)."""
+        _check(self._L.nf_set_orientation(self._h, mode, kappa, pref_phi, pref_theta), self._h,
+               "nf_set_orientation")
+
     def reduce(self, min_contacts=2):
         """Dead-end pruning (nf_reduce): keep the rods with at least
         min_contacts unscreened contacts, repeatedly; electrodes stay."""

@@ -184,6 +184,7 @@ SIGNATURES = {
     "nf_get_internal_network": (_st, [_H, _P(NfInternalNet)]),
     "nf_write_internal_coo": (_st, [_H, C.c_char_p]),
     "nf_reduce": (_st, [_H, C.c_int32, _P(NfReduceStats)]),
+    "nf_set_orientation": (_st, [_H, C.c_int32, C.c_float, C.c_float, C.c_float]),
     "nf_stat_nematic": (_st, [_H, C.c_void_p, _P(C.c_double)]),
     "nf_stat_phitheta": (_st, [_H, C.c_int32, C.c_int32, C.c_void_p]),
     "nf_stat_pairs": (_st, [_H, C.c_int32, C.c_void_p, C.c_void_p, C.c_size_t, _P(NfPairStats)]),

@@ -594,6 +594,25 @@ nf_status nf_write_internal_coo(nf_handle* h, const char* dir) {
     return NF_OK;
 }
 
+nf_status nf_set_orientation(nf_handle* h, int32_t mode, float kappa, float pref_phi, float pref_theta) {
+    if (!h) return NF_ERR_PARAM;
+    nf::Engine& E = h->E;
+    std::vector<nf_params> ps = E.prm;
+    for (nf_params& p : ps) {
+        p.orient_mode = mode;
+        p.vmf_kappa = kappa;
+        p.pref_ort[0] = pref_phi;
+        p.pref_ort[1] = pref_theta;
+        std::string why;
+        if (mode != NF_ORIENT_ISOTROPIC && mode != NF_ORIENT_VMF) return fail(h, NF_ERR_PARAM, "unknown orientation mode");
+        if (!std::isfinite(pref_phi) || !std::isfinite(pref_theta)) return fail(h, NF_ERR_PARAM, "axis angles must be finite");
+        nf_status s = validate(p, &why);
+        if (s != NF_OK) return fail(h, s, why);
+    }
+    E.prm = ps;
+    return E.setup();  // the device descriptors follow at once
+}
+
 nf_status nf_reduce(nf_handle* h, int32_t min_contacts, nf_reduce_stats* stats) {
     if (!h) return NF_ERR_PARAM;
     if (min_contacts < 0) return fail(h, NF_ERR_PARAM, "min_contacts must be >= 0");

@@ -135,3 +135,27 @@ def test_single_and_duplicated_rods(gpu, oracle):
     assert np.array_equal(ct["I"], co["I"]) and np.array_equal(ct["D"], co["D"])
     # identical axes take the routine's parallel branch: a distance at rounding level
     assert len(ct["I"]) == 1 and ct["D"][0] < 1e-7
+
+
+def test_set_orientation_equals_creation_parameters(gpu):
+    base = dict(gpu.configs.SMALL, vf=0.02)
+    aligned = dict(base, orient_mode=1, vmf_kappa=20.0, pref_ort=(0.0, np.pi / 2))  # about x
+    with gpu.Simulation(base) as sim:
+        sim.set_orientation(1, 20.0, 0.0, np.pi / 2)
+        sim.generate()
+        r1 = sim.rods()
+        S = sim.nematic((1.0, 0.0, 0.0))
+        s1 = sim.stream(0, 1000)
+        with pytest.raises(gpu.NanoFillerError) as ei:
+            sim.set_orientation(1, 0.0)  # a von Mises-Fisher law needs kappa > 0
+        assert ei.value.status == 1
+        sim.set_orientation(0)
+        s0 = sim.stream(0, 1000)
+    with gpu.Simulation(aligned) as ref:
+        ref.generate()
+        r2 = ref.rods()
+        s2 = ref.stream(0, 1000)
+    for f in ("x", "y", "z", "cx", "cy", "cz", "stream_index"):
+        assert np.array_equal(r1[f], r2[f]), f
+    assert np.array_equal(s1, s2) and S > 0.7
+    assert np.mean(np.abs(s0[:, 3])) < 0.6 < np.mean(np.abs(s1[:, 3]))  # isotropic again
