@@ -197,6 +197,20 @@ class Clocks:
                 "samples": len(sm), "samples_nvidia_smi": smi, "samples_nvml": len(self.nv)}
 
 
+def fp32_roofline(g, old_ms, clk):
+    """FP32 side of the old-rod sweep: 60 flops per candidate-rod pair within
+    sphere reach (the hard-core predicate's count), against the FP32 pipe
+    peak of the device: SMs x 128 lanes x 2 flops x the SM clock sampled in the
+    timed window (the nominal figure; no FP32 peak is measured)."""
+    import torch
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    mhz = (clk or {}).get("sm_mhz") or (clk or {}).get("sm_max_mhz") or 2070.0
+    peak = sms * 128 * 2 * mhz * 1e6 / 1e12
+    achieved = 60.0 * g["sphere_pairs"] / (old_ms * 1e-3) / 1e12 if old_ms > 0 else 0.0
+    return {"kernel": "old_test", "bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+            "frac": achieved / peak, "peak_source": "nominal: SMs x 128 FP32 lanes x 2 x sampled SM clock"}
+
+
 # --------------------------------------------------------------------------- CPU (oracle) leg
 def cpu_run(params, mesh, budget_s=12.0, max_reps=200):
     """The oracle on all host threads; returns (rods per second, cores, sample text)."""
@@ -420,6 +434,10 @@ def run_ours(args, rank, world):
         "roofline": {"kernel": dom, "bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                      "frac": achieved / hbm, "traffic": traffic, "peak_source": peak_note,
                      "note": "pair-test kernels are FP32-issue bound; bytes are the algorithmic bytes"},
+        "roofline_fp32": fp32_roofline(g, kern["old_test"]["ms"] / args.steps, clk),
+        "contacts_per_s": (c["contacts"] + c["n_source"] + c["n_sink"]) / (c["ms"] / 1000) if c["ms"] > 0 else None,
+        "solve": {"residual": s["residual"], "outer_iters": s["outer_iters"], "inner_iters": s["inner_iters"],
+                  "n_active": s["n_active"], "ms": s["ms"]},
         "clocks": clk,
     }
     sim.set_kernel_timing(False)
