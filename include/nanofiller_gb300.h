@@ -419,7 +419,9 @@ typedef struct nf_ac_params {
     int32_t own_radii;  /* 0: gap D - 2 r_cnt for every contact (the tool);
                            1: D - a_I - a_J, electrode contacts D - a_I (the
                            handle's own network with plane electrodes) */
-    int32_t pad;
+    int32_t method;     /* 0: banded LDL^T per frequency when the reordered
+                           band is narrow enough, else COCG; 1: banded
+                           (NF_ERR_PARAM if too wide); 2: COCG */
     double tol;         /* relative FP64 residual per frequency (1e-10) */
 } nf_ac_params;
 
@@ -442,6 +444,8 @@ typedef struct nf_ac_stats {
     uint64_t n_nodes, n_active, n_contacts, n_kept, n_segments;
     double R0, C0, omega0;  /* ohm, F, rad/s */
     double ms;              /* device time of the call */
+    uint32_t bandwidth;     /* of the active system after reverse Cuthill-McKee */
+    int32_t direct;         /* 1: banded LDL^T per frequency; 0: COCG (bands too wide) */
 } nf_ac_stats;
 
 /* A network given on the host (the tool's input files): nodes 0..n_nodes-1,

@@ -108,7 +108,7 @@ class NfPairStats(C.Structure):
 class NfAcParams(C.Structure):
     _fields_ = [("r_cnt", C.c_double), ("l_cnt", C.c_double), ("phi_ev", C.c_double), ("eps_r", C.c_double),
                 ("delta_min", C.c_double), ("delta_tun", C.c_double), ("delta_eff", C.c_double),
-                ("c_min", C.c_double), ("l_box", C.c_double), ("own_radii", C.c_int32), ("pad", C.c_int32),
+                ("c_min", C.c_double), ("l_box", C.c_double), ("own_radii", C.c_int32), ("method", C.c_int32),
                 ("tol", C.c_double)]
 
 
@@ -121,7 +121,7 @@ class NfAcPoint(C.Structure):
 class NfAcStats(C.Structure):
     _fields_ = [("n_nodes", C.c_uint64), ("n_active", C.c_uint64), ("n_contacts", C.c_uint64),
                 ("n_kept", C.c_uint64), ("n_segments", C.c_uint64), ("R0", C.c_double), ("C0", C.c_double),
-                ("omega0", C.c_double), ("ms", C.c_double)]
+                ("omega0", C.c_double), ("ms", C.c_double), ("bandwidth", C.c_uint32), ("direct", C.c_int32)]
 
 
 class NfAcNet(C.Structure):

@@ -26,6 +26,7 @@
 // cannot resolve (2^-24 ~ 6e-8 of the largest term). Pivots of a chain are
 // series combinations of admittances with G, C >= 0, so they stay in the
 // first quadrant and no cancellation arises.
+#include <algorithm>
 #include <cmath>
 #include <vector>
 
@@ -388,6 +389,254 @@ __global__ void __launch_bounds__(NT) k_ac_cocg(int nf, const double* __restrict
     }
 }
 
+// ---------------------------------------------------------------------------
+// Direct form: banded complex-symmetric LDL^T per frequency.
+//
+// The active system is reordered by reverse Cuthill-McKee on the host (the
+// networks of the tool are sparse and nearly one-dimensional: the jammed
+// node network of 2 777 active nodes has bandwidth 30 after it), and every
+// frequency's CTA assembles its band, factors it without pivoting (all
+// admittances lie in the first quadrant, the matrix is complex symmetric and
+// diagonally dominant in the sense that each diagonal is the sum of its row's
+// off-diagonal admittances plus the electrode ones), and refines x on the
+// difference-form residual as the oracle's refined LU does. This is the
+// tool's own method (a direct factorisation per frequency) and does not
+// stagnate on stiff networks. Band storage: row p of the reordered matrix
+// holds A[p][p - o] for o = 0..b.
+// ---------------------------------------------------------------------------
+constexpr uint32_t kBandMax = 512;
+
+template <int NT>
+__global__ void __launch_bounds__(NT) k_ac_band(int nf, const double* __restrict__ wsc, uint32_t na, uint32_t b,
+                                                const uint32_t* __restrict__ perm, const uint32_t* __restrict__ rowp,
+                                                const uint32_t* __restrict__ col, const double* __restrict__ vG,
+                                                const double* __restrict__ vC, const double* __restrict__ eG,
+                                                const double* __restrict__ eC, const double* __restrict__ ch64,
+                                                int chains, const double* __restrict__ bG,
+                                                const double* __restrict__ bC, const double* __restrict__ chi,
+                                                double2* __restrict__ bwork, double2* __restrict__ vwork,
+                                                AcOut* __restrict__ out) {
+    __shared__ double sh[4 * 40 + 8];
+    __shared__ double2 lsh[kBandMax], ush[kBandMax];
+    const int f = blockIdx.x;
+    if (f >= nf) return;
+    const double w = wsc[f];
+    const size_t bw = (size_t)b + 1;
+    double2* A = bwork + (size_t)f * na * bw;
+    double2* x = vwork + (size_t)f * 5 * na;  // unknowns, original order
+    double2* rv = x + na;                      // residual, original order
+    double2* xc = rv + na;                     // chi
+    double2* t = xc + na;                      // solve vector, reordered
+    double2* xt = t + na;                      // candidate x
+    const double* glG = ch64;
+    const double* grG = ch64 + na;
+    const double* glC = ch64 + 2ull * na;
+    const double* grC = ch64 + 3ull * na;
+    AcOut o{};
+    // band assembly, one row per thread
+    for (uint32_t i = threadIdx.x; i < na; i += NT) {
+        const uint32_t p = perm[i];
+        double2* row = A + (size_t)p * bw;
+        for (uint32_t q = 1; q < bw; ++q) row[q] = cd(0.0, 0.0);
+        double2 d = cd(eG[i], w * eC[i]);
+        for (uint32_t k = rowp[i], k1 = rowp[i + 1]; k < k1; ++k) {
+            const double2 y = cd(vG[k], w * vC[k]);
+            d = cadd(d, y);
+            const uint32_t q = perm[col[k]];
+            if (q < p && p - q <= b) row[p - q] = csub(row[p - q], y);
+        }
+        if (chains) {
+            if (glG[i] > 0.0) {
+                const double2 y = cd(glG[i], w * glC[i]);
+                d = cadd(d, y);
+                const uint32_t q = perm[i - 1];
+                if (q < p && p - q <= b) row[p - q] = csub(row[p - q], y);
+            }
+            if (grG[i] > 0.0) {
+                const double2 y = cd(grG[i], w * grC[i]);
+                d = cadd(d, y);
+                const uint32_t q = perm[i + 1];
+                if (q < p && p - q <= b) row[p - q] = csub(row[p - q], y);
+            }
+        }
+        row[0] = d;
+        x[i] = cd(0.0, 0.0);
+        xc[i] = cd(chi[i], 0.0);
+    }
+    __syncthreads();
+    // LDL^T, right-looking: column k scales by 1 / d_k, the trailing triangle
+    // loses l_i (d_k l_j) = l_i A[j][j-k]
+    for (uint32_t k = 0; k < na; ++k) {
+        const double2 dk = A[(size_t)k * bw];
+        const uint32_t m = min(b, na - 1 - k);
+        for (uint32_t u = threadIdx.x; u < m; u += NT) {
+            const double2 a = A[(size_t)(k + 1 + u) * bw + (u + 1)];
+            ush[u] = a;
+            lsh[u] = cdiv(a, dk);
+        }
+        __syncthreads();
+        const uint32_t ntri = m * (m + 1) / 2;
+        for (uint32_t v = threadIdx.x; v < ntri; v += NT) {
+            uint32_t ii = (uint32_t)((sqrt(8.0 * v + 1.0) - 1.0) * 0.5);
+            while ((ii + 1) * (ii + 2) / 2 <= v) ++ii;  // exact triangular root
+            while (ii * (ii + 1) / 2 > v) --ii;
+            const uint32_t jj = v - ii * (ii + 1) / 2;
+            const uint32_t i = k + 1 + ii;
+            double2* e = A + (size_t)i * bw + (ii - jj);
+            *e = csub(*e, cmul(lsh[ii], ush[jj]));
+        }
+        __syncthreads();
+        for (uint32_t u = threadIdx.x; u < m; u += NT) A[(size_t)(k + 1 + u) * bw + (u + 1)] = lsh[u];
+        __syncthreads();
+    }
+    // refinement on K x = K chi - b (x = chi - V), residual in difference form
+    double rn = 0.0, bn = 0.0;
+    {
+        double nrm[2] = {0.0, 0.0};
+        for (uint32_t i = threadIdx.x; i < na; i += NT) {
+            const double2 bb = cd(bG[i], w * bC[i]);
+            const double2 c = csub(ac_row(i, w, xc, rowp, col, vG, vC, eG, eC, chains, glG, grG, glC, grC), bb);
+            rv[i] = c;
+            nrm[0] += c.x * c.x + c.y * c.y;
+            nrm[1] += bb.x * bb.x + bb.y * bb.y;
+        }
+        block_sum_k<NT, 2>(nrm, sh);
+        rn = sqrt(nrm[0]);
+        bn = sqrt(nrm[1]);
+    }
+    int steps = 0;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (; steps < 12 && rn > 1e-15 * bn; ++steps) {
+        for (uint32_t i = threadIdx.x; i < na; i += NT) t[perm[i]] = rv[i];
+        __syncthreads();
+        if (warp == 0) {
+            // forward: t_i -= l_ik t_k below the diagonal, column by column
+            for (uint32_t k = 0; k < na; ++k) {
+                const double2 tk = t[k];
+                const uint32_t m = min(b, na - 1 - k);
+                for (uint32_t u = lane; u < m; u += 32) {
+                    const uint32_t i = k + 1 + u;
+                    t[i] = csub(t[i], cmul(A[(size_t)i * bw + (u + 1)], tk));
+                }
+                __syncwarp();
+            }
+            for (uint32_t k = lane; k < na; k += 32) t[k] = cdiv(t[k], A[(size_t)k * bw]);
+            __syncwarp();
+            // backward: t_k -= sum_i l_ik t_i over the band below k
+            for (uint32_t kk = na; kk-- > 0;) {
+                const uint32_t m = min(b, na - 1 - kk);
+                double2 acc = cd(0.0, 0.0);
+                for (uint32_t u = lane; u < m; u += 32) {
+                    const uint32_t i = kk + 1 + u;
+                    acc = cadd(acc, cmul(A[(size_t)i * bw + (u + 1)], t[i]));
+                }
+#pragma unroll
+                for (int s = 16; s > 0; s >>= 1) {
+                    acc.x += __shfl_down_sync(0xffffffffu, acc.x, s);
+                    acc.y += __shfl_down_sync(0xffffffffu, acc.y, s);
+                }
+                if (lane == 0) t[kk] = csub(t[kk], acc);
+                __syncwarp();
+            }
+        }
+        __syncthreads();
+        for (uint32_t i = threadIdx.x; i < na; i += NT) xt[i] = cadd(x[i], t[perm[i]]);
+        __syncthreads();
+        double part = 0.0;
+        for (uint32_t i = threadIdx.x; i < na; i += NT) {
+            const double2 a = ac_row(i, w, xt, rowp, col, vG, vC, eG, eC, chains, glG, grG, glC, grC);
+            const double2 c = ac_row(i, w, xc, rowp, col, vG, vC, eG, eC, chains, glG, grG, glC, grC);
+            const double2 ri = csub(csub(c, cd(bG[i], w * bC[i])), a);
+            t[perm[i]] = ri;  // the solve vector is free again: hold the candidate residual
+            part += ri.x * ri.x + ri.y * ri.y;
+        }
+        const double rn_new = sqrt(block_sum<NT>(part, sh));
+        if (!(rn_new < rn)) { ++steps; break; }  // at the rounding floor
+        for (uint32_t i = threadIdx.x; i < na; i += NT) {
+            x[i] = xt[i];
+            rv[i] = t[perm[i]];
+        }
+        __syncthreads();
+        rn = rn_new;
+    }
+    double cur[4] = {0.0, 0.0, 0.0, 0.0};
+    for (uint32_t i = threadIdx.x; i < na; i += NT) {
+        const double2 tt = cmul(cd(bG[i], w * bC[i]), cadd(cd(1.0 - chi[i], 0.0), x[i]));
+        cur[0] += tt.x;
+        cur[1] += tt.y;
+        const double2 d = cmul(csub(cd(chi[i], 0.0), x[i]), rv[i]);
+        cur[2] += d.x;
+        cur[3] += d.y;
+    }
+    block_sum_k<NT, 4>(cur, sh);
+    if (threadIdx.x == 0) {
+        o.i_re = cur[0];
+        o.i_im = cur[1];
+        o.rms = rn;
+        o.res = bn > 0 ? rn / bn : 0.0;
+        o.i_err = sqrt(cur[2] * cur[2] + cur[3] * cur[3]);
+        o.inner = steps;
+        o.outer = steps;
+        out[f] = o;
+    }
+}
+
+// Reverse Cuthill-McKee order of the active system (CSR rows plus the chain
+// links i -> i + 1): perm[old] = new; returns the bandwidth.
+static uint32_t rcm_order(uint32_t n, const std::vector<uint32_t>& rowp, const std::vector<uint32_t>& col,
+                          const std::vector<char>& up, std::vector<uint32_t>* perm) {
+    std::vector<uint32_t> deg(n, 0);
+    for (uint32_t i = 0; i < n; ++i) deg[i] = rowp[i + 1] - rowp[i] + (up[i] ? 1 : 0) + (i > 0 && up[i - 1] ? 1 : 0);
+    auto nbrs = [&](uint32_t i, std::vector<uint32_t>& out) {
+        out.clear();
+        for (uint32_t k = rowp[i]; k < rowp[i + 1]; ++k) out.push_back(col[k]);
+        if (up[i]) out.push_back(i + 1);
+        if (i > 0 && up[i - 1]) out.push_back(i - 1);
+    };
+    std::vector<int64_t> level(n, -1);
+    std::vector<uint32_t> order;
+    order.reserve(n);
+    std::vector<char> done(n, 0);
+    std::vector<uint32_t> nb, q;
+    auto bfs = [&](uint32_t s, std::vector<uint32_t>* seq) {  // returns the last node reached
+        q.assign(1, s);
+        level[s] = 0;
+        std::vector<uint32_t> touched(1, s);
+        size_t h = 0;
+        while (h < q.size()) {
+            const uint32_t v = q[h++];
+            nbrs(v, nb);
+            std::sort(nb.begin(), nb.end(), [&](uint32_t a, uint32_t c) { return deg[a] != deg[c] ? deg[a] < deg[c] : a < c; });
+            for (uint32_t u : nb)
+                if (level[u] < 0 && !done[u]) { level[u] = level[v] + 1; q.push_back(u); touched.push_back(u); }
+        }
+        if (seq) *seq = q;
+        const uint32_t last = q.back();
+        for (uint32_t v : touched) level[v] = -1;
+        return last;
+    };
+    for (uint32_t s0 = 0; s0 < n; ++s0) {
+        if (done[s0]) continue;
+        uint32_t s = s0;  // pseudo-peripheral start: two sweeps from the component's first node
+        s = bfs(s, nullptr);
+        s = bfs(s, nullptr);
+        std::vector<uint32_t> seq;
+        bfs(s, &seq);
+        for (uint32_t v : seq) { done[v] = 1; order.push_back(v); }
+    }
+    perm->assign(n, 0);
+    for (uint32_t k = 0; k < n; ++k) (*perm)[order[n - 1 - k]] = k;
+    uint32_t bwid = 0;
+    for (uint32_t i = 0; i < n; ++i) {
+        nbrs(i, nb);
+        for (uint32_t j : nb) {
+            const uint32_t a = (*perm)[i], c = (*perm)[j];
+            bwid = std::max(bwid, a > c ? a - c : c - a);
+        }
+    }
+    return bwid;
+}
+
 nf_status Engine::ac_spectrum(const nf_ac_net* net, const nf_ac_params& P, const double* freq, size_t nfreq,
                               nf_ac_point* out, nf_ac_stats* stats) {
     EventPair ev;
@@ -523,15 +772,47 @@ nf_status Engine::ac_spectrum(const nf_ac_net* net, const nf_ac_params& P, const
     }
     const double tol = P.tol > 0 ? P.tol : 1e-10;
     const int max_inner = prm[0].solve_max_iter > 0 ? prm[0].solve_max_iter : 20000;
-    // Frequencies per launch: the work of one (160 B per active row) held to ~4 GB.
-    const size_t per = kAcD2 * sizeof(double2) * (size_t)std::max<uint32_t>(na, 1);
-    const size_t batch = std::max<size_t>(1, std::min<size_t>(nfreq, (size_t)4e9 / per));
-    DBuf<double2> dw;
+    // Direct form when the reordered band is narrow enough: bandwidth <= 512,
+    // at most 1 GB of band and ~4e9 complex updates per frequency.
+    uint32_t bandw = 0;
+    bool direct = false;
+    DBuf<uint32_t> dperm;
+    if (na > 0) {
+        std::vector<uint32_t> hrow(na + 1), hcol(A.nnz);
+        std::vector<double> hgr(na);
+        NF_CK(cudaMemcpyAsync(hrow.data(), rowp.p, sizeof(uint32_t) * (na + 1), cudaMemcpyDeviceToHost, st));
+        if (A.nnz) NF_CK(cudaMemcpyAsync(hcol.data(), col.p, sizeof(uint32_t) * A.nnz, cudaMemcpyDeviceToHost, st));
+        NF_CK(cudaMemcpyAsync(hgr.data(), chain64.p + na, sizeof(double) * na, cudaMemcpyDeviceToHost, st));
+        NF_CK(cudaStreamSynchronize(st));
+        std::vector<char> up(na, 0);
+        if (A.chains)
+            for (uint32_t a = 0; a + 1 < na; ++a) up[a] = hgr[a] > 0.0 ? 1 : 0;
+        std::vector<uint32_t> hperm;
+        bandw = rcm_order(na, hrow, hcol, up, &hperm);
+        const bool fits = bandw <= kBandMax && (double)na * (bandw + 1) * sizeof(double2) <= 1e9 &&
+                          (double)na * bandw * bandw <= 4e9;
+        if (P.method == 1 && !fits) { err = "the reordered band is too wide for the direct form"; return NF_ERR_PARAM; }
+        direct = P.method != 2 && fits;
+        if (direct) {
+            NF_CK(dperm.ensure(na));
+            NF_CK(cudaMemcpyAsync(dperm.p, hperm.data(), sizeof(uint32_t) * na, cudaMemcpyHostToDevice, st));
+        }
+    }
+    // Frequencies per launch: the work memory of the batch held to ~4 GB.
+    const size_t per = direct ? ((size_t)na * (bandw + 1) + 5 * (size_t)na) * sizeof(double2)
+                              : kAcD2 * sizeof(double2) * (size_t)std::max<uint32_t>(na, 1);
+    const size_t batch = std::max<size_t>(1, std::min<size_t>(nfreq, (size_t)4e9 / std::max<size_t>(per, 1)));
+    DBuf<double2> dw, bwk;
     DBuf<double> wd;
     DBuf<AcOut> od;
     bool conv = true;
     if (na > 0) {
-        NF_CK(dw.ensure(kAcD2 * (size_t)na * batch));
+        if (direct) {
+            NF_CK(bwk.ensure((size_t)na * (bandw + 1) * batch));
+            NF_CK(dw.ensure(5 * (size_t)na * batch));
+        } else {
+            NF_CK(dw.ensure(kAcD2 * (size_t)na * batch));
+        }
         NF_CK(wd.ensure(batch));
         NF_CK(od.ensure(batch));
     }
@@ -542,9 +823,14 @@ nf_status Engine::ac_spectrum(const nf_ac_net* net, const nf_ac_params& P, const
         if (na > 0) {
             for (size_t j = 0; j < nb; ++j) hw[j] = 2.0 * kPi * freq[f0 + j] / w0;
             NF_CK(cudaMemcpyAsync(wd.p, hw.data(), 8 * nb, cudaMemcpyHostToDevice, st));
-            NF_LAUNCH(k_ac_cocg<512>, (unsigned)nb, 512, 0, st)(
-                (int)nb, wd.p, na, rowp.p, col.p, val64.p, valC64.p, diag64.p, diagC64.p, cdiag.p, cdiagC.p,
-                chain64.p, A.chains ? 1 : 0, bvec.p, bvecC.p, acchi.p, dw.p, tol, max_inner, od.p);
+            if (direct)
+                NF_LAUNCH(k_ac_band<256>, (unsigned)nb, 256, 0, st)(
+                    (int)nb, wd.p, na, bandw, dperm.p, rowp.p, col.p, val64.p, valC64.p, diag64.p, diagC64.p,
+                    chain64.p, A.chains ? 1 : 0, bvec.p, bvecC.p, acchi.p, bwk.p, dw.p, od.p);
+            else
+                NF_LAUNCH(k_ac_cocg<512>, (unsigned)nb, 512, 0, st)(
+                    (int)nb, wd.p, na, rowp.p, col.p, val64.p, valC64.p, diag64.p, diagC64.p, cdiag.p, cdiagC.p,
+                    chain64.p, A.chains ? 1 : 0, bvec.p, bvecC.p, acchi.p, dw.p, tol, max_inner, od.p);
             NF_CK(cudaGetLastError());
             NF_CK(cudaMemcpyAsync(ho.data(), od.p, sizeof(AcOut) * nb, cudaMemcpyDeviceToHost, st));
             NF_CK(cudaStreamSynchronize(st));
@@ -587,6 +873,8 @@ nf_status Engine::ac_spectrum(const nf_ac_net* net, const nf_ac_params& P, const
         stats->C0 = C0;
         stats->omega0 = w0;
         stats->ms = ms;
+        stats->bandwidth = bandw;
+        stats->direct = direct ? 1 : 0;
     }
     if (!conv) { err = "AC solve did not reach its tolerance at some frequency"; return NF_ERR_NOT_CONVERGED; }
     return NF_OK;

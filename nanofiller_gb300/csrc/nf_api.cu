@@ -763,7 +763,7 @@ nf_status nf_ac_spectrum(nf_handle* h, const nf_ac_net* net, const nf_ac_params*
     nf::Engine& E = h->E;
     if (!(p->r_cnt > 0) || !(p->l_cnt > 0) || !(p->phi_ev > 0) || !(p->eps_r > 0) || !(p->delta_min > 0) ||
         !(p->delta_tun >= 0) || !(p->delta_eff > 0) || !(p->c_min >= 0) || !(p->l_box > 0) ||
-        (p->own_radii != 0 && p->own_radii != 1))
+        (p->own_radii != 0 && p->own_radii != 1) || p->method < 0 || p->method > 2)
         return fail(h, NF_ERR_PARAM, "AC parameters out of range");
     for (size_t f = 0; f < n_freq; ++f)
         if (!(freq[f] > 0) || !std::isfinite(freq[f])) return fail(h, NF_ERR_PARAM, "frequencies must be positive");
