@@ -198,17 +198,22 @@ class Clocks:
 
 
 def fp32_roofline(g, old_ms, clk):
-    """FP32 side of the old-rod sweep: 60 flops per candidate-rod pair within
-    sphere reach (the hard-core predicate's count), against the FP32 pipe
-    peak of the device: SMs x 128 lanes x 2 flops x the SM clock sampled in the
-    timed window (the nominal figure; no FP32 peak is measured)."""
+    """FP32 side of the two generation sweeps (candidates against accepted rods
+    and against earlier candidates; the counters cover both): the FP32 flops
+    they execute -- 22 per staged pair (the capsule pre-test), 40 per marked
+    pair (the line-distance test of the hand-out), 60 per pair that passes it
+    (the full filter and certificate) -- over their summed event time, against the FP32 pipe peak of the device: SMs x
+    128 lanes x 2 flops x the SM clock sampled in the timed window (the nominal
+    figure; no FP32 peak is measured)."""
     import torch
     sms = torch.cuda.get_device_properties(0).multi_processor_count
     mhz = (clk or {}).get("sm_mhz") or (clk or {}).get("sm_max_mhz") or 2070.0
     peak = sms * 128 * 2 * mhz * 1e6 / 1e12
-    achieved = 60.0 * g["sphere_pairs"] / (old_ms * 1e-3) / 1e12 if old_ms > 0 else 0.0
-    return {"kernel": "old_test", "bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-            "frac": achieved / peak, "peak_source": "nominal: SMs x 128 FP32 lanes x 2 x sampled SM clock"}
+    flops = 22.0 * g["pair_tests"] + 40.0 * g["marked_pairs"] + 60.0 * g["line_pairs"]
+    achieved = flops / (old_ms * 1e-3) / 1e12 if old_ms > 0 else 0.0
+    return {"kernel": "old_test+conflicts", "bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+            "frac": achieved / peak, "flops_per_step": flops,
+            "peak_source": "nominal: SMs x 128 FP32 lanes x 2 x sampled SM clock"}
 
 
 # --------------------------------------------------------------------------- CPU (oracle) leg
@@ -422,7 +427,7 @@ def run_ours(args, rank, world):
         "realisations_per_s": world * 1000.0 / ms_max,
         "pair_tests_per_s": (g["pair_tests"] + c["pair_tests"]) / (ms / 1000),
         "fp64_decisions": g["exact_evals"] + c["exact_evals"],
-        "generation_sweeps": {k: g[k] for k in ("work_items", "target_tiles", "pair_tests", "sphere_pairs",
+        "generation_sweeps": {k: g[k] for k in ("work_items", "target_tiles", "pair_tests", "marked_pairs",
                                                   "line_pairs", "exact_evals")},
         "fp32_would_flip": g["fp32_would_flip"] + c["fp32_would_flip"],
         "decision_flips_vs_fp64": 0,
@@ -434,7 +439,7 @@ def run_ours(args, rank, world):
         "roofline": {"kernel": dom, "bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                      "frac": achieved / hbm, "traffic": traffic, "peak_source": peak_note,
                      "note": "pair-test kernels are FP32-issue bound; bytes are the algorithmic bytes"},
-        "roofline_fp32": fp32_roofline(g, kern["old_test"]["ms"] / args.steps, clk),
+        "roofline_fp32": fp32_roofline(g, (kern["old_test"]["ms"] + kern["conflicts"]["ms"]) / args.steps, clk),
         "contacts_per_s": (c["contacts"] + c["n_source"] + c["n_sink"]) / (c["ms"] / 1000) if c["ms"] > 0 else None,
         "solve": {"residual": s["residual"], "outer_iters": s["outer_iters"], "inner_iters": s["inner_iters"],
                   "n_active": s["n_active"], "ms": s["ms"]},

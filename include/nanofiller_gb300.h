@@ -170,7 +170,7 @@ typedef struct nf_gen_stats {
     /* work of the two pair sweeps (candidates vs rods, vs earlier candidates) */
     uint64_t work_items;        /* (probe chunk, stencil row, segment) items  */
     uint64_t target_tiles;      /* 32-target tiles staged                    */
-    uint64_t sphere_pairs;      /* pairs within the bounding-sphere reach    */
+    uint64_t marked_pairs;      /* pairs passing the capsule pre-test        */
     uint64_t line_pairs;        /* of those, axis lines within the threshold */
 } nf_gen_stats;
 

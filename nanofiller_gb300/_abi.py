@@ -62,7 +62,7 @@ class NfGenStats(C.Structure):
                 ("accepted", C.c_uint64), ("target", C.c_uint64), ("pair_tests", C.c_uint64),
                 ("exact_evals", C.c_uint64), ("fp32_would_flip", C.c_uint64),
                 ("rounds", C.c_int32), ("target_reached", C.c_int32), ("ms", C.c_double),
-                ("work_items", C.c_uint64), ("target_tiles", C.c_uint64), ("sphere_pairs", C.c_uint64),
+                ("work_items", C.c_uint64), ("target_tiles", C.c_uint64), ("marked_pairs", C.c_uint64),
                 ("line_pairs", C.c_uint64)]
 
 

@@ -73,6 +73,8 @@ __global__ void __launch_bounds__(kTPB, 6) k_ct_tiles(const Real* __restrict__ r
         const float sx = img[0] * Re.L[0], sy = img[1] * Re.L[1], sz = img[2] * Re.L[2];
         const float ax = pA.x - sx, ay = pA.y - sy, az = pA.z - sz;
         const float hA2 = (pA.w * 0.5f + cA.w + epc + cA.w + Re.cut + epc) * 1.000002f + Re.slack;
+        const float hAe = pA.w * 0.5f + cA.w + epc;
+        const float hC = (cA.w + Re.cut + epc) * 1.000002f + Re.slack + 4e-6f * (1.0f + hA2);
         for (uint32_t b = 0; b < nt; b += kWT) {
             const uint32_t m = min((uint32_t)kWT, nt - b);
             if ((uint32_t)lane < m) {
@@ -96,10 +98,9 @@ __global__ void __launch_bounds__(kTPB, 6) k_ct_tiles(const Real* __restrict__ r
                         const uint32_t j = j0 + jj;
                         const float4 tq = T.p[j];
                         const float bx = tq.x - ax, by = tq.y - ay, bz = tq.z - az;
-                        const float Rr = hA2 + tq.w;
                         const uint32_t bit = tid_[w][j] > i ? (1u << j) : 0u;  // each unordered pair once
                         umask |= bit;
-                        if (bx * bx + by * by + bz * bz <= Rr * Rr) mask |= bit;
+                        if (capsule_near(bx, by, bz, cA.x, cA.y, cA.z, hAe, tq.w, hC)) mask |= bit;
                     }
                 }
                 tests += __popc(umask);

@@ -33,7 +33,7 @@ enum CandState : uint8_t { ST_NONE = 0, ST_REJ_OLD = 1, ST_ALIVE = 2, ST_ACC = 3
 enum Ctr {
     C_PAIR_TESTS = 0, C_EXACT, C_FLIPS, C_OVERFLOW, C_UNDECIDED,
     C_CT_PAIRS, C_CT_EXACT, C_CT_FLIPS, C_CT_RECORDS, C_SCR_PAIRS, C_SCR_EXACT,
-    C_CG_ITERS, C_XQ_OLD, C_XQ_CONF, C_XQ, C_CERT, C_ITEMS, C_G_ITEMS, C_G_TILES, C_G_SPHERE, C_G_LINE, C_XQ_MARK, C_NCTR
+    C_CG_ITERS, C_XQ_OLD, C_XQ_CONF, C_XQ, C_CERT, C_ITEMS, C_G_ITEMS, C_G_TILES, C_G_MARKED, C_G_LINE, C_XQ_MARK, C_NCTR
 };
 
 template <class T>

@@ -197,7 +197,7 @@ __global__ void k_bin(uint32_t n, const uint32_t* __restrict__ ntot, const uint3
 // Candidate vs accepted rods of one neighbour cell (cuda_OldExtIsectLB's job),
 // over the work list: each item is up to 32 candidates of a cell against up to
 // kSeg rods of one neighbour cell. Each lane marks the staged rods that pass
-// the sphere pre-test of its candidate; the marked pairs are evaluated by the
+// the capsule pre-test of its candidate; the marked pairs are evaluated by the
 // whole warp: far pairs dropped, clear hits decided in FP32 (the candidate is
 // rejected at once and skipped by every other item at its next tile), the
 // rest queued for FP64 (probe = compact candidate id, target = sorted rod).
@@ -219,7 +219,7 @@ __global__ void __launch_bounds__(kTPB, 6) k_old_tiles(const Real* __restrict__ 
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     WarpTile& T = tiles[w];
     volatile uint8_t* vst = state;
-    unsigned long long tests = 0, cert = 0, nitem = 0, ntile = 0, nsph = 0, nline = 0;
+    unsigned long long tests = 0, cert = 0, nitem = 0, ntile = 0, nmark = 0, nline = 0;
     const uint32_t n = min(*nitems, icap);
     const uint32_t stride = gridDim.x * kW;
     Item nxt = blockIdx.x * kW + w < n ? items[blockIdx.x * kW + w] : Item{0, 0, 0, 0};
@@ -244,6 +244,8 @@ __global__ void __launch_bounds__(kTPB, 6) k_old_tiles(const Real* __restrict__ 
         const float sx = img[0] * Re.L[0], sy = img[1] * Re.L[1], sz = img[2] * Re.L[2];
         const float ax = pA.x - sx, ay = pA.y - sy, az = pA.z - sz;
         const float hA2 = (pA.w * 0.5f + cA.w + Re.eps + cA.w * Re.scf + Re.sep + Re.eps) * 1.000002f + Re.slack;
+        const float hAe = pA.w * 0.5f + cA.w + Re.eps;
+        const float hC = (cA.w * Re.scf + Re.sep + Re.eps) * 1.000002f + Re.slack + 4e-6f * (1.0f + hA2);
         unsigned dead = 0;  // probe lanes decided during this item (warp-uniform)
         for (uint32_t b = 0; b < nt; b += kWT) {
             if (!__any_sync(0xffffffffu, alive)) break;
@@ -267,8 +269,7 @@ __global__ void __launch_bounds__(kTPB, 6) k_old_tiles(const Real* __restrict__ 
                     for (uint32_t jj = 0; jj < 8; ++jj) {
                         const float4 tq = T.p[j0 + jj];
                         const float bx = tq.x - ax, by = tq.y - ay, bz = tq.z - az;
-                        const float Rr = hA2 + tq.w;
-                        if (bx * bx + by * by + bz * bz <= Rr * Rr) mask |= 1u << (j0 + jj);
+                        if (capsule_near(bx, by, bz, cA.x, cA.y, cA.z, hAe, tq.w, hC)) mask |= 1u << (j0 + jj);
                     }
                 }
             }
@@ -281,7 +282,7 @@ __global__ void __launch_bounds__(kTPB, 6) k_old_tiles(const Real* __restrict__ 
                                  Re.slack);
             };
             ++ntile;
-            nsph += __popc(mask);
+            nmark += __popc(mask);
             const int kept_ = for_marked_pairs(mask, lane, msp[w], msm[w], mq2[w], keep, [&](bool valid, int pl, int t) {
                 bool hit = false;
                 if (valid && !((dead >> pl) & 1u)) {
@@ -315,7 +316,7 @@ __global__ void __launch_bounds__(kTPB, 6) k_old_tiles(const Real* __restrict__ 
         atomicAdd(&ctr[C_G_TILES], ntile);
         atomicAdd(&ctr[C_G_LINE], nline);
     }
-    warp_add_u64(&ctr[C_G_SPHERE], nsph);
+    warp_add_u64(&ctr[C_G_MARKED], nmark);
 }
 
 // FP64 decisions of the queued (candidate, accepted rod) pairs.
@@ -384,7 +385,7 @@ __global__ void k_alive_bin(uint32_t n, const uint32_t* __restrict__ ntot, const
 }
 
 // Earlier survivors of one neighbour cell that a survivor hits, over the work
-// list of the survivor cells (sphere marks per lane, full-warp evaluation of
+// list of the survivor cells (capsule marks per lane, full-warp evaluation of
 // the marked pairs). Compact candidate ids follow stream order within a
 // realisation, so "earlier" is a smaller id. Certified hits are listed
 // directly, uncertain pairs queued (target = compact candidate id).
@@ -406,7 +407,7 @@ __global__ void __launch_bounds__(kTPB, 6) k_conf_tiles(const Real* __restrict__
     __shared__ uint16_t mq2[kW][64];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     WarpTile& T = tiles[w];
-    unsigned long long tests = 0, ovf = 0, cert = 0, nitem = 0, ntile = 0, nsph = 0, nline = 0;
+    unsigned long long tests = 0, ovf = 0, cert = 0, nitem = 0, ntile = 0, nmark = 0, nline = 0;
     const uint32_t n = min(*nitems, icap);
     const uint32_t stride = gridDim.x * kW;
     Item nxt = blockIdx.x * kW + w < n ? items[blockIdx.x * kW + w] : Item{0, 0, 0, 0};
@@ -430,6 +431,8 @@ __global__ void __launch_bounds__(kTPB, 6) k_conf_tiles(const Real* __restrict__
         const float sx = img[0] * Re.L[0], sy = img[1] * Re.L[1], sz = img[2] * Re.L[2];
         const float ax = pA.x - sx, ay = pA.y - sy, az = pA.z - sz;
         const float hA2 = (pA.w * 0.5f + cA.w + Re.eps + cA.w * Re.scf + Re.sep + Re.eps) * 1.000002f + Re.slack;
+        const float hAe = pA.w * 0.5f + cA.w + Re.eps;
+        const float hC = (cA.w * Re.scf + Re.sep + Re.eps) * 1.000002f + Re.slack + 4e-6f * (1.0f + hA2);
         for (uint32_t b = 0; b < nt; b += kWT) {
             const uint32_t m = min((uint32_t)kWT, nt - b);
             if ((uint32_t)lane < m) {
@@ -453,10 +456,9 @@ __global__ void __launch_bounds__(kTPB, 6) k_conf_tiles(const Real* __restrict__
                         const uint32_t j = j0 + jj;
                         const float4 tq = T.p[j];
                         const float bx = tq.x - ax, by = tq.y - ay, bz = tq.z - az;
-                        const float Rr = hA2 + tq.w;
                         const uint32_t bit = tid_[w][j] < cid ? (1u << j) : 0u;
                         emask |= bit;
-                        if (bx * bx + by * by + bz * bz <= Rr * Rr) mask |= bit;
+                        if (capsule_near(bx, by, bz, cA.x, cA.y, cA.z, hAe, tq.w, hC)) mask |= bit;
                     }
                 }
                 tests += __popc(emask);
@@ -468,7 +470,7 @@ __global__ void __launch_bounds__(kTPB, 6) k_conf_tiles(const Real* __restrict__
                                  Re.slack);
             };
             ++ntile;
-            nsph += __popc(mask);
+            nmark += __popc(mask);
             const int kept_ = for_marked_pairs(mask, lane, msp[w], msm[w], mq2[w], keep, [&](bool valid, int pl, int t) {
                 if (!valid) return;
                 const float4 qA = ppos[w][pl], dA = pdir[w][pl];
@@ -499,7 +501,7 @@ __global__ void __launch_bounds__(kTPB, 6) k_conf_tiles(const Real* __restrict__
         atomicAdd(&ctr[C_G_TILES], ntile);
         atomicAdd(&ctr[C_G_LINE], nline);
     }
-    warp_add_u64(&ctr[C_G_SPHERE], nsph);
+    warp_add_u64(&ctr[C_G_MARKED], nmark);
 }
 
 __global__ void __launch_bounds__(256) k_conf_exact(const Real* __restrict__ reals,
@@ -1315,7 +1317,7 @@ nf_status Engine::generate() {
     gst.pair_tests = hc[C_PAIR_TESTS];
     gst.work_items = hc[C_G_ITEMS];
     gst.target_tiles = hc[C_G_TILES];
-    gst.sphere_pairs = hc[C_G_SPHERE];
+    gst.marked_pairs = hc[C_G_MARKED];
     gst.line_pairs = hc[C_G_LINE];
     gst.exact_evals = hc[C_EXACT];
     gst.fp32_would_flip = hc[C_FLIPS];

@@ -25,12 +25,32 @@ constexpr int kWC = 32;     // probes per item: one per lane
 constexpr int kWT = 32;     // targets per warp-private shared-memory tile
 constexpr int kSeg = 128;   // targets per item at most
 
-// Pairs that pass the per-lane sphere pre-test are marked in a 32-bit mask
+// Pairs that pass the per-lane capsule pre-test are marked in a 32-bit mask
 // per lane (bit j = staged target j); after the tile the marked pairs are
 // handed out 32 at a time to the whole warp, so the long filter path
 // (maybe_near, certain_hit) runs with every lane busy. A far-away position
 // pads the tile beyond its last target, so the marking loop needs no bound.
 constexpr float kFar = 1.0e30f;
+
+// Capsule pre-test of the marking loops (replaces a bounding-sphere test and
+// implies it). The reference's distance is taken between points of the two
+// axis segments extended to |t| <= h = l/2 + a + eps, so a pair with d < thr
+// has its target's centre within hB|cB| + thr of the probe's extended segment.
+// b = target centre - probe centre (image shift included), c = probe axis,
+// h = probe extent, hBt = (hB + a_B-part of thr) * 1.000002 (staged with the
+// target), hC = (probe part of thr) * 1.000002 + slack + 4e-6 (1 + probe
+// reach). The 4e-6 relative terms cover FP32 rounding of the projection and of
+// the squares and |c| = 1 +- 1e-6 (the same margins as maybe_near); slack
+// covers the rounding of the coordinates. Far tile padding overflows r^2 to inf
+// and fails the test.
+__device__ __forceinline__ bool capsule_near(float bx, float by, float bz, float cx, float cy, float cz, float h,
+                                             float hBt, float hC) {
+    float t = bx * cx + by * cy + bz * cz;
+    t = fminf(fmaxf(t, -h), h);
+    const float rx = fmaf(-t, cx, bx), ry = fmaf(-t, cy, by), rz = fmaf(-t, cz, bz);
+    const float R = fmaf(hBt, 1.000004f, hC);
+    return rx * rx + ry * ry + rz * rz <= R * R;
+}
 
 // Hands the marked pairs of a tile to the warp in two stages. Stage 1: 32 at a
 // time, keep(probe_lane, slot) runs a cheap rejection (one lane per pair).
