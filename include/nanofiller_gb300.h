@@ -81,9 +81,9 @@ typedef struct nf_params {
     float tol;              /* TOL: geometric epsilon (1e-6)                 */
     float stat_dist_lim;    /* STAT_DIST_LIM: tunnelling cutoff              */
     int32_t wrt_bin;        /* WRT_BIN                                       */
-    int32_t self_align_step;/* SELF_ALLIGN_STEP (only 0 is run)              */
-    int32_t clust_flag;     /* CLUST_FLAG (only 0 is run)                    */
-    int32_t reduce_flag;    /* REDUCE_FLAG (only 0 is run)                   */
+    int32_t self_align_step;/* SELF_ALLIGN_STEP: law refit period in epochs  */
+    int32_t clust_flag;     /* CLUST_FLAG: snap candidates to older rods     */
+    int32_t reduce_flag;    /* REDUCE_FLAG: thin out after each refit        */
     /* --- project keys --- */
     uint64_t seed;          /* SEED: Philox4x32-10 key                       */
     uint64_t n_candidates;  /* CANDIDATES: stream budget                     */
@@ -131,6 +131,28 @@ typedef struct nf_params {
                                (get_elec_dmnID, inc/conductivity.h:71-90), one
                                per image rod                                 */
     int32_t pad_end;
+    /* --- adaptive generation: self-alignment, thin-out, clusterisation ---
+     * The reference refits per-cell orientation laws every SELF_ALLIGN_STEP
+     * rounds or when a round gained fewer than 1 % of the rods still missing
+     * (src/cudaMain.cu:122-132), deletes rods that the new laws make unlikely
+     * when REDUCE_FLAG is set (cudaThinOUT, src/cudaMain.cu:354-396) and, with
+     * CLUST_FLAG, snaps each new candidate parallel to a nearby older rod
+     * (cuda_Clusterize2Old, inc/cuda_Clusterize.h:14-100). Here the three act
+     * at fixed epochs of the candidate stream (rounds are not part of the
+     * result): self_align_step s > 0 refits after epoch e > 0 when e % s == 0
+     * or the epoch gained fewer than (target - count) / 100 rods; reduce_flag
+     * thins after each refit; clust_flag snaps the candidates of an epoch to
+     * the rods present when it starts.                                      */
+    float clust_dist;       /* CLUST_DIST_LIM (um): snap when the rods' closest
+                               points are at most this far apart (0.015)   */
+    float clust_angl;       /* CLUST_ANGL_LIM (rad): and their axes at most
+                               this angle apart (pi / 12)                  */
+    float align_cell;       /* ALIGN_CELL (um): edge of the orientation-law
+                               cells; 0 -> the rod length INC_LEN_MED      */
+    int32_t align_min;      /* ALIGN_MIN_RODS: rods a cell needs for a refit
+                               (4); cells with fewer keep their law        */
+    int64_t epoch_candidates; /* EPOCH_CANDIDATES: candidates per epoch;
+                               0 -> max(1024, target count)                */
 } nf_params;
 
 /* Rods, structure of arrays, caller-owned host buffers. Any array may be NULL. */
@@ -172,6 +194,11 @@ typedef struct nf_gen_stats {
     uint64_t target_tiles;      /* 32-target tiles staged                    */
     uint64_t marked_pairs;      /* pairs passing the capsule pre-test        */
     uint64_t line_pairs;        /* of those, axis lines within the threshold */
+    /* adaptive generation (zero when it is off) */
+    uint64_t epochs;            /* epochs of the candidate stream begun      */
+    uint64_t refits;            /* orientation-law refits                     */
+    uint64_t thinned;           /* rods removed by thin-out                   */
+    uint64_t snapped;           /* snaps of candidates to older rods          */
 } nf_gen_stats;
 
 typedef struct nf_contact_stats {
@@ -333,6 +360,16 @@ nf_status nf_write_internal_coo(nf_handle *h, const char *dir);
  * NF_ORIENT_VMF with concentration kappa > 0 about the preferred axis
  * (pref_phi, pref_theta) in radians. Rods already accepted stay. */
 nf_status nf_set_orientation(nf_handle *h, int32_t mode, float kappa, float pref_phi, float pref_theta);
+
+/* Per-cell orientation laws of the adaptive generation (self_align_step > 0
+ * or clust_flag), after nf_generate. ext[3] receives the law grid; for cell
+ * i + ext[0] (j + ext[1] k), axis[3 cell..] the law's axis and kappa[cell]
+ * its von Mises-Fisher concentration (0: isotropic). The reference keeps the
+ * same per cell (d_prefOrt, d_thetaMed/Dev, d_phiMed/Dev; resetOrt and
+ * resetAvgVec, inc/allignment_fit.h:214-458). NF_ERR_STATE when the handle
+ * generates without adaptive laws; NF_ERR_CAPACITY (count in *cells) when
+ * cap is too small. Either array may be NULL. */
+nf_status nf_orientation_laws(nf_handle *h, size_t cap, int32_t ext[3], float *axis, float *kappa, size_t *cells);
 
 /* ---- dead-end pruning: the `reduce` verb (src/NanoFiller.cpp:71-91) ---- */
 /* Replaces the reference's reduce loop (reduce(), src/conductivity.cu:79-138;

@@ -278,6 +278,21 @@ class Simulation:
         _check(self._L.nf_set_orientation(self._h, mode, kappa, pref_phi, pref_theta), self._h,
                "nf_set_orientation")
 
+    def orientation_laws(self):
+        """Per-cell orientation laws of the adaptive generation after
+        generate() (nf_orientation_laws): {"ext": (nx, ny, nz), "axis": (cells, 3),
+        "kappa": (cells,)}, cell = i + nx (j + ny k)."""
+        ext = np.zeros(3, np.int32)
+        n = C.c_size_t()
+        _check(self._L.nf_orientation_laws(self._h, 0, ext.ctypes.data_as(C.c_void_p), None, None, C.byref(n)),
+               self._h, "nf_orientation_laws")
+        axis = np.zeros((n.value, 3), np.float32)
+        kappa = np.zeros(n.value, np.float32)
+        _check(self._L.nf_orientation_laws(self._h, n.value, ext.ctypes.data_as(C.c_void_p),
+                                           axis.ctypes.data_as(C.c_void_p), kappa.ctypes.data_as(C.c_void_p),
+                                           C.byref(n)), self._h, "nf_orientation_laws")
+        return {"ext": tuple(int(v) for v in ext), "axis": axis, "kappa": kappa}
+
     def reduce(self, min_contacts=2):
         """Dead-end pruning (nf_reduce): keep the rods with at least
         min_contacts unscreened contacts, repeatedly; electrodes stay."""

@@ -40,6 +40,8 @@ class NfParams(C.Structure):
         ("stencil_radius", C.c_int32), ("round_overshoot", C.c_float), ("two_phase_work", C.c_double),
         ("rod_sigma", C.c_double),
         ("elec_buffer", C.c_int32), ("pad_end", C.c_int32),
+        ("clust_dist", C.c_float), ("clust_angl", C.c_float), ("align_cell", C.c_float),
+        ("align_min", C.c_int32), ("epoch_candidates", C.c_int64),
     ]
 
 
@@ -63,7 +65,8 @@ class NfGenStats(C.Structure):
                 ("exact_evals", C.c_uint64), ("fp32_would_flip", C.c_uint64),
                 ("rounds", C.c_int32), ("target_reached", C.c_int32), ("ms", C.c_double),
                 ("work_items", C.c_uint64), ("target_tiles", C.c_uint64), ("marked_pairs", C.c_uint64),
-                ("line_pairs", C.c_uint64)]
+                ("line_pairs", C.c_uint64), ("epochs", C.c_uint64), ("refits", C.c_uint64),
+                ("thinned", C.c_uint64), ("snapped", C.c_uint64)]
 
 
 class NfContactStats(C.Structure):
@@ -185,6 +188,7 @@ SIGNATURES = {
     "nf_write_internal_coo": (_st, [_H, C.c_char_p]),
     "nf_reduce": (_st, [_H, C.c_int32, _P(NfReduceStats)]),
     "nf_set_orientation": (_st, [_H, C.c_int32, C.c_float, C.c_float, C.c_float]),
+    "nf_orientation_laws": (_st, [_H, C.c_size_t, C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(C.c_size_t)]),
     "nf_stat_nematic": (_st, [_H, C.c_void_p, _P(C.c_double)]),
     "nf_stat_phitheta": (_st, [_H, C.c_int32, C.c_int32, C.c_void_p]),
     "nf_stat_pairs": (_st, [_H, C.c_int32, C.c_void_p, C.c_void_p, C.c_size_t, _P(NfPairStats)]),

@@ -52,8 +52,19 @@ nf_status validate(const nf_params& p, std::string* why) {
     if (p.field_dir != 0 && p.field_dir != 1 && p.field_dir != 2 && p.field_dir != 4) {
         *why = "FIELD_DIR must be 0, 1, 2 or 4"; return NF_ERR_PARAM;
     }
-    if (p.self_align_step > 0 || p.clust_flag || p.reduce_flag) {
-        *why = "self-alignment, clusterisation and thin-out are not run by this path"; return NF_ERR_UNSUPPORTED;
+    if (p.self_align_step < 0 || p.clust_flag < 0 || p.clust_flag > 1 || p.reduce_flag < 0 || p.reduce_flag > 1) {
+        *why = "SELF_ALLIGN_STEP must be >= 0, CLUST_FLAG and REDUCE_FLAG 0 or 1"; return NF_ERR_PARAM;
+    }
+    if (!(p.clust_dist >= 0) || !(p.clust_angl >= 0 && p.clust_angl <= 1.5707964f) || !(p.align_cell >= 0) ||
+        p.align_min < 0 || p.epoch_candidates < 0) {
+        *why = "CLUST_DIST_LIM >= 0, CLUST_ANGL_LIM in [0, pi/2], ALIGN_CELL >= 0, ALIGN_MIN_RODS >= 0 and "
+               "EPOCH_CANDIDATES >= 0 required";
+        return NF_ERR_PARAM;
+    }
+    if (p.clust_flag) {  // a candidate's neighbours are searched among the images -1..1
+        const float lmax = p.len_mode == NF_SIZE_LOGNORMAL ? p.len_max : p.l;
+        for (int d = 0; d < 3; ++d)
+            if (p.box[d] < lmax) { *why = "clusterisation needs box edges of at least the longest rod"; return NF_ERR_PARAM; }
     }
     if (p.theta_dev > 0 || p.phi_dev > 0) {
         *why = "truncated-normal orientation is not run by this path (use ORIENT VMF)"; return NF_ERR_UNSUPPORTED;
@@ -119,8 +130,14 @@ nf_status nf_params_default(nf_params* p) {
     p->sep = 0; p->sc_frac = 1.0f;
     p->stat_dist_lim = 0.015f;
     p->wrt_bin = 0;
-    p->self_align_step = 0;  // the reference defaults to 50; this path runs without self-alignment
+    p->self_align_step = 0;  // the reference defaults to 50 (and samples isotropically
+                             // while DEF_THETA_DEV is -1); here adaptation is asked for
     p->clust_flag = 0; p->reduce_flag = 0;
+    p->clust_dist = 0.015f;
+    p->clust_angl = 3.14159265359f / 12;  // Pi/12, src/simPrms.cpp:62-63
+    p->align_cell = 0;
+    p->align_min = 4;
+    p->epoch_candidates = 0;
     // project keys
     p->seed = 0;
     p->n_candidates = 1ull << 20;
@@ -184,7 +201,12 @@ nf_status nf_params_from_file(const char* path, nf_params* p, int* n_unknown) {
         else if (key == "SELF_ALLIGN_STEP") in >> p->self_align_step;
         else if (key == "REDUCE_FLAG") in >> p->reduce_flag;
         else if (key == "CLUST_FLAG") in >> p->clust_flag;
-        else if (key == "CLUST_DIST_LIM" || key == "CLUST_ANGL_LIM" || key == "SPAT_DIMENSIONS" ||
+        else if (key == "CLUST_DIST_LIM") in >> p->clust_dist;
+        else if (key == "CLUST_ANGL_LIM") in >> p->clust_angl;  // radians, read as is (src/simPrms.cpp:307)
+        else if (key == "ALIGN_CELL") in >> p->align_cell;
+        else if (key == "ALIGN_MIN_RODS") in >> p->align_min;
+        else if (key == "EPOCH_CANDIDATES") { long long s; in >> s; p->epoch_candidates = s; }
+        else if (key == "SPAT_DIMENSIONS" ||
                  key == "ORNT_DISTR_FILE" || key == "IDIM_DISTR_FILE" || key == "MATH_TOLERANCE" ||
                  key == "DMN_CELL_MARGE") { /* parsed and ignored, as the reference does */ }
         // project keys
@@ -613,6 +635,13 @@ nf_status nf_set_orientation(nf_handle* h, int32_t mode, float kappa, float pref
     return E.setup();  // the device descriptors follow at once
 }
 
+nf_status nf_orientation_laws(nf_handle* h, size_t cap, int32_t ext[3], float* axis, float* kappa, size_t* cells) {
+    if (!h) return NF_ERR_PARAM;
+    nf_status s = h->E.orientation_laws(cap, ext, axis, kappa, cells);
+    if (s != NF_OK) return fail(h, s, h->E.err);
+    return NF_OK;
+}
+
 nf_status nf_reduce(nf_handle* h, int32_t min_contacts, nf_reduce_stats* stats) {
     if (!h) return NF_ERR_PARAM;
     if (min_contacts < 0) return fail(h, NF_ERR_PARAM, "min_contacts must be >= 0");
@@ -798,6 +827,8 @@ nf_status nf_batch_run(const nf_params* params, int n, nf_batch_result* out, nf_
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return NF_ERR_NO_DEVICE;
     std::vector<nf_params> ps(params, params + n);
+    for (int r = 0; r < n; ++r)  // the adaptive generation runs on single-realisation handles
+        if (ps[r].self_align_step > 0 || ps[r].clust_flag) return NF_ERR_UNSUPPORTED;
     for (int r = 1; r < n; ++r)  // one electrode model and field axis per engine when buffer layers are used
         if ((ps[r].elec_buffer || ps[0].elec_buffer) &&
             (ps[r].elec_buffer != ps[0].elec_buffer || ps[r].field_dir != ps[0].field_dir))

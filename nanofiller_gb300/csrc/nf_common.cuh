@@ -172,7 +172,31 @@ struct Real {
     int32_t field_axis;     // 0,1,2 or -1
     int32_t ebuf;           // electrodes are buffer layers of images (else planes)
     double G0, lambda, dc;
+    // per-cell orientation laws of the adaptive generation (null: the global
+    // law above): kLawF floats per law cell, grid an[] with an[d] / L[d] in ainv
+    const float* law;
+    int32_t an[3];
+    float ainv[3];
 };
+
+// One orientation law: rotation m[9] (row-major, applied to the drawn
+// direction; column 2 is the law's axis), kappa, exp(-2 kappa), sampling
+// flags (bit 0: von Mises-Fisher with that kappa, else isotropic; bit 1:
+// rotate the draw by m). kappa > 0 with bit 0 clear: a fitted law that only
+// the thin-out uses.
+constexpr int kLawF = 12;
+
+// Law cell of a point: floor(x an / L) per axis, clamped to the grid.
+NF_HD uint32_t law_cell(const Real& R, float x, float y, float z) {
+    int c[3];
+    const float v[3] = {x, y, z};
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        int i = (int)fmul(v[d], R.ainv[d]);
+        c[d] = i < 0 ? 0 : (i >= R.an[d] ? R.an[d] - 1 : i);
+    }
+    return (uint32_t)(c[0] + R.an[0] * (c[1] + R.an[1] * c[2]));
+}
 
 NF_HD float lerp_nf(float a, float b, float f) { return fadd(a, fmul(fsub(b, a), f)); }
 
@@ -215,11 +239,24 @@ NF_HD void candidate(const Real& R, uint64_t k, float4* pos, float4* dir, float*
     float y = fmul(uni(A.y), R.L[1]);
     float z = fmul(uni(A.z), R.L[2]);
     float uu = uni(A.w);
+    // the law of the realisation, or of the candidate's law cell
+    const float* m = R.m;
+    float kappa = R.kappa, E2 = R.E2;
+    bool vmf = R.orient == 1, rot = R.rot != 0;
+    if (R.law) {
+        const float* Lw = R.law + (size_t)kLawF * law_cell(R, x, y, z);
+        m = Lw;
+        kappa = Lw[9];
+        E2 = Lw[10];
+        const int fl = (int)Lw[11];
+        vmf = (fl & 1) != 0;
+        rot = (fl & 2) != 0;
+    }
     float cz;
-    if (R.orient == 1) {
+    if (vmf) {
         float w = fsub(1.0f, uni(B.x));
-        float v = fadd(w, fmul(fsub(1.0f, w), R.E2));
-        cz = fadd(1.0f, fdiv(log_nf(v), R.kappa));
+        float v = fadd(w, fmul(fsub(1.0f, w), E2));
+        cz = fadd(1.0f, fdiv(log_nf(v), kappa));
         cz = cz < -1.0f ? -1.0f : (cz > 1.0f ? 1.0f : cz);
     } else {
         cz = fsub(fmul(uni(B.x), 2.0f), 1.0f);
@@ -229,10 +266,10 @@ NF_HD void candidate(const Real& R, uint64_t k, float4* pos, float4* dir, float*
     float sr = fsub(1.0f, fmul(cz, cz));
     float s = fsqrt(sr > 0.0f ? sr : 0.0f);
     float cx = fmul(s, cp), cy = fmul(s, sp);
-    if (R.rot) {
-        float rx = fadd(fadd(fmul(R.m[0], cx), fmul(R.m[1], cy)), fmul(R.m[2], cz));
-        float ry = fadd(fadd(fmul(R.m[3], cx), fmul(R.m[4], cy)), fmul(R.m[5], cz));
-        float rz = fadd(fadd(fmul(R.m[6], cx), fmul(R.m[7], cy)), fmul(R.m[8], cz));
+    if (rot) {
+        float rx = fadd(fadd(fmul(m[0], cx), fmul(m[1], cy)), fmul(m[2], cz));
+        float ry = fadd(fadd(fmul(m[3], cx), fmul(m[4], cy)), fmul(m[5], cz));
+        float rz = fadd(fadd(fmul(m[6], cx), fmul(m[7], cy)), fmul(m[8], cz));
         cx = rx; cy = ry; cz = rz;
     }
     float len = R.l;

@@ -36,10 +36,16 @@ enum Ctr {
     C_CG_ITERS, C_XQ_OLD, C_XQ_CONF, C_XQ, C_CERT, C_ITEMS, C_G_ITEMS, C_G_TILES, C_G_MARKED, C_G_LINE, C_XQ_MARK, C_NCTR
 };
 
+// Device buffer owned by its object: freed by release() or the destructor
+// (cudaFree waits for the device work that may still use it).
 template <class T>
 struct DBuf {
     T* p = nullptr;
     size_t cap = 0;
+    DBuf() = default;
+    DBuf(const DBuf&) = delete;
+    DBuf& operator=(const DBuf&) = delete;
+    ~DBuf() { release(); }
     cudaError_t ensure(size_t n) {
         if (n <= cap && p) return cudaSuccess;
         if (p) cudaFree(p);
@@ -177,6 +183,17 @@ struct Engine {
     std::vector<nf_solve_stats> solve_st;
     bool solve_valid = false;
 
+    // adaptive generation (single realisation): per-cell orientation laws,
+    // their tensor sums, and the clusterisation neighbour lists
+    std::vector<float> hlaw;        // kLawF floats per law cell (host mirror)
+    DBuf<float> law;
+    DBuf<unsigned long long> lacc;  // 7 fixed-point sums per law cell
+    int32_t lawn[3] = {0, 0, 0};
+    bool laws_set = false;          // hlaw holds the laws of the last generation
+    DBuf<uint32_t> clu_cnt, clu_off, clu_snaps;
+    DBuf<unsigned long long> clu_key, clu_key2;
+    uint64_t ad_epochs = 0, ad_refits = 0, ad_thinned = 0, ad_snapped = 0;
+
     // stats
     nf_gen_stats gst{};
     nf_contact_stats cst{};
@@ -213,6 +230,20 @@ struct Engine {
     // Dead-end pruning (the reference's reduce): keep the min_cont-core of the
     // unscreened contact graph, electrodes kept.
     nf_status prune(int min_cont, nf_reduce_stats* out);
+    // Stable compaction of rods [0, n) of a single realisation to those with
+    // keep[i] != 0 (stream order kept), then a rebuild of the cell lists.
+    nf_status compact_rods(const uint32_t* keep, uint32_t n, uint32_t left);
+    // Adaptive generation: whether it is on, the law grid set-up (global law
+    // in every cell), the refit + thin-out at an epoch boundary, and the
+    // clusterisation of the round's kept candidates onto the n_old rods
+    // present when the epoch began.
+    bool adaptive() const;
+    nf_status laws_reset();
+    nf_status epoch_boundary(uint64_t epoch_done, uint32_t gained);
+    nf_status clusterize(uint64_t slots, const uint32_t* ntot, uint32_t n_old);
+    // adds the snaps of the round's candidates with stream index < limit
+    nf_status count_snaps(uint64_t slots, const uint32_t* ntot, uint64_t limit);
+    nf_status orientation_laws(size_t cap, int32_t ext[3], float* axis, float* kappa, size_t* cells);
     // AC admittance spectrum of the handle's network (net == nullptr) or of a
     // host-given network.
     nf_status ac_spectrum(const nf_ac_net* net, const nf_ac_params& p, const double* freq, size_t nfreq,

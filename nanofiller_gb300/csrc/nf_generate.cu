@@ -1014,6 +1014,18 @@ nf_status Engine::generate() {
     contacts_valid = false;
     solve_valid = false;
     int_valid = false;
+    // Adaptive generation: epochs of the candidate stream (a round never
+    // crosses a boundary); laws refit and rods thinned at boundaries; the
+    // candidates of an epoch snap to the n_old rods present when it began.
+    s = laws_reset();
+    if (s != NF_OK) return s;
+    const bool adapt = adaptive();
+    ad_epochs = ad_refits = ad_thinned = ad_snapped = 0;
+    const uint64_t epoch_len = adapt ? (prm[0].epoch_candidates > 0 ? (uint64_t)prm[0].epoch_candidates
+                                                                      : std::max<uint64_t>(1024, hreal[0].target))
+                                     : 0;
+    uint64_t epoch_begun = ~0ull;
+    uint32_t epoch_count0 = 0, n_old = 0;
 
     // Round sizing statistics.
     std::vector<double> p_dens(R), alive_max(R);
@@ -1043,6 +1055,17 @@ nf_status Engine::generate() {
     int rounds = 0;
     const int max_rounds = 100000;
     for (; rounds < max_rounds; ++rounds) {
+        if (adapt && count[0] < hreal[0].target && knext[0] < prm[0].n_candidates && knext[0] % epoch_len == 0 &&
+            knext[0] != epoch_begun) {
+            if (knext[0] > 0) {
+                s = epoch_boundary(knext[0] / epoch_len - 1, count[0] - epoch_count0);
+                if (s != NF_OK) return s;
+            }
+            epoch_begun = knext[0];
+            epoch_count0 = count[0];
+            n_old = count[0];
+            ++ad_epochs;
+        }
         uint64_t slots = 0;
         int active = 0;
         for (int r = 0; r < R; ++r) {
@@ -1070,6 +1093,7 @@ nf_status Engine::generate() {
                 c = (uint64_t)std::max(64.0, cr);
                 c = std::min<uint64_t>(c, p.n_candidates - knext[r]);
                 c = std::min<uint64_t>(c, 1u << 24);
+                if (adapt) c = std::min<uint64_t>(c, epoch_len - knext[r] % epoch_len);
                 ++active;
             }
             c_round[r] = c;
@@ -1128,6 +1152,11 @@ nf_status Engine::generate() {
         NF_LAUNCH(k_compact, gs, 256, 0, st)(dreal.p, R, coff.p, kbeg.p, (uint32_t)slots, keep.p, kpos.p, cpos.p, cdir.p,
                                      csidx.p, creal.p, ccell.p, ccount.p, state.p);
         NF_CK(cudaGetLastError());
+        const bool clustered = adapt && prm[0].clust_flag && n_old > 0;
+        if (clustered) {
+            s = clusterize(slots, ntot, n_old);
+            if (s != NF_OK) return s;
+        }
         s = scan_u32(ccount.p, cstart.p, ncell + 1);
         if (s != NF_OK) return s;
         NF_CK(cudaMemsetAsync(ccursor.p, 0, sizeof(uint32_t) * (ncell + 1), st));
@@ -1292,6 +1321,10 @@ nf_status Engine::generate() {
             knext[r] += c_round[r];
             if (count[r] < hreal[r].target) drawn[r] = knext[r];
         }
+        if (clustered) {  // snaps of the candidates this round consumed
+            s = count_snaps(slots, ntot, drawn[0]);
+            if (s != NF_OK) return s;
+        }
         NF_CK(cudaMemcpyAsync(dcount.p, count.data(), sizeof(uint32_t) * R, cudaMemcpyHostToDevice, st));
         if (any_new) {
             s = rebuild_cells();
@@ -1323,6 +1356,10 @@ nf_status Engine::generate() {
     gst.fp32_would_flip = hc[C_FLIPS];
     gst.exact_evals = hc[C_EXACT];
     gst.rounds = rounds;
+    gst.epochs = ad_epochs;
+    gst.refits = ad_refits;
+    gst.thinned = ad_thinned;
+    gst.snapped = ad_snapped;
     gst.target_reached = gst.accepted == gst.target;
     gst.ms = ms;
     return NF_OK;

@@ -65,6 +65,33 @@ __global__ void k_prune_gather(uint32_t n, const uint32_t* __restrict__ alive, c
     s2[q] = s[i];
 }
 
+nf_status Engine::compact_rods(const uint32_t* keepf, uint32_t n, uint32_t left) {
+    if (R != 1) { err = "rod compaction runs on a single-realisation handle"; return NF_ERR_STATE; }
+    DBuf<uint32_t> posn;
+    NF_CK(posn.ensure(n + 1));
+    nf_status s = scan_u32(keepf, posn.p, n + 1);
+    if (s != NF_OK) return s;
+    DBuf<float4> p2, d2;
+    DBuf<uint64_t> s2;
+    NF_CK(p2.ensure(left + 1));
+    NF_CK(d2.ensure(left + 1));
+    NF_CK(s2.ensure(left + 1));
+    if (n)
+        NF_LAUNCH(k_prune_gather, grid_for(n, 256), 256, 0, st)(n, keepf, posn.p, pos.p, dir.p, sidx.p, p2.p, d2.p,
+                                                               s2.p);
+    NF_CK(cudaGetLastError());
+    if (left) {
+        NF_CK(cudaMemcpyAsync(pos.p, p2.p, sizeof(float4) * left, cudaMemcpyDeviceToDevice, st));
+        NF_CK(cudaMemcpyAsync(dir.p, d2.p, sizeof(float4) * left, cudaMemcpyDeviceToDevice, st));
+        NF_CK(cudaMemcpyAsync(sidx.p, s2.p, sizeof(uint64_t) * left, cudaMemcpyDeviceToDevice, st));
+    }
+    count[0] = left;
+    NF_CK(cudaMemcpyAsync(dcount.p, count.data(), sizeof(uint32_t), cudaMemcpyHostToDevice, st));
+    // the temporaries are freed on return: finish their use first
+    NF_CK(cudaStreamSynchronize(st));
+    return rebuild_cells();
+}
+
 nf_status Engine::prune(int min_cont, nf_reduce_stats* out) {
     if (R != 1) { err = "pruning runs on a single-realisation handle"; return NF_ERR_STATE; }
     if (min_cont < 0) return NF_ERR_PARAM;
@@ -79,10 +106,9 @@ nf_status Engine::prune(int min_cont, nf_reduce_stats* out) {
     if (s != NF_OK) return s;
     const uint32_t n = count[0];
     const uint32_t m = (uint32_t)ct_off[1];
-    DBuf<uint32_t> alive, deg, posn, ctr1;
+    DBuf<uint32_t> alive, deg, ctr1;
     NF_CK(alive.ensure(n + 1));
     NF_CK(deg.ensure(n + 1));
-    NF_CK(posn.ensure(n + 1));
     NF_CK(ctr1.ensure(1));
     // every rod starts alive
     std::vector<uint32_t> ones(n + 1, 1u);
@@ -105,24 +131,7 @@ nf_status Engine::prune(int min_cont, nf_reduce_stats* out) {
     }
     // stable compaction of the survivors
     if (left < n) {
-        s = scan_u32(alive.p, posn.p, n + 1);
-        if (s != NF_OK) return s;
-        DBuf<float4> p2, d2;
-        DBuf<uint64_t> s2;
-        NF_CK(p2.ensure(left + 1));
-        NF_CK(d2.ensure(left + 1));
-        NF_CK(s2.ensure(left + 1));
-        NF_LAUNCH(k_prune_gather, grid_for(n, 256), 256, 0, st)(n, alive.p, posn.p, pos.p, dir.p, sidx.p, p2.p, d2.p,
-                                                               s2.p);
-        NF_CK(cudaGetLastError());
-        if (left) {
-            NF_CK(cudaMemcpyAsync(pos.p, p2.p, sizeof(float4) * left, cudaMemcpyDeviceToDevice, st));
-            NF_CK(cudaMemcpyAsync(dir.p, d2.p, sizeof(float4) * left, cudaMemcpyDeviceToDevice, st));
-            NF_CK(cudaMemcpyAsync(sidx.p, s2.p, sizeof(uint64_t) * left, cudaMemcpyDeviceToDevice, st));
-        }
-        count[0] = left;
-        NF_CK(cudaMemcpyAsync(dcount.p, count.data(), sizeof(uint32_t), cudaMemcpyHostToDevice, st));
-        s = rebuild_cells();
+        s = compact_rods(alive.p, n, left);
         if (s != NF_OK) return s;
     }
     contacts_valid = false;

@@ -131,7 +131,25 @@ struct Stream {
     const float* mesh;
     int n[3];
     float dflt;
+    // per-cell orientation laws of the adaptive generation (null: the law above)
+    const float* law = nullptr;
+    int an[3] = {1, 1, 1};
+    float ainv[3] = {0, 0, 0};
 };
+
+// Law layout: m[9] row-major (column 2 the axis), kappa, exp(-2 kappa),
+// sampling flags (bit 0 von Mises-Fisher, bit 1 rotate).
+constexpr int kLawF = 12;
+
+int law_cell(const Stream& S, float x, float y, float z) {
+    const float v[3] = {x, y, z};
+    int c[3];
+    for (int d = 0; d < 3; ++d) {
+        int i = (int)(v[d] * S.ainv[d]);
+        c[d] = i < 0 ? 0 : (i >= S.an[d] ? S.an[d] - 1 : i);
+    }
+    return c[0] + S.an[0] * (c[1] + S.an[1] * c[2]);
+}
 
 Stream make_stream(const nf_params* p, const float* mesh, int nx, int ny, int nz) {
     Stream S;
@@ -198,11 +216,23 @@ void candidate(const Stream& S, uint64_t k, float* o) {
     float y = uni(A[1]) * S.L[1];
     float z = uni(A[2]) * S.L[2];
     float u = uni(A[3]);
+    const float* m = S.m;
+    float kappa = S.kappa, E2 = S.E2;
+    bool vmf = S.orient == NF_ORIENT_VMF, rot = S.rot;
+    if (S.law) {  // the law of the candidate's cell
+        const float* Lw = S.law + (size_t)kLawF * law_cell(S, x, y, z);
+        m = Lw;
+        kappa = Lw[9];
+        E2 = Lw[10];
+        const int fl = (int)Lw[11];
+        vmf = (fl & 1) != 0;
+        rot = (fl & 2) != 0;
+    }
     float cz;
-    if (S.orient == NF_ORIENT_VMF) {
+    if (vmf) {
         float w = 1.0f - uni(B[0]);
-        float v = w + (1.0f - w) * S.E2;
-        cz = 1.0f + logf_nf(v) / S.kappa;
+        float v = w + (1.0f - w) * E2;
+        cz = 1.0f + logf_nf(v) / kappa;
         if (cz < -1.0f) cz = -1.0f;
         if (cz > 1.0f) cz = 1.0f;
     } else {
@@ -213,10 +243,10 @@ void candidate(const Stream& S, uint64_t k, float* o) {
     float sr = 1.0f - cz * cz;
     float s = std::sqrt(sr > 0.0f ? sr : 0.0f);
     float cx = s * cp, cy = s * sp;
-    if (S.rot) {
-        float rx = (S.m[0] * cx + S.m[1] * cy) + S.m[2] * cz;
-        float ry = (S.m[3] * cx + S.m[4] * cy) + S.m[5] * cz;
-        float rz = (S.m[6] * cx + S.m[7] * cy) + S.m[8] * cz;
+    if (rot) {
+        float rx = (m[0] * cx + m[1] * cy) + m[2] * cz;
+        float ry = (m[3] * cx + m[4] * cy) + m[5] * cz;
+        float rz = (m[6] * cx + m[7] * cy) + m[8] * cz;
         cx = rx; cy = ry; cz = rz;
     }
     float len = S.l;
@@ -470,6 +500,184 @@ struct DSU {
     }
 };
 
+// ---------------------------------------------------------------------------
+// Adaptive generation (project-defined restatement of the reference's
+// self-alignment, thin-out and clusterisation; src/cudaMain.cu:112-132,
+// 254-273, 354-396, inc/allignment_fit.h, inc/cuda_Clusterize.h).
+// ---------------------------------------------------------------------------
+constexpr double kFix40 = 1099511627776.0;  // 2^40
+
+void law_grid(const nf_params* p, int n[3], float inv[3]) {
+    const double e = p->align_cell > 0 ? (double)p->align_cell : (double)p->l;
+    for (int d = 0; d < 3; ++d) {
+        const double c = std::floor((double)p->box[d] / e);
+        n[d] = c < 1 ? 1 : (c > 256 ? 256 : (int)c);
+        inv[d] = (float)((double)n[d] / (double)p->box[d]);
+    }
+}
+
+// Eigen-decomposition of a symmetric 3x3 matrix by cyclic Jacobi rotations
+// (Golub & Van Loan, Matrix Computations, sec. 8.5): A diagonal on return,
+// eigenvectors in the columns of V.
+void sym_eig3(double A[3][3], double V[3][3]) {
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) V[i][j] = i == j ? 1.0 : 0.0;
+    const int pairs[3][2] = {{0, 1}, {0, 2}, {1, 2}};
+    for (int sweep = 0; sweep < 64; ++sweep) {
+        if (A[0][1] == 0.0 && A[0][2] == 0.0 && A[1][2] == 0.0) break;
+        for (int r = 0; r < 3; ++r) {
+            const int p = pairs[r][0], q = pairs[r][1];
+            if (A[p][q] == 0.0) continue;
+            const double th = (A[q][q] - A[p][p]) / (2.0 * A[p][q]);
+            const double at = th < 0 ? -th : th;
+            double t = at > 1e150 ? 0.5 / at : 1.0 / (at + std::sqrt(th * th + 1.0));
+            if (th < 0) t = -t;
+            const double c = 1.0 / std::sqrt(t * t + 1.0), sn = t * c;
+            for (int k = 0; k < 3; ++k) {
+                const double x = A[k][p], y = A[k][q];
+                A[k][p] = c * x - sn * y;
+                A[k][q] = sn * x + c * y;
+            }
+            for (int k = 0; k < 3; ++k) {
+                const double x = A[p][k], y = A[q][k];
+                A[p][k] = c * x - sn * y;
+                A[q][k] = sn * x + c * y;
+            }
+            A[p][q] = A[q][p] = 0.0;
+            for (int k = 0; k < 3; ++k) {
+                const double x = V[k][p], y = V[k][q];
+                V[k][p] = c * x - sn * y;
+                V[k][q] = sn * x + c * y;
+            }
+        }
+    }
+}
+
+// E[(c.mu)^2] under a von Mises-Fisher law of concentration k.
+double vmf_second_moment(double k) {
+    if (k < 0.05) {
+        const double k2 = k * k;
+        return 1.0 / 3.0 + k2 * (2.0 / 45.0 - k2 * (4.0 / 945.0));
+    }
+    return 1.0 - 2.0 / (k * std::tanh(k)) + 2.0 / (k * k);
+}
+
+// A cell's law from its exact sums {n, xx, yy, zz, xy, xz, yz}.
+void law_from_sums(const int64_t sm[7], bool sample, float* Lw) {
+    const double f = 1.0 / ((double)sm[0] * kFix40);
+    double A[3][3] = {{sm[1] * f, sm[4] * f, sm[5] * f}, {sm[4] * f, sm[2] * f, sm[6] * f},
+                      {sm[5] * f, sm[6] * f, sm[3] * f}};
+    double V[3][3];
+    sym_eig3(A, V);
+    int b = 0;
+    for (int k = 1; k < 3; ++k)
+        if (A[k][k] > A[b][b]) b = k;
+    double mu[3] = {V[0][b], V[1][b], V[2][b]};
+    const double nm = std::sqrt(mu[0] * mu[0] + mu[1] * mu[1] + mu[2] * mu[2]);
+    for (int d = 0; d < 3; ++d) mu[d] /= nm;
+    if (mu[2] < 0 || (mu[2] == 0 && (mu[1] < 0 || (mu[1] == 0 && mu[0] < 0))))
+        for (int d = 0; d < 3; ++d) mu[d] = -mu[d];
+    const double lam = A[b][b];
+    double kap = 0.0;
+    if (lam > 1.0 / 3.0 + 1e-9) {
+        double lo = 0.0, hi = 500.0;
+        if (vmf_second_moment(hi) <= lam) {
+            kap = hi;
+        } else {
+            for (int it = 0; it < 64; ++it) {
+                const double mid = 0.5 * (lo + hi);
+                if (vmf_second_moment(mid) < lam) lo = mid; else hi = mid;
+            }
+            kap = 0.5 * (lo + hi);
+        }
+    }
+    // basis with mu as third column (Duff et al. 2017, "Building an
+    // Orthonormal Basis, Revisited"); mu_z >= 0 here
+    const double sg = mu[2] >= 0 ? 1.0 : -1.0;
+    const double a = -1.0 / (sg + mu[2]), bb = mu[0] * mu[1] * a;
+    const double e1[3] = {1.0 + sg * mu[0] * mu[0] * a, sg * bb, -sg * mu[0]};
+    const double e2[3] = {bb, sg + mu[1] * mu[1] * a, -mu[1]};
+    for (int r = 0; r < 3; ++r) {
+        Lw[3 * r] = (float)e1[r];
+        Lw[3 * r + 1] = (float)e2[r];
+        Lw[3 * r + 2] = (float)mu[r];
+    }
+    const float kf = (float)kap;
+    Lw[9] = kf;
+    Lw[10] = (float)std::exp(-2.0 * (double)kf);
+    Lw[11] = sample ? (float)((kf > 0.0f ? 1 : 0) | 2) : 0.0f;
+}
+
+inline float dotf(const float* a, const float* b) { return (a[0] * b[0] + a[1] * b[1]) + a[2] * b[2]; }
+
+// cnt_minDist (inc/intersection_dev.h:85-160) in FP32; the parameters before
+// the clamp in *t0u, *t1u.
+float min_dist_f32(const float r1[3], const float c1[3], float l1, float a1, const float r2[3], const float c2[3],
+                   float l2, float a2, float eps, bool typo, float* t0u, float* t1u) {
+    const float b[3] = {r2[0] - r1[0], r2[1] - r1[1], r2[2] - r1[2]};
+    const float d = dotf(c1, c2);
+    float t0, t1;
+    if (1.0f - std::fabs(d) > eps) {
+        float a[3] = {d * c2[0] - c1[0], d * c2[1] - c1[1], d * c2[2] - c1[2]};
+        t0 = dotf(a, b);
+        const float a2v[3] = {c2[0] - d * c1[0], c2[1] - d * c1[1], c2[2] - d * c1[2]};
+        t1 = dotf(a2v, b);
+        const float den = d * d - 1.0f;
+        t0 /= den;
+        t1 /= den;
+    } else {
+        t0 = std::copysign(l1 / 2.0f, dotf(b, c1));
+        const float dt = typo ? (b[0] * c2[0] + b[0] * c2[1]) + b[0] * c2[2] : dotf(b, c2);
+        t1 = -1.0f * dt + d * t0;
+    }
+    *t0u = t0;
+    *t1u = t1;
+    const float h1 = l1 / 2.0f, h2 = l2 / 2.0f;
+    const bool f1 = std::fabs(t0) <= (h1 + a1) + eps;
+    const bool f2 = std::fabs(t1) <= (h2 + a2) + eps;
+    if (!(f1 && f2)) {
+        if (std::fabs(t0) - h1 < std::fabs(t1) - h2) {
+            t1 = std::copysign(h2, t1);
+            t0 = dotf(b, c1) + d * t1;
+            if (std::fabs(t0) > h1) t0 = std::copysign(h1, t0);
+        } else {
+            t0 = std::copysign(h1, t0);
+            t1 = -1.0f * dotf(b, c2) + d * t0;
+            if (std::fabs(t1) > h2) t1 = std::copysign(h2, t1);
+        }
+    }
+    float e[3];
+    for (int k = 0; k < 3; ++k) e[k] = ((r1[k] + t0 * c1[k]) - r2[k]) - t1 * c2[k];
+    return std::sqrt(dotf(e, e));
+}
+
+// One clusterisation step (cuda_Clusterize2Old, inc/cuda_Clusterize.h:66-90):
+// the candidate (r1, c1, l1, a1) against an older rod (r2, c2, l2, a2) already
+// shifted to its image. Returns true when the candidate moved.
+bool clu_snap(float r1[3], float c1[3], float l1, float a1, const float r2[3], const float c2[3], float l2,
+              float a2, float eps, bool typo, float sep, float cos_lim, float dist_lim) {
+    const float e[3] = {r1[0] - r2[0], r1[1] - r2[1], r1[2] - r2[2]};
+    if (!(std::sqrt(dotf(e, e)) < std::max(l1, l2) * 0.5f)) return false;
+    if (!(std::fabs(dotf(c1, c2)) >= cos_lim)) return false;
+    float t0, t1;
+    const float d = min_dist_f32(r1, c1, l1, a1, r2, c2, l2, a2, eps, typo, &t0, &t1);
+    if (!(d <= dist_lim)) return false;
+    const float qq[3] = {r2[0] + c2[0] * t1, r2[1] + c2[1] * t1, r2[2] + c2[2] * t1};
+    float v[3];
+    for (int k = 0; k < 3; ++k) v[k] = (r1[k] + c1[k] * t0) - qq[k];
+    const float vc = dotf(v, c2);
+    for (int k = 0; k < 3; ++k) v[k] = v[k] - c2[k] * vc;
+    const float nv = std::sqrt(dotf(v, v));
+    if (!(nv > 0.0f)) return false;  // the axes meet: no direction to move along
+    const float inv = 1.0f / nv;
+    for (int k = 0; k < 3; ++k) v[k] = v[k] * inv;
+    const float sd = (a1 + a2) + sep;
+    const float tt = dotf(c1, c2) * t0;
+    for (int k = 0; k < 3; ++k) r1[k] = (qq[k] + v[k] * sd) - c2[k] * tt;
+    for (int k = 0; k < 3; ++k) c1[k] = c2[k];
+    return true;
+}
+
 }  // namespace
 
 // ===========================================================================
@@ -603,6 +811,25 @@ int64_t nfo_first_hits(const nf_params* p, const nfo_rod* probes, const uint64_t
     return m;
 }
 
+int nfo_clust_snap(const nf_params* p, const nfo_rod* cand, const nfo_rod* older, const float shift[3],
+                   nfo_rod* out) {
+    if (!p || !cand || !older || !out) return -1;
+    float r1[3] = {cand->x, cand->y, cand->z}, c1[3] = {cand->cx, cand->cy, cand->cz};
+    const float r2[3] = {older->x + shift[0], older->y + shift[1], older->z + shift[2]};
+    const float c2[3] = {older->cx, older->cy, older->cz};
+    const bool moved = clu_snap(r1, c1, cand->l, cand->a, r2, c2, older->l, older->a, p->tol,
+                                p->ref_parallel_typo != 0, p->sep, (float)std::cos((double)p->clust_angl),
+                                p->clust_dist);
+    *out = nfo_rod{r1[0], r1[1], r1[2], c1[0], c1[1], c1[2], cand->l, cand->a};
+    return moved ? 1 : 0;
+}
+
+int nfo_fit_law(const int64_t sums[7], int sample, float law[12]) {
+    if (!sums || !law || sums[0] <= 0) return -1;
+    law_from_sums(sums, sample != 0, law);
+    return 0;
+}
+
 int nfo_candidates(const nf_params* p, const float* mesh, int nx, int ny, int nz, uint64_t k0,
                    uint64_t n, float* out) {
     if (!p || !out) return -1;
@@ -613,7 +840,8 @@ int nfo_candidates(const nf_params* p, const float* mesh, int nx, int ny, int nz
 
 int64_t nfo_generate(const nf_params* p, const float* mesh, int nx, int ny, int nz,
                      int nthreads, int64_t batch, int brute_force, int64_t cap, nfo_rod* rods,
-                     uint64_t* stream_index, uint64_t stats[3]) {
+                     uint64_t* stream_index, uint64_t stats[7], float* laws_out, int64_t laws_cap,
+                     int32_t law_ext[3]) {
     if (!p || !rods) return -1;
     const int nt = nthreads_of(nthreads);
     Stream S = make_stream(p, mesh, nx, ny, nz);
@@ -625,6 +853,7 @@ int64_t nfo_generate(const nf_params* p, const float* mesh, int nx, int ny, int 
     std::vector<std::vector<int64_t>> cells(g.ncell());
     std::vector<RodT<double>> accD;
     accD.reserve((size_t)std::max<int64_t>(target, 0));
+    std::vector<uint64_t> sidx_all;  // stream index of every accepted rod
     int64_t acc = 0;
     uint64_t k = 0, drawn = 0, dens_acc = 0, evals = 0;
     const uint64_t budget = p->n_candidates;
@@ -634,6 +863,138 @@ int64_t nfo_generate(const nf_params* p, const float* mesh, int nx, int ny, int 
     std::vector<uint64_t> ev_thread(nt, 0);
     auto cell_of = [&](const RodT<double>& r, int c[3]) {
         c[0] = g.coord(0, (float)r.x); c[1] = g.coord(1, (float)r.y); c[2] = g.coord(2, (float)r.z);
+    };
+    // adaptive generation: epochs of epoch_len candidates, per-cell laws
+    const bool adapt = p->self_align_step > 0 || p->clust_flag;
+    const uint64_t epoch_len = adapt ? (p->epoch_candidates > 0 ? (uint64_t)p->epoch_candidates
+                                                                : std::max<uint64_t>(1024, (uint64_t)target))
+                                     : 0;
+    std::vector<float> laws;
+    int an[3] = {1, 1, 1};
+    if (adapt) {
+        float ainv[3];
+        law_grid(p, an, ainv);
+        const size_t nc = (size_t)an[0] * an[1] * an[2];
+        laws.assign(nc * kLawF, 0.0f);
+        for (size_t c = 0; c < nc; ++c) {  // every cell starts with the global law
+            float* Lw = &laws[c * kLawF];
+            for (int q = 0; q < 9; ++q) Lw[q] = S.m[q];
+            Lw[9] = S.orient == NF_ORIENT_VMF ? S.kappa : 0.0f;
+            Lw[10] = S.orient == NF_ORIENT_VMF ? S.E2 : 0.0f;
+            Lw[11] = (float)((S.orient == NF_ORIENT_VMF ? 1 : 0) | (S.rot ? 2 : 0));
+        }
+        S.law = laws.data();
+        for (int d = 0; d < 3; ++d) { S.an[d] = an[d]; S.ainv[d] = ainv[d]; }
+    }
+    uint64_t epochs = 0, refits = 0, thinned = 0, snapped = 0;
+    uint64_t epoch_begun = ~0ull;
+    int64_t epoch_count0 = 0, n_old = 0;
+    const float cos_lim = (float)std::cos((double)p->clust_angl);
+    const float Lf[3] = {p->box[0], p->box[1], p->box[2]};
+    auto rebuild = [&]() {
+        for (auto& c : cells) c.clear();
+        if (brute_force) return;
+        for (int64_t j = 0; j < acc; ++j) {
+            int c[3];
+            cell_of(accD[j], c);
+            cells[c[0] + g.n[0] * (c[1] + g.n[1] * c[2])].push_back(j);
+        }
+    };
+    // the refit after epoch e (and the thin-out that follows it)
+    auto boundary = [&](uint64_t e, int64_t gained) {
+        const int st = p->self_align_step;
+        const bool refit = st > 0 && e > 0 &&
+                           ((e % (uint64_t)st) == 0 || (double)gained < (double)(target - acc) / 100.0);
+        if (!refit) return;
+        const size_t nc = (size_t)an[0] * an[1] * an[2];
+        std::vector<int64_t> sums(7 * nc, 0);
+        for (int64_t j = 0; j < acc; ++j) {
+            const nfo_rod& r = rods[j];
+            int64_t* sm = &sums[7 * (size_t)law_cell(S, r.x, r.y, r.z)];
+            const double x = r.cx, y = r.cy, z = r.cz;
+            const double pr[6] = {x * x, y * y, z * z, x * y, x * z, y * z};
+            sm[0] += 1;
+            for (int q = 0; q < 6; ++q) sm[1 + q] += (int64_t)std::llrint(pr[q] * kFix40);
+        }
+        const int64_t need = p->align_min > 0 ? p->align_min : 1;
+        for (size_t c = 0; c < nc; ++c)
+            if (sums[7 * c] >= need) law_from_sums(&sums[7 * c], p->orient_mode == NF_ORIENT_VMF, &laws[c * kLawF]);
+        ++refits;
+        if (!p->reduce_flag) return;
+        // thin-out: keep when 2 exp(kappa (|c.mu| - 1)) >= u(stream index, 3, e + 1)
+        int64_t w = 0;
+        for (int64_t j = 0; j < acc; ++j) {
+            const nfo_rod& r = rods[j];
+            const float* Lw = &laws[(size_t)kLawF * law_cell(S, r.x, r.y, r.z)];
+            bool kp = true;
+            if (Lw[9] > 0.0f) {
+                const float dd = std::fabs((r.cx * Lw[2] + r.cy * Lw[5]) + r.cz * Lw[8]);
+                const float F = expf_nf(Lw[9] * (dd - 1.0f));
+                const uint64_t si = sidx_all[j];
+                uint32_t ctr[4] = {(uint32_t)si, (uint32_t)(si >> 32), 3u, (uint32_t)(e + 1)}, o[4];
+                philox(ctr, S.key, o);
+                kp = 2.0f * F >= uni(o[0]);
+            }
+            if (!kp) continue;
+            rods[w] = rods[j];
+            accD[w] = accD[j];
+            sidx_all[w] = sidx_all[j];
+            ++w;
+        }
+        thinned += (uint64_t)(acc - w);
+        acc = w;
+        accD.resize(acc);
+        sidx_all.resize(acc);
+        rebuild();
+    };
+    // clusterisation of one kept candidate o (x y z cx cy cz l a) onto the
+    // rods [0, n_old); returns false when it leaves the box on an open axis
+    auto clusterize = [&](float* o, uint64_t* nsnap) -> bool {
+        const float h0[3] = {o[0], o[1], o[2]};
+        std::vector<std::pair<int64_t, int>> nb;  // (rod, image code)
+        auto visit = [&](int64_t j, const int img[3]) {
+            if (j >= n_old) return;
+            const nfo_rod& r = rods[j];
+            float sh[3];
+            for (int d = 0; d < 3; ++d) sh[d] = (float)img[d] * Lf[d];
+            const float e[3] = {(r.x + sh[0]) - h0[0], (r.y + sh[1]) - h0[1], (r.z + sh[2]) - h0[2]};
+            if (std::sqrt(dotf(e, e)) < std::max(o[6], r.l) * 0.5f)
+                nb.push_back({j, (img[0] + 1) + 3 * (img[1] + 1) + 9 * (img[2] + 1)});
+        };
+        if (brute_force) {
+            for (int64_t j = 0; j < n_old; ++j) for_images(g.periodic, [&](const int img[3]) { visit(j, img); });
+        } else {
+            RodT<double> A{};
+            A.x = o[0]; A.y = o[1]; A.z = o[2];
+            int c[3];
+            cell_of(A, c);
+            for_stencil(g, c, [&](int cell, const int img[3]) {
+                for (int64_t j : cells[cell]) visit(j, img);
+            });
+        }
+        std::sort(nb.begin(), nb.end());
+        nb.erase(std::unique(nb.begin(), nb.end()), nb.end());
+        float r1[3] = {o[0], o[1], o[2]}, c1[3] = {o[3], o[4], o[5]};
+        const float l1 = o[6], a1 = o[7];
+        for (const auto& jb : nb) {
+            const nfo_rod& q = rods[jb.first];
+            const int im[3] = {jb.second % 3 - 1, (jb.second / 3) % 3 - 1, jb.second / 9 - 1};
+            const float r2[3] = {q.x + (float)im[0] * Lf[0], q.y + (float)im[1] * Lf[1], q.z + (float)im[2] * Lf[2]};
+            const float c2[3] = {q.cx, q.cy, q.cz};
+            if (clu_snap(r1, c1, l1, a1, r2, c2, q.l, q.a, p->tol, p->ref_parallel_typo != 0, p->sep, cos_lim,
+                         p->clust_dist))
+                ++*nsnap;
+        }
+        bool inside = true;
+        for (int d = 0; d < 3; ++d) {
+            if (g.periodic & (1 << d)) {
+                if (r1[d] < 0.0f) r1[d] = r1[d] + Lf[d];
+                if (r1[d] >= Lf[d]) r1[d] = r1[d] - Lf[d];
+            }
+            if (!(r1[d] >= 0.0f && r1[d] < Lf[d])) inside = false;
+        }
+        for (int d = 0; d < 3; ++d) { o[d] = r1[d]; o[3 + d] = c1[d]; }
+        return inside;
     };
     auto test_vs = [&](const RodT<double>& A, const std::vector<std::vector<int64_t>>& cl,
                        const std::vector<RodT<double>>& pool, uint64_t* ev) -> bool {
@@ -660,29 +1021,46 @@ int64_t nfo_generate(const nf_params* p, const float* mesh, int nx, int ny, int 
         });
         return hit;
     };
+    std::vector<uint32_t> snaps_c;  // snaps per candidate of the batch
     while (k < budget && acc < target) {
+        if (adapt && k % epoch_len == 0 && k != epoch_begun) {
+            if (k > 0) boundary(k / epoch_len - 1, acc - epoch_count0);
+            epoch_begun = k;
+            epoch_count0 = acc;
+            n_old = acc;
+            ++epochs;
+            if (acc >= target) break;
+        }
         uint64_t b = std::min<uint64_t>((uint64_t)batch, budget - k);
+        if (adapt) b = std::min<uint64_t>(b, epoch_len - k % epoch_len);
         cand.assign(10 * b, 0.0f);
         keep.assign(b, 0);
+        snaps_c.assign(b, 0);
         #pragma omp parallel for num_threads(nt) schedule(dynamic, 64)
         for (int64_t i = 0; i < (int64_t)b; ++i) {
             float* o = &cand[10 * i];
             candidate(S, k + i, o);
             if (!(o[8] < o[9])) continue;  // von Neumann: u < rho(x)
             keep[i] = 1;
-            nfo_rod r{o[0], o[1], o[2], o[3], o[4], o[5], o[6], o[7]};
-            RodT<double> A = rodT<double>(r);
 #ifdef _OPENMP
             int tid = omp_get_thread_num();
 #else
             int tid = 0;
 #endif
+            uint64_t ns = 0;
+            const bool inside = !(adapt && p->clust_flag && n_old > 0) || clusterize(o, &ns);
+            snaps_c[i] = (uint32_t)ns;
+            if (!inside) {
+                keep[i] = 2;  // moved out of the box
+                continue;
+            }
+            nfo_rod r{o[0], o[1], o[2], o[3], o[4], o[5], o[6], o[7]};
+            RodT<double> A = rodT<double>(r);
             if (test_vs(A, cells, accD, &ev_thread[tid])) keep[i] = 2;  // hit an accepted rod
         }
         // In-batch conflicts, resolved in stream order.
         std::vector<std::vector<int64_t>> newcells(brute_force ? 0 : g.ncell());
         std::vector<RodT<double>> newD;
-        std::vector<int64_t> touched;
         uint64_t last = k + b;
         for (uint64_t i = 0; i < b; ++i) {
             if (keep[i] == 0) continue;
@@ -694,8 +1072,8 @@ int64_t nfo_generate(const nf_params* p, const float* mesh, int nx, int ny, int 
             if (test_vs(A, newcells, newD, &evals)) continue;
             if (acc >= cap) return -2;
             rods[acc] = r;
-            if (stream_index) stream_index[acc] = k + i;
             accD.push_back(A);
+            sidx_all.push_back(k + i);
             newD.push_back(A);
             if (!brute_force) {
                 int c[3];
@@ -708,11 +1086,20 @@ int64_t nfo_generate(const nf_params* p, const float* mesh, int nx, int ny, int 
             if (acc == target) { last = k + i + 1; break; }
         }
         drawn = last;
+        for (uint64_t i = 0; i < last - k; ++i) snapped += snaps_c[i];  // candidates consumed
         k += b;
     }
     if (acc < target) drawn = std::min<uint64_t>(k, budget);
     for (uint64_t e : ev_thread) evals += e;
-    if (stats) { stats[0] = drawn; stats[1] = dens_acc; stats[2] = evals; }
+    if (stream_index)
+        for (int64_t j = 0; j < acc; ++j) stream_index[j] = sidx_all[j];
+    if (stats) {
+        stats[0] = drawn; stats[1] = dens_acc; stats[2] = evals;
+        stats[3] = epochs; stats[4] = refits; stats[5] = thinned; stats[6] = snapped;
+    }
+    if (law_ext) for (int d = 0; d < 3; ++d) law_ext[d] = adapt ? an[d] : 0;
+    if (laws_out && adapt && laws_cap >= (int64_t)laws.size())
+        std::memcpy(laws_out, laws.data(), sizeof(float) * laws.size());
     return acc;
 }
 

@@ -13,6 +13,8 @@
  *   - the virtual inclusion    generate_virt_inclusions  inc/conductKernels.h:289-361
  *   - the contact-area estimate surf_to_cylinder_capped (same file :204-293)
  *   - the target count         simPrms::set_numCNT       src/simPrms.cpp:987-1002
+ *   - the clusterisation snap  cuda_Clusterize2Old / cnt_minDist
+ *                              inc/cuda_Clusterize.h:14-100, inc/intersection_dev.h:85-160
  *   - the Norton assembly and G_eff  tools/kirchhoff/kirchhoff.py:232-269
  * plus the project-defined seeded candidate stream (Philox4x32-10, Salmon et al.
  * 2011) and sequential insertion in stream order.
@@ -72,16 +74,37 @@ int64_t nfo_internal_network(const nf_params *p, const nfo_rod *rods, int64_t n_
                              int64_t cap, uint32_t *node_rod, double *node_t, uint32_t *seg_i, uint32_t *seg_j,
                              double *seg_l, double *seg_g, uint32_t *edge_i, uint32_t *edge_j, int64_t counts[3]);
 
+/* One clusterisation step of a candidate against an older rod shifted by
+ * shift[] (its periodic image): centre test, axis angle <= clust_angl,
+ * cnt_minDist <= clust_dist, then the move parallel to the older rod at
+ * a + a' + sep from its axis. out = the candidate after the step; returns 1
+ * when it moved. */
+int nfo_clust_snap(const nf_params *p, const nfo_rod *cand, const nfo_rod *older, const float shift[3],
+                   nfo_rod *out);
+
+/* Orientation law of a cell from its tensor sums {n, xx, yy, zz, xy, xz, yz}
+ * (each product c_i c_j rounded to 2^-40 units): law[0..8] rotation (column 2
+ * the axis), law[9] kappa, law[10] exp(-2 kappa), law[11] sampling flags. */
+int nfo_fit_law(const int64_t sums[7], int sample, float law[12]);
+
 /* Candidate stream k0..k0+n-1: out[10*i + f], f = x y z cx cy cz l a u rho. */
 int nfo_candidates(const nf_params *p, const float *mesh, int nx, int ny, int nz,
                    uint64_t k0, uint64_t n, float *out);
 
 /* Sequential insertion in stream order. batch>1 tests batches in parallel and
  * resolves in-batch conflicts in index order (identical result).
- * stats = {drawn, density_accepted, pair_evals}. Returns accepted count or <0. */
+ * With self_align_step > 0 or clust_flag, the adaptive generation: epochs of
+ * epoch_candidates, per-cell orientation laws refit at epoch boundaries from
+ * exact tensor sums (principal axis, von Mises-Fisher concentration matched
+ * to the largest eigenvalue), thin-out after a refit (reduce_flag), and the
+ * snap of each kept candidate to the older rods near it (clust_flag).
+ * stats = {drawn, density_accepted, pair_evals, epochs, refits, thinned,
+ * snapped}; laws_out (12 floats per law cell, if laws_cap allows) and
+ * law_ext receive the final laws. Returns accepted count or <0. */
 int64_t nfo_generate(const nf_params *p, const float *mesh, int nx, int ny, int nz,
                      int nthreads, int64_t batch, int brute_force, int64_t cap,
-                     nfo_rod *rods, uint64_t *stream_index, uint64_t stats[3]);
+                     nfo_rod *rods, uint64_t *stream_index, uint64_t stats[7], float *laws_out,
+                     int64_t laws_cap, int32_t law_ext[3]);
 
 /* Contacts: rod-rod (sorted I,J,image; screened ones removed), then sink, then
  * source. counts = {internal, screened, sink, source}. Returns total or <0.

@@ -43,6 +43,8 @@ class NfParams(C.Structure):
         ("stencil_radius", C.c_int32), ("round_overshoot", C.c_float), ("two_phase_work", C.c_double),
         ("rod_sigma", C.c_double),
         ("elec_buffer", C.c_int32), ("pad_end", C.c_int32),
+        ("clust_dist", C.c_float), ("clust_angl", C.c_float), ("align_cell", C.c_float),
+        ("align_min", C.c_int32), ("epoch_candidates", C.c_int64),
     ]
 
 
@@ -57,6 +59,8 @@ DEFAULTS = dict(
     rad_min=0.0, rad_max=0.0, density_default=1.0, cell_edge=0.0, G0=1e-5, lambda_=0.00018,
     d_c=0.00034, ref_parallel_typo=0, screening=1, round_candidates=0, solve_max_iter=20000,
     solve_tol=1e-10, stencil_radius=0, round_overshoot=0.0, two_phase_work=0.0, rod_sigma=67.0, elec_buffer=0,
+    clust_dist=0.015, clust_angl=float(np.float32(3.14159265359) / np.float32(12)), align_cell=0.0, align_min=4,
+    epoch_candidates=0,
 )
 
 
@@ -104,8 +108,10 @@ def lib():
                                          C.c_uint64, C.c_uint64, C.c_void_p]
             L.nfo_generate.argtypes = [P(NfParams), C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int,
                                        C.c_int64, C.c_int, C.c_int64, C.c_void_p, C.c_void_p,
-                                       P(C.c_uint64)]
+                                       P(C.c_uint64), C.c_void_p, C.c_int64, C.c_void_p]
             L.nfo_generate.restype = C.c_int64
+            L.nfo_clust_snap.argtypes = [P(NfParams), C.c_void_p, C.c_void_p, P(C.c_float), C.c_void_p]
+            L.nfo_fit_law.argtypes = [P(C.c_int64), C.c_int, P(C.c_float)]
             L.nfo_contacts.argtypes = [P(NfParams), C.c_void_p, C.c_int64, C.c_int, C.c_int,
                                        C.c_int64] + [C.c_void_p] * 8 + [P(C.c_int64)]
             L.nfo_contacts.restype = C.c_int64
@@ -297,14 +303,57 @@ def generate(params, mesh=None, nthreads=0, batch=4096, brute_force=False, cap=N
         cap = int(params.get("n_target") or 0) or 4 * 10 ** 6
     rods = np.zeros(cap, ROD_DTYPE)
     idx = np.zeros(cap, np.uint64)
-    st = (C.c_uint64 * 3)()
+    st = (C.c_uint64 * 7)()
     nx, ny, nz = mesh.shape if mesh is not None else (0, 0, 0)
     m = None if mesh is None else np.ascontiguousarray(mesh, np.float32)
+    ext = np.zeros(3, np.int32)
+    lcap = 12 * 256 ** 3 if (p.self_align_step > 0 or p.clust_flag) else 0
+    laws = np.zeros(0, np.float32)
+    if lcap:
+        bx = np.array(p.box[:], np.float64)
+        e = p.align_cell if p.align_cell > 0 else p.l
+        nc = int(np.prod(np.clip(np.floor(bx / e), 1, 256)))
+        laws = np.zeros(12 * nc, np.float32)
+        lcap = laws.size
     n = lib().nfo_generate(C.byref(p), _ptr(m), nx, ny, nz, nthreads, batch, int(brute_force),
-                           cap, _ptr(rods), _ptr(idx), st)
+                           cap, _ptr(rods), _ptr(idx), st, _ptr(laws) if lcap else None, lcap, _ptr(ext))
     if n < 0:
         raise RuntimeError(f"nfo_generate failed ({n})")
-    return rods[:n].copy(), idx[:n].copy(), dict(drawn=st[0], density_accepted=st[1], exact_evals=st[2])
+    info = dict(drawn=st[0], density_accepted=st[1], exact_evals=st[2], epochs=st[3], refits=st[4],
+                thinned=st[5], snapped=st[6])
+    if lcap:
+        info["laws"] = laws.reshape(-1, 12)
+        info["law_ext"] = tuple(int(v) for v in ext)
+    return rods[:n].copy(), idx[:n].copy(), info
+
+
+def clust_snap(params, cand, older, shift=(0.0, 0.0, 0.0)):
+    """One clusterisation step; returns (moved, candidate after the step)."""
+    c = np.array([tuple(cand)], ROD_DTYPE)
+    o = np.array([tuple(older)], ROD_DTYPE)
+    out = np.zeros(1, ROD_DTYPE)
+    sh = (C.c_float * 3)(*shift)
+    r = lib().nfo_clust_snap(C.byref(make_params(params)), _ptr(c), _ptr(o), sh, _ptr(out))
+    return bool(r == 1), out[0]
+
+
+def law_sums(dirs):
+    """Tensor sums {n, xx, yy, zz, xy, xz, yz} of unit directions (float32
+    rows), each product rounded to 2^-40 units as the generation does."""
+    d = np.asarray(dirs, np.float32).astype(np.float64)
+    pr = [d[:, 0] * d[:, 0], d[:, 1] * d[:, 1], d[:, 2] * d[:, 2], d[:, 0] * d[:, 1], d[:, 0] * d[:, 2],
+          d[:, 1] * d[:, 2]]
+    return [len(d)] + [int(np.rint(v * 2.0 ** 40).astype(np.int64).sum()) for v in pr]
+
+
+def fit_law(sums, sample=True):
+    """The law of one cell from its tensor sums: {"m": 3x3, "axis", "kappa", "flags"}."""
+    s = (C.c_int64 * 7)(*sums)
+    out = (C.c_float * 12)()
+    if lib().nfo_fit_law(s, int(sample), out) != 0:
+        raise ValueError("empty cell")
+    v = np.array(out[:], np.float32)
+    return dict(m=v[:9].reshape(3, 3), axis=v[[2, 5, 8]], kappa=float(v[9]), E2=float(v[10]), flags=int(v[11]))
 
 
 def contacts(params, rods, nthreads=0, brute_force=False):

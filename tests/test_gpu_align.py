@@ -1,0 +1,99 @@
+"""Adaptive generation on the device against the oracle, bit for bit
+(tolerance 0: the same FP32 stream, exact integer tensor sums, the same FP64
+fits, FP32 snaps with every operation rounded on its own):
+
+- self-alignment + thin-out + clusterisation under a von Mises-Fisher law:
+  every rod field and stream index, the epoch / refit / thin-out / snap
+  counts and the final per-cell laws (axis, kappa) equal the oracle's;
+- the same with small rounds (round_candidates 300): rounds never cross an
+  epoch boundary, so the result does not depend on them;
+- an isotropic law with thin-out (the fitted laws act only through the
+  thin-out) and a dense box with clusterisation alone;
+- a batch with adaptive realisations is refused (NF_ERR_UNSUPPORTED) and a
+  plain handle has no laws to read (NF_ERR_STATE).
+"""
+import numpy as np
+import pytest
+
+from conftest import rods_struct
+
+pytestmark = pytest.mark.gpu
+
+NM = 1e-3
+FIELDS = ("x", "y", "z", "cx", "cy", "cz", "l", "a", "stream_index")
+
+ADAPT = dict(vf=0.03, box=(2.0, 2.0, 2.0), l=1.0, a=5 * NM, sep=0.34 * NM, stat_dist_lim=1.4 * NM, tol=1e-6,
+             sc_frac=1.0, gen_periodic=3, field_dir=4, seed=3, n_candidates=30000, orient_mode=1, vmf_kappa=2.0,
+             self_align_step=1, reduce_flag=1, clust_flag=1, epoch_candidates=2000, align_cell=1.0,
+             density_default=1.0)
+
+
+def run_both(gpu, oracle, cfg):
+    with gpu.Simulation(cfg) as sim:
+        g = sim.generate()
+        rods = sim.rods()
+        laws = sim.orientation_laws()
+    ro, io, so = oracle.generate(cfg)
+    return g, rods, laws, ro, io, so
+
+
+def check_equal(g, rods, laws, ro, io, so):
+    n = len(ro)
+    assert g["accepted"] == n
+    rs = rods_struct(rods)
+    for f in ("x", "y", "z", "cx", "cy", "cz", "l", "a"):
+        assert np.array_equal(rs[f], ro[f]), f
+    assert np.array_equal(rods["stream_index"], io)
+    for k, ko in (("candidates_drawn", "drawn"), ("density_accepted", "density_accepted"), ("epochs", "epochs"),
+                  ("refits", "refits"), ("thinned", "thinned"), ("snapped", "snapped")):
+        assert g[k] == so[ko], k
+    assert laws["ext"] == so["law_ext"]
+    assert np.array_equal(laws["axis"], so["laws"][:, [2, 5, 8]])
+    assert np.array_equal(laws["kappa"], so["laws"][:, 9])
+
+
+def test_adaptive_vmf_matches_oracle(gpu, oracle):
+    out = run_both(gpu, oracle, ADAPT)
+    check_equal(*out)
+    g = out[0]
+    assert g["refits"] > 0 and g["thinned"] > 0 and g["snapped"] > 0
+    assert np.any(out[2]["kappa"] != np.float32(2.0))  # refit laws differ from the global one
+
+
+def test_adaptive_round_size_independent(gpu, oracle):
+    with gpu.Simulation(ADAPT) as a, gpu.Simulation(dict(ADAPT, round_candidates=300)) as b:
+        ga, gb = a.generate(), b.generate()
+        ra, rb = a.rods(), b.rods()
+    assert gb["rounds"] > ga["rounds"]
+    for f in FIELDS:
+        assert np.array_equal(ra[f], rb[f]), f
+    for k in ("epochs", "refits", "thinned", "snapped", "candidates_drawn"):
+        assert ga[k] == gb[k], k
+
+
+def test_isotropic_thinout_matches_oracle(gpu, oracle):
+    cfg = dict(ADAPT, orient_mode=0, clust_flag=0, vf=0.02, seed=5)
+    out = run_both(gpu, oracle, cfg)
+    check_equal(*out)
+    assert out[0]["thinned"] > 0 and out[0]["snapped"] == 0
+
+
+def test_dense_clusterisation_matches_oracle(gpu, oracle):
+    cfg = dict(ADAPT, box=(2.5, 2.5, 2.5), vf=0.04, self_align_step=0, reduce_flag=0, orient_mode=0,
+               n_candidates=120000, epoch_candidates=10000, seed=11, clust_angl=0.5, clust_dist=0.02)
+    out = run_both(gpu, oracle, cfg)
+    check_equal(*out)
+    assert out[0]["snapped"] > 100 and out[0]["refits"] == 0
+
+
+def test_adaptive_limits(gpu):
+    with pytest.raises(gpu.NanoFillerError) as ei:
+        gpu.batch_run([dict(ADAPT)])
+    assert ei.value.status == 11
+    with gpu.Simulation(dict(gpu.configs.SMALL)) as sim:
+        sim.generate()
+        with pytest.raises(gpu.NanoFillerError) as ei:
+            sim.orientation_laws()
+        assert ei.value.status == 10
+    with pytest.raises(gpu.NanoFillerError):
+        gpu.Simulation(dict(ADAPT, box=(0.8, 2.0, 2.0)))  # clusterisation needs edges >= the rod length
