@@ -199,10 +199,12 @@ class Clocks:
 
 def fp32_roofline(g, old_ms, clk):
     """FP32 side of the two generation sweeps (candidates against accepted rods
-    and against earlier candidates; the counters cover both): the FP32 flops
-    they execute -- 22 per staged pair (the capsule pre-test), 40 per marked
-    pair (the line-distance test of the hand-out), 60 per pair that passes it
-    (the full filter and certificate) -- over their summed event time, against the FP32 pipe peak of the device: SMs x
+    and against earlier candidates; the counters cover both): FP32 flops they
+    execute at least -- 22 per staged pair (the line bound of the old-rod
+    sweep, or the capsule test of the conflict sweep; the capsule test that
+    follows a line bound is not counted), 40 per marked pair (the hand-out's
+    line test), 60 per pair that passes it (the full filter and certificate)
+    -- over their summed event time, against the FP32 pipe peak of the device: SMs x
     128 lanes x 2 flops x the SM clock sampled in the timed window (the nominal
     figure; no FP32 peak is measured)."""
     import torch

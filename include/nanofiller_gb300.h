@@ -192,8 +192,9 @@ typedef struct nf_gen_stats {
     /* work of the two pair sweeps (candidates vs rods, vs earlier candidates) */
     uint64_t work_items;        /* (probe chunk, stencil row, segment) items  */
     uint64_t target_tiles;      /* 32-target tiles staged                    */
-    uint64_t marked_pairs;      /* pairs passing the capsule pre-test        */
-    uint64_t line_pairs;        /* of those, axis lines within the threshold */
+    uint64_t marked_pairs;      /* pairs passing the marking pre-tests (line
+                                   bound for candidates vs rods, capsule)     */
+    uint64_t line_pairs;        /* of those, kept by the hand-out's line bound */
     /* adaptive generation (zero when it is off) */
     uint64_t epochs;            /* epochs of the candidate stream begun      */
     uint64_t refits;            /* orientation-law refits                     */

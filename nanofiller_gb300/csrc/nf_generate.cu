@@ -246,6 +246,11 @@ __global__ void __launch_bounds__(kTPB, 6) k_old_tiles(const Real* __restrict__ 
         const float hA2 = (pA.w * 0.5f + cA.w + Re.eps + cA.w * Re.scf + Re.sep + Re.eps) * 1.000002f + Re.slack;
         const float hAe = pA.w * 0.5f + cA.w + Re.eps;
         const float hC = (cA.w * Re.scf + Re.sep + Re.eps) * 1.000002f + Re.slack + 4e-6f * (1.0f + hA2);
+        // line bound of the marking loop: margin bounded with the pair's reach
+        // (errA + 4e-6 hBt covers 4e-6 |b| + slack for any pair within reach),
+        // threshold thA + a_B scf2, both sides squared
+        const float errA = 4e-6f * (1.0f + hA2) + Re.slack;
+        const float thA = (cA.w * Re.scf + Re.sep + Re.eps) * 1.0002f, scf2 = Re.scf * 1.0002f;
         unsigned dead = 0;  // probe lanes decided during this item (warp-uniform)
         for (uint32_t b = 0; b < nt; b += kWT) {
             if (!__any_sync(0xffffffffu, alive)) break;
@@ -269,7 +274,18 @@ __global__ void __launch_bounds__(kTPB, 6) k_old_tiles(const Real* __restrict__ 
                     for (uint32_t jj = 0; jj < 8; ++jj) {
                         const float4 tq = T.p[j0 + jj];
                         const float bx = tq.x - ax, by = tq.y - ay, bz = tq.z - az;
-                        if (capsule_near(bx, by, bz, cA.x, cA.y, cA.z, hAe, tq.w, hC)) mask |= 1u << (j0 + jj);
+                        // the axis lines certainly farther apart than the threshold (the
+                        // test of line_far without its square root); near-parallel pairs
+                        // are never far. Evaluated first: most staged pairs end here.
+                        const float4 cB = T.c[j0 + jj];
+                        const float nx = cA.y * cB.z - cA.z * cB.y;
+                        const float ny = cA.z * cB.x - cA.x * cB.z;
+                        const float nz = cA.x * cB.y - cA.y * cB.x;
+                        const float nn = nx * nx + ny * ny + nz * nz;
+                        const float nb = fabsf(nx * bx + ny * by + nz * bz) - fmaf(4e-6f, tq.w, errA);
+                        const float thL = fmaf(cB.w, scf2, thA);
+                        const bool lfar = nn > 1e-4f && nb > 0.0f && nb * nb > thL * thL * nn;
+                        if (!lfar && capsule_near(bx, by, bz, cA.x, cA.y, cA.z, hAe, tq.w, hC)) mask |= 1u << (j0 + jj);
                     }
                 }
             }

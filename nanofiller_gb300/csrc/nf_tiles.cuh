@@ -116,7 +116,7 @@ __device__ __forceinline__ int for_marked_pairs(uint32_t mask, int lane, int* sp
 }
 
 // Warp-private staging of one tile of targets: position with the target's
-// sphere term folded into .w, axis + radius, length.
+// reach term folded into .w, axis + radius, length.
 struct WarpTile {
     float4 p[kWT];
     float4 c[kWT];
