@@ -1181,12 +1181,17 @@ nf_status Engine::generate() {
         // Cell-sorted candidate copy and the chunk table of this round.
         NF_LAUNCH(k_gather_pd, gs, 256, 0, st)((uint32_t)slots, ntot, cperm.p, cpos.p, cdir.p, gpos.p, gdir.p);
         NF_CK(cudaGetLastError());
-        // The old-rod test runs in two phases when the grid has outer stencil
-        // rows and the round is heavy: every candidate against the inner rows
-        // (|dy|, |dz| <= 1: a third of the volume, most of the hits), then only
-        // the survivors, packed densely again, against the outer rows. Same
-        // decisions as one pass; the second pass costs a binning, a work list and
-        // two launches (~0.1 ms), repaid once candidates x rods passes ~1e10.
+        // The old-rod test runs in three phases when the grid has outer stencil
+        // rows and the round is heavy: every candidate against the centre row
+        // (dy = dz = 0: the 5 cells nearest along x, 1/25 of the volume, where
+        // most rejected candidates find their first hit), then only the
+        // survivors, packed densely again, against the rest of the inner rows
+        // (|dy|, |dz| <= 1), then the survivors of that against the outer rows.
+        // A warp pays for its dead lanes until its item ends; the packing keeps
+        // the lanes busy. Same decisions as one pass; each further pass costs a
+        // binning, a work list and two launches (~0.1 ms), repaid once
+        // candidates x rods passes ~1e10 (jammed box: old_test 84.5 -> 31.5 ms
+        // per step, against two phases split at the inner ring).
         bool outer_rows = false;
         double work = 0;
         for (int r = 0; r < R; ++r) {
@@ -1194,9 +1199,9 @@ nf_status Engine::generate() {
             work += (double)c_round[r] * (double)count[r];
         }
         const double two_work = prm[0].two_phase_work != 0 ? prm[0].two_phase_work : 1e10;
-        const bool two_phase = outer_rows && two_work >= 0 && work > two_work;
+        const bool phased = outer_rows && two_work >= 0 && work > two_work;
         NF_CK(cudaMemsetAsync(ctr.p + C_ITEMS, 0, sizeof(unsigned long long), st));
-        s = build_items(cstart.p, rstart.p, 0, slots, total_rods(), two_phase ? 1 : 0);
+        s = build_items(cstart.p, rstart.p, 0, slots, total_rods(), phased ? 3 : 0);
         if (s != NF_OK) return s;
         const unsigned xg = (unsigned)(4 * nsm);
         xq_cap = std::max(xq_cap, (size_t)(slots / 8));  // first guess; grown and redone on overflow
@@ -1225,12 +1230,13 @@ nf_status Engine::generate() {
                                                    creal.p, spos.p, sdir.p, state.p, ctr.p);
         }
         NF_CK(cudaGetLastError());
-        if (two_phase) {
+        for (int ring : {4, 2}) {  // the survivors against the rest of the inner rows, then the outer rows
+            if (!phased) break;
             NF_CK(cudaMemcpyAsync(ctr.p + C_XQ_MARK, ctr.p + C_XQ_OLD, sizeof(unsigned long long),
                                   cudaMemcpyDeviceToDevice, st));
             s = bin_survivors();
             if (s != NF_OK) return s;
-            s = build_items(astart.p, rstart.p, 0, slots, total_rods(), 2);
+            s = build_items(astart.p, rstart.p, 0, slots, total_rods(), ring);
             if (s != NF_OK) return s;
             NF_LAUNCH(k_old_tiles, persistent_grid(k_old_tiles), kTPB, 0, st)(dreal.p, item_count(), (uint32_t)items.cap, items.p, aperm.p, apos.p,
                                                     adir.p, spos.p, sdir.p, state.p, xq.p, xq.cap, ctr.p);

@@ -152,14 +152,21 @@ __device__ __forceinline__ void cell_xyz(const Real& Re, uint32_t c, int cc[3]) 
     cc[2] = (int)(loc / ((uint32_t)Re.n[0] * (uint32_t)Re.n[1]));
 }
 
-// Row r of a radius-S stencil belongs to ring 1 (|dy|, |dz| <= 1) or ring 2;
-// ring 0 selects every row.
+// Row r = (dy, dz) of a radius-S stencil: ring 0 selects every row, ring 1
+// the inner rows (|dy|, |dz| <= 1), ring 2 the others, ring 3 the centre row
+// (dy = dz = 0), ring 4 the inner rows but the centre one.
 __device__ __forceinline__ bool row_in_ring(const Real& Re, int r, int ring) {
     if (ring == 0) return true;
     const int w = 2 * Re.S + 1;
     const int dy = r % w - Re.S, dz = r / w - Re.S;
     const bool inner = dy >= -1 && dy <= 1 && dz >= -1 && dz <= 1;
-    return ring == 1 ? inner : !inner;
+    const bool centre = dy == 0 && dz == 0;
+    switch (ring) {
+        case 1: return inner;
+        case 3: return centre;
+        case 4: return inner && !centre;
+        default: return !inner;
+    }
 }
 
 // Items of (cell c, stencil row r) for t = c * kRows + r: probe chunks of the
