@@ -158,40 +158,78 @@ __global__ void k_stream_keep(const Real* __restrict__ reals, int R, const uint3
     keep[s] = (u < rho) ? 1u : 0u;
 }
 
+// Cell counters of the round's candidates: with few cells, millions of
+// atomics on a handful of counters serialise in L2. Grids of at most
+// kShCells cells count in shared memory per 1024-thread block and add one
+// global atomic per touched cell.
+constexpr uint32_t kShCells = 4096;
+constexpr int kBinTPB = 1024;
+
 // Compaction in stream order + cell counts.
-__global__ void k_compact(const Real* __restrict__ reals, int R, const uint32_t* __restrict__ coff,
+__global__ void __launch_bounds__(kBinTPB) k_compact(const Real* __restrict__ reals, int R, const uint32_t* __restrict__ coff,
                           const uint64_t* __restrict__ kbeg, uint32_t nslots, const uint32_t* __restrict__ keep,
                           const uint32_t* __restrict__ kpos, float4* __restrict__ cpos, float4* __restrict__ cdir,
                           uint64_t* __restrict__ csidx, uint32_t* __restrict__ creal, uint32_t* __restrict__ ccell,
-                          uint32_t* __restrict__ ccount, uint8_t* __restrict__ state) {
-    uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= nslots || !keep[s]) return;
-    int r = find_real(coff, R, s);
-    const Real& Re = reals[r];
-    uint64_t k = kbeg[r] + (s - coff[r]);
-    float4 p, d;
-    float u, rho;
-    candidate(Re, k, &p, &d, &u, &rho);
-    uint32_t c = kpos[s];
-    cpos[c] = p;
-    cdir[c] = d;
-    csidx[c] = k;
-    creal[c] = (uint32_t)r;
-    uint32_t cell = cell_of(Re, p.x, p.y, p.z);
-    ccell[c] = cell;
-    state[c] = ST_ALIVE;
-    atomicAdd(&ccount[cell], 1u);
+                          uint32_t* __restrict__ ccount, uint8_t* __restrict__ state, uint32_t ncell) {
+    extern __shared__ uint32_t shc[];
+    const bool sh = ncell <= kShCells;
+    if (sh) {
+        for (uint32_t c = threadIdx.x; c < ncell; c += blockDim.x) shc[c] = 0;
+        __syncthreads();
+    }
+    const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s < nslots && keep[s]) {
+        int r = find_real(coff, R, s);
+        const Real& Re = reals[r];
+        uint64_t k = kbeg[r] + (s - coff[r]);
+        float4 p, d;
+        float u, rho;
+        candidate(Re, k, &p, &d, &u, &rho);
+        uint32_t c = kpos[s];
+        cpos[c] = p;
+        cdir[c] = d;
+        csidx[c] = k;
+        creal[c] = (uint32_t)r;
+        uint32_t cell = cell_of(Re, p.x, p.y, p.z);
+        ccell[c] = cell;
+        state[c] = ST_ALIVE;
+        atomicAdd(sh ? &shc[cell] : &ccount[cell], 1u);
+    }
+    if (sh) {
+        __syncthreads();
+        for (uint32_t c = threadIdx.x; c < ncell; c += blockDim.x)
+            if (shc[c]) atomicAdd(&ccount[c], shc[c]);
+    }
 }
 
-// Counting-sort scatter: perm[start[cell] + cursor] = id.
-__global__ void k_bin(uint32_t n, const uint32_t* __restrict__ ntot, const uint32_t* __restrict__ cellof,
-                      const uint32_t* __restrict__ start, uint32_t* __restrict__ cursor, uint32_t* __restrict__ perm) {
-    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    uint32_t m = ntot ? *ntot : n;
-    if (i >= m) return;
-    uint32_t cell = cellof[i];
-    uint32_t q = start[cell] + atomicAdd(&cursor[cell], 1u);
-    perm[q] = i;
+// Counting-sort scatter: perm[start[cell] + cursor] = id. With few cells the
+// block ranks its ids per cell in shared memory and reserves one range per
+// touched cell.
+__global__ void __launch_bounds__(kBinTPB) k_bin(uint32_t n, const uint32_t* __restrict__ ntot, const uint32_t* __restrict__ cellof,
+                      const uint32_t* __restrict__ start, uint32_t* __restrict__ cursor, uint32_t* __restrict__ perm,
+                      uint32_t ncell) {
+    extern __shared__ uint32_t shb[];  // local count, then base, per cell
+    const bool sh = ncell <= kShCells;
+    if (sh) {
+        for (uint32_t c = threadIdx.x; c < ncell; c += blockDim.x) shb[c] = 0;
+        __syncthreads();
+    }
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t m = ntot ? *ntot : n;
+    const bool valid = i < m;
+    uint32_t cell = 0, rank = 0;
+    if (valid) {
+        cell = cellof[i];
+        rank = atomicAdd(sh ? &shb[cell] : &cursor[cell], 1u);
+    }
+    if (sh) {
+        __syncthreads();
+        for (uint32_t c = threadIdx.x; c < ncell; c += blockDim.x)
+            shb[ncell + c] = shb[c] ? atomicAdd(&cursor[c], shb[c]) : 0u;
+        __syncthreads();
+        rank += shb[ncell + cell];
+    }
+    if (valid) perm[start[cell] + rank] = i;
 }
 
 // Candidate vs accepted rods of one neighbour cell (cuda_OldExtIsectLB's job),
@@ -374,27 +412,52 @@ __global__ void __launch_bounds__(256) k_old_exact(const Real* __restrict__ real
 
 // Survivors of the old-rod test, binned by cell (stream order is kept in the
 // per-candidate key): the in-round conflict sweep runs over these only.
+// Warp-aggregated increment of ctr[key] for the active lanes (lanes of a
+// warp that share a key add once); returns each lane's slot. Every lane of
+// the warp calls it.
+__device__ __forceinline__ uint32_t warp_agg_inc(uint32_t* ctr, uint32_t key, bool active) {
+    const unsigned act = __ballot_sync(0xffffffffu, active);
+    if (!active) return 0u;
+    const unsigned peers = __match_any_sync(act, key);
+    const int lane = threadIdx.x & 31, leader = __ffs(peers) - 1;
+    uint32_t base = 0u;
+    if (lane == leader) base = atomicAdd(&ctr[key], (uint32_t)__popc(peers));
+    base = __shfl_sync(peers, base, leader);
+    return base + (uint32_t)__popc(peers & ((1u << lane) - 1u));
+}
+
+// Survivors per cell; the walk is in cell order, so a warp's lanes mostly
+// share one counter and add to it once.
 __global__ void k_alive_count(uint32_t n, const uint32_t* __restrict__ ntot, const uint32_t* __restrict__ cperm,
                               const uint8_t* __restrict__ state, const uint32_t* __restrict__ ccell,
                               uint32_t* __restrict__ acount) {
-    uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
-    if (q >= *ntot) return;
-    uint32_t cid = cperm[q];
-    if (state[cid] == ST_ALIVE) atomicAdd(&acount[ccell[cid]], 1u);
+    const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
+    bool alive = false;
+    uint32_t cell = 0;
+    if (q < *ntot) {
+        const uint32_t cid = cperm[q];
+        alive = state[cid] == ST_ALIVE;
+        cell = ccell[cid];
+    }
+    (void)warp_agg_inc(acount, cell, alive);
 }
-
 __global__ void k_alive_bin(uint32_t n, const uint32_t* __restrict__ ntot, const uint32_t* __restrict__ cperm,
                             const uint8_t* __restrict__ state, const uint32_t* __restrict__ ccell,
                             const uint32_t* __restrict__ astart, uint32_t* __restrict__ acur,
                             const float4* __restrict__ gpos, const float4* __restrict__ gdir,
                             uint32_t* __restrict__ aperm, float4* __restrict__ apos,
                             float4* __restrict__ adir) {
-    uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
-    if (q >= *ntot) return;
-    uint32_t cid = cperm[q];
-    if (state[cid] != ST_ALIVE) return;
-    uint32_t cell = ccell[cid];
-    uint32_t d = astart[cell] + atomicAdd(&acur[cell], 1u);
+    const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
+    bool alive = false;
+    uint32_t cid = 0, cell = 0;
+    if (q < *ntot) {
+        cid = cperm[q];
+        alive = state[cid] == ST_ALIVE;
+        cell = ccell[cid];
+    }
+    const uint32_t slot = warp_agg_inc(acur, cell, alive);
+    if (!alive) return;
+    const uint32_t d = astart[cell] + slot;
     aperm[d] = cid;
     apos[d] = gpos[q];
     adir[d] = gdir[q];
@@ -1165,8 +1228,10 @@ nf_status Engine::generate() {
         if (s != NF_OK) return s;
         uint32_t* ntot = kpos.p + slots;
         NF_CK(cudaMemsetAsync(ccount.p, 0, sizeof(uint32_t) * (ncell + 1), st));
-        NF_LAUNCH(k_compact, gs, 256, 0, st)(dreal.p, R, coff.p, kbeg.p, (uint32_t)slots, keep.p, kpos.p, cpos.p, cdir.p,
-                                     csidx.p, creal.p, ccell.p, ccount.p, state.p);
+        const size_t shc = ncell <= kShCells ? sizeof(uint32_t) * ncell : 0;
+        const unsigned gb = grid_for(slots, kBinTPB);
+        NF_LAUNCH(k_compact, gb, kBinTPB, shc, st)(dreal.p, R, coff.p, kbeg.p, (uint32_t)slots, keep.p, kpos.p, cpos.p,
+                                                   cdir.p, csidx.p, creal.p, ccell.p, ccount.p, state.p, ncell);
         NF_CK(cudaGetLastError());
         const bool clustered = adapt && prm[0].clust_flag && n_old > 0;
         if (clustered) {
@@ -1176,7 +1241,7 @@ nf_status Engine::generate() {
         s = scan_u32(ccount.p, cstart.p, ncell + 1);
         if (s != NF_OK) return s;
         NF_CK(cudaMemsetAsync(ccursor.p, 0, sizeof(uint32_t) * (ncell + 1), st));
-        NF_LAUNCH(k_bin, gs, 256, 0, st)((uint32_t)slots, ntot, ccell.p, cstart.p, ccursor.p, cperm.p);
+        NF_LAUNCH(k_bin, gb, kBinTPB, 2 * shc, st)((uint32_t)slots, ntot, ccell.p, cstart.p, ccursor.p, cperm.p, ncell);
         NF_CK(cudaGetLastError());
         // Cell-sorted candidate copy and the chunk table of this round.
         NF_LAUNCH(k_gather_pd, gs, 256, 0, st)((uint32_t)slots, ntot, cperm.p, cpos.p, cdir.p, gpos.p, gdir.p);
