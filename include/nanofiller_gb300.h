@@ -155,6 +155,10 @@ typedef struct nf_params {
                                (4); cells with fewer keep their law        */
     int64_t epoch_candidates; /* EPOCH_CANDIDATES: candidates per epoch;
                                0 -> max(1024, target count)                */
+    int32_t solve_method;   /* SOLVE_METHOD: 0 auto (direct when the network's
+                               band after reverse Cuthill-McKee is narrow),
+                               1 direct (banded LDL^T), 2 iterative (PCG)   */
+    int32_t pad_solve;
 } nf_params;
 
 /* Rods, structure of arrays, caller-owned host buffers. Any array may be NULL. */
@@ -221,6 +225,9 @@ typedef struct nf_solve_stats {
     int64_t n_active;           /* unknowns: rods linked to both electrodes*/
     int32_t percolating;        /* a path joins source and sink            */
     double ms;
+    int32_t direct;             /* 1: banded LDL^T (outer_iters = refinement
+                                   steps, inner_iters = 0); 0: PCG          */
+    uint32_t bandwidth;         /* widest band after reordering (direct)    */
 } nf_solve_stats;
 
 typedef struct nf_batch_result {

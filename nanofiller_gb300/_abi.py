@@ -42,6 +42,7 @@ class NfParams(C.Structure):
         ("elec_buffer", C.c_int32), ("pad_end", C.c_int32),
         ("clust_dist", C.c_float), ("clust_angl", C.c_float), ("align_cell", C.c_float),
         ("align_min", C.c_int32), ("epoch_candidates", C.c_int64),
+        ("solve_method", C.c_int32), ("pad_solve", C.c_int32),
     ]
 
 
@@ -78,7 +79,8 @@ class NfContactStats(C.Structure):
 class NfSolveStats(C.Structure):
     _fields_ = [("G_eff", C.c_double), ("residual", C.c_double), ("outer_iters", C.c_int32),
                 ("inner_iters", C.c_int32), ("n_nodes", C.c_int64), ("n_active", C.c_int64),
-                ("percolating", C.c_int32), ("ms", C.c_double)]
+                ("percolating", C.c_int32), ("ms", C.c_double), ("direct", C.c_int32),
+                ("bandwidth", C.c_uint32)]
 
 
 class NfBatchResult(C.Structure):

@@ -583,8 +583,8 @@ __global__ void __launch_bounds__(NT) k_ac_band(int nf, const double* __restrict
 
 // Reverse Cuthill-McKee order of the active system (CSR rows plus the chain
 // links i -> i + 1): perm[old] = new; returns the bandwidth.
-static uint32_t rcm_order(uint32_t n, const std::vector<uint32_t>& rowp, const std::vector<uint32_t>& col,
-                          const std::vector<char>& up, std::vector<uint32_t>* perm) {
+uint32_t rcm_order(uint32_t n, const std::vector<uint32_t>& rowp, const std::vector<uint32_t>& col,
+                   const std::vector<char>& up, std::vector<uint32_t>* perm) {
     std::vector<uint32_t> deg(n, 0);
     for (uint32_t i = 0; i < n; ++i) deg[i] = rowp[i + 1] - rowp[i] + (up[i] ? 1 : 0) + (i > 0 && up[i - 1] ? 1 : 0);
     auto nbrs = [&](uint32_t i, std::vector<uint32_t>& out) {

@@ -52,6 +52,7 @@ nf_status validate(const nf_params& p, std::string* why) {
     if (p.field_dir != 0 && p.field_dir != 1 && p.field_dir != 2 && p.field_dir != 4) {
         *why = "FIELD_DIR must be 0, 1, 2 or 4"; return NF_ERR_PARAM;
     }
+    if (p.solve_method < 0 || p.solve_method > 2) { *why = "SOLVE_METHOD must be 0, 1 or 2"; return NF_ERR_PARAM; }
     if (p.self_align_step < 0 || p.clust_flag < 0 || p.clust_flag > 1 || p.reduce_flag < 0 || p.reduce_flag > 1) {
         *why = "SELF_ALLIGN_STEP must be >= 0, CLUST_FLAG and REDUCE_FLAG 0 or 1"; return NF_ERR_PARAM;
     }
@@ -206,6 +207,7 @@ nf_status nf_params_from_file(const char* path, nf_params* p, int* n_unknown) {
         else if (key == "ALIGN_CELL") in >> p->align_cell;
         else if (key == "ALIGN_MIN_RODS") in >> p->align_min;
         else if (key == "EPOCH_CANDIDATES") { long long s; in >> s; p->epoch_candidates = s; }
+        else if (key == "SOLVE_METHOD") in >> p->solve_method;
         else if (key == "SPAT_DIMENSIONS" ||
                  key == "ORNT_DISTR_FILE" || key == "IDIM_DISTR_FILE" || key == "MATH_TOLERANCE" ||
                  key == "DMN_CELL_MARGE") { /* parsed and ignored, as the reference does */ }

@@ -63,6 +63,12 @@ struct DBuf {
     }
 };
 
+// Reverse Cuthill-McKee order of a symmetric sparse graph given as CSR rows
+// plus chain links i -> i + 1 where up[i]: perm[old] = new; returns the
+// bandwidth of the reordered graph.
+uint32_t rcm_order(uint32_t n, const std::vector<uint32_t>& rowp, const std::vector<uint32_t>& col,
+                   const std::vector<char>& up, std::vector<uint32_t>* perm);
+
 // Two CUDA events, destroyed with the object (early returns included).
 struct EventPair {
     cudaEvent_t a = nullptr, b = nullptr;
@@ -180,6 +186,10 @@ struct Engine {
     DBuf<uint32_t> ecnt, eoff, elist;             // electrode edges per node (network assembly)
     DBuf<float> cgbuf;
     DBuf<double> cgred;
+    DBuf<double> dcband, dcwork;   // banded factors and solve vectors of the direct DC form
+    DBuf<uint32_t> dcperm;         // per-realisation RCM order (local indices)
+    DBuf<unsigned long long> dcboff;  // band offset per realisation
+    DBuf<uint32_t> dcbw;           // bandwidth per realisation
     std::vector<nf_solve_stats> solve_st;
     bool solve_valid = false;
 

@@ -590,6 +590,368 @@ nf_status Engine::assemble(uint32_t n, const std::vector<uint32_t>& off, uint32_
 }
 
 // Laplacian solve on the graph (see assemble); node voltages land in volt.
+// ---------------------------------------------------------------------------
+// Direct form: banded LDL^T per realisation.
+//
+// The rod networks are sparse and nearly one-dimensional between the
+// electrodes: after reverse Cuthill-McKee (on the host, per realisation) the
+// jammed box's 1 231 active rods have bandwidth 28, against ~800 PCG
+// iterations of a stiff system (tunnelling conductances spread over orders
+// of magnitude). One CTA per realisation assembles its band (row p holds
+// A[p][p - o], o = 0..b), factors it without pivoting (the matrix is
+// symmetric positive definite: each diagonal is its row's conductances plus
+// the electrode ones), and refines x on the FP64 difference-form residual
+// until it stops falling. Forward and backward substitution run on one warp.
+// ---------------------------------------------------------------------------
+constexpr uint32_t kDcBandMax = 512;
+
+template <int NT>
+__global__ void __launch_bounds__(NT) k_dc_band(int R, const uint32_t* __restrict__ abase,
+                                                const unsigned long long* __restrict__ boff,
+                                                const uint32_t* __restrict__ bwid, const uint32_t* __restrict__ permL,
+                                                const uint32_t* __restrict__ rowp, const uint32_t* __restrict__ col,
+                                                const double* __restrict__ v64, const double* __restrict__ e64,
+                                                const double* __restrict__ ch64, int chains,
+                                                const double* __restrict__ b, double* __restrict__ x,
+                                                double* __restrict__ r64, double* __restrict__ band,
+                                                double* __restrict__ work, double tol, CgOut* __restrict__ out) {
+    __shared__ double sh[96];
+    __shared__ double lsh[kDcBandMax], ush[kDcBandMax];
+    const int rr = blockIdx.x;
+    if (rr >= R) return;
+    const uint32_t base = abase[rr], n = abase[rr + 1] - base, bw = bwid[rr], bs = bw + 1;
+    CgOut o{};
+    o.n = (int)n;
+    if (n == 0) {
+        if (threadIdx.x == 0) out[rr] = o;
+        return;
+    }
+    double* A = band + boff[rr];
+    const uint32_t* perm = permL + base;
+    const double* bb = b + base;
+    double* xx = x + base;
+    double* rv = r64 + base;
+    double* t = work + base;                 // solve vector, reordered
+    double* xt = work + abase[R] + base;     // candidate x
+    const double* gl64 = ch64 + base;
+    const double* gr64 = ch64 + abase[R] + base;
+    for (uint32_t i = threadIdx.x; i < n; i += NT) {
+        const uint32_t g = base + i, p = perm[i];
+        double* row = A + (size_t)p * bs;
+        for (uint32_t q = 1; q < bs; ++q) row[q] = 0.0;
+        double d = e64[g];
+        for (uint32_t k = rowp[g], k1 = rowp[g + 1]; k < k1; ++k) {
+            d += v64[k];
+            const uint32_t q = perm[col[k] - base];
+            if (q < p && p - q <= bw) row[p - q] -= v64[k];
+        }
+        if (chains) {
+            if (gl64[i] > 0.0) {
+                d += gl64[i];
+                const uint32_t q = perm[i - 1];
+                if (q < p && p - q <= bw) row[p - q] -= gl64[i];
+            }
+            if (gr64[i] > 0.0) {
+                d += gr64[i];
+                const uint32_t q = perm[i + 1];
+                if (q < p && p - q <= bw) row[p - q] -= gr64[i];
+            }
+        }
+        row[0] = d;
+        xx[i] = 0.0;
+    }
+    __syncthreads();
+    // LDL^T, right-looking: column k scaled by 1 / d_k, the trailing triangle
+    // loses l_i (d_k l_j) = l_i A[j][j - k]
+    for (uint32_t k = 0; k < n; ++k) {
+        const double dk = A[(size_t)k * bs];
+        const uint32_t m = min(bw, n - 1 - k);
+        for (uint32_t u = threadIdx.x; u < m; u += NT) {
+            const double a = A[(size_t)(k + 1 + u) * bs + (u + 1)];
+            ush[u] = a;
+            lsh[u] = a / dk;
+        }
+        __syncthreads();
+        const uint32_t ntri = m * (m + 1) / 2;
+        for (uint32_t v = threadIdx.x; v < ntri; v += NT) {
+            uint32_t ii = (uint32_t)((sqrt(8.0 * v + 1.0) - 1.0) * 0.5);
+            while ((ii + 1) * (ii + 2) / 2 <= v) ++ii;  // exact triangular root
+            while (ii * (ii + 1) / 2 > v) --ii;
+            const uint32_t jj = v - ii * (ii + 1) / 2;
+            A[(size_t)(k + 1 + ii) * bs + (ii - jj)] -= lsh[ii] * ush[jj];
+        }
+        __syncthreads();
+        for (uint32_t u = threadIdx.x; u < m; u += NT) A[(size_t)(k + 1 + u) * bs + (u + 1)] = lsh[u];
+        __syncthreads();
+    }
+    // residual of the FP64 system in difference form, row order
+    auto residual = [&](const double* xv, double* out_r, bool reordered) -> double {
+        double part = 0.0;
+        for (uint32_t i = threadIdx.x; i < n; i += NT) {
+            const uint32_t g = base + i;
+            const double xi = xv[i];
+            double acc = e64[g] * xi;
+            for (uint32_t k = rowp[g], k1 = rowp[g + 1]; k < k1; ++k) acc += v64[k] * (xi - xv[col[k] - base]);
+            if (chains) {
+                const double a = gl64[i], c = gr64[i];
+                if (a != 0.0) acc += a * (xi - xv[i - 1]);
+                if (c != 0.0) acc += c * (xi - xv[i + 1]);
+            }
+            const double ri = bb[i] - acc;
+            out_r[reordered ? perm[i] : i] = ri;
+            part += ri * ri;
+        }
+        return sqrt(block_sum<NT>(part, sh));
+    };
+    double part = 0.0;
+    for (uint32_t i = threadIdx.x; i < n; i += NT) {
+        rv[i] = bb[i];
+        part += bb[i] * bb[i];
+    }
+    const double bn = sqrt(block_sum<NT>(part, sh));
+    double rn = bn;
+    int steps = 0;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (; steps < 12 && rn > 1e-16 * bn; ++steps) {
+        for (uint32_t i = threadIdx.x; i < n; i += NT) t[perm[i]] = rv[i];
+        __syncthreads();
+        if (warp == 0) {
+            for (uint32_t k = 0; k < n; ++k) {  // forward: t_i -= l_ik t_k
+                const double tk = t[k];
+                const uint32_t m = min(bw, n - 1 - k);
+                for (uint32_t u = lane; u < m; u += 32) t[k + 1 + u] -= A[(size_t)(k + 1 + u) * bs + (u + 1)] * tk;
+                __syncwarp();
+            }
+            for (uint32_t k = lane; k < n; k += 32) t[k] /= A[(size_t)k * bs];
+            __syncwarp();
+            for (uint32_t kk = n; kk-- > 0;) {  // backward: t_k -= sum_i l_ik t_i
+                const uint32_t m = min(bw, n - 1 - kk);
+                double acc = 0.0;
+                for (uint32_t u = lane; u < m; u += 32) acc += A[(size_t)(kk + 1 + u) * bs + (u + 1)] * t[kk + 1 + u];
+#pragma unroll
+                for (int s2 = 16; s2 > 0; s2 >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, s2);
+                if (lane == 0) t[kk] -= acc;
+                __syncwarp();
+            }
+        }
+        __syncthreads();
+        for (uint32_t i = threadIdx.x; i < n; i += NT) xt[i] = xx[i] + t[perm[i]];
+        __syncthreads();
+        const double rn_new = residual(xt, t, true);  // t is free again: it holds the candidate residual
+        if (!(rn_new < rn)) { ++steps; break; }  // at the rounding floor
+        for (uint32_t i = threadIdx.x; i < n; i += NT) {
+            xx[i] = xt[i];
+            rv[i] = t[perm[i]];
+        }
+        __syncthreads();
+        rn = rn_new;
+        if (rn <= tol * bn * 1e-3) { ++steps; break; }
+    }
+    part = 0.0;
+    for (uint32_t i = threadIdx.x; i < n; i += NT) part += bb[i] * (1.0 - xx[i]);
+    const double G = block_sum<NT>(part, sh);
+    if (threadIdx.x == 0) {
+        o.G = G;
+        o.res = bn > 0 ? rn / bn : 0.0;
+        o.outer = steps;
+        o.inner = 0;
+        out[rr] = o;
+    }
+}
+
+// Narrow bands (b <= kDcWin): the same factorisation with the b + 1 active
+// rows in a shared-memory window (row i in slot i mod (b + 1)), the next row
+// fetched while the current pivot updates, L written by columns
+// (Lc[k b + u] = l_{k+1+u,k}) and the pivots to D, so the substitutions read
+// one contiguous column per step; the solve vector lives in shared memory when
+// it fits (n <= kDcShN).
+constexpr uint32_t kDcWin = 64;
+constexpr uint32_t kDcShN = 12288;
+
+template <int NT>
+__global__ void __launch_bounds__(NT) k_dc_band_win(int R, const uint32_t* __restrict__ abase,
+                                                    const unsigned long long* __restrict__ boff,
+                                                    const uint32_t* __restrict__ bwid,
+                                                    const uint32_t* __restrict__ permL,
+                                                    const uint32_t* __restrict__ rowp, const uint32_t* __restrict__ col,
+                                                    const double* __restrict__ v64, const double* __restrict__ e64,
+                                                    const double* __restrict__ ch64, int chains,
+                                                    const double* __restrict__ b, double* __restrict__ x,
+                                                    double* __restrict__ r64, double* __restrict__ band,
+                                                    double* __restrict__ work, double tol, int tshared,
+                                                    CgOut* __restrict__ out) {
+    __shared__ double sh[96];
+    __shared__ double win[(kDcWin + 1) * (kDcWin + 1)];
+    __shared__ double lsh[kDcWin], ush[kDcWin];
+    extern __shared__ double tsh[];
+    const int rr = blockIdx.x;
+    if (rr >= R) return;
+    const uint32_t base = abase[rr], n = abase[rr + 1] - base, bw = bwid[rr], bs = bw + 1;
+    CgOut o{};
+    o.n = (int)n;
+    if (n == 0) {
+        if (threadIdx.x == 0) out[rr] = o;
+        return;
+    }
+    // band rows (n x bs), then L by columns (n x bw), then D (n)
+    double* A = band + boff[rr] * 2;  // rows (n bs) + L (n bw) + D (n) = 2 n bs
+    double* Lc = A + (size_t)n * bs;
+    double* D = Lc + (size_t)n * bw;
+    const uint32_t* perm = permL + base;
+    const double* bb = b + base;
+    double* xx = x + base;
+    double* rv = r64 + base;
+    double* tg = work + base;              // solve vector in global memory (large n)
+    double* xt = work + abase[R] + base;   // candidate x
+    double* t = tshared ? tsh : tg;  // the launch sized tsh for every realisation
+    const double* gl64 = ch64 + base;
+    const double* gr64 = ch64 + abase[R] + base;
+    for (uint32_t i = threadIdx.x; i < n; i += NT) {
+        const uint32_t g = base + i, p = perm[i];
+        double* row = A + (size_t)p * bs;
+        for (uint32_t q = 1; q < bs; ++q) row[q] = 0.0;
+        double d = e64[g];
+        for (uint32_t k = rowp[g], k1 = rowp[g + 1]; k < k1; ++k) {
+            d += v64[k];
+            const uint32_t q = perm[col[k] - base];
+            if (q < p && p - q <= bw) row[p - q] -= v64[k];
+        }
+        if (chains) {
+            if (gl64[i] > 0.0) {
+                d += gl64[i];
+                const uint32_t q = perm[i - 1];
+                if (q < p && p - q <= bw) row[p - q] -= gl64[i];
+            }
+            if (gr64[i] > 0.0) {
+                d += gr64[i];
+                const uint32_t q = perm[i + 1];
+                if (q < p && p - q <= bw) row[p - q] -= gr64[i];
+            }
+        }
+        row[0] = d;
+        xx[i] = 0.0;
+    }
+    __syncthreads();
+    const uint32_t w0 = min(bs, n);  // rows 0..b into the window
+    for (uint32_t e = threadIdx.x; e < w0 * bs; e += NT) win[e] = A[e];
+    __syncthreads();
+    for (uint32_t k = 0; k < n; ++k) {
+        const uint32_t m = min(bw, n - 1 - k);
+        const uint32_t sk = k % bs;
+        const double dk = win[sk * bs];
+        const uint32_t nxt = k + bs;  // the row that takes this slot
+        double pre = 0.0;
+        if (nxt < n && threadIdx.x < bs) pre = A[(size_t)nxt * bs + threadIdx.x];
+        for (uint32_t u = threadIdx.x; u < m; u += NT) {
+            const double a = win[((k + 1 + u) % bs) * bs + (u + 1)];
+            ush[u] = a;
+            lsh[u] = a / dk;
+        }
+        __syncthreads();
+        for (uint32_t v = threadIdx.x; v < m * m; v += NT) {
+            const uint32_t ii = v / m, jj = v - ii * m;
+            if (jj <= ii) win[((k + 1 + ii) % bs) * bs + (ii - jj)] -= lsh[ii] * ush[jj];
+        }
+        __syncthreads();
+        for (uint32_t u = threadIdx.x; u < m; u += NT) {
+            win[((k + 1 + u) % bs) * bs + (u + 1)] = lsh[u];
+            Lc[(size_t)k * bw + u] = lsh[u];
+        }
+        if (threadIdx.x == 0) D[k] = dk;
+        if (nxt < n && threadIdx.x < bs) win[sk * bs + threadIdx.x] = pre;
+        __syncthreads();
+    }
+    auto residual = [&](const double* xv, bool reordered) -> double {
+        double part = 0.0;
+        for (uint32_t i = threadIdx.x; i < n; i += NT) {
+            const uint32_t g = base + i;
+            const double xi = xv[i];
+            double acc = e64[g] * xi;
+            for (uint32_t k = rowp[g], k1 = rowp[g + 1]; k < k1; ++k) acc += v64[k] * (xi - xv[col[k] - base]);
+            if (chains) {
+                const double a = gl64[i], c = gr64[i];
+                if (a != 0.0) acc += a * (xi - xv[i - 1]);
+                if (c != 0.0) acc += c * (xi - xv[i + 1]);
+            }
+            const double ri = bb[i] - acc;
+            if (reordered) t[perm[i]] = ri; else rv[i] = ri;
+            part += ri * ri;
+        }
+        return sqrt(block_sum<NT>(part, sh));
+    };
+    double part = 0.0;
+    for (uint32_t i = threadIdx.x; i < n; i += NT) {
+        rv[i] = bb[i];
+        part += bb[i] * bb[i];
+    }
+    const double bn = sqrt(block_sum<NT>(part, sh));
+    double rn = bn;
+    int steps = 0;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (; steps < 12 && rn > 1e-16 * bn; ++steps) {
+        for (uint32_t i = threadIdx.x; i < n; i += NT) t[perm[i]] = rv[i];
+        __syncthreads();
+        if (warp == 0) {
+            // forward: t_{k+1+u} -= l_{k+1+u,k} t_k, the next column prefetched
+            double l0 = 0.0, l1 = 0.0;
+            if (n > 1) {
+                const uint32_t m0 = min(bw, n - 1);
+                if ((uint32_t)lane < m0) l0 = Lc[lane];
+                if ((uint32_t)lane + 32 < m0) l1 = Lc[lane + 32];
+            }
+            for (uint32_t k = 0; k < n; ++k) {
+                const uint32_t m = min(bw, n - 1 - k);
+                double n0 = 0.0, n1 = 0.0;
+                if (k + 1 < n) {
+                    const uint32_t mn = min(bw, n - 2 - k);
+                    if ((uint32_t)lane < mn) n0 = Lc[(size_t)(k + 1) * bw + lane];
+                    if ((uint32_t)lane + 32 < mn) n1 = Lc[(size_t)(k + 1) * bw + lane + 32];
+                }
+                const double tk = t[k];
+                if ((uint32_t)lane < m) t[k + 1 + lane] -= l0 * tk;
+                if ((uint32_t)lane + 32 < m) t[k + 33 + lane] -= l1 * tk;
+                __syncwarp();
+                l0 = n0;
+                l1 = n1;
+            }
+            for (uint32_t k = lane; k < n; k += 32) t[k] /= D[k];
+            __syncwarp();
+            for (uint32_t kk = n; kk-- > 0;) {  // backward: t_k -= sum_u l_{k+1+u,k} t_{k+1+u}
+                const uint32_t m = min(bw, n - 1 - kk);
+                double acc = 0.0;
+                if ((uint32_t)lane < m) acc = Lc[(size_t)kk * bw + lane] * t[kk + 1 + lane];
+                if ((uint32_t)lane + 32 < m) acc += Lc[(size_t)kk * bw + lane + 32] * t[kk + 33 + lane];
+#pragma unroll
+                for (int s2 = 16; s2 > 0; s2 >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, s2);
+                if (lane == 0) t[kk] -= acc;
+                __syncwarp();
+            }
+        }
+        __syncthreads();
+        for (uint32_t i = threadIdx.x; i < n; i += NT) xt[i] = xx[i] + t[perm[i]];
+        __syncthreads();
+        const double rn_new = residual(xt, true);  // t is free again: it holds the candidate residual
+        if (!(rn_new < rn)) { ++steps; break; }  // at the rounding floor
+        for (uint32_t i = threadIdx.x; i < n; i += NT) {
+            xx[i] = xt[i];
+            rv[i] = t[perm[i]];
+        }
+        __syncthreads();
+        rn = rn_new;
+        if (rn <= tol * bn * 1e-3) { ++steps; break; }
+    }
+    part = 0.0;
+    for (uint32_t i = threadIdx.x; i < n; i += NT) part += bb[i] * (1.0 - xx[i]);
+    const double G = block_sum<NT>(part, sh);
+    if (threadIdx.x == 0) {
+        o.G = G;
+        o.res = bn > 0 ? rn / bn : 0.0;
+        o.outer = steps;
+        o.inner = 0;
+        out[rr] = o;
+    }
+}
+
 nf_status Engine::solve_graph(uint32_t n, const std::vector<uint32_t>& off, const std::vector<uint32_t>& nodes,
                               uint32_t mc, uint32_t m, const uint32_t* eI, const uint32_t* eJ, const double* eG) {
     EventPair ev;
@@ -615,10 +977,73 @@ nf_status Engine::solve_graph(uint32_t n, const std::vector<uint32_t>& off, cons
     NF_CK(outs.ensure(R));
     const double tol = prm[0].solve_tol > 0 ? prm[0].solve_tol : 1e-10;
     const int max_inner = prm[0].solve_max_iter > 0 ? prm[0].solve_max_iter : 20000;
+    // Direct form when every realisation's band after reverse Cuthill-McKee
+    // is narrow: bandwidth <= 512, n b^2 <= 1e9 updates, 1 GB of band at most.
+    const int method = prm[0].solve_method;
+    bool direct = false;
+    uint32_t bmax = 0;
+    if (na > 0 && method != 2) {
+        std::vector<uint32_t> hrow(na + 1), hcol(nnz);
+        std::vector<double> hgr(na);
+        NF_CK(cudaMemcpyAsync(hrow.data(), rowp.p, sizeof(uint32_t) * (na + 1), cudaMemcpyDeviceToHost, st));
+        if (nnz) NF_CK(cudaMemcpyAsync(hcol.data(), col.p, sizeof(uint32_t) * nnz, cudaMemcpyDeviceToHost, st));
+        NF_CK(cudaMemcpyAsync(hgr.data(), chain64.p + na, sizeof(double) * na, cudaMemcpyDeviceToHost, st));
+        NF_CK(cudaStreamSynchronize(st));
+        std::vector<uint32_t> hperm(na), hbw(R, 0);
+        std::vector<unsigned long long> hoff(R + 1, 0);
+        bool fits = true;
+        for (int r = 0; r < R && fits; ++r) {
+            const uint32_t b0 = A.habase[r], nr = A.habase[r + 1] - b0;
+            std::vector<uint32_t> lrow(nr + 1), lcol;
+            std::vector<char> up(nr, 0);
+            lcol.reserve(hrow[b0 + nr] - hrow[b0]);
+            for (uint32_t i = 0; i < nr; ++i) {
+                lrow[i] = (uint32_t)lcol.size();
+                for (uint32_t k = hrow[b0 + i]; k < hrow[b0 + i + 1]; ++k) lcol.push_back(hcol[k] - b0);
+                if (A.chains && i + 1 < nr) up[i] = hgr[b0 + i] > 0.0 ? 1 : 0;
+            }
+            lrow[nr] = (uint32_t)lcol.size();
+            std::vector<uint32_t> lp;
+            const uint32_t bw = nr ? rcm_order(nr, lrow, lcol, up, &lp) : 0;
+            for (uint32_t i = 0; i < nr; ++i) hperm[b0 + i] = lp[i];
+            hbw[r] = bw;
+            bmax = std::max(bmax, bw);
+            hoff[r + 1] = hoff[r] + (unsigned long long)nr * (bw + 1);  // rows; the window form adds L and D
+            fits = bw <= kDcBandMax && (double)nr * bw * bw <= 1e9;
+        }
+        fits = fits && (double)hoff[R] * sizeof(double) <= 1e9;
+        if (method == 1 && !fits) { err = "the reordered band is too wide for the direct form"; return NF_ERR_PARAM; }
+        direct = fits;
+        if (direct) {
+            NF_CK(dcperm.ensure(na));
+            NF_CK(dcbw.ensure(R));
+            NF_CK(dcboff.ensure(R + 1));
+            NF_CK(dcband.ensure(2 * hoff[R] + na + 1));
+            NF_CK(dcwork.ensure(2 * (size_t)na + 2));
+            NF_CK(cudaMemcpyAsync(dcperm.p, hperm.data(), sizeof(uint32_t) * na, cudaMemcpyHostToDevice, st));
+            NF_CK(cudaMemcpyAsync(dcbw.p, hbw.data(), sizeof(uint32_t) * R, cudaMemcpyHostToDevice, st));
+            NF_CK(cudaMemcpyAsync(dcboff.p, hoff.data(), sizeof(unsigned long long) * (R + 1), cudaMemcpyHostToDevice, st));
+        }
+    }
     tstart(KT_CG);
-    NF_LAUNCH(k_cg<512>, R, 512, 0, st)(R, dab.p, rowp.p, col.p, val32.p, val64.p, diag32.p, diag64.p, chain64.p,
-                                 chain32.p, na, A.chains ? 1 : 0, bvec.p, xvec.p, cgred.p, cgbuf.p, tol, max_inner,
-                                 outs.p);
+    if (direct && bmax <= kDcWin) {
+        uint32_t nmax = 0;
+        for (int r = 0; r < R; ++r) nmax = std::max(nmax, A.habase[r + 1] - A.habase[r]);
+        const size_t shb = nmax <= kDcShN ? sizeof(double) * nmax : 0;
+        NF_CK(cudaFuncSetAttribute(k_dc_band_win<256>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)(sizeof(double) * kDcShN)));
+        NF_LAUNCH(k_dc_band_win<256>, R, 256, shb, st)(R, dab.p, dcboff.p, dcbw.p, dcperm.p, rowp.p, col.p, val64.p,
+                                                      diag64.p, chain64.p, A.chains ? 1 : 0, bvec.p, xvec.p, cgred.p,
+                                                      dcband.p, dcwork.p, tol, shb ? 1 : 0, outs.p);
+    } else if (direct) {
+        NF_LAUNCH(k_dc_band<256>, R, 256, 0, st)(R, dab.p, dcboff.p, dcbw.p, dcperm.p, rowp.p, col.p, val64.p, diag64.p,
+                                                chain64.p, A.chains ? 1 : 0, bvec.p, xvec.p, cgred.p, dcband.p,
+                                                dcwork.p, tol, outs.p);
+    } else {
+        NF_LAUNCH(k_cg<512>, R, 512, 0, st)(R, dab.p, rowp.p, col.p, val32.p, val64.p, diag32.p, diag64.p, chain64.p,
+                                     chain32.p, na, A.chains ? 1 : 0, bvec.p, xvec.p, cgred.p, cgbuf.p, tol, max_inner,
+                                     outs.p);
+    }
     NF_CK(cudaGetLastError());
     tstop(KT_CG);
     if (nslot)
@@ -649,6 +1074,8 @@ nf_status Engine::solve_graph(uint32_t n, const std::vector<uint32_t>& off, cons
         S.n_active = A.habase[r + 1] - A.habase[r];
         S.percolating = S.n_active > 0;
         S.ms = ms;
+        S.direct = direct ? 1 : 0;
+        S.bandwidth = direct ? bmax : 0;
         if (S.n_active > 0 && !(S.residual <= tol)) conv = false;
     }
     solve_valid = true;

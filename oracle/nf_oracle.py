@@ -45,6 +45,7 @@ class NfParams(C.Structure):
         ("elec_buffer", C.c_int32), ("pad_end", C.c_int32),
         ("clust_dist", C.c_float), ("clust_angl", C.c_float), ("align_cell", C.c_float),
         ("align_min", C.c_int32), ("epoch_candidates", C.c_int64),
+        ("solve_method", C.c_int32), ("pad_solve", C.c_int32),
     ]
 
 
@@ -60,7 +61,7 @@ DEFAULTS = dict(
     d_c=0.00034, ref_parallel_typo=0, screening=1, round_candidates=0, solve_max_iter=20000,
     solve_tol=1e-10, stencil_radius=0, round_overshoot=0.0, two_phase_work=0.0, rod_sigma=67.0, elec_buffer=0,
     clust_dist=0.015, clust_angl=float(np.float32(3.14159265359) / np.float32(12)), align_cell=0.0, align_min=4,
-    epoch_candidates=0,
+    epoch_candidates=0, solve_method=0,
 )
 
 
