@@ -764,11 +764,16 @@ __global__ void __launch_bounds__(NT) k_dc_band(int R, const uint32_t* __restric
 // fetched while the current pivot updates, L written by columns
 // (Lc[k b + u] = l_{k+1+u,k}) and the pivots to D, so the substitutions read
 // one contiguous column per step; the solve vector lives in shared memory when
-// it fits (n <= kDcShN).
+// it fits (n <= kDcShN). T is the type of the factors and of the correction
+// solves: float by default (a GB300 SM issues FP64 at a small fraction of its
+// FP32 rate, and one CTA factors sequentially), double when refinement with
+// FP32 factors stalls above the tolerance (condition number near 1 / eps32).
+// The residual and x stay in FP64 either way; each correction solves for the
+// residual scaled to unit norm.
 constexpr uint32_t kDcWin = 64;
 constexpr uint32_t kDcShN = 12288;
 
-template <int NT>
+template <int NT, typename T>
 __global__ void __launch_bounds__(NT) k_dc_band_win(int R, const uint32_t* __restrict__ abase,
                                                     const unsigned long long* __restrict__ boff,
                                                     const uint32_t* __restrict__ bwid,
@@ -781,9 +786,10 @@ __global__ void __launch_bounds__(NT) k_dc_band_win(int R, const uint32_t* __res
                                                     double* __restrict__ work, double tol, int tshared,
                                                     CgOut* __restrict__ out) {
     __shared__ double sh[96];
-    __shared__ double win[(kDcWin + 1) * (kDcWin + 1)];
-    __shared__ double lsh[kDcWin], ush[kDcWin];
-    extern __shared__ double tsh[];
+    __shared__ T win[(kDcWin + 1) * (kDcWin + 1)];
+    __shared__ T lsh[kDcWin], ush[kDcWin];
+    extern __shared__ __align__(8) unsigned char tsh_raw[];
+    T* tsh = reinterpret_cast<T*>(tsh_raw);
     const int rr = blockIdx.x;
     if (rr >= R) return;
     const uint32_t base = abase[rr], n = abase[rr + 1] - base, bw = bwid[rr], bs = bw + 1;
@@ -795,15 +801,16 @@ __global__ void __launch_bounds__(NT) k_dc_band_win(int R, const uint32_t* __res
     }
     // band rows (n x bs), then L by columns (n x bw), then D (n)
     double* A = band + boff[rr] * 2;  // rows (n bs) + L (n bw) + D (n) = 2 n bs
-    double* Lc = A + (size_t)n * bs;
-    double* D = Lc + (size_t)n * bw;
+    T* Lc = reinterpret_cast<T*>(A + (size_t)n * bs);
+    T* D = Lc + (size_t)n * bw;
     const uint32_t* perm = permL + base;
     const double* bb = b + base;
     double* xx = x + base;
     double* rv = r64 + base;
-    double* tg = work + base;              // solve vector in global memory (large n)
-    double* xt = work + abase[R] + base;   // candidate x
-    double* t = tshared ? tsh : tg;  // the launch sized tsh for every realisation
+    T* tg = reinterpret_cast<T*>(work + base);  // solve vector in global memory (large n)
+    double* xt = work + abase[R] + base;        // candidate x
+    double* rc = r64 + abase[R] + base;         // candidate residual, reordered
+    T* t = tshared ? tsh : tg;  // the launch sized tsh for every realisation
     const double* gl64 = ch64 + base;
     const double* gr64 = ch64 + abase[R] + base;
     for (uint32_t i = threadIdx.x; i < n; i += NT) {
@@ -833,32 +840,47 @@ __global__ void __launch_bounds__(NT) k_dc_band_win(int R, const uint32_t* __res
     }
     __syncthreads();
     const uint32_t w0 = min(bs, n);  // rows 0..b into the window
-    for (uint32_t e = threadIdx.x; e < w0 * bs; e += NT) win[e] = A[e];
+    for (uint32_t e = threadIdx.x; e < w0 * bs; e += NT) win[e] = (T)A[e];
+    // row k + bs enters slot k % bs after pivot k; it is fetched one pivot
+    // ahead so that its load overlaps a whole pivot
+    T pre = 0;
+    if (bs < n && threadIdx.x < bs) pre = (T)A[(size_t)bs * bs + threadIdx.x];
     __syncthreads();
+    uint32_t sk = 0;  // slot of row k
     for (uint32_t k = 0; k < n; ++k) {
         const uint32_t m = min(bw, n - 1 - k);
-        const uint32_t sk = k % bs;
-        const double dk = win[sk * bs];
-        const uint32_t nxt = k + bs;  // the row that takes this slot
-        double pre = 0.0;
-        if (nxt < n && threadIdx.x < bs) pre = A[(size_t)nxt * bs + threadIdx.x];
+        const T dk = win[sk * bs];
+        T pre2 = 0;
+        if (k + 1 + bs < n && threadIdx.x < bs) pre2 = (T)A[(size_t)(k + 1 + bs) * bs + threadIdx.x];
         for (uint32_t u = threadIdx.x; u < m; u += NT) {
-            const double a = win[((k + 1 + u) % bs) * bs + (u + 1)];
+            uint32_t sl = sk + 1 + u;
+            sl -= sl >= bs ? bs : 0;
+            const T a = win[sl * bs + (u + 1)];
             ush[u] = a;
             lsh[u] = a / dk;
         }
         __syncthreads();
-        for (uint32_t v = threadIdx.x; v < m * m; v += NT) {
-            const uint32_t ii = v / m, jj = v - ii * m;
-            if (jj <= ii) win[((k + 1 + ii) % bs) * bs + (ii - jj)] -= lsh[ii] * ush[jj];
+        // trailing triangle, (ii, jj) from a power-of-two split of the index
+        const uint32_t lg = m > 1 ? 32 - __clz(m - 1) : 0;
+        for (uint32_t v = threadIdx.x; v < (m << lg); v += NT) {
+            const uint32_t ii = v >> lg, jj = v & ((1u << lg) - 1u);
+            if (jj <= ii) {
+                uint32_t sl = sk + 1 + ii;
+                sl -= sl >= bs ? bs : 0;
+                win[sl * bs + (ii - jj)] -= lsh[ii] * ush[jj];
+            }
         }
         __syncthreads();
         for (uint32_t u = threadIdx.x; u < m; u += NT) {
-            win[((k + 1 + u) % bs) * bs + (u + 1)] = lsh[u];
+            uint32_t sl = sk + 1 + u;
+            sl -= sl >= bs ? bs : 0;
+            win[sl * bs + (u + 1)] = lsh[u];
             Lc[(size_t)k * bw + u] = lsh[u];
         }
         if (threadIdx.x == 0) D[k] = dk;
-        if (nxt < n && threadIdx.x < bs) win[sk * bs + threadIdx.x] = pre;
+        if (k + bs < n && threadIdx.x < bs) win[sk * bs + threadIdx.x] = pre;
+        pre = pre2;
+        sk = sk + 1 == bs ? 0 : sk + 1;
         __syncthreads();
     }
     auto residual = [&](const double* xv, bool reordered) -> double {
@@ -874,7 +896,7 @@ __global__ void __launch_bounds__(NT) k_dc_band_win(int R, const uint32_t* __res
                 if (c != 0.0) acc += c * (xi - xv[i + 1]);
             }
             const double ri = bb[i] - acc;
-            if (reordered) t[perm[i]] = ri; else rv[i] = ri;
+            if (reordered) rc[i] = ri; else rv[i] = ri;
             part += ri * ri;
         }
         return sqrt(block_sum<NT>(part, sh));
@@ -888,53 +910,73 @@ __global__ void __launch_bounds__(NT) k_dc_band_win(int R, const uint32_t* __res
     double rn = bn;
     int steps = 0;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    for (; steps < 12 && rn > 1e-16 * bn; ++steps) {
-        for (uint32_t i = threadIdx.x; i < n; i += NT) t[perm[i]] = rv[i];
+    const int max_steps = sizeof(T) == 4 ? 40 : 12;
+    for (; steps < max_steps && rn > 1e-16 * bn; ++steps) {
+        const double sc = 1.0 / rn;
+        for (uint32_t i = threadIdx.x; i < n; i += NT) t[perm[i]] = (T)(rv[i] * sc);
         __syncthreads();
         if (warp == 0) {
-            // forward: t_{k+1+u} -= l_{k+1+u,k} t_k, the next column prefetched
-            double l0 = 0.0, l1 = 0.0;
-            if (n > 1) {
-                const uint32_t m0 = min(bw, n - 1);
-                if ((uint32_t)lane < m0) l0 = Lc[lane];
-                if ((uint32_t)lane + 32 < m0) l1 = Lc[lane + 32];
-            }
-            for (uint32_t k = 0; k < n; ++k) {
-                const uint32_t m = min(bw, n - 1 - k);
-                double n0 = 0.0, n1 = 0.0;
-                if (k + 1 < n) {
-                    const uint32_t mn = min(bw, n - 2 - k);
-                    if ((uint32_t)lane < mn) n0 = Lc[(size_t)(k + 1) * bw + lane];
-                    if ((uint32_t)lane + 32 < mn) n1 = Lc[(size_t)(k + 1) * bw + lane + 32];
+            // forward: t_{k+1+u} -= l_{k+1+u,k} t_k; the columns come from an
+            // 8-deep register ring, each fetched 8 steps before its use
+            constexpr int P = 8;
+            T r0[P], r1[P];
+            auto col_of = [&](uint32_t k, T* a0, T* a1) {
+                *a0 = 0;
+                *a1 = 0;
+                if (k < n) {
+                    const uint32_t m = min(bw, n - 1 - k);
+                    if ((uint32_t)lane < m) *a0 = Lc[(size_t)k * bw + lane];
+                    if ((uint32_t)lane + 32 < m) *a1 = Lc[(size_t)k * bw + lane + 32];
                 }
-                const double tk = t[k];
-                if ((uint32_t)lane < m) t[k + 1 + lane] -= l0 * tk;
-                if ((uint32_t)lane + 32 < m) t[k + 33 + lane] -= l1 * tk;
-                __syncwarp();
-                l0 = n0;
-                l1 = n1;
+            };
+#pragma unroll
+            for (int j = 0; j < P; ++j) col_of((uint32_t)j, &r0[j], &r1[j]);
+            for (uint32_t k0 = 0; k0 < n; k0 += P) {
+#pragma unroll
+                for (int j = 0; j < P; ++j) {
+                    const uint32_t k = k0 + j;
+                    if (k < n) {
+                        const uint32_t m = min(bw, n - 1 - k);
+                        const T tk = t[k];
+                        if ((uint32_t)lane < m) t[k + 1 + lane] -= r0[j] * tk;
+                        if ((uint32_t)lane + 32 < m) t[k + 33 + lane] -= r1[j] * tk;
+                        col_of(k + P, &r0[j], &r1[j]);
+                    }
+                    __syncwarp();
+                }
             }
             for (uint32_t k = lane; k < n; k += 32) t[k] /= D[k];
             __syncwarp();
-            for (uint32_t kk = n; kk-- > 0;) {  // backward: t_k -= sum_u l_{k+1+u,k} t_{k+1+u}
-                const uint32_t m = min(bw, n - 1 - kk);
-                double acc = 0.0;
-                if ((uint32_t)lane < m) acc = Lc[(size_t)kk * bw + lane] * t[kk + 1 + lane];
-                if ((uint32_t)lane + 32 < m) acc += Lc[(size_t)kk * bw + lane + 32] * t[kk + 33 + lane];
+            // backward: t_k -= sum_u l_{k+1+u,k} t_{k+1+u}, columns from the ring
 #pragma unroll
-                for (int s2 = 16; s2 > 0; s2 >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, s2);
-                if (lane == 0) t[kk] -= acc;
-                __syncwarp();
+            for (int j = 0; j < P; ++j) col_of(n - 1 - (uint32_t)j < n ? n - 1 - (uint32_t)j : n, &r0[j], &r1[j]);
+            for (uint32_t k0 = 0; k0 < n; k0 += P) {
+#pragma unroll
+                for (int j = 0; j < P; ++j) {
+                    const uint32_t step = k0 + j;
+                    if (step < n) {
+                        const uint32_t kk = n - 1 - step;
+                        const uint32_t m = min(bw, n - 1 - kk);
+                        T acc = 0;
+                        if ((uint32_t)lane < m) acc = r0[j] * t[kk + 1 + lane];
+                        if ((uint32_t)lane + 32 < m) acc += r1[j] * t[kk + 33 + lane];
+#pragma unroll
+                        for (int s2 = 16; s2 > 0; s2 >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, s2);
+                        if (lane == 0) t[kk] -= acc;
+                        col_of(step + P < n ? n - 1 - (step + P) : n, &r0[j], &r1[j]);
+                    }
+                    __syncwarp();
+                }
             }
         }
         __syncthreads();
-        for (uint32_t i = threadIdx.x; i < n; i += NT) xt[i] = xx[i] + t[perm[i]];
+        for (uint32_t i = threadIdx.x; i < n; i += NT) xt[i] = xx[i] + rn * (double)t[perm[i]];
         __syncthreads();
-        const double rn_new = residual(xt, true);  // t is free again: it holds the candidate residual
+        const double rn_new = residual(xt, true);
         if (!(rn_new < rn)) { ++steps; break; }  // at the rounding floor
         for (uint32_t i = threadIdx.x; i < n; i += NT) {
             xx[i] = xt[i];
-            rv[i] = t[perm[i]];
+            rv[i] = rc[i];
         }
         __syncthreads();
         rn = rn_new;
@@ -1029,12 +1071,30 @@ nf_status Engine::solve_graph(uint32_t n, const std::vector<uint32_t>& off, cons
     if (direct && bmax <= kDcWin) {
         uint32_t nmax = 0;
         for (int r = 0; r < R; ++r) nmax = std::max(nmax, A.habase[r + 1] - A.habase[r]);
-        const size_t shb = nmax <= kDcShN ? sizeof(double) * nmax : 0;
-        NF_CK(cudaFuncSetAttribute(k_dc_band_win<256>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   (int)(sizeof(double) * kDcShN)));
-        NF_LAUNCH(k_dc_band_win<256>, R, 256, shb, st)(R, dab.p, dcboff.p, dcbw.p, dcperm.p, rowp.p, col.p, val64.p,
-                                                      diag64.p, chain64.p, A.chains ? 1 : 0, bvec.p, xvec.p, cgred.p,
-                                                      dcband.p, dcwork.p, tol, shb ? 1 : 0, outs.p);
+        NF_CK(cgred.ensure(2 * (size_t)na + 2));
+        const size_t sh4 = nmax <= kDcShN ? sizeof(float) * nmax : 0;
+        auto* kf32 = k_dc_band_win<256, float>;
+        auto* kf64 = k_dc_band_win<256, double>;
+        NF_CK(cudaFuncSetAttribute(kf32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(sizeof(float) * kDcShN)));
+        NF_LAUNCH(kf32, R, 256, sh4, st)(R, dab.p, dcboff.p, dcbw.p, dcperm.p, rowp.p, col.p,
+                                                             val64.p, diag64.p, chain64.p, A.chains ? 1 : 0, bvec.p,
+                                                             xvec.p, cgred.p, dcband.p, dcwork.p, tol, sh4 ? 1 : 0,
+                                                             outs.p);
+        NF_CK(cudaGetLastError());
+        std::vector<CgOut> h1(R);
+        NF_CK(cudaMemcpyAsync(h1.data(), outs.p, sizeof(CgOut) * R, cudaMemcpyDeviceToHost, st));
+        NF_CK(cudaStreamSynchronize(st));
+        bool again = false;
+        for (int r = 0; r < R; ++r) again |= h1[r].n > 0 && !(h1[r].res <= tol);
+        if (again) {  // FP32 factors too coarse for this system: FP64 factors
+            const size_t sh8 = nmax <= kDcShN ? sizeof(double) * nmax : 0;
+            NF_CK(cudaFuncSetAttribute(kf64, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)(sizeof(double) * kDcShN)));
+            NF_LAUNCH(kf64, R, 256, sh8, st)(R, dab.p, dcboff.p, dcbw.p, dcperm.p, rowp.p, col.p,
+                                                                  val64.p, diag64.p, chain64.p, A.chains ? 1 : 0,
+                                                                  bvec.p, xvec.p, cgred.p, dcband.p, dcwork.p, tol,
+                                                                  sh8 ? 1 : 0, outs.p);
+        }
     } else if (direct) {
         NF_LAUNCH(k_dc_band<256>, R, 256, 0, st)(R, dab.p, dcboff.p, dcbw.p, dcperm.p, rowp.p, col.p, val64.p, diag64.p,
                                                 chain64.p, A.chains ? 1 : 0, bvec.p, xvec.p, cgred.p, dcband.p,
