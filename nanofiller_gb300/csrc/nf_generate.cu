@@ -1246,17 +1246,19 @@ nf_status Engine::generate() {
         // Cell-sorted candidate copy and the chunk table of this round.
         NF_LAUNCH(k_gather_pd, gs, 256, 0, st)((uint32_t)slots, ntot, cperm.p, cpos.p, cdir.p, gpos.p, gdir.p);
         NF_CK(cudaGetLastError());
-        // The old-rod test runs in three phases when the grid has outer stencil
-        // rows and the round is heavy: every candidate against the centre row
+        // The old-rod test runs in phases when the grid has outer stencil rows
+        // and the round is heavy: every candidate against the centre row
         // (dy = dz = 0: the 5 cells nearest along x, 1/25 of the volume, where
         // most rejected candidates find their first hit), then only the
-        // survivors, packed densely again, against the rest of the inner rows
-        // (|dy|, |dz| <= 1), then the survivors of that against the outer rows.
-        // A warp pays for its dead lanes until its item ends; the packing keeps
-        // the lanes busy. Same decisions as one pass; each further pass costs a
-        // binning, a work list and two launches (~0.1 ms), repaid once
-        // candidates x rods passes ~1e10 (jammed box: old_test 84.5 -> 31.5 ms
-        // per step, against two phases split at the inner ring).
+        // survivors, packed densely again, against the four rows next to it,
+        // then the four inner corner rows, then the outer rows. A warp pays for
+        // its dead lanes until its item ends; the packing keeps the lanes busy.
+        // Same decisions as one pass; each further pass costs a binning, a work
+        // list and two launches (~0.1 ms), repaid once candidates x rods passes
+        // ~1e10 (jammed box: old_test 84.5 -> 31.5 ms per step with three
+        // phases against two split at the inner ring; four phases save another
+        // 1.5 % there and 3.6 % on the large box; five, with the outer rows
+        // split, no more).
         bool outer_rows = false;
         double work = 0;
         for (int r = 0; r < R; ++r) {
@@ -1295,7 +1297,7 @@ nf_status Engine::generate() {
                                                    creal.p, spos.p, sdir.p, state.p, ctr.p);
         }
         NF_CK(cudaGetLastError());
-        for (int ring : {4, 2}) {  // the survivors against the rest of the inner rows, then the outer rows
+        for (int ring : {5, 6, 2}) {  // the survivors against the next inner rows, the inner corners, the outer rows
             if (!phased) break;
             NF_CK(cudaMemcpyAsync(ctr.p + C_XQ_MARK, ctr.p + C_XQ_OLD, sizeof(unsigned long long),
                                   cudaMemcpyDeviceToDevice, st));

@@ -154,17 +154,22 @@ __device__ __forceinline__ void cell_xyz(const Real& Re, uint32_t c, int cc[3]) 
 
 // Row r = (dy, dz) of a radius-S stencil: ring 0 selects every row, ring 1
 // the inner rows (|dy|, |dz| <= 1), ring 2 the others, ring 3 the centre row
-// (dy = dz = 0), ring 4 the inner rows but the centre one.
+// (dy = dz = 0), ring 4 the inner rows but the centre one, ring 5 the four
+// inner rows next to the centre (|dy| + |dz| = 1), ring 6 the four inner
+// corner rows (|dy| = |dz| = 1).
 __device__ __forceinline__ bool row_in_ring(const Real& Re, int r, int ring) {
     if (ring == 0) return true;
     const int w = 2 * Re.S + 1;
     const int dy = r % w - Re.S, dz = r / w - Re.S;
     const bool inner = dy >= -1 && dy <= 1 && dz >= -1 && dz <= 1;
     const bool centre = dy == 0 && dz == 0;
+    const int ady = dy < 0 ? -dy : dy, adz = dz < 0 ? -dz : dz;
     switch (ring) {
         case 1: return inner;
         case 3: return centre;
         case 4: return inner && !centre;
+        case 5: return ady + adz == 1;
+        case 6: return ady == 1 && adz == 1;
         default: return !inner;
     }
 }

@@ -10,7 +10,10 @@ fits, FP32 snaps with every operation rounded on its own):
 - an isotropic law with thin-out (the fitted laws act only through the
   thin-out) and a dense box with clusterisation alone;
 - a batch with adaptive realisations is refused (NF_ERR_UNSUPPORTED) and a
-  plain handle has no laws to read (NF_ERR_STATE).
+  plain handle has no laws to read (NF_ERR_STATE);
+- the command line reads SELF_ALLIGN_STEP, REDUCE_FLAG, CLUST_FLAG,
+  CLUST_ANGL_LIM and the project keys and writes the library's output.bin
+  byte for byte.
 """
 import numpy as np
 import pytest
@@ -97,3 +100,27 @@ def test_adaptive_limits(gpu):
         assert ei.value.status == 10
     with pytest.raises(gpu.NanoFillerError):
         gpu.Simulation(dict(ADAPT, box=(0.8, 2.0, 2.0)))  # clusterisation needs edges >= the rod length
+
+
+def test_cli_adaptive_keywords(gpu, tmp_path):
+    """The reference's keywords drive the adaptive generation of the command
+    line, which writes the library's output.bin byte for byte."""
+    from test_cli import SMALL_KEYS, cli, run
+    exe = cli(gpu)
+    keys = SMALL_KEYS.replace("VOLUME_PERCENT 0.5", "VOLUME_PERCENT 3").replace(
+        "SELF_ALLIGN_STEP 0", "SELF_ALLIGN_STEP 1\nREDUCE_FLAG 1\nCLUST_FLAG 1\nCLUST_ANGL_LIM 0.5\n"
+        "ORIENT VMF\nVMF_KAPPA 2\nEPOCH_CANDIDATES 2000\nALIGN_CELL 1.0")
+    a, b = tmp_path / "cli", tmp_path / "lib"
+    a.mkdir()
+    b.mkdir()
+    (a / "in.txt").write_text(keys)
+    r = run(exe, ["in.txt", "generate"], a)
+    assert r.returncode == 0, r.stderr
+    params, unknown = gpu.params_from_file(a / "in.txt")
+    assert unknown == 0 and params["self_align_step"] == 1 and params["clust_flag"] == 1
+    assert params["clust_angl"] == pytest.approx(0.5) and params["epoch_candidates"] == 2000
+    with gpu.Simulation(params) as sim:
+        g = sim.generate()
+        sim.write_state(b / "output.bin")
+    assert g["refits"] > 0 and g["snapped"] > 0
+    assert (a / "output.bin").read_bytes() == (b / "output.bin").read_bytes()
