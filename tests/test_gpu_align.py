@@ -11,6 +11,8 @@ fits, FP32 snaps with every operation rounded on its own):
   thin-out) and a dense box with clusterisation alone;
 - a batch with adaptive realisations is refused (NF_ERR_UNSUPPORTED) and a
   plain handle has no laws to read (NF_ERR_STATE);
+- the medium agglomerate box (density mesh, von Mises-Fisher) with all
+  three steps, bit for bit;
 - the command line reads SELF_ALLIGN_STEP, REDUCE_FLAG, CLUST_FLAG,
   CLUST_ANGL_LIM and the project keys and writes the library's output.bin
   byte for byte.
@@ -124,3 +126,19 @@ def test_cli_adaptive_keywords(gpu, tmp_path):
         sim.write_state(b / "output.bin")
     assert g["refits"] > 0 and g["snapped"] > 0
     assert (a / "output.bin").read_bytes() == (b / "output.bin").read_bytes()
+
+
+def test_adaptive_with_density_mesh(gpu, oracle):
+    """The medium agglomerate box (8-Gaussian density, von Mises-Fisher kappa
+    4 about z) with all three steps: the per-cell laws and the density draw
+    act together; equal to the oracle bit for bit."""
+    cfg = dict(gpu.configs.MEDIUM, self_align_step=2, reduce_flag=1, clust_flag=1, epoch_candidates=50000,
+               n_candidates=400000)
+    mesh = gpu.configs.gaussian_mesh()
+    with gpu.Simulation(cfg, mesh=mesh) as sim:
+        g = sim.generate()
+        rods = sim.rods()
+        laws = sim.orientation_laws()
+    ro, io, so = oracle.generate(cfg, mesh=mesh)
+    check_equal(g, rods, laws, ro, io, so)
+    assert g["refits"] > 0 and g["thinned"] > 0 and g["snapped"] > 0
