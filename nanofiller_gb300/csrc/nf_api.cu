@@ -408,12 +408,20 @@ nf_status nf_get_rods(nf_handle* h, nf_rods* out) {
     size_t n = E.count[0];
     out->count = n;
     if (out->capacity < n) return NF_ERR_CAPACITY;
-    std::vector<float4> p(n), d(n);
-    std::vector<uint64_t> k(n);
-    cudaError_t e = cudaMemcpyAsync(p.data(), E.pos.p, sizeof(float4) * n, cudaMemcpyDeviceToHost, E.st);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(d.data(), E.dir.p, sizeof(float4) * n, cudaMemcpyDeviceToHost, E.st);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(k.data(), E.sidx.p, sizeof(uint64_t) * n, cudaMemcpyDeviceToHost, E.st);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(E.st);
+    // staged through the handle's pinned host buffer (asynchronous copies at
+    // the link's rate), then unpacked into the caller's arrays
+    nf_status st = E.ensure_pinned(n * (2 * sizeof(float4) + sizeof(uint64_t)) + 16);
+    if (st != NF_OK) return st;
+    float4* p = reinterpret_cast<float4*>(E.hpin);
+    float4* d = p + n;
+    uint64_t* k = reinterpret_cast<uint64_t*>(d + n);
+    cudaError_t e = cudaSuccess;
+    if (n) {
+        e = cudaMemcpyAsync(p, E.pos.p, sizeof(float4) * n, cudaMemcpyDeviceToHost, E.st);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(d, E.dir.p, sizeof(float4) * n, cudaMemcpyDeviceToHost, E.st);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(k, E.sidx.p, sizeof(uint64_t) * n, cudaMemcpyDeviceToHost, E.st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(E.st);
+    }
     if (e != cudaSuccess) return E.cuda_fail(e, "nf_get_rods");
     const nf::Real& Re = E.hreal[0];
     for (size_t i = 0; i < n; ++i) {
@@ -457,17 +465,25 @@ nf_status nf_get_contacts(nf_handle* h, nf_contact_list* out) {
     size_t lo = E.ct_off[0], n = E.ct_off[1] - lo;
     out->count = n;
     if (out->capacity < n) return NF_ERR_CAPACITY;
-    std::vector<uint32_t> I(n), J(n);
-    std::vector<double> t0(n), t1(n), D(n), G(n), S(n);
-    std::vector<int8_t> img(3 * n);
+    // staged through the handle's pinned host buffer: doubles, then ids, then images
+    nf_status st = E.ensure_pinned(n * (5 * sizeof(double) + 2 * sizeof(uint32_t) + 3) + 16);
+    if (st != NF_OK) return st;
+    double* t0 = reinterpret_cast<double*>(E.hpin);
+    double* t1 = t0 + n;
+    double* D = t1 + n;
+    double* G = D + n;
+    double* S = G + n;
+    uint32_t* I = reinterpret_cast<uint32_t*>(S + n);
+    uint32_t* J = I + n;
+    int8_t* img = reinterpret_cast<int8_t*>(J + n);
     cudaError_t e = cudaSuccess;
     auto cp = [&](void* dst, const void* src, size_t bytes) {
         if (e == cudaSuccess && bytes) e = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, E.st);
     };
-    cp(I.data(), E.cI.p + lo, 4 * n); cp(J.data(), E.cJ.p + lo, 4 * n);
-    cp(t0.data(), E.ct0.p + lo, 8 * n); cp(t1.data(), E.ct1.p + lo, 8 * n);
-    cp(D.data(), E.cD.p + lo, 8 * n); cp(G.data(), E.cG.p + lo, 8 * n); cp(S.data(), E.cS.p + lo, 8 * n);
-    cp(img.data(), E.cimg.p + 3 * lo, 3 * n);
+    cp(I, E.cI.p + lo, 4 * n); cp(J, E.cJ.p + lo, 4 * n);
+    cp(t0, E.ct0.p + lo, 8 * n); cp(t1, E.ct1.p + lo, 8 * n);
+    cp(D, E.cD.p + lo, 8 * n); cp(G, E.cG.p + lo, 8 * n); cp(S, E.cS.p + lo, 8 * n);
+    cp(img, E.cimg.p + 3 * lo, 3 * n);
     if (e == cudaSuccess) e = cudaStreamSynchronize(E.st);
     if (e != cudaSuccess) return E.cuda_fail(e, "nf_get_contacts");
     const uint32_t off = E.hreal[0].rod_off;

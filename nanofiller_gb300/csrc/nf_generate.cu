@@ -957,12 +957,16 @@ static nf_status setup_reals(Engine& E) {
         e = E.mesh.ensure(mtot + 1);
         if (e != cudaSuccess) return E.cuda_fail(e, "mesh alloc");
     }
-    for (int r = 0; r < E.R && E.mesh_dirty; ++r)
-        if (!E.hmesh[r].empty()) {
-            e = cudaMemcpyAsync(E.mesh.p + mesh_off[r], E.hmesh[r].data(), E.hmesh[r].size() * sizeof(float),
-                                cudaMemcpyHostToDevice, E.st);
-            if (e != cudaSuccess) return E.cuda_fail(e, "mesh upload");
-        }
+    if (E.mesh_dirty && mtot) {  // one copy through the pinned host buffer
+        nf_status ps = E.ensure_pinned(mtot * sizeof(float));
+        if (ps != NF_OK) return ps;
+        float* stage = reinterpret_cast<float*>(E.hpin);
+        for (int r = 0; r < E.R; ++r)
+            if (!E.hmesh[r].empty()) std::memcpy(stage + mesh_off[r], E.hmesh[r].data(), E.hmesh[r].size() * sizeof(float));
+        e = cudaMemcpyAsync(E.mesh.p, stage, mtot * sizeof(float), cudaMemcpyHostToDevice, E.st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(E.st);  // the staging buffer is reused later
+        if (e != cudaSuccess) return E.cuda_fail(e, "mesh upload");
+    }
     E.mesh_dirty = false;
     E.hreal.resize(E.R);
     uint32_t coffs = 0;
