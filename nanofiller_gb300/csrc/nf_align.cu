@@ -161,13 +161,13 @@ __global__ void k_clu_count(uint32_t slots, const uint32_t* __restrict__ ntot, c
     cnt[i] = k;
 }
 
-__global__ void k_clu_fill(uint32_t slots, const uint32_t* __restrict__ ntot, const Real* __restrict__ reals,
+__global__ void k_clu_fill(uint32_t i0, uint32_t i1, const Real* __restrict__ reals,
                            const float4* __restrict__ cpos, const uint32_t* __restrict__ rstart,
                            const float4* __restrict__ spos, const uint32_t* __restrict__ sid, uint32_t n_old,
                            const uint32_t* __restrict__ off, unsigned long long* __restrict__ key) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= slots || i >= *ntot) return;
-    uint32_t w = off[i];
+    const uint32_t i = i0 + blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= i1) return;
+    uint32_t w = off[i] - off[i0];
     clu_neighbours(reals[0], cpos[i], rstart, spos, sid, n_old, [&](uint32_t j, uint32_t code) {
         key[w++] = ((unsigned long long)i << 37) | ((unsigned long long)j << 5) | code;
     });
@@ -229,20 +229,20 @@ NF_HD float clu_min_dist(const float r1[3], const float c1[3], float l1, float a
 // (rod, image) order and snaps; then the centre is wrapped on periodic axes,
 // and a candidate left outside the box on an open axis is rejected. Cell of
 // the final centre recounted for the binning.
-__global__ void k_clu_apply(uint32_t slots, const uint32_t* __restrict__ ntot, const Real* __restrict__ reals,
+__global__ void k_clu_apply(uint32_t i0, uint32_t i1, const Real* __restrict__ reals,
                             const uint32_t* __restrict__ off, const unsigned long long* __restrict__ key,
                             const float4* __restrict__ pos, const float4* __restrict__ dir, float cos_lim,
                             float dist_lim, float4* __restrict__ cpos, float4* __restrict__ cdir,
                             uint8_t* __restrict__ state, uint32_t* __restrict__ ccell, uint32_t* __restrict__ ccount,
                             uint32_t* __restrict__ nsnap) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= slots || i >= *ntot) return;
+    const uint32_t i = i0 + blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= i1) return;
     const Real& Re = reals[0];
     float4 P = cpos[i], C = cdir[i];
     float r1[3] = {P.x, P.y, P.z}, c1[3] = {C.x, C.y, C.z};
     const float l1 = P.w, a1 = C.w;
     unsigned snaps = 0;
-    for (uint32_t e = off[i]; e < off[i + 1]; ++e) {
+    for (uint32_t e = off[i] - off[i0]; e < off[i + 1] - off[i0]; ++e) {
         const unsigned long long kk = key[e];
         const uint32_t j = (uint32_t)((kk >> 5) & 0xffffffffull), code = (uint32_t)(kk & 31ull);
         const int im[3] = {(int)(code % 3) - 1, (int)((code / 3) % 3) - 1, (int)(code / 9) - 1};
@@ -499,38 +499,72 @@ nf_status Engine::epoch_boundary(uint64_t e, uint32_t gained) {
     return NF_OK;
 }
 
+// Neighbour keys held at once: the round's candidates are processed in chunks
+// whose lists fit (2 x 1 GB of keys), so a dense box with many candidates
+// per round does not need one list for all of them.
+constexpr uint64_t kCluKeyCap = 1ull << 27;
+
 nf_status Engine::clusterize(uint64_t slots, const uint32_t* ntot, uint32_t n_old) {
     const nf_params& p = prm[0];
     NF_CK(clu_cnt.ensure(slots + 1));
     NF_CK(clu_off.ensure(slots + 1));
+    NF_CK(clu_snaps.ensure(slots + 1));
     const unsigned gs = grid_for(slots + 1, 256);
     NF_LAUNCH(k_clu_count, gs, 256, 0, st)((uint32_t)slots, ntot, dreal.p, cpos.p, rstart.p, spos.p, sid.p, n_old,
                                            clu_cnt.p);
     NF_CK(cudaGetLastError());
     nf_status s = scan_u32(clu_cnt.p, clu_off.p, slots + 1);
     if (s != NF_OK) return s;
-    uint32_t total = 0;
+    uint32_t hn = 0, total = 0;
+    NF_CK(cudaMemcpyAsync(&hn, ntot, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
     NF_CK(cudaMemcpyAsync(&total, clu_off.p + slots, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
     NF_CK(cudaStreamSynchronize(st));
-    NF_CK(clu_key.ensure((size_t)total + 1));
-    NF_CK(clu_key2.ensure((size_t)total + 1));
-    if (total) {
-        NF_LAUNCH(k_clu_fill, gs, 256, 0, st)((uint32_t)slots, ntot, dreal.p, cpos.p, rstart.p, spos.p, sid.p, n_old,
-                                              clu_off.p, clu_key.p);
-        NF_CK(cudaGetLastError());
-        g_launches += 1;
-        size_t bytes = 0;
-        NF_CK(cub::DeviceRadixSort::SortKeys(nullptr, bytes, clu_key.p, clu_key2.p, (int)total, 0, 61, st));
-        NF_CK(cubtmp.ensure(bytes));
-        NF_CK(cub::DeviceRadixSort::SortKeys(cubtmp.p, bytes, clu_key.p, clu_key2.p, (int)total, 0, 61, st));
+    // chunks of candidates [i0, i1) with at most kCluKeyCap keys each
+    std::vector<uint32_t> cuts{0u};
+    if ((uint64_t)total > kCluKeyCap) {
+        std::vector<uint32_t> ho(hn + 1);
+        NF_CK(cudaMemcpyAsync(ho.data(), clu_off.p, sizeof(uint32_t) * (hn + 1), cudaMemcpyDeviceToHost, st));
+        NF_CK(cudaStreamSynchronize(st));
+        uint32_t i0 = 0;
+        while (i0 < hn) {
+            uint32_t i1 = i0 + 1;
+            while (i1 < hn && (uint64_t)ho[i1 + 1] - ho[i0] <= kCluKeyCap) ++i1;
+            cuts.push_back(i1);
+            i0 = i1;
+        }
+    } else {
+        cuts.push_back(hn);
     }
+    const uint64_t cap = std::min<uint64_t>(total, kCluKeyCap) + 1;
+    NF_CK(clu_key.ensure(cap));
+    NF_CK(clu_key2.ensure(cap));
     // the snap moves centres: recount the cells
     NF_CK(cudaMemsetAsync(ccount.p, 0, sizeof(uint32_t) * (ncell + 1), st));
-    NF_CK(clu_snaps.ensure(slots + 1));
     const float cos_lim = (float)std::cos((double)p.clust_angl);
-    NF_LAUNCH(k_clu_apply, gs, 256, 0, st)((uint32_t)slots, ntot, dreal.p, clu_off.p, clu_key2.p, pos.p, dir.p, cos_lim,
-                                           p.clust_dist, cpos.p, cdir.p, state.p, ccell.p, ccount.p, clu_snaps.p);
-    NF_CK(cudaGetLastError());
+    for (size_t c = 0; c + 1 < cuts.size(); ++c) {
+        const uint32_t i0 = cuts[c], i1 = cuts[c + 1];
+        if (i1 <= i0) continue;
+        const unsigned gc = grid_for(i1 - i0, 256);
+        NF_LAUNCH(k_clu_fill, gc, 256, 0, st)(i0, i1, dreal.p, cpos.p, rstart.p, spos.p, sid.p, n_old, clu_off.p,
+                                              clu_key.p);
+        NF_CK(cudaGetLastError());
+        uint32_t nk = 0;
+        NF_CK(cudaMemcpyAsync(&nk, clu_off.p + i1, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+        uint32_t nk0 = 0;
+        NF_CK(cudaMemcpyAsync(&nk0, clu_off.p + i0, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+        NF_CK(cudaStreamSynchronize(st));
+        nk -= nk0;
+        if (nk) {
+            g_launches += 1;
+            size_t bytes = 0;
+            NF_CK(cub::DeviceRadixSort::SortKeys(nullptr, bytes, clu_key.p, clu_key2.p, (int)nk, 0, 61, st));
+            NF_CK(cubtmp.ensure(bytes));
+            NF_CK(cub::DeviceRadixSort::SortKeys(cubtmp.p, bytes, clu_key.p, clu_key2.p, (int)nk, 0, 61, st));
+        }
+        NF_LAUNCH(k_clu_apply, gc, 256, 0, st)(i0, i1, dreal.p, clu_off.p, clu_key2.p, pos.p, dir.p, cos_lim,
+                                               p.clust_dist, cpos.p, cdir.p, state.p, ccell.p, ccount.p, clu_snaps.p);
+        NF_CK(cudaGetLastError());
+    }
     return NF_OK;
 }
 

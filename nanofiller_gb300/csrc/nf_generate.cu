@@ -1177,6 +1177,9 @@ nf_status Engine::generate() {
                 c = std::min<uint64_t>(c, p.n_candidates - knext[r]);
                 c = std::min<uint64_t>(c, 1u << 24);
                 if (adapt) c = std::min<uint64_t>(c, epoch_len - knext[r] % epoch_len);
+                // clusterisation lists: candidates x older rods within half a
+                // rod length (a few hundred at jamming) stay below 2^32
+                if (adapt && p.clust_flag) c = std::min<uint64_t>(c, 1u << 20);
                 ++active;
             }
             c_round[r] = c;
