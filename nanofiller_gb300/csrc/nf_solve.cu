@@ -511,6 +511,25 @@ nf_status Engine::assemble(uint32_t n, const std::vector<uint32_t>& off, uint32_
         NF_LAUNCH(k_uf_union, grid_for(m, 256), 256, 0, st)(m, eI, eJ, eG, eC, parent.p, errw);
         NF_LAUNCH(k_uf_flags, grid_for(m, 256), 256, 0, st)(m, eI, eJ, eG, eC, parent.p, cflag.p, errw);
     }
+    if (nslot) NF_LAUNCH(k_active, grid_for(nslot, 256), 256, 0, st)(nslot, parent.p, cflag.p, act, errw);
+    NF_CK(cudaGetLastError());
+    nf_status s = scan_u32(act, aidx.p, nslot + 1);
+    if (s != NF_OK) return s;
+    // Active count per realisation: aidx at the node-range boundaries.
+    out->habase.assign(RR + 1, 0);
+    for (int r = 0; r <= RR; ++r)
+        NF_CK(cudaMemcpyAsync(&out->habase[r], aidx.p + off[r], sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+    uint32_t herr = 0;
+    NF_CK(cudaMemcpyAsync(&herr, errw, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+    NF_CK(cudaStreamSynchronize(st));
+    if (herr) { err = "union-find walk exceeded its bound"; return NF_ERR_TIMEOUT; }
+    const uint32_t na = out->habase[RR];
+    out->na = na;
+    out->chains = m > mc;
+    if (na == 0) {  // no component joins both electrodes: nothing to assemble
+        out->nnz = 0;
+        return NF_OK;
+    }
     // electrode admittance per node
     NF_CK(ecnt.ensure(nslot + 1));
     NF_CK(eoff.ensure(nslot + 1));
@@ -527,20 +546,6 @@ nf_status Engine::assemble(uint32_t n, const std::vector<uint32_t>& off, uint32_
     if (nslot)
         NF_LAUNCH(k_esum, grid_for(nslot, 256), 256, 0, st)(nslot, eoff.p, elist.p, eJ, eG, eC, vsrc.p, vsnk.p, sC, tC);
     NF_CK(cudaGetLastError());
-    if (nslot) NF_LAUNCH(k_active, grid_for(nslot, 256), 256, 0, st)(nslot, parent.p, cflag.p, act, errw);
-    NF_CK(cudaGetLastError());
-    nf_status s = scan_u32(act, aidx.p, nslot + 1);
-    if (s != NF_OK) return s;
-    // Active count per realisation: aidx at the node-range boundaries.
-    out->habase.assign(RR + 1, 0);
-    for (int r = 0; r <= RR; ++r)
-        NF_CK(cudaMemcpyAsync(&out->habase[r], aidx.p + off[r], sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
-    uint32_t herr = 0;
-    NF_CK(cudaMemcpyAsync(&herr, errw, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
-    NF_CK(cudaStreamSynchronize(st));
-    if (herr) { err = "union-find walk exceeded its bound"; return NF_ERR_TIMEOUT; }
-    const uint32_t na = out->habase[RR];
-    out->na = na;
     NF_CK(deg.ensure(na + 1));
     NF_CK(rowp.ensure(na + 1));
     NF_CK(cudaMemsetAsync(deg.p, 0, sizeof(uint32_t) * (na + 1), st));
@@ -1068,7 +1073,9 @@ nf_status Engine::solve_graph(uint32_t n, const std::vector<uint32_t>& off, cons
         }
     }
     tstart(KT_CG);
-    if (direct && bmax <= kDcWin) {
+    if (na == 0) {
+        // every realisation's network is empty: G = 0, voltages from the components alone
+    } else if (direct && bmax <= kDcWin) {
         uint32_t nmax = 0;
         for (int r = 0; r < R; ++r) nmax = std::max(nmax, A.habase[r + 1] - A.habase[r]);
         NF_CK(cgred.ensure(2 * (size_t)na + 2));
@@ -1111,7 +1118,7 @@ nf_status Engine::solve_graph(uint32_t n, const std::vector<uint32_t>& off, cons
                                                                  errw);
     NF_CK(cudaGetLastError());
     std::vector<CgOut> ho(R);
-    NF_CK(cudaMemcpyAsync(ho.data(), outs.p, sizeof(CgOut) * R, cudaMemcpyDeviceToHost, st));
+    if (na) NF_CK(cudaMemcpyAsync(ho.data(), outs.p, sizeof(CgOut) * R, cudaMemcpyDeviceToHost, st));
     NF_CK(cudaEventRecord(ev.b, st));
     NF_CK(cudaEventSynchronize(ev.b));
     outs.release();
