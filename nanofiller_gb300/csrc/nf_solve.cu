@@ -851,7 +851,54 @@ __global__ void __launch_bounds__(NT) k_dc_band_win(int R, const uint32_t* __res
     T pre = 0;
     if (bs < n && threadIdx.x < bs) pre = (T)A[(size_t)bs * bs + threadIdx.x];
     __syncthreads();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     uint32_t sk = 0;  // slot of row k
+    if (bw < 32) {
+        // one warp, no block barriers: lane ii owns trailing row k + 1 + ii and
+        // receives the pivot column's entries by shuffle; rows enter the window
+        // from a 4-deep register ring (row k + bs + j fetched four pivots early)
+        if (warp == 0) {
+            (void)pre;
+            T ring[4];
+#pragma unroll
+            for (int j = 0; j < 4; ++j)
+                ring[j] = (bs + j < n && (uint32_t)lane < bs) ? (T)A[(size_t)(bs + j) * bs + lane] : (T)0;
+            for (uint32_t k0 = 0; k0 < n; k0 += 4) {
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    const uint32_t k = k0 + j;
+                    if (k < n) {
+                        const uint32_t m = min(bw, n - 1 - k);
+                        const T dk = win[sk * bs];
+                        uint32_t sl = sk + 1 + lane;
+                        sl -= sl >= bs ? bs : 0;
+                        T a = 0, l = 0;
+                        if ((uint32_t)lane < m) {
+                            a = win[sl * bs + lane + 1];
+                            l = a / dk;
+                        }
+#pragma unroll 4
+                        for (uint32_t jj = 0; jj < m; ++jj) {
+                            const T u = __shfl_sync(0xffffffffu, a, jj);
+                            if ((uint32_t)lane < m && jj <= (uint32_t)lane) win[sl * bs + (lane - jj)] -= l * u;
+                        }
+                        if ((uint32_t)lane < m) {
+                            win[sl * bs + lane + 1] = l;
+                            Lc[(size_t)k * bw + lane] = l;
+                        }
+                        if (lane == 0) D[k] = dk;
+                        __syncwarp();
+                        if (k + bs < n && (uint32_t)lane < bs) win[sk * bs + lane] = ring[j];
+                        const uint32_t nr = k + bs + 4;
+                        ring[j] = (nr < n && (uint32_t)lane < bs) ? (T)A[(size_t)nr * bs + lane] : (T)0;
+                        sk = sk + 1 == bs ? 0 : sk + 1;
+                        __syncwarp();
+                    }
+                }
+            }
+        }
+        __syncthreads();
+    } else
     for (uint32_t k = 0; k < n; ++k) {
         const uint32_t m = min(bw, n - 1 - k);
         const T dk = win[sk * bs];
@@ -914,13 +961,86 @@ __global__ void __launch_bounds__(NT) k_dc_band_win(int R, const uint32_t* __res
     const double bn = sqrt(block_sum<NT>(part, sh));
     double rn = bn;
     int steps = 0;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int max_steps = sizeof(T) == 4 ? 40 : 12;
     for (; steps < max_steps && rn > 1e-16 * bn; ++steps) {
         const double sc = 1.0 / rn;
         for (uint32_t i = threadIdx.x; i < n; i += NT) t[perm[i]] = (T)(rv[i] * sc);
         __syncthreads();
-        if (warp == 0) {
+        if (warp == 0 && bw < 32) {
+            // blocks of 32 rows, lane j on row B + j. Forward: the rows' sums
+            // over the columns of earlier blocks (all loads issued first), then
+            // the block's own triangle through shuffles: t_c final, the rows
+            // below it lose l_{jc} t_c.
+            for (uint32_t B = 0; B < n; B += 32) {
+                const uint32_t i = B + lane;
+                const bool on = i < n;
+                T acc = on ? t[i] : (T)0;
+                {
+                    T lv[32], tv[32];
+#pragma unroll
+                    for (int kk = 0; kk < 32; ++kk) {
+                        const bool ok = on && (uint32_t)kk < bw && B + kk >= bw;
+                        const uint32_t k = ok ? B + kk - bw : 0;
+                        const bool in = ok && i - k <= bw;
+                        lv[kk] = in ? Lc[(size_t)k * bw + (i - k - 1)] : (T)0;
+                        tv[kk] = in ? t[k] : (T)0;
+                    }
+#pragma unroll
+                    for (int kk = 0; kk < 32; ++kk) acc -= lv[kk] * tv[kk];
+                }
+                T lr[32];
+#pragma unroll
+                for (int c = 0; c < 32; ++c) {
+                    const uint32_t kc = B + c;
+                    lr[c] = (on && c < lane && (uint32_t)(lane - c) <= bw && kc < n)
+                                ? Lc[(size_t)kc * bw + (lane - c - 1)] : (T)0;
+                }
+#pragma unroll
+                for (int c = 0; c < 32; ++c) {
+                    const T tc = __shfl_sync(0xffffffffu, acc, c);
+                    if (c < lane) acc -= lr[c] * tc;
+                }
+                if (on) t[i] = acc;
+                __syncwarp();
+            }
+            for (uint32_t k = lane; k < n; k += 32) t[k] /= D[k];
+            __syncwarp();
+            // backward, blocks from the last: the rows' sums over the rows of
+            // later blocks (their own columns, contiguous), then the block's
+            // triangle from its last row up
+            const uint32_t nb = (n + 31) / 32;
+            for (uint32_t bi = nb; bi-- > 0;) {
+                const uint32_t B = bi * 32, k = B + lane;
+                const bool on = k < n;
+                T acc = on ? t[k] : (T)0;
+                const uint32_t top = B + 32;  // first row of the next block
+                {
+                    T lv[32], tv[32];
+#pragma unroll
+                    for (int u = 0; u < 32; ++u) {
+                        const uint32_t r = k + 1 + u;
+                        const bool in = on && (uint32_t)u < bw && r >= top && r < n;
+                        lv[u] = in ? Lc[(size_t)k * bw + u] : (T)0;
+                        tv[u] = in ? t[r] : (T)0;
+                    }
+#pragma unroll
+                    for (int u = 0; u < 32; ++u) acc -= lv[u] * tv[u];
+                }
+                T lr[32];
+#pragma unroll
+                for (int c = 0; c < 32; ++c) {
+                    lr[c] = (on && c > lane && (uint32_t)(c - lane) <= bw && B + c < n)
+                                ? Lc[(size_t)k * bw + (c - lane - 1)] : (T)0;
+                }
+#pragma unroll
+                for (int c = 31; c >= 0; --c) {
+                    const T tc = __shfl_sync(0xffffffffu, acc, c);
+                    if (c > lane) acc -= lr[c] * tc;
+                }
+                if (on) t[k] = acc;
+                __syncwarp();
+            }
+        } else if (warp == 0) {
             // forward: t_{k+1+u} -= l_{k+1+u,k} t_k; the columns come from an
             // 8-deep register ring, each fetched 8 steps before its use
             constexpr int P = 8;
