@@ -16,7 +16,9 @@ inc/allignment_fit.h, inc/cuda_Clusterize.h):
 - the generation does not depend on the batch size, the thread count or the
   neighbour search (cells or brute force), refits, thins and snaps;
 - with an isotropic law, refits alone change nothing: the rods equal the
-  plain generation's.
+  plain generation's;
+- REDUCE_FLAG without refits thins nothing, one epoch longer than the budget
+  has no boundary, and a rod minimum no cell reaches keeps every law global.
 """
 import math
 
@@ -145,3 +147,18 @@ def test_isotropic_refits_alone_change_nothing():
     assert np.array_equal(r0, r1) and np.array_equal(i0, i1)
     assert np.any(s1["laws"][:, 9] > 0)  # fitted, for the thin-out only
     assert np.all(s1["laws"][:, 11] == 0)
+
+
+def test_adaptive_edge_rules():
+    base = dict(ADAPT, clust_flag=0)
+    plain = dict(base, self_align_step=0, reduce_flag=0)
+    r0, i0, _ = O.generate(plain)
+    # thin-out only follows a refit (src/cudaMain.cu:128-131): REDUCE_FLAG alone changes nothing
+    r1, i1, s1 = O.generate(dict(base, self_align_step=0, reduce_flag=1))
+    assert np.array_equal(r0, r1) and np.array_equal(i0, i1) and s1["refits"] == 0 and s1["thinned"] == 0
+    # one epoch longer than the budget: no boundary, no refit
+    r2, i2, s2 = O.generate(dict(base, epoch_candidates=10 ** 9))
+    assert s2["epochs"] == 1 and s2["refits"] == 0 and np.array_equal(r0, r2)
+    # a cell needs ALIGN_MIN_RODS rods for a refit: with an impossible minimum every law stays global
+    _, _, s3 = O.generate(dict(base, align_min=10 ** 6))
+    assert s3["refits"] > 0 and np.all(s3["laws"][:, 9] == np.float32(2.0))
