@@ -169,9 +169,10 @@ class Simulation:
 
     def rods(self):
         n = self.n_rods()
-        out = {f: np.zeros(n, np.float32) for f in ("x", "y", "z", "cx", "cy", "cz", "l", "a")}
-        out["stream_index"] = np.zeros(n, np.uint64)
-        out["cell"] = np.zeros(n, np.uint32)
+        # every element is written by nf_get_rods
+        out = {f: np.empty(n, np.float32) for f in ("x", "y", "z", "cx", "cy", "cz", "l", "a")}
+        out["stream_index"] = np.empty(n, np.uint64)
+        out["cell"] = np.empty(n, np.uint32)
         r = NfRods()
         r.capacity = n
         for f in ("x", "y", "z", "cx", "cy", "cz", "l", "a"):
@@ -202,9 +203,10 @@ class Simulation:
         if st not in (0, 5):
             _check(st, self._h, "nf_get_contacts")
         n = int(c.count)
-        out = dict(I=np.zeros(n, np.uint32), J=np.zeros(n, np.uint32), tI=np.zeros(n, np.float32),
-                   tJ=np.zeros(n, np.float32), D=np.zeros(n), G=np.zeros(n), S=np.zeros(n),
-                   image=np.zeros((n, 3), np.int8))
+        # every element is written by nf_get_contacts
+        out = dict(I=np.empty(n, np.uint32), J=np.empty(n, np.uint32), tI=np.empty(n, np.float32),
+                   tJ=np.empty(n, np.float32), D=np.empty(n), G=np.empty(n), S=np.empty(n),
+                   image=np.empty((n, 3), np.int8))
         c.capacity = n
         c.I = out["I"].ctypes.data_as(C.POINTER(C.c_uint32))
         c.J = out["J"].ctypes.data_as(C.POINTER(C.c_uint32))

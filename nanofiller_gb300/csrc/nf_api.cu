@@ -424,6 +424,18 @@ nf_status nf_get_rods(nf_handle* h, nf_rods* out) {
     }
     if (e != cudaSuccess) return E.cuda_fail(e, "nf_get_rods");
     const nf::Real& Re = E.hreal[0];
+    // one pass over the staging buffer; no per-element tests when every field is wanted
+    if (out->x && out->y && out->z && out->l && out->cx && out->cy && out->cz && out->a && out->stream_index &&
+        out->cell) {
+        for (size_t i = 0; i < n; ++i) {
+            const float4 pi = p[i], di = d[i];
+            out->x[i] = pi.x; out->y[i] = pi.y; out->z[i] = pi.z; out->l[i] = pi.w;
+            out->cx[i] = di.x; out->cy[i] = di.y; out->cz[i] = di.z; out->a[i] = di.w;
+            out->stream_index[i] = k[i];
+            out->cell[i] = nf::cell_of(Re, pi.x, pi.y, pi.z);
+        }
+        return NF_OK;
+    }
     for (size_t i = 0; i < n; ++i) {
         if (out->x) out->x[i] = p[i].x;
         if (out->y) out->y[i] = p[i].y;
@@ -487,16 +499,14 @@ nf_status nf_get_contacts(nf_handle* h, nf_contact_list* out) {
     if (e == cudaSuccess) e = cudaStreamSynchronize(E.st);
     if (e != cudaSuccess) return E.cuda_fail(e, "nf_get_contacts");
     const uint32_t off = E.hreal[0].rod_off;
-    for (size_t q = 0; q < n; ++q) {
-        if (out->I) out->I[q] = I[q] - off;
-        if (out->J) out->J[q] = J[q] >= NF_SNK_ELEC ? J[q] : J[q] - off;
-        if (out->tI) out->tI[q] = (float)t0[q];
-        if (out->tJ) out->tJ[q] = (float)t1[q];
-        if (out->D) out->D[q] = D[q];
-        if (out->G) out->G[q] = G[q];
-        if (out->S) out->S[q] = S[q];
-        if (out->image) for (int d = 0; d < 3; ++d) out->image[3 * q + d] = img[3 * q + d];
-    }
+    if (out->I) for (size_t q = 0; q < n; ++q) out->I[q] = I[q] - off;
+    if (out->J) for (size_t q = 0; q < n; ++q) out->J[q] = J[q] >= NF_SNK_ELEC ? J[q] : J[q] - off;
+    if (out->tI) for (size_t q = 0; q < n; ++q) out->tI[q] = (float)t0[q];
+    if (out->tJ) for (size_t q = 0; q < n; ++q) out->tJ[q] = (float)t1[q];
+    if (out->D) std::memcpy(out->D, D, sizeof(double) * n);
+    if (out->G) std::memcpy(out->G, G, sizeof(double) * n);
+    if (out->S) std::memcpy(out->S, S, sizeof(double) * n);
+    if (out->image) std::memcpy(out->image, img, 3 * n);
     return NF_OK;
 }
 
