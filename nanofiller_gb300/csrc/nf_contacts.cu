@@ -282,6 +282,10 @@ __global__ void __launch_bounds__(kTPB) k_scr_tiles(const Real* __restrict__ rea
                                                     unsigned long long* __restrict__ xq, unsigned long long xcap,
                                                     unsigned long long* __restrict__ ctr) {
     __shared__ WarpTile tiles[kTPB / 32];
+    // the chunk's virtual rods for the transposed loop (lanes on targets)
+    __shared__ float4 vps[kTPB / 32][32], vds[kTPB / 32][32];
+    __shared__ float vsh[kTPB / 32][32][3];
+    __shared__ uint32_t vid[kTPB / 32][32];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     WarpTile& T = tiles[w];
     const float epsf = 1e-6f;
@@ -302,7 +306,14 @@ __global__ void __launch_bounds__(kTPB) k_scr_tiles(const Real* __restrict__ rea
             for (int d = 0; d < 3; ++d) svf[d] = (float)dsub(o[8 + d], img[d] * (double)Re.L[d]);
             pV = vpf[id];
             cV = vdf[id];
+            vps[w][lane] = pV;
+            vds[w][lane] = cV;
+            vsh[w][lane][0] = svf[0];
+            vsh[w][lane][1] = svf[1];
+            vsh[w][lane][2] = svf[2];
+            vid[w][lane] = id;
         }
+        __syncwarp();
         for (uint32_t b = 0; b < nt; b += kWT) {
             if (b + lane < nt) {
                 T.p[lane] = spos[I.tfirst + b + lane];
@@ -310,7 +321,21 @@ __global__ void __launch_bounds__(kTPB) k_scr_tiles(const Real* __restrict__ rea
             }
             __syncwarp();
             const uint32_t m = min((uint32_t)kWT, nt - b);
-            if (have) {
+            if (np < m) {
+                // fewer virtual rods than staged rods (contacts are sparse):
+                // lane = rod, the warp walks the chunk's np virtual rods
+                if ((uint32_t)lane < m) {
+                    tests += np;
+                    const float4 pR = T.p[lane], cR = T.c[lane];
+                    for (uint32_t pi = 0; pi < np; ++pi) {
+                        const float4 pv = vps[w][pi], cv = vds[w][pi];
+                        const float thr = (cv.w + cR.w) + epsf;
+                        if (maybe_near(pR, cR, pv, cv, vsh[w][pi][0], vsh[w][pi][1], vsh[w][pi][2], thr, epsf,
+                                       Re.slack))
+                            xq_push(xq, xcap, &ctr[C_XQ], xq_pack(vid[w][pi], I.tfirst + b + lane, img));
+                    }
+                }
+            } else if (have) {
                 tests += m;
                 for (uint32_t j = 0; j < m; ++j) {
                     const float4 pR = T.p[j], cR = T.c[j];
