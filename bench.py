@@ -72,7 +72,7 @@ def workload_config(name, params):
 
 # --------------------------------------------------------------------------- clocks
 class Nvml:
-    """Read-only NVML queries through the driver's libnvidia-ml (ctypes): the
+    """Read-only NVML queries through NVIDIA's libnvidia-ml (ctypes): the
     SM clock, its maximum and the clock-event reason mask. Nothing is set."""
     # reason bits of nvmlClocksEventReason* (nvml.h)
     BITS = {"sw_power_cap": 0x4, "hw_slowdown": 0x8, "sw_thermal_slowdown": 0x20,

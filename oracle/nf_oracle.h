@@ -1,8 +1,9 @@
 /*
  * nf_oracle.h -- CPU oracle for the NanoFiller hot path (TEST INFRASTRUCTURE).
  *
- * This library is the checker: only the tests, __graft_entry__.smoke() and the
- * CPU-baseline leg of bench.py load it. The product library never links it.
+ * This library is the oracle, used only to check and to time a CPU baseline:
+ * only the tests, __graft_entry__.smoke() and the CPU-baseline leg of bench.py
+ * load it. The product library never links it.
  *
  * It restates, in plain C++ evaluated in FP64 (or FP32 for pinning against the
  * reference's own source), the reference's algorithm for:
