@@ -115,8 +115,9 @@ typedef struct nf_params {
                                the expected need; 0 -> 2                      */
     double two_phase_work;  /* TWO_PHASE_WORK: candidates x rods of a round
                                above which the old-rod test runs in phases
-                               (centre stencil row, other inner rows, outer
-                               rows; survivors packed between them);
+                               (centre stencil row, the four rows beside it,
+                               the four inner corner rows, outer rows;
+                               survivors packed between them);
                                0 -> 1e10, < 0 -> never                      */
     /* --- intra-rod resistor network (stat_conduct ... internal) --- */
     double rod_sigma;       /* ROD_CONDUCTIVITY (S/um): a rod segment between
