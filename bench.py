@@ -246,7 +246,12 @@ def run_batched(args, rank, world):
     from nanofiller_gb300 import build as nb
 
     nb.build()
-    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     reals = nf.configs.batched_realisations(args.batch)
     for p in reals:
         p["seed"] += rank * args.batch
@@ -265,19 +270,21 @@ def run_batched(args, rank, world):
         out, st = nf.batch_run(reals)
         return [(r["accepted"], r["contacts"], r["G_eff"], r["percolating"]) for r in out]
 
-    clocks = Clocks(int(os.environ.get("LOCAL_RANK", "0")))
+    clocks = Clocks(local)
     clocks.start()
     for _ in range(max(1, min(args.warmup, 2))):
         rb = batched()
     clocks.mark()
     l0 = nf.kernel_launches()
     torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
     t0 = time.perf_counter()
     steps = max(1, args.steps)
     for _ in range(steps):
         rb = batched()
     torch.cuda.synchronize()
-    tb = (time.perf_counter() - t0) / steps
+    tb = over_ranks(dist, (time.perf_counter() - t0) / steps, "max", "cuda")
     launches = nf.kernel_launches() - l0
     clk = clocks.stop()
     plain()  # warm
@@ -286,7 +293,7 @@ def run_batched(args, rank, world):
     tp = time.perf_counter() - t0
     same = all(a[0] == b[0] and a[1] == b[1] and abs(a[2] - b[2]) <= 1e-9 * max(abs(a[2]), 1e-30)
                for a, b in zip(rp, rb))
-    rods = sum(r[0] for r in rb)
+    rods = over_ranks(dist, sum(r[0] for r in rb), "sum", "cuda")
     vf = [p["vf"] for p in reals]
     bins = [0.002, 0.004, 0.008, 0.016, 0.0201]
     table = []
@@ -303,10 +310,13 @@ def run_batched(args, rank, world):
             "scaling": "weak", "vs_baseline": None, "dtype": "f32 filter + f64 decisions", "data": "synthetic",
             "config": {"workload": "batched", "realisations": len(reals), "box_um": [2.0, 10.0],
                        "vf": [0.002, 0.02], "rod_um": [1.0, 0.005], "parallelism": f"replicas x{world}"},
-            "rods_per_s": world * rods / tb, "plain_realisations_per_s": len(reals) / tp,
+            "rods_per_s": rods / tb, "plain_realisations_per_s": len(reals) / tp,
             "batched_over_plain": tp / tb, "batched_equals_plain": same, "gpu_launches": int(launches),
             "vs_vf": table, "clocks": clk,
         }))
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
     return 0
 
 
@@ -339,6 +349,20 @@ def run_reference(args, rank, world):
         "e2e": {"value": value, "unit": "rods/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }))
     return 0
+
+
+# --------------------------------------------------------------------------- replicas
+def over_ranks(dist, v, how, device):
+    """v reduced over the ranks of a replica run: "max" for step times (the
+    slowest rank sets the job's time), "sum" for the rods every rank placed.
+    v itself without a process group. device is the process group's tensor
+    device ("cuda" under NCCL, "cpu" under gloo)."""
+    if not dist:
+        return v
+    import torch
+    t = torch.tensor([float(v)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX if how == "max" else dist.ReduceOp.SUM)
+    return float(t.item())
 
 
 # --------------------------------------------------------------------------- GPU leg
@@ -395,12 +419,9 @@ def run_ours(args, rank, world):
     ms = sum(a.elapsed_time(b) for a, b in evs) / len(evs)
     g, c, s = res
     rods = g["accepted"]
-    ms_max = ms
-    if dist:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms_max = float(t.item())
-    value = world * rods / (ms_max / 1000)
+    ms_max = over_ranks(dist, ms, "max", "cuda")
+    rods_all = over_ranks(dist, rods, "sum", "cuda")
+    value = rods_all / (ms_max / 1000)
     # Kernel breakdown of the timed steps (CUDA events on the library's stream).
     kern = {k: sim.kernel_time(k) for k in ("stream", "old_test", "conflicts", "ct_pairs", "screen", "cg")}
     dom = max(kern, key=lambda k: kern[k]["ms"])
@@ -483,12 +504,8 @@ def run_ours(args, rank, world):
                 times.append(time.perf_counter() - t0)
             h2d = (mesh.nbytes if mesh is not None else 0)
             d2h = sum(a.nbytes for a in r.values()) + sum(a.nbytes for a in ct.values()) + 8
-        e_ms = 1000 * sum(times) / len(times)
-        if dist:
-            t = torch.tensor([e_ms], device="cuda")
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            e_ms = float(t.item())
-        out["e2e"] = {"value": world * rods / (e_ms / 1000), "unit": "rods/s", "h2d_bytes_per_step": int(h2d),
+        e_ms = over_ranks(dist, 1000 * sum(times) / len(times), "max", "cuda")
+        out["e2e"] = {"value": rods_all / (e_ms / 1000), "unit": "rods/s", "h2d_bytes_per_step": int(h2d),
                       "d2h_bytes_per_step": int(d2h), "ms_per_step": e_ms}
     sim.close()
     if rank == 0 and not args.no_cpu_baseline:
