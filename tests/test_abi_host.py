@@ -186,3 +186,37 @@ def test_create_reports_status_codes(lib):
     st = L.nf_create(ctypes.byref(bad), ctypes.byref(h))
     assert st in (1, 3)  # NF_ERR_PARAM, or NF_ERR_NO_DEVICE on a host without GPU
     assert L.nf_destroy(None) == 1
+
+
+STRUCTS = {"NfParams": "nf_params", "NfRods": "nf_rods", "NfContactList": "nf_contact_list",
+           "NfGenStats": "nf_gen_stats", "NfContactStats": "nf_contact_stats", "NfSolveStats": "nf_solve_stats",
+           "NfBatchResult": "nf_batch_result", "NfBatchStats": "nf_batch_stats",
+           "NfInternalStats": "nf_internal_stats", "NfInternalNet": "nf_internal_net",
+           "NfReduceStats": "nf_reduce_stats", "NfPairStats": "nf_pair_stats", "NfAcParams": "nf_ac_params",
+           "NfAcPoint": "nf_ac_point", "NfAcStats": "nf_ac_stats", "NfAcNet": "nf_ac_net",
+           "NfTuneResult": "nf_tune_result", "NfStateHeader": "nf_state_header"}
+
+
+def test_ctypes_layouts_match_the_header(lib, tmp_path):
+    """Every structure of the header, compiled by the C compiler, has the
+    size and field offsets of its ctypes mirror (a field appended to one side
+    only shows up here)."""
+    from nanofiller_gb300 import _abi
+    src = tmp_path / "layout.c"
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "nanofiller_gb300.h"', "int main(void) {"]
+    want = []
+    for py, cname in STRUCTS.items():
+        cls = getattr(_abi, py)
+        lines.append(f'printf("%zu\\n", sizeof({cname}));')
+        want.append(C.sizeof(cls))
+        for f, _ in cls._fields_:
+            lines.append(f'printf("%zu\\n", offsetof({cname}, {"lambda" if f == "lambda_" else f}));')
+            want.append(getattr(cls, f).offset)
+    lines += ["return 0;", "}"]
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    subprocess.run(["gcc", "-std=c11", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)],
+                   check=True, capture_output=True)
+    got = [int(x) for x in subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split()]
+    assert got == want
+    assert set(STRUCTS.values()) == set(re.findall(r"\}\s*(nf_[a-z_]+)\s*;", open(HEADER).read())) - {"nf_status"}
