@@ -250,6 +250,20 @@ def test_small_golden_fixture(oracle):
     np.testing.assert_allclose(ct["G"], g["G"], rtol=1e-14)
 
 
+def test_empty_inputs(oracle):
+    """No candidates: no rods, no contacts of any role, and a network with no
+    nodes solves to G_eff = 0 without iterating (the empty cases the GPU path
+    is held to in test_empty_rod_set_through_every_stage)."""
+    from nanofiller_gb300 import configs
+    p = dict(configs.SMALL, n_candidates=0)
+    rods, idx, st = oracle.generate(p)
+    assert len(rods) == len(idx) == 0 and st["drawn"] == 0
+    ct = oracle.contacts(p, rods)
+    assert ct["counts"] == {"internal": 0, "screened": 0, "sink": 0, "source": 0} and len(ct["I"]) == 0
+    G, v, info = oracle.solve(0, ct)
+    assert G == 0.0 and len(v) == 0 and info["n_active"] == 0 and not info["percolating"]
+
+
 def test_contacts_cells_vs_bruteforce(oracle):
     from nanofiller_gb300 import configs
     p = dict(configs._COMMON, box=(2.5, 2.5, 2.5), vf=0.02, n_candidates=200000, seed=5)
