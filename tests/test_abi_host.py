@@ -5,6 +5,7 @@ import ctypes as C
 import os
 import re
 import subprocess
+import sys
 
 import numpy as np
 import pytest
@@ -220,3 +221,24 @@ def test_ctypes_layouts_match_the_header(lib, tmp_path):
     got = [int(x) for x in subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split()]
     assert got == want
     assert set(STRUCTS.values()) == set(re.findall(r"\}\s*(nf_[a-z_]+)\s*;", open(HEADER).read())) - {"nf_status"}
+
+
+def test_no_fallback_without_the_library(tmp_path):
+    """With the shared library absent the package raises on first use; nothing
+    runs on the CPU in its place."""
+    code = (
+        "import sys; sys.path.insert(0, %r)\n"
+        "import nanofiller_gb300 as nf\n"
+        "from nanofiller_gb300 import _abi\n"
+        "_abi.LIB_PATH = %r\n"
+        "for f in (lambda: nf.Simulation(dict(nf.configs.SMALL)), lambda: nf.batch_run([dict(nf.configs.SMALL)]),\n"
+        "          nf.kernel_launches):\n"
+        "    try:\n"
+        "        f()\n"
+        "    except RuntimeError as e:\n"
+        "        assert 'no CPU fallback' in str(e), e\n"
+        "    else:\n"
+        "        raise SystemExit('ran without the library')\n"
+        "print('ok')\n" % (ROOT, str(tmp_path / "absent.so")))
+    r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0 and r.stdout.strip() == "ok", r.stderr[-2000:]
