@@ -69,9 +69,13 @@ typedef struct nf_params {
     char density_file[256]; /* SPAT_DISTR_FILE <file> (read_density format)  */
     float pref_ort[2];      /* PREF_ORT_PHI, PREF_ORT_THETA (rad)            */
     float theta_med;        /* DEF_THETA_MED (rad)                           */
-    float theta_dev;        /* DEF_THETA_DEV (rad, <=0: isotropic)           */
+    float theta_dev;        /* DEF_THETA_DEV (rad, <=0: cos theta uniform);
+                               > 0: theta truncated normal about theta_med,
+                               measured from the preferred axis            */
     float phi_med;          /* DEF_PHI_MED (rad)                             */
-    float phi_dev;          /* DEF_PHI_DEV (rad, <=0: uniform)               */
+    float phi_dev;          /* DEF_PHI_DEV (rad, <=0: phi uniform); > 0: phi
+                               truncated normal about phi_med (genCosine,
+                               inc/cuda_CNTgenerate.h:262-270)             */
     float l;                /* INC_LEN_MED: rod length (median if lognormal) */
     float a;                /* INC_RAD_MED: rod radius                       */
     float l_dev;            /* INC_LEN_DEV (parsed)                          */
@@ -133,7 +137,13 @@ typedef struct nf_params {
                                source contact and above it a sink contact
                                (get_elec_dmnID, inc/conductivity.h:71-90), one
                                per image rod                                 */
-    int32_t pad_end;
+    int32_t ref_trunc_normal; /* TRUNC_NORMAL_REF: 1 draws DEF_THETA_DEV / DEF_PHI_DEV
+                               angles by the reference's own formula a + 2 s
+                               sqrt2 erfinv(Fa (1 - 2u)), Fa = erf(-w/s/sqrt2)/2
+                               (sym_truncNormal, inc/cuda_CNTgenerate.h:271-275:
+                               not a normal law); 0 (default) the exact normal
+                               of deviation s truncated to a +- w (w = pi/2 for
+                               theta, pi for phi)                            */
     /* --- adaptive generation: self-alignment, thin-out, clusterisation ---
      * The reference refits per-cell orientation laws every SELF_ALLIGN_STEP
      * rounds or when a round gained fewer than 1 % of the rods still missing

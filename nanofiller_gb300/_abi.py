@@ -39,7 +39,7 @@ class NfParams(C.Structure):
         ("round_candidates", C.c_int32), ("solve_max_iter", C.c_int32), ("solve_tol", C.c_double),
         ("stencil_radius", C.c_int32), ("round_overshoot", C.c_float), ("two_phase_work", C.c_double),
         ("rod_sigma", C.c_double),
-        ("elec_buffer", C.c_int32), ("pad_end", C.c_int32),
+        ("elec_buffer", C.c_int32), ("ref_trunc_normal", C.c_int32),
         ("clust_dist", C.c_float), ("clust_angl", C.c_float), ("align_cell", C.c_float),
         ("align_min", C.c_int32), ("epoch_candidates", C.c_int64),
         ("solve_method", C.c_int32), ("pad_solve", C.c_int32),

@@ -67,8 +67,16 @@ nf_status validate(const nf_params& p, std::string* why) {
         for (int d = 0; d < 3; ++d)
             if (p.box[d] < lmax) { *why = "clusterisation needs box edges of at least the longest rod"; return NF_ERR_PARAM; }
     }
-    if (p.theta_dev > 0 || p.phi_dev > 0) {
-        *why = "truncated-normal orientation is not run by this path (use ORIENT VMF)"; return NF_ERR_UNSUPPORTED;
+    if ((p.theta_dev > 0 || p.phi_dev > 0) && p.orient_mode == NF_ORIENT_VMF) {
+        *why = "ORIENT VMF and DEF_THETA_DEV / DEF_PHI_DEV > 0 are exclusive orientation laws"; return NF_ERR_PARAM;
+    }
+    if ((p.theta_dev > 0 || p.phi_dev > 0) && p.self_align_step > 0) {
+        *why = "adaptive generation refits von Mises-Fisher laws; it does not run with DEF_THETA_DEV / DEF_PHI_DEV > 0";
+        return NF_ERR_UNSUPPORTED;
+    }
+    if (!std::isfinite(p.theta_med) || !std::isfinite(p.phi_med) || !std::isfinite(p.theta_dev) ||
+        !std::isfinite(p.phi_dev) || p.ref_trunc_normal < 0 || p.ref_trunc_normal > 1) {
+        *why = "DEF_THETA_* / DEF_PHI_* must be finite and TRUNC_NORMAL_REF 0 or 1"; return NF_ERR_PARAM;
     }
     if (p.orient_mode == NF_ORIENT_VMF && !(p.vmf_kappa > 0)) { *why = "VMF_KAPPA must be positive"; return NF_ERR_PARAM; }
     if (p.len_mode == NF_SIZE_LOGNORMAL && !(p.len_min > 0 && p.len_max >= p.len_min)) {
@@ -233,6 +241,7 @@ nf_status nf_params_from_file(const char* path, nf_params* p, int* n_unknown) {
         else if (key == "TUNNEL_LAMBDA") in >> p->lambda;
         else if (key == "TUNNEL_DC") in >> p->d_c;
         else if (key == "REF_PARALLEL_TYPO") in >> p->ref_parallel_typo;
+        else if (key == "TRUNC_NORMAL_REF") in >> p->ref_trunc_normal;
         else if (key == "SCREENING") in >> p->screening;
         else if (key == "ROUND_CANDIDATES") in >> p->round_candidates;
         else if (key == "SOLVE_MAX_ITER") in >> p->solve_max_iter;

@@ -142,6 +142,141 @@ NF_HD float exp_nf(float x) {
 }
 
 // ---------------------------------------------------------------------------
+// FP64 error function and its inverse, for the truncated-normal angle law
+// (sym_truncNormal, inc/cuda_CNTgenerate.h:271-275). Written from the
+// mathematics, one operation sequence on host and device (no fused
+// multiply-add), so the oracle reproduces every bit:
+//  * ln x: exponent split, 2 atanh((m-1)/(m+1)) by its odd series to s^27;
+//  * e^x: Cody-Waite reduction by ln 2 (high part with 32 significant bits),
+//    Taylor polynomial of degree 13, 2^k scaling;
+//  * erf x: Maclaurin series (35 terms, Horner in -x^2) below 2; above,
+//    1 - erfc x with erfc from the Laplace continued fraction
+//    e^{-x^2} / (sqrt(pi) (x + (1/2)/(x + 1/(x + (3/2)/(x + ...))))),
+//    evaluated bottom-up to depth 50;
+//  * erfinv y: the closed-form start of Winitzki ("A handy approximation for
+//    the error function and its inverse", 2008; a = 0.147), or sqrt(pi)/2 y
+//    below 1e-3, then two Halley steps on erf (residual formed from erfc
+//    above 2, where 1 - |y| is exact).
+// Relative error against 50-digit arithmetic: ln and e^x below 3e-16, erf below
+// 1e-15, erfinv below 2e-14 down to 1 - |y| = 1e-16.
+// ---------------------------------------------------------------------------
+#ifdef __CUDA_ARCH__
+NF_HD uint64_t d2u(double v) { return (uint64_t)__double_as_longlong(v); }
+NF_HD double u2d(uint64_t u) { return __longlong_as_double((long long)u); }
+#else
+NF_HD uint64_t d2u(double v) { uint64_t u; memcpy(&u, &v, 8); return u; }
+NF_HD double u2d(uint64_t u) { double v; memcpy(&v, &u, 8); return v; }
+#endif
+constexpr double kLn2Hi = 0.6931471803691238;      // ln 2 rounded to 32 bits
+constexpr double kLn2Lo = 1.9082149292705877e-10;  // ln 2 - kLn2Hi
+constexpr double kInvLn2 = 1.4426950408889634;
+constexpr double kSqrt2 = 1.4142135623730951;
+constexpr double kSqrtPiHalf = 0.886226925452758;  // sqrt(pi) / 2
+constexpr double kTwoInvSqrtPi = 1.1283791670955126;
+constexpr double kInvSqrtPi = 0.5641895835477563;
+constexpr double kPiD = 3.141592653589793;
+constexpr double kInv2PiD = 0.15915494309189535;
+constexpr double kErfSplit = 2.0;
+
+NF_HD double log_d(double x) {
+    const uint64_t b = d2u(x);
+    int e = (int)((b >> 52) & 0x7ffu) - 1023;
+    double m = u2d((b & 0x000fffffffffffffull) | 0x3ff0000000000000ull);
+    if (m > kSqrt2) { m = dmul(m, 0.5); e += 1; }
+    const double s = ddiv(dsub(m, 1.0), dadd(m, 1.0));
+    const double s2 = dmul(s, s);
+    double p = 1.0 / 27;
+#pragma unroll
+    for (int k = 25; k >= 3; k -= 2) p = dadd(dmul(p, s2), 1.0 / k);
+    const double two_s = dadd(s, s);
+    const double lm = dadd(two_s, dmul(two_s, dmul(s2, p)));
+    return dadd(dmul((double)e, kLn2Hi), dadd(dmul((double)e, kLn2Lo), lm));
+}
+
+NF_HD double exp_d(double x) {
+    const double c[14] = {1.0, 1.0, 0.5, 0.16666666666666666, 0.041666666666666664, 0.008333333333333333,
+                          0.001388888888888889, 0.0001984126984126984, 2.48015873015873e-05,
+                          2.7557319223985893e-06, 2.755731922398589e-07, 2.505210838544172e-08,
+                          2.08767569878681e-09, 1.6059043836821613e-10};
+    const double kf = floor(dadd(dmul(x, kInvLn2), 0.5));
+    const double r = dsub(dsub(x, dmul(kf, kLn2Hi)), dmul(kf, kLn2Lo));
+    double p = c[13];
+#pragma unroll
+    for (int n = 12; n >= 0; --n) p = dadd(dmul(p, r), c[n]);
+    int k = (int)kf;
+    k = k < -1022 ? -1022 : (k > 1023 ? 1023 : k);
+    return dmul(p, u2d((uint64_t)(k + 1023) << 52));
+}
+
+// erf x for 0 <= x < 2: 2/sqrt(pi) sum_n (-1)^n x^(2n+1) / (n! (2n+1)).
+NF_HD double erf_series(double x) {
+    const double c[35] = {1.0, 0.3333333333333333, 0.1, 0.023809523809523808, 0.004629629629629629,
+                          0.0007575757575757576, 0.00010683760683760684, 1.3227513227513228e-05,
+                          1.4589169000933706e-06, 1.4503852223150468e-07, 1.3122532963802806e-08,
+                          1.0892221037148573e-09, 8.35070279514724e-11, 5.9477940136376354e-12,
+                          3.9554295164585257e-13, 2.466827010264457e-14, 1.4483264643598138e-15,
+                          8.032735012415773e-17, 4.221407288807088e-18, 2.107855191442136e-19,
+                          1.0025164934907719e-20, 4.5518467589282e-22, 1.977064753877905e-23,
+                          8.230149299214221e-25, 3.289260349175752e-26, 1.2641078988989164e-27,
+                          4.6784835155184856e-29, 1.669761793417372e-30, 5.754191643982172e-32,
+                          1.9169428621097826e-33, 6.180307588222796e-35, 1.930357208815108e-36,
+                          5.846755007468836e-38, 1.7188560628017835e-39, 4.908923964523423e-41};
+    const double mx2 = -dmul(x, x);
+    double p = c[34];
+#pragma unroll
+    for (int n = 33; n >= 0; --n) p = dadd(dmul(p, mx2), c[n]);
+    return dmul(kTwoInvSqrtPi, dmul(x, p));
+}
+
+// erfc x for x >= 2: the Laplace continued fraction, depth 50.
+NF_HD double erfc_cf(double x) {
+    double f = x;
+    for (int k = 50; k >= 1; --k) f = dadd(x, ddiv(dmul((double)k, 0.5), f));
+    return ddiv(dmul(exp_d(-dmul(x, x)), kInvSqrtPi), f);
+}
+
+NF_HD double erf_d(double x) {
+    const double a = dabs(x);
+    const double v = a < kErfSplit ? erf_series(a) : dsub(1.0, erfc_cf(a));
+    return x < 0.0 ? -v : v;
+}
+
+// erfinv y, its magnitude capped at zmax (|y| >= 1 gives +-zmax).
+NF_HD double erfinv_d(double y, double zmax) {
+    const double a = dabs(y);
+    double x;
+    if (!(a < 1.0)) {
+        x = zmax;
+    } else {
+        if (a < 1e-3) {
+            x = dmul(kSqrtPiHalf, a);
+        } else {
+            const double L = log_d(dmul(dsub(1.0, a), dadd(1.0, a)));
+            const double A = 0.147;
+            const double B = dadd(ddiv(2.0, dmul(kPiD, A)), dmul(L, 0.5));
+            x = dsqrt(dsub(dsqrt(dsub(dmul(B, B), ddiv(L, A))), B));
+        }
+        for (int it = 0; it < 2; ++it) {
+            const double r = x < kErfSplit ? dsub(erf_series(x), a) : dsub(dsub(1.0, a), erfc_cf(x));
+            const double d = dmul(dmul(r, kSqrtPiHalf), exp_d(dmul(x, x)));
+            x = dsub(x, ddiv(d, dadd(1.0, dmul(x, d))));
+        }
+        if (x > zmax) x = zmax;
+    }
+    return y < 0.0 ? -x : x;
+}
+
+// One angle of the reference's law: med + c2 erfinv(c1 (2u - 1)), where
+// (c1, c2, zmax) = (erf z, s sqrt 2, z) with z = w / (s sqrt 2) for the exact
+// normal of deviation s truncated to med +- w, or (erf(z) / 2, 2 s sqrt 2,
+// inf) for the reference's own form a + 2 s sqrt2 erfinv(Fa (1 - 2u)),
+// Fa = erf(-z) / 2 (Fa (1 - 2u) = (erf(z) / 2)(2u - 1): erf is odd).
+NF_HD double tn_angle(float u, float med, double c1, double c2, double zmax) {
+    const double v = dmul(c1, dsub(dmul(2.0, (double)u), 1.0));
+    return dadd((double)med, dmul(c2, erfinv_d(v, zmax)));
+}
+
+// ---------------------------------------------------------------------------
 // Realisation descriptor: stream, density, grid, thresholds.
 // ---------------------------------------------------------------------------
 struct Real {
@@ -151,6 +286,11 @@ struct Real {
     int32_t orient, len_mode, rad_mode, rot;
     float kappa, E2;
     float m[9];
+    // the reference's truncated-normal angle law (DEF_THETA_*/DEF_PHI_*):
+    // bit 0 theta, bit 1 phi drawn by tn_angle with (c1, c2, zmax)
+    int32_t tn;
+    float tmed, pmed;
+    double tc1, tc2, tz, pc1, pc2, pz;
     float l, a, sigma, lmin, lmax, rmin, rmax;
     // density
     const float* mesh;
@@ -258,11 +398,20 @@ NF_HD void candidate(const Real& R, uint64_t k, float4* pos, float4* dir, float*
         float v = fadd(w, fmul(fsub(1.0f, w), E2));
         cz = fadd(1.0f, fdiv(log_nf(v), kappa));
         cz = cz < -1.0f ? -1.0f : (cz > 1.0f ? 1.0f : cz);
+    } else if (R.tn & 1) {  // genCosine: cos of a truncated-normal theta
+        const double th = tn_angle(uni(B.x), R.tmed, R.tc1, R.tc2, R.tz);
+        float st;
+        sincos_turns((float)dmul(th, kInv2PiD), &cz, &st);
     } else {
         cz = fsub(fmul(uni(B.x), 2.0f), 1.0f);
     }
     float cp, sp;
-    sincos_turns(uni(B.y), &cp, &sp);
+    if (R.tn & 2) {  // truncated-normal phi
+        const double ph = tn_angle(uni(B.y), R.pmed, R.pc1, R.pc2, R.pz);
+        sincos_turns((float)dmul(ph, kInv2PiD), &cp, &sp);
+    } else {
+        sincos_turns(uni(B.y), &cp, &sp);
+    }
     float sr = fsub(1.0f, fmul(cz, cz));
     float s = fsqrt(sr > 0.0f ? sr : 0.0f);
     float cx = fmul(s, cp), cy = fmul(s, sp);

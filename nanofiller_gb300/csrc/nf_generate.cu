@@ -75,6 +75,31 @@ double stage_reach(const nf_params& p) {
     return std::max(gen, con);
 }
 
+// The reference's angle law (genCosine / sym_truncNormal,
+// inc/cuda_CNTgenerate.h:262-275): theta (from the preferred axis) normal about
+// DEF_THETA_MED truncated to +- pi/2, phi about DEF_PHI_MED truncated to +- pi,
+// each only where its deviation is positive; the constants of tn_angle.
+void set_tn_law(Real& R, const nf_params& p) {
+    auto law = [&](float s, double w, double* c1, double* c2, double* zmax) {
+        const double sd = (double)s;
+        const double z = ddiv(ddiv(w, sd), kSqrt2);
+        if (p.ref_trunc_normal) {
+            *c1 = dmul(0.5, erf_d(z));
+            *c2 = dmul(dmul(2.0, sd), kSqrt2);
+            *zmax = 1e300;
+        } else {
+            *c1 = erf_d(z);
+            *c2 = dmul(sd, kSqrt2);
+            *zmax = z;
+        }
+    };
+    R.tn = (p.theta_dev > 0 ? 1 : 0) | (p.phi_dev > 0 ? 2 : 0);
+    R.tmed = p.theta_med;
+    R.pmed = p.phi_med;
+    if (R.tn & 1) law(p.theta_dev, dmul(kPiD, 0.5), &R.tc1, &R.tc2, &R.tz);
+    if (R.tn & 2) law(p.phi_dev, kPiD, &R.pc1, &R.pc2, &R.pz);
+}
+
 Real make_real(const nf_params& p, const float* dmesh, int mn[3], double reach) {
     Real R;
     std::memset(&R, 0, sizeof(R));
@@ -94,6 +119,7 @@ Real make_real(const nf_params& p, const float* dmesh, int mn[3], double reach) 
     R.m[0] = fmul(cM, cX);  R.m[1] = sM;   R.m[2] = fmul(-sX, cM);
     R.m[3] = fmul(-sM, cX); R.m[4] = cM;   R.m[5] = fmul(sX, sM);
     R.m[6] = sX;            R.m[7] = 0.0f; R.m[8] = cX;
+    set_tn_law(R, p);
     R.l = p.l;
     R.a = p.a;
     R.sigma = p.len_sigma_ln;

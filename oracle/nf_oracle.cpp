@@ -117,6 +117,109 @@ inline float expf_nf(float x) {
 }
 
 // ---------------------------------------------------------------------------
+// FP64 erf / erfinv of the truncated-normal angle law (sym_truncNormal,
+// inc/cuda_CNTgenerate.h:271-275), the product's operation sequence:
+// ln by the atanh series to s^27, e^x by Cody-Waite + degree-13 Taylor, erf by
+// its Maclaurin series below 2 and 1 - erfc (Laplace continued fraction, depth
+// 50) above, erfinv by Winitzki's start (2008, a = 0.147) + two Halley steps.
+// ---------------------------------------------------------------------------
+inline uint64_t dbits(double v) { uint64_t u; std::memcpy(&u, &v, 8); return u; }
+inline double bitsd(uint64_t u) { double v; std::memcpy(&v, &u, 8); return v; }
+constexpr double kLn2Hi = 0.6931471803691238, kLn2Lo = 1.9082149292705877e-10;
+constexpr double kInvLn2 = 1.4426950408889634, kSqrt2 = 1.4142135623730951;
+constexpr double kSqrtPiHalf = 0.886226925452758, kTwoInvSqrtPi = 1.1283791670955126;
+constexpr double kInvSqrtPi = 0.5641895835477563, kPiD = 3.141592653589793;
+constexpr double kInv2PiD = 0.15915494309189535;
+
+double log_d(double x) {
+    const uint64_t b = dbits(x);
+    int e = (int)((b >> 52) & 0x7ffu) - 1023;
+    double m = bitsd((b & 0x000fffffffffffffull) | 0x3ff0000000000000ull);
+    if (m > kSqrt2) { m = m * 0.5; e += 1; }
+    const double s = (m - 1.0) / (m + 1.0), s2 = s * s;
+    double p = 1.0 / 27;
+    for (int k = 25; k >= 3; k -= 2) p = p * s2 + 1.0 / k;
+    const double two_s = s + s;
+    const double lm = two_s + two_s * (s2 * p);
+    return (double)e * kLn2Hi + ((double)e * kLn2Lo + lm);
+}
+
+double exp_d(double x) {
+    static const double c[14] = {1.0, 1.0, 0.5, 0.16666666666666666, 0.041666666666666664, 0.008333333333333333,
+                                 0.001388888888888889, 0.0001984126984126984, 2.48015873015873e-05,
+                                 2.7557319223985893e-06, 2.755731922398589e-07, 2.505210838544172e-08,
+                                 2.08767569878681e-09, 1.6059043836821613e-10};
+    const double kf = std::floor(x * kInvLn2 + 0.5);
+    const double r = (x - kf * kLn2Hi) - kf * kLn2Lo;
+    double p = c[13];
+    for (int n = 12; n >= 0; --n) p = p * r + c[n];
+    int k = (int)kf;
+    if (k < -1022) k = -1022;
+    if (k > 1023) k = 1023;
+    return p * bitsd((uint64_t)(k + 1023) << 52);
+}
+
+double erf_series(double x) {
+    static const double c[35] = {1.0, 0.3333333333333333, 0.1, 0.023809523809523808, 0.004629629629629629,
+                                 0.0007575757575757576, 0.00010683760683760684, 1.3227513227513228e-05,
+                                 1.4589169000933706e-06, 1.4503852223150468e-07, 1.3122532963802806e-08,
+                                 1.0892221037148573e-09, 8.35070279514724e-11, 5.9477940136376354e-12,
+                                 3.9554295164585257e-13, 2.466827010264457e-14, 1.4483264643598138e-15,
+                                 8.032735012415773e-17, 4.221407288807088e-18, 2.107855191442136e-19,
+                                 1.0025164934907719e-20, 4.5518467589282e-22, 1.977064753877905e-23,
+                                 8.230149299214221e-25, 3.289260349175752e-26, 1.2641078988989164e-27,
+                                 4.6784835155184856e-29, 1.669761793417372e-30, 5.754191643982172e-32,
+                                 1.9169428621097826e-33, 6.180307588222796e-35, 1.930357208815108e-36,
+                                 5.846755007468836e-38, 1.7188560628017835e-39, 4.908923964523423e-41};
+    const double mx2 = -(x * x);
+    double p = c[34];
+    for (int n = 33; n >= 0; --n) p = p * mx2 + c[n];
+    return kTwoInvSqrtPi * (x * p);
+}
+
+double erfc_cf(double x) {
+    double f = x;
+    for (int k = 50; k >= 1; --k) f = x + ((double)k * 0.5) / f;
+    return (exp_d(-(x * x)) * kInvSqrtPi) / f;
+}
+
+double erf_d(double x) {
+    const double a = std::fabs(x);
+    const double v = a < 2.0 ? erf_series(a) : 1.0 - erfc_cf(a);
+    return x < 0.0 ? -v : v;
+}
+
+double erfinv_d(double y, double zmax) {
+    const double a = std::fabs(y);
+    double x;
+    if (!(a < 1.0)) {
+        x = zmax;
+    } else {
+        if (a < 1e-3) {
+            x = kSqrtPiHalf * a;
+        } else {
+            const double L = log_d((1.0 - a) * (1.0 + a));
+            const double A = 0.147;
+            const double B = 2.0 / (kPiD * A) + L * 0.5;
+            x = std::sqrt(std::sqrt(B * B - L / A) - B);
+        }
+        for (int it = 0; it < 2; ++it) {
+            const double r = x < 2.0 ? erf_series(x) - a : (1.0 - a) - erfc_cf(x);
+            const double d = (r * kSqrtPiHalf) * exp_d(x * x);
+            x = x - d / (1.0 + x * d);
+        }
+        if (x > zmax) x = zmax;
+    }
+    return y < 0.0 ? -x : x;
+}
+
+// med + c2 erfinv(c1 (2u - 1)): one angle of the reference's law.
+inline double tn_angle(float u, float med, double c1, double c2, double zmax) {
+    const double v = c1 * (2.0 * (double)u - 1.0);
+    return (double)med + c2 * erfinv_d(v, zmax);
+}
+
+// ---------------------------------------------------------------------------
 // Derived stream constants (computed identically by the product's host code).
 // ---------------------------------------------------------------------------
 struct Stream {
@@ -126,6 +229,10 @@ struct Stream {
     float kappa, E2;
     bool rot;
     float m[9];
+    // truncated-normal angle law: bit 0 theta, bit 1 phi
+    int tn = 0;
+    float tmed = 0, pmed = 0;
+    double tc1 = 0, tc2 = 0, tz = 0, pc1 = 0, pc2 = 0, pz = 0;
     float l, a, sigma, lmin, lmax, rmin, rmax;
     // density
     const float* mesh;
@@ -169,6 +276,23 @@ Stream make_stream(const nf_params* p, const float* mesh, int nx, int ny, int nz
     S.m[0] = cM * cX;  S.m[1] = sM;  S.m[2] = -sX * cM;
     S.m[3] = -sM * cX; S.m[4] = cM;  S.m[5] = sX * sM;
     S.m[6] = sX;       S.m[7] = 0.0f; S.m[8] = cX;
+    // genCosine / sym_truncNormal (inc/cuda_CNTgenerate.h:262-275): theta
+    // truncated to med +- pi/2, phi to med +- pi; exact normal by default,
+    // the reference's 2 s sqrt2 erfinv(Fa (1 - 2u)) form on request (Q2)
+    auto law = [&](float sdev, double w, double* c1, double* c2, double* zmax) {
+        const double sd = (double)sdev;
+        const double z = (w / sd) / kSqrt2;
+        if (p->ref_trunc_normal) {
+            *c1 = 0.5 * erf_d(z); *c2 = (2.0 * sd) * kSqrt2; *zmax = 1e300;
+        } else {
+            *c1 = erf_d(z); *c2 = sd * kSqrt2; *zmax = z;
+        }
+    };
+    S.tn = (p->theta_dev > 0 ? 1 : 0) | (p->phi_dev > 0 ? 2 : 0);
+    S.tmed = p->theta_med;
+    S.pmed = p->phi_med;
+    if (S.tn & 1) law(p->theta_dev, kPiD * 0.5, &S.tc1, &S.tc2, &S.tz);
+    if (S.tn & 2) law(p->phi_dev, kPiD, &S.pc1, &S.pc2, &S.pz);
     S.l = p->l; S.a = p->a;
     S.sigma = p->len_sigma_ln; S.lmin = p->len_min; S.lmax = p->len_max;
     S.rmin = p->rad_min; S.rmax = p->rad_max;
@@ -235,11 +359,20 @@ void candidate(const Stream& S, uint64_t k, float* o) {
         cz = 1.0f + logf_nf(v) / kappa;
         if (cz < -1.0f) cz = -1.0f;
         if (cz > 1.0f) cz = 1.0f;
+    } else if (S.tn & 1) {  // cos of a truncated-normal theta
+        const double th = tn_angle(uni(B[0]), S.tmed, S.tc1, S.tc2, S.tz);
+        float st;
+        sincos_turns((float)(th * kInv2PiD), &cz, &st);
     } else {
         cz = uni(B[0]) * 2.0f - 1.0f;
     }
     float cp, sp;
-    sincos_turns(uni(B[1]), &cp, &sp);
+    if (S.tn & 2) {  // truncated-normal phi
+        const double ph = tn_angle(uni(B[1]), S.pmed, S.pc1, S.pc2, S.pz);
+        sincos_turns((float)(ph * kInv2PiD), &cp, &sp);
+    } else {
+        sincos_turns(uni(B[1]), &cp, &sp);
+    }
     float sr = 1.0f - cz * cz;
     float s = std::sqrt(sr > 0.0f ? sr : 0.0f);
     float cx = s * cp, cy = s * sp;
@@ -687,6 +820,10 @@ void nfo_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t ou
     philox(ctr, key, out);
 }
 void nfo_sincos_turns(float t, float* c, float* s) { sincos_turns(t, c, s); }
+double nfo_erf(double x) { return erf_d(x); }
+double nfo_erfinv(double y, double zmax) { return erfinv_d(y, zmax); }
+double nfo_log_d(double x) { return log_d(x); }
+double nfo_exp_d(double x) { return exp_d(x); }
 float nfo_logf(float v) { return logf_nf(v); }
 float nfo_expf(float x) { return expf_nf(x); }
 

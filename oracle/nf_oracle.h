@@ -36,6 +36,10 @@ void nfo_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t ou
 
 /* Deterministic float math of the stream contract. */
 void nfo_sincos_turns(float t, float *c, float *s);
+double nfo_erf(double x);
+double nfo_erfinv(double y, double zmax);
+double nfo_log_d(double x);
+double nfo_exp_d(double x);
 float nfo_logf(float v);
 float nfo_expf(float x);
 

@@ -42,7 +42,7 @@ class NfParams(C.Structure):
         ("round_candidates", C.c_int32), ("solve_max_iter", C.c_int32), ("solve_tol", C.c_double),
         ("stencil_radius", C.c_int32), ("round_overshoot", C.c_float), ("two_phase_work", C.c_double),
         ("rod_sigma", C.c_double),
-        ("elec_buffer", C.c_int32), ("pad_end", C.c_int32),
+        ("elec_buffer", C.c_int32), ("ref_trunc_normal", C.c_int32),
         ("clust_dist", C.c_float), ("clust_angl", C.c_float), ("align_cell", C.c_float),
         ("align_min", C.c_int32), ("epoch_candidates", C.c_int64),
         ("solve_method", C.c_int32), ("pad_solve", C.c_int32),
@@ -100,6 +100,10 @@ def lib():
             L.nfo_sincos_turns.argtypes = [C.c_float, P(C.c_float), P(C.c_float)]
             L.nfo_logf.argtypes = [C.c_float]; L.nfo_logf.restype = C.c_float
             L.nfo_expf.argtypes = [C.c_float]; L.nfo_expf.restype = C.c_float
+            for nm in ("nfo_erf", "nfo_log_d", "nfo_exp_d"):
+                getattr(L, nm).argtypes = [C.c_double]
+                getattr(L, nm).restype = C.c_double
+            L.nfo_erfinv.argtypes = [C.c_double, C.c_double]; L.nfo_erfinv.restype = C.c_double
             L.nfo_pair_eval.argtypes = [C.c_int, C.c_int, C.c_void_p, C.c_void_p, P(C.c_double),
                                         C.c_double, C.c_double, C.c_double, C.c_int, P(C.c_double)]
             L.nfo_pair_eval.restype = C.c_int
@@ -151,6 +155,22 @@ def sincos_turns(t):
     c, s = C.c_float(), C.c_float()
     lib().nfo_sincos_turns(t, C.byref(c), C.byref(s))
     return c.value, s.value
+
+
+def erf(x):
+    return lib().nfo_erf(float(x))
+
+
+def erfinv(y, zmax=1e300):
+    return lib().nfo_erfinv(float(y), float(zmax))
+
+
+def log_d(x):
+    return lib().nfo_log_d(float(x))
+
+
+def exp_d(x):
+    return lib().nfo_exp_d(float(x))
 
 
 def candidates(params, k0, n, mesh=None):

@@ -50,3 +50,10 @@ def rods_struct(rods):
     for f in ("x", "y", "z", "cx", "cy", "cz", "l", "a"):
         out[f] = rods[f]
     return out
+
+
+@pytest.fixture(scope="session")
+def cfg():
+    """The workload presets (no library or device needed)."""
+    from nanofiller_gb300 import configs
+    return configs
