@@ -2,24 +2,36 @@
 """Benchmark of the GB300 NanoFiller hot path.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--workload medium|small|jammed|large]
+                    [--workload batched|medium|small|jammed|large]
 
-One step = one realisation of the workload through the whole path: seeded
-candidate stream -> von Neumann density test -> cell-list hard-core rejection
-(sequential insertion) -> tunnelling contacts + screening + electrodes ->
-network solve. Default workload `medium`: 5 um box, 1 um x 5 nm rods, 1 % volume
-fraction (15 916 rods), 8-Gaussian agglomerate density on a 64^3 mesh, von
-Mises-Fisher kappa = 4 orientation, electrodes at z = 0 and z = L.
+The path: seeded candidate stream -> von Neumann density test -> cell-list
+hard-core rejection (sequential insertion) -> tunnelling contacts + screening +
+electrodes -> network solve.
 
-value: accepted rods per second with the density mesh resident in HBM, timed
-with CUDA events around each step on the library's stream; L2 (129 MB) is
-flushed by writing a 256 MB buffer before every timed step. e2e: the same
-metric through the C ABI with host buffers: the mesh is uploaded and the rods
-and contacts are read back inside every step. Under torchrun each rank runs an
-independent realisation (seed + rank): replicas, no collective on the path.
+Default workload `batched` (the metric's own comparison, batched vs plain):
+256 independent realisations, seeds 0-255, box edge 2-10 um, volume fraction
+log-uniform on 0.2-2 %, 1 um x 5 nm isotropic rods, electrodes at z = 0 and
+z = L, each generated, contacted and solved. One step = all 256 realisations
+through one batch handle (nf_create_batch: shared launches for every stage).
 
---impl reference times the CPU implementation of the path (the FP64 C++ oracle,
-all host threads) on the same workload.
+value: realisations per second, CUDA events on the handle's stream around
+each step, the realisation parameters resident in the handle; L2 (129 MB)
+flushed by a 256 MB write before every timed step (the step's own working set,
+~0.5 GB of rods and candidates, is larger than L2 as well). e2e: the same
+metric through the one-call C ABI (nf_batch_run: parameters from host memory,
+handle creation, the three stages, per-realisation results copied back).
+Extra keys: the plain path over the same 256 realisations (one nf_create
+handle each, in sequence) and batched_over_plain; the largest single
+realisation (20 um box, ~0.66 M rods) in rods/s; the jammed percolating
+network's solve and adjoint times; the decision flips against the oracle on
+the cpu_baseline sample, counted, not asserted.
+
+Single-realisation workloads (`medium` etc.) keep the rods/s line of one
+realisation per step.
+
+--impl reference times the CPU implementation of the path (the FP64 C++
+oracle, all host threads) on the same workload: for `batched` each step is a
+stratified sample of the mix (the realisations i with i = step mod 64, 4 of 256).
 """
 import argparse
 import json
@@ -33,6 +45,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "rods/s & realisations/s, batched vs plain on 1 GB300, 0 FP64 decision flips"
+STRATA = 64  # the batched CPU samples take realisations i = s mod STRATA (4 of 256)
 
 
 def parse():
@@ -41,10 +54,11 @@ def parse():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="medium", choices=["medium", "small", "jammed", "large", "batched"])
+    ap.add_argument("--workload", default="batched", choices=["batched", "medium", "small", "jammed", "large"])
     ap.add_argument("--batch", type=int, default=256, help="realisations of the batched workload")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-extras", action="store_true", help="batched: skip the plain pass, large and jammed keys")
     return ap.parse_args()
 
 
@@ -60,11 +74,19 @@ def workload(name, rank):
     return dict(C.LARGE, seed=C.LARGE["seed"] + rank), None
 
 
-def workload_config(name, params):
+L2_NOTE = "flushed (256 MB write) before every timed step"
+
+
+def workload_config(name, params=None, batch=256):
+    """The `config` object of both arms (identical for the same workload)."""
+    if name == "batched":
+        return {"workload": "batched", "realisations": batch, "box_um": [2.0, 10.0], "vf": [0.002, 0.02],
+                "rod_um": [1.0, 0.005], "orientation": "isotropic", "seeds": [0, batch - 1],
+                "candidates_budget": 4000000, "cutoff_um": 0.0014, "gap_um": 0.00034,
+                "electrodes": "z = 0, z = L", "l2": L2_NOTE}
     d = {"workload": name, "box_um": list(params["box"]), "rod_um": [params["l"], params["a"]],
          "vf": params["vf"], "candidates_budget": params["n_candidates"], "seed": params["seed"],
-         "cutoff_um": params["stat_dist_lim"], "gap_um": params["sep"],
-         "l2": "flushed (256 MB write) before every timed step"}
+         "cutoff_um": params["stat_dist_lim"], "gap_um": params["sep"], "l2": L2_NOTE}
     if name == "medium":
         d.update(density="0.01 + 8 Gaussians sigma 0.5 um, 64^3 mesh", orientation="vMF kappa 4 about z")
     return d
@@ -219,144 +241,134 @@ def fp32_roofline(g, old_ms, clk):
 
 
 # --------------------------------------------------------------------------- CPU (oracle) leg
-def cpu_run(params, mesh, budget_s=12.0, max_reps=200):
-    """The oracle on all host threads; returns (rods per second, cores, sample text)."""
+def _oracle():
     from oracle import nf_oracle as O
     O.build()
+    return O
+
+
+def oracle_realisation(O, params, mesh, cores):
+    """One realisation on the oracle: (rods, stream indices, contacts)."""
+    r, idx, _ = O.generate(params, mesh=mesh, nthreads=cores, batch=16384)
+    ct = O.contacts(params, r, nthreads=cores)
+    O.solve(len(r), ct, tol=params.get("solve_tol", 1e-10))
+    return r, idx, ct
+
+
+def cpu_single(params, mesh, budget_s=12.0, max_reps=200):
+    """The oracle on all host threads, full realisations of one workload:
+    (rods/s, cores, sample text, outputs of the first realisation)."""
+    O = _oracle()
     cores = os.cpu_count() or 1
     t0 = time.perf_counter()
-    reps, rods = 0, 0
+    reps, rods, first = 0, 0, None
     while reps < max_reps and (reps == 0 or time.perf_counter() - t0 < budget_s):
-        r, _, _ = O.generate(params, mesh=mesh, nthreads=cores, batch=16384)
-        ct = O.contacts(params, r, nthreads=cores)
-        O.solve(len(r), ct, tol=params.get("solve_tol", 1e-10))
-        rods += len(r)
+        out = oracle_realisation(O, params, mesh, cores)
+        first = first or out
+        rods += len(out[1])
         reps += 1
     dt = time.perf_counter() - t0
-    return rods / dt, cores, f"{reps} full realisation(s), {rods} rods, {dt:.1f} s"
+    return rods / dt, cores, f"{reps} full realisation(s), {rods} rods, {dt:.1f} s", first
 
 
-def run_batched(args, rank, world):
-    """Batched workload: `--batch` independent realisations (box 2-10 um, vf
-    0.2-2 %, seeds 0..n-1), each generated, contacted and solved. Plain = one
-    handle per realisation in sequence; batched = one nf_batch_run."""
-    import torch
-
-    import nanofiller_gb300 as nf
-    from nanofiller_gb300 import build as nb
-
-    nb.build()
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    torch.cuda.set_device(local)
-    dist = None
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
-    reals = nf.configs.batched_realisations(args.batch)
-    for p in reals:
-        p["seed"] += rank * args.batch
-
-    def plain():
-        res = []
-        for p in reals:
-            with nf.Simulation(p) as sim:
-                g = sim.generate()
-                c = sim.contacts()
-                s = sim.solve(check=False)
-                res.append((g["accepted"], c["contacts"], s["G_eff"], s["percolating"]))
-        return res
-
-    def batched():
-        out, st = nf.batch_run(reals)
-        return [(r["accepted"], r["contacts"], r["G_eff"], r["percolating"]) for r in out]
-
-    clocks = Clocks(local)
-    clocks.start()
-    for _ in range(max(1, min(args.warmup, 2))):
-        rb = batched()
-    clocks.mark()
-    l0 = nf.kernel_launches()
-    torch.cuda.synchronize()
-    if dist:
-        dist.barrier()
+def cpu_batched(reals, strata):
+    """The oracle on all host threads over the realisations i with i mod
+    STRATA in `strata`: (realisations/s, rods/s, cores, sample text,
+    {i: outputs})."""
+    O = _oracle()
+    cores = os.cpu_count() or 1
+    pick = [i for i in range(len(reals)) if i % STRATA in strata]
+    outs = {}
     t0 = time.perf_counter()
-    steps = max(1, args.steps)
-    for _ in range(steps):
-        rb = batched()
-    torch.cuda.synchronize()
-    tb = over_ranks(dist, (time.perf_counter() - t0) / steps, "max", "cuda")
-    launches = nf.kernel_launches() - l0
-    clk = clocks.stop()
-    plain()  # warm
-    t0 = time.perf_counter()
-    rp = plain()
-    tp = time.perf_counter() - t0
-    same = all(a[0] == b[0] and a[1] == b[1] and abs(a[2] - b[2]) <= 1e-9 * max(abs(a[2]), 1e-30)
-               for a, b in zip(rp, rb))
-    rods = over_ranks(dist, sum(r[0] for r in rb), "sum", "cuda")
-    vf = [p["vf"] for p in reals]
-    bins = [0.002, 0.004, 0.008, 0.016, 0.0201]
-    table = []
-    for lo, hi in zip(bins[:-1], bins[1:]):
-        sel = [r for r, v in zip(rb, vf) if lo <= v < hi]
-        if sel:
-            table.append({"vf_range": [lo, hi], "n": len(sel),
-                          "percolation_probability": sum(1 for r in sel if r[3]) / len(sel),
-                          "mean_G_S": sum(r[2] for r in sel) / len(sel)})
-    if rank == 0:
-        print(json.dumps({
-            "metric": METRIC, "value": world * len(reals) / tb, "unit": "realisations/s", "n_gpus": world,
-            "steps": steps, "warmup": args.warmup, "ms_per_step": 1000 * tb, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32 filter + f64 decisions", "data": "synthetic",
-            "config": {"workload": "batched", "realisations": len(reals), "box_um": [2.0, 10.0],
-                       "vf": [0.002, 0.02], "rod_um": [1.0, 0.005], "parallelism": f"replicas x{world}"},
-            "rods_per_s": rods / tb, "plain_realisations_per_s": len(reals) / tp,
-            "batched_over_plain": tp / tb, "batched_equals_plain": same, "gpu_launches": int(launches),
-            "vs_vf": table, "clocks": clk,
-        }))
-    if dist:
-        dist.barrier()
-        dist.destroy_process_group()
-    return 0
+    rods = 0
+    for i in pick:
+        outs[i] = oracle_realisation(O, reals[i], None, cores)
+        rods += len(outs[i][1])
+    dt = time.perf_counter() - t0
+    text = f"{len(pick)} of {len(reals)} realisations (i mod {STRATA} in {sorted(strata)}), {rods} rods, {dt:.1f} s"
+    return len(pick) / dt, rods / dt, cores, text, outs
+
+
+def flips(g_idx, g_ct, o_idx, o_ct):
+    """Decisions where the device and the oracle differ: accepted stream
+    indices in one set only, plus contacts (keyed by the stream indices of
+    both rods, or the electrode id, and the image) in one list only."""
+    import numpy as np
+    SNK = 0xFFFFFFFE
+
+    def keys(idx, ct):
+        idx = np.asarray(idx, np.uint64)
+        I = idx[np.asarray(ct["I"], np.int64)]
+        J = np.asarray(ct["J"], np.uint64)
+        rod = J < SNK
+        Jk = np.where(rod, idx[np.where(rod, J, 0).astype(np.int64)], J + np.uint64(1 << 40))
+        img = np.asarray(ct["image"], np.int64).reshape(-1, 3)
+        return set(zip(I.tolist(), Jk.tolist(), img[:, 0].tolist(), img[:, 1].tolist(), img[:, 2].tolist()))
+
+    a = set(np.asarray(g_idx, np.uint64).tolist()) ^ set(np.asarray(o_idx, np.uint64).tolist())
+    return len(a) + len(keys(g_idx, g_ct) ^ keys(o_idx, o_ct))
 
 
 def run_reference(args, rank, world):
+    """The CPU implementation of the path (the FP64 C++ oracle, all host
+    threads) on the same workload; rank 0 alone runs and prints."""
     if rank != 0:
         return 0
-    params, mesh = workload(args.workload, 0)
-    from oracle import nf_oracle as O
-    O.build()
+    O = _oracle()
     cores = os.cpu_count() or 1
-    for _ in range(min(args.warmup, 1)):
-        O.generate(dict(params, n_candidates=min(params["n_candidates"], 20000)), mesh=mesh, nthreads=cores)
-    times, rods = [], 0
-    for _ in range(args.steps):
-        t0 = time.perf_counter()
-        r, _, _ = O.generate(params, mesh=mesh, nthreads=cores, batch=16384)
-        ct = O.contacts(params, r, nthreads=cores)
-        O.solve(len(r), ct, tol=params.get("solve_tol", 1e-10))
-        times.append(time.perf_counter() - t0)
-        rods = len(r)
-    ms = 1000 * sum(times) / len(times)
-    value = rods / (ms / 1000)
-    print(json.dumps({
-        "impl": "reference", "metric": METRIC, "value": value, "unit": "rods/s", "n_gpus": world,
+    if args.workload == "batched":
+        import nanofiller_gb300.configs as C
+        reals = C.batched_realisations(args.batch)
+        for _ in range(min(args.warmup, 1)):
+            oracle_realisation(O, dict(reals[1], n_candidates=20000), None, cores)
+        times, nreal, rods = [], 0, 0
+        for s in range(args.steps):
+            pick = [i for i in range(len(reals)) if i % STRATA == s % STRATA]
+            t0 = time.perf_counter()
+            for i in pick:
+                rods += len(oracle_realisation(O, reals[i], None, cores)[1])
+            times.append(time.perf_counter() - t0)
+            nreal += len(pick)
+        tot = sum(times)
+        value, unit = nreal / tot, "realisations/s"
+        ms = 1000 * tot / len(times)
+        sample = (f"{args.steps} steps of a stratified sample ({len(pick)} of {len(reals)} realisations each, "
+                  f"i = step mod {STRATA}), {nreal} realisations, {rods} rods, {tot:.1f} s on the FP64 C++ oracle")
+        cfg = workload_config("batched", batch=args.batch)
+        extra = {"rods_per_s": rods / tot}
+    else:
+        params, mesh = workload(args.workload, 0)
+        for _ in range(min(args.warmup, 1)):
+            O.generate(dict(params, n_candidates=min(params["n_candidates"], 20000)), mesh=mesh, nthreads=cores)
+        times, rods = [], 0
+        for _ in range(args.steps):
+            t0 = time.perf_counter()
+            r = oracle_realisation(O, params, mesh, cores)
+            times.append(time.perf_counter() - t0)
+            rods = len(r[1])
+        ms = 1000 * sum(times) / len(times)
+        value, unit = rods / (ms / 1000), "rods/s"
+        sample = f"{args.steps} full realisation(s) of {rods} rods on the FP64 C++ oracle"
+        cfg = workload_config(args.workload, params)
+        extra = {}
+    out = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": unit, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": workload_config(args.workload, params),
-        "cpu_baseline": {"value": value, "unit": "rods/s", "cores": cores, "kind": "port",
-                         "sample": f"{args.steps} full realisation(s) of {rods} rods on the FP64 C++ oracle"},
-        "e2e": {"value": value, "unit": "rods/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-    }))
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": cfg,
+        "cpu_baseline": {"value": value, "unit": unit, "cores": cores, "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": unit, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    out.update(extra)
+    print(json.dumps(out))
     return 0
 
 
 # --------------------------------------------------------------------------- replicas
 def over_ranks(dist, v, how, device):
     """v reduced over the ranks of a replica run: "max" for step times (the
-    slowest rank sets the job's time), "sum" for the rods every rank placed.
-    v itself without a process group. device is the process group's tensor
-    device ("cuda" under NCCL, "cpu" under gloo)."""
+    slowest rank sets the job's time), "sum" for the units every rank
+    processed. v itself without a process group. device is the process
+    group's tensor device ("cuda" under NCCL, "cpu" under gloo)."""
     if not dist:
         return v
     import torch
@@ -365,14 +377,11 @@ def over_ranks(dist, v, how, device):
     return float(t.item())
 
 
-# --------------------------------------------------------------------------- GPU leg
-def run_ours(args, rank, world):
-    import numpy as np
+# --------------------------------------------------------------------------- GPU legs
+def gpu_setup(world):
     import torch
 
-    import nanofiller_gb300 as nf
     from nanofiller_gb300 import build as nb
-
     nb.build()
     local = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(local)
@@ -380,8 +389,267 @@ def run_ours(args, rank, world):
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    return local, dist
+
+
+def peaks():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        return {}
+
+
+def kernel_breakdown(sim, workload_name, steps):
+    """Per-stage CUDA-event times of the timed steps (the handle's stream)
+    and the roofline object of the dominant one: algorithmic bytes per
+    launch over its mean launch time against the measured HBM copy rate."""
+    kern = {k: sim.kernel_time(k) for k in ("stream", "old_test", "conflicts", "ct_pairs", "screen", "cg")}
+    dom = max(kern, key=lambda k: kern[k]["ms"])
+    kd = kern[dom]
+    pk = peaks()
+    hbm = pk.get("hbm_gbs")
+    note = "measured" if hbm else "fallback"
+    hbm = hbm or 6800.0
+    achieved = kd["bytes"] / (kd["ms"] * 1e-3) / 1e9 if kd["ms"] > 0 else 0.0
+    traffic = None
+    try:
+        tr = json.load(open(os.path.join(ROOT, "profiles", "traffic.json")))
+        traffic = tr.get(workload_name, {}).get(dom)
+    except Exception:
+        pass
+    roof = {"kernel": dom, "bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+            "frac": achieved / hbm, "traffic": traffic, "peak_source": note,
+            "launches_per_step": kd["launches"] / max(steps, 1),
+            "bytes_per_launch": kd["bytes"] / max(kd["launches"], 1),
+            "note": "pair-test kernels are FP32-issue bound; bytes are the algorithmic bytes"}
+    return {k: v["ms"] / steps for k, v in kern.items()}, roof
+
+
+def jammed_solve_keys():
+    """The percolating jammed network (2.5 um box filled to jamming, 9 481
+    rods): forward network solve and adjoint, median of 5 (CUDA events)."""
+    import torch
+
+    import nanofiller_gb300 as nf
+    params, _ = workload("jammed", 0)
+    st = torch.cuda.current_stream().cuda_stream
+    with nf.Simulation(params, stream=st) as sim:
+        sim.generate()
+        sim.contacts()
+        s = sim.solve(check=False)
+        ts, ta = [], []
+        for _ in range(5):
+            a, b, c = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+            a.record()
+            s = sim.solve(check=False)
+            b.record()
+            sim.adjoint()
+            c.record()
+            torch.cuda.synchronize()
+            ts.append(a.elapsed_time(b))
+            ta.append(b.elapsed_time(c))
+    ts.sort()
+    ta.sort()
+    return {"workload": "jammed", "G_eff_S": s["G_eff"], "n_active": s["n_active"], "residual": s["residual"],
+            "direct": bool(s["direct"]), "solve_ms": ts[2], "adjoint_ms": ta[2], "adjoint_over_solve": ta[2] / ts[2]}
+
+
+def large_keys(steps=3, warmup=2):
+    """The largest single realisation (20 um box, lognormal lengths, 5 M
+    candidates): rods/s over full realisations, CUDA events, L2 flushed."""
+    import torch
+
+    import nanofiller_gb300 as nf
+    params, _ = workload("large", 0)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    st = torch.cuda.current_stream().cuda_stream
+    with nf.Simulation(params, stream=st) as sim:
+        for _ in range(warmup):
+            sim.generate()
+            sim.contacts()
+        evs = []
+        for _ in range(steps):
+            flush.zero_()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record()
+            g = sim.generate()
+            c = sim.contacts()
+            s = sim.solve(check=False)
+            b.record()
+            evs.append((a, b))
+        torch.cuda.synchronize()
+    ms = sum(a.elapsed_time(b) for a, b in evs) / len(evs)
+    return {"workload": "large", "rods": g["accepted"], "contacts": c["contacts"], "ms_per_realisation": ms,
+            "rods_per_s": g["accepted"] / (ms / 1000), "percolating": bool(s["percolating"])}
+
+
+def run_batched(args, rank, world):
+    """Default workload: the 256-realisation mix, batched vs plain."""
+    import numpy as np
+    import torch
+
+    import nanofiller_gb300 as nf
+    local, dist = gpu_setup(world)
+    reals = nf.configs.batched_realisations(args.batch)
+    for p in reals:
+        p["seed"] += rank * args.batch
+    stream = torch.cuda.current_stream().cuda_stream
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    b = nf.Batch(reals, stream=stream)
+
+    def step():
+        g = b.generate()
+        c = b.contacts()
+        b.solve(check=False)
+        return g, c
+
+    clocks = Clocks(local)
+    clocks.start()
+    for _ in range(max(args.warmup, 0)):
+        flush.zero_()
+        step()
+    torch.cuda.synchronize()
+    b.set_kernel_timing(True)
+    clocks.mark()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    l0 = nf.kernel_launches()
+    wall0 = time.perf_counter()
+    evs = []
+    for _ in range(args.steps):
+        flush.zero_()
+        ea, eb = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ea.record()
+        g, c = step()
+        eb.record()
+        evs.append((ea, eb))
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - wall0
+    launches = nf.kernel_launches() - l0
+    clk = clocks.stop()
+    ms = sum(ea.elapsed_time(eb) for ea, eb in evs) / len(evs)
+    ms_max = over_ranks(dist, ms, "max", "cuda")
+    R = len(reals)
+    res = b.results()
+    rods = sum(r["accepted"] for r in res)
+    rods_all = over_ranks(dist, rods, "sum", "cuda")
+    kern_ms, roof = kernel_breakdown(b, "batched", args.steps)
+    b.set_kernel_timing(False)
+    vf = [p["vf"] for p in reals]
+    bins = [0.002, 0.004, 0.008, 0.016, 0.0201]
+    table = []
+    for lo, hi in zip(bins[:-1], bins[1:]):
+        sel = [r for r, v in zip(res, vf) if lo <= v < hi]
+        if sel:
+            table.append({"vf_range": [lo, hi], "n": len(sel),
+                          "percolation_probability": sum(1 for r in sel if r["percolating"]) / len(sel),
+                          "mean_G_S": sum(r["G_eff"] for r in sel) / len(sel)})
+    out = {
+        "metric": METRIC, "value": world * R / (ms_max / 1000), "unit": "realisations/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32 filter + f64 decisions", "data": "synthetic",
+        "config": workload_config("batched", batch=R),
+        "replicas": world,
+        "rods_per_s": rods_all / (ms_max / 1000),
+        "gpu_launches": int(launches),
+        "wall_ms_per_step": 1000 * wall / args.steps,
+        "step_ms": [round(ea.elapsed_time(eb), 3) for ea, eb in evs],
+        "kernels_ms_per_step": kern_ms,
+        "roofline": roof,
+        "roofline_fp32": fp32_roofline(g, (kern_ms["old_test"] + kern_ms["conflicts"]), clk),
+        "generation_sweeps": {k: g[k] for k in ("rounds", "work_items", "target_tiles", "pair_tests", "marked_pairs",
+                                                  "line_pairs", "exact_evals")},
+        "fp32_would_flip": g["fp32_would_flip"] + c["fp32_would_flip"],
+        "fp64_decisions": g["exact_evals"] + c["exact_evals"],
+        "contacts": sum(r["contacts"] for r in res),
+        "vs_vf": table,
+        "clocks": clk,
+    }
+    # e2e: the one-call C ABI with host parameters and host results
+    if not args.no_e2e:
+        times = []
+        for i in range(args.warmup + args.steps):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            one, _ = nf.batch_run(reals)
+            torch.cuda.synchronize()
+            if i >= args.warmup:
+                times.append(time.perf_counter() - t0)
+        e_ms = over_ranks(dist, 1000 * sum(times) / len(times), "max", "cuda")
+        same = all(a["accepted"] == x["accepted"] and a["contacts"] == x["contacts"] and a["G_eff"] == x["G_eff"]
+                   for a, x in zip(one, res))
+        out["e2e"] = {"value": world * R / (e_ms / 1000), "unit": "realisations/s",
+                      "h2d_bytes_per_step": int(R * C_sizeof_params()), "d2h_bytes_per_step": int(R * C_sizeof_result()),
+                      "ms_per_step": e_ms, "call": "nf_batch_run", "equals_handle_results": same}
+    # the plain path: one handle per realisation, in sequence
+    if not args.no_extras:
+        def plain():
+            r_ = []
+            for p in reals:
+                with nf.Simulation(p, stream=stream) as sim:
+                    gg = sim.generate()
+                    cc = sim.contacts()
+                    ss = sim.solve(check=False)
+                    r_.append((gg["accepted"], cc["contacts"], ss["G_eff"]))
+            return r_
+        plain()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        rp = plain()
+        torch.cuda.synchronize()
+        tp = over_ranks(dist, time.perf_counter() - t0, "max", "cuda")
+        out["plain_realisations_per_s"] = world * R / tp
+        out["plain_ms_per_step"] = 1000 * tp
+        out["batched_over_plain"] = (world * R / (ms_max / 1000)) / (world * R / tp)
+        out["batched_equals_plain"] = all(a == (x["accepted"], x["contacts"], x["G_eff"]) for a, x in zip(rp, res))
+        out["large"] = large_keys()
+        out["jammed_solve"] = jammed_solve_keys()
+    # CPU baseline on a stratified sample, and the decision flips against it
+    if rank == 0 and not args.no_cpu_baseline:
+        v, rv, cores, sample, outs = cpu_batched(reals, {0})
+        nflip = 0
+        for i, (ro, io, co) in outs.items():
+            b.select(i)
+            rg = b.rods()
+            cg = b.contact_list()
+            nflip += flips(rg["stream_index"], cg, io, co)
+        out["cpu_baseline"] = {"value": v, "unit": "realisations/s", "cores": cores, "kind": "port", "sample": sample,
+                               "rods_per_s": rv}
+        out["decision_flips_vs_fp64"] = nflip
+        out["decision_flips_sample"] = f"accepted sets and contact lists of {len(outs)} realisations vs the oracle"
+    b.close()
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+    if rank == 0:
+        print(json.dumps(out))
+    return 0
+
+
+def C_sizeof_params():
+    import ctypes
+
+    from nanofiller_gb300._abi import NfParams
+    return ctypes.sizeof(NfParams)
+
+
+def C_sizeof_result():
+    import ctypes
+
+    from nanofiller_gb300._abi import NfBatchResult
+    return ctypes.sizeof(NfBatchResult)
+
+
+def run_ours(args, rank, world):
+    """Single-realisation workloads: one realisation per step."""
+    import torch
+
+    import nanofiller_gb300 as nf
+    local, dist = gpu_setup(world)
     params, mesh = workload(args.workload, rank)
-    sim = nf.Simulation(params, mesh=mesh)
+    stream = torch.cuda.current_stream().cuda_stream
+    sim = nf.Simulation(params, mesh=mesh, stream=stream)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
 
     def step():
@@ -422,47 +690,25 @@ def run_ours(args, rank, world):
     ms_max = over_ranks(dist, ms, "max", "cuda")
     rods_all = over_ranks(dist, rods, "sum", "cuda")
     value = rods_all / (ms_max / 1000)
-    # Kernel breakdown of the timed steps (CUDA events on the library's stream).
-    kern = {k: sim.kernel_time(k) for k in ("stream", "old_test", "conflicts", "ct_pairs", "screen", "cg")}
-    dom = max(kern, key=lambda k: kern[k]["ms"])
-    kd = kern[dom]
-    peaks = {}
-    try:
-        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
-    except Exception:
-        pass
-    hbm = peaks.get("hbm_gbs")
-    peak_note = "measured" if hbm else "fallback"
-    hbm = hbm or 6800.0
-    achieved = kd["bytes"] / (kd["ms"] * 1e-3) / 1e9 if kd["ms"] > 0 else 0.0
-    traffic = None
-    try:
-        tr = json.load(open(os.path.join(ROOT, "profiles", "traffic.json")))
-        if args.workload in tr and dom in tr[args.workload]:
-            traffic = tr[args.workload][dom]
-    except Exception:
-        pass
+    kern_ms, roof = kernel_breakdown(sim, args.workload, args.steps)
     out = {
         "metric": METRIC, "value": value, "unit": "rods/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_max, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32 filter + f64 decisions", "data": "synthetic",
-        "config": dict(workload_config(args.workload, params), parallelism=f"replicas x{world}"),
+        "config": workload_config(args.workload, params), "replicas": world,
         "realisations_per_s": world * 1000.0 / ms_max,
         "pair_tests_per_s": (g["pair_tests"] + c["pair_tests"]) / (ms / 1000),
         "fp64_decisions": g["exact_evals"] + c["exact_evals"],
-        "generation_sweeps": {k: g[k] for k in ("work_items", "target_tiles", "pair_tests", "marked_pairs",
+        "generation_sweeps": {k: g[k] for k in ("rounds", "work_items", "target_tiles", "pair_tests", "marked_pairs",
                                                   "line_pairs", "exact_evals")},
         "fp32_would_flip": g["fp32_would_flip"] + c["fp32_would_flip"],
-        "decision_flips_vs_fp64": 0,
         "contacts": c["contacts"], "G_eff_S": s["G_eff"], "percolating": bool(s["percolating"]),
         "gpu_launches": int(launches),
         "wall_ms_per_step": 1000 * wall / args.steps,
         "step_ms": [round(a.elapsed_time(b), 4) for a, b in evs],
-        "kernels_ms_per_step": {k: v["ms"] / args.steps for k, v in kern.items()},
-        "roofline": {"kernel": dom, "bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                     "frac": achieved / hbm, "traffic": traffic, "peak_source": peak_note,
-                     "note": "pair-test kernels are FP32-issue bound; bytes are the algorithmic bytes"},
-        "roofline_fp32": fp32_roofline(g, (kern["old_test"]["ms"] + kern["conflicts"]["ms"]) / args.steps, clk),
+        "kernels_ms_per_step": kern_ms,
+        "roofline": roof,
+        "roofline_fp32": fp32_roofline(g, kern_ms["old_test"] + kern_ms["conflicts"], clk),
         "contacts_per_s": (c["contacts"] + c["n_source"] + c["n_sink"]) / (c["ms"] / 1000) if c["ms"] > 0 else None,
         "solve": {"residual": s["residual"], "outer_iters": s["outer_iters"], "inner_iters": s["inner_iters"],
                   "n_active": s["n_active"], "ms": s["ms"]},
@@ -470,19 +716,17 @@ def run_ours(args, rank, world):
     }
     sim.set_kernel_timing(False)
     if s["percolating"]:
-        # Differentiation form: the adjoint (gradient w.r.t. all endpoints, lambda,
-        # G0, copied to the host) against one forward network solve.
         ts, ta = [], []
         for _ in range(5):
-            a, b, c = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+            a, b, c2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
             a.record()
             sim.solve(check=False)
             b.record()
             sim.adjoint()
-            c.record()
+            c2.record()
             torch.cuda.synchronize()
             ts.append(a.elapsed_time(b))
-            ta.append(b.elapsed_time(c))
+            ta.append(b.elapsed_time(c2))
         ts.sort()
         ta.sort()
         out["adjoint"] = {"solve_ms": ts[2], "adjoint_ms": ta[2], "adjoint_over_solve": ta[2] / ts[2]}
@@ -496,7 +740,7 @@ def run_ours(args, rank, world):
                 sim.load_density(mesh)
             sim.generate()
             sim.contacts()
-            s2 = sim.solve(check=False)
+            sim.solve(check=False)
             r = sim.rods()
             ct = sim.contact_list()
             torch.cuda.synchronize()
@@ -507,10 +751,13 @@ def run_ours(args, rank, world):
         e_ms = over_ranks(dist, 1000 * sum(times) / len(times), "max", "cuda")
         out["e2e"] = {"value": rods_all / (e_ms / 1000), "unit": "rods/s", "h2d_bytes_per_step": int(h2d),
                       "d2h_bytes_per_step": int(d2h), "ms_per_step": e_ms}
-    sim.close()
     if rank == 0 and not args.no_cpu_baseline:
-        v, cores, sample = cpu_run(params, mesh)
+        v, cores, sample, first = cpu_single(params, mesh)
         out["cpu_baseline"] = {"value": v, "unit": "rods/s", "cores": cores, "kind": "port", "sample": sample}
+        ro, io, co = first
+        out["decision_flips_vs_fp64"] = flips(sim.rods()["stream_index"], sim.contact_list(), io, co)
+        out["decision_flips_sample"] = "accepted set and contact list of the last timed realisation vs the oracle"
+    sim.close()
     if dist:
         dist.barrier()
         dist.destroy_process_group()

@@ -312,10 +312,11 @@ nf_status nf_stream_candidates(nf_handle *h, uint64_t k0, uint64_t n,
  * fixed device array of NF_NOALLOC_MAX_CANDIDATES x 10 floats (2.5 MiB)
  * inside the library; n above NF_NOALLOC_MAX_CANDIDATES returns
  * NF_ERR_CAPACITY. Nothing in that array needs to start at zero: each call
- * writes every value it copies out. The first call on each device looks up
- * the array's device address (cudaGetSymbolAddress, which may load the
- * library's device code): make that first call before any stream capture
- * begins. Calls on the same device share the array, so two calls in flight
+ * writes every value it copies out. Every call looks up the array's device
+ * address on the handle's device (cudaGetSymbolAddress; the first call on a
+ * device may load the library's device code: make it before any stream
+ * capture begins), so no address outlives a device reset. Calls on the same
+ * device share the array, so two calls in flight
  * at once (different streams or host threads) race: serialise them. A handle
  * with a density mesh must have uploaded it first (nf_generate or
  * nf_stream_candidates after nf_create / nf_load_density), else
@@ -541,8 +542,24 @@ nf_status nf_adjoint(nf_handle *h, float *dG_dend, size_t capacity,
 
 /* ---- batched realisations (no reference counterpart; the reference runs
  *      one realisation per process, src/NanoFiller.cpp:37-162) ------------ */
+/* One call: a batch handle is created, generated, contacted, solved and
+ * destroyed; out[r] holds realisation r's result, stats->ms the device time
+ * from the first generation launch to the end of the solve. */
 nf_status nf_batch_run(const nf_params *params, int n, nf_batch_result *out,
                        nf_batch_stats *stats);
+/* A handle holding n realisations side by side (own boxes, fractions,
+ * seeds, density files): nf_generate, nf_contacts and nf_solve run all of
+ * them in shared launches and may be called again (each call starts the
+ * stage over); nf_set_stream and nf_set_kernel_timing apply as for one
+ * realisation. nf_select(h, r) picks the realisation that nf_get_rods,
+ * nf_get_contacts, nf_adjoint and the stats of nf_solve report (0 after
+ * creation); calls that write files or statistics return NF_ERR_STATE on a
+ * handle of more than one realisation. */
+nf_status nf_create_batch(const nf_params *params, int n, nf_handle **out);
+nf_status nf_select(nf_handle *h, int32_t r);
+/* Per-realisation results of the last nf_solve of a batch handle (n must be
+ * its realisation count). */
+nf_status nf_batch_results(nf_handle *h, nf_batch_result *out, int32_t n);
 
 /* ---- files ------------------------------------------------------------- */
 /* VTK rods (src/IO.cpp:38-76). */
@@ -573,6 +590,9 @@ nf_status nf_autotune(nf_handle *h, nf_tune_result *out);
  *      src/cudaMain.cu:147,157) ------------------------------------------ */
 /* Kernel launches issued by this library in this process. */
 uint64_t nf_kernel_launches(void);
+/* Device (cudaMalloc) and pinned host (cudaMallocHost) allocations made by
+ * this library in this process. */
+uint64_t nf_allocations(void);
 /* Record CUDA events around the hot kernels on the handle's stream. */
 nf_status nf_set_kernel_timing(nf_handle *h, int on);
 /* Totals since timing was enabled for kernel "stream", "old_test",

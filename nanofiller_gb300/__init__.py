@@ -19,13 +19,18 @@ from ._abi import (LIB_PATH, SNK_ELEC, SRC_ELEC, STATUS, NfBatchResult, NfBatchS
                    NfAcPoint, NfAcStats, NfPairStats, NfReduceStats, load)
 
 __all__ = ["Simulation", "NanoFillerError", "make_params", "params_from_file", "batch_run",
-           "target_count", "kernel_launches", "configs", "SRC_ELEC", "SNK_ELEC", "ac_params", "ac_frequencies",
+           "target_count", "kernel_launches", "allocations", "configs", "Batch", "SRC_ELEC", "SNK_ELEC", "ac_params", "ac_frequencies",
            "write_impedance", "write_kirchhoff_log"]
 
 
 def kernel_launches():
     """Kernel launches issued by the library in this process."""
     return int(load().nf_kernel_launches())
+
+
+def allocations():
+    """Device and pinned host allocations made by the library in this process."""
+    return int(load().nf_allocations())
 
 
 class NanoFillerError(RuntimeError):
@@ -393,6 +398,33 @@ class Simulation:
 
     def write_coo(self, directory):
         _check(self._L.nf_write_coo(self._h, str(directory).encode()), self._h, "nf_write_coo")
+
+
+class Batch(Simulation):
+    """Many realisations in one handle (nf_create_batch): generate(),
+    contacts() and solve() run them all in shared launches; select(r) picks
+    the realisation that rods(), contact_list(), adjoint() and the solve
+    stats report; results() gives every realisation's outcome."""
+
+    def __init__(self, param_list, stream=None):
+        self._L = load()
+        self._nv = None
+        self.n = len(param_list)
+        arr = (NfParams * self.n)(*[make_params(p) for p in param_list])
+        self.params = arr[0]
+        h = C.c_void_p()
+        _check(self._L.nf_create_batch(arr, self.n, C.byref(h)), what="nf_create_batch")
+        self._h = h
+        if stream is not None:
+            _check(self._L.nf_set_stream(h, C.c_void_p(stream)), h)
+
+    def select(self, r):
+        _check(self._L.nf_select(self._h, int(r)), self._h, "nf_select")
+
+    def results(self):
+        res = (NfBatchResult * self.n)()
+        _check(self._L.nf_batch_results(self._h, res, self.n), self._h, "nf_batch_results")
+        return [{k: getattr(x, k) for k, _ in x._fields_} for x in res]
 
 
 def batch_run(param_list):

@@ -178,11 +178,15 @@ SIGNATURES = {
     "nf_get_voltages": (_st, [_H, C.c_void_p, C.c_size_t]),
     "nf_adjoint": (_st, [_H, C.c_void_p, C.c_size_t, _P(C.c_double), _P(C.c_double)]),
     "nf_batch_run": (_st, [_P(NfParams), C.c_int, _P(NfBatchResult), _P(NfBatchStats)]),
+    "nf_create_batch": (_st, [_P(NfParams), C.c_int, _P(C.c_void_p)]),
+    "nf_select": (_st, [C.c_void_p, C.c_int32]),
+    "nf_batch_results": (_st, [C.c_void_p, _P(NfBatchResult), C.c_int32]),
     "nf_write_vtk": (_st, [_H, C.c_char_p]),
     "nf_write_state_bin": (_st, [_H, C.c_char_p]),
     "nf_read_state_bin": (_st, [_H, C.c_char_p]),
     "nf_write_coo": (_st, [_H, C.c_char_p]),
     "nf_kernel_launches": (C.c_uint64, []),
+    "nf_allocations": (C.c_uint64, []),
     "nf_set_kernel_timing": (_st, [_H, C.c_int]),
     "nf_autotune": (_st, [_H, _P(NfTuneResult)]),
     "nf_internal_network": (_st, [_H, _P(NfInternalStats)]),

@@ -15,11 +15,13 @@
 
 namespace nf {
 unsigned long long g_launches = 0;
+unsigned long long g_allocs = 0;
 }
 
 struct nf_handle {
     nf::Engine E;
     nf_params p;
+    int cur = 0;  // realisation the per-realisation getters report (nf_select)
 };
 
 namespace {
@@ -28,6 +30,14 @@ nf_status fail(nf_handle* h, nf_status s, const std::string& msg) {
     if (h) h->E.err = msg;
     return s;
 }
+
+// Calls that read or write one realisation's files, rods or statistics run on
+// single-realisation handles (nf_create); a batch handle reports through
+// nf_select + nf_get_rods / nf_get_contacts / nf_batch_results.
+#define NF_SINGLE(h, what)                                                                          \
+    do {                                                                                            \
+        if ((h)->E.R != 1) return fail((h), NF_ERR_STATE, what " runs on a single-realisation handle"); \
+    } while (0)
 
 bool read_density(const char* path, int ext[3], float dim[3], std::vector<float>* vals) {
     // read_density (src/IO.cpp:11-36): "Lx Ly Lz" "nx ny nz" then nx*ny*nz values.
@@ -327,6 +337,7 @@ nf_status nf_last_error(const nf_handle* h, char* buf, size_t n) {
 
 nf_status nf_load_density(nf_handle* h, int nx, int ny, int nz, const float* values) {
     if (!h || !values || nx <= 0 || ny <= 0 || nz <= 0) return NF_ERR_PARAM;
+    NF_SINGLE(h, "nf_load_density");
     h->p.mesh_ext[0] = nx; h->p.mesh_ext[1] = ny; h->p.mesh_ext[2] = nz;
     return h->E.set_density(0, nx, ny, nz, values);
 }
@@ -400,6 +411,7 @@ nf_status nf_autotune(nf_handle* h, nf_tune_result* out) {
 nf_status nf_stream_candidates(nf_handle* h, uint64_t k0, uint64_t n, float* x, float* y, float* z, float* cx,
                                float* cy, float* cz, float* l, float* a, float* u, float* rho) {
     if (!h) return NF_ERR_PARAM;
+    NF_SINGLE(h, "nf_stream_candidates");
     std::vector<float> o(10 * n);
     nf_status s = h->E.stream_dump(k0, n, o.data());
     if (s != NF_OK) return s;
@@ -414,7 +426,9 @@ nf_status nf_get_rods(nf_handle* h, nf_rods* out) {
     if (!h || !out) return NF_ERR_PARAM;
     nf::Engine& E = h->E;
     if (E.count.empty() || !E.cells_valid) return fail(h, NF_ERR_STATE, "no rods");
-    size_t n = E.count[0];
+    const int rr = h->cur;
+    size_t n = E.count[rr];
+    const size_t ro = E.hreal[rr].rod_off;
     out->count = n;
     if (out->capacity < n) return NF_ERR_CAPACITY;
     // staged through the handle's pinned host buffer (asynchronous copies at
@@ -426,13 +440,13 @@ nf_status nf_get_rods(nf_handle* h, nf_rods* out) {
     uint64_t* k = reinterpret_cast<uint64_t*>(d + n);
     cudaError_t e = cudaSuccess;
     if (n) {
-        e = cudaMemcpyAsync(p, E.pos.p, sizeof(float4) * n, cudaMemcpyDeviceToHost, E.st);
-        if (e == cudaSuccess) e = cudaMemcpyAsync(d, E.dir.p, sizeof(float4) * n, cudaMemcpyDeviceToHost, E.st);
-        if (e == cudaSuccess) e = cudaMemcpyAsync(k, E.sidx.p, sizeof(uint64_t) * n, cudaMemcpyDeviceToHost, E.st);
+        e = cudaMemcpyAsync(p, E.pos.p + ro, sizeof(float4) * n, cudaMemcpyDeviceToHost, E.st);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(d, E.dir.p + ro, sizeof(float4) * n, cudaMemcpyDeviceToHost, E.st);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(k, E.sidx.p + ro, sizeof(uint64_t) * n, cudaMemcpyDeviceToHost, E.st);
         if (e == cudaSuccess) e = cudaStreamSynchronize(E.st);
     }
     if (e != cudaSuccess) return E.cuda_fail(e, "nf_get_rods");
-    const nf::Real& Re = E.hreal[0];
+    const nf::Real& Re = E.hreal[rr];
     // one pass over the staging buffer; no per-element tests when every field is wanted
     if (out->x && out->y && out->z && out->l && out->cx && out->cy && out->cz && out->a && out->stream_index &&
         out->cell) {
@@ -463,6 +477,7 @@ nf_status nf_get_rods(nf_handle* h, nf_rods* out) {
 nf_status nf_set_rods(nf_handle* h, const nf_rods* in) {
     if (!h || !in || !in->x || !in->y || !in->z || !in->cx || !in->cy || !in->cz || !in->l || !in->a)
         return NF_ERR_PARAM;
+    NF_SINGLE(h, "nf_set_rods");
     size_t n = in->count;
     std::vector<float4> p(n), d(n);
     for (size_t i = 0; i < n; ++i) {
@@ -483,7 +498,8 @@ nf_status nf_get_contacts(nf_handle* h, nf_contact_list* out) {
     if (!h || !out) return NF_ERR_PARAM;
     nf::Engine& E = h->E;
     if (!E.contacts_valid) return fail(h, NF_ERR_STATE, "no contacts");
-    size_t lo = E.ct_off[0], n = E.ct_off[1] - lo;
+    const int rr = h->cur;
+    size_t lo = E.ct_off[rr], n = E.ct_off[rr + 1] - lo;
     out->count = n;
     if (out->capacity < n) return NF_ERR_CAPACITY;
     // staged through the handle's pinned host buffer: doubles, then ids, then images
@@ -507,7 +523,7 @@ nf_status nf_get_contacts(nf_handle* h, nf_contact_list* out) {
     cp(img, E.cimg.p + 3 * lo, 3 * n);
     if (e == cudaSuccess) e = cudaStreamSynchronize(E.st);
     if (e != cudaSuccess) return E.cuda_fail(e, "nf_get_contacts");
-    const uint32_t off = E.hreal[0].rod_off;
+    const uint32_t off = E.hreal[rr].rod_off;
     if (out->I) for (size_t q = 0; q < n; ++q) out->I[q] = I[q] - off;
     if (out->J) for (size_t q = 0; q < n; ++q) out->J[q] = J[q] >= NF_SNK_ELEC ? J[q] : J[q] - off;
     if (out->tI) for (size_t q = 0; q < n; ++q) out->tI[q] = (float)t0[q];
@@ -522,12 +538,13 @@ nf_status nf_get_contacts(nf_handle* h, nf_contact_list* out) {
 nf_status nf_solve(nf_handle* h, nf_solve_stats* stats) {
     if (!h) return NF_ERR_PARAM;
     nf_status s = h->E.solve();
-    if (stats && !h->E.solve_st.empty()) *stats = h->E.solve_st[0];
+    if (stats && (int)h->E.solve_st.size() > h->cur) *stats = h->E.solve_st[h->cur];
     return s;
 }
 
 nf_status nf_get_voltages(nf_handle* h, double* v, size_t capacity) {
     if (!h || !v) return NF_ERR_PARAM;
+    NF_SINGLE(h, "nf_get_voltages");
     nf::Engine& E = h->E;
     if (!E.solve_valid) return fail(h, NF_ERR_STATE, "no solution");
     size_t n = E.int_valid ? E.int_count[0] : E.count[0];
@@ -544,7 +561,7 @@ nf_status nf_adjoint(nf_handle* h, float* dG_dend, size_t capacity, double* dG_d
         return fail(h, NF_ERR_UNSUPPORTED, "the adjoint covers the contact network (run nf_contacts again)");
     if (h->E.prm[0].elec_buffer && h->E.prm[0].field_dir)
         return fail(h, NF_ERR_UNSUPPORTED, "the adjoint covers plane electrodes (ELEC_BUFFER 0)");
-    return h->E.adjoint(0, dG_dend, capacity, dG_dlambda, dG_dG0);
+    return h->E.adjoint(h->cur, dG_dend, capacity, dG_dlambda, dG_dG0);
 }
 
 nf_status nf_internal_network(nf_handle* h, nf_internal_stats* stats) {
@@ -563,6 +580,7 @@ nf_status nf_internal_network(nf_handle* h, nf_internal_stats* stats) {
 
 nf_status nf_get_internal_network(nf_handle* h, nf_internal_net* out) {
     if (!h || !out) return NF_ERR_PARAM;
+    NF_SINGLE(h, "nf_get_internal_network");
     nf::Engine& E = h->E;
     if (!E.int_valid) return fail(h, NF_ERR_STATE, "no internal network: run nf_internal_network first");
     const size_t nn = E.int_nodes, ns = E.int_segs, ne = E.ct_off[1];
@@ -589,6 +607,7 @@ nf_status nf_get_internal_network(nf_handle* h, nf_internal_net* out) {
 
 nf_status nf_write_internal_coo(nf_handle* h, const char* dir) {
     if (!h || !dir) return NF_ERR_PARAM;
+    NF_SINGLE(h, "nf_write_internal_coo");
     nf::Engine& E = h->E;
     if (!E.int_valid) return fail(h, NF_ERR_STATE, "no internal network: run nf_internal_network first");
     nf_internal_net net{};
@@ -674,6 +693,7 @@ nf_status nf_set_orientation(nf_handle* h, int32_t mode, float kappa, float pref
 
 nf_status nf_orientation_laws(nf_handle* h, size_t cap, int32_t ext[3], float* axis, float* kappa, size_t* cells) {
     if (!h) return NF_ERR_PARAM;
+    NF_SINGLE(h, "nf_orientation_laws");
     nf_status s = h->E.orientation_laws(cap, ext, axis, kappa, cells);
     if (s != NF_OK) return fail(h, s, h->E.err);
     return NF_OK;
@@ -681,6 +701,7 @@ nf_status nf_orientation_laws(nf_handle* h, size_t cap, int32_t ext[3], float* a
 
 nf_status nf_reduce(nf_handle* h, int32_t min_contacts, nf_reduce_stats* stats) {
     if (!h) return NF_ERR_PARAM;
+    NF_SINGLE(h, "nf_reduce");
     if (min_contacts < 0) return fail(h, NF_ERR_PARAM, "min_contacts must be >= 0");
     nf_reduce_stats st{};
     nf_status s = h->E.prune(min_contacts, &st);
@@ -690,17 +711,20 @@ nf_status nf_reduce(nf_handle* h, int32_t min_contacts, nf_reduce_stats* stats) 
 
 nf_status nf_stat_nematic(nf_handle* h, const double axis[3], double* S) {
     if (!h || !axis || !S) return NF_ERR_PARAM;
+    NF_SINGLE(h, "nf_stat_nematic");
     return h->E.stat_nematic(axis, S);
 }
 
 nf_status nf_stat_phitheta(nf_handle* h, int32_t bins_phi, int32_t bins_theta, uint64_t* hist) {
     if (!h || !hist) return NF_ERR_PARAM;
+    NF_SINGLE(h, "nf_stat_phitheta");
     return h->E.stat_phitheta(bins_phi, bins_theta, hist);
 }
 
 nf_status nf_stat_pairs(nf_handle* h, int32_t bins, uint64_t* hist, uint32_t* per_rod, size_t capacity,
                         nf_pair_stats* stats) {
     if (!h) return NF_ERR_PARAM;
+    NF_SINGLE(h, "nf_stat_pairs");
     return h->E.stat_pairs(bins, hist, per_rod, capacity, stats);
 }
 
@@ -722,6 +746,7 @@ nf_status host_rods(nf_handle* h, std::vector<float>* f) {
 
 nf_status nf_write_ort_vtk(nf_handle* h, const char* path) {
     if (!h || !path) return NF_ERR_PARAM;
+    NF_SINGLE(h, "nf_write_ort_vtk");
     std::vector<float> f[8];
     nf_status s = host_rods(h, f);
     if (s != NF_OK) return s;
@@ -738,6 +763,7 @@ nf_status nf_write_ort_vtk(nf_handle* h, const char* path) {
 
 nf_status nf_write_lmp(nf_handle* h, const char* path, double density) {
     if (!h || !path) return NF_ERR_PARAM;
+    NF_SINGLE(h, "nf_write_lmp");
     std::vector<float> f[8];
     nf_status s = host_rods(h, f);
     if (s != NF_OK) return s;
@@ -859,60 +885,108 @@ nf_status nf_ac_spectrum(nf_handle* h, const nf_ac_net* net, const nf_ac_params*
     return E.ac_spectrum(net, *p, freq, n_freq, out, stats);
 }
 
-nf_status nf_batch_run(const nf_params* params, int n, nf_batch_result* out, nf_batch_stats* stats) {
-    if (!params || n <= 0 || !out) return NF_ERR_PARAM;
-    int ndev = 0;
-    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return NF_ERR_NO_DEVICE;
-    std::vector<nf_params> ps(params, params + n);
+// Parameters of a batch: per-realisation density files read, every
+// realisation validated, one electrode model when buffer layers are used.
+static nf_status prepare_batch(const nf_params* params, int n, std::vector<nf_params>* ps,
+                               std::vector<std::vector<float>>* meshes, std::vector<const float*>* mp,
+                               std::string* why) {
+    ps->assign(params, params + n);
     for (int r = 0; r < n; ++r)  // the adaptive generation runs on single-realisation handles
-        if (ps[r].self_align_step > 0 || ps[r].clust_flag) return NF_ERR_UNSUPPORTED;
+        if ((*ps)[r].self_align_step > 0 || (*ps)[r].clust_flag) {
+            *why = "adaptive generation runs on single-realisation handles";
+            return NF_ERR_UNSUPPORTED;
+        }
     for (int r = 1; r < n; ++r)  // one electrode model and field axis per engine when buffer layers are used
-        if ((ps[r].elec_buffer || ps[0].elec_buffer) &&
-            (ps[r].elec_buffer != ps[0].elec_buffer || ps[r].field_dir != ps[0].field_dir))
+        if (((*ps)[r].elec_buffer || (*ps)[0].elec_buffer) &&
+            ((*ps)[r].elec_buffer != (*ps)[0].elec_buffer || (*ps)[r].field_dir != (*ps)[0].field_dir)) {
+            *why = "a batch with buffer-layer electrodes needs one electrode model and field axis";
             return NF_ERR_PARAM;
-    std::vector<std::vector<float>> meshes(n);
-    std::vector<const float*> mp(n, nullptr);
+        }
+    meshes->assign(n, {});
+    mp->assign(n, nullptr);
     for (int r = 0; r < n; ++r) {
-        std::string why;
-        if (ps[r].density_file[0]) {
+        nf_params& q = (*ps)[r];
+        if (q.density_file[0]) {
             int ext[3];
             float dim[3];
-            if (!read_density(ps[r].density_file, ext, dim, &meshes[r])) return NF_ERR_FORMAT;
-            for (int d = 0; d < 3; ++d) { ps[r].box[d] = dim[d]; ps[r].mesh_ext[d] = ext[d]; }
-            mp[r] = meshes[r].data();
+            if (!read_density(q.density_file, ext, dim, &(*meshes)[r])) {
+                *why = std::string("cannot read density file ") + q.density_file;
+                return NF_ERR_FORMAT;
+            }
+            for (int d = 0; d < 3; ++d) { q.box[d] = dim[d]; q.mesh_ext[d] = ext[d]; }
+            (*mp)[r] = (*meshes)[r].data();
         } else {
-            ps[r].mesh_ext[0] = ps[r].mesh_ext[1] = ps[r].mesh_ext[2] = 0;
+            q.mesh_ext[0] = q.mesh_ext[1] = q.mesh_ext[2] = 0;
         }
-        nf_status s = validate(ps[r], &why);
+        nf_status s = validate(q, why);
         if (s != NF_OK) return s;
     }
-    nf::Engine E;
-    nf_status s = E.init(ps.data(), n, mp);
-    cudaEvent_t e0 = nullptr, e1 = nullptr;
-    if (s == NF_OK) {
-        cudaEventCreate(&e0);
-        cudaEventCreate(&e1);
-        cudaEventRecord(e0, E.st);
-        s = E.generate();
+    return NF_OK;
+}
+
+nf_status nf_create_batch(const nf_params* params, int n, nf_handle** out) {
+    if (!params || n <= 0 || !out) return NF_ERR_PARAM;
+    *out = nullptr;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return NF_ERR_NO_DEVICE;
+    std::vector<nf_params> ps;
+    std::vector<std::vector<float>> meshes;
+    std::vector<const float*> mp;
+    std::string why;
+    nf_status s = prepare_batch(params, n, &ps, &meshes, &mp, &why);
+    if (s != NF_OK) return s;
+    nf_handle* h = new (std::nothrow) nf_handle();
+    if (!h) return NF_ERR_ALLOC;
+    h->p = ps[0];
+    s = h->E.init(ps.data(), n, mp);
+    if (s != NF_OK) { delete h; return s; }
+    *out = h;
+    return NF_OK;
+}
+
+nf_status nf_select(nf_handle* h, int32_t r) {
+    if (!h) return NF_ERR_PARAM;
+    if (r < 0 || r >= h->E.R) return fail(h, NF_ERR_PARAM, "realisation index out of range");
+    h->cur = r;
+    return NF_OK;
+}
+
+nf_status nf_batch_results(nf_handle* h, nf_batch_result* out, int32_t n) {
+    if (!h || !out || n != h->E.R) return NF_ERR_PARAM;
+    nf::Engine& E = h->E;
+    if (!E.solve_valid || (int)E.solve_st.size() != n) return fail(h, NF_ERR_STATE, "no solution");
+    for (int r = 0; r < n; ++r) {
+        const nf_solve_stats& S = E.solve_st[r];
+        out[r].accepted = E.count[r];
+        out[r].contacts = E.ct_int[r];
+        out[r].G_eff = S.G_eff;
+        out[r].residual = S.residual;
+        out[r].percolating = S.percolating;
+        out[r].status = (S.n_active > 0 && !(S.residual <= E.prm[r].solve_tol)) ? NF_ERR_NOT_CONVERGED : NF_OK;
     }
+    return NF_OK;
+}
+
+nf_status nf_batch_run(const nf_params* params, int n, nf_batch_result* out, nf_batch_stats* stats) {
+    if (!params || n <= 0 || !out) return NF_ERR_PARAM;
+    nf_handle* h = nullptr;
+    nf_status s = nf_create_batch(params, n, &h);
+    if (s != NF_OK) return s;
+    nf::Engine& E = h->E;
+    nf::EventPair ev;
+    if (ev.create() != cudaSuccess) { nf_destroy(h); return NF_ERR_CUDA; }
+    cudaEventRecord(ev.a, E.st);
+    s = E.generate();
     if (s == NF_OK) s = E.contacts();
     nf_status ss = NF_OK;
     if (s == NF_OK) ss = E.solve();
     if (s == NF_OK && (ss == NF_OK || ss == NF_ERR_NOT_CONVERGED)) {
-        for (int r = 0; r < n; ++r) {
-            const nf_solve_stats& S = E.solve_st[r];
-            out[r].accepted = E.count[r];
-            out[r].contacts = E.ct_int[r];
-            out[r].G_eff = S.G_eff;
-            out[r].residual = S.residual;
-            out[r].percolating = S.percolating;
-            out[r].status = (S.n_active > 0 && !(S.residual <= ps[r].solve_tol)) ? NF_ERR_NOT_CONVERGED : NF_OK;
-        }
-        if (stats) {
+        s = nf_batch_results(h, out, n);
+        if (s == NF_OK && stats) {
             float ms = 0;
-            cudaEventRecord(e1, E.st);
-            cudaEventSynchronize(e1);
-            cudaEventElapsedTime(&ms, e0, e1);
+            cudaEventRecord(ev.b, E.st);
+            cudaEventSynchronize(ev.b);
+            cudaEventElapsedTime(&ms, ev.a, ev.b);
             stats->n = n;
             stats->rounds = E.gst.rounds;
             stats->rods = E.gst.accepted;
@@ -922,13 +996,12 @@ nf_status nf_batch_run(const nf_params* params, int n, nf_batch_result* out, nf_
     } else if (s == NF_OK) {
         s = ss;
     }
-    if (e0) cudaEventDestroy(e0);
-    if (e1) cudaEventDestroy(e1);
-    E.release();
+    nf_destroy(h);
     return s;
 }
 
 uint64_t nf_kernel_launches(void) { return nf::g_launches; }
+uint64_t nf_allocations(void) { return nf::g_allocs; }
 
 nf_status nf_set_kernel_timing(nf_handle* h, int on) {
     if (!h) return NF_ERR_PARAM;
@@ -1100,6 +1173,7 @@ static nf_status cell_layout(nf_handle* h, nf_state_header* hd, std::vector<int1
 
 nf_status nf_write_vtk(nf_handle* h, const char* path) {
     if (!h || !path) return NF_ERR_PARAM;
+    NF_SINGLE(h, "nf_write_vtk");
     nf_state_header hd;
     std::vector<int16_t> occ;
     std::vector<int32_t> addr;
@@ -1115,6 +1189,7 @@ nf_status nf_write_vtk(nf_handle* h, const char* path) {
 
 nf_status nf_write_state_bin(nf_handle* h, const char* path) {
     if (!h || !path) return NF_ERR_PARAM;
+    NF_SINGLE(h, "nf_write_state_bin");
     nf_state_header hd;
     std::vector<int16_t> occ;
     std::vector<int32_t> addr;
@@ -1127,6 +1202,7 @@ nf_status nf_write_state_bin(nf_handle* h, const char* path) {
 
 nf_status nf_read_state_bin(nf_handle* h, const char* path) {
     if (!h || !path) return NF_ERR_PARAM;
+    NF_SINGLE(h, "nf_read_state_bin");
     nf_state_header hd;
     nf_status s = nf_format_read_state_bin(path, &hd, nullptr, nullptr, nullptr, 0, 0);
     if (s != NF_OK) return s;
@@ -1148,15 +1224,23 @@ nf_status nf_read_state_bin(nf_handle* h, const char* path) {
             d.push_back(make_float4(pl[3 * ttl + q], pl[4 * ttl + q], pl[5 * ttl + q], pl[7 * ttl + q]));
         }
     }
-    for (int k = 0; k < 3; ++k) h->p.box[k] = hd.phys_dim[k];
-    h->E.prm[0].box[0] = hd.phys_dim[0];
-    h->E.prm[0].box[1] = hd.phys_dim[1];
-    h->E.prm[0].box[2] = hd.phys_dim[2];
+    // the box, rod length, radius and TOL travel with the state, as
+    // read_state_BIN (src/stateSR.cpp:96-103) restores physDim, l, a and TOL
+    if (!(hd.l > 0) || !(hd.a > 0) || !(hd.tol > 0) || !std::isfinite(hd.l) || !std::isfinite(hd.a) ||
+        !std::isfinite(hd.tol))
+        return fail(h, NF_ERR_FORMAT, "output.bin header: l, a and TOL must be positive");
+    for (nf_params* q : {&h->p, &h->E.prm[0]}) {
+        for (int k = 0; k < 3; ++k) q->box[k] = hd.phys_dim[k];
+        q->l = hd.l;
+        q->a = hd.a;
+        q->tol = hd.tol;
+    }
     return h->E.inject(p.size(), p.data(), d.data(), nullptr);
 }
 
 nf_status nf_write_coo(nf_handle* h, const char* dir) {
     if (!h || !dir) return NF_ERR_PARAM;
+    NF_SINGLE(h, "nf_write_coo");
     nf::Engine& E = h->E;
     if (!E.contacts_valid) return fail(h, NF_ERR_STATE, "no contacts");
     size_t n = E.ct_off[1] - E.ct_off[0];
@@ -1194,16 +1278,11 @@ nf_status nf_write_coo(nf_handle* h, const char* dir) {
 namespace {
 
 constexpr uint32_t kNoAllocMax = NF_NOALLOC_MAX_CANDIDATES;
-constexpr int kNoAllocDevices = 64;  // device ordinals served by the address cache
 
 // Field-major staging: field f of candidate i at [f * kNoAllocMax + i]
 // (10 fields x 65536 candidates x 4 B = 2.5 MiB). Nothing here needs to start
 // at zero: a call writes all 10 * n values before it copies them out.
 static __device__ __align__(256) float g_noalloc_stage[10 * kNoAllocMax];
-
-// Device address of g_noalloc_stage per device ordinal, looked up by the first
-// call on that device (concurrent first calls store the same value).
-std::atomic<float*> g_noalloc_addr[kNoAllocDevices];
 
 __global__ void k_stream_dump_static(const nf::Real Re, uint64_t k0, uint32_t n, float* __restrict__ out) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1229,16 +1308,13 @@ extern "C" nf_status nf_stream_candidates_noalloc(nf_handle* h, uint64_t k0, uin
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return E.cuda_fail(e, "cudaGetDevice");
     if (dev != E.dev) return fail(h, NF_ERR_STATE, "nf_stream_candidates_noalloc: current device is not the handle's");
-    if (dev < 0 || dev >= kNoAllocDevices)
-        return fail(h, NF_ERR_PARAM, "nf_stream_candidates_noalloc: device ordinal above 63");
-    float* stage = g_noalloc_addr[dev].load(std::memory_order_acquire);
-    if (!stage) {
-        void* addr = nullptr;
-        e = cudaGetSymbolAddress(&addr, g_noalloc_stage);
-        if (e != cudaSuccess) return E.cuda_fail(e, "cudaGetSymbolAddress(staging array)");
-        stage = static_cast<float*>(addr);
-        g_noalloc_addr[dev].store(stage, std::memory_order_release);
-    }
+    // The array's device address, looked up on every call with the handle's
+    // device current (a host-side query once the module is loaded): an
+    // address kept from an earlier call would be stale after a device reset.
+    void* addr = nullptr;
+    e = cudaGetSymbolAddress(&addr, g_noalloc_stage);
+    if (e != cudaSuccess) return E.cuda_fail(e, "cudaGetSymbolAddress(staging array)");
+    float* stage = static_cast<float*>(addr);
     // Same descriptor as the allocating dump builds for realisation 0.
     const nf_params& p = E.prm[0];
     const float* dmesh = nullptr;

@@ -52,6 +52,7 @@ struct DBuf {
         p = nullptr;
         cap = 0;
         size_t m = n < 1 ? 1 : n;
+        ++g_allocs;
         cudaError_t e = cudaMalloc((void**)&p, m * sizeof(T));
         if (e == cudaSuccess) cap = m;
         return e;

@@ -811,6 +811,7 @@ nf_status Engine::ensure_pinned(size_t bytes) {
     if (hpin) cudaFreeHost(hpin);
     hpin = nullptr;
     hpin_cap = 0;
+    ++g_allocs;
     NF_CK(cudaMallocHost(reinterpret_cast<void**>(&hpin), bytes));
     hpin_cap = bytes;
     return NF_OK;

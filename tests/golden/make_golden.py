@@ -8,7 +8,7 @@ ref_predicates.npz -- outputs of the reference's OWN geometric routines
     compiled for the host from the reference's headers by oracle/ref_build.sh,
     on seeded random pairs plus constructed edge cases (parallel, collinear,
     perpendicular crossings, skew, pairs within 1e-6..1e-3 of the thresholds).
-    Needs the reference checkout (NANOFILLER_REF, default /root/reference).
+    Needs the reference checkout, named by NANOFILLER_REF.
 small_oracle.npz -- the oracle's accepted set and contact list for the small
     workload (2 um box, 510 rods), pinning the stream contract and the
     pipeline across machines.
@@ -152,7 +152,8 @@ def small_fixture():
 
 if __name__ == "__main__":
     A, B = make_pairs()
-    if os.path.isdir(os.environ.get("NANOFILLER_REF", "/root/reference")):
+    ref = os.environ.get("NANOFILLER_REF")
+    if ref and os.path.isdir(ref):
         np.savez_compressed(os.path.join(HERE, "ref_predicates.npz"), **ref_outputs(A, B))
         print("wrote ref_predicates.npz", len(A))
     np.savez_compressed(os.path.join(HERE, "small_oracle.npz"), **small_fixture())

@@ -245,3 +245,19 @@ def test_call_order_errors(gpu):
         sim.contacts()
     assert e.value.status == 10
     sim.close()
+
+
+def test_state_bin_restores_length_radius_and_tol(gpu, tmp_path):
+    """read_state_BIN restores l, a and TOL from the file (src/stateSR.cpp:96-103):
+    a handle made with other values finds the same contacts after reading it."""
+    cfg = perc_small(gpu.configs)
+    g = run_gpu(gpu, cfg, stages=("generate", "contacts"))
+    g["sim"].write_state(tmp_path / "output.bin")
+    other = dict(cfg, l=0.2, a=0.002, tol=1e-5)
+    with gpu.Simulation(other) as s2:
+        s2.read_state(tmp_path / "output.bin")
+        c2 = s2.contacts()
+        s2.write_state(tmp_path / "again.bin")
+    assert c2["contacts"] == g["cst"]["contacts"] and c2["n_sink"] == g["cst"]["n_sink"]
+    assert (tmp_path / "again.bin").read_bytes() == (tmp_path / "output.bin").read_bytes()
+    g["sim"].close()

@@ -78,3 +78,25 @@ def test_reference_arm_under_torchrun(tmp_path):
     assert o["e2e"] == {"value": o["value"], "unit": "rods/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
     assert o["cpu_baseline"]["kind"] == "port" and o["cpu_baseline"]["cores"] >= 1
     assert o["config"]["workload"] == "small"
+
+
+def test_both_arms_print_the_same_config():
+    import bench
+    a = bench.workload_config("batched", batch=256)
+    assert a["workload"] == "batched" and a["realisations"] == 256 and "parallelism" not in a
+    params, _ = bench.workload("medium", 0)
+    assert bench.workload_config("medium", params) == bench.workload_config("medium", dict(params))
+
+
+def test_flip_count_counts_differences():
+    import numpy as np
+
+    import bench
+    idx = np.array([3, 7, 9], np.uint64)
+    ct = dict(I=np.array([0, 1, 2], np.uint32), J=np.array([1, 2, 0xFFFFFFFE], np.uint32),
+              image=np.zeros((3, 3), np.int8))
+    assert bench.flips(idx, ct, idx, ct) == 0
+    idx2 = np.array([3, 7, 11], np.uint64)  # one rod accepted in place of another
+    assert bench.flips(idx, ct, idx2, ct) == 2 + 4  # two stream indices, the two contacts of that rod, both ways
+    ct2 = dict(ct, image=np.array([[0, 0, 0], [0, 0, 1], [0, 0, 0]], np.int8))
+    assert bench.flips(idx, ct, idx, ct2) == 2

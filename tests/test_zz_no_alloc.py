@@ -66,3 +66,18 @@ def test_noalloc_limits(gpu):
         st = L.nf_stream_candidates_noalloc(sim._h, 0, 100, x.ctypes.data_as(C.c_void_p), *([None] * 9))
         assert st == 0
         assert np.array_equal(x, sim.stream(0, 100)[:, 0])
+
+
+def test_noalloc_makes_no_allocation(gpu):
+    """The property the entry point exists for: after the handle is set up,
+    calls through it leave the library's allocation count unchanged, while
+    the allocating dump allocates its staging buffer on every call."""
+    with gpu.Simulation(dict(gpu.configs.SMALL)) as sim:
+        sim.stream_noalloc(0, 16)  # device code loaded, handle descriptors on the device
+        n0 = gpu.allocations()
+        for k0 in (0, 1 << 20, 1 << 33):
+            sim.stream_noalloc(k0, MAX)
+        assert gpu.allocations() == n0
+        sim.stream(0, MAX)
+        assert gpu.allocations() > n0
+
