@@ -59,6 +59,7 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extras", action="store_true", help="batched: skip the plain pass, large and jammed keys")
+    ap.add_argument("--tube-load", type=float, default=None, help="TUBE_LOAD of every realisation (speed only)")
     return ap.parse_args()
 
 
@@ -493,6 +494,8 @@ def run_batched(args, rank, world):
     reals = nf.configs.batched_realisations(args.batch)
     for p in reals:
         p["seed"] += rank * args.batch
+        if args.tube_load is not None:
+            p["tube_load"] = args.tube_load
     stream = torch.cuda.current_stream().cuda_stream
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
     b = nf.Batch(reals, stream=stream)
@@ -648,6 +651,8 @@ def run_ours(args, rank, world):
     import nanofiller_gb300 as nf
     local, dist = gpu_setup(world)
     params, mesh = workload(args.workload, rank)
+    if args.tube_load is not None:
+        params["tube_load"] = args.tube_load
     stream = torch.cuda.current_stream().cuda_stream
     sim = nf.Simulation(params, mesh=mesh, stream=stream)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")

@@ -169,7 +169,13 @@ typedef struct nf_params {
     int32_t solve_method;   /* SOLVE_METHOD: 0 auto (direct when the network's
                                band after reverse Cuthill-McKee is narrow),
                                1 direct (banded LDL^T), 2 iterative (PCG)   */
-    int32_t pad_solve;
+    float tube_load;        /* TUBE_LOAD (tuning, speed only): the pair sweeps
+                               register every rod in each cell of a fine grid
+                               that its axis segment, dilated by half the
+                               widest pair threshold, touches, and test the
+                               pairs that share a cell; the cell edge is chosen
+                               for about this many registrations per cell
+                               (0 -> 24); < 0 -> the cell-stencil sweeps     */
 } nf_params;
 
 /* Rods, structure of arrays, caller-owned host buffers. Any array may be NULL. */

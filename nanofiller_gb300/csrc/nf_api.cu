@@ -96,6 +96,7 @@ nf_status validate(const nf_params& p, std::string* why) {
         *why = "RAD_RANGE lo hi required for uniform radii"; return NF_ERR_PARAM;
     }
     if (!(p.lambda > 0) || !(p.G0 > 0)) { *why = "tunnelling law needs G0 > 0 and lambda > 0"; return NF_ERR_PARAM; }
+    if (!std::isfinite(p.tube_load)) { *why = "TUBE_LOAD must be finite"; return NF_ERR_PARAM; }
     if (p.stencil_radius < 0 || p.stencil_radius > 2 || !(p.round_overshoot >= 0) || p.two_phase_work != p.two_phase_work) {
         *why = "STENCIL_RADIUS must be 0, 1 or 2 and ROUND_OVERSHOOT >= 0"; return NF_ERR_PARAM;
     }
@@ -252,6 +253,7 @@ nf_status nf_params_from_file(const char* path, nf_params* p, int* n_unknown) {
         else if (key == "TUNNEL_DC") in >> p->d_c;
         else if (key == "REF_PARALLEL_TYPO") in >> p->ref_parallel_typo;
         else if (key == "TRUNC_NORMAL_REF") in >> p->ref_trunc_normal;
+        else if (key == "TUBE_LOAD") in >> p->tube_load;
         else if (key == "SCREENING") in >> p->screening;
         else if (key == "ROUND_CANDIDATES") in >> p->round_candidates;
         else if (key == "SOLVE_MAX_ITER") in >> p->solve_max_iter;

@@ -306,6 +306,17 @@ struct Real {
     int32_t S;
     int32_t per_gen, per_con;
     uint32_t cell_off, ncell;
+    // tube grid of the pair sweeps (tube == 0: the cell-stencil sweeps): tcn
+    // cells of edge tce = L / tcn across the box per axis (tci = 1 / tce), tcm
+    // margin cells beyond each
+    // face of an axis open in some stage; every object registers in each cell
+    // that its axis segment, extended to l/2 + a + eps and dilated by trho,
+    // touches (tube_walk)
+    int32_t tube;
+    int32_t tcn[3], tcm[3];
+    float tci[3], tce[3];
+    float trho;
+    uint32_t toff, tncell;
     // rods
     uint32_t rod_off, target;
     // hard core (cnt_intersec_shr) and contacts (distance_cylinder_capped)
@@ -572,7 +583,7 @@ NF_HD bool sphere_far(float bx, float by, float bz, float hA_plus, float hB, flo
 // |t| at least dt inside their limits, and the line distance at least err
 // below the threshold. Certified pairs are hits in FP64 as well.
 NF_HD bool certain_hit(const float4& pA, const float4& cA, const float4& pB, const float4& cB, float sx, float sy,
-                       float sz, float thr, float eps, float slack) {
+                       float sz, float thr, float eps, float slack, float* t0o = nullptr, float* t1o = nullptr) {
     float bx = (pB.x + sx) - pA.x, by = (pB.y + sy) - pA.y, bz = (pB.z + sz) - pA.z;
     float d = cA.x * cB.x + cA.y * cB.y + cA.z * cB.z;
     if (fabsf(d) > 0.995f) return false;
@@ -583,6 +594,7 @@ NF_HD bool certain_hit(const float4& pA, const float4& cA, const float4& pB, con
     float dt = (2e-5f * (1.0f + nb) + 2.0f * slack) / fabsf(den);
     if (fabsf(t0) + dt >= (pA.w * 0.5f + cA.w + eps) * 0.99999f) return false;
     if (fabsf(t1) + dt >= (pB.w * 0.5f + cB.w + eps) * 0.99999f) return false;
+    if (t0o) { *t0o = t0; *t1o = t1; }
     float nx = cA.y * cB.z - cA.z * cB.y;
     float ny = cA.z * cB.x - cA.x * cB.z;
     float nz = cA.x * cB.y - cA.y * cB.x;

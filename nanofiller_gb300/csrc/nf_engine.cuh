@@ -22,6 +22,7 @@
 #include "../../include/nanofiller_gb300.h"
 #include "nf_common.cuh"
 #include "nf_tiles.cuh"
+#include "nf_tube.cuh"
 
 namespace nf {
 
@@ -157,6 +158,19 @@ struct Engine {
     DBuf<unsigned char> cubtmp;
     DBuf<uint32_t> u32tmp;
 
+    // tube grid of the pair sweeps (nf_tube.cuh): registrations of the placed
+    // rods (trod*), of the round's candidates or survivors (tcnd*), per-cell
+    // CSR over ntcell cells, and the work list of a tube sweep
+    bool tube = false;
+    uint32_t ntcell = 0;
+    int trod_stage = -1;                    // stage of the current rod registrations (-1: stale)
+    DBuf<uint32_t> toffs;                   // R + 1 prefix of tube cells
+    DBuf<uint32_t> trod_start, trod_cur, trod_ent;
+    DBuf<uint32_t> tcnd_start, tcnd_cur, tcnd_ent;
+    DBuf<TItem> titems;
+    size_t tit_cap = 1 << 20;
+    DBuf<uint32_t> tioff;
+
     // contacts
     DBuf<Rec> rec, rec2;
     DBuf<uint32_t> rcnt, rpos, rcur;
@@ -282,6 +296,13 @@ struct Engine {
     // ring: 0 all stencil rows, 1 the inner rows (|dy|, |dz| <= 1), 2 the others.
     nf_status build_items(const uint32_t* pstart, const uint32_t* tstart, int stage, uint64_t np, uint64_t nt,
                           int ring = 0);
+    // Tube registrations: the placed rods (stage 0 generation, 1 contacts)
+    // into trod_*, the round's candidates (all kept, or the survivors of the
+    // old-rod test) into tcnd_*; then the work list of probes x targets.
+    nf_status tube_register_rods(int stage);
+    nf_status tube_register_cands(uint64_t slots, const uint32_t* ntot, bool alive_only);
+    nf_status tube_items(const uint32_t* pstart, const uint32_t* tstart);
+    const uint32_t* titem_count() const { return tioff.p + ntcell; }
     // Pinned host block for the per-round read-backs.
     uint8_t* hpin = nullptr;
     size_t hpin_cap = 0;

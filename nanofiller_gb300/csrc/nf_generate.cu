@@ -100,6 +100,55 @@ void set_tn_law(Real& R, const nf_params& p) {
     if (R.tn & 2) law(p.phi_dev, kPiD, &R.pc1, &R.pc2, &R.pz);
 }
 
+// Tube grid of the pair sweeps (nf_tube.cuh). The registration radius is half
+// the widest pair threshold of the three sweeps (hard core, contacts,
+// screening) with margins far above the FP32 rounding of the walk; the cell
+// edge e solves n (2 l e^2 + e^3) = load, the registrations per cell of n rods
+// per unit volume of mean length l (each registers in ~2 l / e + 1 cells of
+// volume e^3). A periodic axis must be longer than a rod's reach, so that a
+// registration is one image away at most; otherwise the stencil sweeps run.
+void set_tube_grid(Real& R, const nf_params& p) {
+    R.tube = 0;
+    if (!(p.tube_load > 0)) return;
+    double lmax, amax;
+    size_bounds(p, &lmax, &amax);
+    const double eps = std::max((double)p.tol, (double)1e-6f);
+    const double thr = std::max(2 * amax * p.sc_frac + p.sep + eps, 2 * amax + p.stat_dist_lim + eps);
+    const double Lmax = std::max((double)p.box[0], std::max((double)p.box[1], (double)p.box[2]));
+    const double rho = 0.5 * thr * 1.0001 + 1e-5 * (1.0 + Lmax) + 8.0 * R.slack;
+    const double h = (lmax / 2 + amax + eps) * 1.00001 + R.slack;
+    const int per = (R.per_gen | R.per_con) & 7;
+    for (int d = 0; d < 3; ++d)
+        if (((per >> d) & 1) && !(h + rho < 0.999 * p.box[d])) return;
+    const double V = (double)p.box[0] * p.box[1] * p.box[2];
+    const double nrod = (double)std::max<int64_t>(target_count(p), 1);
+    double lmean = p.l;
+    if (p.len_mode == NF_SIZE_LOGNORMAL) lmean = std::min((double)p.len_max, p.l * std::exp(0.5 * p.len_sigma_ln * p.len_sigma_ln));
+    const double load = (double)p.tube_load;
+    const double nd = nrod / V;
+    double lo = 4 * rho, hi = std::max(lo, std::min((double)p.box[0], std::min((double)p.box[1], (double)p.box[2])));
+    for (int it = 0; it < 60; ++it) {
+        const double e = 0.5 * (lo + hi);
+        if (nd * (2 * lmean * e * e + e * e * e) > load) hi = e; else lo = e;
+    }
+    double e = std::max(0.5 * (lo + hi), 4 * rho);
+    for (;;) {
+        uint64_t cells = 1;
+        for (int d = 0; d < 3; ++d) {
+            int n = (int)std::floor((double)p.box[d] / e);
+            R.tcn[d] = n < 1 ? 1 : n;
+            R.tce[d] = (float)((double)p.box[d] / R.tcn[d]);
+            R.tci[d] = (float)((double)R.tcn[d] / (double)p.box[d]);
+            R.tcm[d] = ((per >> d) & 1) ? 0 : (int)std::ceil((h + rho) / R.tce[d]) + 1;
+            cells *= (uint64_t)(R.tcn[d] + 2 * R.tcm[d]);
+        }
+        if (cells <= (1ull << 26)) { R.tncell = (uint32_t)cells; break; }
+        e *= 1.25;
+    }
+    R.trho = (float)rho;
+    R.tube = 1;
+}
+
 Real make_real(const nf_params& p, const float* dmesh, int mn[3], double reach) {
     Real R;
     std::memset(&R, 0, sizeof(R));
@@ -164,6 +213,7 @@ Real make_real(const nf_params& p, const float* dmesh, int mn[3], double reach) 
     R.G0 = p.G0;
     R.lambda = p.lambda;
     R.dc = p.d_c;
+    set_tube_grid(R, p);
     return R;
 }
 
@@ -646,6 +696,346 @@ __global__ void __launch_bounds__(256) k_conf_exact(const Real* __restrict__ rea
     warp_add_u64(&ctr[C_OVERFLOW], ovf);
 }
 
+// ---------------------------------------------------------------------------
+// Tube sweeps of the generation (nf_tube.cuh): the pairs registered together
+// in a tube cell. Items are (<= 32 probe entries, <= kTSeg target entries) of
+// one cell; a lane holds a probe, the warp stages 32 targets at a time. Every
+// entry carries the image of its object's copy in the cell: the marking loop
+// works on the copies, the filters and the FP64 queue on the original
+// coordinates with the relative image (target copy image - probe copy image).
+// ---------------------------------------------------------------------------
+struct TubeTile {
+    float4 ps[kWT];  // target copy centre, .w = its reach term of the capsule test
+    float4 p[kWT];   // target centre (original coordinates), .w = length
+    float4 c[kWT];   // axis, .w = radius
+    uint32_t id[kWT];
+    uint32_t im[kWT];  // image code of the target's copy
+};
+
+__device__ __forceinline__ void img_of(uint32_t code, int img[3]) {
+    img[0] = (int)(code & 3u) - 1;
+    img[1] = (int)((code >> 2) & 3u) - 1;
+    img[2] = (int)((code >> 4) & 3u) - 1;
+}
+
+// Relative image of a pair (target copy image - probe copy image); false when
+// it is beyond one box (such a pair is farther apart than a box edge).
+__device__ __forceinline__ bool rel_img(uint32_t ip, uint32_t it, int img[3]) {
+    int a[3], b[3];
+    img_of(ip, a);
+    img_of(it, b);
+    bool ok = true;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        img[d] = b[d] - a[d];
+        ok = ok && img[d] >= -1 && img[d] <= 1;
+    }
+    return ok;
+}
+
+// Whether the tube cell `cell`, holding the probe's copy of image code ip,
+// is the one cell that claims a pair whose points are P_A = A + t0 cA and
+// P_B = B + img L + t1 cB: the cell of their midpoint in A's frame (both
+// objects are registered there: the midpoint is within the pair's distance /
+// 2 of both segments).
+__device__ __forceinline__ bool tube_claims(const Real& Re, int per, uint32_t cell, uint32_t ip, const float4& pA,
+                                            const float4& cA, const float4& pB, const float4& cB, float sx, float sy,
+                                            float sz, float t0, float t1) {
+    const float mx = 0.5f * ((pA.x + t0 * cA.x) + ((pB.x + sx) + t1 * cB.x));
+    const float my = 0.5f * ((pA.y + t0 * cA.y) + ((pB.y + sy) + t1 * cB.y));
+    const float mz = 0.5f * ((pA.z + t0 * cA.z) + ((pB.z + sz) + t1 * cB.z));
+    const int u[3] = {(int)floorf(mx * Re.tci[0]), (int)floorf(my * Re.tci[1]), (int)floorf(mz * Re.tci[2])};
+    uint32_t c2;
+    int im[3];
+    if (!tube_cell(Re, per, u, &c2, im)) return false;
+    return c2 == cell && tube_entry(0, im) == (ip & 63u);
+}
+
+// Candidates (probe entries) against placed rods (target entries) of one tube
+// cell: cuda_OldExtIsectLB's job (inc/intersection_kern.h:245-364) on the
+// tube grid. Marking, hand-out, certificate and FP64 queue as k_old_tiles.
+__global__ void __launch_bounds__(kTPB, 6) k_tube_old(const Real* __restrict__ reals, int R,
+                                                   const uint32_t* __restrict__ toffs,
+                                                   const uint32_t* __restrict__ nitems, uint32_t icap,
+                                                   const TItem* __restrict__ items,
+                                                   const uint32_t* __restrict__ pent,
+                                                   const float4* __restrict__ cpos, const float4* __restrict__ cdir,
+                                                   const uint32_t* __restrict__ tent,
+                                                   const float4* __restrict__ rpos, const float4* __restrict__ rdir,
+                                                   uint8_t* state, unsigned long long* __restrict__ xq,
+                                                   unsigned long long xcap, unsigned long long* __restrict__ ctr) {
+    constexpr int kW = kTPB / 32;
+    __shared__ TubeTile tiles[kW];
+    __shared__ float4 ppos[kW][32], pdir[kW][32];
+    __shared__ uint32_t pcid[kW][32], pim[kW][32];
+    __shared__ int msp[kW][32];
+    __shared__ uint32_t msm[kW][32];
+    __shared__ uint16_t mq2[kW][64];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    TubeTile& T = tiles[w];
+    volatile uint8_t* vst = state;
+    unsigned long long tests = 0, cert = 0, nitem = 0, ntile = 0, nmark = 0, nline = 0;
+    const uint32_t n = min(*nitems, icap);
+    const uint32_t stride = gridDim.x * kW;
+    TItem nxt = blockIdx.x * kW + w < n ? items[blockIdx.x * kW + w] : TItem{0, 0, 0, 0};
+    for (uint32_t it = blockIdx.x * kW + w; it < n; it += stride) {
+        const TItem I = nxt;
+        if (it + stride < n) nxt = items[it + stride];
+        ++nitem;
+        const uint32_t np = I.cnt & 63u, nt = I.cnt >> 6;
+        const Real& Re = reals[find_real(toffs, R, I.cell)];
+        const bool have = (uint32_t)lane < np;
+        uint32_t cid = 0, ipc = 0;
+        float4 pA = make_float4(0, 0, 0, 0), cA = pA;
+        if (have) {
+            const uint32_t e = pent[I.pfirst + lane];
+            cid = e >> kTubeIdShift;
+            ipc = e & 63u;
+            pA = cpos[cid];
+            cA = cdir[cid];
+        }
+        bool alive = have && vst[cid] != ST_REJ_OLD;
+        __syncwarp();
+        ppos[w][lane] = pA;
+        pdir[w][lane] = cA;
+        pcid[w][lane] = cid;
+        pim[w][lane] = ipc;
+        int ia[3];
+        img_of(ipc, ia);
+        // the probe's copy in this cell
+        const float ax = pA.x + ia[0] * Re.L[0], ay = pA.y + ia[1] * Re.L[1], az = pA.z + ia[2] * Re.L[2];
+        const float hA2 = (pA.w * 0.5f + cA.w + Re.eps + cA.w * Re.scf + Re.sep + Re.eps) * 1.000002f + Re.slack;
+        const float hAe = pA.w * 0.5f + cA.w + Re.eps;
+        const float hC = (cA.w * Re.scf + Re.sep + Re.eps) * 1.000002f + Re.slack + 4e-6f * (1.0f + hA2);
+        const float errA = 4e-6f * (1.0f + hA2) + 2.0f * Re.slack;
+        const float thA = (cA.w * Re.scf + Re.sep + Re.eps) * 1.0002f, scf2 = Re.scf * 1.0002f;
+        unsigned dead = 0;
+        for (uint32_t b = 0; b < nt; b += kWT) {
+            if (!__any_sync(0xffffffffu, alive)) break;
+            const uint32_t m = min((uint32_t)kWT, nt - b);
+            if ((uint32_t)lane < m) {
+                const uint32_t e = tent[I.tfirst + b + lane];
+                const uint32_t k = e >> kTubeIdShift;
+                const float4 p = rpos[k], c = rdir[k];
+                int ib[3];
+                img_of(e & 63u, ib);
+                T.p[lane] = p;
+                T.ps[lane] = make_float4(p.x + ib[0] * Re.L[0], p.y + ib[1] * Re.L[1], p.z + ib[2] * Re.L[2],
+                                         (p.w * 0.5f + c.w + Re.eps + c.w * Re.scf) * 1.000002f);
+                T.c[lane] = c;
+                T.id[lane] = k;
+                T.im[lane] = e & 63u;
+            } else {
+                T.ps[lane] = make_float4(kFar, kFar, kFar, 0.0f);
+            }
+            __syncwarp();
+            uint32_t mask = 0;
+            if (alive) {
+                tests += m;
+                const uint32_t m8 = (m + 7u) & ~7u;
+                for (uint32_t j0 = 0; j0 < m8; j0 += 8) {
+#pragma unroll
+                    for (uint32_t jj = 0; jj < 8; ++jj) {
+                        const float4 tq = T.ps[j0 + jj];
+                        const float bx = tq.x - ax, by = tq.y - ay, bz = tq.z - az;
+                        const float4 cB = T.c[j0 + jj];
+                        const float nx = cA.y * cB.z - cA.z * cB.y;
+                        const float ny = cA.z * cB.x - cA.x * cB.z;
+                        const float nz = cA.x * cB.y - cA.y * cB.x;
+                        const float nn = nx * nx + ny * ny + nz * nz;
+                        const float nb = fabsf(nx * bx + ny * by + nz * bz) - fmaf(4e-6f, tq.w, errA);
+                        const float thL = fmaf(cB.w, scf2, thA);
+                        const bool lfar = nn > 1e-4f && nb > 0.0f && nb * nb > thL * thL * nn;
+                        if (!lfar && capsule_near(bx, by, bz, cA.x, cA.y, cA.z, hAe, tq.w, hC)) mask |= 1u << (j0 + jj);
+                    }
+                }
+            }
+            auto keep = [&](int pl, int t) {
+                if ((dead >> pl) & 1u) return false;
+                int img[3];
+                if (!rel_img(pim[w][pl], T.im[t], img)) return false;
+                const float4 dA = pdir[w][pl], cB = T.c[t];
+                return !line_far(ppos[w][pl], dA, T.p[t], cB, img[0] * Re.L[0], img[1] * Re.L[1], img[2] * Re.L[2],
+                                 (cB.w + dA.w) * Re.scf + Re.sep + Re.eps, Re.slack);
+            };
+            ++ntile;
+            nmark += __popc(mask);
+            const int kept_ = for_marked_pairs(mask, lane, msp[w], msm[w], mq2[w], keep, [&](bool valid, int pl, int t) {
+                bool hit = false;
+                if (valid && !((dead >> pl) & 1u)) {
+                    const float4 qA = ppos[w][pl], dA = pdir[w][pl];
+                    const float4 pB = T.p[t], cB = T.c[t];
+                    int img[3];
+                    rel_img(pim[w][pl], T.im[t], img);
+                    const float sx = img[0] * Re.L[0], sy = img[1] * Re.L[1], sz = img[2] * Re.L[2];
+                    const float thr = (cB.w + dA.w) * Re.scf + Re.sep + Re.eps;
+                    if (maybe_near(qA, dA, pB, cB, sx, sy, sz, thr, Re.eps, Re.slack)) {
+                        const uint32_t c = pcid[w][pl];
+                        if (!Re.typo && certain_hit(qA, dA, pB, cB, sx, sy, sz, thr, Re.eps, Re.slack)) {
+                            hit = true;
+                            ++cert;
+                            vst[c] = ST_REJ_OLD;
+                        } else {
+                            xq_push(xq, xcap, &ctr[C_XQ_OLD], xq_pack(c, T.id[t], img));
+                        }
+                    }
+                }
+                dead |= __reduce_or_sync(0xffffffffu, hit ? (1u << pl) : 0u);
+            });
+            if (lane == 0) nline += kept_;
+            if ((dead >> lane) & 1u) alive = false;
+            if (alive && vst[cid] == ST_REJ_OLD) alive = false;
+            __syncwarp();
+        }
+    }
+    warp_add_u64(&ctr[C_PAIR_TESTS], tests);
+    warp_add_u64(&ctr[C_CERT], cert);
+    if (lane == 0) {
+        atomicAdd(&ctr[C_G_ITEMS], nitem);
+        atomicAdd(&ctr[C_G_TILES], ntile);
+        atomicAdd(&ctr[C_G_LINE], nline);
+    }
+    warp_add_u64(&ctr[C_G_MARKED], nmark);
+}
+
+// Survivors against earlier survivors of one tube cell (probe and target
+// entries are the same list): k_conf_tiles on the tube grid. A certified hit
+// is listed by the one cell that claims it (tube_claims), so no pair enters a
+// conflict list twice from the FP32 path; uncertain pairs are queued from
+// every cell they share (the FP64 pass may list a pair again, which the
+// resolution ignores).
+__global__ void __launch_bounds__(kTPB, 6) k_tube_conf(const Real* __restrict__ reals, int R,
+                                                    const uint32_t* __restrict__ toffs,
+                                                    const uint32_t* __restrict__ nitems, uint32_t icap,
+                                                    const TItem* __restrict__ items,
+                                                    const uint32_t* __restrict__ ent,
+                                                    const float4* __restrict__ cpos, const float4* __restrict__ cdir,
+                                                    uint32_t* __restrict__ ccnt, uint32_t* __restrict__ clist,
+                                                    unsigned long long* __restrict__ xq, unsigned long long xcap,
+                                                    unsigned long long* __restrict__ ctr) {
+    constexpr int kW = kTPB / 32;
+    __shared__ TubeTile tiles[kW];
+    __shared__ float4 ppos[kW][32], pdir[kW][32];
+    __shared__ uint32_t pcid[kW][32], pim[kW][32];
+    __shared__ int msp[kW][32];
+    __shared__ uint32_t msm[kW][32];
+    __shared__ uint16_t mq2[kW][64];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    TubeTile& T = tiles[w];
+    unsigned long long tests = 0, ovf = 0, cert = 0, nitem = 0, ntile = 0, nmark = 0, nline = 0;
+    const uint32_t n = min(*nitems, icap);
+    const uint32_t stride = gridDim.x * kW;
+    TItem nxt = blockIdx.x * kW + w < n ? items[blockIdx.x * kW + w] : TItem{0, 0, 0, 0};
+    for (uint32_t it = blockIdx.x * kW + w; it < n; it += stride) {
+        const TItem I = nxt;
+        if (it + stride < n) nxt = items[it + stride];
+        ++nitem;
+        const uint32_t np = I.cnt & 63u, nt = I.cnt >> 6;
+        const Real& Re = reals[find_real(toffs, R, I.cell)];
+        const bool have = (uint32_t)lane < np;
+        uint32_t cid = 0, ipc = 0;
+        float4 pA = make_float4(0, 0, 0, 0), cA = pA;
+        if (have) {
+            const uint32_t e = ent[I.pfirst + lane];
+            cid = e >> kTubeIdShift;
+            ipc = e & 63u;
+            pA = cpos[cid];
+            cA = cdir[cid];
+        }
+        __syncwarp();
+        ppos[w][lane] = pA;
+        pdir[w][lane] = cA;
+        pcid[w][lane] = cid;
+        pim[w][lane] = ipc;
+        int ia[3];
+        img_of(ipc, ia);
+        const float ax = pA.x + ia[0] * Re.L[0], ay = pA.y + ia[1] * Re.L[1], az = pA.z + ia[2] * Re.L[2];
+        const float hA2 = (pA.w * 0.5f + cA.w + Re.eps + cA.w * Re.scf + Re.sep + Re.eps) * 1.000002f + Re.slack;
+        const float hAe = pA.w * 0.5f + cA.w + Re.eps;
+        const float hC = (cA.w * Re.scf + Re.sep + Re.eps) * 1.000002f + 2.0f * Re.slack + 4e-6f * (1.0f + hA2);
+        for (uint32_t b = 0; b < nt; b += kWT) {
+            const uint32_t m = min((uint32_t)kWT, nt - b);
+            if ((uint32_t)lane < m) {
+                const uint32_t e = ent[I.tfirst + b + lane];
+                const uint32_t k = e >> kTubeIdShift;
+                const float4 p = cpos[k], c = cdir[k];
+                int ib[3];
+                img_of(e & 63u, ib);
+                T.p[lane] = p;
+                T.ps[lane] = make_float4(p.x + ib[0] * Re.L[0], p.y + ib[1] * Re.L[1], p.z + ib[2] * Re.L[2],
+                                         (p.w * 0.5f + c.w + Re.eps + c.w * Re.scf) * 1.000002f);
+                T.c[lane] = c;
+                T.id[lane] = k;
+                T.im[lane] = e & 63u;
+            } else {
+                T.ps[lane] = make_float4(kFar, kFar, kFar, 0.0f);
+                T.id[lane] = 0xffffffffu;
+            }
+            __syncwarp();
+            uint32_t mask = 0, emask = 0;  // marked pairs; earlier survivors
+            if (have) {
+                const uint32_t m8 = (m + 7u) & ~7u;
+                for (uint32_t j0 = 0; j0 < m8; j0 += 8) {
+#pragma unroll
+                    for (uint32_t jj = 0; jj < 8; ++jj) {
+                        const uint32_t j = j0 + jj;
+                        const float4 tq = T.ps[j];
+                        const float bx = tq.x - ax, by = tq.y - ay, bz = tq.z - az;
+                        const uint32_t bit = T.id[j] < cid ? (1u << j) : 0u;
+                        emask |= bit;
+                        if (capsule_near(bx, by, bz, cA.x, cA.y, cA.z, hAe, tq.w, hC)) mask |= bit;
+                    }
+                }
+                tests += __popc(emask);
+            }
+            auto keep = [&](int pl, int t) {
+                int img[3];
+                if (!rel_img(pim[w][pl], T.im[t], img)) return false;
+                const float4 dA = pdir[w][pl], cB = T.c[t];
+                return !line_far(ppos[w][pl], dA, T.p[t], cB, img[0] * Re.L[0], img[1] * Re.L[1], img[2] * Re.L[2],
+                                 (cB.w + dA.w) * Re.scf + Re.sep + Re.eps, Re.slack);
+            };
+            ++ntile;
+            nmark += __popc(mask);
+            const int kept_ = for_marked_pairs(mask, lane, msp[w], msm[w], mq2[w], keep, [&](bool valid, int pl, int t) {
+                if (!valid) return;
+                const float4 qA = ppos[w][pl], dA = pdir[w][pl];
+                const float4 pB = T.p[t], cB = T.c[t];
+                int img[3];
+                rel_img(pim[w][pl], T.im[t], img);
+                const float sx = img[0] * Re.L[0], sy = img[1] * Re.L[1], sz = img[2] * Re.L[2];
+                const float thr = (cB.w + dA.w) * Re.scf + Re.sep + Re.eps;
+                if (maybe_near(qA, dA, pB, cB, sx, sy, sz, thr, Re.eps, Re.slack)) {
+                    const uint32_t c = pcid[w][pl];
+                    float t0 = 0.0f, t1 = 0.0f;
+                    if (!Re.typo && certain_hit(qA, dA, pB, cB, sx, sy, sz, thr, Re.eps, Re.slack, &t0, &t1)) {
+                        // listed once: by the cell of the midpoint of the two feet
+                        if (tube_claims(Re, Re.per_gen, I.cell, pim[w][pl], qA, dA, pB, cB, sx, sy, sz, t0, t1)) {
+                            ++cert;
+                            uint32_t slot = atomicAdd(&ccnt[c], 1u);
+                            if (slot < (uint32_t)kConflictCap) clist[(size_t)c * kConflictCap + slot] = T.id[t];
+                            else ++ovf;
+                        }
+                    } else {
+                        xq_push(xq, xcap, &ctr[C_XQ_CONF], xq_pack(c, T.id[t], img));
+                    }
+                }
+            });
+            if (lane == 0) nline += kept_;
+            __syncwarp();
+        }
+    }
+    warp_add_u64(&ctr[C_PAIR_TESTS], tests);
+    warp_add_u64(&ctr[C_OVERFLOW], ovf);
+    warp_add_u64(&ctr[C_CERT], cert);
+    if (lane == 0) {
+        atomicAdd(&ctr[C_G_ITEMS], nitem);
+        atomicAdd(&ctr[C_G_TILES], ntile);
+        atomicAdd(&ctr[C_G_LINE], nline);
+    }
+    warp_add_u64(&ctr[C_G_MARKED], nmark);
+}
+
 // In-order resolution: a surviving candidate is rejected once one of its
 // earlier conflicts is accepted and accepted once all of them are rejected.
 // States only move from ST_ALIVE to a final state, so the passes need no grid
@@ -878,6 +1268,94 @@ __global__ void __launch_bounds__(1024) k_scan_small(const uint32_t* in, uint32_
     }
 }
 
+// Object sources of the tube registrations: placed rods of every realisation
+// (slots beyond a realisation's count take no part), and the round's
+// candidates still alive (compact ids, so the entries follow stream order).
+struct TubeRodSrc {
+    const uint32_t* rodoff;
+    const uint32_t* dcount;
+    int R;
+    const float4* pos;
+    const float4* dir;
+    __device__ bool operator()(uint32_t i, int* r, float4* p, float4* c) const {
+        const int q = find_real(rodoff, R, i);
+        if (i - rodoff[q] >= dcount[q]) return false;
+        *r = q;
+        *p = pos[i];
+        *c = dir[i];
+        return true;
+    }
+};
+struct TubeCandSrc {
+    const uint32_t* creal;
+    const float4* cpos;
+    const float4* cdir;
+    const uint8_t* state;
+    __device__ bool operator()(uint32_t i, int* r, float4* p, float4* c) const {
+        if (state[i] != ST_ALIVE) return false;
+        *r = (int)creal[i];
+        *p = cpos[i];
+        *c = cdir[i];
+        return true;
+    }
+};
+
+// Count, scan, size (one 4-byte read-back), fill.
+template <class Src>
+static nf_status tube_register(Engine& E, uint32_t n, const uint32_t* ntot, int stage, Src src, DBuf<uint32_t>& start,
+                               DBuf<uint32_t>& cur, DBuf<uint32_t>& ent) {
+    const uint32_t nc = E.ntcell;
+    cudaStream_t st = E.st;
+#define NF_CKT(x) do { cudaError_t e_ = (x); if (e_ != cudaSuccess) return E.cuda_fail(e_, #x); } while (0)
+    NF_CKT(start.ensure(nc + 1));
+    NF_CKT(cur.ensure(nc + 1));
+    NF_CKT(cudaMemsetAsync(cur.p, 0, sizeof(uint32_t) * (nc + 1), st));
+    if (n) {
+        NF_LAUNCH(k_treg_count<Src>, grid_for(n, 256), 256, 0, st)(n, ntot, E.dreal.p, stage, src, cur.p);
+        NF_CKT(cudaGetLastError());
+    }
+    nf_status s = E.scan_u32(cur.p, start.p, nc + 1);
+    if (s != NF_OK) return s;
+    s = E.ensure_pinned(16);
+    if (s != NF_OK) return s;
+    uint32_t* h = reinterpret_cast<uint32_t*>(E.hpin);
+    NF_CKT(cudaMemcpyAsync(h, start.p + nc, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+    NF_CKT(cudaStreamSynchronize(st));
+    const uint32_t total = *h;
+    NF_CKT(ent.ensure((size_t)total + 1));
+    NF_CKT(cudaMemsetAsync(cur.p, 0, sizeof(uint32_t) * (nc + 1), st));
+    if (n && total) {
+        NF_LAUNCH(k_treg_fill<Src>, grid_for(n, 256), 256, 0, st)(n, ntot, E.dreal.p, stage, src, start.p, cur.p, ent.p);
+        NF_CKT(cudaGetLastError());
+    }
+#undef NF_CKT
+    return NF_OK;
+}
+
+nf_status Engine::tube_register_rods(int stage) {
+    TubeRodSrc src{rodoff.p, dcount.p, R, pos.p, dir.p};
+    return tube_register(*this, (uint32_t)rod_slots, nullptr, stage, src, trod_start, trod_cur, trod_ent);
+}
+
+nf_status Engine::tube_register_cands(uint64_t slots, const uint32_t* ntot, bool /*alive_only*/) {
+    TubeCandSrc src{creal.p, cpos.p, cdir.p, state.p};
+    return tube_register(*this, (uint32_t)slots, ntot, 0, src, tcnd_start, tcnd_cur, tcnd_ent);
+}
+
+nf_status Engine::tube_items(const uint32_t* pstart, const uint32_t* tstart) {
+    NF_CK(icnt.ensure((size_t)ntcell + 1));
+    NF_CK(tioff.ensure((size_t)ntcell + 1));
+    NF_CK(titems.ensure(tit_cap));
+    NF_LAUNCH(k_titem_count, grid_for((size_t)ntcell + 1, 256), 256, 0, st)(ntcell, pstart, tstart, icnt.p);
+    NF_CK(cudaGetLastError());
+    nf_status s = scan_u32(icnt.p, tioff.p, (size_t)ntcell + 1);
+    if (s != NF_OK) return s;
+    NF_LAUNCH(k_titem_fill, grid_for(ntcell, 256), 256, 0, st)(ntcell, pstart, tstart, tioff.p, titems.p,
+                                                               (uint32_t)titems.cap, ctr.p + C_ITEMS);
+    NF_CK(cudaGetLastError());
+    return NF_OK;
+}
+
 nf_status Engine::scan_u32(const uint32_t* in, uint32_t* out, size_t n) {
     if (n <= kSmallScan) {
         NF_LAUNCH(k_scan_small, 1, 1024, 0, st)(in, out, (uint32_t)n);
@@ -971,6 +1449,7 @@ nf_status Engine::rebuild_cells() {
         NF_CK(cudaGetLastError());
     }
     cells_valid = true;
+    trod_stage = -1;  // the tube registrations of the rods are stale
     return NF_OK;
 }
 
@@ -997,7 +1476,7 @@ static nf_status setup_reals(Engine& E) {
     E.mesh_dirty = false;
     E.hreal.resize(E.R);
     uint32_t coffs = 0;
-    uint64_t roff = 0;
+    uint64_t roff = 0, toffs = 0;
     std::vector<uint32_t> hrodoff(E.R + 1);
     for (int r = 0; r < E.R; ++r) {
         const nf_params& p = E.prm[r];
@@ -1007,6 +1486,9 @@ static nf_status setup_reals(Engine& E) {
         Re.cell_off = coffs;
         Re.ncell = (uint32_t)(Re.n[0] * Re.n[1] * Re.n[2]);
         coffs += Re.ncell;
+        Re.toff = (uint32_t)toffs;
+        toffs += Re.tube ? Re.tncell : 0;
+        if (toffs > 0xfffffff0ull) { E.err = "too many tube cells"; return NF_ERR_PARAM; }
         int64_t tgt = target_count(p);
         if (tgt < 0 || tgt > 0x7fffffff) { E.err = "target count out of range"; return NF_ERR_PARAM; }
         Re.target = (uint32_t)tgt;
@@ -1018,11 +1500,22 @@ static nf_status setup_reals(Engine& E) {
     }
     hrodoff[E.R] = (uint32_t)roff;
     E.ncell = coffs;
+    E.ntcell = (uint32_t)toffs;
+    // the tube sweeps run when every realisation has a tube grid
+    E.tube = E.ntcell > 0;
+    for (int r = 0; r < E.R; ++r) E.tube = E.tube && E.hreal[r].tube;
     E.rod_slots = roff;
 #define NF_CKS(x) do { cudaError_t e_ = (x); if (e_ != cudaSuccess) return E.cuda_fail(e_, #x); } while (0)
     std::vector<uint32_t> hcelloff(E.R + 1);
     for (int r = 0; r < E.R; ++r) hcelloff[r] = E.hreal[r].cell_off;
     hcelloff[E.R] = E.ncell;
+    if (E.tube) {
+        std::vector<uint32_t> ht(E.R + 1);
+        for (int r = 0; r < E.R; ++r) ht[r] = E.hreal[r].toff;
+        ht[E.R] = E.ntcell;
+        NF_CKS(E.toffs.ensure(E.R + 1));
+        NF_CKS(cudaMemcpyAsync(E.toffs.p, ht.data(), sizeof(uint32_t) * (E.R + 1), cudaMemcpyHostToDevice, E.st));
+    }
     NF_CKS(E.celloff.ensure(E.R + 1));
     NF_CKS(cudaMemcpyAsync(E.celloff.p, hcelloff.data(), sizeof(uint32_t) * (E.R + 1), cudaMemcpyHostToDevice, E.st));
     NF_CKS(E.dreal.ensure(E.R));
@@ -1302,8 +1795,10 @@ nf_status Engine::generate() {
         const double two_work = prm[0].two_phase_work != 0 ? prm[0].two_phase_work : 1e10;
         const bool phased = outer_rows && two_work >= 0 && work > two_work;
         NF_CK(cudaMemsetAsync(ctr.p + C_ITEMS, 0, sizeof(unsigned long long), st));
-        s = build_items(cstart.p, rstart.p, 0, slots, total_rods(), phased ? 3 : 0);
-        if (s != NF_OK) return s;
+        if (!tube) {
+            s = build_items(cstart.p, rstart.p, 0, slots, total_rods(), phased ? 3 : 0);
+            if (s != NF_OK) return s;
+        }
         const unsigned xg = (unsigned)(4 * nsm);
         xq_cap = std::max(xq_cap, (size_t)(slots / 8));  // first guess; grown and redone on overflow
         NF_CK(xq.ensure(xq_cap));
@@ -1323,7 +1818,24 @@ nf_status Engine::generate() {
             return NF_OK;
         };
         tstart(KT_OLD);
-        if (total_rods() > 0) {
+        if (tube && total_rods() > 0) {
+            // tube grid: the kept candidates against the placed rods that share a cell
+            if (trod_stage != 0) {
+                s = tube_register_rods(0);
+                if (s != NF_OK) return s;
+                trod_stage = 0;
+            }
+            s = tube_register_cands(slots, ntot, true);
+            if (s != NF_OK) return s;
+            s = tube_items(tcnd_start.p, trod_start.p);
+            if (s != NF_OK) return s;
+            NF_LAUNCH(k_tube_old, persistent_grid(k_tube_old), kTPB, 0, st)(dreal.p, R, toffs.p, titem_count(),
+                                                    (uint32_t)titems.cap, titems.p, tcnd_ent.p, cpos.p, cdir.p,
+                                                    trod_ent.p, pos.p, dir.p, state.p, xq.p, xq.cap, ctr.p);
+            NF_CK(cudaGetLastError());
+            NF_LAUNCH(k_old_exact, xg, 256, 0, st)(dreal.p, xq.p, nullptr, ctr.p + C_XQ_OLD, xq.cap, cpos.p, cdir.p,
+                                                   creal.p, pos.p, dir.p, state.p, ctr.p);
+        } else if (total_rods() > 0) {
             NF_LAUNCH(k_old_tiles, persistent_grid(k_old_tiles), kTPB, 0, st)(dreal.p, item_count(), (uint32_t)items.cap, items.p, cperm.p, gpos.p,
                                                     gdir.p, spos.p, sdir.p, state.p, xq.p, xq.cap, ctr.p);
             NF_CK(cudaGetLastError());
@@ -1332,7 +1844,7 @@ nf_status Engine::generate() {
         }
         NF_CK(cudaGetLastError());
         for (int ring : {5, 6, 2}) {  // the survivors against the next inner rows, the inner corners, the outer rows
-            if (!phased) break;
+            if (!phased || tube) break;
             NF_CK(cudaMemcpyAsync(ctr.p + C_XQ_MARK, ctr.p + C_XQ_OLD, sizeof(unsigned long long),
                                   cudaMemcpyDeviceToDevice, st));
             s = bin_survivors();
@@ -1347,15 +1859,28 @@ nf_status Engine::generate() {
             NF_CK(cudaGetLastError());
         }
         tstop(KT_OLD);
-        s = bin_survivors();
-        if (s != NF_OK) return s;
-        s = build_items(astart.p, astart.p, 0, slots, slots);
-        if (s != NF_OK) return s;
+        if (tube) {  // the survivors, registered on the tube grid
+            s = tube_register_cands(slots, ntot, true);
+            if (s != NF_OK) return s;
+            s = tube_items(tcnd_start.p, tcnd_start.p);
+            if (s != NF_OK) return s;
+        } else {
+            s = bin_survivors();
+            if (s != NF_OK) return s;
+            s = build_items(astart.p, astart.p, 0, slots, slots);
+            if (s != NF_OK) return s;
+        }
         NF_CK(cudaMemsetAsync(ctr.p + C_OVERFLOW, 0, sizeof(unsigned long long), st));
         NF_CK(cudaMemsetAsync(ccnt.p, 0, sizeof(uint32_t) * slots, st));
         tstart(KT_CONF);
-        NF_LAUNCH(k_conf_tiles, persistent_grid(k_conf_tiles), kTPB, 0, st)(dreal.p, item_count(), (uint32_t)items.cap, items.p, aperm.p, apos.p,
+        if (tube) {
+            NF_LAUNCH(k_tube_conf, persistent_grid(k_tube_conf), kTPB, 0, st)(dreal.p, R, toffs.p, titem_count(),
+                                                    (uint32_t)titems.cap, titems.p, tcnd_ent.p, cpos.p, cdir.p,
+                                                    ccnt.p, clist.p, xq2.p, xq2.cap, ctr.p);
+        } else {
+            NF_LAUNCH(k_conf_tiles, persistent_grid(k_conf_tiles), kTPB, 0, st)(dreal.p, item_count(), (uint32_t)items.cap, items.p, aperm.p, apos.p,
                                                  adir.p, ccnt.p, clist.p, xq2.p, xq2.cap, ctr.p);
+        }
         NF_CK(cudaGetLastError());
         NF_LAUNCH(k_conf_exact, xg, 256, 0, st)(dreal.p, xq2.p, ctr.p + C_XQ_CONF, xq2.cap, cpos.p, cdir.p, creal.p,
                                                 ccnt.p, clist.p, ctr.p);
@@ -1397,8 +1922,13 @@ nf_status Engine::generate() {
             NF_CK(cudaMemcpyAsync(hout, recn.p, sizeof(uint64_t) * 2 * R, cudaMemcpyDeviceToHost, st));
             NF_CK(cudaMemcpyAsync(hmeta, meta.p, sizeof(uint32_t) * 4 * R, cudaMemcpyDeviceToHost, st));
             NF_CK(cudaStreamSynchronize(st));
-            if (hv[6] > items.cap) {  // work list too small: grow it and redo the round
+            if (!tube && hv[6] > items.cap) {  // work list too small: grow it and redo the round
                 it_cap = (size_t)(hv[6] * 1.25) + 4096;
+                redo = true;
+                break;
+            }
+            if (tube && hv[6] > titems.cap) {
+                tit_cap = (size_t)(hv[6] * 1.25) + 4096;
                 redo = true;
                 break;
             }

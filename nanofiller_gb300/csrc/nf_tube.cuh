@@ -1,0 +1,178 @@
+// nf_tube.cuh -- the tube grid of the pair sweeps.
+//
+// Two rods whose reference distance is below a threshold thr have points P_A,
+// P_B on their axis segments (extended to |t| <= l/2 + a + eps, where the
+// reference routine takes its points) with |P_A - P_B| < thr; the midpoint of
+// P_A and P_B lies within thr/2 of both segments. So if every object is
+// registered in each cell of a grid that its segment, dilated by
+// trho >= thr_max / 2, touches, every pair within reach shares a cell, and
+// testing the pairs registered together in each cell finds all of them. For
+// rods of length l in cells of edge e ~ l/5 an object registers in about
+// 2 l / e + 1 cells holding ~24 registrations each, so a probe meets ~200
+// targets instead of the ~4 000 of a 5 x 5 x 5 stencil of cells of edge
+// reach / 2 at 2 % volume fraction.
+//
+// A pair can share several cells, so it can be tested more than once: the
+// boolean hard-core tests do not mind; the conflict lists drop repeats on
+// insertion; the contact records are deduplicated by their sort.
+//
+// Registration entry: object id << 6 | image code, the image (x, y, z in
+// -1..1, 2 bits each, +1) of the object's copy that the cell holds (on a
+// periodic axis an object near a face also registers in the cells across
+// it). Open axes have margin cells beyond both faces instead.
+#pragma once
+#include <cstdint>
+
+#include "nf_common.cuh"
+
+namespace nf {
+
+constexpr uint32_t kTubeIdShift = 6;
+
+__host__ __device__ __forceinline__ uint32_t tube_entry(uint32_t id, const int img[3]) {
+    return (id << kTubeIdShift) | (uint32_t)(img[0] + 1) | ((uint32_t)(img[1] + 1) << 2) |
+           ((uint32_t)(img[2] + 1) << 4);
+}
+
+__host__ __device__ __forceinline__ void tube_unpack(uint32_t e, uint32_t* id, int img[3]) {
+    *id = e >> kTubeIdShift;
+    img[0] = (int)(e & 3u) - 1;
+    img[1] = (int)((e >> 2) & 3u) - 1;
+    img[2] = (int)((e >> 4) & 3u) - 1;
+}
+
+// Wraps unwrapped cell index u[3] for the stage's periodic mask: the global
+// cell and the image of the object's copy in it; false when the cell lies
+// beyond the margin of an open axis.
+__device__ __forceinline__ bool tube_cell(const Real& R, int per, const int u[3], uint32_t* cell, int img[3]) {
+    int w[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        const int n = R.tcn[d];
+        int v = u[d], im = 0;
+        if ((per >> d) & 1) {
+            if (v < 0) { v += n; im = 1; }         // the copy shifted by +L lands here
+            else if (v >= n) { v -= n; im = -1; }  // the copy shifted by -L
+            if (v < 0 || v >= n) return false;     // beyond one image (excluded by set-up)
+        } else {
+            v += R.tcm[d];
+            if (v < 0 || v >= n + 2 * R.tcm[d]) return false;
+        }
+        w[d] = v;
+        img[d] = im;
+    }
+    const uint32_t nx = (uint32_t)(R.tcn[0] + 2 * R.tcm[0]), ny = (uint32_t)(R.tcn[1] + 2 * R.tcm[1]);
+    *cell = R.toff + (uint32_t)w[0] + nx * ((uint32_t)w[1] + ny * (uint32_t)w[2]);
+    return true;
+}
+
+// Visits every cell (global id, image of the copy) that the object's axis
+// segment, extended to h = (l/2 + a + eps) and dilated by trho, touches:
+// slabs of cells along the axis's dominant direction, in each the cells of the
+// bounding box of the slab's piece of segment (the slab widened by trho),
+// widened by trho. Every point within trho of the segment is inside a
+// visited cell; no cell is visited twice. FP32 throughout; trho carries
+// margins far above its rounding.
+template <class F>
+__device__ __forceinline__ void tube_walk(const Real& R, int per, const float4& p, const float4& c, F&& visit) {
+    const float h = (p.w * 0.5f + c.w + R.eps) * 1.00001f + R.slack;
+    const float rho = R.trho;
+    const float pc[3] = {p.x, p.y, p.z}, cc[3] = {c.x, c.y, c.z};
+    const float ax = fabsf(c.x), ay = fabsf(c.y), az = fabsf(c.z);
+    const int d = (ax >= ay && ax >= az) ? 0 : (ay >= az ? 1 : 2);
+    const int o1 = d == 0 ? 1 : 0, o2 = d == 2 ? 1 : 2;
+    const float e0 = pc[d] - h * cc[d], e1 = pc[d] + h * cc[d];
+    const float lo = fminf(e0, e1) - rho, hi = fmaxf(e0, e1) + rho;
+    const int s0 = (int)floorf(lo * R.tci[d]), s1 = (int)floorf(hi * R.tci[d]);
+    const float inv_cd = 1.0f / cc[d];
+    for (int s = s0; s <= s1; ++s) {
+        const float x0 = (float)s * R.tce[d] - rho, x1 = (float)(s + 1) * R.tce[d] + rho;
+        const float ta = (x0 - pc[d]) * inv_cd, tb = (x1 - pc[d]) * inv_cd;
+        const float t0 = fmaxf(fminf(ta, tb), -h), t1 = fminf(fmaxf(ta, tb), h);
+        if (t0 > t1) continue;
+        const float qa1 = pc[o1] + t0 * cc[o1], qb1 = pc[o1] + t1 * cc[o1];
+        const float qa2 = pc[o2] + t0 * cc[o2], qb2 = pc[o2] + t1 * cc[o2];
+        const int y0 = (int)floorf((fminf(qa1, qb1) - rho) * R.tci[o1]);
+        const int y1 = (int)floorf((fmaxf(qa1, qb1) + rho) * R.tci[o1]);
+        const int z0 = (int)floorf((fminf(qa2, qb2) - rho) * R.tci[o2]);
+        const int z1 = (int)floorf((fmaxf(qa2, qb2) + rho) * R.tci[o2]);
+        for (int y = y0; y <= y1; ++y)
+            for (int z = z0; z <= z1; ++z) {
+                int u[3];
+                u[d] = s;
+                u[o1] = y;
+                u[o2] = z;
+                uint32_t cell;
+                int img[3];
+                if (tube_cell(R, per, u, &cell, img)) visit(cell, img);
+            }
+    }
+}
+
+// Registration of a set of objects: count pass (per-cell totals) and fill
+// pass (entries at start[cell] + cursor). Src(i, &real, &p, &c) gives object
+// i's realisation and geometry, or false when it takes no part.
+template <class Src>
+__global__ void k_treg_count(uint32_t n, const uint32_t* __restrict__ ntot, const Real* __restrict__ reals,
+                             int stage, Src src, uint32_t* __restrict__ tcount) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (ntot ? *ntot : n)) return;
+    int r;
+    float4 p, c;
+    if (!src(i, &r, &p, &c)) return;
+    const Real& Re = reals[r];
+    tube_walk(Re, stage ? Re.per_con : Re.per_gen, p, c, [&](uint32_t cell, const int*) { atomicAdd(&tcount[cell], 1u); });
+}
+
+template <class Src>
+__global__ void k_treg_fill(uint32_t n, const uint32_t* __restrict__ ntot, const Real* __restrict__ reals, int stage,
+                            Src src, const uint32_t* __restrict__ tstart, uint32_t* __restrict__ tcur,
+                            uint32_t* __restrict__ tent) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (ntot ? *ntot : n)) return;
+    int r;
+    float4 p, c;
+    if (!src(i, &r, &p, &c)) return;
+    const Real& Re = reals[r];
+    tube_walk(Re, stage ? Re.per_con : Re.per_gen, p, c, [&](uint32_t cell, const int* img) {
+        const uint32_t q = tstart[cell] + atomicAdd(&tcur[cell], 1u);
+        tent[q] = tube_entry(i, img);
+    });
+}
+
+// Work items of the tube sweeps: per cell with probes and targets, probe
+// chunks of <= 32 times target segments of <= kTSeg. Item layout (16 B):
+// first probe entry, first target entry, cell, np | nt << 6.
+constexpr uint32_t kTSeg = 128;
+
+static __global__ void k_titem_count(uint32_t ncell, const uint32_t* __restrict__ pstart,
+                              const uint32_t* __restrict__ tstart, uint32_t* __restrict__ icnt) {
+    const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c > ncell) return;
+    if (c == ncell) { icnt[c] = 0; return; }
+    const uint32_t np = pstart[c + 1] - pstart[c], nt = tstart[c + 1] - tstart[c];
+    icnt[c] = (np && nt) ? ((np + 31u) / 32u) * ((nt + kTSeg - 1u) / kTSeg) : 0u;
+}
+
+struct TItem {
+    uint32_t pfirst, tfirst, cell, cnt;  // cnt = np | nt << 6
+};
+
+static __global__ void k_titem_fill(uint32_t ncell, const uint32_t* __restrict__ pstart, const uint32_t* __restrict__ tstart,
+                             const uint32_t* __restrict__ ioff, TItem* __restrict__ items, uint32_t cap,
+                             unsigned long long* __restrict__ imax) {
+    const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c == 0) atomicMax(imax, (unsigned long long)ioff[ncell]);
+    if (c >= ncell) return;
+    const uint32_t k0 = ioff[c], k1 = ioff[c + 1];
+    if (k1 == k0) return;
+    const uint32_t p0 = pstart[c], np = pstart[c + 1] - p0, t0 = tstart[c], nt = tstart[c + 1] - t0;
+    const uint32_t segs = (nt + kTSeg - 1u) / kTSeg;
+    for (uint32_t k = k0; k < k1 && k < cap; ++k) {
+        const uint32_t idx = k - k0, a = (idx / segs) * 32u, b = (idx % segs) * kTSeg;
+        const uint32_t pa = min(32u, np - a), tb = min(kTSeg, nt - b);
+        items[k] = TItem{p0 + a, t0 + b, c, pa | (tb << 6)};
+    }
+}
+
+}  // namespace nf
