@@ -223,6 +223,8 @@ typedef struct nf_gen_stats {
     uint64_t refits;            /* orientation-law refits                     */
     uint64_t thinned;           /* rods removed by thin-out                   */
     uint64_t snapped;           /* snaps of candidates to older rods          */
+    int32_t tube_grid;          /* 1: the pair sweeps ran on the tube grid    */
+    int32_t pad_gen;
 } nf_gen_stats;
 
 typedef struct nf_contact_stats {

@@ -174,6 +174,166 @@ __global__ void __launch_bounds__(256) k_ct_exact(const Real* __restrict__ reals
     warp_add_u64(&ctr[C_CT_FLIPS], flips);
 }
 
+// Contact sweep on the tube grid: rod I against rods J > I registered in the
+// same tube cell (entries carry the image of each rod's copy); pairs the FP32
+// filter cannot rule out are queued with their cell (rod ids, relative image).
+__global__ void __launch_bounds__(kTPB, 6) k_tube_ct(const Real* __restrict__ reals, int R,
+                                                  const uint32_t* __restrict__ toffs,
+                                                  const uint32_t* __restrict__ nitems, uint32_t icap,
+                                                  const TItem* __restrict__ items, const uint32_t* __restrict__ ent,
+                                                  const float4* __restrict__ pos, const float4* __restrict__ dir,
+                                                  unsigned long long* __restrict__ xq, uint32_t* __restrict__ xqc,
+                                                  unsigned long long xcap, unsigned long long* __restrict__ ctr) {
+    constexpr int kW = kTPB / 32;
+    __shared__ TubeTile tiles[kW];
+    __shared__ float4 ppos[kW][32], pdir[kW][32];
+    __shared__ uint32_t pid[kW][32], pim[kW][32];
+    __shared__ int msp[kW][32];
+    __shared__ uint32_t msm[kW][32];
+    __shared__ uint16_t mq2[kW][64];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    TubeTile& T = tiles[w];
+    const float epc = 1e-6f;  // DEV_PRECISION (inc/definitions.h:5)
+    unsigned long long tests = 0;
+    const uint32_t n = min(*nitems, icap);
+    const uint32_t stride = gridDim.x * kW;
+    TItem nxt = blockIdx.x * kW + w < n ? items[blockIdx.x * kW + w] : TItem{0, 0, 0, 0};
+    for (uint32_t it = blockIdx.x * kW + w; it < n; it += stride) {
+        const TItem I = nxt;
+        if (it + stride < n) nxt = items[it + stride];
+        const uint32_t np = I.cnt & 63u, nt = I.cnt >> 6;
+        const Real& Re = reals[find_real(toffs, R, I.cell)];
+        const bool have = (uint32_t)lane < np;
+        uint32_t i = 0xffffffffu, ip = 0;
+        float4 pA = make_float4(0, 0, 0, 0), cA = pA;
+        if (have) {
+            const uint32_t e = ent[I.pfirst + lane];
+            i = e >> kTubeIdShift;
+            ip = e & 63u;
+            pA = pos[i];
+            cA = dir[i];
+        }
+        __syncwarp();
+        ppos[w][lane] = pA;
+        pdir[w][lane] = cA;
+        pid[w][lane] = i;
+        pim[w][lane] = ip;
+        int ia[3];
+        img_of(ip, ia);
+        const float ax = pA.x + ia[0] * Re.L[0], ay = pA.y + ia[1] * Re.L[1], az = pA.z + ia[2] * Re.L[2];
+        const float hA2 = (pA.w * 0.5f + cA.w + epc + cA.w + Re.cut + epc) * 1.000002f + Re.slack;
+        const float hAe = pA.w * 0.5f + cA.w + epc;
+        const float hC = (cA.w + Re.cut + epc) * 1.000002f + 2.0f * Re.slack + 4e-6f * (1.0f + hA2);
+        for (uint32_t b = 0; b < nt; b += kWT) {
+            const uint32_t m = min((uint32_t)kWT, nt - b);
+            if ((uint32_t)lane < m) {
+                const uint32_t e = ent[I.tfirst + b + lane];
+                const uint32_t k = e >> kTubeIdShift;
+                const float4 p = pos[k], c = dir[k];
+                int ib[3];
+                img_of(e & 63u, ib);
+                T.p[lane] = p;
+                T.ps[lane] = make_float4(p.x + ib[0] * Re.L[0], p.y + ib[1] * Re.L[1], p.z + ib[2] * Re.L[2],
+                                         (p.w * 0.5f + c.w + epc + c.w) * 1.000002f);
+                T.c[lane] = c;
+                T.id[lane] = k;
+                T.im[lane] = e & 63u;
+            } else {
+                T.ps[lane] = make_float4(kFar, kFar, kFar, 0.0f);
+                T.id[lane] = 0u;
+            }
+            __syncwarp();
+            uint32_t mask = 0, umask = 0;  // marked pairs; pairs with J > I
+            if (have) {
+                const uint32_t m8 = (m + 7u) & ~7u;
+                for (uint32_t j0 = 0; j0 < m8; j0 += 8) {
+#pragma unroll
+                    for (uint32_t jj = 0; jj < 8; ++jj) {
+                        const uint32_t j = j0 + jj;
+                        const float4 tq = T.ps[j];
+                        const float bx = tq.x - ax, by = tq.y - ay, bz = tq.z - az;
+                        const uint32_t bit = T.id[j] > i ? (1u << j) : 0u;  // each unordered pair once per cell
+                        umask |= bit;
+                        if (capsule_near(bx, by, bz, cA.x, cA.y, cA.z, hAe, tq.w, hC)) mask |= bit;
+                    }
+                }
+                tests += __popc(umask);
+            }
+            auto keep = [&](int pl, int t) {
+                int img[3];
+                if (!rel_img(pim[w][pl], T.im[t], img)) return false;
+                const float4 dA = pdir[w][pl], cB = T.c[t];
+                return !line_far(ppos[w][pl], dA, T.p[t], cB, img[0] * Re.L[0], img[1] * Re.L[1], img[2] * Re.L[2],
+                                 (cB.w + dA.w) + Re.cut + epc, Re.slack);
+            };
+            (void)for_marked_pairs(mask, lane, msp[w], msm[w], mq2[w], keep, [&](bool valid, int pl, int t) {
+                if (!valid) return;
+                const float4 qA = ppos[w][pl], dA = pdir[w][pl];
+                const float4 pB = T.p[t], cB = T.c[t];
+                int img[3];
+                rel_img(pim[w][pl], T.im[t], img);
+                const float thr = (cB.w + dA.w) + Re.cut + epc;
+                if (maybe_near(qA, dA, pB, cB, img[0] * Re.L[0], img[1] * Re.L[1], img[2] * Re.L[2], thr, epc,
+                               Re.slack))
+                    xq_push_cell(xq, xqc, xcap, &ctr[C_XQ], xq_pack(pid[w][pl], T.id[t], img), I.cell);
+            });
+            __syncwarp();
+        }
+    }
+    warp_add_u64(&ctr[C_CT_PAIRS], tests);
+}
+
+// FP64 records of the tube sweep's queue; a pair found in several cells is
+// recorded by the one that holds the midpoint of its two points.
+__global__ void __launch_bounds__(256) k_ct_exact_tube(const Real* __restrict__ reals, int R,
+                                                       const uint32_t* __restrict__ rodoff,
+                                                       const unsigned long long* __restrict__ xq,
+                                                       const uint32_t* __restrict__ xqc,
+                                                       const unsigned long long* __restrict__ count,
+                                                       unsigned long long xcap, const float4* __restrict__ pos,
+                                                       const float4* __restrict__ dir, Rec* __restrict__ rec,
+                                                       unsigned long long cap, unsigned long long* __restrict__ recn,
+                                                       uint32_t* __restrict__ rcnt, unsigned long long* __restrict__ ctr) {
+    const unsigned long long n = min(*count, xcap);
+    const float epc = 1e-6f;
+    unsigned long long exact = 0, flips = 0;
+    for (unsigned long long e = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; e < n;
+         e += (unsigned long long)gridDim.x * blockDim.x) {
+        uint32_t i, j;
+        int img[3];
+        xq_unpack(xq[e], &i, &j, img);
+        const Real& Re = reals[find_real(rodoff, R, i)];
+        const float4 pA = pos[i], cA = dir[i], pB = pos[j], cB = dir[j];
+        ++exact;
+        const RodD a = rodd(pA, cA), b = rodd(pB, cB);
+        const double sx = img[0] * (double)Re.L[0], sy = img[1] * (double)Re.L[1], sz = img[2] * (double)Re.L[2];
+        double t0d, t1d, u0, u1, Dx;
+        double d = ref_distance_d(a, b, sx, sy, sz, (double)epc, false, &t0d, &t1d, &u0, &u1, &Dx);
+        bool h = d < thresh_d(a.a, b.a, 1.0, (double)Re.cut, (double)epc);
+        if (h && !tube_claims_d(Re, Re.per_con, xqc[e], a, b, sx, sy, sz, t0d, t1d)) continue;
+        const float thr = (cB.w + cA.w) + Re.cut + epc;
+        if (ref_hit_f32(pA, cA, pB, cB, img[0] * Re.L[0], img[1] * Re.L[1], img[2] * Re.L[2], epc, thr, false) != h)
+            ++flips;
+        if (!h) continue;
+        unsigned long long slot = atomicAdd(recn, 1ull);
+        atomicAdd(&rcnt[i], 1u);
+        if (slot < cap) {
+            Rec x;
+            x.i = i;
+            x.j = j;
+            x.img[0] = (int8_t)img[0];
+            x.img[1] = (int8_t)img[1];
+            x.img[2] = (int8_t)img[2];
+            x.img[3] = 0;
+            x.flags = 0;
+            x.t0 = t0d; x.t1 = t1d; x.d = d; x.Dx = Dx; x.u0 = u0; x.u1 = u1;
+            rec[slot] = x;
+        }
+    }
+    warp_add_u64(&ctr[C_CT_EXACT], exact);
+    warp_add_u64(&ctr[C_CT_FLIPS], flips);
+}
+
 __global__ void k_rec_scatter(uint32_t n, const Rec* __restrict__ rec, const uint32_t* __restrict__ rpos,
                               uint32_t* __restrict__ rcur, Rec* __restrict__ out) {
     uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
@@ -348,6 +508,92 @@ __global__ void __launch_bounds__(kTPB) k_scr_tiles(const Real* __restrict__ rea
         }
     }
     warp_add_u64(&ctr[C_SCR_PAIRS], tests);
+}
+
+// Screening on the tube grid: the virtual rods of one cell (probe entries)
+// against the rods registered there (target entries); one lane per rod, the
+// warp walks the cell's virtual rods (contacts are sparse). Virtual rods sit
+// at their unwrapped centre; a pair's shift is the relative image of the
+// virtual rod's copy.
+__global__ void __launch_bounds__(kTPB) k_tube_scr(const Real* __restrict__ reals, int R,
+                                                   const uint32_t* __restrict__ toffs,
+                                                   const uint32_t* __restrict__ nitems, uint32_t icap,
+                                                   const TItem* __restrict__ items, const uint32_t* __restrict__ vent,
+                                                   const float4* __restrict__ vpf, const float4* __restrict__ vdf,
+                                                   const uint32_t* __restrict__ rent, const float4* __restrict__ pos,
+                                                   const float4* __restrict__ dir, unsigned long long* __restrict__ xq,
+                                                   unsigned long long xcap, unsigned long long* __restrict__ ctr) {
+    constexpr int kW = kTPB / 32;
+    __shared__ float4 vps[kW][32], vds[kW][32];
+    __shared__ uint32_t vid[kW][32], vim[kW][32];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const float epsf = 1e-6f;
+    unsigned long long tests = 0;
+    const uint32_t n = min(*nitems, icap);
+    for (uint32_t it = blockIdx.x * kW + w; it < n; it += gridDim.x * kW) {
+        const TItem I = items[it];
+        const uint32_t np = I.cnt & 63u, nt = I.cnt >> 6;
+        const Real& Re = reals[find_real(toffs, R, I.cell)];
+        if ((uint32_t)lane < np) {
+            const uint32_t e = vent[I.pfirst + lane];
+            const uint32_t id = e >> kTubeIdShift;
+            vps[w][lane] = vpf[id];
+            vds[w][lane] = vdf[id];
+            vid[w][lane] = id;
+            vim[w][lane] = e & 63u;
+        }
+        __syncwarp();
+        for (uint32_t b = lane; b < nt; b += 32) {
+            const uint32_t e = rent[I.tfirst + b];
+            const uint32_t k = e >> kTubeIdShift, ir = e & 63u;
+            const float4 pR = pos[k], cR = dir[k];
+            tests += np;
+            for (uint32_t pi = 0; pi < np; ++pi) {
+                int img[3];
+                if (!rel_img(ir, vim[w][pi], img)) continue;
+                const float4 pv = vps[w][pi], cv = vds[w][pi];
+                const float thr = (cv.w + cR.w) + epsf;
+                if (maybe_near(pR, cR, pv, cv, img[0] * Re.L[0], img[1] * Re.L[1], img[2] * Re.L[2], thr, epsf,
+                               Re.slack))
+                    xq_push(xq, xcap, &ctr[C_XQ], xq_pack(vid[w][pi], k, img));
+            }
+        }
+        __syncwarp();
+    }
+    warp_add_u64(&ctr[C_SCR_PAIRS], tests);
+}
+
+// FP64 screening decisions of the tube sweep's queue (virtual rod id, rod id,
+// image of the virtual rod relative to the rod): k_scr_exact's test.
+__global__ void __launch_bounds__(256) k_scr_exact_tube(const Real* __restrict__ reals, int R,
+                                                        const uint32_t* __restrict__ rodoff,
+                                                        const unsigned long long* __restrict__ xq,
+                                                        const unsigned long long* __restrict__ count,
+                                                        unsigned long long xcap, const double* __restrict__ vd,
+                                                        const float4* __restrict__ pos, const float4* __restrict__ dir,
+                                                        Rec* rec, unsigned long long* __restrict__ ctr) {
+    const unsigned long long n = min(*count, xcap);
+    const double eps = (double)1e-6f;
+    unsigned long long exact = 0;
+    for (unsigned long long e = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; e < n;
+         e += (unsigned long long)gridDim.x * blockDim.x) {
+        uint32_t id, p;
+        int img[3];
+        xq_unpack(xq[e], &id, &p, img);
+        volatile uint32_t* vflag = &rec[id].flags;
+        if (*vflag & 1u) continue;
+        const Real& Re = reals[find_real(rodoff, R, rec[id].i)];
+        const double* o = vd + (size_t)kVD * id;
+        const RodD V{o[0], o[1], o[2], o[3], o[4], o[5], o[6], o[7]};
+        const RodD Rr = rodd(pos[p], dir[p]);
+        ++exact;
+        double u1, t0d, t1d, u0;
+        double d = ref_distance_d(Rr, V, img[0] * (double)Re.L[0], img[1] * (double)Re.L[1],
+                                  img[2] * (double)Re.L[2], eps, false, &t0d, &t1d, &u0, &u1, nullptr);
+        bool h = d < thresh_d(Rr.a, V.a, 1.0, 0.0, eps);
+        if (h && dsub(ddiv(V.l, 2.0), dabs(u1)) > dadd(V.a, eps)) atomicOr(&rec[id].flags, 1u);
+    }
+    warp_add_u64(&ctr[C_SCR_EXACT], exact);
 }
 
 __global__ void __launch_bounds__(256) k_scr_exact(const Real* __restrict__ reals, int R,
@@ -631,6 +877,24 @@ __global__ void k_final_elec(uint32_t nslot, int R, const uint32_t* __restrict__
         if (e_ != cudaSuccess) return cuda_fail(e_, #x);    \
     } while (0)
 
+// Virtual rods of the screening as objects of the tube registration: the
+// FP32 copy at the unwrapped centre; zero-length segments take no part.
+struct TubeVirtSrc {
+    const uint32_t* vcell;
+    const Rec* rec;
+    const uint32_t* rodoff;
+    int R;
+    const float4* vpf;
+    const float4* vdf;
+    __device__ bool operator()(uint32_t i, int* r, float4* p, float4* c) const {
+        if (vcell[i] == 0xffffffffu) return false;
+        *r = find_real(rodoff, R, rec[i].i);
+        *p = vpf[i];
+        *c = vdf[i];
+        return true;
+    }
+};
+
 nf_status Engine::contacts() {
     if (!cells_valid || rod_slots == 0) { err = "no rods: generate or set rods first"; return NF_ERR_STATE; }
     cudaEvent_t e0, e1;
@@ -652,16 +916,33 @@ nf_status Engine::contacts() {
     for (int attempt = 0; attempt < 5 && !done; ++attempt) {
         if (!items_ok) {
             NF_CK(cudaMemsetAsync(ctr.p + C_ITEMS, 0, sizeof(unsigned long long), st));
-            s = build_items(rstart.p, rstart.p, 1, nrods, nrods);
+            if (tube) {
+                if (trod_stage != 1) {
+                    s = tube_register_rods(1);
+                    if (s != NF_OK) return s;
+                    trod_stage = 1;
+                }
+                s = tube_items(trod_start.p, trod_start.p);
+            } else {
+                s = build_items(rstart.p, rstart.p, 1, nrods, nrods);
+            }
             if (s != NF_OK) return s;
         }
         NF_CK(rec.ensure(cap));
         NF_CK(xq.ensure(xq_cap));
+        if (tube) NF_CK(xqc.ensure(xq.cap));
         NF_CK(cudaMemsetAsync(rcnt.p, 0, sizeof(uint32_t) * (nslot + 1), st));
         NF_CK(cudaMemsetAsync(recn.p, 0, sizeof(unsigned long long), st));
         NF_CK(cudaMemsetAsync(ctr.p + C_XQ, 0, sizeof(unsigned long long), st));
         tstart(KT_CTPAIRS);
-        if (nrods) {
+        if (nrods && tube) {
+            NF_LAUNCH(k_tube_ct, persistent_grid(k_tube_ct), kTPB, 0, st)(dreal.p, R, toffs.p, titem_count(),
+                                                   (uint32_t)titems.cap, titems.p, trod_ent.p, pos.p, dir.p, xq.p,
+                                                   xqc.p, xq.cap, ctr.p);
+            NF_CK(cudaGetLastError());
+            NF_LAUNCH(k_ct_exact_tube, xg, 256, 0, st)(dreal.p, R, rodoff.p, xq.p, xqc.p, ctr.p + C_XQ, xq.cap,
+                                                       pos.p, dir.p, rec.p, rec.cap, recn.p, rcnt.p, ctr.p);
+        } else if (nrods) {
             NF_LAUNCH(k_ct_tiles, persistent_grid(k_ct_tiles), kTPB, 0, st)(dreal.p, item_count(), (uint32_t)items.cap, items.p, spos.p, sdir.p,
                                                    sid.p, xq.p, xq.cap, ctr.p);
             NF_CK(cudaGetLastError());
@@ -670,12 +951,15 @@ nf_status Engine::contacts() {
         }
         NF_CK(cudaGetLastError());
         tstop(KT_CTPAIRS);
-        unsigned long long hv[3] = {0, 0, 0};
+        unsigned long long hv[4] = {0, 0, 0, 0};
         NF_CK(cudaMemcpyAsync(&hv[0], recn.p, sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
         NF_CK(cudaMemcpyAsync(&hv[1], ctr.p + C_XQ, sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
         NF_CK(cudaMemcpyAsync(&hv[2], ctr.p + C_ITEMS, sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
+        NF_CK(cudaMemcpyAsync(&hv[3], ctr.p + C_TUBE_OVF, sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
         NF_CK(cudaStreamSynchronize(st));
-        if (hv[2] > items.cap) { it_cap = (size_t)(hv[2] * 1.25) + 4096; items_ok = false; continue; }
+        if (hv[3]) { err = "tube registration beyond its bound"; return NF_ERR_OVERFLOW; }
+        if (!tube && hv[2] > items.cap) { it_cap = (size_t)(hv[2] * 1.25) + 4096; items_ok = false; continue; }
+        if (tube && hv[2] > titems.cap) { tit_cap = (size_t)(hv[2] * 1.25) + 4096; items_ok = false; continue; }
         items_ok = true;
         if (hv[1] > xq.cap) { xq_cap = (size_t)(hv[1] * 1.25) + 1024; continue; }
         if (hv[0] <= rec.cap) { cap = hv[0]; tbytes(KT_CTPAIRS, 36.0 * nrods + 64.0 * hv[0], 0); done = true; }
@@ -711,27 +995,45 @@ nf_status Engine::contacts() {
             NF_LAUNCH(k_vbin, grid_for(nrec, 256), 256, 0, st)(nrec, vcell.p, vstart.p, vcur.p, vperm.p);
             NF_CK(cudaGetLastError());
             bool vitems_ok = false, vdone = false;
+            if (tube) {  // virtual rods on the tube grid, against the rods' stage-1 registrations
+                TubeVirtSrc vsrc{vcell.p, rec2.p, rodoff.p, R, vpf.p, vdf.p};
+                s = tube_register_objects(nrec, vsrc);
+                if (s != NF_OK) return s;
+            }
             for (int attempt = 0; attempt < 4 && !vdone; ++attempt) {
                 if (!vitems_ok) {
                     NF_CK(cudaMemsetAsync(ctr.p + C_ITEMS, 0, sizeof(unsigned long long), st));
-                    s = build_items(vstart.p, rstart.p, 1, nrec, nrods);
+                    s = tube ? tube_items(tcnd_start.p, trod_start.p) : build_items(vstart.p, rstart.p, 1, nrec, nrods);
                     if (s != NF_OK) return s;
                 }
                 NF_CK(xq.ensure(xq_cap));
                 NF_CK(cudaMemsetAsync(ctr.p + C_XQ, 0, sizeof(unsigned long long), st));
-                NF_LAUNCH(k_scr_tiles, persistent_grid(k_scr_tiles), kTPB, 0, st)(dreal.p, item_count(), (uint32_t)items.cap, items.p, vperm.p, vdbl.p,
-                                                        vpf.p, vdf.p, spos.p, sdir.p, xq.p, xq.cap, ctr.p);
+                if (tube) {
+                    NF_LAUNCH(k_tube_scr, persistent_grid(k_tube_scr), kTPB, 0, st)(dreal.p, R, toffs.p, titem_count(),
+                                                        (uint32_t)titems.cap, titems.p, tcnd_ent.p, vpf.p, vdf.p,
+                                                        trod_ent.p, pos.p, dir.p, xq.p, xq.cap, ctr.p);
+                    NF_CK(cudaGetLastError());
+                    NF_LAUNCH(k_scr_exact_tube, xg, 256, 0, st)(dreal.p, R, rodoff.p, xq.p, ctr.p + C_XQ, xq.cap,
+                                                                vdbl.p, pos.p, dir.p, rec2.p, ctr.p);
+                } else {
+                    NF_LAUNCH(k_scr_tiles, persistent_grid(k_scr_tiles), kTPB, 0, st)(dreal.p, item_count(), (uint32_t)items.cap, items.p, vperm.p, vdbl.p,
+                                                            vpf.p, vdf.p, spos.p, sdir.p, xq.p, xq.cap, ctr.p);
+                    NF_CK(cudaGetLastError());
+                    NF_LAUNCH(k_scr_exact, xg, 256, 0, st)(dreal.p, R, rodoff.p, xq.p, ctr.p + C_XQ, xq.cap, vdbl.p,
+                                                           spos.p, sdir.p, rec2.p, ctr.p);
+                }
                 NF_CK(cudaGetLastError());
-                NF_LAUNCH(k_scr_exact, xg, 256, 0, st)(dreal.p, R, rodoff.p, xq.p, ctr.p + C_XQ, xq.cap, vdbl.p,
-                                                       spos.p, sdir.p, rec2.p, ctr.p);
-                NF_CK(cudaGetLastError());
-                unsigned long long nq[2] = {0, 0};
+                unsigned long long nq[3] = {0, 0, 0};
                 NF_CK(cudaMemcpyAsync(&nq[0], ctr.p + C_XQ, sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
                 NF_CK(cudaMemcpyAsync(&nq[1], ctr.p + C_ITEMS, sizeof(unsigned long long), cudaMemcpyDeviceToHost,
                                       st));
+                NF_CK(cudaMemcpyAsync(&nq[2], ctr.p + C_TUBE_OVF, sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                                      st));
                 NF_CK(cudaStreamSynchronize(st));
+                if (nq[2]) { err = "tube registration beyond its bound"; return NF_ERR_OVERFLOW; }
                 // Screening flags are idempotent: an incomplete pass is simply rerun.
-                if (nq[1] > items.cap) { it_cap = (size_t)(nq[1] * 1.25) + 4096; vitems_ok = false; }
+                if (tube && nq[1] > titems.cap) { tit_cap = (size_t)(nq[1] * 1.25) + 4096; vitems_ok = false; }
+                else if (!tube && nq[1] > items.cap) { it_cap = (size_t)(nq[1] * 1.25) + 4096; vitems_ok = false; }
                 else if (nq[0] > xq.cap) { vitems_ok = true; xq_cap = (size_t)(nq[0] * 1.25) + 1024; }
                 else vdone = true;
             }

@@ -34,7 +34,8 @@ enum CandState : uint8_t { ST_NONE = 0, ST_REJ_OLD = 1, ST_ALIVE = 2, ST_ACC = 3
 enum Ctr {
     C_PAIR_TESTS = 0, C_EXACT, C_FLIPS, C_OVERFLOW, C_UNDECIDED,
     C_CT_PAIRS, C_CT_EXACT, C_CT_FLIPS, C_CT_RECORDS, C_SCR_PAIRS, C_SCR_EXACT,
-    C_CG_ITERS, C_XQ_OLD, C_XQ_CONF, C_XQ, C_CERT, C_ITEMS, C_G_ITEMS, C_G_TILES, C_G_MARKED, C_G_LINE, C_XQ_MARK, C_NCTR
+    C_CG_ITERS, C_XQ_OLD, C_XQ_CONF, C_XQ, C_CERT, C_ITEMS, C_G_ITEMS, C_G_TILES, C_G_MARKED, C_G_LINE, C_XQ_MARK,
+    C_TUBE_OVF, C_NCTR
 };
 
 // Device buffer owned by its object: freed by release() or the destructor
@@ -150,6 +151,7 @@ struct Engine {
     DBuf<Item> items;            // work list of the pair kernels
     size_t it_cap = 1 << 20;     // its capacity (grown on overflow)
     DBuf<unsigned long long> xq, xq2;  // exact queues (pairs left to FP64)
+    DBuf<uint32_t> xqc;                // tube cell of each contact-queue entry
     size_t xq_cap = 1 << 16;
     DBuf<uint32_t> icnt, ioff, celloff;
     DBuf<uint8_t> state;
@@ -163,6 +165,7 @@ struct Engine {
     // CSR over ntcell cells, and the work list of a tube sweep
     bool tube = false;
     uint32_t ntcell = 0;
+    uint32_t tube_regs_max = 0;             // registrations of one object at most
     int trod_stage = -1;                    // stage of the current rod registrations (-1: stale)
     DBuf<uint32_t> toffs;                   // R + 1 prefix of tube cells
     DBuf<uint32_t> trod_start, trod_cur, trod_ent;
@@ -302,6 +305,9 @@ struct Engine {
     nf_status tube_register_rods(int stage);
     nf_status tube_register_cands(uint64_t slots, const uint32_t* ntot, bool alive_only);
     nf_status tube_items(const uint32_t* pstart, const uint32_t* tstart);
+    // Registers objects [0, n) of any source (stage-1 periodicity) into tcnd_*.
+    template <class Src>
+    nf_status tube_register_objects(uint32_t n, Src src);
     const uint32_t* titem_count() const { return tioff.p + ntcell; }
     // Pinned host block for the per-round read-backs.
     uint8_t* hpin = nullptr;
@@ -320,6 +326,41 @@ struct Engine {
     }
     uint64_t total_rods() const;
 };
+
+// Count, scan, fill.
+template <class Src>
+inline nf_status tube_register(Engine& E, uint32_t n, const uint32_t* ntot, int stage, Src src, DBuf<uint32_t>& start,
+                               DBuf<uint32_t>& cur, DBuf<uint32_t>& ent) {
+    const uint32_t nc = E.ntcell;
+    cudaStream_t st = E.st;
+#define NF_CKT(x) do { cudaError_t e_ = (x); if (e_ != cudaSuccess) return E.cuda_fail(e_, #x); } while (0)
+    NF_CKT(start.ensure(nc + 1));
+    NF_CKT(cur.ensure(nc + 1));
+    NF_CKT(cudaMemsetAsync(cur.p, 0, sizeof(uint32_t) * (nc + 1), st));
+    if (n) {
+        NF_LAUNCH(k_treg_count<Src>, (unsigned)((n + 255) / 256), 256, 0, st)(n, ntot, E.dreal.p, stage, src, cur.p);
+        NF_CKT(cudaGetLastError());
+    }
+    nf_status s = E.scan_u32(cur.p, start.p, nc + 1);
+    if (s != NF_OK) return s;
+    // entries sized by the geometric bound (no read-back); an entry beyond it
+    // is counted in C_TUBE_OVF, which fails the stage
+    NF_CKT(ent.ensure((size_t)n * E.tube_regs_max + 1));
+    NF_CKT(cudaMemsetAsync(cur.p, 0, sizeof(uint32_t) * (nc + 1), st));
+    if (n) {
+        NF_LAUNCH(k_treg_fill<Src>, (unsigned)((n + 255) / 256), 256, 0, st)(n, ntot, E.dreal.p, stage, src, start.p,
+                                                                             cur.p, ent.p, (uint32_t)ent.cap,
+                                                                             E.ctr.p + C_TUBE_OVF);
+        NF_CKT(cudaGetLastError());
+    }
+#undef NF_CKT
+    return NF_OK;
+}
+
+template <class Src>
+nf_status Engine::tube_register_objects(uint32_t n, Src src) {
+    return tube_register(*this, n, nullptr, 1, src, tcnd_start, tcnd_cur, tcnd_ent);
+}
 
 // Derived realisation descriptor (identical arithmetic to the oracle).
 Real make_real(const nf_params& p, const float* dmesh, int mn[3], double reach);

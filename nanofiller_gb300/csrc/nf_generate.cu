@@ -105,11 +105,12 @@ void set_tn_law(Real& R, const nf_params& p) {
 // screening) with margins far above the FP32 rounding of the walk; the cell
 // edge e solves n (2 l e^2 + e^3) = load, the registrations per cell of n rods
 // per unit volume of mean length l (each registers in ~2 l / e + 1 cells of
-// volume e^3). A periodic axis must be longer than a rod's reach, so that a
-// registration is one image away at most; otherwise the stencil sweeps run.
+// volume e^3), capped so that along a periodic axis a dilated segment spans
+// less than the box edge minus two cells; where no cell of at least 4 trho
+// allows that, the stencil sweeps run.
 void set_tube_grid(Real& R, const nf_params& p) {
     R.tube = 0;
-    if (!(p.tube_load > 0)) return;
+    if (p.tube_load < 0) return;
     double lmax, amax;
     size_bounds(p, &lmax, &amax);
     const double eps = std::max((double)p.tol, (double)1e-6f);
@@ -117,14 +118,12 @@ void set_tube_grid(Real& R, const nf_params& p) {
     const double Lmax = std::max((double)p.box[0], std::max((double)p.box[1], (double)p.box[2]));
     const double rho = 0.5 * thr * 1.0001 + 1e-5 * (1.0 + Lmax) + 8.0 * R.slack;
     const double h = (lmax / 2 + amax + eps) * 1.00001 + R.slack;
-    const int per = (R.per_gen | R.per_con) & 7;
-    for (int d = 0; d < 3; ++d)
-        if (((per >> d) & 1) && !(h + rho < 0.999 * p.box[d])) return;
+    const int per = (R.per_gen | R.per_con) & 7, per_both = R.per_gen & R.per_con & 7;
     const double V = (double)p.box[0] * p.box[1] * p.box[2];
     const double nrod = (double)std::max<int64_t>(target_count(p), 1);
     double lmean = p.l;
     if (p.len_mode == NF_SIZE_LOGNORMAL) lmean = std::min((double)p.len_max, p.l * std::exp(0.5 * p.len_sigma_ln * p.len_sigma_ln));
-    const double load = (double)p.tube_load;
+    const double load = p.tube_load > 0 ? (double)p.tube_load : 24.0;
     const double nd = nrod / V;
     double lo = 4 * rho, hi = std::max(lo, std::min((double)p.box[0], std::min((double)p.box[1], (double)p.box[2])));
     for (int it = 0; it < 60; ++it) {
@@ -132,19 +131,32 @@ void set_tube_grid(Real& R, const nf_params& p) {
         if (nd * (2 * lmean * e * e + e * e * e) > load) hi = e; else lo = e;
     }
     double e = std::max(0.5 * (lo + hi), 4 * rho);
+    // along a periodic axis a dilated segment must span less than the box
+    // edge minus two cells, so that an object reaches a cell through one copy
+    // only (one image away at most)
+    for (int d = 0; d < 3; ++d)
+        if ((per >> d) & 1) e = std::min(e, 0.5 * (0.999 * p.box[d] - 2 * (h + rho)));
+    if (!(e >= 4 * rho)) return;
     for (;;) {
         uint64_t cells = 1;
         for (int d = 0; d < 3; ++d) {
             int n = (int)std::floor((double)p.box[d] / e);
-            R.tcn[d] = n < 1 ? 1 : n;
+            n = n < 1 ? 1 : n;
+            // one copy per cell along a periodic axis (finer cells where the edge rounded up)
+            while (((per >> d) & 1) && !(2 * (h + rho) < 0.999 * p.box[d] - 2.0 * p.box[d] / n) && n < (1 << 20)) ++n;
+            R.tcn[d] = n;
             R.tce[d] = (float)((double)p.box[d] / R.tcn[d]);
             R.tci[d] = (float)((double)R.tcn[d] / (double)p.box[d]);
-            R.tcm[d] = ((per >> d) & 1) ? 0 : (int)std::ceil((h + rho) / R.tce[d]) + 1;
+            // margin cells beyond both faces of an axis open in some stage (an
+            // object near an open face reaches past it)
+            R.tcm[d] = ((per_both >> d) & 1) ? 0 : (int)std::ceil((h + rho) / R.tce[d]) + 1;
             cells *= (uint64_t)(R.tcn[d] + 2 * R.tcm[d]);
         }
         if (cells <= (1ull << 26)) { R.tncell = (uint32_t)cells; break; }
         e *= 1.25;
     }
+    for (int d = 0; d < 3; ++d)
+        if (((per >> d) & 1) && !(2 * (h + rho) < 0.999 * p.box[d] - 2.0 * R.tce[d])) return;
     R.trho = (float)rho;
     R.tube = 1;
 }
@@ -661,6 +673,7 @@ __global__ void __launch_bounds__(kTPB, 6) k_conf_tiles(const Real* __restrict__
 
 __global__ void __launch_bounds__(256) k_conf_exact(const Real* __restrict__ reals,
                                                     const unsigned long long* __restrict__ xq,
+                                                    const uint32_t* __restrict__ xqc,
                                                     const unsigned long long* __restrict__ count,
                                                     unsigned long long cap, const float4* __restrict__ cpos,
                                                     const float4* __restrict__ cdir, const uint32_t* __restrict__ creal,
@@ -677,10 +690,14 @@ __global__ void __launch_bounds__(256) k_conf_exact(const Real* __restrict__ rea
         const float4 pA = cpos[cid], cA = cdir[cid], pB = cpos[j], cB = cdir[j];
         ++exact;
         const RodD a = rodd(pA, cA), b = rodd(pB, cB);
-        double d = ref_distance_d(a, b, img[0] * (double)Re.L[0], img[1] * (double)Re.L[1],
-                                  img[2] * (double)Re.L[2], (double)Re.eps, Re.typo != 0, nullptr, nullptr,
-                                  nullptr, nullptr, nullptr);
+        const double sx = img[0] * (double)Re.L[0], sy = img[1] * (double)Re.L[1], sz = img[2] * (double)Re.L[2];
+        double t0d, t1d;
+        double d = ref_distance_d(a, b, sx, sy, sz, (double)Re.eps, Re.typo != 0, &t0d, &t1d, nullptr, nullptr,
+                                  nullptr);
         bool h = d < thresh_d(a.a, b.a, (double)Re.scf, (double)Re.sep, (double)Re.eps);
+        // tube sweeps: a pair queued from several cells is listed by the one
+        // holding the midpoint of its points
+        if (xqc && h && !tube_claims_d(Re, Re.per_gen, xqc[e], a, b, sx, sy, sz, t0d, t1d)) continue;
         const float thr = (cB.w + cA.w) * Re.scf + Re.sep + Re.eps;
         if (ref_hit_f32(pA, cA, pB, cB, img[0] * Re.L[0], img[1] * Re.L[1], img[2] * Re.L[2], Re.eps, thr,
                         Re.typo != 0) != h)
@@ -704,53 +721,6 @@ __global__ void __launch_bounds__(256) k_conf_exact(const Real* __restrict__ rea
 // works on the copies, the filters and the FP64 queue on the original
 // coordinates with the relative image (target copy image - probe copy image).
 // ---------------------------------------------------------------------------
-struct TubeTile {
-    float4 ps[kWT];  // target copy centre, .w = its reach term of the capsule test
-    float4 p[kWT];   // target centre (original coordinates), .w = length
-    float4 c[kWT];   // axis, .w = radius
-    uint32_t id[kWT];
-    uint32_t im[kWT];  // image code of the target's copy
-};
-
-__device__ __forceinline__ void img_of(uint32_t code, int img[3]) {
-    img[0] = (int)(code & 3u) - 1;
-    img[1] = (int)((code >> 2) & 3u) - 1;
-    img[2] = (int)((code >> 4) & 3u) - 1;
-}
-
-// Relative image of a pair (target copy image - probe copy image); false when
-// it is beyond one box (such a pair is farther apart than a box edge).
-__device__ __forceinline__ bool rel_img(uint32_t ip, uint32_t it, int img[3]) {
-    int a[3], b[3];
-    img_of(ip, a);
-    img_of(it, b);
-    bool ok = true;
-#pragma unroll
-    for (int d = 0; d < 3; ++d) {
-        img[d] = b[d] - a[d];
-        ok = ok && img[d] >= -1 && img[d] <= 1;
-    }
-    return ok;
-}
-
-// Whether the tube cell `cell`, holding the probe's copy of image code ip,
-// is the one cell that claims a pair whose points are P_A = A + t0 cA and
-// P_B = B + img L + t1 cB: the cell of their midpoint in A's frame (both
-// objects are registered there: the midpoint is within the pair's distance /
-// 2 of both segments).
-__device__ __forceinline__ bool tube_claims(const Real& Re, int per, uint32_t cell, uint32_t ip, const float4& pA,
-                                            const float4& cA, const float4& pB, const float4& cB, float sx, float sy,
-                                            float sz, float t0, float t1) {
-    const float mx = 0.5f * ((pA.x + t0 * cA.x) + ((pB.x + sx) + t1 * cB.x));
-    const float my = 0.5f * ((pA.y + t0 * cA.y) + ((pB.y + sy) + t1 * cB.y));
-    const float mz = 0.5f * ((pA.z + t0 * cA.z) + ((pB.z + sz) + t1 * cB.z));
-    const int u[3] = {(int)floorf(mx * Re.tci[0]), (int)floorf(my * Re.tci[1]), (int)floorf(mz * Re.tci[2])};
-    uint32_t c2;
-    int im[3];
-    if (!tube_cell(Re, per, u, &c2, im)) return false;
-    return c2 == cell && tube_entry(0, im) == (ip & 63u);
-}
-
 // Candidates (probe entries) against placed rods (target entries) of one tube
 // cell: cuda_OldExtIsectLB's job (inc/intersection_kern.h:245-364) on the
 // tube grid. Marking, hand-out, certificate and FP64 queue as k_old_tiles.
@@ -911,8 +881,8 @@ __global__ void __launch_bounds__(kTPB, 6) k_tube_conf(const Real* __restrict__ 
                                                     const uint32_t* __restrict__ ent,
                                                     const float4* __restrict__ cpos, const float4* __restrict__ cdir,
                                                     uint32_t* __restrict__ ccnt, uint32_t* __restrict__ clist,
-                                                    unsigned long long* __restrict__ xq, unsigned long long xcap,
-                                                    unsigned long long* __restrict__ ctr) {
+                                                    unsigned long long* __restrict__ xq, uint32_t* __restrict__ xqc,
+                                                    unsigned long long xcap, unsigned long long* __restrict__ ctr) {
     constexpr int kW = kTPB / 32;
     __shared__ TubeTile tiles[kW];
     __shared__ float4 ppos[kW][32], pdir[kW][32];
@@ -1017,7 +987,7 @@ __global__ void __launch_bounds__(kTPB, 6) k_tube_conf(const Real* __restrict__ 
                             else ++ovf;
                         }
                     } else {
-                        xq_push(xq, xcap, &ctr[C_XQ_CONF], xq_pack(c, T.id[t], img));
+                        xq_push_cell(xq, xqc, xcap, &ctr[C_XQ_CONF], xq_pack(c, T.id[t], img), I.cell);
                     }
                 }
             });
@@ -1300,38 +1270,6 @@ struct TubeCandSrc {
     }
 };
 
-// Count, scan, size (one 4-byte read-back), fill.
-template <class Src>
-static nf_status tube_register(Engine& E, uint32_t n, const uint32_t* ntot, int stage, Src src, DBuf<uint32_t>& start,
-                               DBuf<uint32_t>& cur, DBuf<uint32_t>& ent) {
-    const uint32_t nc = E.ntcell;
-    cudaStream_t st = E.st;
-#define NF_CKT(x) do { cudaError_t e_ = (x); if (e_ != cudaSuccess) return E.cuda_fail(e_, #x); } while (0)
-    NF_CKT(start.ensure(nc + 1));
-    NF_CKT(cur.ensure(nc + 1));
-    NF_CKT(cudaMemsetAsync(cur.p, 0, sizeof(uint32_t) * (nc + 1), st));
-    if (n) {
-        NF_LAUNCH(k_treg_count<Src>, grid_for(n, 256), 256, 0, st)(n, ntot, E.dreal.p, stage, src, cur.p);
-        NF_CKT(cudaGetLastError());
-    }
-    nf_status s = E.scan_u32(cur.p, start.p, nc + 1);
-    if (s != NF_OK) return s;
-    s = E.ensure_pinned(16);
-    if (s != NF_OK) return s;
-    uint32_t* h = reinterpret_cast<uint32_t*>(E.hpin);
-    NF_CKT(cudaMemcpyAsync(h, start.p + nc, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
-    NF_CKT(cudaStreamSynchronize(st));
-    const uint32_t total = *h;
-    NF_CKT(ent.ensure((size_t)total + 1));
-    NF_CKT(cudaMemsetAsync(cur.p, 0, sizeof(uint32_t) * (nc + 1), st));
-    if (n && total) {
-        NF_LAUNCH(k_treg_fill<Src>, grid_for(n, 256), 256, 0, st)(n, ntot, E.dreal.p, stage, src, start.p, cur.p, ent.p);
-        NF_CKT(cudaGetLastError());
-    }
-#undef NF_CKT
-    return NF_OK;
-}
-
 nf_status Engine::tube_register_rods(int stage) {
     TubeRodSrc src{rodoff.p, dcount.p, R, pos.p, dir.p};
     return tube_register(*this, (uint32_t)rod_slots, nullptr, stage, src, trod_start, trod_cur, trod_ent);
@@ -1503,7 +1441,16 @@ static nf_status setup_reals(Engine& E) {
     E.ntcell = (uint32_t)toffs;
     // the tube sweeps run when every realisation has a tube grid
     E.tube = E.ntcell > 0;
-    for (int r = 0; r < E.R; ++r) E.tube = E.tube && E.hreal[r].tube;
+    E.tube_regs_max = 0;
+    for (int r = 0; r < E.R; ++r) {
+        E.tube = E.tube && E.hreal[r].tube;
+        if (E.hreal[r].tube) {
+            double lmax, amax;
+            size_bounds(E.prm[r], &lmax, &amax);
+            const double h = (lmax / 2 + amax + std::max((double)E.prm[r].tol, (double)1e-6f)) * 1.00001 + E.hreal[r].slack;
+            E.tube_regs_max = std::max(E.tube_regs_max, tube_regs_bound(E.hreal[r], h));
+        }
+    }
     E.rod_slots = roff;
 #define NF_CKS(x) do { cudaError_t e_ = (x); if (e_ != cudaSuccess) return E.cuda_fail(e_, #x); } while (0)
     std::vector<uint32_t> hcelloff(E.R + 1);
@@ -1765,14 +1712,19 @@ nf_status Engine::generate() {
             s = clusterize(slots, ntot, n_old);
             if (s != NF_OK) return s;
         }
-        s = scan_u32(ccount.p, cstart.p, ncell + 1);
-        if (s != NF_OK) return s;
-        NF_CK(cudaMemsetAsync(ccursor.p, 0, sizeof(uint32_t) * (ncell + 1), st));
-        NF_LAUNCH(k_bin, gb, kBinTPB, 2 * shc, st)((uint32_t)slots, ntot, ccell.p, cstart.p, ccursor.p, cperm.p, ncell);
-        NF_CK(cudaGetLastError());
-        // Cell-sorted candidate copy and the chunk table of this round.
-        NF_LAUNCH(k_gather_pd, gs, 256, 0, st)((uint32_t)slots, ntot, cperm.p, cpos.p, cdir.p, gpos.p, gdir.p);
-        NF_CK(cudaGetLastError());
+        // the tube sweeps read the compact candidates directly; the stencil
+        // sweeps need them binned by cell
+        const bool tube_round = tube && !adapt;
+        if (!tube_round) {
+            s = scan_u32(ccount.p, cstart.p, ncell + 1);
+            if (s != NF_OK) return s;
+            NF_CK(cudaMemsetAsync(ccursor.p, 0, sizeof(uint32_t) * (ncell + 1), st));
+            NF_LAUNCH(k_bin, gb, kBinTPB, 2 * shc, st)((uint32_t)slots, ntot, ccell.p, cstart.p, ccursor.p, cperm.p, ncell);
+            NF_CK(cudaGetLastError());
+            // Cell-sorted candidate copy and the chunk table of this round.
+            NF_LAUNCH(k_gather_pd, gs, 256, 0, st)((uint32_t)slots, ntot, cperm.p, cpos.p, cdir.p, gpos.p, gdir.p);
+            NF_CK(cudaGetLastError());
+        }
         // The old-rod test runs in phases when the grid has outer stencil rows
         // and the round is heavy: every candidate against the centre row
         // (dy = dz = 0: the 5 cells nearest along x, 1/25 of the volume, where
@@ -1874,16 +1826,17 @@ nf_status Engine::generate() {
         NF_CK(cudaMemsetAsync(ccnt.p, 0, sizeof(uint32_t) * slots, st));
         tstart(KT_CONF);
         if (tube) {
+            NF_CK(xqc.ensure(xq2.cap));
             NF_LAUNCH(k_tube_conf, persistent_grid(k_tube_conf), kTPB, 0, st)(dreal.p, R, toffs.p, titem_count(),
                                                     (uint32_t)titems.cap, titems.p, tcnd_ent.p, cpos.p, cdir.p,
-                                                    ccnt.p, clist.p, xq2.p, xq2.cap, ctr.p);
+                                                    ccnt.p, clist.p, xq2.p, xqc.p, xq2.cap, ctr.p);
         } else {
             NF_LAUNCH(k_conf_tiles, persistent_grid(k_conf_tiles), kTPB, 0, st)(dreal.p, item_count(), (uint32_t)items.cap, items.p, aperm.p, apos.p,
                                                  adir.p, ccnt.p, clist.p, xq2.p, xq2.cap, ctr.p);
         }
         NF_CK(cudaGetLastError());
-        NF_LAUNCH(k_conf_exact, xg, 256, 0, st)(dreal.p, xq2.p, ctr.p + C_XQ_CONF, xq2.cap, cpos.p, cdir.p, creal.p,
-                                                ccnt.p, clist.p, ctr.p);
+        NF_LAUNCH(k_conf_exact, xg, 256, 0, st)(dreal.p, xq2.p, tube ? xqc.p : nullptr, ctr.p + C_XQ_CONF, xq2.cap,
+                                                cpos.p, cdir.p, creal.p, ccnt.p, clist.p, ctr.p);
         NF_CK(cudaGetLastError());
         tstop(KT_CONF);
         // Resolution passes (chains are short), then the append, optimistic
@@ -1980,10 +1933,19 @@ nf_status Engine::generate() {
         }
         NF_CK(cudaMemcpyAsync(dcount.p, count.data(), sizeof(uint32_t) * R, cudaMemcpyHostToDevice, st));
         if (any_new) {
-            s = rebuild_cells();
-            if (s != NF_OK) return s;
+            if (tube_round) {  // the cell lists wait for the end of the generation
+                cells_valid = false;
+                trod_stage = -1;
+            } else {
+                s = rebuild_cells();
+                if (s != NF_OK) return s;
+            }
         }
         scale = std::min(1.0, scale * 2.0);
+    }
+    if (!cells_valid) {
+        s = rebuild_cells();
+        if (s != NF_OK) return s;
     }
     NF_CK(cudaEventRecord(e1, st));
     NF_CK(cudaEventSynchronize(e1));
@@ -1993,6 +1955,7 @@ nf_status Engine::generate() {
     cudaEventDestroy(e1);
     unsigned long long hc[C_NCTR];
     NF_CK(cudaMemcpy(hc, ctr.p, sizeof(hc), cudaMemcpyDeviceToHost));
+    if (hc[C_TUBE_OVF]) { err = "tube registration beyond its bound"; return NF_ERR_OVERFLOW; }
     std::memset(&gst, 0, sizeof(gst));
     for (int r = 0; r < R; ++r) {
         gst.candidates_drawn += drawn[r];
@@ -2015,6 +1978,7 @@ nf_status Engine::generate() {
     gst.snapped = ad_snapped;
     gst.target_reached = gst.accepted == gst.target;
     gst.ms = ms;
+    gst.tube_grid = tube ? 1 : 0;
     return NF_OK;
 }
 

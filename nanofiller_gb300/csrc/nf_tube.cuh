@@ -12,9 +12,14 @@
 // targets instead of the ~4 000 of a 5 x 5 x 5 stencil of cells of edge
 // reach / 2 at 2 % volume fraction.
 //
-// A pair can share several cells, so it can be tested more than once: the
-// boolean hard-core tests do not mind; the conflict lists drop repeats on
-// insertion; the contact records are deduplicated by their sort.
+// A pair can share several cells, so it can be tested more than once. The
+// boolean tests (a candidate against placed rods, screening) do not mind. A
+// record (a contact, an in-round conflict) is written only by the cell that
+// holds the midpoint of the pair's two points (tube_claims, tube_claims_d):
+// the points of a pair within reach are closer than the threshold, so their
+// midpoint lies within trho of both segments and its cell holds both
+// objects. FP64-decided conflicts may be listed twice; the in-order
+// resolution reads a list as a set.
 //
 // Registration entry: object id << 6 | image code, the image (x, y, z in
 // -1..1, 2 bits each, +1) of the object's copy that the cell holds (on a
@@ -24,6 +29,11 @@
 #include <cstdint>
 
 #include "nf_common.cuh"
+#include "nf_tiles.cuh"
+
+#include <cooperative_groups.h>
+#include <algorithm>
+#include <cmath>
 
 namespace nf {
 
@@ -109,6 +119,83 @@ __device__ __forceinline__ void tube_walk(const Real& R, int per, const float4& 
     }
 }
 
+// Warp-private staging of one tile of target entries.
+struct TubeTile {
+    float4 ps[kWT];  // target copy centre, .w = its reach term of the capsule test
+    float4 p[kWT];   // target centre (original coordinates), .w = length
+    float4 c[kWT];   // axis, .w = radius
+    uint32_t id[kWT];
+    uint32_t im[kWT];  // image code of the target's copy
+};
+
+__device__ __forceinline__ void img_of(uint32_t code, int img[3]) {
+    img[0] = (int)(code & 3u) - 1;
+    img[1] = (int)((code >> 2) & 3u) - 1;
+    img[2] = (int)((code >> 4) & 3u) - 1;
+}
+
+// Relative image of a pair (target copy image - probe copy image); false when
+// it is beyond one box (such a pair is farther apart than a box edge).
+__device__ __forceinline__ bool rel_img(uint32_t ip, uint32_t it, int img[3]) {
+    int a[3], b[3];
+    img_of(ip, a);
+    img_of(it, b);
+    bool ok = true;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        img[d] = b[d] - a[d];
+        ok = ok && img[d] >= -1 && img[d] <= 1;
+    }
+    return ok;
+}
+
+// Whether the tube cell `cell`, holding the probe's copy of image code ip,
+// is the one cell that claims a pair whose points are P_A = A + t0 cA and
+// P_B = B + img L + t1 cB: the cell of their midpoint in A's frame (both
+// objects are registered there: the midpoint is within the pair's distance /
+// 2 of both segments).
+__device__ __forceinline__ bool tube_claims(const Real& Re, int per, uint32_t cell, uint32_t ip, const float4& pA,
+                                            const float4& cA, const float4& pB, const float4& cB, float sx, float sy,
+                                            float sz, float t0, float t1) {
+    const float mx = 0.5f * ((pA.x + t0 * cA.x) + ((pB.x + sx) + t1 * cB.x));
+    const float my = 0.5f * ((pA.y + t0 * cA.y) + ((pB.y + sy) + t1 * cB.y));
+    const float mz = 0.5f * ((pA.z + t0 * cA.z) + ((pB.z + sz) + t1 * cB.z));
+    const int u[3] = {(int)floorf(mx * Re.tci[0]), (int)floorf(my * Re.tci[1]), (int)floorf(mz * Re.tci[2])};
+    uint32_t c2;
+    int im[3];
+    if (!tube_cell(Re, per, u, &c2, im)) return false;
+    return c2 == cell && tube_entry(0, im) == (ip & 63u);
+}
+
+// Exact-queue append that also records the tube cell the pair came from.
+__device__ __forceinline__ void xq_push_cell(unsigned long long* q, uint32_t* qc, unsigned long long cap,
+                                             unsigned long long* count, unsigned long long e, uint32_t cell) {
+    namespace cg = cooperative_groups;
+    cg::coalesced_group g = cg::coalesced_threads();
+    unsigned long long base = 0;
+    if (g.thread_rank() == 0) base = atomicAdd(count, (unsigned long long)g.size());
+    base = g.shfl(base, 0);
+    const unsigned long long slot = base + g.thread_rank();
+    if (slot < cap) {
+        q[slot] = e;
+        qc[slot] = cell;
+    }
+}
+
+// tube_claims in FP64 (the points of the FP64 routine): the cell of the
+// midpoint of P_A = A + t0 cA and P_B = B + s + t1 cB in A's frame.
+__device__ __forceinline__ bool tube_claims_d(const Real& Re, int per, uint32_t cell, const RodD& A, const RodD& B,
+                                              double sx, double sy, double sz, double t0, double t1) {
+    const double mx = dmul(0.5, dadd(dadd(A.x, dmul(t0, A.cx)), dadd(dadd(B.x, sx), dmul(t1, B.cx))));
+    const double my = dmul(0.5, dadd(dadd(A.y, dmul(t0, A.cy)), dadd(dadd(B.y, sy), dmul(t1, B.cy))));
+    const double mz = dmul(0.5, dadd(dadd(A.z, dmul(t0, A.cz)), dadd(dadd(B.z, sz), dmul(t1, B.cz))));
+    const int u[3] = {(int)floor(mx * (double)Re.tci[0]), (int)floor(my * (double)Re.tci[1]),
+                      (int)floor(mz * (double)Re.tci[2])};
+    uint32_t c2;
+    int im[3];
+    return tube_cell(Re, per, u, &c2, im) && c2 == cell;
+}
+
 // Registration of a set of objects: count pass (per-cell totals) and fill
 // pass (entries at start[cell] + cursor). Src(i, &real, &p, &c) gives object
 // i's realisation and geometry, or false when it takes no part.
@@ -127,7 +214,7 @@ __global__ void k_treg_count(uint32_t n, const uint32_t* __restrict__ ntot, cons
 template <class Src>
 __global__ void k_treg_fill(uint32_t n, const uint32_t* __restrict__ ntot, const Real* __restrict__ reals, int stage,
                             Src src, const uint32_t* __restrict__ tstart, uint32_t* __restrict__ tcur,
-                            uint32_t* __restrict__ tent) {
+                            uint32_t* __restrict__ tent, uint32_t cap, unsigned long long* __restrict__ ovf) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= (ntot ? *ntot : n)) return;
     int r;
@@ -136,8 +223,25 @@ __global__ void k_treg_fill(uint32_t n, const uint32_t* __restrict__ ntot, const
     const Real& Re = reals[r];
     tube_walk(Re, stage ? Re.per_con : Re.per_gen, p, c, [&](uint32_t cell, const int* img) {
         const uint32_t q = tstart[cell] + atomicAdd(&tcur[cell], 1u);
-        tent[q] = tube_entry(i, img);
+        if (q < cap) tent[q] = tube_entry(i, img);
+        else atomicAdd(ovf, 1ull);
     });
+}
+
+// Registrations of one object at most: slabs along the dominant axis d times
+// cells per slab (the slab's piece of segment spans at most tce_d + 2 trho
+// along another axis, widened by trho on both sides).
+__host__ inline uint32_t tube_regs_bound(const Real& R, double hmax) {
+    uint64_t best = 1;
+    for (int d = 0; d < 3; ++d) {
+        const double ed = R.tce[d], rho = R.trho;
+        uint64_t slabs = (uint64_t)std::floor((2 * hmax + 2 * rho) / ed) + 3;
+        uint64_t per = 1;
+        for (int o = 0; o < 3; ++o)
+            if (o != d) per *= (uint64_t)std::floor((ed + 4 * rho) / R.tce[o]) + 3;
+        best = std::max(best, slabs * per);
+    }
+    return (uint32_t)std::min<uint64_t>(best, 1u << 20);
 }
 
 // Work items of the tube sweeps: per cell with probes and targets, probe
