@@ -338,7 +338,9 @@ inline nf_status tube_register(Engine& E, uint32_t n, const uint32_t* ntot, int 
     NF_CKT(cur.ensure(nc + 1));
     NF_CKT(cudaMemsetAsync(cur.p, 0, sizeof(uint32_t) * (nc + 1), st));
     if (n) {
-        NF_LAUNCH(k_treg_count<Src>, (unsigned)((n + 255) / 256), 256, 0, st)(n, ntot, E.dreal.p, stage, src, cur.p);
+        auto kcount = k_treg<Src, false>;
+        NF_LAUNCH(kcount, (unsigned)((n + kRegTPB - 1) / kRegTPB), kRegTPB, 0, st)(
+            n, ntot, E.dreal.p, stage, src, cur.p, nullptr, nullptr, 0u, nullptr);
         NF_CKT(cudaGetLastError());
     }
     nf_status s = E.scan_u32(cur.p, start.p, nc + 1);
@@ -348,9 +350,9 @@ inline nf_status tube_register(Engine& E, uint32_t n, const uint32_t* ntot, int 
     NF_CKT(ent.ensure((size_t)n * E.tube_regs_max + 1));
     NF_CKT(cudaMemsetAsync(cur.p, 0, sizeof(uint32_t) * (nc + 1), st));
     if (n) {
-        NF_LAUNCH(k_treg_fill<Src>, (unsigned)((n + 255) / 256), 256, 0, st)(n, ntot, E.dreal.p, stage, src, start.p,
-                                                                             cur.p, ent.p, (uint32_t)ent.cap,
-                                                                             E.ctr.p + C_TUBE_OVF);
+        auto kfill = k_treg<Src, true>;
+        NF_LAUNCH(kfill, (unsigned)((n + kRegTPB - 1) / kRegTPB), kRegTPB, 0, st)(
+            n, ntot, E.dreal.p, stage, src, cur.p, start.p, ent.p, (uint32_t)ent.cap, E.ctr.p + C_TUBE_OVF);
         NF_CKT(cudaGetLastError());
     }
 #undef NF_CKT

@@ -199,33 +199,101 @@ __device__ __forceinline__ bool tube_claims_d(const Real& Re, int per, uint32_t 
 // Registration of a set of objects: count pass (per-cell totals) and fill
 // pass (entries at start[cell] + cursor). Src(i, &real, &p, &c) gives object
 // i's realisation and geometry, or false when it takes no part.
-template <class Src>
-__global__ void k_treg_count(uint32_t n, const uint32_t* __restrict__ ntot, const Real* __restrict__ reals,
-                             int stage, Src src, uint32_t* __restrict__ tcount) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= (ntot ? *ntot : n)) return;
-    int r;
-    float4 p, c;
-    if (!src(i, &r, &p, &c)) return;
-    const Real& Re = reals[r];
-    tube_walk(Re, stage ? Re.per_con : Re.per_gen, p, c, [&](uint32_t cell, const int*) { atomicAdd(&tcount[cell], 1u); });
-}
+//
+// One object per lane would leave most lanes idle (objects that take no part,
+// segments with fewer slabs than their neighbours), so a warp first lists the
+// slabs of its 32 objects (warp prefix sum of the slab counts) and then hands
+// them out 32 at a time: lane g takes slab g of the list, finds its object by
+// a binary search over the prefix and visits that slab's cells.
+constexpr int kRegTPB = 256;
 
-template <class Src>
-__global__ void k_treg_fill(uint32_t n, const uint32_t* __restrict__ ntot, const Real* __restrict__ reals, int stage,
-                            Src src, const uint32_t* __restrict__ tstart, uint32_t* __restrict__ tcur,
-                            uint32_t* __restrict__ tent, uint32_t cap, unsigned long long* __restrict__ ovf) {
+template <class Src, bool kFill>
+__global__ void __launch_bounds__(kRegTPB) k_treg(uint32_t n, const uint32_t* __restrict__ ntot,
+                                                  const Real* __restrict__ reals, int stage, Src src,
+                                                  uint32_t* __restrict__ tcnt, const uint32_t* __restrict__ tstart,
+                                                  uint32_t* __restrict__ tent, uint32_t cap,
+                                                  unsigned long long* __restrict__ ovf) {
+    constexpr int kW = kRegTPB / 32;
+    __shared__ float4 sp[kW][32], sc[kW][32];
+    __shared__ int sr[kW][32], ss0[kW][32], sex[kW][32];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= (ntot ? *ntot : n)) return;
-    int r;
-    float4 p, c;
-    if (!src(i, &r, &p, &c)) return;
-    const Real& Re = reals[r];
-    tube_walk(Re, stage ? Re.per_con : Re.per_gen, p, c, [&](uint32_t cell, const int* img) {
-        const uint32_t q = tstart[cell] + atomicAdd(&tcur[cell], 1u);
-        if (q < cap) tent[q] = tube_entry(i, img);
-        else atomicAdd(ovf, 1ull);
-    });
+    const uint32_t lim = ntot ? *ntot : n;
+    int r = 0;
+    float4 p = make_float4(0, 0, 0, 0), c = p;
+    int ns = 0, s0 = 0;
+    if (i < lim && src(i, &r, &p, &c)) {
+        const Real& Re = reals[r];
+        const float h = (p.w * 0.5f + c.w + Re.eps) * 1.00001f + Re.slack;
+        const float pc[3] = {p.x, p.y, p.z}, cc[3] = {c.x, c.y, c.z};
+        const float ax = fabsf(c.x), ay = fabsf(c.y), az = fabsf(c.z);
+        const int d = (ax >= ay && ax >= az) ? 0 : (ay >= az ? 1 : 2);
+        const float e0 = pc[d] - h * cc[d], e1 = pc[d] + h * cc[d];
+        s0 = (int)floorf((fminf(e0, e1) - Re.trho) * Re.tci[d]);
+        const int s1 = (int)floorf((fmaxf(e0, e1) + Re.trho) * Re.tci[d]);
+        ns = s1 - s0 + 1;
+    }
+    int incl = ns;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int v = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += v;
+    }
+    const int total = __shfl_sync(0xffffffffu, incl, 31);
+    sp[w][lane] = p;
+    sc[w][lane] = c;
+    sr[w][lane] = r;
+    ss0[w][lane] = s0;
+    sex[w][lane] = incl - ns;
+    __syncwarp();
+    for (int base = 0; base < total; base += 32) {
+        const int g = base + lane;
+        if (g >= total) break;
+        int l = 0;
+#pragma unroll
+        for (int step = 16; step; step >>= 1)
+            if (l + step < 32 && sex[w][l + step] <= g) l += step;
+        const Real& Re = reals[sr[w][l]];
+        const int per = stage ? Re.per_con : Re.per_gen;
+        const float4 q = sp[w][l], cq = sc[w][l];
+        const uint32_t id = i - (uint32_t)lane + (uint32_t)l;
+        const int s = ss0[w][l] + (g - sex[w][l]);
+        // the cells of slab s of object id (tube_walk's slab loop body)
+        const float h = (q.w * 0.5f + cq.w + Re.eps) * 1.00001f + Re.slack;
+        const float rho = Re.trho;
+        const float pc[3] = {q.x, q.y, q.z}, cc[3] = {cq.x, cq.y, cq.z};
+        const float ax = fabsf(cq.x), ay = fabsf(cq.y), az = fabsf(cq.z);
+        const int d = (ax >= ay && ax >= az) ? 0 : (ay >= az ? 1 : 2);
+        const int o1 = d == 0 ? 1 : 0, o2 = d == 2 ? 1 : 2;
+        const float inv_cd = 1.0f / cc[d];
+        const float x0 = (float)s * Re.tce[d] - rho, x1 = (float)(s + 1) * Re.tce[d] + rho;
+        const float ta = (x0 - pc[d]) * inv_cd, tb = (x1 - pc[d]) * inv_cd;
+        const float t0 = fmaxf(fminf(ta, tb), -h), t1 = fminf(fmaxf(ta, tb), h);
+        if (t0 > t1) continue;
+        const float qa1 = pc[o1] + t0 * cc[o1], qb1 = pc[o1] + t1 * cc[o1];
+        const float qa2 = pc[o2] + t0 * cc[o2], qb2 = pc[o2] + t1 * cc[o2];
+        const int y0 = (int)floorf((fminf(qa1, qb1) - rho) * Re.tci[o1]);
+        const int y1 = (int)floorf((fmaxf(qa1, qb1) + rho) * Re.tci[o1]);
+        const int z0 = (int)floorf((fminf(qa2, qb2) - rho) * Re.tci[o2]);
+        const int z1 = (int)floorf((fmaxf(qa2, qb2) + rho) * Re.tci[o2]);
+        for (int y = y0; y <= y1; ++y)
+            for (int z = z0; z <= z1; ++z) {
+                int u[3];
+                u[d] = s;
+                u[o1] = y;
+                u[o2] = z;
+                uint32_t cell;
+                int img[3];
+                if (!tube_cell(Re, per, u, &cell, img)) continue;
+                if (kFill) {
+                    const uint32_t qd = tstart[cell] + atomicAdd(&tcnt[cell], 1u);
+                    if (qd < cap) tent[qd] = tube_entry(id, img);
+                    else atomicAdd(ovf, 1ull);
+                } else {
+                    atomicAdd(&tcnt[cell], 1u);
+                }
+            }
+    }
 }
 
 // Registrations of one object at most: slabs along the dominant axis d times
