@@ -598,9 +598,14 @@ nf_status nf_autotune(nf_handle *h, nf_tune_result *out);
  *      src/cudaMain.cu:147,157) ------------------------------------------ */
 /* Kernel launches issued by this library in this process. */
 uint64_t nf_kernel_launches(void);
-/* Device (cudaMalloc) and pinned host (cudaMallocHost) allocations made by
- * this library in this process. */
+/* Device and pinned host blocks this library requested in this process
+ * (served by cudaMalloc, cudaMallocHost or its own block cache). */
 uint64_t nf_allocations(void);
+/* The library keeps the device blocks that destroyed handles and regrown
+ * buffers give back, per device, and hands them to the next handle of the
+ * process (at most a quarter of the device's memory, at most 64 GiB); this
+ * call returns every cached block to the driver. (No reference counterpart.) */
+nf_status nf_release_cached_memory(void);
 /* Record CUDA events around the hot kernels on the handle's stream. */
 nf_status nf_set_kernel_timing(nf_handle *h, int on);
 /* Totals since timing was enabled for kernel "stream", "old_test",

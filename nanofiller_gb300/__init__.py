@@ -29,7 +29,7 @@ def kernel_launches():
 
 
 def allocations():
-    """Device and pinned host allocations made by the library in this process."""
+    """Device and pinned host blocks the library requested in this process."""
     return int(load().nf_allocations())
 
 

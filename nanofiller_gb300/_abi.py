@@ -188,6 +188,7 @@ SIGNATURES = {
     "nf_write_coo": (_st, [_H, C.c_char_p]),
     "nf_kernel_launches": (C.c_uint64, []),
     "nf_allocations": (C.c_uint64, []),
+    "nf_release_cached_memory": (_st, []),
     "nf_set_kernel_timing": (_st, [_H, C.c_int]),
     "nf_autotune": (_st, [_H, _P(NfTuneResult)]),
     "nf_internal_network": (_st, [_H, _P(NfInternalStats)]),

@@ -17,7 +17,7 @@ SRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libnanofiller_gb300.so")
 CLI = os.path.join(OUT, "nanofiller")
-SOURCES = ["nf_generate.cu", "nf_contacts.cu", "nf_solve.cu", "nf_internal.cu", "nf_ac.cu", "nf_prune.cu", "nf_stats.cu", "nf_align.cu", "nf_api.cu"]
+SOURCES = ["nf_generate.cu", "nf_contacts.cu", "nf_solve.cu", "nf_internal.cu", "nf_ac.cu", "nf_prune.cu", "nf_stats.cu", "nf_align.cu", "nf_api.cu", "nf_alloc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

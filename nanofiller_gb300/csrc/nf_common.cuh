@@ -20,8 +20,8 @@
 namespace nf {
 // Kernel launches issued by this library (process-wide diagnostic).
 extern unsigned long long g_launches;
-// Device (cudaMalloc) and pinned host (cudaMallocHost) allocations made by
-// this library (process-wide diagnostic).
+// Device and pinned host blocks requested by this library, from cudaMalloc,
+// cudaMallocHost or the block cache (process-wide diagnostic).
 extern unsigned long long g_allocs;
 }
 #define NF_LAUNCH(kernel, ...) ++nf::g_launches, kernel<<<__VA_ARGS__>>>

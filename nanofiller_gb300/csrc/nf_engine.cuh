@@ -38,8 +38,15 @@ enum Ctr {
     C_TUBE_OVF, C_NCTR
 };
 
-// Device buffer owned by its object: freed by release() or the destructor
-// (cudaFree waits for the device work that may still use it).
+// Device memory of the library's buffers (nf_alloc.cu): blocks come from a
+// process-wide cache of freed blocks (per device, sizes rounded up to four
+// classes per power of two) before cudaMalloc; a freed block returns to the
+// cache after the device has finished the work that may still use it.
+// *bytes is rounded up to the block's size.
+cudaError_t dev_alloc(void** p, size_t* bytes);
+void dev_free(void* p, size_t bytes);
+
+// Device buffer owned by its object: released by release() or the destructor.
 template <class T>
 struct DBuf {
     T* p = nullptr;
@@ -50,17 +57,15 @@ struct DBuf {
     ~DBuf() { release(); }
     cudaError_t ensure(size_t n) {
         if (n <= cap && p) return cudaSuccess;
-        if (p) cudaFree(p);
-        p = nullptr;
-        cap = 0;
-        size_t m = n < 1 ? 1 : n;
-        ++g_allocs;
-        cudaError_t e = cudaMalloc((void**)&p, m * sizeof(T));
-        if (e == cudaSuccess) cap = m;
+        release();
+        size_t bytes = (n < 1 ? 1 : n) * sizeof(T);
+        cudaError_t e = dev_alloc((void**)&p, &bytes);
+        if (e == cudaSuccess) cap = bytes / sizeof(T);
+        else p = nullptr;
         return e;
     }
     void release() {
-        if (p) cudaFree(p);
+        if (p) dev_free(p, cap * sizeof(T));
         p = nullptr;
         cap = 0;
     }

@@ -125,3 +125,15 @@ def test_batch_handle_reruns_and_guards(gpu, tmp_path):
             b.write_vtk(tmp_path / "x.vtk")
         with pytest.raises(gpu.NanoFillerError):
             b.select(6)
+
+
+def test_block_cache_reuse_and_release(gpu):
+    """Blocks of a destroyed handle serve the next one without changing any
+    result; nf_release_cached_memory hands them back to the driver."""
+    reals = gpu.configs.batched_realisations(8)
+    a, _ = gpu.batch_run(reals)
+    b, _ = gpu.batch_run(reals)
+    assert gpu.load().nf_release_cached_memory() == 0
+    c, _ = gpu.batch_run(reals)
+    key = lambda res: [(x["accepted"], x["contacts"], x["G_eff"]) for x in res]
+    assert key(a) == key(b) == key(c)

@@ -70,8 +70,8 @@ def test_noalloc_limits(gpu):
 
 def test_noalloc_makes_no_allocation(gpu):
     """The property the entry point exists for: after the handle is set up,
-    calls through it leave the library's allocation count unchanged, while
-    the allocating dump allocates its staging buffer on every call."""
+    calls through it leave the library's count of requested blocks unchanged,
+    while the allocating dump requests a staging block on every call."""
     with gpu.Simulation(dict(gpu.configs.SMALL)) as sim:
         sim.stream_noalloc(0, 16)  # device code loaded, handle descriptors on the device
         n0 = gpu.allocations()
