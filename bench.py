@@ -60,6 +60,8 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extras", action="store_true", help="batched: skip the plain pass, large and jammed keys")
     ap.add_argument("--tube-load", type=float, default=None, help="TUBE_LOAD of every realisation (speed only)")
+    ap.add_argument("--param", action="append", default=[], metavar="KEY=VALUE",
+                    help="set an nf_params tuning field of every realisation (speed only), e.g. round_overshoot=3")
     return ap.parse_args()
 
 
@@ -76,6 +78,20 @@ def workload(name, rank):
 
 
 L2_NOTE = "flushed (256 MB write) before every timed step"
+
+# tuning fields that change speed only (the accepted set, contacts and G_eff do not depend on them)
+TUNING = {"tube_load": float, "round_overshoot": float, "two_phase_work": float, "stencil_radius": int,
+          "round_candidates": int}
+
+
+def extra_params(args):
+    out = {}
+    for kv in args.param:
+        k, v = kv.split("=", 1)
+        if k not in TUNING:
+            raise SystemExit(f"--param {k}: only the tuning fields {sorted(TUNING)} may be set")
+        out[k] = TUNING[k](v)
+    return out
 
 
 def workload_config(name, params=None, batch=256):
@@ -496,6 +512,7 @@ def run_batched(args, rank, world):
         p["seed"] += rank * args.batch
         if args.tube_load is not None:
             p["tube_load"] = args.tube_load
+        p.update(extra_params(args))
     stream = torch.cuda.current_stream().cuda_stream
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
     b = nf.Batch(reals, stream=stream)
@@ -653,6 +670,7 @@ def run_ours(args, rank, world):
     params, mesh = workload(args.workload, rank)
     if args.tube_load is not None:
         params["tube_load"] = args.tube_load
+    params.update(extra_params(args))
     stream = torch.cuda.current_stream().cuda_stream
     sim = nf.Simulation(params, mesh=mesh, stream=stream)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")

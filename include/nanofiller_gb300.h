@@ -619,6 +619,14 @@ nf_status nf_format_write_vtk(const char *path, size_t n, const float *x,
                               const float *y, const float *z, const float *cx,
                               const float *cy, const float *cz, const float *l,
                               const float *a, const float *k);
+/* orient.vtk: the directions as points (write_CNT_ORTvtk, src/IO.cpp:77-99). */
+nf_status nf_format_write_ort_vtk(const char *path, size_t n, const float *cx,
+                                  const float *cy, const float *cz);
+/* output.lmp.data: LAMMPS ellipsoids (write_CNTlmp, src/IO.cpp:100-146). */
+nf_status nf_format_write_lmp(const char *path, size_t n, const float *x,
+                              const float *y, const float *z, const float *cx,
+                              const float *cy, const float *cz, const float *l,
+                              const float *a, const float box[3], double density);
 typedef struct nf_state_header {
     float phys_dim[3];
     float edge[3];

@@ -201,6 +201,8 @@ SIGNATURES = {
     "nf_stat_phitheta": (_st, [_H, C.c_int32, C.c_int32, C.c_void_p]),
     "nf_stat_pairs": (_st, [_H, C.c_int32, C.c_void_p, C.c_void_p, C.c_size_t, _P(NfPairStats)]),
     "nf_write_ort_vtk": (_st, [_H, C.c_char_p]),
+    "nf_format_write_ort_vtk": (_st, [C.c_char_p, C.c_size_t] + [C.c_void_p] * 3),
+    "nf_format_write_lmp": (_st, [C.c_char_p, C.c_size_t] + [C.c_void_p] * 9 + [C.c_double]),
     "nf_write_lmp": (_st, [_H, C.c_char_p, C.c_double]),
     "nf_format_write_rho": (_st, [C.c_char_p, C.c_int32, C.c_int32, C.c_void_p]),
     "nf_format_write_gamma": (_st, [C.c_char_p, C.c_int32, C.c_void_p]),

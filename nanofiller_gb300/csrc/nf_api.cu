@@ -752,15 +752,8 @@ nf_status nf_write_ort_vtk(nf_handle* h, const char* path) {
     std::vector<float> f[8];
     nf_status s = host_rods(h, f);
     if (s != NF_OK) return s;
-    std::ofstream o(path, std::ios::out | std::ios::trunc);
-    if (!o) return fail(h, NF_ERR_IO, path);
-    const size_t n = f[0].size();
-    o << "# vtk DataFile Version 2.0" << std::endl << "CUDA generated CNTs" << std::endl << "ASCII" << std::endl
-      << "DATASET UNSTRUCTURED_GRID" << std::endl << "POINTS " << n << " float" << std::endl;
-    for (size_t i = 0; i < n; ++i)
-        o << std::setw(15) << std::setprecision(6) << f[3][i] << std::setw(15) << std::setprecision(6) << f[4][i]
-          << std::setw(15) << std::setprecision(6) << f[5][i] << std::endl;
-    return o.good() ? NF_OK : fail(h, NF_ERR_IO, path);
+    s = nf_format_write_ort_vtk(path, f[0].size(), f[3].data(), f[4].data(), f[5].data());
+    return s == NF_OK ? s : fail(h, s, path);
 }
 
 nf_status nf_write_lmp(nf_handle* h, const char* path, double density) {
@@ -769,29 +762,9 @@ nf_status nf_write_lmp(nf_handle* h, const char* path, double density) {
     std::vector<float> f[8];
     nf_status s = host_rods(h, f);
     if (s != NF_OK) return s;
-    std::ofstream o(path, std::ios::out | std::ios::trunc);
-    if (!o) return fail(h, NF_ERR_IO, path);
-    const size_t n = f[0].size();
-    const float* box = h->E.prm[0].box;
-    o << "CUDA generated aspherical particles" << std::endl << std::endl << n << " atoms" << std::endl
-      << 1 << " atom types" << std::endl << n << " ellipsoids" << std::endl << std::endl
-      << 0.0f << ' ' << box[0] << " xlo xhi" << std::endl << 0.0f << ' ' << box[1] << " ylo yhi" << std::endl
-      << 0.0f << ' ' << box[2] << " zlo zhi" << std::endl << std::endl << "Atoms" << std::endl << std::endl;
-    for (size_t i = 0; i < n; ++i)
-        o << i + 1 << ' ' << 1 << ' ' << 1 << ' ' << (float)density << std::setw(12) << std::setprecision(6)
-          << f[0][i] << std::setw(12) << std::setprecision(6) << f[1][i] << std::setw(12) << std::setprecision(6)
-          << f[2][i] << std::endl;
-    o << std::endl << "Ellipsoids" << std::endl << std::endl;
-    // quaternion of the rotation from x to c: axis (0, -cz, cy), angle acos(cx)
-    for (size_t i = 0; i < n; ++i) {
-        const float cx = f[3][i], cy = f[4][i], cz = f[5][i], l = f[6][i], a = f[7][i];
-        const float sh = sqrtf((1 - cx) / 2);
-        o << i + 1 << std::setw(12) << std::setprecision(6) << l + 2 * a << std::setw(12) << std::setprecision(6)
-          << 2 * a << std::setw(12) << std::setprecision(6) << 2 * a << std::setw(15) << std::setprecision(6)
-          << sqrtf((1 + cx) / 2) << std::setw(15) << std::setprecision(6) << 0.0f << std::setw(15)
-          << std::setprecision(6) << -cz * sh << std::setw(15) << std::setprecision(6) << +cy * sh << std::endl;
-    }
-    return o.good() ? NF_OK : fail(h, NF_ERR_IO, path);
+    s = nf_format_write_lmp(path, f[0].size(), f[0].data(), f[1].data(), f[2].data(), f[3].data(), f[4].data(),
+                            f[5].data(), f[6].data(), f[7].data(), h->E.prm[0].box, density);
+    return s == NF_OK ? s : fail(h, s, path);
 }
 
 nf_status nf_format_write_rho(const char* path, int32_t bx, int32_t by, const uint64_t* hist) {
@@ -1040,6 +1013,47 @@ nf_status nf_kernel_time(nf_handle* h, const char* kernel, double* ms, uint64_t*
 // ---------------------------------------------------------------------------
 // Files.
 // ---------------------------------------------------------------------------
+nf_status nf_format_write_ort_vtk(const char* path, size_t n, const float* cx, const float* cy, const float* cz) {
+    if (!path || (n && (!cx || !cy || !cz))) return NF_ERR_PARAM;
+    // write_CNT_ORTvtk (src/IO.cpp:77-99): the directions as points
+    std::ofstream o(path, std::ios::out | std::ios::trunc);
+    if (!o) return NF_ERR_IO;
+    o << "# vtk DataFile Version 2.0" << std::endl << "CUDA generated CNTs" << std::endl << "ASCII" << std::endl
+      << "DATASET UNSTRUCTURED_GRID" << std::endl << "POINTS " << n << " float" << std::endl;
+    for (size_t i = 0; i < n; ++i)
+        o << std::setw(15) << std::setprecision(6) << cx[i] << std::setw(15) << std::setprecision(6) << cy[i]
+          << std::setw(15) << std::setprecision(6) << cz[i] << std::endl;
+    return o.good() ? NF_OK : NF_ERR_IO;
+}
+
+nf_status nf_format_write_lmp(const char* path, size_t n, const float* x, const float* y, const float* z,
+                              const float* cx, const float* cy, const float* cz, const float* l, const float* a,
+                              const float box[3], double density) {
+    if (!path || !box || (n && (!x || !y || !z || !cx || !cy || !cz || !l || !a))) return NF_ERR_PARAM;
+    // write_CNTlmp (src/IO.cpp:100-146): LAMMPS data file of ellipsoids
+    std::ofstream o(path, std::ios::out | std::ios::trunc);
+    if (!o) return NF_ERR_IO;
+    o << "CUDA generated aspherical particles" << std::endl << std::endl << n << " atoms" << std::endl
+      << 1 << " atom types" << std::endl << n << " ellipsoids" << std::endl << std::endl
+      << 0.0f << ' ' << box[0] << " xlo xhi" << std::endl << 0.0f << ' ' << box[1] << " ylo yhi" << std::endl
+      << 0.0f << ' ' << box[2] << " zlo zhi" << std::endl << std::endl << "Atoms" << std::endl << std::endl;
+    for (size_t i = 0; i < n; ++i)
+        o << i + 1 << ' ' << 1 << ' ' << 1 << ' ' << (float)density << std::setw(12) << std::setprecision(6)
+          << x[i] << std::setw(12) << std::setprecision(6) << y[i] << std::setw(12) << std::setprecision(6)
+          << z[i] << std::endl;
+    o << std::endl << "Ellipsoids" << std::endl << std::endl;
+    // quaternion of the rotation from x to c: axis (0, -cz, cy), angle acos(cx)
+    for (size_t i = 0; i < n; ++i) {
+        const float sh = sqrtf((1 - cx[i]) / 2);
+        o << i + 1 << std::setw(12) << std::setprecision(6) << l[i] + 2 * a[i] << std::setw(12)
+          << std::setprecision(6) << 2 * a[i] << std::setw(12) << std::setprecision(6) << 2 * a[i] << std::setw(15)
+          << std::setprecision(6) << sqrtf((1 + cx[i]) / 2) << std::setw(15) << std::setprecision(6) << 0.0f
+          << std::setw(15) << std::setprecision(6) << -cz[i] * sh << std::setw(15) << std::setprecision(6)
+          << +cy[i] * sh << std::endl;
+    }
+    return o.good() ? NF_OK : NF_ERR_IO;
+}
+
 nf_status nf_format_write_vtk(const char* path, size_t n, const float* x, const float* y, const float* z,
                               const float* cx, const float* cy, const float* cz, const float* l, const float* a,
                               const float* k) {

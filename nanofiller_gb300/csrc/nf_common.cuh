@@ -546,6 +546,41 @@ NF_HD bool maybe_near(const float4& pA, const float4& cA, const float4& pB, cons
         float s = sqrtf(nn);
         if (nb - err > thr_s * s) return false;
     }
+    // (4) separating axis through approximate closest points of the two
+    // extended segments: for any direction u, min over B of u.x - max over A
+    // of u.x bounds d from below (the reference's points lie on these
+    // segments); u from the clamped closest points (Ericson, Real-Time
+    // Collision Detection, 5.1.9) makes the bound nearly tight, and how
+    // accurate those points are does not matter for its validity. Catches
+    // segments whose lines pass close but whose ends stay apart.
+    {
+        const float ha = hA * 1.00001f, hb = hB * 1.00001f;
+        const float d1x = 2.0f * ha * cA.x, d1y = 2.0f * ha * cA.y, d1z = 2.0f * ha * cA.z;
+        const float d2x = 2.0f * hb * cB.x, d2y = 2.0f * hb * cB.y, d2z = 2.0f * hb * cB.z;
+        const float a0x = -ha * cA.x, a0y = -ha * cA.y, a0z = -ha * cA.z;  // A from a0 to a0 + d1
+        const float b0x = bx - hb * cB.x, b0y = by - hb * cB.y, b0z = bz - hb * cB.z;  // B from b0 to b0 + d2
+        const float rx = a0x - b0x, ry = a0y - b0y, rz = a0z - b0z;
+        const float a = d1x * d1x + d1y * d1y + d1z * d1z, e = d2x * d2x + d2y * d2y + d2z * d2z;
+        const float f = d2x * rx + d2y * ry + d2z * rz, c = d1x * rx + d1y * ry + d1z * rz;
+        const float bq = d1x * d2x + d1y * d2y + d1z * d2z;
+        const float den = a * e - bq * bq;
+        float sA = den > 1e-12f * a * e ? fminf(fmaxf((bq * f - c * e) / den, 0.0f), 1.0f) : 0.0f;
+        float tB = e > 0.0f ? (bq * sA + f) / e : 0.0f;
+        if (tB < 0.0f) { tB = 0.0f; sA = a > 0.0f ? fminf(fmaxf(-c / a, 0.0f), 1.0f) : 0.0f; }
+        else if (tB > 1.0f) { tB = 1.0f; sA = a > 0.0f ? fminf(fmaxf((bq - c) / a, 0.0f), 1.0f) : 0.0f; }
+        const float ux = (b0x + d2x * tB) - (a0x + d1x * sA);
+        const float uy = (b0y + d2y * tB) - (a0y + d1y * sA);
+        const float uz = (b0z + d2z * tB) - (a0z + d1z * sA);
+        const float nu = sqrtf(ux * ux + uy * uy + uz * uz);
+        if (nu > 1e-12f) {
+            const float pa0 = ux * a0x + uy * a0y + uz * a0z;
+            const float pa1 = pa0 + (ux * d1x + uy * d1y + uz * d1z);
+            const float pb0 = ux * b0x + uy * b0y + uz * b0z;
+            const float pb1 = pb0 + (ux * d2x + uy * d2y + uz * d2z);
+            const float sep = (fminf(pb0, pb1) - fmaxf(pa0, pa1)) / nu;
+            if (sep * 0.99999f - err - 4e-6f * (ha + hb) > thr_s) return false;
+        }
+    }
     return true;
 }
 

@@ -210,8 +210,8 @@ __global__ void __launch_bounds__(kTPB, 6) k_tube_ct(const Real* __restrict__ re
             const uint32_t e = ent[I.pfirst + lane];
             i = e >> kTubeIdShift;
             ip = e & 63u;
-            pA = pos[i];
-            cA = dir[i];
+            pA = pos[I.pfirst + lane];
+            cA = dir[I.pfirst + lane];
         }
         __syncwarp();
         ppos[w][lane] = pA;
@@ -229,7 +229,7 @@ __global__ void __launch_bounds__(kTPB, 6) k_tube_ct(const Real* __restrict__ re
             if ((uint32_t)lane < m) {
                 const uint32_t e = ent[I.tfirst + b + lane];
                 const uint32_t k = e >> kTubeIdShift;
-                const float4 p = pos[k], c = dir[k];
+                const float4 p = pos[I.tfirst + b + lane], c = dir[I.tfirst + b + lane];
                 int ib[3];
                 img_of(e & 63u, ib);
                 T.p[lane] = p;
@@ -537,8 +537,8 @@ __global__ void __launch_bounds__(kTPB) k_tube_scr(const Real* __restrict__ real
         if ((uint32_t)lane < np) {
             const uint32_t e = vent[I.pfirst + lane];
             const uint32_t id = e >> kTubeIdShift;
-            vps[w][lane] = vpf[id];
-            vds[w][lane] = vdf[id];
+            vps[w][lane] = vpf[I.pfirst + lane];
+            vds[w][lane] = vdf[I.pfirst + lane];
             vid[w][lane] = id;
             vim[w][lane] = e & 63u;
         }
@@ -546,7 +546,7 @@ __global__ void __launch_bounds__(kTPB) k_tube_scr(const Real* __restrict__ real
         for (uint32_t b = lane; b < nt; b += 32) {
             const uint32_t e = rent[I.tfirst + b];
             const uint32_t k = e >> kTubeIdShift, ir = e & 63u;
-            const float4 pR = pos[k], cR = dir[k];
+            const float4 pR = pos[I.tfirst + b], cR = dir[I.tfirst + b];
             tests += np;
             for (uint32_t pi = 0; pi < np; ++pi) {
                 int img[3];
@@ -937,8 +937,8 @@ nf_status Engine::contacts() {
         tstart(KT_CTPAIRS);
         if (nrods && tube) {
             NF_LAUNCH(k_tube_ct, persistent_grid(k_tube_ct), kTPB, 0, st)(dreal.p, R, toffs.p, titem_count(),
-                                                   (uint32_t)titems.cap, titems.p, trod_ent.p, pos.p, dir.p, xq.p,
-                                                   xqc.p, xq.cap, ctr.p);
+                                                   (uint32_t)titems.cap, titems.p, trod_ent.p, trod_pos.p, trod_dir.p,
+                                                   xq.p, xqc.p, xq.cap, ctr.p);
             NF_CK(cudaGetLastError());
             NF_LAUNCH(k_ct_exact_tube, xg, 256, 0, st)(dreal.p, R, rodoff.p, xq.p, xqc.p, ctr.p + C_XQ, xq.cap,
                                                        pos.p, dir.p, rec.p, rec.cap, recn.p, rcnt.p, ctr.p);
@@ -1010,8 +1010,9 @@ nf_status Engine::contacts() {
                 NF_CK(cudaMemsetAsync(ctr.p + C_XQ, 0, sizeof(unsigned long long), st));
                 if (tube) {
                     NF_LAUNCH(k_tube_scr, persistent_grid(k_tube_scr), kTPB, 0, st)(dreal.p, R, toffs.p, titem_count(),
-                                                        (uint32_t)titems.cap, titems.p, tcnd_ent.p, vpf.p, vdf.p,
-                                                        trod_ent.p, pos.p, dir.p, xq.p, xq.cap, ctr.p);
+                                                        (uint32_t)titems.cap, titems.p, tcnd_ent.p, tcnd_pos.p,
+                                                        tcnd_dir.p, trod_ent.p, trod_pos.p, trod_dir.p, xq.p, xq.cap,
+                                                        ctr.p);
                     NF_CK(cudaGetLastError());
                     NF_LAUNCH(k_scr_exact_tube, xg, 256, 0, st)(dreal.p, R, rodoff.p, xq.p, ctr.p + C_XQ, xq.cap,
                                                                 vdbl.p, pos.p, dir.p, rec2.p, ctr.p);

@@ -13,6 +13,7 @@
 //          cell the same way; per-candidate state + a fixed-capacity list of
 //          earlier conflicting candidates.
 #pragma once
+#include <algorithm>
 #include <cstdint>
 #include <string>
 #include <vector>
@@ -170,11 +171,11 @@ struct Engine {
     // CSR over ntcell cells, and the work list of a tube sweep
     bool tube = false;
     uint32_t ntcell = 0;
-    uint32_t tube_regs_max = 0;             // registrations of one object at most
     int trod_stage = -1;                    // stage of the current rod registrations (-1: stale)
     DBuf<uint32_t> toffs;                   // R + 1 prefix of tube cells
     DBuf<uint32_t> trod_start, trod_cur, trod_ent;
     DBuf<uint32_t> tcnd_start, tcnd_cur, tcnd_ent;
+    DBuf<float4> trod_pos, trod_dir, tcnd_pos, tcnd_dir;  // each entry's object geometry
     DBuf<TItem> titems;
     size_t tit_cap = 1 << 20;
     DBuf<uint32_t> tioff;
@@ -335,7 +336,7 @@ struct Engine {
 // Count, scan, fill.
 template <class Src>
 inline nf_status tube_register(Engine& E, uint32_t n, const uint32_t* ntot, int stage, Src src, DBuf<uint32_t>& start,
-                               DBuf<uint32_t>& cur, DBuf<uint32_t>& ent) {
+                               DBuf<uint32_t>& cur, DBuf<uint32_t>& ent, DBuf<float4>& epos, DBuf<float4>& edir) {
     const uint32_t nc = E.ntcell;
     cudaStream_t st = E.st;
 #define NF_CKT(x) do { cudaError_t e_ = (x); if (e_ != cudaSuccess) return E.cuda_fail(e_, #x); } while (0)
@@ -345,19 +346,29 @@ inline nf_status tube_register(Engine& E, uint32_t n, const uint32_t* ntot, int 
     if (n) {
         auto kcount = k_treg<Src, false>;
         NF_LAUNCH(kcount, (unsigned)((n + kRegTPB - 1) / kRegTPB), kRegTPB, 0, st)(
-            n, ntot, E.dreal.p, stage, src, cur.p, nullptr, nullptr, 0u, nullptr);
+            n, ntot, E.dreal.p, stage, src, cur.p, nullptr, nullptr, nullptr, nullptr, 0u, nullptr);
         NF_CKT(cudaGetLastError());
     }
     nf_status s = E.scan_u32(cur.p, start.p, nc + 1);
     if (s != NF_OK) return s;
-    // entries sized by the geometric bound (no read-back); an entry beyond it
-    // is counted in C_TUBE_OVF, which fails the stage
-    NF_CKT(ent.ensure((size_t)n * E.tube_regs_max + 1));
+    // entries (with their objects' geometry, 36 B each) sized by the count:
+    // one 4-byte read-back; an entry beyond the buffers would be counted in
+    // C_TUBE_OVF, which fails the stage
+    s = E.ensure_pinned(16);
+    if (s != NF_OK) return s;
+    uint32_t* h = reinterpret_cast<uint32_t*>(E.hpin);
+    NF_CKT(cudaMemcpyAsync(h, start.p + nc, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+    NF_CKT(cudaStreamSynchronize(st));
+    const size_t total = *h;
+    NF_CKT(ent.ensure(total + 1));
+    NF_CKT(epos.ensure(total + 1));
+    NF_CKT(edir.ensure(total + 1));
     NF_CKT(cudaMemsetAsync(cur.p, 0, sizeof(uint32_t) * (nc + 1), st));
     if (n) {
         auto kfill = k_treg<Src, true>;
         NF_LAUNCH(kfill, (unsigned)((n + kRegTPB - 1) / kRegTPB), kRegTPB, 0, st)(
-            n, ntot, E.dreal.p, stage, src, cur.p, start.p, ent.p, (uint32_t)ent.cap, E.ctr.p + C_TUBE_OVF);
+            n, ntot, E.dreal.p, stage, src, cur.p, start.p, ent.p, epos.p, edir.p,
+            (uint32_t)std::min(ent.cap, std::min(epos.cap, edir.cap)), E.ctr.p + C_TUBE_OVF);
         NF_CKT(cudaGetLastError());
     }
 #undef NF_CKT
@@ -366,7 +377,7 @@ inline nf_status tube_register(Engine& E, uint32_t n, const uint32_t* ntot, int 
 
 template <class Src>
 nf_status Engine::tube_register_objects(uint32_t n, Src src) {
-    return tube_register(*this, n, nullptr, 1, src, tcnd_start, tcnd_cur, tcnd_ent);
+    return tube_register(*this, n, nullptr, 1, src, tcnd_start, tcnd_cur, tcnd_ent, tcnd_pos, tcnd_dir);
 }
 
 // Derived realisation descriptor (identical arithmetic to the oracle).

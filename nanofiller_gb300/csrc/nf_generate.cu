@@ -761,8 +761,8 @@ __global__ void __launch_bounds__(kTPB, 6) k_tube_old(const Real* __restrict__ r
             const uint32_t e = pent[I.pfirst + lane];
             cid = e >> kTubeIdShift;
             ipc = e & 63u;
-            pA = cpos[cid];
-            cA = cdir[cid];
+            pA = cpos[I.pfirst + lane];
+            cA = cdir[I.pfirst + lane];
         }
         bool alive = have && vst[cid] != ST_REJ_OLD;
         __syncwarp();
@@ -786,7 +786,7 @@ __global__ void __launch_bounds__(kTPB, 6) k_tube_old(const Real* __restrict__ r
             if ((uint32_t)lane < m) {
                 const uint32_t e = tent[I.tfirst + b + lane];
                 const uint32_t k = e >> kTubeIdShift;
-                const float4 p = rpos[k], c = rdir[k];
+                const float4 p = rpos[I.tfirst + b + lane], c = rdir[I.tfirst + b + lane];
                 int ib[3];
                 img_of(e & 63u, ib);
                 T.p[lane] = p;
@@ -909,8 +909,8 @@ __global__ void __launch_bounds__(kTPB, 6) k_tube_conf(const Real* __restrict__ 
             const uint32_t e = ent[I.pfirst + lane];
             cid = e >> kTubeIdShift;
             ipc = e & 63u;
-            pA = cpos[cid];
-            cA = cdir[cid];
+            pA = cpos[I.pfirst + lane];
+            cA = cdir[I.pfirst + lane];
         }
         __syncwarp();
         ppos[w][lane] = pA;
@@ -928,7 +928,7 @@ __global__ void __launch_bounds__(kTPB, 6) k_tube_conf(const Real* __restrict__ 
             if ((uint32_t)lane < m) {
                 const uint32_t e = ent[I.tfirst + b + lane];
                 const uint32_t k = e >> kTubeIdShift;
-                const float4 p = cpos[k], c = cdir[k];
+                const float4 p = cpos[I.tfirst + b + lane], c = cdir[I.tfirst + b + lane];
                 int ib[3];
                 img_of(e & 63u, ib);
                 T.p[lane] = p;
@@ -1272,12 +1272,13 @@ struct TubeCandSrc {
 
 nf_status Engine::tube_register_rods(int stage) {
     TubeRodSrc src{rodoff.p, dcount.p, R, pos.p, dir.p};
-    return tube_register(*this, (uint32_t)rod_slots, nullptr, stage, src, trod_start, trod_cur, trod_ent);
+    return tube_register(*this, (uint32_t)rod_slots, nullptr, stage, src, trod_start, trod_cur, trod_ent, trod_pos,
+                         trod_dir);
 }
 
 nf_status Engine::tube_register_cands(uint64_t slots, const uint32_t* ntot, bool /*alive_only*/) {
     TubeCandSrc src{creal.p, cpos.p, cdir.p, state.p};
-    return tube_register(*this, (uint32_t)slots, ntot, 0, src, tcnd_start, tcnd_cur, tcnd_ent);
+    return tube_register(*this, (uint32_t)slots, ntot, 0, src, tcnd_start, tcnd_cur, tcnd_ent, tcnd_pos, tcnd_dir);
 }
 
 nf_status Engine::tube_items(const uint32_t* pstart, const uint32_t* tstart) {
@@ -1441,16 +1442,7 @@ static nf_status setup_reals(Engine& E) {
     E.ntcell = (uint32_t)toffs;
     // the tube sweeps run when every realisation has a tube grid
     E.tube = E.ntcell > 0;
-    E.tube_regs_max = 0;
-    for (int r = 0; r < E.R; ++r) {
-        E.tube = E.tube && E.hreal[r].tube;
-        if (E.hreal[r].tube) {
-            double lmax, amax;
-            size_bounds(E.prm[r], &lmax, &amax);
-            const double h = (lmax / 2 + amax + std::max((double)E.prm[r].tol, (double)1e-6f)) * 1.00001 + E.hreal[r].slack;
-            E.tube_regs_max = std::max(E.tube_regs_max, tube_regs_bound(E.hreal[r], h));
-        }
-    }
+    for (int r = 0; r < E.R; ++r) E.tube = E.tube && E.hreal[r].tube;
     E.rod_slots = roff;
 #define NF_CKS(x) do { cudaError_t e_ = (x); if (e_ != cudaSuccess) return E.cuda_fail(e_, #x); } while (0)
     std::vector<uint32_t> hcelloff(E.R + 1);
@@ -1782,8 +1774,8 @@ nf_status Engine::generate() {
             s = tube_items(tcnd_start.p, trod_start.p);
             if (s != NF_OK) return s;
             NF_LAUNCH(k_tube_old, persistent_grid(k_tube_old), kTPB, 0, st)(dreal.p, R, toffs.p, titem_count(),
-                                                    (uint32_t)titems.cap, titems.p, tcnd_ent.p, cpos.p, cdir.p,
-                                                    trod_ent.p, pos.p, dir.p, state.p, xq.p, xq.cap, ctr.p);
+                                                    (uint32_t)titems.cap, titems.p, tcnd_ent.p, tcnd_pos.p, tcnd_dir.p,
+                                                    trod_ent.p, trod_pos.p, trod_dir.p, state.p, xq.p, xq.cap, ctr.p);
             NF_CK(cudaGetLastError());
             NF_LAUNCH(k_old_exact, xg, 256, 0, st)(dreal.p, xq.p, nullptr, ctr.p + C_XQ_OLD, xq.cap, cpos.p, cdir.p,
                                                    creal.p, pos.p, dir.p, state.p, ctr.p);
@@ -1828,7 +1820,7 @@ nf_status Engine::generate() {
         if (tube) {
             NF_CK(xqc.ensure(xq2.cap));
             NF_LAUNCH(k_tube_conf, persistent_grid(k_tube_conf), kTPB, 0, st)(dreal.p, R, toffs.p, titem_count(),
-                                                    (uint32_t)titems.cap, titems.p, tcnd_ent.p, cpos.p, cdir.p,
+                                                    (uint32_t)titems.cap, titems.p, tcnd_ent.p, tcnd_pos.p, tcnd_dir.p,
                                                     ccnt.p, clist.p, xq2.p, xqc.p, xq2.cap, ctr.p);
         } else {
             NF_LAUNCH(k_conf_tiles, persistent_grid(k_conf_tiles), kTPB, 0, st)(dreal.p, item_count(), (uint32_t)items.cap, items.p, aperm.p, apos.p,

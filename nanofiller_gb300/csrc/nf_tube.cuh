@@ -211,7 +211,8 @@ template <class Src, bool kFill>
 __global__ void __launch_bounds__(kRegTPB) k_treg(uint32_t n, const uint32_t* __restrict__ ntot,
                                                   const Real* __restrict__ reals, int stage, Src src,
                                                   uint32_t* __restrict__ tcnt, const uint32_t* __restrict__ tstart,
-                                                  uint32_t* __restrict__ tent, uint32_t cap,
+                                                  uint32_t* __restrict__ tent, float4* __restrict__ tpos,
+                                                  float4* __restrict__ tdir, uint32_t cap,
                                                   unsigned long long* __restrict__ ovf) {
     constexpr int kW = kRegTPB / 32;
     __shared__ float4 sp[kW][32], sc[kW][32];
@@ -287,29 +288,17 @@ __global__ void __launch_bounds__(kRegTPB) k_treg(uint32_t n, const uint32_t* __
                 if (!tube_cell(Re, per, u, &cell, img)) continue;
                 if (kFill) {
                     const uint32_t qd = tstart[cell] + atomicAdd(&tcnt[cell], 1u);
-                    if (qd < cap) tent[qd] = tube_entry(id, img);
+                    if (qd < cap) {
+                        tent[qd] = tube_entry(id, img);
+                        tpos[qd] = q;  // the object's geometry beside its entry: the sweeps read it coalesced
+                        tdir[qd] = cq;
+                    }
                     else atomicAdd(ovf, 1ull);
                 } else {
                     atomicAdd(&tcnt[cell], 1u);
                 }
             }
     }
-}
-
-// Registrations of one object at most: slabs along the dominant axis d times
-// cells per slab (the slab's piece of segment spans at most tce_d + 2 trho
-// along another axis, widened by trho on both sides).
-__host__ inline uint32_t tube_regs_bound(const Real& R, double hmax) {
-    uint64_t best = 1;
-    for (int d = 0; d < 3; ++d) {
-        const double ed = R.tce[d], rho = R.trho;
-        uint64_t slabs = (uint64_t)std::floor((2 * hmax + 2 * rho) / ed) + 3;
-        uint64_t per = 1;
-        for (int o = 0; o < 3; ++o)
-            if (o != d) per *= (uint64_t)std::floor((ed + 4 * rho) / R.tce[o]) + 3;
-        best = std::max(best, slabs * per);
-    }
-    return (uint32_t)std::min<uint64_t>(best, 1u << 20);
 }
 
 // Work items of the tube sweeps: per cell with probes and targets, probe
