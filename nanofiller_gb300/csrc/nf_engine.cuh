@@ -174,7 +174,7 @@ struct Engine {
     int trod_stage = -1;                    // stage of the current rod registrations (-1: stale)
     DBuf<uint32_t> toffs;                   // R + 1 prefix of tube cells
     DBuf<uint32_t> trod_start, trod_cur, trod_ent;
-    DBuf<uint32_t> tcnd_start, tcnd_cur, tcnd_ent;
+    DBuf<uint32_t> tcnd_start, tcnd_cur, tcnd_ent, tcnd_cnt;
     DBuf<float4> trod_pos, trod_dir, tcnd_pos, tcnd_dir;  // each entry's object geometry
     DBuf<TItem> titems;
     size_t tit_cap = 1 << 20;
@@ -310,7 +310,11 @@ struct Engine {
     // old-rod test) into tcnd_*; then the work list of probes x targets.
     nf_status tube_register_rods(int stage);
     nf_status tube_register_cands(uint64_t slots, const uint32_t* ntot, bool alive_only);
-    nf_status tube_items(const uint32_t* pstart, const uint32_t* tstart);
+    nf_status tube_items(const uint32_t* pstart, const uint32_t* tstart, const uint32_t* pcnt = nullptr,
+                         const uint32_t* tcnt = nullptr);
+    // Compacts the candidate registration (tcnd_*) in place to the candidates
+    // still alive; per-cell lengths in tcnd_cnt.
+    nf_status tube_compact_cands();
     // Registers objects [0, n) of any source (stage-1 periodicity) into tcnd_*.
     template <class Src>
     nf_status tube_register_objects(uint32_t n, Src src);

@@ -1281,16 +1281,28 @@ nf_status Engine::tube_register_cands(uint64_t slots, const uint32_t* ntot, bool
     return tube_register(*this, (uint32_t)slots, ntot, 0, src, tcnd_start, tcnd_cur, tcnd_ent, tcnd_pos, tcnd_dir);
 }
 
-nf_status Engine::tube_items(const uint32_t* pstart, const uint32_t* tstart) {
+nf_status Engine::tube_items(const uint32_t* pstart, const uint32_t* tstart, const uint32_t* pcnt,
+                              const uint32_t* tcnt) {
     NF_CK(icnt.ensure((size_t)ntcell + 1));
     NF_CK(tioff.ensure((size_t)ntcell + 1));
     NF_CK(titems.ensure(tit_cap));
-    NF_LAUNCH(k_titem_count, grid_for((size_t)ntcell + 1, 256), 256, 0, st)(ntcell, pstart, tstart, icnt.p);
+    NF_LAUNCH(k_titem_count, grid_for((size_t)ntcell + 1, 256), 256, 0, st)(ntcell, pstart, tstart, pcnt, tcnt,
+                                                                           icnt.p);
     NF_CK(cudaGetLastError());
     nf_status s = scan_u32(icnt.p, tioff.p, (size_t)ntcell + 1);
     if (s != NF_OK) return s;
-    NF_LAUNCH(k_titem_fill, grid_for(ntcell, 256), 256, 0, st)(ntcell, pstart, tstart, tioff.p, titems.p,
-                                                               (uint32_t)titems.cap, ctr.p + C_ITEMS);
+    NF_LAUNCH(k_titem_fill, grid_for(ntcell, 256), 256, 0, st)(ntcell, pstart, tstart, pcnt, tcnt, tioff.p,
+                                                               titems.p, (uint32_t)titems.cap, ctr.p + C_ITEMS);
+    NF_CK(cudaGetLastError());
+    return NF_OK;
+}
+
+nf_status Engine::tube_compact_cands() {
+    NF_CK(tcnd_cnt.ensure((size_t)ntcell + 1));
+    const unsigned blocks = (unsigned)std::min<size_t>(((size_t)ntcell + 7) / 8, (size_t)nsm * 16);
+    NF_LAUNCH(k_treg_compact, std::max(1u, blocks), 256, 0, st)(ntcell, tcnd_start.p, tcnd_cnt.p, tcnd_ent.p,
+                                                                 tcnd_pos.p, tcnd_dir.p, state.p,
+                                                                 (uint8_t)ST_ALIVE);
     NF_CK(cudaGetLastError());
     return NF_OK;
 }
@@ -1762,6 +1774,7 @@ nf_status Engine::generate() {
             return NF_OK;
         };
         tstart(KT_OLD);
+        bool cands_registered = false;  // the tube registration of this round's candidates
         if (tube && total_rods() > 0) {
             // tube grid: the kept candidates against the placed rods that share a cell
             if (trod_stage != 0) {
@@ -1771,6 +1784,7 @@ nf_status Engine::generate() {
             }
             s = tube_register_cands(slots, ntot, true);
             if (s != NF_OK) return s;
+            cands_registered = true;
             s = tube_items(tcnd_start.p, trod_start.p);
             if (s != NF_OK) return s;
             NF_LAUNCH(k_tube_old, persistent_grid(k_tube_old), kTPB, 0, st)(dreal.p, R, toffs.p, titem_count(),
@@ -1803,10 +1817,16 @@ nf_status Engine::generate() {
             NF_CK(cudaGetLastError());
         }
         tstop(KT_OLD);
-        if (tube) {  // the survivors, registered on the tube grid
-            s = tube_register_cands(slots, ntot, true);
+        const uint32_t* scnt = nullptr;  // per-cell survivor counts of a compacted registration
+        if (tube) {  // the survivors on the tube grid: the round's registration compacted, or registered
+            if (cands_registered) {
+                s = tube_compact_cands();
+                scnt = tcnd_cnt.p;
+            } else {
+                s = tube_register_cands(slots, ntot, true);
+            }
             if (s != NF_OK) return s;
-            s = tube_items(tcnd_start.p, tcnd_start.p);
+            s = tube_items(tcnd_start.p, tcnd_start.p, scnt, scnt);
             if (s != NF_OK) return s;
         } else {
             s = bin_survivors();

@@ -301,17 +301,60 @@ __global__ void __launch_bounds__(kRegTPB) k_treg(uint32_t n, const uint32_t* __
     }
 }
 
+// In-place compaction of a candidate registration to the candidates still
+// alive (the survivors of the old-rod test), one warp per cell: the list of
+// each cell keeps its order and its start; cnt[c] receives its new length.
+// A chunk of 32 entries is read before any of it is written, and writes go to
+// positions at or below the chunk's, so no entry is overwritten unread.
+static __global__ void k_treg_compact(uint32_t ncell, const uint32_t* __restrict__ start, uint32_t* __restrict__ cnt,
+                                      uint32_t* __restrict__ ent, float4* __restrict__ epos, float4* __restrict__ edir,
+                                      const uint8_t* __restrict__ state, uint8_t alive_state) {
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
+    const unsigned lt = (1u << lane) - 1u;
+    for (uint32_t c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; c < ncell; c += nw) {
+        const uint32_t b = start[c], e = start[c + 1];
+        uint32_t w = b;
+        for (uint32_t k = b; k < e; k += 32) {
+            const uint32_t i = k + lane;
+            const bool valid = i < e;
+            uint32_t en = 0;
+            float4 p = make_float4(0, 0, 0, 0), d = p;
+            if (valid) { en = ent[i]; p = epos[i]; d = edir[i]; }
+            const bool alive = valid && state[en >> kTubeIdShift] == alive_state;
+            const unsigned bal = __ballot_sync(0xffffffffu, alive);
+            __syncwarp();
+            if (alive) {
+                const uint32_t q = w + __popc(bal & lt);
+                ent[q] = en;
+                epos[q] = p;
+                edir[q] = d;
+            }
+            w += __popc(bal);
+            __syncwarp();
+        }
+        if (lane == 0) cnt[c] = w - b;
+    }
+}
+
 // Work items of the tube sweeps: per cell with probes and targets, probe
 // chunks of <= 32 times target segments of <= kTSeg. Item layout (16 B):
 // first probe entry, first target entry, cell, np | nt << 6.
 constexpr uint32_t kTSeg = 128;
 
+// Entries of cell c: [start[c], start[c] + cnt[c]) when a count array is
+// given (a list compacted in place), else [start[c], start[c + 1]).
+__device__ __forceinline__ uint32_t tube_count(const uint32_t* start, const uint32_t* cnt, uint32_t c) {
+    return cnt ? cnt[c] : start[c + 1] - start[c];
+}
+
 static __global__ void k_titem_count(uint32_t ncell, const uint32_t* __restrict__ pstart,
-                              const uint32_t* __restrict__ tstart, uint32_t* __restrict__ icnt) {
+                              const uint32_t* __restrict__ tstart, const uint32_t* __restrict__ pcnt,
+                              const uint32_t* __restrict__ tcnt, uint32_t* __restrict__ icnt) {
     const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c > ncell) return;
     if (c == ncell) { icnt[c] = 0; return; }
-    const uint32_t np = pstart[c + 1] - pstart[c], nt = tstart[c + 1] - tstart[c];
+    const uint32_t np = tube_count(pstart, pcnt, c), nt = tube_count(tstart, tcnt, c);
     icnt[c] = (np && nt) ? ((np + 31u) / 32u) * ((nt + kTSeg - 1u) / kTSeg) : 0u;
 }
 
@@ -320,6 +363,7 @@ struct TItem {
 };
 
 static __global__ void k_titem_fill(uint32_t ncell, const uint32_t* __restrict__ pstart, const uint32_t* __restrict__ tstart,
+                             const uint32_t* __restrict__ pcnt, const uint32_t* __restrict__ tcnt,
                              const uint32_t* __restrict__ ioff, TItem* __restrict__ items, uint32_t cap,
                              unsigned long long* __restrict__ imax) {
     const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
@@ -327,7 +371,7 @@ static __global__ void k_titem_fill(uint32_t ncell, const uint32_t* __restrict__
     if (c >= ncell) return;
     const uint32_t k0 = ioff[c], k1 = ioff[c + 1];
     if (k1 == k0) return;
-    const uint32_t p0 = pstart[c], np = pstart[c + 1] - p0, t0 = tstart[c], nt = tstart[c + 1] - t0;
+    const uint32_t p0 = pstart[c], np = tube_count(pstart, pcnt, c), t0 = tstart[c], nt = tube_count(tstart, tcnt, c);
     const uint32_t segs = (nt + kTSeg - 1u) / kTSeg;
     for (uint32_t k = k0; k < k1 && k < cap; ++k) {
         const uint32_t idx = k - k0, a = (idx / segs) * 32u, b = (idx % segs) * kTSeg;
