@@ -167,8 +167,11 @@ typedef struct nf_params {
     int64_t epoch_candidates; /* EPOCH_CANDIDATES: candidates per epoch;
                                0 -> max(1024, target count)                */
     int32_t solve_method;   /* SOLVE_METHOD: 0 auto (direct when the network's
-                               band after reverse Cuthill-McKee is narrow),
-                               1 direct (banded LDL^T), 2 iterative (PCG)   */
+                               band after reverse Cuthill-McKee is narrow:
+                               block cyclic reduction up to 32, banded LDL^T
+                               up to 512), 1 direct (the same, an error when
+                               the band is wider), 2 iterative (PCG),
+                               3 banded LDL^T                               */
     float tube_load;        /* TUBE_LOAD (tuning, speed only): the pair sweeps
                                register every rod in each cell of a fine grid
                                that its axis segment, dilated by half the
@@ -244,8 +247,9 @@ typedef struct nf_solve_stats {
     int64_t n_active;           /* unknowns: rods linked to both electrodes*/
     int32_t percolating;        /* a path joins source and sink            */
     double ms;
-    int32_t direct;             /* 1: banded LDL^T (outer_iters = refinement
-                                   steps, inner_iters = 0); 0: PCG          */
+    int32_t direct;             /* 2: block cyclic reduction, 1: banded
+                                   LDL^T (outer_iters = refinement steps,
+                                   inner_iters = 0); 0: PCG                 */
     uint32_t bandwidth;         /* widest band after reordering (direct)    */
 } nf_solve_stats;
 

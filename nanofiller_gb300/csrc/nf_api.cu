@@ -62,7 +62,7 @@ nf_status validate(const nf_params& p, std::string* why) {
     if (p.field_dir != 0 && p.field_dir != 1 && p.field_dir != 2 && p.field_dir != 4) {
         *why = "FIELD_DIR must be 0, 1, 2 or 4"; return NF_ERR_PARAM;
     }
-    if (p.solve_method < 0 || p.solve_method > 2) { *why = "SOLVE_METHOD must be 0, 1 or 2"; return NF_ERR_PARAM; }
+    if (p.solve_method < 0 || p.solve_method > 3) { *why = "SOLVE_METHOD must be 0, 1, 2 or 3"; return NF_ERR_PARAM; }
     if (p.self_align_step < 0 || p.clust_flag < 0 || p.clust_flag > 1 || p.reduce_flag < 0 || p.reduce_flag > 1) {
         *why = "SELF_ALLIGN_STEP must be >= 0, CLUST_FLAG and REDUCE_FLAG 0 or 1"; return NF_ERR_PARAM;
     }

@@ -214,6 +214,8 @@ struct Engine {
     DBuf<uint32_t> dcperm;         // per-realisation RCM order (local indices)
     DBuf<unsigned long long> dcboff;  // band offset per realisation
     DBuf<uint32_t> dcbw;           // bandwidth per realisation
+    DBuf<double> bcrbuf;           // block cyclic reduction: blocks, then solve vectors
+    DBuf<uint32_t> bcroff;         // first block per realisation
     std::vector<nf_solve_stats> solve_st;
     bool solve_valid = false;
 

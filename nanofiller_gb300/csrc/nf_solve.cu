@@ -36,6 +36,7 @@
 
 #include "nf_engine.cuh"
 #include "nf_graph.cuh"
+#include "nf_bcr.cuh"
 
 namespace nf {
 
@@ -1119,6 +1120,145 @@ __global__ void __launch_bounds__(NT) k_dc_band_win(int R, const uint32_t* __res
     }
 }
 
+// Direct form for bands of at most 32 (the rod and node networks of the
+// jammed box: 28 and 30): block cyclic reduction (nf_bcr.cuh) in one CTA per
+// realisation, then the same FP64 refinement as the banded forms. The blocks
+// are assembled straight from the CSR rows in band order (row p of the band
+// is block p / 32, row p mod 32); the rows past n pad the last block with an
+// identity. Factors in T (float first, double when float stalls above the
+// tolerance); x and the residual stay in FP64.
+template <int NT, typename T>
+__global__ void __launch_bounds__(NT) k_dc_bcr(int R, const uint32_t* __restrict__ abase,
+                                               const uint32_t* __restrict__ boff, const uint32_t* __restrict__ permL,
+                                               const uint32_t* __restrict__ rowp, const uint32_t* __restrict__ col,
+                                               const double* __restrict__ v64, const double* __restrict__ e64,
+                                               const double* __restrict__ ch64, int chains,
+                                               const double* __restrict__ b, double* __restrict__ x,
+                                               double* __restrict__ r64, T* __restrict__ blocks,
+                                               T* __restrict__ tvec, double* __restrict__ work, double tol,
+                                               int retry, CgOut* __restrict__ out) {
+    __shared__ double sh[96];
+    __shared__ int bad;
+    extern __shared__ __align__(16) unsigned char bcr_sh[];
+    T* S = reinterpret_cast<T*>(bcr_sh) + (threadIdx.x >> 5) * kBcrScratch;  // this warp's scratch
+    const int rr = blockIdx.x;
+    if (rr >= R) return;
+    if (retry && (out[rr].n == 0 || out[rr].res <= tol)) return;  // solved by the previous pass
+    const uint32_t base = abase[rr], n = abase[rr + 1] - base;
+    CgOut o{};
+    o.n = (int)n;
+    if (n == 0) {
+        if (threadIdx.x == 0) out[rr] = o;
+        return;
+    }
+    const uint32_t m = boff[rr + 1] - boff[rr];
+    T* blk = blocks + (size_t)boff[rr] * kBcrPer;
+    T* t = tvec + (size_t)boff[rr] * kBcrW;
+    const uint32_t* perm = permL + base;
+    const double* bb = b + base;
+    double* xx = x + base;
+    double* rv = r64 + base;
+    double* xt = work + base;            // candidate x
+    double* rc = r64 + abase[R] + base;  // candidate residual
+    const double* gl64 = ch64 + base;
+    const double* gr64 = ch64 + abase[R] + base;
+    for (size_t e = threadIdx.x; e < (size_t)m * 2 * kBcrBlk; e += NT)
+        blk[(e / (2 * kBcrBlk)) * kBcrPer + e % (2 * kBcrBlk)] = T(0);  // D and K of every block
+    if (threadIdx.x == 0) bad = 0;
+    __syncthreads();
+    for (uint32_t i = threadIdx.x; i < n; i += NT) {
+        const uint32_t g = base + i, p = perm[i], I = p >> 5;
+        T* drow = blk + (size_t)I * kBcrPer + (p & 31u) * 32;
+        T* krow = drow + kBcrBlk;
+        auto put = [&](uint32_t q, double v) {
+            const uint32_t J = q >> 5;
+            if (J == I) drow[q & 31u] -= (T)v;
+            else if (J + 1 == I) krow[q & 31u] -= (T)v;  // J == I + 1: the row of q writes it
+        };
+        double d = e64[g];
+        for (uint32_t k = rowp[g], k1 = rowp[g + 1]; k < k1; ++k) {
+            d += v64[k];
+            put(perm[col[k] - base], v64[k]);
+        }
+        if (chains) {
+            if (gl64[i] > 0.0) {
+                d += gl64[i];
+                put(perm[i - 1], gl64[i]);
+            }
+            if (gr64[i] > 0.0) {
+                d += gr64[i];
+                put(perm[i + 1], gr64[i]);
+            }
+        }
+        drow[p & 31u] += (T)d;
+        xx[i] = 0.0;
+    }
+    for (uint32_t p = n + threadIdx.x; p < m * kBcrW; p += NT)
+        blk[(size_t)(p >> 5) * kBcrPer + (p & 31u) * 33] = T(1);
+    __syncthreads();
+    const bool ok = bcr_factor<NT, T>(blk, m, S, &bad);
+    double part = 0.0;
+    for (uint32_t i = threadIdx.x; i < n; i += NT) {
+        rv[i] = bb[i];
+        part += bb[i] * bb[i];
+    }
+    const double bn = sqrt(block_sum<NT>(part, sh));
+    double rn = bn;
+    int steps = 0;
+    const int max_steps = sizeof(T) == 4 ? 40 : 12;
+    auto residual = [&](const double* xv) -> double {
+        double acc2 = 0.0;
+        for (uint32_t i = threadIdx.x; i < n; i += NT) {
+            const uint32_t g = base + i;
+            const double xi = xv[i];
+            double acc = e64[g] * xi;
+            for (uint32_t k = rowp[g], k1 = rowp[g + 1]; k < k1; ++k) acc += v64[k] * (xi - xv[col[k] - base]);
+            if (chains) {
+                const double a = gl64[i], c = gr64[i];
+                if (a != 0.0) acc += a * (xi - xv[i - 1]);
+                if (c != 0.0) acc += c * (xi - xv[i + 1]);
+            }
+            const double ri = bb[i] - acc;
+            rc[i] = ri;
+            acc2 += ri * ri;
+        }
+        return sqrt(block_sum<NT>(acc2, sh));
+    };
+    for (; ok && steps < max_steps && rn > 1e-16 * bn; ++steps) {
+        const double sc = 1.0 / rn;
+        for (uint32_t i = threadIdx.x; i < n; i += NT) t[perm[i]] = (T)(rv[i] * sc);
+        for (uint32_t p = n + threadIdx.x; p < m * kBcrW; p += NT) t[p] = T(0);
+        __syncthreads();
+        bcr_solve<NT, T>(blk, m, t);
+        for (uint32_t i = threadIdx.x; i < n; i += NT) xt[i] = xx[i] + rn * (double)t[perm[i]];
+        __syncthreads();
+        const double rn_new = residual(xt);
+        if (!(rn_new < rn)) { ++steps; break; }  // at the rounding floor
+        for (uint32_t i = threadIdx.x; i < n; i += NT) {
+            xx[i] = xt[i];
+            rv[i] = rc[i];
+        }
+        __syncthreads();
+        const bool slow = rn_new > 1e-2 * rn;
+        rn = rn_new;
+        if (rn <= tol * bn * 1e-3) { ++steps; break; }
+        // FP32 factors that gain fewer than two digits a step while still
+        // above the tolerance would need tens of steps: the host refactors in
+        // FP64 instead
+        if (sizeof(T) == 4 && slow && rn > tol * bn) { ++steps; break; }
+    }
+    part = 0.0;
+    for (uint32_t i = threadIdx.x; i < n; i += NT) part += bb[i] * (1.0 - xx[i]);
+    const double G = block_sum<NT>(part, sh);
+    if (threadIdx.x == 0) {
+        o.G = G;
+        o.res = !ok ? INFINITY : bn > 0 ? rn / bn : 0.0;
+        o.outer = steps;
+        o.inner = 0;
+        out[rr] = o;
+    }
+}
+
 nf_status Engine::solve_graph(uint32_t n, const std::vector<uint32_t>& off, const std::vector<uint32_t>& nodes,
                               uint32_t mc, uint32_t m, const uint32_t* eI, const uint32_t* eJ, const double* eG) {
     EventPair ev;
@@ -1145,10 +1285,13 @@ nf_status Engine::solve_graph(uint32_t n, const std::vector<uint32_t>& off, cons
     const double tol = prm[0].solve_tol > 0 ? prm[0].solve_tol : 1e-10;
     const int max_inner = prm[0].solve_max_iter > 0 ? prm[0].solve_max_iter : 20000;
     // Direct form when every realisation's band after reverse Cuthill-McKee
-    // is narrow: bandwidth <= 512, n b^2 <= 1e9 updates, 1 GB of band at most.
+    // is narrow: block cyclic reduction for bands up to 32 (SOLVE_METHOD 0 or
+    // 1), else a banded LDL^T for bandwidth <= 512, n b^2 <= 1e9 updates, 1 GB
+    // of band at most (SOLVE_METHOD 3 forces the banded form).
     const int method = prm[0].solve_method;
-    bool direct = false;
+    bool direct = false, bcr = false;
     uint32_t bmax = 0;
+    size_t nblk = 0;  // blocks of 32 unknowns over all realisations (block cyclic reduction)
     if (na > 0 && method != 2) {
         std::vector<uint32_t> hrow(na + 1), hcol(nnz);
         std::vector<double> hgr(na);
@@ -1158,8 +1301,9 @@ nf_status Engine::solve_graph(uint32_t n, const std::vector<uint32_t>& off, cons
         NF_CK(cudaStreamSynchronize(st));
         std::vector<uint32_t> hperm(na), hbw(R, 0);
         std::vector<unsigned long long> hoff(R + 1, 0);
-        bool fits = true;
-        for (int r = 0; r < R && fits; ++r) {
+        bool fits = true, narrow = true;  // every band so far: banded form / block cyclic reduction
+        int r = 0;
+        for (; r < R && (fits || narrow); ++r) {
             const uint32_t b0 = A.habase[r], nr = A.habase[r + 1] - b0;
             std::vector<uint32_t> lrow(nr + 1), lcol;
             std::vector<char> up(nr, 0);
@@ -1176,25 +1320,60 @@ nf_status Engine::solve_graph(uint32_t n, const std::vector<uint32_t>& off, cons
             hbw[r] = bw;
             bmax = std::max(bmax, bw);
             hoff[r + 1] = hoff[r] + (unsigned long long)nr * (bw + 1);  // rows; the window form adds L and D
-            fits = bw <= kDcBandMax && (double)nr * bw * bw <= 1e9;
+            fits = fits && bw <= kDcBandMax && (double)nr * bw * bw <= 1e9;
+            narrow = narrow && bw <= kBcrW;
         }
-        fits = fits && (double)hoff[R] * sizeof(double) <= 1e9;
-        if (method == 1 && !fits) { err = "the reordered band is too wide for the direct form"; return NF_ERR_PARAM; }
+        const bool all = r == R;  // every realisation ordered
+        std::vector<uint32_t> hbo(R + 1, 0);
+        for (int q = 0; q < R; ++q) hbo[q + 1] = hbo[q] + (A.habase[q + 1] - A.habase[q] + kBcrW - 1) / kBcrW;
+        nblk = hbo[R];
+        bcr = all && narrow && method != 3 && (double)nblk * (kBcrPer + kBcrW) * sizeof(double) <= 4e9;
+        fits = bcr || (all && fits && (double)hoff[R] * sizeof(double) <= 1e9);
+        if ((method == 1 || method == 3) && !fits) {
+            err = "the reordered band is too wide for the direct form";
+            return NF_ERR_PARAM;
+        }
         direct = fits;
         if (direct) {
             NF_CK(dcperm.ensure(na));
-            NF_CK(dcbw.ensure(R));
-            NF_CK(dcboff.ensure(R + 1));
-            NF_CK(dcband.ensure(2 * hoff[R] + na + 1));
             NF_CK(dcwork.ensure(2 * (size_t)na + 2));
             NF_CK(cudaMemcpyAsync(dcperm.p, hperm.data(), sizeof(uint32_t) * na, cudaMemcpyHostToDevice, st));
-            NF_CK(cudaMemcpyAsync(dcbw.p, hbw.data(), sizeof(uint32_t) * R, cudaMemcpyHostToDevice, st));
-            NF_CK(cudaMemcpyAsync(dcboff.p, hoff.data(), sizeof(unsigned long long) * (R + 1), cudaMemcpyHostToDevice, st));
+            if (bcr) {
+                NF_CK(bcrbuf.ensure(nblk * (kBcrPer + kBcrW)));
+                NF_CK(bcroff.ensure(R + 1));
+                NF_CK(cudaMemcpyAsync(bcroff.p, hbo.data(), sizeof(uint32_t) * (R + 1), cudaMemcpyHostToDevice, st));
+            } else {
+                NF_CK(dcbw.ensure(R));
+                NF_CK(dcboff.ensure(R + 1));
+                NF_CK(dcband.ensure(2 * hoff[R] + na + 1));
+                NF_CK(cudaMemcpyAsync(dcbw.p, hbw.data(), sizeof(uint32_t) * R, cudaMemcpyHostToDevice, st));
+                NF_CK(cudaMemcpyAsync(dcboff.p, hoff.data(), sizeof(unsigned long long) * (R + 1),
+                                      cudaMemcpyHostToDevice, st));
+            }
         }
     }
     tstart(KT_CG);
     if (na == 0) {
         // every realisation's network is empty: G = 0, voltages from the components alone
+    } else if (bcr) {
+        NF_CK(cgred.ensure(2 * (size_t)na + 2));
+        constexpr int kNtF = 384, kNtD = 256;  // registers: 170 a thread for float, 255 for double
+        auto* kf32 = k_dc_bcr<kNtF, float>;
+        auto* kf64 = k_dc_bcr<kNtD, double>;
+        const int sh4 = (kNtF / 32) * kBcrScratch * (int)sizeof(float);
+        const int sh8 = (kNtD / 32) * kBcrScratch * (int)sizeof(double);
+        NF_CK(cudaFuncSetAttribute(kf32, cudaFuncAttributeMaxDynamicSharedMemorySize, sh4));
+        NF_CK(cudaFuncSetAttribute(kf64, cudaFuncAttributeMaxDynamicSharedMemorySize, sh8));
+        float* f32 = reinterpret_cast<float*>(bcrbuf.p);
+        NF_LAUNCH(kf32, R, kNtF, sh4, st)(R, dab.p, bcroff.p, dcperm.p, rowp.p, col.p, val64.p, diag64.p, chain64.p,
+                                          A.chains ? 1 : 0, bvec.p, xvec.p, cgred.p, f32, f32 + nblk * kBcrPer,
+                                          dcwork.p, tol, 0, outs.p);
+        NF_CK(cudaGetLastError());
+        // FP64 factors for the realisations whose FP32 factors stayed above
+        // the tolerance (the others return at once): no host round trip
+        NF_LAUNCH(kf64, R, kNtD, sh8, st)(R, dab.p, bcroff.p, dcperm.p, rowp.p, col.p, val64.p, diag64.p,
+                                          chain64.p, A.chains ? 1 : 0, bvec.p, xvec.p, cgred.p, bcrbuf.p,
+                                          bcrbuf.p + nblk * kBcrPer, dcwork.p, tol, 1, outs.p);
     } else if (direct && bmax <= kDcWin) {
         uint32_t nmax = 0;
         for (int r = 0; r < R; ++r) nmax = std::max(nmax, A.habase[r + 1] - A.habase[r]);
@@ -1261,7 +1440,7 @@ nf_status Engine::solve_graph(uint32_t n, const std::vector<uint32_t>& off, cons
         S.n_active = A.habase[r + 1] - A.habase[r];
         S.percolating = S.n_active > 0;
         S.ms = ms;
-        S.direct = direct ? 1 : 0;
+        S.direct = bcr ? 2 : direct ? 1 : 0;
         S.bandwidth = direct ? bmax : 0;
         if (S.n_active > 0 && !(S.residual <= tol)) conv = false;
     }
