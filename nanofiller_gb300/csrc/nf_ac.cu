@@ -598,21 +598,27 @@ uint32_t rcm_order(uint32_t n, const std::vector<uint32_t>& rowp, const std::vec
     order.reserve(n);
     std::vector<char> done(n, 0);
     std::vector<uint32_t> nb, q;
-    auto bfs = [&](uint32_t s, std::vector<uint32_t>* seq) {  // returns the last node reached
+    q.reserve(n);
+    // Breadth-first sweep from s over nodes not yet ordered; returns the last
+    // node reached. Only the ordering sweep (seq given) visits neighbours by
+    // increasing degree; the two sweeps that look for a pseudo-peripheral
+    // start need the level structure alone.
+    auto bfs = [&](uint32_t s, std::vector<uint32_t>* seq) {
         q.assign(1, s);
         level[s] = 0;
-        std::vector<uint32_t> touched(1, s);
         size_t h = 0;
         while (h < q.size()) {
             const uint32_t v = q[h++];
             nbrs(v, nb);
-            std::sort(nb.begin(), nb.end(), [&](uint32_t a, uint32_t c) { return deg[a] != deg[c] ? deg[a] < deg[c] : a < c; });
+            if (seq)
+                std::sort(nb.begin(), nb.end(),
+                          [&](uint32_t a, uint32_t c) { return deg[a] != deg[c] ? deg[a] < deg[c] : a < c; });
             for (uint32_t u : nb)
-                if (level[u] < 0 && !done[u]) { level[u] = level[v] + 1; q.push_back(u); touched.push_back(u); }
+                if (level[u] < 0 && !done[u]) { level[u] = level[v] + 1; q.push_back(u); }
         }
         if (seq) *seq = q;
         const uint32_t last = q.back();
-        for (uint32_t v : touched) level[v] = -1;
+        for (uint32_t v : q) level[v] = -1;  // q holds every node this sweep reached
         return last;
     };
     for (uint32_t s0 = 0; s0 < n; ++s0) {

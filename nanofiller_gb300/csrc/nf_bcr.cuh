@@ -37,20 +37,29 @@ namespace nf {
 
 constexpr uint32_t kBcrW = 32;                    // block edge; the band must not be wider
 constexpr uint32_t kBcrBlk = kBcrW * kBcrW;       // entries of one block
-constexpr size_t kBcrPer = 5 * (size_t)kBcrBlk + kBcrW;  // D, K, Li, Vl, Vr, g per block
+constexpr size_t kBcrPer = 8 * (size_t)kBcrBlk + kBcrW;  // D, K, Li, Lr, Vl, Vr, VlT, VrT, g per block
 
 // Storage of block i: D (diagonal block, Schur-updated), K (A[i][left
-// neighbour], updated as neighbours are eliminated), Li ((L_i^-1)^T), Vl, Vr
-// and g (inverse pivots 1 / Delta).
+// neighbour], updated as neighbours are eliminated), Li ((L_i^-1)^T) and Lr
+// (L_i^-1), Vl, Vr and their transposes, g (inverse pivots 1 / Delta). Each
+// product of a solve reads one of them by columns (coalesced).
 template <typename T>
 struct BcrBlock {
-    T *D, *K, *Li, *Vl, *Vr, *g;
+    T *D, *K, *Li, *Lr, *Vl, *Vr, *VlT, *VrT, *g;
 };
 
 template <typename T>
 __device__ __forceinline__ BcrBlock<T> bcr_block(T* base, uint32_t i) {
     T* p = base + (size_t)i * kBcrPer;
-    return {p, p + kBcrBlk, p + 2 * kBcrBlk, p + 3 * kBcrBlk, p + 4 * kBcrBlk, p + 5 * kBcrBlk};
+    return {p,
+            p + kBcrBlk,
+            p + 2 * kBcrBlk,
+            p + 3 * kBcrBlk,
+            p + 4 * kBcrBlk,
+            p + 5 * kBcrBlk,
+            p + 6 * kBcrBlk,
+            p + 7 * kBcrBlk,
+            p + 8 * kBcrBlk};
 }
 
 // v[a] = M[a][lane] (column `lane`; one coalesced row per a)
@@ -89,6 +98,19 @@ __device__ __forceinline__ void bcr_ld_row(const double* M, int lane, double (&v
     }
 }
 
+// M[lane][a] = v[a] (row `lane`, 16-byte stores)
+__device__ __forceinline__ void bcr_st_row(float* M, int lane, const float (&v)[32]) {
+    float4* p = reinterpret_cast<float4*>(M + lane * 32);
+#pragma unroll
+    for (int q = 0; q < 8; ++q) p[q] = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+}
+
+__device__ __forceinline__ void bcr_st_row(double* M, int lane, const double (&v)[32]) {
+    double2* p = reinterpret_cast<double2*>(M + lane * 32);
+#pragma unroll
+    for (int q = 0; q < 16; ++q) p[q] = make_double2(v[2 * q], v[2 * q + 1]);
+}
+
 // In-register LDL^T of the symmetric block held by columns in c. On return
 // c[t] (t > lane) holds the unscaled column A^(lane)[t][lane], c[lane] the
 // pivot, *inv its inverse; false when a pivot is not a positive finite number.
@@ -102,12 +124,12 @@ __device__ __forceinline__ bool bcr_ldl(T (&c)[32], int lane, T* inv) {
         ok = ok && dk > T(0) && dk < T(INFINITY);
         const T ik = T(1) / dk;
         if (lane == k) my = ik;
-        const T akj = c[k];  // A[k][lane], the column's own copy of the symmetric entry
+        const T f = c[k] * ik;  // A[k][lane] / pivot (the column's own copy of the symmetric entry)
 #pragma unroll
         for (int t = 0; t < 32; ++t) {  // a constant trip count keeps both loops unrolled
             if (t > k) {
-                const T l = __shfl_sync(0xffffffffu, c[t], k) * ik;
-                if (lane > k) c[t] -= l * akj;
+                const T a = __shfl_sync(0xffffffffu, c[t], k);
+                if (lane > k) c[t] -= a * f;
             }
         }
     }
@@ -153,9 +175,9 @@ __device__ __forceinline__ void bcr_lmul(const T* S, const T (&m)[32], T (&v)[32
 #pragma unroll
     for (int r = 0; r < 32; ++r) {
         T row[32];
-        bcr_ld_sh(S + r * 32, row);  // L^-1[a][r] over a
+        bcr_ld_sh(S + r * 32, row);  // L^-1[a][r] over a (zero above the diagonal)
 #pragma unroll
-        for (int a = 0; a < 32; ++a) v[a] += row[a] * m[r];
+        for (int a = r; a < 32; ++a) v[a] += row[a] * m[r];
     }
 }
 
@@ -186,17 +208,6 @@ __device__ __forceinline__ void bcr_schur(const T* V, const T* g, int lane, T* S
     Sg[lane] = gl;
     __syncwarp();
     bcr_sub_vgv(S, Sg, lane, d);
-}
-
-// y_lane = sum_k M[lane][k] x_k (x one element per lane)
-template <typename T>
-__device__ __forceinline__ T bcr_mv(const T* M, T x, int lane) {
-    T row[32];
-    bcr_ld_row(M, lane, row);
-    T acc = 0;
-#pragma unroll
-    for (int k = 0; k < 32; ++k) acc += row[k] * __shfl_sync(0xffffffffu, x, k);
-    return acc;
 }
 
 // y_lane = sum_k M[k][lane] x_k
@@ -246,7 +257,8 @@ __device__ bool bcr_factor(T* base, uint32_t m, T* sc, int* bad) {
             {
                 T x[32];
                 bcr_linv(d, inv, lane, S, x);
-                bcr_st_col(B.Li, lane, x);  // (L^-1)^T, row-major
+                bcr_st_col(B.Li, lane, x);  // (L^-1)^T
+                bcr_st_row(B.Lr, lane, x);  // L^-1
             }
             B.g[lane] = inv;
             if (!elim) continue;  // the last block
@@ -254,6 +266,7 @@ __device__ bool bcr_factor(T* base, uint32_t m, T* sc, int* bad) {
             bcr_ld_col(B.K, lane, mm);  // A[i][i - s], column `lane`
             bcr_lmul(S, mm, v);
             bcr_st_col(B.Vl, lane, v);
+            bcr_st_row(B.VlT, lane, v);
             const uint32_t q = i + s;
             if (q < m) {
                 BcrBlock<T> Q = bcr_block(base, q);
@@ -263,6 +276,7 @@ __device__ bool bcr_factor(T* base, uint32_t m, T* sc, int* bad) {
                 bcr_ld_row(Q.K, lane, mm);  // A[i][q] = A[q][i]^T: column `lane` is row `lane` of Q.K
                 bcr_lmul(S, mm, v);
                 bcr_st_col(B.Vr, lane, v);
+                bcr_st_row(B.VrT, lane, v);
                 __syncwarp();
 #pragma unroll
                 for (int k = 0; k < 32; ++k) S[k * 32 + lane] = v[k];  // Vr
@@ -305,10 +319,10 @@ __device__ void bcr_solve(T* base, uint32_t m, T* t) {
                 if (i >= h) tv -= bcr_mtv(bcr_block(base, i - h).Vr, t[(i - h) * 32 + lane], lane);
                 if (i + h < m) tv -= bcr_mtv(bcr_block(base, i + h).Vl, t[(i + h) * 32 + lane], lane);
             }
-            if (elim || s >= m) {  // Li holds (L^-1)^T
+            if (elim || s >= m) {  // Li holds (L^-1)^T, Lr L^-1
                 BcrBlock<T> B = bcr_block(base, i);
                 tv = bcr_mtv(B.Li, tv, lane) * B.g[lane];
-                if (!elim) tv = bcr_mv(B.Li, tv, lane);  // the last block: x_0
+                if (!elim) tv = bcr_mtv(B.Lr, tv, lane);  // the last block: x_0
             }
             t[i * 32 + lane] = tv;
         }
@@ -320,10 +334,10 @@ __device__ void bcr_solve(T* base, uint32_t m, T* t) {
         for (uint32_t task = 1 + 2 * (uint32_t)warp; task < ntask; task += 2 * (NT / 32)) {
             const uint32_t i = task * s;
             BcrBlock<T> B = bcr_block(base, i);
-            T u = bcr_mv(B.Vl, t[(i - s) * 32 + lane], lane);
-            if (i + s < m) u += bcr_mv(B.Vr, t[(i + s) * 32 + lane], lane);
+            T u = bcr_mtv(B.VlT, t[(i - s) * 32 + lane], lane);
+            if (i + s < m) u += bcr_mtv(B.VrT, t[(i + s) * 32 + lane], lane);
             const T v = t[i * 32 + lane] - B.g[lane] * u;
-            t[i * 32 + lane] = bcr_mv(B.Li, v, lane);
+            t[i * 32 + lane] = bcr_mtv(B.Lr, v, lane);
         }
         __syncthreads();
     }

@@ -893,6 +893,10 @@ struct TubeVirtSrc {
         *c = vdf[i];
         return true;
     }
+    __device__ void geom(uint32_t i, float4* p, float4* c) const {
+        *p = vpf[i];
+        *c = vdf[i];
+    }
 };
 
 nf_status Engine::contacts() {

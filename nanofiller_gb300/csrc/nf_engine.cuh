@@ -216,6 +216,8 @@ struct Engine {
     DBuf<uint32_t> dcbw;           // bandwidth per realisation
     DBuf<double> bcrbuf;           // block cyclic reduction: blocks, then solve vectors
     DBuf<uint32_t> bcroff;         // first block per realisation
+    DBuf<double> cgout;            // per-realisation solve results (CgOut records)
+    DBuf<uint32_t> asmoff;         // assembly read-back: node offsets, then active bases and the error word
     std::vector<nf_solve_stats> solve_st;
     bool solve_valid = false;
 
@@ -359,7 +361,8 @@ inline nf_status tube_register(Engine& E, uint32_t n, const uint32_t* ntot, int 
     if (s != NF_OK) return s;
     // entries (with their objects' geometry, 36 B each) sized by the count:
     // one 4-byte read-back; an entry beyond the buffers would be counted in
-    // C_TUBE_OVF, which fails the stage
+    // C_TUBE_OVF, which fails the stage. The fill writes the 4-byte entries
+    // alone (scattered); a second pass adds the geometry in entry order.
     s = E.ensure_pinned(16);
     if (s != NF_OK) return s;
     uint32_t* h = reinterpret_cast<uint32_t*>(E.hpin);
@@ -373,9 +376,15 @@ inline nf_status tube_register(Engine& E, uint32_t n, const uint32_t* ntot, int 
     if (n) {
         auto kfill = k_treg<Src, true>;
         NF_LAUNCH(kfill, (unsigned)((n + kRegTPB - 1) / kRegTPB), kRegTPB, 0, st)(
-            n, ntot, E.dreal.p, stage, src, cur.p, start.p, ent.p, epos.p, edir.p,
+            n, ntot, E.dreal.p, stage, src, cur.p, start.p, ent.p, nullptr, nullptr,
             (uint32_t)std::min(ent.cap, std::min(epos.cap, edir.cap)), E.ctr.p + C_TUBE_OVF);
         NF_CKT(cudaGetLastError());
+        if (total) {
+            auto kgeom = k_treg_geom<Src>;
+            NF_LAUNCH(kgeom, (unsigned)std::min<size_t>((total + 255) / 256, (size_t)E.nsm * 32), 256, 0, st)(
+                (uint32_t)total, ent.p, epos.p, edir.p, src);
+            NF_CKT(cudaGetLastError());
+        }
     }
 #undef NF_CKT
     return NF_OK;

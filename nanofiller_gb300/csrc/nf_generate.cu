@@ -1255,6 +1255,10 @@ struct TubeRodSrc {
         *c = dir[i];
         return true;
     }
+    __device__ void geom(uint32_t i, float4* p, float4* c) const {
+        *p = pos[i];
+        *c = dir[i];
+    }
 };
 struct TubeCandSrc {
     const uint32_t* creal;
@@ -1267,6 +1271,10 @@ struct TubeCandSrc {
         *p = cpos[i];
         *c = cdir[i];
         return true;
+    }
+    __device__ void geom(uint32_t i, float4* p, float4* c) const {
+        *p = cpos[i];
+        *c = cdir[i];
     }
 };
 

@@ -49,6 +49,35 @@ __global__ void k_uf_init(uint32_t n, uint32_t* parent, uint32_t* flag) {
     flag[i] = 0;
 }
 
+// The assembly's first launch: union-find roots, electrode accumulators
+// vsrc / vsnk (2 n + 2 each), the active-count sentinel act[n] and the error
+// word.
+__global__ void k_asm_init(uint32_t n, uint32_t* __restrict__ parent, uint32_t* __restrict__ flag,
+                           double* __restrict__ vsrc, double* __restrict__ vsnk, uint32_t* __restrict__ act,
+                           uint32_t* __restrict__ errw) {
+    const size_t nv = 2ull * n + 2;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < nv; i += (size_t)gridDim.x * blockDim.x) {
+        vsrc[i] = 0.0;
+        vsnk[i] = 0.0;
+        if (i < n) {
+            parent[i] = (uint32_t)i;
+            flag[i] = 0;
+        }
+        if (i == 0) {
+            act[n] = 0;
+            *errw = 0;
+        }
+    }
+}
+
+// out[r] = aidx[off[r]] (active rows before realisation r), r <= R; out[R + 1]
+// the error word.
+__global__ void k_asm_bases(int R, const uint32_t* __restrict__ off, const uint32_t* __restrict__ aidx,
+                            const uint32_t* __restrict__ errw, uint32_t* __restrict__ out) {
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r <= R + 1; r += gridDim.x * blockDim.x)
+        out[r] = r <= R ? aidx[off[r]] : *errw;
+}
+
 // An edge conducts unless the admittance form gives it G = C = 0 (an AC
 // contact beyond the electrostatic range); without C every edge conducts.
 __device__ __forceinline__ bool edge_on(const double* G, const double* C, uint32_t e) {
@@ -503,11 +532,8 @@ nf_status Engine::assemble(uint32_t n, const std::vector<uint32_t>& off, uint32_
     uint32_t* errw = eflag.p + nslot + 1;
     double* sC = vsrc.p + nslot + 1;
     double* tC = vsnk.p + nslot + 1;
-    NF_CK(cudaMemsetAsync(errw, 0, sizeof(uint32_t), st));
-    NF_CK(cudaMemsetAsync(vsrc.p, 0, sizeof(double) * (2ull * nslot + 2), st));
-    NF_CK(cudaMemsetAsync(vsnk.p, 0, sizeof(double) * (2ull * nslot + 2), st));
-    NF_CK(cudaMemsetAsync(act + nslot, 0, sizeof(uint32_t), st));
-    if (nslot) NF_LAUNCH(k_uf_init, grid_for(nslot, 256), 256, 0, st)(nslot, parent.p, cflag.p);
+    NF_LAUNCH(k_asm_init, std::min(grid_for(2ull * nslot + 2, 256), 4096u), 256, 0, st)(nslot, parent.p, cflag.p,
+                                                                                       vsrc.p, vsnk.p, act, errw);
     if (m) {
         NF_LAUNCH(k_uf_union, grid_for(m, 256), 256, 0, st)(m, eI, eJ, eG, eC, parent.p, errw);
         NF_LAUNCH(k_uf_flags, grid_for(m, 256), 256, 0, st)(m, eI, eJ, eG, eC, parent.p, cflag.p, errw);
@@ -516,13 +542,22 @@ nf_status Engine::assemble(uint32_t n, const std::vector<uint32_t>& off, uint32_
     NF_CK(cudaGetLastError());
     nf_status s = scan_u32(act, aidx.p, nslot + 1);
     if (s != NF_OK) return s;
-    // Active count per realisation: aidx at the node-range boundaries.
-    out->habase.assign(RR + 1, 0);
-    for (int r = 0; r <= RR; ++r)
-        NF_CK(cudaMemcpyAsync(&out->habase[r], aidx.p + off[r], sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
-    uint32_t herr = 0;
-    NF_CK(cudaMemcpyAsync(&herr, errw, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+    // Active count per realisation (aidx at the node-range boundaries) and
+    // the error word: one gather, one copy through the pinned buffer.
+    {
+        nf_status sp = ensure_pinned(sizeof(uint32_t) * (2 * (size_t)RR + 4));
+        if (sp != NF_OK) return sp;
+    }
+    NF_CK(asmoff.ensure(2 * (size_t)RR + 4));
+    uint32_t* hp = reinterpret_cast<uint32_t*>(hpin);
+    std::memcpy(hp, off.data(), sizeof(uint32_t) * (RR + 1));
+    NF_CK(cudaMemcpyAsync(asmoff.p, hp, sizeof(uint32_t) * (RR + 1), cudaMemcpyHostToDevice, st));
+    NF_LAUNCH(k_asm_bases, grid_for((size_t)RR + 2, 256), 256, 0, st)(RR, asmoff.p, aidx.p, errw,
+                                                                      asmoff.p + RR + 1);
+    NF_CK(cudaMemcpyAsync(hp + RR + 1, asmoff.p + RR + 1, sizeof(uint32_t) * (RR + 2), cudaMemcpyDeviceToHost, st));
     NF_CK(cudaStreamSynchronize(st));
+    out->habase.assign(hp + RR + 1, hp + 2 * RR + 2);
+    uint32_t herr = hp[2 * RR + 2];
     if (herr) { err = "union-find walk exceeded its bound"; return NF_ERR_TIMEOUT; }
     const uint32_t na = out->habase[RR];
     out->na = na;
@@ -563,10 +598,11 @@ nf_status Engine::assemble(uint32_t n, const std::vector<uint32_t>& off, uint32_
     NF_CK(cudaGetLastError());
     s = scan_u32(deg.p, rowp.p, na + 1);
     if (s != NF_OK) return s;
-    uint32_t nnz = 0;
-    NF_CK(cudaMemcpyAsync(&nnz, rowp.p + na, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
-    NF_CK(cudaMemcpyAsync(&herr, errw, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+    NF_CK(cudaMemcpyAsync(hp, rowp.p + na, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+    NF_CK(cudaMemcpyAsync(hp + 1, errw, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
     NF_CK(cudaStreamSynchronize(st));
+    const uint32_t nnz = hp[0];
+    herr = hp[1];
     if (herr) { err = "chain link between non-consecutive active nodes"; return NF_ERR_STATE; }
     out->nnz = nnz;
     NF_CK(col.ensure(nnz + 1));
@@ -1277,11 +1313,34 @@ nf_status Engine::solve_graph(uint32_t n, const std::vector<uint32_t>& off, cons
     if (na)
         NF_LAUNCH(k_chain_factor, grid_for(na, 256), 256, 0, st)(na, chain64.p, chain64.p + na, cdiag.p, chain32.p);
     NF_CK(cudaGetLastError());
+    // Host staging through the pinned buffer, 8-byte aligned regions:
+    // active bases, the CSR rows for the ordering, the orders and block or
+    // band offsets going back, the per-realisation results.
+    size_t pofs = 0;
+    auto region = [&](size_t bytes) {
+        const size_t at = pofs;
+        pofs = (pofs + bytes + 7) & ~size_t(7);
+        return at;
+    };
+    const bool want_order = na > 0 && prm[0].solve_method != 2;
+    const size_t p_ab = region(sizeof(uint32_t) * (R + 1));
+    const size_t p_row = region(want_order ? sizeof(uint32_t) * (na + 1) : 0);
+    const size_t p_col = region(want_order ? sizeof(uint32_t) * nnz : 0);
+    const size_t p_gr = region(want_order ? sizeof(double) * na : 0);
+    const size_t p_perm = region(want_order ? sizeof(uint32_t) * na : 0);
+    const size_t p_bo = region(sizeof(uint32_t) * (R + 1));
+    const size_t p_bw = region(sizeof(uint32_t) * R);
+    const size_t p_hoff = region(sizeof(unsigned long long) * (R + 1));
+    const size_t p_out = region(sizeof(CgOut) * R);
+    s = ensure_pinned(pofs);
+    if (s != NF_OK) return s;
+    auto pin = [&](size_t at) { return hpin + at; };
     DBuf<uint32_t>& dab = rcur;  // per-realisation active base (R+1)
     NF_CK(dab.ensure(R + 1));
-    NF_CK(cudaMemcpyAsync(dab.p, A.habase.data(), sizeof(uint32_t) * (R + 1), cudaMemcpyHostToDevice, st));
-    DBuf<CgOut> outs;
-    NF_CK(outs.ensure(R));
+    std::memcpy(pin(p_ab), A.habase.data(), sizeof(uint32_t) * (R + 1));
+    NF_CK(cudaMemcpyAsync(dab.p, pin(p_ab), sizeof(uint32_t) * (R + 1), cudaMemcpyHostToDevice, st));
+    NF_CK(cgout.ensure(sizeof(CgOut) / sizeof(double) * (size_t)R + 1));
+    CgOut* outs = reinterpret_cast<CgOut*>(cgout.p);
     const double tol = prm[0].solve_tol > 0 ? prm[0].solve_tol : 1e-10;
     const int max_inner = prm[0].solve_max_iter > 0 ? prm[0].solve_max_iter : 20000;
     // Direct form when every realisation's band after reverse Cuthill-McKee
@@ -1292,21 +1351,28 @@ nf_status Engine::solve_graph(uint32_t n, const std::vector<uint32_t>& off, cons
     bool direct = false, bcr = false;
     uint32_t bmax = 0;
     size_t nblk = 0;  // blocks of 32 unknowns over all realisations (block cyclic reduction)
-    if (na > 0 && method != 2) {
-        std::vector<uint32_t> hrow(na + 1), hcol(nnz);
-        std::vector<double> hgr(na);
-        NF_CK(cudaMemcpyAsync(hrow.data(), rowp.p, sizeof(uint32_t) * (na + 1), cudaMemcpyDeviceToHost, st));
-        if (nnz) NF_CK(cudaMemcpyAsync(hcol.data(), col.p, sizeof(uint32_t) * nnz, cudaMemcpyDeviceToHost, st));
-        NF_CK(cudaMemcpyAsync(hgr.data(), chain64.p + na, sizeof(double) * na, cudaMemcpyDeviceToHost, st));
+    if (want_order) {
+        uint32_t* hrow = reinterpret_cast<uint32_t*>(pin(p_row));
+        uint32_t* hcol = reinterpret_cast<uint32_t*>(pin(p_col));
+        double* hgr = reinterpret_cast<double*>(pin(p_gr));
+        NF_CK(cudaMemcpyAsync(hrow, rowp.p, sizeof(uint32_t) * (na + 1), cudaMemcpyDeviceToHost, st));
+        if (nnz) NF_CK(cudaMemcpyAsync(hcol, col.p, sizeof(uint32_t) * nnz, cudaMemcpyDeviceToHost, st));
+        NF_CK(cudaMemcpyAsync(hgr, chain64.p + na, sizeof(double) * na, cudaMemcpyDeviceToHost, st));
         NF_CK(cudaStreamSynchronize(st));
-        std::vector<uint32_t> hperm(na), hbw(R, 0);
-        std::vector<unsigned long long> hoff(R + 1, 0);
+        uint32_t* hperm = reinterpret_cast<uint32_t*>(pin(p_perm));
+        uint32_t* hbo = reinterpret_cast<uint32_t*>(pin(p_bo));
+        uint32_t* hbw = reinterpret_cast<uint32_t*>(pin(p_bw));
+        unsigned long long* hoff = reinterpret_cast<unsigned long long*>(pin(p_hoff));
+        hoff[0] = 0;
         bool fits = true, narrow = true;  // every band so far: banded form / block cyclic reduction
         int r = 0;
+        std::vector<uint32_t> lrow, lcol, lp;
+        std::vector<char> up;
         for (; r < R && (fits || narrow); ++r) {
             const uint32_t b0 = A.habase[r], nr = A.habase[r + 1] - b0;
-            std::vector<uint32_t> lrow(nr + 1), lcol;
-            std::vector<char> up(nr, 0);
+            lrow.assign(nr + 1, 0);
+            lcol.clear();
+            up.assign(nr, 0);
             lcol.reserve(hrow[b0 + nr] - hrow[b0]);
             for (uint32_t i = 0; i < nr; ++i) {
                 lrow[i] = (uint32_t)lcol.size();
@@ -1314,7 +1380,6 @@ nf_status Engine::solve_graph(uint32_t n, const std::vector<uint32_t>& off, cons
                 if (A.chains && i + 1 < nr) up[i] = hgr[b0 + i] > 0.0 ? 1 : 0;
             }
             lrow[nr] = (uint32_t)lcol.size();
-            std::vector<uint32_t> lp;
             const uint32_t bw = nr ? rcm_order(nr, lrow, lcol, up, &lp) : 0;
             for (uint32_t i = 0; i < nr; ++i) hperm[b0 + i] = lp[i];
             hbw[r] = bw;
@@ -1324,7 +1389,7 @@ nf_status Engine::solve_graph(uint32_t n, const std::vector<uint32_t>& off, cons
             narrow = narrow && bw <= kBcrW;
         }
         const bool all = r == R;  // every realisation ordered
-        std::vector<uint32_t> hbo(R + 1, 0);
+        hbo[0] = 0;
         for (int q = 0; q < R; ++q) hbo[q + 1] = hbo[q] + (A.habase[q + 1] - A.habase[q] + kBcrW - 1) / kBcrW;
         nblk = hbo[R];
         bcr = all && narrow && method != 3 && (double)nblk * (kBcrPer + kBcrW) * sizeof(double) <= 4e9;
@@ -1337,18 +1402,18 @@ nf_status Engine::solve_graph(uint32_t n, const std::vector<uint32_t>& off, cons
         if (direct) {
             NF_CK(dcperm.ensure(na));
             NF_CK(dcwork.ensure(2 * (size_t)na + 2));
-            NF_CK(cudaMemcpyAsync(dcperm.p, hperm.data(), sizeof(uint32_t) * na, cudaMemcpyHostToDevice, st));
+            NF_CK(cudaMemcpyAsync(dcperm.p, hperm, sizeof(uint32_t) * na, cudaMemcpyHostToDevice, st));
             if (bcr) {
                 NF_CK(bcrbuf.ensure(nblk * (kBcrPer + kBcrW)));
                 NF_CK(bcroff.ensure(R + 1));
-                NF_CK(cudaMemcpyAsync(bcroff.p, hbo.data(), sizeof(uint32_t) * (R + 1), cudaMemcpyHostToDevice, st));
+                NF_CK(cudaMemcpyAsync(bcroff.p, hbo, sizeof(uint32_t) * (R + 1), cudaMemcpyHostToDevice, st));
             } else {
                 NF_CK(dcbw.ensure(R));
                 NF_CK(dcboff.ensure(R + 1));
                 NF_CK(dcband.ensure(2 * hoff[R] + na + 1));
-                NF_CK(cudaMemcpyAsync(dcbw.p, hbw.data(), sizeof(uint32_t) * R, cudaMemcpyHostToDevice, st));
-                NF_CK(cudaMemcpyAsync(dcboff.p, hoff.data(), sizeof(unsigned long long) * (R + 1),
-                                      cudaMemcpyHostToDevice, st));
+                NF_CK(cudaMemcpyAsync(dcbw.p, hbw, sizeof(uint32_t) * R, cudaMemcpyHostToDevice, st));
+                NF_CK(cudaMemcpyAsync(dcboff.p, hoff, sizeof(unsigned long long) * (R + 1), cudaMemcpyHostToDevice,
+                                      st));
             }
         }
     }
@@ -1367,13 +1432,13 @@ nf_status Engine::solve_graph(uint32_t n, const std::vector<uint32_t>& off, cons
         float* f32 = reinterpret_cast<float*>(bcrbuf.p);
         NF_LAUNCH(kf32, R, kNtF, sh4, st)(R, dab.p, bcroff.p, dcperm.p, rowp.p, col.p, val64.p, diag64.p, chain64.p,
                                           A.chains ? 1 : 0, bvec.p, xvec.p, cgred.p, f32, f32 + nblk * kBcrPer,
-                                          dcwork.p, tol, 0, outs.p);
+                                          dcwork.p, tol, 0, outs);
         NF_CK(cudaGetLastError());
         // FP64 factors for the realisations whose FP32 factors stayed above
         // the tolerance (the others return at once): no host round trip
         NF_LAUNCH(kf64, R, kNtD, sh8, st)(R, dab.p, bcroff.p, dcperm.p, rowp.p, col.p, val64.p, diag64.p,
                                           chain64.p, A.chains ? 1 : 0, bvec.p, xvec.p, cgred.p, bcrbuf.p,
-                                          bcrbuf.p + nblk * kBcrPer, dcwork.p, tol, 1, outs.p);
+                                          bcrbuf.p + nblk * kBcrPer, dcwork.p, tol, 1, outs);
     } else if (direct && bmax <= kDcWin) {
         uint32_t nmax = 0;
         for (int r = 0; r < R; ++r) nmax = std::max(nmax, A.habase[r + 1] - A.habase[r]);
@@ -1385,10 +1450,10 @@ nf_status Engine::solve_graph(uint32_t n, const std::vector<uint32_t>& off, cons
         NF_LAUNCH(kf32, R, 256, sh4, st)(R, dab.p, dcboff.p, dcbw.p, dcperm.p, rowp.p, col.p,
                                                              val64.p, diag64.p, chain64.p, A.chains ? 1 : 0, bvec.p,
                                                              xvec.p, cgred.p, dcband.p, dcwork.p, tol, sh4 ? 1 : 0,
-                                                             outs.p);
+                                                             outs);
         NF_CK(cudaGetLastError());
-        std::vector<CgOut> h1(R);
-        NF_CK(cudaMemcpyAsync(h1.data(), outs.p, sizeof(CgOut) * R, cudaMemcpyDeviceToHost, st));
+        const CgOut* h1 = reinterpret_cast<const CgOut*>(pin(p_out));
+        NF_CK(cudaMemcpyAsync(pin(p_out), outs, sizeof(CgOut) * R, cudaMemcpyDeviceToHost, st));
         NF_CK(cudaStreamSynchronize(st));
         bool again = false;
         for (int r = 0; r < R; ++r) again |= h1[r].n > 0 && !(h1[r].res <= tol);
@@ -1399,16 +1464,16 @@ nf_status Engine::solve_graph(uint32_t n, const std::vector<uint32_t>& off, cons
             NF_LAUNCH(kf64, R, 256, sh8, st)(R, dab.p, dcboff.p, dcbw.p, dcperm.p, rowp.p, col.p,
                                                                   val64.p, diag64.p, chain64.p, A.chains ? 1 : 0,
                                                                   bvec.p, xvec.p, cgred.p, dcband.p, dcwork.p, tol,
-                                                                  sh8 ? 1 : 0, outs.p);
+                                                                  sh8 ? 1 : 0, outs);
         }
     } else if (direct) {
         NF_LAUNCH(k_dc_band<256>, R, 256, 0, st)(R, dab.p, dcboff.p, dcbw.p, dcperm.p, rowp.p, col.p, val64.p, diag64.p,
                                                 chain64.p, A.chains ? 1 : 0, bvec.p, xvec.p, cgred.p, dcband.p,
-                                                dcwork.p, tol, outs.p);
+                                                dcwork.p, tol, outs);
     } else {
         NF_LAUNCH(k_cg<512>, R, 512, 0, st)(R, dab.p, rowp.p, col.p, val32.p, val64.p, diag32.p, diag64.p, chain64.p,
                                      chain32.p, na, A.chains ? 1 : 0, bvec.p, xvec.p, cgred.p, cgbuf.p, tol, max_inner,
-                                     outs.p);
+                                     outs);
     }
     NF_CK(cudaGetLastError());
     tstop(KT_CG);
@@ -1416,11 +1481,11 @@ nf_status Engine::solve_graph(uint32_t n, const std::vector<uint32_t>& off, cons
         NF_LAUNCH(k_scatter_v, grid_for(nslot, 256), 256, 0, st)(nslot, act, aidx.p, xvec.p, parent.p, cflag.p, volt.p,
                                                                  errw);
     NF_CK(cudaGetLastError());
-    std::vector<CgOut> ho(R);
-    if (na) NF_CK(cudaMemcpyAsync(ho.data(), outs.p, sizeof(CgOut) * R, cudaMemcpyDeviceToHost, st));
+    const CgOut* ho = reinterpret_cast<const CgOut*>(pin(p_out));
+    if (na) NF_CK(cudaMemcpyAsync(pin(p_out), outs, sizeof(CgOut) * R, cudaMemcpyDeviceToHost, st));
+    else std::memset(pin(p_out), 0, sizeof(CgOut) * R);
     NF_CK(cudaEventRecord(ev.b, st));
     NF_CK(cudaEventSynchronize(ev.b));
-    outs.release();
     float ms = 0;
     NF_CK(cudaEventElapsedTime(&ms, ev.a, ev.b));
     {

@@ -288,16 +288,26 @@ __global__ void __launch_bounds__(kRegTPB) k_treg(uint32_t n, const uint32_t* __
                 if (!tube_cell(Re, per, u, &cell, img)) continue;
                 if (kFill) {
                     const uint32_t qd = tstart[cell] + atomicAdd(&tcnt[cell], 1u);
-                    if (qd < cap) {
-                        tent[qd] = tube_entry(id, img);
-                        tpos[qd] = q;  // the object's geometry beside its entry: the sweeps read it coalesced
-                        tdir[qd] = cq;
-                    }
+                    if (qd < cap) tent[qd] = tube_entry(id, img);
                     else atomicAdd(ovf, 1ull);
                 } else {
                     atomicAdd(&tcnt[cell], 1u);
                 }
             }
+    }
+}
+
+// The objects' geometry beside their entries (the sweeps then read it
+// coalesced): entry q's object through the source's geometry accessor, read
+// at random, written in entry order.
+template <class Src>
+__global__ void __launch_bounds__(256) k_treg_geom(uint32_t n, const uint32_t* __restrict__ ent,
+                                                   float4* __restrict__ epos, float4* __restrict__ edir, Src src) {
+    for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
+        float4 p, c;
+        src.geom(ent[q] >> kTubeIdShift, &p, &c);
+        epos[q] = p;
+        edir[q] = c;
     }
 }
 
