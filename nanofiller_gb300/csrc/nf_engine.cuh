@@ -178,6 +178,7 @@ struct Engine {
     DBuf<float4> trod_pos, trod_dir, tcnd_pos, tcnd_dir;  // each entry's object geometry
     DBuf<TItem> titems;
     size_t tit_cap = 1 << 20;
+    uint32_t tit_nseg = 0;  // cell segments of the last tube_items (its item count sits at tioff[tit_nseg])
     DBuf<uint32_t> tioff;
 
     // contacts
@@ -314,15 +315,18 @@ struct Engine {
     // old-rod test) into tcnd_*; then the work list of probes x targets.
     nf_status tube_register_rods(int stage);
     nf_status tube_register_cands(uint64_t slots, const uint32_t* ntot, bool alive_only);
+    // Work items of a tube sweep (probe entries at pstart, target entries at
+    // tstart, per-cell counts when compacted); pack: small cells in packed
+    // items (the generation's sweeps read both kinds).
     nf_status tube_items(const uint32_t* pstart, const uint32_t* tstart, const uint32_t* pcnt = nullptr,
-                         const uint32_t* tcnt = nullptr);
+                         const uint32_t* tcnt = nullptr, bool pack = false);
     // Compacts the candidate registration (tcnd_*) in place to the candidates
     // still alive; per-cell lengths in tcnd_cnt.
     nf_status tube_compact_cands();
     // Registers objects [0, n) of any source (stage-1 periodicity) into tcnd_*.
     template <class Src>
     nf_status tube_register_objects(uint32_t n, Src src);
-    const uint32_t* titem_count() const { return tioff.p + ntcell; }
+    const uint32_t* titem_count() const { return tioff.p + tit_nseg; }
     // Pinned host block for the per-round read-backs.
     uint8_t* hpin = nullptr;
     size_t hpin_cap = 0;

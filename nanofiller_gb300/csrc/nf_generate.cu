@@ -715,12 +715,66 @@ __global__ void __launch_bounds__(256) k_conf_exact(const Real* __restrict__ rea
 
 // ---------------------------------------------------------------------------
 // Tube sweeps of the generation (nf_tube.cuh): the pairs registered together
-// in a tube cell. Items are (<= 32 probe entries, <= kTSeg target entries) of
-// one cell; a lane holds a probe, the warp stages 32 targets at a time. Every
-// entry carries the image of its object's copy in the cell: the marking loop
-// works on the copies, the filters and the FP64 queue on the original
-// coordinates with the relative image (target copy image - probe copy image).
+// in a tube cell. A cell item is (<= 32 probe entries, <= kTSeg target
+// entries) of one cell: a lane holds a probe, the warp stages 32 targets at a
+// time. A packed item holds the small cells of a run of consecutive cells
+// (<= 32 probes and <= 32 targets in all): a lane holds a probe of any of
+// them and tests it against its own cell's targets (a range of the one
+// staged tile). Every entry carries the image of its object's copy in the
+// cell: the marking loop works on the copies, the filters and the FP64 queue
+// on the original coordinates with the relative image (target copy image -
+// probe copy image). Per-pair values come from the probe lane's realisation
+// and cell.
 // ---------------------------------------------------------------------------
+
+// Probe side of item I for this lane: entry index, cell, and (packed items)
+// the lane's target range in the tile; np / nt the item's probe and target
+// counts.
+struct TubeLane {
+    uint32_t np, nt, pe, cell, tlo, tlen;
+    bool packed;
+};
+
+__device__ __forceinline__ TubeLane tube_lane(const TItem& I, int lane, const uint32_t* __restrict__ pstart,
+                                              const uint32_t* __restrict__ tstart, const uint32_t* __restrict__ pcnt,
+                                              const uint32_t* __restrict__ tcnt, TubePack& pk) {
+    TubeLane L;
+    L.packed = (I.cnt & kPackBit) != 0u;
+    L.cell = I.cell;
+    L.tlo = 0;
+    L.tlen = 0;
+    if (L.packed) {
+        tube_pack_load(I, lane, pstart, tstart, pcnt, tcnt, pk);
+        L.np = (I.cnt >> 6) & 63u;
+        L.nt = (I.cnt >> 12) & 63u;
+        L.pe = 0;
+        if ((uint32_t)lane < L.np) {
+            const int k = tube_pack_find(pk.P, (uint32_t)lane);
+            L.pe = pk.ps[k] + ((uint32_t)lane - pk.P[k]);
+            L.cell = I.cell + (uint32_t)k;
+            L.tlo = pk.Q[k];
+            L.tlen = pk.nt[k];
+        }
+    } else {
+        L.np = I.cnt & 63u;
+        L.nt = I.cnt >> 6;
+        L.pe = I.pfirst + (uint32_t)lane;
+    }
+    return L;
+}
+
+// Target entry of tile slot `slot` (< the tile's count) of stage b, and its cell.
+__device__ __forceinline__ uint32_t tube_target(const TItem& I, const TubeLane& L, const TubePack& pk, uint32_t b,
+                                                uint32_t slot, uint32_t* cell) {
+    if (L.packed) {
+        const int k = tube_pack_find(pk.Q, slot);
+        *cell = I.cell + (uint32_t)k;
+        return pk.ts[k] + (slot - pk.Q[k]);
+    }
+    *cell = I.cell;
+    return I.tfirst + b + slot;
+}
+
 // Candidates (probe entries) against placed rods (target entries) of one tube
 // cell: cuda_OldExtIsectLB's job (inc/intersection_kern.h:245-364) on the
 // tube grid. Marking, hand-out, certificate and FP64 queue as k_old_tiles.
@@ -728,6 +782,8 @@ __global__ void __launch_bounds__(kTPB, 6) k_tube_old(const Real* __restrict__ r
                                                    const uint32_t* __restrict__ toffs,
                                                    const uint32_t* __restrict__ nitems, uint32_t icap,
                                                    const TItem* __restrict__ items,
+                                                   const uint32_t* __restrict__ pstart,
+                                                   const uint32_t* __restrict__ tstart,
                                                    const uint32_t* __restrict__ pent,
                                                    const float4* __restrict__ cpos, const float4* __restrict__ cdir,
                                                    const uint32_t* __restrict__ tent,
@@ -736,8 +792,9 @@ __global__ void __launch_bounds__(kTPB, 6) k_tube_old(const Real* __restrict__ r
                                                    unsigned long long xcap, unsigned long long* __restrict__ ctr) {
     constexpr int kW = kTPB / 32;
     __shared__ TubeTile tiles[kW];
+    __shared__ TubePack packs[kW];
     __shared__ float4 ppos[kW][32], pdir[kW][32];
-    __shared__ uint32_t pcid[kW][32], pim[kW][32];
+    __shared__ uint32_t pcid[kW][32], pim[kW][32], preal[kW][32];
     __shared__ int msp[kW][32];
     __shared__ uint32_t msm[kW][32];
     __shared__ uint16_t mq2[kW][64];
@@ -752,17 +809,18 @@ __global__ void __launch_bounds__(kTPB, 6) k_tube_old(const Real* __restrict__ r
         const TItem I = nxt;
         if (it + stride < n) nxt = items[it + stride];
         ++nitem;
-        const uint32_t np = I.cnt & 63u, nt = I.cnt >> 6;
-        const Real& Re = reals[find_real(toffs, R, I.cell)];
-        const bool have = (uint32_t)lane < np;
+        const TubeLane L = tube_lane(I, lane, pstart, tstart, nullptr, nullptr, packs[w]);
+        const int rl = find_real(toffs, R, L.cell);
+        const Real& Re = reals[rl];
+        const bool have = (uint32_t)lane < L.np;
         uint32_t cid = 0, ipc = 0;
         float4 pA = make_float4(0, 0, 0, 0), cA = pA;
         if (have) {
-            const uint32_t e = pent[I.pfirst + lane];
+            const uint32_t e = pent[L.pe];
             cid = e >> kTubeIdShift;
             ipc = e & 63u;
-            pA = cpos[I.pfirst + lane];
-            cA = cdir[I.pfirst + lane];
+            pA = cpos[L.pe];
+            cA = cdir[L.pe];
         }
         bool alive = have && vst[cid] != ST_REJ_OLD;
         __syncwarp();
@@ -770,6 +828,7 @@ __global__ void __launch_bounds__(kTPB, 6) k_tube_old(const Real* __restrict__ r
         pdir[w][lane] = cA;
         pcid[w][lane] = cid;
         pim[w][lane] = ipc;
+        preal[w][lane] = (uint32_t)rl;
         int ia[3];
         img_of(ipc, ia);
         // the probe's copy in this cell
@@ -780,18 +839,21 @@ __global__ void __launch_bounds__(kTPB, 6) k_tube_old(const Real* __restrict__ r
         const float errA = 4e-6f * (1.0f + hA2) + 2.0f * Re.slack;
         const float thA = (cA.w * Re.scf + Re.sep + Re.eps) * 1.0002f, scf2 = Re.scf * 1.0002f;
         unsigned dead = 0;
-        for (uint32_t b = 0; b < nt; b += kWT) {
+        for (uint32_t b = 0; b < L.nt; b += kWT) {
             if (!__any_sync(0xffffffffu, alive)) break;
-            const uint32_t m = min((uint32_t)kWT, nt - b);
+            const uint32_t m = min((uint32_t)kWT, L.nt - b);
             if ((uint32_t)lane < m) {
-                const uint32_t e = tent[I.tfirst + b + lane];
+                uint32_t tc;
+                const uint32_t q = tube_target(I, L, packs[w], b, (uint32_t)lane, &tc);
+                const Real& Rt = L.packed ? reals[find_real(toffs, R, tc)] : Re;
+                const uint32_t e = tent[q];
                 const uint32_t k = e >> kTubeIdShift;
-                const float4 p = rpos[I.tfirst + b + lane], c = rdir[I.tfirst + b + lane];
+                const float4 p = rpos[q], c = rdir[q];
                 int ib[3];
                 img_of(e & 63u, ib);
                 T.p[lane] = p;
-                T.ps[lane] = make_float4(p.x + ib[0] * Re.L[0], p.y + ib[1] * Re.L[1], p.z + ib[2] * Re.L[2],
-                                         (p.w * 0.5f + c.w + Re.eps + c.w * Re.scf) * 1.000002f);
+                T.ps[lane] = make_float4(p.x + ib[0] * Rt.L[0], p.y + ib[1] * Rt.L[1], p.z + ib[2] * Rt.L[2],
+                                         (p.w * 0.5f + c.w + Rt.eps + c.w * Rt.scf) * 1.000002f);
                 T.c[lane] = c;
                 T.id[lane] = k;
                 T.im[lane] = e & 63u;
@@ -799,24 +861,28 @@ __global__ void __launch_bounds__(kTPB, 6) k_tube_old(const Real* __restrict__ r
                 T.ps[lane] = make_float4(kFar, kFar, kFar, 0.0f);
             }
             __syncwarp();
+            const uint32_t lo = L.packed ? L.tlo : 0u, len = L.packed ? L.tlen : m;
             uint32_t mask = 0;
             if (alive) {
-                tests += m;
-                const uint32_t m8 = (m + 7u) & ~7u;
-                for (uint32_t j0 = 0; j0 < m8; j0 += 8) {
+                tests += len;
+                for (uint32_t u0 = 0; u0 < len; u0 += 8) {
 #pragma unroll
                     for (uint32_t jj = 0; jj < 8; ++jj) {
-                        const float4 tq = T.ps[j0 + jj];
-                        const float bx = tq.x - ax, by = tq.y - ay, bz = tq.z - az;
-                        const float4 cB = T.c[j0 + jj];
-                        const float nx = cA.y * cB.z - cA.z * cB.y;
-                        const float ny = cA.z * cB.x - cA.x * cB.z;
-                        const float nz = cA.x * cB.y - cA.y * cB.x;
-                        const float nn = nx * nx + ny * ny + nz * nz;
-                        const float nb = fabsf(nx * bx + ny * by + nz * bz) - fmaf(4e-6f, tq.w, errA);
-                        const float thL = fmaf(cB.w, scf2, thA);
-                        const bool lfar = nn > 1e-4f && nb > 0.0f && nb * nb > thL * thL * nn;
-                        if (!lfar && capsule_near(bx, by, bz, cA.x, cA.y, cA.z, hAe, tq.w, hC)) mask |= 1u << (j0 + jj);
+                        const uint32_t u = u0 + jj;
+                        if (u < len) {
+                            const uint32_t j = lo + u;
+                            const float4 tq = T.ps[j];
+                            const float bx = tq.x - ax, by = tq.y - ay, bz = tq.z - az;
+                            const float4 cB = T.c[j];
+                            const float nx = cA.y * cB.z - cA.z * cB.y;
+                            const float ny = cA.z * cB.x - cA.x * cB.z;
+                            const float nz = cA.x * cB.y - cA.y * cB.x;
+                            const float nn = nx * nx + ny * ny + nz * nz;
+                            const float nb = fabsf(nx * bx + ny * by + nz * bz) - fmaf(4e-6f, tq.w, errA);
+                            const float thL = fmaf(cB.w, scf2, thA);
+                            const bool lfar = nn > 1e-4f && nb > 0.0f && nb * nb > thL * thL * nn;
+                            if (!lfar && capsule_near(bx, by, bz, cA.x, cA.y, cA.z, hAe, tq.w, hC)) mask |= 1u << j;
+                        }
                     }
                 }
             }
@@ -824,24 +890,26 @@ __global__ void __launch_bounds__(kTPB, 6) k_tube_old(const Real* __restrict__ r
                 if ((dead >> pl) & 1u) return false;
                 int img[3];
                 if (!rel_img(pim[w][pl], T.im[t], img)) return false;
+                const Real& Rp = reals[preal[w][pl]];
                 const float4 dA = pdir[w][pl], cB = T.c[t];
-                return !line_far(ppos[w][pl], dA, T.p[t], cB, img[0] * Re.L[0], img[1] * Re.L[1], img[2] * Re.L[2],
-                                 (cB.w + dA.w) * Re.scf + Re.sep + Re.eps, Re.slack);
+                return !line_far(ppos[w][pl], dA, T.p[t], cB, img[0] * Rp.L[0], img[1] * Rp.L[1], img[2] * Rp.L[2],
+                                 (cB.w + dA.w) * Rp.scf + Rp.sep + Rp.eps, Rp.slack);
             };
             ++ntile;
             nmark += __popc(mask);
             const int kept_ = for_marked_pairs(mask, lane, msp[w], msm[w], mq2[w], keep, [&](bool valid, int pl, int t) {
                 bool hit = false;
                 if (valid && !((dead >> pl) & 1u)) {
+                    const Real& Rp = reals[preal[w][pl]];
                     const float4 qA = ppos[w][pl], dA = pdir[w][pl];
                     const float4 pB = T.p[t], cB = T.c[t];
                     int img[3];
                     rel_img(pim[w][pl], T.im[t], img);
-                    const float sx = img[0] * Re.L[0], sy = img[1] * Re.L[1], sz = img[2] * Re.L[2];
-                    const float thr = (cB.w + dA.w) * Re.scf + Re.sep + Re.eps;
-                    if (maybe_near(qA, dA, pB, cB, sx, sy, sz, thr, Re.eps, Re.slack)) {
+                    const float sx = img[0] * Rp.L[0], sy = img[1] * Rp.L[1], sz = img[2] * Rp.L[2];
+                    const float thr = (cB.w + dA.w) * Rp.scf + Rp.sep + Rp.eps;
+                    if (maybe_near(qA, dA, pB, cB, sx, sy, sz, thr, Rp.eps, Rp.slack)) {
                         const uint32_t c = pcid[w][pl];
-                        if (!Re.typo && certain_hit(qA, dA, pB, cB, sx, sy, sz, thr, Re.eps, Re.slack)) {
+                        if (!Rp.typo && certain_hit(qA, dA, pB, cB, sx, sy, sz, thr, Rp.eps, Rp.slack)) {
                             hit = true;
                             ++cert;
                             vst[c] = ST_REJ_OLD;
@@ -878,6 +946,8 @@ __global__ void __launch_bounds__(kTPB, 6) k_tube_conf(const Real* __restrict__ 
                                                     const uint32_t* __restrict__ toffs,
                                                     const uint32_t* __restrict__ nitems, uint32_t icap,
                                                     const TItem* __restrict__ items,
+                                                    const uint32_t* __restrict__ start,
+                                                    const uint32_t* __restrict__ cnt,
                                                     const uint32_t* __restrict__ ent,
                                                     const float4* __restrict__ cpos, const float4* __restrict__ cdir,
                                                     uint32_t* __restrict__ ccnt, uint32_t* __restrict__ clist,
@@ -885,8 +955,9 @@ __global__ void __launch_bounds__(kTPB, 6) k_tube_conf(const Real* __restrict__ 
                                                     unsigned long long xcap, unsigned long long* __restrict__ ctr) {
     constexpr int kW = kTPB / 32;
     __shared__ TubeTile tiles[kW];
+    __shared__ TubePack packs[kW];
     __shared__ float4 ppos[kW][32], pdir[kW][32];
-    __shared__ uint32_t pcid[kW][32], pim[kW][32];
+    __shared__ uint32_t pcid[kW][32], pim[kW][32], preal[kW][32], pcel[kW][32];
     __shared__ int msp[kW][32];
     __shared__ uint32_t msm[kW][32];
     __shared__ uint16_t mq2[kW][64];
@@ -900,40 +971,46 @@ __global__ void __launch_bounds__(kTPB, 6) k_tube_conf(const Real* __restrict__ 
         const TItem I = nxt;
         if (it + stride < n) nxt = items[it + stride];
         ++nitem;
-        const uint32_t np = I.cnt & 63u, nt = I.cnt >> 6;
-        const Real& Re = reals[find_real(toffs, R, I.cell)];
-        const bool have = (uint32_t)lane < np;
+        const TubeLane L = tube_lane(I, lane, start, start, cnt, cnt, packs[w]);
+        const int rl = find_real(toffs, R, L.cell);
+        const Real& Re = reals[rl];
+        const bool have = (uint32_t)lane < L.np;
         uint32_t cid = 0, ipc = 0;
         float4 pA = make_float4(0, 0, 0, 0), cA = pA;
         if (have) {
-            const uint32_t e = ent[I.pfirst + lane];
+            const uint32_t e = ent[L.pe];
             cid = e >> kTubeIdShift;
             ipc = e & 63u;
-            pA = cpos[I.pfirst + lane];
-            cA = cdir[I.pfirst + lane];
+            pA = cpos[L.pe];
+            cA = cdir[L.pe];
         }
         __syncwarp();
         ppos[w][lane] = pA;
         pdir[w][lane] = cA;
         pcid[w][lane] = cid;
         pim[w][lane] = ipc;
+        preal[w][lane] = (uint32_t)rl;
+        pcel[w][lane] = L.cell;
         int ia[3];
         img_of(ipc, ia);
         const float ax = pA.x + ia[0] * Re.L[0], ay = pA.y + ia[1] * Re.L[1], az = pA.z + ia[2] * Re.L[2];
         const float hA2 = (pA.w * 0.5f + cA.w + Re.eps + cA.w * Re.scf + Re.sep + Re.eps) * 1.000002f + Re.slack;
         const float hAe = pA.w * 0.5f + cA.w + Re.eps;
         const float hC = (cA.w * Re.scf + Re.sep + Re.eps) * 1.000002f + 2.0f * Re.slack + 4e-6f * (1.0f + hA2);
-        for (uint32_t b = 0; b < nt; b += kWT) {
-            const uint32_t m = min((uint32_t)kWT, nt - b);
+        for (uint32_t b = 0; b < L.nt; b += kWT) {
+            const uint32_t m = min((uint32_t)kWT, L.nt - b);
             if ((uint32_t)lane < m) {
-                const uint32_t e = ent[I.tfirst + b + lane];
+                uint32_t tc;
+                const uint32_t q = tube_target(I, L, packs[w], b, (uint32_t)lane, &tc);
+                const Real& Rt = L.packed ? reals[find_real(toffs, R, tc)] : Re;
+                const uint32_t e = ent[q];
                 const uint32_t k = e >> kTubeIdShift;
-                const float4 p = cpos[I.tfirst + b + lane], c = cdir[I.tfirst + b + lane];
+                const float4 p = cpos[q], c = cdir[q];
                 int ib[3];
                 img_of(e & 63u, ib);
                 T.p[lane] = p;
-                T.ps[lane] = make_float4(p.x + ib[0] * Re.L[0], p.y + ib[1] * Re.L[1], p.z + ib[2] * Re.L[2],
-                                         (p.w * 0.5f + c.w + Re.eps + c.w * Re.scf) * 1.000002f);
+                T.ps[lane] = make_float4(p.x + ib[0] * Rt.L[0], p.y + ib[1] * Rt.L[1], p.z + ib[2] * Rt.L[2],
+                                         (p.w * 0.5f + c.w + Rt.eps + c.w * Rt.scf) * 1.000002f);
                 T.c[lane] = c;
                 T.id[lane] = k;
                 T.im[lane] = e & 63u;
@@ -942,18 +1019,21 @@ __global__ void __launch_bounds__(kTPB, 6) k_tube_conf(const Real* __restrict__ 
                 T.id[lane] = 0xffffffffu;
             }
             __syncwarp();
+            const uint32_t lo = L.packed ? L.tlo : 0u, len = L.packed ? L.tlen : m;
             uint32_t mask = 0, emask = 0;  // marked pairs; earlier survivors
             if (have) {
-                const uint32_t m8 = (m + 7u) & ~7u;
-                for (uint32_t j0 = 0; j0 < m8; j0 += 8) {
+                for (uint32_t u0 = 0; u0 < len; u0 += 8) {
 #pragma unroll
                     for (uint32_t jj = 0; jj < 8; ++jj) {
-                        const uint32_t j = j0 + jj;
-                        const float4 tq = T.ps[j];
-                        const float bx = tq.x - ax, by = tq.y - ay, bz = tq.z - az;
-                        const uint32_t bit = T.id[j] < cid ? (1u << j) : 0u;
-                        emask |= bit;
-                        if (capsule_near(bx, by, bz, cA.x, cA.y, cA.z, hAe, tq.w, hC)) mask |= bit;
+                        const uint32_t u = u0 + jj;
+                        if (u < len) {
+                            const uint32_t j = lo + u;
+                            const float4 tq = T.ps[j];
+                            const float bx = tq.x - ax, by = tq.y - ay, bz = tq.z - az;
+                            const uint32_t bit = T.id[j] < cid ? (1u << j) : 0u;
+                            emask |= bit;
+                            if (capsule_near(bx, by, bz, cA.x, cA.y, cA.z, hAe, tq.w, hC)) mask |= bit;
+                        }
                     }
                 }
                 tests += __popc(emask);
@@ -961,33 +1041,36 @@ __global__ void __launch_bounds__(kTPB, 6) k_tube_conf(const Real* __restrict__ 
             auto keep = [&](int pl, int t) {
                 int img[3];
                 if (!rel_img(pim[w][pl], T.im[t], img)) return false;
+                const Real& Rp = reals[preal[w][pl]];
                 const float4 dA = pdir[w][pl], cB = T.c[t];
-                return !line_far(ppos[w][pl], dA, T.p[t], cB, img[0] * Re.L[0], img[1] * Re.L[1], img[2] * Re.L[2],
-                                 (cB.w + dA.w) * Re.scf + Re.sep + Re.eps, Re.slack);
+                return !line_far(ppos[w][pl], dA, T.p[t], cB, img[0] * Rp.L[0], img[1] * Rp.L[1], img[2] * Rp.L[2],
+                                 (cB.w + dA.w) * Rp.scf + Rp.sep + Rp.eps, Rp.slack);
             };
             ++ntile;
             nmark += __popc(mask);
             const int kept_ = for_marked_pairs(mask, lane, msp[w], msm[w], mq2[w], keep, [&](bool valid, int pl, int t) {
                 if (!valid) return;
+                const Real& Rp = reals[preal[w][pl]];
                 const float4 qA = ppos[w][pl], dA = pdir[w][pl];
                 const float4 pB = T.p[t], cB = T.c[t];
                 int img[3];
                 rel_img(pim[w][pl], T.im[t], img);
-                const float sx = img[0] * Re.L[0], sy = img[1] * Re.L[1], sz = img[2] * Re.L[2];
-                const float thr = (cB.w + dA.w) * Re.scf + Re.sep + Re.eps;
-                if (maybe_near(qA, dA, pB, cB, sx, sy, sz, thr, Re.eps, Re.slack)) {
+                const float sx = img[0] * Rp.L[0], sy = img[1] * Rp.L[1], sz = img[2] * Rp.L[2];
+                const float thr = (cB.w + dA.w) * Rp.scf + Rp.sep + Rp.eps;
+                if (maybe_near(qA, dA, pB, cB, sx, sy, sz, thr, Rp.eps, Rp.slack)) {
                     const uint32_t c = pcid[w][pl];
+                    const uint32_t cell = pcel[w][pl];
                     float t0 = 0.0f, t1 = 0.0f;
-                    if (!Re.typo && certain_hit(qA, dA, pB, cB, sx, sy, sz, thr, Re.eps, Re.slack, &t0, &t1)) {
+                    if (!Rp.typo && certain_hit(qA, dA, pB, cB, sx, sy, sz, thr, Rp.eps, Rp.slack, &t0, &t1)) {
                         // listed once: by the cell of the midpoint of the two feet
-                        if (tube_claims(Re, Re.per_gen, I.cell, pim[w][pl], qA, dA, pB, cB, sx, sy, sz, t0, t1)) {
+                        if (tube_claims(Rp, Rp.per_gen, cell, pim[w][pl], qA, dA, pB, cB, sx, sy, sz, t0, t1)) {
                             ++cert;
                             uint32_t slot = atomicAdd(&ccnt[c], 1u);
                             if (slot < (uint32_t)kConflictCap) clist[(size_t)c * kConflictCap + slot] = T.id[t];
                             else ++ovf;
                         }
                     } else {
-                        xq_push_cell(xq, xqc, xcap, &ctr[C_XQ_CONF], xq_pack(c, T.id[t], img), I.cell);
+                        xq_push_cell(xq, xqc, xcap, &ctr[C_XQ_CONF], xq_pack(c, T.id[t], img), cell);
                     }
                 }
             });
@@ -1290,17 +1373,22 @@ nf_status Engine::tube_register_cands(uint64_t slots, const uint32_t* ntot, bool
 }
 
 nf_status Engine::tube_items(const uint32_t* pstart, const uint32_t* tstart, const uint32_t* pcnt,
-                              const uint32_t* tcnt) {
-    NF_CK(icnt.ensure((size_t)ntcell + 1));
-    NF_CK(tioff.ensure((size_t)ntcell + 1));
+                              const uint32_t* tcnt, bool pack) {
+    const uint32_t nseg = (ntcell + 31u) / 32u;
+    NF_CK(icnt.ensure((size_t)nseg + 1));
+    NF_CK(tioff.ensure((size_t)nseg + 1));
     NF_CK(titems.ensure(tit_cap));
-    NF_LAUNCH(k_titem_count, grid_for((size_t)ntcell + 1, 256), 256, 0, st)(ntcell, pstart, tstart, pcnt, tcnt,
-                                                                           icnt.p);
+    tit_nseg = nseg;
+    const unsigned g = (unsigned)std::max<size_t>(1, std::min<size_t>(((size_t)nseg * 32 + 255) / 256, (size_t)nsm * 64));
+    auto kcount = k_titem<false>;
+    auto kfill = k_titem<true>;
+    NF_LAUNCH(kcount, g, 256, 0, st)(ntcell, pack ? 1 : 0, pstart, tstart, pcnt, tcnt, icnt.p, nullptr, nullptr, 0u,
+                                     nullptr);
     NF_CK(cudaGetLastError());
-    nf_status s = scan_u32(icnt.p, tioff.p, (size_t)ntcell + 1);
+    nf_status s = scan_u32(icnt.p, tioff.p, (size_t)nseg + 1);
     if (s != NF_OK) return s;
-    NF_LAUNCH(k_titem_fill, grid_for(ntcell, 256), 256, 0, st)(ntcell, pstart, tstart, pcnt, tcnt, tioff.p,
-                                                               titems.p, (uint32_t)titems.cap, ctr.p + C_ITEMS);
+    NF_LAUNCH(kfill, g, 256, 0, st)(ntcell, pack ? 1 : 0, pstart, tstart, pcnt, tcnt, nullptr, tioff.p, titems.p,
+                                    (uint32_t)titems.cap, ctr.p + C_ITEMS);
     NF_CK(cudaGetLastError());
     return NF_OK;
 }
@@ -1793,10 +1881,11 @@ nf_status Engine::generate() {
             s = tube_register_cands(slots, ntot, true);
             if (s != NF_OK) return s;
             cands_registered = true;
-            s = tube_items(tcnd_start.p, trod_start.p);
+            s = tube_items(tcnd_start.p, trod_start.p, nullptr, nullptr, true);
             if (s != NF_OK) return s;
             NF_LAUNCH(k_tube_old, persistent_grid(k_tube_old), kTPB, 0, st)(dreal.p, R, toffs.p, titem_count(),
-                                                    (uint32_t)titems.cap, titems.p, tcnd_ent.p, tcnd_pos.p, tcnd_dir.p,
+                                                    (uint32_t)titems.cap, titems.p, tcnd_start.p, trod_start.p,
+                                                    tcnd_ent.p, tcnd_pos.p, tcnd_dir.p,
                                                     trod_ent.p, trod_pos.p, trod_dir.p, state.p, xq.p, xq.cap, ctr.p);
             NF_CK(cudaGetLastError());
             NF_LAUNCH(k_old_exact, xg, 256, 0, st)(dreal.p, xq.p, nullptr, ctr.p + C_XQ_OLD, xq.cap, cpos.p, cdir.p,
@@ -1834,7 +1923,7 @@ nf_status Engine::generate() {
                 s = tube_register_cands(slots, ntot, true);
             }
             if (s != NF_OK) return s;
-            s = tube_items(tcnd_start.p, tcnd_start.p, scnt, scnt);
+            s = tube_items(tcnd_start.p, tcnd_start.p, scnt, scnt, true);
             if (s != NF_OK) return s;
         } else {
             s = bin_survivors();
@@ -1848,7 +1937,8 @@ nf_status Engine::generate() {
         if (tube) {
             NF_CK(xqc.ensure(xq2.cap));
             NF_LAUNCH(k_tube_conf, persistent_grid(k_tube_conf), kTPB, 0, st)(dreal.p, R, toffs.p, titem_count(),
-                                                    (uint32_t)titems.cap, titems.p, tcnd_ent.p, tcnd_pos.p, tcnd_dir.p,
+                                                    (uint32_t)titems.cap, titems.p, tcnd_start.p, scnt,
+                                                    tcnd_ent.p, tcnd_pos.p, tcnd_dir.p,
                                                     ccnt.p, clist.p, xq2.p, xqc.p, xq2.cap, ctr.p);
         } else {
             NF_LAUNCH(k_conf_tiles, persistent_grid(k_conf_tiles), kTPB, 0, st)(dreal.p, item_count(), (uint32_t)items.cap, items.p, aperm.p, apos.p,

@@ -347,10 +347,18 @@ static __global__ void k_treg_compact(uint32_t ncell, const uint32_t* __restrict
     }
 }
 
-// Work items of the tube sweeps: per cell with probes and targets, probe
-// chunks of <= 32 times target segments of <= kTSeg. Item layout (16 B):
-// first probe entry, first target entry, cell, np | nt << 6.
+// Work items of the tube sweeps. Item layout (16 B): first probe entry,
+// first target entry, cell, count word.
+// - A cell item: probe chunks of <= 32 times target segments of <= kTSeg of
+//   one cell; count word np | nt << 6.
+// - A packed item (kPackBit set): a run of consecutive cells from `cell`
+//   whose small cells (1-32 probes and 1-32 targets each) hold <= 32 probes
+//   and <= 32 targets together; count word span | np << 6 | nt << 12 | bit.
+//   A lane takes one probe of any of them and tests it against its own cell's
+//   targets, so the warp's lanes fill up where cells hold a few objects each.
+// Cells that are not small get cell items.
 constexpr uint32_t kTSeg = 128;
+constexpr uint32_t kPackBit = 0x80000000u;
 
 // Entries of cell c: [start[c], start[c] + cnt[c]) when a count array is
 // given (a list compacted in place), else [start[c], start[c + 1]).
@@ -358,36 +366,137 @@ __device__ __forceinline__ uint32_t tube_count(const uint32_t* start, const uint
     return cnt ? cnt[c] : start[c + 1] - start[c];
 }
 
-static __global__ void k_titem_count(uint32_t ncell, const uint32_t* __restrict__ pstart,
-                              const uint32_t* __restrict__ tstart, const uint32_t* __restrict__ pcnt,
-                              const uint32_t* __restrict__ tcnt, uint32_t* __restrict__ icnt) {
-    const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c > ncell) return;
-    if (c == ncell) { icnt[c] = 0; return; }
-    const uint32_t np = tube_count(pstart, pcnt, c), nt = tube_count(tstart, tcnt, c);
-    icnt[c] = (np && nt) ? ((np + 31u) / 32u) * ((nt + kTSeg - 1u) / kTSeg) : 0u;
+__device__ __forceinline__ bool tube_small(uint32_t np, uint32_t nt) {
+    return np != 0u && nt != 0u && np <= 32u && nt <= 32u;
 }
 
 struct TItem {
-    uint32_t pfirst, tfirst, cell, cnt;  // cnt = np | nt << 6
+    uint32_t pfirst, tfirst, cell, cnt;
 };
 
-static __global__ void k_titem_fill(uint32_t ncell, const uint32_t* __restrict__ pstart, const uint32_t* __restrict__ tstart,
-                             const uint32_t* __restrict__ pcnt, const uint32_t* __restrict__ tcnt,
-                             const uint32_t* __restrict__ ioff, TItem* __restrict__ items, uint32_t cap,
-                             unsigned long long* __restrict__ imax) {
-    const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c == 0) atomicMax(imax, (unsigned long long)ioff[ncell]);
-    if (c >= ncell) return;
-    const uint32_t k0 = ioff[c], k1 = ioff[c + 1];
-    if (k1 == k0) return;
-    const uint32_t p0 = pstart[c], np = tube_count(pstart, pcnt, c), t0 = tstart[c], nt = tube_count(tstart, tcnt, c);
-    const uint32_t segs = (nt + kTSeg - 1u) / kTSeg;
-    for (uint32_t k = k0; k < k1 && k < cap; ++k) {
-        const uint32_t idx = k - k0, a = (idx / segs) * 32u, b = (idx % segs) * kTSeg;
-        const uint32_t pa = min(32u, np - a), tb = min(kTSeg, nt - b);
-        items[k] = TItem{p0 + a, t0 + b, c, pa | (tb << 6)};
+__device__ __forceinline__ uint32_t warp_excl_scan(uint32_t v, int lane, uint32_t* total) {
+    uint32_t incl = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t u = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += u;
     }
+    *total = __shfl_sync(0xffffffffu, incl, 31);
+    return incl - v;
+}
+
+// One warp per segment of 32 consecutive cells: count pass (items per
+// segment into icnt) or fill pass (items at ioff[segment]). With pack, the
+// segment's small cells go into packed items, greedily in cell order; the
+// other cells (and every cell without pack) get cell items.
+template <bool kFill>
+__global__ void __launch_bounds__(256) k_titem(uint32_t ncell, int pack, const uint32_t* __restrict__ pstart,
+                                               const uint32_t* __restrict__ tstart, const uint32_t* __restrict__ pcnt,
+                                               const uint32_t* __restrict__ tcnt, uint32_t* __restrict__ icnt,
+                                               const uint32_t* __restrict__ ioff, TItem* __restrict__ items,
+                                               uint32_t cap, unsigned long long* __restrict__ imax) {
+    const int lane = threadIdx.x & 31;
+    const uint32_t nseg = (ncell + 31u) / 32u;
+    if (kFill && blockIdx.x == 0 && threadIdx.x == 0) atomicMax(imax, (unsigned long long)ioff[nseg]);
+    if (!kFill && blockIdx.x == 0 && threadIdx.x == 0) icnt[nseg] = 0;
+    const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
+    for (uint32_t sg = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; sg < nseg; sg += nw) {
+        const uint32_t c = sg * 32u + (uint32_t)lane;
+        uint32_t np = 0, nt = 0;
+        if (c < ncell) {
+            np = tube_count(pstart, pcnt, c);
+            nt = tube_count(tstart, tcnt, c);
+        }
+        const bool small = pack && tube_small(np, nt);
+        const uint32_t nbig = (!small && np && nt) ? ((np + 31u) / 32u) * ((nt + kTSeg - 1u) / kTSeg) : 0u;
+        // greedy groups of the small cells: a group ends before the first
+        // small cell that would take it past 32 probes or 32 targets
+        uint32_t ta, tb;
+        const uint32_t ea = warp_excl_scan(small ? np : 0u, lane, &ta);
+        const uint32_t eb = warp_excl_scan(small ? nt : 0u, lane, &tb);
+        const uint32_t ia = ea + (small ? np : 0u), ib = eb + (small ? nt : 0u);
+        unsigned starts = 0;
+        const unsigned smask = __ballot_sync(0xffffffffu, small);
+        if (smask) {
+            int g = __ffs(smask) - 1;
+            for (;;) {
+                starts |= 1u << g;
+                const uint32_t ba = __shfl_sync(0xffffffffu, ea, g), bb = __shfl_sync(0xffffffffu, eb, g);
+                const unsigned over = __ballot_sync(0xffffffffu, lane > g && small && (ia - ba > 32u || ib - bb > 32u));
+                if (!over) break;
+                g = __ffs(over) - 1;
+            }
+        }
+        const bool st = (starts >> lane) & 1u;
+        uint32_t tot;
+        const uint32_t off = warp_excl_scan((st ? 1u : 0u) + nbig, lane, &tot);
+        // every lane's group end (the next start, or the segment's end)
+        const unsigned later = starts & ~((2u << lane) - 1u);
+        const int end = later ? __ffs(later) - 1 : 32;
+        const uint32_t ia_end = __shfl_sync(0xffffffffu, ia, end - 1), ib_end = __shfl_sync(0xffffffffu, ib, end - 1);
+        if (!kFill) {
+            if (lane == 0) icnt[sg] = tot;
+            continue;
+        }
+        uint32_t k = ioff[sg] + off;
+        if (st && k < cap) {
+            const uint32_t span = (uint32_t)(end - lane), gp = ia_end - ea, gt = ib_end - eb;
+            items[k] = TItem{0u, 0u, c, kPackBit | span | (gp << 6) | (gt << 12)};
+        }
+        k += st ? 1u : 0u;
+        if (nbig) {
+            const uint32_t p0 = pstart[c], t0 = tstart[c];
+            const uint32_t segs = (nt + kTSeg - 1u) / kTSeg;
+            for (uint32_t idx = 0; idx < nbig && k + idx < cap; ++idx) {
+                const uint32_t a = (idx / segs) * 32u, b = (idx % segs) * kTSeg;
+                const uint32_t pa = min(32u, np - a), tb2 = min(kTSeg, nt - b);
+                items[k + idx] = TItem{p0 + a, t0 + b, c, pa | (tb2 << 6)};
+            }
+        }
+    }
+}
+
+// The cells of a packed item, one per lane of the warp's scratch: prefix of
+// probes and targets (P, Q; 0xffffffff past the span), first entries, counts.
+struct TubePack {
+    uint32_t P[32], Q[32], ps[32], ts[32], np[32], nt[32];
+};
+
+// Fills pk for packed item I (all lanes); returns nothing, counts from I.
+__device__ __forceinline__ void tube_pack_load(const TItem& I, int lane, const uint32_t* __restrict__ pstart,
+                                               const uint32_t* __restrict__ tstart, const uint32_t* __restrict__ pcnt,
+                                               const uint32_t* __restrict__ tcnt, TubePack& pk) {
+    const uint32_t span = I.cnt & 63u;
+    uint32_t a = 0, b = 0, ps = 0, ts = 0;
+    if ((uint32_t)lane < span) {
+        const uint32_t c = I.cell + (uint32_t)lane;
+        const uint32_t np = tube_count(pstart, pcnt, c), nt = tube_count(tstart, tcnt, c);
+        if (tube_small(np, nt)) {
+            a = np;
+            b = nt;
+            ps = pstart[c];
+            ts = tstart[c];
+        }
+    }
+    uint32_t ta, tb;
+    const uint32_t ea = warp_excl_scan(a, lane, &ta), eb = warp_excl_scan(b, lane, &tb);
+    __syncwarp();
+    pk.P[lane] = (uint32_t)lane < span ? ea : 0xffffffffu;
+    pk.Q[lane] = (uint32_t)lane < span ? eb : 0xffffffffu;
+    pk.ps[lane] = ps;
+    pk.ts[lane] = ts;
+    pk.np[lane] = a;
+    pk.nt[lane] = b;
+    __syncwarp();
+}
+
+// The cell (lane of pk) holding slot j of prefix X: the last k with X[k] <= j.
+__device__ __forceinline__ int tube_pack_find(const uint32_t* X, uint32_t j) {
+    int k = 0;
+#pragma unroll
+    for (int step = 16; step; step >>= 1)
+        if (X[k + step] <= j) k += step;
+    return k;
 }
 
 }  // namespace nf
