@@ -178,7 +178,7 @@ typedef struct nf_params {
                                widest pair threshold, touches, and test the
                                pairs that share a cell; the cell edge is chosen
                                for about this many registrations per cell
-                               (0 -> 24); < 0 -> the cell-stencil sweeps     */
+                               (0 -> 48); < 0 -> the cell-stencil sweeps     */
 } nf_params;
 
 /* Rods, structure of arrays, caller-owned host buffers. Any array may be NULL. */

@@ -201,8 +201,8 @@ __global__ void __launch_bounds__(kTPB, 6) k_tube_ct(const Real* __restrict__ re
     for (uint32_t it = blockIdx.x * kW + w; it < n; it += stride) {
         const TItem I = nxt;
         if (it + stride < n) nxt = items[it + stride];
-        const uint32_t np = I.cnt & 63u, nt = I.cnt >> 6;
-        const Real& Re = reals[find_real(toffs, R, I.cell)];
+        const uint32_t np = I.cnt & 63u, nt = (I.cnt >> 6) & 0xFFu;
+        const Real& Re = reals[item_real(I.pfirst, I.cnt, I.cell, toffs, R)];
         const bool have = (uint32_t)lane < np;
         uint32_t i = 0xffffffffu, ip = 0;
         float4 pA = make_float4(0, 0, 0, 0), cA = pA;
@@ -532,8 +532,8 @@ __global__ void __launch_bounds__(kTPB) k_tube_scr(const Real* __restrict__ real
     const uint32_t n = min(*nitems, icap);
     for (uint32_t it = blockIdx.x * kW + w; it < n; it += gridDim.x * kW) {
         const TItem I = items[it];
-        const uint32_t np = I.cnt & 63u, nt = I.cnt >> 6;
-        const Real& Re = reals[find_real(toffs, R, I.cell)];
+        const uint32_t np = I.cnt & 63u, nt = (I.cnt >> 6) & 0xFFu;
+        const Real& Re = reals[item_real(I.pfirst, I.cnt, I.cell, toffs, R)];
         if ((uint32_t)lane < np) {
             const uint32_t e = vent[I.pfirst + lane];
             const uint32_t id = e >> kTubeIdShift;

@@ -123,7 +123,7 @@ void set_tube_grid(Real& R, const nf_params& p) {
     const double nrod = (double)std::max<int64_t>(target_count(p), 1);
     double lmean = p.l;
     if (p.len_mode == NF_SIZE_LOGNORMAL) lmean = std::min((double)p.len_max, p.l * std::exp(0.5 * p.len_sigma_ln * p.len_sigma_ln));
-    const double load = p.tube_load > 0 ? (double)p.tube_load : 24.0;
+    const double load = p.tube_load > 0 ? (double)p.tube_load : 48.0;
     const double nd = nrod / V;
     double lo = 4 * rho, hi = std::max(lo, std::min((double)p.box[0], std::min((double)p.box[1], (double)p.box[2])));
     for (int it = 0; it < 60; ++it) {
@@ -723,8 +723,8 @@ __global__ void __launch_bounds__(256) k_conf_exact(const Real* __restrict__ rea
 // staged tile). Every entry carries the image of its object's copy in the
 // cell: the marking loop works on the copies, the filters and the FP64 queue
 // on the original coordinates with the relative image (target copy image -
-// probe copy image). Per-pair values come from the probe lane's realisation
-// and cell.
+// probe copy image). An item's cells belong to one realisation (carried in
+// the item); per-pair cells come from the probe lane.
 // ---------------------------------------------------------------------------
 
 // Probe side of item I for this lane: entry index, cell, and (packed items)
@@ -757,7 +757,7 @@ __device__ __forceinline__ TubeLane tube_lane(const TItem& I, int lane, const ui
         }
     } else {
         L.np = I.cnt & 63u;
-        L.nt = I.cnt >> 6;
+        L.nt = (I.cnt >> 6) & 0xFFu;
         L.pe = I.pfirst + (uint32_t)lane;
     }
     return L;
@@ -778,7 +778,7 @@ __device__ __forceinline__ uint32_t tube_target(const TItem& I, const TubeLane& 
 // Candidates (probe entries) against placed rods (target entries) of one tube
 // cell: cuda_OldExtIsectLB's job (inc/intersection_kern.h:245-364) on the
 // tube grid. Marking, hand-out, certificate and FP64 queue as k_old_tiles.
-__global__ void __launch_bounds__(kTPB, 6) k_tube_old(const Real* __restrict__ reals, int R,
+__global__ void __launch_bounds__(kTPB, 7) k_tube_old(const Real* __restrict__ reals, int R,
                                                    const uint32_t* __restrict__ toffs,
                                                    const uint32_t* __restrict__ nitems, uint32_t icap,
                                                    const TItem* __restrict__ items,
@@ -794,7 +794,7 @@ __global__ void __launch_bounds__(kTPB, 6) k_tube_old(const Real* __restrict__ r
     __shared__ TubeTile tiles[kW];
     __shared__ TubePack packs[kW];
     __shared__ float4 ppos[kW][32], pdir[kW][32];
-    __shared__ uint32_t pcid[kW][32], pim[kW][32], preal[kW][32];
+    __shared__ uint32_t pcid[kW][32], pim[kW][32];
     __shared__ int msp[kW][32];
     __shared__ uint32_t msm[kW][32];
     __shared__ uint16_t mq2[kW][64];
@@ -810,7 +810,7 @@ __global__ void __launch_bounds__(kTPB, 6) k_tube_old(const Real* __restrict__ r
         if (it + stride < n) nxt = items[it + stride];
         ++nitem;
         const TubeLane L = tube_lane(I, lane, pstart, tstart, nullptr, nullptr, packs[w]);
-        const int rl = find_real(toffs, R, L.cell);
+        const int rl = item_real(I.pfirst, I.cnt, I.cell, toffs, R);
         const Real& Re = reals[rl];
         const bool have = (uint32_t)lane < L.np;
         uint32_t cid = 0, ipc = 0;
@@ -828,7 +828,6 @@ __global__ void __launch_bounds__(kTPB, 6) k_tube_old(const Real* __restrict__ r
         pdir[w][lane] = cA;
         pcid[w][lane] = cid;
         pim[w][lane] = ipc;
-        preal[w][lane] = (uint32_t)rl;
         int ia[3];
         img_of(ipc, ia);
         // the probe's copy in this cell
@@ -845,7 +844,8 @@ __global__ void __launch_bounds__(kTPB, 6) k_tube_old(const Real* __restrict__ r
             if ((uint32_t)lane < m) {
                 uint32_t tc;
                 const uint32_t q = tube_target(I, L, packs[w], b, (uint32_t)lane, &tc);
-                const Real& Rt = L.packed ? reals[find_real(toffs, R, tc)] : Re;
+                const Real& Rt = Re;  // an item's cells belong to one realisation
+                (void)tc;
                 const uint32_t e = tent[q];
                 const uint32_t k = e >> kTubeIdShift;
                 const float4 p = rpos[q], c = rdir[q];
@@ -890,7 +890,7 @@ __global__ void __launch_bounds__(kTPB, 6) k_tube_old(const Real* __restrict__ r
                 if ((dead >> pl) & 1u) return false;
                 int img[3];
                 if (!rel_img(pim[w][pl], T.im[t], img)) return false;
-                const Real& Rp = reals[preal[w][pl]];
+                const Real& Rp = Re;
                 const float4 dA = pdir[w][pl], cB = T.c[t];
                 return !line_far(ppos[w][pl], dA, T.p[t], cB, img[0] * Rp.L[0], img[1] * Rp.L[1], img[2] * Rp.L[2],
                                  (cB.w + dA.w) * Rp.scf + Rp.sep + Rp.eps, Rp.slack);
@@ -900,7 +900,7 @@ __global__ void __launch_bounds__(kTPB, 6) k_tube_old(const Real* __restrict__ r
             const int kept_ = for_marked_pairs(mask, lane, msp[w], msm[w], mq2[w], keep, [&](bool valid, int pl, int t) {
                 bool hit = false;
                 if (valid && !((dead >> pl) & 1u)) {
-                    const Real& Rp = reals[preal[w][pl]];
+                    const Real& Rp = Re;
                     const float4 qA = ppos[w][pl], dA = pdir[w][pl];
                     const float4 pB = T.p[t], cB = T.c[t];
                     int img[3];
@@ -942,7 +942,7 @@ __global__ void __launch_bounds__(kTPB, 6) k_tube_old(const Real* __restrict__ r
 // conflict list twice from the FP32 path; uncertain pairs are queued from
 // every cell they share (the FP64 pass may list a pair again, which the
 // resolution ignores).
-__global__ void __launch_bounds__(kTPB, 6) k_tube_conf(const Real* __restrict__ reals, int R,
+__global__ void __launch_bounds__(kTPB, 7) k_tube_conf(const Real* __restrict__ reals, int R,
                                                     const uint32_t* __restrict__ toffs,
                                                     const uint32_t* __restrict__ nitems, uint32_t icap,
                                                     const TItem* __restrict__ items,
@@ -957,7 +957,7 @@ __global__ void __launch_bounds__(kTPB, 6) k_tube_conf(const Real* __restrict__ 
     __shared__ TubeTile tiles[kW];
     __shared__ TubePack packs[kW];
     __shared__ float4 ppos[kW][32], pdir[kW][32];
-    __shared__ uint32_t pcid[kW][32], pim[kW][32], preal[kW][32], pcel[kW][32];
+    __shared__ uint32_t pcid[kW][32], pim[kW][32], pcel[kW][32];
     __shared__ int msp[kW][32];
     __shared__ uint32_t msm[kW][32];
     __shared__ uint16_t mq2[kW][64];
@@ -972,7 +972,7 @@ __global__ void __launch_bounds__(kTPB, 6) k_tube_conf(const Real* __restrict__ 
         if (it + stride < n) nxt = items[it + stride];
         ++nitem;
         const TubeLane L = tube_lane(I, lane, start, start, cnt, cnt, packs[w]);
-        const int rl = find_real(toffs, R, L.cell);
+        const int rl = item_real(I.pfirst, I.cnt, I.cell, toffs, R);
         const Real& Re = reals[rl];
         const bool have = (uint32_t)lane < L.np;
         uint32_t cid = 0, ipc = 0;
@@ -989,7 +989,6 @@ __global__ void __launch_bounds__(kTPB, 6) k_tube_conf(const Real* __restrict__ 
         pdir[w][lane] = cA;
         pcid[w][lane] = cid;
         pim[w][lane] = ipc;
-        preal[w][lane] = (uint32_t)rl;
         pcel[w][lane] = L.cell;
         int ia[3];
         img_of(ipc, ia);
@@ -1002,7 +1001,8 @@ __global__ void __launch_bounds__(kTPB, 6) k_tube_conf(const Real* __restrict__ 
             if ((uint32_t)lane < m) {
                 uint32_t tc;
                 const uint32_t q = tube_target(I, L, packs[w], b, (uint32_t)lane, &tc);
-                const Real& Rt = L.packed ? reals[find_real(toffs, R, tc)] : Re;
+                const Real& Rt = Re;  // an item's cells belong to one realisation
+                (void)tc;
                 const uint32_t e = ent[q];
                 const uint32_t k = e >> kTubeIdShift;
                 const float4 p = cpos[q], c = cdir[q];
@@ -1041,7 +1041,7 @@ __global__ void __launch_bounds__(kTPB, 6) k_tube_conf(const Real* __restrict__ 
             auto keep = [&](int pl, int t) {
                 int img[3];
                 if (!rel_img(pim[w][pl], T.im[t], img)) return false;
-                const Real& Rp = reals[preal[w][pl]];
+                const Real& Rp = Re;
                 const float4 dA = pdir[w][pl], cB = T.c[t];
                 return !line_far(ppos[w][pl], dA, T.p[t], cB, img[0] * Rp.L[0], img[1] * Rp.L[1], img[2] * Rp.L[2],
                                  (cB.w + dA.w) * Rp.scf + Rp.sep + Rp.eps, Rp.slack);
@@ -1050,7 +1050,7 @@ __global__ void __launch_bounds__(kTPB, 6) k_tube_conf(const Real* __restrict__ 
             nmark += __popc(mask);
             const int kept_ = for_marked_pairs(mask, lane, msp[w], msm[w], mq2[w], keep, [&](bool valid, int pl, int t) {
                 if (!valid) return;
-                const Real& Rp = reals[preal[w][pl]];
+                const Real& Rp = Re;
                 const float4 qA = ppos[w][pl], dA = pdir[w][pl];
                 const float4 pB = T.p[t], cB = T.c[t];
                 int img[3];
@@ -1382,13 +1382,13 @@ nf_status Engine::tube_items(const uint32_t* pstart, const uint32_t* tstart, con
     const unsigned g = (unsigned)std::max<size_t>(1, std::min<size_t>(((size_t)nseg * 32 + 255) / 256, (size_t)nsm * 64));
     auto kcount = k_titem<false>;
     auto kfill = k_titem<true>;
-    NF_LAUNCH(kcount, g, 256, 0, st)(ntcell, pack ? 1 : 0, pstart, tstart, pcnt, tcnt, icnt.p, nullptr, nullptr, 0u,
-                                     nullptr);
+    NF_LAUNCH(kcount, g, 256, 0, st)(ntcell, pack ? 1 : 0, toffs.p, R, pstart, tstart, pcnt, tcnt, icnt.p, nullptr,
+                                     nullptr, 0u, nullptr);
     NF_CK(cudaGetLastError());
     nf_status s = scan_u32(icnt.p, tioff.p, (size_t)nseg + 1);
     if (s != NF_OK) return s;
-    NF_LAUNCH(kfill, g, 256, 0, st)(ntcell, pack ? 1 : 0, pstart, tstart, pcnt, tcnt, nullptr, tioff.p, titems.p,
-                                    (uint32_t)titems.cap, ctr.p + C_ITEMS);
+    NF_LAUNCH(kfill, g, 256, 0, st)(ntcell, pack ? 1 : 0, toffs.p, R, pstart, tstart, pcnt, tcnt, nullptr, tioff.p,
+                                    titems.p, (uint32_t)titems.cap, ctr.p + C_ITEMS);
     NF_CK(cudaGetLastError());
     return NF_OK;
 }

@@ -7,10 +7,10 @@
 // registered in each cell of a grid that its segment, dilated by
 // trho >= thr_max / 2, touches, every pair within reach shares a cell, and
 // testing the pairs registered together in each cell finds all of them. For
-// rods of length l in cells of edge e ~ l/5 an object registers in about
-// 2 l / e + 1 cells holding ~24 registrations each, so a probe meets ~200
-// targets instead of the ~4 000 of a 5 x 5 x 5 stencil of cells of edge
-// reach / 2 at 2 % volume fraction.
+// rods of length l in cells of edge e ~ l/4 an object registers in about
+// 2 l / e + 1 cells holding ~48 registrations each, so a probe meets a few
+// hundred targets instead of the ~4 000 of a 5 x 5 x 5 stencil of cells of
+// edge reach / 2 at 2 % volume fraction.
 //
 // A pair can share several cells, so it can be tested more than once. The
 // boolean tests (a candidate against placed rods, screening) do not mind. A
@@ -350,15 +350,26 @@ static __global__ void k_treg_compact(uint32_t ncell, const uint32_t* __restrict
 // Work items of the tube sweeps. Item layout (16 B): first probe entry,
 // first target entry, cell, count word.
 // - A cell item: probe chunks of <= 32 times target segments of <= kTSeg of
-//   one cell; count word np | nt << 6.
-// - A packed item (kPackBit set): a run of consecutive cells from `cell`
-//   whose small cells (1-32 probes and 1-32 targets each) hold <= 32 probes
-//   and <= 32 targets together; count word span | np << 6 | nt << 12 | bit.
-//   A lane takes one probe of any of them and tests it against its own cell's
-//   targets, so the warp's lanes fill up where cells hold a few objects each.
-// Cells that are not small get cell items.
+//   one cell; count word np | nt << 6 | realisation << 14.
+// - A packed item (kPackBit set): a run of consecutive cells from `cell`, of
+//   one realisation (in the first word), whose small cells (1-32 probes and
+//   1-32 targets each) hold <= 32 probes and <= 32 targets together; count
+//   word span | np << 6 | nt << 12 | bit. A lane takes one probe of any of
+//   them and tests it against its own cell's targets, so the warp's lanes
+//   fill up where cells hold a few objects each.
+// Cells that are not small get cell items. With more realisations than the
+// count word holds (kItemRealMax), cell items carry none and the sweeps look
+// it up.
 constexpr uint32_t kTSeg = 128;
 constexpr uint32_t kPackBit = 0x80000000u;
+constexpr int kItemRealMax = (1 << 17) - 1;
+
+// Realisation of item I (whose count word is cnt) for R realisations.
+__device__ __forceinline__ int item_real(uint32_t pfirst, uint32_t cnt, uint32_t cell, const uint32_t* toffs, int R) {
+    if (cnt & kPackBit) return (int)pfirst;
+    if (R <= kItemRealMax) return (int)((cnt >> 14) & 0x1FFFFu);
+    return find_real(toffs, R, cell);
+}
 
 // Entries of cell c: [start[c], start[c] + cnt[c]) when a count array is
 // given (a list compacted in place), else [start[c], start[c + 1]).
@@ -390,7 +401,8 @@ __device__ __forceinline__ uint32_t warp_excl_scan(uint32_t v, int lane, uint32_
 // segment's small cells go into packed items, greedily in cell order; the
 // other cells (and every cell without pack) get cell items.
 template <bool kFill>
-__global__ void __launch_bounds__(256) k_titem(uint32_t ncell, int pack, const uint32_t* __restrict__ pstart,
+__global__ void __launch_bounds__(256) k_titem(uint32_t ncell, int pack, const uint32_t* __restrict__ toffs, int R,
+                                               const uint32_t* __restrict__ pstart,
                                                const uint32_t* __restrict__ tstart, const uint32_t* __restrict__ pcnt,
                                                const uint32_t* __restrict__ tcnt, uint32_t* __restrict__ icnt,
                                                const uint32_t* __restrict__ ioff, TItem* __restrict__ items,
@@ -409,8 +421,10 @@ __global__ void __launch_bounds__(256) k_titem(uint32_t ncell, int pack, const u
         }
         const bool small = pack && tube_small(np, nt);
         const uint32_t nbig = (!small && np && nt) ? ((np + 31u) / 32u) * ((nt + kTSeg - 1u) / kTSeg) : 0u;
+        const int rl = (np && nt) ? find_real(toffs, R, min(c, ncell - 1u)) : 0;
         // greedy groups of the small cells: a group ends before the first
-        // small cell that would take it past 32 probes or 32 targets
+        // small cell that would take it past 32 probes or 32 targets, or that
+        // belongs to another realisation
         uint32_t ta, tb;
         const uint32_t ea = warp_excl_scan(small ? np : 0u, lane, &ta);
         const uint32_t eb = warp_excl_scan(small ? nt : 0u, lane, &tb);
@@ -422,7 +436,9 @@ __global__ void __launch_bounds__(256) k_titem(uint32_t ncell, int pack, const u
             for (;;) {
                 starts |= 1u << g;
                 const uint32_t ba = __shfl_sync(0xffffffffu, ea, g), bb = __shfl_sync(0xffffffffu, eb, g);
-                const unsigned over = __ballot_sync(0xffffffffu, lane > g && small && (ia - ba > 32u || ib - bb > 32u));
+                const int rg = __shfl_sync(0xffffffffu, rl, g);
+                const unsigned over =
+                    __ballot_sync(0xffffffffu, lane > g && small && (ia - ba > 32u || ib - bb > 32u || rl != rg));
                 if (!over) break;
                 g = __ffs(over) - 1;
             }
@@ -441,7 +457,7 @@ __global__ void __launch_bounds__(256) k_titem(uint32_t ncell, int pack, const u
         uint32_t k = ioff[sg] + off;
         if (st && k < cap) {
             const uint32_t span = (uint32_t)(end - lane), gp = ia_end - ea, gt = ib_end - eb;
-            items[k] = TItem{0u, 0u, c, kPackBit | span | (gp << 6) | (gt << 12)};
+            items[k] = TItem{(uint32_t)rl, 0u, c, kPackBit | span | (gp << 6) | (gt << 12)};
         }
         k += st ? 1u : 0u;
         if (nbig) {
@@ -450,7 +466,8 @@ __global__ void __launch_bounds__(256) k_titem(uint32_t ncell, int pack, const u
             for (uint32_t idx = 0; idx < nbig && k + idx < cap; ++idx) {
                 const uint32_t a = (idx / segs) * 32u, b = (idx % segs) * kTSeg;
                 const uint32_t pa = min(32u, np - a), tb2 = min(kTSeg, nt - b);
-                items[k + idx] = TItem{p0 + a, t0 + b, c, pa | (tb2 << 6)};
+                const uint32_t rw = R <= kItemRealMax ? (uint32_t)rl << 14 : 0u;
+                items[k + idx] = TItem{p0 + a, t0 + b, c, pa | (tb2 << 6) | rw};
             }
         }
     }
