@@ -177,17 +177,19 @@ __global__ void __launch_bounds__(256) k_ct_exact(const Real* __restrict__ reals
 // Contact sweep on the tube grid: rod I against rods J > I registered in the
 // same tube cell (entries carry the image of each rod's copy); pairs the FP32
 // filter cannot rule out are queued with their cell (rod ids, relative image).
-__global__ void __launch_bounds__(kTPB, 6) k_tube_ct(const Real* __restrict__ reals, int R,
+__global__ void __launch_bounds__(kTPB, 7) k_tube_ct(const Real* __restrict__ reals, int R,
                                                   const uint32_t* __restrict__ toffs,
                                                   const uint32_t* __restrict__ nitems, uint32_t icap,
-                                                  const TItem* __restrict__ items, const uint32_t* __restrict__ ent,
+                                                  const TItem* __restrict__ items,
+                                                  const uint32_t* __restrict__ start, const uint32_t* __restrict__ ent,
                                                   const float4* __restrict__ pos, const float4* __restrict__ dir,
                                                   unsigned long long* __restrict__ xq, uint32_t* __restrict__ xqc,
                                                   unsigned long long xcap, unsigned long long* __restrict__ ctr) {
     constexpr int kW = kTPB / 32;
     __shared__ TubeTile tiles[kW];
+    __shared__ TubePack packs[kW];
     __shared__ float4 ppos[kW][32], pdir[kW][32];
-    __shared__ uint32_t pid[kW][32], pim[kW][32];
+    __shared__ uint32_t pid[kW][32], pim[kW][32], pcel[kW][32];
     __shared__ int msp[kW][32];
     __shared__ uint32_t msm[kW][32];
     __shared__ uint16_t mq2[kW][64];
@@ -201,23 +203,25 @@ __global__ void __launch_bounds__(kTPB, 6) k_tube_ct(const Real* __restrict__ re
     for (uint32_t it = blockIdx.x * kW + w; it < n; it += stride) {
         const TItem I = nxt;
         if (it + stride < n) nxt = items[it + stride];
-        const uint32_t np = I.cnt & 63u, nt = (I.cnt >> 6) & 0xFFu;
+        const TubeLane L = tube_lane(I, lane, start, start, nullptr, nullptr, packs[w]);
+        const uint32_t np = L.np, nt = L.nt;
         const Real& Re = reals[item_real(I.pfirst, I.cnt, I.cell, toffs, R)];
         const bool have = (uint32_t)lane < np;
         uint32_t i = 0xffffffffu, ip = 0;
         float4 pA = make_float4(0, 0, 0, 0), cA = pA;
         if (have) {
-            const uint32_t e = ent[I.pfirst + lane];
+            const uint32_t e = ent[L.pe];
             i = e >> kTubeIdShift;
             ip = e & 63u;
-            pA = pos[I.pfirst + lane];
-            cA = dir[I.pfirst + lane];
+            pA = pos[L.pe];
+            cA = dir[L.pe];
         }
         __syncwarp();
         ppos[w][lane] = pA;
         pdir[w][lane] = cA;
         pid[w][lane] = i;
         pim[w][lane] = ip;
+        pcel[w][lane] = L.cell;
         int ia[3];
         img_of(ip, ia);
         const float ax = pA.x + ia[0] * Re.L[0], ay = pA.y + ia[1] * Re.L[1], az = pA.z + ia[2] * Re.L[2];
@@ -227,9 +231,12 @@ __global__ void __launch_bounds__(kTPB, 6) k_tube_ct(const Real* __restrict__ re
         for (uint32_t b = 0; b < nt; b += kWT) {
             const uint32_t m = min((uint32_t)kWT, nt - b);
             if ((uint32_t)lane < m) {
-                const uint32_t e = ent[I.tfirst + b + lane];
+                uint32_t tc;
+                const uint32_t q = tube_target(I, L, packs[w], b, (uint32_t)lane, &tc);
+                (void)tc;
+                const uint32_t e = ent[q];
                 const uint32_t k = e >> kTubeIdShift;
-                const float4 p = pos[I.tfirst + b + lane], c = dir[I.tfirst + b + lane];
+                const float4 p = pos[q], c = dir[q];
                 int ib[3];
                 img_of(e & 63u, ib);
                 T.p[lane] = p;
@@ -243,18 +250,21 @@ __global__ void __launch_bounds__(kTPB, 6) k_tube_ct(const Real* __restrict__ re
                 T.id[lane] = 0u;
             }
             __syncwarp();
+            const uint32_t lo = L.packed ? L.tlo : 0u, len = L.packed ? L.tlen : m;
             uint32_t mask = 0, umask = 0;  // marked pairs; pairs with J > I
             if (have) {
-                const uint32_t m8 = (m + 7u) & ~7u;
-                for (uint32_t j0 = 0; j0 < m8; j0 += 8) {
+                for (uint32_t u0 = 0; u0 < len; u0 += 8) {
 #pragma unroll
                     for (uint32_t jj = 0; jj < 8; ++jj) {
-                        const uint32_t j = j0 + jj;
-                        const float4 tq = T.ps[j];
-                        const float bx = tq.x - ax, by = tq.y - ay, bz = tq.z - az;
-                        const uint32_t bit = T.id[j] > i ? (1u << j) : 0u;  // each unordered pair once per cell
-                        umask |= bit;
-                        if (capsule_near(bx, by, bz, cA.x, cA.y, cA.z, hAe, tq.w, hC)) mask |= bit;
+                        const uint32_t u = u0 + jj;
+                        if (u < len) {
+                            const uint32_t j = lo + u;
+                            const float4 tq = T.ps[j];
+                            const float bx = tq.x - ax, by = tq.y - ay, bz = tq.z - az;
+                            const uint32_t bit = T.id[j] > i ? (1u << j) : 0u;  // each unordered pair once per cell
+                            umask |= bit;
+                            if (capsule_near(bx, by, bz, cA.x, cA.y, cA.z, hAe, tq.w, hC)) mask |= bit;
+                        }
                     }
                 }
                 tests += __popc(umask);
@@ -275,7 +285,7 @@ __global__ void __launch_bounds__(kTPB, 6) k_tube_ct(const Real* __restrict__ re
                 const float thr = (cB.w + dA.w) + Re.cut + epc;
                 if (maybe_near(qA, dA, pB, cB, img[0] * Re.L[0], img[1] * Re.L[1], img[2] * Re.L[2], thr, epc,
                                Re.slack))
-                    xq_push_cell(xq, xqc, xcap, &ctr[C_XQ], xq_pack(pid[w][pl], T.id[t], img), I.cell);
+                    xq_push_cell(xq, xqc, xcap, &ctr[C_XQ], xq_pack(pid[w][pl], T.id[t], img), pcel[w][pl]);
             });
             __syncwarp();
         }
@@ -926,7 +936,7 @@ nf_status Engine::contacts() {
                     if (s != NF_OK) return s;
                     trod_stage = 1;
                 }
-                s = tube_items(trod_start.p, trod_start.p);
+                s = tube_items(trod_start.p, trod_start.p, nullptr, nullptr, true);
             } else {
                 s = build_items(rstart.p, rstart.p, 1, nrods, nrods);
             }
@@ -941,7 +951,8 @@ nf_status Engine::contacts() {
         tstart(KT_CTPAIRS);
         if (nrods && tube) {
             NF_LAUNCH(k_tube_ct, persistent_grid(k_tube_ct), kTPB, 0, st)(dreal.p, R, toffs.p, titem_count(),
-                                                   (uint32_t)titems.cap, titems.p, trod_ent.p, trod_pos.p, trod_dir.p,
+                                                   (uint32_t)titems.cap, titems.p, trod_start.p, trod_ent.p,
+                                                   trod_pos.p, trod_dir.p,
                                                    xq.p, xqc.p, xq.cap, ctr.p);
             NF_CK(cudaGetLastError());
             NF_LAUNCH(k_ct_exact_tube, xg, 256, 0, st)(dreal.p, R, rodoff.p, xq.p, xqc.p, ctr.p + C_XQ, xq.cap,

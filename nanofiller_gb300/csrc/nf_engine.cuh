@@ -179,6 +179,7 @@ struct Engine {
     DBuf<TItem> titems;
     size_t tit_cap = 1 << 20;
     uint32_t tit_nseg = 0;  // cell segments of the last tube_items (its item count sits at tioff[tit_nseg])
+    size_t trod_total = 0, tcnd_total = 0;  // entries of the last rod / candidate (or virtual rod) registration
     DBuf<uint32_t> tioff;
 
     // contacts
@@ -373,6 +374,7 @@ inline nf_status tube_register(Engine& E, uint32_t n, const uint32_t* ntot, int 
     NF_CKT(cudaMemcpyAsync(h, start.p + nc, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
     NF_CKT(cudaStreamSynchronize(st));
     const size_t total = *h;
+    (&start == &E.trod_start ? E.trod_total : E.tcnd_total) = total;
     NF_CKT(ent.ensure(total + 1));
     NF_CKT(epos.ensure(total + 1));
     NF_CKT(edir.ensure(total + 1));

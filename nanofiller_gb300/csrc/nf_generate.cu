@@ -727,54 +727,6 @@ __global__ void __launch_bounds__(256) k_conf_exact(const Real* __restrict__ rea
 // the item); per-pair cells come from the probe lane.
 // ---------------------------------------------------------------------------
 
-// Probe side of item I for this lane: entry index, cell, and (packed items)
-// the lane's target range in the tile; np / nt the item's probe and target
-// counts.
-struct TubeLane {
-    uint32_t np, nt, pe, cell, tlo, tlen;
-    bool packed;
-};
-
-__device__ __forceinline__ TubeLane tube_lane(const TItem& I, int lane, const uint32_t* __restrict__ pstart,
-                                              const uint32_t* __restrict__ tstart, const uint32_t* __restrict__ pcnt,
-                                              const uint32_t* __restrict__ tcnt, TubePack& pk) {
-    TubeLane L;
-    L.packed = (I.cnt & kPackBit) != 0u;
-    L.cell = I.cell;
-    L.tlo = 0;
-    L.tlen = 0;
-    if (L.packed) {
-        tube_pack_load(I, lane, pstart, tstart, pcnt, tcnt, pk);
-        L.np = (I.cnt >> 6) & 63u;
-        L.nt = (I.cnt >> 12) & 63u;
-        L.pe = 0;
-        if ((uint32_t)lane < L.np) {
-            const int k = tube_pack_find(pk.P, (uint32_t)lane);
-            L.pe = pk.ps[k] + ((uint32_t)lane - pk.P[k]);
-            L.cell = I.cell + (uint32_t)k;
-            L.tlo = pk.Q[k];
-            L.tlen = pk.nt[k];
-        }
-    } else {
-        L.np = I.cnt & 63u;
-        L.nt = (I.cnt >> 6) & 0xFFu;
-        L.pe = I.pfirst + (uint32_t)lane;
-    }
-    return L;
-}
-
-// Target entry of tile slot `slot` (< the tile's count) of stage b, and its cell.
-__device__ __forceinline__ uint32_t tube_target(const TItem& I, const TubeLane& L, const TubePack& pk, uint32_t b,
-                                                uint32_t slot, uint32_t* cell) {
-    if (L.packed) {
-        const int k = tube_pack_find(pk.Q, slot);
-        *cell = I.cell + (uint32_t)k;
-        return pk.ts[k] + (slot - pk.Q[k]);
-    }
-    *cell = I.cell;
-    return I.tfirst + b + slot;
-}
-
 // Candidates (probe entries) against placed rods (target entries) of one tube
 // cell: cuda_OldExtIsectLB's job (inc/intersection_kern.h:245-364) on the
 // tube grid. Marking, hand-out, certificate and FP64 queue as k_old_tiles.
@@ -1375,6 +1327,11 @@ nf_status Engine::tube_register_cands(uint64_t slots, const uint32_t* ntot, bool
 nf_status Engine::tube_items(const uint32_t* pstart, const uint32_t* tstart, const uint32_t* pcnt,
                               const uint32_t* tcnt, bool pack) {
     const uint32_t nseg = (ntcell + 31u) / 32u;
+    // every item holds at least one probe entry, so the probe registration's
+    // size bounds the items but where a cell's targets need several segments
+    // (an overflow, counted in C_ITEMS, redoes the stage with more room)
+    const size_t nprobe = pstart == trod_start.p ? trod_total : tcnd_total;
+    tit_cap = std::max(tit_cap, nprobe + 4096);
     NF_CK(icnt.ensure((size_t)nseg + 1));
     NF_CK(tioff.ensure((size_t)nseg + 1));
     NF_CK(titems.ensure(tit_cap));

@@ -516,4 +516,52 @@ __device__ __forceinline__ int tube_pack_find(const uint32_t* X, uint32_t j) {
     return k;
 }
 
+// Probe side of item I for this lane: entry index, cell, and (packed items)
+// the lane's target range in the tile; np / nt the item's probe and target
+// counts.
+struct TubeLane {
+    uint32_t np, nt, pe, cell, tlo, tlen;
+    bool packed;
+};
+
+__device__ __forceinline__ TubeLane tube_lane(const TItem& I, int lane, const uint32_t* __restrict__ pstart,
+                                              const uint32_t* __restrict__ tstart, const uint32_t* __restrict__ pcnt,
+                                              const uint32_t* __restrict__ tcnt, TubePack& pk) {
+    TubeLane L;
+    L.packed = (I.cnt & kPackBit) != 0u;
+    L.cell = I.cell;
+    L.tlo = 0;
+    L.tlen = 0;
+    if (L.packed) {
+        tube_pack_load(I, lane, pstart, tstart, pcnt, tcnt, pk);
+        L.np = (I.cnt >> 6) & 63u;
+        L.nt = (I.cnt >> 12) & 63u;
+        L.pe = 0;
+        if ((uint32_t)lane < L.np) {
+            const int k = tube_pack_find(pk.P, (uint32_t)lane);
+            L.pe = pk.ps[k] + ((uint32_t)lane - pk.P[k]);
+            L.cell = I.cell + (uint32_t)k;
+            L.tlo = pk.Q[k];
+            L.tlen = pk.nt[k];
+        }
+    } else {
+        L.np = I.cnt & 63u;
+        L.nt = (I.cnt >> 6) & 0xFFu;
+        L.pe = I.pfirst + (uint32_t)lane;
+    }
+    return L;
+}
+
+// Target entry of tile slot `slot` (< the tile's count) of stage b, and its cell.
+__device__ __forceinline__ uint32_t tube_target(const TItem& I, const TubeLane& L, const TubePack& pk, uint32_t b,
+                                                uint32_t slot, uint32_t* cell) {
+    if (L.packed) {
+        const int k = tube_pack_find(pk.Q, slot);
+        *cell = I.cell + (uint32_t)k;
+        return pk.ts[k] + (slot - pk.Q[k]);
+    }
+    *cell = I.cell;
+    return I.tfirst + b + slot;
+}
+
 }  // namespace nf
