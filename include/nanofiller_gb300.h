@@ -179,6 +179,22 @@ typedef struct nf_params {
                                pairs that share a cell; the cell edge is chosen
                                for about this many registrations per cell
                                (0 -> 48); < 0 -> the cell-stencil sweeps     */
+    int32_t align_law;      /* ALIGN_LAW: the law a self-alignment refit gives
+                               a cell. 0 (default) a von Mises-Fisher law
+                               about the principal axis of the cell's
+                               orientation tensor. 1 the reference's law
+                               (crossMtxBuild / resetOrt / resetAvgVec,
+                               inc/allignment_fit.h:154-458): preferred axis
+                               = the eigenvector of the largest eigenvalue
+                               when the two smaller ones are within 10 %,
+                               else of the smallest; truncated-normal theta /
+                               phi about the mean direction of the cell's
+                               rods (when its norm per rod exceeds 0.5) with
+                               their mean squared deviations as the scales,
+                               drawn as DEF_THETA_DEV / DEF_PHI_DEV select
+                               and rotated by the preferred axis; thin-out
+                               by the reference's Gaussian likelihood        */
+    int32_t reserved;       /* 0                                           */
 } nf_params;
 
 /* Rods, structure of arrays, caller-owned host buffers. Any array may be NULL. */

@@ -42,7 +42,8 @@ class NfParams(C.Structure):
         ("elec_buffer", C.c_int32), ("ref_trunc_normal", C.c_int32),
         ("clust_dist", C.c_float), ("clust_angl", C.c_float), ("align_cell", C.c_float),
         ("align_min", C.c_int32), ("epoch_candidates", C.c_int64),
-        ("solve_method", C.c_int32), ("tube_load", C.c_float),
+        ("solve_method", C.c_int32), ("tube_load", C.c_float), ("align_law", C.c_int32),
+        ("reserved", C.c_int32),
     ]
 
 

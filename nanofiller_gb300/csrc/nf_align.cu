@@ -330,6 +330,8 @@ static void global_law(const Real& Re, float* Lw) {
     Lw[9] = Re.orient == 1 ? Re.kappa : 0.0f;
     Lw[10] = Re.orient == 1 ? Re.E2 : 0.0f;
     Lw[11] = (float)((Re.orient == 1 ? 1 : 0) | (Re.rot ? 2 : 0));
+    Lw[12] = 0.0f;
+    Lw[13] = 0.0f;
 }
 
 nf_status Engine::laws_reset() {
@@ -343,11 +345,15 @@ nf_status Engine::laws_reset() {
     const size_t nc = (size_t)lawn[0] * lawn[1] * lawn[2];
     hlaw.assign(nc * kLawF, 0.0f);
     for (size_t c = 0; c < nc; ++c) global_law(hreal[0], &hlaw[c * kLawF]);
+    hlawd.assign(nc * kLawD, 0.0);
     NF_CK(law.ensure(nc * kLawF));
+    NF_CK(lawd.ensure(nc * kLawD));
     NF_CK(lacc.ensure(nc * 7));
     NF_CK(cudaMemcpyAsync(law.p, hlaw.data(), sizeof(float) * hlaw.size(), cudaMemcpyHostToDevice, st));
+    NF_CK(cudaMemcpyAsync(lawd.p, hlawd.data(), sizeof(double) * hlawd.size(), cudaMemcpyHostToDevice, st));
     Real& Re = hreal[0];
     Re.law = law.p;
+    Re.lawd = lawd.p;
     for (int d = 0; d < 3; ++d) {
         Re.an[d] = lawn[d];
         Re.ainv[d] = inv[d];
@@ -460,6 +466,112 @@ static void fit_law(const long long s[7], bool sample, float* Lw) {
     Lw[11] = sample ? (float)((kf > 0.0f ? 1 : 0) | 2) : 0.0f;
 }
 
+// ALIGN_LAW 1: the reference's cell law (crossMtxBuild, resetOrt,
+// resetAvgVec; inc/allignment_fit.h:154-210, 214-274, 353-458), fitted on the
+// host in FP64 from the cell's rods in rod order:
+//   - preferred axis: the unit eigenvector of <c c^T> of the largest
+//     eigenvalue when the two smaller eigenvalues (by magnitude) are within
+//     10 % of each other ("cone-like"), else of the smallest ("disk-like"),
+//     signed with v_z > 0 (then v_y, v_x); theta_o = acos(v_z),
+//     phi_o = acos(v_x / sin theta_o) with the reference's 1e-6 guards; the
+//     draw is rotated by inc_rotation(Mu = phi_o, Xi = -theta_o);
+//   - law: when the mean of the rods' directions has a norm per rod above
+//     0.5 (def_minOrtNorm, src/simPrms.cpp:42), theta = asin |a_xy|,
+//     phi = acos(a_x / |a_xy|) of the unit mean a, and the mean squared
+//     deviations of asin |c_xy| and acos(c_x / |c_xy|) from them are the
+//     scales of the truncated-normal draws (the reference hands its "mean
+//     squared deviation" arrays to sym_truncNormal as s). The angles are taken
+//     in the box frame: the reference's rotation into the preferred frame
+//     (rot_Z / rot_Y on a float3, whose result is discarded) leaves the
+//     vectors as they are. Otherwise the cell keeps its truncated-normal laws.
+// Angles of a direction in the box frame (Ort2Angle, inc/vectorMath.h:85-90).
+static void box_angles(double cx, double cy, double* th, double* ph) {
+    const double nxy = std::sqrt(cx * cx + cy * cy);
+    *th = std::asin(nxy > 1.0 ? 1.0 : nxy);
+    double q = nxy > 1e-6 ? cx / nxy : 0.0;
+    q = q > 1.0 ? 1.0 : (q < -1.0 ? -1.0 : q);
+    *ph = nxy > 1e-6 ? std::acos(q) : 0.0;
+}
+
+static void fit_tn_cell(const float4* dirs, const std::vector<uint32_t>& idx, int ref, float* Lw, double* Ld) {
+    const double n = (double)idx.size();
+    double A[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+    double ax = 0, ay = 0, az = 0;
+    for (uint32_t i : idx) {
+        const double x = dirs[i].x, y = dirs[i].y, z = dirs[i].z;
+        A[0][0] += x * x; A[1][1] += y * y; A[2][2] += z * z;
+        A[0][1] += x * y; A[0][2] += x * z; A[1][2] += y * z;
+        ax += x; ay += y; az += z;
+    }
+    for (int r = 0; r < 3; ++r)
+        for (int c = r; c < 3; ++c) A[r][c] /= n;
+    A[1][0] = A[0][1]; A[2][0] = A[0][2]; A[2][1] = A[1][2];
+    double V[3][3];
+    jacobi3(A, V);
+    int o[3] = {0, 1, 2};  // eigenvalues by decreasing magnitude
+    for (int a = 0; a < 3; ++a)
+        for (int b = a + 1; b < 3; ++b)
+            if (std::fabs(A[o[b]][o[b]]) > std::fabs(A[o[a]][o[a]])) std::swap(o[a], o[b]);
+    const double e1 = A[o[1]][o[1]], e2 = A[o[2]][o[2]];
+    const int k = std::fabs((e1 - e2) / e1) < 0.1 ? o[0] : o[2];
+    double v[3] = {V[0][k], V[1][k], V[2][k]};
+    const double nv = std::sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+    for (double& q : v) q /= nv;
+    if (v[2] < 0 || (v[2] == 0 && (v[1] < 0 || (v[1] == 0 && v[0] < 0))))
+        for (double& q : v) q = -q;
+    const double tho = std::fabs(v[2]) <= 1.0 - 1e-6 ? std::acos(v[2]) : (v[2] > 0 ? 0.0 : kPiD);
+    const double sth = std::sin(tho);
+    double cph = std::fabs(sth) > 1e-6 ? v[0] / sth : 1.0;
+    const double pho = std::fabs(cph) <= 1.0 - 1e-6 ? std::acos(cph) : (cph > 0 ? 0.0 : kPiD);
+    float cM, sM, cX, sX;  // inc_rotation, Mu = phi_o, Xi = -theta_o (as the global PREF_ORT rotation)
+    sincos_turns((float)(pho / (2.0 * kPiD)), &cM, &sM);
+    sincos_turns((float)(-tho / (2.0 * kPiD)), &cX, &sX);
+    Lw[0] = fmul(cM, cX);  Lw[1] = sM;   Lw[2] = fmul(-sX, cM);
+    Lw[3] = fmul(-sM, cX); Lw[4] = cM;   Lw[5] = fmul(sX, sM);
+    Lw[6] = sX;            Lw[7] = 0.0f; Lw[8] = cX;
+    Lw[9] = 0.0f;
+    Lw[10] = 0.0f;
+    int fl = 2 | ((int)Lw[11] & 4);
+    const double na = std::sqrt(ax * ax + ay * ay + az * az);
+    if (na / n > 0.5) {
+        double th, ph;
+        box_angles(ax / na, ay / na, &th, &ph);
+        double st = 0.0, sp = 0.0;
+        for (uint32_t i : idx) {
+            double dt, dp;
+            box_angles(dirs[i].x, dirs[i].y, &dt, &dp);
+            st += (dt - th) * (dt - th);
+            sp += (dp - ph) * (dp - ph);
+        }
+        // the reference keeps these in float arrays; a zero spread is kept
+        // finite (all of the cell's rods parallel: the draws collapse onto the mean)
+        const float ft = (float)th, fp = (float)ph;
+        const float dt = std::max((float)(st / n), 1e-12f), dp = std::max((float)(sp / n), 1e-12f);
+        Lw[12] = ft;
+        Lw[13] = fp;
+        Ld[0] = ft; Ld[1] = dt; Ld[2] = fp; Ld[3] = dp;
+        tn_consts(dt, kPiD * 0.5, ref, &Ld[4], &Ld[5], &Ld[6]);
+        tn_consts(dp, kPiD, ref, &Ld[7], &Ld[8], &Ld[9]);
+        fl |= 4;
+    }
+    Lw[11] = (float)fl;
+}
+
+// Thin-out under ALIGN_LAW 1 (randomThinOut / check_probability,
+// inc/allignment_fit.h:466-578): F = exp(-((theta - theta_m) / s_theta)^2 / 2)
+// exp(-((phi - phi_m) / s_phi)^2 / 2) in the box frame, a factor 1 where a
+// scale is 0; the rod stays when 2 F >= u, u from Philox at (stream index, 3,
+// epoch). Rods of cells without a fitted law stay.
+static bool tn_keep(const Real& Re, const float* Lw, const double* Ld, const float4& c, uint64_t si, uint32_t epoch) {
+    if (!(((int)Lw[11]) & 4)) return true;
+    double th, ph;
+    box_angles(c.x, c.y, &th, &ph);
+    const double qt = (th - Ld[0]) / Ld[1], qp = (ph - Ld[2]) / Ld[3];
+    const double F = std::exp(-0.5 * qt * qt) * std::exp(-0.5 * qp * qp);
+    const U4 r = philox((uint32_t)si, (uint32_t)(si >> 32), 3u, epoch, Re.key[0], Re.key[1]);
+    return 2.0 * F >= (double)uni(r.x);
+}
+
 nf_status Engine::epoch_boundary(uint64_t e, uint32_t gained) {
     const nf_params& p = prm[0];
     const uint32_t n = count[0];
@@ -468,6 +580,7 @@ nf_status Engine::epoch_boundary(uint64_t e, uint32_t gained) {
     const bool refit = s > 0 && e > 0 && ((e % (uint64_t)s) == 0 || (double)gained < (double)(tgt - n) / 100.0);
     if (!refit) return NF_OK;
     const size_t nc = (size_t)lawn[0] * lawn[1] * lawn[2];
+    if (p.align_law == 1) return epoch_boundary_tn(e, n);
     NF_CK(cudaMemsetAsync(lacc.p, 0, sizeof(unsigned long long) * 7 * nc, st));
     if (n) NF_LAUNCH(k_law_acc, grid_for(n, 256), 256, 0, st)(n, dreal.p, pos.p, dir.p, lacc.p);
     NF_CK(cudaGetLastError());
@@ -496,6 +609,48 @@ nf_status Engine::epoch_boundary(uint64_t e, uint32_t gained) {
             ad_thinned += removed;
         }
     }
+    return NF_OK;
+}
+
+// Refit (and thin-out) under ALIGN_LAW 1 after epoch e: the rods come to the
+// host, the cell laws are fitted there in FP64 (fit_tn_cell) and the thin-out
+// decided there (tn_keep).
+nf_status Engine::epoch_boundary_tn(uint64_t e, uint32_t n) {
+    const nf_params& p = prm[0];
+    const size_t nc = (size_t)lawn[0] * lawn[1] * lawn[2];
+    std::vector<float4> hp(n), hd(n);
+    std::vector<uint64_t> hs(n);
+    if (n) {
+        NF_CK(cudaMemcpyAsync(hp.data(), pos.p, sizeof(float4) * n, cudaMemcpyDeviceToHost, st));
+        NF_CK(cudaMemcpyAsync(hd.data(), dir.p, sizeof(float4) * n, cudaMemcpyDeviceToHost, st));
+        NF_CK(cudaMemcpyAsync(hs.data(), sidx.p, sizeof(uint64_t) * n, cudaMemcpyDeviceToHost, st));
+        NF_CK(cudaStreamSynchronize(st));
+    }
+    const Real& Re = hreal[0];
+    std::vector<std::vector<uint32_t>> members(nc);
+    for (uint32_t i = 0; i < n; ++i) members[law_cell(Re, hp[i].x, hp[i].y, hp[i].z)].push_back(i);
+    const size_t need = p.align_min > 0 ? (size_t)p.align_min : 1;
+    for (size_t c = 0; c < nc; ++c)
+        if (members[c].size() >= need)
+            fit_tn_cell(hd.data(), members[c], p.ref_trunc_normal, &hlaw[c * kLawF], &hlawd[c * kLawD]);
+    NF_CK(cudaMemcpyAsync(law.p, hlaw.data(), sizeof(float) * hlaw.size(), cudaMemcpyHostToDevice, st));
+    NF_CK(cudaMemcpyAsync(lawd.p, hlawd.data(), sizeof(double) * hlawd.size(), cudaMemcpyHostToDevice, st));
+    ++ad_refits;
+    if (!(p.reduce_flag && n)) return NF_OK;
+    std::vector<uint32_t> keepf(n + 1, 0u);
+    uint32_t removed = 0;
+    for (uint32_t i = 0; i < n; ++i) {
+        const size_t c = law_cell(Re, hp[i].x, hp[i].y, hp[i].z);
+        keepf[i] = tn_keep(Re, &hlaw[c * kLawF], &hlawd[c * kLawD], hd[i], hs[i], (uint32_t)(e + 1)) ? 1u : 0u;
+        removed += keepf[i] ? 0u : 1u;
+    }
+    if (!removed) return NF_OK;
+    DBuf<uint32_t> kf;
+    NF_CK(kf.ensure(n + 1));
+    NF_CK(cudaMemcpyAsync(kf.p, keepf.data(), sizeof(uint32_t) * (n + 1), cudaMemcpyHostToDevice, st));
+    nf_status r = compact_rods(kf.p, n, n - removed);
+    if (r != NF_OK) return r;
+    ad_thinned += removed;
     return NF_OK;
 }
 

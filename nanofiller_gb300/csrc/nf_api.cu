@@ -80,8 +80,9 @@ nf_status validate(const nf_params& p, std::string* why) {
     if ((p.theta_dev > 0 || p.phi_dev > 0) && p.orient_mode == NF_ORIENT_VMF) {
         *why = "ORIENT VMF and DEF_THETA_DEV / DEF_PHI_DEV > 0 are exclusive orientation laws"; return NF_ERR_PARAM;
     }
-    if ((p.theta_dev > 0 || p.phi_dev > 0) && p.self_align_step > 0) {
-        *why = "adaptive generation refits von Mises-Fisher laws; it does not run with DEF_THETA_DEV / DEF_PHI_DEV > 0";
+    if ((p.theta_dev > 0 || p.phi_dev > 0) && p.self_align_step > 0 && p.align_law == 0) {
+        *why = "ALIGN_LAW 0 refits von Mises-Fisher laws; with DEF_THETA_DEV / DEF_PHI_DEV > 0 use ALIGN_LAW 1 "
+               "(the reference's truncated-normal cell laws)";
         return NF_ERR_UNSUPPORTED;
     }
     if (!std::isfinite(p.theta_med) || !std::isfinite(p.phi_med) || !std::isfinite(p.theta_dev) ||
@@ -97,6 +98,7 @@ nf_status validate(const nf_params& p, std::string* why) {
     }
     if (!(p.lambda > 0) || !(p.G0 > 0)) { *why = "tunnelling law needs G0 > 0 and lambda > 0"; return NF_ERR_PARAM; }
     if (!std::isfinite(p.tube_load)) { *why = "TUBE_LOAD must be finite"; return NF_ERR_PARAM; }
+    if (p.align_law < 0 || p.align_law > 1) { *why = "ALIGN_LAW must be 0 or 1"; return NF_ERR_PARAM; }
     if (p.stencil_radius < 0 || p.stencil_radius > 2 || !(p.round_overshoot >= 0) || p.two_phase_work != p.two_phase_work) {
         *why = "STENCIL_RADIUS must be 0, 1 or 2 and ROUND_OVERSHOOT >= 0"; return NF_ERR_PARAM;
     }
@@ -254,6 +256,7 @@ nf_status nf_params_from_file(const char* path, nf_params* p, int* n_unknown) {
         else if (key == "REF_PARALLEL_TYPO") in >> p->ref_parallel_typo;
         else if (key == "TRUNC_NORMAL_REF") in >> p->ref_trunc_normal;
         else if (key == "TUBE_LOAD") in >> p->tube_load;
+        else if (key == "ALIGN_LAW") in >> p->align_law;
         else if (key == "SCREENING") in >> p->screening;
         else if (key == "ROUND_CANDIDATES") in >> p->round_candidates;
         else if (key == "SOLVE_MAX_ITER") in >> p->solve_max_iter;

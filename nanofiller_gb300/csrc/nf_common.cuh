@@ -327,8 +327,10 @@ struct Real {
     int32_t ebuf;           // electrodes are buffer layers of images (else planes)
     double G0, lambda, dc;
     // per-cell orientation laws of the adaptive generation (null: the global
-    // law above): kLawF floats per law cell, grid an[] with an[d] / L[d] in ainv
+    // law above): kLawF floats per law cell, grid an[] with an[d] / L[d] in ainv;
+    // lawd: kLawD doubles per law cell (the truncated-normal laws of ALIGN_LAW 1)
     const float* law;
+    const double* lawd;
     int32_t an[3];
     float ainv[3];
 };
@@ -336,9 +338,13 @@ struct Real {
 // One orientation law: rotation m[9] (row-major, applied to the drawn
 // direction; column 2 is the law's axis), kappa, exp(-2 kappa), sampling
 // flags (bit 0: von Mises-Fisher with that kappa, else isotropic; bit 1:
-// rotate the draw by m). kappa > 0 with bit 0 clear: a fitted law that only
-// the thin-out uses.
-constexpr int kLawF = 12;
+// rotate the draw by m; bit 2: theta / phi drawn by the cell's own
+// truncated-normal laws where the realisation's law draws them so), the
+// cell's median theta and phi. kappa > 0 with bit 0 clear: a fitted law that
+// only the thin-out uses. The doubles of a cell: theta median and scale, phi
+// median and scale, then (c1, c2, zmax) of tn_angle for theta and for phi.
+constexpr int kLawF = 14;
+constexpr int kLawD = 10;
 
 // Law cell of a point: floor(x an / L) per axis, clamped to the grid.
 NF_HD uint32_t law_cell(const Real& R, float x, float y, float z) {
@@ -397,14 +403,24 @@ NF_HD void candidate(const Real& R, uint64_t k, float4* pos, float4* dir, float*
     const float* m = R.m;
     float kappa = R.kappa, E2 = R.E2;
     bool vmf = R.orient == 1, rot = R.rot != 0;
+    float tmed = R.tmed, pmed = R.pmed;
+    double tc1 = R.tc1, tc2 = R.tc2, tz = R.tz, pc1 = R.pc1, pc2 = R.pc2, pz = R.pz;
     if (R.law) {
-        const float* Lw = R.law + (size_t)kLawF * law_cell(R, x, y, z);
+        const uint32_t lc = law_cell(R, x, y, z);
+        const float* Lw = R.law + (size_t)kLawF * lc;
         m = Lw;
         kappa = Lw[9];
         E2 = Lw[10];
         const int fl = (int)Lw[11];
         vmf = (fl & 1) != 0;
         rot = (fl & 2) != 0;
+        if (fl & 4) {  // the cell's truncated-normal laws
+            const double* Ld = R.lawd + (size_t)kLawD * lc;
+            tmed = Lw[12];
+            pmed = Lw[13];
+            tc1 = Ld[4]; tc2 = Ld[5]; tz = Ld[6];
+            pc1 = Ld[7]; pc2 = Ld[8]; pz = Ld[9];
+        }
     }
     float cz;
     if (vmf) {
@@ -413,7 +429,7 @@ NF_HD void candidate(const Real& R, uint64_t k, float4* pos, float4* dir, float*
         cz = fadd(1.0f, fdiv(log_nf(v), kappa));
         cz = cz < -1.0f ? -1.0f : (cz > 1.0f ? 1.0f : cz);
     } else if (R.tn & 1) {  // genCosine: cos of a truncated-normal theta
-        const double th = tn_angle(uni(B.x), R.tmed, R.tc1, R.tc2, R.tz);
+        const double th = tn_angle(uni(B.x), tmed, tc1, tc2, tz);
         float st;
         sincos_turns((float)dmul(th, kInv2PiD), &cz, &st);
     } else {
@@ -421,7 +437,7 @@ NF_HD void candidate(const Real& R, uint64_t k, float4* pos, float4* dir, float*
     }
     float cp, sp;
     if (R.tn & 2) {  // truncated-normal phi
-        const double ph = tn_angle(uni(B.y), R.pmed, R.pc1, R.pc2, R.pz);
+        const double ph = tn_angle(uni(B.y), pmed, pc1, pc2, pz);
         sincos_turns((float)dmul(ph, kInv2PiD), &cp, &sp);
     } else {
         sincos_turns(uni(B.y), &cp, &sp);

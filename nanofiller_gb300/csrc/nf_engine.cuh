@@ -226,7 +226,9 @@ struct Engine {
     // adaptive generation (single realisation): per-cell orientation laws,
     // their tensor sums, and the clusterisation neighbour lists
     std::vector<float> hlaw;        // kLawF floats per law cell (host mirror)
+    std::vector<double> hlawd;      // kLawD doubles per law cell (host mirror)
     DBuf<float> law;
+    DBuf<double> lawd;
     DBuf<unsigned long long> lacc;  // 7 fixed-point sums per law cell
     int32_t lawn[3] = {0, 0, 0};
     bool laws_set = false;          // hlaw holds the laws of the last generation
@@ -280,6 +282,7 @@ struct Engine {
     bool adaptive() const;
     nf_status laws_reset();
     nf_status epoch_boundary(uint64_t epoch_done, uint32_t gained);
+    nf_status epoch_boundary_tn(uint64_t epoch_done, uint32_t n);
     nf_status clusterize(uint64_t slots, const uint32_t* ntot, uint32_t n_old);
     // adds the snaps of the round's candidates with stream index < limit
     nf_status count_snaps(uint64_t slots, const uint32_t* ntot, uint64_t limit);
@@ -403,6 +406,9 @@ nf_status Engine::tube_register_objects(uint32_t n, Src src) {
 
 // Derived realisation descriptor (identical arithmetic to the oracle).
 Real make_real(const nf_params& p, const float* dmesh, int mn[3], double reach);
+// Constants (c1, c2, zmax) of tn_angle for scale s on +- w (ref: the
+// reference's sym_truncNormal form).
+void tn_consts(float s, double w, int ref, double* c1, double* c2, double* zmax);
 double stage_reach(const nf_params& p);
 int64_t target_count(const nf_params& p);
 

@@ -79,25 +79,26 @@ double stage_reach(const nf_params& p) {
 // inc/cuda_CNTgenerate.h:262-275): theta (from the preferred axis) normal about
 // DEF_THETA_MED truncated to +- pi/2, phi about DEF_PHI_MED truncated to +- pi,
 // each only where its deviation is positive; the constants of tn_angle.
+void tn_consts(float s, double w, int ref, double* c1, double* c2, double* zmax) {
+    const double sd = (double)s;
+    const double z = ddiv(ddiv(w, sd), kSqrt2);
+    if (ref) {
+        *c1 = dmul(0.5, erf_d(z));
+        *c2 = dmul(dmul(2.0, sd), kSqrt2);
+        *zmax = 1e300;
+    } else {
+        *c1 = erf_d(z);
+        *c2 = dmul(sd, kSqrt2);
+        *zmax = z;
+    }
+}
+
 void set_tn_law(Real& R, const nf_params& p) {
-    auto law = [&](float s, double w, double* c1, double* c2, double* zmax) {
-        const double sd = (double)s;
-        const double z = ddiv(ddiv(w, sd), kSqrt2);
-        if (p.ref_trunc_normal) {
-            *c1 = dmul(0.5, erf_d(z));
-            *c2 = dmul(dmul(2.0, sd), kSqrt2);
-            *zmax = 1e300;
-        } else {
-            *c1 = erf_d(z);
-            *c2 = dmul(sd, kSqrt2);
-            *zmax = z;
-        }
-    };
     R.tn = (p.theta_dev > 0 ? 1 : 0) | (p.phi_dev > 0 ? 2 : 0);
     R.tmed = p.theta_med;
     R.pmed = p.phi_med;
-    if (R.tn & 1) law(p.theta_dev, dmul(kPiD, 0.5), &R.tc1, &R.tc2, &R.tz);
-    if (R.tn & 2) law(p.phi_dev, kPiD, &R.pc1, &R.pc2, &R.pz);
+    if (R.tn & 1) tn_consts(p.theta_dev, dmul(kPiD, 0.5), p.ref_trunc_normal, &R.tc1, &R.tc2, &R.tz);
+    if (R.tn & 2) tn_consts(p.phi_dev, kPiD, p.ref_trunc_normal, &R.pc1, &R.pc2, &R.pz);
 }
 
 // Tube grid of the pair sweeps (nf_tube.cuh). The registration radius is half

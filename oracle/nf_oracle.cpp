@@ -240,13 +240,18 @@ struct Stream {
     float dflt;
     // per-cell orientation laws of the adaptive generation (null: the law above)
     const float* law = nullptr;
+    const double* lawd = nullptr;  // ALIGN_LAW 1: kLawD doubles per cell
     int an[3] = {1, 1, 1};
     float ainv[3] = {0, 0, 0};
 };
 
 // Law layout: m[9] row-major (column 2 the axis), kappa, exp(-2 kappa),
-// sampling flags (bit 0 von Mises-Fisher, bit 1 rotate).
-constexpr int kLawF = 12;
+// sampling flags (bit 0 von Mises-Fisher, bit 1 rotate, bit 2 the cell's own
+// truncated-normal theta / phi laws), the cell's median theta and phi; the
+// doubles: theta median and scale, phi median and scale, tn_angle's
+// (c1, c2, zmax) for theta and for phi.
+constexpr int kLawF = 14;
+constexpr int kLawD = 10;
 
 int law_cell(const Stream& S, float x, float y, float z) {
     const float v[3] = {x, y, z};
@@ -256,6 +261,18 @@ int law_cell(const Stream& S, float x, float y, float z) {
         c[d] = i < 0 ? 0 : (i >= S.an[d] ? S.an[d] - 1 : i);
     }
     return c[0] + S.an[0] * (c[1] + S.an[1] * c[2]);
+}
+
+// Constants of tn_angle for the scale s on +- w: the exact truncated normal,
+// or the reference's own form (ref).
+void tn_law(float sdev, double w, int ref, double* c1, double* c2, double* zmax) {
+    const double sd = (double)sdev;
+    const double z = (w / sd) / kSqrt2;
+    if (ref) {
+        *c1 = 0.5 * erf_d(z); *c2 = (2.0 * sd) * kSqrt2; *zmax = 1e300;
+    } else {
+        *c1 = erf_d(z); *c2 = sd * kSqrt2; *zmax = z;
+    }
 }
 
 Stream make_stream(const nf_params* p, const float* mesh, int nx, int ny, int nz) {
@@ -279,20 +296,11 @@ Stream make_stream(const nf_params* p, const float* mesh, int nx, int ny, int nz
     // genCosine / sym_truncNormal (inc/cuda_CNTgenerate.h:262-275): theta
     // truncated to med +- pi/2, phi to med +- pi; exact normal by default,
     // the reference's 2 s sqrt2 erfinv(Fa (1 - 2u)) form on request (Q2)
-    auto law = [&](float sdev, double w, double* c1, double* c2, double* zmax) {
-        const double sd = (double)sdev;
-        const double z = (w / sd) / kSqrt2;
-        if (p->ref_trunc_normal) {
-            *c1 = 0.5 * erf_d(z); *c2 = (2.0 * sd) * kSqrt2; *zmax = 1e300;
-        } else {
-            *c1 = erf_d(z); *c2 = sd * kSqrt2; *zmax = z;
-        }
-    };
     S.tn = (p->theta_dev > 0 ? 1 : 0) | (p->phi_dev > 0 ? 2 : 0);
     S.tmed = p->theta_med;
     S.pmed = p->phi_med;
-    if (S.tn & 1) law(p->theta_dev, kPiD * 0.5, &S.tc1, &S.tc2, &S.tz);
-    if (S.tn & 2) law(p->phi_dev, kPiD, &S.pc1, &S.pc2, &S.pz);
+    if (S.tn & 1) tn_law(p->theta_dev, kPiD * 0.5, p->ref_trunc_normal, &S.tc1, &S.tc2, &S.tz);
+    if (S.tn & 2) tn_law(p->phi_dev, kPiD, p->ref_trunc_normal, &S.pc1, &S.pc2, &S.pz);
     S.l = p->l; S.a = p->a;
     S.sigma = p->len_sigma_ln; S.lmin = p->len_min; S.lmax = p->len_max;
     S.rmin = p->rad_min; S.rmax = p->rad_max;
@@ -343,14 +351,24 @@ void candidate(const Stream& S, uint64_t k, float* o) {
     const float* m = S.m;
     float kappa = S.kappa, E2 = S.E2;
     bool vmf = S.orient == NF_ORIENT_VMF, rot = S.rot;
+    float tmed = S.tmed, pmed = S.pmed;
+    double tc1 = S.tc1, tc2 = S.tc2, tz = S.tz, pc1 = S.pc1, pc2 = S.pc2, pz = S.pz;
     if (S.law) {  // the law of the candidate's cell
-        const float* Lw = S.law + (size_t)kLawF * law_cell(S, x, y, z);
+        const int lc = law_cell(S, x, y, z);
+        const float* Lw = S.law + (size_t)kLawF * lc;
         m = Lw;
         kappa = Lw[9];
         E2 = Lw[10];
         const int fl = (int)Lw[11];
         vmf = (fl & 1) != 0;
         rot = (fl & 2) != 0;
+        if (fl & 4) {
+            const double* Ld = S.lawd + (size_t)kLawD * lc;
+            tmed = Lw[12];
+            pmed = Lw[13];
+            tc1 = Ld[4]; tc2 = Ld[5]; tz = Ld[6];
+            pc1 = Ld[7]; pc2 = Ld[8]; pz = Ld[9];
+        }
     }
     float cz;
     if (vmf) {
@@ -360,7 +378,7 @@ void candidate(const Stream& S, uint64_t k, float* o) {
         if (cz < -1.0f) cz = -1.0f;
         if (cz > 1.0f) cz = 1.0f;
     } else if (S.tn & 1) {  // cos of a truncated-normal theta
-        const double th = tn_angle(uni(B[0]), S.tmed, S.tc1, S.tc2, S.tz);
+        const double th = tn_angle(uni(B[0]), tmed, tc1, tc2, tz);
         float st;
         sincos_turns((float)(th * kInv2PiD), &cz, &st);
     } else {
@@ -368,7 +386,7 @@ void candidate(const Stream& S, uint64_t k, float* o) {
     }
     float cp, sp;
     if (S.tn & 2) {  // truncated-normal phi
-        const double ph = tn_angle(uni(B[1]), S.pmed, S.pc1, S.pc2, S.pz);
+        const double ph = tn_angle(uni(B[1]), pmed, pc1, pc2, pz);
         sincos_turns((float)(ph * kInv2PiD), &cp, &sp);
     } else {
         sincos_turns(uni(B[1]), &cp, &sp);
@@ -741,6 +759,103 @@ void law_from_sums(const int64_t sm[7], bool sample, float* Lw) {
     Lw[11] = sample ? (float)((kf > 0.0f ? 1 : 0) | 2) : 0.0f;
 }
 
+// ALIGN_LAW 1: the reference's cell law (crossMtxBuild, resetOrt,
+// resetAvgVec; inc/allignment_fit.h:154-210, 214-274, 353-458) from the
+// directions of the cell's rods in rod order, in FP64: the preferred axis is
+// the unit eigenvector of <c c^T> of the largest eigenvalue when the two
+// smaller (by magnitude) are within 10 % of each other, else of the
+// smallest, signed with v_z > 0; theta_o = acos(v_z), phi_o =
+// acos(v_x / sin theta_o) (1e-6 guards), the draw rotated by
+// inc_rotation(phi_o, -theta_o). When the unit-free mean direction has a norm
+// per rod above 0.5 (def_minOrtNorm, src/simPrms.cpp:42), its box-frame
+// angles (Ort2Angle, inc/vectorMath.h:85-90) are the medians and the mean
+// squared deviations of the rods' angles from them the scales of the
+// truncated-normal draws (the reference's rotation into the preferred frame
+// discards its result, so the angles are box-frame angles).
+void box_angles(double cx, double cy, double* th, double* ph) {
+    const double nxy = std::sqrt(cx * cx + cy * cy);
+    *th = std::asin(nxy > 1.0 ? 1.0 : nxy);
+    double q = nxy > 1e-6 ? cx / nxy : 0.0;
+    q = q > 1.0 ? 1.0 : (q < -1.0 ? -1.0 : q);
+    *ph = nxy > 1e-6 ? std::acos(q) : 0.0;
+}
+
+void tn_cell_law(const std::vector<const nfo_rod*>& rs, int ref, float* Lw, double* Ld) {
+    const double n = (double)rs.size();
+    double A[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+    double ax = 0, ay = 0, az = 0;
+    for (const nfo_rod* r : rs) {
+        const double x = r->cx, y = r->cy, z = r->cz;
+        A[0][0] += x * x; A[1][1] += y * y; A[2][2] += z * z;
+        A[0][1] += x * y; A[0][2] += x * z; A[1][2] += y * z;
+        ax += x; ay += y; az += z;
+    }
+    for (int i = 0; i < 3; ++i)
+        for (int j = i; j < 3; ++j) A[i][j] /= n;
+    A[1][0] = A[0][1]; A[2][0] = A[0][2]; A[2][1] = A[1][2];
+    double V[3][3];
+    sym_eig3(A, V);
+    int o[3] = {0, 1, 2};
+    for (int a = 0; a < 3; ++a)
+        for (int b = a + 1; b < 3; ++b)
+            if (std::fabs(A[o[b]][o[b]]) > std::fabs(A[o[a]][o[a]])) std::swap(o[a], o[b]);
+    const double e1 = A[o[1]][o[1]], e2 = A[o[2]][o[2]];
+    const int k = std::fabs((e1 - e2) / e1) < 0.1 ? o[0] : o[2];
+    double v[3] = {V[0][k], V[1][k], V[2][k]};
+    const double nv = std::sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+    for (int d = 0; d < 3; ++d) v[d] /= nv;
+    if (v[2] < 0 || (v[2] == 0 && (v[1] < 0 || (v[1] == 0 && v[0] < 0))))
+        for (int d = 0; d < 3; ++d) v[d] = -v[d];
+    const double tho = std::fabs(v[2]) <= 1.0 - 1e-6 ? std::acos(v[2]) : (v[2] > 0 ? 0.0 : kPiD);
+    const double sth = std::sin(tho);
+    const double cph = std::fabs(sth) > 1e-6 ? v[0] / sth : 1.0;
+    const double pho = std::fabs(cph) <= 1.0 - 1e-6 ? std::acos(cph) : (cph > 0 ? 0.0 : kPiD);
+    float cM, sM, cX, sX;
+    sincos_turns((float)(pho / (2.0 * kPiD)), &cM, &sM);
+    sincos_turns((float)(-tho / (2.0 * kPiD)), &cX, &sX);
+    Lw[0] = cM * cX;  Lw[1] = sM;   Lw[2] = -sX * cM;
+    Lw[3] = -sM * cX; Lw[4] = cM;   Lw[5] = sX * sM;
+    Lw[6] = sX;       Lw[7] = 0.0f; Lw[8] = cX;
+    Lw[9] = 0.0f;
+    Lw[10] = 0.0f;
+    int fl = 2 | ((int)Lw[11] & 4);
+    const double na = std::sqrt(ax * ax + ay * ay + az * az);
+    if (na / n > 0.5) {
+        double th, ph;
+        box_angles(ax / na, ay / na, &th, &ph);
+        double st = 0.0, sp = 0.0;
+        for (const nfo_rod* r : rs) {
+            double dt, dp;
+            box_angles(r->cx, r->cy, &dt, &dp);
+            st += (dt - th) * (dt - th);
+            sp += (dp - ph) * (dp - ph);
+        }
+        const float ft = (float)th, fp = (float)ph;
+        const float dt = std::max((float)(st / n), 1e-12f), dp = std::max((float)(sp / n), 1e-12f);
+        Lw[12] = ft;
+        Lw[13] = fp;
+        Ld[0] = ft; Ld[1] = dt; Ld[2] = fp; Ld[3] = dp;
+        tn_law(dt, kPiD * 0.5, ref, &Ld[4], &Ld[5], &Ld[6]);
+        tn_law(dp, kPiD, ref, &Ld[7], &Ld[8], &Ld[9]);
+        fl |= 4;
+    }
+    Lw[11] = (float)fl;
+}
+
+// Thin-out under ALIGN_LAW 1 (randomThinOut / check_probability,
+// inc/allignment_fit.h:466-578): the rod stays when 2 F >= u, F the product of
+// the Gaussian factors of its box-frame theta and phi under the cell's law.
+bool tn_keep(const Stream& S, const float* Lw, const double* Ld, const nfo_rod& r, uint64_t si, uint32_t epoch) {
+    if (!(((int)Lw[11]) & 4)) return true;
+    double th, ph;
+    box_angles(r.cx, r.cy, &th, &ph);
+    const double qt = (th - Ld[0]) / Ld[1], qp = (ph - Ld[2]) / Ld[3];
+    const double F = std::exp(-0.5 * qt * qt) * std::exp(-0.5 * qp * qp);
+    uint32_t ctr[4] = {(uint32_t)si, (uint32_t)(si >> 32), 3u, epoch}, o[4];
+    philox(ctr, S.key, o);
+    return 2.0 * F >= (double)uni(o[0]);
+}
+
 inline float dotf(const float* a, const float* b) { return (a[0] * b[0] + a[1] * b[1]) + a[2] * b[2]; }
 
 // cnt_minDist (inc/intersection_dev.h:85-160) in FP32; the parameters before
@@ -967,6 +1082,20 @@ int nfo_fit_law(const int64_t sums[7], int sample, float law[12]) {
     return 0;
 }
 
+int nfo_tn_cell_law(const float* dirs, int64_t n, int ref, float law[14], double lawd[10]) {
+    if (!dirs || !law || !lawd || n <= 0) return -1;
+    std::vector<nfo_rod> rs((size_t)n);
+    std::vector<const nfo_rod*> ptr((size_t)n);
+    for (int64_t i = 0; i < n; ++i) {
+        rs[i] = nfo_rod{0, 0, 0, dirs[3 * i], dirs[3 * i + 1], dirs[3 * i + 2], 0, 0};
+        ptr[i] = &rs[i];
+    }
+    for (int q = 0; q < kLawF; ++q) law[q] = 0.0f;
+    for (int q = 0; q < kLawD; ++q) lawd[q] = 0.0;
+    tn_cell_law(ptr, ref, law, lawd);
+    return 0;
+}
+
 int nfo_candidates(const nf_params* p, const float* mesh, int nx, int ny, int nz, uint64_t k0,
                    uint64_t n, float* out) {
     if (!p || !out) return -1;
@@ -1007,6 +1136,7 @@ int64_t nfo_generate(const nf_params* p, const float* mesh, int nx, int ny, int 
                                                                 : std::max<uint64_t>(1024, (uint64_t)target))
                                      : 0;
     std::vector<float> laws;
+    std::vector<double> lawsd;
     int an[3] = {1, 1, 1};
     if (adapt) {
         float ainv[3];
@@ -1020,7 +1150,9 @@ int64_t nfo_generate(const nf_params* p, const float* mesh, int nx, int ny, int 
             Lw[10] = S.orient == NF_ORIENT_VMF ? S.E2 : 0.0f;
             Lw[11] = (float)((S.orient == NF_ORIENT_VMF ? 1 : 0) | (S.rot ? 2 : 0));
         }
+        lawsd.assign(nc * kLawD, 0.0);
         S.law = laws.data();
+        S.lawd = lawsd.data();
         for (int d = 0; d < 3; ++d) { S.an[d] = an[d]; S.ainv[d] = ainv[d]; }
     }
     uint64_t epochs = 0, refits = 0, thinned = 0, snapped = 0;
@@ -1044,6 +1176,35 @@ int64_t nfo_generate(const nf_params* p, const float* mesh, int nx, int ny, int 
                            ((e % (uint64_t)st) == 0 || (double)gained < (double)(target - acc) / 100.0);
         if (!refit) return;
         const size_t nc = (size_t)an[0] * an[1] * an[2];
+        if (p->align_law == 1) {  // the reference's truncated-normal cell laws
+            std::vector<std::vector<const nfo_rod*>> members(nc);
+            for (int64_t j = 0; j < acc; ++j) {
+                const nfo_rod& r = rods[j];
+                members[(size_t)law_cell(S, r.x, r.y, r.z)].push_back(&rods[j]);
+            }
+            const size_t need = p->align_min > 0 ? (size_t)p->align_min : 1;
+            for (size_t c = 0; c < nc; ++c)
+                if (members[c].size() >= need)
+                    tn_cell_law(members[c], p->ref_trunc_normal, &laws[c * kLawF], &lawsd[c * kLawD]);
+            ++refits;
+            if (!p->reduce_flag) return;
+            int64_t w = 0;
+            for (int64_t j = 0; j < acc; ++j) {
+                const nfo_rod& r = rods[j];
+                const size_t c = (size_t)law_cell(S, r.x, r.y, r.z);
+                if (!tn_keep(S, &laws[c * kLawF], &lawsd[c * kLawD], r, sidx_all[j], (uint32_t)(e + 1))) continue;
+                rods[w] = rods[j];
+                accD[w] = accD[j];
+                sidx_all[w] = sidx_all[j];
+                ++w;
+            }
+            thinned += (uint64_t)(acc - w);
+            acc = w;
+            accD.resize(acc);
+            sidx_all.resize(acc);
+            rebuild();
+            return;
+        }
         std::vector<int64_t> sums(7 * nc, 0);
         for (int64_t j = 0; j < acc; ++j) {
             const nfo_rod& r = rods[j];

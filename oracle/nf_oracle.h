@@ -91,6 +91,10 @@ int nfo_clust_snap(const nf_params *p, const nfo_rod *cand, const nfo_rod *older
  * (each product c_i c_j rounded to 2^-40 units): law[0..8] rotation (column 2
  * the axis), law[9] kappa, law[10] exp(-2 kappa), law[11] sampling flags. */
 int nfo_fit_law(const int64_t sums[7], int sample, float law[12]);
+/* ALIGN_LAW 1: the reference's truncated-normal law of one cell from the
+ * directions (n x 3) of its rods: law[14] (rotation, flags, medians), lawd[10]
+ * (medians and scales, tn_angle constants). */
+int nfo_tn_cell_law(const float* dirs, int64_t n, int ref, float law[14], double lawd[10]);
 
 /* Candidate stream k0..k0+n-1: out[10*i + f], f = x y z cx cy cz l a u rho. */
 int nfo_candidates(const nf_params *p, const float *mesh, int nx, int ny, int nz,

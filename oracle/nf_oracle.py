@@ -45,7 +45,8 @@ class NfParams(C.Structure):
         ("elec_buffer", C.c_int32), ("ref_trunc_normal", C.c_int32),
         ("clust_dist", C.c_float), ("clust_angl", C.c_float), ("align_cell", C.c_float),
         ("align_min", C.c_int32), ("epoch_candidates", C.c_int64),
-        ("solve_method", C.c_int32), ("tube_load", C.c_float),
+        ("solve_method", C.c_int32), ("tube_load", C.c_float), ("align_law", C.c_int32),
+        ("reserved", C.c_int32),
     ]
 
 
@@ -117,6 +118,7 @@ def lib():
             L.nfo_generate.restype = C.c_int64
             L.nfo_clust_snap.argtypes = [P(NfParams), C.c_void_p, C.c_void_p, P(C.c_float), C.c_void_p]
             L.nfo_fit_law.argtypes = [P(C.c_int64), C.c_int, P(C.c_float)]
+            L.nfo_tn_cell_law.argtypes = [P(C.c_float), C.c_int64, C.c_int, P(C.c_float), P(C.c_double)]
             L.nfo_contacts.argtypes = [P(NfParams), C.c_void_p, C.c_int64, C.c_int, C.c_int,
                                        C.c_int64] + [C.c_void_p] * 8 + [P(C.c_int64)]
             L.nfo_contacts.restype = C.c_int64
@@ -318,6 +320,9 @@ def solve_internal(net, ct):
     return float(np.sum(b * (1.0 - x))), v, info
 
 
+LAW_F = 14  # floats per law cell (kLawF)
+
+
 def generate(params, mesh=None, nthreads=0, batch=4096, brute_force=False, cap=None):
     p = make_params(params)
     if cap is None:
@@ -328,13 +333,13 @@ def generate(params, mesh=None, nthreads=0, batch=4096, brute_force=False, cap=N
     nx, ny, nz = mesh.shape if mesh is not None else (0, 0, 0)
     m = None if mesh is None else np.ascontiguousarray(mesh, np.float32)
     ext = np.zeros(3, np.int32)
-    lcap = 12 * 256 ** 3 if (p.self_align_step > 0 or p.clust_flag) else 0
+    lcap = LAW_F * 256 ** 3 if (p.self_align_step > 0 or p.clust_flag) else 0
     laws = np.zeros(0, np.float32)
     if lcap:
         bx = np.array(p.box[:], np.float64)
         e = p.align_cell if p.align_cell > 0 else p.l
         nc = int(np.prod(np.clip(np.floor(bx / e), 1, 256)))
-        laws = np.zeros(12 * nc, np.float32)
+        laws = np.zeros(LAW_F * nc, np.float32)
         lcap = laws.size
     n = lib().nfo_generate(C.byref(p), _ptr(m), nx, ny, nz, nthreads, batch, int(brute_force),
                            cap, _ptr(rods), _ptr(idx), st, _ptr(laws) if lcap else None, lcap, _ptr(ext))
@@ -343,7 +348,7 @@ def generate(params, mesh=None, nthreads=0, batch=4096, brute_force=False, cap=N
     info = dict(drawn=st[0], density_accepted=st[1], exact_evals=st[2], epochs=st[3], refits=st[4],
                 thinned=st[5], snapped=st[6])
     if lcap:
-        info["laws"] = laws.reshape(-1, 12)
+        info["laws"] = laws.reshape(-1, LAW_F)
         info["law_ext"] = tuple(int(v) for v in ext)
     return rods[:n].copy(), idx[:n].copy(), info
 
@@ -375,6 +380,21 @@ def fit_law(sums, sample=True):
         raise ValueError("empty cell")
     v = np.array(out[:], np.float32)
     return dict(m=v[:9].reshape(3, 3), axis=v[[2, 5, 8]], kappa=float(v[9]), E2=float(v[10]), flags=int(v[11]))
+
+
+def tn_cell_law(dirs, ref=False):
+    """ALIGN_LAW 1 law of one cell from its rods' directions (n x 3):
+    {"m": 3x3 rotation, "flags", "theta", "phi" (medians), "theta_scale",
+    "phi_scale", "consts": tn_angle (c1, c2, zmax) for theta then phi}."""
+    d = np.ascontiguousarray(dirs, np.float32).reshape(-1, 3)
+    law = (C.c_float * 14)()
+    lawd = (C.c_double * 10)()
+    if lib().nfo_tn_cell_law(d.ctypes.data_as(C.POINTER(C.c_float)), len(d), int(ref), law, lawd) != 0:
+        raise ValueError("empty cell")
+    v = np.array(law[:], np.float32)
+    w = np.array(lawd[:])
+    return dict(m=v[:9].reshape(3, 3), flags=int(v[11]), theta=float(w[0]), theta_scale=float(w[1]),
+                phi=float(w[2]), phi_scale=float(w[3]), consts=w[4:])
 
 
 def contacts(params, rods, nthreads=0, brute_force=False):

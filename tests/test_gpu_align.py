@@ -13,6 +13,8 @@ fits, FP32 snaps with every operation rounded on its own):
   plain handle has no laws to read (NF_ERR_STATE);
 - the medium agglomerate box (density mesh, von Mises-Fisher) with all
   three steps, bit for bit;
+- ALIGN_LAW 1, the reference's truncated-normal cell laws and Gaussian
+  thin-out with DEF_THETA_* / DEF_PHI_* set, bit for bit in both draw forms;
 - the command line reads SELF_ALLIGN_STEP, REDUCE_FLAG, CLUST_FLAG,
   CLUST_ANGL_LIM and the project keys and writes the library's output.bin
   byte for byte.
@@ -81,6 +83,23 @@ def test_isotropic_thinout_matches_oracle(gpu, oracle):
     out = run_both(gpu, oracle, cfg)
     check_equal(*out)
     assert out[0]["thinned"] > 0 and out[0]["snapped"] == 0
+
+
+def test_reference_cell_law_matches_oracle(gpu, oracle):
+    """ALIGN_LAW 1 (the reference's truncated-normal cell laws, its
+    Gaussian-likelihood thin-out) with DEF_THETA_* / DEF_PHI_* set, refits,
+    thin-out and clusterisation: bit for bit, both forms of the draw."""
+    base = dict(ADAPT, orient_mode=0, vmf_kappa=0.0, theta_med=0.5, theta_dev=0.3, phi_med=0.8, phi_dev=0.4,
+                align_law=1, seed=11)
+    for ref in (0, 1):
+        out = run_both(gpu, oracle, dict(base, ref_trunc_normal=ref))
+        check_equal(*out)
+        g, so = out[0], out[5]
+        assert g["refits"] > 0 and g["thinned"] > 0 and g["snapped"] > 0
+        assert any(int(f) & 4 for f in so["laws"][:, 11])  # cells drew from their own laws
+    with pytest.raises(gpu.NanoFillerError) as ei:  # the von Mises-Fisher refit does not take these laws
+        gpu.Simulation(dict(base, align_law=0))
+    assert ei.value.status == 11
 
 
 def test_dense_clusterisation_matches_oracle(gpu, oracle):
