@@ -194,7 +194,11 @@ typedef struct nf_params {
                                drawn as DEF_THETA_DEV / DEF_PHI_DEV select
                                and rotated by the preferred axis; thin-out
                                by the reference's Gaussian likelihood        */
-    int32_t reserved;       /* 0                                           */
+    int32_t autotune;       /* AUTOTUNE (tuning, speed only): 1 -> nf_batch_run
+                               first runs nf_autotune on its batch (nine
+                               more generations) and then contacts and
+                               solves under the settings chosen; 0 (default)
+                               the settings given                          */
 } nf_params;
 
 /* Rods, structure of arrays, caller-owned host buffers. Any array may be NULL. */
@@ -572,7 +576,9 @@ nf_status nf_adjoint(nf_handle *h, float *dG_dend, size_t capacity,
  *      one realisation per process, src/NanoFiller.cpp:37-162) ------------ */
 /* One call: a batch handle is created, generated, contacted, solved and
  * destroyed; out[r] holds realisation r's result, stats->ms the device time
- * from the first generation launch to the end of the solve. */
+ * from the first generation launch to the end of the solve (tuning included
+ * when params[0].autotune is 1: the tuner's settings then apply to every
+ * realisation). */
 nf_status nf_batch_run(const nf_params *params, int n, nf_batch_result *out,
                        nf_batch_stats *stats);
 /* A handle holding n realisations side by side (own boxes, fractions,
@@ -599,11 +605,15 @@ nf_status nf_read_state_bin(nf_handle *h, const char *path);
 nf_status nf_write_coo(nf_handle *h, const char *dir);
 
 /* ---- autotuner (no reference counterpart) -------------------------------- */
-/* Times full generations of the handle's realisation under candidate values
- * of stencil_radius, round_overshoot and two_phase_work (one coordinate at a
- * time, each trial run twice and timed on the second) and keeps the fastest
- * in the handle's parameters. The accepted set does not depend on them: the
- * handle ends holding the rods nf_generate gives. out may be NULL. */
+/* Times full generations of the handle's realisations (one, or all of a
+ * batch) under candidate values of the speed-only settings, one coordinate at
+ * a time, each trial run twice and timed on the second, and keeps the fastest
+ * in every realisation's parameters: on the tube grid (the default) the cell
+ * edge through tube_load (24, 32, 64, 96 besides the value on entry) and the
+ * candidates per round through round_overshoot (1.5, 2, 3); on the stencil
+ * sweeps stencil_radius, round_overshoot and two_phase_work. The accepted
+ * sets do not depend on them: the handle ends holding the rods nf_generate
+ * gives. out may be NULL. */
 typedef struct nf_tune_result {
     int32_t stencil_radius;
     float round_overshoot;
@@ -611,6 +621,7 @@ typedef struct nf_tune_result {
     double ms_first;        /* generation time with the settings on entry   */
     double ms_best;         /* with the settings chosen                     */
     int32_t trials;
+    float tube_load;        /* chosen tube load (0: the default, 48)        */
 } nf_tune_result;
 nf_status nf_autotune(nf_handle *h, nf_tune_result *out);
 

@@ -262,8 +262,10 @@ class Simulation:
         _check(self._L.nf_write_internal_coo(self._h, str(path).encode()), self._h, "nf_write_internal_coo")
 
     def autotune(self):
-        """Pick stencil_radius, round_overshoot and two_phase_work by timing
-        generations (nf_autotune); the handle keeps the fastest settings."""
+        """Pick the speed-only settings by timing generations (nf_autotune):
+        tube_load and round_overshoot on the tube grid, stencil_radius,
+        round_overshoot and two_phase_work on the stencil sweeps; the handle
+        (every realisation of a batch) keeps the fastest settings."""
         r = NfTuneResult()
         _check(self._L.nf_autotune(self._h, C.byref(r)), self._h, "nf_autotune")
         return {k: getattr(r, k) for k, _ in r._fields_}

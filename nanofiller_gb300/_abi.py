@@ -43,7 +43,7 @@ class NfParams(C.Structure):
         ("clust_dist", C.c_float), ("clust_angl", C.c_float), ("align_cell", C.c_float),
         ("align_min", C.c_int32), ("epoch_candidates", C.c_int64),
         ("solve_method", C.c_int32), ("tube_load", C.c_float), ("align_law", C.c_int32),
-        ("reserved", C.c_int32),
+        ("autotune", C.c_int32),
     ]
 
 
@@ -139,7 +139,8 @@ class NfAcNet(C.Structure):
 
 class NfTuneResult(C.Structure):
     _fields_ = [("stencil_radius", C.c_int32), ("round_overshoot", C.c_float), ("two_phase_work", C.c_double),
-                ("ms_first", C.c_double), ("ms_best", C.c_double), ("trials", C.c_int32)]
+                ("ms_first", C.c_double), ("ms_best", C.c_double), ("trials", C.c_int32),
+                ("tube_load", C.c_float)]
 
 
 class NfBatchStats(C.Structure):

@@ -99,6 +99,7 @@ nf_status validate(const nf_params& p, std::string* why) {
     if (!(p.lambda > 0) || !(p.G0 > 0)) { *why = "tunnelling law needs G0 > 0 and lambda > 0"; return NF_ERR_PARAM; }
     if (!std::isfinite(p.tube_load)) { *why = "TUBE_LOAD must be finite"; return NF_ERR_PARAM; }
     if (p.align_law < 0 || p.align_law > 1) { *why = "ALIGN_LAW must be 0 or 1"; return NF_ERR_PARAM; }
+    if (p.autotune < 0 || p.autotune > 1) { *why = "AUTOTUNE must be 0 or 1"; return NF_ERR_PARAM; }
     if (p.stencil_radius < 0 || p.stencil_radius > 2 || !(p.round_overshoot >= 0) || p.two_phase_work != p.two_phase_work) {
         *why = "STENCIL_RADIUS must be 0, 1 or 2 and ROUND_OVERSHOOT >= 0"; return NF_ERR_PARAM;
     }
@@ -257,6 +258,7 @@ nf_status nf_params_from_file(const char* path, nf_params* p, int* n_unknown) {
         else if (key == "TRUNC_NORMAL_REF") in >> p->ref_trunc_normal;
         else if (key == "TUBE_LOAD") in >> p->tube_load;
         else if (key == "ALIGN_LAW") in >> p->align_law;
+        else if (key == "AUTOTUNE") in >> p->autotune;
         else if (key == "SCREENING") in >> p->screening;
         else if (key == "ROUND_CANDIDATES") in >> p->round_candidates;
         else if (key == "SOLVE_MAX_ITER") in >> p->solve_max_iter;
@@ -357,13 +359,27 @@ nf_status nf_generate(nf_handle* h, nf_gen_stats* stats) {
 nf_status nf_autotune(nf_handle* h, nf_tune_result* out) {
     if (!h) return NF_ERR_PARAM;
     nf::Engine& E = h->E;
-    if (E.R != 1) return fail(h, NF_ERR_STATE, "the autotuner runs on a single-realisation handle");
+    if (E.R != 1 && E.adaptive()) return fail(h, NF_ERR_STATE, "adaptive generation runs on single handles");
     int trials = 0;
-    // Generation time under q: one untimed run (buffers grow to the new sizes),
-    // then one timed run (CUDA events inside nf_generate).
-    auto time_of = [&](const nf_params& q, double* ms) -> nf_status {
-        E.prm[0] = q;
-        h->p = q;
+    // The speed-only settings, applied to every realisation of the handle.
+    struct Tune {
+        int32_t stencil_radius;
+        float round_overshoot, tube_load;
+        double two_phase_work;
+    };
+    auto apply = [&](const Tune& t) {
+        for (auto& q : E.prm) {
+            q.stencil_radius = t.stencil_radius;
+            q.round_overshoot = t.round_overshoot;
+            q.tube_load = t.tube_load;
+            q.two_phase_work = t.two_phase_work;
+        }
+        h->p = E.prm[0];
+    };
+    // Generation time under t: one untimed run (buffers grow to the new
+    // sizes), then one timed run (CUDA events inside nf_generate).
+    auto time_of = [&](const Tune& t, double* ms) -> nf_status {
+        apply(t);
         nf_status s = E.generate();
         if (s == NF_OK) s = E.generate();
         if (s != NF_OK) return s;
@@ -371,13 +387,14 @@ nf_status nf_autotune(nf_handle* h, nf_tune_result* out) {
         ++trials;
         return NF_OK;
     };
-    nf_params best = h->p;
+    const nf_params& p0 = E.prm[0];
+    Tune best{p0.stencil_radius, p0.round_overshoot, p0.tube_load, p0.two_phase_work};
     double t_best = 0;
     nf_status s = time_of(best, &t_best);
     if (s != NF_OK) return s;
     const double ms_first = t_best;
     auto try_value = [&](auto set, auto value) -> nf_status {
-        nf_params q = best;
+        Tune q = best;
         set(q, value);
         double t = 0;
         nf_status st = time_of(q, &t);
@@ -385,21 +402,33 @@ nf_status nf_autotune(nf_handle* h, nf_tune_result* out) {
         if (t < t_best) { t_best = t; best = q; }
         return NF_OK;
     };
-    for (int r : {1, 2}) {
-        s = try_value([](nf_params& q, int v) { q.stencil_radius = v; }, r);
-        if (s != NF_OK) return s;
-    }
-    for (float f : {1.5f, 2.0f, 3.0f}) {
-        s = try_value([](nf_params& q, float v) { q.round_overshoot = v; }, f);
-        if (s != NF_OK) return s;
-    }
-    for (double w : {1e9, 1e10, -1.0}) {
-        s = try_value([](nf_params& q, double v) { q.two_phase_work = v; }, w);
-        if (s != NF_OK) return s;
+    if (E.tube) {  // tube grid: the cell edge (through the load) and the round size
+        const float on_entry = best.tube_load > 0 ? best.tube_load : 48.0f;
+        for (float l : {24.0f, 32.0f, 64.0f, 96.0f}) {
+            if (l == on_entry) continue;
+            s = try_value([](Tune& q, float v) { q.tube_load = v; }, l);
+            if (s != NF_OK) return s;
+        }
+        for (float f : {1.5f, 2.0f, 3.0f}) {
+            s = try_value([](Tune& q, float v) { q.round_overshoot = v; }, f);
+            if (s != NF_OK) return s;
+        }
+    } else {
+        for (int r : {1, 2}) {
+            s = try_value([](Tune& q, int v) { q.stencil_radius = v; }, r);
+            if (s != NF_OK) return s;
+        }
+        for (float f : {1.5f, 2.0f, 3.0f}) {
+            s = try_value([](Tune& q, float v) { q.round_overshoot = v; }, f);
+            if (s != NF_OK) return s;
+        }
+        for (double w : {1e9, 1e10, -1.0}) {
+            s = try_value([](Tune& q, double v) { q.two_phase_work = v; }, w);
+            if (s != NF_OK) return s;
+        }
     }
     // Leave the handle generated under the chosen settings.
-    E.prm[0] = best;
-    h->p = best;
+    apply(best);
     s = E.generate();
     if (s != NF_OK) return s;
     if (out) {
@@ -409,6 +438,7 @@ nf_status nf_autotune(nf_handle* h, nf_tune_result* out) {
         out->ms_first = ms_first;
         out->ms_best = t_best;
         out->trials = trials;
+        out->tube_load = best.tube_load;
     }
     return NF_OK;
 }
@@ -954,7 +984,9 @@ nf_status nf_batch_run(const nf_params* params, int n, nf_batch_result* out, nf_
     nf::EventPair ev;
     if (ev.create() != cudaSuccess) { nf_destroy(h); return NF_ERR_CUDA; }
     cudaEventRecord(ev.a, E.st);
-    s = E.generate();
+    // with AUTOTUNE the tuner's last generation (under the settings it keeps)
+    // is the batch's generation
+    s = params[0].autotune == 1 ? nf_autotune(h, nullptr) : E.generate();
     if (s == NF_OK) s = E.contacts();
     nf_status ss = NF_OK;
     if (s == NF_OK) ss = E.solve();

@@ -46,7 +46,7 @@ class NfParams(C.Structure):
         ("clust_dist", C.c_float), ("clust_angl", C.c_float), ("align_cell", C.c_float),
         ("align_min", C.c_int32), ("epoch_candidates", C.c_int64),
         ("solve_method", C.c_int32), ("tube_load", C.c_float), ("align_law", C.c_int32),
-        ("reserved", C.c_int32),
+        ("autotune", C.c_int32),
     ]
 
 

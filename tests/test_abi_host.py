@@ -82,6 +82,9 @@ def test_keyword_file(lib, tmp_path):
         "RAD_RANGE 0.004 0.008",
         "RAD_LAW UNIFORM",
         "TUNNEL_LAMBDA 0.00018",
+        "TUBE_LOAD 32",
+        "ALIGN_LAW 1",
+        "AUTOTUNE 1",
         "SOME_UNKNOWN_KEY 3",
         "",
     ]))
@@ -93,6 +96,7 @@ def test_keyword_file(lib, tmp_path):
     assert d["seed"] == 42 and d["n_candidates"] == 12345 and d["orient_mode"] == 1
     assert d["len_mode"] == 1 and d["len_min"] == pytest.approx(0.5) and d["rad_mode"] == 2
     assert d["lambda_"] == pytest.approx(0.00018)
+    assert d["tube_load"] == 32 and d["align_law"] == 1 and d["autotune"] == 1
     missing = lib.load().nf_params_from_file(str(tmp_path / "nope.txt").encode(),
                                              C.byref(lib.make_params()), None)
     assert missing == 8  # NF_ERR_IO

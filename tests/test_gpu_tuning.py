@@ -2,7 +2,9 @@
 round_overshoot and two_phase_work gives the oracle's accepted set and contact
 list bit for bit (two_phase_work = 1 forces the two-phase old-rod test on every
 round, which the default threshold keeps for heavy rounds only), and
-nf_autotune leaves the handle holding the same rods."""
+nf_autotune (on the tube grid: tube_load and round_overshoot; on the stencil
+sweeps: the three above) leaves the handle, single or batch, holding the same
+rods."""
 import numpy as np
 import pytest
 
@@ -46,13 +48,18 @@ def test_settings_do_not_change_results(gpu, medium_oracle, setting):
             assert g["work_items"] > 0
 
 
-def test_autotune_keeps_results(gpu, medium_oracle):
+@pytest.mark.parametrize("load", [0.0, -1.0])
+def test_autotune_keeps_results(gpu, medium_oracle, load):
+    """Tube grid (load 0: the default): tube_load and round_overshoot, 8
+    trials; stencil sweeps (load -1): stencil_radius, round_overshoot and
+    two_phase_work, 9 trials."""
     cfg, mesh, rods_o, idx_o, co = medium_oracle
-    with gpu.Simulation(cfg, mesh=mesh) as sim:
+    with gpu.Simulation(dict(cfg, tube_load=load), mesh=mesh) as sim:
         t = sim.autotune()
-        assert t["trials"] == 9
+        assert t["trials"] == (9 if load < 0 else 8)
         assert 0 < t["ms_best"] <= t["ms_first"] * 1.05
         assert t["stencil_radius"] in (0, 1, 2) and t["round_overshoot"] in (0.0, 1.5, 2.0, 3.0)
+        assert t["tube_load"] == load if load < 0 else t["tube_load"] in (0.0, 24.0, 32.0, 64.0, 96.0)
         sim.contacts()
         check(sim, rods_o, idx_o, co)
         # the chosen settings stay on the handle
@@ -60,8 +67,34 @@ def test_autotune_keeps_results(gpu, medium_oracle):
         assert g["accepted"] == len(idx_o)
 
 
+def test_autotune_batch_keeps_results(gpu):
+    """A batch handle is tuned as one: every realisation keeps its rods and
+    contacts whatever settings the tuner picks."""
+    reals = gpu.configs.batched_realisations(16)
+    ref, _ = gpu.batch_run(reals)
+    with gpu.Batch(reals) as b:
+        t = b.autotune()
+        assert t["trials"] == 8 and 0 < t["ms_best"] <= t["ms_first"] * 1.05
+        b.contacts()
+        b.solve(check=False)
+        res = b.results()
+    assert [(r["accepted"], r["contacts"], r["G_eff"]) for r in res] == \
+           [(r["accepted"], r["contacts"], r["G_eff"]) for r in ref]
+
+
+def test_batch_run_autotune_keeps_results(gpu):
+    """AUTOTUNE 1: nf_batch_run tunes its own batch first; the results are
+    the untuned call's."""
+    reals = gpu.configs.batched_realisations(16)
+    ref, _ = gpu.batch_run(reals)
+    tuned, st = gpu.batch_run([dict(p, autotune=1) for p in reals])
+    assert [(r["accepted"], r["contacts"], r["G_eff"]) for r in tuned] == \
+           [(r["accepted"], r["contacts"], r["G_eff"]) for r in ref]
+    assert st["rods"] == sum(r["accepted"] for r in ref)
+
+
 def test_tuning_parameters_validated(gpu):
-    for bad in (dict(stencil_radius=3), dict(round_overshoot=-1.0)):
+    for bad in (dict(stencil_radius=3), dict(round_overshoot=-1.0), dict(autotune=2)):
         with pytest.raises(gpu.NanoFillerError) as e:
             gpu.Simulation(dict(gpu.configs.SMALL, **bad))
         assert e.value.status == 1
