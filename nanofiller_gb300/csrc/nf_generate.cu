@@ -815,30 +815,51 @@ __global__ void __launch_bounds__(kTPB, 7) k_tube_old(const Real* __restrict__ r
             }
             __syncwarp();
             const uint32_t lo = L.packed ? L.tlo : 0u, len = L.packed ? L.tlen : m;
-            uint32_t mask = 0;
-            if (alive) {
-                tests += len;
-                for (uint32_t u0 = 0; u0 < len; u0 += 8) {
+            if (alive) tests += len;
+            // Pair-parallel marking: the na live probes take 2^s >= na lanes
+            // each (slot = lane mod 2^s); a lane tests its slot's probe
+            // against every (32 >> s)-th target of the probe's range, and the
+            // lanes of a slot OR their marks together for the probe's lane.
+            const unsigned am = __ballot_sync(0xffffffffu, alive);
+            const int na = __popc(am);
+            const int sh = na <= 1 ? 0 : 32 - __clz(na - 1);
+            const int slot = lane & ((1 << sh) - 1);
+            const bool qv = slot < na;
+            const int src = qv ? nth_set_bit(am, slot) : lane;
+            const float qx = __shfl_sync(0xffffffffu, ax, src), qy = __shfl_sync(0xffffffffu, ay, src),
+                        qz = __shfl_sync(0xffffffffu, az, src);
+            const float qcx = __shfl_sync(0xffffffffu, cA.x, src), qcy = __shfl_sync(0xffffffffu, cA.y, src),
+                        qcz = __shfl_sync(0xffffffffu, cA.z, src);
+            const float qh = __shfl_sync(0xffffffffu, hAe, src), qC = __shfl_sync(0xffffffffu, hC, src);
+            const float qerr = __shfl_sync(0xffffffffu, errA, src), qth = __shfl_sync(0xffffffffu, thA, src);
+            const uint32_t qlo = __shfl_sync(0xffffffffu, lo, src);
+            const uint32_t qlen0 = __shfl_sync(0xffffffffu, len, src);
+            const uint32_t qlen = qv ? qlen0 : 0u;
+            const uint32_t step = 32u >> sh;
+            uint32_t qmask = 0;
+            for (uint32_t u0 = (uint32_t)lane >> sh; u0 < qlen; u0 += 4u * step) {
 #pragma unroll
-                    for (uint32_t jj = 0; jj < 8; ++jj) {
-                        const uint32_t u = u0 + jj;
-                        if (u < len) {
-                            const uint32_t j = lo + u;
-                            const float4 tq = T.ps[j];
-                            const float bx = tq.x - ax, by = tq.y - ay, bz = tq.z - az;
-                            const float4 cB = T.c[j];
-                            const float nx = cA.y * cB.z - cA.z * cB.y;
-                            const float ny = cA.z * cB.x - cA.x * cB.z;
-                            const float nz = cA.x * cB.y - cA.y * cB.x;
-                            const float nn = nx * nx + ny * ny + nz * nz;
-                            const float nb = fabsf(nx * bx + ny * by + nz * bz) - fmaf(4e-6f, tq.w, errA);
-                            const float thL = fmaf(cB.w, scf2, thA);
-                            const bool lfar = nn > 1e-4f && nb > 0.0f && nb * nb > thL * thL * nn;
-                            if (!lfar && capsule_near(bx, by, bz, cA.x, cA.y, cA.z, hAe, tq.w, hC)) mask |= 1u << j;
-                        }
+                for (uint32_t jj = 0; jj < 4; ++jj) {
+                    const uint32_t u = u0 + jj * step;
+                    if (u < qlen) {
+                        const uint32_t j = qlo + u;
+                        const float4 tq = T.ps[j];
+                        const float bx = tq.x - qx, by = tq.y - qy, bz = tq.z - qz;
+                        const float4 cB = T.c[j];
+                        const float nx = qcy * cB.z - qcz * cB.y;
+                        const float ny = qcz * cB.x - qcx * cB.z;
+                        const float nz = qcx * cB.y - qcy * cB.x;
+                        const float nn = nx * nx + ny * ny + nz * nz;
+                        const float nb = fabsf(nx * bx + ny * by + nz * bz) - fmaf(4e-6f, tq.w, qerr);
+                        const float thL = fmaf(cB.w, scf2, qth);
+                        const bool lfar = nn > 1e-4f && nb > 0.0f && nb * nb > thL * thL * nn;
+                        if (!lfar && capsule_near(bx, by, bz, qcx, qcy, qcz, qh, tq.w, qC)) qmask |= 1u << j;
                     }
                 }
             }
+            for (int o = 1 << sh; o < 32; o <<= 1) qmask |= __shfl_xor_sync(0xffffffffu, qmask, o);
+            const uint32_t mine = __shfl_sync(0xffffffffu, qmask, __popc(am & ((1u << lane) - 1u)));
+            const uint32_t mask = alive ? mine : 0u;
             auto keep = [&](int pl, int t) {
                 if ((dead >> pl) & 1u) return false;
                 int img[3];
@@ -973,24 +994,43 @@ __global__ void __launch_bounds__(kTPB, 7) k_tube_conf(const Real* __restrict__ 
             }
             __syncwarp();
             const uint32_t lo = L.packed ? L.tlo : 0u, len = L.packed ? L.tlen : m;
-            uint32_t mask = 0, emask = 0;  // marked pairs; earlier survivors
-            if (have) {
-                for (uint32_t u0 = 0; u0 < len; u0 += 8) {
+            // pair-parallel marking as in k_tube_old (every probe of the item)
+            const int na = (int)L.np;
+            const int sh = na <= 1 ? 0 : 32 - __clz(na - 1);
+            const int slot = lane & ((1 << sh) - 1);
+            const bool qv = slot < na;
+            const int src = qv ? slot : lane;
+            const float qx = __shfl_sync(0xffffffffu, ax, src), qy = __shfl_sync(0xffffffffu, ay, src),
+                        qz = __shfl_sync(0xffffffffu, az, src);
+            const float qcx = __shfl_sync(0xffffffffu, cA.x, src), qcy = __shfl_sync(0xffffffffu, cA.y, src),
+                        qcz = __shfl_sync(0xffffffffu, cA.z, src);
+            const float qh = __shfl_sync(0xffffffffu, hAe, src), qC = __shfl_sync(0xffffffffu, hC, src);
+            const uint32_t qcid = __shfl_sync(0xffffffffu, cid, src);
+            const uint32_t qlo = __shfl_sync(0xffffffffu, lo, src);
+            const uint32_t qlen0 = __shfl_sync(0xffffffffu, len, src);
+            const uint32_t qlen = qv ? qlen0 : 0u;
+            const uint32_t step = 32u >> sh;
+            uint32_t qmask = 0, qemask = 0;  // marked pairs; earlier survivors
+            for (uint32_t u0 = (uint32_t)lane >> sh; u0 < qlen; u0 += 4u * step) {
 #pragma unroll
-                    for (uint32_t jj = 0; jj < 8; ++jj) {
-                        const uint32_t u = u0 + jj;
-                        if (u < len) {
-                            const uint32_t j = lo + u;
-                            const float4 tq = T.ps[j];
-                            const float bx = tq.x - ax, by = tq.y - ay, bz = tq.z - az;
-                            const uint32_t bit = T.id[j] < cid ? (1u << j) : 0u;
-                            emask |= bit;
-                            if (capsule_near(bx, by, bz, cA.x, cA.y, cA.z, hAe, tq.w, hC)) mask |= bit;
-                        }
+                for (uint32_t jj = 0; jj < 4; ++jj) {
+                    const uint32_t u = u0 + jj * step;
+                    if (u < qlen) {
+                        const uint32_t j = qlo + u;
+                        const float4 tq = T.ps[j];
+                        const float bx = tq.x - qx, by = tq.y - qy, bz = tq.z - qz;
+                        const uint32_t bit = T.id[j] < qcid ? (1u << j) : 0u;
+                        qemask |= bit;
+                        if (capsule_near(bx, by, bz, qcx, qcy, qcz, qh, tq.w, qC)) qmask |= bit;
                     }
                 }
-                tests += __popc(emask);
             }
+            for (int o = 1 << sh; o < 32; o <<= 1) {
+                qmask |= __shfl_xor_sync(0xffffffffu, qmask, o);
+                qemask |= __shfl_xor_sync(0xffffffffu, qemask, o);
+            }
+            const uint32_t mask = have ? qmask : 0u, emask = have ? qemask : 0u;
+            if (have) tests += __popc(emask);
             auto keep = [&](int pl, int t) {
                 int img[3];
                 if (!rel_img(pim[w][pl], T.im[t], img)) return false;

@@ -10,7 +10,10 @@
 // probe, the warp stages the segment's targets 32 at a time in its own
 // shared-memory tile (one coalesced load per lane) and every lane tests its
 // probe against each staged target (broadcast reads, no bank conflict).
-// Warps only meet at __syncwarp.
+// (The generation's tube-grid kernels mark pair-parallel instead: an item's
+// live probes share the warp's lanes, 2^s lanes per probe, so that items of
+// few probes keep every lane marking; in the contact sweep the same measured
+// 4 % slower.) Warps only meet at __syncwarp.
 #pragma once
 #include <cstdint>
 
@@ -52,6 +55,20 @@ __device__ __forceinline__ bool capsule_near(float bx, float by, float bz, float
     return rx * rx + ry * ry + rz * rz <= R * R;
 }
 
+// Position of the k-th (from 0) set bit of m, k < popc(m): a binary search on
+// population counts of halves, quarters, ... (no loop, no divergence).
+__device__ __forceinline__ int nth_set_bit(uint32_t m, int k) {
+    int pos = 0, c = __popc(m & 0xffffu);
+    if (k >= c) { k -= c; m >>= 16; pos = 16; }
+    c = __popc(m & 0xffu);
+    if (k >= c) { k -= c; m >>= 8; pos += 8; }
+    c = __popc(m & 0xfu);
+    if (k >= c) { k -= c; m >>= 4; pos += 4; }
+    c = __popc(m & 0x3u);
+    if (k >= c) { k -= c; m >>= 2; pos += 2; }
+    return pos + (k >= (int)(m & 1u) ? 1 : 0);
+}
+
 // Hands the marked pairs of a tile to the warp in two stages. Stage 1: 32 at a
 // time, keep(probe_lane, slot) runs a cheap rejection (one lane per pair).
 // Stage 2: the pairs kept are gathered in a second per-warp list q2 (64 entries)
@@ -87,10 +104,8 @@ __device__ __forceinline__ int for_marked_pairs(uint32_t mask, int lane, int* sp
 #pragma unroll
             for (int step = 16; step; step >>= 1)
                 if (sp[src + step] <= g) src += step;
-            uint32_t m = sm[src];
-            for (int k = g - sp[src]; k > 0; --k) m &= m - 1u;
             pl = src;
-            t = __ffs(m) - 1;
+            t = nth_set_bit(sm[src], g - sp[src]);
             kept = keep(pl, t);
         }
         const unsigned bal = __ballot_sync(0xffffffffu, kept);
