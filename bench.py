@@ -242,10 +242,9 @@ class Clocks:
 def fp32_roofline(g, old_ms, clk):
     """FP32 side of the two generation sweeps (candidates against accepted rods
     and against earlier candidates; the counters cover both): FP32 flops they
-    execute at least -- 22 per staged pair (the line bound of the old-rod
-    sweep, or the capsule test of the conflict sweep; the capsule test that
-    follows a line bound is not counted), 40 per marked pair (the hand-out's
-    line test), 60 per pair that passes it (the full filter and certificate)
+    execute at least -- 22 per staged pair (the line bound that opens the
+    marking test of both sweeps; the capsule test that follows it is not
+    counted) and 60 per marked pair (the full filter and certificate)
     -- over their summed event time, against the FP32 pipe peak of the device: SMs x
     128 lanes x 2 flops x the SM clock sampled in the timed window (the nominal
     figure; no FP32 peak is measured)."""
@@ -253,7 +252,7 @@ def fp32_roofline(g, old_ms, clk):
     sms = torch.cuda.get_device_properties(0).multi_processor_count
     mhz = (clk or {}).get("sm_mhz") or (clk or {}).get("sm_max_mhz") or 2070.0
     peak = sms * 128 * 2 * mhz * 1e6 / 1e12
-    flops = 22.0 * g["pair_tests"] + 40.0 * g["marked_pairs"] + 60.0 * g["line_pairs"]
+    flops = 22.0 * g["pair_tests"] + 60.0 * g["line_pairs"]
     achieved = flops / (old_ms * 1e-3) / 1e12 if old_ms > 0 else 0.0
     return {"kernel": "old_test+conflicts", "bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
             "frac": achieved / peak, "flops_per_step": flops,

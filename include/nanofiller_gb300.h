@@ -239,8 +239,11 @@ typedef struct nf_gen_stats {
     uint64_t work_items;        /* (probe chunk, stencil row, segment) items  */
     uint64_t target_tiles;      /* 32-target tiles staged                    */
     uint64_t marked_pairs;      /* pairs passing the marking pre-tests (line
-                                   bound for candidates vs rods, capsule)     */
-    uint64_t line_pairs;        /* of those, kept by the hand-out's line bound */
+                                   bound, then capsule; on the stencil sweeps
+                                   the conflict sweep marks by capsule only)  */
+    uint64_t line_pairs;        /* of those, kept by the hand-out (relative
+                                   image in range; on the stencil sweeps also
+                                   its line bound)                            */
     /* adaptive generation (zero when it is off) */
     uint64_t epochs;            /* epochs of the candidate stream begun      */
     uint64_t refits;            /* orientation-law refits                     */

@@ -177,6 +177,8 @@ __global__ void __launch_bounds__(256) k_ct_exact(const Real* __restrict__ reals
 // Contact sweep on the tube grid: rod I against rods J > I registered in the
 // same tube cell (entries carry the image of each rod's copy); pairs the FP32
 // filter cannot rule out are queued with their cell (rod ids, relative image).
+// Marking: the line bound, then the capsule test (the hand-out then only
+// checks the relative image).
 __global__ void __launch_bounds__(kTPB, 7) k_tube_ct(const Real* __restrict__ reals, int R,
                                                   const uint32_t* __restrict__ toffs,
                                                   const uint32_t* __restrict__ nitems, uint32_t icap,
@@ -228,6 +230,8 @@ __global__ void __launch_bounds__(kTPB, 7) k_tube_ct(const Real* __restrict__ re
         const float hA2 = (pA.w * 0.5f + cA.w + epc + cA.w + Re.cut + epc) * 1.000002f + Re.slack;
         const float hAe = pA.w * 0.5f + cA.w + epc;
         const float hC = (cA.w + Re.cut + epc) * 1.000002f + 2.0f * Re.slack + 4e-6f * (1.0f + hA2);
+        const float errA = 4e-6f * (1.0f + hA2) + 2.0f * Re.slack;
+        const float thA = (cA.w + Re.cut + epc) * 1.0002f;
         for (uint32_t b = 0; b < nt; b += kWT) {
             const uint32_t m = min((uint32_t)kWT, nt - b);
             if ((uint32_t)lane < m) {
@@ -263,7 +267,15 @@ __global__ void __launch_bounds__(kTPB, 7) k_tube_ct(const Real* __restrict__ re
                             const float bx = tq.x - ax, by = tq.y - ay, bz = tq.z - az;
                             const uint32_t bit = T.id[j] > i ? (1u << j) : 0u;  // each unordered pair once per cell
                             umask |= bit;
-                            if (capsule_near(bx, by, bz, cA.x, cA.y, cA.z, hAe, tq.w, hC)) mask |= bit;
+                            const float4 cB = T.c[j];
+                            const float nx = cA.y * cB.z - cA.z * cB.y;
+                            const float ny = cA.z * cB.x - cA.x * cB.z;
+                            const float nz = cA.x * cB.y - cA.y * cB.x;
+                            const float nn = nx * nx + ny * ny + nz * nz;
+                            const float nb = fabsf(nx * bx + ny * by + nz * bz) - fmaf(4e-6f, tq.w, errA);
+                            const float thL = fmaf(cB.w, 1.0002f, thA);
+                            const bool lfar = nn > 1e-4f && nb > 0.0f && nb * nb > thL * thL * nn;
+                            if (!lfar && capsule_near(bx, by, bz, cA.x, cA.y, cA.z, hAe, tq.w, hC)) mask |= bit;
                         }
                     }
                 }
@@ -271,10 +283,7 @@ __global__ void __launch_bounds__(kTPB, 7) k_tube_ct(const Real* __restrict__ re
             }
             auto keep = [&](int pl, int t) {
                 int img[3];
-                if (!rel_img(pim[w][pl], T.im[t], img)) return false;
-                const float4 dA = pdir[w][pl], cB = T.c[t];
-                return !line_far(ppos[w][pl], dA, T.p[t], cB, img[0] * Re.L[0], img[1] * Re.L[1], img[2] * Re.L[2],
-                                 (cB.w + dA.w) + Re.cut + epc, Re.slack);
+                return rel_img(pim[w][pl], T.im[t], img);
             };
             (void)for_marked_pairs(mask, lane, msp[w], msm[w], mq2[w], keep, [&](bool valid, int pl, int t) {
                 if (!valid) return;

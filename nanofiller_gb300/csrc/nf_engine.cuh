@@ -36,7 +36,7 @@ enum Ctr {
     C_PAIR_TESTS = 0, C_EXACT, C_FLIPS, C_OVERFLOW, C_UNDECIDED,
     C_CT_PAIRS, C_CT_EXACT, C_CT_FLIPS, C_CT_RECORDS, C_SCR_PAIRS, C_SCR_EXACT,
     C_CG_ITERS, C_XQ_OLD, C_XQ_CONF, C_XQ, C_CERT, C_ITEMS, C_G_ITEMS, C_G_TILES, C_G_MARKED, C_G_LINE, C_XQ_MARK,
-    C_TUBE_OVF, C_NCTR
+    C_TUBE_OVF, C_TROD_OVF, C_NCTR
 };
 
 // Device memory of the library's buffers (nf_alloc.cu): blocks come from a
@@ -172,6 +172,11 @@ struct Engine {
     bool tube = false;
     uint32_t ntcell = 0;
     int trod_stage = -1;                    // stage of the current rod registrations (-1: stale)
+    bool trod_append = false;               // rods appended since the stage 0 registration
+    bool trod_room = false;                 // that registration left room in its cells
+    std::vector<uint32_t> trod_nreg;        // per realisation: rods in the registration
+    DBuf<uint32_t> trod_dnreg;              // the same on the device (the append's first rod)
+    DBuf<float> trod_grow;                  // per realisation: growth expected after the registration
     DBuf<uint32_t> toffs;                   // R + 1 prefix of tube cells
     DBuf<uint32_t> trod_start, trod_cur, trod_ent;
     DBuf<uint32_t> tcnd_start, tcnd_cur, tcnd_ent, tcnd_cnt;
@@ -317,8 +322,13 @@ struct Engine {
     // Tube registrations: the placed rods (stage 0 generation, 1 contacts)
     // into trod_*, the round's candidates (all kept, or the survivors of the
     // old-rod test) into tcnd_*; then the work list of probes x targets.
-    nf_status tube_register_rods(int stage);
-    nf_status tube_register_cands(uint64_t slots, const uint32_t* ntot, bool alive_only);
+    // room: leave room in each cell for the rods of later rounds (appended by
+    // tube_append_rods, the generation's rounds)
+    nf_status tube_register_rods(int stage, bool room = false);
+    nf_status tube_append_rods();
+    // extra (a device counter) is read back with the registration's total
+    nf_status tube_register_cands(uint64_t slots, const uint32_t* ntot, bool alive_only,
+                                  const unsigned long long* extra = nullptr, unsigned long long* extra_out = nullptr);
     // Work items of a tube sweep (probe entries at pstart, target entries at
     // tstart, per-cell counts when compacted); pack: small cells in packed
     // items (the generation's sweeps read both kinds).
@@ -350,9 +360,14 @@ struct Engine {
 };
 
 // Count, scan, fill.
+// grow (per realisation, on the device): leave room in each cell for that
+// much growth (k_treg_room), the free slots marked kTubeRoom; the per-cell
+// counts are then in cur. extra: a device counter read back with the total.
 template <class Src>
 inline nf_status tube_register(Engine& E, uint32_t n, const uint32_t* ntot, int stage, Src src, DBuf<uint32_t>& start,
-                               DBuf<uint32_t>& cur, DBuf<uint32_t>& ent, DBuf<float4>& epos, DBuf<float4>& edir) {
+                               DBuf<uint32_t>& cur, DBuf<uint32_t>& ent, DBuf<float4>& epos, DBuf<float4>& edir,
+                               const float* grow = nullptr, const unsigned long long* extra = nullptr,
+                               unsigned long long* extra_out = nullptr) {
     const uint32_t nc = E.ntcell;
     cudaStream_t st = E.st;
 #define NF_CKT(x) do { cudaError_t e_ = (x); if (e_ != cudaSuccess) return E.cuda_fail(e_, #x); } while (0)
@@ -360,9 +375,13 @@ inline nf_status tube_register(Engine& E, uint32_t n, const uint32_t* ntot, int 
     NF_CKT(cur.ensure(nc + 1));
     NF_CKT(cudaMemsetAsync(cur.p, 0, sizeof(uint32_t) * (nc + 1), st));
     if (n) {
-        auto kcount = k_treg<Src, false>;
+        auto kcount = k_treg<Src, 0>;
         NF_LAUNCH(kcount, (unsigned)((n + kRegTPB - 1) / kRegTPB), kRegTPB, 0, st)(
             n, ntot, E.dreal.p, stage, src, cur.p, nullptr, nullptr, nullptr, nullptr, 0u, nullptr);
+        NF_CKT(cudaGetLastError());
+    }
+    if (grow && nc) {
+        NF_LAUNCH(k_treg_room, (nc + 255) / 256, 256, 0, st)(nc, cur.p, E.toffs.p, E.R, grow);
         NF_CKT(cudaGetLastError());
     }
     nf_status s = E.scan_u32(cur.p, start.p, nc + 1);
@@ -374,16 +393,20 @@ inline nf_status tube_register(Engine& E, uint32_t n, const uint32_t* ntot, int 
     s = E.ensure_pinned(16);
     if (s != NF_OK) return s;
     uint32_t* h = reinterpret_cast<uint32_t*>(E.hpin);
+    unsigned long long* hx = reinterpret_cast<unsigned long long*>(E.hpin) + 1;
     NF_CKT(cudaMemcpyAsync(h, start.p + nc, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+    if (extra) NF_CKT(cudaMemcpyAsync(hx, extra, sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
     NF_CKT(cudaStreamSynchronize(st));
     const size_t total = *h;
+    if (extra && extra_out) *extra_out = *hx;
     (&start == &E.trod_start ? E.trod_total : E.tcnd_total) = total;
     NF_CKT(ent.ensure(total + 1));
     NF_CKT(epos.ensure(total + 1));
     NF_CKT(edir.ensure(total + 1));
     NF_CKT(cudaMemsetAsync(cur.p, 0, sizeof(uint32_t) * (nc + 1), st));
+    if (grow) NF_CKT(cudaMemsetAsync(ent.p, 0xff, sizeof(uint32_t) * total, st));  // every slot kTubeRoom
     if (n) {
-        auto kfill = k_treg<Src, true>;
+        auto kfill = k_treg<Src, 1>;
         NF_LAUNCH(kfill, (unsigned)((n + kRegTPB - 1) / kRegTPB), kRegTPB, 0, st)(
             n, ntot, E.dreal.p, stage, src, cur.p, start.p, ent.p, nullptr, nullptr,
             (uint32_t)std::min(ent.cap, std::min(epos.cap, edir.cap)), E.ctr.p + C_TUBE_OVF);

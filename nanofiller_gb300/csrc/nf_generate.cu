@@ -725,18 +725,24 @@ __global__ void __launch_bounds__(256) k_conf_exact(const Real* __restrict__ rea
 // cell: the marking loop works on the copies, the filters and the FP64 queue
 // on the original coordinates with the relative image (target copy image -
 // probe copy image). An item's cells belong to one realisation (carried in
-// the item); per-pair cells come from the probe lane.
+// the item); per-pair cells come from the probe lane. The marking test is the
+// line bound and then the capsule test (pair-parallel), so the hand-out's
+// first stage only drops pairs whose relative image is out of range; the
+// full filter, certificate and FP64 queue follow as in the stencil kernels.
+// The rods' cells are [start, start + count) (the registration leaves room
+// for the rods of later rounds).
 // ---------------------------------------------------------------------------
 
 // Candidates (probe entries) against placed rods (target entries) of one tube
 // cell: cuda_OldExtIsectLB's job (inc/intersection_kern.h:245-364) on the
-// tube grid. Marking, hand-out, certificate and FP64 queue as k_old_tiles.
+// tube grid.
 __global__ void __launch_bounds__(kTPB, 7) k_tube_old(const Real* __restrict__ reals, int R,
                                                    const uint32_t* __restrict__ toffs,
                                                    const uint32_t* __restrict__ nitems, uint32_t icap,
                                                    const TItem* __restrict__ items,
                                                    const uint32_t* __restrict__ pstart,
                                                    const uint32_t* __restrict__ tstart,
+                                                   const uint32_t* __restrict__ tcnt,
                                                    const uint32_t* __restrict__ pent,
                                                    const float4* __restrict__ cpos, const float4* __restrict__ cdir,
                                                    const uint32_t* __restrict__ tent,
@@ -762,7 +768,7 @@ __global__ void __launch_bounds__(kTPB, 7) k_tube_old(const Real* __restrict__ r
         const TItem I = nxt;
         if (it + stride < n) nxt = items[it + stride];
         ++nitem;
-        const TubeLane L = tube_lane(I, lane, pstart, tstart, nullptr, nullptr, packs[w]);
+        const TubeLane L = tube_lane(I, lane, pstart, tstart, nullptr, tcnt, packs[w]);
         const int rl = item_real(I.pfirst, I.cnt, I.cell, toffs, R);
         const Real& Re = reals[rl];
         const bool have = (uint32_t)lane < L.np;
@@ -863,11 +869,7 @@ __global__ void __launch_bounds__(kTPB, 7) k_tube_old(const Real* __restrict__ r
             auto keep = [&](int pl, int t) {
                 if ((dead >> pl) & 1u) return false;
                 int img[3];
-                if (!rel_img(pim[w][pl], T.im[t], img)) return false;
-                const Real& Rp = Re;
-                const float4 dA = pdir[w][pl], cB = T.c[t];
-                return !line_far(ppos[w][pl], dA, T.p[t], cB, img[0] * Rp.L[0], img[1] * Rp.L[1], img[2] * Rp.L[2],
-                                 (cB.w + dA.w) * Rp.scf + Rp.sep + Rp.eps, Rp.slack);
+                return rel_img(pim[w][pl], T.im[t], img);
             };
             ++ntile;
             nmark += __popc(mask);
@@ -970,6 +972,8 @@ __global__ void __launch_bounds__(kTPB, 7) k_tube_conf(const Real* __restrict__ 
         const float hA2 = (pA.w * 0.5f + cA.w + Re.eps + cA.w * Re.scf + Re.sep + Re.eps) * 1.000002f + Re.slack;
         const float hAe = pA.w * 0.5f + cA.w + Re.eps;
         const float hC = (cA.w * Re.scf + Re.sep + Re.eps) * 1.000002f + 2.0f * Re.slack + 4e-6f * (1.0f + hA2);
+        const float errA = 4e-6f * (1.0f + hA2) + 2.0f * Re.slack;
+        const float thA = (cA.w * Re.scf + Re.sep + Re.eps) * 1.0002f, scf2 = Re.scf * 1.0002f;
         for (uint32_t b = 0; b < L.nt; b += kWT) {
             const uint32_t m = min((uint32_t)kWT, L.nt - b);
             if ((uint32_t)lane < m) {
@@ -1005,6 +1009,7 @@ __global__ void __launch_bounds__(kTPB, 7) k_tube_conf(const Real* __restrict__ 
             const float qcx = __shfl_sync(0xffffffffu, cA.x, src), qcy = __shfl_sync(0xffffffffu, cA.y, src),
                         qcz = __shfl_sync(0xffffffffu, cA.z, src);
             const float qh = __shfl_sync(0xffffffffu, hAe, src), qC = __shfl_sync(0xffffffffu, hC, src);
+            const float qerr = __shfl_sync(0xffffffffu, errA, src), qth = __shfl_sync(0xffffffffu, thA, src);
             const uint32_t qcid = __shfl_sync(0xffffffffu, cid, src);
             const uint32_t qlo = __shfl_sync(0xffffffffu, lo, src);
             const uint32_t qlen0 = __shfl_sync(0xffffffffu, len, src);
@@ -1021,7 +1026,15 @@ __global__ void __launch_bounds__(kTPB, 7) k_tube_conf(const Real* __restrict__ 
                         const float bx = tq.x - qx, by = tq.y - qy, bz = tq.z - qz;
                         const uint32_t bit = T.id[j] < qcid ? (1u << j) : 0u;
                         qemask |= bit;
-                        if (capsule_near(bx, by, bz, qcx, qcy, qcz, qh, tq.w, qC)) qmask |= bit;
+                        const float4 cB = T.c[j];
+                        const float nx = qcy * cB.z - qcz * cB.y;
+                        const float ny = qcz * cB.x - qcx * cB.z;
+                        const float nz = qcx * cB.y - qcy * cB.x;
+                        const float nn = nx * nx + ny * ny + nz * nz;
+                        const float nb = fabsf(nx * bx + ny * by + nz * bz) - fmaf(4e-6f, tq.w, qerr);
+                        const float thL = fmaf(cB.w, scf2, qth);
+                        const bool lfar = nn > 1e-4f && nb > 0.0f && nb * nb > thL * thL * nn;
+                        if (!lfar && capsule_near(bx, by, bz, qcx, qcy, qcz, qh, tq.w, qC)) qmask |= bit;
                     }
                 }
             }
@@ -1033,11 +1046,7 @@ __global__ void __launch_bounds__(kTPB, 7) k_tube_conf(const Real* __restrict__ 
             if (have) tests += __popc(emask);
             auto keep = [&](int pl, int t) {
                 int img[3];
-                if (!rel_img(pim[w][pl], T.im[t], img)) return false;
-                const Real& Rp = Re;
-                const float4 dA = pdir[w][pl], cB = T.c[t];
-                return !line_far(ppos[w][pl], dA, T.p[t], cB, img[0] * Rp.L[0], img[1] * Rp.L[1], img[2] * Rp.L[2],
-                                 (cB.w + dA.w) * Rp.scf + Rp.sep + Rp.eps, Rp.slack);
+                return rel_img(pim[w][pl], T.im[t], img);
             };
             ++ntile;
             nmark += __popc(mask);
@@ -1323,9 +1332,11 @@ struct TubeRodSrc {
     int R;
     const float4* pos;
     const float4* dir;
+    const uint32_t* dfirst;  // per realisation: first rod taken (null: 0)
     __device__ bool operator()(uint32_t i, int* r, float4* p, float4* c) const {
         const int q = find_real(rodoff, R, i);
         if (i - rodoff[q] >= dcount[q]) return false;
+        if (dfirst && i - rodoff[q] < dfirst[q]) return false;
         *r = q;
         *p = pos[i];
         *c = dir[i];
@@ -1354,15 +1365,58 @@ struct TubeCandSrc {
     }
 };
 
-nf_status Engine::tube_register_rods(int stage) {
-    TubeRodSrc src{rodoff.p, dcount.p, R, pos.p, dir.p};
-    return tube_register(*this, (uint32_t)rod_slots, nullptr, stage, src, trod_start, trod_cur, trod_ent, trod_pos,
-                         trod_dir);
+nf_status Engine::tube_register_rods(int stage, bool room) {
+    TubeRodSrc src{rodoff.p, dcount.p, R, pos.p, dir.p, nullptr};
+    trod_append = false;
+    // room for the rods still to come: growth (target - count) / count of each
+    // realisation; none while some realisation has under a fifth of its
+    // target (the room would be most of the registration)
+    std::vector<float> g(R);
+    for (int r = 0; room && r < R; ++r) {
+        const double c = (double)count[r], t = (double)hreal[r].target;
+        g[r] = (float)(t > c ? (t - c) / std::max(c, 1.0) : 0.0);
+        if (g[r] > 4.0f) room = false;
+    }
+    trod_room = room;
+    if (!room)
+        return tube_register(*this, (uint32_t)rod_slots, nullptr, stage, src, trod_start, trod_cur, trod_ent, trod_pos,
+                             trod_dir);
+    // the cell counts then sit in trod_cur
+    NF_CK(trod_grow.ensure(R));
+    NF_CK(cudaMemcpyAsync(trod_grow.p, g.data(), sizeof(float) * R, cudaMemcpyHostToDevice, st));
+    nf_status s = tube_register(*this, (uint32_t)rod_slots, nullptr, stage, src, trod_start, trod_cur, trod_ent,
+                                trod_pos, trod_dir, trod_grow.p);  // g: a pageable copy, read in the call
+    if (s != NF_OK) return s;
+    trod_nreg = count;
+    return NF_OK;
 }
 
-nf_status Engine::tube_register_cands(uint64_t slots, const uint32_t* ntot, bool /*alive_only*/) {
+// The rods appended since the registration (rods trod_nreg[r] .. count[r] of
+// each realisation) into the room of their cells: no count pass, no scan, no
+// read-back; a cell without room counts in C_TROD_OVF (read back with the
+// candidates' registration, which then registers all rods again).
+nf_status Engine::tube_append_rods() {
+    NF_CK(trod_dnreg.ensure(R));
+    NF_CK(cudaMemcpyAsync(trod_dnreg.p, trod_nreg.data(), sizeof(uint32_t) * R, cudaMemcpyHostToDevice, st));
+    NF_CK(cudaMemsetAsync(ctr.p + C_TROD_OVF, 0, sizeof(unsigned long long), st));
+    TubeRodSrc src{rodoff.p, dcount.p, R, pos.p, dir.p, trod_dnreg.p};
+    if (rod_slots) {
+        auto kapp = k_treg<TubeRodSrc, 2>;
+        NF_LAUNCH(kapp, (unsigned)((rod_slots + kRegTPB - 1) / kRegTPB), kRegTPB, 0, st)(
+            (uint32_t)rod_slots, nullptr, dreal.p, 0, src, trod_cur.p, trod_start.p, trod_ent.p, trod_pos.p,
+            trod_dir.p, 0u, ctr.p + C_TROD_OVF);
+        NF_CK(cudaGetLastError());
+    }
+    trod_nreg = count;
+    trod_append = false;
+    return NF_OK;
+}
+
+nf_status Engine::tube_register_cands(uint64_t slots, const uint32_t* ntot, bool /*alive_only*/,
+                                      const unsigned long long* extra, unsigned long long* extra_out) {
     TubeCandSrc src{creal.p, cpos.p, cdir.p, state.p};
-    return tube_register(*this, (uint32_t)slots, ntot, 0, src, tcnd_start, tcnd_cur, tcnd_ent, tcnd_pos, tcnd_dir);
+    return tube_register(*this, (uint32_t)slots, ntot, 0, src, tcnd_start, tcnd_cur, tcnd_ent, tcnd_pos, tcnd_dir,
+                         nullptr, extra, extra_out);
 }
 
 nf_status Engine::tube_items(const uint32_t* pstart, const uint32_t* tstart, const uint32_t* pcnt,
@@ -1870,20 +1924,33 @@ nf_status Engine::generate() {
         tstart(KT_OLD);
         bool cands_registered = false;  // the tube registration of this round's candidates
         if (tube && total_rods() > 0) {
-            // tube grid: the kept candidates against the placed rods that share a cell
-            if (trod_stage != 0) {
-                s = tube_register_rods(0);
+            // tube grid: the kept candidates against the placed rods that share
+            // a cell. The rods' registration (stage 0) leaves room in every
+            // cell; the rods of the rounds after it are appended, and a full
+            // registration follows only when a cell runs out of room.
+            bool appended = false;
+            if (trod_stage == 0 && trod_append && trod_room) {
+                s = tube_append_rods();
+                if (s != NF_OK) return s;
+                appended = true;
+            } else if (trod_stage != 0 || trod_append) {
+                s = tube_register_rods(0, tube_round);
                 if (s != NF_OK) return s;
                 trod_stage = 0;
             }
-            s = tube_register_cands(slots, ntot, true);
+            unsigned long long rod_ovf = 0;
+            s = tube_register_cands(slots, ntot, true, appended ? ctr.p + C_TROD_OVF : nullptr, &rod_ovf);
             if (s != NF_OK) return s;
+            if (rod_ovf) {
+                s = tube_register_rods(0, true);
+                if (s != NF_OK) return s;
+            }
             cands_registered = true;
-            s = tube_items(tcnd_start.p, trod_start.p, nullptr, nullptr, true);
+            s = tube_items(tcnd_start.p, trod_start.p, nullptr, trod_cur.p, true);
             if (s != NF_OK) return s;
             NF_LAUNCH(k_tube_old, persistent_grid(k_tube_old), kTPB, 0, st)(dreal.p, R, toffs.p, titem_count(),
                                                     (uint32_t)titems.cap, titems.p, tcnd_start.p, trod_start.p,
-                                                    tcnd_ent.p, tcnd_pos.p, tcnd_dir.p,
+                                                    trod_cur.p, tcnd_ent.p, tcnd_pos.p, tcnd_dir.p,
                                                     trod_ent.p, trod_pos.p, trod_dir.p, state.p, xq.p, xq.cap, ctr.p);
             NF_CK(cudaGetLastError());
             NF_LAUNCH(k_old_exact, xg, 256, 0, st)(dreal.p, xq.p, nullptr, ctr.p + C_XQ_OLD, xq.cap, cpos.p, cdir.p,
@@ -2043,7 +2110,7 @@ nf_status Engine::generate() {
         if (any_new) {
             if (tube_round) {  // the cell lists wait for the end of the generation
                 cells_valid = false;
-                trod_stage = -1;
+                trod_append = true;  // the new rods go into the room of the registration
             } else {
                 s = rebuild_cells();
                 if (s != NF_OK) return s;

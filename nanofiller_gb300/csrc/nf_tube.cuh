@@ -38,6 +38,8 @@
 namespace nf {
 
 constexpr uint32_t kTubeIdShift = 6;
+// An entry slot left free in a cell (image code 3 on every axis: no entry).
+constexpr uint32_t kTubeRoom = 0xffffffffu;
 
 __host__ __device__ __forceinline__ uint32_t tube_entry(uint32_t id, const int img[3]) {
     return (id << kTubeIdShift) | (uint32_t)(img[0] + 1) | ((uint32_t)(img[1] + 1) << 2) |
@@ -207,7 +209,11 @@ __device__ __forceinline__ bool tube_claims_d(const Real& Re, int per, uint32_t 
 // a binary search over the prefix and visits that slab's cells.
 constexpr int kRegTPB = 256;
 
-template <class Src, bool kFill>
+// kMode: 0 count pass, 1 fill pass, 2 append (objects added to a registration
+// that left room in its cells: entry and geometry at start[cell] + the cell's
+// count when below start[cell + 1], else the count is restored and the
+// registration counted in ovf).
+template <class Src, int kMode>
 __global__ void __launch_bounds__(kRegTPB) k_treg(uint32_t n, const uint32_t* __restrict__ ntot,
                                                   const Real* __restrict__ reals, int stage, Src src,
                                                   uint32_t* __restrict__ tcnt, const uint32_t* __restrict__ tstart,
@@ -286,10 +292,22 @@ __global__ void __launch_bounds__(kRegTPB) k_treg(uint32_t n, const uint32_t* __
                 uint32_t cell;
                 int img[3];
                 if (!tube_cell(Re, per, u, &cell, img)) continue;
-                if (kFill) {
+                if (kMode == 1) {
                     const uint32_t qd = tstart[cell] + atomicAdd(&tcnt[cell], 1u);
                     if (qd < cap) tent[qd] = tube_entry(id, img);
                     else atomicAdd(ovf, 1ull);
+                } else if (kMode == 2) {
+                    const uint32_t qd = tstart[cell] + atomicAdd(&tcnt[cell], 1u);
+                    if (qd < tstart[cell + 1]) {
+                        tent[qd] = tube_entry(id, img);
+                        tpos[qd] = q;
+                        tdir[qd] = cq;
+                    } else {
+                        // a count never ends above the room: every increment
+                        // that found the cell full is taken back
+                        atomicSub(&tcnt[cell], 1u);
+                        atomicAdd(ovf, 1ull);
+                    }
                 } else {
                     atomicAdd(&tcnt[cell], 1u);
                 }
@@ -304,11 +322,29 @@ template <class Src>
 __global__ void __launch_bounds__(256) k_treg_geom(uint32_t n, const uint32_t* __restrict__ ent,
                                                    float4* __restrict__ epos, float4* __restrict__ edir, Src src) {
     for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
+        const uint32_t e = ent[q];
+        if (e == kTubeRoom) continue;  // room left in a cell for later objects
         float4 p, c;
-        src.geom(ent[q] >> kTubeIdShift, &p, &c);
+        src.geom(e >> kTubeIdShift, &p, &c);
         epos[q] = p;
         edir[q] = c;
     }
+}
+
+// Room per cell for the objects later rounds add (a registration that is
+// appended to): on entry cnt[c] holds the cell's count k, on exit its
+// capacity (1 + g) (k + 3 sqrt(k + 1) + 3) + 8, g the growth expected for its
+// realisation (objects to come over present ones): a Poisson count k puts
+// the cell's final count below (1 + g) (k + 3 sqrt(k + 1) + 3) at about
+// three standard deviations, so a cell runs out of room rarely even when k
+// is a small sample of it.
+static __global__ void k_treg_room(uint32_t ncell, uint32_t* __restrict__ cnt, const uint32_t* __restrict__ toffs,
+                                   int R, const float* __restrict__ grow) {
+    const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= ncell) return;
+    const float k = (float)cnt[c];
+    const float g = grow[find_real(toffs, R, c)];
+    cnt[c] = (uint32_t)ceilf((1.0f + g) * (k + 3.0f * sqrtf(k + 1.0f) + 3.0f)) + 8u;
 }
 
 // In-place compaction of a candidate registration to the candidates still
