@@ -116,7 +116,7 @@ typedef struct nf_params {
     int32_t stencil_radius; /* STENCIL_RADIUS: cells of edge >= reach / r and a
                                (2r+1)^3 stencil; 0 -> 2 where the box allows  */
     float round_overshoot;  /* ROUND_OVERSHOOT: candidates drawn per round over
-                               the expected need; 0 -> 2                      */
+                               the expected need; 0 -> 1.5                    */
     double two_phase_work;  /* TWO_PHASE_WORK: candidates x rods of a round
                                above which the old-rod test runs in phases
                                (centre stencil row, the four rows beside it,
@@ -178,7 +178,7 @@ typedef struct nf_params {
                                widest pair threshold, touches, and test the
                                pairs that share a cell; the cell edge is chosen
                                for about this many registrations per cell
-                               (0 -> 48); < 0 -> the cell-stencil sweeps     */
+                               (0 -> 64); < 0 -> the cell-stencil sweeps     */
     int32_t align_law;      /* ALIGN_LAW: the law a self-alignment refit gives
                                a cell. 0 (default) a von Mises-Fisher law
                                about the principal axis of the cell's
@@ -612,8 +612,9 @@ nf_status nf_write_coo(nf_handle *h, const char *dir);
  * batch) under candidate values of the speed-only settings, one coordinate at
  * a time, each trial run twice and timed on the second, and keeps the fastest
  * in every realisation's parameters: on the tube grid (the default) the cell
- * edge through tube_load (24, 32, 64, 96 besides the value on entry) and the
- * candidates per round through round_overshoot (1.5, 2, 3); on the stencil
+ * edge through tube_load (32, 48, 64, 96, 128 but the value on entry) and
+ * the candidates per round through round_overshoot (three of 1.25, 1.5, 2, 3
+ * besides the value on entry); on the stencil
  * sweeps stencil_radius, round_overshoot and two_phase_work. The accepted
  * sets do not depend on them: the handle ends holding the rods nf_generate
  * gives. out may be NULL. */
@@ -624,7 +625,7 @@ typedef struct nf_tune_result {
     double ms_first;        /* generation time with the settings on entry   */
     double ms_best;         /* with the settings chosen                     */
     int32_t trials;
-    float tube_load;        /* chosen tube load (0: the default, 48)        */
+    float tube_load;        /* chosen tube load (0: the default, 64)        */
 } nf_tune_result;
 nf_status nf_autotune(nf_handle *h, nf_tune_result *out);
 

@@ -402,26 +402,34 @@ nf_status nf_autotune(nf_handle* h, nf_tune_result* out) {
         if (t < t_best) { t_best = t; best = q; }
         return NF_OK;
     };
+    // the round size: three values besides the one on entry (0: 1.5)
+    auto try_overshoot = [&]() -> nf_status {
+        const float on_entry = best.round_overshoot > 0 ? best.round_overshoot : 1.5f;
+        int n = 0;
+        for (float f : {1.25f, 1.5f, 2.0f, 3.0f}) {
+            if (f == on_entry || n == 3) continue;
+            ++n;
+            nf_status st = try_value([](Tune& q, float v) { q.round_overshoot = v; }, f);
+            if (st != NF_OK) return st;
+        }
+        return NF_OK;
+    };
     if (E.tube) {  // tube grid: the cell edge (through the load) and the round size
-        const float on_entry = best.tube_load > 0 ? best.tube_load : 48.0f;
-        for (float l : {24.0f, 32.0f, 64.0f, 96.0f}) {
+        const float on_entry = best.tube_load > 0 ? best.tube_load : 64.0f;
+        for (float l : {32.0f, 48.0f, 64.0f, 96.0f, 128.0f}) {
             if (l == on_entry) continue;
             s = try_value([](Tune& q, float v) { q.tube_load = v; }, l);
             if (s != NF_OK) return s;
         }
-        for (float f : {1.5f, 2.0f, 3.0f}) {
-            s = try_value([](Tune& q, float v) { q.round_overshoot = v; }, f);
-            if (s != NF_OK) return s;
-        }
+        s = try_overshoot();
+        if (s != NF_OK) return s;
     } else {
         for (int r : {1, 2}) {
             s = try_value([](Tune& q, int v) { q.stencil_radius = v; }, r);
             if (s != NF_OK) return s;
         }
-        for (float f : {1.5f, 2.0f, 3.0f}) {
-            s = try_value([](Tune& q, float v) { q.round_overshoot = v; }, f);
-            if (s != NF_OK) return s;
-        }
+        s = try_overshoot();
+        if (s != NF_OK) return s;
         for (double w : {1e9, 1e10, -1.0}) {
             s = try_value([](Tune& q, double v) { q.two_phase_work = v; }, w);
             if (s != NF_OK) return s;

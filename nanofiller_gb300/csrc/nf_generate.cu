@@ -124,7 +124,7 @@ void set_tube_grid(Real& R, const nf_params& p) {
     const double nrod = (double)std::max<int64_t>(target_count(p), 1);
     double lmean = p.l;
     if (p.len_mode == NF_SIZE_LOGNORMAL) lmean = std::min((double)p.len_max, p.l * std::exp(0.5 * p.len_sigma_ln * p.len_sigma_ln));
-    const double load = p.tube_load > 0 ? (double)p.tube_load : 48.0;
+    const double load = p.tube_load > 0 ? (double)p.tube_load : 64.0;
     const double nd = nrod / V;
     double lo = 4 * rho, hi = std::max(lo, std::min((double)p.box[0], std::min((double)p.box[1], (double)p.box[2])));
     for (int it = 0; it < 60; ++it) {
@@ -1778,11 +1778,11 @@ nf_status Engine::generate() {
                 // Acceptance per candidate: the density acceptance before the
                 // first round, then the last round's own rate (the rate only
                 // falls as the box fills, so the cumulative rate would
-                // overestimate it). Rounds draw round_overshoot (2 by default)
+                // overestimate it). Rounds draw round_overshoot (1.5 by default)
                 // times the expected need: extra candidates cost sweep work, a
                 // short round costs a round.
                 const double acc_rate = rounds_r[r] > 0 ? last_rate[r] : p_dens[r];
-                const double over = p.round_overshoot > 0 ? (double)p.round_overshoot : 2.0;
+                const double over = p.round_overshoot > 0 ? (double)p.round_overshoot : 1.5;
                 double want = (tgt - count[r]) / std::max(acc_rate, 1e-6) * over + 256;
                 // Survivors of the old-rod test per round: at most alive_max
                 // (bounds the conflict lists) and at most the target count

@@ -1,7 +1,7 @@
 """The tube sweeps (the default; TUBE_LOAD < 0 selects the stencil sweeps):
 the pair tests of the generation, contacts and screening run over the pairs
 registered together in the cells of a fine grid along each rod's axis instead
-of a stencil of cells around its centre (load 0 = the default, 48
+of a stencil of cells around its centre (load 0 = the default, 64
 registrations per cell; small cells share packed items). Speed only: the accepted
 set and every rod float must equal the oracle's bit for bit, whatever the
 load, on every kind of workload (uniform, agglomerate with von Mises-Fisher

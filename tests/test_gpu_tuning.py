@@ -58,8 +58,8 @@ def test_autotune_keeps_results(gpu, medium_oracle, load):
         t = sim.autotune()
         assert t["trials"] == (9 if load < 0 else 8)
         assert 0 < t["ms_best"] <= t["ms_first"] * 1.05
-        assert t["stencil_radius"] in (0, 1, 2) and t["round_overshoot"] in (0.0, 1.5, 2.0, 3.0)
-        assert t["tube_load"] == load if load < 0 else t["tube_load"] in (0.0, 24.0, 32.0, 64.0, 96.0)
+        assert t["stencil_radius"] in (0, 1, 2) and t["round_overshoot"] in (0.0, 1.25, 2.0, 3.0)
+        assert t["tube_load"] == load if load < 0 else t["tube_load"] in (0.0, 32.0, 48.0, 96.0, 128.0)
         sim.contacts()
         check(sim, rods_o, idx_o, co)
         # the chosen settings stay on the handle
