@@ -250,7 +250,9 @@ typedef struct nf_gen_stats {
     uint64_t thinned;           /* rods removed by thin-out                   */
     uint64_t snapped;           /* snaps of candidates to older rods          */
     int32_t tube_grid;          /* 1: the pair sweeps ran on the tube grid    */
-    int32_t pad_gen;
+    int32_t redone_rounds;      /* rounds run again after a work list, FP64
+                                   queue or conflict list overflowed (their
+                                   buffers grow; results are unchanged)       */
 } nf_gen_stats;
 
 typedef struct nf_contact_stats {

@@ -69,7 +69,7 @@ class NfGenStats(C.Structure):
                 ("work_items", C.c_uint64), ("target_tiles", C.c_uint64), ("marked_pairs", C.c_uint64),
                 ("line_pairs", C.c_uint64), ("epochs", C.c_uint64), ("refits", C.c_uint64),
                 ("thinned", C.c_uint64), ("snapped", C.c_uint64), ("tube_grid", C.c_int32),
-                ("pad_gen", C.c_int32)]
+                ("redone_rounds", C.c_int32)]
 
 
 class NfContactStats(C.Structure):

@@ -1424,9 +1424,12 @@ nf_status Engine::tube_items(const uint32_t* pstart, const uint32_t* tstart, con
     const uint32_t nseg = (ntcell + 31u) / 32u;
     // every item holds at least one probe entry, so the probe registration's
     // size bounds the items but where a cell's targets need several segments
-    // (an overflow, counted in C_ITEMS, redoes the stage with more room)
+    // (one more item per 128 targets of a cell beyond its first segment;
+    // 1/64 of the targets is the allowance, and an overflow, counted in
+    // C_ITEMS, redoes the stage with more room)
     const size_t nprobe = pstart == trod_start.p ? trod_total : tcnd_total;
-    tit_cap = std::max(tit_cap, nprobe + 4096);
+    const size_t ntarget = tstart == trod_start.p ? trod_total : tcnd_total;
+    tit_cap = std::max(tit_cap, nprobe + ntarget / 64 + 4096);
     NF_CK(icnt.ensure((size_t)nseg + 1));
     NF_CK(tioff.ensure((size_t)nseg + 1));
     NF_CK(titems.ensure(tit_cap));
@@ -1754,7 +1757,7 @@ nf_status Engine::generate() {
     std::vector<uint64_t> c_round(R);
     std::vector<double> last_rate(R, 1.0);  // accepted / drawn in the last round
     double scale = 1.0;
-    int rounds = 0;
+    int rounds = 0, redone = 0;
     const int max_rounds = 100000;
     for (; rounds < max_rounds; ++rounds) {
         if (adapt && count[0] < hreal[0].target && knext[0] < prm[0].n_candidates && knext[0] % epoch_len == 0 &&
@@ -1904,7 +1907,9 @@ nf_status Engine::generate() {
             if (s != NF_OK) return s;
         }
         const unsigned xg = (unsigned)(4 * nsm);
-        xq_cap = std::max(xq_cap, (size_t)(slots / 8));  // first guess; grown and redone on overflow
+        // first guess (8 B a slot, a fresh handle's first rounds must not
+        // overflow it); grown and the round redone on overflow
+        xq_cap = std::max(xq_cap, (size_t)(slots / 2));
         NF_CK(xq.ensure(xq_cap));
         NF_CK(xq2.ensure(xq_cap));
         NF_CK(cudaMemsetAsync(ctr.p + C_XQ_OLD, 0, 2 * sizeof(unsigned long long), st));
@@ -2076,6 +2081,7 @@ nf_status Engine::generate() {
         }
         if (redo) {
             --rounds;
+            ++redone;
             continue;
         }
         bool any_new = false;
@@ -2154,6 +2160,7 @@ nf_status Engine::generate() {
     gst.target_reached = gst.accepted == gst.target;
     gst.ms = ms;
     gst.tube_grid = tube ? 1 : 0;
+    gst.redone_rounds = redone;
     return NF_OK;
 }
 
