@@ -57,7 +57,10 @@ def test_large_full_size_matches_oracle(gpu):
 def batch256(gpu):
     reals = gpu.configs.batched_realisations(256)
     b = gpu.Batch(reals)
-    b.generate()
+    g = b.generate()
+    # a fresh handle's first-guess capacities hold the mix's rounds: no round
+    # is run twice for an overflowing work list, FP64 queue or conflict list
+    assert g["redone_rounds"] == 0
     b.contacts()
     b.solve(check=False)
     res = b.results()
