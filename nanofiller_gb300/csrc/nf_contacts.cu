@@ -234,6 +234,13 @@ __global__ void __launch_bounds__(kTPB, 7) k_tube_ct(const Real* __restrict__ re
         const float thA = (cA.w + Re.cut + epc) * 1.0002f;
         for (uint32_t b = 0; b < nt; b += kWT) {
             const uint32_t m = min((uint32_t)kWT, nt - b);
+            // each pair once (probe and target entries are one list): tiles
+            // before the item's probe chunk are left to the items whose chunk
+            // they are; on the chunk's own tile (and in packed items, where
+            // probe lane p is target slot p) a rod tests the next half of its
+            // range, cyclically; tiles after the chunk are tested whole
+            if (!L.packed && I.tfirst + b < I.pfirst) continue;
+            const bool self = L.packed || I.tfirst + b == I.pfirst;
             if ((uint32_t)lane < m) {
                 uint32_t tc;
                 const uint32_t q = tube_target(I, L, packs[w], b, (uint32_t)lane, &tc);
@@ -255,18 +262,21 @@ __global__ void __launch_bounds__(kTPB, 7) k_tube_ct(const Real* __restrict__ re
             }
             __syncwarp();
             const uint32_t lo = L.packed ? L.tlo : 0u, len = L.packed ? L.tlen : m;
-            uint32_t mask = 0, umask = 0;  // marked pairs; pairs with J > I
+            const uint32_t xl = (uint32_t)lane - lo;
+            const uint32_t nd = !self ? len : (len ? (len - 1u) / 2u + ((len & 1u) == 0u && xl < len / 2u) : 0u);
+            uint32_t mask = 0;  // marked pairs
             if (have) {
-                for (uint32_t u0 = 0; u0 < len; u0 += 8) {
+                for (uint32_t u0 = 0; u0 < nd; u0 += 8) {
 #pragma unroll
                     for (uint32_t jj = 0; jj < 8; ++jj) {
                         const uint32_t u = u0 + jj;
-                        if (u < len) {
-                            const uint32_t j = lo + u;
+                        if (u < nd) {
+                            uint32_t y = self ? xl + 1u + u : u;
+                            if (y >= len) y -= len;
+                            const uint32_t j = lo + y;
                             const float4 tq = T.ps[j];
                             const float bx = tq.x - ax, by = tq.y - ay, bz = tq.z - az;
-                            const uint32_t bit = T.id[j] > i ? (1u << j) : 0u;  // each unordered pair once per cell
-                            umask |= bit;
+                            const uint32_t bit = 1u << j;
                             const float4 cB = T.c[j];
                             const float nx = cA.y * cB.z - cA.z * cB.y;
                             const float ny = cA.z * cB.x - cA.x * cB.z;
@@ -279,7 +289,7 @@ __global__ void __launch_bounds__(kTPB, 7) k_tube_ct(const Real* __restrict__ re
                         }
                     }
                 }
-                tests += __popc(umask);
+                tests += nd;
             }
             auto keep = [&](int pl, int t) {
                 int img[3];
@@ -287,14 +297,22 @@ __global__ void __launch_bounds__(kTPB, 7) k_tube_ct(const Real* __restrict__ re
             };
             (void)for_marked_pairs(mask, lane, msp[w], msm[w], mq2[w], keep, [&](bool valid, int pl, int t) {
                 if (!valid) return;
-                const float4 qA = ppos[w][pl], dA = pdir[w][pl];
-                const float4 pB = T.p[t], cB = T.c[t];
+                // the rod of the smaller id is the pair's first rod I
+                const bool sw = T.id[t] < pid[w][pl];
+                const float4 qA = sw ? T.p[t] : ppos[w][pl], dA = sw ? T.c[t] : pdir[w][pl];
+                const float4 pB = sw ? ppos[w][pl] : T.p[t], cB = sw ? pdir[w][pl] : T.c[t];
                 int img[3];
                 rel_img(pim[w][pl], T.im[t], img);
+                if (sw) {
+                    img[0] = -img[0];
+                    img[1] = -img[1];
+                    img[2] = -img[2];
+                }
                 const float thr = (cB.w + dA.w) + Re.cut + epc;
                 if (maybe_near(qA, dA, pB, cB, img[0] * Re.L[0], img[1] * Re.L[1], img[2] * Re.L[2], thr, epc,
                                Re.slack))
-                    xq_push_cell(xq, xqc, xcap, &ctr[C_XQ], xq_pack(pid[w][pl], T.id[t], img), pcel[w][pl]);
+                    xq_push_cell(xq, xqc, xcap, &ctr[C_XQ],
+                                 xq_pack(sw ? T.id[t] : pid[w][pl], sw ? pid[w][pl] : T.id[t], img), pcel[w][pl]);
             });
             __syncwarp();
         }

@@ -736,7 +736,7 @@ __global__ void __launch_bounds__(256) k_conf_exact(const Real* __restrict__ rea
 // Candidates (probe entries) against placed rods (target entries) of one tube
 // cell: cuda_OldExtIsectLB's job (inc/intersection_kern.h:245-364) on the
 // tube grid.
-__global__ void __launch_bounds__(kTPB, 7) k_tube_old(const Real* __restrict__ reals, int R,
+__global__ void __launch_bounds__(kTPB, 8) k_tube_old(const Real* __restrict__ reals, int R,
                                                    const uint32_t* __restrict__ toffs,
                                                    const uint32_t* __restrict__ nitems, uint32_t icap,
                                                    const TItem* __restrict__ items,
@@ -820,6 +820,22 @@ __global__ void __launch_bounds__(kTPB, 7) k_tube_old(const Real* __restrict__ r
                 T.ps[lane] = make_float4(kFar, kFar, kFar, 0.0f);
             }
             __syncwarp();
+            if (b == 0 && it + stride < n) {  // the next item's first loads, into L2
+                const uint32_t span = nxt.cnt & 63u;
+                if ((uint32_t)lane < span) {
+                    if (!(nxt.cnt & kPackBit)) {
+                        const uint32_t q = nxt.pfirst + (uint32_t)lane;
+                        asm volatile("prefetch.global.L2 [%0];" ::"l"(pent + q));
+                        asm volatile("prefetch.global.L2 [%0];" ::"l"(cpos + q));
+                        asm volatile("prefetch.global.L2 [%0];" ::"l"(cdir + q));
+                    } else {
+                        const uint32_t c = nxt.cell + (uint32_t)lane;
+                        asm volatile("prefetch.global.L2 [%0];" ::"l"(pstart + c));
+                        asm volatile("prefetch.global.L2 [%0];" ::"l"(tstart + c));
+                        asm volatile("prefetch.global.L2 [%0];" ::"l"(tcnt + c));
+                    }
+                }
+            }
             const uint32_t lo = L.packed ? L.tlo : 0u, len = L.packed ? L.tlen : m;
             if (alive) tests += len;
             // Pair-parallel marking: the na live probes take 2^s >= na lanes
@@ -913,7 +929,9 @@ __global__ void __launch_bounds__(kTPB, 7) k_tube_old(const Real* __restrict__ r
 }
 
 // Survivors against earlier survivors of one tube cell (probe and target
-// entries are the same list): k_conf_tiles on the tube grid. A certified hit
+// entries are the same list, so every pair is tested once, in whichever
+// order it is met, and evaluated with the later survivor as the probe):
+// k_conf_tiles on the tube grid. A certified hit
 // is listed by the one cell that claims it (tube_claims), so no pair enters a
 // conflict list twice from the FP32 path; uncertain pairs are queued from
 // every cell they share (the FP64 pass may list a pair again, which the
@@ -976,6 +994,15 @@ __global__ void __launch_bounds__(kTPB, 7) k_tube_conf(const Real* __restrict__ 
         const float thA = (cA.w * Re.scf + Re.sep + Re.eps) * 1.0002f, scf2 = Re.scf * 1.0002f;
         for (uint32_t b = 0; b < L.nt; b += kWT) {
             const uint32_t m = min((uint32_t)kWT, L.nt - b);
+            // Each pair once: probe and target entries are one list, so a
+            // cell item's tiles before its probe chunk are left to the items
+            // whose chunk they are; on the chunk's own tile (and in packed
+            // items, where probe lane p is target slot p) a probe tests the
+            // next half of its range, cyclically; tiles after the chunk are
+            // tested whole. The evaluation takes the later survivor as the
+            // probe of the pair.
+            if (!L.packed && I.tfirst + b < I.pfirst) continue;
+            const bool self = L.packed || I.tfirst + b == I.pfirst;
             if ((uint32_t)lane < m) {
                 uint32_t tc;
                 const uint32_t q = tube_target(I, L, packs[w], b, (uint32_t)lane, &tc);
@@ -1015,17 +1042,23 @@ __global__ void __launch_bounds__(kTPB, 7) k_tube_conf(const Real* __restrict__ 
             const uint32_t qlen0 = __shfl_sync(0xffffffffu, len, src);
             const uint32_t qlen = qv ? qlen0 : 0u;
             const uint32_t step = 32u >> sh;
-            uint32_t qmask = 0, qemask = 0;  // marked pairs; earlier survivors
-            for (uint32_t u0 = (uint32_t)lane >> sh; u0 < qlen; u0 += 4u * step) {
+            // on a self tile the probe (slot = its target slot) tests the
+            // half of its range that follows it: nd targets from xl + 1 on
+            const uint32_t xl = (uint32_t)src - qlo;
+            const uint32_t nd = !self ? qlen : (qlen ? (qlen - 1u) / 2u + ((qlen & 1u) == 0u && xl < qlen / 2u) : 0u);
+            uint32_t qmask = 0;  // marked pairs
+            for (uint32_t u0 = (uint32_t)lane >> sh; u0 < nd; u0 += 4u * step) {
 #pragma unroll
                 for (uint32_t jj = 0; jj < 4; ++jj) {
                     const uint32_t u = u0 + jj * step;
-                    if (u < qlen) {
-                        const uint32_t j = qlo + u;
+                    if (u < nd) {
+                        uint32_t y = self ? xl + 1u + u : u;
+                        if (y >= qlen) y -= qlen;
+                        const uint32_t j = qlo + y;
+                        ++tests;
                         const float4 tq = T.ps[j];
                         const float bx = tq.x - qx, by = tq.y - qy, bz = tq.z - qz;
-                        const uint32_t bit = T.id[j] < qcid ? (1u << j) : 0u;
-                        qemask |= bit;
+                        const uint32_t bit = 1u << j;
                         const float4 cB = T.c[j];
                         const float nx = qcy * cB.z - qcz * cB.y;
                         const float ny = qcz * cB.x - qcx * cB.z;
@@ -1038,12 +1071,8 @@ __global__ void __launch_bounds__(kTPB, 7) k_tube_conf(const Real* __restrict__ 
                     }
                 }
             }
-            for (int o = 1 << sh; o < 32; o <<= 1) {
-                qmask |= __shfl_xor_sync(0xffffffffu, qmask, o);
-                qemask |= __shfl_xor_sync(0xffffffffu, qemask, o);
-            }
-            const uint32_t mask = have ? qmask : 0u, emask = have ? qemask : 0u;
-            if (have) tests += __popc(emask);
+            for (int o = 1 << sh; o < 32; o <<= 1) qmask |= __shfl_xor_sync(0xffffffffu, qmask, o);
+            const uint32_t mask = have ? qmask : 0u;
             auto keep = [&](int pl, int t) {
                 int img[3];
                 return rel_img(pim[w][pl], T.im[t], img);
@@ -1053,26 +1082,34 @@ __global__ void __launch_bounds__(kTPB, 7) k_tube_conf(const Real* __restrict__ 
             const int kept_ = for_marked_pairs(mask, lane, msp[w], msm[w], mq2[w], keep, [&](bool valid, int pl, int t) {
                 if (!valid) return;
                 const Real& Rp = Re;
-                const float4 qA = ppos[w][pl], dA = pdir[w][pl];
-                const float4 pB = T.p[t], cB = T.c[t];
+                // the later survivor is the pair's probe (it lists the pair)
+                const bool sw = T.id[t] > pcid[w][pl];
+                const float4 qA = sw ? T.p[t] : ppos[w][pl], dA = sw ? T.c[t] : pdir[w][pl];
+                const float4 pB = sw ? ppos[w][pl] : T.p[t], cB = sw ? pdir[w][pl] : T.c[t];
                 int img[3];
                 rel_img(pim[w][pl], T.im[t], img);
+                if (sw) {
+                    img[0] = -img[0];
+                    img[1] = -img[1];
+                    img[2] = -img[2];
+                }
                 const float sx = img[0] * Rp.L[0], sy = img[1] * Rp.L[1], sz = img[2] * Rp.L[2];
                 const float thr = (cB.w + dA.w) * Rp.scf + Rp.sep + Rp.eps;
                 if (maybe_near(qA, dA, pB, cB, sx, sy, sz, thr, Rp.eps, Rp.slack)) {
-                    const uint32_t c = pcid[w][pl];
+                    const uint32_t c = sw ? T.id[t] : pcid[w][pl], other = sw ? pcid[w][pl] : T.id[t];
                     const uint32_t cell = pcel[w][pl];
                     float t0 = 0.0f, t1 = 0.0f;
                     if (!Rp.typo && certain_hit(qA, dA, pB, cB, sx, sy, sz, thr, Rp.eps, Rp.slack, &t0, &t1)) {
                         // listed once: by the cell of the midpoint of the two feet
-                        if (tube_claims(Rp, Rp.per_gen, cell, pim[w][pl], qA, dA, pB, cB, sx, sy, sz, t0, t1)) {
+                        if (tube_claims(Rp, Rp.per_gen, cell, sw ? T.im[t] : pim[w][pl], qA, dA, pB, cB, sx, sy, sz,
+                                        t0, t1)) {
                             ++cert;
                             uint32_t slot = atomicAdd(&ccnt[c], 1u);
-                            if (slot < (uint32_t)kConflictCap) clist[(size_t)c * kConflictCap + slot] = T.id[t];
+                            if (slot < (uint32_t)kConflictCap) clist[(size_t)c * kConflictCap + slot] = other;
                             else ++ovf;
                         }
                     } else {
-                        xq_push_cell(xq, xqc, xcap, &ctr[C_XQ_CONF], xq_pack(c, T.id[t], img), cell);
+                        xq_push_cell(xq, xqc, xcap, &ctr[C_XQ_CONF], xq_pack(c, other, img), cell);
                     }
                 }
             });
