@@ -261,7 +261,8 @@ __global__ void __launch_bounds__(kBinTPB) k_compact(const Real* __restrict__ re
                           uint64_t* __restrict__ csidx, uint32_t* __restrict__ creal, uint32_t* __restrict__ ccell,
                           uint32_t* __restrict__ ccount, uint8_t* __restrict__ state, uint32_t ncell) {
     extern __shared__ uint32_t shc[];
-    const bool sh = ncell <= kShCells;
+    const bool bin = ccell != nullptr;  // the cell-stencil sweeps bin the candidates; the tube sweeps do not
+    const bool sh = bin && ncell <= kShCells;
     if (sh) {
         for (uint32_t c = threadIdx.x; c < ncell; c += blockDim.x) shc[c] = 0;
         __syncthreads();
@@ -279,10 +280,12 @@ __global__ void __launch_bounds__(kBinTPB) k_compact(const Real* __restrict__ re
         cdir[c] = d;
         csidx[c] = k;
         creal[c] = (uint32_t)r;
-        uint32_t cell = cell_of(Re, p.x, p.y, p.z);
-        ccell[c] = cell;
         state[c] = ST_ALIVE;
-        atomicAdd(sh ? &shc[cell] : &ccount[cell], 1u);
+        if (bin) {
+            const uint32_t cell = cell_of(Re, p.x, p.y, p.z);
+            ccell[c] = cell;
+            atomicAdd(sh ? &shc[cell] : &ccount[cell], 1u);
+        }
     }
     if (sh) {
         __syncthreads();
@@ -1893,20 +1896,21 @@ nf_status Engine::generate() {
         s = scan_u32(keep.p, kpos.p, slots + 1);  // kpos[slots] = compacted total
         if (s != NF_OK) return s;
         uint32_t* ntot = kpos.p + slots;
-        NF_CK(cudaMemsetAsync(ccount.p, 0, sizeof(uint32_t) * (ncell + 1), st));
-        const size_t shc = ncell <= kShCells ? sizeof(uint32_t) * ncell : 0;
+        // the tube sweeps read the compact candidates directly; the stencil
+        // sweeps need them binned by cell
+        const bool tube_round = tube && !adapt;
+        if (!tube_round) NF_CK(cudaMemsetAsync(ccount.p, 0, sizeof(uint32_t) * (ncell + 1), st));
+        const size_t shc = !tube_round && ncell <= kShCells ? sizeof(uint32_t) * ncell : 0;
         const unsigned gb = grid_for(slots, kBinTPB);
         NF_LAUNCH(k_compact, gb, kBinTPB, shc, st)(dreal.p, R, coff.p, kbeg.p, (uint32_t)slots, keep.p, kpos.p, cpos.p,
-                                                   cdir.p, csidx.p, creal.p, ccell.p, ccount.p, state.p, ncell);
+                                                   cdir.p, csidx.p, creal.p, tube_round ? nullptr : ccell.p,
+                                                   ccount.p, state.p, ncell);
         NF_CK(cudaGetLastError());
         const bool clustered = adapt && prm[0].clust_flag && n_old > 0;
         if (clustered) {
             s = clusterize(slots, ntot, n_old);
             if (s != NF_OK) return s;
         }
-        // the tube sweeps read the compact candidates directly; the stencil
-        // sweeps need them binned by cell
-        const bool tube_round = tube && !adapt;
         if (!tube_round) {
             s = scan_u32(ccount.p, cstart.p, ncell + 1);
             if (s != NF_OK) return s;
