@@ -8,7 +8,7 @@
 // trho >= thr_max / 2, touches, every pair within reach shares a cell, and
 // testing the pairs registered together in each cell finds all of them. For
 // rods of length l in cells of edge e ~ l/4 an object registers in about
-// 2 l / e + 1 cells holding ~48 registrations each, so a probe meets a few
+// 2 l / e + 1 cells holding ~64 registrations each (TUBE_LOAD), so a probe meets a few
 // hundred targets instead of the ~4 000 of a 5 x 5 x 5 stencil of cells of
 // edge reach / 2 at 2 % volume fraction.
 //
